@@ -1,0 +1,350 @@
+#!/usr/bin/env python
+"""Benchmark of the contact hot path on GB300.
+
+Workload (N=1): the sphere pack of 512 icospheres (642 vertices and 1280
+triangles each; 328,704 vertices) on a jittered 8x8x8 lattice with gaps
+U(0.1e-3, 1.5e-3), dhat = 1e-3, stiffness 1e4 -- seeded synthetic data
+(numpy PCG64, seed 1).  One step = BarrierPotential energy + gradient +
+PSD-projected (CLAMP) Hessian with CSR assembly over the prebuilt collision
+set, exactly the three reference calls of one Newton iteration.
+
+    value   contacts/s with positions resident in HBM (device pointers)
+    e2e     the same calls through the public API with host (pinned) buffers:
+            positions copied in, energy / gradient / CSR Hessian copied out
+            inside the timed region
+    roofline  the dominant kernel's algorithmic bytes per launch over its
+            average launch time (CUDA events on the launching stream)
+    cpu_baseline  the CPU restatement timed on this host's cores
+
+--impl reference times the reference algorithm on the host cores (the CPU
+restatement under oracle/, since the reference itself cannot be built here)
+and prints the same line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "ipc-toolkit_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "barrier E+grad+Hess contacts/s"
+UNIT = "contacts/s"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--workload", choices=["sphere_pack", "two_sheet", "layered_cloth"], default="sphere_pack")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_scene(name):
+    from ipctk_gb300 import scenes
+    if name == "sphere_pack":
+        return scenes.sphere_pack(), "sphere_pack 512 icospheres x 642 verts (328,704 verts, 655,360 tris)"
+    if name == "two_sheet":
+        return scenes.two_sheet(), "two_sheet 2 x 64x64 grid (8,192 verts, 15,876 tris)"
+    return scenes.layered_cloth(), "layered_cloth 8 x 256x256 (524,288 verts)"
+
+
+# algorithmic bytes per contact of one E+G+H pass: positions + ids + weight
+# in, gradient contribution + Hessian values + CSR column indices out
+BYTES_PER_CONTACT = {2: 504, 3: 1104, 4: 1944}
+
+
+def algorithmic_bytes(counts, ndof):
+    nvv, nev, nee, nfv = (int(x) for x in counts[:4])
+    b = nvv * BYTES_PER_CONTACT[2] + nev * BYTES_PER_CONTACT[3] + (nee + nfv) * BYTES_PER_CONTACT[4]
+    b += nee * 9  # eps_x + dtype
+    b += 8 * (ndof + 1)  # CSR row pointers
+    return b
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, workload):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            t = json.load(f)
+        return t.get(workload, {}).get(kernel)
+    except Exception:
+        return None
+
+
+def cpu_baseline_run(sc, steps, budget_s=20.0):
+    """Time the CPU restatement (oracle/) on this host: E + grad + PSD Hessian
+    with CSR assembly over the collision set, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    nt = os.cpu_count() or 1
+    col = oracle.build_collisions(V, E, F, sc["dhat"], nthreads=nt)
+    C = len(col)
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        oracle.barrier_energy(col, V, E, F, sc["dhat"], sc["kappa"], nthreads=nt)
+        oracle.barrier_gradient(col, V, E, F, sc["dhat"], sc["kappa"], nthreads=nt)
+        oracle.barrier_hessian(col, V, E, F, sc["dhat"], sc["kappa"], psd="clamp", nthreads=nt)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    med = statistics.median(times)
+    return {"value": C / med, "unit": UNIT, "cores": nt, "kind": "port",
+            "sample": f"full collision set ({C} contacts), {len(times)} passes, median"}, C, times
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    sc, desc = make_scene(args.workload)
+    # a bounded number of passes: each pass is the whole collision set
+    warm = max(0, min(args.warmup, 1))
+    if warm:
+        cpu_baseline_run(sc, 1, budget_s=60)
+    base, C, times = cpu_baseline_run(sc, args.steps, budget_s=120.0)
+    ms = 1000 * statistics.median(times)
+    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": len(times), "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded numpy PCG64 scene)",
+            "config": {"workload": desc, "contacts": C, "psd": "clamp"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, world):
+    import torch
+    import ipctk_gb300 as ipctk
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sc, desc = make_scene(args.workload)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    dhat, kappa = sc["dhat"], sc["kappa"]
+    mesh = ipctk.CollisionMesh(V, E, F)
+    Vd = torch.from_numpy(V).to(dev)
+    V1d = torch.from_numpy(sc["V1"]).to(dev)
+    col = ipctk.NormalCollisions()
+    col.build(mesh, Vd, dhat)
+    counts = col.counts()
+    C = int(counts[:4].sum())
+    B = ipctk.BarrierPotential(dhat, kappa)
+    CLAMP = ipctk.PSDProjectionMethod.CLAMP
+    ndof = 3 * V.shape[0]
+    stream = torch.cuda.ExternalStream(mesh.stream, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    grad_d = None
+
+    def step():
+        nonlocal grad_d
+        B(col, mesh, Vd)
+        grad_d = B.gradient(col, mesh, Vd)
+        H = B.hessian_device(col, mesh, Vd, CLAMP)
+        nnz = H.nnz
+        H.free()
+        return nnz
+
+    for _ in range(max(3, args.warmup)):
+        nnz = step()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    ipctk.profile_enable(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ipctk.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()  # L2 flush between timed steps (outside the events)
+        torch.cuda.synchronize()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    launches = ipctk.launch_count() - launches0
+    clk = clocks.stop()
+    prof = ipctk.profile_report()
+    ipctk.profile_enable(False)
+    per = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(per)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    ms_per_step = total_ms / args.steps
+    value = world * C / (ms_per_step / 1000.0)
+
+    # roofline of the dominant kernel (largest accumulated time)
+    own = {k: v for k, v in prof.items() if k.startswith("k_")}
+    top = max(own, key=lambda k: own[k]["ms"])
+    top_ms = own[top]["ms"] / max(1, own[top]["launches"])
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if top == "k_hessian":
+        abytes = algorithmic_bytes(counts, ndof)
+        achieved = abytes / (top_ms / 1000.0) / 1e9
+        traffic = ncu_traffic(top, args.workload)
+        roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": abytes,
+                "avg_launch_ms": top_ms, "peak_source": f"{peak_kind} hbm_gbs"}
+    else:
+        roof = {"kernel": top, "bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
+                "traffic": None, "avg_launch_ms": top_ms}
+    step_share = {k: round(v["ms"] / total_ms, 4) for k, v in sorted(own.items(), key=lambda kv: -kv[1]["ms"])}
+
+    # end to end through the public API with pinned host buffers
+    Vh = torch.from_numpy(V).pin_memory().numpy()
+    e2e_times = []
+    for i in range(max(2, args.warmup // 2) + args.steps):
+        t0 = time.perf_counter()
+        e = B(col, mesh, Vh)
+        g = B.gradient(col, mesh, Vh)
+        H = B.hessian(col, mesh, Vh, CLAMP)
+        if i >= max(2, args.warmup // 2):
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_ms = 1000 * statistics.median(e2e_times)
+    h2d = 3 * V.nbytes
+    d2h = 8 + g.nbytes + H.indptr.nbytes + H.indices.nbytes + H.data.nbytes
+
+    # CCD and collision-set build (device-resident inputs)
+    ccd_ms, build_ms = [], []
+    for i in range(2 + max(3, args.steps // 4)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ipctk.compute_collision_free_stepsize(mesh, Vd, V1d)
+        t1 = time.perf_counter()
+        col.build(mesh, Vd, dhat)
+        t2 = time.perf_counter()
+        if i >= 2:
+            ccd_ms.append(1000 * (t1 - t0))
+            build_ms.append(1000 * (t2 - t1))
+    step_size = ipctk.compute_collision_free_stepsize(mesh, Vd, V1d)
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu, _, _ = cpu_baseline_run(sc, 3, budget_s=20.0)
+    pct = lambda a, q: float(np.percentile(np.array(a), q))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded numpy PCG64 scene; the reference publishes no dataset for this path)",
+        "config": {"workload": desc, "contacts": C, "contacts_by_type": {"vv": int(counts[0]), "ev": int(counts[1]),
+                   "ee": int(counts[2]), "fv": int(counts[3])}, "dhat": dhat, "stiffness": kappa,
+                   "psd": "clamp", "hessian_nnz": int(nnz), "l2": "flushed between steps (258 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "p50_ms": pct(per, 50), "p99_ms": pct(per, 99),
+        "roofline": roof, "kernel_share": step_share,
+        "cpu_baseline": cpu,
+        "e2e": {"value": C / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+        "gpu_launches": int(launches), "gpu_launches_per_step": launches / args.steps,
+        "clocks": clk,
+        "ccd": {"steps_per_s": 1000.0 / statistics.median(ccd_ms), "p50_ms": pct(ccd_ms, 50),
+                "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "candidates": col.num_candidates},
+        "collision_build": {"p50_ms": pct(build_ms, 50), "p99_ms": pct(build_ms, 99)},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    try:
+        run_gb300(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,201 @@
+/*
+ * ipcg.h — C ABI of the GB300-native IPC contact hot path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, and
+ * returns an int status (IPCG_OK = 0).  On failure ipcg_last_error() gives a
+ * message for the calling thread.  Position arrays are row-major (n, 3)
+ * float64, index arrays row-major int32, exactly as the reference's
+ * Eigen::MatrixXd / Eigen::MatrixXi arguments are laid out.
+ *
+ * Pointer arguments may be host memory or device memory of the current CUDA
+ * device (unified addressing decides which); host inputs are copied to the
+ * device inside the call and host outputs are written before the call
+ * returns.  Objects are not thread-safe: do not use one ipcg_mesh or
+ * ipcg_collisions from two threads at once.
+ */
+#ifndef IPCG_H
+#define IPCG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define IPCG_OK 0
+#define IPCG_ERR_INVALID 1      /* bad argument (maps to std::invalid_argument) */
+#define IPCG_ERR_CUDA 2         /* CUDA runtime error (maps to std::runtime_error) */
+#define IPCG_ERR_OOM 3          /* device allocation failed */
+#define IPCG_ERR_TOPOLOGY 4     /* face edge missing from E ("Unable to find edge!") */
+#define IPCG_ERR_NO_DEVICE 5    /* no CUDA device */
+
+/* PSD projection methods (src/ipc/utils/eigen_ext.hpp:202-206) */
+#define IPCG_PSD_NONE 0
+#define IPCG_PSD_CLAMP 1
+#define IPCG_PSD_ABS 2
+
+typedef struct ipcg_mesh ipcg_mesh;
+typedef struct ipcg_collisions ipcg_collisions;
+typedef struct ipcg_csr ipcg_csr;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* ipcg_last_error(void);
+
+/* Library version string. */
+const char* ipcg_version(void);
+
+/* Per-kernel timing: with profiling on, every kernel launch (and every CUB
+ * device call) is bracketed by CUDA events on its stream.  Enabling or
+ * disabling clears the accumulated statistics. */
+int ipcg_profile_enable(int on);
+/* JSON {"kernel": {"launches": n, "ms": total}, ...} into buf (truncated to
+ * buflen); *needed receives the full length including the terminator. */
+int ipcg_profile_report(char* buf, int64_t buflen, int64_t* needed);
+/* Number of kernel launches issued by the library since it was loaded. */
+int ipcg_launch_count(int64_t* count);
+
+/* ---------------------------------------------------------------------- */
+/* CollisionMesh                                                           */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces CollisionMesh::CollisionMesh(V, E, F)
+ * (src/ipc/collision_mesh.hpp:21-26, src/ipc/collision_mesh.cpp:15-125):
+ * uploads rest positions, edges and faces, builds faces_to_edges
+ * (collision_mesh.cpp:510-543) and keeps them resident on the device. */
+int ipcg_mesh_create(const double* rest_positions, int64_t num_vertices,
+                     const int32_t* edges, int64_t num_edges,
+                     const int32_t* faces, int64_t num_faces,
+                     ipcg_mesh** out);
+int ipcg_mesh_destroy(ipcg_mesh* mesh);
+
+/* CollisionMesh::num_vertices/num_edges/num_faces (collision_mesh.hpp) */
+int ipcg_mesh_sizes(const ipcg_mesh* mesh, int64_t sizes[3]);
+
+/* CollisionMesh::faces_to_edges() (collision_mesh.hpp:327-329): num_faces*3 */
+int ipcg_mesh_faces_to_edges(const ipcg_mesh* mesh, int32_t* out);
+
+/* The cudaStream_t (as void*) on which all work for this mesh runs. */
+int ipcg_mesh_stream(const ipcg_mesh* mesh, void** stream);
+
+/* ---------------------------------------------------------------------- */
+/* NormalCollisions                                                        */
+/* ---------------------------------------------------------------------- */
+
+int ipcg_collisions_create(ipcg_collisions** out);
+int ipcg_collisions_destroy(ipcg_collisions* collisions);
+
+/* Replaces NormalCollisions::build(mesh, V, dhat, dmin, broad_phase=nullptr)
+ * (src/ipc/collisions/normal/normal_collisions.hpp:45-50,
+ *  normal_collisions.cpp:20-158): device LBVH broad phase, FP64 distance
+ * filter d^2 < (dhat+dmin)^2, reduction to VV/EV/EE/FV with summed weights.
+ * The result stays on the device; entries are sorted by index key. */
+int ipcg_collisions_build(ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                          const double* vertices, double dhat, double dmin);
+
+/* Number of vv, ev, ee, fv collisions (NormalCollisions::{vv,ev,ee,fv}_collisions.size())
+ * and of broad-phase candidates of the last build (ee, fv): counts[6]. */
+int ipcg_collisions_counts(const ipcg_collisions* collisions, int64_t counts[6]);
+
+/* Copy the collision set out (any pointer may be NULL to skip it).
+ * vv: (nvv,2) sorted vertex pairs (min,max); ev: (nev,2) (edge, vertex);
+ * ee: (nee,2) edge pairs (ea<eb) with mollifier threshold eps_x and the
+ * stored distance type (EdgeEdgeDistanceType, distance_type.hpp);
+ * fv: (nfv,2) (face, vertex). *_w are the merged weights. */
+int ipcg_collisions_get(const ipcg_collisions* collisions,
+                        int32_t* vv, double* vv_w,
+                        int32_t* ev, double* ev_w,
+                        int32_t* ee, double* ee_eps_x, int8_t* ee_dtype, double* ee_w,
+                        int32_t* fv, double* fv_w);
+
+/* Load an explicit collision set (same layout as ipcg_collisions_get),
+ * e.g. one built elsewhere, for evaluating the potential on it. */
+int ipcg_collisions_set(ipcg_collisions* collisions, double dmin,
+                        int64_t nvv, const int32_t* vv, const double* vv_w,
+                        int64_t nev, const int32_t* ev, const double* ev_w,
+                        int64_t nee, const int32_t* ee, const double* ee_eps_x,
+                        const int8_t* ee_dtype, const double* ee_w,
+                        int64_t nfv, const int32_t* fv, const double* fv_w);
+
+/* ---------------------------------------------------------------------- */
+/* BarrierPotential (ClampedLogBarrier)                                    */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces BarrierPotential::operator()(collisions, mesh, V)
+ * (src/ipc/potentials/potential.hpp:34-40, potential.cpp:36-56,
+ *  normal_potential.cpp:127-136, barrier_potential.cpp:62-73). */
+int ipcg_barrier_energy(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                        const double* vertices, double dhat, double stiffness,
+                        int use_physical_barrier, double* energy);
+
+/* Replaces BarrierPotential::gradient(collisions, mesh, V)
+ * (potential.hpp:42-48, potential.cpp:59-95, normal_potential.cpp:138-172):
+ * gradient is a dense 3*num_vertices vector, vertex-major (3v+d). */
+int ipcg_barrier_gradient(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                          const double* vertices, double dhat, double stiffness,
+                          int use_physical_barrier, double* gradient);
+
+/* Replaces BarrierPotential::hessian(collisions, mesh, V, project_hessian_to_psd)
+ * (potential.hpp:50-60, potential.cpp:97-222, normal_potential.cpp:174-232,
+ *  eigen_ext.tpp:64-108).  Produces a (3nV x 3nV) CSR matrix held by *out;
+ * read it with ipcg_csr_* and release it with ipcg_csr_destroy.  The
+ * matrix is symmetric, so these arrays are also its CSC (Eigen ColMajor)
+ * form.  Every 3x3 vertex block touched by a contact is stored, so entries
+ * the reference skips as exact zeros may appear as explicit zeros. */
+int ipcg_barrier_hessian(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                         const double* vertices, double dhat, double stiffness,
+                         int use_physical_barrier, int psd_method, ipcg_csr** out);
+
+/* Energy, gradient and Hessian in one pass over the contacts (any output
+ * may be NULL).  Same values as the three calls above. */
+int ipcg_barrier_energy_gradient_hessian(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                                         const double* vertices, double dhat, double stiffness,
+                                         int use_physical_barrier, int psd_method,
+                                         double* energy, double* gradient, ipcg_csr** hessian);
+
+int ipcg_csr_shape(const ipcg_csr* csr, int64_t* rows, int64_t* nnz);
+/* row_ptr: rows+1 int64, col: nnz int32, val: nnz float64 (host or device) */
+int ipcg_csr_get(const ipcg_csr* csr, int64_t* row_ptr, int32_t* col, double* val);
+int ipcg_csr_destroy(ipcg_csr* csr);
+
+/* ---------------------------------------------------------------------- */
+/* compute_collision_free_stepsize                                         */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces compute_collision_free_stepsize(mesh, V0, V1, min_distance,
+ * broad_phase=nullptr, TightInclusionCCD(tolerance, max_iterations,
+ * conservative_rescaling)) (src/ipc/ipc.hpp:41-47, ipc.cpp:42-106,
+ * candidates.cpp:252-292, tight_inclusion_ccd.cpp:33-336).
+ * Defaults of the reference: tolerance 1e-6, max_iterations 1e7,
+ * conservative_rescaling 0.8.  n_candidates (may be NULL) receives the
+ * broad-phase candidate count. */
+int ipcg_collision_free_stepsize(const ipcg_mesh* mesh,
+                                 const double* vertices_t0, const double* vertices_t1,
+                                 double min_distance, double tolerance,
+                                 int64_t max_iterations, double conservative_rescaling,
+                                 double* step, int64_t* n_candidates);
+
+/* ---------------------------------------------------------------------- */
+/* Single-stencil primitives (for known-answer tests and plugin use)       */
+/* ---------------------------------------------------------------------- */
+
+/* TightInclusionCCD::point_triangle_ccd / edge_edge_ccd
+ * (tight_inclusion_ccd.cpp:229-336) on a batch of n stencils:
+ * x0, x1: (n, 4, 3) positions at t=0 and t=1 (VF: p,t0,t1,t2; EE: a0,a1,b0,b1);
+ * hit[n] (int8), toi[n]. */
+int ipcg_ccd_stencils(int is_edge_edge, int64_t n, const double* x0, const double* x1,
+                      double min_distance, double tmax, double tolerance,
+                      int64_t max_iterations, double conservative_rescaling,
+                      int8_t* hit, double* toi);
+
+/* Distance types and squared distances of a batch of n stencils
+ * (distance_type.cpp:10-211, point_triangle.cpp:11-48, edge_edge.cpp:13-56,
+ * point_edge.cpp:10-38).  kind: 0 point-edge (x: n,3,3), 1 point-triangle
+ * (n,4,3), 2 edge-edge (n,4,3).  dtype[n] (int8), dist[n]. */
+int ipcg_distance_stencils(int kind, int64_t n, const double* x, int8_t* dtype, double* dist);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* IPCG_H */

@@ -1,0 +1,543 @@
+// abi.cu — the extern "C" boundary (include/ipcg.h).
+//
+// Each entry point validates its arguments, stages host inputs on the
+// device, runs the device path and converts C++ exceptions into status
+// codes with a per-thread error message.  No entry point falls back to host
+// computation: without a CUDA device every compute call fails with
+// IPCG_ERR_NO_DEVICE.
+#include <atomic>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <unordered_map>
+
+#include "internal.cuh"
+#include "profile.cuh"
+
+using namespace ipcg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F> int guarded(F&& f)
+{
+    try {
+        f();
+        g_last_error.clear();
+        return IPCG_OK;
+    } catch (const Error& e) {
+        g_last_error = e.what();
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_last_error = "host allocation failed";
+        return IPCG_ERR_OOM;
+    } catch (const std::exception& e) {
+        g_last_error = e.what();
+        return IPCG_ERR_INVALID;
+    }
+}
+
+void require(bool ok, const char* msg)
+{
+    if (!ok) throw Error(IPCG_ERR_INVALID, msg);
+}
+
+void require_device()
+{
+    int n = 0;
+    const cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        throw Error(IPCG_ERR_NO_DEVICE, "no CUDA device available");
+    }
+}
+
+void copy_out(void* dst, const void* src_dev, size_t bytes, cudaStream_t s)
+{
+    if (bytes == 0 || dst == nullptr) return;
+    IPCG_CUDA(cudaMemcpyAsync(dst, src_dev, bytes, cudaMemcpyDefault, s));
+}
+
+} // namespace
+
+namespace ipcg {
+
+namespace prof {
+namespace {
+std::atomic<bool> g_enabled { false };
+std::atomic<long long> g_launches { 0 };
+std::mutex g_mu;
+struct Pending {
+    const char* name;
+    cudaEvent_t a, b;
+};
+std::vector<Pending> g_pending;
+std::vector<cudaEvent_t> g_free_events;
+struct Stat {
+    long long launches = 0;
+    double ms = 0;
+};
+std::map<std::string, Stat> g_stats;
+
+void drain()
+{
+    for (auto& p : g_pending) {
+        float ms = 0;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            Stat& s = g_stats[p.name];
+            s.launches++;
+            s.ms += ms;
+        }
+        g_free_events.push_back(p.a);
+        g_free_events.push_back(p.b);
+    }
+    g_pending.clear();
+    cudaGetLastError();
+}
+} // namespace
+
+bool enabled() { return g_enabled.load(std::memory_order_relaxed); }
+void count() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void make_events(cudaEvent_t* a, cudaEvent_t* b)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    for (cudaEvent_t* e : { a, b }) {
+        if (!g_free_events.empty()) {
+            *e = g_free_events.back();
+            g_free_events.pop_back();
+        } else {
+            cudaEventCreate(e);
+        }
+    }
+}
+void record(const char* name, cudaEvent_t a, cudaEvent_t b)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_pending.push_back({ name, a, b });
+}
+} // namespace prof
+
+bool is_device_ptr(const void* p)
+{
+    cudaPointerAttributes a;
+    const cudaError_t e = cudaPointerGetAttributes(&a, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf)
+{
+    if (is_device_ptr(V)) return V;
+    buf.reserve(3 * m->nV + 1);
+    if (m->nV) IPCG_CUDA(cudaMemcpyAsync(buf.p, V, sizeof(double) * 3 * m->nV, cudaMemcpyHostToDevice, m->stream));
+    return buf.p;
+}
+
+} // namespace ipcg
+
+ipcg_mesh::~ipcg_mesh()
+{
+    if (stream) cudaStreamDestroy(stream);
+}
+
+namespace {
+template <typename T> void upload(DBuf<T>& b, const T* src, size_t n, cudaStream_t s)
+{
+    b.reserve(n + 1);
+    if (n) IPCG_CUDA(cudaMemcpyAsync(b.p, src, n * sizeof(T), cudaMemcpyDefault, s));
+}
+template <typename T> std::vector<T> to_host(const T* src, size_t n)
+{
+    std::vector<T> v(n);
+    if (n) IPCG_CUDA(cudaMemcpy(v.data(), src, n * sizeof(T), cudaMemcpyDefault));
+    return v;
+}
+} // namespace
+
+extern "C" {
+
+const char* ipcg_last_error(void) { return g_last_error.c_str(); }
+
+const char* ipcg_version(void) { return "ipcg 0.1.0 (sm_103a)"; }
+
+int ipcg_profile_enable(int on)
+{
+    return guarded([&] {
+        std::lock_guard<std::mutex> lk(prof::g_mu);
+        prof::drain();
+        prof::g_stats.clear();
+        prof::g_enabled.store(on != 0);
+    });
+}
+
+int ipcg_launch_count(int64_t* count)
+{
+    return guarded([&] {
+        require(count != nullptr, "NULL argument");
+        *count = prof::g_launches.load();
+    });
+}
+
+int ipcg_profile_report(char* buf, int64_t buflen, int64_t* needed)
+{
+    return guarded([&] {
+        std::lock_guard<std::mutex> lk(prof::g_mu);
+        prof::drain();
+        std::string js = "{";
+        bool first = true;
+        for (auto& kv : prof::g_stats) {
+            char line[256];
+            snprintf(line, sizeof(line), "%s\"%s\": {\"launches\": %lld, \"ms\": %.6f}", first ? "" : ", ",
+                kv.first.c_str(), kv.second.launches, kv.second.ms);
+            js += line;
+            first = false;
+        }
+        js += "}";
+        if (needed) *needed = (int64_t)js.size() + 1;
+        if (buf && buflen > 0) {
+            const size_t n = std::min<size_t>((size_t)buflen - 1, js.size());
+            memcpy(buf, js.data(), n);
+            buf[n] = 0;
+        }
+    });
+}
+
+int ipcg_mesh_stream(const ipcg_mesh* m, void** stream)
+{
+    return guarded([&] {
+        require(m && stream, "NULL argument");
+        *stream = (void*)m->stream;
+    });
+}
+
+int ipcg_mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE, const int32_t* faces,
+    int64_t nF, ipcg_mesh** out)
+{
+    return guarded([&] {
+        require(out != nullptr, "out is NULL");
+        require(nV >= 0 && nE >= 0 && nF >= 0, "negative size");
+        require(nV < INT32_MAX && nE < INT32_MAX && nF < INT32_MAX, "mesh too large for int32 indices");
+        require(nV == 0 || rest, "rest_positions is NULL");
+        require(nE == 0 || edges, "edges is NULL");
+        require(nF == 0 || faces, "faces is NULL");
+        require(nF == 0 || nE > 0, "faces given without edges");
+        require_device();
+        // host copies of topology (for validation and faces_to_edges)
+        std::vector<int32_t> hE = to_host(edges, 2 * nE), hF = to_host(faces, 3 * nF);
+        for (int32_t v : hE) require(v >= 0 && v < nV, "edge vertex index out of range");
+        for (int32_t v : hF) require(v >= 0 && v < nV, "face vertex index out of range");
+        // faces_to_edges (collision_mesh.cpp:510-543)
+        std::unordered_map<uint64_t, int32_t> emap;
+        emap.reserve(2 * nE + 1);
+        for (int64_t e = 0; e < nE; ++e) {
+            const uint32_t a = std::min(hE[2 * e], hE[2 * e + 1]), b = std::max(hE[2 * e], hE[2 * e + 1]);
+            emap.emplace(((uint64_t)a << 32) | b, (int32_t)e);
+        }
+        std::vector<int32_t> f2e(3 * nF);
+        for (int64_t f = 0; f < nF; ++f)
+            for (int j = 0; j < 3; ++j) {
+                const uint32_t vi = hF[3 * f + j], vj = hF[3 * f + (j + 1) % 3];
+                auto it = emap.find(((uint64_t)std::min(vi, vj) << 32) | std::max(vi, vj));
+                if (it == emap.end()) throw Error(IPCG_ERR_TOPOLOGY, "Unable to find edge!");
+                f2e[3 * f + j] = it->second;
+            }
+        auto* m = new ipcg_mesh();
+        try {
+            IPCG_CUDA(cudaGetDevice(&m->device));
+            IPCG_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+            m->nV = nV;
+            m->nE = nE;
+            m->nF = nF;
+            upload(m->rest, rest, 3 * nV, m->stream);
+            upload(m->E, (const int*)hE.data(), 2 * nE, m->stream);
+            upload(m->F, (const int*)hF.data(), 3 * nF, m->stream);
+            upload(m->F2E, (const int*)f2e.data(), 3 * nF, m->stream);
+            m->h_F2E = std::move(f2e);
+            m->counters.reserve(16);
+            m->h_counters.reserve(16);
+            IPCG_CUDA(cudaStreamSynchronize(m->stream));
+        } catch (...) {
+            delete m;
+            throw;
+        }
+        *out = m;
+    });
+}
+
+int ipcg_mesh_destroy(ipcg_mesh* mesh)
+{
+    return guarded([&] { delete mesh; });
+}
+
+int ipcg_mesh_sizes(const ipcg_mesh* m, int64_t sizes[3])
+{
+    return guarded([&] {
+        require(m && sizes, "NULL argument");
+        sizes[0] = m->nV;
+        sizes[1] = m->nE;
+        sizes[2] = m->nF;
+    });
+}
+
+int ipcg_mesh_faces_to_edges(const ipcg_mesh* m, int32_t* out)
+{
+    return guarded([&] {
+        require(m && (out || m->nF == 0), "NULL argument");
+        if (m->nF) IPCG_CUDA(cudaMemcpy(out, m->h_F2E.data(), sizeof(int32_t) * 3 * m->nF, cudaMemcpyDefault));
+    });
+}
+
+int ipcg_collisions_create(ipcg_collisions** out)
+{
+    return guarded([&] {
+        require(out != nullptr, "out is NULL");
+        *out = new ipcg_collisions();
+    });
+}
+
+int ipcg_collisions_destroy(ipcg_collisions* c)
+{
+    return guarded([&] { delete c; });
+}
+
+int ipcg_collisions_build(ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat, double dmin)
+{
+    return guarded([&] {
+        require(c && mesh && (V || mesh->nV == 0), "NULL argument");
+        require(dhat > 0, "dhat must be positive");
+        require(dmin >= 0, "dmin must be non-negative");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        build_collision_set(c, m, dV, dhat, dmin);
+    });
+}
+
+int ipcg_collisions_counts(const ipcg_collisions* c, int64_t counts[6])
+{
+    return guarded([&] {
+        require(c && counts, "NULL argument");
+        counts[0] = c->nvv;
+        counts[1] = c->nev;
+        counts[2] = c->nee;
+        counts[3] = c->nfv;
+        counts[4] = c->n_cand_ee;
+        counts[5] = c->n_cand_fv;
+    });
+}
+
+int ipcg_collisions_get(const ipcg_collisions* c, int32_t* vv, double* vv_w, int32_t* ev, double* ev_w, int32_t* ee,
+    double* ee_eps, int8_t* ee_dtype, double* ee_w, int32_t* fv, double* fv_w)
+{
+    return guarded([&] {
+        require(c != nullptr, "NULL argument");
+        cudaStream_t s = 0;
+        copy_out(vv, c->vv.p, sizeof(int2) * c->nvv, s);
+        copy_out(vv_w, c->vv_w.p, sizeof(double) * c->nvv, s);
+        copy_out(ev, c->ev.p, sizeof(int2) * c->nev, s);
+        copy_out(ev_w, c->ev_w.p, sizeof(double) * c->nev, s);
+        copy_out(ee, c->ee.p, sizeof(int2) * c->nee, s);
+        copy_out(ee_eps, c->ee_eps.p, sizeof(double) * c->nee, s);
+        copy_out(ee_dtype, c->ee_dtype.p, sizeof(int8_t) * c->nee, s);
+        copy_out(ee_w, c->ee_w.p, sizeof(double) * c->nee, s);
+        copy_out(fv, c->fv.p, sizeof(int2) * c->nfv, s);
+        copy_out(fv_w, c->fv_w.p, sizeof(double) * c->nfv, s);
+        IPCG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int ipcg_collisions_set(ipcg_collisions* c, double dmin, int64_t nvv, const int32_t* vv, const double* vv_w,
+    int64_t nev, const int32_t* ev, const double* ev_w, int64_t nee, const int32_t* ee, const double* ee_eps,
+    const int8_t* ee_dtype, const double* ee_w, int64_t nfv, const int32_t* fv, const double* fv_w)
+{
+    return guarded([&] {
+        require(c != nullptr, "NULL argument");
+        require(nvv >= 0 && nev >= 0 && nee >= 0 && nfv >= 0, "negative count");
+        require_device();
+        for (int64_t i = 0; i < nee; ++i) {
+            if (ee_dtype && !is_device_ptr(ee_dtype)) require(ee_dtype[i] >= 0 && ee_dtype[i] <= 8, "bad EE dtype");
+        }
+        cudaStream_t s = 0;
+        upload(c->vv, (const int2*)vv, nvv, s);
+        upload(c->vv_w, vv_w, nvv, s);
+        upload(c->ev, (const int2*)ev, nev, s);
+        upload(c->ev_w, ev_w, nev, s);
+        upload(c->ee, (const int2*)ee, nee, s);
+        upload(c->ee_eps, ee_eps, nee, s);
+        upload(c->ee_dtype, ee_dtype, nee, s);
+        upload(c->ee_w, ee_w, nee, s);
+        upload(c->fv, (const int2*)fv, nfv, s);
+        upload(c->fv_w, fv_w, nfv, s);
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        c->nvv = nvv;
+        c->nev = nev;
+        c->nee = nee;
+        c->nfv = nfv;
+        c->dmin = dmin;
+        c->n_cand_ee = c->n_cand_fv = 0;
+    });
+}
+
+static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
+    double stiffness, int physical, int psd, double* energy, double* gradient, ipcg_csr** hessian)
+{
+    return guarded([&] {
+        require(c && mesh && (V || mesh->nV == 0), "NULL argument");
+        require(dhat > 0, "dhat must be positive");
+        require(psd >= IPCG_PSD_NONE && psd <= IPCG_PSD_ABS, "Invalid type of PSD projection!");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        BarrierArgs a { dhat, stiffness, c->dmin, physical ? 1 : 0, psd };
+        double* gdev = nullptr;
+        DBuf<double> gtmp;
+        if (gradient) {
+            if (is_device_ptr(gradient)) gdev = gradient;
+            else {
+                gtmp.reserve(3 * m->nV + 1);
+                gdev = gtmp.p;
+            }
+        }
+        ipcg_csr* H = nullptr;
+        if (hessian) H = new ipcg_csr();
+        try {
+            barrier_evaluate(c, m, dV, a, energy, gdev, H);
+            if (gradient && gdev != gradient) {
+                IPCG_CUDA(cudaMemcpyAsync(gradient, gdev, sizeof(double) * 3 * m->nV, cudaMemcpyDeviceToHost,
+                    m->stream));
+                IPCG_CUDA(cudaStreamSynchronize(m->stream));
+            }
+        } catch (...) {
+            delete H;
+            throw;
+        }
+        if (hessian) *hessian = H;
+    });
+}
+
+int ipcg_barrier_energy(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
+    double stiffness, int physical, double* energy)
+{
+    if (!energy) {
+        g_last_error = "energy is NULL";
+        return IPCG_ERR_INVALID;
+    }
+    return barrier_call(c, mesh, V, dhat, stiffness, physical, IPCG_PSD_NONE, energy, nullptr, nullptr);
+}
+
+int ipcg_barrier_gradient(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
+    double stiffness, int physical, double* gradient)
+{
+    if (!gradient) {
+        g_last_error = "gradient is NULL";
+        return IPCG_ERR_INVALID;
+    }
+    return barrier_call(c, mesh, V, dhat, stiffness, physical, IPCG_PSD_NONE, nullptr, gradient, nullptr);
+}
+
+int ipcg_barrier_hessian(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
+    double stiffness, int physical, int psd, ipcg_csr** out)
+{
+    if (!out) {
+        g_last_error = "out is NULL";
+        return IPCG_ERR_INVALID;
+    }
+    return barrier_call(c, mesh, V, dhat, stiffness, physical, psd, nullptr, nullptr, out);
+}
+
+int ipcg_barrier_energy_gradient_hessian(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V,
+    double dhat, double stiffness, int physical, int psd, double* energy, double* gradient, ipcg_csr** hessian)
+{
+    return barrier_call(c, mesh, V, dhat, stiffness, physical, psd, energy, gradient, hessian);
+}
+
+int ipcg_csr_shape(const ipcg_csr* h, int64_t* rows, int64_t* nnz)
+{
+    return guarded([&] {
+        require(h != nullptr, "NULL argument");
+        if (rows) *rows = h->rows;
+        if (nnz) *nnz = h->nnz;
+    });
+}
+
+int ipcg_csr_get(const ipcg_csr* h, int64_t* row_ptr, int32_t* col, double* val)
+{
+    return guarded([&] {
+        require(h != nullptr, "NULL argument");
+        cudaStream_t s = 0;
+        copy_out(row_ptr, h->row_ptr.p, sizeof(int64_t) * (h->rows + 1), s);
+        copy_out(col, h->col.p, sizeof(int32_t) * h->nnz, s);
+        copy_out(val, h->val.p, sizeof(double) * h->nnz, s);
+        IPCG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int ipcg_csr_destroy(ipcg_csr* h)
+{
+    return guarded([&] { delete h; });
+}
+
+int ipcg_collision_free_stepsize(const ipcg_mesh* mesh, const double* V0, const double* V1, double min_distance,
+    double tolerance, int64_t max_iterations, double rescale, double* step, int64_t* n_candidates)
+{
+    return guarded([&] {
+        require(mesh && step && ((V0 && V1) || mesh->nV == 0), "NULL argument");
+        require(min_distance >= 0, "min_distance must be non-negative");
+        require(tolerance > 0, "tolerance must be positive");
+        require(rescale > 0 && rescale <= 1, "conservative_rescaling must be in (0, 1]");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* d0 = stage_positions(m, V0, m->V0);
+        const double* d1 = stage_positions(m, V1, m->V1);
+        *step = collision_free_stepsize(m, d0, d1, min_distance, tolerance, max_iterations, rescale, n_candidates);
+    });
+}
+
+int ipcg_ccd_stencils(int is_ee, int64_t n, const double* x0, const double* x1, double min_distance, double tmax,
+    double tolerance, int64_t max_iterations, double rescale, int8_t* hit, double* toi)
+{
+    return guarded([&] {
+        require(n >= 0 && n < INT32_MAX, "bad n");
+        require(n == 0 || (x0 && x1 && hit && toi), "NULL argument");
+        require(tmax >= 0 && tmax <= 1, "tmax must be in [0, 1]");
+        require_device();
+        if (n == 0) return;
+        DBuf<double> a, b, t;
+        DBuf<int8_t> h;
+        upload(a, x0, 12 * n, 0);
+        upload(b, x1, 12 * n, 0);
+        t.reserve(n);
+        h.reserve(n);
+        ccd_stencils(0, is_ee, n, a.p, b.p, min_distance, tmax, tolerance, max_iterations, rescale, h.p, t.p);
+        copy_out(hit, h.p, n, 0);
+        copy_out(toi, t.p, sizeof(double) * n, 0);
+        IPCG_CUDA(cudaStreamSynchronize(0));
+    });
+}
+
+int ipcg_distance_stencils(int kind, int64_t n, const double* x, int8_t* dtype, double* dist)
+{
+    return guarded([&] {
+        require(kind >= 0 && kind <= 2, "bad kind");
+        require(n >= 0 && n < INT32_MAX, "bad n");
+        require(n == 0 || (x && dtype && dist), "NULL argument");
+        require_device();
+        if (n == 0) return;
+        const int per = kind == 0 ? 9 : 12;
+        DBuf<double> a, d;
+        DBuf<int8_t> t;
+        upload(a, x, per * n, 0);
+        d.reserve(n);
+        t.reserve(n);
+        distance_stencils(0, kind, n, a.p, t.p, d.p);
+        copy_out(dtype, t.p, n, 0);
+        copy_out(dist, d.p, sizeof(double) * n, 0);
+        IPCG_CUDA(cudaStreamSynchronize(0));
+    });
+}
+
+} // extern "C"

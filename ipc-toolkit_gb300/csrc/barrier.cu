@@ -1,0 +1,827 @@
+// barrier.cu — BarrierPotential energy, gradient and Hessian on the device.
+//
+// Restates src/ipc/potentials/potential.cpp:36-222 (sum over contacts,
+// dense gradient, sparse Hessian), normal_potential.cpp:127-232 (per-contact
+// w·m(x)·f(d(x)) with the mollifier product rule for edge-edge contacts),
+// barrier_potential.cpp:62-99 and barrier.cpp:11-43 (clamped log barrier on
+// d² - dmin² against (2 dmin + dhat) dhat), and eigen_ext.tpp:64-108 (PSD
+// projection by clamping or flipping negative eigenvalues).
+//
+// Design: one thread per contact.  GB300 executes FP64 at a small fraction
+// of its FP32 rate, so the per-contact 12×12 work is FP64-issue-bound and a
+// full warp of independent contacts keeps that pipe busy without any
+// intra-warp reductions.  Distance derivatives use closed forms in vertex-
+// difference variables (d = N²/D for point-plane and line-line, |a×b|²/|b−a|²
+// for point-line); the PSD projection works in the 3(n-1)-dimensional
+// complement of rigid translations (the barrier is translation invariant),
+// where a Householder tridiagonalisation plus implicit QR with Wilkinson
+// shifts gives the eigenpairs, and only the negative ones are removed from
+// the 3n×3n Hessian.  The Hessian is assembled into a CSR matrix whose
+// pattern is the union of the contacts' 3×3 vertex blocks: block keys are
+// radix-sorted and de-duplicated, and each contact adds its values with
+// FP64 atomics at positions found by binary search in its block row.
+#include <cub/block/block_reduce.cuh>
+
+#include "geom.cuh"
+#include "internal.cuh"
+#include "profile.cuh"
+
+namespace ipcg {
+
+namespace {
+
+constexpr int BLOCK = 128;
+
+struct ContactsView {
+    int64_t nvv, nev, nee, nfv;
+    const int2 *vv, *ev, *ee, *fv;
+    const double *vv_w, *ev_w, *ee_w, *fv_w, *ee_eps;
+    const int8_t* ee_dt;
+};
+
+enum : int { CT_VV = 0, CT_EV = 1, CT_EE = 2, CT_FV = 3 };
+
+struct Local {
+    int type, n, dtype;
+    int vid[4];
+    double w, eps;
+};
+
+__device__ __forceinline__ void load_contact(const ContactsView& cv, const int* __restrict__ E,
+    const int* __restrict__ F, int64_t i, Local& c)
+{
+    if (i < cv.nvv) {
+        const int2 p = cv.vv[i];
+        c.type = CT_VV;
+        c.n = 2;
+        c.vid[0] = p.x;
+        c.vid[1] = p.y;
+        c.w = cv.vv_w[i];
+        return;
+    }
+    i -= cv.nvv;
+    if (i < cv.nev) {
+        const int2 p = cv.ev[i];
+        c.type = CT_EV;
+        c.n = 3;
+        c.vid[0] = p.y;
+        c.vid[1] = E[2 * p.x];
+        c.vid[2] = E[2 * p.x + 1];
+        c.w = cv.ev_w[i];
+        return;
+    }
+    i -= cv.nev;
+    if (i < cv.nee) {
+        const int2 p = cv.ee[i];
+        c.type = CT_EE;
+        c.n = 4;
+        c.vid[0] = E[2 * p.x];
+        c.vid[1] = E[2 * p.x + 1];
+        c.vid[2] = E[2 * p.y];
+        c.vid[3] = E[2 * p.y + 1];
+        c.w = cv.ee_w[i];
+        c.eps = cv.ee_eps[i];
+        c.dtype = cv.ee_dt[i];
+        return;
+    }
+    i -= cv.nee;
+    const int2 p = cv.fv[i];
+    c.type = CT_FV;
+    c.n = 4;
+    c.vid[0] = p.y;
+    c.vid[1] = F[3 * p.x];
+    c.vid[2] = F[3 * p.x + 1];
+    c.vid[3] = F[3 * p.x + 2];
+    c.w = cv.fv_w[i];
+}
+
+// ---- barrier (barrier.cpp:11-43) ----
+__device__ __forceinline__ double barrier0(double d, double dh)
+{
+    if (d <= 0.0) return __longlong_as_double(0x7ff0000000000000ULL);
+    if (d >= dh) return 0;
+    const double dm = d - dh;
+    return -dm * dm * log(d / dh);
+}
+__device__ __forceinline__ double barrier1(double d, double dh)
+{
+    if (d <= 0.0 || d >= dh) return 0.0;
+    return (dh - d) * (2 * log(d / dh) - dh / d + 1);
+}
+__device__ __forceinline__ double barrier2(double d, double dh)
+{
+    if (d <= 0.0 || d >= dh) return 0.0;
+    const double r = dh / d;
+    return (r + 2) * r - 2 * log(d / dh) - 3;
+}
+
+struct Params {
+    double kappa, dmin2, xhat, scale; // scale = physical factor (or 1)
+    int psd;
+};
+
+// ---- closed-form squared-distance derivatives ----
+__device__ __forceinline__ void skew(V3 a, double M[3][3])
+{
+    M[0][0] = 0;
+    M[0][1] = -a.z;
+    M[0][2] = a.y;
+    M[1][0] = a.z;
+    M[1][1] = 0;
+    M[1][2] = -a.x;
+    M[2][0] = -a.y;
+    M[2][1] = a.x;
+    M[2][2] = 0;
+}
+
+// Accumulate reduced derivatives into stencil coordinates: reduced vector k
+// is x[pos[k]] - x[neg[k]].
+template <int M>
+__device__ __forceinline__ void expand_g(int N, const int* pos, const int* neg, const double* gr, double* g)
+{
+    for (int i = 0; i < N; ++i) g[i] = 0;
+    for (int k = 0; k < M; ++k)
+        for (int c = 0; c < 3; ++c) {
+            g[3 * pos[k] + c] += gr[3 * k + c];
+            g[3 * neg[k] + c] -= gr[3 * k + c];
+        }
+}
+template <int M>
+__device__ __forceinline__ void expand_h(int N, const int* pos, const int* neg, const double* Hr, double* H)
+{
+    for (int i = 0; i < N * N; ++i) H[i] = 0;
+    for (int k = 0; k < M; ++k)
+        for (int l = 0; l < M; ++l)
+            for (int c = 0; c < 3; ++c)
+                for (int e = 0; e < 3; ++e) {
+                    const double h = Hr[(3 * k + c) * (3 * M) + 3 * l + e];
+                    H[(3 * pos[k] + c) * N + 3 * pos[l] + e] += h;
+                    H[(3 * pos[k] + c) * N + 3 * neg[l] + e] -= h;
+                    H[(3 * neg[k] + c) * N + 3 * pos[l] + e] -= h;
+                    H[(3 * neg[k] + c) * N + 3 * neg[l] + e] += h;
+                }
+}
+
+// d = N²/D, N = a·(u×v), D = |u×v|²; r = (a,u,v)
+__device__ void triple_quot(V3 a, V3 u, V3 v, double* g, double* H /*81 or null*/)
+{
+    const V3 w = cross(u, v);
+    const double Nn = dot(a, w);
+    const double D = sqnorm(w);
+    const double iD = 1.0 / D;
+    const V3 gNa = w, gNu = cross(v, a), gNv = cross(a, u);
+    const V3 gDu = cross(v, w) * 2.0, gDv = cross(w, u) * 2.0;
+    double gN[9], gD[9];
+    for (int i = 0; i < 3; ++i) {
+        gN[i] = comp(gNa, i);
+        gN[3 + i] = comp(gNu, i);
+        gN[6 + i] = comp(gNv, i);
+        gD[i] = 0;
+        gD[3 + i] = comp(gDu, i);
+        gD[6 + i] = comp(gDv, i);
+    }
+    const double c1 = 2 * Nn * iD, c2 = Nn * Nn * iD * iD;
+    for (int i = 0; i < 9; ++i) g[i] = c1 * gN[i] - c2 * gD[i];
+    if (!H) return;
+    double Sv[3][3], Su[3][3], Sa[3][3], Sw[3][3];
+    skew(v, Sv);
+    skew(u, Su);
+    skew(a, Sa);
+    skew(w, Sw);
+    double HN[81], HD[81];
+    for (int i = 0; i < 81; ++i) {
+        HN[i] = 0;
+        HD[i] = 0;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            HN[i * 9 + 3 + j] = HN[(3 + j) * 9 + i] = -Sv[i][j];
+            HN[i * 9 + 6 + j] = HN[(6 + j) * 9 + i] = Su[i][j];
+            HN[(3 + i) * 9 + 6 + j] = HN[(6 + j) * 9 + 3 + i] = -Sa[i][j];
+            double uu = 0, vv = 0, uv = 0;
+            for (int k = 0; k < 3; ++k) {
+                uu += Sv[k][i] * Sv[k][j];
+                vv += Su[k][i] * Su[k][j];
+                uv -= Sv[k][i] * Su[k][j];
+            }
+            HD[(3 + i) * 9 + 3 + j] = 2 * uu;
+            HD[(6 + i) * 9 + 6 + j] = 2 * vv;
+            HD[(3 + i) * 9 + 6 + j] = HD[(6 + j) * 9 + 3 + i] = 2 * (uv - Sw[i][j]);
+        }
+    const double iD2 = iD * iD;
+    const double k1 = 2 * iD, k2 = 2 * Nn * iD, k3 = 2 * Nn * iD2, k4 = Nn * Nn * iD2, k5 = 2 * Nn * Nn * iD2 * iD;
+    for (int i = 0; i < 9; ++i)
+        for (int j = 0; j < 9; ++j)
+            H[i * 9 + j] = k1 * gN[i] * gN[j] + k2 * HN[i * 9 + j] - k3 * (gN[i] * gD[j] + gD[i] * gN[j])
+                - k4 * HD[i * 9 + j] + k5 * gD[i] * gD[j];
+}
+
+// D = |u×v|² in r = (u,v)
+__device__ void cross_sq(V3 u, V3 v, double* g, double* H /*36 or null*/)
+{
+    const V3 w = cross(u, v);
+    const V3 gu = cross(v, w) * 2.0, gv = cross(w, u) * 2.0;
+    for (int i = 0; i < 3; ++i) {
+        g[i] = comp(gu, i);
+        g[3 + i] = comp(gv, i);
+    }
+    if (!H) return;
+    double Sv[3][3], Su[3][3], Sw[3][3];
+    skew(v, Sv);
+    skew(u, Su);
+    skew(w, Sw);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double uu = 0, vv = 0, uv = 0;
+            for (int k = 0; k < 3; ++k) {
+                uu += Sv[k][i] * Sv[k][j];
+                vv += Su[k][i] * Su[k][j];
+                uv -= Sv[k][i] * Su[k][j];
+            }
+            H[i * 6 + j] = 2 * uu;
+            H[(3 + i) * 6 + 3 + j] = 2 * vv;
+            H[i * 6 + 3 + j] = H[(3 + j) * 6 + i] = 2 * (uv - Sw[i][j]);
+        }
+}
+
+// d = |a×b|²/|b−a|² in r = (a,b)
+__device__ void point_line_r(V3 a, V3 b, double* g, double* H /*36 or null*/)
+{
+    const V3 c = cross(a, b);
+    const double P = sqnorm(c);
+    const V3 e = b - a;
+    const double L = sqnorm(e);
+    const double iL = 1.0 / L;
+    double gP[6], gL[6];
+    const V3 gPa = cross(b, c) * 2.0, gPb = cross(c, a) * 2.0;
+    for (int i = 0; i < 3; ++i) {
+        gP[i] = comp(gPa, i);
+        gP[3 + i] = comp(gPb, i);
+        gL[i] = -2 * comp(e, i);
+        gL[3 + i] = 2 * comp(e, i);
+    }
+    const double iL2 = iL * iL;
+    for (int i = 0; i < 6; ++i) g[i] = gP[i] * iL - P * gL[i] * iL2;
+    if (!H) return;
+    double Sa[3][3], Sb[3][3], Sc[3][3];
+    skew(a, Sa);
+    skew(b, Sb);
+    skew(c, Sc);
+    // ∇²P = 2(JᵀJ + Σ c_k ∇²c_k) with J = [-[b]×, [a]×], ∂²c_k/∂a_i∂b_j = ε_kij
+    double HP[36];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double aa = 0, bb = 0, ab = 0;
+            for (int k = 0; k < 3; ++k) {
+                aa += Sb[k][i] * Sb[k][j];
+                bb += Sa[k][i] * Sa[k][j];
+                ab -= Sb[k][i] * Sa[k][j];
+            }
+            HP[i * 6 + j] = 2 * aa;
+            HP[(3 + i) * 6 + 3 + j] = 2 * bb;
+            HP[i * 6 + 3 + j] = HP[(3 + j) * 6 + i] = 2 * (ab - Sc[i][j]);
+        }
+    // ∇²L = 2 [[I, -I], [-I, I]]
+    const double k5 = 2 * P * iL2 * iL;
+    for (int r = 0; r < 6; ++r)
+        for (int q = 0; q < 6; ++q) {
+            const double hl = (r % 3 == q % 3) ? ((r < 3) == (q < 3) ? 2.0 : -2.0) : 0.0;
+            H[r * 6 + q] = HP[r * 6 + q] * iL - (gP[r] * gL[q] + gL[r] * gP[q]) * iL2 - P * hl * iL2
+                + k5 * gL[r] * gL[q];
+        }
+}
+
+// stencil-local squared distance + derivatives (H may be null)
+__device__ double pp_local(const V3* x, int N, int i, int j, double* g, double* H)
+{
+    const V3 r = x[i] - x[j];
+    const double gr[3] = { 2 * r.x, 2 * r.y, 2 * r.z };
+    const int pos[1] = { i }, neg[1] = { j };
+    expand_g<1>(N, pos, neg, gr, g);
+    if (H) {
+        const double Hr[9] = { 2, 0, 0, 0, 2, 0, 0, 0, 2 };
+        expand_h<1>(N, pos, neg, Hr, H);
+    }
+    return point_point_distance(x[i], x[j]);
+}
+__device__ double pl_local(const V3* x, int N, int p, int e0, int e1, double* g, double* H)
+{
+    double gr[6], Hr[36];
+    point_line_r(x[e0] - x[p], x[e1] - x[p], gr, H ? Hr : nullptr);
+    const int pos[2] = { e0, e1 }, neg[2] = { p, p };
+    expand_g<2>(N, pos, neg, gr, g);
+    if (H) expand_h<2>(N, pos, neg, Hr, H);
+    return point_line_distance(x[p], x[e0], x[e1]);
+}
+__device__ double pplane_local(const V3* x, double* g, double* H)
+{
+    double gr[9], Hr[81];
+    triple_quot(x[0] - x[1], x[2] - x[1], x[3] - x[1], gr, H ? Hr : nullptr);
+    const int pos[3] = { 0, 2, 3 }, neg[3] = { 1, 1, 1 };
+    expand_g<3>(12, pos, neg, gr, g);
+    if (H) expand_h<3>(12, pos, neg, Hr, H);
+    return point_plane_distance(x[0], x[1], x[2], x[3]);
+}
+__device__ double ll_local(const V3* x, double* g, double* H)
+{
+    double gr[9], Hr[81];
+    triple_quot(x[2] - x[0], x[1] - x[0], x[3] - x[2], gr, H ? Hr : nullptr);
+    const int pos[3] = { 2, 1, 3 }, neg[3] = { 0, 0, 2 };
+    expand_g<3>(12, pos, neg, gr, g);
+    if (H) expand_h<3>(12, pos, neg, Hr, H);
+    return line_line_distance(x[0], x[1], x[2], x[3]);
+}
+__device__ double ee_local(const V3* x, int dtype, double* g, double* H)
+{
+    switch (dtype) {
+    case EA0_EB0: return pp_local(x, 12, 0, 2, g, H);
+    case EA0_EB1: return pp_local(x, 12, 0, 3, g, H);
+    case EA1_EB0: return pp_local(x, 12, 1, 2, g, H);
+    case EA1_EB1: return pp_local(x, 12, 1, 3, g, H);
+    case EA_EB0: return pl_local(x, 12, 2, 0, 1, g, H);
+    case EA_EB1: return pl_local(x, 12, 3, 0, 1, g, H);
+    case EA0_EB: return pl_local(x, 12, 0, 2, 3, g, H);
+    case EA1_EB: return pl_local(x, 12, 1, 2, 3, g, H);
+    default: return ll_local(x, g, H);
+    }
+}
+__device__ double contact_distance(const Local& c, const V3* x, double* g, double* H)
+{
+    switch (c.type) {
+    case CT_VV: return pp_local(x, 6, 0, 1, g, H);
+    case CT_EV: return pl_local(x, 9, 0, 1, 2, g, H);
+    case CT_EE: return ee_local(x, c.dtype, g, H);
+    default: return pplane_local(x, g, H);
+    }
+}
+
+// EE mollifier m(x) (edge_edge_mollifier.cpp:42-136); gm/Hm filled iff active
+__device__ double mollifier(const Local& c, const V3* x, double* gm, double* Hm, bool& active)
+{
+    active = false;
+    if (c.type != CT_EE) return 1.0;
+    const double s = ee_cross_sqnorm(x[0], x[1], x[2], x[3]);
+    if (!(s < c.eps)) return 1.0;
+    active = true;
+    const double xe = s / c.eps;
+    const double m = (-xe + 2) * xe;
+    if (!gm) return m;
+    const double inv = 1 / c.eps;
+    const double m1 = 2 * inv * fma(-inv, s, 1.0);
+    double gr[6], Hr[36];
+    cross_sq(x[1] - x[0], x[3] - x[2], gr, Hm ? Hr : nullptr);
+    const int pos[2] = { 1, 3 }, neg[2] = { 0, 2 };
+    double gs[12];
+    expand_g<2>(12, pos, neg, gr, gs);
+    for (int i = 0; i < 12; ++i) gm[i] = m1 * gs[i];
+    if (Hm) {
+        const double m2 = -2 / (c.eps * c.eps);
+        expand_h<2>(12, pos, neg, Hr, Hm);
+        for (int i = 0; i < 12; ++i)
+            for (int j = 0; j < 12; ++j) Hm[i * 12 + j] = m1 * Hm[i * 12 + j] + m2 * gs[i] * gs[j];
+    }
+    return m;
+}
+
+// ---- symmetric eigendecomposition (n <= 9): Householder + implicit QR ----
+constexpr int MAXR = 9;
+
+__device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* d, double* Q)
+{
+    double e[MAXR];
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) Q[i * MAXR + j] = (i == j) ? 1.0 : 0.0;
+    for (int k = 0; k + 2 < n; ++k) {
+        double sig = 0;
+        for (int i = k + 2; i < n; ++i) sig += A[i * MAXR + k] * A[i * MAXR + k];
+        const double x0 = A[(k + 1) * MAXR + k];
+        if (sig == 0) {
+            e[k] = x0;
+            continue;
+        }
+        const double nx = sqrt(x0 * x0 + sig);
+        const double alpha = (x0 >= 0) ? -nx : nx;
+        double v[MAXR], p[MAXR];
+        v[k + 1] = x0 - alpha;
+        for (int i = k + 2; i < n; ++i) v[i] = A[i * MAXR + k];
+        const double tau = 2.0 / (v[k + 1] * v[k + 1] + sig);
+        double K = 0;
+        for (int i = k + 1; i < n; ++i) {
+            double s = 0;
+            for (int j = k + 1; j < n; ++j) s += A[i * MAXR + j] * v[j];
+            p[i] = tau * s;
+            K += p[i] * v[i];
+        }
+        K *= 0.5 * tau;
+        for (int i = k + 1; i < n; ++i) p[i] -= K * v[i];
+        for (int i = k + 1; i < n; ++i)
+            for (int j = k + 1; j < n; ++j) A[i * MAXR + j] -= v[i] * p[j] + p[i] * v[j];
+        e[k] = alpha;
+        for (int r = 0; r < n; ++r) {
+            double s = 0;
+            for (int j = k + 1; j < n; ++j) s += Q[r * MAXR + j] * v[j];
+            s *= tau;
+            for (int j = k + 1; j < n; ++j) Q[r * MAXR + j] -= s * v[j];
+        }
+    }
+    if (n >= 2) e[n - 2] = A[(n - 1) * MAXR + n - 2];
+    e[n - 1] = 0;
+    for (int i = 0; i < n; ++i) d[i] = A[i * MAXR + i];
+    const double eps = 2.220446049250313e-16;
+    int end = n - 1, iter = 0;
+    while (end > 0) {
+        for (int i = 0; i < end; ++i)
+            if (fabs(e[i]) <= eps * (fabs(d[i]) + fabs(d[i + 1])) || fabs(e[i]) <= 1e-300) e[i] = 0;
+        while (end > 0 && e[end - 1] == 0) --end;
+        if (end <= 0) break;
+        if (++iter > 40 * n) return false;
+        int start = end - 1;
+        while (start > 0 && e[start - 1] != 0) --start;
+        const double td = 0.5 * (d[end - 1] - d[end]);
+        const double b = e[end - 1];
+        double mu = d[end];
+        if (td == 0) mu -= fabs(b);
+        else {
+            const double h = hypot(td, b);
+            mu -= b * b / (td + (td > 0 ? h : -h));
+        }
+        double x = d[start] - mu, z = e[start];
+        for (int k = start; k < end; ++k) {
+            const double r = hypot(x, z);
+            double c = 1, s = 0;
+            if (r != 0) {
+                c = x / r;
+                s = -z / r;
+            }
+            if (k > start) e[k - 1] = c * e[k - 1] - s * z;
+            const double dk = d[k], dk1 = d[k + 1], ek = e[k];
+            d[k] = c * c * dk - 2 * c * s * ek + s * s * dk1;
+            d[k + 1] = s * s * dk + 2 * c * s * ek + c * c * dk1;
+            e[k] = c * s * (dk - dk1) + (c * c - s * s) * ek;
+            if (k < end - 1) {
+                z = -s * e[k + 1];
+                e[k + 1] = c * e[k + 1];
+            }
+            x = e[k];
+            for (int q = 0; q < n; ++q) {
+                const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
+                Q[q * MAXR + k] = c * qa - s * qb;
+                Q[q * MAXR + k + 1] = s * qa + c * qb;
+            }
+        }
+    }
+    return true;
+}
+
+// Orthonormal contrasts (rows orthogonal to (1,..,1)) for n = 2, 3, 4.
+__device__ __forceinline__ double contrast(int n, int k, int a)
+{
+    if (n == 4) {
+        const int s[3][4] = { { 1, -1, 1, -1 }, { 1, 1, -1, -1 }, { 1, -1, -1, 1 } };
+        return 0.5 * s[k][a];
+    }
+    if (n == 3) {
+        const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637;
+        const double c[2][3] = { { r2, -r2, 0.0 }, { r6, r6, -2 * r6 } };
+        return c[k][a];
+    }
+    return a == 0 ? 0.70710678118654752440 : -0.70710678118654752440;
+}
+
+// In-place PSD projection of the 3n×3n local Hessian (row-major, N = 3n).
+// Returns false if the eigensolver did not converge.
+__device__ bool project_psd(int n, double* H, int method)
+{
+    if (method == IPCG_PSD_NONE) return true;
+    const int N = 3 * n, m = 3 * (n - 1);
+    double T[MAXR * 12];
+    for (int k = 0; k < n - 1; ++k)
+        for (int c = 0; c < 3; ++c)
+            for (int j = 0; j < N; ++j) {
+                double s = 0;
+                for (int a = 0; a < n; ++a) s += contrast(n, k, a) * H[(3 * a + c) * N + j];
+                T[(3 * k + c) * 12 + j] = s;
+            }
+    double M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
+    for (int r = 0; r < m; ++r)
+        for (int l = 0; l < n - 1; ++l)
+            for (int e = 0; e < 3; ++e) {
+                double s = 0;
+                for (int b = 0; b < n; ++b) s += contrast(n, l, b) * T[r * 12 + 3 * b + e];
+                M[r * MAXR + 3 * l + e] = s;
+            }
+    // symmetrise (rounding)
+    for (int r = 0; r < m; ++r)
+        for (int s = r + 1; s < m; ++s) {
+            const double avg = 0.5 * (M[r * MAXR + s] + M[s * MAXR + r]);
+            M[r * MAXR + s] = M[s * MAXR + r] = avg;
+        }
+    if (!sym_eig(m, M, lam, Q)) return false;
+    const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
+    for (int i = 0; i < m; ++i) {
+        if (!(lam[i] < 0)) continue;
+        double v[12];
+        for (int a = 0; a < n; ++a)
+            for (int c = 0; c < 3; ++c) {
+                double s = 0;
+                for (int k = 0; k < n - 1; ++k) s += contrast(n, k, a) * Q[(3 * k + c) * MAXR + i];
+                v[3 * a + c] = s;
+            }
+        const double sl = f * lam[i];
+        for (int r = 0; r < N; ++r)
+            for (int s = 0; s < N; ++s) H[r * N + s] -= sl * v[r] * v[s];
+    }
+    return true;
+}
+
+__device__ __forceinline__ double fval(const Params& P, double d2)
+{
+    return P.kappa * (barrier0(d2 - P.dmin2, P.xhat) * P.scale);
+}
+__device__ __forceinline__ double fd1(const Params& P, double d2)
+{
+    return P.kappa * (barrier1(d2 - P.dmin2, P.xhat) * P.scale);
+}
+__device__ __forceinline__ double fd2(const Params& P, double d2)
+{
+    return P.kappa * (barrier2(d2 - P.dmin2, P.xhat) * P.scale);
+}
+
+__device__ __forceinline__ void gather(const double* __restrict__ V, const Local& c, V3* x)
+{
+    for (int i = 0; i < c.n; ++i) x[i] = load_v3(V, c.vid[i]);
+}
+
+// ---- kernels ----
+__global__ void __launch_bounds__(BLOCK) k_energy(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, Params P, double* __restrict__ partial)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (i < n) {
+        Local c;
+        load_contact(cv, E, F, i, c);
+        V3 x[4];
+        gather(V, c, x);
+        double g[12];
+        const double d = contact_distance(c, x, g, nullptr);
+        bool act;
+        const double m = mollifier(c, x, nullptr, nullptr, act);
+        e = c.w * m * fval(P, d);
+    }
+    typedef cub::BlockReduce<double, BLOCK> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const double s = BR(tmp).Sum(e);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int n, double* __restrict__ out)
+{
+    typedef cub::BlockReduce<double, 1024> BR;
+    __shared__ typename BR::TempStorage tmp;
+    double s = 0;
+    // fixed per-thread strided order => deterministic
+    for (int i = threadIdx.x; i < n; i += 1024) s += partial[i];
+    const double t = BR(tmp).Sum(s);
+    if (threadIdx.x == 0) *out = t;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_gradient(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, Params P, double* __restrict__ grad)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    V3 x[4];
+    gather(V, c, x);
+    const int N = 3 * c.n;
+    double gm[12];
+    bool act;
+    const double m = mollifier(c, x, gm, nullptr, act);
+    if (m <= 0) return;
+    double g[12];
+    const double d = contact_distance(c, x, g, nullptr);
+    const double fd = fd1(P, d);
+    double out[12];
+    if (c.type != CT_EE) {
+        for (int k = 0; k < N; ++k) out[k] = (c.w * fd) * g[k];
+    } else {
+        const double fv = fval(P, d);
+        for (int k = 0; k < N; ++k) out[k] = (c.w * fv) * (act ? gm[k] : 0.0) + (c.w * m * fd) * g[k];
+    }
+    for (int a = 0; a < c.n; ++a)
+        for (int k = 0; k < 3; ++k) {
+            const double v = out[3 * a + k];
+            if (v != 0) atomicAdd(grad + 3 * (int64_t)c.vid[a] + k, v);
+        }
+}
+
+__device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restrict__ a, int lo, int hi,
+    unsigned long long key)
+{
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_hessian(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, Params P, const unsigned long long* __restrict__ ukeys,
+    const int* __restrict__ bptr, double* __restrict__ val, int* __restrict__ fail)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    V3 x[4];
+    gather(V, c, x);
+    const int N = 3 * c.n;
+    double g[12], H[144];
+    const double d = contact_distance(c, x, g, H);
+    double Hl[144];
+    bool project = true;
+    if (c.type == CT_EE) {
+        double gm[12], Hm[144];
+        bool act;
+        const double m = mollifier(c, x, gm, Hm, act);
+        if (!act) {
+            for (int k = 0; k < 12; ++k) gm[k] = 0;
+            for (int k = 0; k < 144; ++k) Hm[k] = 0;
+        }
+        const double fv = fval(P, d);
+        if (m <= 0) {
+            for (int k = 0; k < 144; ++k) Hl[k] = (c.w * fv) * Hm[k];
+            project = false;
+        } else {
+            const double fd = fd1(P, d), fdd = fd2(P, d);
+            const double wm = c.w * m;
+            for (int r = 0; r < 12; ++r)
+                for (int s = 0; s < 12; ++s) {
+                    const double gfm_rs = (c.w * fd) * g[r] * gm[s];
+                    const double gfm_sr = (c.w * fd) * g[s] * gm[r];
+                    Hl[r * 12 + s] = (c.w * fv) * Hm[r * 12 + s] + gfm_rs + gfm_sr + (wm * fdd) * g[r] * g[s]
+                        + (wm * fd) * H[r * 12 + s];
+                }
+        }
+    } else {
+        const double fd = fd1(P, d), fdd = fd2(P, d);
+        for (int r = 0; r < N; ++r)
+            for (int s = 0; s < N; ++s) Hl[r * N + s] = (c.w * fdd) * g[r] * g[s] + (c.w * fd) * H[r * N + s];
+    }
+    if (project && !project_psd(c.n, Hl, P.psd)) atomicOr(fail, 1);
+    // scatter into CSR
+    for (int a = 0; a < c.n; ++a) {
+        const int ra = c.vid[a];
+        const int b0 = bptr[ra], b1 = bptr[ra + 1];
+        const int nbr = b1 - b0;
+        const int64_t rowbase = 9 * (int64_t)b0;
+        for (int b = 0; b < c.n; ++b) {
+            const unsigned long long key = ((unsigned long long)ra << 32) | (unsigned)c.vid[b];
+            const int q = lower_bound_u64(ukeys, b0, b1, key);
+            if (q >= b1 || ukeys[q] != key) {
+                atomicOr(fail, 2); // pattern does not hold this block: report, never write out of range
+                continue;
+            }
+            const int64_t base = rowbase + 3 * (int64_t)(q - b0);
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) {
+                    const double v = Hl[(3 * a + k) * N + 3 * b + l];
+                    if (v != 0) atomicAdd(val + base + 3 * (int64_t)k * nbr + l, v);
+                }
+        }
+    }
+}
+
+__global__ void k_block_keys(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    unsigned long long* __restrict__ keys)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    int64_t off;
+    if (i < cv.nvv) off = 4 * i;
+    else if (i < cv.nvv + cv.nev) off = 4 * cv.nvv + 9 * (i - cv.nvv);
+    else off = 4 * cv.nvv + 9 * cv.nev + 16 * (i - cv.nvv - cv.nev);
+    for (int a = 0; a < c.n; ++a)
+        for (int b = 0; b < c.n; ++b)
+            keys[off + a * c.n + b] = ((unsigned long long)c.vid[a] << 32) | (unsigned)c.vid[b];
+}
+
+__global__ void k_block_rowptr(const unsigned long long* __restrict__ ukeys, const int* __restrict__ d_nb, int nV,
+    int* __restrict__ bptr)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > nV) return;
+    bptr[r] = lower_bound_u64(ukeys, 0, *d_nb, (unsigned long long)r << 32);
+}
+
+__global__ void k_csr_rows(const int* __restrict__ bptr, int nV, int64_t* __restrict__ row_ptr)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > nV) return;
+    const int64_t b0 = bptr[r];
+    if (r == nV) {
+        row_ptr[3 * (int64_t)nV] = 9 * b0;
+        return;
+    }
+    const int64_t nbr = bptr[r + 1] - b0;
+    for (int k = 0; k < 3; ++k) row_ptr[3 * (int64_t)r + k] = 9 * b0 + 3 * k * nbr;
+}
+
+__global__ void k_csr_cols(const unsigned long long* __restrict__ ukeys, int nb, const int* __restrict__ bptr,
+    int* __restrict__ col)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nb) return;
+    const unsigned long long key = ukeys[q];
+    const int r = (int)(key >> 32), cc = (int)(key & 0xffffffffu);
+    const int b0 = bptr[r];
+    const int64_t nbr = bptr[r + 1] - b0;
+    const int64_t base = 9 * (int64_t)b0 + 3 * (int64_t)(q - b0);
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) col[base + 3 * k * nbr + l] = 3 * cc + l;
+}
+
+} // namespace
+
+void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    double* energy_host, double* grad_dev, ipcg_csr* hess)
+{
+    cudaStream_t s = m->stream;
+    ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
+        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
+    const int64_t n = cs->size();
+    const double xhat = (2 * cs->dmin + a.dhat) * a.dhat;
+    Params P { a.kappa, cs->dmin * cs->dmin, xhat, a.physical ? a.dhat / (xhat * xhat) : 1.0, a.psd };
+    const int nblk = grid_for(n, BLOCK);
+    const int64_t nV = m->nV;
+    if (energy_host) {
+        m->partial.reserve(nblk + 2);
+        if (n > 0) {
+            IPCG_LAUNCH("k_energy", s, k_energy<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, m->partial.p));
+            IPCG_LAUNCH("k_sum_partials", s, k_sum_partials<<<1, 1024, 0, s>>>(m->partial.p, nblk, m->partial.p + nblk));
+            IPCG_CHECK_LAUNCH();
+            IPCG_CUDA(cudaMemcpyAsync(energy_host, m->partial.p + nblk, sizeof(double), cudaMemcpyDeviceToHost, s));
+        } else {
+            *energy_host = 0;
+        }
+    }
+    if (grad_dev) {
+        IPCG_CUDA(cudaMemsetAsync(grad_dev, 0, sizeof(double) * 3 * nV, s));
+        if (n > 0) {
+            IPCG_LAUNCH("k_gradient", s, k_gradient<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, grad_dev));
+            IPCG_CHECK_LAUNCH();
+        }
+    }
+    if (hess) {
+        hess->rows = 3 * nV;
+        hess->stream = s;
+        const int64_t nk = 4 * cs->nvv + 9 * cs->nev + 16 * (cs->nee + cs->nfv);
+        m->keys_a.reserve(nk + 1);
+        m->keys_b.reserve(nk + 1);
+        m->counters.reserve(16);
+        int* d_nb = m->counters.p + 14;
+        int* d_fail = m->counters.p + 15;
+        IPCG_CUDA(cudaMemsetAsync(d_fail, 0, sizeof(int), s));
+        int nb = 0;
+        if (n > 0) {
+            IPCG_LAUNCH("k_block_keys", s, k_block_keys<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, m->keys_a.p));
+            IPCG_CHECK_LAUNCH();
+            sort_keys_u64(m, m->keys_a.p, m->keys_b.p, (int)nk, 32 + bits_for(nV + 1));
+            unique_u64(m, m->keys_b.p, m->keys_a.p, d_nb, (int)nk);
+            IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, s));
+            IPCG_CUDA(cudaStreamSynchronize(s));
+            nb = m->h_counters.p[0];
+        } else {
+            IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), s));
+        }
+        hess->nnz = 9 * (int64_t)nb;
+        m->ivals_a.reserve(nV + 2);
+        hess->row_ptr.reserve(3 * nV + 1);
+        hess->col.reserve(hess->nnz + 1);
+        hess->val.reserve(hess->nnz + 1);
+        int* bptr = m->ivals_a.p;
+        IPCG_LAUNCH("k_block_rowptr", s, k_block_rowptr<<<grid_for(nV + 1, 256), 256, 0, s>>>(m->keys_a.p, d_nb, (int)nV, bptr));
+        IPCG_LAUNCH("k_csr_rows", s, k_csr_rows<<<grid_for(nV + 1, 256), 256, 0, s>>>(bptr, (int)nV, hess->row_ptr.p));
+        if (nb > 0) IPCG_LAUNCH("k_csr_cols", s, k_csr_cols<<<grid_for(nb, 256), 256, 0, s>>>(m->keys_a.p, nb, bptr, hess->col.p));
+        IPCG_CUDA(cudaMemsetAsync(hess->val.p, 0, sizeof(double) * (hess->nnz + 1), s));
+        if (n > 0)
+            IPCG_LAUNCH("k_hessian", s, k_hessian<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, m->keys_a.p, bptr, hess->val.p, d_fail));
+        IPCG_CHECK_LAUNCH();
+        IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p + 1, d_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+    }
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    if (hess && (m->h_counters.p[1] & 2)) throw Error(IPCG_ERR_CUDA, "Hessian block missing from the CSR pattern");
+    if (hess && (m->h_counters.p[1] & 1))
+        throw Error(IPCG_ERR_CUDA, "unable to project matrix onto positive semi-definite cone");
+}
+
+} // namespace ipcg

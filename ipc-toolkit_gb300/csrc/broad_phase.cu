@@ -1,0 +1,367 @@
+// broad_phase.cu — device LBVH broad phase.
+//
+// Restates the reference's default broad phase (src/ipc/broad_phase/lbvh.cpp)
+// for the GPU: per-vertex boxes inflated outward with nextafter
+// (aabb.cpp:35-126), edge/face boxes as unions, FP32 node boxes rounded
+// outward (lbvh.cpp:29-41), Morton order, a Karras radix tree with atomic
+// bottom-up refit, and one-thread-per-query stack traversal emitting
+// candidates with warp-aggregated appends.  EE uses the triangular
+// self-traversal (lbvh.cpp:409-418) and FV queries vertex boxes against the
+// face tree (lbvh.cpp:756-769); both reject stencils that share a vertex
+// (lbvh.cpp:810-834).
+#include <cooperative_groups.h>
+
+#include <cfloat>
+
+#include "geom.cuh"
+#include "internal.cuh"
+#include "profile.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace ipcg {
+
+namespace {
+
+constexpr int BLOCK = 256;
+constexpr int STACK = 64;
+
+__device__ __forceinline__ void vertex_box(const double* V0, const double* V1, int v, double r, double mn[3],
+    double mx[3])
+{
+    for (int d = 0; d < 3; ++d) {
+        double a = V0[3 * v + d], b = a;
+        if (V1) {
+            const double c = V1[3 * v + d];
+            a = fmin(a, c);
+            b = fmax(b, c);
+        }
+        mn[d] = nextafter(a - r, __longlong_as_double(0xfff0000000000000ULL));
+        mx[d] = nextafter(b + r, __longlong_as_double(0x7ff0000000000000ULL));
+    }
+}
+
+__global__ void k_bounds_partial(const double* __restrict__ V0, const double* __restrict__ V1, int nV,
+    double* __restrict__ partial)
+{
+    double mn[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, mx[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x)
+        for (int d = 0; d < 3; ++d) {
+            double a = V0[3 * v + d];
+            mn[d] = fmin(mn[d], a);
+            mx[d] = fmax(mx[d], a);
+            if (V1) {
+                a = V1[3 * v + d];
+                mn[d] = fmin(mn[d], a);
+                mx[d] = fmax(mx[d], a);
+            }
+        }
+    __shared__ double s[6][BLOCK];
+    for (int d = 0; d < 3; ++d) {
+        s[d][threadIdx.x] = mn[d];
+        s[3 + d][threadIdx.x] = mx[d];
+    }
+    __syncthreads();
+    for (int w = BLOCK / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int d = 0; d < 3; ++d) {
+                s[d][threadIdx.x] = fmin(s[d][threadIdx.x], s[d][threadIdx.x + w]);
+                s[3 + d][threadIdx.x] = fmax(s[3 + d][threadIdx.x], s[3 + d][threadIdx.x + w]);
+            }
+        __syncthreads();
+    }
+    if (threadIdx.x < 6) partial[6 * blockIdx.x + threadIdx.x] = s[threadIdx.x][0];
+}
+
+__global__ void k_bounds_final(double* __restrict__ partial, int nblocks)
+{
+    // single thread: few hundred partials
+    if (threadIdx.x != 0) return;
+    double b[6] = { DBL_MAX, DBL_MAX, DBL_MAX, -DBL_MAX, -DBL_MAX, -DBL_MAX };
+    for (int i = 0; i < nblocks; ++i)
+        for (int d = 0; d < 3; ++d) {
+            b[d] = fmin(b[d], partial[6 * i + d]);
+            b[3 + d] = fmax(b[3 + d], partial[6 * i + 3 + d]);
+        }
+    for (int d = 0; d < 6; ++d) partial[d] = b[d];
+}
+
+__device__ __forceinline__ unsigned spread10(unsigned x)
+{
+    x &= 0x3ff;
+    x = (x | (x << 16)) & 0x030000FF;
+    x = (x | (x << 8)) & 0x0300F00F;
+    x = (x | (x << 4)) & 0x030C30C3;
+    x = (x | (x << 2)) & 0x09249249;
+    return x;
+}
+
+template <int K>
+__global__ void k_prim_boxes(const int* __restrict__ ids, int n, const double* __restrict__ V0,
+    const double* __restrict__ V1, double r, const double* __restrict__ bounds, float4* __restrict__ plo,
+    float4* __restrict__ phi, unsigned* __restrict__ codes, int* __restrict__ order)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double mn[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, mx[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
+    for (int k = 0; k < K; ++k) {
+        double a[3], b[3];
+        vertex_box(V0, V1, ids[K * i + k], r, a, b);
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = fmin(mn[d], a[d]);
+            mx[d] = fmax(mx[d], b[d]);
+        }
+    }
+    plo[i] = make_float4(__double2float_rd(mn[0]), __double2float_rd(mn[1]), __double2float_rd(mn[2]), 0.f);
+    phi[i] = make_float4(__double2float_ru(mx[0]), __double2float_ru(mx[1]), __double2float_ru(mx[2]), 0.f);
+    unsigned q[3];
+    for (int d = 0; d < 3; ++d) {
+        const double ext = bounds[3 + d] - bounds[d];
+        double c = ext > 0 ? (0.5 * (mn[d] + mx[d]) - bounds[d]) / ext : 0.0;
+        c = fmin(fmax(c * 1024.0, 0.0), 1023.0);
+        q[d] = (unsigned)c;
+    }
+    codes[i] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+    order[i] = i;
+}
+
+__device__ __forceinline__ int delta(const unsigned* __restrict__ c, int n, int i, int j)
+{
+    if (j < 0 || j >= n) return -1;
+    const unsigned a = c[i], b = c[j];
+    if (a == b) return 32 + __clz(i ^ j);
+    return __clz(a ^ b);
+}
+
+// Karras (2012) radix-tree construction, one thread per internal node.
+__global__ void k_karras(const unsigned* __restrict__ c, int n, float4* __restrict__ lo, float4* __restrict__ hi,
+    int* __restrict__ last, int* __restrict__ parent)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int dir = (delta(c, n, i, i + 1) - delta(c, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = delta(c, n, i, i - dir);
+    int lmax = 2;
+    while (delta(c, n, i, i + lmax * dir) > dmin) lmax *= 2;
+    int l = 0;
+    for (int t = lmax / 2; t >= 1; t /= 2)
+        if (delta(c, n, i, i + (l + t) * dir) > dmin) l += t;
+    const int j = i + l * dir;
+    const int dnode = delta(c, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) / 2;
+        if (delta(c, n, i, i + (s + t) * dir) > dnode) s += t;
+    } while (t > 1);
+    const int gamma = i + s * dir + min(dir, 0);
+    const int lo_i = min(i, j), hi_i = max(i, j);
+    const int left = (lo_i == gamma) ? (n - 1 + gamma) : gamma;
+    const int right = (hi_i == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
+    lo[i].w = __int_as_float(left);
+    hi[i].w = __int_as_float(right);
+    last[i] = hi_i;
+    parent[left] = i;
+    parent[right] = i;
+    if (i == 0) parent[0] = -1;
+}
+
+__global__ void k_leaves(const int* __restrict__ ids_sorted, int n, const float4* __restrict__ plo,
+    const float4* __restrict__ phi, float4* __restrict__ lo, float4* __restrict__ hi, int* __restrict__ last,
+    int* __restrict__ parent)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int p = ids_sorted[i];
+    float4 a = plo[p], b = phi[p];
+    a.w = __int_as_float(p);
+    b.w = __int_as_float(-1);
+    lo[n - 1 + i] = a;
+    hi[n - 1 + i] = b;
+    last[n - 1 + i] = i;
+    if (n == 1) parent[0] = -1;
+}
+
+// Bottom-up refit: the second thread to reach a node merges its children.
+__global__ void k_refit(int n, float4* lo, float4* hi, const int* __restrict__ parent, int* flags)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int node = parent[n - 1 + i];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(flags + node, 1) == 0) return;
+        __threadfence();
+        const float4 nlo = __ldcg(lo + node), nhi = __ldcg(hi + node);
+        const int l = __float_as_int(nlo.w), r = __float_as_int(nhi.w);
+        const float4 a0 = __ldcg(lo + l), a1 = __ldcg(hi + l), b0 = __ldcg(lo + r), b1 = __ldcg(hi + r);
+        __stcg(lo + node, make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), nlo.w));
+        __stcg(hi + node, make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), nhi.w));
+        node = parent[node];
+    }
+}
+
+__device__ __forceinline__ bool overlap(float4 alo, float4 ahi, float4 blo, float4 bhi)
+{
+    return alo.x <= bhi.x && blo.x <= ahi.x && alo.y <= bhi.y && blo.y <= ahi.y && alo.z <= bhi.z && blo.z <= ahi.z;
+}
+
+__device__ __forceinline__ void emit(int2* __restrict__ out, int* __restrict__ count, int cap, int2 val)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (int)g.size());
+    base = g.shfl(base, 0) + (int)g.thread_rank();
+    if (base < cap) out[base] = val;
+}
+
+// EE: triangular self traversal, one thread per sorted edge leaf.
+__global__ void k_traverse_ee(const float4* __restrict__ lo, const float4* __restrict__ hi,
+    const int* __restrict__ last, int n, const int* __restrict__ E, int2* __restrict__ out, int* __restrict__ count,
+    int cap, int* __restrict__ guard)
+{
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= n || n < 2) return;
+    const float4 qlo = lo[n - 1 + qi], qhi = hi[n - 1 + qi];
+    const int ea = __float_as_int(qlo.w);
+    const int a0 = E[2 * ea], a1 = E[2 * ea + 1];
+    int stack[STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int v = stack[--sp];
+        if (last[v] <= qi) continue;
+        const float4 vlo = lo[v], vhi = hi[v];
+        if (!overlap(qlo, qhi, vlo, vhi)) continue;
+        if (v >= n - 1) {
+            const int eb = __float_as_int(vlo.w);
+            const int b0 = E[2 * eb], b1 = E[2 * eb + 1];
+            if (a0 != b0 && a0 != b1 && a1 != b0 && a1 != b1) emit(out, count, cap, make_int2(min(ea, eb), max(ea, eb)));
+        } else {
+            if (sp + 2 > STACK) {
+                atomicOr(guard, GUARD_STACK);
+                return;
+            }
+            stack[sp++] = __float_as_int(vhi.w);
+            stack[sp++] = __float_as_int(vlo.w);
+        }
+    }
+}
+
+// FV: each vertex box queries the face tree.
+__global__ void k_traverse_fv(const float4* __restrict__ lo, const float4* __restrict__ hi, int n,
+    const double* __restrict__ V0, const double* __restrict__ V1, double r, int nV, const int* __restrict__ F,
+    int2* __restrict__ out, int* __restrict__ count, int cap, int* __restrict__ guard)
+{
+    const int vi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (vi >= nV || n < 1) return;
+    double mn[3], mx[3];
+    vertex_box(V0, V1, vi, r, mn, mx);
+    const float4 qlo = make_float4(__double2float_rd(mn[0]), __double2float_rd(mn[1]), __double2float_rd(mn[2]), 0.f);
+    const float4 qhi = make_float4(__double2float_ru(mx[0]), __double2float_ru(mx[1]), __double2float_ru(mx[2]), 0.f);
+    int stack[STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const int v = stack[--sp];
+        const float4 vlo = lo[v], vhi = hi[v];
+        if (!overlap(qlo, qhi, vlo, vhi)) continue;
+        if (v >= n - 1) {
+            const int f = __float_as_int(vlo.w);
+            if (F[3 * f] != vi && F[3 * f + 1] != vi && F[3 * f + 2] != vi) emit(out, count, cap, make_int2(f, vi));
+        } else {
+            if (sp + 2 > STACK) {
+                atomicOr(guard, GUARD_STACK);
+                return;
+            }
+            stack[sp++] = __float_as_int(vhi.w);
+            stack[sp++] = __float_as_int(vlo.w);
+        }
+    }
+}
+
+} // namespace
+
+void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const double* V1, double inflation)
+{
+    const int n = (int)(kind == 2 ? m->nE : m->nF);
+    bvh.n = n;
+    if (n == 0) return;
+    const int nn = 2 * n - 1;
+    bvh.lo.reserve(nn);
+    bvh.hi.reserve(nn);
+    bvh.last.reserve(nn);
+    bvh.parent.reserve(nn);
+    bvh.flags.reserve(n);
+    bvh.codes.reserve(n);
+    bvh.codes_sorted.reserve(n);
+    bvh.ids.reserve(n);
+    bvh.ids_sorted.reserve(n);
+    bvh.plo.reserve(n);
+    bvh.phi.reserve(n);
+    cudaStream_t s = m->stream;
+    if (kind == 2)
+        IPCG_LAUNCH("k_prim_boxes", s, k_prim_boxes<2><<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->E.p, n, V0, V1, inflation, m->bounds.p, bvh.plo.p,
+            bvh.phi.p, bvh.codes.p, bvh.ids.p));
+    else
+        IPCG_LAUNCH("k_prim_boxes", s, k_prim_boxes<3><<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->F.p, n, V0, V1, inflation, m->bounds.p, bvh.plo.p,
+            bvh.phi.p, bvh.codes.p, bvh.ids.p));
+    IPCG_CHECK_LAUNCH();
+    sort_pairs_u32(m, bvh.codes.p, bvh.codes_sorted.p, bvh.ids.p, bvh.ids_sorted.p, n, 30);
+    if (n > 1) {
+        IPCG_LAUNCH("k_karras", s, k_karras<<<grid_for(n - 1, BLOCK), BLOCK, 0, s>>>(bvh.codes_sorted.p, n, bvh.lo.p, bvh.hi.p, bvh.last.p,
+            bvh.parent.p));
+        IPCG_CHECK_LAUNCH();
+    }
+    IPCG_LAUNCH("k_leaves", s, k_leaves<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(bvh.ids_sorted.p, n, bvh.plo.p, bvh.phi.p, bvh.lo.p, bvh.hi.p,
+        bvh.last.p, bvh.parent.p));
+    IPCG_CHECK_LAUNCH();
+    if (n > 1) {
+        IPCG_CUDA(cudaMemsetAsync(bvh.flags.p, 0, sizeof(int) * (n - 1), s));
+        IPCG_LAUNCH("k_refit", s, k_refit<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(n, bvh.lo.p, bvh.hi.p, bvh.parent.p, bvh.flags.p));
+        IPCG_CHECK_LAUNCH();
+    }
+}
+
+void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, double inflation, int64_t& n_ee,
+    int64_t& n_fv)
+{
+    cudaStream_t s = m->stream;
+    const int nV = (int)m->nV;
+    // mesh bounds for the Morton normalisation
+    const int nb = 256;
+    m->bounds.reserve(6 * nb);
+    IPCG_LAUNCH("k_bounds_partial", s, k_bounds_partial<<<nb, BLOCK, 0, s>>>(V0, V1, nV, m->bounds.p));
+    IPCG_LAUNCH("k_bounds_final", s, k_bounds_final<<<1, 32, 0, s>>>(m->bounds.p, nb));
+    IPCG_CHECK_LAUNCH();
+    build_lbvh(m, m->ebvh, 2, V0, V1, inflation);
+    build_lbvh(m, m->fbvh, 3, V0, V1, inflation);
+    m->counters.reserve(8);
+    m->h_counters.reserve(8);
+    if (m->cand_cap == 0) m->cand_cap = 4 * (m->nE + m->nV) + 1024;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        const int64_t cap = m->cand_cap; // per region
+        m->cand.reserve(2 * cap);
+        IPCG_CUDA(cudaMemsetAsync(m->counters.p, 0, sizeof(int) * 8, s));
+        const int icap = (int)std::min<int64_t>(cap, INT32_MAX);
+        if (m->ebvh.n >= 2)
+            IPCG_LAUNCH("k_traverse_ee", s, k_traverse_ee<<<grid_for(m->ebvh.n, 128), 128, 0, s>>>(m->ebvh.lo.p,
+                m->ebvh.hi.p, m->ebvh.last.p, m->ebvh.n, m->E.p, m->cand.p, m->counters.p + 0, icap, m->counters.p + 2));
+        if (m->fbvh.n >= 1 && nV > 0)
+            IPCG_LAUNCH("k_traverse_fv", s, k_traverse_fv<<<grid_for(nV, 128), 128, 0, s>>>(m->fbvh.lo.p, m->fbvh.hi.p, m->fbvh.n, V0, V1, inflation,
+                nV, m->F.p, m->cand.p + cap, m->counters.p + 1, icap, m->counters.p + 2));
+        IPCG_CHECK_LAUNCH();
+        IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, m->counters.p, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        if (m->h_counters.p[2] & GUARD_STACK) throw Error(IPCG_ERR_CUDA, "LBVH traversal stack overflow");
+        const int64_t ce = (unsigned)m->h_counters.p[0], cf = (unsigned)m->h_counters.p[1];
+        if (ce <= cap && cf <= cap) {
+            n_ee = ce;
+            n_fv = cf;
+            return;
+        }
+        m->cand_cap = std::max(ce, cf) + std::max(ce, cf) / 2 + 1024;
+    }
+    throw Error(IPCG_ERR_OOM, "candidate buffer could not be sized");
+}
+
+} // namespace ipcg

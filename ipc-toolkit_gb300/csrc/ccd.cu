@@ -1,0 +1,375 @@
+// ccd.cu — compute_collision_free_stepsize on the device.
+//
+// Restates src/ipc/ipc.cpp:42-106 -> candidates.cpp:128-222 (swept-box
+// broad phase, inflation 0.5*min_distance) -> candidates.cpp:252-292
+// (earliest time of impact over all candidates with tmax pruning) ->
+// tight_inclusion_ccd.cpp:33-336 (the TightInclusionCCD strategy: initial
+// distance check, effective minimum separation, small-ToI rerun without
+// minimum separation and with no-zero-ToI, conservative rescaling).
+//
+// The root finder restates the published inclusion-based method of
+// Tight-Inclusion (Wang et al., "A Large-Scale Benchmark and an
+// Inclusion-Based Algorithm for Continuous Collision Detection", ACM TOG
+// 2021; library version 1.0.6 is what the reference links): the vertex-face
+// / edge-edge co-planarity function F(t,u,v) is multilinear, so the box of
+// its image over a parameter box is the box of its 8 corner values; boxes
+// whose image misses [-eps-ms, eps+ms]^3 are discarded and the rest are
+// bisected.  The search is a depth-first branch and bound on the earliest
+// time (earlier time halves first, boxes starting at or after the best
+// accepted time pruned), which returns the smallest lower time bound of an
+// accepted box, so the result does not depend on the tmax handed in by other
+// candidates.  One thread per candidate; this file is compiled with
+// -fmad=false so every value matches the CPU oracle bit for bit.
+#include "geom.cuh"
+#include "internal.cuh"
+#include "profile.cuh"
+
+namespace ipcg {
+
+namespace {
+
+constexpr int CCD_STACK = 128;
+constexpr int BLOCK = 128;
+
+struct Query {
+    V3 s[4], e[4];
+    bool vf;
+};
+
+struct CBox {
+    double lo[3];
+    int8_t lvl[3];
+};
+
+__device__ __forceinline__ double width_of(int lvl) { return ldexp(1.0, -lvl); }
+
+__device__ __forceinline__ double F_comp(const Query& q, int c, double t, double u, double v)
+{
+    double x[4];
+    for (int k = 0; k < 4; ++k) {
+        const double a = comp(q.s[k], c), b = comp(q.e[k], c);
+        x[k] = (b - a) * t + a;
+    }
+    if (q.vf) {
+        const double pt = (x[2] - x[1]) * u + (x[3] - x[1]) * v + x[1];
+        return x[0] - pt;
+    }
+    const double ea = (x[1] - x[0]) * u + x[0];
+    const double eb = (x[3] - x[2]) * v + x[2];
+    return ea - eb;
+}
+
+__device__ void numerical_error(const Query& q, bool use_ms, double err[3])
+{
+    const double vf_f = use_ms ? 7.549516567451064e-15 : 6.661338147750939e-15;
+    const double ee_f = use_ms ? 7.105427357601002e-15 : 6.217248937900877e-15;
+    const double filt = q.vf ? vf_f : ee_f;
+    for (int c = 0; c < 3; ++c) {
+        double m = 0;
+        for (int k = 0; k < 4; ++k) {
+            m = fmax(m, fabs(comp(q.s[k], c)));
+            m = fmax(m, fabs(comp(q.e[k], c)));
+        }
+        const double dl = fmin(m, 1.0);
+        err[c] = filt * (dl * dl * dl);
+    }
+}
+
+__device__ void domain_tol(const Query& q, double delta, double tol[3])
+{
+    for (int dim = 0; dim < 3; ++dim) {
+        double L = 0;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) {
+                double c0[3], c1[3];
+                int o = 0;
+                for (int k = 0; k < 3; ++k) {
+                    if (k == dim) {
+                        c0[k] = 0;
+                        c1[k] = 1;
+                    } else {
+                        c0[k] = c1[k] = (o++ == 0) ? a : b;
+                    }
+                }
+                double m = 0;
+                for (int c = 0; c < 3; ++c)
+                    m = fmax(m, fabs(F_comp(q, c, c1[0], c1[1], c1[2]) - F_comp(q, c, c0[0], c0[1], c0[2])));
+                L = fmax(L, m);
+            }
+        L *= 3;
+        tol[dim] = (L == 0) ? delta : delta / L;
+    }
+}
+
+__device__ bool inclusion(const Query& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3])
+{
+    const double ts[2] = { b.lo[0], b.lo[0] + width_of(b.lvl[0]) };
+    const double us[2] = { b.lo[1], b.lo[1] + width_of(b.lvl[1]) };
+    const double vs[2] = { b.lo[2], b.lo[2] + width_of(b.lvl[2]) };
+    bool zin = true;
+    box_in = true;
+    for (int c = 0; c < 3; ++c) {
+        double mn = __longlong_as_double(0x7ff0000000000000ULL), mx = -mn;
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) {
+                    const double f = F_comp(q, c, ts[i], us[j], vs[k]);
+                    mn = fmin(mn, f);
+                    mx = fmax(mx, f);
+                }
+        const double r = err[c] + ms;
+        if (mn > r || mx < -r) zin = false;
+        if (!(mn >= -r && mx <= r)) box_in = false;
+        cw[c] = mx - mn;
+    }
+    return zin;
+}
+
+__device__ bool root_finder(const Query& q, const double err[3], double ms, const double tol[3], double delta,
+    double tmax, long long max_itr, double& toi, double& out_tol)
+{
+    CBox st[CCD_STACK];
+    int sp = 0;
+    st[sp].lo[0] = st[sp].lo[1] = st[sp].lo[2] = 0;
+    st[sp].lvl[0] = st[sp].lvl[1] = st[sp].lvl[2] = 0;
+    ++sp;
+    double best = tmax;
+    bool found = false;
+    // "unlimited" iterations are capped so that no query can run away; the
+    // cap falls back to the conservative earliest unresolved time
+    const long long cap = max_itr > 0 ? max_itr : (long long)100000000;
+    long long itr = 0;
+    out_tol = 0;
+    while (sp) {
+        const CBox b = st[--sp];
+        if (b.lo[0] >= best) continue;
+        ++itr;
+        bool box_in;
+        double cw[3];
+        if (!inclusion(q, b, err, ms, box_in, cw)) continue;
+        const double w[3] = { width_of(b.lvl[0]), width_of(b.lvl[1]), width_of(b.lvl[2]) };
+        const bool small_co = cw[0] <= delta && cw[1] <= delta && cw[2] <= delta;
+        const bool small_dom = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
+        const bool too_deep = b.lvl[0] >= 60 || b.lvl[1] >= 60 || b.lvl[2] >= 60;
+        if (small_co || box_in || small_dom || too_deep || sp + 2 > CCD_STACK) {
+            best = b.lo[0];
+            found = true;
+            out_tol = fmax(out_tol, fmax(cw[0], fmax(cw[1], cw[2])));
+            continue;
+        }
+        if (itr > cap) {
+            double t = b.lo[0];
+            for (int i = 0; i < sp; ++i) t = fmin(t, st[i].lo[0]);
+            best = fmin(best, t);
+            found = true;
+            out_tol = fmax(out_tol, fmax(cw[0], fmax(cw[1], cw[2])));
+            break;
+        }
+        int sd = 0;
+        double br = w[0] / tol[0];
+        for (int d = 1; d < 3; ++d)
+            if (w[d] / tol[d] > br) {
+                br = w[d] / tol[d];
+                sd = d;
+            }
+        CBox lo = b, hi = b;
+        lo.lvl[sd] = hi.lvl[sd] = (int8_t)(b.lvl[sd] + 1);
+        hi.lo[sd] = b.lo[sd] + width_of(lo.lvl[sd]);
+        const bool keep_hi = !(q.vf && sd != 0 && hi.lo[1] + hi.lo[2] > 1.0);
+        const bool keep_lo = !(q.vf && sd != 0 && lo.lo[1] + lo.lo[2] > 1.0);
+        if (keep_hi) st[sp++] = hi;
+        if (keep_lo) st[sp++] = lo;
+    }
+    if (found) toi = best;
+    return found;
+}
+
+__device__ bool ti_ccd(const Query& q, double ms_in, double& toi, double tol_in, double tmax_in, long long max_itr,
+    double& out_tol, bool no_zero_toi)
+{
+    double err[3];
+    numerical_error(q, ms_in > 0, err);
+    double tmax = tmax_in, delta = tol_in, ms = ms_in;
+    double tol[3];
+    domain_tol(q, delta, tol);
+    bool hit = false;
+    for (int it = 0; it < 256; ++it) {
+        double t = 0;
+        hit = root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol);
+        if (hit) toi = t;
+        if (!(no_zero_toi && hit && toi == 0)) return hit;
+        if (out_tol > delta) tmax *= 0.9;
+        else if (10 * delta < ms) ms *= 0.5;
+        else {
+            delta *= 0.5;
+            domain_tol(q, delta, tol);
+        }
+    }
+    return hit;
+}
+
+struct CCDParams {
+    double tolerance;
+    long long max_iterations;
+    double rescale;
+};
+
+__device__ bool strategy(const Query& q, double min_distance, double d0, const CCDParams& P, double adj, double tmax,
+    double& toi)
+{
+    if (d0 <= min_distance) {
+        toi = 0;
+        return true;
+    }
+    double mind = (1.0 - P.rescale) * (d0 - min_distance);
+    mind = fmin(mind, 1e-4);
+    mind += min_distance;
+    double out_tol;
+    bool hit = ti_ccd(q, mind, toi, adj, tmax, P.max_iterations, out_tol, false);
+    if (hit && toi < 1e-6) {
+        hit = ti_ccd(q, min_distance, toi, adj, tmax, -1, out_tol, true);
+        if (hit) toi *= P.rescale;
+    }
+    return hit;
+}
+
+__device__ __forceinline__ bool v3eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+__device__ bool stencil_ccd(Query& q, double min_distance, const CCDParams& P, double tmax, double& toi)
+{
+    double d2;
+    if (q.vf) d2 = point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
+        point_triangle_distance_type(q.s[0], q.s[1], q.s[2], q.s[3]));
+    else d2 = edge_edge_distance(q.s[0], q.s[1], q.s[2], q.s[3],
+        edge_edge_distance_type(q.s[0], q.s[1], q.s[2], q.s[3]));
+    const double d0 = sqrt(d2);
+    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) {
+        if (d0 <= min_distance) {
+            toi = 0;
+            return true;
+        }
+        return false;
+    }
+    const double adj = fmin(0.5 * d0, P.tolerance);
+    return strategy(q, min_distance, d0, P, adj, tmax, toi);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee, int n_ee,
+    const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
+    const int* __restrict__ E, const int* __restrict__ F, double min_distance, CCDParams P,
+    unsigned long long* toi_bits)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_ee + n_fv) return;
+    Query q;
+    int ids[4];
+    if (i < n_ee) {
+        const int2 c = cand_ee[i];
+        q.vf = false;
+        ids[0] = E[2 * c.x];
+        ids[1] = E[2 * c.x + 1];
+        ids[2] = E[2 * c.y];
+        ids[3] = E[2 * c.y + 1];
+    } else {
+        const int2 c = cand_fv[i - n_ee];
+        q.vf = true;
+        ids[0] = c.y;
+        ids[1] = F[3 * c.x];
+        ids[2] = F[3 * c.x + 1];
+        ids[3] = F[3 * c.x + 2];
+    }
+    for (int k = 0; k < 4; ++k) {
+        q.s[k] = load_v3(V0, ids[k]);
+        q.e[k] = load_v3(V1, ids[k]);
+    }
+    const double tmax = __longlong_as_double((long long)*(volatile unsigned long long*)toi_bits);
+    double toi = __longlong_as_double(0x7ff0000000000000ULL);
+    if (stencil_ccd(q, min_distance, P, tmax, toi) && toi < tmax)
+        atomicMin(toi_bits, (unsigned long long)__double_as_longlong(toi));
+}
+
+__global__ void k_ccd_stencils(int is_ee, int n, const double* __restrict__ x0, const double* __restrict__ x1,
+    double min_distance, double tmax, CCDParams P, int8_t* __restrict__ hit, double* __restrict__ toi)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Query q;
+    q.vf = !is_ee;
+    for (int k = 0; k < 4; ++k) {
+        q.s[k] = load_v3(x0 + 12 * (int64_t)i, k);
+        q.e[k] = load_v3(x1 + 12 * (int64_t)i, k);
+    }
+    double t = __longlong_as_double(0x7ff0000000000000ULL);
+    const bool h = stencil_ccd(q, min_distance, P, tmax, t);
+    hit[i] = h ? 1 : 0;
+    toi[i] = t;
+}
+
+__global__ void k_distance_stencils(int kind, int n, const double* __restrict__ x, int8_t* __restrict__ dtype,
+    double* __restrict__ dist)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (kind == 0) {
+        const double* p = x + 9 * (int64_t)i;
+        const V3 a = load_v3(p, 0), b = load_v3(p, 1), c = load_v3(p, 2);
+        const int t = point_edge_distance_type(a, b, c);
+        dtype[i] = (int8_t)t;
+        dist[i] = point_edge_distance(a, b, c, t);
+    } else {
+        const double* p = x + 12 * (int64_t)i;
+        const V3 a = load_v3(p, 0), b = load_v3(p, 1), c = load_v3(p, 2), d = load_v3(p, 3);
+        if (kind == 1) {
+            const int t = point_triangle_distance_type(a, b, c, d);
+            dtype[i] = (int8_t)t;
+            dist[i] = point_triangle_distance(a, b, c, d, t);
+        } else {
+            const int t = edge_edge_distance_type(a, b, c, d);
+            dtype[i] = (int8_t)t;
+            dist[i] = edge_edge_distance(a, b, c, d, t);
+        }
+    }
+}
+
+} // namespace
+
+double collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, double min_distance,
+    double tolerance, int64_t max_iterations, double rescale, int64_t* n_candidates)
+{
+    cudaStream_t s = m->stream;
+    int64_t n_ee = 0, n_fv = 0;
+    detect_candidates(m, V0, V1, 0.5 * min_distance, n_ee, n_fv);
+    if (n_candidates) *n_candidates = n_ee + n_fv;
+    if (n_ee + n_fv == 0) return 1.0;
+    m->toi_bits.reserve(1);
+    const unsigned long long one = 0x3ff0000000000000ULL; // 1.0
+    IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    const CCDParams P { tolerance, (long long)max_iterations, rescale };
+    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(n_ee + n_fv, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p + m->cand_cap, (int)n_fv, V0,
+        V1, m->E.p, m->F.p, min_distance, P, m->toi_bits.p));
+    IPCG_CHECK_LAUNCH();
+    unsigned long long bits = 0;
+    IPCG_CUDA(cudaMemcpyAsync(&bits, m->toi_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    double t;
+    memcpy(&t, &bits, sizeof(t));
+    return t;
+}
+
+void ccd_stencils(cudaStream_t s, int is_ee, int64_t n, const double* x0, const double* x1, double min_distance,
+    double tmax, double tolerance, int64_t max_iterations, double rescale, int8_t* hit, double* toi)
+{
+    if (n <= 0) return;
+    const CCDParams P { tolerance, (long long)max_iterations, rescale };
+    IPCG_LAUNCH("k_ccd_stencils", s, k_ccd_stencils<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(is_ee, (int)n, x0, x1, min_distance, tmax, P, hit, toi));
+    IPCG_CHECK_LAUNCH();
+}
+
+void distance_stencils(cudaStream_t s, int kind, int64_t n, const double* x, int8_t* dtype, double* dist)
+{
+    if (n <= 0) return;
+    IPCG_LAUNCH("k_distance_stencils", s, k_distance_stencils<<<grid_for(n, 256), 256, 0, s>>>(kind, (int)n, x, dtype, dist));
+    IPCG_CHECK_LAUNCH();
+}
+
+} // namespace ipcg

@@ -1,0 +1,245 @@
+// collisions.cu — NormalCollisions::build on the device.
+//
+// Restates src/ipc/collisions/normal/normal_collisions.cpp:20-158 and
+// normal_collisions_builder.cpp:26-336,547-689: every EE / FV broad-phase
+// candidate is classified and measured in FP64 (bit-exact with the
+// reference's unfused evaluation; this file is compiled with -fmad=false),
+// kept if d^2 < (dhat+dmin)^2 (strict), and reduced by distance type to a
+// VV / EV / EE / FV record.  VV and EV records are merged by key with summed
+// weights (weights are 1 without area weighting, so the merged weight is the
+// multiplicity); EE and FV records are unique by construction.  All four
+// lists are sorted by key, which fixes the (thread-dependent) order of the
+// reference.
+#include <cooperative_groups.h>
+
+#include <algorithm>
+
+#include "geom.cuh"
+#include "internal.cuh"
+#include "profile.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace ipcg {
+
+namespace {
+
+constexpr int BLOCK = 256;
+
+__device__ __forceinline__ unsigned long long key2(unsigned a, unsigned b)
+{
+    return ((unsigned long long)a << 32) | (unsigned long long)b;
+}
+
+__device__ __forceinline__ int append(int* __restrict__ count)
+{
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (int)g.size());
+    return g.shfl(base, 0) + (int)g.thread_rank();
+}
+
+struct Out {
+    unsigned long long* vv; // VV keys (min,max)
+    unsigned long long* ev; // EV keys (e,v)
+    unsigned long long* ee; // EE keys (ea,eb)
+    int* ee_rec;            // EE record slot -> candidate id
+    double* ee_eps;
+    int8_t* ee_dt;
+    unsigned long long* fv; // FV keys (f,v)
+    int* count;             // [vv, ev, ee, fv]
+};
+
+__device__ __forceinline__ void put_vv(const Out& o, int a, int b)
+{
+    const int s = append(o.count + 0);
+    o.vv[s] = key2(min(a, b), max(a, b));
+}
+__device__ __forceinline__ void put_ev(const Out& o, int e, int v)
+{
+    const int s = append(o.count + 1);
+    o.ev[s] = key2(e, v);
+}
+
+// normal_collisions_builder.cpp:140-237, candidate oriented ea < eb
+__global__ void k_filter_ee(const int2* __restrict__ cand, int n, const double* __restrict__ V,
+    const double* __restrict__ rest, const int* __restrict__ E, double offset_sqr, Out o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 c = cand[i];
+    const int ea = c.x, eb = c.y;
+    const int a0 = E[2 * ea], a1 = E[2 * ea + 1], b0 = E[2 * eb], b1 = E[2 * eb + 1];
+    const V3 xa0 = load_v3(V, a0), xa1 = load_v3(V, a1), xb0 = load_v3(V, b0), xb1 = load_v3(V, b1);
+    const int actual = edge_edge_distance_type(xa0, xa1, xb0, xb1);
+    const double d = edge_edge_distance(xa0, xa1, xb0, xb1, actual);
+    if (!(d < offset_sqr)) return;
+    const double eps_x = ee_mollifier_threshold(load_v3(rest, a0), load_v3(rest, a1), load_v3(rest, b0),
+        load_v3(rest, b1));
+    const double cr = ee_cross_sqnorm(xa0, xa1, xb0, xb1);
+    const int dtype = cr < eps_x ? (int)EA_EB : actual;
+    switch (dtype) {
+    case EA0_EB0: put_vv(o, a0, b0); break;
+    case EA0_EB1: put_vv(o, a0, b1); break;
+    case EA1_EB0: put_vv(o, a1, b0); break;
+    case EA1_EB1: put_vv(o, a1, b1); break;
+    case EA_EB0: put_ev(o, ea, b0); break;
+    case EA_EB1: put_ev(o, ea, b1); break;
+    case EA0_EB: put_ev(o, eb, a0); break;
+    case EA1_EB: put_ev(o, eb, a1); break;
+    default: {
+        const int s = append(o.count + 2);
+        o.ee[s] = key2(ea, eb);
+        o.ee_rec[s] = s;
+        o.ee_eps[s] = eps_x;
+        o.ee_dt[s] = (int8_t)actual;
+    }
+    }
+}
+
+// normal_collisions_builder.cpp:239-336
+__global__ void k_filter_fv(const int2* __restrict__ cand, int n, const double* __restrict__ V,
+    const int* __restrict__ F, const int* __restrict__ F2E, double offset_sqr, Out o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 c = cand[i];
+    const int fi = c.x, vi = c.y;
+    const int f0 = F[3 * fi], f1 = F[3 * fi + 1], f2 = F[3 * fi + 2];
+    const V3 p = load_v3(V, vi), t0 = load_v3(V, f0), t1 = load_v3(V, f1), t2 = load_v3(V, f2);
+    const int dtype = point_triangle_distance_type(p, t0, t1, t2);
+    const double d = point_triangle_distance(p, t0, t1, t2, dtype);
+    if (!(d < offset_sqr)) return;
+    switch (dtype) {
+    case P_T0: put_vv(o, vi, f0); break;
+    case P_T1: put_vv(o, vi, f1); break;
+    case P_T2: put_vv(o, vi, f2); break;
+    case P_E0T: put_ev(o, F2E[3 * fi + 0], vi); break;
+    case P_E1T: put_ev(o, F2E[3 * fi + 1], vi); break;
+    case P_E2T: put_ev(o, F2E[3 * fi + 2], vi); break;
+    default: {
+        const int s = append(o.count + 3);
+        o.fv[s] = key2(fi, vi);
+    }
+    }
+}
+
+__global__ void k_unpack_rle(const unsigned long long* __restrict__ uniq, const int* __restrict__ counts,
+    const int* __restrict__ d_num, int2* __restrict__ ids, double* __restrict__ w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *d_num) return;
+    const unsigned long long k = uniq[i];
+    ids[i] = make_int2((int)(k >> 32), (int)(k & 0xffffffffu));
+    w[i] = (double)counts[i];
+}
+
+__global__ void k_unpack_keys(const unsigned long long* __restrict__ keys, int n, int2* __restrict__ ids,
+    double* __restrict__ w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = keys[i];
+    ids[i] = make_int2((int)(k >> 32), (int)(k & 0xffffffffu));
+    w[i] = 1.0;
+}
+
+__global__ void k_gather_ee(const unsigned long long* __restrict__ keys, const int* __restrict__ perm, int n,
+    const double* __restrict__ eps_in, const int8_t* __restrict__ dt_in, int2* __restrict__ ids,
+    double* __restrict__ eps, int8_t* __restrict__ dt, double* __restrict__ w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = keys[i];
+    const int p = perm[i];
+    ids[i] = make_int2((int)(k >> 32), (int)(k & 0xffffffffu));
+    eps[i] = eps_in[p];
+    dt[i] = dt_in[p];
+    w[i] = 1.0;
+}
+
+} // namespace
+
+void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, double dhat, double dmin)
+{
+    cudaStream_t s = m->stream;
+    int64_t n_ee = 0, n_fv = 0;
+    detect_candidates(m, V, nullptr, 0.5 * (dhat + dmin), n_ee, n_fv);
+    c->n_cand_ee = n_ee;
+    c->n_cand_fv = n_fv;
+    c->dmin = dmin;
+    const int64_t nc = n_ee + n_fv;
+    // raw records: at most one per candidate
+    const int64_t cap = nc + 16;
+    m->keys_a.reserve(4 * cap);
+    m->keys_b.reserve(4 * cap);
+    m->ivals_a.reserve(2 * cap);
+    m->ivals_b.reserve(3 * cap);
+    m->partial.reserve(cap);
+    m->i8tmp.reserve(cap);
+    unsigned long long* kv = m->keys_a.p;           // [vv | ev | ee | fv] regions of size cap
+    Out o;
+    o.vv = kv;
+    o.ev = kv + cap;
+    o.ee = kv + 2 * cap;
+    o.fv = kv + 3 * cap;
+    o.ee_rec = m->ivals_a.p;
+    o.ee_eps = m->partial.p;
+    o.ee_dt = m->i8tmp.p;
+    m->counters.reserve(16);
+    o.count = m->counters.p + 4;
+    IPCG_CUDA(cudaMemsetAsync(o.count, 0, sizeof(int) * 8, s));
+    const double off = (dmin + dhat) * (dmin + dhat);
+    if (n_ee)
+        IPCG_LAUNCH("k_filter_ee", s, k_filter_ee<<<grid_for(n_ee, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, V, m->rest.p, m->E.p, off, o));
+    if (n_fv)
+        IPCG_LAUNCH("k_filter_fv", s, k_filter_fv<<<grid_for(n_fv, BLOCK), BLOCK, 0, s>>>(m->cand.p + m->cand_cap, (int)n_fv, V, m->F.p,
+            m->F2E.p, off, o));
+    IPCG_CHECK_LAUNCH();
+    IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, o.count, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    const int rvv = m->h_counters.p[0], rev = m->h_counters.p[1], ree = m->h_counters.p[2], rfv = m->h_counters.p[3];
+
+    unsigned long long* ks = m->keys_b.p;
+    int* d_num = m->counters.p + 12;
+    const int idbits = 32 + bits_for(std::max(std::max(m->nV, m->nE), std::max(m->nF, (int64_t)2)));
+    // VV: sort + run-length (weights = multiplicities)
+    sort_keys_u64(m, o.vv, ks, rvv, idbits);
+    c->vv.reserve(rvv + 1);
+    c->vv_w.reserve(rvv + 1);
+    int* counts = m->ivals_b.p;
+    rle_u64(m, ks, o.vv, counts, d_num + 0, rvv); // unique keys written back into the raw vv region
+    if (rvv) IPCG_LAUNCH("k_unpack_rle", s, k_unpack_rle<<<grid_for(rvv, BLOCK), BLOCK, 0, s>>>(o.vv, counts, d_num + 0, c->vv.p, c->vv_w.p));
+    // EV
+    sort_keys_u64(m, o.ev, ks + cap, rev, idbits);
+    c->ev.reserve(rev + 1);
+    c->ev_w.reserve(rev + 1);
+    rle_u64(m, ks + cap, o.ev, counts + cap, d_num + 1, rev);
+    if (rev) IPCG_LAUNCH("k_unpack_rle", s, k_unpack_rle<<<grid_for(rev, BLOCK), BLOCK, 0, s>>>(o.ev, counts + cap, d_num + 1, c->ev.p, c->ev_w.p));
+    // EE: sort keys with record ids, gather eps / dtype
+    c->ee.reserve(ree + 1);
+    c->ee_w.reserve(ree + 1);
+    c->ee_eps.reserve(ree + 1);
+    c->ee_dtype.reserve(ree + 1);
+    if (ree) {
+        sort_pairs_u64(m, o.ee, ks + 2 * cap, o.ee_rec, m->ivals_b.p + 2 * cap, ree, idbits);
+        IPCG_LAUNCH("k_gather_ee", s, k_gather_ee<<<grid_for(ree, BLOCK), BLOCK, 0, s>>>(ks + 2 * cap, m->ivals_b.p + 2 * cap, ree, o.ee_eps, o.ee_dt,
+            c->ee.p, c->ee_eps.p, c->ee_dtype.p, c->ee_w.p));
+    }
+    // FV
+    c->fv.reserve(rfv + 1);
+    c->fv_w.reserve(rfv + 1);
+    if (rfv) {
+        sort_keys_u64(m, o.fv, ks + 3 * cap, rfv, idbits);
+        IPCG_LAUNCH("k_unpack_keys", s, k_unpack_keys<<<grid_for(rfv, BLOCK), BLOCK, 0, s>>>(ks + 3 * cap, rfv, c->fv.p, c->fv_w.p));
+    }
+    IPCG_CHECK_LAUNCH();
+    IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_num, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    c->nvv = m->h_counters.p[0];
+    c->nev = m->h_counters.p[1];
+    c->nee = ree;
+    c->nfv = rfv;
+}
+
+} // namespace ipcg

@@ -1,0 +1,185 @@
+// internal.cuh — host-side objects of the C ABI (device-resident state).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ipcg.h"
+
+namespace ipcg {
+
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) { }
+};
+
+#define IPCG_CUDA(x)                                                                                              \
+    do {                                                                                                          \
+        cudaError_t e_ = (x);                                                                                     \
+        if (e_ != cudaSuccess) {                                                                                  \
+            throw ::ipcg::Error(e_ == cudaErrorMemoryAllocation ? IPCG_ERR_OOM : IPCG_ERR_CUDA,                  \
+                std::string(#x) + ": " + cudaGetErrorString(e_));                                                 \
+        }                                                                                                         \
+    } while (0)
+
+#define IPCG_CHECK_LAUNCH() IPCG_CUDA(cudaGetLastError())
+
+// Grow-only device buffer.
+template <typename T> struct DBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    void reserve(size_t n)
+    {
+        if (n <= cap && p) return;
+        release();
+        size_t c = n < 16 ? 16 : n + n / 4;
+        IPCG_CUDA(cudaMalloc((void**)&p, c * sizeof(T)));
+        cap = c;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    ~DBuf() { release(); }
+};
+
+// Pinned host staging (for small count read-backs).
+template <typename T> struct HBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    void reserve(size_t n)
+    {
+        if (n <= cap && p) return;
+        release();
+        IPCG_CUDA(cudaMallocHost((void**)&p, n * sizeof(T)));
+        cap = n;
+    }
+    void release()
+    {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+    }
+    ~HBuf() { release(); }
+};
+
+// Linear BVH over FP32 outward-rounded boxes.  Nodes 0..n-2 are internal
+// (root = 0), n-1..2n-2 leaves in Morton order.  lo.w / hi.w hold the two
+// child indices (internal) or the primitive id / -1 (leaf) as int bits;
+// last[i] is the largest sorted leaf index under node i.
+struct LBVH {
+    int n = 0;
+    DBuf<float4> lo, hi;
+    DBuf<int> last, parent, flags;
+    DBuf<unsigned> codes, codes_sorted;
+    DBuf<int> ids, ids_sorted;
+    DBuf<float4> plo, phi; // per-primitive leaf boxes before sorting
+};
+
+// Flags of device-side guards (bit set => the call fails loudly).
+enum : int { GUARD_STACK = 1, GUARD_CAPACITY = 2 };
+
+} // namespace ipcg
+
+struct ipcg_mesh {
+    int device = 0;
+    int64_t nV = 0, nE = 0, nF = 0;
+    cudaStream_t stream = nullptr;
+    ipcg::DBuf<double> rest;
+    ipcg::DBuf<int> E, F, F2E;
+    std::vector<int32_t> h_F2E;
+    // work space shared by the calls on this mesh
+    ipcg::DBuf<double> V0, V1;       // device copies of host position inputs
+    ipcg::DBuf<double> bounds;       // mesh AABB scratch
+    ipcg::LBVH ebvh, fbvh;
+    ipcg::DBuf<int2> cand;           // broad-phase candidates (EE then FV)
+    ipcg::DBuf<int> counters;        // device counters
+    ipcg::HBuf<int> h_counters;
+    ipcg::DBuf<char> tmp;            // CUB temporary storage
+    ipcg::DBuf<unsigned long long> keys_a, keys_b;
+    ipcg::DBuf<int> ivals_a, ivals_b;
+    ipcg::DBuf<int8_t> i8tmp;
+    ipcg::DBuf<double> partial;      // reduction partials
+    ipcg::DBuf<unsigned long long> toi_bits;
+    int64_t cand_cap = 0;
+    ~ipcg_mesh();
+};
+
+struct ipcg_collisions {
+    int64_t nvv = 0, nev = 0, nee = 0, nfv = 0;
+    int64_t n_cand_ee = 0, n_cand_fv = 0;
+    double dmin = 0;
+    ipcg::DBuf<int2> vv, ev, ee, fv;
+    ipcg::DBuf<double> vv_w, ev_w, ee_w, fv_w, ee_eps;
+    ipcg::DBuf<int8_t> ee_dtype;
+    int64_t size() const { return nvv + nev + nee + nfv; }
+};
+
+struct ipcg_csr {
+    int64_t rows = 0, nnz = 0;
+    ipcg::DBuf<int64_t> row_ptr;
+    ipcg::DBuf<int> col;
+    ipcg::DBuf<double> val;
+    cudaStream_t stream = nullptr;
+};
+
+namespace ipcg {
+
+// Stage a position array on the device: returns a device pointer (the input
+// itself if it already is device memory).
+const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf);
+bool is_device_ptr(const void* p);
+
+// broad_phase.cu
+void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind /*2 edges, 3 faces*/, const double* V0, const double* V1,
+    double inflation);
+// Detect EE + FV candidates into m->cand; returns (n_ee, n_fv).
+void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, double inflation, int64_t& n_ee,
+    int64_t& n_fv);
+
+// collisions.cu
+void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, double dhat, double dmin);
+
+// barrier.cu
+struct BarrierArgs {
+    double dhat, kappa, dmin;
+    int physical;
+    int psd;
+};
+void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null);
+
+// ccd.cu
+double collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, double min_distance,
+    double tolerance, int64_t max_iterations, double rescale, int64_t* n_candidates);
+void ccd_stencils(cudaStream_t s, int is_ee, int64_t n, const double* x0, const double* x1, double min_distance,
+    double tmax, double tolerance, int64_t max_iterations, double rescale, int8_t* hit, double* toi);
+void distance_stencils(cudaStream_t s, int kind, int64_t n, const double* x, int8_t* dtype, double* dist);
+
+// sort.cu (CUB wrappers)
+void sort_pairs_u32(ipcg_mesh* m, const unsigned* k_in, unsigned* k_out, const int* v_in, int* v_out, int n,
+    int end_bit);
+void sort_keys_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* k_out, int n, int end_bit);
+void sort_pairs_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* k_out, const int* v_in,
+    int* v_out, int n, int end_bit);
+// run-length encode sorted keys; writes the number of runs to d_num (device)
+void rle_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* counts, int* d_num, int n);
+void unique_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* d_num, int n);
+
+inline int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
+inline int bits_for(int64_t n)
+{
+    int b = 1;
+    while ((1ll << b) < n) ++b;
+    return b;
+}
+
+} // namespace ipcg

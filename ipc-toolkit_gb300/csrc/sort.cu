@@ -1,0 +1,73 @@
+// sort.cu — radix sort / run-length / unique primitives (CUB device
+// algorithms), kept in one translation unit so the template instantiations
+// are compiled once.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_run_length_encode.cuh>
+#include <cub/device/device_select.cuh>
+
+#include "internal.cuh"
+#include "profile.cuh"
+
+namespace ipcg {
+
+namespace {
+// CUB device calls are timed and counted as one launch each.
+template <typename F> void with_temp(ipcg_mesh* m, const char* name, F&& f)
+{
+    size_t bytes = 0;
+    IPCG_CUDA(f(nullptr, bytes));
+    m->tmp.reserve(bytes + 256);
+    bytes = m->tmp.cap;
+    IPCG_LAUNCH(name, m->stream, IPCG_CUDA(f((void*)m->tmp.p, bytes)));
+}
+} // namespace
+
+void sort_pairs_u32(ipcg_mesh* m, const unsigned* k_in, unsigned* k_out, const int* v_in, int* v_out, int n,
+    int end_bit)
+{
+    if (n <= 0) return;
+    with_temp(m, "cub_radix_sort_pairs", [&](void* t, size_t& b) {
+        return cub::DeviceRadixSort::SortPairs(t, b, k_in, k_out, v_in, v_out, n, 0, end_bit, m->stream);
+    });
+}
+
+void sort_keys_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* k_out, int n, int end_bit)
+{
+    if (n <= 0) return;
+    with_temp(m, "cub_radix_sort_keys", [&](void* t, size_t& b) {
+        return cub::DeviceRadixSort::SortKeys(t, b, k_in, k_out, n, 0, end_bit, m->stream);
+    });
+}
+
+void sort_pairs_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* k_out, const int* v_in,
+    int* v_out, int n, int end_bit)
+{
+    if (n <= 0) return;
+    with_temp(m, "cub_radix_sort_pairs", [&](void* t, size_t& b) {
+        return cub::DeviceRadixSort::SortPairs(t, b, k_in, k_out, v_in, v_out, n, 0, end_bit, m->stream);
+    });
+}
+
+void rle_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* counts, int* d_num, int n)
+{
+    if (n <= 0) {
+        IPCG_CUDA(cudaMemsetAsync(d_num, 0, sizeof(int), m->stream));
+        return;
+    }
+    with_temp(m, "cub_run_length_encode", [&](void* t, size_t& b) {
+        return cub::DeviceRunLengthEncode::Encode(t, b, k_in, uniq, counts, d_num, n, m->stream);
+    });
+}
+
+void unique_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* d_num, int n)
+{
+    if (n <= 0) {
+        IPCG_CUDA(cudaMemsetAsync(d_num, 0, sizeof(int), m->stream));
+        return;
+    }
+    with_temp(m, "cub_select_unique", [&](void* t, size_t& b) {
+        return cub::DeviceSelect::Unique(t, b, k_in, uniq, d_num, n, m->stream);
+    });
+}
+
+} // namespace ipcg

@@ -1,0 +1,527 @@
+"""ipctk_gb300 — the reference's ``ipctk`` contact API, computed on a GB300.
+
+Mirrors the names, argument meanings and defaults of the reference's Python
+bindings for the contact hot path (python/src/collision_mesh.cpp,
+python/src/collisions/normal/normal_collisions.cpp,
+python/src/potentials/barrier_potential.cpp, python/src/ipc.cpp,
+python/src/ccd/tight_inclusion_ccd.cpp):
+
+    mesh = CollisionMesh(V, E, F)
+    collisions = NormalCollisions()
+    collisions.build(mesh, V, dhat, dmin=0.0)
+    B = BarrierPotential(dhat, stiffness)
+    E = B(collisions, mesh, V)
+    g = B.gradient(collisions, mesh, V)
+    H = B.hessian(collisions, mesh, V, PSDProjectionMethod.CLAMP)
+    alpha = compute_collision_free_stepsize(mesh, V0, V1)
+
+Every computation runs in the CUDA library ``libipcg.so`` through its C ABI
+(include/ipcg.h).  Inputs may be numpy arrays (host) or CUDA torch tensors
+(device, passed without copies).  There is no CPU fallback: if the library
+or a GPU is missing, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import os
+
+import numpy as np
+
+from . import scenes  # noqa: F401  (seeded benchmark scenes)
+
+_PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG_DIR, "_build", "libipcg.so")
+_lib = None
+
+OK = 0
+_ERRORS = {1: ValueError, 2: RuntimeError, 3: MemoryError, 4: RuntimeError, 5: RuntimeError}
+
+
+def _load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"CUDA library not built: {LIB_PATH} is missing (run the package build first)")
+    L = C.CDLL(LIB_PATH)
+    P, i64, i32, d = C.c_void_p, C.c_int64, C.c_int, C.c_double
+    PP = C.POINTER(C.c_void_p)
+    sig = {
+        "ipcg_last_error": (C.c_char_p, []),
+        "ipcg_version": (C.c_char_p, []),
+        "ipcg_mesh_create": (i32, [P, i64, P, i64, P, i64, PP]),
+        "ipcg_mesh_destroy": (i32, [P]),
+        "ipcg_mesh_sizes": (i32, [P, P]),
+        "ipcg_mesh_faces_to_edges": (i32, [P, P]),
+        "ipcg_collisions_create": (i32, [PP]),
+        "ipcg_collisions_destroy": (i32, [P]),
+        "ipcg_collisions_build": (i32, [P, P, P, d, d]),
+        "ipcg_collisions_counts": (i32, [P, P]),
+        "ipcg_collisions_get": (i32, [P] + [P] * 10),
+        "ipcg_collisions_set": (i32, [P, d, i64, P, P, i64, P, P, i64, P, P, P, P, i64, P, P]),
+        "ipcg_barrier_energy": (i32, [P, P, P, d, d, i32, P]),
+        "ipcg_barrier_gradient": (i32, [P, P, P, d, d, i32, P]),
+        "ipcg_barrier_hessian": (i32, [P, P, P, d, d, i32, i32, PP]),
+        "ipcg_barrier_energy_gradient_hessian": (i32, [P, P, P, d, d, i32, i32, P, P, PP]),
+        "ipcg_csr_shape": (i32, [P, P, P]),
+        "ipcg_csr_get": (i32, [P, P, P, P]),
+        "ipcg_csr_destroy": (i32, [P]),
+        "ipcg_collision_free_stepsize": (i32, [P, P, P, d, d, i64, d, P, P]),
+        "ipcg_ccd_stencils": (i32, [i32, i64, P, P, d, d, d, i64, d, P, P]),
+        "ipcg_distance_stencils": (i32, [i32, i64, P, P, P]),
+        "ipcg_profile_enable": (i32, [i32]),
+        "ipcg_profile_report": (i32, [C.c_char_p, i64, P]),
+        "ipcg_launch_count": (i32, [P]),
+        "ipcg_mesh_stream": (i32, [P, PP]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def lib():
+    """The loaded C-ABI library (ctypes.CDLL)."""
+    return _load()
+
+
+def _check(status):
+    if status != OK:
+        msg = _load().ipcg_last_error().decode()
+        raise _ERRORS.get(status, RuntimeError)(msg)
+
+
+def _is_torch_cuda(x):
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if _is_torch_cuda(x):
+        return C.c_void_p(x.data_ptr())
+    return x.ctypes.data_as(C.c_void_p)
+
+
+def _as_f64(x, ncols=3):
+    if _is_torch_cuda(x):
+        import torch
+        x = x.to(torch.float64).contiguous()
+        return x
+    a = np.ascontiguousarray(x, dtype=np.float64)
+    if a.ndim != 2 or (ncols and a.shape[1] != ncols):
+        raise ValueError(f"expected an (n, {ncols}) array")
+    return a
+
+
+def _as_i32(x, ncols):
+    a = np.ascontiguousarray(np.asarray(x), dtype=np.int32)
+    if a.size == 0:
+        return np.zeros((0, ncols), np.int32)
+    if a.ndim != 2 or a.shape[1] != ncols:
+        raise ValueError(f"expected an (n, {ncols}) index array")
+    return a
+
+
+def profile_enable(on: bool = True):
+    """Time every library kernel with CUDA events on its stream (clears stats)."""
+    _check(_load().ipcg_profile_enable(int(on)))
+
+
+def profile_report() -> dict:
+    """{kernel: {"launches": n, "ms": total}} accumulated since profile_enable."""
+    import json
+    L = _load()
+    need = C.c_int64()
+    _check(L.ipcg_profile_report(None, 0, C.byref(need)))
+    buf = C.create_string_buffer(need.value)
+    _check(L.ipcg_profile_report(buf, need.value, C.byref(need)))
+    return json.loads(buf.value.decode())
+
+
+def launch_count() -> int:
+    """Kernel launches issued by the library since it was loaded."""
+    n = C.c_int64()
+    _check(_load().ipcg_launch_count(C.byref(n)))
+    return int(n.value)
+
+
+class DeviceCSR:
+    """A CSR matrix held on the device by the library (ipcg_csr)."""
+
+    def __init__(self, handle, ndof):
+        self._h = handle
+        self.ndof = ndof
+        rows, nnz = C.c_int64(), C.c_int64()
+        _check(_load().ipcg_csr_shape(handle, C.byref(rows), C.byref(nnz)))
+        self.nnz = int(nnz.value)
+
+    def to_scipy(self):
+        h, self._h = self._h, None
+        return _csr_to_scipy(h, self.ndof)
+
+    def free(self):
+        if self._h:
+            _load().ipcg_csr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.ipcg_csr_destroy(self._h)
+
+
+class PSDProjectionMethod(enum.IntEnum):
+    """src/ipc/utils/eigen_ext.hpp:202-206"""
+    NONE = 0
+    CLAMP = 1
+    ABS = 2
+
+
+class EdgeEdgeDistanceType(enum.IntEnum):
+    EA0_EB0 = 0
+    EA0_EB1 = 1
+    EA1_EB0 = 2
+    EA1_EB1 = 3
+    EA_EB0 = 4
+    EA_EB1 = 5
+    EA0_EB = 6
+    EA1_EB = 7
+    EA_EB = 8
+    AUTO = 9
+
+
+class PointTriangleDistanceType(enum.IntEnum):
+    P_T0 = 0
+    P_T1 = 1
+    P_T2 = 2
+    P_E0 = 3
+    P_E1 = 4
+    P_E2 = 5
+    P_T = 6
+    AUTO = 7
+
+
+class PointEdgeDistanceType(enum.IntEnum):
+    P_E0 = 0
+    P_E1 = 1
+    P_E = 2
+    AUTO = 3
+
+
+class CollisionMesh:
+    """CollisionMesh(rest_positions, edges, faces) (src/ipc/collision_mesh.hpp:21-26).
+
+    Topology and rest positions are uploaded once and stay on the device."""
+
+    def __init__(self, rest_positions, edges=None, faces=None):
+        L = _load()
+        V = np.ascontiguousarray(np.asarray(rest_positions, dtype=np.float64))
+        if V.ndim != 2 or V.shape[1] != 3:
+            raise ValueError("only 3D meshes are supported: rest_positions must be (n, 3)")
+        E = _as_i32(edges if edges is not None else np.zeros((0, 2)), 2)
+        F = _as_i32(faces if faces is not None else np.zeros((0, 3)), 3)
+        h = C.c_void_p()
+        _check(L.ipcg_mesh_create(_ptr(V), V.shape[0], _ptr(E), E.shape[0], _ptr(F), F.shape[0], C.byref(h)))
+        self._h = h
+        self._rest = V
+        self._E = E
+        self._F = F
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.ipcg_mesh_destroy(h)
+            self._h = None
+
+    @property
+    def num_vertices(self):
+        return self._rest.shape[0]
+
+    @property
+    def num_edges(self):
+        return self._E.shape[0]
+
+    @property
+    def num_faces(self):
+        return self._F.shape[0]
+
+    @property
+    def dim(self):
+        return 3
+
+    @property
+    def ndof(self):
+        return 3 * self.num_vertices
+
+    @property
+    def rest_positions(self):
+        return self._rest
+
+    @property
+    def edges(self):
+        return self._E
+
+    @property
+    def faces(self):
+        return self._F
+
+    @property
+    def stream(self) -> int:
+        """Address of the cudaStream_t all work on this mesh runs on."""
+        p = C.c_void_p()
+        _check(_load().ipcg_mesh_stream(self._h, C.byref(p)))
+        return int(p.value or 0)
+
+    @property
+    def faces_to_edges(self):
+        out = np.zeros_like(self._F)
+        _check(_load().ipcg_mesh_faces_to_edges(self._h, _ptr(out)))
+        return out
+
+
+class NormalCollisions:
+    """NormalCollisions (src/ipc/collisions/normal/normal_collisions.hpp).
+
+    The set lives on the device; the ``*_collisions`` properties copy it out
+    as index arrays (sorted by key)."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _check(_load().ipcg_collisions_create(C.byref(h)))
+        self._h = h
+        self._cache = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.ipcg_collisions_destroy(h)
+            self._h = None
+
+    def build(self, mesh: CollisionMesh, vertices, dhat: float, dmin: float = 0.0, broad_phase=None):
+        """normal_collisions.cpp:20-36.  ``broad_phase`` is accepted for API
+        compatibility; the device LBVH is always used."""
+        V = _as_f64(vertices)
+        _check(_load().ipcg_collisions_build(self._h, mesh._h, _ptr(V), float(dhat), float(dmin)))
+        self._cache = None
+
+    def counts(self):
+        c = np.zeros(6, np.int64)
+        _check(_load().ipcg_collisions_counts(self._h, _ptr(c)))
+        return c
+
+    def __len__(self):
+        return int(self.counts()[:4].sum())
+
+    def size(self):
+        return len(self)
+
+    def empty(self):
+        return len(self) == 0
+
+    @property
+    def num_candidates(self):
+        c = self.counts()
+        return int(c[4] + c[5])
+
+    def to_arrays(self):
+        """dict with vv, vv_w, ev, ev_w, ee, ee_eps_x, ee_dtype, ee_w, fv, fv_w."""
+        if self._cache is None:
+            nvv, nev, nee, nfv = (int(x) for x in self.counts()[:4])
+            a = dict(vv=np.zeros((nvv, 2), np.int32), vv_w=np.zeros(nvv), ev=np.zeros((nev, 2), np.int32),
+                     ev_w=np.zeros(nev), ee=np.zeros((nee, 2), np.int32), ee_eps_x=np.zeros(nee),
+                     ee_dtype=np.zeros(nee, np.int8), ee_w=np.zeros(nee), fv=np.zeros((nfv, 2), np.int32),
+                     fv_w=np.zeros(nfv))
+            _check(_load().ipcg_collisions_get(self._h, *(_ptr(a[k]) for k in (
+                "vv", "vv_w", "ev", "ev_w", "ee", "ee_eps_x", "ee_dtype", "ee_w", "fv", "fv_w"))))
+            self._cache = a
+        return self._cache
+
+    def set_arrays(self, vv, vv_w, ev, ev_w, ee, ee_eps_x, ee_dtype, ee_w, fv, fv_w, dmin=0.0):
+        arrs = [_as_i32(vv, 2), np.ascontiguousarray(vv_w, np.float64), _as_i32(ev, 2),
+                np.ascontiguousarray(ev_w, np.float64), _as_i32(ee, 2), np.ascontiguousarray(ee_eps_x, np.float64),
+                np.ascontiguousarray(ee_dtype, np.int8), np.ascontiguousarray(ee_w, np.float64),
+                _as_i32(fv, 2), np.ascontiguousarray(fv_w, np.float64)]
+        _check(_load().ipcg_collisions_set(
+            self._h, float(dmin), len(arrs[1]), _ptr(arrs[0]), _ptr(arrs[1]), len(arrs[3]), _ptr(arrs[2]),
+            _ptr(arrs[3]), len(arrs[5]), _ptr(arrs[4]), _ptr(arrs[5]), _ptr(arrs[6]), _ptr(arrs[7]),
+            len(arrs[9]), _ptr(arrs[8]), _ptr(arrs[9])))
+        self._cache = None
+
+    @property
+    def vv_collisions(self):
+        return self.to_arrays()["vv"]
+
+    @property
+    def ev_collisions(self):
+        return self.to_arrays()["ev"]
+
+    @property
+    def ee_collisions(self):
+        return self.to_arrays()["ee"]
+
+    @property
+    def fv_collisions(self):
+        return self.to_arrays()["fv"]
+
+
+def _csr_to_scipy(h, ndof):
+    import scipy.sparse as sp
+    L = _load()
+    rows, nnz = C.c_int64(), C.c_int64()
+    _check(L.ipcg_csr_shape(h, C.byref(rows), C.byref(nnz)))
+    rp = np.zeros(rows.value + 1, np.int64)
+    ci = np.zeros(nnz.value, np.int32)
+    va = np.zeros(nnz.value)
+    _check(L.ipcg_csr_get(h, _ptr(rp), _ptr(ci), _ptr(va)))
+    _check(L.ipcg_csr_destroy(h))
+    # symmetric: CSR arrays are also the CSC arrays (Eigen ColMajor)
+    return sp.csc_matrix((va, ci, rp), shape=(ndof, ndof))
+
+
+class BarrierPotential:
+    """BarrierPotential(dhat, stiffness, use_physical_barrier=False)
+    (src/ipc/potentials/barrier_potential.hpp:24-27) with the default
+    ClampedLogBarrier."""
+
+    def __init__(self, dhat: float, stiffness: float, use_physical_barrier: bool = False):
+        if not dhat > 0:
+            raise ValueError("dhat must be positive")
+        self.dhat = float(dhat)
+        self.stiffness = float(stiffness)
+        self.use_physical_barrier = bool(use_physical_barrier)
+
+    def __call__(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices) -> float:
+        V = _as_f64(vertices)
+        e = np.zeros(1)
+        _check(_load().ipcg_barrier_energy(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
+                                           int(self.use_physical_barrier), _ptr(e)))
+        return float(e[0])
+
+    def gradient(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices):
+        V = _as_f64(vertices)
+        if _is_torch_cuda(V):
+            import torch
+            g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
+        else:
+            g = np.zeros(V.size)
+        _check(_load().ipcg_barrier_gradient(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
+                                             int(self.use_physical_barrier), _ptr(g)))
+        return g
+
+    def hessian(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices,
+                project_hessian_to_psd=PSDProjectionMethod.NONE):
+        V = _as_f64(vertices)
+        h = C.c_void_p()
+        _check(_load().ipcg_barrier_hessian(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
+                                            int(self.use_physical_barrier), int(project_hessian_to_psd),
+                                            C.byref(h)))
+        return _csr_to_scipy(h, 3 * mesh.num_vertices)
+
+    def hessian_device(self, collisions, mesh, vertices, project_hessian_to_psd=PSDProjectionMethod.NONE):
+        """Like hessian() but the CSR stays on the device (DeviceCSR)."""
+        V = _as_f64(vertices)
+        h = C.c_void_p()
+        _check(_load().ipcg_barrier_hessian(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
+                                            int(self.use_physical_barrier), int(project_hessian_to_psd),
+                                            C.byref(h)))
+        return DeviceCSR(h, 3 * mesh.num_vertices)
+
+    def energy_gradient_hessian(self, collisions, mesh, vertices, project_hessian_to_psd=PSDProjectionMethod.NONE):
+        """Energy, gradient and Hessian from one call."""
+        V = _as_f64(vertices)
+        e = np.zeros(1)
+        g = np.zeros(3 * mesh.num_vertices)
+        h = C.c_void_p()
+        _check(_load().ipcg_barrier_energy_gradient_hessian(
+            collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, int(self.use_physical_barrier),
+            int(project_hessian_to_psd), _ptr(e), _ptr(g), C.byref(h)))
+        return float(e[0]), g, _csr_to_scipy(h, 3 * mesh.num_vertices)
+
+
+class TightInclusionCCD:
+    """TightInclusionCCD(tolerance, max_iterations, conservative_rescaling)
+    (src/ipc/ccd/tight_inclusion_ccd.hpp:11-28)."""
+    DEFAULT_TOLERANCE = 1e-6
+    DEFAULT_MAX_ITERATIONS = 10_000_000
+    DEFAULT_CONSERVATIVE_RESCALING = 0.8
+    SMALL_TOI = 1e-6
+
+    def __init__(self, tolerance=DEFAULT_TOLERANCE, max_iterations=DEFAULT_MAX_ITERATIONS,
+                 conservative_rescaling=DEFAULT_CONSERVATIVE_RESCALING):
+        self.tolerance = float(tolerance)
+        self.max_iterations = int(max_iterations)
+        self.conservative_rescaling = float(conservative_rescaling)
+
+    def _batch(self, is_ee, x0, x1, min_distance, tmax):
+        x0 = np.ascontiguousarray(x0, np.float64).reshape(-1, 4, 3)
+        x1 = np.ascontiguousarray(x1, np.float64).reshape(-1, 4, 3)
+        n = x0.shape[0]
+        hit = np.zeros(n, np.int8)
+        toi = np.zeros(n)
+        _check(_load().ipcg_ccd_stencils(int(is_ee), n, _ptr(x0), _ptr(x1), float(min_distance), float(tmax),
+                                         self.tolerance, self.max_iterations, self.conservative_rescaling,
+                                         _ptr(hit), _ptr(toi)))
+        return hit.astype(bool), toi
+
+    def point_triangle_ccd(self, p_t0, t0_t0, t1_t0, t2_t0, p_t1, t0_t1, t1_t1, t2_t1, min_distance=0.0, tmax=1.0):
+        hit, toi = self._batch(False, np.stack([p_t0, t0_t0, t1_t0, t2_t0]), np.stack([p_t1, t0_t1, t1_t1, t2_t1]),
+                               min_distance, tmax)
+        return bool(hit[0]), float(toi[0])
+
+    def edge_edge_ccd(self, ea0_t0, ea1_t0, eb0_t0, eb1_t0, ea0_t1, ea1_t1, eb0_t1, eb1_t1, min_distance=0.0,
+                      tmax=1.0):
+        hit, toi = self._batch(True, np.stack([ea0_t0, ea1_t0, eb0_t0, eb1_t0]),
+                               np.stack([ea0_t1, ea1_t1, eb0_t1, eb1_t1]), min_distance, tmax)
+        return bool(hit[0]), float(toi[0])
+
+    def point_edge_ccd(self, p_t0, e0_t0, e1_t0, p_t1, e0_t1, e1_t1, min_distance=0.0, tmax=1.0):
+        """Degenerate edge-edge, as tight_inclusion_ccd.cpp:171-180."""
+        return self.edge_edge_ccd(p_t0, p_t0, e0_t0, e1_t0, p_t1, p_t1, e0_t1, e1_t1, min_distance, tmax)
+
+    def point_point_ccd(self, p0_t0, p1_t0, p0_t1, p1_t1, min_distance=0.0, tmax=1.0):
+        """Degenerate edge-edge, as tight_inclusion_ccd.cpp:98-107."""
+        return self.edge_edge_ccd(p0_t0, p0_t0, p1_t0, p1_t0, p0_t1, p0_t1, p1_t1, p1_t1, min_distance, tmax)
+
+
+DEFAULT_NARROW_PHASE_CCD = TightInclusionCCD()
+
+
+def compute_collision_free_stepsize(mesh: CollisionMesh, vertices_t0, vertices_t1, min_distance: float = 0.0,
+                                    broad_phase=None, narrow_phase_ccd: TightInclusionCCD = DEFAULT_NARROW_PHASE_CCD):
+    """src/ipc/ipc.hpp:41-47.  ``broad_phase`` is accepted for API
+    compatibility; the device LBVH is always used."""
+    V0, V1 = _as_f64(vertices_t0), _as_f64(vertices_t1)
+    step = np.zeros(1)
+    _check(_load().ipcg_collision_free_stepsize(
+        mesh._h, _ptr(V0), _ptr(V1), float(min_distance), narrow_phase_ccd.tolerance,
+        narrow_phase_ccd.max_iterations, narrow_phase_ccd.conservative_rescaling, _ptr(step), None))
+    return float(step[0])
+
+
+def distance_stencils(kind: int, x):
+    """Batched distance types + squared distances (kind 0 point-edge, 1
+    point-triangle, 2 edge-edge) computed on the device."""
+    per = 3 if kind == 0 else 4
+    x = np.ascontiguousarray(x, np.float64).reshape(-1, per, 3)
+    n = x.shape[0]
+    dt = np.zeros(n, np.int8)
+    d = np.zeros(n)
+    _check(_load().ipcg_distance_stencils(int(kind), n, _ptr(x), _ptr(dt), _ptr(d)))
+    return dt, d
+
+
+def edges(F):
+    """Unique undirected edges of a triangle mesh (like igl::edges)."""
+    return scenes.edges_from_faces(np.asarray(F))
+
+
+__all__ = [
+    "CollisionMesh", "NormalCollisions", "BarrierPotential", "PSDProjectionMethod", "TightInclusionCCD",
+    "compute_collision_free_stepsize", "EdgeEdgeDistanceType", "PointTriangleDistanceType",
+    "PointEdgeDistanceType", "distance_stencils", "edges", "lib", "LIB_PATH", "profile_enable",
+    "profile_report", "launch_count", "DeviceCSR",
+]

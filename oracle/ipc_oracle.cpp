@@ -1,0 +1,1875 @@
+// ipc_oracle.cpp — CPU restatement of IPC Toolkit's contact hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library:
+// only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+// it.  Nothing in the product links or calls it.
+//
+// It restates, in plain C++17 (no Eigen/TBB), the reference algorithms of
+// ipc-sim/ipc-toolkit v1.6.0 for:
+//   * collision-mesh topology     src/ipc/collision_mesh.cpp:510-543
+//   * AABB inflation + LBVH       src/ipc/broad_phase/aabb.cpp:35-126,
+//                                 src/ipc/broad_phase/lbvh.cpp:29-330,368-455
+//   * distance types / distances  src/ipc/distance/distance_type.cpp:10-211,
+//                                 point_point.cpp:5-9, point_line.cpp:5-23,
+//                                 point_plane.cpp:10-26, line_line.cpp:7-16,
+//                                 point_triangle.cpp:11-48, edge_edge.cpp:13-56
+//   * collision-set build         src/ipc/collisions/normal/normal_collisions.cpp:20-158,
+//                                 normal_collisions_builder.cpp:26-336,547-689
+//   * barrier potential E/G/H     src/ipc/barrier/barrier.cpp:11-43,
+//                                 src/ipc/potentials/barrier_potential.cpp:62-99,
+//                                 normal_potential.cpp:127-232, potential.cpp:36-222
+//   * PSD projection              src/ipc/utils/eigen_ext.tpp:64-108 (own Jacobi solver)
+//   * collision-free step size    src/ipc/ipc.cpp:42-106, candidates.cpp:252-292,
+//                                 src/ipc/ccd/tight_inclusion_ccd.cpp:33-336
+//     with an inclusion-based root finder restated from the published
+//     Tight-Inclusion method (Wang et al., ACM TOG 2021; the library
+//     Tight-Inclusion v1.0.6 is not vendored in the reference).
+//
+// Floating point: every expression is evaluated unfused and left to right,
+// as an SSE2 build of the reference evaluates Eigen's 3-vector reductions
+// ((x0*y0 + x1*y1) + x2*y2).  Build with -ffp-contract=off.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <mutex>
+#include <numeric>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace orc {
+
+// ---------------------------------------------------------------------------
+// 3-vectors
+// ---------------------------------------------------------------------------
+struct V3 {
+    double x, y, z;
+};
+static inline V3 sub(V3 a, V3 b) { return { a.x - b.x, a.y - b.y, a.z - b.z }; }
+static inline V3 add(V3 a, V3 b) { return { a.x + b.x, a.y + b.y, a.z + b.z }; }
+static inline V3 scale(V3 a, double s) { return { a.x * s, a.y * s, a.z * s }; }
+static inline double dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+static inline double sqnorm(V3 a) { return dot(a, a); }
+static inline V3 cross(V3 a, V3 b)
+{
+    return { a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x };
+}
+static inline double comp(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+static inline V3 row(const double* V, int64_t i) { return { V[3 * i], V[3 * i + 1], V[3 * i + 2] }; }
+
+// ---------------------------------------------------------------------------
+// Distance types (src/ipc/distance/distance_type.hpp enum order)
+// ---------------------------------------------------------------------------
+enum PE { P_E0 = 0, P_E1 = 1, P_E = 2 };
+enum PT { P_T0 = 0, P_T1, P_T2, P_E0t, P_E1t, P_E2t, P_T };
+enum EE { EA0_EB0 = 0, EA0_EB1, EA1_EB0, EA1_EB1, EA_EB0, EA_EB1, EA0_EB, EA1_EB, EA_EB };
+
+// distance_type.cpp:10-34
+static int point_edge_distance_type(V3 p, V3 e0, V3 e1)
+{
+    const V3 e = sub(e1, e0);
+    const double e_length_sqr = sqnorm(e);
+    if (e_length_sqr == 0) return P_E0;
+    const double ratio = dot(e, sub(p, e0)) / e_length_sqr;
+    if (ratio < 0) return P_E0;
+    if (ratio > 1) return P_E1;
+    return P_E;
+}
+
+// Solve (B Bᵀ) x = B r for the 2×3 basis B=[b0;b1] with the pivoted LDLᵀ
+// factorisation used by distance_type.cpp:48,55,62 (diagonal pivoting on the
+// larger diagonal, unit-lower L, D⁻¹ with a DBL_MIN cutoff).
+static void ldlt2_solve(V3 b0, V3 b1, V3 r, double& x0, double& x1)
+{
+    double a00 = dot(b0, b0);
+    double a10 = dot(b1, b0);
+    double a11 = dot(b1, b1);
+    double y0 = dot(b0, r), y1 = dot(b1, r);
+    bool swapped = false;
+    if (std::fabs(a11) > std::fabs(a00)) {
+        std::swap(a00, a11);
+        swapped = true;
+        std::swap(y0, y1);
+    }
+    const double d0 = a00;
+    double l10 = a10;
+    if (d0 == 0.0) {
+        // Whole diagonal zero: factorisation stops with L = I, D = 0.
+        x0 = 0;
+        x1 = 0;
+        return;
+    }
+    l10 = a10 / d0;
+    const double d1 = a11 - l10 * (d0 * l10);
+    // forward: L y = P b
+    y1 = y1 - l10 * y0;
+    // diagonal (pseudo-inverse with DBL_MIN tolerance)
+    const double tiny = std::numeric_limits<double>::min();
+    y0 = (std::fabs(d0) > tiny) ? y0 / d0 : 0.0;
+    y1 = (std::fabs(d1) > tiny) ? y1 / d1 : 0.0;
+    // backward: Lᵀ x = y
+    y0 = y0 - l10 * y1;
+    if (swapped) std::swap(y0, y1);
+    x0 = y0;
+    x1 = y1;
+}
+
+// distance_type.cpp:36-79
+static int point_triangle_distance_type(V3 p, V3 t0, V3 t1, V3 t2)
+{
+    const V3 normal = cross(sub(t1, t0), sub(t2, t0));
+    double param0[3], param1[3];
+    V3 b0, b1;
+
+    b0 = sub(t1, t0);
+    b1 = cross(b0, normal);
+    ldlt2_solve(b0, b1, sub(p, t0), param0[0], param1[0]);
+    if (param0[0] > 0.0 && param0[0] < 1.0 && param1[0] >= 0.0) return P_E0t;
+
+    b0 = sub(t2, t1);
+    b1 = cross(b0, normal);
+    ldlt2_solve(b0, b1, sub(p, t1), param0[1], param1[1]);
+    if (param0[1] > 0.0 && param0[1] < 1.0 && param1[1] >= 0.0) return P_E1t;
+
+    b0 = sub(t0, t2);
+    b1 = cross(b0, normal);
+    ldlt2_solve(b0, b1, sub(p, t2), param0[2], param1[2]);
+    if (param0[2] > 0.0 && param0[2] < 1.0 && param1[2] >= 0.0) return P_E2t;
+
+    if (param0[0] <= 0.0 && param0[2] >= 1.0) return P_T0;
+    if (param0[1] <= 0.0 && param0[0] >= 1.0) return P_T1;
+    if (param0[2] <= 0.0 && param0[1] >= 1.0) return P_T2;
+    return P_T;
+}
+
+// distance_type.cpp:176-211
+static int edge_edge_parallel_distance_type(V3 ea0, V3 ea1, V3 eb0, V3 eb1)
+{
+    const V3 ea = sub(ea1, ea0);
+    const double alpha = dot(sub(eb0, ea0), ea) / sqnorm(ea);
+    const double beta = dot(sub(eb1, ea0), ea) / sqnorm(ea);
+    int eac, ebc;
+    if (alpha < 0) {
+        eac = (0 <= beta && beta <= 1) ? 2 : 0;
+        ebc = (beta <= alpha) ? 0 : (beta <= 1 ? 1 : 2);
+    } else if (alpha > 1) {
+        eac = (0 <= beta && beta <= 1) ? 2 : 1;
+        ebc = (beta >= alpha) ? 0 : (0 <= beta ? 1 : 2);
+    } else {
+        eac = 2;
+        ebc = 0;
+    }
+    return ebc < 2 ? ((eac << 1) | ebc) : (6 + eac);
+}
+
+// distance_type.cpp:82-174
+static int edge_edge_distance_type(V3 ea0, V3 ea1, V3 eb0, V3 eb1)
+{
+    const double PARALLEL_THRESHOLD = 2.5e-16;
+    const V3 u = sub(ea1, ea0), v = sub(eb1, eb0), w = sub(ea0, eb0);
+    const double a = sqnorm(u), b = dot(u, v), c = sqnorm(v), d = dot(u, w), e = dot(v, w);
+    const double D = a * c - b * b;
+    if (a == 0.0 && c == 0.0) return EA0_EB0;
+    if (a == 0.0) return EA0_EB;
+    if (c == 0.0) return EA_EB0;
+    const double parallel_tolerance = PARALLEL_THRESHOLD * a * c;
+    if (sqnorm(cross(u, v)) < parallel_tolerance)
+        return edge_edge_parallel_distance_type(ea0, ea1, eb0, eb1);
+
+    int default_case = EA_EB;
+    const double sN = (b * e - c * d);
+    double tN, tD;
+    if (sN <= 0.0) {
+        tN = e;
+        tD = c;
+        default_case = EA0_EB;
+    } else if (sN >= D) {
+        tN = e + b;
+        tD = c;
+        default_case = EA1_EB;
+    } else {
+        tN = (a * e - b * d);
+        tD = D;
+        if (tN > 0.0 && tN < tD && sqnorm(cross(u, v)) < parallel_tolerance) {
+            if (sN < D / 2) {
+                tN = e;
+                tD = c;
+                default_case = EA0_EB;
+            } else {
+                tN = e + b;
+                tD = c;
+                default_case = EA1_EB;
+            }
+        }
+    }
+    if (tN <= 0.0) {
+        if (-d <= 0.0) return EA0_EB0;
+        if (-d >= a) return EA1_EB0;
+        return EA_EB0;
+    } else if (tN >= tD) {
+        if ((-d + b) <= 0.0) return EA0_EB1;
+        if ((-d + b) >= a) return EA1_EB1;
+        return EA_EB1;
+    }
+    return default_case;
+}
+
+// ---------------------------------------------------------------------------
+// Squared distances
+// ---------------------------------------------------------------------------
+static double point_point_distance(V3 p0, V3 p1) { return sqnorm(sub(p1, p0)); }   // point_point.cpp:5-9
+static double point_line_distance(V3 p, V3 e0, V3 e1)                              // point_line.cpp:19-21
+{
+    return sqnorm(cross(sub(e0, p), sub(e1, p))) / sqnorm(sub(e1, e0));
+}
+static V3 triangle_normal(V3 a, V3 b, V3 c)                                       // normal.hpp:149-168
+{
+    const V3 n = cross(sub(b, a), sub(c, a));
+    const double z = sqnorm(n);
+    if (z > 0) {
+        const double s = std::sqrt(z);
+        return { n.x / s, n.y / s, n.z / s };
+    }
+    return n;
+}
+static double point_plane_distance(V3 p, V3 t0, V3 t1, V3 t2)                     // point_plane.cpp:10-26
+{
+    const V3 n = triangle_normal(t0, t1, t2);
+    const double ptp = dot(sub(p, t0), n);
+    return ptp * ptp / sqnorm(n);
+}
+static double line_line_distance(V3 ea0, V3 ea1, V3 eb0, V3 eb1)                  // line_line.cpp:7-16
+{
+    const V3 n = cross(sub(ea1, ea0), sub(eb1, eb0));
+    const double ltl = dot(sub(eb0, ea0), n);
+    return ltl * ltl / sqnorm(n);
+}
+static double point_triangle_distance(V3 p, V3 t0, V3 t1, V3 t2, int dtype)       // point_triangle.cpp:11-48
+{
+    switch (dtype) {
+    case P_T0: return point_point_distance(p, t0);
+    case P_T1: return point_point_distance(p, t1);
+    case P_T2: return point_point_distance(p, t2);
+    case P_E0t: return point_line_distance(p, t0, t1);
+    case P_E1t: return point_line_distance(p, t1, t2);
+    case P_E2t: return point_line_distance(p, t2, t0);
+    default: return point_plane_distance(p, t0, t1, t2);
+    }
+}
+static double edge_edge_distance(V3 ea0, V3 ea1, V3 eb0, V3 eb1, int dtype)         // edge_edge.cpp:13-56
+{
+    switch (dtype) {
+    case EA0_EB0: return point_point_distance(ea0, eb0);
+    case EA0_EB1: return point_point_distance(ea0, eb1);
+    case EA1_EB0: return point_point_distance(ea1, eb0);
+    case EA1_EB1: return point_point_distance(ea1, eb1);
+    case EA_EB0: return point_line_distance(eb0, ea0, ea1);
+    case EA_EB1: return point_line_distance(eb1, ea0, ea1);
+    case EA0_EB: return point_line_distance(ea0, eb0, eb1);
+    case EA1_EB: return point_line_distance(ea1, eb0, eb1);
+    default: return line_line_distance(ea0, ea1, eb0, eb1);
+    }
+}
+static double point_edge_distance(V3 p, V3 e0, V3 e1, int dtype)                  // point_edge.cpp:10-38
+{
+    switch (dtype) {
+    case P_E0: return point_point_distance(p, e0);
+    case P_E1: return point_point_distance(p, e1);
+    default: return point_line_distance(p, e0, e1);
+    }
+}
+// edge_edge_mollifier.cpp:7-14, 194-202
+static double ee_cross_sqnorm(V3 ea0, V3 ea1, V3 eb0, V3 eb1) { return sqnorm(cross(sub(ea1, ea0), sub(eb1, eb0))); }
+static double ee_mollifier_threshold(V3 ea0, V3 ea1, V3 eb0, V3 eb1)
+{
+    return 1e-3 * sqnorm(sub(ea0, ea1)) * sqnorm(sub(eb0, eb1));
+}
+
+// ---------------------------------------------------------------------------
+// Boxes and LBVH (aabb.cpp:35-126; lbvh.cpp)
+// ---------------------------------------------------------------------------
+struct Box {
+    double mn[3], mx[3];
+};
+static inline double down(double v) { return std::nextafter(v, -std::numeric_limits<double>::infinity()); }
+static inline double up(double v) { return std::nextafter(v, std::numeric_limits<double>::infinity()); }
+
+static void vertex_boxes_static(const double* V, int64_t nV, double r, std::vector<Box>& out)
+{
+    out.resize(nV);
+    for (int64_t i = 0; i < nV; ++i)
+        for (int d = 0; d < 3; ++d) {
+            out[i].mn[d] = down(V[3 * i + d] - r);
+            out[i].mx[d] = up(V[3 * i + d] + r);
+        }
+}
+static void vertex_boxes_dynamic(const double* V0, const double* V1, int64_t nV, double r, std::vector<Box>& out)
+{
+    out.resize(nV);
+    for (int64_t i = 0; i < nV; ++i)
+        for (int d = 0; d < 3; ++d) {
+            const double a = V0[3 * i + d], b = V1[3 * i + d];
+            out[i].mn[d] = down(std::min(a, b) - r);
+            out[i].mx[d] = up(std::max(a, b) + r);
+        }
+}
+static void prim_boxes(const std::vector<Box>& vb, const int32_t* ids, int64_t n, int k, std::vector<Box>& out)
+{
+    out.resize(n);
+    for (int64_t i = 0; i < n; ++i) {
+        Box b = vb[ids[k * i]];
+        for (int j = 1; j < k; ++j) {
+            const Box& c = vb[ids[k * i + j]];
+            for (int d = 0; d < 3; ++d) {
+                b.mn[d] = std::min(b.mn[d], c.mn[d]);
+                b.mx[d] = std::max(b.mx[d], c.mx[d]);
+            }
+        }
+        out[i] = b;
+    }
+}
+
+// FP32 node with outward rounding (lbvh.cpp:29-41)
+struct FBox {
+    float mn[3], mx[3];
+};
+static inline float f_down(double v)
+{
+    float f = (float)v;
+    if ((double)f > v) f = std::nextafter(f, -std::numeric_limits<float>::infinity());
+    return f;
+}
+static inline float f_up(double v)
+{
+    float f = (float)v;
+    if ((double)f < v) f = std::nextafter(f, std::numeric_limits<float>::infinity());
+    return f;
+}
+static inline FBox to_fbox(const Box& b)
+{
+    FBox f;
+    for (int d = 0; d < 3; ++d) {
+        f.mn[d] = f_down(b.mn[d]);
+        f.mx[d] = f_up(b.mx[d]);
+    }
+    return f;
+}
+static inline bool overlap(const FBox& a, const FBox& b)
+{
+    return a.mn[0] <= b.mx[0] && b.mn[0] <= a.mx[0] && a.mn[1] <= b.mx[1] && b.mn[1] <= a.mx[1]
+        && a.mn[2] <= b.mx[2] && b.mn[2] <= a.mx[2];
+}
+
+// 21-bit-per-axis Morton code (morton.hpp:53-62 semantics: clamp to [0,2^21-1])
+static inline uint64_t spread21(uint64_t x)
+{
+    x &= 0x1fffff;
+    x = (x | x << 32) & 0x1f00000000ffffULL;
+    x = (x | x << 16) & 0x1f0000ff0000ffULL;
+    x = (x | x << 8) & 0x100f00f00f00f00fULL;
+    x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
+    x = (x | x << 2) & 0x1249249249249249ULL;
+    return x;
+}
+static inline uint64_t morton63(double x, double y, double z)
+{
+    auto q = [](double t) -> uint64_t {
+        double s = t * 2097152.0;
+        if (!(s > 0)) s = 0;
+        if (s > 2097151.0) s = 2097151.0;
+        return (uint64_t)s;
+    };
+    return (spread21(q(x)) << 2) | (spread21(q(y)) << 1) | spread21(q(z));
+}
+
+// Karras (2012) radix-tree LBVH over sorted Morton codes.  Internal nodes
+// 0..n-2, leaves n-1..2n-2 in sorted order.  Each node records the sorted
+// leaf range it covers so that triangular self-traversal can skip subtrees
+// entirely to the left of the query (lbvh.cpp:409-418).
+struct LBVH {
+    int n = 0;
+    std::vector<FBox> box;       // 2n-1
+    std::vector<int> left, right; // children (internal nodes only)
+    std::vector<int> last;       // rightmost sorted leaf index of each subtree
+    std::vector<int> prim;       // sorted position -> primitive id
+};
+
+static void build_lbvh(const std::vector<Box>& boxes, const double mesh_min[3], const double mesh_max[3], LBVH& bvh)
+{
+    const int n = (int)boxes.size();
+    bvh.n = n;
+    bvh.box.assign(n > 0 ? 2 * n - 1 : 0, FBox {});
+    bvh.left.assign(n > 1 ? n - 1 : 0, -1);
+    bvh.right.assign(n > 1 ? n - 1 : 0, -1);
+    bvh.last.assign(n > 0 ? 2 * n - 1 : 0, 0);
+    bvh.prim.resize(n);
+    if (n == 0) return;
+    std::vector<uint64_t> code(n);
+    double ext[3];
+    for (int d = 0; d < 3; ++d) ext[d] = mesh_max[d] - mesh_min[d];
+    for (int i = 0; i < n; ++i) {
+        double c[3];
+        for (int d = 0; d < 3; ++d) {
+            const double mid = 0.5 * (boxes[i].mn[d] + boxes[i].mx[d]);
+            c[d] = ext[d] > 0 ? (mid - mesh_min[d]) / ext[d] : 0.0;
+        }
+        code[i] = morton63(c[0], c[1], c[2]);
+    }
+    std::iota(bvh.prim.begin(), bvh.prim.end(), 0);
+    std::stable_sort(bvh.prim.begin(), bvh.prim.end(), [&](int a, int b) { return code[a] < code[b]; });
+    std::vector<uint64_t> sc(n);
+    for (int i = 0; i < n; ++i) sc[i] = code[bvh.prim[i]];
+    for (int i = 0; i < n; ++i) {
+        bvh.box[n - 1 + i] = to_fbox(boxes[bvh.prim[i]]);
+        bvh.last[n - 1 + i] = i;
+    }
+    if (n == 1) return;
+    // delta(i,j): common-prefix length of the (code, index) keys; -1 outside
+    auto delta_safe = [&](int i, int j) -> int {
+        if (j < 0 || j >= n) return -1;
+        if (sc[i] == sc[j]) return 64 + __builtin_clz((unsigned)(i ^ j));
+        return __builtin_clzll(sc[i] ^ sc[j]);
+    };
+    for (int i = 0; i < n - 1; ++i) {
+        const int dir = (delta_safe(i, i + 1) - delta_safe(i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta_safe(i, i - dir);
+        int lmax = 2;
+        while (delta_safe(i, i + lmax * dir) > dmin) lmax *= 2;
+        int l = 0;
+        for (int t = lmax / 2; t >= 1; t /= 2)
+            if (delta_safe(i, i + (l + t) * dir) > dmin) l += t;
+        const int j = i + l * dir;
+        const int dnode = delta_safe(i, j);
+        int s = 0;
+        int t = l;
+        do {
+            t = (t + 1) / 2;
+            if (delta_safe(i, i + (s + t) * dir) > dnode) s += t;
+        } while (t > 1);
+        const int gamma = i + s * dir + std::min(dir, 0);
+        const int lo = std::min(i, j), hi = std::max(i, j);
+        bvh.left[i] = (lo == gamma) ? (n - 1 + gamma) : gamma;
+        bvh.right[i] = (hi == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
+        bvh.last[i] = hi;
+    }
+    // bottom-up boxes: post-order via explicit stack from the root (node 0)
+    std::vector<int> order;
+    order.reserve(n - 1);
+    std::vector<int> st { 0 };
+    while (!st.empty()) {
+        int v = st.back();
+        st.pop_back();
+        order.push_back(v);
+        if (bvh.left[v] < n - 1) st.push_back(bvh.left[v]);
+        if (bvh.right[v] < n - 1) st.push_back(bvh.right[v]);
+    }
+    for (auto it = order.rbegin(); it != order.rend(); ++it) {
+        const int v = *it;
+        const FBox& a = bvh.box[bvh.left[v]];
+        const FBox& b = bvh.box[bvh.right[v]];
+        FBox& c = bvh.box[v];
+        for (int d = 0; d < 3; ++d) {
+            c.mn[d] = std::min(a.mn[d], b.mn[d]);
+            c.mx[d] = std::max(a.mx[d], b.mx[d]);
+        }
+    }
+}
+
+// Visit every leaf whose box overlaps q; triangular => only leaves with sorted
+// index > qi.  cb(primitive_id).
+template <typename F>
+static void traverse(const LBVH& bvh, const FBox& q, int qi, bool triangular, F&& cb)
+{
+    const int n = bvh.n;
+    if (n == 0) return;
+    if (n == 1) {
+        if (!triangular && overlap(bvh.box[0], q)) cb(bvh.prim[0]);
+        return;
+    }
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+        const int v = stack[--sp];
+        if (triangular && bvh.last[v] <= qi) continue;
+        if (!overlap(bvh.box[v], q)) continue;
+        if (v >= n - 1) {
+            const int li = v - (n - 1);
+            if (!triangular || li > qi) cb(bvh.prim[li]);
+        } else {
+            if (sp + 2 > 128) std::abort();
+            stack[sp++] = bvh.right[v];
+            stack[sp++] = bvh.left[v];
+        }
+    }
+}
+
+static void mesh_aabb(const std::vector<Box>& vb, double mn[3], double mx[3])
+{
+    for (int d = 0; d < 3; ++d) {
+        mn[d] = std::numeric_limits<double>::max();
+        mx[d] = std::numeric_limits<double>::lowest();
+    }
+    for (const Box& b : vb)
+        for (int d = 0; d < 3; ++d) {
+            mn[d] = std::min(mn[d], b.mn[d]);
+            mx[d] = std::max(mx[d], b.mx[d]);
+        }
+}
+
+template <typename F>
+static void parallel_for(int64_t n, int nthreads, F&& f)
+{
+    if (nthreads <= 1 || n < 1024) {
+        f(0, n, 0);
+        return;
+    }
+    std::vector<std::thread> th;
+    std::atomic<int64_t> next { 0 };
+    const int64_t chunk = std::max<int64_t>(256, n / (nthreads * 16));
+    for (int t = 0; t < nthreads; ++t)
+        th.emplace_back([&, t] {
+            for (;;) {
+                const int64_t b = next.fetch_add(chunk);
+                if (b >= n) break;
+                f(b, std::min(n, b + chunk), t);
+            }
+        });
+    for (auto& x : th) x.join();
+}
+
+struct Candidates {
+    std::vector<int32_t> ee; // pairs (ea, eb) with ea < eb
+    std::vector<int32_t> fv; // pairs (f, v)
+};
+
+// BroadPhase::detect_collision_candidates in 3D (broad_phase.cpp:79-91):
+// EE by triangular self-traversal, FV by vertex queries into the face BVH,
+// with the shared-vertex filters of lbvh.cpp:810-834.
+static void detect_candidates(const std::vector<Box>& vb, const int32_t* E, int64_t nE, const int32_t* F, int64_t nF,
+    int nthreads, Candidates& out)
+{
+    std::vector<Box> eb, fb;
+    prim_boxes(vb, E, nE, 2, eb);
+    prim_boxes(vb, F, nF, 3, fb);
+    double mn[3], mx[3];
+    mesh_aabb(vb, mn, mx);
+    LBVH ebvh, fbvh;
+    build_lbvh(eb, mn, mx, ebvh);
+    build_lbvh(fb, mn, mx, fbvh);
+    const int nt = std::max(1, nthreads);
+    std::vector<std::vector<int32_t>> ee_local(nt), fv_local(nt);
+    parallel_for(nE, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t qi = b; qi < e; ++qi) {
+            const int ea = ebvh.prim[qi];
+            const FBox& q = ebvh.box[ebvh.n - 1 + qi];
+            traverse(ebvh, q, (int)qi, true, [&](int ebi) {
+                const int a0 = E[2 * ea], a1 = E[2 * ea + 1], b0 = E[2 * ebi], b1 = E[2 * ebi + 1];
+                if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
+                ee_local[t].push_back(std::min(ea, ebi));
+                ee_local[t].push_back(std::max(ea, ebi));
+            });
+        }
+    });
+    const int64_t nV = (int64_t)vb.size();
+    parallel_for(nV, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t vi = b; vi < e; ++vi) {
+            const FBox q = to_fbox(vb[vi]);
+            traverse(fbvh, q, -1, false, [&](int fi) {
+                if (F[3 * fi] == vi || F[3 * fi + 1] == vi || F[3 * fi + 2] == vi) return;
+                fv_local[t].push_back(fi);
+                fv_local[t].push_back((int32_t)vi);
+            });
+        }
+    });
+    out.ee.clear();
+    out.fv.clear();
+    for (int t = 0; t < nt; ++t) {
+        out.ee.insert(out.ee.end(), ee_local[t].begin(), ee_local[t].end());
+        out.fv.insert(out.fv.end(), fv_local[t].begin(), fv_local[t].end());
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Collision set (normal_collisions_builder.cpp)
+// ---------------------------------------------------------------------------
+struct Collisions {
+    std::vector<int32_t> vv;   // (v0 < v1)
+    std::vector<double> vv_w;
+    std::vector<int32_t> ev;   // (e, v)
+    std::vector<double> ev_w;
+    std::vector<int32_t> ee;   // (ea < eb)
+    std::vector<double> ee_eps;
+    std::vector<int8_t> ee_dtype;
+    std::vector<double> ee_w;
+    std::vector<int32_t> fv;   // (f, v)
+    std::vector<double> fv_w;
+    std::vector<int32_t> cand; // last candidate set: ee pairs then fv pairs
+    int64_t n_cand_ee = 0, n_cand_fv = 0;
+};
+
+struct Raw {
+    std::vector<uint64_t> vv, ev;
+    std::vector<int32_t> ee;
+    std::vector<double> ee_eps;
+    std::vector<int8_t> ee_dt;
+    std::vector<int32_t> fv;
+};
+
+static inline uint64_t key2(uint32_t a, uint32_t b) { return ((uint64_t)a << 32) | b; }
+
+static void add_vv(Raw& r, int a, int b) { r.vv.push_back(key2(std::min(a, b), std::max(a, b))); }
+static void add_ev(Raw& r, int e, int v) { r.ev.push_back(key2(e, v)); }
+
+// builder.cpp:239-336
+static void add_face_vertex(Raw& r, const double* V, const int32_t* F, const int32_t* F2E, int fi, int vi, double offset_sqr)
+{
+    const int f0 = F[3 * fi], f1 = F[3 * fi + 1], f2 = F[3 * fi + 2];
+    const V3 p = row(V, vi), t0 = row(V, f0), t1 = row(V, f1), t2 = row(V, f2);
+    const int dtype = point_triangle_distance_type(p, t0, t1, t2);
+    const double d = point_triangle_distance(p, t0, t1, t2, dtype);
+    if (!(d < offset_sqr)) return;
+    switch (dtype) {
+    case P_T0: add_vv(r, vi, f0); break;
+    case P_T1: add_vv(r, vi, f1); break;
+    case P_T2: add_vv(r, vi, f2); break;
+    case P_E0t: add_ev(r, F2E[3 * fi + 0], vi); break;
+    case P_E1t: add_ev(r, F2E[3 * fi + 1], vi); break;
+    case P_E2t: add_ev(r, F2E[3 * fi + 2], vi); break;
+    default:
+        r.fv.push_back(fi);
+        r.fv.push_back(vi);
+    }
+}
+
+// builder.cpp:140-237 (candidate oriented ea < eb)
+static void add_edge_edge(Raw& r, const double* V, const double* Vrest, const int32_t* E, int ea, int eb, double offset_sqr)
+{
+    const int a0 = E[2 * ea], a1 = E[2 * ea + 1], b0 = E[2 * eb], b1 = E[2 * eb + 1];
+    const V3 xa0 = row(V, a0), xa1 = row(V, a1), xb0 = row(V, b0), xb1 = row(V, b1);
+    const int actual = edge_edge_distance_type(xa0, xa1, xb0, xb1);
+    const double d = edge_edge_distance(xa0, xa1, xb0, xb1, actual);
+    if (!(d < offset_sqr)) return;
+    const double eps_x = ee_mollifier_threshold(row(Vrest, a0), row(Vrest, a1), row(Vrest, b0), row(Vrest, b1));
+    const double c = ee_cross_sqnorm(xa0, xa1, xb0, xb1);
+    const int dtype = c < eps_x ? (int)EA_EB : actual;
+    switch (dtype) {
+    case EA0_EB0: add_vv(r, a0, b0); break;
+    case EA0_EB1: add_vv(r, a0, b1); break;
+    case EA1_EB0: add_vv(r, a1, b0); break;
+    case EA1_EB1: add_vv(r, a1, b1); break;
+    case EA_EB0: add_ev(r, ea, b0); break;
+    case EA_EB1: add_ev(r, ea, b1); break;
+    case EA0_EB: add_ev(r, eb, a0); break;
+    case EA1_EB: add_ev(r, eb, a1); break;
+    default:
+        r.ee.push_back(ea);
+        r.ee.push_back(eb);
+        r.ee_eps.push_back(eps_x);
+        r.ee_dt.push_back((int8_t)actual);
+    }
+}
+
+static void finalize(Raw& all, Collisions& C)
+{
+    // builder.cpp:547-689: duplicates merge with summed weights; all weights
+    // here are 1 (no area weighting) so the merged weight is a count.  Output
+    // is sorted by key (the reference order is thread-dependent).
+    auto rle = [](std::vector<uint64_t>& keys, std::vector<int32_t>& ids, std::vector<double>& w) {
+        std::sort(keys.begin(), keys.end());
+        ids.clear();
+        w.clear();
+        for (size_t i = 0; i < keys.size();) {
+            size_t j = i;
+            while (j < keys.size() && keys[j] == keys[i]) ++j;
+            ids.push_back((int32_t)(keys[i] >> 32));
+            ids.push_back((int32_t)(keys[i] & 0xffffffffu));
+            w.push_back((double)(j - i));
+            i = j;
+        }
+    };
+    rle(all.vv, C.vv, C.vv_w);
+    rle(all.ev, C.ev, C.ev_w);
+    // EE: unique pairs by construction; sort by (ea, eb)
+    const size_t nee = all.ee_eps.size();
+    std::vector<size_t> perm(nee);
+    std::iota(perm.begin(), perm.end(), 0);
+    std::sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
+        return key2(all.ee[2 * a], all.ee[2 * a + 1]) < key2(all.ee[2 * b], all.ee[2 * b + 1]);
+    });
+    C.ee.resize(2 * nee);
+    C.ee_eps.resize(nee);
+    C.ee_dtype.resize(nee);
+    C.ee_w.assign(nee, 1.0);
+    for (size_t i = 0; i < nee; ++i) {
+        C.ee[2 * i] = all.ee[2 * perm[i]];
+        C.ee[2 * i + 1] = all.ee[2 * perm[i] + 1];
+        C.ee_eps[i] = all.ee_eps[perm[i]];
+        C.ee_dtype[i] = all.ee_dt[perm[i]];
+    }
+    const size_t nfv = all.fv.size() / 2;
+    std::vector<uint64_t> fk(nfv);
+    for (size_t i = 0; i < nfv; ++i) fk[i] = key2(all.fv[2 * i], all.fv[2 * i + 1]);
+    std::sort(fk.begin(), fk.end());
+    C.fv.resize(2 * nfv);
+    C.fv_w.assign(nfv, 1.0);
+    for (size_t i = 0; i < nfv; ++i) {
+        C.fv[2 * i] = (int32_t)(fk[i] >> 32);
+        C.fv[2 * i + 1] = (int32_t)(fk[i] & 0xffffffffu);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Barrier (barrier.cpp:11-43, barrier_potential.cpp:62-99)
+// ---------------------------------------------------------------------------
+static double barrier(double d, double dhat)
+{
+    if (d <= 0.0) return std::numeric_limits<double>::infinity();
+    if (d >= dhat) return 0;
+    const double dm = (d - dhat);
+    return -dm * dm * std::log(d / dhat);
+}
+static double barrier_d1(double d, double dhat)
+{
+    if (d <= 0.0 || d >= dhat) return 0.0;
+    return (dhat - d) * (2 * std::log(d / dhat) - dhat / d + 1);
+}
+static double barrier_d2(double d, double dhat)
+{
+    if (d <= 0.0 || d >= dhat) return 0.0;
+    const double dd = dhat / d;
+    return (dd + 2) * dd - 2 * std::log(d / dhat) - 3;
+}
+struct BarrierParams {
+    double dhat, kappa, dmin;
+    int physical;
+};
+// ClampedLogBarrier::units(x̂) = x̂² (barrier.hpp:133-137): the physical
+// scaling is dhat / x̂² with x̂ = (2 dmin + dhat) dhat.
+static inline double phys_scale(const BarrierParams& P)
+{
+    const double xh = (2 * P.dmin + P.dhat) * P.dhat;
+    return P.physical ? P.dhat / (xh * xh) : 1.0;
+}
+static double f0(const BarrierParams& P, double d2)
+{
+    return P.kappa * (barrier(d2 - P.dmin * P.dmin, (2 * P.dmin + P.dhat) * P.dhat) * phys_scale(P));
+}
+static double f1(const BarrierParams& P, double d2)
+{
+    return P.kappa * (barrier_d1(d2 - P.dmin * P.dmin, (2 * P.dmin + P.dhat) * P.dhat) * phys_scale(P));
+}
+static double f2(const BarrierParams& P, double d2)
+{
+    return P.kappa * (barrier_d2(d2 - P.dmin * P.dmin, (2 * P.dmin + P.dhat) * P.dhat) * phys_scale(P));
+}
+
+// ---------------------------------------------------------------------------
+// Closed-form squared-distance derivatives (own derivation).
+//
+// PT (point-plane) and EE (line-line) both have the form
+//     d = N² / D,   N = a·(u×v),   D = |u×v|²
+// in reduced variables r = (a, u, v) ∈ R⁹ that are vertex differences.
+// PE (point-line) is d = |a×b|² / |b−a|² in r = (a, b) ∈ R⁶, PP is |r|².
+// Derivatives in r are mapped to the 3n stencil coordinates through the ±1
+// selection map S (r = S x):  ∇ₓd = Sᵀ∇ᵣd,  ∇²ₓd = Sᵀ∇²ᵣd S.
+// ---------------------------------------------------------------------------
+static inline void skew(V3 a, double M[3][3])
+{
+    M[0][0] = 0;
+    M[0][1] = -a.z;
+    M[0][2] = a.y;
+    M[1][0] = a.z;
+    M[1][1] = 0;
+    M[1][2] = -a.x;
+    M[2][0] = -a.y;
+    M[2][1] = a.x;
+    M[2][2] = 0;
+}
+
+// d = N²/D with N = a·(u×v), D = |u×v|² ; outputs value, g[9], H[9][9]
+static double triple_quot(V3 a, V3 u, V3 v, double g[9], double H[9][9])
+{
+    const V3 w = cross(u, v);
+    const double N = dot(a, w);
+    const double D = sqnorm(w);
+    // ∇N = (w, v×a, a×u)
+    double gN[9], gD[9];
+    const V3 gNu = cross(v, a), gNv = cross(a, u);
+    // ∇D = (0, 2 v×w, 2 w×u)
+    const V3 gDu = scale(cross(v, w), 2.0), gDv = scale(cross(w, u), 2.0);
+    const V3 gNa = w;
+    const V3 parts_N[3] = { gNa, gNu, gNv };
+    const V3 parts_D[3] = { { 0, 0, 0 }, gDu, gDv };
+    for (int b = 0; b < 3; ++b)
+        for (int i = 0; i < 3; ++i) {
+            gN[3 * b + i] = comp(parts_N[b], i);
+            gD[3 * b + i] = comp(parts_D[b], i);
+        }
+    // ∇²N: blocks (a,u) = -[v]×, (a,v) = [u]×, (u,v) = -[a]× ; symmetric
+    double HN[9][9] = {}, HD[9][9] = {};
+    double Sv[3][3], Su[3][3], Sa[3][3], Sw[3][3];
+    skew(v, Sv);
+    skew(u, Su);
+    skew(a, Sa);
+    skew(w, Sw);
+    // ∂²N/∂a_i∂u_j = ε_ijk v_k = -[v]×_ij ; ∂²N/∂a_i∂v_j = ε_ikj u_k = [u]×_ij ;
+    // ∂²N/∂u_i∂v_j = ε_kij a_k = -[a]×_ij
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            HN[i][3 + j] = -Sv[i][j];
+            HN[3 + j][i] = -Sv[i][j];
+            HN[i][6 + j] = Su[i][j];
+            HN[6 + j][i] = Su[i][j];
+            HN[3 + i][6 + j] = -Sa[i][j];
+            HN[6 + j][3 + i] = -Sa[i][j];
+        }
+    // ∇²D = 2(JᵀJ + Σ w_k ∇²w_k), J = [-[v]×, [u]×] over (u,v)
+    // uu: 2 [v]×ᵀ[v]× ; vv: 2 [u]×ᵀ[u]× ; uv: 2(-[v]×ᵀ[u]× - [w]×)
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double uu = 0, vv = 0, uv = 0;
+            for (int k = 0; k < 3; ++k) {
+                uu += Sv[k][i] * Sv[k][j];
+                vv += Su[k][i] * Su[k][j];
+                uv += -Sv[k][i] * Su[k][j];
+            }
+            HD[3 + i][3 + j] = 2 * uu;
+            HD[6 + i][6 + j] = 2 * vv;
+            HD[3 + i][6 + j] = 2 * (uv - Sw[i][j]);
+            HD[6 + j][3 + i] = HD[3 + i][6 + j];
+        }
+    const double iD = 1.0 / D;
+    const double d = N * N * iD;
+    for (int i = 0; i < 9; ++i) g[i] = 2 * N * gN[i] * iD - N * N * gD[i] * iD * iD;
+    for (int i = 0; i < 9; ++i)
+        for (int j = 0; j < 9; ++j) {
+            H[i][j] = 2 * gN[i] * gN[j] * iD + 2 * N * HN[i][j] * iD
+                - 2 * N * (gN[i] * gD[j] + gD[i] * gN[j]) * iD * iD - N * N * HD[i][j] * iD * iD
+                + 2 * N * N * gD[i] * gD[j] * iD * iD * iD;
+        }
+    return d;
+}
+
+// D = |u×v|² alone (edge-edge cross squared norm) in r=(u,v) ∈ R⁶
+static double cross_sq(V3 u, V3 v, double g[6], double H[6][6])
+{
+    const V3 w = cross(u, v);
+    const V3 gu = scale(cross(v, w), 2.0), gv = scale(cross(w, u), 2.0);
+    for (int i = 0; i < 3; ++i) {
+        g[i] = comp(gu, i);
+        g[3 + i] = comp(gv, i);
+    }
+    double Sv[3][3], Su[3][3], Sw[3][3];
+    skew(v, Sv);
+    skew(u, Su);
+    skew(w, Sw);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double uu = 0, vv = 0, uv = 0;
+            for (int k = 0; k < 3; ++k) {
+                uu += Sv[k][i] * Sv[k][j];
+                vv += Su[k][i] * Su[k][j];
+                uv += -Sv[k][i] * Su[k][j];
+            }
+            H[i][j] = 2 * uu;
+            H[3 + i][3 + j] = 2 * vv;
+            H[i][3 + j] = 2 * (uv - Sw[i][j]);
+            H[3 + j][i] = H[i][3 + j];
+        }
+    return sqnorm(w);
+}
+
+// d = |a×b|²/|b−a|² in r=(a,b) ∈ R⁶
+static double point_line_r(V3 a, V3 b, double g[6], double H[6][6])
+{
+    const V3 c = cross(a, b);
+    const double P = sqnorm(c);
+    const V3 e = sub(b, a);
+    const double L = sqnorm(e);
+    double Sa[3][3], Sb[3][3], Sc[3][3];
+    skew(a, Sa);
+    skew(b, Sb);
+    skew(c, Sc);
+    // J = [-[b]×, [a]×]; ∇P = 2Jᵀc ; ∇²P = 2(JᵀJ + Σ c_k∇²c_k), ∂²c_k/∂a_i∂b_j = ε_kij
+    double gP[6], HP[6][6], gL[6], HL[6][6];
+    const V3 gPa = scale(cross(b, c), 2.0); // 2(-[b]×)ᵀc = 2 [b]× c = 2 b×c
+    const V3 gPb = scale(cross(c, a), 2.0); // 2 [a]×ᵀ c = -2 a×c = 2 c×a
+    for (int i = 0; i < 3; ++i) {
+        gP[i] = comp(gPa, i);
+        gP[3 + i] = comp(gPb, i);
+        gL[i] = -2 * comp(e, i);
+        gL[3 + i] = 2 * comp(e, i);
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double aa = 0, bb = 0, ab = 0;
+            for (int k = 0; k < 3; ++k) {
+                aa += Sb[k][i] * Sb[k][j];
+                bb += Sa[k][i] * Sa[k][j];
+                ab += -Sb[k][i] * Sa[k][j];
+            }
+            HP[i][j] = 2 * aa;
+            HP[3 + i][3 + j] = 2 * bb;
+            HP[i][3 + j] = 2 * (ab - Sc[i][j]);
+            HP[3 + j][i] = HP[i][3 + j];
+            const double id = (i == j) ? 2.0 : 0.0;
+            HL[i][j] = id;
+            HL[3 + i][3 + j] = id;
+            HL[i][3 + j] = -id;
+            HL[3 + j][i] = -id;
+        }
+    const double iL = 1.0 / L;
+    for (int i = 0; i < 6; ++i) g[i] = gP[i] * iL - P * gL[i] * iL * iL;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j)
+            H[i][j] = HP[i][j] * iL - (gP[i] * gL[j] + gL[i] * gP[j]) * iL * iL - P * HL[i][j] * iL * iL
+                + 2 * P * gL[i] * gL[j] * iL * iL * iL;
+    return P * iL;
+}
+
+// Stencil-local distance derivative: x = n vertices (3n coords).  A reduced
+// variable k is x[pos[k]] - x[neg[k]] (vertex indices).  Returns d.
+struct Reduced {
+    int m;          // number of reduced 3-vectors (1,2,3)
+    int pos[3], neg[3];
+};
+
+static void expand(const Reduced& R, int n, const double* gr, const double* Hr, int ldr, double* g, double* H)
+{
+    const int N = 3 * n;
+    for (int i = 0; i < N; ++i) g[i] = 0;
+    for (int i = 0; i < N * N; ++i) H[i] = 0;
+    for (int k = 0; k < R.m; ++k)
+        for (int c = 0; c < 3; ++c) {
+            g[3 * R.pos[k] + c] += gr[3 * k + c];
+            g[3 * R.neg[k] + c] -= gr[3 * k + c];
+        }
+    for (int k = 0; k < R.m; ++k)
+        for (int l = 0; l < R.m; ++l)
+            for (int c = 0; c < 3; ++c)
+                for (int e = 0; e < 3; ++e) {
+                    const double h = Hr[(3 * k + c) * ldr + 3 * l + e];
+                    H[(3 * R.pos[k] + c) * N + 3 * R.pos[l] + e] += h;
+                    H[(3 * R.pos[k] + c) * N + 3 * R.neg[l] + e] -= h;
+                    H[(3 * R.neg[k] + c) * N + 3 * R.pos[l] + e] -= h;
+                    H[(3 * R.neg[k] + c) * N + 3 * R.neg[l] + e] += h;
+                }
+}
+
+// PP over local vertices (i, j)
+static double dist_pp(const V3* x, int n, int i, int j, double* g, double* H)
+{
+    const V3 r = sub(x[i], x[j]);
+    double gr[3] = { 2 * r.x, 2 * r.y, 2 * r.z };
+    double Hr[9] = { 2, 0, 0, 0, 2, 0, 0, 0, 2 };
+    Reduced R { 1, { i, 0, 0 }, { j, 0, 0 } };
+    expand(R, n, gr, Hr, 3, g, H);
+    return point_point_distance(x[i], x[j]);
+}
+// point p vs line (e0,e1) over local vertices
+static double dist_pl(const V3* x, int n, int p, int e0, int e1, double* g, double* H)
+{
+    double gr[6], Hr[6][6];
+    point_line_r(sub(x[e0], x[p]), sub(x[e1], x[p]), gr, Hr);
+    Reduced R { 2, { e0, e1, 0 }, { p, p, 0 } };
+    expand(R, n, gr, &Hr[0][0], 6, g, H);
+    return point_line_distance(x[p], x[e0], x[e1]);
+}
+// point p vs plane (t0,t1,t2)
+static double dist_pplane(const V3* x, int n, int p, int t0, int t1, int t2, double* g, double* H)
+{
+    double gr[9], Hr[9][9];
+    triple_quot(sub(x[p], x[t0]), sub(x[t1], x[t0]), sub(x[t2], x[t0]), gr, Hr);
+    Reduced R { 3, { p, t1, t2 }, { t0, t0, t0 } };
+    expand(R, n, gr, &Hr[0][0], 9, g, H);
+    return point_plane_distance(x[p], x[t0], x[t1], x[t2]);
+}
+// line (a0,a1) vs line (b0,b1)
+static double dist_ll(const V3* x, int n, int a0, int a1, int b0, int b1, double* g, double* H)
+{
+    double gr[9], Hr[9][9];
+    triple_quot(sub(x[b0], x[a0]), sub(x[a1], x[a0]), sub(x[b1], x[b0]), gr, Hr);
+    Reduced R { 3, { b0, a1, b1 }, { a0, a0, b0 } };
+    expand(R, n, gr, &Hr[0][0], 9, g, H);
+    return line_line_distance(x[a0], x[a1], x[b0], x[b1]);
+}
+// EE distance with known dtype over local (ea0,ea1,eb0,eb1) = (0,1,2,3)
+static double dist_ee(const V3* x, int dtype, double* g, double* H)
+{
+    switch (dtype) {
+    case EA0_EB0: return dist_pp(x, 4, 0, 2, g, H);
+    case EA0_EB1: return dist_pp(x, 4, 0, 3, g, H);
+    case EA1_EB0: return dist_pp(x, 4, 1, 2, g, H);
+    case EA1_EB1: return dist_pp(x, 4, 1, 3, g, H);
+    case EA_EB0: return dist_pl(x, 4, 2, 0, 1, g, H);
+    case EA_EB1: return dist_pl(x, 4, 3, 0, 1, g, H);
+    case EA0_EB: return dist_pl(x, 4, 0, 2, 3, g, H);
+    case EA1_EB: return dist_pl(x, 4, 1, 2, 3, g, H);
+    default: return dist_ll(x, 4, 0, 1, 2, 3, g, H);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// PSD projection (eigen_ext.tpp:64-108) via cyclic Jacobi
+// ---------------------------------------------------------------------------
+static void jacobi_eig(int n, const double* A_in, double* lam, double* Vec)
+{
+    double A[144];
+    std::memcpy(A, A_in, sizeof(double) * n * n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) Vec[i * n + j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0, tot = 0;
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) {
+                tot += A[i * n + j] * A[i * n + j];
+                if (i != j) off += A[i * n + j] * A[i * n + j];
+            }
+        if (off <= 1e-34 * tot || off == 0) break;
+        for (int p = 0; p < n - 1; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[p * n + q];
+                if (apq == 0) continue;
+                const double app = A[p * n + p], aqq = A[q * n + q];
+                const double theta = (aqq - app) / (2 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+                const double c = 1 / std::sqrt(t * t + 1), s = t * c;
+                for (int k = 0; k < n; ++k) {
+                    const double akp = A[k * n + p], akq = A[k * n + q];
+                    A[k * n + p] = c * akp - s * akq;
+                    A[k * n + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double apk = A[p * n + k], aqk = A[q * n + k];
+                    A[p * n + k] = c * apk - s * aqk;
+                    A[q * n + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = Vec[k * n + p], vkq = Vec[k * n + q];
+                    Vec[k * n + p] = c * vkp - s * vkq;
+                    Vec[k * n + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < n; ++i) lam[i] = A[i * n + i];
+}
+
+static void project_psd(int n, double* H, int method)
+{
+    if (method == 0) return;
+    double lam[12], V[144];
+    jacobi_eig(n, H, lam, V);
+    double mn = lam[0];
+    for (int i = 1; i < n; ++i) mn = std::min(mn, lam[i]);
+    if (mn >= 0.0) return;
+    for (int i = 0; i < n; ++i)
+        if (lam[i] < 0) lam[i] = (method == 1) ? 0.0 : -lam[i];
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            double s = 0;
+            for (int k = 0; k < n; ++k) s += V[i * n + k] * lam[k] * V[j * n + k];
+            H[i * n + j] = s;
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Per-contact E/G/H (normal_potential.cpp:127-232)
+// ---------------------------------------------------------------------------
+enum CType { CT_VV = 0, CT_EV = 1, CT_EE = 2, CT_FV = 3 };
+
+struct Contact {
+    int type;
+    int n;          // stencil vertices
+    int vid[4];
+    double w;
+    double eps;     // EE only
+    int dtype;      // EE only
+};
+
+static void contact_stencil(const Collisions& C, const int32_t* E, const int32_t* F, int64_t idx, Contact& c)
+{
+    const int64_t nvv = C.vv_w.size(), nev = C.ev_w.size(), nee = C.ee_w.size();
+    if (idx < nvv) {
+        c.type = CT_VV;
+        c.n = 2;
+        c.vid[0] = C.vv[2 * idx];
+        c.vid[1] = C.vv[2 * idx + 1];
+        c.w = C.vv_w[idx];
+        return;
+    }
+    idx -= nvv;
+    if (idx < nev) {
+        const int e = C.ev[2 * idx], v = C.ev[2 * idx + 1];
+        c.type = CT_EV;
+        c.n = 3;
+        c.vid[0] = v;
+        c.vid[1] = E[2 * e];
+        c.vid[2] = E[2 * e + 1];
+        c.w = C.ev_w[idx];
+        return;
+    }
+    idx -= nev;
+    if (idx < nee) {
+        const int ea = C.ee[2 * idx], eb = C.ee[2 * idx + 1];
+        c.type = CT_EE;
+        c.n = 4;
+        c.vid[0] = E[2 * ea];
+        c.vid[1] = E[2 * ea + 1];
+        c.vid[2] = E[2 * eb];
+        c.vid[3] = E[2 * eb + 1];
+        c.w = C.ee_w[idx];
+        c.eps = C.ee_eps[idx];
+        c.dtype = C.ee_dtype[idx];
+        return;
+    }
+    idx -= nee;
+    const int f = C.fv[2 * idx], v = C.fv[2 * idx + 1];
+    c.type = CT_FV;
+    c.n = 4;
+    c.vid[0] = v;
+    c.vid[1] = F[3 * f];
+    c.vid[2] = F[3 * f + 1];
+    c.vid[3] = F[3 * f + 2];
+    c.w = C.fv_w[idx];
+}
+
+// distance value + derivatives for a contact (stencil-local x)
+static double contact_distance(const Contact& c, const V3* x, double* g, double* H)
+{
+    switch (c.type) {
+    case CT_VV: return dist_pp(x, 2, 0, 1, g, H);
+    case CT_EV: return dist_pl(x, 3, 0, 1, 2, g, H);
+    case CT_EE: return dist_ee(x, c.dtype, g, H);
+    default: return dist_pplane(x, 4, 0, 1, 2, 3, g, H);
+    }
+}
+
+// mollifier m(x) and derivatives for EE (edge_edge_mollifier.cpp:42-136)
+static double mollifier(const Contact& c, const V3* x, double* gm, double* Hm, bool& active)
+{
+    active = false;
+    if (c.type != CT_EE) return 1.0;
+    double gr[6], Hr[6][6];
+    const double s = cross_sq(sub(x[1], x[0]), sub(x[3], x[2]), gr, Hr);
+    if (!(s < c.eps)) return 1.0;
+    active = true;
+    const double xe = s / c.eps;
+    const double m = (-xe + 2) * xe;
+    const double inv = 1 / c.eps;
+    const double m1 = 2 * inv * std::fma(-inv, s, 1);
+    const double m2 = -2 / (c.eps * c.eps);
+    double gs[12], Hs[144];
+    Reduced R { 2, { 1, 3, 0 }, { 0, 2, 0 } };
+    expand(R, 4, gr, &Hr[0][0], 6, gs, Hs);
+    for (int i = 0; i < 12; ++i) gm[i] = m1 * gs[i];
+    for (int i = 0; i < 12; ++i)
+        for (int j = 0; j < 12; ++j) Hm[i * 12 + j] = m1 * Hs[i * 12 + j] + m2 * gs[i] * gs[j];
+    return m;
+}
+
+static double contact_energy(const BarrierParams& P, const Contact& c, const V3* x)
+{
+    double g[12], H[144];
+    const double d = contact_distance(c, x, g, H);
+    double gm[12], Hm[144];
+    bool act;
+    const double m = mollifier(c, x, gm, Hm, act);
+    return c.w * m * f0(P, d);
+}
+
+static void contact_gradient(const BarrierParams& P, const Contact& c, const V3* x, double* out)
+{
+    const int N = 3 * c.n;
+    double gm[12], Hm[144];
+    bool act;
+    const double m = mollifier(c, x, gm, Hm, act);
+    if (m <= 0) {
+        for (int i = 0; i < N; ++i) out[i] = 0;
+        return;
+    }
+    double g[12], H[144];
+    const double d = contact_distance(c, x, g, H);
+    const double fv = f0(P, d), fd = f1(P, d);
+    if (c.type != CT_EE) {
+        for (int i = 0; i < N; ++i) out[i] = (c.w * fd) * g[i];
+        return;
+    }
+    for (int i = 0; i < N; ++i) out[i] = (c.w * fv) * (act ? gm[i] : 0.0) + (c.w * m * fd) * g[i];
+}
+
+static void contact_hessian(const BarrierParams& P, const Contact& c, const V3* x, int psd, double* out)
+{
+    const int N = 3 * c.n;
+    double g[12], H[144];
+    const double d = contact_distance(c, x, g, H);
+    double gm[12] = {}, Hm[144] = {};
+    bool act;
+    const double m = mollifier(c, x, gm, Hm, act);
+    if (c.type == CT_EE && m <= 0) {
+        const double fv = f0(P, d);
+        for (int i = 0; i < N * N; ++i) out[i] = (c.w * fv) * Hm[i];
+        return;
+    }
+    const double fd = f1(P, d), fdd = f2(P, d);
+    if (c.type != CT_EE) {
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) out[i * N + j] = (c.w * fdd) * g[i] * g[j] + (c.w * fd) * H[i * N + j];
+    } else {
+        const double fv = f0(P, d);
+        const double wm = c.w * m;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                const double gfm_ij = (c.w * fd) * g[i] * gm[j];
+                const double gfm_ji = (c.w * fd) * g[j] * gm[i];
+                out[i * N + j] = (c.w * fv) * Hm[i * N + j] + gfm_ij + gfm_ji + (wm * fdd) * g[i] * g[j]
+                    + (wm * fd) * H[i * N + j];
+            }
+    }
+    project_psd(N, out, psd);
+}
+
+// ---------------------------------------------------------------------------
+// Tight-Inclusion-style inclusion-based CCD (restated from the published
+// method) + IPC strategy (tight_inclusion_ccd.cpp:33-75).
+// ---------------------------------------------------------------------------
+static const int CCD_STACK = 128;
+
+struct CCDQuery {
+    V3 s[4], e[4]; // start/end positions; VF: p,t0,t1,t2 ; EE: a0,a1,b0,b1
+    bool vf;
+};
+
+// F(t,u,v) component c at one corner (Tight-Inclusion evaluation form)
+static inline double ccd_F(const CCDQuery& q, int c, double t, double u, double v)
+{
+    double x[4];
+    for (int k = 0; k < 4; ++k) {
+        const double a = comp(q.s[k], c), b = comp(q.e[k], c);
+        x[k] = (b - a) * t + a;
+    }
+    if (q.vf) {
+        // p - (t0 + u (t1 - t0) + v (t2 - t0))
+        const double pt = (x[2] - x[1]) * u + (x[3] - x[1]) * v + x[1];
+        return x[0] - pt;
+    }
+    const double ea = (x[1] - x[0]) * u + x[0];
+    const double eb = (x[3] - x[2]) * v + x[2];
+    return ea - eb;
+}
+
+static void ccd_numerical_error(const CCDQuery& q, bool use_ms, double err[3])
+{
+    const double vf_f = use_ms ? 7.549516567451064e-15 : 6.661338147750939e-15;
+    const double ee_f = use_ms ? 7.105427357601002e-15 : 6.217248937900877e-15;
+    const double filt = q.vf ? vf_f : ee_f;
+    for (int c = 0; c < 3; ++c) {
+        double m = 0;
+        for (int k = 0; k < 4; ++k) {
+            m = std::max(m, std::fabs(comp(q.s[k], c)));
+            m = std::max(m, std::fabs(comp(q.e[k], c)));
+        }
+        const double dl = std::min(m, 1.0);
+        err[c] = filt * (dl * dl * dl);
+    }
+}
+
+// Domain tolerances: δ divided by 3× the largest ∞-norm change of F along
+// each parameter between opposite corners of the unit box.
+static void ccd_domain_tol(const CCDQuery& q, double delta, double tol[3])
+{
+    for (int dim = 0; dim < 3; ++dim) {
+        double L = 0;
+        for (int a = 0; a < 2; ++a)
+            for (int b = 0; b < 2; ++b) {
+                // corners with parameter `dim` at 0 and 1, the others at (a, b)
+                double c0[3], c1[3];
+                int o = 0;
+                for (int k = 0; k < 3; ++k) {
+                    if (k == dim) {
+                        c0[k] = 0;
+                        c1[k] = 1;
+                    } else {
+                        c0[k] = c1[k] = (o++ == 0) ? a : b;
+                    }
+                }
+                double m = 0;
+                for (int c = 0; c < 3; ++c)
+                    m = std::max(m, std::fabs(ccd_F(q, c, c1[0], c1[1], c1[2]) - ccd_F(q, c, c0[0], c0[1], c0[2])));
+                L = std::max(L, m);
+            }
+        L *= 3;
+        tol[dim] = (L == 0) ? delta : delta / L;
+    }
+}
+
+struct CBox {
+    double lo[3];
+    int8_t lvl[3]; // width = 2^-lvl
+};
+
+static inline double cbox_w(const CBox& b, int d) { return std::ldexp(1.0, -b.lvl[d]); }
+
+// Inclusion test.  Returns zero_in; sets box_in and codomain widths.
+static bool ccd_inclusion(const CCDQuery& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3])
+{
+    const double t0 = b.lo[0], t1 = b.lo[0] + cbox_w(b, 0);
+    const double u0 = b.lo[1], u1 = b.lo[1] + cbox_w(b, 1);
+    const double v0 = b.lo[2], v1 = b.lo[2] + cbox_w(b, 2);
+    bool zin = true;
+    box_in = true;
+    for (int c = 0; c < 3; ++c) {
+        double mn = std::numeric_limits<double>::infinity(), mx = -mn;
+        const double ts[2] = { t0, t1 }, us[2] = { u0, u1 }, vs[2] = { v0, v1 };
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) {
+                    const double f = ccd_F(q, c, ts[i], us[j], vs[k]);
+                    mn = std::min(mn, f);
+                    mx = std::max(mx, f);
+                }
+        const double r = err[c] + ms;
+        if (mn > r || mx < -r) zin = false;
+        if (!(mn >= -r && mx <= r)) box_in = false;
+        cw[c] = mx - mn;
+    }
+    return zin;
+}
+
+// Earliest-time branch and bound over (t,u,v) ∈ [0,1]³.  Returns whether a
+// root box was found before tmax; toi = its lower time bound.
+static bool ccd_root_finder(const CCDQuery& q, const double err[3], double ms, const double tol[3], double delta,
+    double tmax, long max_itr, double& toi, double& out_tol)
+{
+    CBox st[CCD_STACK];
+    int sp = 0;
+    st[sp++] = CBox { { 0, 0, 0 }, { 0, 0, 0 } };
+    double best = tmax;
+    bool found = false;
+    // "unlimited" iterations are capped so that no query can run away; the
+    // cap falls back to the conservative earliest unresolved time
+    const long cap = max_itr > 0 ? max_itr : (long)100000000;
+    long itr = 0;
+    out_tol = 0;
+    while (sp) {
+        const CBox b = st[--sp];
+        if (b.lo[0] >= best) continue;
+        ++itr;
+        bool box_in;
+        double cw[3];
+        if (!ccd_inclusion(q, b, err, ms, box_in, cw)) continue;
+        const double w[3] = { cbox_w(b, 0), cbox_w(b, 1), cbox_w(b, 2) };
+        const bool small_co = cw[0] <= delta && cw[1] <= delta && cw[2] <= delta;
+        const bool small_dom = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
+        const bool too_deep = b.lvl[0] >= 60 || b.lvl[1] >= 60 || b.lvl[2] >= 60;
+        if (small_co || box_in || small_dom || too_deep || sp + 2 > CCD_STACK) {
+            best = b.lo[0];
+            found = true;
+            out_tol = std::max(out_tol, std::max(cw[0], std::max(cw[1], cw[2])));
+            continue;
+        }
+        if (itr > cap) {
+            // Out of iterations: the earliest unresolved time bounds the root.
+            double t = b.lo[0];
+            for (int i = 0; i < sp; ++i) t = std::min(t, st[i].lo[0]);
+            best = std::min(best, t);
+            found = true;
+            out_tol = std::max(out_tol, std::max(cw[0], std::max(cw[1], cw[2])));
+            break;
+        }
+        // split the dimension with the largest width / tolerance
+        int sd = 0;
+        double br = w[0] / tol[0];
+        for (int d = 1; d < 3; ++d)
+            if (w[d] / tol[d] > br) {
+                br = w[d] / tol[d];
+                sd = d;
+            }
+        CBox lo = b, hi = b;
+        lo.lvl[sd] = hi.lvl[sd] = (int8_t)(b.lvl[sd] + 1);
+        hi.lo[sd] = b.lo[sd] + cbox_w(lo, sd);
+        // VF: drop halves entirely outside u + v <= 1
+        const bool keep_hi = !(q.vf && sd != 0 && hi.lo[1] + hi.lo[2] > 1.0);
+        const bool keep_lo = !(q.vf && sd != 0 && lo.lo[1] + lo.lo[2] > 1.0);
+        // push the later / second half first so the earlier one pops first
+        if (keep_hi) st[sp++] = hi;
+        if (keep_lo) st[sp++] = lo;
+    }
+    if (found) toi = best;
+    return found;
+}
+
+// ticcd::{vertexFace,edgeEdge}CCD with automatic error and the no-zero-toi loop
+static bool ti_ccd(const CCDQuery& q, double ms_in, double& toi, double tol_in, double tmax_in, long max_itr,
+    double& out_tol, bool no_zero_toi)
+{
+    double err[3];
+    ccd_numerical_error(q, ms_in > 0, err);
+    double tmax = tmax_in, delta = tol_in, ms = ms_in;
+    double tol[3];
+    ccd_domain_tol(q, delta, tol);
+    bool hit = false;
+    for (int it = 0; it < 256; ++it) {
+        double t = 0;
+        hit = ccd_root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol);
+        if (hit) toi = t;
+        if (!(no_zero_toi && hit && toi == 0)) return hit;
+        if (out_tol > delta) tmax *= 0.9;
+        else if (10 * delta < ms) ms *= 0.5;
+        else {
+            delta *= 0.5;
+            ccd_domain_tol(q, delta, tol);
+        }
+    }
+    return hit;
+}
+
+struct CCDParams {
+    double tolerance;
+    long max_iterations;
+    double rescale;
+};
+
+// tight_inclusion_ccd.cpp:33-75
+static bool ccd_strategy(const CCDQuery& q, double min_distance, double d0, const CCDParams& P, double adjusted_tol,
+    double tmax, double& toi)
+{
+    if (d0 <= min_distance) {
+        toi = 0;
+        return true;
+    }
+    double mind = (1.0 - P.rescale) * (d0 - min_distance);
+    mind = std::min(mind, 1e-4);
+    mind += min_distance;
+    double out_tol;
+    bool hit = ti_ccd(q, mind, toi, adjusted_tol, tmax, P.max_iterations, out_tol, false);
+    if (hit && toi < 1e-6) {
+        hit = ti_ccd(q, min_distance, toi, adjusted_tol, tmax, -1, out_tol, true);
+        if (hit) toi *= P.rescale;
+    }
+    return hit;
+}
+
+static inline bool v3eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+
+// FaceVertexCandidate::ccd -> point_triangle_ccd (tight_inclusion_ccd.cpp:285-336)
+static bool fv_ccd(const double* V0, const double* V1, const int32_t* F, int f, int v, double min_distance,
+    const CCDParams& P, double tmax, double& toi)
+{
+    CCDQuery q;
+    q.vf = true;
+    const int ids[4] = { v, F[3 * f], F[3 * f + 1], F[3 * f + 2] };
+    for (int k = 0; k < 4; ++k) {
+        q.s[k] = row(V0, ids[k]);
+        q.e[k] = row(V1, ids[k]);
+    }
+    const double d0 = std::sqrt(point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
+        point_triangle_distance_type(q.s[0], q.s[1], q.s[2], q.s[3])));
+    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) {
+        if (d0 <= min_distance) {
+            toi = 0;
+            return true;
+        }
+        return false;
+    }
+    const double adj = std::min(0.5 * d0, P.tolerance);
+    return ccd_strategy(q, min_distance, d0, P, adj, tmax, toi);
+}
+
+// EdgeEdgeCandidate::ccd -> edge_edge_ccd (tight_inclusion_ccd.cpp:229-283)
+static bool ee_ccd(const double* V0, const double* V1, const int32_t* E, int ea, int eb, double min_distance,
+    const CCDParams& P, double tmax, double& toi)
+{
+    CCDQuery q;
+    q.vf = false;
+    const int ids[4] = { E[2 * ea], E[2 * ea + 1], E[2 * eb], E[2 * eb + 1] };
+    for (int k = 0; k < 4; ++k) {
+        q.s[k] = row(V0, ids[k]);
+        q.e[k] = row(V1, ids[k]);
+    }
+    const double d0 = std::sqrt(edge_edge_distance(q.s[0], q.s[1], q.s[2], q.s[3],
+        edge_edge_distance_type(q.s[0], q.s[1], q.s[2], q.s[3])));
+    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) {
+        if (d0 <= min_distance) {
+            toi = 0;
+            return true;
+        }
+        return false;
+    }
+    const double adj = std::min(0.5 * d0, P.tolerance);
+    return ccd_strategy(q, min_distance, d0, P, adj, tmax, toi);
+}
+
+} // namespace orc
+
+// ===========================================================================
+// C ABI for the test harness (ctypes)
+// ===========================================================================
+using namespace orc;
+
+extern "C" {
+
+// --- primitives (for known-answer tests) ---
+int orc_point_edge_distance_type(const double* p, const double* e0, const double* e1)
+{
+    return point_edge_distance_type(row(p, 0), row(e0, 0), row(e1, 0));
+}
+int orc_point_triangle_distance_type(const double* p, const double* t0, const double* t1, const double* t2)
+{
+    return point_triangle_distance_type(row(p, 0), row(t0, 0), row(t1, 0), row(t2, 0));
+}
+int orc_edge_edge_distance_type(const double* a0, const double* a1, const double* b0, const double* b1)
+{
+    return edge_edge_distance_type(row(a0, 0), row(a1, 0), row(b0, 0), row(b1, 0));
+}
+double orc_point_triangle_distance(const double* p, const double* t0, const double* t1, const double* t2, int dtype)
+{
+    const V3 P = row(p, 0), T0 = row(t0, 0), T1 = row(t1, 0), T2 = row(t2, 0);
+    if (dtype < 0) dtype = point_triangle_distance_type(P, T0, T1, T2);
+    return point_triangle_distance(P, T0, T1, T2, dtype);
+}
+double orc_edge_edge_distance(const double* a0, const double* a1, const double* b0, const double* b1, int dtype)
+{
+    const V3 A0 = row(a0, 0), A1 = row(a1, 0), B0 = row(b0, 0), B1 = row(b1, 0);
+    if (dtype < 0) dtype = edge_edge_distance_type(A0, A1, B0, B1);
+    return edge_edge_distance(A0, A1, B0, B1, dtype);
+}
+double orc_point_edge_distance(const double* p, const double* e0, const double* e1, int dtype)
+{
+    const V3 P = row(p, 0), E0 = row(e0, 0), E1 = row(e1, 0);
+    if (dtype < 0) dtype = point_edge_distance_type(P, E0, E1);
+    return point_edge_distance(P, E0, E1, dtype);
+}
+double orc_barrier(double d, double dhat, int deriv)
+{
+    return deriv == 0 ? barrier(d, dhat) : (deriv == 1 ? barrier_d1(d, dhat) : barrier_d2(d, dhat));
+}
+
+// Squared-distance gradient/Hessian of a stencil.  kind: 0 PP(2 verts),
+// 1 PE-line(3: p,e0,e1), 2 PT-plane(4: p,t0,t1,t2), 3 EE(4) with dtype.
+double orc_distance_derivatives(int kind, int dtype, const double* x, double* g, double* H)
+{
+    V3 v[4];
+    const int n = kind == 0 ? 2 : (kind == 1 ? 3 : 4);
+    for (int i = 0; i < n; ++i) v[i] = row(x, i);
+    switch (kind) {
+    case 0: return dist_pp(v, 2, 0, 1, g, H);
+    case 1: return dist_pl(v, 3, 0, 1, 2, g, H);
+    case 2: return dist_pplane(v, 4, 0, 1, 2, 3, g, H);
+    default: return dist_ee(v, dtype, g, H);
+    }
+}
+
+// faces_to_edges (collision_mesh.cpp:510-543); returns 0 or -1 if an edge is missing
+int orc_faces_to_edges(const int32_t* F, int64_t nF, const int32_t* E, int64_t nE, int32_t* out)
+{
+    std::unordered_map<uint64_t, int32_t> m;
+    m.reserve(nE * 2);
+    for (int64_t e = 0; e < nE; ++e) {
+        const uint32_t a = std::min(E[2 * e], E[2 * e + 1]), b = std::max(E[2 * e], E[2 * e + 1]);
+        m.emplace(key2(a, b), (int32_t)e);
+    }
+    for (int64_t f = 0; f < nF; ++f)
+        for (int j = 0; j < 3; ++j) {
+            const uint32_t vi = F[3 * f + j], vj = F[3 * f + (j + 1) % 3];
+            auto it = m.find(key2(std::min(vi, vj), std::max(vi, vj)));
+            if (it == m.end()) return -1;
+            out[3 * f + j] = it->second;
+        }
+    return 0;
+}
+
+// --- collision set ---
+void* orc_collisions_build(const double* V, const double* Vrest, int64_t nV, const int32_t* E, int64_t nE,
+    const int32_t* F, int64_t nF, const int32_t* F2E, double dhat, double dmin, int nthreads)
+{
+    Collisions* C = new Collisions();
+    std::vector<Box> vb;
+    vertex_boxes_static(V, nV, 0.5 * (dhat + dmin), vb);
+    Candidates cand;
+    detect_candidates(vb, E, nE, F, nF, nthreads, cand);
+    const double offset_sqr = (dmin + dhat) * (dmin + dhat);
+    const int nt = std::max(1, nthreads);
+    std::vector<Raw> raw(nt);
+    const int64_t nee = cand.ee.size() / 2, nfv = cand.fv.size() / 2;
+    parallel_for(nee, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t i = b; i < e; ++i) add_edge_edge(raw[t], V, Vrest, E, cand.ee[2 * i], cand.ee[2 * i + 1], offset_sqr);
+    });
+    parallel_for(nfv, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t i = b; i < e; ++i) add_face_vertex(raw[t], V, F, F2E, cand.fv[2 * i], cand.fv[2 * i + 1], offset_sqr);
+    });
+    Raw all;
+    for (auto& r : raw) {
+        all.vv.insert(all.vv.end(), r.vv.begin(), r.vv.end());
+        all.ev.insert(all.ev.end(), r.ev.begin(), r.ev.end());
+        all.ee.insert(all.ee.end(), r.ee.begin(), r.ee.end());
+        all.ee_eps.insert(all.ee_eps.end(), r.ee_eps.begin(), r.ee_eps.end());
+        all.ee_dt.insert(all.ee_dt.end(), r.ee_dt.begin(), r.ee_dt.end());
+        all.fv.insert(all.fv.end(), r.fv.begin(), r.fv.end());
+    }
+    finalize(all, *C);
+    C->n_cand_ee = nee;
+    C->n_cand_fv = nfv;
+    return C;
+}
+
+// Build from explicit arrays (to evaluate potentials on a given set)
+void* orc_collisions_from_arrays(int64_t nvv, const int32_t* vv, const double* vvw, int64_t nev, const int32_t* ev,
+    const double* evw, int64_t nee, const int32_t* ee, const double* eeeps, const int8_t* eedt, const double* eew,
+    int64_t nfv, const int32_t* fv, const double* fvw)
+{
+    Collisions* C = new Collisions();
+    C->vv.assign(vv, vv + 2 * nvv);
+    C->vv_w.assign(vvw, vvw + nvv);
+    C->ev.assign(ev, ev + 2 * nev);
+    C->ev_w.assign(evw, evw + nev);
+    C->ee.assign(ee, ee + 2 * nee);
+    C->ee_eps.assign(eeeps, eeeps + nee);
+    C->ee_dtype.assign(eedt, eedt + nee);
+    C->ee_w.assign(eew, eew + nee);
+    C->fv.assign(fv, fv + 2 * nfv);
+    C->fv_w.assign(fvw, fvw + nfv);
+    return C;
+}
+
+void orc_collisions_counts(void* h, int64_t* out)
+{
+    Collisions* C = (Collisions*)h;
+    out[0] = C->vv_w.size();
+    out[1] = C->ev_w.size();
+    out[2] = C->ee_w.size();
+    out[3] = C->fv_w.size();
+    out[4] = C->n_cand_ee;
+    out[5] = C->n_cand_fv;
+}
+
+void orc_collisions_get(void* h, int32_t* vv, double* vvw, int32_t* ev, double* evw, int32_t* ee, double* eeeps,
+    int8_t* eedt, double* eew, int32_t* fv, double* fvw)
+{
+    Collisions* C = (Collisions*)h;
+    std::copy(C->vv.begin(), C->vv.end(), vv);
+    std::copy(C->vv_w.begin(), C->vv_w.end(), vvw);
+    std::copy(C->ev.begin(), C->ev.end(), ev);
+    std::copy(C->ev_w.begin(), C->ev_w.end(), evw);
+    std::copy(C->ee.begin(), C->ee.end(), ee);
+    std::copy(C->ee_eps.begin(), C->ee_eps.end(), eeeps);
+    std::copy(C->ee_dtype.begin(), C->ee_dtype.end(), eedt);
+    std::copy(C->ee_w.begin(), C->ee_w.end(), eew);
+    std::copy(C->fv.begin(), C->fv.end(), fv);
+    std::copy(C->fv_w.begin(), C->fv_w.end(), fvw);
+}
+
+void orc_collisions_free(void* h) { delete (Collisions*)h; }
+
+// --- potentials ---
+static inline void gather(const double* V, const Contact& c, V3* x)
+{
+    for (int i = 0; i < c.n; ++i) x[i] = row(V, c.vid[i]);
+}
+
+double orc_barrier_energy(void* h, const double* V, const int32_t* E, const int32_t* F, double dhat, double kappa,
+    double dmin, int physical, int nthreads)
+{
+    Collisions* C = (Collisions*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    const int64_t n = C->vv_w.size() + C->ev_w.size() + C->ee_w.size() + C->fv_w.size();
+    const int nt = std::max(1, nthreads);
+    std::vector<double> part(nt, 0.0);
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        double s = 0;
+        for (int64_t i = b; i < e; ++i) {
+            Contact c;
+            contact_stencil(*C, E, F, i, c);
+            V3 x[4];
+            gather(V, c, x);
+            s += contact_energy(P, c, x);
+        }
+        part[t] += s;
+    });
+    double s = 0;
+    for (double p : part) s += p;
+    return s;
+}
+
+void orc_barrier_gradient(void* h, const double* V, int64_t nV, const int32_t* E, const int32_t* F, double dhat,
+    double kappa, double dmin, int physical, int nthreads, double* grad)
+{
+    Collisions* C = (Collisions*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    const int64_t n = C->vv_w.size() + C->ev_w.size() + C->ee_w.size() + C->fv_w.size();
+    const int nt = std::max(1, nthreads);
+    std::vector<std::vector<double>> loc(nt, std::vector<double>(3 * nV, 0.0));
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t i = b; i < e; ++i) {
+            Contact c;
+            contact_stencil(*C, E, F, i, c);
+            V3 x[4];
+            gather(V, c, x);
+            double g[12];
+            contact_gradient(P, c, x, g);
+            for (int k = 0; k < c.n; ++k)
+                for (int d = 0; d < 3; ++d) loc[t][3 * c.vid[k] + d] += g[3 * k + d];
+        }
+    });
+    for (int64_t i = 0; i < 3 * nV; ++i) {
+        double s = 0;
+        for (int t = 0; t < nt; ++t) s += loc[t][i];
+        grad[i] = s;
+    }
+}
+
+struct CSR {
+    int64_t n = 0;
+    std::vector<int64_t> rowptr;
+    std::vector<int32_t> col;
+    std::vector<double> val;
+};
+
+// Local Hessians → triplets (skip exact zeros, local_to_global.hpp:291) →
+// duplicates summed → compressed rows.
+void* orc_barrier_hessian(void* h, const double* V, int64_t nV, const int32_t* E, const int32_t* F, double dhat,
+    double kappa, double dmin, int physical, int psd, int nthreads)
+{
+    Collisions* C = (Collisions*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    const int64_t n = C->vv_w.size() + C->ev_w.size() + C->ee_w.size() + C->fv_w.size();
+    const int nt = std::max(1, nthreads);
+    struct Trip {
+        int64_t key;
+        double v;
+    };
+    std::vector<std::vector<Trip>> loc(nt);
+    const int64_t ndof = 3 * nV;
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t i = b; i < e; ++i) {
+            Contact c;
+            contact_stencil(*C, E, F, i, c);
+            V3 x[4];
+            gather(V, c, x);
+            double Hl[144];
+            contact_hessian(P, c, x, psd, Hl);
+            const int N = 3 * c.n;
+            for (int a = 0; a < c.n; ++a)
+                for (int bb = 0; bb < c.n; ++bb)
+                    for (int k = 0; k < 3; ++k)
+                        for (int l = 0; l < 3; ++l) {
+                            const double val = Hl[(3 * a + k) * N + 3 * bb + l];
+                            if (val != 0) {
+                                const int64_t r = 3 * (int64_t)c.vid[a] + k, cc = 3 * (int64_t)c.vid[bb] + l;
+                                loc[t].push_back({ r * ndof + cc, val });
+                            }
+                        }
+        }
+    });
+    std::vector<Trip> all;
+    for (auto& l : loc) all.insert(all.end(), l.begin(), l.end());
+    std::stable_sort(all.begin(), all.end(), [](const Trip& a, const Trip& b) { return a.key < b.key; });
+    CSR* M = new CSR();
+    M->n = ndof;
+    M->rowptr.assign(ndof + 1, 0);
+    for (size_t i = 0; i < all.size();) {
+        size_t j = i;
+        double s = 0;
+        while (j < all.size() && all[j].key == all[i].key) s += all[j++].v;
+        const int64_t r = all[i].key / ndof, c = all[i].key % ndof;
+        M->col.push_back((int32_t)c);
+        M->val.push_back(s);
+        M->rowptr[r + 1]++;
+        i = j;
+    }
+    for (int64_t r = 0; r < ndof; ++r) M->rowptr[r + 1] += M->rowptr[r];
+    return M;
+}
+
+int64_t orc_csr_nnz(void* h) { return (int64_t)((CSR*)h)->val.size(); }
+void orc_csr_get(void* h, int64_t* rowptr, int32_t* col, double* val)
+{
+    CSR* M = (CSR*)h;
+    std::copy(M->rowptr.begin(), M->rowptr.end(), rowptr);
+    std::copy(M->col.begin(), M->col.end(), col);
+    std::copy(M->val.begin(), M->val.end(), val);
+}
+void orc_csr_free(void* h) { delete (CSR*)h; }
+
+// Local (stencil) Hessian of one contact for kernel-level tests.
+// type: 0 VV,1 EV,2 EE,3 FV; x: stencil positions (3n)
+void orc_contact_local(int type, int dtype, double eps, double w, const double* x, double dhat, double kappa,
+    double dmin, int physical, int psd, double* energy, double* grad, double* hess)
+{
+    Contact c {};
+    c.type = type;
+    c.n = type == 0 ? 2 : (type == 1 ? 3 : 4);
+    c.w = w;
+    c.eps = eps;
+    c.dtype = dtype;
+    V3 v[4];
+    for (int i = 0; i < c.n; ++i) v[i] = row(x, i);
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    *energy = contact_energy(P, c, v);
+    contact_gradient(P, c, v, grad);
+    contact_hessian(P, c, v, psd, hess);
+}
+
+// --- CCD ---
+int orc_point_triangle_ccd(const double* x0, const double* x1, double min_distance, double tmax, double tolerance,
+    long max_iterations, double rescale, double* toi)
+{
+    // x0/x1: (p, t0, t1, t2) rows
+    const int32_t F[3] = { 1, 2, 3 };
+    const CCDParams P { tolerance, max_iterations, rescale };
+    double t = std::numeric_limits<double>::infinity();
+    const bool hit = fv_ccd(x0, x1, F, 0, 0, min_distance, P, tmax, t);
+    *toi = t;
+    return hit;
+}
+int orc_edge_edge_ccd(const double* x0, const double* x1, double min_distance, double tmax, double tolerance,
+    long max_iterations, double rescale, double* toi)
+{
+    const int32_t E[4] = { 0, 1, 2, 3 };
+    const CCDParams P { tolerance, max_iterations, rescale };
+    double t = std::numeric_limits<double>::infinity();
+    const bool hit = ee_ccd(x0, x1, E, 0, 1, min_distance, P, tmax, t);
+    *toi = t;
+    return hit;
+}
+
+// compute_collision_free_stepsize (ipc.cpp:42-106, candidates.cpp:252-292)
+double orc_collision_free_stepsize(const double* V0, const double* V1, int64_t nV, const int32_t* E, int64_t nE,
+    const int32_t* F, int64_t nF, double min_distance, double tolerance, long max_iterations, double rescale,
+    int nthreads, int64_t* n_candidates)
+{
+    std::vector<Box> vb;
+    vertex_boxes_dynamic(V0, V1, nV, 0.5 * min_distance, vb);
+    Candidates cand;
+    detect_candidates(vb, E, nE, F, nF, nthreads, cand);
+    const int64_t nee = cand.ee.size() / 2, nfv = cand.fv.size() / 2;
+    if (n_candidates) *n_candidates = nee + nfv;
+    if (nee + nfv == 0) return 1.0;
+    const CCDParams P { tolerance, max_iterations, rescale };
+    std::atomic<double> earliest(1.0);
+    const int nt = std::max(1, nthreads);
+    parallel_for(nee + nfv, nt, [&](int64_t b, int64_t e, int) {
+        for (int64_t i = b; i < e; ++i) {
+            const double tmax = earliest.load(std::memory_order_relaxed);
+            double toi = std::numeric_limits<double>::infinity();
+            bool hit;
+            if (i < nee) hit = ee_ccd(V0, V1, E, cand.ee[2 * i], cand.ee[2 * i + 1], min_distance, P, tmax, toi);
+            else {
+                const int64_t k = i - nee;
+                hit = fv_ccd(V0, V1, F, cand.fv[2 * k], cand.fv[2 * k + 1], min_distance, P, tmax, toi);
+            }
+            if (hit) {
+                double prev = earliest.load(std::memory_order_relaxed);
+                while (toi < prev && !earliest.compare_exchange_weak(prev, toi, std::memory_order_relaxed)) { }
+            }
+        }
+    });
+    return earliest.load();
+}
+
+} // extern "C"

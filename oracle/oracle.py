@@ -1,0 +1,257 @@
+"""ctypes front-end of the CPU oracle (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this module: it is the checker for the GPU library, never part of it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libipc_oracle.so")
+_lib = None
+
+PSD = {"none": 0, "clamp": 1, "abs": 2}
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library with its Makefile."""
+    src = os.path.join(_HERE, "ipc_oracle.cpp")
+    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        d, i64, i32, vp = C.c_double, C.c_int64, C.c_int, C.c_void_p
+        P = C.c_void_p
+        L.orc_point_edge_distance_type.restype = i32
+        L.orc_point_triangle_distance_type.restype = i32
+        L.orc_edge_edge_distance_type.restype = i32
+        L.orc_point_triangle_distance.restype = d
+        L.orc_point_triangle_distance.argtypes = [P, P, P, P, i32]
+        L.orc_edge_edge_distance.restype = d
+        L.orc_edge_edge_distance.argtypes = [P, P, P, P, i32]
+        L.orc_point_edge_distance.restype = d
+        L.orc_point_edge_distance.argtypes = [P, P, P, i32]
+        L.orc_barrier.restype = d
+        L.orc_barrier.argtypes = [d, d, i32]
+        L.orc_distance_derivatives.restype = d
+        L.orc_distance_derivatives.argtypes = [i32, i32, P, P, P]
+        L.orc_faces_to_edges.restype = i32
+        L.orc_faces_to_edges.argtypes = [P, i64, P, i64, P]
+        L.orc_collisions_build.restype = vp
+        L.orc_collisions_build.argtypes = [P, P, i64, P, i64, P, i64, P, d, d, i32]
+        L.orc_collisions_from_arrays.restype = vp
+        L.orc_collisions_from_arrays.argtypes = [i64, P, P, i64, P, P, i64, P, P, P, P, i64, P, P]
+        L.orc_collisions_counts.argtypes = [vp, P]
+        L.orc_collisions_get.argtypes = [vp] + [P] * 10
+        L.orc_collisions_free.argtypes = [vp]
+        L.orc_barrier_energy.restype = d
+        L.orc_barrier_energy.argtypes = [vp, P, P, P, d, d, d, i32, i32]
+        L.orc_barrier_gradient.argtypes = [vp, P, i64, P, P, d, d, d, i32, i32, P]
+        L.orc_barrier_hessian.restype = vp
+        L.orc_barrier_hessian.argtypes = [vp, P, i64, P, P, d, d, d, i32, i32, i32]
+        L.orc_csr_nnz.restype = i64
+        L.orc_csr_nnz.argtypes = [vp]
+        L.orc_csr_get.argtypes = [vp, P, P, P]
+        L.orc_csr_free.argtypes = [vp]
+        L.orc_contact_local.argtypes = [i32, i32, d, d, P, d, d, d, i32, i32, P, P, P]
+        L.orc_point_triangle_ccd.restype = i32
+        L.orc_point_triangle_ccd.argtypes = [P, P, d, d, d, C.c_long, d, P]
+        L.orc_edge_edge_ccd.restype = i32
+        L.orc_edge_edge_ccd.argtypes = [P, P, d, d, d, C.c_long, d, P]
+        L.orc_collision_free_stepsize.restype = d
+        L.orc_collision_free_stepsize.argtypes = [P, P, i64, P, i64, P, i64, d, d, C.c_long, d, i32, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# --- primitives -------------------------------------------------------------
+def point_triangle_distance_type(p, t0, t1, t2):
+    return lib().orc_point_triangle_distance_type(*(_p(_f64(x)) for x in (p, t0, t1, t2)))
+
+
+def edge_edge_distance_type(a0, a1, b0, b1):
+    return lib().orc_edge_edge_distance_type(*(_p(_f64(x)) for x in (a0, a1, b0, b1)))
+
+
+def point_edge_distance_type(p, e0, e1):
+    return lib().orc_point_edge_distance_type(*(_p(_f64(x)) for x in (p, e0, e1)))
+
+
+def point_triangle_distance(p, t0, t1, t2, dtype=-1):
+    a = [_f64(x) for x in (p, t0, t1, t2)]
+    return lib().orc_point_triangle_distance(*(_p(x) for x in a), dtype)
+
+
+def edge_edge_distance(a0, a1, b0, b1, dtype=-1):
+    a = [_f64(x) for x in (a0, a1, b0, b1)]
+    return lib().orc_edge_edge_distance(*(_p(x) for x in a), dtype)
+
+
+def point_edge_distance(p, e0, e1, dtype=-1):
+    a = [_f64(x) for x in (p, e0, e1)]
+    return lib().orc_point_edge_distance(*(_p(x) for x in a), dtype)
+
+
+def barrier(d, dhat, deriv=0):
+    return lib().orc_barrier(float(d), float(dhat), int(deriv))
+
+
+def distance_derivatives(kind, x, dtype=8):
+    """kind 0 PP, 1 point-line, 2 point-plane, 3 edge-edge(dtype)."""
+    x = _f64(x).ravel()
+    n = x.size
+    g = np.zeros(n)
+    H = np.zeros((n, n))
+    d = lib().orc_distance_derivatives(kind, dtype, _p(x), _p(g), _p(H))
+    return d, g, H
+
+
+def contact_local(ctype, x, dhat, kappa, dmin=0.0, physical=False, psd="none", w=1.0, eps=0.0, dtype=8):
+    x = _f64(x).ravel()
+    n = x.size
+    e = np.zeros(1)
+    g = np.zeros(n)
+    H = np.zeros((n, n))
+    lib().orc_contact_local(ctype, dtype, eps, w, _p(x), dhat, kappa, dmin, int(physical), PSD[psd], _p(e), _p(g), _p(H))
+    return e[0], g, H
+
+
+def faces_to_edges(F, E):
+    F, E = _i32(F), _i32(E)
+    out = np.zeros_like(F)
+    if lib().orc_faces_to_edges(_p(F), F.shape[0], _p(E), E.shape[0], _p(out)) != 0:
+        raise RuntimeError("Unable to find edge!")
+    return out
+
+
+# --- collision set ------------------------------------------------------------
+class Collisions:
+    """Sorted collision set: vv (min,max), ev (e,v), ee (ea<eb)+eps+dtype, fv (f,v)."""
+
+    def __init__(self, handle):
+        self.h = handle
+        L = lib()
+        cnt = np.zeros(6, np.int64)
+        L.orc_collisions_counts(self.h, _p(cnt))
+        nvv, nev, nee, nfv, self.n_cand_ee, self.n_cand_fv = (int(c) for c in cnt)
+        self.vv = np.zeros((nvv, 2), np.int32)
+        self.vv_w = np.zeros(nvv)
+        self.ev = np.zeros((nev, 2), np.int32)
+        self.ev_w = np.zeros(nev)
+        self.ee = np.zeros((nee, 2), np.int32)
+        self.ee_eps = np.zeros(nee)
+        self.ee_dtype = np.zeros(nee, np.int8)
+        self.ee_w = np.zeros(nee)
+        self.fv = np.zeros((nfv, 2), np.int32)
+        self.fv_w = np.zeros(nfv)
+        L.orc_collisions_get(self.h, *(_p(a) for a in (self.vv, self.vv_w, self.ev, self.ev_w, self.ee,
+                                                        self.ee_eps, self.ee_dtype, self.ee_w, self.fv, self.fv_w)))
+
+    def __len__(self):
+        return len(self.vv_w) + len(self.ev_w) + len(self.ee_w) + len(self.fv_w)
+
+    def __del__(self):
+        try:
+            lib().orc_collisions_free(self.h)
+        except Exception:
+            pass
+
+    @staticmethod
+    def from_arrays(vv, vv_w, ev, ev_w, ee, ee_eps, ee_dtype, ee_w, fv, fv_w):
+        arrs = [_i32(vv), _f64(vv_w), _i32(ev), _f64(ev_w), _i32(ee), _f64(ee_eps),
+                np.ascontiguousarray(ee_dtype, np.int8), _f64(ee_w), _i32(fv), _f64(fv_w)]
+        h = lib().orc_collisions_from_arrays(
+            len(arrs[1]), _p(arrs[0]), _p(arrs[1]), len(arrs[3]), _p(arrs[2]), _p(arrs[3]),
+            len(arrs[5]), _p(arrs[4]), _p(arrs[5]), _p(arrs[6]), _p(arrs[7]),
+            len(arrs[9]), _p(arrs[8]), _p(arrs[9]))
+        c = Collisions(h)
+        c._keep = arrs
+        return c
+
+
+def build_collisions(V, E, F, dhat, dmin=0.0, rest=None, nthreads=None):
+    V, E, F = _f64(V), _i32(E), _i32(F)
+    rest = V if rest is None else _f64(rest)
+    F2E = faces_to_edges(F, E)
+    nt = nthreads or os.cpu_count() or 1
+    h = lib().orc_collisions_build(_p(V), _p(rest), V.shape[0], _p(E), E.shape[0], _p(F), F.shape[0], _p(F2E),
+                                   float(dhat), float(dmin), int(nt))
+    return Collisions(h)
+
+
+def barrier_energy(col, V, E, F, dhat, kappa, dmin=0.0, physical=False, nthreads=None):
+    V, E, F = _f64(V), _i32(E), _i32(F)
+    return lib().orc_barrier_energy(col.h, _p(V), _p(E), _p(F), dhat, kappa, dmin, int(physical),
+                                    int(nthreads or os.cpu_count() or 1))
+
+
+def barrier_gradient(col, V, E, F, dhat, kappa, dmin=0.0, physical=False, nthreads=None):
+    V, E, F = _f64(V), _i32(E), _i32(F)
+    g = np.zeros(V.size)
+    lib().orc_barrier_gradient(col.h, _p(V), V.shape[0], _p(E), _p(F), dhat, kappa, dmin, int(physical),
+                               int(nthreads or os.cpu_count() or 1), _p(g))
+    return g
+
+
+def barrier_hessian(col, V, E, F, dhat, kappa, dmin=0.0, physical=False, psd="none", nthreads=None):
+    """Returns (indptr int64, indices int32, data float64) of the ndof x ndof CSR."""
+    V, E, F = _f64(V), _i32(E), _i32(F)
+    L = lib()
+    h = L.orc_barrier_hessian(col.h, _p(V), V.shape[0], _p(E), _p(F), dhat, kappa, dmin, int(physical),
+                              PSD[psd], int(nthreads or os.cpu_count() or 1))
+    nnz = L.orc_csr_nnz(h)
+    rp = np.zeros(V.size + 1, np.int64)
+    ci = np.zeros(nnz, np.int32)
+    va = np.zeros(nnz)
+    L.orc_csr_get(h, _p(rp), _p(ci), _p(va))
+    L.orc_csr_free(h)
+    return rp, ci, va
+
+
+# --- CCD -----------------------------------------------------------------------
+def point_triangle_ccd(x0, x1, min_distance=0.0, tmax=1.0, tolerance=1e-6, max_iterations=10_000_000,
+                       rescale=0.8):
+    x0, x1 = _f64(x0).reshape(4, 3), _f64(x1).reshape(4, 3)
+    toi = np.zeros(1)
+    hit = lib().orc_point_triangle_ccd(_p(x0), _p(x1), min_distance, tmax, tolerance, max_iterations, rescale, _p(toi))
+    return bool(hit), float(toi[0])
+
+
+def edge_edge_ccd(x0, x1, min_distance=0.0, tmax=1.0, tolerance=1e-6, max_iterations=10_000_000, rescale=0.8):
+    x0, x1 = _f64(x0).reshape(4, 3), _f64(x1).reshape(4, 3)
+    toi = np.zeros(1)
+    hit = lib().orc_edge_edge_ccd(_p(x0), _p(x1), min_distance, tmax, tolerance, max_iterations, rescale, _p(toi))
+    return bool(hit), float(toi[0])
+
+
+def collision_free_stepsize(V0, V1, E, F, min_distance=0.0, tolerance=1e-6, max_iterations=10_000_000,
+                            rescale=0.8, nthreads=None):
+    V0, V1, E, F = _f64(V0), _f64(V1), _i32(E), _i32(F)
+    nc = np.zeros(1, np.int64)
+    t = lib().orc_collision_free_stepsize(_p(V0), _p(V1), V0.shape[0], _p(E), E.shape[0], _p(F), F.shape[0],
+                                          min_distance, tolerance, max_iterations, rescale,
+                                          int(nthreads or os.cpu_count() or 1), _p(nc))
+    return float(t), int(nc[0])

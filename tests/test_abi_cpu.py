@@ -1,0 +1,65 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads, exports
+every entry point declared in include/ipcg.h, and refuses to compute (with
+IPCG_ERR_NO_DEVICE, never a CPU fallback) when no CUDA device is present."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "ipcg.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ipcg_\w+)\s*\(", txt)))
+
+
+def test_header_declares_the_hot_path():
+    syms = declared_symbols()
+    for s in ("ipcg_mesh_create", "ipcg_collisions_build", "ipcg_barrier_energy", "ipcg_barrier_gradient",
+              "ipcg_barrier_hessian", "ipcg_collision_free_stepsize"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol(ipctk):
+    lib = C.CDLL(ipctk.LIB_PATH)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_version_and_error_strings(ipctk):
+    L = ipctk.lib()
+    assert L.ipcg_version().decode().startswith("ipcg")
+    assert L.ipcg_last_error() is not None
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="checks the no-device path")
+def test_no_device_fails_loudly(ipctk):
+    V = np.zeros((3, 3))
+    E = np.array([[0, 1], [1, 2], [2, 0]])
+    F = np.array([[0, 1, 2]])
+    with pytest.raises(RuntimeError, match="no CUDA device"):
+        ipctk.CollisionMesh(V, E, F)
+    x = np.zeros((1, 4, 3))
+    with pytest.raises(RuntimeError, match="no CUDA device"):
+        ipctk.distance_stencils(1, x)
+
+
+def test_argument_validation_precedes_device(ipctk):
+    # invalid sizes are rejected as invalid arguments, before any device work
+    L = ipctk.lib()
+    h = C.c_void_p()
+    st = L.ipcg_mesh_create(None, -1, None, 0, None, 0, C.byref(h))
+    assert st == 1
+    assert "negative" in L.ipcg_last_error().decode()
