@@ -22,6 +22,8 @@
 // FP64 atomics at positions found by binary search in its block row.
 #include <cub/block/block_reduce.cuh>
 
+#include <cstdio>
+
 #include "geom.cuh"
 #include "internal.cuh"
 #include "profile.cuh"
@@ -619,6 +621,22 @@ __global__ void __launch_bounds__(BLOCK) k_gradient(ContactsView cv, const int* 
         }
 }
 
+// Self-check of the Hessian path: an index outside its buffer is recorded
+// (first one wins) and the access is skipped.
+struct Guard {
+    long long* rec; // [code, index, limit, contact]
+};
+__device__ __forceinline__ bool in_range(const Guard& gd, int code, long long idx, long long limit, long long who)
+{
+    if (idx >= 0 && idx < limit) return true;
+    if (atomicCAS((unsigned long long*)gd.rec, 0ull, (unsigned long long)code) == 0ull) {
+        gd.rec[1] = idx;
+        gd.rec[2] = limit;
+        gd.rec[3] = who;
+    }
+    return false;
+}
+
 __device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restrict__ a, int lo, int hi,
     unsigned long long key)
 {
@@ -630,76 +648,149 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restr
     return lo;
 }
 
-__global__ void __launch_bounds__(BLOCK) k_hessian(ContactsView cv, const int* __restrict__ E,
-    const int* __restrict__ F, const double* __restrict__ V, Params P, const unsigned long long* __restrict__ ukeys,
-    const int* __restrict__ bptr, double* __restrict__ val, int* __restrict__ fail)
+// Local Hessian of one contact (normal_potential.cpp:174-232 before the PSD
+// projection) written to its 144-double slab of Hs (row-major, N = 3n).
+// One instantiation per contact type (contacts of a type are contiguous:
+// VV, EV, EE, FV), so each kernel holds only its own distance function.
+// proj[i] = 0 marks the mollified edge-edge case with m(x) <= 0, which the
+// reference returns without projection.
+template <int TYPE>
+__global__ void __launch_bounds__(BLOCK) k_local_hessian(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, Params P, double* __restrict__ Hs,
+    uint8_t* __restrict__ proj, int64_t first, int64_t count)
 {
-    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t i = first + t;
     Local c;
     load_contact(cv, E, F, i, c);
     V3 x[4];
     gather(V, c, x);
-    const int N = 3 * c.n;
+    constexpr int NS = TYPE == CT_VV ? 2 : (TYPE == CT_EV ? 3 : 4);
+    constexpr int N = 3 * NS;
+    double* __restrict__ out = Hs + 144 * i;
     double g[12], H[144];
-    const double d = contact_distance(c, x, g, H);
-    double Hl[144];
-    bool project = true;
-    if (c.type == CT_EE) {
-        double gm[12], Hm[144];
+    double d;
+    if (TYPE == CT_VV) d = pp_local(x, 6, 0, 1, g, H);
+    else if (TYPE == CT_EV) d = pl_local(x, 9, 0, 1, 2, g, H);
+    else if (TYPE == CT_EE) d = ee_local(x, c.dtype, g, H);
+    else d = pplane_local(x, g, H);
+    uint8_t pr = 1;
+    if (TYPE == CT_EE) {
+        // w m(x) f(d(x)): the distance terms first, then the mollifier terms
+        // added in place (the distance Hessian buffer is reused for the
+        // mollifier Hessian to halve the local memory of this kernel)
         bool act;
-        const double m = mollifier(c, x, gm, Hm, act);
-        if (!act) {
-            for (int k = 0; k < 12; ++k) gm[k] = 0;
-            for (int k = 0; k < 144; ++k) Hm[k] = 0;
-        }
+        const double m = mollifier(c, x, nullptr, nullptr, act);
         const double fv = fval(P, d);
-        if (m <= 0) {
-            for (int k = 0; k < 144; ++k) Hl[k] = (c.w * fv) * Hm[k];
-            project = false;
+        if (act && m <= 0) {
+            double gm[12];
+            mollifier(c, x, gm, H, act);
+            for (int k = 0; k < 144; ++k) out[k] = (c.w * fv) * H[k];
+            pr = 0;
         } else {
             const double fd = fd1(P, d), fdd = fd2(P, d);
             const double wm = c.w * m;
             for (int r = 0; r < 12; ++r)
-                for (int s = 0; s < 12; ++s) {
-                    const double gfm_rs = (c.w * fd) * g[r] * gm[s];
-                    const double gfm_sr = (c.w * fd) * g[s] * gm[r];
-                    Hl[r * 12 + s] = (c.w * fv) * Hm[r * 12 + s] + gfm_rs + gfm_sr + (wm * fdd) * g[r] * g[s]
-                        + (wm * fd) * H[r * 12 + s];
-                }
+                for (int q = 0; q < 12; ++q) out[r * 12 + q] = (wm * fdd) * g[r] * g[q] + (wm * fd) * H[r * 12 + q];
+            if (act) {
+                double gm[12];
+                mollifier(c, x, gm, H, act);
+                for (int r = 0; r < 12; ++r)
+                    for (int q = 0; q < 12; ++q) {
+                        const double gfm_rq = (c.w * fd) * g[r] * gm[q];
+                        const double gfm_qr = (c.w * fd) * g[q] * gm[r];
+                        out[r * 12 + q] += (c.w * fv) * H[r * 12 + q] + gfm_rq + gfm_qr;
+                    }
+            }
         }
     } else {
         const double fd = fd1(P, d), fdd = fd2(P, d);
         for (int r = 0; r < N; ++r)
-            for (int s = 0; s < N; ++s) Hl[r * N + s] = (c.w * fdd) * g[r] * g[s] + (c.w * fd) * H[r * N + s];
+            for (int q = 0; q < N; ++q) out[r * N + q] = (c.w * fdd) * g[r] * g[q] + (c.w * fd) * H[r * N + q];
     }
-    if (project && !project_psd(c.n, Hl, P.psd)) atomicOr(fail, 1);
-    // scatter into CSR
-    for (int a = 0; a < c.n; ++a) {
-        const int ra = c.vid[a];
-        const int b0 = bptr[ra], b1 = bptr[ra + 1];
-        const int nbr = b1 - b0;
-        const int64_t rowbase = 9 * (int64_t)b0;
-        for (int b = 0; b < c.n; ++b) {
-            const unsigned long long key = ((unsigned long long)ra << 32) | (unsigned)c.vid[b];
-            const int q = lower_bound_u64(ukeys, b0, b1, key);
-            if (q >= b1 || ukeys[q] != key) {
-                atomicOr(fail, 2); // pattern does not hold this block: report, never write out of range
-                continue;
-            }
-            const int64_t base = rowbase + 3 * (int64_t)(q - b0);
-            for (int k = 0; k < 3; ++k)
-                for (int l = 0; l < 3; ++l) {
-                    const double v = Hl[(3 * a + k) * N + 3 * b + l];
-                    if (v != 0) atomicAdd(val + base + 3 * (int64_t)k * nbr + l, v);
-                }
-        }
+    proj[i] = pr;
+}
+
+__device__ __forceinline__ int stencil_size(const ContactsView& cv, int64_t i)
+{
+    return i < cv.nvv ? 2 : (i < cv.nvv + cv.nev ? 3 : 4);
+}
+
+// PSD projection (eigen_ext.tpp:64-108) of every local Hessian, in place.
+__global__ void __launch_bounds__(BLOCK) k_psd(ContactsView cv, double* __restrict__ Hs,
+    const uint8_t* __restrict__ proj, int method, int* __restrict__ fail)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !proj[i]) return;
+    const int ns = stencil_size(cv, i);
+    const int N = 3 * ns;
+    double Hl[144];
+    double* __restrict__ slab = Hs + 144 * i;
+    for (int k = 0; k < N * N; ++k) Hl[k] = slab[k];
+    if (!project_psd(ns, Hl, method)) {
+        atomicOr(fail, 1);
+        return;
+    }
+    for (int k = 0; k < N * N; ++k) slab[k] = Hl[k];
+}
+
+// Contribution id j (position in the block-key list) -> contact, local
+// vertex pair (a, b) and stencil size.
+__device__ __forceinline__ void decode_contribution(const ContactsView& cv, int64_t j, int64_t& i, int& a, int& b,
+    int& ns)
+{
+    const int64_t e1 = 4 * cv.nvv, e2 = e1 + 9 * cv.nev;
+    if (j < e1) {
+        i = j / 4;
+        ns = 2;
+        const int r = (int)(j % 4);
+        a = r / 2;
+        b = r % 2;
+    } else if (j < e2) {
+        i = cv.nvv + (j - e1) / 9;
+        ns = 3;
+        const int r = (int)((j - e1) % 9);
+        a = r / 3;
+        b = r % 3;
+    } else {
+        i = cv.nvv + cv.nev + (j - e2) / 16;
+        ns = 4;
+        const int r = (int)((j - e2) % 16);
+        a = r / 4;
+        b = r % 4;
     }
 }
 
+// Sort-by-key reduction into CSR: one thread per stored value (block q,
+// entry k,l) sums the contributions of block q in sorted (deterministic)
+// order and writes the value once.
+__global__ void k_assemble(ContactsView cv, const unsigned long long* __restrict__ ukeys,
+    const int* __restrict__ run_start, const int* __restrict__ run_len, const int* __restrict__ contrib,
+    const double* __restrict__ Hs, const int* __restrict__ bptr, int nb, double* __restrict__ val)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 9 * (int64_t)nb) return;
+    const int q = (int)(t / 9), kl = (int)(t % 9), k = kl / 3, l = kl % 3;
+    double sum = 0;
+    const int s0 = run_start[q], s1 = s0 + run_len[q];
+    for (int s = s0; s < s1; ++s) {
+        int64_t i;
+        int a, b, ns;
+        decode_contribution(cv, contrib[s], i, a, b, ns);
+        const int N = 3 * ns;
+        sum += Hs[144 * i + (3 * a + k) * N + 3 * b + l];
+    }
+    const unsigned long long key = ukeys[q];
+    const int r = (int)(key >> 32);
+    const int b0 = bptr[r];
+    const int64_t nbr = bptr[r + 1] - b0;
+    val[9 * (int64_t)b0 + 3 * (int64_t)(q - b0) + 3 * k * nbr + l] = sum;
+}
+
 __global__ void k_block_keys(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
-    unsigned long long* __restrict__ keys)
+    unsigned long long* __restrict__ keys, int* __restrict__ ids, long long nk, Guard gd)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -712,15 +803,20 @@ __global__ void k_block_keys(ContactsView cv, const int* __restrict__ E, const i
     else off = 4 * cv.nvv + 9 * cv.nev + 16 * (i - cv.nvv - cv.nev);
     for (int a = 0; a < c.n; ++a)
         for (int b = 0; b < c.n; ++b)
-            keys[off + a * c.n + b] = ((unsigned long long)c.vid[a] << 32) | (unsigned)c.vid[b];
+            if (in_range(gd, 6, off + a * c.n + b, nk, i)) {
+                keys[off + a * c.n + b] = ((unsigned long long)c.vid[a] << 32) | (unsigned)c.vid[b];
+                ids[off + a * c.n + b] = (int)(off + a * c.n + b);
+            }
 }
 
 __global__ void k_block_rowptr(const unsigned long long* __restrict__ ukeys, const int* __restrict__ d_nb, int nV,
-    int* __restrict__ bptr)
+    int* __restrict__ bptr, long long ucap, Guard gd)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r > nV) return;
-    bptr[r] = lower_bound_u64(ukeys, 0, *d_nb, (unsigned long long)r << 32);
+    const int nb = *d_nb;
+    if (!in_range(gd, 7, nb, ucap + 1, r)) return;
+    bptr[r] = lower_bound_u64(ukeys, 0, nb, (unsigned long long)r << 32);
 }
 
 __global__ void k_csr_rows(const int* __restrict__ bptr, int nV, int64_t* __restrict__ row_ptr)
@@ -737,17 +833,19 @@ __global__ void k_csr_rows(const int* __restrict__ bptr, int nV, int64_t* __rest
 }
 
 __global__ void k_csr_cols(const unsigned long long* __restrict__ ukeys, int nb, const int* __restrict__ bptr,
-    int* __restrict__ col)
+    int* __restrict__ col, int nV, Guard gd)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nb) return;
     const unsigned long long key = ukeys[q];
     const int r = (int)(key >> 32), cc = (int)(key & 0xffffffffu);
+    if (!in_range(gd, 8, r, nV, q)) return;
     const int b0 = bptr[r];
     const int64_t nbr = bptr[r + 1] - b0;
     const int64_t base = 9 * (int64_t)b0 + 3 * (int64_t)(q - b0);
     for (int k = 0; k < 3; ++k)
-        for (int l = 0; l < 3; ++l) col[base + 3 * k * nbr + l] = 3 * cc + l;
+        for (int l = 0; l < 3; ++l)
+            if (in_range(gd, 9, base + 3 * k * nbr + l, 9LL * nb, q)) col[base + 3 * k * nbr + l] = 3 * cc + l;
 }
 
 } // namespace
@@ -787,39 +885,76 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         const int64_t nk = 4 * cs->nvv + 9 * cs->nev + 16 * (cs->nee + cs->nfv);
         m->keys_a.reserve(nk + 1);
         m->keys_b.reserve(nk + 1);
+        m->ivals_a.reserve(nk + nV + 2);
+        m->ivals_b.reserve(3 * nk + 3);
+        m->hs.reserve(144 * (n + 1));
+        m->proj.reserve(n + 1);
         m->counters.reserve(16);
         int* d_nb = m->counters.p + 14;
         int* d_fail = m->counters.p + 15;
         IPCG_CUDA(cudaMemsetAsync(d_fail, 0, sizeof(int), s));
+        m->guard.reserve(4);
+        IPCG_CUDA(cudaMemsetAsync(m->guard.p, 0, sizeof(long long) * 4, s));
+        const Guard gd { m->guard.p };
+        int* ids_in = m->ivals_b.p;                  // contribution ids (unsorted)
+        int* contrib = m->ivals_b.p + (nk + 1);      // contribution ids sorted by block key
+        int* run_len = m->ivals_b.p + 2 * (nk + 1);  // contributions per block
+        int* run_start = m->ivals_a.p + (nV + 2);    // first contribution of each block
+        int* bptr = m->ivals_a.p;
         int nb = 0;
         if (n > 0) {
-            IPCG_LAUNCH("k_block_keys", s, k_block_keys<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, m->keys_a.p));
-            IPCG_CHECK_LAUNCH();
-            sort_keys_u64(m, m->keys_a.p, m->keys_b.p, (int)nk, 32 + bits_for(nV + 1));
-            unique_u64(m, m->keys_b.p, m->keys_a.p, d_nb, (int)nk);
+            // local Hessians (FP64 work) and PSD projection into the scratch slabs
+            const int64_t first[4] = { 0, cs->nvv, cs->nvv + cs->nev, cs->nvv + cs->nev + cs->nee };
+            const int64_t count[4] = { cs->nvv, cs->nev, cs->nee, cs->nfv };
+            if (count[0])
+                IPCG_LAUNCH("k_local_hessian_vv", s, k_local_hessian<CT_VV><<<grid_for(count[0], BLOCK), BLOCK, 0, s>>>(
+                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[0], count[0]));
+            if (count[1])
+                IPCG_LAUNCH("k_local_hessian_ev", s, k_local_hessian<CT_EV><<<grid_for(count[1], BLOCK), BLOCK, 0, s>>>(
+                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[1], count[1]));
+            if (count[2])
+                IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], BLOCK), BLOCK, 0, s>>>(
+                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[2], count[2]));
+            if (count[3])
+                IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], BLOCK), BLOCK, 0, s>>>(
+                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[3], count[3]));
+            if (a.psd != IPCG_PSD_NONE)
+                IPCG_LAUNCH("k_psd", s, k_psd<<<nblk, BLOCK, 0, s>>>(cv, m->hs.p, m->proj.p, a.psd, d_fail));
+            // sparsity pattern: sort (block key, contribution) and run-length encode
+            IPCG_LAUNCH("k_block_keys", s, k_block_keys<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, m->keys_a.p,
+                ids_in, nk, gd));
+            sort_pairs_u64(m, m->keys_a.p, m->keys_b.p, ids_in, contrib, (int)nk, 32 + bits_for(nV + 1));
+            rle_u64(m, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
             IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, s));
             IPCG_CUDA(cudaStreamSynchronize(s));
             nb = m->h_counters.p[0];
+            exclusive_sum_i32(m, run_len, run_start, nb);
         } else {
             IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), s));
         }
         hess->nnz = 9 * (int64_t)nb;
-        m->ivals_a.reserve(nV + 2);
         hess->row_ptr.reserve(3 * nV + 1);
         hess->col.reserve(hess->nnz + 1);
         hess->val.reserve(hess->nnz + 1);
-        int* bptr = m->ivals_a.p;
-        IPCG_LAUNCH("k_block_rowptr", s, k_block_rowptr<<<grid_for(nV + 1, 256), 256, 0, s>>>(m->keys_a.p, d_nb, (int)nV, bptr));
+        IPCG_LAUNCH("k_block_rowptr", s, k_block_rowptr<<<grid_for(nV + 1, 256), 256, 0, s>>>(m->keys_a.p, d_nb,
+            (int)nV, bptr, nk, gd));
         IPCG_LAUNCH("k_csr_rows", s, k_csr_rows<<<grid_for(nV + 1, 256), 256, 0, s>>>(bptr, (int)nV, hess->row_ptr.p));
-        if (nb > 0) IPCG_LAUNCH("k_csr_cols", s, k_csr_cols<<<grid_for(nb, 256), 256, 0, s>>>(m->keys_a.p, nb, bptr, hess->col.p));
-        IPCG_CUDA(cudaMemsetAsync(hess->val.p, 0, sizeof(double) * (hess->nnz + 1), s));
-        if (n > 0)
-            IPCG_LAUNCH("k_hessian", s, k_hessian<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, m->keys_a.p, bptr, hess->val.p, d_fail));
-        IPCG_CHECK_LAUNCH();
+        if (nb > 0) {
+            IPCG_LAUNCH("k_csr_cols", s, k_csr_cols<<<grid_for(nb, 256), 256, 0, s>>>(m->keys_a.p, nb, bptr,
+                hess->col.p, (int)nV, gd));
+            IPCG_LAUNCH("k_assemble", s, k_assemble<<<grid_for(9 * (int64_t)nb, 256), 256, 0, s>>>(cv, m->keys_a.p,
+                run_start, run_len, contrib, m->hs.p, bptr, nb, hess->val.p));
+        }
         IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p + 1, d_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaMemcpyAsync(m->h_guard, m->guard.p, sizeof(long long) * 4, cudaMemcpyDeviceToHost, s));
     }
     IPCG_CUDA(cudaStreamSynchronize(s));
-    if (hess && (m->h_counters.p[1] & 2)) throw Error(IPCG_ERR_CUDA, "Hessian block missing from the CSR pattern");
+    if (hess && m->h_guard[0]) {
+        char msg[256];
+        snprintf(msg, sizeof(msg), "Hessian assembly index check %lld failed: index %lld, limit %lld, item %lld",
+            m->h_guard[0], m->h_guard[1], m->h_guard[2], m->h_guard[3]);
+        throw Error(IPCG_ERR_CUDA, msg);
+    }
     if (hess && (m->h_counters.p[1] & 1))
         throw Error(IPCG_ERR_CUDA, "unable to project matrix onto positive semi-definite cone");
 }

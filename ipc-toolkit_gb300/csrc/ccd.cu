@@ -14,11 +14,15 @@
 // / edge-edge co-planarity function F(t,u,v) is multilinear, so the box of
 // its image over a parameter box is the box of its 8 corner values; boxes
 // whose image misses [-eps-ms, eps+ms]^3 are discarded and the rest are
-// bisected.  The search is a depth-first branch and bound on the earliest
-// time (earlier time halves first, boxes starting at or after the best
-// accepted time pruned), which returns the smallest lower time bound of an
-// accepted box, so the result does not depend on the tmax handed in by other
-// candidates.  One thread per candidate; this file is compiled with
+// bisected, each time across the parameter along which the components
+// still straddling the separation box change most.  A box is accepted when
+// every component is either inside the separation box or narrower than the
+// codomain tolerance (the union of Tight-Inclusion's two acceptance tests),
+// or when the box is below the domain tolerances.  The search is a
+// depth-first branch and bound on the earliest time (earlier time halves
+// first, boxes starting at or after the best accepted time pruned), which
+// returns the smallest lower time bound of an accepted box, so the result
+// does not depend on the tmax handed in by other candidates.  One thread per candidate; this file is compiled with
 // -fmad=false so every value matches the CPU oracle bit for bit.
 #include "geom.cuh"
 #include "internal.cuh"
@@ -101,7 +105,11 @@ __device__ void domain_tol(const Query& q, double delta, double tol[3])
     }
 }
 
-__device__ bool inclusion(const Query& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3])
+// Returns zero_in; sets box_in, the codomain widths cw[c], whether component
+// c lies inside [-eps-ms, eps+ms] (inside[c]) and the largest change of
+// component c between the two faces of the box across parameter d.
+__device__ bool inclusion(const Query& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3],
+    double var[3][3], bool inside[3])
 {
     const double ts[2] = { b.lo[0], b.lo[0] + width_of(b.lvl[0]) };
     const double us[2] = { b.lo[1], b.lo[1] + width_of(b.lvl[1]) };
@@ -109,24 +117,36 @@ __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], do
     bool zin = true;
     box_in = true;
     for (int c = 0; c < 3; ++c) {
+        double f[2][2][2];
         double mn = __longlong_as_double(0x7ff0000000000000ULL), mx = -mn;
         for (int i = 0; i < 2; ++i)
             for (int j = 0; j < 2; ++j)
                 for (int k = 0; k < 2; ++k) {
-                    const double f = F_comp(q, c, ts[i], us[j], vs[k]);
-                    mn = fmin(mn, f);
-                    mx = fmax(mx, f);
+                    f[i][j][k] = F_comp(q, c, ts[i], us[j], vs[k]);
+                    mn = fmin(mn, f[i][j][k]);
+                    mx = fmax(mx, f[i][j][k]);
                 }
+        var[c][0] = var[c][1] = var[c][2] = 0;
+        for (int j = 0; j < 2; ++j)
+            for (int k = 0; k < 2; ++k) {
+                var[c][0] = fmax(var[c][0], fabs(f[1][j][k] - f[0][j][k]));
+                var[c][1] = fmax(var[c][1], fabs(f[j][1][k] - f[j][0][k]));
+                var[c][2] = fmax(var[c][2], fabs(f[j][k][1] - f[j][k][0]));
+            }
         const double r = err[c] + ms;
         if (mn > r || mx < -r) zin = false;
-        if (!(mn >= -r && mx <= r)) box_in = false;
+        inside[c] = (mn >= -r && mx <= r);
+        if (!inside[c]) box_in = false;
         cw[c] = mx - mn;
     }
     return zin;
 }
 
+// `shared_best` (may be null) is the earliest time of impact found so far by
+// any candidate; boxes starting at or after it cannot lower the final
+// minimum, so it is re-read every 64 boxes to prune.
 __device__ bool root_finder(const Query& q, const double err[3], double ms, const double tol[3], double delta,
-    double tmax, long long max_itr, double& toi, double& out_tol)
+    double tmax, long long max_itr, double& toi, double& out_tol, const unsigned long long* shared_best)
 {
     CBox st[CCD_STACK];
     int sp = 0;
@@ -135,22 +155,26 @@ __device__ bool root_finder(const Query& q, const double err[3], double ms, cons
     ++sp;
     double best = tmax;
     bool found = false;
+    long long itr = 0;
     // "unlimited" iterations are capped so that no query can run away; the
     // cap falls back to the conservative earliest unresolved time
     const long long cap = max_itr > 0 ? max_itr : (long long)100000000;
-    long long itr = 0;
     out_tol = 0;
+    double prune = tmax;
     while (sp) {
+        if (shared_best && (itr & 63) == 0)
+            prune = fmin(prune, __longlong_as_double((long long)*(volatile const unsigned long long*)shared_best));
         const CBox b = st[--sp];
-        if (b.lo[0] >= best) continue;
+        if (b.lo[0] >= best || b.lo[0] >= prune) continue;
         ++itr;
-        bool box_in;
-        double cw[3];
-        if (!inclusion(q, b, err, ms, box_in, cw)) continue;
+        bool box_in, inside[3];
+        double cw[3], var[3][3];
+        if (!inclusion(q, b, err, ms, box_in, cw, var, inside)) continue;
         const double w[3] = { width_of(b.lvl[0]), width_of(b.lvl[1]), width_of(b.lvl[2]) };
-        const bool small_co = cw[0] <= delta && cw[1] <= delta && cw[2] <= delta;
+        const bool small_co = (inside[0] || cw[0] <= delta) && (inside[1] || cw[1] <= delta)
+            && (inside[2] || cw[2] <= delta);
         const bool small_dom = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
-        const bool too_deep = b.lvl[0] >= 60 || b.lvl[1] >= 60 || b.lvl[2] >= 60;
+        const bool too_deep = b.lvl[0] >= 60 && b.lvl[1] >= 60 && b.lvl[2] >= 60;
         if (small_co || box_in || small_dom || too_deep || sp + 2 > CCD_STACK) {
             best = b.lo[0];
             found = true;
@@ -165,13 +189,19 @@ __device__ bool root_finder(const Query& q, const double err[3], double ms, cons
             out_tol = fmax(out_tol, fmax(cw[0], fmax(cw[1], cw[2])));
             break;
         }
-        int sd = 0;
-        double br = w[0] / tol[0];
-        for (int d = 1; d < 3; ++d)
-            if (w[d] / tol[d] > br) {
-                br = w[d] / tol[d];
+        // split the parameter across which the still-straddling components
+        // change most (parameters at the depth limit are not split)
+        int sd = -1;
+        double best_var = -1;
+        for (int d = 0; d < 3; ++d) {
+            double vd = 0;
+            for (int c = 0; c < 3; ++c)
+                if (!inside[c]) vd = fmax(vd, var[c][d]);
+            if (b.lvl[d] < 60 && vd > best_var) {
+                best_var = vd;
                 sd = d;
             }
+        }
         CBox lo = b, hi = b;
         lo.lvl[sd] = hi.lvl[sd] = (int8_t)(b.lvl[sd] + 1);
         hi.lo[sd] = b.lo[sd] + width_of(lo.lvl[sd]);
@@ -185,7 +215,7 @@ __device__ bool root_finder(const Query& q, const double err[3], double ms, cons
 }
 
 __device__ bool ti_ccd(const Query& q, double ms_in, double& toi, double tol_in, double tmax_in, long long max_itr,
-    double& out_tol, bool no_zero_toi)
+    double& out_tol, bool no_zero_toi, const unsigned long long* shared_best)
 {
     double err[3];
     numerical_error(q, ms_in > 0, err);
@@ -195,7 +225,7 @@ __device__ bool ti_ccd(const Query& q, double ms_in, double& toi, double tol_in,
     bool hit = false;
     for (int it = 0; it < 256; ++it) {
         double t = 0;
-        hit = root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol);
+        hit = root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol, shared_best);
         if (hit) toi = t;
         if (!(no_zero_toi && hit && toi == 0)) return hit;
         if (out_tol > delta) tmax *= 0.9;
@@ -215,7 +245,7 @@ struct CCDParams {
 };
 
 __device__ bool strategy(const Query& q, double min_distance, double d0, const CCDParams& P, double adj, double tmax,
-    double& toi)
+    double& toi, const unsigned long long* shared_best)
 {
     if (d0 <= min_distance) {
         toi = 0;
@@ -225,9 +255,9 @@ __device__ bool strategy(const Query& q, double min_distance, double d0, const C
     mind = fmin(mind, 1e-4);
     mind += min_distance;
     double out_tol;
-    bool hit = ti_ccd(q, mind, toi, adj, tmax, P.max_iterations, out_tol, false);
+    bool hit = ti_ccd(q, mind, toi, adj, tmax, P.max_iterations, out_tol, false, shared_best);
     if (hit && toi < 1e-6) {
-        hit = ti_ccd(q, min_distance, toi, adj, tmax, -1, out_tol, true);
+        hit = ti_ccd(q, min_distance, toi, adj, tmax, -1, out_tol, true, shared_best);
         if (hit) toi *= P.rescale;
     }
     return hit;
@@ -235,7 +265,8 @@ __device__ bool strategy(const Query& q, double min_distance, double d0, const C
 
 __device__ __forceinline__ bool v3eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 
-__device__ bool stencil_ccd(Query& q, double min_distance, const CCDParams& P, double tmax, double& toi)
+__device__ bool stencil_ccd(Query& q, double min_distance, const CCDParams& P, double tmax, double& toi,
+    const unsigned long long* shared_best)
 {
     double d2;
     if (q.vf) d2 = point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
@@ -251,7 +282,7 @@ __device__ bool stencil_ccd(Query& q, double min_distance, const CCDParams& P, d
         return false;
     }
     const double adj = fmin(0.5 * d0, P.tolerance);
-    return strategy(q, min_distance, d0, P, adj, tmax, toi);
+    return strategy(q, min_distance, d0, P, adj, tmax, toi, shared_best);
 }
 
 __global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee, int n_ee,
@@ -284,7 +315,7 @@ __global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee,
     }
     const double tmax = __longlong_as_double((long long)*(volatile unsigned long long*)toi_bits);
     double toi = __longlong_as_double(0x7ff0000000000000ULL);
-    if (stencil_ccd(q, min_distance, P, tmax, toi) && toi < tmax)
+    if (stencil_ccd(q, min_distance, P, tmax, toi, toi_bits) && toi < tmax)
         atomicMin(toi_bits, (unsigned long long)__double_as_longlong(toi));
 }
 
@@ -300,7 +331,7 @@ __global__ void k_ccd_stencils(int is_ee, int n, const double* __restrict__ x0, 
         q.e[k] = load_v3(x1 + 12 * (int64_t)i, k);
     }
     double t = __longlong_as_double(0x7ff0000000000000ULL);
-    const bool h = stencil_ccd(q, min_distance, P, tmax, t);
+    const bool h = stencil_ccd(q, min_distance, P, tmax, t, nullptr);
     hit[i] = h ? 1 : 0;
     toi[i] = t;
 }

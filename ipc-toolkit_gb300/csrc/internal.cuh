@@ -109,6 +109,10 @@ struct ipcg_mesh {
     ipcg::DBuf<int8_t> i8tmp;
     ipcg::DBuf<double> partial;      // reduction partials
     ipcg::DBuf<unsigned long long> toi_bits;
+    ipcg::DBuf<long long> guard;     // device-side index self-check record
+    ipcg::DBuf<double> hs;           // per-contact local Hessian slabs (144 doubles each)
+    ipcg::DBuf<uint8_t> proj;        // per-contact "project to PSD" flags
+    long long h_guard[4] = { 0, 0, 0, 0 };
     int64_t cand_cap = 0;
     ~ipcg_mesh();
 };
@@ -173,6 +177,7 @@ void sort_pairs_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long 
 // run-length encode sorted keys; writes the number of runs to d_num (device)
 void rle_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* counts, int* d_num, int n);
 void unique_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* d_num, int n);
+void exclusive_sum_i32(ipcg_mesh* m, const int* in, int* out, int n);
 
 inline int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
 inline int bits_for(int64_t n)

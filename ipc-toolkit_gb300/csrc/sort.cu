@@ -3,6 +3,7 @@
 // are compiled once.
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_run_length_encode.cuh>
+#include <cub/device/device_scan.cuh>
 #include <cub/device/device_select.cuh>
 
 #include "internal.cuh"
@@ -67,6 +68,14 @@ void unique_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long
     }
     with_temp(m, "cub_select_unique", [&](void* t, size_t& b) {
         return cub::DeviceSelect::Unique(t, b, k_in, uniq, d_num, n, m->stream);
+    });
+}
+
+void exclusive_sum_i32(ipcg_mesh* m, const int* in, int* out, int n)
+{
+    if (n <= 0) return;
+    with_temp(m, "cub_exclusive_sum", [&](void* t, size_t& b) {
+        return cub::DeviceScan::ExclusiveSum(t, b, in, out, n, m->stream);
     });
 }
 

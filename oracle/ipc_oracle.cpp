@@ -1060,11 +1060,105 @@ static void jacobi_eig(int n, const double* A_in, double* lam, double* Vec)
     for (int i = 0; i < n; ++i) lam[i] = A[i * n + i];
 }
 
+// Householder tridiagonalisation + implicit symmetric QR with Wilkinson
+// shifts (Golub & Van Loan, Alg. 8.3.1/8.3.2) -- the method family of
+// Eigen::SelfAdjointEigenSolver.  Eigenvectors are the columns of Q.
+static bool ql_eig(int n, const double* A_in, double* d, double* Q)
+{
+    double A[144], e[12];
+    std::memcpy(A, A_in, sizeof(double) * n * n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) Q[i * n + j] = (i == j) ? 1.0 : 0.0;
+    for (int k = 0; k + 2 < n; ++k) {
+        double sig = 0;
+        for (int i = k + 2; i < n; ++i) sig += A[i * n + k] * A[i * n + k];
+        const double x0 = A[(k + 1) * n + k];
+        if (sig == 0) {
+            e[k] = x0;
+            continue;
+        }
+        const double nx = std::sqrt(x0 * x0 + sig);
+        const double alpha = (x0 >= 0) ? -nx : nx;
+        double v[12], p[12];
+        v[k + 1] = x0 - alpha;
+        for (int i = k + 2; i < n; ++i) v[i] = A[i * n + k];
+        const double tau = 2.0 / (v[k + 1] * v[k + 1] + sig);
+        double K = 0;
+        for (int i = k + 1; i < n; ++i) {
+            double s = 0;
+            for (int j = k + 1; j < n; ++j) s += A[i * n + j] * v[j];
+            p[i] = tau * s;
+            K += p[i] * v[i];
+        }
+        K *= 0.5 * tau;
+        for (int i = k + 1; i < n; ++i) p[i] -= K * v[i];
+        for (int i = k + 1; i < n; ++i)
+            for (int j = k + 1; j < n; ++j) A[i * n + j] -= v[i] * p[j] + p[i] * v[j];
+        e[k] = alpha;
+        for (int r = 0; r < n; ++r) {
+            double s = 0;
+            for (int j = k + 1; j < n; ++j) s += Q[r * n + j] * v[j];
+            s *= tau;
+            for (int j = k + 1; j < n; ++j) Q[r * n + j] -= s * v[j];
+        }
+    }
+    if (n >= 2) e[n - 2] = A[(n - 1) * n + n - 2];
+    e[n - 1] = 0;
+    for (int i = 0; i < n; ++i) d[i] = A[i * n + i];
+    const double eps = 2.220446049250313e-16;
+    int end = n - 1, iter = 0;
+    while (end > 0) {
+        for (int i = 0; i < end; ++i)
+            if (std::fabs(e[i]) <= eps * (std::fabs(d[i]) + std::fabs(d[i + 1])) || std::fabs(e[i]) <= 1e-300) e[i] = 0;
+        while (end > 0 && e[end - 1] == 0) --end;
+        if (end <= 0) break;
+        if (++iter > 40 * n) return false;
+        int start = end - 1;
+        while (start > 0 && e[start - 1] != 0) --start;
+        const double td = 0.5 * (d[end - 1] - d[end]);
+        const double b = e[end - 1];
+        double mu = d[end];
+        if (td == 0) mu -= std::fabs(b);
+        else {
+            const double h = std::hypot(td, b);
+            mu -= b * b / (td + (td > 0 ? h : -h));
+        }
+        double x = d[start] - mu, z = e[start];
+        for (int k = start; k < end; ++k) {
+            const double r = std::hypot(x, z);
+            double c = 1, s = 0;
+            if (r != 0) {
+                c = x / r;
+                s = -z / r;
+            }
+            if (k > start) e[k - 1] = c * e[k - 1] - s * z;
+            const double dk = d[k], dk1 = d[k + 1], ek = e[k];
+            d[k] = c * c * dk - 2 * c * s * ek + s * s * dk1;
+            d[k + 1] = s * s * dk + 2 * c * s * ek + c * c * dk1;
+            e[k] = c * s * (dk - dk1) + (c * c - s * s) * ek;
+            if (k < end - 1) {
+                z = -s * e[k + 1];
+                e[k + 1] = c * e[k + 1];
+            }
+            x = e[k];
+            for (int q = 0; q < n; ++q) {
+                const double qa = Q[q * n + k], qb = Q[q * n + k + 1];
+                Q[q * n + k] = c * qa - s * qb;
+                Q[q * n + k + 1] = s * qa + c * qb;
+            }
+        }
+    }
+    return true;
+}
+
+// 0: tridiagonal QR (default), 1: cyclic Jacobi (independent cross-check)
+static int g_psd_solver = 0;
+
 static void project_psd(int n, double* H, int method)
 {
     if (method == 0) return;
     double lam[12], V[144];
-    jacobi_eig(n, H, lam, V);
+    if (g_psd_solver == 1 || !ql_eig(n, H, lam, V)) jacobi_eig(n, H, lam, V);
     double mn = lam[0];
     for (int i = 1; i < n; ++i) mn = std::min(mn, lam[i]);
     if (mn >= 0.0) return;
@@ -1239,6 +1333,7 @@ static void contact_hessian(const BarrierParams& P, const Contact& c, const V3* 
 // method) + IPC strategy (tight_inclusion_ccd.cpp:33-75).
 // ---------------------------------------------------------------------------
 static const int CCD_STACK = 128;
+static thread_local long long g_ccd_iters = 0; // boxes examined (diagnostics)
 
 struct CCDQuery {
     V3 s[4], e[4]; // start/end positions; VF: p,t0,t1,t2 ; EE: a0,a1,b0,b1
@@ -1315,34 +1410,52 @@ struct CBox {
 
 static inline double cbox_w(const CBox& b, int d) { return std::ldexp(1.0, -b.lvl[d]); }
 
-// Inclusion test.  Returns zero_in; sets box_in and codomain widths.
-static bool ccd_inclusion(const CCDQuery& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3])
+// Inclusion test.  Returns zero_in; sets box_in, the codomain widths cw[c],
+// whether component c lies inside [-eps-ms, eps+ms] (inside[c]) and the
+// largest change of component c between the two faces of the box across
+// parameter d (var[c][d]).
+static bool ccd_inclusion(const CCDQuery& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3],
+    double var[3][3], bool inside[3])
 {
-    const double t0 = b.lo[0], t1 = b.lo[0] + cbox_w(b, 0);
-    const double u0 = b.lo[1], u1 = b.lo[1] + cbox_w(b, 1);
-    const double v0 = b.lo[2], v1 = b.lo[2] + cbox_w(b, 2);
+    const double ts[2] = { b.lo[0], b.lo[0] + cbox_w(b, 0) };
+    const double us[2] = { b.lo[1], b.lo[1] + cbox_w(b, 1) };
+    const double vs[2] = { b.lo[2], b.lo[2] + cbox_w(b, 2) };
     bool zin = true;
     box_in = true;
     for (int c = 0; c < 3; ++c) {
+        double f[2][2][2];
+        var[c][0] = var[c][1] = var[c][2] = 0;
         double mn = std::numeric_limits<double>::infinity(), mx = -mn;
-        const double ts[2] = { t0, t1 }, us[2] = { u0, u1 }, vs[2] = { v0, v1 };
         for (int i = 0; i < 2; ++i)
             for (int j = 0; j < 2; ++j)
                 for (int k = 0; k < 2; ++k) {
-                    const double f = ccd_F(q, c, ts[i], us[j], vs[k]);
-                    mn = std::min(mn, f);
-                    mx = std::max(mx, f);
+                    f[i][j][k] = ccd_F(q, c, ts[i], us[j], vs[k]);
+                    mn = std::min(mn, f[i][j][k]);
+                    mx = std::max(mx, f[i][j][k]);
                 }
+        for (int j = 0; j < 2; ++j)
+            for (int k = 0; k < 2; ++k) {
+                var[c][0] = std::max(var[c][0], std::fabs(f[1][j][k] - f[0][j][k]));
+                var[c][1] = std::max(var[c][1], std::fabs(f[j][1][k] - f[j][0][k]));
+                var[c][2] = std::max(var[c][2], std::fabs(f[j][k][1] - f[j][k][0]));
+            }
         const double r = err[c] + ms;
         if (mn > r || mx < -r) zin = false;
-        if (!(mn >= -r && mx <= r)) box_in = false;
+        inside[c] = (mn >= -r && mx <= r);
+        if (!inside[c]) box_in = false;
         cw[c] = mx - mn;
     }
     return zin;
 }
 
-// Earliest-time branch and bound over (t,u,v) ∈ [0,1]³.  Returns whether a
-// root box was found before tmax; toi = its lower time bound.
+// Earliest-time branch and bound over (t,u,v) in [0,1]^3.  A box is
+// accepted when every component of its function box is inside the
+// separation box or narrower than the codomain tolerance delta (the union of
+// Tight-Inclusion's "box inside the eps-box" and "codomain width below
+// delta" tests), or when it is below the domain tolerances; it is split
+// across the parameter along which the still-straddling components change
+// most.  Returns whether a root box was found before tmax; toi = the
+// smallest lower time bound of an accepted box.
 static bool ccd_root_finder(const CCDQuery& q, const double err[3], double ms, const double tol[3], double delta,
     double tmax, long max_itr, double& toi, double& out_tol)
 {
@@ -1360,13 +1473,18 @@ static bool ccd_root_finder(const CCDQuery& q, const double err[3], double ms, c
         const CBox b = st[--sp];
         if (b.lo[0] >= best) continue;
         ++itr;
+        ++g_ccd_iters;
         bool box_in;
-        double cw[3];
-        if (!ccd_inclusion(q, b, err, ms, box_in, cw)) continue;
+        double cw[3], var[3][3];
+        bool inside[3];
+        if (!ccd_inclusion(q, b, err, ms, box_in, cw, var, inside)) continue;
         const double w[3] = { cbox_w(b, 0), cbox_w(b, 1), cbox_w(b, 2) };
-        const bool small_co = cw[0] <= delta && cw[1] <= delta && cw[2] <= delta;
+        // every component of the function box is either inside the
+        // [-eps-ms, eps+ms] box or narrower than the codomain tolerance
+        const bool small_co = (inside[0] || cw[0] <= delta) && (inside[1] || cw[1] <= delta)
+            && (inside[2] || cw[2] <= delta);
         const bool small_dom = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
-        const bool too_deep = b.lvl[0] >= 60 || b.lvl[1] >= 60 || b.lvl[2] >= 60;
+        const bool too_deep = b.lvl[0] >= 60 && b.lvl[1] >= 60 && b.lvl[2] >= 60;
         if (small_co || box_in || small_dom || too_deep || sp + 2 > CCD_STACK) {
             best = b.lo[0];
             found = true;
@@ -1382,14 +1500,21 @@ static bool ccd_root_finder(const CCDQuery& q, const double err[3], double ms, c
             out_tol = std::max(out_tol, std::max(cw[0], std::max(cw[1], cw[2])));
             break;
         }
-        // split the dimension with the largest width / tolerance
-        int sd = 0;
-        double br = w[0] / tol[0];
-        for (int d = 1; d < 3; ++d)
-            if (w[d] / tol[d] > br) {
-                br = w[d] / tol[d];
+        // Split the parameter across which the components that still
+        // straddle the separation box change most: that halves the dominant
+        // term of their (multilinear) range.  Parameters already at the
+        // depth limit are not split.
+        int sd = -1;
+        double best_var = -1;
+        for (int d = 0; d < 3; ++d) {
+            double vd = 0;
+            for (int c = 0; c < 3; ++c)
+                if (!inside[c]) vd = std::max(vd, var[c][d]);
+            if (b.lvl[d] < 60 && vd > best_var) {
+                best_var = vd;
                 sd = d;
             }
+        }
         CBox lo = b, hi = b;
         lo.lvl[sd] = hi.lvl[sd] = (int8_t)(b.lvl[sd] + 1);
         hi.lo[sd] = b.lo[sd] + cbox_w(lo, sd);
@@ -1545,6 +1670,8 @@ double orc_point_edge_distance(const double* p, const double* e0, const double* 
     if (dtype < 0) dtype = point_edge_distance_type(P, E0, E1);
     return point_edge_distance(P, E0, E1, dtype);
 }
+void orc_set_psd_solver(int which) { g_psd_solver = which; }
+
 double orc_barrier(double d, double dhat, int deriv)
 {
     return deriv == 0 ? barrier(d, dhat) : (deriv == 1 ? barrier_d1(d, dhat) : barrier_d2(d, dhat));
@@ -1836,6 +1963,51 @@ int orc_edge_edge_ccd(const double* x0, const double* x1, double min_distance, d
     const bool hit = ee_ccd(x0, x1, E, 0, 1, min_distance, P, tmax, t);
     *toi = t;
     return hit;
+}
+
+// Batched single-stencil CCD (VF: p,t0,t1,t2; EE: a0,a1,b0,b1 rows) with the
+// number of boxes each query examined.
+void orc_ccd_stencils(int is_ee, int64_t n, const double* x0, const double* x1, double min_distance, double tmax,
+    double tolerance, long max_iterations, double rescale, int8_t* hit, double* toi, int64_t* iters)
+{
+    const CCDParams P { tolerance, max_iterations, rescale };
+    for (int64_t i = 0; i < n; ++i) {
+        g_ccd_iters = 0;
+        double t = std::numeric_limits<double>::infinity();
+        bool h;
+        if (is_ee) {
+            const int32_t E[4] = { 0, 1, 2, 3 };
+            h = ee_ccd(x0 + 12 * i, x1 + 12 * i, E, 0, 1, min_distance, P, tmax, t);
+        } else {
+            const int32_t F[3] = { 1, 2, 3 };
+            h = fv_ccd(x0 + 12 * i, x1 + 12 * i, F, 0, 0, min_distance, P, tmax, t);
+        }
+        hit[i] = h;
+        toi[i] = t;
+        if (iters) iters[i] = g_ccd_iters;
+    }
+}
+
+// Broad-phase candidates of the swept boxes (candidates.cpp:128-222):
+// returns counts; fills ee / fv pairs when the output pointers are given.
+void* orc_ccd_candidates(const double* V0, const double* V1, int64_t nV, const int32_t* E, int64_t nE,
+    const int32_t* F, int64_t nF, double min_distance, int nthreads, int64_t* counts)
+{
+    std::vector<Box> vb;
+    vertex_boxes_dynamic(V0, V1, nV, 0.5 * min_distance, vb);
+    Candidates* cand = new Candidates();
+    detect_candidates(vb, E, nE, F, nF, nthreads, *cand);
+    std::vector<std::pair<int, int>> ee(cand->ee.size() / 2), fv(cand->fv.size() / 2);
+    counts[0] = cand->ee.size() / 2;
+    counts[1] = cand->fv.size() / 2;
+    return cand;
+}
+void orc_ccd_candidates_get(void* h, int32_t* ee, int32_t* fv)
+{
+    Candidates* c = (Candidates*)h;
+    std::copy(c->ee.begin(), c->ee.end(), ee);
+    std::copy(c->fv.begin(), c->fv.end(), fv);
+    delete c;
 }
 
 // compute_collision_free_stepsize (ipc.cpp:42-106, candidates.cpp:252-292)

@@ -42,6 +42,7 @@ def lib():
         L.orc_edge_edge_distance.argtypes = [P, P, P, P, i32]
         L.orc_point_edge_distance.restype = d
         L.orc_point_edge_distance.argtypes = [P, P, P, i32]
+        L.orc_set_psd_solver.argtypes = [i32]
         L.orc_barrier.restype = d
         L.orc_barrier.argtypes = [d, d, i32]
         L.orc_distance_derivatives.restype = d
@@ -69,6 +70,10 @@ def lib():
         L.orc_point_triangle_ccd.argtypes = [P, P, d, d, d, C.c_long, d, P]
         L.orc_edge_edge_ccd.restype = i32
         L.orc_edge_edge_ccd.argtypes = [P, P, d, d, d, C.c_long, d, P]
+        L.orc_ccd_stencils.argtypes = [i32, i64, P, P, d, d, d, C.c_long, d, P, P, P]
+        L.orc_ccd_candidates.restype = vp
+        L.orc_ccd_candidates.argtypes = [P, P, i64, P, i64, P, i64, d, i32, P]
+        L.orc_ccd_candidates_get.argtypes = [vp, P, P]
         L.orc_collision_free_stepsize.restype = d
         L.orc_collision_free_stepsize.argtypes = [P, P, i64, P, i64, P, i64, d, d, C.c_long, d, i32, P]
         _lib = L
@@ -113,6 +118,11 @@ def edge_edge_distance(a0, a1, b0, b1, dtype=-1):
 def point_edge_distance(p, e0, e1, dtype=-1):
     a = [_f64(x) for x in (p, e0, e1)]
     return lib().orc_point_edge_distance(*(_p(x) for x in a), dtype)
+
+
+def set_psd_solver(name: str):
+    """'ql' (tridiagonal QR, default) or 'jacobi' (independent cross-check)."""
+    lib().orc_set_psd_solver({"ql": 0, "jacobi": 1}[name])
 
 
 def barrier(d, dhat, deriv=0):
@@ -255,3 +265,36 @@ def collision_free_stepsize(V0, V1, E, F, min_distance=0.0, tolerance=1e-6, max_
                                           min_distance, tolerance, max_iterations, rescale,
                                           int(nthreads or os.cpu_count() or 1), _p(nc))
     return float(t), int(nc[0])
+
+
+def ccd_stencils(is_ee, x0, x1, min_distance=0.0, tmax=1.0, tolerance=1e-6, max_iterations=10_000_000,
+                 rescale=0.8):
+    """Batched single-stencil CCD; returns (hit bool[n], toi[n], boxes examined[n])."""
+    x0 = _f64(x0).reshape(-1, 4, 3)
+    x1 = _f64(x1).reshape(-1, 4, 3)
+    n = x0.shape[0]
+    hit = np.zeros(n, np.int8)
+    toi = np.zeros(n)
+    it = np.zeros(n, np.int64)
+    lib().orc_ccd_stencils(int(is_ee), n, _p(x0), _p(x1), min_distance, tmax, tolerance, max_iterations, rescale,
+                           _p(hit), _p(toi), _p(it))
+    return hit.astype(bool), toi, it
+
+
+def ccd_candidates(V0, V1, E, F, min_distance=0.0, nthreads=None):
+    """Swept-box broad-phase candidates: (ee pairs (k,2), fv pairs (k,2))."""
+    V0, V1, E, F = _f64(V0), _f64(V1), _i32(E), _i32(F)
+    cnt = np.zeros(2, np.int64)
+    h = lib().orc_ccd_candidates(_p(V0), _p(V1), V0.shape[0], _p(E), E.shape[0], _p(F), F.shape[0], min_distance,
+                                 int(nthreads or os.cpu_count() or 1), _p(cnt))
+    ee = np.zeros((int(cnt[0]), 2), np.int32)
+    fv = np.zeros((int(cnt[1]), 2), np.int32)
+    lib().orc_ccd_candidates_get(h, _p(ee), _p(fv))
+    return ee, fv
+
+
+def ccd_stencil_positions(V0, V1, E, F, ee, fv):
+    """Stencil positions (x0, x1) of EE candidates then FV candidates."""
+    ids_ee = np.concatenate([E[ee[:, 0]], E[ee[:, 1]]], axis=1)
+    ids_fv = np.concatenate([fv[:, 1:2], F[fv[:, 0]]], axis=1)
+    return (V0[ids_ee], V1[ids_ee]), (V0[ids_fv], V1[ids_fv])

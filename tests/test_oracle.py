@@ -1,0 +1,424 @@
+"""The CPU oracle pinned against the reference's own known-answer tests.
+
+Each test restates an analytic test of the reference (cited by file:line of
+tests/src/tests/ in ipc-toolkit) or checks a derivative by central finite
+differences, the way the reference's FD tests do.  The reference itself
+cannot be built in this container (its CMake dependencies are absent), so
+these tests and the committed fixtures in tests/golden/ are what pins the
+oracle.
+"""
+import numpy as np
+import pytest
+
+EPS32 = float(np.finfo(np.float32).eps)
+
+
+def approx(a, b, margin=0.0, eps=100 * EPS32):
+    """Catch::Approx semantics: |a-b| <= margin or relative eps."""
+    return abs(a - b) <= margin or abs(a - b) <= eps * (max(abs(a), abs(b)))
+
+
+# --- distances ---------------------------------------------------------------
+
+def test_point_triangle_distance_grid(oracle_mod):
+    """distance/test_point_triangle.cpp:31-112"""
+    from test_gpu_parity import _pt_grid
+    x, cps = _pt_grid()
+    for i in range(len(x)):
+        d = oracle_mod.point_triangle_distance(*x[i])
+        assert approx(d, float(((x[i, 0] - cps[i]) ** 2).sum()), margin=1e-12)
+
+
+def test_edge_edge_distance_grid(oracle_mod):
+    """distance/test_edge_edge.cpp:31-66"""
+    n = 0
+    for e0y in (-10, -1, -1e-4, 0, 1e-4, 1, 10):
+        for shiftx in (-2, 0, 2):
+            for shiftz in (-2, 0, 2):
+                for ox in (-1, -0.5, 0, 0.5, 1):
+                    for oz in (-1, -0.5, 0, 0.5, 1):
+                        e0x, e0z = shiftx + ox, shiftz + oz
+                        e00 = np.array([-1 + e0x, e0y, e0z])
+                        e01 = np.array([1 + e0x, e0y, e0z])
+                        e10 = np.array([0.0, 0, -1])
+                        e11 = np.array([0.0, 0, 1])
+                        c0 = e00 if shiftx > 1 else (e01 if shiftx < -1 else np.array([0, e0y, e0z]))
+                        c1 = e11 if shiftz > 1 else (e10 if shiftz < -1 else np.array([0, 0, e0z]))
+                        d = oracle_mod.edge_edge_distance(e00, e01, e10, e11)
+                        assert approx(d, float(((c0 - c1) ** 2).sum()), margin=1e-12)
+                        n += 1
+    assert n == 7 * 9 * 25
+
+
+def test_edge_edge_distance_not_line_line(oracle_mod):
+    """distance/test_edge_edge.cpp:68-128 (closest points at an endpoint)"""
+    rng = np.random.Generator(np.random.PCG64(11))
+    sign = lambda x: -1 if x < 0 else 1
+    for alpha0 in np.arange(-1.0, 2.0, 0.1):
+        for s0 in np.arange(-10.0, 10.0, 1.0):
+            if s0 == 0:
+                continue
+            for swap_ea in (False, True):
+                for swap_eb in (False, True):
+                    for swap_edges in (False, True):
+                        for _ in range(3):
+                            alpha, s = alpha0, s0
+                            ea0, ea1 = rng.uniform(-1, 1, 3), rng.uniform(-1, 1, 3)
+                            n = np.cross(ea1 - ea0, [1, 0, 0])
+                            n /= np.linalg.norm(n)
+                            eb0 = ((ea1 - ea0) * alpha + ea0) + s * n
+                            if alpha < 0:
+                                alpha = 0
+                                n = eb0 - ea0
+                                s = np.linalg.norm(n)
+                                n /= s
+                            elif alpha > 1:
+                                alpha = 1
+                                n = eb0 - ea1
+                                s = np.linalg.norm(n)
+                                n /= s
+                            eb1 = ((ea1 - ea0) * alpha + ea0) + (s + sign(s) * 1) * n
+                            a0, a1, b0, b1 = ea0, ea1, eb0, eb1
+                            if swap_ea:
+                                a0, a1 = a1, a0
+                            if swap_eb:
+                                b0, b1 = b1, b0
+                            if swap_edges:
+                                a0, b0 = b0, a0
+                                a1, b1 = b1, a1
+                            d = oracle_mod.edge_edge_distance(a0, a1, b0, b1)
+                            assert approx(d, s * s, margin=1e-15)
+
+
+def test_edge_edge_distance_line_line(oracle_mod):
+    """distance/test_edge_edge.cpp:130-180 (interior closest points)"""
+    rng = np.random.Generator(np.random.PCG64(12))
+    for _ in range(500):
+        alpha, beta = rng.uniform(0.01, 0.99, 2)
+        s = rng.uniform(-5, 5)
+        ea1, eb1 = rng.uniform(-1, 1, 3), rng.uniform(-1, 1, 3)
+        u = rng.normal(size=3)
+        v = rng.normal(size=3)
+        n = np.cross(u, v)
+        n /= np.linalg.norm(n)
+        pa = rng.uniform(-1, 1, 3)
+        pb = pa + s * n
+        ea0 = pa - alpha * u
+        ea1 = ea0 + u
+        eb0 = pb - beta * v
+        eb1 = eb0 + v
+        d = oracle_mod.edge_edge_distance(ea0, ea1, eb0, eb1)
+        assert oracle_mod.edge_edge_distance_type(ea0, ea1, eb0, eb1) == 8
+        assert abs(d - s * s) <= 1e-12 * max(1, s * s)
+
+
+def test_point_edge_distance(oracle_mod):
+    """distance/test_point_edge.cpp: closest to e0 / e1 / interior"""
+    e0, e1 = np.array([-1.0, 0, 0]), np.array([1.0, 0, 0])
+    for px in np.linspace(-3, 3, 25):
+        for py in (-2, -1e-8, 0, 1e-8, 2):
+            p = np.array([px, py, 0.5])
+            cx = min(max(px, -1), 1)
+            exp = (px - cx) ** 2 + py ** 2 + 0.25
+            assert approx(oracle_mod.point_edge_distance(p, e0, e1), exp, margin=1e-12)
+            t = oracle_mod.point_edge_distance_type(p, e0, e1)
+            assert t == (0 if px < -1 else (1 if px > 1 else 2))
+
+
+def test_edge_edge_parallel_types(oracle_mod):
+    """distance/test_distance_type.cpp: parallel edges classify by overlap"""
+    a0, a1 = np.array([0.0, 0, 0]), np.array([1.0, 0, 0])
+    # b entirely beyond a1 -> EA1_EB0
+    assert oracle_mod.edge_edge_distance_type(a0, a1, np.array([2.0, 1, 0]), np.array([3.0, 1, 0])) == 2
+    # b before a0 -> EA0_EB1
+    assert oracle_mod.edge_edge_distance_type(a0, a1, np.array([-3.0, 1, 0]), np.array([-2.0, 1, 0])) == 1
+    # overlapping -> an edge-point type, never line-line
+    t = oracle_mod.edge_edge_distance_type(a0, a1, np.array([0.5, 1, 0]), np.array([1.5, 1, 0]))
+    assert t in (4, 5, 6, 7)
+    d = oracle_mod.edge_edge_distance(a0, a1, np.array([0.5, 1, 0]), np.array([1.5, 1, 0]))
+    assert approx(d, 1.0, margin=1e-15)
+
+
+def test_degenerate_edges(oracle_mod):
+    """distance_type.cpp:19-24 and :97-103: zero-length edges"""
+    p = np.array([0.0, 1, 0])
+    z = np.zeros(3)
+    assert oracle_mod.point_edge_distance_type(p, z, z) == 0
+    assert oracle_mod.edge_edge_distance_type(z, z, p, p) == 0
+    assert oracle_mod.edge_edge_distance_type(z, z, p, 2 * p) == 6
+    assert oracle_mod.edge_edge_distance_type(p, 2 * p, z, z) == 4
+
+
+# --- barrier -----------------------------------------------------------------
+
+@pytest.mark.parametrize("use_sq", [False, True])
+def test_barrier_derivatives_fd(oracle_mod, use_sq):
+    """barrier/test_barrier.cpp:398-461 (ClampedLogBarrier)"""
+    for k in range(-2 if use_sq else -5, 0):
+        dhat = 10.0 ** k
+        for d in np.linspace(0.5 * dhat, 0.9 * dhat, 10, endpoint=False):
+            if use_sq:
+                d, dh = d * d, dhat * dhat
+            else:
+                dh = dhat
+            h = 1e-10 * max(1.0, d) if not use_sq else d * 1e-6
+            fd1 = (oracle_mod.barrier(d + h, dh) - oracle_mod.barrier(d - h, dh)) / (2 * h)
+            fd2 = (oracle_mod.barrier(d + h, dh, 1) - oracle_mod.barrier(d - h, dh, 1)) / (2 * h)
+            assert abs(oracle_mod.barrier(d, dh, 1) - fd1) <= 1e-4 * max(abs(fd1), 1e-30) + 1e-9 * dh
+            assert abs(oracle_mod.barrier(d, dh, 2) - fd2) <= 1e-4 * max(abs(fd2), 1e-30) + 1e-9
+
+
+def test_barrier_values(oracle_mod):
+    """barrier.cpp:11-43: b(d)=-(d-dh)^2 ln(d/dh) on (0,dh), 0 beyond, inf at 0"""
+    assert oracle_mod.barrier(0.0, 1.0) == float("inf")
+    assert oracle_mod.barrier(1.0, 1.0) == 0.0
+    assert oracle_mod.barrier(2.0, 1.0) == 0.0
+    assert oracle_mod.barrier(2.0, 1.0, 1) == 0.0
+    d, dh = 0.3, 1.0
+    assert oracle_mod.barrier(d, dh) == pytest.approx(-(d - dh) ** 2 * np.log(d / dh), rel=1e-15)
+
+
+# --- distance derivatives (finite differences) --------------------------------
+
+def _fd(f, x, h=1e-7):
+    g = np.zeros_like(x)
+    for i in range(x.size):
+        e = np.zeros_like(x)
+        e[i] = h
+        g[i] = (f(x + e) - f(x - e)) / (2 * h)
+    return g
+
+
+@pytest.mark.parametrize("kind,dtype", [(0, 8), (1, 8), (2, 8), (3, 8), (3, 0), (3, 4), (3, 6)])
+def test_distance_derivatives_fd(oracle_mod, kind, dtype):
+    rng = np.random.Generator(np.random.PCG64(100 + kind * 10 + dtype))
+    n = {0: 2, 1: 3, 2: 4, 3: 4}[kind]
+    for _ in range(20):
+        x = rng.uniform(-1, 1, 3 * n)
+        d, g, H = oracle_mod.distance_derivatives(kind, x, dtype)
+        fg = _fd(lambda y: oracle_mod.distance_derivatives(kind, y, dtype)[0], x)
+        assert np.linalg.norm(g - fg) <= 1e-6 * max(1.0, np.linalg.norm(fg))
+        fH = np.stack([_fd(lambda y: oracle_mod.distance_derivatives(kind, y, dtype)[1][i], x)
+                       for i in range(3 * n)])
+        assert np.linalg.norm(H - fH) <= 1e-5 * max(1.0, np.linalg.norm(fH))
+        assert np.allclose(H, H.T, atol=1e-12 * max(1, np.abs(H).max()))
+
+
+@pytest.mark.parametrize("ctype", [0, 1, 2, 3])
+def test_contact_local_derivatives_fd(oracle_mod, ctype):
+    """potential/test_barrier_potential.cpp:119-246 style FD checks of the
+    per-contact energy / gradient / Hessian, including mollified EE."""
+    rng = np.random.Generator(np.random.PCG64(200 + ctype))
+    n = {0: 2, 1: 3, 2: 4, 3: 4}[ctype]
+    dhat, kappa = 1e-1, 1.0
+    checked = 0
+    for _ in range(200):
+        x = rng.uniform(-0.1, 0.1, (n, 3))
+        if ctype == 2:
+            # nearly parallel edges close together -> mollified
+            x[1] = x[0] + np.array([0.2, 0.0, 0.0])
+            x[2] = x[0] + np.array([0.05, 0.03, 0.01]) + rng.uniform(-0.005, 0.005, 3)
+            x[3] = x[2] + np.array([0.2, 0.001, 0.0]) + rng.uniform(-0.002, 0.002, 3)
+            eps = 1e-3 * 0.04 * 0.04
+            dtype = oracle_mod.edge_edge_distance_type(*x)
+        else:
+            eps, dtype = 0.0, 8
+        x = x.ravel()
+        e, g, H = oracle_mod.contact_local(ctype, x, dhat, kappa, eps=eps, dtype=dtype)
+        if e == 0 or not np.isfinite(e):
+            continue
+        fe = lambda y: oracle_mod.contact_local(ctype, y, dhat, kappa, eps=eps, dtype=dtype)[0]
+        fg = _fd(fe, x, 1e-8)
+        assert np.linalg.norm(g - fg) <= 1e-4 * np.linalg.norm(fg) + 1e-12
+        fH = np.stack([_fd(lambda y: oracle_mod.contact_local(ctype, y, dhat, kappa, eps=eps, dtype=dtype)[1][i],
+                           x, 1e-8) for i in range(x.size)])
+        assert np.linalg.norm(H - fH) <= 1e-3 * np.linalg.norm(fH) + 1e-9
+        checked += 1
+        if checked >= 5:
+            break
+    assert checked > 0
+
+
+@pytest.mark.parametrize("psd", ["clamp", "abs"])
+def test_psd_projection(oracle_mod, psd):
+    """eigen_ext.tpp:64-108: projected Hessian is PSD; clamp keeps the
+    non-negative spectrum, abs flips the negative part."""
+    rng = np.random.Generator(np.random.PCG64(7))
+    for ctype in (0, 1, 3):
+        n = {0: 2, 1: 3, 3: 4}[ctype]
+        for _ in range(5):
+            x = rng.uniform(-0.02, 0.02, 3 * n)
+            _, _, H0 = oracle_mod.contact_local(ctype, x, 0.1, 1.0, psd="none")
+            _, _, H = oracle_mod.contact_local(ctype, x, 0.1, 1.0, psd=psd)
+            lam0 = np.linalg.eigvalsh(H0)
+            lam = np.linalg.eigvalsh(H)
+            scale = np.abs(lam0).max()
+            assert lam.min() >= -1e-12 * scale
+            exp = np.sort(np.maximum(lam0, 0) if psd == "clamp" else np.abs(lam0))
+            assert np.allclose(np.sort(lam), exp, atol=1e-11 * scale)
+
+
+# --- CCD ---------------------------------------------------------------------
+
+def test_point_triangle_ccd_cases(oracle_mod):
+    """ccd/test_point_triangle_ccd.cpp:25-123"""
+    from test_gpu_parity import _pt_ccd_cases
+    for a, b, exp, conservative in _pt_ccd_cases():
+        hit, toi = oracle_mod.point_triangle_ccd(a, b)
+        if conservative:
+            assert hit or not exp
+        else:
+            assert hit == exp
+        if hit:
+            assert 0 <= toi <= 1
+
+
+def _ee_ccd_general():
+    """ccd/test_edge_edge_ccd.cpp:29-56"""
+    out = []
+    for uy in (-1.0, 0.0, 1 - EPS32, 1.0, 1 + EPS32, 2.0):
+        for e1x in (-1 - EPS32, -1, -1 + EPS32, -0.5, 0, 0.5, 1 - EPS32, 1, 1 + EPS32):
+            x0 = np.array([[-1, -1, 0], [1, -1, 0], [e1x, 1, -1], [e1x, 1, 1]], float)
+            for moving in (True, False):
+                if moving:
+                    u0, u1 = np.array([0, uy, 0]), np.array([0, -uy, 0])
+                    exp = uy >= 1.0 and -1 <= e1x <= 1
+                else:
+                    u0, u1 = np.array([0, 2 * uy, 0]), np.zeros(3)
+                    exp = uy >= 2.0 and -1 <= e1x <= 1
+                x1 = x0 + np.stack([u0, u0, u1, u1])
+                out.append((x0, x1, exp))
+    return out
+
+
+def test_edge_edge_ccd_cases(oracle_mod):
+    for a, b, exp in _ee_ccd_general():
+        hit, toi = oracle_mod.edge_edge_ccd(a, b)
+        assert hit or not exp
+
+
+def test_edge_edge_ccd_adversarial(oracle_mod):
+    """ccd/test_edge_edge_ccd.cpp 'Adversarial ACCD Case'"""
+    for d0 in (1e-2, 1e-4, 1e-6, 1e-8):
+        x0 = np.array([[-1.0, -d0 / 2, 0], [1.0, -d0 / 2, 0], [0, d0 / 2, -1.0], [0, d0 / 2, 1.0]])
+        s = 1e-3
+        x1 = x0 + np.array([[-s, d0, -s], [s, d0, s], [s, -d0, s], [-s, -d0, -s]])
+        hit, toi = oracle_mod.edge_edge_ccd(x0, x1)
+        assert hit
+
+
+def test_ccd_conservative_on_linear_impacts(oracle_mod):
+    """A point falling onto a static triangle at a known time: the returned
+    ToI never exceeds the analytic impact time and is within the TI
+    tolerance of it (rescaled by 0.8 only for tiny ToIs)."""
+    rng = np.random.Generator(np.random.PCG64(21))
+    for _ in range(40):
+        t_hit = rng.uniform(0.05, 0.95)
+        z0 = rng.uniform(0.01, 0.1)
+        p0 = np.array([rng.uniform(0.1, 0.3), rng.uniform(0.1, 0.3), z0])
+        tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], float)
+        p1 = p0 - np.array([0, 0, z0 / t_hit])
+        hit, toi = oracle_mod.point_triangle_ccd(np.vstack([p0, tri]), np.vstack([p1, tri]))
+        assert hit
+        assert toi <= t_hit
+        # effective minimum separation min(0.2*d0, 1e-4) plus tolerance
+        speed = z0 / t_hit
+        slack = (min(0.2 * z0, 1e-4) + 2e-6) / speed
+        assert toi >= t_hit - slack - 1e-9
+
+
+# --- collision set -------------------------------------------------------------
+
+def _brute_force(V, E, F, dhat, oracle_mod):
+    """All EE and FV pairs without a broad phase (brute_force.cpp semantics),
+    then the same filter: the collision set must not depend on the broad phase."""
+    from itertools import combinations
+    off = dhat * dhat
+    vv, ev, ee, fv = {}, {}, [], []
+    F2E = oracle_mod.faces_to_edges(F, E)
+    for ea, eb in combinations(range(len(E)), 2):
+        if set(E[ea]) & set(E[eb]):
+            continue
+        x = V[[E[ea][0], E[ea][1], E[eb][0], E[eb][1]]]
+        t = oracle_mod.edge_edge_distance_type(*x)
+        if not oracle_mod.edge_edge_distance(*x, dtype=t) < off:
+            continue
+        ids = [E[ea][0], E[ea][1], E[eb][0], E[eb][1]]
+        ra = V[ids]
+        eps = 1e-3 * np.sum((ra[0] - ra[1]) ** 2) * np.sum((ra[2] - ra[3]) ** 2)
+        c = np.sum(np.cross(x[1] - x[0], x[3] - x[2]) ** 2)
+        tt = 8 if c < eps else t
+        if tt < 4:
+            a, b = [(0, 2), (0, 3), (1, 2), (1, 3)][tt]
+            k = (min(ids[a], ids[b]), max(ids[a], ids[b]))
+            vv[k] = vv.get(k, 0) + 1
+        elif tt < 8:
+            e, v = [(ea, ids[2]), (ea, ids[3]), (eb, ids[0]), (eb, ids[1])][tt - 4]
+            ev[(e, v)] = ev.get((e, v), 0) + 1
+        else:
+            ee.append((ea, eb, t))
+    for f in range(len(F)):
+        for v in range(len(V)):
+            if v in F[f]:
+                continue
+            x = V[[v, F[f][0], F[f][1], F[f][2]]]
+            t = oracle_mod.point_triangle_distance_type(*x)
+            if not oracle_mod.point_triangle_distance(*x, dtype=t) < off:
+                continue
+            if t < 3:
+                k = (min(v, F[f][t]), max(v, F[f][t]))
+                vv[k] = vv.get(k, 0) + 1
+            elif t < 6:
+                k = (F2E[f][t - 3], v)
+                ev[k] = ev.get(k, 0) + 1
+            else:
+                fv.append((f, v))
+    return vv, ev, sorted(ee), sorted(fv)
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_collision_set_independent_of_broad_phase(oracle_mod, seed):
+    from ipctk_gb300 import scenes
+    sc = scenes.two_sheet(side=6, seed=seed, gap=3e-3, jitter=1e-3, dhat=4e-3)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    vv, ev, ee, fv = _brute_force(V, E, F, sc["dhat"], oracle_mod)
+    col = oracle_mod.build_collisions(V, E, F, sc["dhat"])
+    assert dict(zip(map(tuple, col.vv.tolist()), col.vv_w.tolist())) == vv
+    assert dict(zip(map(tuple, col.ev.tolist()), col.ev_w.tolist())) == ev
+    assert [(a, b, int(t)) for (a, b), t in zip(col.ee.tolist(), col.ee_dtype)] == ee
+    assert list(map(tuple, col.fv.tolist())) == fv
+    assert len(col) > 0
+
+
+def test_collision_set_thread_independent(oracle_mod):
+    from ipctk_gb300 import scenes
+    sc = scenes.two_sheet(side=32, seed=2)
+    a = oracle_mod.build_collisions(sc["V"], sc["E"], sc["F"], sc["dhat"], nthreads=1)
+    b = oracle_mod.build_collisions(sc["V"], sc["E"], sc["F"], sc["dhat"], nthreads=8)
+    for k in ("vv", "vv_w", "ev", "ev_w", "ee", "ee_dtype", "ee_eps", "fv"):
+        assert np.array_equal(getattr(a, k), getattr(b, k))
+
+
+def test_faces_to_edges_missing_edge(oracle_mod):
+    F = np.array([[0, 1, 2]])
+    E = np.array([[0, 1], [1, 2]])
+    with pytest.raises(RuntimeError, match="Unable to find edge"):
+        oracle_mod.faces_to_edges(F, E)
+
+
+def test_psd_solvers_agree(oracle_mod):
+    """The tridiagonal-QR projection used by default and an independent
+    cyclic-Jacobi projection give the same projected Hessian."""
+    rng = np.random.Generator(np.random.PCG64(31))
+    try:
+        for ctype in (0, 1, 3):
+            n = {0: 2, 1: 3, 3: 4}[ctype]
+            for _ in range(10):
+                x = rng.uniform(-0.02, 0.02, 3 * n)
+                oracle_mod.set_psd_solver("ql")
+                _, _, A = oracle_mod.contact_local(ctype, x, 0.1, 1.0, psd="clamp")
+                oracle_mod.set_psd_solver("jacobi")
+                _, _, B = oracle_mod.contact_local(ctype, x, 0.1, 1.0, psd="clamp")
+                assert np.linalg.norm(A - B) <= 1e-12 * np.linalg.norm(B)
+    finally:
+        oracle_mod.set_psd_solver("ql")
