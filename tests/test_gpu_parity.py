@@ -100,14 +100,16 @@ def test_hessian(built, ipctk, oracle_mod, name, psd):
     H_ref = sp.csr_matrix((va, ci, rp), shape=H.shape)
     assert sp.linalg.norm(H - H_ref) <= REL * sp.linalg.norm(H_ref)
     # pattern: every stored oracle entry is stored by the GPU matrix; the GPU
-    # may store extra explicit zeros inside touched 3x3 blocks
+    # stores whole 3x3 vertex blocks, so it may hold entries the oracle skips
+    # as exact zeros -- those must be zero up to the same tolerance
     Hc = H.tocsr()
     Hc.sort_indices()
     pat = sp.csr_matrix((np.ones_like(H_ref.data), H_ref.indices, H_ref.indptr), shape=H.shape)
     gpat = sp.csr_matrix((np.ones_like(Hc.data), Hc.indices, Hc.indptr), shape=H.shape)
     assert (pat - pat.multiply(gpat)).nnz == 0
     extra = Hc.multiply(gpat - pat.multiply(gpat))
-    assert abs(extra).max() == 0 if extra.nnz else True
+    if extra.nnz:
+        assert abs(extra).max() <= REL * sp.linalg.norm(H_ref)
     # symmetric
     assert sp.linalg.norm(H - H.T) <= 1e-14 * sp.linalg.norm(H)
 
