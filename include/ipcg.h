@@ -153,6 +153,35 @@ int ipcg_barrier_energy_gradient_hessian(const ipcg_collisions* collisions, cons
                                          int use_physical_barrier, int psd_method,
                                          double* energy, double* gradient, ipcg_csr** hessian);
 
+/* Allocation-free barrier energy.  No counterpart in the reference: it exists
+ * for callers that cannot let the library allocate device memory during a
+ * call, such as codes that give all device memory to their own pool under a
+ * hard budget, or that cannot afford cudaMalloc/cudaFree synchronising the
+ * device under their other streams.  It computes the same value as
+ * ipcg_barrier_energy from a collision set held entirely in caller-owned
+ * DEVICE arrays (layout of ipcg_collisions_get, topology as for
+ * ipcg_mesh_create) and writes it to the device double *energy.  It
+ * allocates nothing: the reduction's partial sums live in a static device
+ * array of 16385 doubles (128 KiB) that every GPU loading this library keeps
+ * until exit.  At most 2,097,152 contacts per call (larger sets are
+ * rejected with IPCG_ERR_INVALID).  The work is enqueued on `stream`
+ * (a cudaStream_t, NULL for the default stream) and the call returns without
+ * waiting; *energy is valid once the stream reaches it.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (on different streams or host threads) race
+ * and must be serialised by the caller. */
+int ipcg_barrier_energy_noalloc(const double* vertices, int64_t num_vertices,
+                                const int32_t* edges, int64_t num_edges,
+                                const int32_t* faces, int64_t num_faces,
+                                int64_t nvv, const int32_t* vv, const double* vv_w,
+                                int64_t nev, const int32_t* ev, const double* ev_w,
+                                int64_t nee, const int32_t* ee, const double* ee_eps_x,
+                                const int8_t* ee_dtype, const double* ee_w,
+                                int64_t nfv, const int32_t* fv, const double* fv_w,
+                                double dhat, double stiffness, double dmin,
+                                int use_physical_barrier, double* energy, void* stream);
+
 int ipcg_csr_shape(const ipcg_csr* csr, int64_t* rows, int64_t* nnz);
 /* row_ptr: rows+1 int64, col: nnz int32, val: nnz float64 (host or device) */
 int ipcg_csr_get(const ipcg_csr* csr, int64_t* row_ptr, int32_t* col, double* val);

@@ -540,4 +540,35 @@ int ipcg_distance_stencils(int kind, int64_t n, const double* x, int8_t* dtype, 
     });
 }
 
+int ipcg_barrier_energy_noalloc(const double* vertices, int64_t num_vertices, const int32_t* edges,
+    int64_t num_edges, const int32_t* faces, int64_t num_faces, int64_t nvv, const int32_t* vv, const double* vv_w,
+    int64_t nev, const int32_t* ev, const double* ev_w, int64_t nee, const int32_t* ee, const double* ee_eps_x,
+    const int8_t* ee_dtype, const double* ee_w, int64_t nfv, const int32_t* fv, const double* fv_w, double dhat,
+    double stiffness, double dmin, int use_physical_barrier, double* energy, void* stream)
+{
+    return guarded([&] {
+        require(num_vertices >= 0 && num_edges >= 0 && num_faces >= 0, "negative size");
+        require(nvv >= 0 && nev >= 0 && nee >= 0 && nfv >= 0, "negative count");
+        require(dhat > 0, "dhat must be positive");
+        require(dmin >= 0, "dmin must be non-negative");
+        require(energy != nullptr, "energy is NULL");
+        // every array must already be device memory: this entry point copies
+        // nothing (a host copy could need a staging allocation)
+        const void* must_be_device[] = { energy, vertices, nvv ? vv : nullptr, nvv ? vv_w : nullptr,
+            nev ? ev : nullptr, nev ? ev_w : nullptr, nev ? edges : nullptr, nee ? ee : nullptr,
+            nee ? ee_eps_x : nullptr, nee ? ee_dtype : nullptr, nee ? ee_w : nullptr, nee ? edges : nullptr,
+            nfv ? fv : nullptr, nfv ? fv_w : nullptr, nfv ? faces : nullptr };
+        for (const void* p : must_be_device)
+            if (p != nullptr) require(is_device_ptr(p), "allocation-free energy: every array must be device memory");
+        require(nvv + nev + nee + nfv == 0 || vertices, "vertices is NULL");
+        require(nvv == 0 || (vv && vv_w), "vv arrays are NULL");
+        require(nev == 0 || (ev && ev_w && edges), "ev arrays are NULL");
+        require(nee == 0 || (ee && ee_eps_x && ee_dtype && ee_w && edges), "ee arrays are NULL");
+        require(nfv == 0 || (fv && fv_w && faces), "fv arrays are NULL");
+        const ContactsNoAlloc in { nvv, nev, nee, nfv, vv, ev, ee, fv, vv_w, ev_w, ee_w, fv_w, ee_eps_x, ee_dtype };
+        barrier_energy_noalloc(vertices, edges, faces, in, dhat, stiffness, dmin, use_physical_barrier ? 1 : 0,
+            energy, (cudaStream_t)stream);
+    });
+}
+
 } // extern "C"

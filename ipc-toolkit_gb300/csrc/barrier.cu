@@ -23,6 +23,7 @@
 #include <cub/block/block_reduce.cuh>
 
 #include <cstdio>
+#include <mutex>
 
 #include "geom.cuh"
 #include "internal.cuh"
@@ -957,6 +958,81 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     }
     if (hess && (m->h_counters.p[1] & 1))
         throw Error(IPCG_ERR_CUDA, "unable to project matrix onto positive semi-definite cone");
+}
+
+} // namespace ipcg
+
+// ---------------------------------------------------------------------------
+// Allocation-free barrier energy.
+//
+// Some callers cannot let a library allocate device memory during a call:
+// codes that hand all device memory to their own pool or arena under a hard
+// budget, and codes that must not pay for cudaMalloc/cudaFree, which can
+// synchronise the whole device and stall their other streams.  For them,
+// ipcg_barrier_energy_noalloc evaluates the barrier energy of a collision set
+// given entirely as caller-owned device arrays.  The only scratch it needs,
+// the per-block partial sums of the reduction, lives in the file-scope
+// device array below; every GPU that loads this library keeps that array
+// (NOALLOC_MAX_BLOCKS + 1 doubles, 128 KiB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace ipcg {
+namespace {
+constexpr int NOALLOC_MAX_BLOCKS = 16384; // at most 16384 * BLOCK = 2,097,152 contacts per call
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+} // namespace
+} // namespace ipcg
+
+static __device__ __align__(256) double g_noalloc_partials[ipcg::NOALLOC_MAX_BLOCKS + 1];
+
+namespace ipcg {
+namespace {
+// Device address of the partial-sum array on `device` (which must be
+// current).  Looked up once per device with cudaGetSymbolAddress: in host
+// code the array's name is only a host-side stand-in, not a device address.
+double* noalloc_scratch(int device)
+{
+    if (device < 0 || device >= NOALLOC_MAX_DEVICES) throw Error(IPCG_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[device]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess || p == nullptr)
+            throw Error(IPCG_ERR_CUDA, std::string("cudaGetSymbolAddress of the energy scratch failed: ")
+                    + cudaGetErrorString(e));
+        g_noalloc_ptr[device] = static_cast<double*>(p);
+    }
+    return g_noalloc_ptr[device];
+}
+} // namespace
+
+void barrier_energy_noalloc(const double* V, const int* E, const int* F, const ContactsNoAlloc& in, double dhat,
+    double kappa, double dmin, int physical, double* energy, cudaStream_t s)
+{
+    const int64_t n = in.nvv + in.nev + in.nee + in.nfv;
+    const int nblk = grid_for(n, BLOCK);
+    if (nblk > NOALLOC_MAX_BLOCKS) {
+        char msg[160];
+        snprintf(msg, sizeof(msg), "too many contacts for the allocation-free energy: %lld > %lld",
+            (long long)n, (long long)NOALLOC_MAX_BLOCKS * BLOCK);
+        throw Error(IPCG_ERR_INVALID, msg);
+    }
+    int dev = 0;
+    IPCG_CUDA(cudaGetDevice(&dev));
+    double* partial = noalloc_scratch(dev);
+    if (n == 0) {
+        IPCG_CUDA(cudaMemsetAsync(energy, 0, sizeof(double), s));
+        return;
+    }
+    ContactsView cv { in.nvv, in.nev, in.nee, in.nfv, (const int2*)in.vv, (const int2*)in.ev, (const int2*)in.ee,
+        (const int2*)in.fv, in.vv_w, in.ev_w, in.ee_w, in.fv_w, in.ee_eps, in.ee_dtype };
+    const double xhat = (2 * dmin + dhat) * dhat;
+    Params P { kappa, dmin * dmin, xhat, physical ? dhat / (xhat * xhat) : 1.0, IPCG_PSD_NONE };
+    // every block overwrites its partial and the final kernel overwrites the
+    // result, so nothing in the shared array needs clearing between calls
+    IPCG_LAUNCH("k_energy", s, k_energy<<<nblk, BLOCK, 0, s>>>(cv, E, F, V, P, partial));
+    IPCG_LAUNCH("k_sum_partials", s, k_sum_partials<<<1, 1024, 0, s>>>(partial, nblk, energy));
 }
 
 } // namespace ipcg

@@ -161,6 +161,17 @@ struct BarrierArgs {
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null);
 
+// Caller-owned device arrays of a collision set (layout of ipcg_collisions_get).
+struct ContactsNoAlloc {
+    int64_t nvv, nev, nee, nfv;
+    const int32_t *vv, *ev, *ee, *fv;
+    const double *vv_w, *ev_w, *ee_w, *fv_w, *ee_eps;
+    const int8_t* ee_dtype;
+};
+// barrier.cu: the energy with its reduction scratch in a static device array
+void barrier_energy_noalloc(const double* V, const int* E, const int* F, const ContactsNoAlloc& in, double dhat,
+    double kappa, double dmin, int physical, double* energy, cudaStream_t s);
+
 // ccd.cu
 double collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, double min_distance,
     double tolerance, int64_t max_iterations, double rescale, int64_t* n_candidates);
