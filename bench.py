@@ -67,6 +67,35 @@ def make_scene(name):
 BYTES_PER_CONTACT = {2: 504, 3: 1104, 4: 1944}
 
 
+# per contact, the PSD pass reads and writes its 3n x 3n local Hessian slab
+PSD_BYTES = {2: 2 * 8 * 36, 3: 2 * 8 * 81, 4: 2 * 8 * 144}
+
+
+def psd_bytes(counts):
+    nvv, nev, nee, nfv = (int(x) for x in counts[:4])
+    return nvv * PSD_BYTES[2] + nev * PSD_BYTES[3] + (nee + nfv) * PSD_BYTES[4]
+
+
+def fp64_peak_tflops(dev):
+    """Measured FP64 rate: cuBLAS DGEMM (4096^3) through torch, best of 3."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1000.0)
+    del a, b
+    return 2.0 * n ** 3 / best / 1e12
+
+
 def algorithmic_bytes(counts, ndof):
     nvv, nev, nee, nfv = (int(x) for x in counts[:4])
     b = nvv * BYTES_PER_CONTACT[2] + nev * BYTES_PER_CONTACT[3] + (nee + nfv) * BYTES_PER_CONTACT[4]
@@ -132,14 +161,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel, workload):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+def ncu_counts(kernel, workload):
+    """Per-launch DRAM bytes and FP64 flops of `kernel` on `workload` from the
+    committed ncu summary (profiles/ncu_counts.json), or {}."""
     try:
-        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+        with open(os.path.join(ROOT, "profiles", "ncu_counts.json")) as f:
             t = json.load(f)
-        return t.get(workload, {}).get(kernel)
+        return t.get(workload, {}).get(kernel, {})
     except Exception:
-        return None
+        return {}
 
 
 def cpu_baseline_run(sc, steps, budget_s=20.0):
@@ -165,6 +195,26 @@ def cpu_baseline_run(sc, steps, budget_s=20.0):
     med = statistics.median(times)
     return {"value": C / med, "unit": UNIT, "cores": nt, "kind": "port",
             "sample": f"full collision set ({C} contacts), {len(times)} passes, median"}, C, times
+
+
+def ccd_baseline_run(sc, budget_s=20.0):
+    """compute_collision_free_stepsize of the CPU restatement on all host
+    threads (median of up to 3 runs within the budget)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    nt = os.cpu_count() or 1
+    times = []
+    t_start = time.perf_counter()
+    step = None
+    for _ in range(3):
+        t0 = time.perf_counter()
+        step, _ = oracle.collision_free_stepsize(sc["V"], sc["V1"], sc["E"], sc["F"], nthreads=nt)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > budget_s:
+            break
+    med = statistics.median(times)
+    return {"steps_per_s": 1.0 / med, "ms": 1000 * med, "cores": nt, "kind": "port", "step_size": step,
+            "sample": f"full scene, {len(times)} runs, median"}
 
 
 def run_reference(args, rank):
@@ -258,18 +308,36 @@ def run_gb300(args, rank, world):
     top = max(own, key=lambda k: own[k]["ms"])
     top_ms = own[top]["ms"] / max(1, own[top]["launches"])
     peak, peak_kind = measured_peaks()
-    roof = None
-    if top == "k_hessian":
-        abytes = algorithmic_bytes(counts, ndof)
-        achieved = abytes / (top_ms / 1000.0) / 1e9
-        traffic = ncu_traffic(top, args.workload)
-        roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes": abytes,
-                "avg_launch_ms": top_ms, "peak_source": f"{peak_kind} hbm_gbs"}
+    if top == "k_psd":
+        abytes = psd_bytes(counts)
     else:
-        roof = {"kernel": top, "bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s", "frac": None,
-                "traffic": None, "avg_launch_ms": top_ms}
+        abytes = algorithmic_bytes(counts, ndof)
+    achieved = abytes / (top_ms / 1000.0) / 1e9
+    nc = ncu_counts(top, args.workload)
+    roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": nc.get("dram_bytes"), "algorithmic_bytes": abytes,
+            "avg_launch_ms": top_ms, "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)"}
+    fp64_peak = fp64_peak_tflops(dev)
+    if nc.get("fp64_flops"):
+        ach = nc["fp64_flops"] / (top_ms / 1000.0) / 1e12
+        roof["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
+                        "flops_per_launch": nc["fp64_flops"], "pipe_util_ncu": nc.get("fp64_pipe_pct"),
+                        "peak_source": "measured: cuBLAS DGEMM 4096^3 on this GPU"}
+    else:
+        roof["fp64"] = {"peak_tflops": fp64_peak, "peak_source": "measured: cuBLAS DGEMM 4096^3 on this GPU"}
     step_share = {k: round(v["ms"] / total_ms, 4) for k, v in sorted(own.items(), key=lambda kv: -kv[1]["ms"])}
+
+    # the same three quantities from the fused entry point (one pass, one copy-in)
+    fused = []
+    for i in range(3 + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e_, g_, Hd = B.energy_gradient_hessian_device(col, mesh, Vd, CLAMP)
+        Hd.free()
+        torch.cuda.synchronize()
+        if i >= 3:
+            fused.append(time.perf_counter() - t0)
+    fused_ms = 1000 * statistics.median(fused)
 
     # end to end through the public API with pinned host buffers
     Vh = torch.from_numpy(V).pin_memory().numpy()
@@ -302,8 +370,10 @@ def run_gb300(args, rank, world):
     if rank != 0:
         return
     cpu = None
+    ccd_cpu = None
     if not args.no_cpu_baseline:
         cpu, _, _ = cpu_baseline_run(sc, 3, budget_s=20.0)
+        ccd_cpu = ccd_baseline_run(sc)
     pct = lambda a, q: float(np.percentile(np.array(a), q))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -321,8 +391,9 @@ def run_gb300(args, rank, world):
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
         "gpu_launches": int(launches), "gpu_launches_per_step": launches / args.steps,
         "clocks": clk,
+        "fused_egh": {"value": C / (fused_ms / 1000.0), "unit": UNIT, "ms_per_step": fused_ms},
         "ccd": {"steps_per_s": 1000.0 / statistics.median(ccd_ms), "p50_ms": pct(ccd_ms, 50),
-                "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "candidates": col.num_candidates},
+                "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "cpu_baseline": ccd_cpu},
         "collision_build": {"p50_ms": pct(build_ms, 50), "p99_ms": pct(build_ms, 99)},
     }
     print(json.dumps(line), flush=True)

@@ -34,6 +34,8 @@ namespace {
 
 constexpr int CCD_STACK = 128;
 constexpr int BLOCK = 128;
+// boxes a query may examine in the first pass before it is deferred
+constexpr long long CCD_PASS1_BUDGET = 512;
 
 struct Query {
     V3 s[4], e[4];
@@ -145,8 +147,17 @@ __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], do
 // `shared_best` (may be null) is the earliest time of impact found so far by
 // any candidate; boxes starting at or after it cannot lower the final
 // minimum, so it is re-read every 64 boxes to prune.
-__device__ bool root_finder(const Query& q, const double err[3], double ms, const double tol[3], double delta,
-    double tmax, long long max_itr, double& toi, double& out_tol, const unsigned long long* shared_best)
+// Search status: no root before tmax, a root box found, or the caller's box
+// budget ran out before the search finished (result unknown).
+enum : int { CCD_MISS = 0, CCD_HIT = 1, CCD_UNRESOLVED = 2 };
+
+struct Budget {
+    long long limit; // <= 0: unlimited
+    long long spent;
+};
+
+__device__ int root_finder(const Query& q, const double err[3], double ms, const double tol[3], double delta,
+    double tmax, long long max_itr, double& toi, double& out_tol, const unsigned long long* shared_best, Budget& bud)
 {
     CBox st[CCD_STACK];
     int sp = 0;
@@ -167,6 +178,7 @@ __device__ bool root_finder(const Query& q, const double err[3], double ms, cons
         const CBox b = st[--sp];
         if (b.lo[0] >= best || b.lo[0] >= prune) continue;
         ++itr;
+        if (bud.limit > 0 && ++bud.spent > bud.limit) return CCD_UNRESOLVED;
         bool box_in, inside[3];
         double cw[3], var[3][3];
         if (!inclusion(q, b, err, ms, box_in, cw, var, inside)) continue;
@@ -211,23 +223,24 @@ __device__ bool root_finder(const Query& q, const double err[3], double ms, cons
         if (keep_lo) st[sp++] = lo;
     }
     if (found) toi = best;
-    return found;
+    return found ? CCD_HIT : CCD_MISS;
 }
 
-__device__ bool ti_ccd(const Query& q, double ms_in, double& toi, double tol_in, double tmax_in, long long max_itr,
-    double& out_tol, bool no_zero_toi, const unsigned long long* shared_best)
+__device__ int ti_ccd(const Query& q, double ms_in, double& toi, double tol_in, double tmax_in, long long max_itr,
+    double& out_tol, bool no_zero_toi, const unsigned long long* shared_best, Budget& bud)
 {
     double err[3];
     numerical_error(q, ms_in > 0, err);
     double tmax = tmax_in, delta = tol_in, ms = ms_in;
     double tol[3];
     domain_tol(q, delta, tol);
-    bool hit = false;
+    int hit = CCD_MISS;
     for (int it = 0; it < 256; ++it) {
         double t = 0;
-        hit = root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol, shared_best);
-        if (hit) toi = t;
-        if (!(no_zero_toi && hit && toi == 0)) return hit;
+        hit = root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol, shared_best, bud);
+        if (hit == CCD_UNRESOLVED) return hit;
+        if (hit == CCD_HIT) toi = t;
+        if (!(no_zero_toi && hit == CCD_HIT && toi == 0)) return hit;
         if (out_tol > delta) tmax *= 0.9;
         else if (10 * delta < ms) ms *= 0.5;
         else {
@@ -244,29 +257,29 @@ struct CCDParams {
     double rescale;
 };
 
-__device__ bool strategy(const Query& q, double min_distance, double d0, const CCDParams& P, double adj, double tmax,
-    double& toi, const unsigned long long* shared_best)
+__device__ int strategy(const Query& q, double min_distance, double d0, const CCDParams& P, double adj, double tmax,
+    double& toi, const unsigned long long* shared_best, Budget& bud)
 {
     if (d0 <= min_distance) {
         toi = 0;
-        return true;
+        return CCD_HIT;
     }
     double mind = (1.0 - P.rescale) * (d0 - min_distance);
     mind = fmin(mind, 1e-4);
     mind += min_distance;
     double out_tol;
-    bool hit = ti_ccd(q, mind, toi, adj, tmax, P.max_iterations, out_tol, false, shared_best);
-    if (hit && toi < 1e-6) {
-        hit = ti_ccd(q, min_distance, toi, adj, tmax, -1, out_tol, true, shared_best);
-        if (hit) toi *= P.rescale;
+    int hit = ti_ccd(q, mind, toi, adj, tmax, P.max_iterations, out_tol, false, shared_best, bud);
+    if (hit == CCD_HIT && toi < 1e-6) {
+        hit = ti_ccd(q, min_distance, toi, adj, tmax, -1, out_tol, true, shared_best, bud);
+        if (hit == CCD_HIT) toi *= P.rescale;
     }
     return hit;
 }
 
 __device__ __forceinline__ bool v3eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 
-__device__ bool stencil_ccd(Query& q, double min_distance, const CCDParams& P, double tmax, double& toi,
-    const unsigned long long* shared_best)
+__device__ int stencil_ccd(Query& q, double min_distance, const CCDParams& P, double tmax, double& toi,
+    const unsigned long long* shared_best, Budget& bud)
 {
     double d2;
     if (q.vf) d2 = point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
@@ -277,22 +290,18 @@ __device__ bool stencil_ccd(Query& q, double min_distance, const CCDParams& P, d
     if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) {
         if (d0 <= min_distance) {
             toi = 0;
-            return true;
+            return CCD_HIT;
         }
-        return false;
+        return CCD_MISS;
     }
     const double adj = fmin(0.5 * d0, P.tolerance);
-    return strategy(q, min_distance, d0, P, adj, tmax, toi, shared_best);
+    return strategy(q, min_distance, d0, P, adj, tmax, toi, shared_best, bud);
 }
 
-__global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee, int n_ee,
-    const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
-    const int* __restrict__ E, const int* __restrict__ F, double min_distance, CCDParams P,
-    unsigned long long* toi_bits)
+__device__ __forceinline__ void load_query(int i, const int2* __restrict__ cand_ee, int n_ee,
+    const int2* __restrict__ cand_fv, const double* __restrict__ V0, const double* __restrict__ V1,
+    const int* __restrict__ E, const int* __restrict__ F, Query& q)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_ee + n_fv) return;
-    Query q;
     int ids[4];
     if (i < n_ee) {
         const int2 c = cand_ee[i];
@@ -313,10 +322,32 @@ __global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee,
         q.s[k] = load_v3(V0, ids[k]);
         q.e[k] = load_v3(V1, ids[k]);
     }
+}
+
+// One thread per candidate (candidates.cpp:252-292).  With a box budget
+// (pass 1) a query that does not finish within it is appended to `hard`
+// instead; those are run to completion in pass 2 (hard != null selects the
+// candidate list), by which time the earliest time of the easy queries
+// prunes them.  Each query's result does not depend on the pass, so the
+// minimum is the same as a single full pass.
+__global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee, int n_ee,
+    const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
+    const int* __restrict__ E, const int* __restrict__ F, double min_distance, CCDParams P,
+    unsigned long long* toi_bits, long long budget, const int* __restrict__ list, const int* __restrict__ list_n,
+    int* __restrict__ hard, int* __restrict__ hard_n)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = list ? *list_n : n_ee + n_fv;
+    if (t >= n) return;
+    const int i = list ? list[t] : t;
+    Query q;
+    load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q);
     const double tmax = __longlong_as_double((long long)*(volatile unsigned long long*)toi_bits);
     double toi = __longlong_as_double(0x7ff0000000000000ULL);
-    if (stencil_ccd(q, min_distance, P, tmax, toi, toi_bits) && toi < tmax)
-        atomicMin(toi_bits, (unsigned long long)__double_as_longlong(toi));
+    Budget bud { budget, 0 };
+    const int st = stencil_ccd(q, min_distance, P, tmax, toi, toi_bits, bud);
+    if (st == CCD_HIT && toi < tmax) atomicMin(toi_bits, (unsigned long long)__double_as_longlong(toi));
+    else if (st == CCD_UNRESOLVED) hard[atomicAdd(hard_n, 1)] = i;
 }
 
 __global__ void k_ccd_stencils(int is_ee, int n, const double* __restrict__ x0, const double* __restrict__ x1,
@@ -331,8 +362,9 @@ __global__ void k_ccd_stencils(int is_ee, int n, const double* __restrict__ x0, 
         q.e[k] = load_v3(x1 + 12 * (int64_t)i, k);
     }
     double t = __longlong_as_double(0x7ff0000000000000ULL);
-    const bool h = stencil_ccd(q, min_distance, P, tmax, t, nullptr);
-    hit[i] = h ? 1 : 0;
+    Budget bud { 0, 0 };
+    const int h = stencil_ccd(q, min_distance, P, tmax, t, nullptr, bud);
+    hit[i] = h == CCD_HIT ? 1 : 0;
     toi[i] = t;
 }
 
@@ -376,9 +408,18 @@ double collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1,
     const unsigned long long one = 0x3ff0000000000000ULL; // 1.0
     IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, &one, sizeof(one), cudaMemcpyHostToDevice, s));
     const CCDParams P { tolerance, (long long)max_iterations, rescale };
-    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(n_ee + n_fv, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p + m->cand_cap, (int)n_fv, V0,
-        V1, m->E.p, m->F.p, min_distance, P, m->toi_bits.p));
-    IPCG_CHECK_LAUNCH();
+    const int nc = (int)(n_ee + n_fv);
+    m->ivals_a.reserve(nc + 1);
+    int* hard = m->ivals_a.p;
+    int* hard_n = m->counters.p + 3;
+    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
+    // pass 1: every query with a small box budget; pass 2: the unresolved ones
+    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p + m->cand_cap,
+        (int)n_fv, V0, V1, m->E.p, m->F.p, min_distance, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard,
+        hard_n));
+    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p +
+        m->cand_cap, (int)n_fv, V0, V1, m->E.p, m->F.p, min_distance, P, m->toi_bits.p, 0, hard, hard_n, nullptr,
+        nullptr));
     unsigned long long bits = 0;
     IPCG_CUDA(cudaMemcpyAsync(&bits, m->toi_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
     IPCG_CUDA(cudaStreamSynchronize(s));

@@ -430,6 +430,23 @@ class BarrierPotential:
                                             C.byref(h)))
         return DeviceCSR(h, 3 * mesh.num_vertices)
 
+    def energy_gradient_hessian_device(self, collisions, mesh, vertices,
+                                       project_hessian_to_psd=PSDProjectionMethod.NONE):
+        """Energy (float), gradient (device tensor when vertices is one) and
+        a DeviceCSR Hessian from one call; results stay on the device."""
+        V = _as_f64(vertices)
+        e = np.zeros(1)
+        if _is_torch_cuda(V):
+            import torch
+            g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
+        else:
+            g = np.zeros(3 * mesh.num_vertices)
+        h = C.c_void_p()
+        _check(_load().ipcg_barrier_energy_gradient_hessian(
+            collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, int(self.use_physical_barrier),
+            int(project_hessian_to_psd), _ptr(e), _ptr(g), C.byref(h)))
+        return float(e[0]), g, DeviceCSR(h, 3 * mesh.num_vertices)
+
     def energy_gradient_hessian(self, collisions, mesh, vertices, project_hessian_to_psd=PSDProjectionMethod.NONE):
         """Energy, gradient and Hessian from one call."""
         V = _as_f64(vertices)
