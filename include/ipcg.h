@@ -78,6 +78,24 @@ int ipcg_mesh_faces_to_edges(const ipcg_mesh* mesh, int32_t* out);
 /* The cudaStream_t (as void*) on which all work for this mesh runs. */
 int ipcg_mesh_stream(const ipcg_mesh* mesh, void** stream);
 
+/* Batched scenes: n_scenes independent CollisionMesh objects packed into
+ * one mesh (the reference runs one CollisionMesh per simulation; a batch
+ * evaluates many simulations in one set of launches).  Scene k owns the
+ * vertex range [vertex_offsets[k], vertex_offsets[k+1]); edges and faces use
+ * packed (global) vertex indices and may not join two scenes.  Contacts are
+ * only found within a scene.  Every per-scene result equals that of the
+ * scene's own ipcg_mesh_create mesh.  ipcg_mesh_create is the n_scenes = 1
+ * case.  The *_batch calls below take one dhat / dmin / stiffness /
+ * min_distance per scene (host arrays of n_scenes) and return per-scene
+ * energies and step sizes; the gradient and the Hessian are the packed
+ * (block-diagonal) ones. */
+int ipcg_mesh_create_batch(const double* rest_positions, int64_t num_vertices,
+                           const int32_t* edges, int64_t num_edges,
+                           const int32_t* faces, int64_t num_faces,
+                           int64_t n_scenes, const int64_t* vertex_offsets,
+                           ipcg_mesh** out);
+int ipcg_mesh_scenes(const ipcg_mesh* mesh, int64_t* n_scenes);
+
 /* ---------------------------------------------------------------------- */
 /* NormalCollisions                                                        */
 /* ---------------------------------------------------------------------- */
@@ -92,6 +110,12 @@ int ipcg_collisions_destroy(ipcg_collisions* collisions);
  * The result stays on the device; entries are sorted by index key. */
 int ipcg_collisions_build(ipcg_collisions* collisions, const ipcg_mesh* mesh,
                           const double* vertices, double dhat, double dmin);
+
+/* NormalCollisions::build on every scene of a batch: dhat[n_scenes],
+ * dmin[n_scenes].  The result is the concatenation of the scenes' sets
+ * (each list stays sorted by packed index key). */
+int ipcg_collisions_build_batch(ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                                const double* vertices, const double* dhat, const double* dmin);
 
 /* Number of vv, ev, ee, fv collisions (NormalCollisions::{vv,ev,ee,fv}_collisions.size())
  * and of broad-phase candidates of the last build (ee, fv): counts[6]. */
@@ -153,6 +177,13 @@ int ipcg_barrier_energy_gradient_hessian(const ipcg_collisions* collisions, cons
                                          int use_physical_barrier, int psd_method,
                                          double* energy, double* gradient, ipcg_csr** hessian);
 
+/* Energy, gradient and Hessian on a batch (any output may be NULL):
+ * dhat[n_scenes], stiffness[n_scenes], energies[n_scenes] (host). */
+int ipcg_barrier_batch(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                       const double* vertices, const double* dhat, const double* stiffness,
+                       int use_physical_barrier, int psd_method,
+                       double* energies, double* gradient, ipcg_csr** hessian);
+
 /* Allocation-free barrier energy.  No counterpart in the reference: it exists
  * for callers that cannot let the library allocate device memory during a
  * call, such as codes that give all device memory to their own pool under a
@@ -203,6 +234,14 @@ int ipcg_collision_free_stepsize(const ipcg_mesh* mesh,
                                  double min_distance, double tolerance,
                                  int64_t max_iterations, double conservative_rescaling,
                                  double* step, int64_t* n_candidates);
+
+/* compute_collision_free_stepsize on every scene of a batch:
+ * min_distance[n_scenes] in, steps[n_scenes] out (host arrays). */
+int ipcg_collision_free_stepsize_batch(const ipcg_mesh* mesh,
+                                       const double* vertices_t0, const double* vertices_t1,
+                                       const double* min_distance, double tolerance,
+                                       int64_t max_iterations, double conservative_rescaling,
+                                       double* steps, int64_t* n_candidates);
 
 /* ---------------------------------------------------------------------- */
 /* Single-stencil primitives (for known-answer tests and plugin use)       */

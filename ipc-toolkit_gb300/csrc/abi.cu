@@ -214,11 +214,16 @@ int ipcg_mesh_stream(const ipcg_mesh* m, void** stream)
     });
 }
 
-int ipcg_mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE, const int32_t* faces,
-    int64_t nF, ipcg_mesh** out)
+} // extern "C"
+
+namespace {
+// One scene is the n_scenes == 1 case of a batch (vertex_offsets {0, nV}).
+int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE, const int32_t* faces, int64_t nF,
+    int64_t n_scenes, const int64_t* vertex_offsets, ipcg_mesh** out)
 {
     return guarded([&] {
         require(out != nullptr, "out is NULL");
+        require(n_scenes >= 1 && n_scenes < (1 << 30), "n_scenes must be in [1, 2^30)");
         require(nV >= 0 && nE >= 0 && nF >= 0, "negative size");
         require(nV < INT32_MAX && nE < INT32_MAX && nF < INT32_MAX, "mesh too large for int32 indices");
         require(nV == 0 || rest, "rest_positions is NULL");
@@ -230,6 +235,27 @@ int ipcg_mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64
         std::vector<int32_t> hE = to_host(edges, 2 * nE), hF = to_host(faces, 3 * nF);
         for (int32_t v : hE) require(v >= 0 && v < nV, "edge vertex index out of range");
         for (int32_t v : hF) require(v >= 0 && v < nV, "face vertex index out of range");
+        // scenes: consecutive vertex ranges; no edge or face spans two scenes
+        std::vector<int64_t> voff(n_scenes + 1);
+        std::vector<int32_t> vscene;
+        if (vertex_offsets) {
+            for (int64_t k = 0; k <= n_scenes; ++k) voff[k] = vertex_offsets[k];
+            require(voff[0] == 0 && voff[n_scenes] == nV, "vertex_offsets must start at 0 and end at num_vertices");
+            for (int64_t k = 0; k < n_scenes; ++k) require(voff[k] <= voff[k + 1], "vertex_offsets must not decrease");
+        } else {
+            require(n_scenes == 1, "vertex_offsets is NULL");
+            voff[1] = nV;
+        }
+        if (n_scenes > 1) {
+            vscene.resize(nV);
+            for (int64_t k = 0; k < n_scenes; ++k)
+                for (int64_t v = voff[k]; v < voff[k + 1]; ++v) vscene[v] = (int32_t)k;
+            for (int64_t e = 0; e < nE; ++e)
+                require(vscene[hE[2 * e]] == vscene[hE[2 * e + 1]], "an edge joins two scenes");
+            for (int64_t f = 0; f < nF; ++f)
+                require(vscene[hF[3 * f]] == vscene[hF[3 * f + 1]] && vscene[hF[3 * f]] == vscene[hF[3 * f + 2]],
+                    "a face joins two scenes");
+        }
         // faces_to_edges (collision_mesh.cpp:510-543)
         std::unordered_map<uint64_t, int32_t> emap;
         emap.reserve(2 * nE + 1);
@@ -257,6 +283,9 @@ int ipcg_mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64
             upload(m->F, (const int*)hF.data(), 3 * nF, m->stream);
             upload(m->F2E, (const int*)f2e.data(), 3 * nF, m->stream);
             m->h_F2E = std::move(f2e);
+            m->n_scenes = n_scenes;
+            m->h_voff = std::move(voff);
+            if (n_scenes > 1) upload(m->vscene, (const int*)vscene.data(), nV, m->stream);
             m->counters.reserve(16);
             m->h_counters.reserve(16);
             IPCG_CUDA(cudaStreamSynchronize(m->stream));
@@ -265,6 +294,33 @@ int ipcg_mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64
             throw;
         }
         *out = m;
+    });
+}
+} // namespace
+
+extern "C" {
+
+int ipcg_mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE, const int32_t* faces,
+    int64_t nF, ipcg_mesh** out)
+{
+    return mesh_create(rest, nV, edges, nE, faces, nF, 1, nullptr, out);
+}
+
+int ipcg_mesh_create_batch(const double* rest, int64_t nV, const int32_t* edges, int64_t nE, const int32_t* faces,
+    int64_t nF, int64_t n_scenes, const int64_t* vertex_offsets, ipcg_mesh** out)
+{
+    if (!vertex_offsets) {
+        g_last_error = "vertex_offsets is NULL";
+        return IPCG_ERR_INVALID;
+    }
+    return mesh_create(rest, nV, edges, nE, faces, nF, n_scenes, vertex_offsets, out);
+}
+
+int ipcg_mesh_scenes(const ipcg_mesh* m, int64_t* n_scenes)
+{
+    return guarded([&] {
+        require(m && n_scenes, "NULL argument");
+        *n_scenes = m->n_scenes;
     });
 }
 
@@ -306,10 +362,22 @@ int ipcg_collisions_destroy(ipcg_collisions* c)
 
 int ipcg_collisions_build(ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat, double dmin)
 {
+    if (mesh && mesh->n_scenes != 1) {
+        g_last_error = "mesh is a batch: use ipcg_collisions_build_batch";
+        return IPCG_ERR_INVALID;
+    }
+    return ipcg_collisions_build_batch(c, mesh, V, &dhat, &dmin);
+}
+
+int ipcg_collisions_build_batch(ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, const double* dhat,
+    const double* dmin)
+{
     return guarded([&] {
-        require(c && mesh && (V || mesh->nV == 0), "NULL argument");
-        require(dhat > 0, "dhat must be positive");
-        require(dmin >= 0, "dmin must be non-negative");
+        require(c && mesh && dhat && dmin && (V || mesh->nV == 0), "NULL argument");
+        for (int64_t k = 0; k < mesh->n_scenes; ++k) {
+            require(dhat[k] > 0, "dhat must be positive");
+            require(dmin[k] >= 0, "dmin must be non-negative");
+        }
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dV = stage_positions(m, V, m->V0);
@@ -382,17 +450,24 @@ int ipcg_collisions_set(ipcg_collisions* c, double dmin, int64_t nvv, const int3
     });
 }
 
-static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
-    double stiffness, int physical, int psd, double* energy, double* gradient, ipcg_csr** hessian)
+// dhat / stiffness: one value (scene_params == 0) or one per scene (host arrays).
+static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, const double* dhat,
+    const double* stiffness, int scene_params, int physical, int psd, double* energy, double* gradient,
+    ipcg_csr** hessian)
 {
     return guarded([&] {
-        require(c && mesh && (V || mesh->nV == 0), "NULL argument");
-        require(dhat > 0, "dhat must be positive");
+        require(c && mesh && dhat && stiffness && (V || mesh->nV == 0), "NULL argument");
+        require(scene_params || mesh->n_scenes == 1, "mesh is a batch: use ipcg_barrier_batch");
+        for (int64_t k = 0; k < (scene_params ? mesh->n_scenes : 1); ++k) require(dhat[k] > 0, "dhat must be positive");
         require(psd >= IPCG_PSD_NONE && psd <= IPCG_PSD_ABS, "Invalid type of PSD projection!");
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dV = stage_positions(m, V, m->V0);
-        BarrierArgs a { dhat, stiffness, c->dmin, physical ? 1 : 0, psd };
+        BarrierArgs a { dhat[0], stiffness[0], c->dmin, physical ? 1 : 0, psd };
+        if (scene_params) {
+            a.scene_dhat = dhat;
+            a.scene_kappa = stiffness;
+        }
         double* gdev = nullptr;
         DBuf<double> gtmp;
         if (gradient) {
@@ -426,7 +501,7 @@ int ipcg_barrier_energy(const ipcg_collisions* c, const ipcg_mesh* mesh, const d
         g_last_error = "energy is NULL";
         return IPCG_ERR_INVALID;
     }
-    return barrier_call(c, mesh, V, dhat, stiffness, physical, IPCG_PSD_NONE, energy, nullptr, nullptr);
+    return barrier_call(c, mesh, V, &dhat, &stiffness, 0, physical, IPCG_PSD_NONE, energy, nullptr, nullptr);
 }
 
 int ipcg_barrier_gradient(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
@@ -436,7 +511,7 @@ int ipcg_barrier_gradient(const ipcg_collisions* c, const ipcg_mesh* mesh, const
         g_last_error = "gradient is NULL";
         return IPCG_ERR_INVALID;
     }
-    return barrier_call(c, mesh, V, dhat, stiffness, physical, IPCG_PSD_NONE, nullptr, gradient, nullptr);
+    return barrier_call(c, mesh, V, &dhat, &stiffness, 0, physical, IPCG_PSD_NONE, nullptr, gradient, nullptr);
 }
 
 int ipcg_barrier_hessian(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
@@ -446,13 +521,19 @@ int ipcg_barrier_hessian(const ipcg_collisions* c, const ipcg_mesh* mesh, const 
         g_last_error = "out is NULL";
         return IPCG_ERR_INVALID;
     }
-    return barrier_call(c, mesh, V, dhat, stiffness, physical, psd, nullptr, nullptr, out);
+    return barrier_call(c, mesh, V, &dhat, &stiffness, 0, physical, psd, nullptr, nullptr, out);
 }
 
 int ipcg_barrier_energy_gradient_hessian(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V,
     double dhat, double stiffness, int physical, int psd, double* energy, double* gradient, ipcg_csr** hessian)
 {
-    return barrier_call(c, mesh, V, dhat, stiffness, physical, psd, energy, gradient, hessian);
+    return barrier_call(c, mesh, V, &dhat, &stiffness, 0, physical, psd, energy, gradient, hessian);
+}
+
+int ipcg_barrier_batch(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, const double* dhat,
+    const double* stiffness, int physical, int psd, double* energies, double* gradient, ipcg_csr** hessian)
+{
+    return barrier_call(c, mesh, V, dhat, stiffness, 1, physical, psd, energies, gradient, hessian);
 }
 
 int ipcg_csr_shape(const ipcg_csr* h, int64_t* rows, int64_t* nnz)
@@ -484,16 +565,29 @@ int ipcg_csr_destroy(ipcg_csr* h)
 int ipcg_collision_free_stepsize(const ipcg_mesh* mesh, const double* V0, const double* V1, double min_distance,
     double tolerance, int64_t max_iterations, double rescale, double* step, int64_t* n_candidates)
 {
+    if (mesh && mesh->n_scenes != 1) {
+        g_last_error = "mesh is a batch: use ipcg_collision_free_stepsize_batch";
+        return IPCG_ERR_INVALID;
+    }
+    return ipcg_collision_free_stepsize_batch(mesh, V0, V1, &min_distance, tolerance, max_iterations, rescale, step,
+        n_candidates);
+}
+
+int ipcg_collision_free_stepsize_batch(const ipcg_mesh* mesh, const double* V0, const double* V1,
+    const double* min_distance, double tolerance, int64_t max_iterations, double rescale, double* steps,
+    int64_t* n_candidates)
+{
     return guarded([&] {
-        require(mesh && step && ((V0 && V1) || mesh->nV == 0), "NULL argument");
-        require(min_distance >= 0, "min_distance must be non-negative");
+        require(mesh && steps && min_distance && ((V0 && V1) || mesh->nV == 0), "NULL argument");
+        for (int64_t k = 0; k < mesh->n_scenes; ++k)
+            require(min_distance[k] >= 0, "min_distance must be non-negative");
         require(tolerance > 0, "tolerance must be positive");
         require(rescale > 0 && rescale <= 1, "conservative_rescaling must be in (0, 1]");
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* d0 = stage_positions(m, V0, m->V0);
         const double* d1 = stage_positions(m, V1, m->V1);
-        *step = collision_free_stepsize(m, d0, d1, min_distance, tolerance, max_iterations, rescale, n_candidates);
+        collision_free_stepsize(m, d0, d1, min_distance, tolerance, max_iterations, rescale, steps, n_candidates);
     });
 }
 

@@ -559,6 +559,7 @@ __device__ __forceinline__ void gather(const double* __restrict__ V, const Local
 __global__ void __launch_bounds__(BLOCK) k_energy(ContactsView cv, const int* __restrict__ E,
     const int* __restrict__ F, const double* __restrict__ V, Params P, double* __restrict__ partial)
 {
+    // one scene: deterministic per-block partial sums
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0;
@@ -590,14 +591,61 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int n, double
     if (threadIdx.x == 0) *out = t;
 }
 
+// Batches: per-scene energies.  Contact lists are sorted by index key and
+// the scenes occupy consecutive index ranges, so a block almost always holds
+// one scene: it then adds one block sum, otherwise each contact adds its own.
+__global__ void __launch_bounds__(BLOCK) k_energy_scenes(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, const Params* __restrict__ sp, SceneView sv,
+    double* __restrict__ energy)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    int scene = -1;
+    if (i < n) {
+        Local c;
+        load_contact(cv, E, F, i, c);
+        scene = sv.of(c.vid[0]);
+        const Params P = sp[scene];
+        V3 x[4];
+        gather(V, c, x);
+        double g[12];
+        const double d = contact_distance(c, x, g, nullptr);
+        bool act;
+        const double m = mollifier(c, x, nullptr, nullptr, act);
+        e = c.w * m * fval(P, d);
+    }
+    __shared__ int s_lo, s_hi;
+    if (threadIdx.x == 0) {
+        s_lo = 0x7fffffff;
+        s_hi = -1;
+    }
+    __syncthreads();
+    if (scene >= 0) {
+        atomicMin(&s_lo, scene);
+        atomicMax(&s_hi, scene);
+    }
+    __syncthreads();
+    if (s_lo == s_hi) {
+        typedef cub::BlockReduce<double, BLOCK> BR;
+        __shared__ typename BR::TempStorage tmp;
+        const double sum = BR(tmp).Sum(e);
+        if (threadIdx.x == 0 && s_hi >= 0) atomicAdd(energy + s_hi, sum);
+    } else if (scene >= 0 && e != 0) {
+        atomicAdd(energy + scene, e);
+    }
+}
+
 __global__ void __launch_bounds__(BLOCK) k_gradient(ContactsView cv, const int* __restrict__ E,
-    const int* __restrict__ F, const double* __restrict__ V, Params P, double* __restrict__ grad)
+    const int* __restrict__ F, const double* __restrict__ V, const Params* __restrict__ sp, SceneView sv,
+    double* __restrict__ grad)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Local c;
     load_contact(cv, E, F, i, c);
+    const Params P = sp[sv.of(c.vid[0])];
     V3 x[4];
     gather(V, c, x);
     const int N = 3 * c.n;
@@ -657,14 +705,15 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restr
 // reference returns without projection.
 template <int TYPE>
 __global__ void __launch_bounds__(BLOCK) k_local_hessian(ContactsView cv, const int* __restrict__ E,
-    const int* __restrict__ F, const double* __restrict__ V, Params P, double* __restrict__ Hs,
-    uint8_t* __restrict__ proj, int64_t first, int64_t count)
+    const int* __restrict__ F, const double* __restrict__ V, const Params* __restrict__ sp, SceneView sv,
+    double* __restrict__ Hs, uint8_t* __restrict__ proj, int64_t first, int64_t count)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
     const int64_t i = first + t;
     Local c;
     load_contact(cv, E, F, i, c);
+    const Params P = sp[sv.of(c.vid[0])];
     V3 x[4];
     gather(V, c, x);
     constexpr int NS = TYPE == CT_VV ? 2 : (TYPE == CT_EV ? 3 : 4);
@@ -858,11 +907,32 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
         cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
     const int64_t n = cs->size();
-    const double xhat = (2 * cs->dmin + a.dhat) * a.dhat;
-    Params P { a.kappa, cs->dmin * cs->dmin, xhat, a.physical ? a.dhat / (xhat * xhat) : 1.0, a.psd };
+    // per-scene barrier parameters (barrier_potential.cpp:62-99)
+    const int ns = (int)m->n_scenes;
+    std::vector<Params> hp(ns);
+    for (int k = 0; k < ns; ++k) {
+        const double dh = a.scene_dhat ? a.scene_dhat[k] : a.dhat;
+        const double kap = a.scene_kappa ? a.scene_kappa[k] : a.kappa;
+        const double dm = (k < (int)cs->scene_dmin.size()) ? cs->scene_dmin[k] : cs->dmin;
+        const double xh = (2 * dm + dh) * dh;
+        hp[k] = Params { kap, dm * dm, xh, a.physical ? dh / (xh * xh) : 1.0, a.psd };
+    }
+    m->params_buf.reserve(sizeof(Params) * ns);
+    const Params* sp = reinterpret_cast<const Params*>(m->params_buf.p);
+    IPCG_CUDA(cudaMemcpyAsync(m->params_buf.p, hp.data(), sizeof(Params) * ns, cudaMemcpyHostToDevice, s));
+    const Params P = hp[0];
+    const SceneView sv = scene_view(m);
     const int nblk = grid_for(n, BLOCK);
     const int64_t nV = m->nV;
-    if (energy_host) {
+    if (energy_host && ns > 1) {
+        // per-scene energies (batches)
+        m->partial.reserve(ns + 2);
+        IPCG_CUDA(cudaMemsetAsync(m->partial.p, 0, sizeof(double) * ns, s));
+        if (n > 0)
+            IPCG_LAUNCH("k_energy_scenes", s, k_energy_scenes<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, sp, sv,
+                m->partial.p));
+        IPCG_CUDA(cudaMemcpyAsync(energy_host, m->partial.p, sizeof(double) * ns, cudaMemcpyDefault, s));
+    } else if (energy_host) {
         m->partial.reserve(nblk + 2);
         if (n > 0) {
             IPCG_LAUNCH("k_energy", s, k_energy<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, m->partial.p));
@@ -876,7 +946,7 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     if (grad_dev) {
         IPCG_CUDA(cudaMemsetAsync(grad_dev, 0, sizeof(double) * 3 * nV, s));
         if (n > 0) {
-            IPCG_LAUNCH("k_gradient", s, k_gradient<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, grad_dev));
+            IPCG_LAUNCH("k_gradient", s, k_gradient<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, sp, sv, grad_dev));
             IPCG_CHECK_LAUNCH();
         }
     }
@@ -909,16 +979,16 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
             const int64_t count[4] = { cs->nvv, cs->nev, cs->nee, cs->nfv };
             if (count[0])
                 IPCG_LAUNCH("k_local_hessian_vv", s, k_local_hessian<CT_VV><<<grid_for(count[0], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[0], count[0]));
+                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[0], count[0]));
             if (count[1])
                 IPCG_LAUNCH("k_local_hessian_ev", s, k_local_hessian<CT_EV><<<grid_for(count[1], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[1], count[1]));
+                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[1], count[1]));
             if (count[2])
                 IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[2], count[2]));
+                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[2], count[2]));
             if (count[3])
                 IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, P, m->hs.p, m->proj.p, first[3], count[3]));
+                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[3], count[3]));
             if (a.psd != IPCG_PSD_NONE)
                 IPCG_LAUNCH("k_psd", s, k_psd<<<nblk, BLOCK, 0, s>>>(cv, m->hs.p, m->proj.p, a.psd, d_fail));
             // sparsity pattern: sort (block key, contribution) and run-length encode

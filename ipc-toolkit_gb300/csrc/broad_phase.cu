@@ -26,9 +26,10 @@ namespace {
 constexpr int BLOCK = 256;
 constexpr int STACK = 64;
 
-__device__ __forceinline__ void vertex_box(const double* V0, const double* V1, int v, double r, double mn[3],
-    double mx[3])
+__device__ __forceinline__ void vertex_box(const double* V0, const double* V1, int v, const double* scene_r,
+    SceneView sv, double mn[3], double mx[3])
 {
+    const double r = __ldg(scene_r + sv.of(v));
     for (int d = 0; d < 3; ++d) {
         double a = V0[3 * v + d], b = a;
         if (V1) {
@@ -98,15 +99,16 @@ __device__ __forceinline__ unsigned spread10(unsigned x)
 
 template <int K>
 __global__ void k_prim_boxes(const int* __restrict__ ids, int n, const double* __restrict__ V0,
-    const double* __restrict__ V1, double r, const double* __restrict__ bounds, float4* __restrict__ plo,
-    float4* __restrict__ phi, unsigned* __restrict__ codes, int* __restrict__ order)
+    const double* __restrict__ V1, const double* __restrict__ scene_r, SceneView sv,
+    const double* __restrict__ bounds, float4* __restrict__ plo, float4* __restrict__ phi,
+    unsigned long long* __restrict__ codes, int* __restrict__ order)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double mn[3] = { DBL_MAX, DBL_MAX, DBL_MAX }, mx[3] = { -DBL_MAX, -DBL_MAX, -DBL_MAX };
     for (int k = 0; k < K; ++k) {
         double a[3], b[3];
-        vertex_box(V0, V1, ids[K * i + k], r, a, b);
+        vertex_box(V0, V1, ids[K * i + k], scene_r, sv, a, b);
         for (int d = 0; d < 3; ++d) {
             mn[d] = fmin(mn[d], a[d]);
             mx[d] = fmax(mx[d], b[d]);
@@ -121,21 +123,22 @@ __global__ void k_prim_boxes(const int* __restrict__ ids, int n, const double* _
         c = fmin(fmax(c * 1024.0, 0.0), 1023.0);
         q[d] = (unsigned)c;
     }
-    codes[i] = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+    const unsigned morton = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
+    codes[i] = ((unsigned long long)sv.of(ids[K * i]) << 32) | morton;
     order[i] = i;
 }
 
-__device__ __forceinline__ int delta(const unsigned* __restrict__ c, int n, int i, int j)
+__device__ __forceinline__ int delta(const unsigned long long* __restrict__ c, int n, int i, int j)
 {
     if (j < 0 || j >= n) return -1;
-    const unsigned a = c[i], b = c[j];
-    if (a == b) return 32 + __clz(i ^ j);
-    return __clz(a ^ b);
+    const unsigned long long a = c[i], b = c[j];
+    if (a == b) return 64 + __clz(i ^ j);
+    return __clzll(a ^ b);
 }
 
 // Karras (2012) radix-tree construction, one thread per internal node.
-__global__ void k_karras(const unsigned* __restrict__ c, int n, float4* __restrict__ lo, float4* __restrict__ hi,
-    int* __restrict__ last, int* __restrict__ parent)
+__global__ void k_karras(const unsigned long long* __restrict__ c, int n, float4* __restrict__ lo,
+    float4* __restrict__ hi, int* __restrict__ first, int* __restrict__ last, int* __restrict__ parent)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
@@ -159,19 +162,23 @@ __global__ void k_karras(const unsigned* __restrict__ c, int n, float4* __restri
     const int right = (hi_i == gamma + 1) ? (n - 1 + gamma + 1) : gamma + 1;
     lo[i].w = __int_as_float(left);
     hi[i].w = __int_as_float(right);
+    first[i] = lo_i;
     last[i] = hi_i;
     parent[left] = i;
     parent[right] = i;
     if (i == 0) parent[0] = -1;
 }
 
-__global__ void k_leaves(const int* __restrict__ ids_sorted, int n, const float4* __restrict__ plo,
-    const float4* __restrict__ phi, float4* __restrict__ lo, float4* __restrict__ hi, int* __restrict__ last,
-    int* __restrict__ parent)
+__global__ void k_leaves(const int* __restrict__ ids_sorted, const unsigned long long* __restrict__ codes_sorted,
+    int n, const float4* __restrict__ plo, const float4* __restrict__ phi, float4* __restrict__ lo,
+    float4* __restrict__ hi, int* __restrict__ first, int* __restrict__ last, int* __restrict__ parent,
+    int* __restrict__ leaf_scene)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int p = ids_sorted[i];
+    leaf_scene[i] = (int)(codes_sorted[i] >> 32);
+    first[n - 1 + i] = i;
     float4 a = plo[p], b = phi[p];
     a.w = __int_as_float(p);
     b.w = __int_as_float(-1);
@@ -215,21 +222,31 @@ __device__ __forceinline__ void emit(int2* __restrict__ out, int* __restrict__ c
 }
 
 // EE: triangular self traversal, one thread per sorted edge leaf.
+// Scene range check of node v for a query in scene qs (batches only).
+__device__ __forceinline__ bool other_scenes(const int* __restrict__ first, const int* __restrict__ last,
+    const int* __restrict__ leaf_scene, bool batched, int v, int qs)
+{
+    return batched && (qs < __ldg(leaf_scene + __ldg(first + v)) || qs > __ldg(leaf_scene + __ldg(last + v)));
+}
+
 __global__ void k_traverse_ee(const float4* __restrict__ lo, const float4* __restrict__ hi,
-    const int* __restrict__ last, int n, const int* __restrict__ E, int2* __restrict__ out, int* __restrict__ count,
-    int cap, int* __restrict__ guard)
+    const int* __restrict__ first, const int* __restrict__ last, const int* __restrict__ leaf_scene, bool batched,
+    int n, const int* __restrict__ E, int2* __restrict__ out, int* __restrict__ count, int cap,
+    int* __restrict__ guard)
 {
     const int qi = blockIdx.x * blockDim.x + threadIdx.x;
     if (qi >= n || n < 2) return;
     const float4 qlo = lo[n - 1 + qi], qhi = hi[n - 1 + qi];
     const int ea = __float_as_int(qlo.w);
     const int a0 = E[2 * ea], a1 = E[2 * ea + 1];
+    const int qs = leaf_scene[qi];
     int stack[STACK];
     int sp = 0;
     stack[sp++] = 0;
     while (sp > 0) {
         const int v = stack[--sp];
         if (last[v] <= qi) continue;
+        if (other_scenes(first, last, leaf_scene, batched, v, qs)) continue;
         const float4 vlo = lo[v], vhi = hi[v];
         if (!overlap(qlo, qhi, vlo, vhi)) continue;
         if (v >= n - 1) {
@@ -248,14 +265,18 @@ __global__ void k_traverse_ee(const float4* __restrict__ lo, const float4* __res
 }
 
 // FV: each vertex box queries the face tree.
-__global__ void k_traverse_fv(const float4* __restrict__ lo, const float4* __restrict__ hi, int n,
-    const double* __restrict__ V0, const double* __restrict__ V1, double r, int nV, const int* __restrict__ F,
-    int2* __restrict__ out, int* __restrict__ count, int cap, int* __restrict__ guard)
+__global__ void k_traverse_fv(const float4* __restrict__ lo, const float4* __restrict__ hi,
+    const int* __restrict__ first, const int* __restrict__ last, const int* __restrict__ leaf_scene, int n,
+    const double* __restrict__ V0, const double* __restrict__ V1, const double* __restrict__ scene_r, SceneView sv,
+    int nV, const int* __restrict__ F, int2* __restrict__ out, int* __restrict__ count, int cap,
+    int* __restrict__ guard)
 {
     const int vi = blockIdx.x * blockDim.x + threadIdx.x;
     if (vi >= nV || n < 1) return;
     double mn[3], mx[3];
-    vertex_box(V0, V1, vi, r, mn, mx);
+    vertex_box(V0, V1, vi, scene_r, sv, mn, mx);
+    const int qs = sv.of(vi);
+    const bool batched = sv.vscene != nullptr;
     const float4 qlo = make_float4(__double2float_rd(mn[0]), __double2float_rd(mn[1]), __double2float_rd(mn[2]), 0.f);
     const float4 qhi = make_float4(__double2float_ru(mx[0]), __double2float_ru(mx[1]), __double2float_ru(mx[2]), 0.f);
     int stack[STACK];
@@ -263,6 +284,7 @@ __global__ void k_traverse_fv(const float4* __restrict__ lo, const float4* __res
     stack[sp++] = 0;
     while (sp > 0) {
         const int v = stack[--sp];
+        if (other_scenes(first, last, leaf_scene, batched, v, qs)) continue;
         const float4 vlo = lo[v], vhi = hi[v];
         if (!overlap(qlo, qhi, vlo, vhi)) continue;
         if (v >= n - 1) {
@@ -281,7 +303,7 @@ __global__ void k_traverse_fv(const float4* __restrict__ lo, const float4* __res
 
 } // namespace
 
-void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const double* V1, double inflation)
+void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const double* V1, const double* scene_r)
 {
     const int n = (int)(kind == 2 ? m->nE : m->nF);
     bvh.n = n;
@@ -289,9 +311,11 @@ void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const doubl
     const int nn = 2 * n - 1;
     bvh.lo.reserve(nn);
     bvh.hi.reserve(nn);
+    bvh.first.reserve(nn);
     bvh.last.reserve(nn);
     bvh.parent.reserve(nn);
     bvh.flags.reserve(n);
+    bvh.leaf_scene.reserve(n);
     bvh.codes.reserve(n);
     bvh.codes_sorted.reserve(n);
     bvh.ids.reserve(n);
@@ -299,30 +323,28 @@ void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const doubl
     bvh.plo.reserve(n);
     bvh.phi.reserve(n);
     cudaStream_t s = m->stream;
+    const SceneView sv = scene_view(m);
     if (kind == 2)
-        IPCG_LAUNCH("k_prim_boxes", s, k_prim_boxes<2><<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->E.p, n, V0, V1, inflation, m->bounds.p, bvh.plo.p,
-            bvh.phi.p, bvh.codes.p, bvh.ids.p));
+        IPCG_LAUNCH("k_prim_boxes", s, k_prim_boxes<2><<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->E.p, n, V0, V1,
+            scene_r, sv, m->bounds.p, bvh.plo.p, bvh.phi.p, bvh.codes.p, bvh.ids.p));
     else
-        IPCG_LAUNCH("k_prim_boxes", s, k_prim_boxes<3><<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->F.p, n, V0, V1, inflation, m->bounds.p, bvh.plo.p,
-            bvh.phi.p, bvh.codes.p, bvh.ids.p));
-    IPCG_CHECK_LAUNCH();
-    sort_pairs_u32(m, bvh.codes.p, bvh.codes_sorted.p, bvh.ids.p, bvh.ids_sorted.p, n, 30);
-    if (n > 1) {
-        IPCG_LAUNCH("k_karras", s, k_karras<<<grid_for(n - 1, BLOCK), BLOCK, 0, s>>>(bvh.codes_sorted.p, n, bvh.lo.p, bvh.hi.p, bvh.last.p,
-            bvh.parent.p));
-        IPCG_CHECK_LAUNCH();
-    }
-    IPCG_LAUNCH("k_leaves", s, k_leaves<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(bvh.ids_sorted.p, n, bvh.plo.p, bvh.phi.p, bvh.lo.p, bvh.hi.p,
-        bvh.last.p, bvh.parent.p));
-    IPCG_CHECK_LAUNCH();
+        IPCG_LAUNCH("k_prim_boxes", s, k_prim_boxes<3><<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->F.p, n, V0, V1,
+            scene_r, sv, m->bounds.p, bvh.plo.p, bvh.phi.p, bvh.codes.p, bvh.ids.p));
+    sort_pairs_u64(m, bvh.codes.p, bvh.codes_sorted.p, bvh.ids.p, bvh.ids_sorted.p, n,
+        32 + bits_for(m->n_scenes + 1));
+    if (n > 1)
+        IPCG_LAUNCH("k_karras", s, k_karras<<<grid_for(n - 1, BLOCK), BLOCK, 0, s>>>(bvh.codes_sorted.p, n, bvh.lo.p,
+            bvh.hi.p, bvh.first.p, bvh.last.p, bvh.parent.p));
+    IPCG_LAUNCH("k_leaves", s, k_leaves<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(bvh.ids_sorted.p, bvh.codes_sorted.p, n,
+        bvh.plo.p, bvh.phi.p, bvh.lo.p, bvh.hi.p, bvh.first.p, bvh.last.p, bvh.parent.p, bvh.leaf_scene.p));
     if (n > 1) {
         IPCG_CUDA(cudaMemsetAsync(bvh.flags.p, 0, sizeof(int) * (n - 1), s));
-        IPCG_LAUNCH("k_refit", s, k_refit<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(n, bvh.lo.p, bvh.hi.p, bvh.parent.p, bvh.flags.p));
-        IPCG_CHECK_LAUNCH();
+        IPCG_LAUNCH("k_refit", s, k_refit<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(n, bvh.lo.p, bvh.hi.p, bvh.parent.p,
+            bvh.flags.p));
     }
 }
 
-void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, double inflation, int64_t& n_ee,
+void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, const double* scene_r, int64_t& n_ee,
     int64_t& n_fv)
 {
     cudaStream_t s = m->stream;
@@ -333,8 +355,10 @@ void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, double 
     IPCG_LAUNCH("k_bounds_partial", s, k_bounds_partial<<<nb, BLOCK, 0, s>>>(V0, V1, nV, m->bounds.p));
     IPCG_LAUNCH("k_bounds_final", s, k_bounds_final<<<1, 32, 0, s>>>(m->bounds.p, nb));
     IPCG_CHECK_LAUNCH();
-    build_lbvh(m, m->ebvh, 2, V0, V1, inflation);
-    build_lbvh(m, m->fbvh, 3, V0, V1, inflation);
+    build_lbvh(m, m->ebvh, 2, V0, V1, scene_r);
+    build_lbvh(m, m->fbvh, 3, V0, V1, scene_r);
+    const SceneView sv = scene_view(m);
+    const bool batched = sv.vscene != nullptr;
     m->counters.reserve(8);
     m->h_counters.reserve(8);
     if (m->cand_cap == 0) m->cand_cap = 4 * (m->nE + m->nV) + 1024;
@@ -345,9 +369,11 @@ void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, double 
         const int icap = (int)std::min<int64_t>(cap, INT32_MAX);
         if (m->ebvh.n >= 2)
             IPCG_LAUNCH("k_traverse_ee", s, k_traverse_ee<<<grid_for(m->ebvh.n, 128), 128, 0, s>>>(m->ebvh.lo.p,
-                m->ebvh.hi.p, m->ebvh.last.p, m->ebvh.n, m->E.p, m->cand.p, m->counters.p + 0, icap, m->counters.p + 2));
+                m->ebvh.hi.p, m->ebvh.first.p, m->ebvh.last.p, m->ebvh.leaf_scene.p, batched, m->ebvh.n, m->E.p,
+                m->cand.p, m->counters.p + 0, icap, m->counters.p + 2));
         if (m->fbvh.n >= 1 && nV > 0)
-            IPCG_LAUNCH("k_traverse_fv", s, k_traverse_fv<<<grid_for(nV, 128), 128, 0, s>>>(m->fbvh.lo.p, m->fbvh.hi.p, m->fbvh.n, V0, V1, inflation,
+            IPCG_LAUNCH("k_traverse_fv", s, k_traverse_fv<<<grid_for(nV, 128), 128, 0, s>>>(m->fbvh.lo.p,
+                m->fbvh.hi.p, m->fbvh.first.p, m->fbvh.last.p, m->fbvh.leaf_scene.p, m->fbvh.n, V0, V1, scene_r, sv,
                 nV, m->F.p, m->cand.p + cap, m->counters.p + 1, icap, m->counters.p + 2));
         IPCG_CHECK_LAUNCH();
         IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, m->counters.p, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));

@@ -298,7 +298,8 @@ __device__ int stencil_ccd(Query& q, double min_distance, const CCDParams& P, do
     return strategy(q, min_distance, d0, P, adj, tmax, toi, shared_best, bud);
 }
 
-__device__ __forceinline__ void load_query(int i, const int2* __restrict__ cand_ee, int n_ee,
+// Loads candidate i; returns its first vertex (which names its scene).
+__device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_ee, int n_ee,
     const int2* __restrict__ cand_fv, const double* __restrict__ V0, const double* __restrict__ V1,
     const int* __restrict__ E, const int* __restrict__ F, Query& q)
 {
@@ -322,6 +323,7 @@ __device__ __forceinline__ void load_query(int i, const int2* __restrict__ cand_
         q.s[k] = load_v3(V0, ids[k]);
         q.e[k] = load_v3(V1, ids[k]);
     }
+    return ids[0];
 }
 
 // One thread per candidate (candidates.cpp:252-292).  With a box budget
@@ -329,24 +331,26 @@ __device__ __forceinline__ void load_query(int i, const int2* __restrict__ cand_
 // instead; those are run to completion in pass 2 (hard != null selects the
 // candidate list), by which time the earliest time of the easy queries
 // prunes them.  Each query's result does not depend on the pass, so the
-// minimum is the same as a single full pass.
+// minimum is the same as a single full pass.  In a batch each scene has its
+// own minimum distance and its own earliest time (toi_bits[scene]).
 __global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee, int n_ee,
     const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
-    const int* __restrict__ E, const int* __restrict__ F, double min_distance, CCDParams P,
-    unsigned long long* toi_bits, long long budget, const int* __restrict__ list, const int* __restrict__ list_n,
-    int* __restrict__ hard, int* __restrict__ hard_n)
+    const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,
+    CCDParams P, unsigned long long* toi_bits, long long budget, const int* __restrict__ list,
+    const int* __restrict__ list_n, int* __restrict__ hard, int* __restrict__ hard_n)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = list ? *list_n : n_ee + n_fv;
     if (t >= n) return;
     const int i = list ? list[t] : t;
     Query q;
-    load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q);
-    const double tmax = __longlong_as_double((long long)*(volatile unsigned long long*)toi_bits);
+    const int scene = sv.of(load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q));
+    unsigned long long* best = toi_bits + scene;
+    const double tmax = __longlong_as_double((long long)*(volatile unsigned long long*)best);
     double toi = __longlong_as_double(0x7ff0000000000000ULL);
     Budget bud { budget, 0 };
-    const int st = stencil_ccd(q, min_distance, P, tmax, toi, toi_bits, bud);
-    if (st == CCD_HIT && toi < tmax) atomicMin(toi_bits, (unsigned long long)__double_as_longlong(toi));
+    const int st = stencil_ccd(q, __ldg(min_distance + scene), P, tmax, toi, best, bud);
+    if (st == CCD_HIT && toi < tmax) atomicMin(best, (unsigned long long)__double_as_longlong(toi));
     else if (st == CCD_UNRESOLVED) hard[atomicAdd(hard_n, 1)] = i;
 }
 
@@ -396,18 +400,33 @@ __global__ void k_distance_stencils(int kind, int n, const double* __restrict__ 
 
 } // namespace
 
-double collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, double min_distance,
-    double tolerance, int64_t max_iterations, double rescale, int64_t* n_candidates)
+void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, const double* min_distance,
+    double tolerance, int64_t max_iterations, double rescale, double* steps, int64_t* n_candidates)
 {
     cudaStream_t s = m->stream;
+    const int ns = (int)m->n_scenes;
+    // per scene: broad-phase inflation 0.5 * min_distance, then min_distance
+    std::vector<double> h(2 * ns);
+    for (int k = 0; k < ns; ++k) {
+        h[k] = 0.5 * min_distance[k];
+        h[ns + k] = min_distance[k];
+    }
+    m->scene_md.reserve(2 * ns);
+    IPCG_CUDA(cudaMemcpyAsync(m->scene_md.p, h.data(), sizeof(double) * 2 * ns, cudaMemcpyHostToDevice, s));
     int64_t n_ee = 0, n_fv = 0;
-    detect_candidates(m, V0, V1, 0.5 * min_distance, n_ee, n_fv);
+    detect_candidates(m, V0, V1, m->scene_md.p, n_ee, n_fv);
     if (n_candidates) *n_candidates = n_ee + n_fv;
-    if (n_ee + n_fv == 0) return 1.0;
-    m->toi_bits.reserve(1);
-    const unsigned long long one = 0x3ff0000000000000ULL; // 1.0
-    IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    if (n_ee + n_fv == 0) {
+        for (int k = 0; k < ns; ++k) steps[k] = 1.0;
+        return;
+    }
+    m->toi_bits.reserve(ns);
+    std::vector<unsigned long long> ones(ns, 0x3ff0000000000000ULL); // 1.0
+    IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, ones.data(), sizeof(unsigned long long) * ns, cudaMemcpyHostToDevice,
+        s));
     const CCDParams P { tolerance, (long long)max_iterations, rescale };
+    const SceneView sv = scene_view(m);
+    const double* md = m->scene_md.p + ns;
     const int nc = (int)(n_ee + n_fv);
     m->ivals_a.reserve(nc + 1);
     int* hard = m->ivals_a.p;
@@ -415,17 +434,16 @@ double collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1,
     IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
     // pass 1: every query with a small box budget; pass 2: the unresolved ones
     IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p + m->cand_cap,
-        (int)n_fv, V0, V1, m->E.p, m->F.p, min_distance, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard,
+        (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard,
         hard_n));
     IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p +
-        m->cand_cap, (int)n_fv, V0, V1, m->E.p, m->F.p, min_distance, P, m->toi_bits.p, 0, hard, hard_n, nullptr,
+        m->cand_cap, (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr,
         nullptr));
-    unsigned long long bits = 0;
-    IPCG_CUDA(cudaMemcpyAsync(&bits, m->toi_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    std::vector<unsigned long long> bits(ns);
+    IPCG_CUDA(cudaMemcpyAsync(bits.data(), m->toi_bits.p, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost,
+        s));
     IPCG_CUDA(cudaStreamSynchronize(s));
-    double t;
-    memcpy(&t, &bits, sizeof(t));
-    return t;
+    for (int k = 0; k < ns; ++k) memcpy(steps + k, &bits[k], sizeof(double));
 }
 
 void ccd_stencils(cudaStream_t s, int is_ee, int64_t n, const double* x0, const double* x1, double min_distance,

@@ -63,13 +63,15 @@ __device__ __forceinline__ void put_ev(const Out& o, int e, int v)
 
 // normal_collisions_builder.cpp:140-237, candidate oriented ea < eb
 __global__ void k_filter_ee(const int2* __restrict__ cand, int n, const double* __restrict__ V,
-    const double* __restrict__ rest, const int* __restrict__ E, double offset_sqr, Out o)
+    const double* __restrict__ rest, const int* __restrict__ E, const double* __restrict__ scene_off2, SceneView sv,
+    Out o)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int2 c = cand[i];
     const int ea = c.x, eb = c.y;
     const int a0 = E[2 * ea], a1 = E[2 * ea + 1], b0 = E[2 * eb], b1 = E[2 * eb + 1];
+    const double offset_sqr = __ldg(scene_off2 + sv.of(a0));
     const V3 xa0 = load_v3(V, a0), xa1 = load_v3(V, a1), xb0 = load_v3(V, b0), xb1 = load_v3(V, b1);
     const int actual = edge_edge_distance_type(xa0, xa1, xb0, xb1);
     const double d = edge_edge_distance(xa0, xa1, xb0, xb1, actual);
@@ -99,12 +101,14 @@ __global__ void k_filter_ee(const int2* __restrict__ cand, int n, const double* 
 
 // normal_collisions_builder.cpp:239-336
 __global__ void k_filter_fv(const int2* __restrict__ cand, int n, const double* __restrict__ V,
-    const int* __restrict__ F, const int* __restrict__ F2E, double offset_sqr, Out o)
+    const int* __restrict__ F, const int* __restrict__ F2E, const double* __restrict__ scene_off2, SceneView sv,
+    Out o)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int2 c = cand[i];
     const int fi = c.x, vi = c.y;
+    const double offset_sqr = __ldg(scene_off2 + sv.of(vi));
     const int f0 = F[3 * fi], f1 = F[3 * fi + 1], f2 = F[3 * fi + 2];
     const V3 p = load_v3(V, vi), t0 = load_v3(V, f0), t1 = load_v3(V, f1), t2 = load_v3(V, f2);
     const int dtype = point_triangle_distance_type(p, t0, t1, t2);
@@ -160,14 +164,27 @@ __global__ void k_gather_ee(const unsigned long long* __restrict__ keys, const i
 
 } // namespace
 
-void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, double dhat, double dmin)
+void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, const double* dhat, const double* dmin)
 {
     cudaStream_t s = m->stream;
+    // per-scene inflation 0.5 (dhat + dmin) (normal_collisions.cpp:30) and
+    // activation threshold (dmin + dhat)^2 (normal_collisions.cpp:52-54)
+    const int ns = (int)m->n_scenes;
+    std::vector<double> hr(ns), hoff(ns);
+    for (int k = 0; k < ns; ++k) {
+        hr[k] = 0.5 * (dhat[k] + dmin[k]);
+        hoff[k] = (dmin[k] + dhat[k]) * (dmin[k] + dhat[k]);
+    }
+    m->scene_r.reserve(ns);
+    m->scene_off2.reserve(ns);
+    IPCG_CUDA(cudaMemcpyAsync(m->scene_r.p, hr.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, s));
+    IPCG_CUDA(cudaMemcpyAsync(m->scene_off2.p, hoff.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, s));
     int64_t n_ee = 0, n_fv = 0;
-    detect_candidates(m, V, nullptr, 0.5 * (dhat + dmin), n_ee, n_fv);
+    detect_candidates(m, V, nullptr, m->scene_r.p, n_ee, n_fv);
     c->n_cand_ee = n_ee;
     c->n_cand_fv = n_fv;
-    c->dmin = dmin;
+    c->dmin = dmin[0];
+    c->scene_dmin.assign(dmin, dmin + ns);
     const int64_t nc = n_ee + n_fv;
     // raw records: at most one per candidate
     const int64_t cap = nc + 16;
@@ -189,12 +206,13 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, doub
     m->counters.reserve(16);
     o.count = m->counters.p + 4;
     IPCG_CUDA(cudaMemsetAsync(o.count, 0, sizeof(int) * 8, s));
-    const double off = (dmin + dhat) * (dmin + dhat);
+    const SceneView sv = scene_view(m);
     if (n_ee)
-        IPCG_LAUNCH("k_filter_ee", s, k_filter_ee<<<grid_for(n_ee, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, V, m->rest.p, m->E.p, off, o));
+        IPCG_LAUNCH("k_filter_ee", s, k_filter_ee<<<grid_for(n_ee, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, V,
+            m->rest.p, m->E.p, m->scene_off2.p, sv, o));
     if (n_fv)
-        IPCG_LAUNCH("k_filter_fv", s, k_filter_fv<<<grid_for(n_fv, BLOCK), BLOCK, 0, s>>>(m->cand.p + m->cand_cap, (int)n_fv, V, m->F.p,
-            m->F2E.p, off, o));
+        IPCG_LAUNCH("k_filter_fv", s, k_filter_fv<<<grid_for(n_fv, BLOCK), BLOCK, 0, s>>>(m->cand.p + m->cand_cap,
+            (int)n_fv, V, m->F.p, m->F2E.p, m->scene_off2.p, sv, o));
     IPCG_CHECK_LAUNCH();
     IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, o.count, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
     IPCG_CUDA(cudaStreamSynchronize(s));

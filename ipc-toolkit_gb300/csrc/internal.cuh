@@ -75,13 +75,24 @@ template <typename T> struct HBuf {
 // (root = 0), n-1..2n-2 leaves in Morton order.  lo.w / hi.w hold the two
 // child indices (internal) or the primitive id / -1 (leaf) as int bits;
 // last[i] is the largest sorted leaf index under node i.
+// Scenes of a batch are kept apart by putting the scene id above the Morton
+// code in the 64-bit sort key: each scene's leaves are contiguous, and
+// leaf_scene[first[i]] .. leaf_scene[last[i]] is the scene range of node i.
 struct LBVH {
     int n = 0;
     DBuf<float4> lo, hi;
-    DBuf<int> last, parent, flags;
-    DBuf<unsigned> codes, codes_sorted;
+    DBuf<int> first, last, parent, flags, leaf_scene;
+    DBuf<unsigned long long> codes, codes_sorted;
     DBuf<int> ids, ids_sorted;
     DBuf<float4> plo, phi; // per-primitive leaf boxes before sorting
+};
+
+// Per-scene view passed to kernels.  For a single scene vscene is null and
+// every array has one entry.
+struct SceneView {
+    int n;                 // number of scenes
+    const int* vscene;     // per-vertex scene id, or null (one scene)
+    __device__ __forceinline__ int of(int v) const { return vscene ? __ldg(vscene + v) : 0; }
 };
 
 // Flags of device-side guards (bit set => the call fails loudly).
@@ -92,6 +103,13 @@ enum : int { GUARD_STACK = 1, GUARD_CAPACITY = 2 };
 struct ipcg_mesh {
     int device = 0;
     int64_t nV = 0, nE = 0, nF = 0;
+    int64_t n_scenes = 1;
+    std::vector<int64_t> h_voff;     // vertex offsets of the scenes (n_scenes + 1)
+    ipcg::DBuf<int> vscene;          // per-vertex scene id (batches only)
+    ipcg::DBuf<double> scene_r;      // per-scene inflation radius of the current build
+    ipcg::DBuf<double> scene_off2;   // per-scene (dhat + dmin)^2 of the current build
+    ipcg::DBuf<unsigned char> params_buf; // per-scene barrier parameters
+    ipcg::DBuf<double> scene_md;     // CCD: per-scene 0.5*min_distance, then min_distance
     cudaStream_t stream = nullptr;
     ipcg::DBuf<double> rest;
     ipcg::DBuf<int> E, F, F2E;
@@ -121,6 +139,7 @@ struct ipcg_collisions {
     int64_t nvv = 0, nev = 0, nee = 0, nfv = 0;
     int64_t n_cand_ee = 0, n_cand_fv = 0;
     double dmin = 0;
+    std::vector<double> scene_dmin;  // per scene (batches)
     ipcg::DBuf<int2> vv, ev, ee, fv;
     ipcg::DBuf<double> vv_w, ev_w, ee_w, fv_w, ee_eps;
     ipcg::DBuf<int8_t> ee_dtype;
@@ -142,21 +161,26 @@ namespace ipcg {
 const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf);
 bool is_device_ptr(const void* p);
 
+inline SceneView scene_view(const ipcg_mesh* m) { return SceneView { (int)m->n_scenes, m->n_scenes > 1 ? m->vscene.p : nullptr }; }
+
 // broad_phase.cu
 void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind /*2 edges, 3 faces*/, const double* V0, const double* V1,
-    double inflation);
-// Detect EE + FV candidates into m->cand; returns (n_ee, n_fv).
-void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, double inflation, int64_t& n_ee,
+    const double* scene_r);
+// Detect EE + FV candidates into m->cand with the per-scene inflation radii
+// scene_r (device, one per scene); returns (n_ee, n_fv).
+void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, const double* scene_r, int64_t& n_ee,
     int64_t& n_fv);
 
-// collisions.cu
-void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, double dhat, double dmin);
+// collisions.cu: per-scene dhat / dmin (host arrays of n_scenes)
+void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, const double* dhat, const double* dmin);
 
 // barrier.cu
 struct BarrierArgs {
     double dhat, kappa, dmin;
     int physical;
     int psd;
+    const double* scene_dhat = nullptr;  // per scene (batches), host
+    const double* scene_kappa = nullptr; // per scene (batches), host
 };
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null);
@@ -173,8 +197,9 @@ void barrier_energy_noalloc(const double* V, const int* E, const int* F, const C
     double kappa, double dmin, int physical, double* energy, cudaStream_t s);
 
 // ccd.cu
-double collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, double min_distance,
-    double tolerance, int64_t max_iterations, double rescale, int64_t* n_candidates);
+// Per scene: min_distance[n_scenes] (host) in, steps[n_scenes] (host) out.
+void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, const double* min_distance,
+    double tolerance, int64_t max_iterations, double rescale, double* steps, int64_t* n_candidates);
 void ccd_stencils(cudaStream_t s, int is_ee, int64_t n, const double* x0, const double* x1, double min_distance,
     double tmax, double tolerance, int64_t max_iterations, double rescale, int8_t* hit, double* toi);
 void distance_stencils(cudaStream_t s, int kind, int64_t n, const double* x, int8_t* dtype, double* dist);

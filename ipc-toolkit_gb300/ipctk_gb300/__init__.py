@@ -75,6 +75,11 @@ def _load():
         "ipcg_profile_report": (i32, [C.c_char_p, i64, P]),
         "ipcg_launch_count": (i32, [P]),
         "ipcg_mesh_stream": (i32, [P, PP]),
+        "ipcg_mesh_create_batch": (i32, [P, i64, P, i64, P, i64, i64, P, PP]),
+        "ipcg_mesh_scenes": (i32, [P, P]),
+        "ipcg_collisions_build_batch": (i32, [P, P, P, P, P]),
+        "ipcg_barrier_batch": (i32, [P, P, P, P, P, i32, i32, P, P, PP]),
+        "ipcg_collision_free_stepsize_batch": (i32, [P, P, P, P, d, i64, d, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -283,6 +288,61 @@ class CollisionMesh:
         return out
 
 
+class SceneBatch(CollisionMesh):
+    """Many independent scenes (one CollisionMesh each in the reference)
+    packed into one device mesh: ``SceneBatch([(V0, E0, F0), (V1, E1, F1), ...])``.
+
+    Edges and faces of each scene use its own vertex indices; they are
+    shifted into the packed numbering here.  Contacts never join two scenes.
+    NormalCollisions.build, BatchBarrierPotential and
+    compute_collision_free_stepsize_batch take one parameter per scene."""
+
+    def __init__(self, scenes):
+        L = _load()
+        Vs, Es, Fs, voff = [], [], [], [0]
+        for sc in scenes:
+            V, E, F = (tuple(sc) + (None, None))[:3]
+            V = np.ascontiguousarray(np.asarray(V, dtype=np.float64))
+            if V.ndim != 2 or V.shape[1] != 3:
+                raise ValueError("only 3D meshes are supported: rest_positions must be (n, 3)")
+            Vs.append(V)
+            Es.append(_as_i32(E if E is not None else np.zeros((0, 2)), 2) + voff[-1])
+            Fs.append(_as_i32(F if F is not None else np.zeros((0, 3)), 3) + voff[-1])
+            voff.append(voff[-1] + V.shape[0])
+        if not Vs:
+            raise ValueError("a batch needs at least one scene")
+        V = np.ascontiguousarray(np.concatenate(Vs))
+        E = np.ascontiguousarray(np.concatenate(Es), dtype=np.int32)
+        F = np.ascontiguousarray(np.concatenate(Fs), dtype=np.int32)
+        self.vertex_offsets = np.asarray(voff, np.int64)
+        h = C.c_void_p()
+        _check(L.ipcg_mesh_create_batch(_ptr(V), V.shape[0], _ptr(E), E.shape[0], _ptr(F), F.shape[0],
+                                        len(Vs), _ptr(self.vertex_offsets), C.byref(h)))
+        self._h = h
+        self._rest = V
+        self._E = E
+        self._F = F
+
+    @property
+    def num_scenes(self):
+        return len(self.vertex_offsets) - 1
+
+    def per_scene(self, x):
+        """Broadcast a scalar (or check an array) to one float per scene."""
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float64), (self.num_scenes,)))
+
+    def pack(self, vertices_per_scene):
+        """Concatenate per-scene (n_k, 3) position arrays."""
+        return np.ascontiguousarray(np.concatenate([np.asarray(v, np.float64) for v in vertices_per_scene]))
+
+    def unpack(self, packed):
+        """Split a packed (nV, 3) array (or 3nV vector) into per-scene arrays."""
+        a = np.asarray(packed)
+        per = 3 if a.ndim == 1 else 1
+        o = self.vertex_offsets * per
+        return [a[o[k]:o[k + 1]] for k in range(self.num_scenes)]
+
+
 class NormalCollisions:
     """NormalCollisions (src/ipc/collisions/normal/normal_collisions.hpp).
 
@@ -305,7 +365,11 @@ class NormalCollisions:
         """normal_collisions.cpp:20-36.  ``broad_phase`` is accepted for API
         compatibility; the device LBVH is always used."""
         V = _as_f64(vertices)
-        _check(_load().ipcg_collisions_build(self._h, mesh._h, _ptr(V), float(dhat), float(dmin)))
+        if isinstance(mesh, SceneBatch):
+            dh, dm = mesh.per_scene(dhat), mesh.per_scene(dmin)
+            _check(_load().ipcg_collisions_build_batch(self._h, mesh._h, _ptr(V), _ptr(dh), _ptr(dm)))
+        else:
+            _check(_load().ipcg_collisions_build(self._h, mesh._h, _ptr(V), float(dhat), float(dmin)))
         self._cache = None
 
     def counts(self):
@@ -459,6 +523,52 @@ class BarrierPotential:
         return float(e[0]), g, _csr_to_scipy(h, 3 * mesh.num_vertices)
 
 
+class BatchBarrierPotential:
+    """BarrierPotential with one dhat and one stiffness per scene of a
+    SceneBatch.  Energies come back per scene; the gradient and Hessian are
+    the packed ones (block diagonal over scenes)."""
+
+    def __init__(self, dhat, stiffness, use_physical_barrier: bool = False):
+        self.dhat = np.asarray(dhat, np.float64)
+        self.stiffness = np.asarray(stiffness, np.float64)
+        if not np.all(self.dhat > 0):
+            raise ValueError("dhat must be positive")
+        self.use_physical_barrier = bool(use_physical_barrier)
+
+    def evaluate(self, collisions: NormalCollisions, batch: SceneBatch, vertices, energy=True, gradient=False,
+                 hessian=False, project_hessian_to_psd=PSDProjectionMethod.NONE, device=False):
+        """(energies, gradient or None, Hessian or None) from one call.  With
+        ``device`` the Hessian is a DeviceCSR, else a scipy matrix."""
+        V = _as_f64(vertices)
+        dh, kap = batch.per_scene(self.dhat), batch.per_scene(self.stiffness)
+        e = np.zeros(batch.num_scenes) if energy else None
+        g = None
+        if gradient:
+            if _is_torch_cuda(V):
+                import torch
+                g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
+            else:
+                g = np.zeros(3 * batch.num_vertices)
+        h = C.c_void_p()
+        _check(_load().ipcg_barrier_batch(collisions._h, batch._h, _ptr(V), _ptr(dh), _ptr(kap),
+                                          int(self.use_physical_barrier), int(project_hessian_to_psd), _ptr(e),
+                                          _ptr(g), C.byref(h) if hessian else None))
+        H = None
+        if hessian:
+            H = DeviceCSR(h, 3 * batch.num_vertices) if device else _csr_to_scipy(h, 3 * batch.num_vertices)
+        return e, g, H
+
+    def __call__(self, collisions, batch, vertices):
+        return self.evaluate(collisions, batch, vertices)[0]
+
+    def gradient(self, collisions, batch, vertices):
+        return self.evaluate(collisions, batch, vertices, energy=False, gradient=True)[1]
+
+    def hessian(self, collisions, batch, vertices, project_hessian_to_psd=PSDProjectionMethod.NONE):
+        return self.evaluate(collisions, batch, vertices, energy=False, hessian=True,
+                             project_hessian_to_psd=project_hessian_to_psd)[2]
+
+
 class TightInclusionCCD:
     """TightInclusionCCD(tolerance, max_iterations, conservative_rescaling)
     (src/ipc/ccd/tight_inclusion_ccd.hpp:11-28)."""
@@ -517,6 +627,19 @@ def compute_collision_free_stepsize(mesh: CollisionMesh, vertices_t0, vertices_t
         mesh._h, _ptr(V0), _ptr(V1), float(min_distance), narrow_phase_ccd.tolerance,
         narrow_phase_ccd.max_iterations, narrow_phase_ccd.conservative_rescaling, _ptr(step), None))
     return float(step[0])
+
+
+def compute_collision_free_stepsize_batch(batch: SceneBatch, vertices_t0, vertices_t1, min_distance=0.0,
+                                          narrow_phase_ccd: TightInclusionCCD = DEFAULT_NARROW_PHASE_CCD):
+    """compute_collision_free_stepsize on every scene of a SceneBatch: one
+    step per scene (equal to the scene's own call)."""
+    V0, V1 = _as_f64(vertices_t0), _as_f64(vertices_t1)
+    md = batch.per_scene(min_distance)
+    steps = np.zeros(batch.num_scenes)
+    _check(_load().ipcg_collision_free_stepsize_batch(
+        batch._h, _ptr(V0), _ptr(V1), _ptr(md), narrow_phase_ccd.tolerance, narrow_phase_ccd.max_iterations,
+        narrow_phase_ccd.conservative_rescaling, _ptr(steps), None))
+    return steps
 
 
 def distance_stencils(kind: int, x):
