@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["sphere_pack", "two_sheet", "layered_cloth"], default="sphere_pack")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 256-scene batched-vs-plain leg")
     return ap.parse_args()
 
 
@@ -237,6 +238,114 @@ def run_reference(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(dev, warmup=2, steps=3):
+    """The 256-scene batch (uneven two-sheet scenes, side log-uniform in
+    [16, 256], per-scene dhat log-uniform in [1e-4, 1e-2]; seed 3): one step
+    is E + grad + CLAMP Hessian of every scene, and one CCD step is the
+    collision-free step of every scene.  "plain" runs the single-scene API
+    once per scene (one CollisionMesh each, as the reference is used);
+    "batched" runs each of the three calls once over a SceneBatch.  The plain
+    objects are released before the batched ones are made (the two sets of
+    device scratch do not fit together)."""
+    import gc
+    import torch
+    import ipctk_gb300 as ipctk
+    from ipctk_gb300 import scenes
+    scs = scenes.batch()
+    CLAMP = ipctk.PSDProjectionMethod.CLAMP
+    nverts = sum(s["V"].shape[0] for s in scs)
+    pct = lambda a, q: float(np.percentile(np.array(a), q))
+
+    def timed(fn, n_warm, n_steps):
+        for _ in range(n_warm):
+            fn()
+        torch.cuda.synchronize()
+        out = []
+        for _ in range(n_steps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            out.append(1000 * (time.perf_counter() - t0))
+        return out
+
+    # plain: one mesh per scene
+    plain = []
+    for s in scs:
+        m = ipctk.CollisionMesh(s["V"], s["E"], s["F"])
+        Vd = torch.from_numpy(s["V"]).to(dev)
+        V1d = torch.from_numpy(s["V1"]).to(dev)
+        c = ipctk.NormalCollisions()
+        plain.append((s, m, Vd, V1d, c, ipctk.BarrierPotential(s["dhat"], s["kappa"])))
+
+    def plain_build():
+        for s, m, Vd, V1d, c, B in plain:
+            c.build(m, Vd, s["dhat"])
+
+    def plain_egh():
+        for s, m, Vd, V1d, c, B in plain:
+            B(c, m, Vd)
+            B.gradient(c, m, Vd)
+            B.hessian_device(c, m, Vd, CLAMP).free()
+
+    def plain_ccd():
+        return [ipctk.compute_collision_free_stepsize(m, Vd, V1d) for s, m, Vd, V1d, c, B in plain]
+
+    p_build = timed(plain_build, 1, 2)
+    C = sum(len(p[4]) for p in plain)
+    l0 = ipctk.launch_count()
+    p_egh = timed(plain_egh, warmup, steps)
+    p_launch = (ipctk.launch_count() - l0) / (warmup + steps)
+    p_ccd = timed(plain_ccd, 1, 2)
+    plain_steps = plain_ccd()
+    free_after_plain = torch.cuda.mem_get_info(dev)[0]
+    del plain
+    gc.collect()
+    torch.cuda.synchronize()
+
+    # batched: one packed mesh
+    batch = ipctk.SceneBatch([(s["V"], s["E"], s["F"]) for s in scs])
+    Vd = torch.from_numpy(batch.pack([s["V"] for s in scs])).to(dev)
+    V1d = torch.from_numpy(batch.pack([s["V1"] for s in scs])).to(dev)
+    dh = np.array([s["dhat"] for s in scs])
+    kap = np.array([s["kappa"] for s in scs])
+    col = ipctk.NormalCollisions()
+    BB = ipctk.BatchBarrierPotential(dh, kap)
+
+    def batch_egh():
+        BB(col, batch, Vd)
+        BB.gradient(col, batch, Vd)
+        BB.evaluate(col, batch, Vd, energy=False, hessian=True, project_hessian_to_psd=CLAMP, device=True)[2].free()
+
+    b_build = timed(lambda: col.build(batch, Vd, dh), 1, 2)
+    Cb = len(col)
+    l0 = ipctk.launch_count()
+    b_egh = timed(batch_egh, warmup, steps)
+    b_launch = (ipctk.launch_count() - l0) / (warmup + steps)
+    b_ccd = timed(lambda: ipctk.compute_collision_free_stepsize_batch(batch, Vd, V1d), 1, 2)
+    batch_steps = ipctk.compute_collision_free_stepsize_batch(batch, Vd, V1d)
+    free_after_batch = torch.cuda.mem_get_info(dev)[0]
+    del col, batch, Vd, V1d
+    gc.collect()
+    ns = len(scs)
+    med = statistics.median
+    return {
+        "workload": f"{ns} uneven two-sheet scenes ({nverts:,} verts; side log-uniform [16, 256], dhat "
+                    "log-uniform [1e-4, 1e-2], gap U(0.2, 0.9) dhat; seed 3)",
+        "contacts": C, "contacts_equal": Cb == C,
+        "steps_equal": bool(np.array_equal(np.array(plain_steps), batch_steps)),
+        "egh": {"unit": UNIT, "warmup": warmup, "steps": steps,
+                "batched": {"value": C / (med(b_egh) / 1000.0), "p50_ms": pct(b_egh, 50), "p99_ms": pct(b_egh, 99),
+                            "launches_per_step": b_launch},
+                "plain": {"value": C / (med(p_egh) / 1000.0), "p50_ms": pct(p_egh, 50), "p99_ms": pct(p_egh, 99),
+                          "launches_per_step": p_launch}},
+        "ccd": {"unit": "scene-steps/s",
+                "batched": {"value": ns / (med(b_ccd) / 1000.0), "p50_ms": pct(b_ccd, 50)},
+                "plain": {"value": ns / (med(p_ccd) / 1000.0), "p50_ms": pct(p_ccd, 50)}},
+        "build_ms": {"batched": med(b_build), "plain": med(p_build)},
+        "free_gb_after": {"plain": free_after_plain / 1e9, "batched": free_after_batch / 1e9},
+    }
+
+
 def run_gb300(args, rank, world):
     import torch
     import ipctk_gb300 as ipctk
@@ -369,6 +478,10 @@ def run_gb300(args, rank, world):
 
     if rank != 0:
         return
+    batch = None
+    if not args.no_batch:
+        del mesh, col, Vd, V1d, flush
+        batch = batch_leg(dev)
     cpu = None
     ccd_cpu = None
     if not args.no_cpu_baseline:
@@ -395,6 +508,7 @@ def run_gb300(args, rank, world):
         "ccd": {"steps_per_s": 1000.0 / statistics.median(ccd_ms), "p50_ms": pct(ccd_ms, 50),
                 "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "cpu_baseline": ccd_cpu},
         "collision_build": {"p50_ms": pct(build_ms, 50), "p99_ms": pct(build_ms, 99)},
+        "batch": batch,
     }
     print(json.dumps(line), flush=True)
 

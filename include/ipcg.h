@@ -96,6 +96,12 @@ int ipcg_mesh_create_batch(const double* rest_positions, int64_t num_vertices,
                            ipcg_mesh** out);
 int ipcg_mesh_scenes(const ipcg_mesh* mesh, int64_t* n_scenes);
 
+/* Memory bound of the batched Hessian: the local 12x12 blocks of at most
+ * `contacts` contacts (1152 bytes each) are held at once; a batch with more
+ * contacts is assembled a run of whole scenes at a time.  0 restores the
+ * default 4,194,304 (4.8 GB).  Process-wide; results do not depend on it. */
+int ipcg_set_hessian_chunk_contacts(int64_t contacts);
+
 /* ---------------------------------------------------------------------- */
 /* NormalCollisions                                                        */
 /* ---------------------------------------------------------------------- */

@@ -246,15 +246,36 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
             require(n_scenes == 1, "vertex_offsets is NULL");
             voff[1] = nV;
         }
+        // offsets: vertex, edge, edge, face (edges and faces are numbered scene by scene)
+        std::vector<int64_t> soff(4 * (n_scenes + 1), 0);
         if (n_scenes > 1) {
             vscene.resize(nV);
             for (int64_t k = 0; k < n_scenes; ++k)
                 for (int64_t v = voff[k]; v < voff[k + 1]; ++v) vscene[v] = (int32_t)k;
-            for (int64_t e = 0; e < nE; ++e)
-                require(vscene[hE[2 * e]] == vscene[hE[2 * e + 1]], "an edge joins two scenes");
-            for (int64_t f = 0; f < nF; ++f)
-                require(vscene[hF[3 * f]] == vscene[hF[3 * f + 1]] && vscene[hF[3 * f]] == vscene[hF[3 * f + 2]],
-                    "a face joins two scenes");
+            std::vector<int64_t> ecount(n_scenes, 0), fcount(n_scenes, 0);
+            int32_t prev = 0;
+            for (int64_t e = 0; e < nE; ++e) {
+                const int32_t k = vscene[hE[2 * e]];
+                require(k == vscene[hE[2 * e + 1]], "an edge joins two scenes");
+                require(k >= prev, "edges must be grouped by scene in scene order");
+                prev = k;
+                ++ecount[k];
+            }
+            prev = 0;
+            for (int64_t f = 0; f < nF; ++f) {
+                const int32_t k = vscene[hF[3 * f]];
+                require(k == vscene[hF[3 * f + 1]] && k == vscene[hF[3 * f + 2]], "a face joins two scenes");
+                require(k >= prev, "faces must be grouped by scene in scene order");
+                prev = k;
+                ++fcount[k];
+            }
+            const int64_t S = n_scenes + 1;
+            for (int64_t k = 0; k <= n_scenes; ++k) soff[k] = voff[k];
+            for (int64_t k = 0; k < n_scenes; ++k) {
+                soff[S + k + 1] = soff[S + k] + ecount[k];
+                soff[3 * S + k + 1] = soff[3 * S + k] + fcount[k];
+            }
+            for (int64_t k = 0; k <= n_scenes; ++k) soff[2 * S + k] = soff[S + k];
         }
         // faces_to_edges (collision_mesh.cpp:510-543)
         std::unordered_map<uint64_t, int32_t> emap;
@@ -285,7 +306,10 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
             m->h_F2E = std::move(f2e);
             m->n_scenes = n_scenes;
             m->h_voff = std::move(voff);
-            if (n_scenes > 1) upload(m->vscene, (const int*)vscene.data(), nV, m->stream);
+            if (n_scenes > 1) {
+                upload(m->vscene, (const int*)vscene.data(), nV, m->stream);
+                upload(m->scene_offs, (const int64_t*)soff.data(), soff.size(), m->stream);
+            }
             m->counters.reserve(16);
             m->h_counters.reserve(16);
             IPCG_CUDA(cudaStreamSynchronize(m->stream));
@@ -314,6 +338,14 @@ int ipcg_mesh_create_batch(const double* rest, int64_t nV, const int32_t* edges,
         return IPCG_ERR_INVALID;
     }
     return mesh_create(rest, nV, edges, nE, faces, nF, n_scenes, vertex_offsets, out);
+}
+
+int ipcg_set_hessian_chunk_contacts(int64_t contacts)
+{
+    return guarded([&] {
+        require(contacts >= 0, "contacts must be non-negative");
+        g_hess_chunk_contacts.store(contacts ? contacts : (int64_t(1) << 22));
+    });
 }
 
 int ipcg_mesh_scenes(const ipcg_mesh* m, int64_t* n_scenes)
@@ -446,6 +478,8 @@ int ipcg_collisions_set(ipcg_collisions* c, double dmin, int64_t nvv, const int3
         c->nee = nee;
         c->nfv = nfv;
         c->dmin = dmin;
+        c->scene_dmin.clear();
+        c->sorted = false;
         c->n_cand_ee = c->n_cand_fv = 0;
     });
 }

@@ -23,7 +23,10 @@
 #include <cub/block/block_reduce.cuh>
 
 #include <cstdio>
+#include <algorithm>
+#include <atomic>
 #include <mutex>
+#include <vector>
 
 #include "geom.cuh"
 #include "internal.cuh"
@@ -818,7 +821,7 @@ __device__ __forceinline__ void decode_contribution(const ContactsView& cv, int6
 // order and writes the value once.
 __global__ void k_assemble(ContactsView cv, const unsigned long long* __restrict__ ukeys,
     const int* __restrict__ run_start, const int* __restrict__ run_len, const int* __restrict__ contrib,
-    const double* __restrict__ Hs, const int* __restrict__ bptr, int nb, double* __restrict__ val)
+    const double* __restrict__ Hs, const int* __restrict__ bptr, int r0, int64_t B0, int nb, double* __restrict__ val)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 9 * (int64_t)nb) return;
@@ -833,10 +836,10 @@ __global__ void k_assemble(ContactsView cv, const unsigned long long* __restrict
         sum += Hs[144 * i + (3 * a + k) * N + 3 * b + l];
     }
     const unsigned long long key = ukeys[q];
-    const int r = (int)(key >> 32);
-    const int b0 = bptr[r];
-    const int64_t nbr = bptr[r + 1] - b0;
-    val[9 * (int64_t)b0 + 3 * (int64_t)(q - b0) + 3 * k * nbr + l] = sum;
+    const int j = (int)(key >> 32) - r0;
+    const int b0 = bptr[j];
+    const int64_t nbr = bptr[j + 1] - b0;
+    val[9 * (B0 + b0) + 3 * (int64_t)(q - b0) + 3 * k * nbr + l] = sum;
 }
 
 __global__ void k_block_keys(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
@@ -859,43 +862,144 @@ __global__ void k_block_keys(ContactsView cv, const int* __restrict__ E, const i
             }
 }
 
-__global__ void k_block_rowptr(const unsigned long long* __restrict__ ukeys, const int* __restrict__ d_nb, int nV,
-    int* __restrict__ bptr, long long ucap, Guard gd)
+// Block row pointers of rows r0 .. r0 + nr (local to this chunk's blocks).
+__global__ void k_block_rowptr(const unsigned long long* __restrict__ ukeys, const int* __restrict__ d_nb, int r0,
+    int nr, int* __restrict__ bptr, long long ucap, Guard gd)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r > nV) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > nr) return;
     const int nb = *d_nb;
-    if (!in_range(gd, 7, nb, ucap + 1, r)) return;
-    bptr[r] = lower_bound_u64(ukeys, 0, nb, (unsigned long long)r << 32);
+    if (!in_range(gd, 7, nb, ucap + 1, j)) return;
+    bptr[j] = lower_bound_u64(ukeys, 0, nb, (unsigned long long)(r0 + j) << 32);
 }
 
-__global__ void k_csr_rows(const int* __restrict__ bptr, int nV, int64_t* __restrict__ row_ptr)
+// CSR row pointers of the 3 nr scalar rows starting at 3 r0; B0 blocks of
+// earlier chunks come first in the value arrays.
+__global__ void k_csr_rows(const int* __restrict__ bptr, int r0, int nr, int64_t B0, int64_t* __restrict__ row_ptr)
 {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r > nV) return;
-    const int64_t b0 = bptr[r];
-    if (r == nV) {
-        row_ptr[3 * (int64_t)nV] = 9 * b0;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > nr) return;
+    const int64_t b0 = B0 + bptr[j];
+    const int64_t r = r0 + (int64_t)j;
+    if (j == nr) {
+        row_ptr[3 * r] = 9 * b0;
         return;
     }
-    const int64_t nbr = bptr[r + 1] - b0;
-    for (int k = 0; k < 3; ++k) row_ptr[3 * (int64_t)r + k] = 9 * b0 + 3 * k * nbr;
+    const int64_t nbr = bptr[j + 1] - bptr[j];
+    for (int k = 0; k < 3; ++k) row_ptr[3 * r + k] = 9 * b0 + 3 * k * nbr;
 }
 
 __global__ void k_csr_cols(const unsigned long long* __restrict__ ukeys, int nb, const int* __restrict__ bptr,
-    int* __restrict__ col, int nV, Guard gd)
+    int r0, int nr, int64_t B0, int* __restrict__ col, Guard gd)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nb) return;
     const unsigned long long key = ukeys[q];
-    const int r = (int)(key >> 32), cc = (int)(key & 0xffffffffu);
-    if (!in_range(gd, 8, r, nV, q)) return;
-    const int b0 = bptr[r];
-    const int64_t nbr = bptr[r + 1] - b0;
+    const int j = (int)(key >> 32) - r0, cc = (int)(key & 0xffffffffu);
+    if (!in_range(gd, 8, j, nr, q)) return;
+    const int b0 = bptr[j];
+    const int64_t nbr = bptr[j + 1] - b0;
     const int64_t base = 9 * (int64_t)b0 + 3 * (int64_t)(q - b0);
     for (int k = 0; k < 3; ++k)
         for (int l = 0; l < 3; ++l)
-            if (in_range(gd, 9, base + 3 * k * nbr + l, 9LL * nb, q)) col[base + 3 * k * nbr + l] = 3 * cc + l;
+            if (in_range(gd, 9, base + 3 * k * nbr + l, 9LL * nb, q)) col[9 * B0 + base + 3 * k * nbr + l] = 3 * cc + l;
+}
+
+// Contact range of every scene boundary in each type list: lists are sorted
+// by their first index (vertex, edge, edge, face) and edges and faces are
+// numbered scene by scene, so scene k's contacts of a type are contiguous.
+__global__ void k_scene_ranges(ContactsView cv, const int64_t* __restrict__ offs, int S, int64_t* __restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * S) return;
+    const int type = t / S;
+    const int2* list = type == 0 ? cv.vv : (type == 1 ? cv.ev : (type == 2 ? cv.ee : cv.fv));
+    const int64_t n = type == 0 ? cv.nvv : (type == 1 ? cv.nev : (type == 2 ? cv.nee : cv.nfv));
+    const int64_t key = offs[t];
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (list[mid].x < key) lo = mid + 1;
+        else hi = mid;
+    }
+    out[t] = lo;
+}
+
+// A run of consecutive scenes whose Hessian is assembled together: contacts
+// [lo[t], hi[t]) of each type t touch only rows of vertices [r0, r1).
+struct Chunk {
+    int64_t lo[4], hi[4];
+    int64_t r0, r1;
+    int64_t size() const { return (hi[0] - lo[0]) + (hi[1] - lo[1]) + (hi[2] - lo[2]) + (hi[3] - lo[3]); }
+};
+
+} // namespace
+
+// Contacts per Hessian chunk of a batch: bounds the 1152-byte-per-contact
+// local-Hessian scratch (4.8 GB at the default 2^22) however large the batch.
+std::atomic<int64_t> g_hess_chunk_contacts { int64_t(1) << 22 };
+
+namespace {
+
+ContactsView sub_view(const ContactsView& cv, const Chunk& c)
+{
+    ContactsView v = cv;
+    v.nvv = c.hi[0] - c.lo[0];
+    v.nev = c.hi[1] - c.lo[1];
+    v.nee = c.hi[2] - c.lo[2];
+    v.nfv = c.hi[3] - c.lo[3];
+    v.vv = cv.vv + c.lo[0];
+    v.vv_w = cv.vv_w + c.lo[0];
+    v.ev = cv.ev + c.lo[1];
+    v.ev_w = cv.ev_w + c.lo[1];
+    v.ee = cv.ee + c.lo[2];
+    v.ee_w = cv.ee_w + c.lo[2];
+    v.ee_eps = cv.ee_eps + c.lo[2];
+    v.ee_dt = cv.ee_dt + c.lo[2];
+    v.fv = cv.fv + c.lo[3];
+    v.fv_w = cv.fv_w + c.lo[3];
+    return v;
+}
+
+// One chunk per run of scenes holding at most g_hess_chunk_contacts contacts (a
+// single chunk for one scene, a small batch, or a set loaded from outside).
+std::vector<Chunk> plan_chunks(const ipcg_collisions* cs, ipcg_mesh* m, const ContactsView& cv)
+{
+    const int64_t n = cs->size();
+    Chunk all { { 0, 0, 0, 0 }, { cs->nvv, cs->nev, cs->nee, cs->nfv }, 0, m->nV };
+    const int64_t ns = m->n_scenes;
+    const int64_t budget = g_hess_chunk_contacts.load();
+    if (ns <= 1 || !cs->sorted || n <= budget) return { all };
+    const int S = (int)(ns + 1);
+    cudaStream_t s = m->stream;
+    DBuf<int64_t> d_out;
+    d_out.reserve(4 * S);
+    IPCG_LAUNCH("k_scene_ranges", s, k_scene_ranges<<<grid_for(4 * S, 256), 256, 0, s>>>(cv, m->scene_offs.p, S,
+        d_out.p));
+    std::vector<int64_t> h(4 * S);
+    IPCG_CUDA(cudaMemcpyAsync(h.data(), d_out.p, sizeof(int64_t) * 4 * S, cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    std::vector<Chunk> out;
+    int64_t k0 = 0;
+    while (k0 < ns) {
+        int64_t k1 = k0 + 1;
+        auto count = [&](int64_t a, int64_t b) {
+            int64_t c = 0;
+            for (int t = 0; t < 4; ++t) c += h[t * S + b] - h[t * S + a];
+            return c;
+        };
+        while (k1 < ns && count(k0, k1 + 1) <= budget) ++k1;
+        Chunk c;
+        for (int t = 0; t < 4; ++t) {
+            c.lo[t] = h[t * S + k0];
+            c.hi[t] = h[t * S + k1];
+        }
+        c.r0 = m->h_voff[k0];
+        c.r1 = m->h_voff[k1];
+        out.push_back(c);
+        k0 = k1;
+    }
+    return out;
 }
 
 } // namespace
@@ -953,13 +1057,22 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     if (hess) {
         hess->rows = 3 * nV;
         hess->stream = s;
-        const int64_t nk = 4 * cs->nvv + 9 * cs->nev + 16 * (cs->nee + cs->nfv);
-        m->keys_a.reserve(nk + 1);
-        m->keys_b.reserve(nk + 1);
-        m->ivals_a.reserve(nk + nV + 2);
-        m->ivals_b.reserve(3 * nk + 3);
-        m->hs.reserve(144 * (n + 1));
-        m->proj.reserve(n + 1);
+        const std::vector<Chunk> chunks = plan_chunks(cs, m, cv);
+        int64_t max_n = 0, max_nk = 0, max_nr = 0;
+        for (const Chunk& c : chunks) {
+            const int64_t nk = 4 * (c.hi[0] - c.lo[0]) + 9 * (c.hi[1] - c.lo[1])
+                + 16 * ((c.hi[2] - c.lo[2]) + (c.hi[3] - c.lo[3]));
+            max_n = std::max(max_n, c.size());
+            max_nk = std::max(max_nk, nk);
+            max_nr = std::max(max_nr, c.r1 - c.r0);
+        }
+        if (max_nk >= INT32_MAX) throw Error(IPCG_ERR_INVALID, "too many Hessian contributions in one scene");
+        m->keys_a.reserve(max_nk + 1);
+        m->keys_b.reserve(max_nk + 1);
+        m->ivals_a.reserve(max_nk + max_nr + 3);
+        m->ivals_b.reserve(3 * max_nk + 3);
+        m->hs.reserve(144 * (max_n + 1));
+        m->proj.reserve(max_n + 1);
         m->counters.reserve(16);
         int* d_nb = m->counters.p + 14;
         int* d_fail = m->counters.p + 15;
@@ -967,55 +1080,70 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         m->guard.reserve(4);
         IPCG_CUDA(cudaMemsetAsync(m->guard.p, 0, sizeof(long long) * 4, s));
         const Guard gd { m->guard.p };
-        int* ids_in = m->ivals_b.p;                  // contribution ids (unsorted)
-        int* contrib = m->ivals_b.p + (nk + 1);      // contribution ids sorted by block key
-        int* run_len = m->ivals_b.p + 2 * (nk + 1);  // contributions per block
-        int* run_start = m->ivals_a.p + (nV + 2);    // first contribution of each block
-        int* bptr = m->ivals_a.p;
-        int nb = 0;
-        if (n > 0) {
-            // local Hessians (FP64 work) and PSD projection into the scratch slabs
-            const int64_t first[4] = { 0, cs->nvv, cs->nvv + cs->nev, cs->nvv + cs->nev + cs->nee };
-            const int64_t count[4] = { cs->nvv, cs->nev, cs->nee, cs->nfv };
-            if (count[0])
-                IPCG_LAUNCH("k_local_hessian_vv", s, k_local_hessian<CT_VV><<<grid_for(count[0], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[0], count[0]));
-            if (count[1])
-                IPCG_LAUNCH("k_local_hessian_ev", s, k_local_hessian<CT_EV><<<grid_for(count[1], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[1], count[1]));
-            if (count[2])
-                IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[2], count[2]));
-            if (count[3])
-                IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], BLOCK), BLOCK, 0, s>>>(
-                    cv, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[3], count[3]));
-            if (a.psd != IPCG_PSD_NONE)
-                IPCG_LAUNCH("k_psd", s, k_psd<<<nblk, BLOCK, 0, s>>>(cv, m->hs.p, m->proj.p, a.psd, d_fail));
-            // sparsity pattern: sort (block key, contribution) and run-length encode
-            IPCG_LAUNCH("k_block_keys", s, k_block_keys<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, m->keys_a.p,
-                ids_in, nk, gd));
-            sort_pairs_u64(m, m->keys_a.p, m->keys_b.p, ids_in, contrib, (int)nk, 32 + bits_for(nV + 1));
-            rle_u64(m, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
-            IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, s));
-            IPCG_CUDA(cudaStreamSynchronize(s));
-            nb = m->h_counters.p[0];
-            exclusive_sum_i32(m, run_len, run_start, nb);
-        } else {
-            IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), s));
-        }
-        hess->nnz = 9 * (int64_t)nb;
         hess->row_ptr.reserve(3 * nV + 1);
-        hess->col.reserve(hess->nnz + 1);
-        hess->val.reserve(hess->nnz + 1);
-        IPCG_LAUNCH("k_block_rowptr", s, k_block_rowptr<<<grid_for(nV + 1, 256), 256, 0, s>>>(m->keys_a.p, d_nb,
-            (int)nV, bptr, nk, gd));
-        IPCG_LAUNCH("k_csr_rows", s, k_csr_rows<<<grid_for(nV + 1, 256), 256, 0, s>>>(bptr, (int)nV, hess->row_ptr.p));
-        if (nb > 0) {
-            IPCG_LAUNCH("k_csr_cols", s, k_csr_cols<<<grid_for(nb, 256), 256, 0, s>>>(m->keys_a.p, nb, bptr,
-                hess->col.p, (int)nV, gd));
-            IPCG_LAUNCH("k_assemble", s, k_assemble<<<grid_for(9 * (int64_t)nb, 256), 256, 0, s>>>(cv, m->keys_a.p,
-                run_start, run_len, contrib, m->hs.p, bptr, nb, hess->val.p));
+        int64_t B0 = 0, done = 0;
+        for (const Chunk& ch : chunks) {
+            const ContactsView cc = sub_view(cv, ch);
+            const int64_t nc = ch.size();
+            const int64_t nk = 4 * cc.nvv + 9 * cc.nev + 16 * (cc.nee + cc.nfv);
+            const int r0 = (int)ch.r0, nr = (int)(ch.r1 - ch.r0);
+            const int nblk_c = grid_for(nc, BLOCK);
+            int* ids_in = m->ivals_b.p;                  // contribution ids (unsorted)
+            int* contrib = m->ivals_b.p + (nk + 1);      // contribution ids sorted by block key
+            int* run_len = m->ivals_b.p + 2 * (nk + 1);  // contributions per block
+            int* bptr = m->ivals_a.p;                    // block row pointers of this chunk's rows
+            int* run_start = m->ivals_a.p + (nr + 2);    // first contribution of each block
+            int nb = 0;
+            if (nc > 0) {
+                // local Hessians (FP64 work) and PSD projection into the scratch slabs
+                const int64_t first[4] = { 0, cc.nvv, cc.nvv + cc.nev, cc.nvv + cc.nev + cc.nee };
+                const int64_t count[4] = { cc.nvv, cc.nev, cc.nee, cc.nfv };
+                if (count[0])
+                    IPCG_LAUNCH("k_local_hessian_vv", s, k_local_hessian<CT_VV><<<grid_for(count[0], BLOCK), BLOCK, 0,
+                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[0], count[0]));
+                if (count[1])
+                    IPCG_LAUNCH("k_local_hessian_ev", s, k_local_hessian<CT_EV><<<grid_for(count[1], BLOCK), BLOCK, 0,
+                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[1], count[1]));
+                if (count[2])
+                    IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], BLOCK), BLOCK, 0,
+                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[2], count[2]));
+                if (count[3])
+                    IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], BLOCK), BLOCK, 0,
+                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[3], count[3]));
+                if (a.psd != IPCG_PSD_NONE)
+                    IPCG_LAUNCH("k_psd", s, k_psd<<<nblk_c, BLOCK, 0, s>>>(cc, m->hs.p, m->proj.p, a.psd, d_fail));
+                // sparsity pattern: sort (block key, contribution) and run-length encode
+                IPCG_LAUNCH("k_block_keys", s, k_block_keys<<<nblk_c, BLOCK, 0, s>>>(cc, m->E.p, m->F.p,
+                    m->keys_a.p, ids_in, nk, gd));
+                sort_pairs_u64(m, m->keys_a.p, m->keys_b.p, ids_in, contrib, (int)nk, 32 + bits_for(nV + 1));
+                rle_u64(m, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
+                IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, s));
+                IPCG_CUDA(cudaStreamSynchronize(s));
+                nb = m->h_counters.p[0];
+                exclusive_sum_i32(m, run_len, run_start, nb);
+            } else {
+                IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), s));
+            }
+            // output arrays grow as chunks finish (the last chunk's estimate is exact)
+            done += nc;
+            const int64_t need = 9 * (B0 + nb);
+            const int64_t guess = done < n ? (int64_t)((double)need * (double)n / (double)std::max<int64_t>(done, 1))
+                                           : need;
+            hess->col.grow_keep(std::max(need, guess) + 1, 9 * B0, s);
+            hess->val.grow_keep(std::max(need, guess) + 1, 9 * B0, s);
+            IPCG_LAUNCH("k_block_rowptr", s, k_block_rowptr<<<grid_for(nr + 1, 256), 256, 0, s>>>(m->keys_a.p, d_nb,
+                r0, nr, bptr, nk, gd));
+            IPCG_LAUNCH("k_csr_rows", s, k_csr_rows<<<grid_for(nr + 1, 256), 256, 0, s>>>(bptr, r0, nr, B0,
+                hess->row_ptr.p));
+            if (nb > 0) {
+                IPCG_LAUNCH("k_csr_cols", s, k_csr_cols<<<grid_for(nb, 256), 256, 0, s>>>(m->keys_a.p, nb, bptr, r0,
+                    nr, B0, hess->col.p, gd));
+                IPCG_LAUNCH("k_assemble", s, k_assemble<<<grid_for(9 * (int64_t)nb, 256), 256, 0, s>>>(cc,
+                    m->keys_a.p, run_start, run_len, contrib, m->hs.p, bptr, r0, B0, nb, hess->val.p));
+            }
+            B0 += nb;
         }
+        hess->nnz = 9 * B0;
         IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p + 1, d_fail, sizeof(int), cudaMemcpyDeviceToHost, s));
         IPCG_CUDA(cudaMemcpyAsync(m->h_guard, m->guard.p, sizeof(long long) * 4, cudaMemcpyDeviceToHost, s));
     }

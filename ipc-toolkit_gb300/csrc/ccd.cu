@@ -14,16 +14,19 @@
 // / edge-edge co-planarity function F(t,u,v) is multilinear, so the box of
 // its image over a parameter box is the box of its 8 corner values; boxes
 // whose image misses [-eps-ms, eps+ms]^3 are discarded and the rest are
-// bisected, each time across the parameter along which the components
-// still straddling the separation box change most.  A box is accepted when
+// bisected (split_dim: a parameter whose halving discards a half, else time
+// unless the straddling components barely change across it, else the
+// parameter across which they change most).  A box is accepted when
 // every component is either inside the separation box or narrower than the
 // codomain tolerance (the union of Tight-Inclusion's two acceptance tests),
-// or when the box is below the domain tolerances.  The search is a
-// depth-first branch and bound on the earliest time (earlier time halves
-// first, boxes starting at or after the best accepted time pruned), which
-// returns the smallest lower time bound of an accepted box, so the result
-// does not depend on the tmax handed in by other candidates.  One thread per candidate; this file is compiled with
-// -fmad=false so every value matches the CPU oracle bit for bit.
+// or when the box is below the domain tolerances.  Boxes are totally ordered
+// (lower corner, then levels) and increase along every path of the box tree,
+// so the result -- the first accepted box in that order -- does not depend
+// on the walk.  Each thread walks best first with a small heap and walks the
+// subtree of any box the full heap cannot take depth first; the CPU oracle
+// walks best first with an unbounded heap and returns the same box.  One
+// thread per candidate; this file is compiled with -fmad=false so every
+// value matches the CPU oracle bit for bit.
 #include "geom.cuh"
 #include "internal.cuh"
 #include "profile.cuh"
@@ -32,7 +35,11 @@ namespace ipcg {
 
 namespace {
 
-constexpr int CCD_STACK = 128;
+// best-first heap per thread; a box the full heap cannot take has its
+// subtree walked depth first on a stack that a 3 x 60-level tree cannot
+// overflow (depth + 1 entries at most)
+constexpr int CCD_HEAP = 64;
+constexpr int CCD_STACK = 184;
 constexpr int BLOCK = 128;
 // boxes a query may examine in the first pass before it is deferred
 constexpr long long CCD_PASS1_BUDGET = 512;
@@ -48,6 +55,17 @@ struct CBox {
 };
 
 __device__ __forceinline__ double width_of(int lvl) { return ldexp(1.0, -lvl); }
+
+// Total order of boxes: lower corner (t, u, v), then levels.  Children come
+// after their parent.
+__device__ __forceinline__ bool box_before(const CBox& a, const CBox& b)
+{
+    for (int d = 0; d < 3; ++d)
+        if (a.lo[d] != b.lo[d]) return a.lo[d] < b.lo[d];
+    for (int d = 0; d < 3; ++d)
+        if (a.lvl[d] != b.lvl[d]) return a.lvl[d] < b.lvl[d];
+    return false;
+}
 
 __device__ __forceinline__ double F_comp(const Query& q, int c, double t, double u, double v)
 {
@@ -107,46 +125,136 @@ __device__ void domain_tol(const Query& q, double delta, double tol[3])
     }
 }
 
+// Corner values of F over a box (f[c][i][j][k] at (t_i, u_j, v_k)) and the
+// separation radius eps_c + ms of each component.
+struct Corners {
+    double f[3][2][2][2];
+    double r[3];
+};
+
 // Returns zero_in; sets box_in, the codomain widths cw[c], whether component
-// c lies inside [-eps-ms, eps+ms] (inside[c]) and the largest change of
-// component c between the two faces of the box across parameter d.
+// c lies inside [-eps-ms, eps+ms] (inside[c]), for the components that do
+// not the largest change of component c between the two faces of the box
+// across parameter d, and the corner values.  The vertex positions are
+// interpolated once per time (the same expression as F_comp, so the same
+// values), and the test stops at the first component that excludes the box.
 __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3],
-    double var[3][3], bool inside[3])
+    double var[3][3], bool inside[3], Corners& cc)
 {
     const double ts[2] = { b.lo[0], b.lo[0] + width_of(b.lvl[0]) };
     const double us[2] = { b.lo[1], b.lo[1] + width_of(b.lvl[1]) };
     const double vs[2] = { b.lo[2], b.lo[2] + width_of(b.lvl[2]) };
-    bool zin = true;
     box_in = true;
     for (int c = 0; c < 3; ++c) {
         double f[2][2][2];
-        double mn = __longlong_as_double(0x7ff0000000000000ULL), mx = -mn;
+        for (int i = 0; i < 2; ++i) {
+            double x[4];
+            for (int k = 0; k < 4; ++k) {
+                const double a = comp(q.s[k], c), e = comp(q.e[k], c);
+                x[k] = (e - a) * ts[i] + a;
+            }
+            if (q.vf) {
+                const double d21 = x[2] - x[1], d31 = x[3] - x[1];
+                for (int j = 0; j < 2; ++j)
+                    for (int k = 0; k < 2; ++k) f[i][j][k] = x[0] - (d21 * us[j] + d31 * vs[k] + x[1]);
+            } else {
+                const double d10 = x[1] - x[0], d32 = x[3] - x[2];
+                const double ea[2] = { d10 * us[0] + x[0], d10 * us[1] + x[0] };
+                const double eb[2] = { d32 * vs[0] + x[2], d32 * vs[1] + x[2] };
+                for (int j = 0; j < 2; ++j)
+                    for (int k = 0; k < 2; ++k) f[i][j][k] = ea[j] - eb[k];
+            }
+        }
+        double mn = f[0][0][0], mx = f[0][0][0];
         for (int i = 0; i < 2; ++i)
             for (int j = 0; j < 2; ++j)
                 for (int k = 0; k < 2; ++k) {
-                    f[i][j][k] = F_comp(q, c, ts[i], us[j], vs[k]);
                     mn = fmin(mn, f[i][j][k]);
                     mx = fmax(mx, f[i][j][k]);
                 }
-        var[c][0] = var[c][1] = var[c][2] = 0;
-        for (int j = 0; j < 2; ++j)
-            for (int k = 0; k < 2; ++k) {
-                var[c][0] = fmax(var[c][0], fabs(f[1][j][k] - f[0][j][k]));
-                var[c][1] = fmax(var[c][1], fabs(f[j][1][k] - f[j][0][k]));
-                var[c][2] = fmax(var[c][2], fabs(f[j][k][1] - f[j][k][0]));
-            }
         const double r = err[c] + ms;
-        if (mn > r || mx < -r) zin = false;
+        if (mn > r || mx < -r) return false;
         inside[c] = (mn >= -r && mx <= r);
-        if (!inside[c]) box_in = false;
         cw[c] = mx - mn;
+        cc.r[c] = r;
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) cc.f[c][i][j][k] = f[i][j][k];
+        var[c][0] = var[c][1] = var[c][2] = 0;
+        if (!inside[c]) {
+            box_in = false;
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) {
+                    var[c][0] = fmax(var[c][0], fabs(f[1][j][k] - f[0][j][k]));
+                    var[c][1] = fmax(var[c][1], fabs(f[j][1][k] - f[j][0][k]));
+                    var[c][2] = fmax(var[c][2], fabs(f[j][k][1] - f[j][k][0]));
+                }
+        }
     }
-    return zin;
+    return true;
 }
 
-// `shared_best` (may be null) is the earliest time of impact found so far by
-// any candidate; boxes starting at or after it cannot lower the final
-// minimum, so it is re-read every 64 boxes to prune.
+// Whether halving the box across parameter d leaves a half whose corner box
+// (the parent's corners, with the halving face's values taken as averages of
+// the two opposite corners -- exact for the multilinear F up to rounding)
+// misses the separation box in some component.  Only used to pick a split.
+__device__ bool split_excludes(const Corners& cc, int d)
+{
+    for (int half = 0; half < 2; ++half)
+        for (int c = 0; c < 3; ++c) {
+            double mn = __longlong_as_double(0x7ff0000000000000ULL), mx = -mn;
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    for (int k = 0; k < 2; ++k) {
+                        const int idx[3] = { i, j, k };
+                        double v = cc.f[c][i][j][k];
+                        if (idx[d] != half) {
+                            int o[3] = { i, j, k };
+                            o[d] = half;
+                            v = (v + cc.f[c][o[0]][o[1]][o[2]]) * 0.5;
+                        }
+                        mn = fmin(mn, v);
+                        mx = fmax(mx, v);
+                    }
+            if (mn > cc.r[c] || mx < -cc.r[c]) return true;
+        }
+    return false;
+}
+
+// Split parameter of a box that is neither discarded nor accepted:
+// (1) a parameter whose halving discards a half at once (the one across
+//     which the straddling components change most, if several);
+// (2) else time, if the straddling components' change across time is at
+//     least 1/16 of their largest change across any parameter: boxes are
+//     visited in order of their earliest time, so a time split defers its
+//     later half, while a u or v split leaves two boxes with the same
+//     earliest time to resolve (this keeps near-parallel edge pairs, whose
+//     root set is a whole segment, from being resolved point by point);
+// (3) else the parameter across which the straddling components change
+//     most.  Parameters at the depth limit are not split.
+__device__ int split_dim(const CBox& b, const double var[3][3], const bool inside[3], const Corners& cc)
+{
+    double vmax[3] = { 0, 0, 0 };
+    for (int c = 0; c < 3; ++c)
+        if (!inside[c])
+            for (int d = 0; d < 3; ++d) vmax[d] = fmax(vmax[d], var[c][d]);
+    int sd = -1;
+    double best = -1;
+    for (int d = 0; d < 3; ++d)
+        if (b.lvl[d] < 60 && vmax[d] > best && split_excludes(cc, d)) {
+            best = vmax[d];
+            sd = d;
+        }
+    if (sd >= 0) return sd;
+    if (b.lvl[0] < 60 && vmax[0] * 16.0 >= fmax(vmax[0], fmax(vmax[1], vmax[2]))) return 0;
+    for (int d = 0; d < 3; ++d)
+        if (b.lvl[d] < 60 && vmax[d] > best) {
+            best = vmax[d];
+            sd = d;
+        }
+    return sd;
+}
+
 // Search status: no root before tmax, a root box found, or the caller's box
 // budget ran out before the search finished (result unknown).
 enum : int { CCD_MISS = 0, CCD_HIT = 1, CCD_UNRESOLVED = 2 };
@@ -156,74 +264,159 @@ struct Budget {
     long long spent;
 };
 
-__device__ int root_finder(const Query& q, const double err[3], double ms, const double tol[3], double delta,
-    double tmax, long long max_itr, double& toi, double& out_tol, const unsigned long long* shared_best, Budget& bud)
-{
-    CBox st[CCD_STACK];
-    int sp = 0;
-    st[sp].lo[0] = st[sp].lo[1] = st[sp].lo[2] = 0;
-    st[sp].lvl[0] = st[sp].lvl[1] = st[sp].lvl[2] = 0;
-    ++sp;
-    double best = tmax;
-    bool found = false;
-    long long itr = 0;
-    // "unlimited" iterations are capped so that no query can run away; the
-    // cap falls back to the conservative earliest unresolved time
-    const long long cap = max_itr > 0 ? max_itr : (long long)100000000;
-    out_tol = 0;
-    double prune = tmax;
-    while (sp) {
-        if (shared_best && (itr & 63) == 0)
-            prune = fmin(prune, __longlong_as_double((long long)*(volatile const unsigned long long*)shared_best));
-        const CBox b = st[--sp];
-        if (b.lo[0] >= best || b.lo[0] >= prune) continue;
+struct BoxHeap {
+    CBox a[CCD_HEAP];
+    int n;
+    __device__ void push(const CBox& b)
+    {
+        int i = n++;
+        while (i > 0) {
+            const int p = (i - 1) >> 1;
+            if (!box_before(b, a[p])) break;
+            a[i] = a[p];
+            i = p;
+        }
+        a[i] = b;
+    }
+    __device__ CBox pop()
+    {
+        const CBox top = a[0];
+        const CBox last = a[--n];
+        int i = 0;
+        for (;;) {
+            int c = 2 * i + 1;
+            if (c >= n) break;
+            if (c + 1 < n && box_before(a[c + 1], a[c])) ++c;
+            if (!box_before(a[c], last)) break;
+            a[i] = a[c];
+            i = c;
+        }
+        if (n > 0) a[i] = last;
+        return top;
+    }
+};
+
+// One step of the search on box b: returns 0 (discarded or accepted), or 1
+// with the kept children in ch[0..nch).
+struct Search {
+    const Query& q;
+    const double* err;
+    double ms, delta;
+    const double* tol;
+    double tmax;    // boxes starting at or after it are skipped
+    CBox best;      // first accepted box so far (in box order)
+    bool found;
+    double out_tol;
+    long long itr, cap;
+    Budget& bud;
+    bool capped, unresolved;
+
+    __device__ bool skip(const CBox& b) const { return b.lo[0] >= tmax || (found && !box_before(b, best)); }
+
+    __device__ int step(const CBox& b, CBox ch[2], int& nch)
+    {
+        nch = 0;
         ++itr;
-        if (bud.limit > 0 && ++bud.spent > bud.limit) return CCD_UNRESOLVED;
+        if (bud.limit > 0 && ++bud.spent > bud.limit) {
+            unresolved = true;
+            return 0;
+        }
         bool box_in, inside[3];
         double cw[3], var[3][3];
-        if (!inclusion(q, b, err, ms, box_in, cw, var, inside)) continue;
+        Corners cc;
+        if (!inclusion(q, b, err, ms, box_in, cw, var, inside, cc)) return 0;
         const double w[3] = { width_of(b.lvl[0]), width_of(b.lvl[1]), width_of(b.lvl[2]) };
         const bool small_co = (inside[0] || cw[0] <= delta) && (inside[1] || cw[1] <= delta)
             && (inside[2] || cw[2] <= delta);
         const bool small_dom = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
         const bool too_deep = b.lvl[0] >= 60 && b.lvl[1] >= 60 && b.lvl[2] >= 60;
-        if (small_co || box_in || small_dom || too_deep || sp + 2 > CCD_STACK) {
-            best = b.lo[0];
+        if (small_co || box_in || small_dom || too_deep) {
+            best = b;
             found = true;
-            out_tol = fmax(out_tol, fmax(cw[0], fmax(cw[1], cw[2])));
-            continue;
+            out_tol = fmax(cw[0], fmax(cw[1], cw[2]));
+            return 0;
         }
         if (itr > cap) {
-            double t = b.lo[0];
-            for (int i = 0; i < sp; ++i) t = fmin(t, st[i].lo[0]);
-            best = fmin(best, t);
-            found = true;
-            out_tol = fmax(out_tol, fmax(cw[0], fmax(cw[1], cw[2])));
-            break;
+            capped = true;
+            out_tol = fmax(cw[0], fmax(cw[1], cw[2]));
+            return 0;
         }
-        // split the parameter across which the still-straddling components
-        // change most (parameters at the depth limit are not split)
-        int sd = -1;
-        double best_var = -1;
-        for (int d = 0; d < 3; ++d) {
-            double vd = 0;
-            for (int c = 0; c < 3; ++c)
-                if (!inside[c]) vd = fmax(vd, var[c][d]);
-            if (b.lvl[d] < 60 && vd > best_var) {
-                best_var = vd;
-                sd = d;
-            }
-        }
+        const int sd = split_dim(b, var, inside, cc);
         CBox lo = b, hi = b;
         lo.lvl[sd] = hi.lvl[sd] = (int8_t)(b.lvl[sd] + 1);
         hi.lo[sd] = b.lo[sd] + width_of(lo.lvl[sd]);
-        const bool keep_hi = !(q.vf && sd != 0 && hi.lo[1] + hi.lo[2] > 1.0);
-        const bool keep_lo = !(q.vf && sd != 0 && lo.lo[1] + lo.lo[2] > 1.0);
-        if (keep_hi) st[sp++] = hi;
-        if (keep_lo) st[sp++] = lo;
+        // VF: drop halves entirely outside u + v <= 1
+        if (!(q.vf && sd != 0 && hi.lo[1] + hi.lo[2] > 1.0)) ch[nch++] = hi;
+        if (!(q.vf && sd != 0 && lo.lo[1] + lo.lo[2] > 1.0)) ch[nch++] = lo;
+        return 1;
     }
-    if (found) toi = best;
-    return found ? CCD_HIT : CCD_MISS;
+};
+
+// `shared_best` (may be null) is the earliest time of impact found so far by
+// any candidate; boxes starting at or after it cannot lower the final
+// minimum, so it is re-read every 64 boxes to prune.
+__device__ int root_finder(const Query& q, const double err[3], double ms, const double tol[3], double delta,
+    double tmax, long long max_itr, double& toi, double& out_tol, const unsigned long long* shared_best, Budget& bud)
+{
+    // "unlimited" iterations are capped so that no query can run away; the
+    // cap falls back to the conservative earliest unresolved time
+    Search S { q, err, ms, delta, tol, tmax, CBox {}, false, 0.0, 0, max_itr > 0 ? max_itr : 100000000LL, bud, false,
+        false };
+    BoxHeap H;
+    H.n = 0;
+    CBox root;
+    root.lo[0] = root.lo[1] = root.lo[2] = 0;
+    root.lvl[0] = root.lvl[1] = root.lvl[2] = 0;
+    H.push(root);
+    CBox st[CCD_STACK];
+    double capped_t = tmax;
+    while (H.n > 0 && !S.capped && !S.unresolved) {
+        if (shared_best && (S.itr & 63) == 0)
+            S.tmax = fmin(S.tmax, __longlong_as_double((long long)*(volatile const unsigned long long*)shared_best));
+        const CBox b = H.pop();
+        if (S.skip(b)) break; // the heap's first box: every other one comes later
+        CBox ch[2];
+        int nch;
+        if (!S.step(b, ch, nch)) {
+            if (S.capped) capped_t = b.lo[0];
+            continue;
+        }
+        for (int c = 0; c < nch; ++c) {
+            if (H.n < CCD_HEAP) {
+                H.push(ch[c]);
+                continue;
+            }
+            // the heap is full: walk this child's subtree depth first
+            int sp = 0;
+            st[sp++] = ch[c];
+            while (sp > 0 && !S.capped && !S.unresolved) {
+                const CBox d = st[--sp];
+                if (S.skip(d)) continue;
+                CBox dc[2];
+                int ndc;
+                if (!S.step(d, dc, ndc)) {
+                    if (S.capped) capped_t = d.lo[0];
+                    continue;
+                }
+                for (int k = 0; k < ndc; ++k) st[sp++] = dc[k]; // the earlier (lower) half pops first
+            }
+            if (S.capped) {
+                for (int k = 0; k < sp; ++k) capped_t = fmin(capped_t, st[k].lo[0]);
+                break;
+            }
+        }
+    }
+    if (S.unresolved) return CCD_UNRESOLVED;
+    if (S.capped) {
+        // out of iterations: the earliest unresolved time bounds the root
+        for (int k = 0; k < H.n; ++k) capped_t = fmin(capped_t, H.a[k].lo[0]);
+        toi = S.found ? fmin(S.best.lo[0], capped_t) : capped_t;
+        out_tol = S.out_tol;
+        return CCD_HIT;
+    }
+    out_tol = S.found ? S.out_tol : 0;
+    if (S.found) toi = S.best.lo[0];
+    return S.found ? CCD_HIT : CCD_MISS;
 }
 
 __device__ int ti_ccd(const Query& q, double ms_in, double& toi, double tol_in, double tmax_in, long long max_itr,

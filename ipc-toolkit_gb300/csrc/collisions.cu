@@ -185,6 +185,7 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     c->n_cand_fv = n_fv;
     c->dmin = dmin[0];
     c->scene_dmin.assign(dmin, dmin + ns);
+    c->sorted = true;
     const int64_t nc = n_ee + n_fv;
     // raw records: at most one per candidate
     const int64_t cap = nc + 16;

@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <atomic>
 #include <vector>
 
 #include "../../include/ipcg.h"
@@ -40,6 +41,25 @@ template <typename T> struct DBuf {
         release();
         size_t c = n < 16 ? 16 : n + n / 4;
         IPCG_CUDA(cudaMalloc((void**)&p, c * sizeof(T)));
+        cap = c;
+    }
+    // Grow to at least n elements keeping the first `used` ones (stream-ordered copy).
+    void grow_keep(size_t n, size_t used, cudaStream_t s)
+    {
+        if (n <= cap && p) return;
+        const size_t c = n < 16 ? 16 : n + n / 4;
+        T* q = nullptr;
+        IPCG_CUDA(cudaMalloc((void**)&q, c * sizeof(T)));
+        if (used && p) {
+            cudaError_t e = cudaMemcpyAsync(q, p, used * sizeof(T), cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s); // the old buffer is freed next
+            if (e != cudaSuccess) {
+                cudaFree(q);
+                IPCG_CUDA(e);
+            }
+        }
+        release();
+        p = q;
         cap = c;
     }
     void release()
@@ -105,6 +125,7 @@ struct ipcg_mesh {
     int64_t nV = 0, nE = 0, nF = 0;
     int64_t n_scenes = 1;
     std::vector<int64_t> h_voff;     // vertex offsets of the scenes (n_scenes + 1)
+    ipcg::DBuf<int64_t> scene_offs;  // batches: vertex, edge, edge, face offsets (4 x (n_scenes + 1))
     ipcg::DBuf<int> vscene;          // per-vertex scene id (batches only)
     ipcg::DBuf<double> scene_r;      // per-scene inflation radius of the current build
     ipcg::DBuf<double> scene_off2;   // per-scene (dhat + dmin)^2 of the current build
@@ -140,6 +161,7 @@ struct ipcg_collisions {
     int64_t n_cand_ee = 0, n_cand_fv = 0;
     double dmin = 0;
     std::vector<double> scene_dmin;  // per scene (batches)
+    bool sorted = false;             // lists sorted by key (built here, not loaded)
     ipcg::DBuf<int2> vv, ev, ee, fv;
     ipcg::DBuf<double> vv_w, ev_w, ee_w, fv_w, ee_eps;
     ipcg::DBuf<int8_t> ee_dtype;
@@ -162,6 +184,9 @@ const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf);
 bool is_device_ptr(const void* p);
 
 inline SceneView scene_view(const ipcg_mesh* m) { return SceneView { (int)m->n_scenes, m->n_scenes > 1 ? m->vscene.p : nullptr }; }
+
+// barrier.cu: contacts per Hessian chunk of a batch (scratch memory bound)
+extern std::atomic<int64_t> g_hess_chunk_contacts;
 
 // broad_phase.cu
 void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind /*2 edges, 3 faces*/, const double* V0, const double* V1,

@@ -80,6 +80,7 @@ def _load():
         "ipcg_collisions_build_batch": (i32, [P, P, P, P, P]),
         "ipcg_barrier_batch": (i32, [P, P, P, P, P, i32, i32, P, P, PP]),
         "ipcg_collision_free_stepsize_batch": (i32, [P, P, P, P, d, i64, d, P, P]),
+        "ipcg_set_hessian_chunk_contacts": (i32, [i64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -146,6 +147,12 @@ def profile_report() -> dict:
     buf = C.create_string_buffer(need.value)
     _check(L.ipcg_profile_report(buf, need.value, C.byref(need)))
     return json.loads(buf.value.decode())
+
+
+def set_hessian_chunk_contacts(contacts: int = 0):
+    """Memory bound of batched Hessians: at most ``contacts`` local 12x12
+    blocks are held at once (0 = default 4,194,304).  Results do not change."""
+    _check(_load().ipcg_set_hessian_chunk_contacts(int(contacts)))
 
 
 def launch_count() -> int:

@@ -24,10 +24,11 @@ import numpy as np
 
 def edges_from_faces(F: np.ndarray) -> np.ndarray:
     """Unique undirected edges of a triangle mesh as sorted (min, max) pairs."""
-    e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]], axis=0)
+    e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]], axis=0).astype(np.int64)
     e = np.sort(e, axis=1)
-    e = np.unique(e, axis=0)
-    return np.ascontiguousarray(e.astype(np.int32))
+    n = int(e.max()) + 1 if e.size else 1
+    key = np.unique(e[:, 0] * n + e[:, 1])  # row order of np.unique(e, axis=0)
+    return np.ascontiguousarray(np.stack([key // n, key % n], axis=1).astype(np.int32))
 
 
 def grid_sheet(n: int, z: float = 0.0, size: float = 1.0):

@@ -40,6 +40,7 @@
 #include <numeric>
 #include <thread>
 #include <unordered_map>
+#include <queue>
 #include <vector>
 
 namespace orc {
@@ -1332,7 +1333,6 @@ static void contact_hessian(const BarrierParams& P, const Contact& c, const V3* 
 // Tight-Inclusion-style inclusion-based CCD (restated from the published
 // method) + IPC strategy (tight_inclusion_ccd.cpp:33-75).
 // ---------------------------------------------------------------------------
-static const int CCD_STACK = 128;
 static thread_local long long g_ccd_iters = 0; // boxes examined (diagnostics)
 
 struct CCDQuery {
@@ -1408,14 +1408,34 @@ struct CBox {
     int8_t lvl[3]; // width = 2^-lvl
 };
 
+// Total order of boxes: lower corner (t, u, v), then levels.  A child is
+// always after its parent (it keeps the parent's corner with one level more,
+// or moves the corner up), so the first accepted box in this order is the
+// same however the tree is walked.
+static inline bool cbox_before(const CBox& a, const CBox& b)
+{
+    for (int d = 0; d < 3; ++d)
+        if (a.lo[d] != b.lo[d]) return a.lo[d] < b.lo[d];
+    for (int d = 0; d < 3; ++d)
+        if (a.lvl[d] != b.lvl[d]) return a.lvl[d] < b.lvl[d];
+    return false;
+}
+
 static inline double cbox_w(const CBox& b, int d) { return std::ldexp(1.0, -b.lvl[d]); }
 
+// Corner values of F over a box: f[c][i][j][k] at (t_i, u_j, v_k), and the
+// separation radius eps_c + ms of each component.
+struct CCorners {
+    double f[3][2][2][2];
+    double r[3];
+};
+
 // Inclusion test.  Returns zero_in; sets box_in, the codomain widths cw[c],
-// whether component c lies inside [-eps-ms, eps+ms] (inside[c]) and the
+// whether component c lies inside [-eps-ms, eps+ms] (inside[c]), the
 // largest change of component c between the two faces of the box across
-// parameter d (var[c][d]).
+// parameter d (var[c][d]) and the corner values.
 static bool ccd_inclusion(const CCDQuery& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3],
-    double var[3][3], bool inside[3])
+    double var[3][3], bool inside[3], CCorners& cc)
 {
     const double ts[2] = { b.lo[0], b.lo[0] + cbox_w(b, 0) };
     const double us[2] = { b.lo[1], b.lo[1] + cbox_w(b, 1) };
@@ -1444,24 +1464,97 @@ static bool ccd_inclusion(const CCDQuery& q, const CBox& b, const double err[3],
         inside[c] = (mn >= -r && mx <= r);
         if (!inside[c]) box_in = false;
         cw[c] = mx - mn;
+        cc.r[c] = r;
+        for (int i = 0; i < 2; ++i)
+            for (int j = 0; j < 2; ++j)
+                for (int k = 0; k < 2; ++k) cc.f[c][i][j][k] = f[i][j][k];
     }
     return zin;
+}
+
+// Whether halving the box across parameter d leaves a half whose corner box
+// (the parent's corners, with the halving face's values taken as averages of
+// the two opposite corners -- exact for the multilinear F up to rounding)
+// misses the separation box in some component.  Only used to pick a split.
+static bool ccd_split_excludes(const CCorners& cc, int d)
+{
+    for (int half = 0; half < 2; ++half)
+        for (int c = 0; c < 3; ++c) {
+            double mn = std::numeric_limits<double>::infinity(), mx = -mn;
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    for (int k = 0; k < 2; ++k) {
+                        const int idx[3] = { i, j, k };
+                        double v = cc.f[c][i][j][k];
+                        if (idx[d] != half) {
+                            int o[3] = { i, j, k };
+                            o[d] = half;
+                            v = (v + cc.f[c][o[0]][o[1]][o[2]]) * 0.5;
+                        }
+                        mn = std::min(mn, v);
+                        mx = std::max(mx, v);
+                    }
+            if (mn > cc.r[c] || mx < -cc.r[c]) return true;
+        }
+    return false;
+}
+
+// Split parameter of a box that is neither discarded nor accepted:
+// (1) a parameter whose halving discards a half at once (the one across
+//     which the straddling components change most, if several);
+// (2) else time, if the straddling components' change across time is at
+//     least 1/16 of their largest change across any parameter: boxes are
+//     visited in order of their earliest time, so a time split defers its
+//     later half, while a u or v split leaves two boxes with the same
+//     earliest time to resolve (this keeps near-parallel edge pairs, whose
+//     root set is a whole segment, from being resolved point by point);
+// (3) else the parameter across which the straddling components change
+//     most.  Parameters at the depth limit are not split.
+static int ccd_split_dim(const CBox& b, const double var[3][3], const bool inside[3], const CCorners& cc)
+{
+    double vmax[3] = { 0, 0, 0 };
+    for (int c = 0; c < 3; ++c)
+        if (!inside[c])
+            for (int d = 0; d < 3; ++d) vmax[d] = std::max(vmax[d], var[c][d]);
+    int sd = -1;
+    double best = -1;
+    for (int d = 0; d < 3; ++d)
+        if (b.lvl[d] < 60 && ccd_split_excludes(cc, d) && vmax[d] > best) {
+            best = vmax[d];
+            sd = d;
+        }
+    if (sd >= 0) return sd;
+    if (b.lvl[0] < 60 && vmax[0] * 16.0 >= std::max(vmax[0], std::max(vmax[1], vmax[2]))) return 0;
+    for (int d = 0; d < 3; ++d)
+        if (b.lvl[d] < 60 && vmax[d] > best) {
+            best = vmax[d];
+            sd = d;
+        }
+    return sd;
 }
 
 // Earliest-time branch and bound over (t,u,v) in [0,1]^3.  A box is
 // accepted when every component of its function box is inside the
 // separation box or narrower than the codomain tolerance delta (the union of
 // Tight-Inclusion's "box inside the eps-box" and "codomain width below
-// delta" tests), or when it is below the domain tolerances; it is split
-// across the parameter along which the still-straddling components change
-// most.  Returns whether a root box was found before tmax; toi = the
+// delta" tests), or when it is below the domain tolerances; otherwise it is
+// halved across ccd_split_dim's parameter.  Returns whether a root box was found before tmax; toi = the
 // smallest lower time bound of an accepted box.
+//
+// The boxes form a fixed binary tree (a box's children depend only on the
+// box) whose boxes increase along every path in the order cbox_before, so
+// the result is the first accepted box in that order (toi = its lower time
+// bound, out_tol = its codomain width) whatever order the tree is walked in;
+// boxes starting at or after tmax are skipped.  Here the boxes are visited
+// best first, in that order, which examines the fewest boxes.  Only a query
+// that exceeds the iteration cap depends on the order: it returns the
+// earliest unresolved time, which in best-first order is the current box's.
 static bool ccd_root_finder(const CCDQuery& q, const double err[3], double ms, const double tol[3], double delta,
     double tmax, long max_itr, double& toi, double& out_tol)
 {
-    CBox st[CCD_STACK];
-    int sp = 0;
-    st[sp++] = CBox { { 0, 0, 0 }, { 0, 0, 0 } };
+    auto later = [](const CBox& a, const CBox& b) { return cbox_before(b, a); };
+    std::priority_queue<CBox, std::vector<CBox>, decltype(later)> pq(later);
+    pq.push(CBox { { 0, 0, 0 }, { 0, 0, 0 } });
     double best = tmax;
     bool found = false;
     // "unlimited" iterations are capped so that no query can run away; the
@@ -1469,15 +1562,17 @@ static bool ccd_root_finder(const CCDQuery& q, const double err[3], double ms, c
     const long cap = max_itr > 0 ? max_itr : (long)100000000;
     long itr = 0;
     out_tol = 0;
-    while (sp) {
-        const CBox b = st[--sp];
-        if (b.lo[0] >= best) continue;
+    while (!pq.empty()) {
+        const CBox b = pq.top();
+        pq.pop();
+        if (b.lo[0] >= best) break; // every remaining box starts later
         ++itr;
         ++g_ccd_iters;
         bool box_in;
         double cw[3], var[3][3];
         bool inside[3];
-        if (!ccd_inclusion(q, b, err, ms, box_in, cw, var, inside)) continue;
+        CCorners cc;
+        if (!ccd_inclusion(q, b, err, ms, box_in, cw, var, inside, cc)) continue;
         const double w[3] = { cbox_w(b, 0), cbox_w(b, 1), cbox_w(b, 2) };
         // every component of the function box is either inside the
         // [-eps-ms, eps+ms] box or narrower than the codomain tolerance
@@ -1485,45 +1580,28 @@ static bool ccd_root_finder(const CCDQuery& q, const double err[3], double ms, c
             && (inside[2] || cw[2] <= delta);
         const bool small_dom = w[0] <= tol[0] && w[1] <= tol[1] && w[2] <= tol[2];
         const bool too_deep = b.lvl[0] >= 60 && b.lvl[1] >= 60 && b.lvl[2] >= 60;
-        if (small_co || box_in || small_dom || too_deep || sp + 2 > CCD_STACK) {
+        if (small_co || box_in || small_dom || too_deep) {
             best = b.lo[0];
             found = true;
-            out_tol = std::max(out_tol, std::max(cw[0], std::max(cw[1], cw[2])));
-            continue;
+            out_tol = std::max(cw[0], std::max(cw[1], cw[2]));
+            break; // best first: every remaining box comes later
         }
         if (itr > cap) {
             // Out of iterations: the earliest unresolved time bounds the root.
-            double t = b.lo[0];
-            for (int i = 0; i < sp; ++i) t = std::min(t, st[i].lo[0]);
-            best = std::min(best, t);
+            best = b.lo[0];
             found = true;
-            out_tol = std::max(out_tol, std::max(cw[0], std::max(cw[1], cw[2])));
+            out_tol = std::max(cw[0], std::max(cw[1], cw[2]));
             break;
         }
-        // Split the parameter across which the components that still
-        // straddle the separation box change most: that halves the dominant
-        // term of their (multilinear) range.  Parameters already at the
-        // depth limit are not split.
-        int sd = -1;
-        double best_var = -1;
-        for (int d = 0; d < 3; ++d) {
-            double vd = 0;
-            for (int c = 0; c < 3; ++c)
-                if (!inside[c]) vd = std::max(vd, var[c][d]);
-            if (b.lvl[d] < 60 && vd > best_var) {
-                best_var = vd;
-                sd = d;
-            }
-        }
+        const int sd = ccd_split_dim(b, var, inside, cc);
         CBox lo = b, hi = b;
         lo.lvl[sd] = hi.lvl[sd] = (int8_t)(b.lvl[sd] + 1);
         hi.lo[sd] = b.lo[sd] + cbox_w(lo, sd);
         // VF: drop halves entirely outside u + v <= 1
         const bool keep_hi = !(q.vf && sd != 0 && hi.lo[1] + hi.lo[2] > 1.0);
         const bool keep_lo = !(q.vf && sd != 0 && lo.lo[1] + lo.lo[2] > 1.0);
-        // push the later / second half first so the earlier one pops first
-        if (keep_hi) st[sp++] = hi;
-        if (keep_lo) st[sp++] = lo;
+        if (keep_hi) pq.push(hi);
+        if (keep_lo) pq.push(lo);
     }
     if (found) toi = best;
     return found;

@@ -137,6 +137,24 @@ def test_batch_hessian_block_diagonal(batch_setup, ipctk, psd):
         assert sp.linalg.norm(sub - blk) <= REL * max(nrm, 1e-300), k
 
 
+def test_batch_hessian_chunked_assembly_is_identical(batch_setup, ipctk):
+    """Assembling the batch a few scenes at a time (a small chunk budget, so
+    that several chunks run and some scene alone exceeds the budget) gives
+    the same CSR arrays, bit for bit, as one pass over the whole batch."""
+    scs, batch, V, V1, dhat, kappa, dmin, col, singles = batch_setup
+    B = ipctk.BatchBarrierPotential(dhat, kappa)
+    H_one = B.hessian(col, batch, V, ipctk.PSDProjectionMethod.CLAMP)
+    try:
+        ipctk.set_hessian_chunk_contacts(1500)
+        H_chunked = B.hessian(col, batch, V, ipctk.PSDProjectionMethod.CLAMP)
+    finally:
+        ipctk.set_hessian_chunk_contacts(0)
+    assert max(len(c) for _, c in singles) > 1500
+    np.testing.assert_array_equal(H_chunked.indptr, H_one.indptr)
+    np.testing.assert_array_equal(H_chunked.indices, H_one.indices)
+    np.testing.assert_array_equal(H_chunked.data, H_one.data)
+
+
 def test_batch_stepsizes_equal_single_scenes(batch_setup, ipctk):
     scs, batch, V, V1, dhat, kappa, dmin, col, singles = batch_setup
     md = np.array([0.0, 0.0, 1e-4, 0.0, 0.0, 0.0])

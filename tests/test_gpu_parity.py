@@ -244,3 +244,25 @@ def test_point_triangle_ccd_cases(ipctk, oracle_mod):
             assert hit[i] or not exp
         else:
             assert bool(hit[i]) == exp
+
+
+@pytest.mark.parametrize("name", ["two_sheet_16", "spheres_27", "cloth_4x48"])
+def test_ccd_every_candidate_matches_oracle(built, ipctk, oracle_mod, name):
+    """Every swept-box candidate of a scene, queried alone (no pruning by
+    other candidates): the GPU's walk (bounded best-first heap, depth first
+    past it) must return the oracle's (unbounded best-first) hit and time of
+    impact exactly."""
+    sc, _, _, _ = built(name)
+    V0, V1, E, F = sc["V"], sc["V1"], sc["E"], sc["F"]
+    ee, fv = oracle_mod.ccd_candidates(V0, V1, E, F)
+    (xe0, xe1), (xf0, xf1) = oracle_mod.ccd_stencil_positions(V0, V1, E, F, ee, fv)
+    rng = np.random.default_rng(7)
+    ccd = ipctk.TightInclusionCCD()
+    for is_ee, x0, x1 in ((True, xe0, xe1), (False, xf0, xf1)):
+        if len(x0) > 4000:
+            idx = rng.choice(len(x0), 4000, replace=False)
+            x0, x1 = x0[idx], x1[idx]
+        hit, toi = ccd._batch(is_ee, x0, x1, 0.0, 1.0)
+        h_ref, t_ref, _ = oracle_mod.ccd_stencils(int(is_ee), x0, x1)
+        np.testing.assert_array_equal(hit, h_ref)
+        np.testing.assert_array_equal(toi[h_ref], t_ref[h_ref])
