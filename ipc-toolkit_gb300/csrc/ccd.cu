@@ -41,7 +41,11 @@ namespace {
 constexpr int CCD_HEAP = 64;
 constexpr int CCD_STACK = 184;
 constexpr int BLOCK = 128;
-// boxes a query may examine in the first pass before it is deferred
+// Two passes over the candidates.  Pass 1 runs every query with a small box
+// budget, pruned by the earliest time found so far (re-read as it runs); a
+// query that does not finish within the budget is deferred to the hard pass,
+// which starts it again with the then earliest time as its horizon and runs
+// it to completion.
 constexpr long long CCD_PASS1_BUDGET = 512;
 
 struct Query {
@@ -125,26 +129,57 @@ __device__ void domain_tol(const Query& q, double delta, double tol[3])
     }
 }
 
-// Corner values of F over a box (f[c][i][j][k] at (t_i, u_j, v_k)) and the
-// separation radius eps_c + ms of each component.
-struct Corners {
-    double f[3][2][2][2];
-    double r[3];
-};
+// Whether halving a box across parameter d leaves a half whose corner box
+// misses [-r, r], for one component with corner values f[i][j][k] at
+// (t_i, u_j, v_k): the halving face's values are taken as averages of the two
+// opposite corners (exact for the multilinear F up to rounding; the average
+// is the same for both halves because addition commutes).  Only used to pick
+// a split, and only called for components that straddle [-r, r] (a half of
+// a component inside it stays inside).
+__device__ __forceinline__ bool halving_excludes(const double f[2][2][2], int d, double r)
+{
+    const double inf = __longlong_as_double(0x7ff0000000000000ULL);
+    double lo0 = inf, hi0 = -inf, lo1 = inf, hi1 = -inf, lom = inf, him = -inf;
+    for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2; ++b) {
+            double f0, f1;
+            if (d == 0) {
+                f0 = f[0][a][b];
+                f1 = f[1][a][b];
+            } else if (d == 1) {
+                f0 = f[a][0][b];
+                f1 = f[a][1][b];
+            } else {
+                f0 = f[a][b][0];
+                f1 = f[a][b][1];
+            }
+            const double m = (f1 + f0) * 0.5;
+            lo0 = fmin(lo0, f0);
+            hi0 = fmax(hi0, f0);
+            lo1 = fmin(lo1, f1);
+            hi1 = fmax(hi1, f1);
+            lom = fmin(lom, m);
+            him = fmax(him, m);
+        }
+    const double a0 = fmin(lo0, lom), b0 = fmax(hi0, him), a1 = fmin(lo1, lom), b1 = fmax(hi1, him);
+    return a0 > r || b0 < -r || a1 > r || b1 < -r;
+}
 
 // Returns zero_in; sets box_in, the codomain widths cw[c], whether component
 // c lies inside [-eps-ms, eps+ms] (inside[c]), for the components that do
 // not the largest change of component c between the two faces of the box
-// across parameter d, and the corner values.  The vertex positions are
-// interpolated once per time (the same expression as F_comp, so the same
-// values), and the test stops at the first component that excludes the box.
+// across parameter d, and in excl (bit d) whether halving across d leaves a
+// half that some component excludes.  The vertex positions are interpolated
+// once per time (the same expression as F_comp, so the same values), and the
+// test stops at the first component that excludes the box.
 __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], double ms, bool& box_in, double cw[3],
-    double var[3][3], bool inside[3], Corners& cc)
+    double var[3][3], bool inside[3], int& excl)
 {
     const double ts[2] = { b.lo[0], b.lo[0] + width_of(b.lvl[0]) };
     const double us[2] = { b.lo[1], b.lo[1] + width_of(b.lvl[1]) };
     const double vs[2] = { b.lo[2], b.lo[2] + width_of(b.lvl[2]) };
     box_in = true;
+    excl = 0;
     for (int c = 0; c < 3; ++c) {
         double f[2][2][2];
         for (int i = 0; i < 2; ++i) {
@@ -176,13 +211,11 @@ __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], do
         if (mn > r || mx < -r) return false;
         inside[c] = (mn >= -r && mx <= r);
         cw[c] = mx - mn;
-        cc.r[c] = r;
-        for (int i = 0; i < 2; ++i)
-            for (int j = 0; j < 2; ++j)
-                for (int k = 0; k < 2; ++k) cc.f[c][i][j][k] = f[i][j][k];
         var[c][0] = var[c][1] = var[c][2] = 0;
         if (!inside[c]) {
             box_in = false;
+            for (int d = 0; d < 3; ++d)
+                if (!(excl >> d & 1) && halving_excludes(f, d, r)) excl |= 1 << d;
             for (int j = 0; j < 2; ++j)
                 for (int k = 0; k < 2; ++k) {
                     var[c][0] = fmax(var[c][0], fabs(f[1][j][k] - f[0][j][k]));
@@ -192,33 +225,6 @@ __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], do
         }
     }
     return true;
-}
-
-// Whether halving the box across parameter d leaves a half whose corner box
-// (the parent's corners, with the halving face's values taken as averages of
-// the two opposite corners -- exact for the multilinear F up to rounding)
-// misses the separation box in some component.  Only used to pick a split.
-__device__ bool split_excludes(const Corners& cc, int d)
-{
-    for (int half = 0; half < 2; ++half)
-        for (int c = 0; c < 3; ++c) {
-            double mn = __longlong_as_double(0x7ff0000000000000ULL), mx = -mn;
-            for (int i = 0; i < 2; ++i)
-                for (int j = 0; j < 2; ++j)
-                    for (int k = 0; k < 2; ++k) {
-                        const int idx[3] = { i, j, k };
-                        double v = cc.f[c][i][j][k];
-                        if (idx[d] != half) {
-                            int o[3] = { i, j, k };
-                            o[d] = half;
-                            v = (v + cc.f[c][o[0]][o[1]][o[2]]) * 0.5;
-                        }
-                        mn = fmin(mn, v);
-                        mx = fmax(mx, v);
-                    }
-            if (mn > cc.r[c] || mx < -cc.r[c]) return true;
-        }
-    return false;
 }
 
 // Split parameter of a box that is neither discarded nor accepted:
@@ -232,7 +238,7 @@ __device__ bool split_excludes(const Corners& cc, int d)
 //     root set is a whole segment, from being resolved point by point);
 // (3) else the parameter across which the straddling components change
 //     most.  Parameters at the depth limit are not split.
-__device__ int split_dim(const CBox& b, const double var[3][3], const bool inside[3], const Corners& cc)
+__device__ int split_dim(const CBox& b, const double var[3][3], const bool inside[3], int excl)
 {
     double vmax[3] = { 0, 0, 0 };
     for (int c = 0; c < 3; ++c)
@@ -241,7 +247,7 @@ __device__ int split_dim(const CBox& b, const double var[3][3], const bool insid
     int sd = -1;
     double best = -1;
     for (int d = 0; d < 3; ++d)
-        if (b.lvl[d] < 60 && vmax[d] > best && split_excludes(cc, d)) {
+        if (b.lvl[d] < 60 && vmax[d] > best && (excl >> d & 1)) {
             best = vmax[d];
             sd = d;
         }
@@ -323,8 +329,8 @@ struct Search {
         }
         bool box_in, inside[3];
         double cw[3], var[3][3];
-        Corners cc;
-        if (!inclusion(q, b, err, ms, box_in, cw, var, inside, cc)) return 0;
+        int excl;
+        if (!inclusion(q, b, err, ms, box_in, cw, var, inside, excl)) return 0;
         const double w[3] = { width_of(b.lvl[0]), width_of(b.lvl[1]), width_of(b.lvl[2]) };
         const bool small_co = (inside[0] || cw[0] <= delta) && (inside[1] || cw[1] <= delta)
             && (inside[2] || cw[2] <= delta);
@@ -341,7 +347,7 @@ struct Search {
             out_tol = fmax(cw[0], fmax(cw[1], cw[2]));
             return 0;
         }
-        const int sd = split_dim(b, var, inside, cc);
+        const int sd = split_dim(b, var, inside, excl);
         CBox lo = b, hi = b;
         lo.lvl[sd] = hi.lvl[sd] = (int8_t)(b.lvl[sd] + 1);
         hi.lo[sd] = b.lo[sd] + width_of(lo.lvl[sd]);
@@ -526,7 +532,7 @@ __device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_e
 // prunes them.  Each query's result does not depend on the pass, so the
 // minimum is the same as a single full pass.  In a batch each scene has its
 // own minimum distance and its own earliest time (toi_bits[scene]).
-__global__ void __launch_bounds__(BLOCK) k_ccd(const int2* __restrict__ cand_ee, int n_ee,
+__global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_ee, int n_ee,
     const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
     const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,
     CCDParams P, unsigned long long* toi_bits, long long budget, const int* __restrict__ list,
@@ -622,16 +628,15 @@ void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, c
     const double* md = m->scene_md.p + ns;
     const int nc = (int)(n_ee + n_fv);
     m->ivals_a.reserve(nc + 1);
-    int* hard = m->ivals_a.p;
+    int* hard = m->ivals_a.p; // deferred by pass 1
     int* hard_n = m->counters.p + 3;
     IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
-    // pass 1: every query with a small box budget; pass 2: the unresolved ones
-    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p + m->cand_cap,
-        (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard,
-        hard_n));
-    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(m->cand.p, (int)n_ee, m->cand.p +
-        m->cand_cap, (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr,
-        nullptr));
+    const int2* cee = m->cand.p;
+    const int2* cfv = m->cand.p + m->cand_cap;
+    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n));
+    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr));
     std::vector<unsigned long long> bits(ns);
     IPCG_CUDA(cudaMemcpyAsync(bits.data(), m->toi_bits.p, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost,
         s));
