@@ -158,6 +158,31 @@ template <typename T> std::vector<T> to_host(const T* src, size_t n)
 }
 } // namespace
 
+namespace ipcg {
+cudaMemPool_t device_pool()
+{
+    constexpr int MAXDEV = 64;
+    static std::mutex mu;
+    static cudaMemPool_t pools[MAXDEV] = {};
+    int dev = 0;
+    IPCG_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= MAXDEV) throw Error(IPCG_ERR_INVALID, "device index out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool;
+        IPCG_CUDA(cudaMemPoolCreate(&pool, &props));
+        uint64_t keep = UINT64_MAX; // keep freed memory for reuse
+        IPCG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        pools[dev] = pool;
+    }
+    return pools[dev];
+}
+} // namespace ipcg
+
 extern "C" {
 
 const char* ipcg_last_error(void) { return g_last_error.c_str(); }

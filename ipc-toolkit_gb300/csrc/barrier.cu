@@ -23,6 +23,7 @@
 #include <cub/block/block_reduce.cuh>
 
 #include <cstdio>
+#include <cstring>
 #include <algorithm>
 #include <atomic>
 #include <mutex>
@@ -389,25 +390,38 @@ __device__ double mollifier(const Local& c, const V3* x, double* gm, double* Hm,
     return m;
 }
 
-// ---- symmetric eigendecomposition (n <= 9): Householder + implicit QR ----
+// ---- PSD projection (eigen_ext.tpp:64-108) -------------------------------
+// The local Hessian annihilates rigid translations (per coordinate its rows
+// sum to zero over the stencil's vertices), so it is projected in the
+// 3(n-1)-dimensional translation-free subspace spanned by orthonormal vertex
+// contrasts: M = C H C^T (at most 9 x 9), and H+ = H - f sum_{lam<0} lam w w^T
+// with w = C^T q over the negative eigenpairs (lam, q) of M (f = 1 to clamp,
+// 2 for the absolute value).  M = Q_h T Q_h^T (Householder), T = G D G^T
+// (implicit QL with Wilkinson shifts, G = G_1 ... G_R plane rotations).
+// Only the negative eigenvectors are formed: q_i = Q_h G_1 ... G_R e_i,
+// replaying the recorded rotations on e_i, which costs a few hundred flops
+// per vector instead of updating all of Q at every rotation.
 constexpr int MAXR = 9;
+constexpr int MAXROT = 256; // recorded rotations; beyond, Q is accumulated
 
-__device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* d, double* Q)
+__device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* d, double* Q, double* rc, double* rs,
+    int8_t* rk, int& nrot, double* hv, double* htau)
 {
+    // Householder tridiagonalisation; reflector k kept in hv[k*MAXR + .], htau[k]
     double e[MAXR];
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) Q[i * MAXR + j] = (i == j) ? 1.0 : 0.0;
     for (int k = 0; k + 2 < n; ++k) {
         double sig = 0;
         for (int i = k + 2; i < n; ++i) sig += A[i * MAXR + k] * A[i * MAXR + k];
         const double x0 = A[(k + 1) * MAXR + k];
+        htau[k] = 0;
         if (sig == 0) {
             e[k] = x0;
             continue;
         }
         const double nx = sqrt(x0 * x0 + sig);
         const double alpha = (x0 >= 0) ? -nx : nx;
-        double v[MAXR], p[MAXR];
+        double* v = hv + k * MAXR;
+        double p[MAXR];
         v[k + 1] = x0 - alpha;
         for (int i = k + 2; i < n; ++i) v[i] = A[i * MAXR + k];
         const double tau = 2.0 / (v[k + 1] * v[k + 1] + sig);
@@ -423,16 +437,13 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
         for (int i = k + 1; i < n; ++i)
             for (int j = k + 1; j < n; ++j) A[i * MAXR + j] -= v[i] * p[j] + p[i] * v[j];
         e[k] = alpha;
-        for (int r = 0; r < n; ++r) {
-            double s = 0;
-            for (int j = k + 1; j < n; ++j) s += Q[r * MAXR + j] * v[j];
-            s *= tau;
-            for (int j = k + 1; j < n; ++j) Q[r * MAXR + j] -= s * v[j];
-        }
+        htau[k] = tau;
     }
     if (n >= 2) e[n - 2] = A[(n - 1) * MAXR + n - 2];
     e[n - 1] = 0;
     for (int i = 0; i < n; ++i) d[i] = A[i * MAXR + i];
+    nrot = 0;
+    bool record = true; // false once MAXROT is exceeded: then Q holds G
     const double eps = 2.220446049250313e-16;
     int end = n - 1, iter = 0;
     while (end > 0) {
@@ -443,6 +454,23 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
         if (++iter > 40 * n) return false;
         int start = end - 1;
         while (start > 0 && e[start - 1] != 0) --start;
+        if (record && nrot + (end - start) > MAXROT) {
+            // too many rotations to record: form G from those so far and
+            // accumulate the rest into it
+            for (int i = 0; i < n; ++i)
+                for (int j = 0; j < n; ++j) Q[i * MAXR + j] = (i == j) ? 1.0 : 0.0;
+            for (int r = 0; r < nrot; ++r) {
+                const int k = rk[r];
+                const double c = rc[r], s = rs[r];
+                for (int q = 0; q < n; ++q) {
+                    const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
+                    Q[q * MAXR + k] = c * qa - s * qb;
+                    Q[q * MAXR + k + 1] = s * qa + c * qb;
+                }
+            }
+            record = false;
+            nrot = -1;
+        }
         const double td = 0.5 * (d[end - 1] - d[end]);
         const double b = e[end - 1];
         double mu = d[end];
@@ -469,29 +497,110 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
                 e[k + 1] = c * e[k + 1];
             }
             x = e[k];
-            for (int q = 0; q < n; ++q) {
-                const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
-                Q[q * MAXR + k] = c * qa - s * qb;
-                Q[q * MAXR + k + 1] = s * qa + c * qb;
+            if (record) {
+                rc[nrot] = c;
+                rs[nrot] = s;
+                rk[nrot] = (int8_t)k;
+                ++nrot;
+            } else {
+                for (int q = 0; q < n; ++q) {
+                    const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
+                    Q[q * MAXR + k] = c * qa - s * qb;
+                    Q[q * MAXR + k + 1] = s * qa + c * qb;
+                }
             }
         }
     }
     return true;
 }
 
-// Orthonormal contrasts (rows orthogonal to (1,..,1)) for n = 2, 3, 4.
-__device__ __forceinline__ double contrast(int n, int k, int a)
+// Eigenvector i of M: Q_h G e_i.  G e_i comes from the recorded rotations
+// (applied last first) or, if they were not recorded (nrot < 0), from
+// column i of Q; then the Householder reflectors, H_{n-3} first.
+__device__ void eigvec(int n, int i, const double* Q, const double* rc, const double* rs, const int8_t* rk, int nrot,
+    const double* hv, const double* htau, double* y)
 {
-    if (n == 4) {
-        const int s[3][4] = { { 1, -1, 1, -1 }, { 1, 1, -1, -1 }, { 1, -1, -1, 1 } };
-        return 0.5 * s[k][a];
+    if (nrot >= 0) {
+        for (int q = 0; q < n; ++q) y[q] = (q == i) ? 1.0 : 0.0;
+        for (int r = nrot - 1; r >= 0; --r) {
+            const int k = rk[r];
+            const double c = rc[r], s = rs[r];
+            const double ya = y[k], yb = y[k + 1];
+            y[k] = c * ya + s * yb;
+            y[k + 1] = c * yb - s * ya;
+        }
+    } else {
+        for (int q = 0; q < n; ++q) y[q] = Q[q * MAXR + i];
     }
-    if (n == 3) {
-        const double r2 = 0.70710678118654752440, r6 = 0.40824829046386301637;
-        const double c[2][3] = { { r2, -r2, 0.0 }, { r6, r6, -2 * r6 } };
-        return c[k][a];
+    for (int k = n - 3; k >= 0; --k) {
+        if (htau[k] == 0) continue;
+        const double* v = hv + k * MAXR;
+        double s = 0;
+        for (int q = k + 1; q < n; ++q) s += v[q] * y[q];
+        s *= htau[k];
+        for (int q = k + 1; q < n; ++q) y[q] -= s * v[q];
     }
-    return a == 0 ? 0.70710678118654752440 : -0.70710678118654752440;
+}
+
+// Orthonormal contrasts (rows orthogonal to (1,..,1)) for NS = 2, 3, 4
+// stencil vertices: C[k][a], k < NS - 1 (compile-time constants).
+template <int NS> __device__ __forceinline__ constexpr double contrast(int k, int a)
+{
+    return NS == 4 ? 0.5 * ((k == 0 ? (a & 1) : k == 1 ? (a >> 1) : ((a ^ (a >> 1)) & 1)) ? -1.0 : 1.0)
+        : NS == 3 ? (k == 0 ? (a == 0 ? 0.70710678118654752440 : a == 1 ? -0.70710678118654752440 : 0.0)
+                            : (a == 2 ? -0.81649658092772603273 : 0.40824829046386301637))
+                  : (a == 0 ? 0.70710678118654752440 : -0.70710678118654752440);
+}
+
+// M = C H C^T (rows of M with stride MAXR), H row-major N x N.
+template <int NS> __device__ void to_contrasts(const double* H, double* M)
+{
+    constexpr int N = 3 * NS, m = 3 * (NS - 1);
+    double T[m * N];
+#pragma unroll 1
+    for (int j = 0; j < N; ++j) {
+        double col[N];
+#pragma unroll
+        for (int r = 0; r < N; ++r) col[r] = H[r * N + j];
+#pragma unroll
+        for (int k = 0; k < NS - 1; ++k)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                double s = 0;
+#pragma unroll
+                for (int a = 0; a < NS; ++a) s += contrast<NS>(k, a) * col[3 * a + c];
+                T[(3 * k + c) * N + j] = s;
+            }
+    }
+#pragma unroll 1
+    for (int r = 0; r < m; ++r) {
+        double row[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) row[j] = T[r * N + j];
+#pragma unroll
+        for (int l = 0; l < NS - 1; ++l)
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                double s = 0;
+#pragma unroll
+                for (int b = 0; b < NS; ++b) s += contrast<NS>(l, b) * row[3 * b + e];
+                M[r * MAXR + 3 * l + e] = s;
+            }
+    }
+}
+
+// w = C^T q (length 3 NS) for a length-3(NS-1) vector q.
+template <int NS> __device__ __forceinline__ void from_contrasts(const double* q, double* w)
+{
+#pragma unroll
+    for (int a = 0; a < NS; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            double s = 0;
+#pragma unroll
+            for (int k = 0; k < NS - 1; ++k) s += contrast<NS>(k, a) * q[3 * k + c];
+            w[3 * a + c] = s;
+        }
 }
 
 // In-place PSD projection of the 3n×3n local Hessian (row-major, N = 3n).
@@ -500,42 +609,33 @@ __device__ bool project_psd(int n, double* H, int method)
 {
     if (method == IPCG_PSD_NONE) return true;
     const int N = 3 * n, m = 3 * (n - 1);
-    double T[MAXR * 12];
-    for (int k = 0; k < n - 1; ++k)
-        for (int c = 0; c < 3; ++c)
-            for (int j = 0; j < N; ++j) {
-                double s = 0;
-                for (int a = 0; a < n; ++a) s += contrast(n, k, a) * H[(3 * a + c) * N + j];
-                T[(3 * k + c) * 12 + j] = s;
-            }
     double M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
-    for (int r = 0; r < m; ++r)
-        for (int l = 0; l < n - 1; ++l)
-            for (int e = 0; e < 3; ++e) {
-                double s = 0;
-                for (int b = 0; b < n; ++b) s += contrast(n, l, b) * T[r * 12 + 3 * b + e];
-                M[r * MAXR + 3 * l + e] = s;
-            }
+    if (n == 4) to_contrasts<4>(H, M);
+    else if (n == 3) to_contrasts<3>(H, M);
+    else to_contrasts<2>(H, M);
     // symmetrise (rounding)
     for (int r = 0; r < m; ++r)
         for (int s = r + 1; s < m; ++s) {
             const double avg = 0.5 * (M[r * MAXR + s] + M[s * MAXR + r]);
             M[r * MAXR + s] = M[s * MAXR + r] = avg;
         }
-    if (!sym_eig(m, M, lam, Q)) return false;
+    double rc[MAXROT], rs[MAXROT], hv[MAXR * MAXR], htau[MAXR];
+    int8_t rk[MAXROT];
+    int nrot;
+    if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, hv, htau)) return false;
     const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
     for (int i = 0; i < m; ++i) {
         if (!(lam[i] < 0)) continue;
-        double v[12];
-        for (int a = 0; a < n; ++a)
-            for (int c = 0; c < 3; ++c) {
-                double s = 0;
-                for (int k = 0; k < n - 1; ++k) s += contrast(n, k, a) * Q[(3 * k + c) * MAXR + i];
-                v[3 * a + c] = s;
-            }
+        double q[MAXR], v[12];
+        eigvec(m, i, Q, rc, rs, rk, nrot, hv, htau, q);
+        if (n == 4) from_contrasts<4>(q, v);
+        else if (n == 3) from_contrasts<3>(q, v);
+        else from_contrasts<2>(q, v);
         const double sl = f * lam[i];
-        for (int r = 0; r < N; ++r)
-            for (int s = 0; s < N; ++s) H[r * N + s] -= sl * v[r] * v[s];
+        for (int r = 0; r < N; ++r) {
+            const double svr = sl * v[r];
+            for (int s = 0; s < N; ++s) H[r * N + s] -= svr * v[s];
+        }
     }
     return true;
 }
@@ -1021,9 +1121,15 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         const double xh = (2 * dm + dh) * dh;
         hp[k] = Params { kap, dm * dm, xh, a.physical ? dh / (xh * xh) : 1.0, a.psd };
     }
-    m->params_buf.reserve(sizeof(Params) * ns);
+    // uploaded only when they change (a Newton loop repeats them)
+    const size_t pbytes = sizeof(Params) * ns;
+    const unsigned char* hb = reinterpret_cast<const unsigned char*>(hp.data());
+    if (m->params_host.size() != pbytes || memcmp(m->params_host.data(), hb, pbytes) != 0) {
+        m->params_buf.reserve(pbytes);
+        IPCG_CUDA(cudaMemcpyAsync(m->params_buf.p, hb, pbytes, cudaMemcpyHostToDevice, s));
+        m->params_host.assign(hb, hb + pbytes);
+    }
     const Params* sp = reinterpret_cast<const Params*>(m->params_buf.p);
-    IPCG_CUDA(cudaMemcpyAsync(m->params_buf.p, hp.data(), sizeof(Params) * ns, cudaMemcpyHostToDevice, s));
     const Params P = hp[0];
     const SceneView sv = scene_view(m);
     const int nblk = grid_for(n, BLOCK);
@@ -1080,7 +1186,7 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         m->guard.reserve(4);
         IPCG_CUDA(cudaMemsetAsync(m->guard.p, 0, sizeof(long long) * 4, s));
         const Guard gd { m->guard.p };
-        hess->row_ptr.reserve(3 * nV + 1);
+        hess->row_ptr.reserve(3 * nV + 1, s);
         int64_t B0 = 0, done = 0;
         for (const Chunk& ch : chunks) {
             const ContactsView cc = sub_view(cv, ch);

@@ -71,6 +71,43 @@ template <typename T> struct DBuf {
     ~DBuf() { release(); }
 };
 
+// The library's stream-ordered memory pool on the current device (memory is
+// kept in the pool when freed, so per-call outputs are reused without
+// cudaMalloc / cudaFree and the device synchronisation cudaFree implies).
+cudaMemPool_t device_pool();
+
+// Device buffer from device_pool(), allocated and freed in stream order;
+// used for per-call outputs handed to the caller.
+template <typename T> struct PBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaStream_t s = nullptr;
+    PBuf() = default;
+    PBuf(const PBuf&) = delete;
+    PBuf& operator=(const PBuf&) = delete;
+    // Grow to at least n elements keeping the first `used` ones.
+    void grow_keep(size_t n, size_t used, cudaStream_t stream)
+    {
+        if (n <= cap && p) return;
+        const size_t c = n < 16 ? 16 : n + n / 4;
+        T* q = nullptr;
+        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&q, c * sizeof(T), device_pool(), stream));
+        if (used && p) IPCG_CUDA(cudaMemcpyAsync(q, p, used * sizeof(T), cudaMemcpyDeviceToDevice, stream));
+        release();
+        p = q;
+        cap = c;
+        s = stream;
+    }
+    void reserve(size_t n, cudaStream_t stream) { grow_keep(n, 0, stream); }
+    void release()
+    {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        cap = 0;
+    }
+    ~PBuf() { release(); }
+};
+
 // Pinned host staging (for small count read-backs).
 template <typename T> struct HBuf {
     T* p = nullptr;
@@ -130,6 +167,7 @@ struct ipcg_mesh {
     ipcg::DBuf<double> scene_r;      // per-scene inflation radius of the current build
     ipcg::DBuf<double> scene_off2;   // per-scene (dhat + dmin)^2 of the current build
     ipcg::DBuf<unsigned char> params_buf; // per-scene barrier parameters
+    std::vector<unsigned char> params_host; // what params_buf holds
     ipcg::DBuf<double> scene_md;     // CCD: per-scene 0.5*min_distance, then min_distance
     cudaStream_t stream = nullptr;
     ipcg::DBuf<double> rest;
@@ -170,10 +208,13 @@ struct ipcg_collisions {
 
 struct ipcg_csr {
     int64_t rows = 0, nnz = 0;
-    ipcg::DBuf<int64_t> row_ptr;
-    ipcg::DBuf<int> col;
-    ipcg::DBuf<double> val;
+    ipcg::PBuf<int64_t> row_ptr;
+    ipcg::PBuf<int> col;
+    ipcg::PBuf<double> val;
     cudaStream_t stream = nullptr;
+    // Freed on the default stream: the matrix may outlive its mesh's stream,
+    // and every call that produced or read it has finished by then.
+    ~ipcg_csr() { row_ptr.s = col.s = val.s = nullptr; }
 };
 
 namespace ipcg {
