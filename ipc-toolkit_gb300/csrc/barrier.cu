@@ -481,11 +481,14 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
         }
         double x = d[start] - mu, z = e[start];
         for (int k = start; k < end; ++k) {
-            const double r = hypot(x, z);
+            // (c, s) from one reciprocal square root: x and z are entries of
+            // a local Hessian, far from the range where x^2 + z^2 overflows
+            const double r2 = x * x + z * z;
             double c = 1, s = 0;
-            if (r != 0) {
-                c = x / r;
-                s = -z / r;
+            if (r2 != 0) {
+                const double ir = rsqrt(r2);
+                c = x * ir;
+                s = -z * ir;
             }
             if (k > start) e[k - 1] = c * e[k - 1] - s * z;
             const double dk = d[k], dk1 = d[k + 1], ek = e[k];
