@@ -141,6 +141,10 @@ const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf)
 
 ipcg_mesh::~ipcg_mesh()
 {
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_side) cudaEventDestroy(ev_side);
+    if (ev_pattern) cudaEventDestroy(ev_pattern);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
 }
 
@@ -321,6 +325,10 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
         try {
             IPCG_CUDA(cudaGetDevice(&m->device));
             IPCG_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+            IPCG_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
+            IPCG_CUDA(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
+            IPCG_CUDA(cudaEventCreateWithFlags(&m->ev_side, cudaEventDisableTiming));
+            IPCG_CUDA(cudaEventCreateWithFlags(&m->ev_pattern, cudaEventDisableTiming));
             m->nV = nV;
             m->nE = nE;
             m->nF = nF;

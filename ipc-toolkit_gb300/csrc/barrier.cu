@@ -1203,53 +1203,66 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
             int* bptr = m->ivals_a.p;                    // block row pointers of this chunk's rows
             int* run_start = m->ivals_a.p + (nr + 2);    // first contribution of each block
             int nb = 0;
+            // The sparsity pattern (block keys, sort, run-length encoding,
+            // row and column arrays) does not depend on the values, so it is
+            // built on the side stream while the main stream computes and
+            // projects the local Hessians; the small VV and EV local Hessian
+            // launches also run there, beside EE and FV.  The side stream
+            // starts after everything queued so far on the main one.
+            cudaStream_t t = m->side;
+            IPCG_CUDA(cudaEventRecord(m->ev_fork, s));
+            IPCG_CUDA(cudaStreamWaitEvent(t, m->ev_fork, 0));
             if (nc > 0) {
-                // local Hessians (FP64 work) and PSD projection into the scratch slabs
                 const int64_t first[4] = { 0, cc.nvv, cc.nvv + cc.nev, cc.nvv + cc.nev + cc.nee };
                 const int64_t count[4] = { cc.nvv, cc.nev, cc.nee, cc.nfv };
                 if (count[0])
-                    IPCG_LAUNCH("k_local_hessian_vv", s, k_local_hessian<CT_VV><<<grid_for(count[0], BLOCK), BLOCK, 0,
-                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[0], count[0]));
+                    IPCG_LAUNCH("k_local_hessian_vv", t, k_local_hessian<CT_VV><<<grid_for(count[0], BLOCK), BLOCK, 0,
+                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[0], count[0]));
                 if (count[1])
-                    IPCG_LAUNCH("k_local_hessian_ev", s, k_local_hessian<CT_EV><<<grid_for(count[1], BLOCK), BLOCK, 0,
-                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[1], count[1]));
+                    IPCG_LAUNCH("k_local_hessian_ev", t, k_local_hessian<CT_EV><<<grid_for(count[1], BLOCK), BLOCK, 0,
+                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[1], count[1]));
+                IPCG_CUDA(cudaEventRecord(m->ev_side, t));
                 if (count[2])
                     IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], BLOCK), BLOCK, 0,
                         s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[2], count[2]));
                 if (count[3])
                     IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], BLOCK), BLOCK, 0,
                         s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[3], count[3]));
+                IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
                 if (a.psd != IPCG_PSD_NONE)
                     IPCG_LAUNCH("k_psd", s, k_psd<<<nblk_c, BLOCK, 0, s>>>(cc, m->hs.p, m->proj.p, a.psd, d_fail));
                 // sparsity pattern: sort (block key, contribution) and run-length encode
-                IPCG_LAUNCH("k_block_keys", s, k_block_keys<<<nblk_c, BLOCK, 0, s>>>(cc, m->E.p, m->F.p,
+                IPCG_LAUNCH("k_block_keys", t, k_block_keys<<<nblk_c, BLOCK, 0, t>>>(cc, m->E.p, m->F.p,
                     m->keys_a.p, ids_in, nk, gd));
-                sort_pairs_u64(m, m->keys_a.p, m->keys_b.p, ids_in, contrib, (int)nk, 32 + bits_for(nV + 1));
-                rle_u64(m, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
-                IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, s));
-                IPCG_CUDA(cudaStreamSynchronize(s));
+                sort_pairs_u64(m, t, m->keys_a.p, m->keys_b.p, ids_in, contrib, (int)nk, 32 + bits_for(nV + 1));
+                rle_u64(m, t, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
+                IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, t));
+                IPCG_CUDA(cudaStreamSynchronize(t)); // the main stream keeps running
                 nb = m->h_counters.p[0];
-                exclusive_sum_i32(m, run_len, run_start, nb);
+                exclusive_sum_i32(m, t, run_len, run_start, nb);
             } else {
-                IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), s));
+                IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), t));
             }
             // output arrays grow as chunks finish (the last chunk's estimate is exact)
             done += nc;
             const int64_t need = 9 * (B0 + nb);
             const int64_t guess = done < n ? (int64_t)((double)need * (double)n / (double)std::max<int64_t>(done, 1))
                                            : need;
-            hess->col.grow_keep(std::max(need, guess) + 1, 9 * B0, s);
-            hess->val.grow_keep(std::max(need, guess) + 1, 9 * B0, s);
-            IPCG_LAUNCH("k_block_rowptr", s, k_block_rowptr<<<grid_for(nr + 1, 256), 256, 0, s>>>(m->keys_a.p, d_nb,
+            hess->col.grow_keep(std::max(need, guess) + 1, 9 * B0, t);
+            hess->val.grow_keep(std::max(need, guess) + 1, 9 * B0, t);
+            IPCG_LAUNCH("k_block_rowptr", t, k_block_rowptr<<<grid_for(nr + 1, 256), 256, 0, t>>>(m->keys_a.p, d_nb,
                 r0, nr, bptr, nk, gd));
-            IPCG_LAUNCH("k_csr_rows", s, k_csr_rows<<<grid_for(nr + 1, 256), 256, 0, s>>>(bptr, r0, nr, B0,
+            IPCG_LAUNCH("k_csr_rows", t, k_csr_rows<<<grid_for(nr + 1, 256), 256, 0, t>>>(bptr, r0, nr, B0,
                 hess->row_ptr.p));
-            if (nb > 0) {
-                IPCG_LAUNCH("k_csr_cols", s, k_csr_cols<<<grid_for(nb, 256), 256, 0, s>>>(m->keys_a.p, nb, bptr, r0,
+            if (nb > 0)
+                IPCG_LAUNCH("k_csr_cols", t, k_csr_cols<<<grid_for(nb, 256), 256, 0, t>>>(m->keys_a.p, nb, bptr, r0,
                     nr, B0, hess->col.p, gd));
+            // join: values need the projected local Hessians and the pattern
+            IPCG_CUDA(cudaEventRecord(m->ev_pattern, t));
+            IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_pattern, 0));
+            if (nb > 0)
                 IPCG_LAUNCH("k_assemble", s, k_assemble<<<grid_for(9 * (int64_t)nb, 256), 256, 0, s>>>(cc,
                     m->keys_a.p, run_start, run_len, contrib, m->hs.p, bptr, r0, B0, nb, hess->val.p));
-            }
             B0 += nb;
         }
         hess->nnz = 9 * B0;

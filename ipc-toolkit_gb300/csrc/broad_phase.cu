@@ -330,7 +330,7 @@ void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const doubl
     else
         IPCG_LAUNCH("k_prim_boxes", s, k_prim_boxes<3><<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->F.p, n, V0, V1,
             scene_r, sv, m->bounds.p, bvh.plo.p, bvh.phi.p, bvh.codes.p, bvh.ids.p));
-    sort_pairs_u64(m, bvh.codes.p, bvh.codes_sorted.p, bvh.ids.p, bvh.ids_sorted.p, n,
+    sort_pairs_u64(m, m->stream, bvh.codes.p, bvh.codes_sorted.p, bvh.ids.p, bvh.ids_sorted.p, n,
         32 + bits_for(m->n_scenes + 1));
     if (n > 1)
         IPCG_LAUNCH("k_karras", s, k_karras<<<grid_for(n - 1, BLOCK), BLOCK, 0, s>>>(bvh.codes_sorted.p, n, bvh.lo.p,

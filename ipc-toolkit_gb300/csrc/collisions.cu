@@ -223,17 +223,17 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     int* d_num = m->counters.p + 12;
     const int idbits = 32 + bits_for(std::max(std::max(m->nV, m->nE), std::max(m->nF, (int64_t)2)));
     // VV: sort + run-length (weights = multiplicities)
-    sort_keys_u64(m, o.vv, ks, rvv, idbits);
+    sort_keys_u64(m, m->stream, o.vv, ks, rvv, idbits);
     c->vv.reserve(rvv + 1);
     c->vv_w.reserve(rvv + 1);
     int* counts = m->ivals_b.p;
-    rle_u64(m, ks, o.vv, counts, d_num + 0, rvv); // unique keys written back into the raw vv region
+    rle_u64(m, m->stream, ks, o.vv, counts, d_num + 0, rvv); // unique keys written back into the raw vv region
     if (rvv) IPCG_LAUNCH("k_unpack_rle", s, k_unpack_rle<<<grid_for(rvv, BLOCK), BLOCK, 0, s>>>(o.vv, counts, d_num + 0, c->vv.p, c->vv_w.p));
     // EV
-    sort_keys_u64(m, o.ev, ks + cap, rev, idbits);
+    sort_keys_u64(m, m->stream, o.ev, ks + cap, rev, idbits);
     c->ev.reserve(rev + 1);
     c->ev_w.reserve(rev + 1);
-    rle_u64(m, ks + cap, o.ev, counts + cap, d_num + 1, rev);
+    rle_u64(m, m->stream, ks + cap, o.ev, counts + cap, d_num + 1, rev);
     if (rev) IPCG_LAUNCH("k_unpack_rle", s, k_unpack_rle<<<grid_for(rev, BLOCK), BLOCK, 0, s>>>(o.ev, counts + cap, d_num + 1, c->ev.p, c->ev_w.p));
     // EE: sort keys with record ids, gather eps / dtype
     c->ee.reserve(ree + 1);
@@ -241,7 +241,7 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     c->ee_eps.reserve(ree + 1);
     c->ee_dtype.reserve(ree + 1);
     if (ree) {
-        sort_pairs_u64(m, o.ee, ks + 2 * cap, o.ee_rec, m->ivals_b.p + 2 * cap, ree, idbits);
+        sort_pairs_u64(m, m->stream, o.ee, ks + 2 * cap, o.ee_rec, m->ivals_b.p + 2 * cap, ree, idbits);
         IPCG_LAUNCH("k_gather_ee", s, k_gather_ee<<<grid_for(ree, BLOCK), BLOCK, 0, s>>>(ks + 2 * cap, m->ivals_b.p + 2 * cap, ree, o.ee_eps, o.ee_dt,
             c->ee.p, c->ee_eps.p, c->ee_dtype.p, c->ee_w.p));
     }
@@ -249,7 +249,7 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     c->fv.reserve(rfv + 1);
     c->fv_w.reserve(rfv + 1);
     if (rfv) {
-        sort_keys_u64(m, o.fv, ks + 3 * cap, rfv, idbits);
+        sort_keys_u64(m, m->stream, o.fv, ks + 3 * cap, rfv, idbits);
         IPCG_LAUNCH("k_unpack_keys", s, k_unpack_keys<<<grid_for(rfv, BLOCK), BLOCK, 0, s>>>(ks + 3 * cap, rfv, c->fv.p, c->fv_w.p));
     }
     IPCG_CHECK_LAUNCH();

@@ -170,6 +170,10 @@ struct ipcg_mesh {
     std::vector<unsigned char> params_host; // what params_buf holds
     ipcg::DBuf<double> scene_md;     // CCD: per-scene 0.5*min_distance, then min_distance
     cudaStream_t stream = nullptr;
+    // second stream for work that overlaps the main one (the Hessian's
+    // sparsity pattern), with the events that fork and join it
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_side = nullptr, ev_pattern = nullptr;
     ipcg::DBuf<double> rest;
     ipcg::DBuf<int> E, F, F2E;
     std::vector<int32_t> h_F2E;
@@ -271,15 +275,15 @@ void ccd_stencils(cudaStream_t s, int is_ee, int64_t n, const double* x0, const 
 void distance_stencils(cudaStream_t s, int kind, int64_t n, const double* x, int8_t* dtype, double* dist);
 
 // sort.cu (CUB wrappers)
-void sort_pairs_u32(ipcg_mesh* m, const unsigned* k_in, unsigned* k_out, const int* v_in, int* v_out, int n,
+void sort_pairs_u32(ipcg_mesh* m, cudaStream_t st, const unsigned* k_in, unsigned* k_out, const int* v_in, int* v_out, int n,
     int end_bit);
-void sort_keys_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* k_out, int n, int end_bit);
-void sort_pairs_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* k_out, const int* v_in,
+void sort_keys_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_in, unsigned long long* k_out, int n, int end_bit);
+void sort_pairs_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_in, unsigned long long* k_out, const int* v_in,
     int* v_out, int n, int end_bit);
 // run-length encode sorted keys; writes the number of runs to d_num (device)
-void rle_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* counts, int* d_num, int n);
-void unique_u64(ipcg_mesh* m, const unsigned long long* k_in, unsigned long long* uniq, int* d_num, int n);
-void exclusive_sum_i32(ipcg_mesh* m, const int* in, int* out, int n);
+void rle_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_in, unsigned long long* uniq, int* counts, int* d_num, int n);
+void unique_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_in, unsigned long long* uniq, int* d_num, int n);
+void exclusive_sum_i32(ipcg_mesh* m, cudaStream_t st, const int* in, int* out, int n);
 
 inline int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
 inline int bits_for(int64_t n)
