@@ -349,6 +349,66 @@ def batch_leg(dev, warmup=1, steps=3):
     }
 
 
+def served_leg(dev, seed=4):
+    """Served request stream: 64 resident scenes drawn from the batch size
+    distribution plus 4 sphere packs; requests alternate barrier (collision
+    set rebuilt at the new positions, E + grad + CLAMP Hessian) and
+    step-size, each at the scene's positions perturbed by seeded U(+-0.1
+    dhat) noise, arriving as a Poisson stream.  Two runs: the offered rate
+    2000 req/s (beyond what one GPU completes on these scenes, so latency is
+    queueing) and a rate below the measured capacity.  HBM admission budget
+    120 GB.  Latency = completion - submission."""
+    import ipctk_gb300 as ipctk
+    from ipctk_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    scs = scenes.batch(n_scenes=64, seed=seed) + [scenes.sphere_pack(seed=10 + i) for i in range(4)]
+    # seeded noise pools (4 per scene), reused in turn
+    pools = [[rng.uniform(-0.1, 0.1, s["V"].shape) * s["dhat"] for _ in range(4)] for s in scs]
+    srv = ipctk.Server(workers=8, hbm_budget_bytes=120e9)
+    ids = []
+    for s in scs:
+        m = ipctk.CollisionMesh(s["V"], s["E"], s["F"])
+        ids.append(srv.add_scene(m, ipctk.NormalCollisions(), s["dhat"], 0.0, s["kappa"]))
+    for t in [srv.submit_barrier(i, s["V"]) for i, s in zip(ids, scs)]:
+        srv.wait(t)  # every scene's collision set and work space resident
+    pct = lambda a, q: float(np.percentile(np.array(a), q))
+
+    def stream(rate, n):
+        arr = np.cumsum(rng.exponential(1.0 / rate, n))
+        picks = rng.integers(len(scs), size=n)
+        tick = []
+        start = time.perf_counter()
+        for j in range(n):
+            while time.perf_counter() - start < arr[j]:
+                pass
+            k = int(picks[j])
+            s = scs[k]
+            V = s["V"] + pools[k][j % 4]
+            tick.append(srv.submit_barrier(ids[k], V) if j % 2 == 0 else srv.submit_stepsize(ids[k], s["V"], V))
+        lat = [[], []]
+        t_first, t_last = None, 0
+        for t in tick:
+            r = srv.wait(t)
+            lat[r["kind"]].append((r["t_end_ns"] - r["t_submit_ns"]) / 1e6)
+            t_first = r["t_submit_ns"] if t_first is None else min(t_first, r["t_submit_ns"])
+            t_last = max(t_last, r["t_end_ns"])
+        allv = lat[0] + lat[1]
+        return {"offered_req_s": rate, "requests": n, "completed_req_s": n / ((t_last - t_first) / 1e9),
+                "p50_ms": pct(allv, 50), "p99_ms": pct(allv, 99),
+                "barrier": {"p50_ms": pct(lat[0], 50), "p99_ms": pct(lat[0], 99)},
+                "stepsize": {"p50_ms": pct(lat[1], 50), "p99_ms": pct(lat[1], 99)}}
+
+    offered = stream(2000.0, 1000)
+    below = stream(0.7 * offered["completed_req_s"], 300)
+    st = srv.stats()
+    srv.close()
+    return {"workload": f"64 two-sheet scenes (batch size distribution, seed {seed}) + 4 sphere packs; "
+                        f"{sum(s['V'].shape[0] for s in scs):,} verts resident; requests alternate barrier "
+                        "(build + E + grad + CLAMP Hessian) and step size, positions +-0.1 dhat noise",
+            "workers": 8, "hbm_budget_gb": 120, "offered": offered, "below_capacity": below,
+            "resident_gb": st["resident_bytes"] / 1e9, "workspace_releases": st["releases"]}
+
+
 def run_gb300(args, rank, world):
     import torch
     import ipctk_gb300 as ipctk
@@ -482,9 +542,13 @@ def run_gb300(args, rank, world):
     if rank != 0:
         return
     batch = None
+    served = None
     if not args.no_batch:
         del mesh, col, Vd, V1d, flush
         batch = batch_leg(dev)
+        import gc
+        gc.collect()
+        served = served_leg(dev)
     cpu = None
     ccd_cpu = None
     if not args.no_cpu_baseline:
@@ -512,6 +576,7 @@ def run_gb300(args, rank, world):
                 "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "cpu_baseline": ccd_cpu},
         "collision_build": {"p50_ms": pct(build_ms, 50), "p99_ms": pct(build_ms, 99)},
         "batch": batch,
+        "served": served,
     }
     print(json.dumps(line), flush=True)
 

@@ -250,6 +250,54 @@ int ipcg_collision_free_stepsize_batch(const ipcg_mesh* mesh,
                                        double* steps, int64_t* n_candidates);
 
 /* ---------------------------------------------------------------------- */
+/* Serving: requests from many simulations over resident scenes            */
+/* ---------------------------------------------------------------------- */
+
+/* No counterpart in the reference, which serves one simulation per call.
+ * A server takes the two per-iteration requests of a Newton loop -- a barrier
+ * request (NormalCollisions::build at the given positions, then the energy,
+ * gradient and PSD-projected Hessian: normal_collisions.hpp:45-50,
+ * potential.hpp:34-60) and a step-size request (compute_collision_free_stepsize,
+ * ipc.hpp:41-47, with the reference's default TightInclusionCCD) -- from many
+ * scenes at once.  Each scene's mesh, broad-phase work space and collision
+ * set stay on the device.  `workers` host threads take requests in arrival
+ * order, at most one per scene at a time, and run them on their scene's own
+ * streams, so requests of different scenes overlap on the GPU as they
+ * arrive.  A request starts only when the working memory of all scenes plus
+ * its own expected need fits `hbm_budget_bytes`; to make room the server
+ * releases idle scenes' work space (never their collision sets), least
+ * recently used first.  Results are those of the same calls made directly. */
+typedef struct ipcg_server ipcg_server;
+
+typedef struct {
+    int status;                 /* IPCG_OK or the request's error code */
+    int kind;                   /* 0 barrier, 1 step size */
+    double energy;              /* barrier requests */
+    double step;                /* step-size requests */
+    int64_t contacts;           /* collision-set size (barrier) or CCD candidates (step) */
+    int64_t t_submit_ns, t_start_ns, t_end_ns; /* steady clock */
+} ipcg_request_result;
+
+int ipcg_server_create(int workers, int64_t hbm_budget_bytes, ipcg_server** out);
+int ipcg_server_destroy(ipcg_server* server);
+/* Registers a single-scene mesh with the collision set it keeps (both stay
+ * owned by the caller and must outlive the server) and its barrier
+ * parameters. */
+int ipcg_server_add_scene(ipcg_server* server, ipcg_mesh* mesh, ipcg_collisions* collisions,
+                          double dhat, double dmin, double stiffness, int64_t* scene);
+/* Host positions are copied at submission. */
+int ipcg_server_submit_barrier(ipcg_server* server, int64_t scene, const double* vertices,
+                               int psd_method, int64_t* ticket);
+int ipcg_server_submit_stepsize(ipcg_server* server, int64_t scene, const double* vertices_t0,
+                                const double* vertices_t1, double min_distance, int64_t* ticket);
+/* Blocks until the request is done.  gradient (3 nV doubles, host) and
+ * hessian (the caller then owns it) may be NULL. */
+int ipcg_server_wait(ipcg_server* server, int64_t ticket, ipcg_request_result* out,
+                     double* gradient, ipcg_csr** hessian);
+/* completed, queued, running, work-space releases, resident bytes */
+int ipcg_server_stats(ipcg_server* server, int64_t stats[5]);
+
+/* ---------------------------------------------------------------------- */
 /* Single-stencil primitives (for known-answer tests and plugin use)       */
 /* ---------------------------------------------------------------------- */
 

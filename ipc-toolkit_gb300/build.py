@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
                  "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 EXACT = {"broad_phase.cu", "collisions.cu", "ccd.cu"}
-SOURCES = ["abi.cu", "broad_phase.cu", "collisions.cu", "barrier.cu", "ccd.cu", "sort.cu"]
+SOURCES = ["abi.cu", "broad_phase.cu", "collisions.cu", "barrier.cu", "ccd.cu", "sort.cu", "server.cu"]
 
 
 def nvcc() -> str:
@@ -58,7 +58,7 @@ def build(verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     if not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -137,6 +137,8 @@ const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf)
     return buf.p;
 }
 
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
 } // namespace ipcg
 
 ipcg_mesh::~ipcg_mesh()

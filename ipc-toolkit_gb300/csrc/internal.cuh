@@ -230,6 +230,9 @@ bool is_device_ptr(const void* p);
 
 inline SceneView scene_view(const ipcg_mesh* m) { return SceneView { (int)m->n_scenes, m->n_scenes > 1 ? m->vscene.p : nullptr }; }
 
+// abi.cu: the calling thread's message for ipcg_last_error()
+void set_last_error(const std::string& msg);
+
 // barrier.cu: contacts per Hessian chunk of a batch (scratch memory bound)
 extern std::atomic<int64_t> g_hess_chunk_contacts;
 

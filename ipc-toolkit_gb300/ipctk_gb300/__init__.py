@@ -81,6 +81,13 @@ def _load():
         "ipcg_barrier_batch": (i32, [P, P, P, P, P, i32, i32, P, P, PP]),
         "ipcg_collision_free_stepsize_batch": (i32, [P, P, P, P, d, i64, d, P, P]),
         "ipcg_set_hessian_chunk_contacts": (i32, [i64]),
+        "ipcg_server_create": (i32, [i32, i64, PP]),
+        "ipcg_server_destroy": (i32, [P]),
+        "ipcg_server_add_scene": (i32, [P, P, P, d, d, d, P]),
+        "ipcg_server_submit_barrier": (i32, [P, i64, P, i32, P]),
+        "ipcg_server_submit_stepsize": (i32, [P, i64, P, P, d, P]),
+        "ipcg_server_wait": (i32, [P, i64, P, P, PP]),
+        "ipcg_server_stats": (i32, [P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -634,6 +641,90 @@ def compute_collision_free_stepsize(mesh: CollisionMesh, vertices_t0, vertices_t
         mesh._h, _ptr(V0), _ptr(V1), float(min_distance), narrow_phase_ccd.tolerance,
         narrow_phase_ccd.max_iterations, narrow_phase_ccd.conservative_rescaling, _ptr(step), None))
     return float(step[0])
+
+
+class RequestResult(C.Structure):
+    """ipcg_request_result (include/ipcg.h)."""
+    _fields_ = [("status", C.c_int), ("kind", C.c_int), ("energy", C.c_double), ("step", C.c_double),
+                ("contacts", C.c_int64), ("t_submit_ns", C.c_int64), ("t_start_ns", C.c_int64),
+                ("t_end_ns", C.c_int64)]
+
+
+class Server:
+    """Request loop over resident scenes (ipcg_server_*): barrier requests
+    (collision set rebuilt at the given positions, then energy, gradient and
+    Hessian) and step-size requests from many simulations, run concurrently
+    on their scenes' streams under an HBM admission budget."""
+
+    def __init__(self, workers: int = 4, hbm_budget_bytes: float = 120e9):
+        h = C.c_void_p()
+        _check(_load().ipcg_server_create(int(workers), int(hbm_budget_bytes), C.byref(h)))
+        self._h = h
+        self._scenes = []
+        self._tickets = {}
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.ipcg_server_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def add_scene(self, mesh: CollisionMesh, collisions: NormalCollisions, dhat: float, dmin: float = 0.0,
+                  stiffness: float = 1.0) -> int:
+        sid = C.c_int64()
+        _check(_load().ipcg_server_add_scene(self._h, mesh._h, collisions._h, float(dhat), float(dmin),
+                                             float(stiffness), C.byref(sid)))
+        self._scenes.append((mesh, collisions))  # keep them alive
+        return sid.value
+
+    def submit_barrier(self, scene: int, vertices, project_hessian_to_psd=PSDProjectionMethod.CLAMP) -> int:
+        V = np.ascontiguousarray(vertices, np.float64)
+        t = C.c_int64()
+        _check(_load().ipcg_server_submit_barrier(self._h, int(scene), _ptr(V), int(project_hessian_to_psd),
+                                                  C.byref(t)))
+        self._tickets[t.value] = int(scene)
+        return t.value
+
+    def submit_stepsize(self, scene: int, vertices_t0, vertices_t1, min_distance: float = 0.0) -> int:
+        V0 = np.ascontiguousarray(vertices_t0, np.float64)
+        V1 = np.ascontiguousarray(vertices_t1, np.float64)
+        t = C.c_int64()
+        _check(_load().ipcg_server_submit_stepsize(self._h, int(scene), _ptr(V0), _ptr(V1), float(min_distance),
+                                                   C.byref(t)))
+        self._tickets[t.value] = int(scene)
+        return t.value
+
+    def wait(self, ticket: int, gradient: bool = False, hessian: str | None = None):
+        """Blocks for a request; returns a dict with energy / step, contacts,
+        times (ns) and, on request, the gradient (numpy) and the Hessian
+        ("device": DeviceCSR, "scipy": scipy matrix)."""
+        scene = self._tickets.pop(int(ticket), None)
+        if scene is None:
+            raise ValueError("unknown ticket")
+        ndof = 3 * self._scenes[scene][0].num_vertices
+        res = RequestResult()
+        gbuf = np.zeros(ndof) if gradient else None
+        h = C.c_void_p()
+        _check(_load().ipcg_server_wait(self._h, int(ticket), C.byref(res), _ptr(gbuf),
+                                        C.byref(h) if hessian else None))
+        out = {"kind": res.kind, "energy": res.energy, "step": res.step, "contacts": res.contacts,
+               "t_submit_ns": res.t_submit_ns, "t_start_ns": res.t_start_ns, "t_end_ns": res.t_end_ns}
+        if gradient:
+            out["gradient"] = gbuf
+        if hessian == "device":
+            out["hessian"] = DeviceCSR(h, ndof)
+        elif hessian:
+            out["hessian"] = _csr_to_scipy(h, ndof)
+        return out
+
+    def stats(self) -> dict:
+        st = np.zeros(5, np.int64)
+        _check(_load().ipcg_server_stats(self._h, _ptr(st)))
+        return {"completed": int(st[0]), "queued": int(st[1]), "running": int(st[2]), "releases": int(st[3]),
+                "resident_bytes": int(st[4])}
 
 
 def compute_collision_free_stepsize_batch(batch: SceneBatch, vertices_t0, vertices_t1, min_distance=0.0,

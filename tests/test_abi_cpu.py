@@ -63,3 +63,23 @@ def test_argument_validation_precedes_device(ipctk):
     st = L.ipcg_mesh_create(None, -1, None, 0, None, 0, C.byref(h))
     assert st == 1
     assert "negative" in L.ipcg_last_error().decode()
+
+
+def test_server_argument_validation_without_gpu(ipctk):
+    """The request server's arguments are checked before any device work."""
+    L = C.CDLL(ipctk.LIB_PATH)
+    L.ipcg_last_error.restype = C.c_char_p
+    h = C.c_void_p()
+    L.ipcg_server_create.restype = C.c_int
+    L.ipcg_server_create.argtypes = [C.c_int, C.c_int64, C.POINTER(C.c_void_p)]
+    assert L.ipcg_server_create(0, 1 << 30, C.byref(h)) == 1
+    assert L.ipcg_server_create(2, 0, C.byref(h)) == 1
+    assert L.ipcg_server_create(2, 1 << 30, None) == 1
+    assert L.ipcg_server_create(2, 1 << 30, C.byref(h)) == 0
+    L.ipcg_server_submit_barrier.restype = C.c_int
+    L.ipcg_server_submit_barrier.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int, C.POINTER(C.c_int64)]
+    t = C.c_int64()
+    assert L.ipcg_server_submit_barrier(h, 0, None, 1, C.byref(t)) == 1  # no scene registered
+    assert b"unknown scene" in L.ipcg_last_error()
+    L.ipcg_server_destroy.argtypes = [C.c_void_p]
+    assert L.ipcg_server_destroy(h) == 0
