@@ -349,6 +349,47 @@ def batch_leg(dev, warmup=1, steps=3):
     }
 
 
+def mixed_leg(dev, warmup=2, steps=5):
+    """Layered cloth (8 stacked 256x256 sheets, 524,288 verts; dhat 1e-3,
+    stiffness 1e4, seed 2): E + grad + CLAMP Hessian in FP64 and in mixed
+    precision (face-vertex contacts in FP32), device-resident positions, and
+    the mixed results' relative error against the FP64 ones (the FP64 path is
+    the one held to the oracle at 1e-10)."""
+    import torch
+    import ipctk_gb300 as ipctk
+    from ipctk_gb300 import scenes
+    import scipy.sparse as sp
+    sc = scenes.layered_cloth()
+    mesh = ipctk.CollisionMesh(sc["V"], sc["E"], sc["F"])
+    Vd = torch.from_numpy(sc["V"]).to(dev)
+    col = ipctk.NormalCollisions()
+    col.build(mesh, Vd, sc["dhat"])
+    counts = col.counts()
+    C = int(counts[:4].sum())
+    CL = ipctk.PSDProjectionMethod.CLAMP
+    out = {"workload": "layered cloth 8 x 256^2 (524,288 verts)", "contacts": C,
+           "contacts_by_type": {"vv": int(counts[0]), "ev": int(counts[1]), "ee": int(counts[2]),
+                                "fv": int(counts[3])}}
+    res = {}
+    for name, mixed in (("fp64", False), ("mixed", True)):
+        B = ipctk.BarrierPotential(sc["dhat"], sc["kappa"], mixed_precision=mixed)
+        ts = []
+        for i in range(warmup + steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e, g, H = B.energy_gradient_hessian_device(col, mesh, Vd, CL)
+            torch.cuda.synchronize()
+            if i >= warmup:
+                ts.append(time.perf_counter() - t0)
+        res[name] = (e, g.cpu().numpy(), H.to_scipy())
+        out[name] = {"value": C / statistics.median(ts), "unit": UNIT, "ms": 1000 * statistics.median(ts)}
+    (e0, g0, H0), (e1, g1, H1) = res["fp64"], res["mixed"]
+    out["rel_error_vs_fp64"] = {"energy": abs(e1 - e0) / abs(e0),
+                                "gradient": float(np.linalg.norm(g1 - g0) / np.linalg.norm(g0)),
+                                "hessian": float(sp.linalg.norm(H1 - H0) / sp.linalg.norm(H0))}
+    return out
+
+
 def served_leg(dev, seed=4):
     """Served request stream: 64 resident scenes drawn from the batch size
     distribution plus 4 sphere packs; requests alternate barrier (collision
@@ -543,12 +584,15 @@ def run_gb300(args, rank, world):
         return
     batch = None
     served = None
+    mixed = None
     if not args.no_batch:
         del mesh, col, Vd, V1d, flush
         batch = batch_leg(dev)
         import gc
         gc.collect()
         served = served_leg(dev)
+        gc.collect()
+        mixed = mixed_leg(dev)
     cpu = None
     ccd_cpu = None
     if not args.no_cpu_baseline:
@@ -577,6 +621,7 @@ def run_gb300(args, rank, world):
         "collision_build": {"p50_ms": pct(build_ms, 50), "p99_ms": pct(build_ms, 99)},
         "batch": batch,
         "served": served,
+        "mixed_precision": mixed,
     }
     print(json.dumps(line), flush=True)
 

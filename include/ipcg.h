@@ -35,6 +35,18 @@ extern "C" {
 #define IPCG_PSD_CLAMP 1
 #define IPCG_PSD_ABS 2
 
+/* Bits of the barrier calls' use_physical_barrier argument.  Bit 0 is the
+ * reference's flag (BarrierPotential(dhat, stiffness, use_physical_barrier),
+ * barrier_potential.hpp:24-27); 0 and 1 mean what they mean there.  Bit 1
+ * (no counterpart in the reference) selects mixed precision: face-vertex
+ * (point-triangle) contacts on non-degenerate triangles compute the
+ * distance, its derivatives and the barrier derivatives in FP32 from FP64
+ * relative vectors; every other contact type, the PSD projection and the
+ * assembly stay FP64.  Energy, gradient and Hessian then agree with FP64 to
+ * about 1e-6 relative. */
+#define IPCG_BARRIER_PHYSICAL 1
+#define IPCG_BARRIER_FP32_PT 2
+
 typedef struct ipcg_mesh ipcg_mesh;
 typedef struct ipcg_collisions ipcg_collisions;
 typedef struct ipcg_csr ipcg_csr;

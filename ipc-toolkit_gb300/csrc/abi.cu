@@ -532,7 +532,10 @@ static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const d
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dV = stage_positions(m, V, m->V0);
-        BarrierArgs a { dhat[0], stiffness[0], c->dmin, physical ? 1 : 0, psd };
+        require(physical >= 0 && physical <= (IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT),
+            "unknown barrier option bits");
+        BarrierArgs a { dhat[0], stiffness[0], c->dmin, (physical & IPCG_BARRIER_PHYSICAL) ? 1 : 0, psd };
+        a.mixed = (physical & IPCG_BARRIER_FP32_PT) ? 1 : 0;
         if (scene_params) {
             a.scene_dhat = dhat;
             a.scene_kappa = stiffness;

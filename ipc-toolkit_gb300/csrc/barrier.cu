@@ -125,7 +125,153 @@ __device__ __forceinline__ double barrier2(double d, double dh)
 struct Params {
     double kappa, dmin2, xhat, scale; // scale = physical factor (or 1)
     int psd;
+    int mixed; // point-triangle contacts in FP32 (IPCG_BARRIER_FP32_PT)
 };
+
+// ---- FP32 point-triangle contacts (mixed precision) ----
+// The point-plane squared distance d = N^2/D (N = a.(u x v), D = |u x v|^2,
+// a = p - t0, u = t1 - t0, v = t2 - t0) and its derivatives, and the barrier
+// derivatives, in FP32.  The relative vectors are formed in FP64 first, so
+// FP32 only sees edge-sized numbers.  Used for triangles that are not
+// degenerate (sin^2 of the corner angle above 1e-6); FV contacts whose
+// triangles are, and every other contact type, stay FP64.
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 to_f3(V3 a) { return F3 { (float)a.x, (float)a.y, (float)a.z }; }
+__device__ __forceinline__ F3 f3_cross(F3 a, F3 b)
+{
+    return F3 { a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x };
+}
+__device__ __forceinline__ float f3_dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float f3c(F3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
+__device__ __forceinline__ void f3_skew(F3 a, float M[3][3])
+{
+    M[0][0] = 0;
+    M[0][1] = -a.z;
+    M[0][2] = a.y;
+    M[1][0] = a.z;
+    M[1][1] = 0;
+    M[1][2] = -a.x;
+    M[2][0] = -a.y;
+    M[2][1] = a.x;
+    M[2][2] = 0;
+}
+
+// FP64 test of the triangle's corner angle at t0 (u = t1 - t0, v = t2 - t0).
+__device__ __forceinline__ bool fv_fp32_ok(const V3* x)
+{
+    const V3 u = x[2] - x[1], v = x[3] - x[1];
+    return sqnorm(cross(u, v)) > 1e-6 * sqnorm(u) * sqnorm(v);
+}
+
+// d, reduced gradient g (9, in r = (a, u, v)) and Hessian H (81 or null).
+__device__ float triple_quot_f(F3 a, F3 u, F3 v, float* g, float* H)
+{
+    const F3 w = f3_cross(u, v);
+    const float Nn = f3_dot(a, w);
+    const float D = f3_dot(w, w);
+    const float iD = 1.0f / D;
+    const F3 gNa = w, gNu = f3_cross(v, a), gNv = f3_cross(a, u);
+    const F3 cvw = f3_cross(v, w), cwu = f3_cross(w, u);
+    float gN[9], gD[9];
+    for (int i = 0; i < 3; ++i) {
+        gN[i] = f3c(gNa, i);
+        gN[3 + i] = f3c(gNu, i);
+        gN[6 + i] = f3c(gNv, i);
+        gD[i] = 0;
+        gD[3 + i] = 2.0f * f3c(cvw, i);
+        gD[6 + i] = 2.0f * f3c(cwu, i);
+    }
+    const float c1 = 2 * Nn * iD, c2 = Nn * Nn * iD * iD;
+    for (int i = 0; i < 9; ++i) g[i] = c1 * gN[i] - c2 * gD[i];
+    if (H) {
+        float Sv[3][3], Su[3][3], Sa[3][3], Sw[3][3];
+        f3_skew(v, Sv);
+        f3_skew(u, Su);
+        f3_skew(a, Sa);
+        f3_skew(w, Sw);
+        float HN[81], HD[81];
+        for (int i = 0; i < 81; ++i) {
+            HN[i] = 0;
+            HD[i] = 0;
+        }
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                HN[i * 9 + 3 + j] = HN[(3 + j) * 9 + i] = -Sv[i][j];
+                HN[i * 9 + 6 + j] = HN[(6 + j) * 9 + i] = Su[i][j];
+                HN[(3 + i) * 9 + 6 + j] = HN[(6 + j) * 9 + 3 + i] = -Sa[i][j];
+                float uu = 0, vv = 0, uv = 0;
+                for (int k = 0; k < 3; ++k) {
+                    uu += Sv[k][i] * Sv[k][j];
+                    vv += Su[k][i] * Su[k][j];
+                    uv -= Sv[k][i] * Su[k][j];
+                }
+                HD[(3 + i) * 9 + 3 + j] = 2 * uu;
+                HD[(6 + i) * 9 + 6 + j] = 2 * vv;
+                HD[(3 + i) * 9 + 6 + j] = HD[(6 + j) * 9 + 3 + i] = 2 * (uv - Sw[i][j]);
+            }
+        const float iD2 = iD * iD;
+        const float k1 = 2 * iD, k2 = 2 * Nn * iD, k3 = 2 * Nn * iD2, k4 = Nn * Nn * iD2, k5 = 2 * Nn * Nn * iD2 * iD;
+        for (int i = 0; i < 9; ++i)
+            for (int j = 0; j < 9; ++j)
+                H[i * 9 + j] = k1 * gN[i] * gN[j] + k2 * HN[i * 9 + j] - k3 * (gN[i] * gD[j] + gD[i] * gN[j])
+                    - k4 * HD[i * 9 + j] + k5 * gD[i] * gD[j];
+    }
+    return Nn * Nn * iD;
+}
+
+// FP32 barrier and its derivatives (barrier.cpp:11-43).
+__device__ __forceinline__ float barrier0f(float d, float dh)
+{
+    if (d <= 0.0f) return __int_as_float(0x7f800000);
+    if (d >= dh) return 0;
+    const float dm = d - dh;
+    return -dm * dm * logf(d / dh);
+}
+__device__ __forceinline__ float barrier1f(float d, float dh)
+{
+    if (d <= 0.0f || d >= dh) return 0.0f;
+    return (dh - d) * (2 * logf(d / dh) - dh / d + 1);
+}
+__device__ __forceinline__ float barrier2f(float d, float dh)
+{
+    if (d <= 0.0f || d >= dh) return 0.0f;
+    const float r = dh / d;
+    return (r + 2) * r - 2 * logf(d / dh) - 3;
+}
+
+// FV contact in FP32: squared distance, stencil gradient (12) and Hessian
+// (144 or null) of d, as floats.
+__device__ float fv_local_f(const V3* x, float* g, float* H)
+{
+    // a = p - t0, u = t1 - t0, v = t2 - t0 (FP64 differences, then FP32)
+    const F3 a = to_f3(x[0] - x[1]), u = to_f3(x[2] - x[1]), v = to_f3(x[3] - x[1]);
+    float gr[9], Hr[81];
+    const float d = triple_quot_f(a, u, v, gr, H ? Hr : nullptr);
+    // expand to the stencil (p, t0, t1, t2): reduced vectors (0-1, 2-1, 3-1)
+    const int pos[3] = { 0, 2, 3 };
+    for (int i = 0; i < 12; ++i) g[i] = 0;
+    for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 3; ++c) {
+            g[3 * pos[k] + c] += gr[3 * k + c];
+            g[3 + c] -= gr[3 * k + c];
+        }
+    if (H) {
+        for (int i = 0; i < 144; ++i) H[i] = 0;
+        for (int k = 0; k < 3; ++k)
+            for (int l = 0; l < 3; ++l)
+                for (int c = 0; c < 3; ++c)
+                    for (int e = 0; e < 3; ++e) {
+                        const float h = Hr[(3 * k + c) * 9 + 3 * l + e];
+                        H[(3 * pos[k] + c) * 12 + 3 * pos[l] + e] += h;
+                        H[(3 * pos[k] + c) * 12 + 3 + e] -= h;
+                        H[(3 + c) * 12 + 3 * pos[l] + e] -= h;
+                        H[(3 + c) * 12 + 3 + e] += h;
+                    }
+    }
+    return d;
+}
 
 // ---- closed-form squared-distance derivatives ----
 __device__ __forceinline__ void skew(V3 a, double M[3][3])
@@ -655,6 +801,24 @@ __device__ __forceinline__ double fd2(const Params& P, double d2)
 {
     return P.kappa * (barrier2(d2 - P.dmin2, P.xhat) * P.scale);
 }
+__device__ __forceinline__ float fvalf(const Params& P, float d2)
+{
+    return (float)P.kappa * (barrier0f(d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
+}
+__device__ __forceinline__ float fd1f(const Params& P, float d2)
+{
+    return (float)P.kappa * (barrier1f(d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
+}
+__device__ __forceinline__ float fd2f(const Params& P, float d2)
+{
+    return (float)P.kappa * (barrier2f(d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
+}
+// Whether contact c is evaluated in FP32 (mixed precision, FV, triangle not
+// degenerate).
+__device__ __forceinline__ bool fp32_contact(const Params& P, const Local& c, const V3* x)
+{
+    return P.mixed && c.type == CT_FV && fv_fp32_ok(x);
+}
 
 __device__ __forceinline__ void gather(const double* __restrict__ V, const Local& c, V3* x)
 {
@@ -674,11 +838,16 @@ __global__ void __launch_bounds__(BLOCK) k_energy(ContactsView cv, const int* __
         load_contact(cv, E, F, i, c);
         V3 x[4];
         gather(V, c, x);
-        double g[12];
-        const double d = contact_distance(c, x, g, nullptr);
-        bool act;
-        const double m = mollifier(c, x, nullptr, nullptr, act);
-        e = c.w * m * fval(P, d);
+        if (fp32_contact(P, c, x)) {
+            float gf[12];
+            e = c.w * (double)fvalf(P, fv_local_f(x, gf, nullptr));
+        } else {
+            double g[12];
+            const double d = contact_distance(c, x, g, nullptr);
+            bool act;
+            const double m = mollifier(c, x, nullptr, nullptr, act);
+            e = c.w * m * fval(P, d);
+        }
     }
     typedef cub::BlockReduce<double, BLOCK> BR;
     __shared__ typename BR::TempStorage tmp;
@@ -715,11 +884,16 @@ __global__ void __launch_bounds__(BLOCK) k_energy_scenes(ContactsView cv, const 
         const Params P = sp[scene];
         V3 x[4];
         gather(V, c, x);
-        double g[12];
-        const double d = contact_distance(c, x, g, nullptr);
-        bool act;
-        const double m = mollifier(c, x, nullptr, nullptr, act);
-        e = c.w * m * fval(P, d);
+        if (fp32_contact(P, c, x)) {
+            float gf[12];
+            e = c.w * (double)fvalf(P, fv_local_f(x, gf, nullptr));
+        } else {
+            double g[12];
+            const double d = contact_distance(c, x, g, nullptr);
+            bool act;
+            const double m = mollifier(c, x, nullptr, nullptr, act);
+            e = c.w * m * fval(P, d);
+        }
     }
     __shared__ int s_lo, s_hi;
     if (threadIdx.x == 0) {
@@ -754,6 +928,16 @@ __global__ void __launch_bounds__(BLOCK) k_gradient(ContactsView cv, const int* 
     const Params P = sp[sv.of(c.vid[0])];
     V3 x[4];
     gather(V, c, x);
+    if (fp32_contact(P, c, x)) {
+        float gf[12];
+        const float fd = fd1f(P, fv_local_f(x, gf, nullptr)) * (float)c.w;
+        for (int a = 0; a < 4; ++a)
+            for (int k = 0; k < 3; ++k) {
+                const double v = (double)(fd * gf[3 * a + k]);
+                if (v != 0) atomicAdd(grad + 3 * (int64_t)c.vid[a] + k, v);
+            }
+        return;
+    }
     const int N = 3 * c.n;
     double gm[12];
     bool act;
@@ -825,6 +1009,15 @@ __global__ void __launch_bounds__(BLOCK) k_local_hessian(ContactsView cv, const 
     constexpr int NS = TYPE == CT_VV ? 2 : (TYPE == CT_EV ? 3 : 4);
     constexpr int N = 3 * NS;
     double* __restrict__ out = Hs + 144 * i;
+    if (TYPE == CT_FV && fp32_contact(P, c, x)) {
+        float gf[12], Hf[144];
+        const float d = fv_local_f(x, gf, Hf);
+        const float w = (float)c.w, a = w * fd2f(P, d), b = w * fd1f(P, d);
+        for (int r = 0; r < 12; ++r)
+            for (int q = 0; q < 12; ++q) out[r * 12 + q] = (double)(a * gf[r] * gf[q] + b * Hf[r * 12 + q]);
+        proj[i] = 1;
+        return;
+    }
     double g[12], H[144];
     double d;
     if (TYPE == CT_VV) d = pp_local(x, 6, 0, 1, g, H);
@@ -1122,7 +1315,7 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         const double kap = a.scene_kappa ? a.scene_kappa[k] : a.kappa;
         const double dm = (k < (int)cs->scene_dmin.size()) ? cs->scene_dmin[k] : cs->dmin;
         const double xh = (2 * dm + dh) * dh;
-        hp[k] = Params { kap, dm * dm, xh, a.physical ? dh / (xh * xh) : 1.0, a.psd };
+        hp[k] = Params { kap, dm * dm, xh, a.physical ? dh / (xh * xh) : 1.0, a.psd, a.mixed };
     }
     // uploaded only when they change (a Newton loop repeats them)
     const size_t pbytes = sizeof(Params) * ns;

@@ -254,6 +254,7 @@ struct BarrierArgs {
     int psd;
     const double* scene_dhat = nullptr;  // per scene (batches), host
     const double* scene_kappa = nullptr; // per scene (batches), host
+    int mixed = 0;                       // FP32 point-triangle contacts
 };
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null);

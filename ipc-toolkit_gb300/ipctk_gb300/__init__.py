@@ -465,18 +465,26 @@ class BarrierPotential:
     (src/ipc/potentials/barrier_potential.hpp:24-27) with the default
     ClampedLogBarrier."""
 
-    def __init__(self, dhat: float, stiffness: float, use_physical_barrier: bool = False):
+    def __init__(self, dhat: float, stiffness: float, use_physical_barrier: bool = False,
+                 mixed_precision: bool = False):
+        """``mixed_precision`` (no counterpart in the reference): face-vertex
+        contacts in FP32, everything else FP64 (IPCG_BARRIER_FP32_PT)."""
         if not dhat > 0:
             raise ValueError("dhat must be positive")
         self.dhat = float(dhat)
         self.stiffness = float(stiffness)
         self.use_physical_barrier = bool(use_physical_barrier)
+        self.mixed_precision = bool(mixed_precision)
+
+    @property
+    def _options(self):
+        return int(self.use_physical_barrier) | (2 if self.mixed_precision else 0)
 
     def __call__(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices) -> float:
         V = _as_f64(vertices)
         e = np.zeros(1)
         _check(_load().ipcg_barrier_energy(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
-                                           int(self.use_physical_barrier), _ptr(e)))
+                                           self._options, _ptr(e)))
         return float(e[0])
 
     def gradient(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices):
@@ -487,7 +495,7 @@ class BarrierPotential:
         else:
             g = np.zeros(V.size)
         _check(_load().ipcg_barrier_gradient(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
-                                             int(self.use_physical_barrier), _ptr(g)))
+                                             self._options, _ptr(g)))
         return g
 
     def hessian(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices,
@@ -495,7 +503,7 @@ class BarrierPotential:
         V = _as_f64(vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_hessian(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
-                                            int(self.use_physical_barrier), int(project_hessian_to_psd),
+                                            self._options, int(project_hessian_to_psd),
                                             C.byref(h)))
         return _csr_to_scipy(h, 3 * mesh.num_vertices)
 
@@ -504,7 +512,7 @@ class BarrierPotential:
         V = _as_f64(vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_hessian(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
-                                            int(self.use_physical_barrier), int(project_hessian_to_psd),
+                                            self._options, int(project_hessian_to_psd),
                                             C.byref(h)))
         return DeviceCSR(h, 3 * mesh.num_vertices)
 
@@ -521,7 +529,7 @@ class BarrierPotential:
             g = np.zeros(3 * mesh.num_vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_energy_gradient_hessian(
-            collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, int(self.use_physical_barrier),
+            collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, self._options,
             int(project_hessian_to_psd), _ptr(e), _ptr(g), C.byref(h)))
         return float(e[0]), g, DeviceCSR(h, 3 * mesh.num_vertices)
 
@@ -532,7 +540,7 @@ class BarrierPotential:
         g = np.zeros(3 * mesh.num_vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_energy_gradient_hessian(
-            collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, int(self.use_physical_barrier),
+            collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, self._options,
             int(project_hessian_to_psd), _ptr(e), _ptr(g), C.byref(h)))
         return float(e[0]), g, _csr_to_scipy(h, 3 * mesh.num_vertices)
 
