@@ -548,7 +548,7 @@ __device__ double mollifier(const Local& c, const V3* x, double* gm, double* Hm,
 // replaying the recorded rotations on e_i, which costs a few hundred flops
 // per vector instead of updating all of Q at every rotation.
 constexpr int MAXR = 9;
-constexpr int MAXROT = 256; // recorded rotations; beyond, Q is accumulated
+constexpr int MAXROT = 128; // recorded rotations; beyond, Q is accumulated
 
 __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* d, double* Q, double* rc, double* rs,
     int8_t* rk, int& nrot, double* hv, double* htau)
@@ -701,31 +701,23 @@ template <int NS> __device__ __forceinline__ constexpr double contrast(int k, in
                   : (a == 0 ? 0.70710678118654752440 : -0.70710678118654752440);
 }
 
-// M = C H C^T (rows of M with stride MAXR), H row-major N x N.
+// M = C H C^T (rows of M with stride MAXR), H row-major N x N, one row of
+// M at a time (row 3k+c of C H, then its product with C^T), so no N-wide
+// intermediate matrix is kept.
 template <int NS> __device__ void to_contrasts(const double* H, double* M)
 {
-    constexpr int N = 3 * NS, m = 3 * (NS - 1);
-    double T[m * N];
+    constexpr int N = 3 * NS;
 #pragma unroll 1
-    for (int j = 0; j < N; ++j) {
-        double col[N];
-#pragma unroll
-        for (int r = 0; r < N; ++r) col[r] = H[r * N + j];
-#pragma unroll
-        for (int k = 0; k < NS - 1; ++k)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                double s = 0;
-#pragma unroll
-                for (int a = 0; a < NS; ++a) s += contrast<NS>(k, a) * col[3 * a + c];
-                T[(3 * k + c) * N + j] = s;
-            }
-    }
-#pragma unroll 1
-    for (int r = 0; r < m; ++r) {
+    for (int r = 0; r < 3 * (NS - 1); ++r) {
+        const int k = r / 3, c = r % 3;
         double row[N];
 #pragma unroll
-        for (int j = 0; j < N; ++j) row[j] = T[r * N + j];
+        for (int j = 0; j < N; ++j) {
+            double s = 0;
+#pragma unroll
+            for (int a = 0; a < NS; ++a) s += contrast<NS>(k, a) * H[(3 * a + c) * N + j];
+            row[j] = s;
+        }
 #pragma unroll
         for (int l = 0; l < NS - 1; ++l)
 #pragma unroll
@@ -987,6 +979,12 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restr
     return lo;
 }
 
+// Launch width of the local Hessian and PSD kernels: one warp per block.
+// Their per-contact work is long and even, and a type's contacts can be few
+// (5,465 FV contacts fill only 43 blocks of 128 threads on 152 SMs), so small
+// blocks spread them over all SMs without a ragged last wave.
+constexpr int LH_BLOCK = 32;
+
 // Local Hessian of one contact (normal_potential.cpp:174-232 before the PSD
 // projection) written to its 144-double slab of Hs (row-major, N = 3n).
 // One instantiation per contact type (contacts of a type are contiguous:
@@ -994,7 +992,7 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restr
 // proj[i] = 0 marks the mollified edge-edge case with m(x) <= 0, which the
 // reference returns without projection.
 template <int TYPE>
-__global__ void __launch_bounds__(BLOCK) k_local_hessian(ContactsView cv, const int* __restrict__ E,
+__global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, const int* __restrict__ E,
     const int* __restrict__ F, const double* __restrict__ V, const Params* __restrict__ sp, SceneView sv,
     double* __restrict__ Hs, uint8_t* __restrict__ proj, int64_t first, int64_t count)
 {
@@ -1067,7 +1065,8 @@ __device__ __forceinline__ int stencil_size(const ContactsView& cv, int64_t i)
 }
 
 // PSD projection (eigen_ext.tpp:64-108) of every local Hessian, in place.
-__global__ void __launch_bounds__(BLOCK) k_psd(ContactsView cv, double* __restrict__ Hs,
+constexpr int PSD_BLOCK = LH_BLOCK;
+__global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, double* __restrict__ Hs,
     const uint8_t* __restrict__ proj, int method, int* __restrict__ fail)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
@@ -1409,21 +1408,22 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
                 const int64_t first[4] = { 0, cc.nvv, cc.nvv + cc.nev, cc.nvv + cc.nev + cc.nee };
                 const int64_t count[4] = { cc.nvv, cc.nev, cc.nee, cc.nfv };
                 if (count[0])
-                    IPCG_LAUNCH("k_local_hessian_vv", t, k_local_hessian<CT_VV><<<grid_for(count[0], BLOCK), BLOCK, 0,
+                    IPCG_LAUNCH("k_local_hessian_vv", t, k_local_hessian<CT_VV><<<grid_for(count[0], LH_BLOCK), LH_BLOCK, 0,
                         t>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[0], count[0]));
                 if (count[1])
-                    IPCG_LAUNCH("k_local_hessian_ev", t, k_local_hessian<CT_EV><<<grid_for(count[1], BLOCK), BLOCK, 0,
+                    IPCG_LAUNCH("k_local_hessian_ev", t, k_local_hessian<CT_EV><<<grid_for(count[1], LH_BLOCK), LH_BLOCK, 0,
                         t>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[1], count[1]));
                 IPCG_CUDA(cudaEventRecord(m->ev_side, t));
                 if (count[2])
-                    IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], BLOCK), BLOCK, 0,
+                    IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], LH_BLOCK), LH_BLOCK, 0,
                         s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[2], count[2]));
                 if (count[3])
-                    IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], BLOCK), BLOCK, 0,
+                    IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], LH_BLOCK), LH_BLOCK, 0,
                         s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[3], count[3]));
                 IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
                 if (a.psd != IPCG_PSD_NONE)
-                    IPCG_LAUNCH("k_psd", s, k_psd<<<nblk_c, BLOCK, 0, s>>>(cc, m->hs.p, m->proj.p, a.psd, d_fail));
+                    IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(nc, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, m->hs.p,
+                        m->proj.p, a.psd, d_fail));
                 // sparsity pattern: sort (block key, contribution) and run-length encode
                 IPCG_LAUNCH("k_block_keys", t, k_block_keys<<<nblk_c, BLOCK, 0, t>>>(cc, m->E.p, m->F.p,
                     m->keys_a.p, ids_in, nk, gd));
