@@ -262,6 +262,32 @@ int ipcg_collision_free_stepsize_batch(const ipcg_mesh* mesh,
                                        double* steps, int64_t* n_candidates);
 
 /* ---------------------------------------------------------------------- */
+/* Newton-loop neighbours of the path                                      */
+/* ---------------------------------------------------------------------- */
+
+/* Replaces NormalCollisions::compute_minimum_distance(mesh, V)
+ * (normal_collisions.cpp:209-233): the smallest SQUARED distance over the
+ * collision set, each contact measured with its own distance; +inf when the
+ * set is empty. */
+int ipcg_collisions_minimum_distance(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                                     const double* vertices, double* out);
+
+/* Replaces is_step_collision_free(mesh, V0, V1, min_distance, nullptr,
+ * TightInclusionCCD(tolerance, max_iterations, conservative_rescaling))
+ * (ipc.hpp, ipc.cpp:20-40, candidates.cpp:224-250): *out = 1 when no
+ * swept-box candidate's CCD reports a hit over the step. */
+int ipcg_is_step_collision_free(const ipcg_mesh* mesh,
+                                const double* vertices_t0, const double* vertices_t1,
+                                double min_distance, double tolerance,
+                                int64_t max_iterations, double conservative_rescaling, int* out);
+
+/* Replaces has_intersections(mesh, V) (ipc.cpp:110-167) for 3D meshes: *out
+ * = 1 when some edge crosses a triangle it does not share a vertex with
+ * (exact orientation predicates, then the crossing point's coordinates as
+ * in geometry/intersection.cpp:120-147). */
+int ipcg_has_intersections(const ipcg_mesh* mesh, const double* vertices, int* out);
+
+/* ---------------------------------------------------------------------- */
 /* Serving: requests from many simulations over resident scenes            */
 /* ---------------------------------------------------------------------- */
 

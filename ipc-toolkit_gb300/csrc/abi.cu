@@ -663,6 +663,44 @@ int ipcg_collision_free_stepsize_batch(const ipcg_mesh* mesh, const double* V0, 
     });
 }
 
+int ipcg_collisions_minimum_distance(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double* out)
+{
+    return guarded([&] {
+        require(c && mesh && out && (V || mesh->nV == 0), "NULL argument");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        *out = collisions_min_distance(c, m, dV);
+    });
+}
+
+int ipcg_is_step_collision_free(const ipcg_mesh* mesh, const double* V0, const double* V1, double min_distance,
+    double tolerance, int64_t max_iterations, double rescale, int* out)
+{
+    return guarded([&] {
+        require(mesh && out && ((V0 && V1) || mesh->nV == 0), "NULL argument");
+        require(min_distance >= 0, "min_distance must be non-negative");
+        require(tolerance > 0, "tolerance must be positive");
+        require(rescale > 0 && rescale <= 1, "conservative_rescaling must be in (0, 1]");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* d0 = stage_positions(m, V0, m->V0);
+        const double* d1 = stage_positions(m, V1, m->V1);
+        *out = step_collision_free(m, d0, d1, min_distance, tolerance, max_iterations, rescale) ? 1 : 0;
+    });
+}
+
+int ipcg_has_intersections(const ipcg_mesh* mesh, const double* V, int* out)
+{
+    return guarded([&] {
+        require(mesh && out && (V || mesh->nV == 0), "NULL argument");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        *out = has_intersections(m, dV) ? 1 : 0;
+    });
+}
+
 int ipcg_ccd_stencils(int is_ee, int64_t n, const double* x0, const double* x1, double min_distance, double tmax,
     double tolerance, int64_t max_iterations, double rescale, int8_t* hit, double* toi)
 {

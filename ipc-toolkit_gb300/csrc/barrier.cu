@@ -1297,6 +1297,30 @@ std::vector<Chunk> plan_chunks(const ipcg_collisions* cs, ipcg_mesh* m, const Co
     return out;
 }
 
+// Smallest squared distance over the collision set
+// (normal_collisions.cpp:209-233: "actually distance squared"), each contact
+// measured with its own distance (the one its energy uses).  Squared
+// distances are non-negative, so their bit patterns order like the values.
+__global__ void __launch_bounds__(BLOCK) k_min_distance(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, unsigned long long* __restrict__ out)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double d = __longlong_as_double(0x7ff0000000000000ULL);
+    if (i < n) {
+        Local c;
+        load_contact(cv, E, F, i, c);
+        V3 x[4];
+        gather(V, c, x);
+        double g[12];
+        d = fmax(contact_distance(c, x, g, nullptr), 0.0);
+    }
+    typedef cub::BlockReduce<double, BLOCK> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const double mn = BR(tmp).Reduce(d, [](double a, double b) { return fmin(a, b); });
+    if (threadIdx.x == 0) atomicMin(out, (unsigned long long)__double_as_longlong(mn));
+}
+
 } // namespace
 
 void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
@@ -1471,6 +1495,26 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     }
     if (hess && (m->h_counters.p[1] & 1))
         throw Error(IPCG_ERR_CUDA, "unable to project matrix onto positive semi-definite cone");
+}
+
+double collisions_min_distance(const ipcg_collisions* cs, ipcg_mesh* m, const double* V)
+{
+    const int64_t n = cs->size();
+    if (n == 0) return __builtin_inf();
+    cudaStream_t s = m->stream;
+    ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
+        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
+    m->toi_bits.reserve(1);
+    const unsigned long long inf = 0x7ff0000000000000ULL;
+    IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, &inf, sizeof(inf), cudaMemcpyHostToDevice, s));
+    IPCG_LAUNCH("k_min_distance", s, k_min_distance<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V,
+        m->toi_bits.p));
+    unsigned long long bits = 0;
+    IPCG_CUDA(cudaMemcpyAsync(&bits, m->toi_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    double d;
+    memcpy(&d, &bits, sizeof(d));
+    return d;
 }
 
 } // namespace ipcg

@@ -15,6 +15,7 @@
 
 #include "geom.cuh"
 #include "internal.cuh"
+#include "predicates.cuh"
 #include "profile.cuh"
 
 namespace cg = cooperative_groups;
@@ -301,6 +302,53 @@ __global__ void k_traverse_fv(const float4* __restrict__ lo, const float4* __res
     }
 }
 
+// has_intersections (ipc.cpp:110-167): every edge (a leaf of the edge
+// tree) queries the face tree; pairs sharing a vertex are skipped
+// (broad_phase.cpp:164-179) and the others get the exact edge-triangle test.
+// The first intersection sets *found, which every thread polls so the
+// search stops early.
+__global__ void k_edges_cross_faces(const float4* __restrict__ elo, const float4* __restrict__ ehi, int ne,
+    const float4* __restrict__ flo, const float4* __restrict__ fhi, const int* __restrict__ ffirst,
+    const int* __restrict__ flast, const int* __restrict__ leaf_scene, SceneView sv, int nf,
+    const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ V, int* found, int* guard)
+{
+    const int qi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qi >= ne || nf < 1) return;
+    const float4 qlo = elo[ne - 1 + qi], qhi = ehi[ne - 1 + qi];
+    const int e = __float_as_int(qlo.w);
+    const int a0 = E[2 * e], a1 = E[2 * e + 1];
+    const int qs = sv.of(a0);
+    const bool batched = sv.vscene != nullptr;
+    const V3 e0 = load_v3(V, a0), e1 = load_v3(V, a1);
+    int stack[STACK];
+    int sp = 0;
+    stack[sp++] = 0;
+    int visits = 0;
+    while (sp > 0) {
+        if ((++visits & 31) == 0 && *(volatile int*)found) return;
+        const int v = stack[--sp];
+        if (other_scenes(ffirst, flast, leaf_scene, batched, v, qs)) continue;
+        const float4 vlo = flo[v], vhi = fhi[v];
+        if (!overlap(qlo, qhi, vlo, vhi)) continue;
+        if (v >= nf - 1) {
+            const int f = __float_as_int(vlo.w);
+            const int b0 = F[3 * f], b1 = F[3 * f + 1], b2 = F[3 * f + 2];
+            if (a0 == b0 || a0 == b1 || a0 == b2 || a1 == b0 || a1 == b1 || a1 == b2) continue;
+            if (exact::edge_intersects_triangle(e0, e1, load_v3(V, b0), load_v3(V, b1), load_v3(V, b2))) {
+                atomicExch(found, 1);
+                return;
+            }
+        } else {
+            if (sp + 2 > STACK) {
+                atomicOr(guard, GUARD_STACK);
+                return;
+            }
+            stack[sp++] = __float_as_int(vhi.w);
+            stack[sp++] = __float_as_int(vlo.w);
+        }
+    }
+}
+
 } // namespace
 
 void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const double* V1, const double* scene_r)
@@ -342,6 +390,39 @@ void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind, const double* V0, const doubl
         IPCG_LAUNCH("k_refit", s, k_refit<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(n, bvh.lo.p, bvh.hi.p, bvh.parent.p,
             bvh.flags.p));
     }
+}
+
+bool has_intersections(ipcg_mesh* m, const double* V)
+{
+    cudaStream_t s = m->stream;
+    const int nV = (int)m->nV;
+    if (m->nE == 0 || m->nF == 0) return false;
+    // boxes inflated by 1e-6 of the bounding-box diagonal (ipc.cpp:127-128)
+    const int nb = 256;
+    m->bounds.reserve(6 * nb);
+    IPCG_LAUNCH("k_bounds_partial", s, k_bounds_partial<<<nb, BLOCK, 0, s>>>(V, V, nV, m->bounds.p));
+    IPCG_LAUNCH("k_bounds_final", s, k_bounds_final<<<1, 32, 0, s>>>(m->bounds.p, nb));
+    double b[6];
+    IPCG_CUDA(cudaMemcpyAsync(b, m->bounds.p, sizeof(b), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    const double dx = b[3] - b[0], dy = b[4] - b[1], dz = b[5] - b[2];
+    const int ns = (int)m->n_scenes;
+    std::vector<double> r(ns, 1e-6 * sqrt(dx * dx + dy * dy + dz * dz));
+    m->scene_r.reserve(ns);
+    IPCG_CUDA(cudaMemcpyAsync(m->scene_r.p, r.data(), sizeof(double) * ns, cudaMemcpyHostToDevice, s));
+    build_lbvh(m, m->ebvh, 2, V, V, m->scene_r.p);
+    build_lbvh(m, m->fbvh, 3, V, V, m->scene_r.p);
+    m->counters.reserve(8);
+    m->h_counters.reserve(8);
+    IPCG_CUDA(cudaMemsetAsync(m->counters.p, 0, sizeof(int) * 8, s));
+    const SceneView sv = scene_view(m);
+    IPCG_LAUNCH("k_edges_cross_faces", s, k_edges_cross_faces<<<grid_for(m->ebvh.n, 128), 128, 0, s>>>(m->ebvh.lo.p,
+        m->ebvh.hi.p, m->ebvh.n, m->fbvh.lo.p, m->fbvh.hi.p, m->fbvh.first.p, m->fbvh.last.p, m->fbvh.leaf_scene.p,
+        sv, m->fbvh.n, m->E.p, m->F.p, V, m->counters.p + 0, m->counters.p + 2));
+    IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, m->counters.p, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    if (m->h_counters.p[2] & GUARD_STACK) throw Error(IPCG_ERR_CUDA, "LBVH traversal stack overflow");
+    return m->h_counters.p[0] != 0;
 }
 
 void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, const double* scene_r, int64_t& n_ee,

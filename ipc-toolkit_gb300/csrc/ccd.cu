@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
     const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,
     CCDParams P, unsigned long long* toi_bits, long long budget, const int* __restrict__ list,
-    const int* __restrict__ list_n, int* __restrict__ hard, int* __restrict__ hard_n)
+    const int* __restrict__ list_n, int* __restrict__ hard, int* __restrict__ hard_n, int any_hit)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = list ? *list_n : n_ee + n_fv;
@@ -549,7 +549,10 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     double toi = __longlong_as_double(0x7ff0000000000000ULL);
     Budget bud { budget, 0 };
     const int st = stencil_ccd(q, __ldg(min_distance + scene), P, tmax, toi, best, bud);
-    if (st == CCD_HIT && toi < tmax) atomicMin(best, (unsigned long long)__double_as_longlong(toi));
+    // any_hit (is_step_collision_free): a hit anywhere answers the question;
+    // setting the scene's earliest time to 0 also stops every other query
+    if (st == CCD_HIT && any_hit) atomicMin(best, 0ULL);
+    else if (st == CCD_HIT && toi < tmax) atomicMin(best, (unsigned long long)__double_as_longlong(toi));
     else if (st == CCD_UNRESOLVED) hard[atomicAdd(hard_n, 1)] = i;
 }
 
@@ -634,14 +637,47 @@ void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, c
     const int2* cee = m->cand.p;
     const int2* cfv = m->cand.p + m->cand_cap;
     IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n));
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n, 0));
     IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr));
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, 0));
     std::vector<unsigned long long> bits(ns);
     IPCG_CUDA(cudaMemcpyAsync(bits.data(), m->toi_bits.p, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost,
         s));
     IPCG_CUDA(cudaStreamSynchronize(s));
     for (int k = 0; k < ns; ++k) memcpy(steps + k, &bits[k], sizeof(double));
+}
+
+bool step_collision_free(ipcg_mesh* m, const double* V0, const double* V1, double min_distance, double tolerance,
+    int64_t max_iterations, double rescale)
+{
+    if (m->n_scenes != 1) throw Error(IPCG_ERR_INVALID, "is_step_collision_free takes a single-scene mesh");
+    cudaStream_t s = m->stream;
+    const double h[2] = { 0.5 * min_distance, min_distance };
+    m->scene_md.reserve(2);
+    IPCG_CUDA(cudaMemcpyAsync(m->scene_md.p, h, sizeof(h), cudaMemcpyHostToDevice, s));
+    int64_t n_ee = 0, n_fv = 0;
+    detect_candidates(m, V0, V1, m->scene_md.p, n_ee, n_fv);
+    if (n_ee + n_fv == 0) return true;
+    m->toi_bits.reserve(1);
+    const unsigned long long one = 0x3ff0000000000000ULL; // 1.0
+    IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    const CCDParams P { tolerance, (long long)max_iterations, rescale };
+    const SceneView sv = scene_view(m);
+    const int nc = (int)(n_ee + n_fv);
+    m->ivals_a.reserve(nc + 1);
+    int* hard = m->ivals_a.p;
+    int* hard_n = m->counters.p + 3;
+    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
+    const int2* cee = m->cand.p;
+    const int2* cfv = m->cand.p + m->cand_cap;
+    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
+        m->E.p, m->F.p, m->scene_md.p + 1, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n, 1));
+    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
+        m->E.p, m->F.p, m->scene_md.p + 1, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, 1));
+    unsigned long long bits = 1;
+    IPCG_CUDA(cudaMemcpyAsync(&bits, m->toi_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    return bits != 0;
 }
 
 void ccd_stencils(cudaStream_t s, int is_ee, int64_t n, const double* x0, const double* x1, double min_distance,

@@ -258,6 +258,14 @@ struct BarrierArgs {
 };
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null);
+// has_intersections (ipc.cpp:110-167): some edge crosses a triangle it does
+// not share a vertex with (a batch answers for all its scenes together).
+bool has_intersections(ipcg_mesh* m, const double* V);
+// Smallest squared distance over the collision set (+inf when empty).
+double collisions_min_distance(const ipcg_collisions* c, ipcg_mesh* m, const double* V);
+// is_step_collision_free (ipc.cpp:20-40): no candidate has a hit in [0, 1].
+bool step_collision_free(ipcg_mesh* m, const double* V0, const double* V1, double min_distance, double tolerance,
+    int64_t max_iterations, double rescale);
 
 // Caller-owned device arrays of a collision set (layout of ipcg_collisions_get).
 struct ContactsNoAlloc {

@@ -81,6 +81,9 @@ def _load():
         "ipcg_barrier_batch": (i32, [P, P, P, P, P, i32, i32, P, P, PP]),
         "ipcg_collision_free_stepsize_batch": (i32, [P, P, P, P, d, i64, d, P, P]),
         "ipcg_set_hessian_chunk_contacts": (i32, [i64]),
+        "ipcg_collisions_minimum_distance": (i32, [P, P, P, P]),
+        "ipcg_is_step_collision_free": (i32, [P, P, P, d, d, i64, d, P]),
+        "ipcg_has_intersections": (i32, [P, P, P]),
         "ipcg_server_create": (i32, [i32, i64, PP]),
         "ipcg_server_destroy": (i32, [P]),
         "ipcg_server_add_scene": (i32, [P, P, P, d, d, d, P]),
@@ -429,6 +432,13 @@ class NormalCollisions:
             len(arrs[9]), _ptr(arrs[8]), _ptr(arrs[9])))
         self._cache = None
 
+    def compute_minimum_distance(self, mesh: CollisionMesh, vertices) -> float:
+        """normal_collisions.cpp:209-233: smallest squared distance (+inf if empty)."""
+        V = _as_f64(vertices)
+        out = np.zeros(1)
+        _check(_load().ipcg_collisions_minimum_distance(self._h, mesh._h, _ptr(V), _ptr(out)))
+        return float(out[0])
+
     @property
     def vv_collisions(self):
         return self.to_arrays()["vv"]
@@ -733,6 +743,25 @@ class Server:
         _check(_load().ipcg_server_stats(self._h, _ptr(st)))
         return {"completed": int(st[0]), "queued": int(st[1]), "running": int(st[2]), "releases": int(st[3]),
                 "resident_bytes": int(st[4])}
+
+
+def is_step_collision_free(mesh: CollisionMesh, vertices_t0, vertices_t1, min_distance: float = 0.0,
+                           broad_phase=None, narrow_phase_ccd: TightInclusionCCD = DEFAULT_NARROW_PHASE_CCD) -> bool:
+    """ipc.hpp is_step_collision_free (ipc.cpp:20-40)."""
+    V0, V1 = _as_f64(vertices_t0), _as_f64(vertices_t1)
+    out = np.zeros(1, np.int32)
+    _check(_load().ipcg_is_step_collision_free(
+        mesh._h, _ptr(V0), _ptr(V1), float(min_distance), narrow_phase_ccd.tolerance,
+        narrow_phase_ccd.max_iterations, narrow_phase_ccd.conservative_rescaling, _ptr(out)))
+    return bool(out[0])
+
+
+def has_intersections(mesh: CollisionMesh, vertices, broad_phase=None) -> bool:
+    """ipc.hpp has_intersections (ipc.cpp:110-167), 3D meshes."""
+    V = _as_f64(vertices)
+    out = np.zeros(1, np.int32)
+    _check(_load().ipcg_has_intersections(mesh._h, _ptr(V), _ptr(out)))
+    return bool(out[0])
 
 
 def compute_collision_free_stepsize_batch(batch: SceneBatch, vertices_t0, vertices_t1, min_distance=0.0,

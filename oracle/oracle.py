@@ -298,3 +298,40 @@ def ccd_stencil_positions(V0, V1, E, F, ee, fv):
     ids_ee = np.concatenate([E[ee[:, 0]], E[ee[:, 1]]], axis=1)
     ids_fv = np.concatenate([fv[:, 1:2], F[fv[:, 0]]], axis=1)
     return (V0[ids_ee], V1[ids_ee]), (V0[ids_fv], V1[ids_fv])
+
+
+def orient3d_exact(a, b, c, d):
+    """Exact sign of det(a-d, b-d, c-d) with rational arithmetic (small cases)."""
+    from fractions import Fraction as Fr
+    A = [[Fr(float(p[k])) - Fr(float(d[k])) for k in range(3)] for p in (a, b, c)]
+    det = (A[0][0] * (A[1][1] * A[2][2] - A[1][2] * A[2][1]) - A[0][1] * (A[1][0] * A[2][2] - A[1][2] * A[2][0])
+           + A[0][2] * (A[1][0] * A[2][1] - A[1][1] * A[2][0]))
+    return (det > 0) - (det < 0)
+
+
+def has_intersections_bruteforce(V, E, F):
+    """has_intersections (ipc.cpp:110-167) over every edge-face pair that shares
+    no vertex: exact orientations of the edge's endpoints against the face's
+    plane (geometry/intersection.cpp:120-147), then the crossing point's
+    barycentric coordinates and edge parameter from a dense solve.  Pure
+    Python: for small meshes only."""
+    V = np.asarray(V, np.float64)
+    for e in np.asarray(E):
+        for f in np.asarray(F):
+            if set(e.tolist()) & set(f.tolist()):
+                continue
+            e0, e1 = V[e[0]], V[e[1]]
+            t0, t1, t2 = V[f[0]], V[f[1]], V[f[2]]
+            o1 = orient3d_exact(t0, t1, t2, e0)
+            o2 = orient3d_exact(t0, t1, t2, e1)
+            if o1 != 0 and o2 != 0 and o1 == o2:
+                continue
+            M = np.stack([t1 - t0, t2 - t0, e0 - e1], axis=1)
+            try:
+                uvt = np.linalg.solve(M, e0 - t0)
+            except np.linalg.LinAlgError:
+                uvt = np.linalg.lstsq(M, e0 - t0, rcond=None)[0]
+            if uvt[0] >= 0 and uvt[1] >= 0 and uvt[0] + uvt[1] <= 1 and 0 <= uvt[2] <= 1:
+                return True
+    return False
+
