@@ -745,6 +745,48 @@ class Server:
                 "resident_bytes": int(st[4])}
 
 
+def _clamped_log_barrier_second_derivative(d, dhat):
+    """barrier.cpp:31-43 (on squared distances)."""
+    if d <= 0.0 or d >= dhat:
+        return 0.0
+    r = dhat / d
+    return (r + 2) * r - 2 * np.log(d / dhat) - 3
+
+
+def initial_barrier_stiffness(bbox_diagonal: float, dhat: float, average_mass: float, grad_energy, grad_barrier,
+                              min_barrier_stiffness_scale: float = 1e11, dmin: float = 0.0):
+    """barrier/adaptive_stiffness.cpp:12-48 with the default ClampedLogBarrier:
+    returns (kappa, max_barrier_stiffness).  The gradients may be numpy
+    arrays or CUDA tensors (their two dot products run where they live)."""
+    if not (average_mass > 0 and min_barrier_stiffness_scale > 0 and bbox_diagonal > 0):
+        raise ValueError("average_mass, min_barrier_stiffness_scale and bbox_diagonal must be positive")
+    dhat2, dmin2 = dhat * dhat, dmin * dmin
+    d0 = 1e-8 * bbox_diagonal + dmin
+    d0 *= d0
+    if d0 - dmin2 >= 2 * dmin * dhat + dhat2:
+        d0 = dmin * dhat + 0.5 * dhat2
+    kmin = 4 * d0 * _clamped_log_barrier_second_derivative(d0 - dmin2, 2 * dmin * dhat + dhat2)
+    kmin = min_barrier_stiffness_scale * average_mass / kmin
+    kmax = 100 * kmin
+    gb2 = float((grad_barrier * grad_barrier).sum())
+    kappa = 1.0
+    if gb2 > 0:
+        kappa = -float((grad_barrier * grad_energy).sum()) / gb2
+    return min(max(kappa, kmin), kmax), kmax
+
+
+def update_barrier_stiffness(prev_min_distance: float, min_distance: float, max_barrier_stiffness: float,
+                             barrier_stiffness: float, bbox_diagonal: float, dhat_epsilon_scale: float = 1e-9,
+                             dmin: float = 0.0) -> float:
+    """barrier/adaptive_stiffness.cpp:51-68: double the stiffness (up to the
+    maximum) while the minimum distance keeps shrinking below
+    (dhat_epsilon_scale (bbox_diagonal + dmin))^2."""
+    eps = (dhat_epsilon_scale * (bbox_diagonal + dmin)) ** 2
+    if prev_min_distance < eps and min_distance < eps and min_distance < prev_min_distance:
+        return min(max_barrier_stiffness, 2 * barrier_stiffness)
+    return barrier_stiffness
+
+
 def is_step_collision_free(mesh: CollisionMesh, vertices_t0, vertices_t1, min_distance: float = 0.0,
                            broad_phase=None, narrow_phase_ccd: TightInclusionCCD = DEFAULT_NARROW_PHASE_CCD) -> bool:
     """ipc.hpp is_step_collision_free (ipc.cpp:20-40)."""

@@ -83,3 +83,24 @@ def test_server_argument_validation_without_gpu(ipctk):
     assert b"unknown scene" in L.ipcg_last_error()
     L.ipcg_server_destroy.argtypes = [C.c_void_p]
     assert L.ipcg_server_destroy(h) == 0
+
+
+def test_adaptive_stiffness_formulas(ipctk):
+    """initial/update_barrier_stiffness (barrier/adaptive_stiffness.cpp:12-68)
+    on hand-checked values."""
+    import math
+    dhat, diag, mass = 1e-3, 2.0, 0.5
+    d0 = (1e-8 * diag) ** 2
+    r = dhat * dhat / d0
+    b2 = (r + 2) * r - 2 * math.log(d0 / (dhat * dhat)) - 3
+    kmin = 1e11 * mass / (4 * d0 * b2)
+    gE = np.array([1.0, -2.0, 0.5])
+    gB = np.array([-0.5, 1.0, 0.0])
+    kappa, kmax = ipctk.initial_barrier_stiffness(diag, dhat, mass, gE, gB)
+    assert math.isclose(kmax, 100 * kmin, rel_tol=1e-14)
+    k_raw = -(gB @ gE) / (gB @ gB)
+    assert kappa == min(max(k_raw, kmin), kmax)
+    eps = (1e-9 * diag) ** 2
+    assert ipctk.update_barrier_stiffness(0.5 * eps, 0.25 * eps, 10.0, 3.0, diag) == 6.0
+    assert ipctk.update_barrier_stiffness(0.5 * eps, 0.25 * eps, 5.0, 3.0, diag) == 5.0
+    assert ipctk.update_barrier_stiffness(0.25 * eps, 0.5 * eps, 10.0, 3.0, diag) == 3.0
