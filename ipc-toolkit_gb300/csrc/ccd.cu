@@ -50,8 +50,24 @@ constexpr long long CCD_PASS1_BUDGET = 512;
 
 struct Query {
     V3 s[4], e[4];
+    V3 d[4]; // e - s: the same value the evaluation form (b - a) t + a computes per box
     bool vf;
+    __device__ void set_deltas()
+    {
+        for (int k = 0; k < 4; ++k) d[k] = e[k] - s[k];
+    }
 };
+
+// Order-preserving integer keys of finite doubles: signed 64-bit comparison
+// of the keys orders the values (negative zero just below positive zero),
+// so minima, maxima and comparisons run on the integer pipe, which GB300
+// issues 32 times faster than FP64.  The results are the same doubles.
+__device__ __forceinline__ long long okey(double x)
+{
+    const long long b = __double_as_longlong(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double ovalue(long long k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
 
 struct CBox {
     double lo[3];
@@ -138,8 +154,8 @@ __device__ void domain_tol(const Query& q, double delta, double tol[3])
 // a component inside it stays inside).
 __device__ __forceinline__ bool halving_excludes(const double f[2][2][2], int d, double r)
 {
-    const double inf = __longlong_as_double(0x7ff0000000000000ULL);
-    double lo0 = inf, hi0 = -inf, lo1 = inf, hi1 = -inf, lom = inf, him = -inf;
+    const long long big = 0x7fffffffffffffffLL;
+    long long lo0 = big, hi0 = -big, lo1 = big, hi1 = -big, lom = big, him = -big;
     for (int a = 0; a < 2; ++a)
         for (int b = 0; b < 2; ++b) {
             double f0, f1;
@@ -153,16 +169,16 @@ __device__ __forceinline__ bool halving_excludes(const double f[2][2][2], int d,
                 f0 = f[a][b][0];
                 f1 = f[a][b][1];
             }
-            const double m = (f1 + f0) * 0.5;
-            lo0 = fmin(lo0, f0);
-            hi0 = fmax(hi0, f0);
-            lo1 = fmin(lo1, f1);
-            hi1 = fmax(hi1, f1);
-            lom = fmin(lom, m);
-            him = fmax(him, m);
+            const long long k0 = okey(f0), k1 = okey(f1), km = okey((f1 + f0) * 0.5);
+            lo0 = min(lo0, k0);
+            hi0 = max(hi0, k0);
+            lo1 = min(lo1, k1);
+            hi1 = max(hi1, k1);
+            lom = min(lom, km);
+            him = max(him, km);
         }
-    const double a0 = fmin(lo0, lom), b0 = fmax(hi0, him), a1 = fmin(lo1, lom), b1 = fmax(hi1, him);
-    return a0 > r || b0 < -r || a1 > r || b1 < -r;
+    const long long kr = okey(r), knr = okey(-r);
+    return min(lo0, lom) > kr || max(hi0, him) < knr || min(lo1, lom) > kr || max(hi1, him) < knr;
 }
 
 // Returns zero_in; sets box_in, the codomain widths cw[c], whether component
@@ -184,10 +200,7 @@ __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], do
         double f[2][2][2];
         for (int i = 0; i < 2; ++i) {
             double x[4];
-            for (int k = 0; k < 4; ++k) {
-                const double a = comp(q.s[k], c), e = comp(q.e[k], c);
-                x[k] = (e - a) * ts[i] + a;
-            }
+            for (int k = 0; k < 4; ++k) x[k] = comp(q.d[k], c) * ts[i] + comp(q.s[k], c);
             if (q.vf) {
                 const double d21 = x[2] - x[1], d31 = x[3] - x[1];
                 for (int j = 0; j < 2; ++j)
@@ -200,28 +213,35 @@ __device__ bool inclusion(const Query& q, const CBox& b, const double err[3], do
                     for (int k = 0; k < 2; ++k) f[i][j][k] = ea[j] - eb[k];
             }
         }
-        double mn = f[0][0][0], mx = f[0][0][0];
+        long long kmn = okey(f[0][0][0]), kmx = kmn;
         for (int i = 0; i < 2; ++i)
             for (int j = 0; j < 2; ++j)
                 for (int k = 0; k < 2; ++k) {
-                    mn = fmin(mn, f[i][j][k]);
-                    mx = fmax(mx, f[i][j][k]);
+                    const long long kf = okey(f[i][j][k]);
+                    kmn = min(kmn, kf);
+                    kmx = max(kmx, kf);
                 }
         const double r = err[c] + ms;
-        if (mn > r || mx < -r) return false;
-        inside[c] = (mn >= -r && mx <= r);
-        cw[c] = mx - mn;
+        const long long kr = okey(r), knr = okey(-r);
+        if (kmn > kr || kmx < knr) return false;
+        inside[c] = (kmn >= knr && kmx <= kr);
+        cw[c] = ovalue(kmx) - ovalue(kmn);
         var[c][0] = var[c][1] = var[c][2] = 0;
         if (!inside[c]) {
             box_in = false;
             for (int d = 0; d < 3; ++d)
                 if (!(excl >> d & 1) && halving_excludes(f, d, r)) excl |= 1 << d;
+            // non-negative doubles order like their bit patterns
+            long long v0 = 0, v1 = 0, v2 = 0;
             for (int j = 0; j < 2; ++j)
                 for (int k = 0; k < 2; ++k) {
-                    var[c][0] = fmax(var[c][0], fabs(f[1][j][k] - f[0][j][k]));
-                    var[c][1] = fmax(var[c][1], fabs(f[j][1][k] - f[j][0][k]));
-                    var[c][2] = fmax(var[c][2], fabs(f[j][k][1] - f[j][k][0]));
+                    v0 = max(v0, __double_as_longlong(fabs(f[1][j][k] - f[0][j][k])));
+                    v1 = max(v1, __double_as_longlong(fabs(f[j][1][k] - f[j][0][k])));
+                    v2 = max(v2, __double_as_longlong(fabs(f[j][k][1] - f[j][k][0])));
                 }
+            var[c][0] = __longlong_as_double(v0);
+            var[c][1] = __longlong_as_double(v1);
+            var[c][2] = __longlong_as_double(v2);
         }
     }
     return true;
@@ -522,6 +542,7 @@ __device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_e
         q.s[k] = load_v3(V0, ids[k]);
         q.e[k] = load_v3(V1, ids[k]);
     }
+    q.set_deltas();
     return ids[0];
 }
 
@@ -567,6 +588,7 @@ __global__ void k_ccd_stencils(int is_ee, int n, const double* __restrict__ x0, 
         q.s[k] = load_v3(x0 + 12 * (int64_t)i, k);
         q.e[k] = load_v3(x1 + 12 * (int64_t)i, k);
     }
+    q.set_deltas();
     double t = __longlong_as_double(0x7ff0000000000000ULL);
     Budget bud { 0, 0 };
     const int h = stencil_ccd(q, min_distance, P, tmax, t, nullptr, bud);
