@@ -979,6 +979,16 @@ __device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restr
     return lo;
 }
 
+// Local-Hessian scratch, element-major: element k (row-major within the
+// 3n x 3n matrix) of contact i is at p[k * stride + i].  A warp's 32
+// consecutive contacts then read and write 256 contiguous bytes per element
+// instead of 32 addresses 1,152 bytes apart.
+struct Slab {
+    double* p;
+    int64_t stride;
+    __device__ __forceinline__ double& at(int64_t i, int k) const { return p[(int64_t)k * stride + i]; }
+};
+
 // Launch width of the local Hessian and PSD kernels: one warp per block.
 // Their per-contact work is long and even, and a type's contacts can be few
 // (5,465 FV contacts fill only 43 blocks of 128 threads on 152 SMs), so small
@@ -994,7 +1004,7 @@ constexpr int LH_BLOCK = 32;
 template <int TYPE>
 __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, const int* __restrict__ E,
     const int* __restrict__ F, const double* __restrict__ V, const Params* __restrict__ sp, SceneView sv,
-    double* __restrict__ Hs, uint8_t* __restrict__ proj, int64_t first, int64_t count)
+    Slab hs, uint8_t* __restrict__ proj, int64_t first, int64_t count)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= count) return;
@@ -1006,13 +1016,12 @@ __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, con
     gather(V, c, x);
     constexpr int NS = TYPE == CT_VV ? 2 : (TYPE == CT_EV ? 3 : 4);
     constexpr int N = 3 * NS;
-    double* __restrict__ out = Hs + 144 * i;
     if (TYPE == CT_FV && fp32_contact(P, c, x)) {
         float gf[12], Hf[144];
         const float d = fv_local_f(x, gf, Hf);
         const float w = (float)c.w, a = w * fd2f(P, d), b = w * fd1f(P, d);
         for (int r = 0; r < 12; ++r)
-            for (int q = 0; q < 12; ++q) out[r * 12 + q] = (double)(a * gf[r] * gf[q] + b * Hf[r * 12 + q]);
+            for (int q = 0; q < 12; ++q) hs.at(i, r * 12 + q) = (double)(a * gf[r] * gf[q] + b * Hf[r * 12 + q]);
         proj[i] = 1;
         return;
     }
@@ -1033,13 +1042,13 @@ __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, con
         if (act && m <= 0) {
             double gm[12];
             mollifier(c, x, gm, H, act);
-            for (int k = 0; k < 144; ++k) out[k] = (c.w * fv) * H[k];
+            for (int k = 0; k < 144; ++k) hs.at(i, k) = (c.w * fv) * H[k];
             pr = 0;
         } else {
             const double fd = fd1(P, d), fdd = fd2(P, d);
             const double wm = c.w * m;
             for (int r = 0; r < 12; ++r)
-                for (int q = 0; q < 12; ++q) out[r * 12 + q] = (wm * fdd) * g[r] * g[q] + (wm * fd) * H[r * 12 + q];
+                for (int q = 0; q < 12; ++q) hs.at(i, r * 12 + q) = (wm * fdd) * g[r] * g[q] + (wm * fd) * H[r * 12 + q];
             if (act) {
                 double gm[12];
                 mollifier(c, x, gm, H, act);
@@ -1047,14 +1056,14 @@ __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, con
                     for (int q = 0; q < 12; ++q) {
                         const double gfm_rq = (c.w * fd) * g[r] * gm[q];
                         const double gfm_qr = (c.w * fd) * g[q] * gm[r];
-                        out[r * 12 + q] += (c.w * fv) * H[r * 12 + q] + gfm_rq + gfm_qr;
+                        hs.at(i, r * 12 + q) += (c.w * fv) * H[r * 12 + q] + gfm_rq + gfm_qr;
                     }
             }
         }
     } else {
         const double fd = fd1(P, d), fdd = fd2(P, d);
         for (int r = 0; r < N; ++r)
-            for (int q = 0; q < N; ++q) out[r * N + q] = (c.w * fdd) * g[r] * g[q] + (c.w * fd) * H[r * N + q];
+            for (int q = 0; q < N; ++q) hs.at(i, r * N + q) = (c.w * fdd) * g[r] * g[q] + (c.w * fd) * H[r * N + q];
     }
     proj[i] = pr;
 }
@@ -1066,7 +1075,7 @@ __device__ __forceinline__ int stencil_size(const ContactsView& cv, int64_t i)
 
 // PSD projection (eigen_ext.tpp:64-108) of every local Hessian, in place.
 constexpr int PSD_BLOCK = LH_BLOCK;
-__global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, double* __restrict__ Hs,
+__global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, Slab hs,
     const uint8_t* __restrict__ proj, int method, int* __restrict__ fail)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
@@ -1075,13 +1084,12 @@ __global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, double* __re
     const int ns = stencil_size(cv, i);
     const int N = 3 * ns;
     double Hl[144];
-    double* __restrict__ slab = Hs + 144 * i;
-    for (int k = 0; k < N * N; ++k) Hl[k] = slab[k];
+    for (int k = 0; k < N * N; ++k) Hl[k] = hs.at(i, k);
     if (!project_psd(ns, Hl, method)) {
         atomicOr(fail, 1);
         return;
     }
-    for (int k = 0; k < N * N; ++k) slab[k] = Hl[k];
+    for (int k = 0; k < N * N; ++k) hs.at(i, k) = Hl[k];
 }
 
 // Contribution id j (position in the block-key list) -> contact, local
@@ -1116,7 +1124,7 @@ __device__ __forceinline__ void decode_contribution(const ContactsView& cv, int6
 // order and writes the value once.
 __global__ void k_assemble(ContactsView cv, const unsigned long long* __restrict__ ukeys,
     const int* __restrict__ run_start, const int* __restrict__ run_len, const int* __restrict__ contrib,
-    const double* __restrict__ Hs, const int* __restrict__ bptr, int r0, int64_t B0, int nb, double* __restrict__ val)
+    Slab hs, const int* __restrict__ bptr, int r0, int64_t B0, int nb, double* __restrict__ val)
 {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 9 * (int64_t)nb) return;
@@ -1128,7 +1136,7 @@ __global__ void k_assemble(ContactsView cv, const unsigned long long* __restrict
         int a, b, ns;
         decode_contribution(cv, contrib[s], i, a, b, ns);
         const int N = 3 * ns;
-        sum += Hs[144 * i + (3 * a + k) * N + 3 * b + l];
+        sum += hs.at(i, (3 * a + k) * N + 3 * b + l);
     }
     const unsigned long long key = ukeys[q];
     const int j = (int)(key >> 32) - r0;
@@ -1397,6 +1405,7 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         m->ivals_a.reserve(max_nk + max_nr + 3);
         m->ivals_b.reserve(3 * max_nk + 3);
         m->hs.reserve(144 * (max_n + 1));
+        const Slab slab { m->hs.p, max_n + 1 };
         m->proj.reserve(max_n + 1);
         m->counters.reserve(16);
         int* d_nb = m->counters.p + 14;
@@ -1433,20 +1442,20 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
                 const int64_t count[4] = { cc.nvv, cc.nev, cc.nee, cc.nfv };
                 if (count[0])
                     IPCG_LAUNCH("k_local_hessian_vv", t, k_local_hessian<CT_VV><<<grid_for(count[0], LH_BLOCK), LH_BLOCK, 0,
-                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[0], count[0]));
+                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[0], count[0]));
                 if (count[1])
                     IPCG_LAUNCH("k_local_hessian_ev", t, k_local_hessian<CT_EV><<<grid_for(count[1], LH_BLOCK), LH_BLOCK, 0,
-                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[1], count[1]));
+                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[1], count[1]));
                 IPCG_CUDA(cudaEventRecord(m->ev_side, t));
                 if (count[2])
                     IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], LH_BLOCK), LH_BLOCK, 0,
-                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[2], count[2]));
+                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[2], count[2]));
                 if (count[3])
                     IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], LH_BLOCK), LH_BLOCK, 0,
-                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, m->hs.p, m->proj.p, first[3], count[3]));
+                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[3], count[3]));
                 IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
                 if (a.psd != IPCG_PSD_NONE)
-                    IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(nc, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, m->hs.p,
+                    IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(nc, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, slab,
                         m->proj.p, a.psd, d_fail));
                 // sparsity pattern: sort (block key, contribution) and run-length encode
                 IPCG_LAUNCH("k_block_keys", t, k_block_keys<<<nblk_c, BLOCK, 0, t>>>(cc, m->E.p, m->F.p,
@@ -1479,7 +1488,7 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
             IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_pattern, 0));
             if (nb > 0)
                 IPCG_LAUNCH("k_assemble", s, k_assemble<<<grid_for(9 * (int64_t)nb, 256), 256, 0, s>>>(cc,
-                    m->keys_a.p, run_start, run_len, contrib, m->hs.p, bptr, r0, B0, nb, hess->val.p));
+                    m->keys_a.p, run_start, run_len, contrib, slab, bptr, r0, B0, nb, hess->val.p));
             B0 += nb;
         }
         hess->nnz = 9 * B0;
