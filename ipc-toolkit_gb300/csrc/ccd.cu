@@ -78,10 +78,15 @@ __device__ __forceinline__ double width_of(int lvl) { return ldexp(1.0, -lvl); }
 
 // Total order of boxes: lower corner (t, u, v), then levels.  Children come
 // after their parent.
+// Lower corners are sums of non-negative powers of two starting from +0, so
+// their bit patterns order like their values: the comparison runs on the
+// integer pipe.
 __device__ __forceinline__ bool box_before(const CBox& a, const CBox& b)
 {
-    for (int d = 0; d < 3; ++d)
-        if (a.lo[d] != b.lo[d]) return a.lo[d] < b.lo[d];
+    for (int d = 0; d < 3; ++d) {
+        const long long x = __double_as_longlong(a.lo[d]), y = __double_as_longlong(b.lo[d]);
+        if (x != y) return x < y;
+    }
     for (int d = 0; d < 3; ++d)
         if (a.lvl[d] != b.lvl[d]) return a.lvl[d] < b.lvl[d];
     return false;
