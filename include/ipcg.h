@@ -287,6 +287,43 @@ int ipcg_is_step_collision_free(const ipcg_mesh* mesh,
  * in geometry/intersection.cpp:120-147). */
 int ipcg_has_intersections(const ipcg_mesh* mesh, const double* vertices, int* out);
 
+/* Candidates (src/ipc/candidates/candidates.hpp): a kept broad-phase
+ * candidate set on the device (EE pairs, then FV (face, vertex) pairs) and
+ * the step-size rules that read it.  Single-scene 3D meshes. */
+typedef struct ipcg_candidates ipcg_candidates;
+int ipcg_candidates_create(ipcg_candidates** out);
+int ipcg_candidates_destroy(ipcg_candidates* candidates);
+/* Candidates::build(mesh, V, inflation_radius) (candidates.cpp:43-125) */
+int ipcg_candidates_build(ipcg_candidates* candidates, const ipcg_mesh* mesh,
+                          const double* vertices, double inflation_radius);
+/* Candidates::build(mesh, V0, V1, inflation_radius) (candidates.cpp:128-222) */
+int ipcg_candidates_build_swept(ipcg_candidates* candidates, const ipcg_mesh* mesh,
+                                const double* vertices_t0, const double* vertices_t1,
+                                double inflation_radius);
+/* number of EE and FV pairs: counts[2]; the pairs (any order) as (n, 2) int32 */
+int ipcg_candidates_counts(const ipcg_candidates* candidates, int64_t counts[2]);
+int ipcg_candidates_get(const ipcg_candidates* candidates, int32_t* ee, int32_t* fv);
+/* Candidates::compute_per_vertex_safe_distances (candidates.cpp:362-404): out[nV] */
+int ipcg_candidates_per_vertex_safe_distances(const ipcg_candidates* candidates, const ipcg_mesh* mesh,
+                                              const double* vertices, double inflation_radius,
+                                              double min_distance, double* out);
+/* Candidates::compute_collision_free_stepsize over the kept pairs (candidates.cpp:252-292) */
+int ipcg_candidates_collision_free_stepsize(const ipcg_candidates* candidates, const ipcg_mesh* mesh,
+                                            const double* vertices_t0, const double* vertices_t1,
+                                            double min_distance, double tolerance,
+                                            int64_t max_iterations, double conservative_rescaling,
+                                            double* step);
+/* Candidates::compute_noncandidate_conservative_stepsize (candidates.cpp:294-329) */
+int ipcg_candidates_noncandidate_conservative_stepsize(const ipcg_candidates* candidates,
+                                                       const ipcg_mesh* mesh,
+                                                       const double* displacements, double dhat,
+                                                       double* step);
+/* Candidates::compute_cfl_stepsize (candidates.cpp:331-360) */
+int ipcg_candidates_cfl_stepsize(const ipcg_candidates* candidates, const ipcg_mesh* mesh,
+                                 const double* vertices_t0, const double* vertices_t1, double dhat,
+                                 double min_distance, double tolerance, int64_t max_iterations,
+                                 double conservative_rescaling, double* step);
+
 /* ---------------------------------------------------------------------- */
 /* Serving: requests from many simulations over resident scenes            */
 /* ---------------------------------------------------------------------- */

@@ -629,6 +629,27 @@ __global__ void k_distance_stencils(int kind, int n, const double* __restrict__ 
 
 } // namespace
 
+// The two CCD passes over candidate lists (EE pairs, then FV (face, vertex)
+// pairs): pass 1 with a box budget, then the unfinished queries to
+// completion.  toi_bits (one per scene, set by the caller) is the scene's
+// earliest time so far; with any_hit a hit sets it to 0 instead.
+void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, int64_t n_fv, const double* V0,
+    const double* V1, const double* md, const CCDParams& P, int any_hit)
+{
+    cudaStream_t s = m->stream;
+    const SceneView sv = scene_view(m);
+    const int nc = (int)(n_ee + n_fv);
+    if (nc == 0) return;
+    m->ivals_a.reserve(nc + 1);
+    int* hard = m->ivals_a.p; // deferred by pass 1
+    int* hard_n = m->counters.p + 3;
+    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
+    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n, any_hit));
+    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, any_hit));
+}
+
 void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, const double* min_distance,
     double tolerance, int64_t max_iterations, double rescale, double* steps, int64_t* n_candidates)
 {
@@ -654,19 +675,7 @@ void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, c
     IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, ones.data(), sizeof(unsigned long long) * ns, cudaMemcpyHostToDevice,
         s));
     const CCDParams P { tolerance, (long long)max_iterations, rescale };
-    const SceneView sv = scene_view(m);
-    const double* md = m->scene_md.p + ns;
-    const int nc = (int)(n_ee + n_fv);
-    m->ivals_a.reserve(nc + 1);
-    int* hard = m->ivals_a.p; // deferred by pass 1
-    int* hard_n = m->counters.p + 3;
-    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
-    const int2* cee = m->cand.p;
-    const int2* cfv = m->cand.p + m->cand_cap;
-    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n, 0));
-    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, 0));
+    ccd_passes(m, m->cand.p, n_ee, m->cand.p + m->cand_cap, n_fv, V0, V1, m->scene_md.p + ns, P, 0);
     std::vector<unsigned long long> bits(ns);
     IPCG_CUDA(cudaMemcpyAsync(bits.data(), m->toi_bits.p, sizeof(unsigned long long) * ns, cudaMemcpyDeviceToHost,
         s));
@@ -689,22 +698,35 @@ bool step_collision_free(ipcg_mesh* m, const double* V0, const double* V1, doubl
     const unsigned long long one = 0x3ff0000000000000ULL; // 1.0
     IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, &one, sizeof(one), cudaMemcpyHostToDevice, s));
     const CCDParams P { tolerance, (long long)max_iterations, rescale };
-    const SceneView sv = scene_view(m);
-    const int nc = (int)(n_ee + n_fv);
-    m->ivals_a.reserve(nc + 1);
-    int* hard = m->ivals_a.p;
-    int* hard_n = m->counters.p + 3;
-    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
-    const int2* cee = m->cand.p;
-    const int2* cfv = m->cand.p + m->cand_cap;
-    IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, m->scene_md.p + 1, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n, 1));
-    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, m->scene_md.p + 1, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, 1));
+    ccd_passes(m, m->cand.p, n_ee, m->cand.p + m->cand_cap, n_fv, V0, V1, m->scene_md.p + 1, P, 1);
     unsigned long long bits = 1;
     IPCG_CUDA(cudaMemcpyAsync(&bits, m->toi_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
     IPCG_CUDA(cudaStreamSynchronize(s));
     return bits != 0;
+}
+
+double candidates_collision_free_stepsize(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv,
+    int64_t n_fv, const double* V0, const double* V1, double min_distance, double tolerance, int64_t max_iterations,
+    double rescale)
+{
+    if (m->n_scenes != 1) throw Error(IPCG_ERR_INVALID, "candidate sets are built on single-scene meshes");
+    if (n_ee + n_fv == 0) return 1.0;
+    cudaStream_t s = m->stream;
+    m->scene_md.reserve(2);
+    const double h[2] = { 0.5 * min_distance, min_distance };
+    IPCG_CUDA(cudaMemcpyAsync(m->scene_md.p, h, sizeof(h), cudaMemcpyHostToDevice, s));
+    m->toi_bits.reserve(1);
+    m->counters.reserve(16);
+    const unsigned long long one = 0x3ff0000000000000ULL; // 1.0
+    IPCG_CUDA(cudaMemcpyAsync(m->toi_bits.p, &one, sizeof(one), cudaMemcpyHostToDevice, s));
+    const CCDParams P { tolerance, (long long)max_iterations, rescale };
+    ccd_passes(m, cee, n_ee, cfv, n_fv, V0, V1, m->scene_md.p + 1, P, 0);
+    unsigned long long bits = 0;
+    IPCG_CUDA(cudaMemcpyAsync(&bits, m->toi_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    double t;
+    memcpy(&t, &bits, sizeof(t));
+    return t;
 }
 
 void ccd_stencils(cudaStream_t s, int is_ee, int64_t n, const double* x0, const double* x1, double min_distance,

@@ -84,6 +84,16 @@ def _load():
         "ipcg_collisions_minimum_distance": (i32, [P, P, P, P]),
         "ipcg_is_step_collision_free": (i32, [P, P, P, d, d, i64, d, P]),
         "ipcg_has_intersections": (i32, [P, P, P]),
+        "ipcg_candidates_create": (i32, [PP]),
+        "ipcg_candidates_destroy": (i32, [P]),
+        "ipcg_candidates_build": (i32, [P, P, P, d]),
+        "ipcg_candidates_build_swept": (i32, [P, P, P, P, d]),
+        "ipcg_candidates_counts": (i32, [P, P]),
+        "ipcg_candidates_get": (i32, [P, P, P]),
+        "ipcg_candidates_per_vertex_safe_distances": (i32, [P, P, P, d, d, P]),
+        "ipcg_candidates_collision_free_stepsize": (i32, [P, P, P, P, d, d, i64, d, P]),
+        "ipcg_candidates_noncandidate_conservative_stepsize": (i32, [P, P, P, d, P]),
+        "ipcg_candidates_cfl_stepsize": (i32, [P, P, P, P, d, d, d, i64, d, P]),
         "ipcg_server_create": (i32, [i32, i64, PP]),
         "ipcg_server_destroy": (i32, [P]),
         "ipcg_server_add_scene": (i32, [P, P, P, d, d, d, P]),
@@ -743,6 +753,84 @@ class Server:
         _check(_load().ipcg_server_stats(self._h, _ptr(st)))
         return {"completed": int(st[0]), "queued": int(st[1]), "running": int(st[2]), "releases": int(st[3]),
                 "resident_bytes": int(st[4])}
+
+
+class Candidates:
+    """Candidates (src/ipc/candidates/candidates.hpp): a broad-phase candidate
+    set kept on the device (edge-edge and face-vertex pairs, 3D meshes) and
+    the step-size rules that read it."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _check(_load().ipcg_candidates_create(C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.ipcg_candidates_destroy(h)
+            self._h = None
+
+    def build(self, mesh: CollisionMesh, vertices_t0, vertices_t1=None, inflation_radius: float = 0.0,
+              broad_phase=None):
+        """candidates.cpp:43-125 (static) or, with vertices_t1, 128-222 (swept)."""
+        V0 = _as_f64(vertices_t0)
+        if vertices_t1 is None:
+            _check(_load().ipcg_candidates_build(self._h, mesh._h, _ptr(V0), float(inflation_radius)))
+        else:
+            V1 = _as_f64(vertices_t1)
+            _check(_load().ipcg_candidates_build_swept(self._h, mesh._h, _ptr(V0), _ptr(V1),
+                                                       float(inflation_radius)))
+
+    def counts(self):
+        c = np.zeros(2, np.int64)
+        _check(_load().ipcg_candidates_counts(self._h, _ptr(c)))
+        return c
+
+    def __len__(self):
+        return int(self.counts().sum())
+
+    def to_arrays(self):
+        n = self.counts()
+        ee = np.zeros((int(n[0]), 2), np.int32)
+        fv = np.zeros((int(n[1]), 2), np.int32)
+        _check(_load().ipcg_candidates_get(self._h, _ptr(ee), _ptr(fv)))
+        return ee, fv
+
+    def compute_per_vertex_safe_distances(self, mesh: CollisionMesh, vertices, inflation_radius: float,
+                                          min_distance: float = 0.0):
+        V = _as_f64(vertices)
+        out = np.zeros(mesh.num_vertices)
+        _check(_load().ipcg_candidates_per_vertex_safe_distances(self._h, mesh._h, _ptr(V), float(inflation_radius),
+                                                                 float(min_distance), _ptr(out)))
+        return out
+
+    def compute_collision_free_stepsize(self, mesh: CollisionMesh, vertices_t0, vertices_t1,
+                                        min_distance: float = 0.0,
+                                        narrow_phase_ccd: TightInclusionCCD = DEFAULT_NARROW_PHASE_CCD) -> float:
+        V0, V1 = _as_f64(vertices_t0), _as_f64(vertices_t1)
+        out = np.zeros(1)
+        _check(_load().ipcg_candidates_collision_free_stepsize(
+            self._h, mesh._h, _ptr(V0), _ptr(V1), float(min_distance), narrow_phase_ccd.tolerance,
+            narrow_phase_ccd.max_iterations, narrow_phase_ccd.conservative_rescaling, _ptr(out)))
+        return float(out[0])
+
+    def compute_noncandidate_conservative_stepsize(self, mesh: CollisionMesh, displacements, dhat: float) -> float:
+        U = _as_f64(displacements)
+        out = np.zeros(1)
+        _check(_load().ipcg_candidates_noncandidate_conservative_stepsize(self._h, mesh._h, _ptr(U), float(dhat),
+                                                                          _ptr(out)))
+        return float(out[0])
+
+    def compute_cfl_stepsize(self, mesh: CollisionMesh, vertices_t0, vertices_t1, dhat: float,
+                             min_distance: float = 0.0, broad_phase=None,
+                             narrow_phase_ccd: TightInclusionCCD = DEFAULT_NARROW_PHASE_CCD) -> float:
+        V0, V1 = _as_f64(vertices_t0), _as_f64(vertices_t1)
+        out = np.zeros(1)
+        _check(_load().ipcg_candidates_cfl_stepsize(
+            self._h, mesh._h, _ptr(V0), _ptr(V1), float(dhat), float(min_distance), narrow_phase_ccd.tolerance,
+            narrow_phase_ccd.max_iterations, narrow_phase_ccd.conservative_rescaling, _ptr(out)))
+        return float(out[0])
 
 
 def _clamped_log_barrier_second_derivative(d, dhat):
