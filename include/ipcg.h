@@ -47,6 +47,19 @@ extern "C" {
 #define IPCG_BARRIER_PHYSICAL 1
 #define IPCG_BARRIER_FP32_PT 2
 
+/* Bits 4-7 of the same argument select the barrier function
+ * (src/ipc/barrier/barrier.hpp; BarrierPotential(barrier, dhat, stiffness,
+ * use_physical_barrier), barrier_potential.hpp:29-37): 0 (the default)
+ * ClampedLogBarrier, then NormalizedBarrier<ClampedLogBarrier>,
+ * ClampedLogSqBarrier, CubicBarrier and TwoStageBarrier.  The physical
+ * scaling divides by the chosen barrier's units(). */
+#define IPCG_BARRIER_CLAMPED_LOG 0
+#define IPCG_BARRIER_NORMALIZED_CLAMPED_LOG 1
+#define IPCG_BARRIER_CLAMPED_LOG_SQ 2
+#define IPCG_BARRIER_CUBIC 3
+#define IPCG_BARRIER_TWO_STAGE 4
+#define IPCG_BARRIER_FUNCTION(kind) ((kind) << 4)
+
 typedef struct ipcg_mesh ipcg_mesh;
 typedef struct ipcg_collisions ipcg_collisions;
 typedef struct ipcg_csr ipcg_csr;
@@ -201,6 +214,20 @@ int ipcg_barrier_batch(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
                        const double* vertices, const double* dhat, const double* stiffness,
                        int use_physical_barrier, int psd_method,
                        double* energies, double* gradient, ipcg_csr** hessian);
+
+/* Gauss-Newton forms of the barrier Hessian
+ * (NormalPotential::gauss_newton_hessian_diagonal / _quadratic_form,
+ * normal_potential.cpp:15-83 and 236-308): with t = sum_i c_i x_i the
+ * collision's distance vector, the Hessian is approximated by
+ * w (4 f''(|t|^2) (J t)(J t)^T + 2 f'(|t|^2) J J^T), mollifier ignored.
+ * diagonal: 3 nV doubles (host or device); p: 3 nV doubles (host or device),
+ * out: the scalar p^T H p. */
+int ipcg_barrier_gauss_newton_hessian_diagonal(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                                               const double* vertices, double dhat, double stiffness,
+                                               int use_physical_barrier, double* diagonal);
+int ipcg_barrier_gauss_newton_hessian_quadratic_form(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                                                     const double* vertices, double dhat, double stiffness,
+                                                     int use_physical_barrier, const double* p, double* out);
 
 /* Allocation-free barrier energy.  No counterpart in the reference: it exists
  * for callers that cannot let the library allocate device memory during a

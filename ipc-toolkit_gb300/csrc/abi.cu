@@ -519,6 +519,19 @@ int ipcg_collisions_set(ipcg_collisions* c, double dmin, int64_t nvv, const int3
     });
 }
 
+// The barrier calls' option bits: physical scaling, FP32 point-triangle
+// contacts and the barrier function.
+static void barrier_options(int bits, BarrierArgs& a)
+{
+    const int kind = (bits >> 4) & 15;
+    require(bits >= 0 && (bits & ~(IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT | IPCG_BARRIER_FUNCTION(15))) == 0
+            && kind <= IPCG_BARRIER_TWO_STAGE,
+        "unknown barrier option bits");
+    a.physical = (bits & IPCG_BARRIER_PHYSICAL) ? 1 : 0;
+    a.mixed = (bits & IPCG_BARRIER_FP32_PT) ? 1 : 0;
+    a.kind = kind;
+}
+
 // dhat / stiffness: one value (scene_params == 0) or one per scene (host arrays).
 static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, const double* dhat,
     const double* stiffness, int scene_params, int physical, int psd, double* energy, double* gradient,
@@ -532,10 +545,8 @@ static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const d
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dV = stage_positions(m, V, m->V0);
-        require(physical >= 0 && physical <= (IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT),
-            "unknown barrier option bits");
-        BarrierArgs a { dhat[0], stiffness[0], c->dmin, (physical & IPCG_BARRIER_PHYSICAL) ? 1 : 0, psd };
-        a.mixed = (physical & IPCG_BARRIER_FP32_PT) ? 1 : 0;
+        BarrierArgs a { dhat[0], stiffness[0], c->dmin, 0, psd };
+        barrier_options(physical, a);
         if (scene_params) {
             a.scene_dhat = dhat;
             a.scene_kappa = stiffness;
@@ -606,6 +617,64 @@ int ipcg_barrier_batch(const ipcg_collisions* c, const ipcg_mesh* mesh, const do
     const double* stiffness, int physical, int psd, double* energies, double* gradient, ipcg_csr** hessian)
 {
     return barrier_call(c, mesh, V, dhat, stiffness, 1, physical, psd, energies, gradient, hessian);
+}
+
+// Gauss-Newton forms (normal_potential.cpp:15-83): the FP64 path serves
+// every option; the FP32 bit does not apply to them.
+static int gauss_newton_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
+    double stiffness, int physical, double* diag, const double* p, double* qf)
+{
+    return guarded([&] {
+        require(c && mesh && (V || mesh->nV == 0), "NULL argument");
+        require(diag || (p && qf) || mesh->nV == 0, "NULL argument");
+        require(dhat > 0, "dhat must be positive");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        BarrierArgs a { dhat, stiffness, c->dmin, 0, IPCG_PSD_NONE };
+        barrier_options(physical, a);
+        const size_t bytes = sizeof(double) * 3 * m->nV;
+        if (diag) {
+            double* ddev = diag;
+            DBuf<double> dtmp;
+            if (!is_device_ptr(diag)) {
+                dtmp.reserve(3 * m->nV + 1);
+                ddev = dtmp.p;
+            }
+            barrier_gauss_newton(c, m, dV, a, ddev, nullptr, nullptr);
+            if (ddev != diag) IPCG_CUDA(cudaMemcpyAsync(diag, ddev, bytes, cudaMemcpyDeviceToHost, m->stream));
+            IPCG_CUDA(cudaStreamSynchronize(m->stream));
+        } else {
+            const double* pdev = p;
+            DBuf<double> ptmp;
+            if (!is_device_ptr(p)) {
+                ptmp.reserve(3 * m->nV + 1);
+                IPCG_CUDA(cudaMemcpyAsync(ptmp.p, p, bytes, cudaMemcpyHostToDevice, m->stream));
+                pdev = ptmp.p;
+            }
+            barrier_gauss_newton(c, m, dV, a, nullptr, pdev, qf);
+        }
+    });
+}
+
+int ipcg_barrier_gauss_newton_hessian_diagonal(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V,
+    double dhat, double stiffness, int physical, double* diagonal)
+{
+    if (!diagonal) {
+        g_last_error = "diagonal is NULL";
+        return IPCG_ERR_INVALID;
+    }
+    return gauss_newton_call(c, mesh, V, dhat, stiffness, physical, diagonal, nullptr, nullptr);
+}
+
+int ipcg_barrier_gauss_newton_hessian_quadratic_form(const ipcg_collisions* c, const ipcg_mesh* mesh,
+    const double* V, double dhat, double stiffness, int physical, const double* p, double* out)
+{
+    if (!p || !out) {
+        g_last_error = "p or out is NULL";
+        return IPCG_ERR_INVALID;
+    }
+    return gauss_newton_call(c, mesh, V, dhat, stiffness, physical, nullptr, p, out);
 }
 
 int ipcg_csr_shape(const ipcg_csr* h, int64_t* rows, int64_t* nnz)

@@ -102,31 +102,90 @@ __device__ __forceinline__ void load_contact(const ContactsView& cv, const int* 
     c.w = cv.fv_w[i];
 }
 
-// ---- barrier (barrier.cpp:11-43) ----
-__device__ __forceinline__ double barrier0(double d, double dh)
+// ---- barrier functions (barrier.cpp:11-154, barrier.hpp:82-340) ----
+// kind: 0 ClampedLogBarrier, 1 NormalizedBarrier<ClampedLogBarrier>,
+// 2 ClampedLogSqBarrier, 3 CubicBarrier, 4 TwoStageBarrier; D = derivative
+// order.  One template serves the FP64 path and the FP32 (mixed) path.
+__device__ __forceinline__ double blog(double x) { return log(x); }
+__device__ __forceinline__ float blog(float x) { return logf(x); }
+__device__ __forceinline__ double binf(double) { return __longlong_as_double(0x7ff0000000000000ULL); }
+__device__ __forceinline__ float binf(float) { return __int_as_float(0x7f800000); }
+
+template <int D, class T> __device__ __forceinline__ T clamped_log(T d, T dh)
 {
-    if (d <= 0.0) return __longlong_as_double(0x7ff0000000000000ULL);
-    if (d >= dh) return 0;
-    const double dm = d - dh;
-    return -dm * dm * log(d / dh);
+    if (D == 0) {
+        if (d <= T(0)) return binf(d);
+        if (d >= dh) return T(0);
+        const T dm = d - dh;
+        return -dm * dm * blog(d / dh);
+    }
+    if (d <= T(0) || d >= dh) return T(0);
+    if (D == 1) return (dh - d) * (T(2) * blog(d / dh) - dh / d + T(1));
+    const T r = dh / d;
+    return (r + T(2)) * r - T(2) * blog(d / dh) - T(3);
 }
-__device__ __forceinline__ double barrier1(double d, double dh)
+template <int D, class T> __device__ __forceinline__ T clamped_log_sq(T d, T dh)
 {
-    if (d <= 0.0 || d >= dh) return 0.0;
-    return (dh - d) * (2 * log(d / dh) - dh / d + 1);
+    if (D == 0) {
+        if (d <= T(0)) return binf(d);
+        if (d >= dh) return T(0);
+        const T dm = d - dh, l = blog(d / dh);
+        return dm * dm * l * l;
+    }
+    if (d <= T(0) || d >= dh) return T(0);
+    if (D == 1) {
+        const T dm = d - dh, l = blog(d / dh);
+        return T(2) * dm * l * (l + dm / d);
+    }
+    const T t0 = dh - d, t1 = blog(d / dh), t2 = (t0 * t0) / (d * d);
+    return T(2) * ((t1 * t1) - (t1 - T(1)) * t2 - T(4) * t1 * t0 / d);
 }
-__device__ __forceinline__ double barrier2(double d, double dh)
+template <int D, class T> __device__ __forceinline__ T cubic(T d, T dh)
 {
-    if (d <= 0.0 || d >= dh) return 0.0;
-    const double r = dh / d;
-    return (r + 2) * r - 2 * log(d / dh) - 3;
+    if (!(d < dh)) return T(0);
+    const T dm = d - dh;
+    if (D == 0) return T(-2) / T(3) / dh * dm * dm * dm;
+    if (D == 1) return T(-2) / dh * dm * dm;
+    return T(4) * (T(1) - d / dh);
+}
+template <int D, class T> __device__ __forceinline__ T two_stage(T d, T dh)
+{
+    if (d >= dh) return T(0);
+    if (d >= T(0.5) * dh) return D == 0 ? T(0.5) * (dh - d) * (dh - d) : (D == 1 ? d - dh : T(1));
+    if (D == 0) return T(-0.25) * dh * dh * (blog(T(2) * d / dh) - T(0.5));
+    if (D == 1) return T(-0.25) * dh * dh / d;
+    return (T(0.25) * dh * dh) / (d * d);
+}
+// The other barriers are called out of line so that the default one adds
+// no registers to the local-Hessian kernels.
+template <int D, class T> __device__ __noinline__ T barrier_other(int kind, T d, T dh)
+{
+    switch (kind) {
+    case 1: {
+        // NormalizedBarrier: b(d / dh, 1) / dh^D
+        const T v = clamped_log<D, T>(d / dh, T(1));
+        return D == 0 ? v : (D == 1 ? v / dh : v / (dh * dh));
+    }
+    case 2: return clamped_log_sq<D, T>(d, dh);
+    case 3: return cubic<D, T>(d, dh);
+    case 4: return two_stage<D, T>(d, dh);
+    default: return clamped_log<D, T>(d, dh);
+    }
+}
+template <int D, class T> __device__ __forceinline__ T barrier_fn(int kind, T d, T dh)
+{
+    return kind == 0 ? clamped_log<D, T>(d, dh) : barrier_other<D, T>(kind, d, dh);
 }
 
 struct Params {
     double kappa, dmin2, xhat, scale; // scale = physical factor (or 1)
     int psd;
     int mixed; // point-triangle contacts in FP32 (IPCG_BARRIER_FP32_PT)
+    int kind;  // barrier function (barrier_fn)
 };
+// Barrier::units(x̂) (barrier.hpp): x̂² for every barrier but the normalized
+// one, which is dimensionless (1).  The physical barrier scales by dhat / units.
+__host__ __device__ inline double barrier_units(int kind, double xhat) { return kind == 1 ? 1.0 : xhat * xhat; }
 
 // ---- FP32 point-triangle contacts (mixed precision) ----
 // The point-plane squared distance d = N^2/D (N = a.(u x v), D = |u x v|^2,
@@ -219,26 +278,6 @@ __device__ float triple_quot_f(F3 a, F3 u, F3 v, float* g, float* H)
                     - k4 * HD[i * 9 + j] + k5 * gD[i] * gD[j];
     }
     return Nn * Nn * iD;
-}
-
-// FP32 barrier and its derivatives (barrier.cpp:11-43).
-__device__ __forceinline__ float barrier0f(float d, float dh)
-{
-    if (d <= 0.0f) return __int_as_float(0x7f800000);
-    if (d >= dh) return 0;
-    const float dm = d - dh;
-    return -dm * dm * logf(d / dh);
-}
-__device__ __forceinline__ float barrier1f(float d, float dh)
-{
-    if (d <= 0.0f || d >= dh) return 0.0f;
-    return (dh - d) * (2 * logf(d / dh) - dh / d + 1);
-}
-__device__ __forceinline__ float barrier2f(float d, float dh)
-{
-    if (d <= 0.0f || d >= dh) return 0.0f;
-    const float r = dh / d;
-    return (r + 2) * r - 2 * logf(d / dh) - 3;
 }
 
 // FV contact in FP32: squared distance, stencil gradient (12) and Hessian
@@ -783,27 +822,27 @@ __device__ bool project_psd(int n, double* H, int method)
 
 __device__ __forceinline__ double fval(const Params& P, double d2)
 {
-    return P.kappa * (barrier0(d2 - P.dmin2, P.xhat) * P.scale);
+    return P.kappa * (barrier_fn<0, double>(P.kind, d2 - P.dmin2, P.xhat) * P.scale);
 }
 __device__ __forceinline__ double fd1(const Params& P, double d2)
 {
-    return P.kappa * (barrier1(d2 - P.dmin2, P.xhat) * P.scale);
+    return P.kappa * (barrier_fn<1, double>(P.kind, d2 - P.dmin2, P.xhat) * P.scale);
 }
 __device__ __forceinline__ double fd2(const Params& P, double d2)
 {
-    return P.kappa * (barrier2(d2 - P.dmin2, P.xhat) * P.scale);
+    return P.kappa * (barrier_fn<2, double>(P.kind, d2 - P.dmin2, P.xhat) * P.scale);
 }
 __device__ __forceinline__ float fvalf(const Params& P, float d2)
 {
-    return (float)P.kappa * (barrier0f(d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
+    return (float)P.kappa * (barrier_fn<0, float>(P.kind, d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
 }
 __device__ __forceinline__ float fd1f(const Params& P, float d2)
 {
-    return (float)P.kappa * (barrier1f(d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
+    return (float)P.kappa * (barrier_fn<1, float>(P.kind, d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
 }
 __device__ __forceinline__ float fd2f(const Params& P, float d2)
 {
-    return (float)P.kappa * (barrier2f(d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
+    return (float)P.kappa * (barrier_fn<2, float>(P.kind, d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
 }
 // Whether contact c is evaluated in FP32 (mixed precision, FV, triangle not
 // degenerate).
@@ -950,6 +989,135 @@ __global__ void __launch_bounds__(BLOCK) k_gradient(ContactsView cv, const int* 
             const double v = out[3 * a + k];
             if (v != 0) atomicAdd(grad + 3 * (int64_t)c.vid[a] + k, v);
         }
+}
+
+// ---- Gauss-Newton forms (normal_potential.cpp:15-83, 236-308) ----
+// Distance-vector coefficients c with t = sum_i c_i x_i, for the collision's
+// known distance type (compute_coefficients in candidates/vertex_vertex.cpp:40-46,
+// edge_vertex.cpp:45-75, edge_edge.cpp:42-96, face_vertex.cpp:42-89): VV and
+// EV (P_E) fixed, EE by its stored type, FV point-plane (P_T).
+__device__ __forceinline__ double pe_alpha(V3 p, V3 e0, V3 e1)
+{
+    const V3 e = e1 - e0;
+    return dot(p - e0, e) / sqnorm(e);
+}
+__device__ void contact_coefficients(const Local& c, const V3* x, double* co)
+{
+    co[0] = co[1] = co[2] = co[3] = 0.0;
+    if (c.type == CT_VV) {
+        co[0] = 1.0;
+        co[1] = -1.0;
+    } else if (c.type == CT_EV) {
+        const double a = pe_alpha(x[0], x[1], x[2]);
+        co[0] = 1.0;
+        co[1] = -1.0 + a;
+        co[2] = -a;
+    } else if (c.type == CT_FV) {
+        // point_triangle_closest_point (tangent/closest_point.cpp:123-137)
+        double u, v;
+        ldlt2_solve(x[2] - x[1], x[3] - x[1], x[0] - x[1], u, v);
+        co[0] = 1.0;
+        co[1] = -1.0 + u + v;
+        co[2] = -u;
+        co[3] = -v;
+    } else {
+        switch (c.dtype) {
+        case EA0_EB0: co[0] = 1.0, co[2] = -1.0; break;
+        case EA0_EB1: co[0] = 1.0, co[3] = -1.0; break;
+        case EA1_EB0: co[1] = 1.0, co[2] = -1.0; break;
+        case EA1_EB1: co[1] = 1.0, co[3] = -1.0; break;
+        case EA_EB0: {
+            const double a = pe_alpha(x[2], x[0], x[1]);
+            co[0] = 1.0 - a, co[1] = a, co[2] = -1.0;
+        } break;
+        case EA_EB1: {
+            const double a = pe_alpha(x[3], x[0], x[1]);
+            co[0] = 1.0 - a, co[1] = a, co[3] = -1.0;
+        } break;
+        case EA0_EB: {
+            const double a = pe_alpha(x[0], x[2], x[3]);
+            co[0] = 1.0, co[2] = -1.0 + a, co[3] = -a;
+        } break;
+        case EA1_EB: {
+            const double a = pe_alpha(x[1], x[2], x[3]);
+            co[1] = 1.0, co[2] = -1.0 + a, co[3] = -a;
+        } break;
+        default: {
+            // edge_edge_closest_point (tangent/closest_point.cpp:65-87): the
+            // Gram system of (ea, -eb) against eb0 - ea0
+            const V3 ea = x[1] - x[0], eb = x[3] - x[2];
+            double a, b;
+            ldlt2_solve(ea, eb * -1.0, x[2] - x[0], a, b);
+            co[0] = 1.0 - a, co[1] = a, co[2] = -1.0 + b, co[3] = -b;
+        }
+        }
+    }
+}
+// t = sum_i c_i x_i in vertex order (collision_stencil.cpp:14-25)
+__device__ __forceinline__ V3 distance_vector(int n, const V3* x, const double* co)
+{
+    V3 t { 0, 0, 0 };
+    for (int i = 0; i < n; ++i) t = t + x[i] * co[i];
+    return t;
+}
+
+// Gauss-Newton Hessian diagonal: w (4 f'' c_i^2 t_d^2 + 2 f' c_i^2) at
+// d^2 = |t|^2, scattered like the gradient.  The mollifier plays no part.
+__global__ void __launch_bounds__(BLOCK) k_gn_diagonal(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, const Params* __restrict__ sp, SceneView sv,
+    double* __restrict__ diag)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    const Params P = sp[sv.of(c.vid[0])];
+    V3 x[4];
+    gather(V, c, x);
+    double co[4];
+    contact_coefficients(c, x, co);
+    const V3 t = distance_vector(c.n, x, co);
+    const double d2 = sqnorm(t);
+    const double s1 = c.w * 4.0 * fd2(P, d2), s2 = c.w * 2.0 * fd1(P, d2);
+    const double t2[3] = { t.x * t.x, t.y * t.y, t.z * t.z };
+    for (int a = 0; a < c.n; ++a) {
+        const double ci2 = co[a] * co[a];
+        for (int k = 0; k < 3; ++k) {
+            const double v = s1 * (ci2 * t2[k]) + s2 * ci2;
+            if (v != 0) atomicAdd(diag + 3 * (int64_t)c.vid[a] + k, v);
+        }
+    }
+}
+
+// Gauss-Newton quadratic form p^T H p: w (4 f'' (J^T p . t)^2 + 2 f' |J^T p|^2)
+// with J^T p = sum_i c_i p_i; per-block partial sums (deterministic).
+__global__ void __launch_bounds__(BLOCK) k_gn_quadratic_form(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, const double* __restrict__ pv,
+    const Params* __restrict__ sp, SceneView sv, double* __restrict__ partial)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double q = 0;
+    if (i < n) {
+        Local c;
+        load_contact(cv, E, F, i, c);
+        const Params P = sp[sv.of(c.vid[0])];
+        V3 x[4], pl[4];
+        gather(V, c, x);
+        gather(pv, c, pl);
+        double co[4];
+        contact_coefficients(c, x, co);
+        const V3 t = distance_vector(c.n, x, co);
+        const double d2 = sqnorm(t);
+        const V3 pj = distance_vector(c.n, pl, co);
+        const double pjt = dot(pj, t);
+        q = c.w * (4.0 * fd2(P, d2) * (pjt * pjt) + 2.0 * fd1(P, d2) * sqnorm(pj));
+    }
+    typedef cub::BlockReduce<double, BLOCK> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const double s = BR(tmp).Sum(q);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
 // Self-check of the Hessian path: an index outside its buffer is recorded
@@ -1331,14 +1499,10 @@ __global__ void __launch_bounds__(BLOCK) k_min_distance(ContactsView cv, const i
 
 } // namespace
 
-void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
-    double* energy_host, double* grad_dev, ipcg_csr* hess)
+// Per-scene barrier parameters (barrier_potential.cpp:62-99) on the device,
+// uploaded only when they change (a Newton loop repeats them); P0 = scene 0's.
+static const Params* upload_params(const ipcg_collisions* cs, ipcg_mesh* m, const BarrierArgs& a, Params& P0)
 {
-    cudaStream_t s = m->stream;
-    ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
-        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
-    const int64_t n = cs->size();
-    // per-scene barrier parameters (barrier_potential.cpp:62-99)
     const int ns = (int)m->n_scenes;
     std::vector<Params> hp(ns);
     for (int k = 0; k < ns; ++k) {
@@ -1346,18 +1510,29 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         const double kap = a.scene_kappa ? a.scene_kappa[k] : a.kappa;
         const double dm = (k < (int)cs->scene_dmin.size()) ? cs->scene_dmin[k] : cs->dmin;
         const double xh = (2 * dm + dh) * dh;
-        hp[k] = Params { kap, dm * dm, xh, a.physical ? dh / (xh * xh) : 1.0, a.psd, a.mixed };
+        hp[k] = Params { kap, dm * dm, xh, a.physical ? dh / barrier_units(a.kind, xh) : 1.0, a.psd, a.mixed, a.kind };
     }
-    // uploaded only when they change (a Newton loop repeats them)
     const size_t pbytes = sizeof(Params) * ns;
     const unsigned char* hb = reinterpret_cast<const unsigned char*>(hp.data());
     if (m->params_host.size() != pbytes || memcmp(m->params_host.data(), hb, pbytes) != 0) {
         m->params_buf.reserve(pbytes);
-        IPCG_CUDA(cudaMemcpyAsync(m->params_buf.p, hb, pbytes, cudaMemcpyHostToDevice, s));
+        IPCG_CUDA(cudaMemcpyAsync(m->params_buf.p, hb, pbytes, cudaMemcpyHostToDevice, m->stream));
         m->params_host.assign(hb, hb + pbytes);
     }
-    const Params* sp = reinterpret_cast<const Params*>(m->params_buf.p);
-    const Params P = hp[0];
+    P0 = hp[0];
+    return reinterpret_cast<const Params*>(m->params_buf.p);
+}
+
+void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    double* energy_host, double* grad_dev, ipcg_csr* hess)
+{
+    cudaStream_t s = m->stream;
+    ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
+        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
+    const int64_t n = cs->size();
+    const int ns = (int)m->n_scenes;
+    Params P;
+    const Params* sp = upload_params(cs, m, a, P);
     const SceneView sv = scene_view(m);
     const int nblk = grid_for(n, BLOCK);
     const int64_t nV = m->nV;
@@ -1526,6 +1701,37 @@ double collisions_min_distance(const ipcg_collisions* cs, ipcg_mesh* m, const do
     return d;
 }
 
+void barrier_gauss_newton(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    double* diag_dev, const double* p_dev, double* qf_host)
+{
+    cudaStream_t s = m->stream;
+    ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
+        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
+    const int64_t n = cs->size();
+    Params P;
+    const Params* sp = upload_params(cs, m, a, P);
+    const SceneView sv = scene_view(m);
+    const int nblk = grid_for(n, BLOCK);
+    if (diag_dev) {
+        IPCG_CUDA(cudaMemsetAsync(diag_dev, 0, sizeof(double) * 3 * m->nV, s));
+        if (n > 0)
+            IPCG_LAUNCH("k_gn_diagonal", s, k_gn_diagonal<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, sp, sv,
+                diag_dev));
+    }
+    if (qf_host) {
+        if (n == 0) {
+            *qf_host = 0;
+            return;
+        }
+        m->partial.reserve(nblk + 2);
+        IPCG_LAUNCH("k_gn_quadratic_form", s, k_gn_quadratic_form<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V,
+            p_dev, sp, sv, m->partial.p));
+        IPCG_LAUNCH("k_sum_partials", s, k_sum_partials<<<1, 1024, 0, s>>>(m->partial.p, nblk, m->partial.p + nblk));
+        IPCG_CUDA(cudaMemcpyAsync(qf_host, m->partial.p + nblk, sizeof(double), cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaStreamSynchronize(s));
+    }
+}
+
 } // namespace ipcg
 
 // ---------------------------------------------------------------------------
@@ -1594,7 +1800,7 @@ void barrier_energy_noalloc(const double* V, const int* E, const int* F, const C
     ContactsView cv { in.nvv, in.nev, in.nee, in.nfv, (const int2*)in.vv, (const int2*)in.ev, (const int2*)in.ee,
         (const int2*)in.fv, in.vv_w, in.ev_w, in.ee_w, in.fv_w, in.ee_eps, in.ee_dtype };
     const double xhat = (2 * dmin + dhat) * dhat;
-    Params P { kappa, dmin * dmin, xhat, physical ? dhat / (xhat * xhat) : 1.0, IPCG_PSD_NONE };
+    Params P { kappa, dmin * dmin, xhat, physical ? dhat / barrier_units(0, xhat) : 1.0, IPCG_PSD_NONE, 0, 0 };
     // every block overwrites its partial and the final kernel overwrites the
     // result, so nothing in the shared array needs clearing between calls
     IPCG_LAUNCH("k_energy", s, k_energy<<<nblk, BLOCK, 0, s>>>(cv, E, F, V, P, partial));

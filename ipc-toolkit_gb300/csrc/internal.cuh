@@ -255,9 +255,14 @@ struct BarrierArgs {
     const double* scene_dhat = nullptr;  // per scene (batches), host
     const double* scene_kappa = nullptr; // per scene (batches), host
     int mixed = 0;                       // FP32 point-triangle contacts
+    int kind = 0;                        // barrier function (IPCG_BARRIER_* kinds)
 };
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null);
+// Gauss-Newton Hessian diagonal (device, 3 nV) and/or quadratic form p^T H p
+// (p on the device, result on the host).
+void barrier_gauss_newton(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    double* diag_dev_or_null, const double* p_dev, double* qf_host_or_null);
 // has_intersections (ipc.cpp:110-167): some edge crosses a triangle it does
 // not share a vertex with (a batch answers for all its scenes together).
 bool has_intersections(ipcg_mesh* m, const double* V);

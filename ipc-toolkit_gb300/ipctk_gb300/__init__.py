@@ -26,6 +26,8 @@ import ctypes as C
 import enum
 import os
 
+import math
+
 import numpy as np
 
 from . import scenes  # noqa: F401  (seeded benchmark scenes)
@@ -84,6 +86,8 @@ def _load():
         "ipcg_collisions_minimum_distance": (i32, [P, P, P, P]),
         "ipcg_is_step_collision_free": (i32, [P, P, P, d, d, i64, d, P]),
         "ipcg_has_intersections": (i32, [P, P, P]),
+        "ipcg_barrier_gauss_newton_hessian_diagonal": (i32, [P, P, P, d, d, i32, P]),
+        "ipcg_barrier_gauss_newton_hessian_quadratic_form": (i32, [P, P, P, d, d, i32, P, P]),
         "ipcg_candidates_create": (i32, [PP]),
         "ipcg_candidates_destroy": (i32, [P]),
         "ipcg_candidates_build": (i32, [P, P, P, d]),
@@ -480,25 +484,158 @@ def _csr_to_scipy(h, ndof):
     return sp.csc_matrix((va, ci, rp), shape=(ndof, ndof))
 
 
-class BarrierPotential:
-    """BarrierPotential(dhat, stiffness, use_physical_barrier=False)
-    (src/ipc/potentials/barrier_potential.hpp:24-27) with the default
-    ClampedLogBarrier."""
+class Barrier:
+    """A barrier function b(d, dhat) (src/ipc/barrier/barrier.hpp).  The
+    potential evaluates it on the device; these host methods are the scalar
+    functions themselves, for callers that tune stiffness or plot them."""
 
-    def __init__(self, dhat: float, stiffness: float, use_physical_barrier: bool = False,
-                 mixed_precision: bool = False):
+    kind = 0
+
+    def __call__(self, d: float, dhat: float) -> float:
+        return self._eval(0, float(d), float(dhat))
+
+    def first_derivative(self, d: float, dhat: float) -> float:
+        return self._eval(1, float(d), float(dhat))
+
+    def second_derivative(self, d: float, dhat: float) -> float:
+        return self._eval(2, float(d), float(dhat))
+
+    def units(self, dhat: float) -> float:
+        return float(dhat) * float(dhat)
+
+    def __repr__(self):
+        return type(self).__name__ + "()"
+
+
+def _clamped_log(k, d, dh):
+    if k == 0:
+        if d <= 0:
+            return math.inf
+        return 0.0 if d >= dh else -(d - dh) * (d - dh) * math.log(d / dh)
+    if d <= 0 or d >= dh:
+        return 0.0
+    if k == 1:
+        return (dh - d) * (2 * math.log(d / dh) - dh / d + 1)
+    r = dh / d
+    return (r + 2) * r - 2 * math.log(d / dh) - 3
+
+
+class ClampedLogBarrier(Barrier):
+    """-(d - dhat)^2 ln(d / dhat) (barrier.cpp:11-43), the default."""
+    kind = 0
+
+    def _eval(self, k, d, dh):
+        return _clamped_log(k, d, dh)
+
+
+class NormalizedClampedLogBarrier(Barrier):
+    """ClampedLogBarrier of d / dhat against 1 (barrier.hpp:145-175)."""
+    kind = 1
+
+    def _eval(self, k, d, dh):
+        return _clamped_log(k, d / dh, 1.0) / dh ** k
+
+    def units(self, dhat):
+        return 1.0
+
+
+class ClampedLogSqBarrier(Barrier):
+    """(d - dhat)^2 ln^2(d / dhat) (barrier.cpp:47-86)."""
+    kind = 2
+
+    def _eval(self, k, d, dh):
+        if k == 0 and d <= 0:
+            return math.inf
+        if d <= 0 or d >= dh:
+            return 0.0
+        lg = math.log(d / dh)
+        if k == 0:
+            return (d - dh) * (d - dh) * lg * lg
+        if k == 1:
+            return 2 * (d - dh) * lg * (lg + (d - dh) / d)
+        t0 = dh - d
+        t2 = (t0 * t0) / (d * d)
+        return 2 * ((lg * lg) - (lg - 1) * t2 - 4 * lg * t0 / d)
+
+
+class CubicBarrier(Barrier):
+    """-2/(3 dhat) (d - dhat)^3 (barrier.cpp:90-117)."""
+    kind = 3
+
+    def _eval(self, k, d, dh):
+        if not d < dh:
+            return 0.0
+        dm = d - dh
+        return (-2.0 / 3.0 / dh * dm * dm * dm, -2 / dh * dm * dm, 4 * (1 - d / dh))[k]
+
+
+class TwoStageBarrier(Barrier):
+    """Two-stage activation (barrier.cpp:121-152)."""
+    kind = 4
+
+    def _eval(self, k, d, dh):
+        if d >= dh:
+            return 0.0
+        if d >= 0.5 * dh:
+            return (0.5 * (dh - d) * (dh - d), d - dh, 1.0)[k]
+        if k == 0:
+            return -0.25 * dh * dh * (math.log(2 * d / dh) - 0.5)
+        return -0.25 * dh * dh / d if k == 1 else (0.25 * dh * dh) / (d * d)
+
+
+class BarrierPotential:
+    """BarrierPotential(dhat, stiffness, use_physical_barrier=False) or
+    BarrierPotential(barrier, dhat, stiffness, use_physical_barrier=False)
+    (src/ipc/potentials/barrier_potential.hpp:24-37); ClampedLogBarrier by
+    default."""
+
+    def __init__(self, *args, use_physical_barrier: bool = False, mixed_precision: bool = False, **kw):
         """``mixed_precision`` (no counterpart in the reference): face-vertex
         contacts in FP32, everything else FP64 (IPCG_BARRIER_FP32_PT)."""
+        args = list(args)
+        barrier = kw.pop("barrier", None)
+        if args and isinstance(args[0], Barrier):
+            barrier = args.pop(0)
+        names = ["dhat", "stiffness", "use_physical_barrier"]
+        vals = dict(zip(names, args))
+        vals.update(kw)
+        if "use_physical_barrier" not in vals:
+            vals["use_physical_barrier"] = use_physical_barrier
+        dhat, stiffness = vals["dhat"], vals["stiffness"]
         if not dhat > 0:
             raise ValueError("dhat must be positive")
+        self.barrier = barrier if barrier is not None else ClampedLogBarrier()
         self.dhat = float(dhat)
         self.stiffness = float(stiffness)
-        self.use_physical_barrier = bool(use_physical_barrier)
+        self.use_physical_barrier = bool(vals["use_physical_barrier"])
         self.mixed_precision = bool(mixed_precision)
 
     @property
     def _options(self):
-        return int(self.use_physical_barrier) | (2 if self.mixed_precision else 0)
+        return (int(self.use_physical_barrier) | (2 if self.mixed_precision else 0)
+                | (int(self.barrier.kind) << 4))
+
+    def gauss_newton_hessian_diagonal(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices):
+        """NormalPotential::gauss_newton_hessian_diagonal (normal_potential.cpp:15-48)."""
+        V = _as_f64(vertices)
+        if _is_torch_cuda(V):
+            import torch
+            g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
+        else:
+            g = np.zeros(V.size)
+        _check(_load().ipcg_barrier_gauss_newton_hessian_diagonal(collisions._h, mesh._h, _ptr(V), self.dhat,
+                                                                  self.stiffness, self._options, _ptr(g)))
+        return g
+
+    def gauss_newton_hessian_quadratic_form(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices,
+                                            p) -> float:
+        """NormalPotential::gauss_newton_hessian_quadratic_form (normal_potential.cpp:50-83)."""
+        V = _as_f64(vertices)
+        P = _as_f64(p if _is_torch_cuda(p) else np.reshape(p, (-1, 3)))
+        out = np.zeros(1)
+        _check(_load().ipcg_barrier_gauss_newton_hessian_quadratic_form(
+            collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, self._options, _ptr(P), _ptr(out)))
+        return float(out[0])
 
     def __call__(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices) -> float:
         V = _as_f64(vertices)

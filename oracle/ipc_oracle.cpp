@@ -726,7 +726,9 @@ static void finalize(Raw& all, Collisions& C)
 }
 
 // ---------------------------------------------------------------------------
-// Barrier (barrier.cpp:11-43, barrier_potential.cpp:62-99)
+// Barrier functions (barrier.cpp:11-154, barrier.hpp:82-340) and the
+// potential's scaling (barrier_potential.cpp:62-99).  kind: 0 ClampedLog,
+// 1 NormalizedBarrier<ClampedLog>, 2 ClampedLogSq, 3 Cubic, 4 TwoStage.
 // ---------------------------------------------------------------------------
 static double barrier(double d, double dhat)
 {
@@ -746,29 +748,75 @@ static double barrier_d2(double d, double dhat)
     const double dd = dhat / d;
     return (dd + 2) * dd - 2 * std::log(d / dhat) - 3;
 }
+// ClampedLogSqBarrier (barrier.cpp:47-86)
+static double logsq(int deriv, double d, double dhat)
+{
+    if (deriv == 0 && d <= 0.0) return std::numeric_limits<double>::infinity();
+    if (d <= 0.0 || d >= dhat) return 0.0;
+    const double l = std::log(d / dhat);
+    if (deriv == 0) return (d - dhat) * (d - dhat) * l * l;
+    if (deriv == 1) return 2 * (d - dhat) * l * (l + (d - dhat) / d);
+    const double t0 = dhat - d, t2 = (t0 * t0) / (d * d);
+    return 2 * ((l * l) - (l - 1) * t2 - 4 * l * t0 / d);
+}
+// CubicBarrier (barrier.cpp:90-117)
+static double cubic(int deriv, double d, double dhat)
+{
+    if (!(d < dhat)) return 0.0;
+    const double dm = d - dhat;
+    if (deriv == 0) return -2.0 / 3.0 / dhat * dm * dm * dm;
+    if (deriv == 1) return -2 / dhat * dm * dm;
+    return 4 * (1 - d / dhat);
+}
+// TwoStageBarrier (barrier.cpp:121-152)
+static double two_stage(int deriv, double d, double dhat)
+{
+    if (d >= dhat) return 0.0;
+    if (d >= 0.5 * dhat) return deriv == 0 ? 0.5 * (dhat - d) * (dhat - d) : (deriv == 1 ? d - dhat : 1.0);
+    if (deriv == 0) return -0.25 * dhat * dhat * (std::log(2 * d / dhat) - 0.5);
+    if (deriv == 1) return -0.25 * dhat * dhat / d;
+    return (0.25 * dhat * dhat) / (d * d);
+}
+static double clamped_log(int deriv, double d, double dhat)
+{
+    return deriv == 0 ? barrier(d, dhat) : (deriv == 1 ? barrier_d1(d, dhat) : barrier_d2(d, dhat));
+}
+static double barrier_any(int kind, int deriv, double d, double dhat)
+{
+    switch (kind) {
+    case 1: {
+        // NormalizedBarrier (barrier.hpp:145-175): b(d / dhat, 1) / dhat^deriv
+        const double v = clamped_log(deriv, d / dhat, 1.0);
+        return deriv == 0 ? v : (deriv == 1 ? v / dhat : v / (dhat * dhat));
+    }
+    case 2: return logsq(deriv, d, dhat);
+    case 3: return cubic(deriv, d, dhat);
+    case 4: return two_stage(deriv, d, dhat);
+    default: return clamped_log(deriv, d, dhat);
+    }
+}
+// bits: 1 = physical barrier, bits 4-7 = barrier kind (the C ABI's encoding)
 struct BarrierParams {
     double dhat, kappa, dmin;
     int physical;
 };
-// ClampedLogBarrier::units(x̂) = x̂² (barrier.hpp:133-137): the physical
-// scaling is dhat / x̂² with x̂ = (2 dmin + dhat) dhat.
+static inline int barrier_kind(const BarrierParams& P) { return (P.physical >> 4) & 15; }
+// Barrier::units(x̂): x̂² (dimensionless 1 for the normalized barrier); the
+// physical scaling is dhat / units(x̂) with x̂ = (2 dmin + dhat) dhat.
 static inline double phys_scale(const BarrierParams& P)
 {
     const double xh = (2 * P.dmin + P.dhat) * P.dhat;
-    return P.physical ? P.dhat / (xh * xh) : 1.0;
+    if (!(P.physical & 1)) return 1.0;
+    return P.dhat / (barrier_kind(P) == 1 ? 1.0 : xh * xh);
 }
-static double f0(const BarrierParams& P, double d2)
+static double fk(const BarrierParams& P, int deriv, double d2)
 {
-    return P.kappa * (barrier(d2 - P.dmin * P.dmin, (2 * P.dmin + P.dhat) * P.dhat) * phys_scale(P));
+    return P.kappa
+        * (barrier_any(barrier_kind(P), deriv, d2 - P.dmin * P.dmin, (2 * P.dmin + P.dhat) * P.dhat) * phys_scale(P));
 }
-static double f1(const BarrierParams& P, double d2)
-{
-    return P.kappa * (barrier_d1(d2 - P.dmin * P.dmin, (2 * P.dmin + P.dhat) * P.dhat) * phys_scale(P));
-}
-static double f2(const BarrierParams& P, double d2)
-{
-    return P.kappa * (barrier_d2(d2 - P.dmin * P.dmin, (2 * P.dmin + P.dhat) * P.dhat) * phys_scale(P));
-}
+static double f0(const BarrierParams& P, double d2) { return fk(P, 0, d2); }
+static double f1(const BarrierParams& P, double d2) { return fk(P, 1, d2); }
+static double f2(const BarrierParams& P, double d2) { return fk(P, 2, d2); }
 
 // ---------------------------------------------------------------------------
 // Closed-form squared-distance derivatives (own derivation).
@@ -1268,6 +1316,104 @@ static double mollifier(const Contact& c, const V3* x, double* gm, double* Hm, b
     return m;
 }
 
+// Distance-vector coefficients c (t = sum_i c_i x_i) with the collision's
+// known distance type (compute_coefficients in candidates/vertex_vertex.cpp:40-46,
+// edge_vertex.cpp:45-75, edge_edge.cpp:42-96, face_vertex.cpp:42-89): VV and
+// EV (P_E) fixed, EE by its stored type, FV point-plane (P_T).
+static void contact_coefficients(const Contact& c, const V3* x, double* co)
+{
+    auto pe_alpha = [](V3 p, V3 e0, V3 e1) {
+        const V3 e = sub(e1, e0);
+        return dot(sub(p, e0), e) / sqnorm(e);
+    };
+    if (c.type == CT_VV) {
+        co[0] = 1.0;
+        co[1] = -1.0;
+    } else if (c.type == CT_EV) {
+        const double a = pe_alpha(x[0], x[1], x[2]);
+        co[0] = 1.0;
+        co[1] = -1.0 + a;
+        co[2] = -a;
+    } else if (c.type == CT_FV) {
+        double u, v;
+        ldlt2_solve(sub(x[2], x[1]), sub(x[3], x[1]), sub(x[0], x[1]), u, v);
+        co[0] = 1.0;
+        co[1] = -1.0 + u + v;
+        co[2] = -u;
+        co[3] = -v;
+    } else {
+        const double Z[4] = { 0, 0, 0, 0 };
+        for (int i = 0; i < 4; ++i) co[i] = Z[i];
+        switch (c.dtype) {
+        case EA0_EB0: co[0] = 1.0, co[2] = -1.0; break;
+        case EA0_EB1: co[0] = 1.0, co[3] = -1.0; break;
+        case EA1_EB0: co[1] = 1.0, co[2] = -1.0; break;
+        case EA1_EB1: co[1] = 1.0, co[3] = -1.0; break;
+        case EA_EB0: {
+            const double a = pe_alpha(x[2], x[0], x[1]);
+            co[0] = 1.0 - a, co[1] = a, co[2] = -1.0;
+        } break;
+        case EA_EB1: {
+            const double a = pe_alpha(x[3], x[0], x[1]);
+            co[0] = 1.0 - a, co[1] = a, co[3] = -1.0;
+        } break;
+        case EA0_EB: {
+            const double a = pe_alpha(x[0], x[2], x[3]);
+            co[0] = 1.0, co[2] = -1.0 + a, co[3] = -a;
+        } break;
+        case EA1_EB: {
+            const double a = pe_alpha(x[1], x[2], x[3]);
+            co[1] = 1.0, co[2] = -1.0 + a, co[3] = -a;
+        } break;
+        default: {
+            // edge_edge_closest_point (tangent/closest_point.cpp:65-87):
+            // [|ea|^2, -eb.ea; -eb.ea, |eb|^2] x = [-(ea0-eb0).ea, (ea0-eb0).eb]
+            const V3 ea = sub(x[1], x[0]), eb = sub(x[3], x[2]);
+            double a, b;
+            ldlt2_solve(ea, scale(eb, -1.0), sub(x[2], x[0]), a, b);
+            co[0] = 1.0 - a, co[1] = a, co[2] = -1.0 + b, co[3] = -b;
+        }
+        }
+    }
+}
+
+// t = sum_i c_i x_i, accumulated in vertex order (collision_stencil.cpp:14-25)
+static V3 distance_vector(const Contact& c, const V3* x, const double* co)
+{
+    V3 t { 0, 0, 0 };
+    for (int i = 0; i < c.n; ++i) t = add(t, scale(x[i], co[i]));
+    return t;
+}
+
+// Gauss-Newton Hessian diagonal of one collision (normal_potential.cpp:236-269):
+// w (4 f''(|t|^2) c_i^2 t_d^2 + 2 f'(|t|^2) c_i^2).  The mollifier plays no part.
+static void contact_gn_diagonal(const BarrierParams& P, const Contact& c, const V3* x, double* out)
+{
+    double co[4];
+    contact_coefficients(c, x, co);
+    const V3 t = distance_vector(c, x, co);
+    const double d2 = sqnorm(t);
+    const double s1 = c.w * 4.0 * f2(P, d2), s2 = c.w * 2.0 * f1(P, d2);
+    const double t2[3] = { t.x * t.x, t.y * t.y, t.z * t.z };
+    for (int i = 0; i < c.n; ++i) {
+        const double ci2 = co[i] * co[i];
+        for (int k = 0; k < 3; ++k) out[3 * i + k] = s1 * (ci2 * t2[k]) + s2 * ci2;
+    }
+}
+
+// p^T H_GN p of one collision (normal_potential.cpp:271-308):
+// w (4 f'' (J^T p . t)^2 + 2 f' |J^T p|^2) with J^T p = sum_i c_i p_i.
+static double contact_gn_quadratic_form(const BarrierParams& P, const Contact& c, const V3* x, const V3* pl)
+{
+    double co[4];
+    contact_coefficients(c, x, co);
+    const V3 t = distance_vector(c, x, co);
+    const double d2 = sqnorm(t);
+    const V3 pj = distance_vector(c, pl, co);
+    const double pjt = dot(pj, t);
+    return c.w * (4.0 * f2(P, d2) * (pjt * pjt) + 2.0 * f1(P, d2) * sqnorm(pj));
+}
+
 static double contact_energy(const BarrierParams& P, const Contact& c, const V3* x)
 {
     double g[12], H[144];
@@ -1752,7 +1898,11 @@ void orc_set_psd_solver(int which) { g_psd_solver = which; }
 
 double orc_barrier(double d, double dhat, int deriv)
 {
-    return deriv == 0 ? barrier(d, dhat) : (deriv == 1 ? barrier_d1(d, dhat) : barrier_d2(d, dhat));
+    return clamped_log(deriv, d, dhat);
+}
+double orc_barrier_kind(int kind, double d, double dhat, int deriv)
+{
+    return barrier_any(kind, deriv, d, dhat);
 }
 
 // Squared-distance gradient/Hessian of a stencil.  kind: 0 PP(2 verts),
@@ -1926,6 +2076,58 @@ void orc_barrier_gradient(void* h, const double* V, int64_t nV, const int32_t* E
         for (int t = 0; t < nt; ++t) s += loc[t][i];
         grad[i] = s;
     }
+}
+
+void orc_barrier_gn_diagonal(void* h, const double* V, int64_t nV, const int32_t* E, const int32_t* F, double dhat,
+    double kappa, double dmin, int physical, int nthreads, double* diag)
+{
+    Collisions* C = (Collisions*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    const int64_t n = C->vv_w.size() + C->ev_w.size() + C->ee_w.size() + C->fv_w.size();
+    const int nt = std::max(1, nthreads);
+    std::vector<std::vector<double>> loc(nt, std::vector<double>(3 * nV, 0.0));
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t i = b; i < e; ++i) {
+            Contact c;
+            contact_stencil(*C, E, F, i, c);
+            V3 x[4];
+            gather(V, c, x);
+            double g[12];
+            contact_gn_diagonal(P, c, x, g);
+            for (int k = 0; k < c.n; ++k)
+                for (int d = 0; d < 3; ++d) loc[t][3 * c.vid[k] + d] += g[3 * k + d];
+        }
+    });
+    for (int64_t i = 0; i < 3 * nV; ++i) {
+        double s = 0;
+        for (int t = 0; t < nt; ++t) s += loc[t][i];
+        diag[i] = s;
+    }
+}
+
+double orc_barrier_gn_quadratic_form(void* h, const double* V, const int32_t* E, const int32_t* F, double dhat,
+    double kappa, double dmin, int physical, const double* p, int nthreads)
+{
+    Collisions* C = (Collisions*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    const int64_t n = C->vv_w.size() + C->ev_w.size() + C->ee_w.size() + C->fv_w.size();
+    const int nt = std::max(1, nthreads);
+    std::vector<double> part(nt, 0.0);
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        double s = 0;
+        for (int64_t i = b; i < e; ++i) {
+            Contact c;
+            contact_stencil(*C, E, F, i, c);
+            V3 x[4], pl[4];
+            gather(V, c, x);
+            gather(p, c, pl);
+            s += contact_gn_quadratic_form(P, c, x, pl);
+        }
+        part[t] += s;
+    });
+    double s = 0;
+    for (double v : part) s += v;
+    return s;
 }
 
 struct CSR {

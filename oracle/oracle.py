@@ -45,6 +45,11 @@ def lib():
         L.orc_set_psd_solver.argtypes = [i32]
         L.orc_barrier.restype = d
         L.orc_barrier.argtypes = [d, d, i32]
+        L.orc_barrier_kind.restype = d
+        L.orc_barrier_kind.argtypes = [i32, d, d, i32]
+        L.orc_barrier_gn_diagonal.argtypes = [vp, P, i64, P, P, d, d, d, i32, i32, P]
+        L.orc_barrier_gn_quadratic_form.restype = d
+        L.orc_barrier_gn_quadratic_form.argtypes = [vp, P, P, P, d, d, d, i32, P, i32]
         L.orc_distance_derivatives.restype = d
         L.orc_distance_derivatives.argtypes = [i32, i32, P, P, P]
         L.orc_faces_to_edges.restype = i32
@@ -125,8 +130,12 @@ def set_psd_solver(name: str):
     lib().orc_set_psd_solver({"ql": 0, "jacobi": 1}[name])
 
 
-def barrier(d, dhat, deriv=0):
-    return lib().orc_barrier(float(d), float(dhat), int(deriv))
+def barrier(d, dhat, deriv=0, kind=0):
+    """Barrier function kind (0 clamped log, 1 normalized clamped log, 2 clamped
+    log squared, 3 cubic, 4 two-stage) or its derivative."""
+    if kind == 0:
+        return lib().orc_barrier(float(d), float(dhat), int(deriv))
+    return lib().orc_barrier_kind(int(kind), float(d), float(dhat), int(deriv))
 
 
 def distance_derivatives(kind, x, dtype=8):
@@ -224,6 +233,20 @@ def barrier_gradient(col, V, E, F, dhat, kappa, dmin=0.0, physical=False, nthrea
     lib().orc_barrier_gradient(col.h, _p(V), V.shape[0], _p(E), _p(F), dhat, kappa, dmin, int(physical),
                                int(nthreads or os.cpu_count() or 1), _p(g))
     return g
+
+
+def barrier_gauss_newton_diagonal(col, V, E, F, dhat, kappa, dmin=0.0, physical=False, nthreads=None):
+    V, E, F = _f64(V), _i32(E), _i32(F)
+    g = np.zeros(V.size)
+    lib().orc_barrier_gn_diagonal(col.h, _p(V), V.shape[0], _p(E), _p(F), dhat, kappa, dmin, int(physical),
+                                  int(nthreads or os.cpu_count() or 1), _p(g))
+    return g
+
+
+def barrier_gauss_newton_quadratic_form(col, V, E, F, p, dhat, kappa, dmin=0.0, physical=False, nthreads=None):
+    V, E, F, p = _f64(V), _i32(E), _i32(F), _f64(p)
+    return lib().orc_barrier_gn_quadratic_form(col.h, _p(V), _p(E), _p(F), dhat, kappa, dmin, int(physical), _p(p),
+                                               int(nthreads or os.cpu_count() or 1))
 
 
 def barrier_hessian(col, V, E, F, dhat, kappa, dmin=0.0, physical=False, psd="none", nthreads=None):

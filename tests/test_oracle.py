@@ -168,6 +168,91 @@ def test_barrier_derivatives_fd(oracle_mod, use_sq):
             assert abs(oracle_mod.barrier(d, dh, 2) - fd2) <= 1e-4 * max(abs(fd2), 1e-30) + 1e-9
 
 
+@pytest.mark.parametrize("kind", [1, 2, 3, 4])
+@pytest.mark.parametrize("use_sq", [False, True])
+def test_barrier_kinds_derivatives_fd(oracle_mod, kind, use_sq):
+    """barrier/test_barrier.cpp:398-461 for the Normalized, ClampedLogSq, Cubic
+    and TwoStage barriers: first and second derivatives against central
+    differences over the same dhat and d grid."""
+    for k in range(-2 if use_sq else -5, 0):
+        dhat = 10.0 ** k
+        for d in np.linspace(0.5 * dhat, 0.9 * dhat, 10, endpoint=False):
+            if use_sq:
+                d, dh = d * d, dhat * dhat
+            else:
+                dh = dhat
+            h = d * 1e-6
+            b = lambda x, n=0: oracle_mod.barrier(x, dh, n, kind)
+            fd1 = (b(d + h) - b(d - h)) / (2 * h)
+            fd2 = (b(d + h, 1) - b(d - h, 1)) / (2 * h)
+            assert abs(b(d, 1) - fd1) <= 1e-5 * max(abs(fd1), abs(b(d, 1)))
+            assert abs(b(d, 2) - fd2) <= 1e-5 * max(abs(fd2), abs(b(d, 2)))
+
+
+def test_barrier_kind_values(oracle_mod):
+    """Closed forms at hand-checked points (barrier.cpp:47-154)."""
+    dh = 2.0
+    # normalized = clamped log of d / dhat against 1, derivatives / dhat^k
+    for k in range(3):
+        assert oracle_mod.barrier(0.6, dh, k, 1) == oracle_mod.barrier(0.3, 1.0, k) / dh ** k
+    # cubic: -2/(3 dhat) (d - dhat)^3, 4 (1 - d / dhat) and 0 at/after dhat
+    assert oracle_mod.barrier(1.0, dh, 0, 3) == pytest.approx(-2.0 / 3.0 / 2.0 * (-1.0) ** 3, rel=1e-15)
+    assert oracle_mod.barrier(1.0, dh, 2, 3) == 2.0
+    assert oracle_mod.barrier(2.0, dh, 0, 3) == 0.0
+    # two-stage: quadratic on [dhat/2, dhat), log below, continuous at dhat/2
+    assert oracle_mod.barrier(1.5, dh, 0, 4) == 0.5 * 0.5 * 0.5
+    assert oracle_mod.barrier(1.5, dh, 2, 4) == 1.0
+    lo = oracle_mod.barrier(1.0 - 1e-12, dh, 0, 4)
+    assert lo == pytest.approx(oracle_mod.barrier(1.0, dh, 0, 4), rel=1e-9)
+    # clamped log squared: (d - dhat)^2 ln^2(d / dhat); infinite at d <= 0
+    assert oracle_mod.barrier(0.5, dh, 0, 2) == pytest.approx(1.5 ** 2 * np.log(0.25) ** 2, rel=1e-15)
+    assert oracle_mod.barrier(0.0, dh, 0, 2) == float("inf")
+
+
+def _vv_collisions(oracle_mod, rng, n):
+    """A VV-only collision set of n random close pairs (weights 1)."""
+    V = rng.uniform(0, 1, (2 * n, 3))
+    V[1::2] = V[0::2] + rng.uniform(-1e-2, 1e-2, (n, 3))
+    vv = np.arange(2 * n, dtype=np.int32).reshape(n, 2)
+    z2, z1 = np.zeros((0, 2), np.int32), np.zeros(0)
+    col = oracle_mod.Collisions.from_arrays(vv, np.ones(n), z2, z1, z2, z1, np.zeros(0, np.int8), z1, z2, z1)
+    return V, col
+
+
+def test_gauss_newton_equals_hessian_on_vertex_pairs(oracle_mod):
+    """For vertex-vertex contacts d^2 = |t|^2 is quadratic in the positions,
+    so the Gauss-Newton Hessian is the Hessian: its diagonal and quadratic
+    form match the assembled Hessian's."""
+    import scipy.sparse as sps
+    rng = np.random.Generator(np.random.PCG64(41))
+    V, col = _vv_collisions(oracle_mod, rng, 50)
+    E, F = np.zeros((0, 2), np.int32), np.zeros((0, 3), np.int32)
+    dhat, kappa = 2e-2, 3.0
+    for kind in range(5):
+        bits = kind << 4
+        rp, ci, va = oracle_mod.barrier_hessian(col, V, E, F, dhat, kappa, physical=bits)
+        H = sps.csr_matrix((va, ci, rp), shape=(V.size, V.size))
+        d = oracle_mod.barrier_gauss_newton_diagonal(col, V, E, F, dhat, kappa, physical=bits)
+        assert np.linalg.norm(d - H.diagonal()) <= 1e-12 * np.linalg.norm(d)
+        p = rng.standard_normal(V.size)
+        q = oracle_mod.barrier_gauss_newton_quadratic_form(col, V, E, F, p, dhat, kappa, physical=bits)
+        assert q == pytest.approx(p @ (H @ p), rel=1e-10)
+
+
+def test_gauss_newton_quadratic_form_axes(oracle_mod):
+    """p = e_i gives diagonal entry i, for every contact type."""
+    from ipctk_gb300 import scenes
+    sc = scenes.two_sheet(side=12, seed=2)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    col = oracle_mod.build_collisions(V, E, F, sc["dhat"])
+    d = oracle_mod.barrier_gauss_newton_diagonal(col, V, E, F, sc["dhat"], sc["kappa"])
+    for i in np.argsort(-np.abs(d))[:12]:
+        e = np.zeros(V.size)
+        e[i] = 1.0
+        q = oracle_mod.barrier_gauss_newton_quadratic_form(col, V, E, F, e, sc["dhat"], sc["kappa"])
+        assert q == pytest.approx(d[i], rel=1e-12)
+
+
 def test_barrier_values(oracle_mod):
     """barrier.cpp:11-43: b(d)=-(d-dh)^2 ln(d/dh) on (0,dh), 0 beyond, inf at 0"""
     assert oracle_mod.barrier(0.0, 1.0) == float("inf")
