@@ -100,6 +100,13 @@ int ipcg_mesh_sizes(const ipcg_mesh* mesh, int64_t sizes[3]);
 /* CollisionMesh::faces_to_edges() (collision_mesh.hpp:327-329): num_faces*3 */
 int ipcg_mesh_faces_to_edges(const ipcg_mesh* mesh, int32_t* out);
 
+/* CollisionMesh::vertex_areas() / edge_areas() (collision_mesh.cpp:309-374):
+ * per-vertex and per-edge areas of the rest mesh (a vertex or edge takes a
+ * third of each incident face's area; without faces, half the incident edge
+ * lengths or the edge's length; an isolated vertex 1).  Either output may be
+ * NULL; sizes num_vertices and num_edges. */
+int ipcg_mesh_areas(const ipcg_mesh* mesh, double* vertex_areas, double* edge_areas);
+
 /* The cudaStream_t (as void*) on which all work for this mesh runs. */
 int ipcg_mesh_stream(const ipcg_mesh* mesh, void** stream);
 
@@ -133,6 +140,15 @@ int ipcg_set_hessian_chunk_contacts(int64_t contacts);
 
 int ipcg_collisions_create(ipcg_collisions** out);
 int ipcg_collisions_destroy(ipcg_collisions* collisions);
+
+/* NormalCollisions::set_use_area_weighting / use_area_weighting
+ * (normal_collisions.cpp:160-175); applies to the next build.  Weights
+ * become FV vertex_area(v)/4 and EE (edge_area(ea) + edge_area(eb))/4
+ * (normal_collisions_builder.cpp:146,181-183), carried by their VV / EV
+ * reductions; duplicate VV / EV keys sum their weights in ascending order
+ * (the reference's order is thread-dependent). */
+int ipcg_collisions_set_use_area_weighting(ipcg_collisions* collisions, int use_area_weighting);
+int ipcg_collisions_use_area_weighting(const ipcg_collisions* collisions, int* use_area_weighting);
 
 /* Replaces NormalCollisions::build(mesh, V, dhat, dmin, broad_phase=nullptr)
  * (src/ipc/collisions/normal/normal_collisions.hpp:45-50,

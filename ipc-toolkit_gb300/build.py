@@ -20,6 +20,7 @@ LIB = os.path.join(OUT_DIR, "libipcg.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                 "-Xcompiler", "-ffp-contract=off",
                  "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 EXACT = {"broad_phase.cu", "collisions.cu", "ccd.cu", "candidates.cu"}
 SOURCES = ["abi.cu", "broad_phase.cu", "collisions.cu", "barrier.cu", "ccd.cu", "sort.cu", "server.cu", "candidates.cu"]

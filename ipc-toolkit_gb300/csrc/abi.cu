@@ -338,6 +338,14 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
             upload(m->E, (const int*)hE.data(), 2 * nE, m->stream);
             upload(m->F, (const int*)hF.data(), 3 * nF, m->stream);
             upload(m->F2E, (const int*)f2e.data(), 3 * nF, m->stream);
+            {
+                const std::vector<double> hR = to_host(rest, 3 * nV);
+                std::vector<double> va(nV), ea(nE);
+                mesh_areas_host(hR.data(), nV, hE.data(), nE, hF.data(), nF, f2e.data(), va.data(), ea.data());
+                upload(m->vertex_area, va.data(), nV, m->stream);
+                upload(m->edge_area, ea.data(), nE, m->stream);
+                IPCG_CUDA(cudaStreamSynchronize(m->stream));
+            }
             m->h_F2E = std::move(f2e);
             m->n_scenes = n_scenes;
             m->h_voff = std::move(voff);
@@ -425,6 +433,33 @@ int ipcg_collisions_create(ipcg_collisions** out)
 int ipcg_collisions_destroy(ipcg_collisions* c)
 {
     return guarded([&] { delete c; });
+}
+
+int ipcg_collisions_set_use_area_weighting(ipcg_collisions* c, int on)
+{
+    return guarded([&] {
+        require(c != nullptr, "NULL argument");
+        c->use_area_weighting = on ? 1 : 0;
+    });
+}
+
+int ipcg_collisions_use_area_weighting(const ipcg_collisions* c, int* on)
+{
+    return guarded([&] {
+        require(c && on, "NULL argument");
+        *on = c->use_area_weighting;
+    });
+}
+
+int ipcg_mesh_areas(const ipcg_mesh* m, double* vertex_areas, double* edge_areas)
+{
+    return guarded([&] {
+        require(m != nullptr, "NULL argument");
+        if (vertex_areas && m->nV)
+            IPCG_CUDA(cudaMemcpy(vertex_areas, m->vertex_area.p, sizeof(double) * m->nV, cudaMemcpyDefault));
+        if (edge_areas && m->nE)
+            IPCG_CUDA(cudaMemcpy(edge_areas, m->edge_area.p, sizeof(double) * m->nE, cudaMemcpyDefault));
+    });
 }
 
 int ipcg_collisions_build(ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat, double dmin)

@@ -177,6 +177,11 @@ struct ipcg_mesh {
     ipcg::DBuf<double> rest;
     ipcg::DBuf<int> E, F, F2E;
     std::vector<int32_t> h_F2E;
+    ipcg::DBuf<double> rec_w;        // area weighting: VV / EV record weights
+    ipcg::DBuf<unsigned long long> wkeys; // weighted merge scratch
+    ipcg::DBuf<int> widx;
+    ipcg::DBuf<double> vertex_area;  // rest-mesh areas (area weighting)
+    ipcg::DBuf<double> edge_area;
     // work space shared by the calls on this mesh
     ipcg::DBuf<double> V0, V1;       // device copies of host position inputs
     ipcg::DBuf<double> bounds;       // mesh AABB scratch
@@ -204,6 +209,7 @@ struct ipcg_collisions {
     double dmin = 0;
     std::vector<double> scene_dmin;  // per scene (batches)
     bool sorted = false;             // lists sorted by key (built here, not loaded)
+    int use_area_weighting = 0;      // NormalCollisions::use_area_weighting()
     ipcg::DBuf<int2> vv, ev, ee, fv;
     ipcg::DBuf<double> vv_w, ev_w, ee_w, fv_w, ee_eps;
     ipcg::DBuf<int8_t> ee_dtype;
@@ -244,6 +250,10 @@ void build_lbvh(ipcg_mesh* m, LBVH& bvh, int kind /*2 edges, 3 faces*/, const do
 void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, const double* scene_r, int64_t& n_ee,
     int64_t& n_fv);
 
+// collisions.cu: per-vertex and per-edge areas of the rest mesh
+// (collision_mesh.cpp:309-374), summed in face order on the host.
+void mesh_areas_host(const double* rest, int64_t nV, const int32_t* E, int64_t nE, const int32_t* F, int64_t nF,
+    const int32_t* F2E, double* vertex_area, double* edge_area);
 // collisions.cu: per-scene dhat / dmin (host arrays of n_scenes)
 void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, const double* dhat, const double* dmin);
 

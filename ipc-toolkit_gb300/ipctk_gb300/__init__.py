@@ -88,6 +88,9 @@ def _load():
         "ipcg_has_intersections": (i32, [P, P, P]),
         "ipcg_barrier_gauss_newton_hessian_diagonal": (i32, [P, P, P, d, d, i32, P]),
         "ipcg_barrier_gauss_newton_hessian_quadratic_form": (i32, [P, P, P, d, d, i32, P, P]),
+        "ipcg_mesh_areas": (i32, [P, P, P]),
+        "ipcg_collisions_set_use_area_weighting": (i32, [P, i32]),
+        "ipcg_collisions_use_area_weighting": (i32, [P, P]),
         "ipcg_candidates_create": (i32, [PP]),
         "ipcg_candidates_destroy": (i32, [P]),
         "ipcg_candidates_build": (i32, [P, P, P, d]),
@@ -318,6 +321,20 @@ class CollisionMesh:
         _check(_load().ipcg_mesh_faces_to_edges(self._h, _ptr(out)))
         return out
 
+    @property
+    def vertex_areas(self):
+        """CollisionMesh::vertex_areas() (collision_mesh.cpp:309-374)."""
+        out = np.zeros(self.num_vertices)
+        _check(_load().ipcg_mesh_areas(self._h, _ptr(out), None))
+        return out
+
+    @property
+    def edge_areas(self):
+        """CollisionMesh::edge_areas() (collision_mesh.cpp:309-374)."""
+        out = np.zeros(self.num_edges)
+        _check(_load().ipcg_mesh_areas(self._h, None, _ptr(out)))
+        return out
+
 
 class SceneBatch(CollisionMesh):
     """Many independent scenes (one CollisionMesh each in the reference)
@@ -385,6 +402,17 @@ class NormalCollisions:
         _check(_load().ipcg_collisions_create(C.byref(h)))
         self._h = h
         self._cache = None
+
+    @property
+    def use_area_weighting(self) -> bool:
+        """NormalCollisions::use_area_weighting (applies to the next build)."""
+        v = C.c_int()
+        _check(_load().ipcg_collisions_use_area_weighting(self._h, C.byref(v)))
+        return bool(v.value)
+
+    @use_area_weighting.setter
+    def use_area_weighting(self, on: bool):
+        _check(_load().ipcg_collisions_set_use_area_weighting(self._h, int(bool(on))))
 
     def __del__(self):
         h = getattr(self, "_h", None)

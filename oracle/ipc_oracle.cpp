@@ -616,41 +616,94 @@ struct Collisions {
 
 struct Raw {
     std::vector<uint64_t> vv, ev;
+    std::vector<double> vv_w, ev_w;
     std::vector<int32_t> ee;
-    std::vector<double> ee_eps;
+    std::vector<double> ee_eps, ee_w;
     std::vector<int8_t> ee_dt;
     std::vector<int32_t> fv;
+    std::vector<double> fv_w;
 };
+
+// Per-vertex and per-edge areas of the rest mesh (collision_mesh.cpp:309-374):
+// a vertex takes 1/3 of each incident face's area, else 1/2 of each incident
+// edge's length, else 1; an edge takes 1/3 of each incident face's area, else
+// its length.  Sums run in face (edge) order, as the reference's loops do.
+static void mesh_areas(const double* R, int64_t nV, const int32_t* E, int64_t nE, const int32_t* F, int64_t nF,
+    const int32_t* F2E, double* va, double* ea)
+{
+    std::vector<double> vea(nV, -1.0), vfa(nV, -1.0);
+    auto len = [&](int64_t e) { return std::sqrt(sqnorm(sub(row(R, E[2 * e + 1]), row(R, E[2 * e])))); };
+    for (int64_t i = 0; i < nE; ++i) {
+        const double l = len(i);
+        for (int j = 0; j < 2; ++j) {
+            double& a = vea[E[2 * i + j]];
+            a = std::max(a, 0.0);
+            a += 0.5 * l;
+        }
+    }
+    for (int64_t i = 0; i < nE; ++i) ea[i] = -1.0;
+    for (int64_t i = 0; i < nF; ++i) {
+        const V3 t0 = row(R, F[3 * i]), t1 = row(R, F[3 * i + 1]), t2 = row(R, F[3 * i + 2]);
+        const double fa = 0.5 * std::sqrt(sqnorm(cross(sub(t1, t0), sub(t2, t0))));
+        for (int j = 0; j < 3; ++j) {
+            double& a = vfa[F[3 * i + j]];
+            a = std::max(a, 0.0);
+            a += fa / 3.0;
+            double& b = ea[F2E[3 * i + j]];
+            b = std::max(b, 0.0);
+            b += fa / 3.0;
+        }
+    }
+    for (int64_t v = 0; v < nV; ++v) va[v] = vfa[v] < 0 ? (vea[v] < 0 ? 1.0 : vea[v]) : vfa[v];
+    for (int64_t i = 0; i < nE; ++i)
+        if (ea[i] < 0) ea[i] = len(i);
+}
 
 static inline uint64_t key2(uint32_t a, uint32_t b) { return ((uint64_t)a << 32) | b; }
 
-static void add_vv(Raw& r, int a, int b) { r.vv.push_back(key2(std::min(a, b), std::max(a, b))); }
-static void add_ev(Raw& r, int e, int v) { r.ev.push_back(key2(e, v)); }
+static void add_vv(Raw& r, int a, int b, double w)
+{
+    r.vv.push_back(key2(std::min(a, b), std::max(a, b)));
+    r.vv_w.push_back(w);
+}
+static void add_ev(Raw& r, int e, int v, double w)
+{
+    r.ev.push_back(key2(e, v));
+    r.ev_w.push_back(w);
+}
 
 // builder.cpp:239-336
-static void add_face_vertex(Raw& r, const double* V, const int32_t* F, const int32_t* F2E, int fi, int vi, double offset_sqr)
+// Area weighting (va, ea non-null): FV weight vertex_area(v) / 4
+// (builder.cpp:146), EE weight (edge_area(ea) + edge_area(eb)) / 4
+// (builder.cpp:181-183); their reductions carry the same weight.
+static void add_face_vertex(Raw& r, const double* V, const int32_t* F, const int32_t* F2E, int fi, int vi,
+    double offset_sqr, const double* va)
 {
+    const double w = va ? 0.25 * va[vi] : 1.0;
     const int f0 = F[3 * fi], f1 = F[3 * fi + 1], f2 = F[3 * fi + 2];
     const V3 p = row(V, vi), t0 = row(V, f0), t1 = row(V, f1), t2 = row(V, f2);
     const int dtype = point_triangle_distance_type(p, t0, t1, t2);
     const double d = point_triangle_distance(p, t0, t1, t2, dtype);
     if (!(d < offset_sqr)) return;
     switch (dtype) {
-    case P_T0: add_vv(r, vi, f0); break;
-    case P_T1: add_vv(r, vi, f1); break;
-    case P_T2: add_vv(r, vi, f2); break;
-    case P_E0t: add_ev(r, F2E[3 * fi + 0], vi); break;
-    case P_E1t: add_ev(r, F2E[3 * fi + 1], vi); break;
-    case P_E2t: add_ev(r, F2E[3 * fi + 2], vi); break;
+    case P_T0: add_vv(r, vi, f0, w); break;
+    case P_T1: add_vv(r, vi, f1, w); break;
+    case P_T2: add_vv(r, vi, f2, w); break;
+    case P_E0t: add_ev(r, F2E[3 * fi + 0], vi, w); break;
+    case P_E1t: add_ev(r, F2E[3 * fi + 1], vi, w); break;
+    case P_E2t: add_ev(r, F2E[3 * fi + 2], vi, w); break;
     default:
         r.fv.push_back(fi);
         r.fv.push_back(vi);
+        r.fv_w.push_back(w);
     }
 }
 
 // builder.cpp:140-237 (candidate oriented ea < eb)
-static void add_edge_edge(Raw& r, const double* V, const double* Vrest, const int32_t* E, int ea, int eb, double offset_sqr)
+static void add_edge_edge(Raw& r, const double* V, const double* Vrest, const int32_t* E, int ea, int eb,
+    double offset_sqr, const double* earea)
 {
+    const double w = earea ? 0.25 * (earea[ea] + earea[eb]) : 1.0;
     const int a0 = E[2 * ea], a1 = E[2 * ea + 1], b0 = E[2 * eb], b1 = E[2 * eb + 1];
     const V3 xa0 = row(V, a0), xa1 = row(V, a1), xb0 = row(V, b0), xb1 = row(V, b1);
     const int actual = edge_edge_distance_type(xa0, xa1, xb0, xb1);
@@ -660,42 +713,50 @@ static void add_edge_edge(Raw& r, const double* V, const double* Vrest, const in
     const double c = ee_cross_sqnorm(xa0, xa1, xb0, xb1);
     const int dtype = c < eps_x ? (int)EA_EB : actual;
     switch (dtype) {
-    case EA0_EB0: add_vv(r, a0, b0); break;
-    case EA0_EB1: add_vv(r, a0, b1); break;
-    case EA1_EB0: add_vv(r, a1, b0); break;
-    case EA1_EB1: add_vv(r, a1, b1); break;
-    case EA_EB0: add_ev(r, ea, b0); break;
-    case EA_EB1: add_ev(r, ea, b1); break;
-    case EA0_EB: add_ev(r, eb, a0); break;
-    case EA1_EB: add_ev(r, eb, a1); break;
+    case EA0_EB0: add_vv(r, a0, b0, w); break;
+    case EA0_EB1: add_vv(r, a0, b1, w); break;
+    case EA1_EB0: add_vv(r, a1, b0, w); break;
+    case EA1_EB1: add_vv(r, a1, b1, w); break;
+    case EA_EB0: add_ev(r, ea, b0, w); break;
+    case EA_EB1: add_ev(r, ea, b1, w); break;
+    case EA0_EB: add_ev(r, eb, a0, w); break;
+    case EA1_EB: add_ev(r, eb, a1, w); break;
     default:
         r.ee.push_back(ea);
         r.ee.push_back(eb);
         r.ee_eps.push_back(eps_x);
         r.ee_dt.push_back((int8_t)actual);
+        r.ee_w.push_back(w);
     }
 }
 
 static void finalize(Raw& all, Collisions& C)
 {
-    // builder.cpp:547-689: duplicates merge with summed weights; all weights
-    // here are 1 (no area weighting) so the merged weight is a count.  Output
-    // is sorted by key (the reference order is thread-dependent).
-    auto rle = [](std::vector<uint64_t>& keys, std::vector<int32_t>& ids, std::vector<double>& w) {
-        std::sort(keys.begin(), keys.end());
+    // builder.cpp:547-689: duplicate VV / EV keys merge with summed weights.
+    // Lists are sorted by key and each key's weights are summed in ascending
+    // order (without area weighting they are all 1, so the sum is a count);
+    // the reference's order is thread-dependent, this one is not.
+    auto merge = [](const std::vector<uint64_t>& keys, const std::vector<double>& win, std::vector<int32_t>& ids,
+                     std::vector<double>& w) {
+        std::vector<size_t> perm(keys.size());
+        std::iota(perm.begin(), perm.end(), 0);
+        std::sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
+            return keys[a] != keys[b] ? keys[a] < keys[b] : win[a] < win[b];
+        });
         ids.clear();
         w.clear();
-        for (size_t i = 0; i < keys.size();) {
+        for (size_t i = 0; i < perm.size();) {
             size_t j = i;
-            while (j < keys.size() && keys[j] == keys[i]) ++j;
-            ids.push_back((int32_t)(keys[i] >> 32));
-            ids.push_back((int32_t)(keys[i] & 0xffffffffu));
-            w.push_back((double)(j - i));
+            double sum = 0.0;
+            while (j < perm.size() && keys[perm[j]] == keys[perm[i]]) sum += win[perm[j++]];
+            ids.push_back((int32_t)(keys[perm[i]] >> 32));
+            ids.push_back((int32_t)(keys[perm[i]] & 0xffffffffu));
+            w.push_back(sum);
             i = j;
         }
     };
-    rle(all.vv, C.vv, C.vv_w);
-    rle(all.ev, C.ev, C.ev_w);
+    merge(all.vv, all.vv_w, C.vv, C.vv_w);
+    merge(all.ev, all.ev_w, C.ev, C.ev_w);
     // EE: unique pairs by construction; sort by (ea, eb)
     const size_t nee = all.ee_eps.size();
     std::vector<size_t> perm(nee);
@@ -706,22 +767,25 @@ static void finalize(Raw& all, Collisions& C)
     C.ee.resize(2 * nee);
     C.ee_eps.resize(nee);
     C.ee_dtype.resize(nee);
-    C.ee_w.assign(nee, 1.0);
+    C.ee_w.resize(nee);
     for (size_t i = 0; i < nee; ++i) {
         C.ee[2 * i] = all.ee[2 * perm[i]];
         C.ee[2 * i + 1] = all.ee[2 * perm[i] + 1];
         C.ee_eps[i] = all.ee_eps[perm[i]];
         C.ee_dtype[i] = all.ee_dt[perm[i]];
+        C.ee_w[i] = all.ee_w[perm[i]];
     }
     const size_t nfv = all.fv.size() / 2;
-    std::vector<uint64_t> fk(nfv);
-    for (size_t i = 0; i < nfv; ++i) fk[i] = key2(all.fv[2 * i], all.fv[2 * i + 1]);
-    std::sort(fk.begin(), fk.end());
+    std::vector<size_t> fp(nfv);
+    std::iota(fp.begin(), fp.end(), 0);
+    auto fkey = [&](size_t i) { return key2(all.fv[2 * i], all.fv[2 * i + 1]); };
+    std::sort(fp.begin(), fp.end(), [&](size_t a, size_t b) { return fkey(a) < fkey(b); });
     C.fv.resize(2 * nfv);
-    C.fv_w.assign(nfv, 1.0);
+    C.fv_w.resize(nfv);
     for (size_t i = 0; i < nfv; ++i) {
-        C.fv[2 * i] = (int32_t)(fk[i] >> 32);
-        C.fv[2 * i + 1] = (int32_t)(fk[i] & 0xffffffffu);
+        C.fv[2 * i] = all.fv[2 * fp[i]];
+        C.fv[2 * i + 1] = all.fv[2 * fp[i] + 1];
+        C.fv_w[i] = all.fv_w[fp[i]];
     }
 }
 
@@ -1940,10 +2004,24 @@ int orc_faces_to_edges(const int32_t* F, int64_t nF, const int32_t* E, int64_t n
 }
 
 // --- collision set ---
+void orc_mesh_areas(const double* Vrest, int64_t nV, const int32_t* E, int64_t nE, const int32_t* F, int64_t nF,
+    const int32_t* F2E, double* vertex_area, double* edge_area)
+{
+    mesh_areas(Vrest, nV, E, nE, F, nF, F2E, vertex_area, edge_area);
+}
+
 void* orc_collisions_build(const double* V, const double* Vrest, int64_t nV, const int32_t* E, int64_t nE,
-    const int32_t* F, int64_t nF, const int32_t* F2E, double dhat, double dmin, int nthreads)
+    const int32_t* F, int64_t nF, const int32_t* F2E, double dhat, double dmin, int area_weighting, int nthreads)
 {
     Collisions* C = new Collisions();
+    std::vector<double> va, ea;
+    if (area_weighting) {
+        va.resize(nV);
+        ea.resize(nE);
+        mesh_areas(Vrest, nV, E, nE, F, nF, F2E, va.data(), ea.data());
+    }
+    const double* pva = area_weighting ? va.data() : nullptr;
+    const double* pea = area_weighting ? ea.data() : nullptr;
     std::vector<Box> vb;
     vertex_boxes_static(V, nV, 0.5 * (dhat + dmin), vb);
     Candidates cand;
@@ -1953,15 +2031,19 @@ void* orc_collisions_build(const double* V, const double* Vrest, int64_t nV, con
     std::vector<Raw> raw(nt);
     const int64_t nee = cand.ee.size() / 2, nfv = cand.fv.size() / 2;
     parallel_for(nee, nt, [&](int64_t b, int64_t e, int t) {
-        for (int64_t i = b; i < e; ++i) add_edge_edge(raw[t], V, Vrest, E, cand.ee[2 * i], cand.ee[2 * i + 1], offset_sqr);
+        for (int64_t i = b; i < e; ++i) add_edge_edge(raw[t], V, Vrest, E, cand.ee[2 * i], cand.ee[2 * i + 1], offset_sqr, pea);
     });
     parallel_for(nfv, nt, [&](int64_t b, int64_t e, int t) {
-        for (int64_t i = b; i < e; ++i) add_face_vertex(raw[t], V, F, F2E, cand.fv[2 * i], cand.fv[2 * i + 1], offset_sqr);
+        for (int64_t i = b; i < e; ++i) add_face_vertex(raw[t], V, F, F2E, cand.fv[2 * i], cand.fv[2 * i + 1], offset_sqr, pva);
     });
     Raw all;
     for (auto& r : raw) {
         all.vv.insert(all.vv.end(), r.vv.begin(), r.vv.end());
+        all.vv_w.insert(all.vv_w.end(), r.vv_w.begin(), r.vv_w.end());
         all.ev.insert(all.ev.end(), r.ev.begin(), r.ev.end());
+        all.ev_w.insert(all.ev_w.end(), r.ev_w.begin(), r.ev_w.end());
+        all.ee_w.insert(all.ee_w.end(), r.ee_w.begin(), r.ee_w.end());
+        all.fv_w.insert(all.fv_w.end(), r.fv_w.begin(), r.fv_w.end());
         all.ee.insert(all.ee.end(), r.ee.begin(), r.ee.end());
         all.ee_eps.insert(all.ee_eps.end(), r.ee_eps.begin(), r.ee_eps.end());
         all.ee_dt.insert(all.ee_dt.end(), r.ee_dt.begin(), r.ee_dt.end());

@@ -507,3 +507,56 @@ def test_psd_solvers_agree(oracle_mod):
                 assert np.linalg.norm(A - B) <= 1e-12 * np.linalg.norm(B)
     finally:
         oracle_mod.set_psd_solver("ql")
+
+
+# --- area weighting ---------------------------------------------------------------
+
+def test_mesh_areas_hand_checked(oracle_mod):
+    """collision_mesh.cpp:309-374 on small meshes: one triangle, a codim
+    polyline with an isolated vertex."""
+    V = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0]])
+    E = np.array([[0, 1], [1, 2], [2, 0]])
+    F = np.array([[0, 1, 2]])
+    va, ea = oracle_mod.mesh_areas(V, E, F)
+    np.testing.assert_array_equal(va, np.full(3, 0.5 / 3.0))
+    np.testing.assert_array_equal(ea, np.full(3, 0.5 / 3.0))
+    # edges only: vertex = half its incident edge lengths; edge = its length;
+    # an isolated vertex = 1
+    V = np.array([[0.0, 0, 0], [2, 0, 0], [2, 3, 0], [9, 9, 9]])
+    E = np.array([[0, 1], [1, 2]])
+    va, ea = oracle_mod.mesh_areas(V, E, np.zeros((0, 3), np.int32))
+    np.testing.assert_array_equal(va, [1.0, 2.5, 1.5, 1.0])
+    np.testing.assert_array_equal(ea, [2.0, 3.0])
+
+
+def test_mesh_areas_partition_the_surface(oracle_mod):
+    """Vertex areas and edge areas each sum to the total surface area."""
+    from ipctk_gb300 import scenes
+    sc = scenes.sphere_pack(n_side=2, subdiv=2, seed=1)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    va, ea = oracle_mod.mesh_areas(V, E, F)
+    a = 0.5 * np.linalg.norm(np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]]), axis=1).sum()
+    assert va.sum() == pytest.approx(a, rel=1e-12)
+    assert ea.sum() == pytest.approx(a, rel=1e-12)
+
+
+def test_area_weighted_collision_set(oracle_mod):
+    """Same contacts as without weighting; FV weight vertex_area/4, EE weight
+    (edge_area(ea)+edge_area(eb))/4 (normal_collisions_builder.cpp:146,181-183);
+    merged VV/EV weights sum their contributions."""
+    from ipctk_gb300 import scenes
+    sc = scenes.two_sheet(side=12, seed=4)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    plain = oracle_mod.build_collisions(V, E, F, sc["dhat"])
+    aw = oracle_mod.build_collisions(V, E, F, sc["dhat"], area_weighting=True)
+    for k in ("vv", "ev", "ee", "fv"):
+        np.testing.assert_array_equal(getattr(plain, k), getattr(aw, k))
+    va, ea = oracle_mod.mesh_areas(V, E, F)
+    np.testing.assert_array_equal(aw.fv_w, 0.25 * va[aw.fv[:, 1]])
+    np.testing.assert_array_equal(aw.ee_w, 0.25 * (ea[aw.ee[:, 0]] + ea[aw.ee[:, 1]]))
+    # every VV/EV contribution is a positive area over 4, at most
+    # multiplicity * (largest contribution)
+    assert np.all(aw.vv_w > 0) and np.all(aw.ev_w > 0)
+    big = 0.25 * max(va.max(), 2 * ea.max())
+    assert np.all(aw.vv_w <= plain.vv_w * big * (1 + 1e-15))
+    assert np.all(aw.ev_w <= plain.ev_w * big * (1 + 1e-15))
