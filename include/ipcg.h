@@ -150,6 +150,19 @@ int ipcg_collisions_destroy(ipcg_collisions* collisions);
 int ipcg_collisions_set_use_area_weighting(ipcg_collisions* collisions, int use_area_weighting);
 int ipcg_collisions_use_area_weighting(const ipcg_collisions* collisions, int* use_area_weighting);
 
+/* NormalCollisions::set_collision_set_type / collision_set_type
+ * (normal_collisions.cpp:177-192); applies to the next build.
+ * IMPROVED_MAX_APPROX (normal_collisions.cpp:84-128,
+ * normal_collisions_builder.cpp:340-543) adds negative edge-vertex and
+ * edge-edge terms and positive vertex-vertex terms so that a contact near a
+ * shared edge or vertex is counted once; merged weights that cancel to zero
+ * are dropped.  Equal edge-edge records (unordered pair and type) merge into
+ * the orientation with ea < eb when one exists.  OGC is not provided. */
+#define IPCG_COLLISION_SET_IPC 0
+#define IPCG_COLLISION_SET_IMPROVED_MAX_APPROX 1
+int ipcg_collisions_set_collision_set_type(ipcg_collisions* collisions, int type);
+int ipcg_collisions_collision_set_type(const ipcg_collisions* collisions, int* type);
+
 /* Replaces NormalCollisions::build(mesh, V, dhat, dmin, broad_phase=nullptr)
  * (src/ipc/collisions/normal/normal_collisions.hpp:45-50,
  *  normal_collisions.cpp:20-158): device LBVH broad phase, FP64 distance

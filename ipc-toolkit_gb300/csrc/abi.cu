@@ -451,6 +451,24 @@ int ipcg_collisions_use_area_weighting(const ipcg_collisions* c, int* on)
     });
 }
 
+int ipcg_collisions_set_collision_set_type(ipcg_collisions* c, int type)
+{
+    return guarded([&] {
+        require(c != nullptr, "NULL argument");
+        require(type == IPCG_COLLISION_SET_IPC || type == IPCG_COLLISION_SET_IMPROVED_MAX_APPROX,
+            "collision set type must be IPCG_COLLISION_SET_IPC or IPCG_COLLISION_SET_IMPROVED_MAX_APPROX");
+        c->set_type = type;
+    });
+}
+
+int ipcg_collisions_collision_set_type(const ipcg_collisions* c, int* type)
+{
+    return guarded([&] {
+        require(c && type, "NULL argument");
+        *type = c->set_type;
+    });
+}
+
 int ipcg_mesh_areas(const ipcg_mesh* m, double* vertex_areas, double* edge_areas)
 {
     return guarded([&] {

@@ -51,6 +51,7 @@ struct Out {
     unsigned long long* ee; // EE keys (ea,eb)
     int* ee_rec;            // EE record slot -> candidate id
     double* ee_eps;
+    double* ee_w;           // EE record weights (improved max approximation; else null)
     int8_t* ee_dt;
     unsigned long long* fv; // FV keys (f,v)
     int* count;             // [vv, ev, ee, fv]
@@ -115,6 +116,7 @@ __global__ void k_filter_ee(const int2* __restrict__ cand, int n, const double* 
         o.ee_rec[s] = s;
         o.ee_eps[s] = eps_x;
         o.ee_dt[s] = (int8_t)actual;
+        if (o.ee_w) o.ee_w[s] = w;
     }
     }
 }
@@ -223,7 +225,287 @@ __global__ void k_sum_runs(const unsigned long long* __restrict__ uniq, const in
     wout[i] = s;
 }
 
+// ---- CollisionSetType::IMPROVED_MAX_APPROX ----------------------------------
+// normal_collisions.cpp:84-128, normal_collisions_builder.cpp:340-543 and the
+// candidate conversions of candidates.cpp:583-692.  The conversions emit
+// keys that are sorted and made unique; the three term kernels then append
+// weighted VV / EV / EE records next to the ordinary ones.
+
+__device__ __forceinline__ double pe_distance(V3 p, V3 e0, V3 e1)
+{
+    return point_edge_distance(p, e0, e1, point_edge_distance_type(p, e0, e1));
+}
+
+// edge-edge candidate -> edge-vertex keys (edge, vertex of the other edge)
+__global__ void k_imp_ee_to_ev(const int2* __restrict__ cand, int n, const double* __restrict__ V,
+    const int* __restrict__ E, const double* __restrict__ off2, SceneView sv, unsigned long long* __restrict__ keys,
+    int* __restrict__ count)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 c = cand[i];
+    const double off = __ldg(off2 + sv.of(E[2 * c.x]));
+    for (int s = 0; s < 2; ++s) {
+        const int ei = s ? c.y : c.x, ej = s ? c.x : c.y;
+        const V3 x0 = load_v3(V, E[2 * ei]), x1 = load_v3(V, E[2 * ei + 1]);
+        for (int j = 0; j < 2; ++j) {
+            const int vj = E[2 * ej + j];
+            if (pe_distance(load_v3(V, vj), x0, x1) < off) keys[append(count)] = key2(ei, vj);
+        }
+    }
+}
+
+// face-vertex candidate -> edge-vertex keys (face edge, vertex) and
+// vertex-vertex keys (unordered: vertex, face vertex)
+__global__ void k_imp_fv_to_ev_vv(const int2* __restrict__ cand, int n, const double* __restrict__ V,
+    const int* __restrict__ E, const int* __restrict__ F, const int* __restrict__ F2E,
+    const double* __restrict__ off2, SceneView sv, unsigned long long* __restrict__ kev, int* __restrict__ nev,
+    unsigned long long* __restrict__ kvv, int* __restrict__ nvv)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int2 c = cand[i];
+    const int f = c.x, v = c.y;
+    const double off = __ldg(off2 + sv.of(v));
+    const V3 p = load_v3(V, v);
+    for (int j = 0; j < 3; ++j) {
+        const int ei = F2E[3 * f + j];
+        if (pe_distance(p, load_v3(V, E[2 * ei]), load_v3(V, E[2 * ei + 1])) < off) kev[append(nev)] = key2(ei, v);
+        const int vj = F[3 * f + j];
+        if (point_point_distance(p, load_v3(V, vj)) < off) kvv[append(nvv)] = key2(min(v, vj), max(v, vj));
+    }
+}
+
+// An edge-vertex term reduced by its point-edge type
+// (normal_collisions_builder.cpp:108-126).
+__device__ __forceinline__ void put_typed(const Out& o, const int* __restrict__ E, int e, int v, int pe, double w)
+{
+    if (pe == P_E0) put_vv(o, v, E[2 * e], w);
+    else if (pe == P_E1) put_vv(o, v, E[2 * e + 1], w);
+    else put_ev(o, e, v, w);
+}
+
+__device__ __forceinline__ bool sorted_contains(const int* __restrict__ a, int lo, int hi, int x)
+{
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const int y = a[mid];
+        if (y == x) return true;
+        if (y < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return false;
+}
+
+// add_edge_edge_negative_edge_vertex_collision (builder.cpp:457-541):
+// (ea, p) with p on edges eb of p's star; mollified pairs become EE terms of
+// weight -w_ea, the rest are counted and leave one EV term of (count-1) w.
+__global__ void k_imp_ee_negative(const unsigned long long* __restrict__ l1, int n, const double* __restrict__ V,
+    const double* __restrict__ rest, const int* __restrict__ E, const int* __restrict__ ve_off,
+    const int* __restrict__ ve_adj, Out o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = l1[i];
+    const int e = (int)(k >> 32), p = (int)(k & 0xffffffffu);
+    const int a0 = E[2 * e], a1 = E[2 * e + 1];
+    const double w = o.earea ? -0.25 * __ldg(o.earea + e) : -1.0;
+    const V3 xp = load_v3(V, p), xa0 = load_v3(V, a0), xa1 = load_v3(V, a1);
+    const int pe = point_edge_distance_type(xp, xa0, xa1);
+    int nonmollified = 0;
+    for (int j = ve_off[p], je = ve_off[p + 1]; j < je; ++j) {
+        const int eb = ve_adj[j];
+        const int b0 = E[2 * eb], b1 = E[2 * eb + 1];
+        const int q = p == b0 ? b1 : b0;
+        if (q == a0 || q == a1) continue;
+        const double eps_x = ee_mollifier_threshold(load_v3(rest, a0), load_v3(rest, a1), load_v3(rest, b0),
+            load_v3(rest, b1));
+        const double cr = ee_cross_sqnorm(xa0, xa1, load_v3(V, b0), load_v3(V, b1));
+        if (cr >= eps_x) {
+            ++nonmollified;
+            continue;
+        }
+        const bool first = p == b0;
+        const int dt = pe == P_E0 ? (first ? EA0_EB0 : EA0_EB1)
+                                  : (pe == P_E1 ? (first ? EA1_EB0 : EA1_EB1) : (first ? EA_EB0 : EA_EB1));
+        const int s = append(o.count + 2);
+        o.ee[s] = key2(e, eb);
+        o.ee_rec[s] = s;
+        o.ee_eps[s] = eps_x;
+        o.ee_dt[s] = (int8_t)dt;
+        o.ee_w[s] = w;
+    }
+    if (nonmollified == 1) return;
+    put_typed(o, E, e, p, pe, (nonmollified - 1) * w);
+}
+
+// add_face_vertex_negative_edge_vertex_collision (builder.cpp:421-455)
+__global__ void k_imp_fv_negative(const unsigned long long* __restrict__ l2, int n, const double* __restrict__ V,
+    const int* __restrict__ E, const int* __restrict__ ev_off, const int* __restrict__ ev_adj, Out o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = l2[i];
+    const int e = (int)(k >> 32), v = (int)(k & 0xffffffffu);
+    const int lo = ev_off[e], hi = ev_off[e + 1];
+    const int amt = (hi - lo) - (sorted_contains(ev_adj, lo, hi, v) ? 1 : 0);
+    if (amt <= 1) return;
+    const double w = (1 - amt) * (o.varea ? 0.25 * __ldg(o.varea + v) : 1.0);
+    const int pe = point_edge_distance_type(load_v3(V, v), load_v3(V, E[2 * e]), load_v3(V, E[2 * e + 1]));
+    put_typed(o, E, e, v, pe, w);
+}
+
+// add_face_vertex_positive_vertex_vertex_collision (builder.cpp:382-419)
+__global__ void k_imp_fv_positive(const unsigned long long* __restrict__ l3, int n, const int* __restrict__ vv_off,
+    const int* __restrict__ vv_adj, const uint8_t* __restrict__ boundary, Out o)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = l3[i];
+    const int a = (int)(k >> 32), b = (int)(k & 0xffffffffu);
+    double w = 0;
+    const int vi[2] = { a, b }, vj[2] = { b, a };
+    for (int t = 0; t < 2; ++t) {
+        if (boundary[vj[t]] || sorted_contains(vv_adj, vv_off[vj[t]], vv_off[vj[t] + 1], vi[t])) continue;
+        w += o.varea ? 0.25 * __ldg(o.varea + vi[t]) : 1.0;
+    }
+    if (w != 0) put_vv(o, a, b, w);
+}
+
+// EE merge of the improved set: records are equal when their edges match as
+// an unordered pair and their types match (normal/edge_edge.cpp:123-142).
+// Composite key (min, max, type); weights summed in ascending order; the
+// merged record keeps the orientation and eps_x of a record with ea < eb
+// when there is one.
+__global__ void k_ee_group_keys(const unsigned long long* __restrict__ pair, const int8_t* __restrict__ dt,
+    const double* __restrict__ w, int n, int bits, unsigned long long* __restrict__ ck, unsigned long long* __restrict__ wk,
+    int* __restrict__ idx)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = pair[i];
+    const unsigned a = (unsigned)(k >> 32), b = (unsigned)(k & 0xffffffffu);
+    const unsigned long long lo = min(a, b), hi = max(a, b);
+    ck[i] = (((lo << bits) | hi) << 4) | (unsigned long long)(uint8_t)dt[i];
+    wk[i] = weight_key(w[i]);
+    idx[i] = i;
+}
+__global__ void k_ee_group_runs(const int* __restrict__ counts, const int* __restrict__ offs,
+    const int* __restrict__ d_num, const int* __restrict__ idx, const unsigned long long* __restrict__ pair,
+    const double* __restrict__ eps, const int8_t* __restrict__ dt, const double* __restrict__ w,
+    int2* __restrict__ ids_out, double* __restrict__ eps_out, int8_t* __restrict__ dt_out, double* __restrict__ w_out,
+    int* __restrict__ keep)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *d_num) return;
+    int rep = idx[offs[i]];
+    bool rep_sorted = (pair[rep] >> 32) < (pair[rep] & 0xffffffffu);
+    double sum = 0.0;
+    for (int j = offs[i], e = offs[i] + counts[i]; j < e; ++j) {
+        const int q = idx[j];
+        sum += w[q];
+        if (!rep_sorted && (pair[q] >> 32) < (pair[q] & 0xffffffffu)) {
+            rep = q;
+            rep_sorted = true;
+        }
+    }
+    const unsigned long long k = pair[rep];
+    ids_out[i] = make_int2((int)(k >> 32), (int)(k & 0xffffffffu));
+    eps_out[i] = eps[rep];
+    dt_out[i] = dt[rep];
+    w_out[i] = sum;
+    keep[i] = sum != 0 ? 1 : 0;
+}
+
+// Zero-weight removal (builder.cpp:666-688): keep[i] -> compacted slot offs[i].
+__global__ void k_flag_nonzero(const double* __restrict__ w, const int* __restrict__ d_num, int* __restrict__ keep)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *d_num) return;
+    keep[i] = w[i] != 0 ? 1 : 0;
+}
+__global__ void k_compact(const int* __restrict__ d_num, const int* __restrict__ keep, const int* __restrict__ offs,
+    const int2* __restrict__ ids, const double* __restrict__ w, const double* __restrict__ eps,
+    const int8_t* __restrict__ dt, int2* __restrict__ ids_out, double* __restrict__ w_out, double* __restrict__ eps_out,
+    int8_t* __restrict__ dt_out, int* __restrict__ n_out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = *d_num;
+    if (i == 0) *n_out = n > 0 ? offs[n - 1] + keep[n - 1] : 0;
+    if (i >= n || !keep[i]) return;
+    const int o = offs[i];
+    ids_out[o] = ids[i];
+    w_out[o] = w[i];
+    if (eps) eps_out[o] = eps[i];
+    if (dt) dt_out[o] = dt[i];
+}
+
 } // namespace
+
+// The improved set's EE group key packs (min edge, max edge, type) in 64 bits.
+static void require_ee_bits(const ipcg_mesh* m)
+{
+    if (2 * bits_for(std::max(m->nE, (int64_t)2)) + 4 > 64)
+        throw Error(IPCG_ERR_INVALID, "IMPROVED_MAX_APPROX supports at most 2^30 edges");
+}
+
+// CollisionMesh::init_adjacencies (collision_mesh.cpp:247-291) on the host,
+// uploaded as CSR lists; built the first time a build needs them.
+static void ensure_adjacency(ipcg_mesh* m)
+{
+    if (m->adj_ready) return;
+    const int64_t nV = m->nV, nE = m->nE, nF = m->nF;
+    std::vector<int32_t> E(2 * nE), F(3 * nF);
+    if (nE) IPCG_CUDA(cudaMemcpy(E.data(), m->E.p, sizeof(int32_t) * 2 * nE, cudaMemcpyDeviceToHost));
+    if (nF) IPCG_CUDA(cudaMemcpy(F.data(), m->F.p, sizeof(int32_t) * 3 * nF, cudaMemcpyDeviceToHost));
+    auto csr = [](std::vector<std::pair<int32_t, int32_t>>& pairs, int64_t rows, std::vector<int32_t>& off,
+                   std::vector<int32_t>& adj) {
+        std::sort(pairs.begin(), pairs.end());
+        pairs.erase(std::unique(pairs.begin(), pairs.end()), pairs.end());
+        off.assign(rows + 1, 0);
+        adj.resize(pairs.size());
+        for (size_t i = 0; i < pairs.size(); ++i) {
+            ++off[pairs[i].first + 1];
+            adj[i] = pairs[i].second;
+        }
+        for (int64_t r = 0; r < rows; ++r) off[r + 1] += off[r];
+    };
+    std::vector<std::pair<int32_t, int32_t>> vv, ve, ev;
+    vv.reserve(2 * nE);
+    ve.reserve(2 * nE);
+    ev.reserve(3 * nF);
+    for (int64_t e = 0; e < nE; ++e) {
+        vv.emplace_back(E[2 * e], E[2 * e + 1]);
+        vv.emplace_back(E[2 * e + 1], E[2 * e]);
+        ve.emplace_back(E[2 * e], (int32_t)e);
+        ve.emplace_back(E[2 * e + 1], (int32_t)e);
+    }
+    for (int64_t f = 0; f < nF; ++f)
+        for (int j = 0; j < 3; ++j) ev.emplace_back(m->h_F2E[3 * f + j], F[3 * f + (j + 2) % 3]);
+    std::vector<int32_t> vv_off, vv_adj, ve_off, ve_adj, ev_off, ev_adj;
+    csr(vv, nV, vv_off, vv_adj);
+    csr(ve, nV, ve_off, ve_adj);
+    csr(ev, nE, ev_off, ev_adj);
+    std::vector<uint8_t> boundary(nV, 1);
+    for (int64_t e = 0; e < nE; ++e)
+        if (ev_off[e + 1] - ev_off[e] >= 2) boundary[E[2 * e]] = boundary[E[2 * e + 1]] = 0;
+    int maxdeg = 0;
+    for (int64_t v = 0; v < nV; ++v) maxdeg = std::max(maxdeg, ve_off[v + 1] - ve_off[v]);
+    auto up = [&](auto& buf, const auto& host) {
+        buf.reserve(host.size() + 1);
+        if (!host.empty())
+            IPCG_CUDA(cudaMemcpy(buf.p, host.data(), sizeof(host[0]) * host.size(), cudaMemcpyHostToDevice));
+    };
+    up(m->vv_off, vv_off);
+    up(m->vv_adj, vv_adj);
+    up(m->ve_off, ve_off);
+    up(m->ve_adj, ve_adj);
+    up(m->ev_off, ev_off);
+    up(m->ev_adj, ev_adj);
+    up(m->boundary, boundary);
+    m->max_vertex_edges = maxdeg;
+    m->adj_ready = true;
+}
 
 void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, const double* dhat, const double* dmin)
 {
@@ -248,8 +530,50 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     c->scene_dmin.assign(dmin, dmin + ns);
     c->sorted = true;
     const int64_t nc = n_ee + n_fv;
-    // raw records: at most one per candidate
-    const int64_t cap = nc + 16;
+    const bool improved = c->set_type == 1;
+    // improved max approximation: candidate conversions (sorted, unique keys)
+    int64_t nl1 = 0, nl2 = 0, nl3 = 0;
+    unsigned long long *l1 = nullptr, *l2 = nullptr, *l3 = nullptr;
+    if (improved) {
+        require_ee_bits(m);
+        ensure_adjacency(m);
+        const int64_t r1 = 4 * n_ee, r23 = 3 * n_fv, tot = r1 + 2 * r23 + 16;
+        m->imp_keys.reserve(2 * tot);
+        unsigned long long* raw = m->imp_keys.p;
+        unsigned long long* srt = m->imp_keys.p + tot;
+        l1 = raw;
+        l2 = raw + r1;
+        l3 = raw + r1 + r23;
+        m->counters.reserve(32);
+        int* kc = m->counters.p + 20;
+        IPCG_CUDA(cudaMemsetAsync(kc, 0, sizeof(int) * 8, s));
+        const SceneView sv0 = scene_view(m);
+        if (n_ee)
+            IPCG_LAUNCH("k_imp_ee_to_ev", s, k_imp_ee_to_ev<<<grid_for(n_ee, BLOCK), BLOCK, 0, s>>>(m->cand.p,
+                (int)n_ee, V, m->E.p, m->scene_off2.p, sv0, l1, kc + 0));
+        if (n_fv)
+            IPCG_LAUNCH("k_imp_fv_to_ev_vv", s, k_imp_fv_to_ev_vv<<<grid_for(n_fv, BLOCK), BLOCK, 0, s>>>(
+                m->cand.p + m->cand_cap, (int)n_fv, V, m->E.p, m->F.p, m->F2E.p, m->scene_off2.p, sv0, l2, kc + 1,
+                l3, kc + 2));
+        m->h_counters.reserve(32);
+        IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, kc, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        const int k1 = m->h_counters.p[0], k2 = m->h_counters.p[1], k3 = m->h_counters.p[2];
+        const int kbits = 32 + bits_for(std::max(std::max(m->nV, m->nE), (int64_t)2));
+        sort_keys_u64(m, s, l1, srt, k1, kbits);
+        unique_u64(m, s, srt, l1, kc + 3, k1);
+        sort_keys_u64(m, s, l2, srt + r1, k2, kbits);
+        unique_u64(m, s, srt + r1, l2, kc + 4, k2);
+        sort_keys_u64(m, s, l3, srt + r1 + r23, k3, kbits);
+        unique_u64(m, s, srt + r1 + r23, l3, kc + 5, k3);
+        IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, kc + 3, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        nl1 = k1 ? m->h_counters.p[0] : 0;
+        nl2 = k2 ? m->h_counters.p[1] : 0;
+        nl3 = k3 ? m->h_counters.p[2] : 0;
+    }
+    // raw records: at most one per candidate, plus the improved terms
+    const int64_t cap = nc + (improved ? nl1 * (m->max_vertex_edges + 1) + nl2 + nl3 : 0) + 16;
     m->keys_a.reserve(4 * cap);
     m->keys_b.reserve(4 * cap);
     m->ivals_a.reserve(2 * cap);
@@ -265,16 +589,22 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     o.ee_rec = m->ivals_a.p;
     o.ee_eps = m->partial.p;
     o.ee_dt = m->i8tmp.p;
-    const bool weighted = c->use_area_weighting != 0;
-    o.vv_w = o.ev_w = nullptr;
-    o.varea = weighted ? m->vertex_area.p : nullptr;
-    o.earea = weighted ? m->edge_area.p : nullptr;
+    const bool area = c->use_area_weighting != 0;
+    const bool weighted = area || improved; // VV / EV records carry weights
+    o.vv_w = o.ev_w = o.ee_w = nullptr;
+    o.varea = area ? m->vertex_area.p : nullptr;
+    o.earea = area ? m->edge_area.p : nullptr;
     if (weighted) {
         m->rec_w.reserve(2 * cap);
         o.vv_w = m->rec_w.p;
         o.ev_w = m->rec_w.p + cap;
     }
-    m->counters.reserve(16);
+    if (improved) {
+        m->rec_ee_w.reserve(cap);
+        o.ee_w = m->rec_ee_w.p;
+    }
+    m->counters.reserve(32);
+    m->h_counters.reserve(32);
     o.count = m->counters.p + 4;
     IPCG_CUDA(cudaMemsetAsync(o.count, 0, sizeof(int) * 8, s));
     const SceneView sv = scene_view(m);
@@ -284,6 +614,17 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     if (n_fv)
         IPCG_LAUNCH("k_filter_fv", s, k_filter_fv<<<grid_for(n_fv, BLOCK), BLOCK, 0, s>>>(m->cand.p + m->cand_cap,
             (int)n_fv, V, m->F.p, m->F2E.p, m->scene_off2.p, sv, o));
+    if (improved) {
+        if (nl1)
+            IPCG_LAUNCH("k_imp_ee_negative", s, k_imp_ee_negative<<<grid_for(nl1, BLOCK), BLOCK, 0, s>>>(l1, (int)nl1,
+                V, m->rest.p, m->E.p, m->ve_off.p, m->ve_adj.p, o));
+        if (nl2)
+            IPCG_LAUNCH("k_imp_fv_negative", s, k_imp_fv_negative<<<grid_for(nl2, BLOCK), BLOCK, 0, s>>>(l2, (int)nl2,
+                V, m->E.p, m->ev_off.p, m->ev_adj.p, o));
+        if (nl3)
+            IPCG_LAUNCH("k_imp_fv_positive", s, k_imp_fv_positive<<<grid_for(nl3, BLOCK), BLOCK, 0, s>>>(l3,
+                (int)nl3, m->vv_off.p, m->vv_adj.p, m->boundary.p, o));
+    }
     IPCG_CHECK_LAUNCH();
     IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, o.count, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
     IPCG_CUDA(cudaStreamSynchronize(s));
@@ -327,15 +668,75 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
             IPCG_LAUNCH("k_sum_runs", s, k_sum_runs<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(raw, cnt, i0, num, i2, w,
                 ids, wout));
         };
-        merge(o.vv, o.vv_w, rvv, ks, counts, d_num + 0, c->vv.p, c->vv_w.p);
-        merge(o.ev, o.ev_w, rev, ks + cap, counts + cap, d_num + 1, c->ev.p, c->ev_w.p);
+        if (!improved) {
+            merge(o.vv, o.vv_w, rvv, ks, counts, d_num + 0, c->vv.p, c->vv_w.p);
+            merge(o.ev, o.ev_w, rev, ks + cap, counts + cap, d_num + 1, c->ev.p, c->ev_w.p);
+        } else {
+            // sums that cancel to zero are dropped (builder.cpp:666-688)
+            m->imp_ids.reserve(cap);
+            m->imp_w.reserve(cap);
+            m->imp_flag.reserve(cap);
+            m->imp_offs.reserve(cap);
+            auto merge_drop = [&](unsigned long long* raw, const double* w, int n, unsigned long long* sorted,
+                                  int* cnt, int* num, int2* ids, double* wout, int* n_out) {
+                merge(raw, w, n, sorted, cnt, num, m->imp_ids.p, m->imp_w.p);
+                if (n == 0) {
+                    IPCG_CUDA(cudaMemsetAsync(n_out, 0, sizeof(int), s));
+                    return;
+                }
+                IPCG_CUDA(cudaMemsetAsync(m->imp_flag.p, 0, sizeof(int) * n, s));
+                IPCG_LAUNCH("k_flag_nonzero", s, k_flag_nonzero<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(m->imp_w.p, num,
+                    m->imp_flag.p));
+                exclusive_sum_i32(m, m->stream, m->imp_flag.p, m->imp_offs.p, n);
+                IPCG_LAUNCH("k_compact", s, k_compact<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(num, m->imp_flag.p,
+                    m->imp_offs.p, m->imp_ids.p, m->imp_w.p, nullptr, nullptr, ids, wout, nullptr, nullptr, n_out));
+            };
+            // compacted counts go to their own slots: k_compact reads the run
+            // count while it writes the kept count
+            merge_drop(o.vv, o.vv_w, rvv, ks, counts, d_num + 0, c->vv.p, c->vv_w.p, d_num + 4);
+            merge_drop(o.ev, o.ev_w, rev, ks + cap, counts + cap, d_num + 1, c->ev.p, c->ev_w.p, d_num + 5);
+        }
     }
     // EE: sort keys with record ids, gather eps / dtype
     c->ee.reserve(ree + 1);
     c->ee_w.reserve(ree + 1);
     c->ee_eps.reserve(ree + 1);
     c->ee_dtype.reserve(ree + 1);
-    if (ree) {
+    int nee_out = ree;
+    if (ree && improved) {
+        // group equal (unordered pair, type) records, sum their weights in
+        // ascending order, drop zero sums
+        const int ebits = bits_for(std::max(m->nE, (int64_t)2));
+        m->wkeys.reserve(2 * cap);
+        unsigned long long* ck = m->wkeys.p;
+        unsigned long long* wk = m->wkeys.p + cap;
+        m->widx.reserve(3 * cap);
+        int *i0 = m->widx.p, *i1 = m->widx.p + cap, *i2 = m->widx.p + 2 * cap;
+        unsigned long long* sorted = ks + 2 * cap;
+        IPCG_LAUNCH("k_ee_group_keys", s, k_ee_group_keys<<<grid_for(ree, BLOCK), BLOCK, 0, s>>>(o.ee, o.ee_dt,
+            o.ee_w, ree, ebits, ck, wk, i0));
+        sort_pairs_u64(m, m->stream, wk, sorted, i0, i1, ree, 64);
+        IPCG_LAUNCH("k_gather_keys", s, k_gather_keys<<<grid_for(ree, BLOCK), BLOCK, 0, s>>>(ck, i1, ree, wk));
+        sort_pairs_u64(m, m->stream, wk, sorted, i1, i2, ree, 2 * ebits + 4);
+        int* ecnt = m->ivals_b.p + 2 * cap;
+        IPCG_CUDA(cudaMemsetAsync(ecnt, 0, sizeof(int) * ree, s));
+        rle_u64(m, m->stream, sorted, ck, ecnt, d_num + 2, ree);
+        exclusive_sum_i32(m, m->stream, ecnt, i0, ree);
+        m->imp_ids.reserve(cap);
+        m->imp_w.reserve(cap);
+        m->imp_eps.reserve(cap);
+        m->imp_dt.reserve(cap);
+        m->imp_flag.reserve(cap);
+        m->imp_offs.reserve(cap);
+        IPCG_CUDA(cudaMemsetAsync(m->imp_flag.p, 0, sizeof(int) * ree, s));
+        IPCG_LAUNCH("k_ee_group_runs", s, k_ee_group_runs<<<grid_for(ree, BLOCK), BLOCK, 0, s>>>(ecnt, i0, d_num + 2,
+            i2, o.ee, o.ee_eps, o.ee_dt, o.ee_w, m->imp_ids.p, m->imp_eps.p, m->imp_dt.p, m->imp_w.p, m->imp_flag.p));
+        exclusive_sum_i32(m, m->stream, m->imp_flag.p, m->imp_offs.p, ree);
+        IPCG_LAUNCH("k_compact", s, k_compact<<<grid_for(ree, BLOCK), BLOCK, 0, s>>>(d_num + 2, m->imp_flag.p,
+            m->imp_offs.p, m->imp_ids.p, m->imp_w.p, m->imp_eps.p, m->imp_dt.p, c->ee.p, c->ee_w.p, c->ee_eps.p,
+            c->ee_dtype.p, d_num + 3));
+        nee_out = -1; // read back below
+    } else if (ree) {
         sort_pairs_u64(m, m->stream, o.ee, ks + 2 * cap, o.ee_rec, m->ivals_b.p + 2 * cap, ree, idbits);
         IPCG_LAUNCH("k_gather_ee", s, k_gather_ee<<<grid_for(ree, BLOCK), BLOCK, 0, s>>>(ks + 2 * cap, m->ivals_b.p + 2 * cap, ree, o.ee_eps, o.ee_dt,
             c->ee.p, c->ee_eps.p, c->ee_dtype.p, c->ee_w.p, o.earea));
@@ -349,11 +750,11 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
             o.varea));
     }
     IPCG_CHECK_LAUNCH();
-    IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_num, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_num, sizeof(int) * 6, cudaMemcpyDeviceToHost, s));
     IPCG_CUDA(cudaStreamSynchronize(s));
-    c->nvv = m->h_counters.p[0];
-    c->nev = m->h_counters.p[1];
-    c->nee = ree;
+    c->nvv = improved ? m->h_counters.p[4] : m->h_counters.p[0];
+    c->nev = improved ? m->h_counters.p[5] : m->h_counters.p[1];
+    c->nee = nee_out >= 0 ? nee_out : m->h_counters.p[3];
     c->nfv = rfv;
 }
 

@@ -180,6 +180,18 @@ struct ipcg_mesh {
     ipcg::DBuf<double> rec_w;        // area weighting: VV / EV record weights
     ipcg::DBuf<unsigned long long> wkeys; // weighted merge scratch
     ipcg::DBuf<int> widx;
+    // adjacencies of CollisionMesh::init_adjacencies (built on first use):
+    // CSR offsets + sorted lists; boundary flags per vertex
+    bool adj_ready = false;
+    int max_vertex_edges = 0;
+    ipcg::DBuf<int> vv_off, vv_adj, ve_off, ve_adj, ev_off, ev_adj;
+    ipcg::DBuf<uint8_t> boundary;
+    // improved-max-approximation scratch
+    ipcg::DBuf<unsigned long long> imp_keys;
+    ipcg::DBuf<int2> imp_ids;
+    ipcg::DBuf<double> imp_w, imp_eps, rec_ee_w;
+    ipcg::DBuf<int8_t> imp_dt;
+    ipcg::DBuf<int> imp_flag, imp_offs;
     ipcg::DBuf<double> vertex_area;  // rest-mesh areas (area weighting)
     ipcg::DBuf<double> edge_area;
     // work space shared by the calls on this mesh
@@ -210,6 +222,7 @@ struct ipcg_collisions {
     std::vector<double> scene_dmin;  // per scene (batches)
     bool sorted = false;             // lists sorted by key (built here, not loaded)
     int use_area_weighting = 0;      // NormalCollisions::use_area_weighting()
+    int set_type = 0;                // CollisionSetType: 0 IPC, 1 IMPROVED_MAX_APPROX
     ipcg::DBuf<int2> vv, ev, ee, fv;
     ipcg::DBuf<double> vv_w, ev_w, ee_w, fv_w, ee_eps;
     ipcg::DBuf<int8_t> ee_dtype;

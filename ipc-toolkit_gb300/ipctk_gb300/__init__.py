@@ -91,6 +91,8 @@ def _load():
         "ipcg_mesh_areas": (i32, [P, P, P]),
         "ipcg_collisions_set_use_area_weighting": (i32, [P, i32]),
         "ipcg_collisions_use_area_weighting": (i32, [P, P]),
+        "ipcg_collisions_set_collision_set_type": (i32, [P, i32]),
+        "ipcg_collisions_collision_set_type": (i32, [P, P]),
         "ipcg_candidates_create": (i32, [PP]),
         "ipcg_candidates_destroy": (i32, [P]),
         "ipcg_candidates_build": (i32, [P, P, P, d]),
@@ -413,6 +415,23 @@ class NormalCollisions:
     @use_area_weighting.setter
     def use_area_weighting(self, on: bool):
         _check(_load().ipcg_collisions_set_use_area_weighting(self._h, int(bool(on))))
+
+    class CollisionSetType(enum.IntEnum):
+        """NormalCollisions::CollisionSetType (normal_collisions.hpp); OGC is
+        not provided."""
+        IPC = 0
+        IMPROVED_MAX_APPROX = 1
+        OGC = 2
+
+    @property
+    def collision_set_type(self):
+        v = C.c_int()
+        _check(_load().ipcg_collisions_collision_set_type(self._h, C.byref(v)))
+        return NormalCollisions.CollisionSetType(v.value)
+
+    @collision_set_type.setter
+    def collision_set_type(self, t):
+        _check(_load().ipcg_collisions_set_collision_set_type(self._h, int(t)))
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -41,6 +41,7 @@
 #include <thread>
 #include <unordered_map>
 #include <queue>
+#include <tuple>
 #include <vector>
 
 namespace orc {
@@ -730,6 +731,149 @@ static void add_edge_edge(Raw& r, const double* V, const double* Vrest, const in
     }
 }
 
+// Mesh adjacencies of CollisionMesh::init_adjacencies (collision_mesh.cpp:247-291):
+// sorted unique vertex->vertex and vertex->edge lists, edge->opposite-vertex
+// lists from the faces, and the boundary flag (a vertex is interior once an
+// incident edge has two or more opposite vertices).
+struct Adjacency {
+    std::vector<std::vector<int32_t>> vv, ve, ev;
+    std::vector<uint8_t> boundary;
+};
+static void build_adjacency(int64_t nV, const int32_t* E, int64_t nE, const int32_t* F, int64_t nF,
+    const int32_t* F2E, Adjacency& A)
+{
+    A.vv.assign(nV, {});
+    A.ve.assign(nV, {});
+    A.ev.assign(nE, {});
+    for (int64_t e = 0; e < nE; ++e) {
+        A.vv[E[2 * e]].push_back(E[2 * e + 1]);
+        A.vv[E[2 * e + 1]].push_back(E[2 * e]);
+        A.ve[E[2 * e]].push_back((int32_t)e);
+        A.ve[E[2 * e + 1]].push_back((int32_t)e);
+    }
+    for (int64_t f = 0; f < nF; ++f)
+        for (int j = 0; j < 3; ++j) A.ev[F2E[3 * f + j]].push_back(F[3 * f + (j + 2) % 3]);
+    auto uniq = [](std::vector<std::vector<int32_t>>& L) {
+        for (auto& l : L) {
+            std::sort(l.begin(), l.end());
+            l.erase(std::unique(l.begin(), l.end()), l.end());
+        }
+    };
+    uniq(A.vv);
+    uniq(A.ve);
+    uniq(A.ev);
+    A.boundary.assign(nV, 1);
+    for (int64_t e = 0; e < nE; ++e)
+        if (A.ev[e].size() >= 2) A.boundary[E[2 * e]] = A.boundary[E[2 * e + 1]] = 0;
+}
+
+// An edge-vertex record reduced by its point-edge type
+// (normal_collisions_builder.cpp:108-126): P_E0 / P_E1 -> VV with that
+// endpoint, P_E -> EV.
+static void add_ev_typed(Raw& r, const int32_t* E, int ei, int vi, int pe, double w)
+{
+    if (pe == P_E0) add_vv(r, vi, E[2 * ei], w);
+    else if (pe == P_E1) add_vv(r, vi, E[2 * ei + 1], w);
+    else add_ev(r, ei, vi, w);
+}
+
+// CollisionSetType::IMPROVED_MAX_APPROX (normal_collisions.cpp:84-128 with
+// normal_collisions_builder.cpp:340-543 and the candidate conversions of
+// candidates.cpp:583-692): edge-edge candidates give negative edge-vertex
+// terms, face-vertex candidates negative edge-vertex and positive
+// vertex-vertex terms, so that a contact near a shared edge or vertex is
+// counted once instead of once per incident element.
+static void improved_max_approx(Raw& r, const double* V, const double* Vrest, const int32_t* E, const int32_t* F,
+    const int32_t* F2E, const std::vector<int32_t>& cee, const std::vector<int32_t>& cfv, double offset_sqr,
+    const double* va, const double* ea, const Adjacency& A)
+{
+    auto active = [&](double d2) { return d2 < offset_sqr; };
+    auto pe_dist = [&](int v, int e) {
+        const V3 p = row(V, v), e0 = row(V, E[2 * e]), e1 = row(V, E[2 * e + 1]);
+        return point_edge_distance(p, e0, e1, point_edge_distance_type(p, e0, e1));
+    };
+    auto sorted_unique = [](std::vector<uint64_t>& k) {
+        std::sort(k.begin(), k.end());
+        k.erase(std::unique(k.begin(), k.end()), k.end());
+    };
+    // edge-edge -> edge-vertex (candidates.cpp:665-692)
+    std::vector<uint64_t> l1;
+    for (size_t c = 0; 2 * c < cee.size(); ++c)
+        for (int i = 0; i < 2; ++i) {
+            const int ei = cee[2 * c + i], ej = cee[2 * c + 1 - i];
+            for (int j = 0; j < 2; ++j) {
+                const int vj = E[2 * ej + j];
+                if (active(pe_dist(vj, ei))) l1.push_back(key2(ei, vj));
+            }
+        }
+    sorted_unique(l1);
+    // add_edge_edge_negative_edge_vertex_collision (builder.cpp:457-541)
+    for (uint64_t k : l1) {
+        const int e = (int)(k >> 32), p = (int)(k & 0xffffffffu);
+        const int a0 = E[2 * e], a1 = E[2 * e + 1];
+        const double w = ea ? -0.25 * ea[e] : -1.0;
+        const int pe = point_edge_distance_type(row(V, p), row(V, a0), row(V, a1));
+        int nonmollified = 0;
+        for (int eb : A.ve[p]) {
+            const int b0 = E[2 * eb], b1 = E[2 * eb + 1];
+            const int q = p == b0 ? b1 : b0;
+            if (q == a0 || q == a1) continue;
+            const double eps_x = ee_mollifier_threshold(row(Vrest, a0), row(Vrest, a1), row(Vrest, b0), row(Vrest, b1));
+            const double cr = ee_cross_sqnorm(row(V, a0), row(V, a1), row(V, b0), row(V, b1));
+            if (cr >= eps_x) {
+                ++nonmollified;
+                continue;
+            }
+            const bool first = p == b0;
+            const int dt = pe == P_E0 ? (first ? EA0_EB0 : EA0_EB1)
+                                      : (pe == P_E1 ? (first ? EA1_EB0 : EA1_EB1) : (first ? EA_EB0 : EA_EB1));
+            r.ee.push_back(e);
+            r.ee.push_back(eb);
+            r.ee_eps.push_back(eps_x);
+            r.ee_dt.push_back((int8_t)dt);
+            r.ee_w.push_back(w);
+        }
+        if (nonmollified == 1) continue;
+        add_ev_typed(r, E, e, p, pe, (nonmollified - 1) * w);
+    }
+    // face-vertex -> edge-vertex (candidates.cpp:640-663)
+    std::vector<uint64_t> l2, l3;
+    for (size_t c = 0; 2 * c < cfv.size(); ++c) {
+        const int f = cfv[2 * c], v = cfv[2 * c + 1];
+        for (int j = 0; j < 3; ++j) {
+            const int ei = F2E[3 * f + j];
+            if (active(pe_dist(v, ei))) l2.push_back(key2(ei, v));
+            // face-vertex -> vertex-vertex (candidates.cpp:583-611), unordered pairs
+            const int vj = F[3 * f + j];
+            if (active(point_point_distance(row(V, v), row(V, vj)))) l3.push_back(key2(std::min(v, vj), std::max(v, vj)));
+        }
+    }
+    sorted_unique(l2);
+    sorted_unique(l3);
+    // add_face_vertex_negative_edge_vertex_collision (builder.cpp:421-455)
+    for (uint64_t k : l2) {
+        const int e = (int)(k >> 32), v = (int)(k & 0xffffffffu);
+        const auto& inc = A.ev[e];
+        const int amt = (int)inc.size() - (std::binary_search(inc.begin(), inc.end(), v) ? 1 : 0);
+        if (amt <= 1) continue;
+        const double w = (1 - amt) * (va ? 0.25 * va[v] : 1.0);
+        add_ev_typed(r, E, e, v, point_edge_distance_type(row(V, v), row(V, E[2 * e]), row(V, E[2 * e + 1])), w);
+    }
+    // add_face_vertex_positive_vertex_vertex_collision (builder.cpp:382-419)
+    for (uint64_t k : l3) {
+        const int a = (int)(k >> 32), b = (int)(k & 0xffffffffu);
+        double w = 0;
+        auto add_w = [&](int vi, int vj) {
+            const auto& inc = A.vv[vj];
+            if (A.boundary[vj] || std::binary_search(inc.begin(), inc.end(), vi)) return;
+            w += va ? 0.25 * va[vi] : 1.0;
+        };
+        add_w(a, b);
+        add_w(b, a);
+        if (w != 0) add_vv(r, a, b, w);
+    }
+}
+
 static void finalize(Raw& all, Collisions& C)
 {
     // builder.cpp:547-689: duplicate VV / EV keys merge with summed weights.
@@ -749,31 +893,57 @@ static void finalize(Raw& all, Collisions& C)
             size_t j = i;
             double sum = 0.0;
             while (j < perm.size() && keys[perm[j]] == keys[perm[i]]) sum += win[perm[j++]];
-            ids.push_back((int32_t)(keys[perm[i]] >> 32));
-            ids.push_back((int32_t)(keys[perm[i]] & 0xffffffffu));
-            w.push_back(sum);
+            if (sum != 0) {
+                // weights that cancel to zero are dropped (builder.cpp:666-688)
+                ids.push_back((int32_t)(keys[perm[i]] >> 32));
+                ids.push_back((int32_t)(keys[perm[i]] & 0xffffffffu));
+                w.push_back(sum);
+            }
             i = j;
         }
     };
     merge(all.vv, all.vv_w, C.vv, C.vv_w);
     merge(all.ev, all.ev_w, C.ev, C.ev_w);
-    // EE: unique pairs by construction; sort by (ea, eb)
+    // EE: records are equal when their edges match as an unordered pair and
+    // their distance types match (normal/edge_edge.cpp:123-142); equal
+    // records sum their weights (ascending order) and zero sums are dropped.
+    // The merged record keeps the orientation and eps_x of a record with
+    // ea < eb when there is one (the candidate's own orientation); the
+    // reference keeps whichever came first.  Sorted by (min, max, type).
     const size_t nee = all.ee_eps.size();
+    auto ekey = [&](size_t i) {
+        const uint32_t a = all.ee[2 * i], b = all.ee[2 * i + 1];
+        return std::make_tuple(std::min(a, b), std::max(a, b), (int)all.ee_dt[i]);
+    };
     std::vector<size_t> perm(nee);
     std::iota(perm.begin(), perm.end(), 0);
     std::sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
-        return key2(all.ee[2 * a], all.ee[2 * a + 1]) < key2(all.ee[2 * b], all.ee[2 * b + 1]);
+        return ekey(a) != ekey(b) ? ekey(a) < ekey(b) : all.ee_w[a] < all.ee_w[b];
     });
-    C.ee.resize(2 * nee);
-    C.ee_eps.resize(nee);
-    C.ee_dtype.resize(nee);
-    C.ee_w.resize(nee);
-    for (size_t i = 0; i < nee; ++i) {
-        C.ee[2 * i] = all.ee[2 * perm[i]];
-        C.ee[2 * i + 1] = all.ee[2 * perm[i] + 1];
-        C.ee_eps[i] = all.ee_eps[perm[i]];
-        C.ee_dtype[i] = all.ee_dt[perm[i]];
-        C.ee_w[i] = all.ee_w[perm[i]];
+    C.ee.clear();
+    C.ee_eps.clear();
+    C.ee_dtype.clear();
+    C.ee_w.clear();
+    for (size_t i = 0; i < nee;) {
+        size_t j = i, rep = perm[i];
+        bool rep_sorted = all.ee[2 * rep] < all.ee[2 * rep + 1];
+        double sum = 0.0;
+        while (j < nee && ekey(perm[j]) == ekey(perm[i])) {
+            const size_t q = perm[j++];
+            sum += all.ee_w[q];
+            if (!rep_sorted && all.ee[2 * q] < all.ee[2 * q + 1]) {
+                rep = q;
+                rep_sorted = true;
+            }
+        }
+        if (sum != 0) {
+            C.ee.push_back(all.ee[2 * rep]);
+            C.ee.push_back(all.ee[2 * rep + 1]);
+            C.ee_eps.push_back(all.ee_eps[rep]);
+            C.ee_dtype.push_back(all.ee_dt[rep]);
+            C.ee_w.push_back(sum);
+        }
+        i = j;
     }
     const size_t nfv = all.fv.size() / 2;
     std::vector<size_t> fp(nfv);
@@ -2011,7 +2181,8 @@ void orc_mesh_areas(const double* Vrest, int64_t nV, const int32_t* E, int64_t n
 }
 
 void* orc_collisions_build(const double* V, const double* Vrest, int64_t nV, const int32_t* E, int64_t nE,
-    const int32_t* F, int64_t nF, const int32_t* F2E, double dhat, double dmin, int area_weighting, int nthreads)
+    const int32_t* F, int64_t nF, const int32_t* F2E, double dhat, double dmin, int area_weighting, int set_type,
+    int nthreads)
 {
     Collisions* C = new Collisions();
     std::vector<double> va, ea;
@@ -2048,6 +2219,11 @@ void* orc_collisions_build(const double* V, const double* Vrest, int64_t nV, con
         all.ee_eps.insert(all.ee_eps.end(), r.ee_eps.begin(), r.ee_eps.end());
         all.ee_dt.insert(all.ee_dt.end(), r.ee_dt.begin(), r.ee_dt.end());
         all.fv.insert(all.fv.end(), r.fv.begin(), r.fv.end());
+    }
+    if (set_type == 1) {
+        Adjacency A;
+        build_adjacency(nV, E, nE, F, nF, F2E, A);
+        improved_max_approx(all, V, Vrest, E, F, F2E, cand.ee, cand.fv, offset_sqr, pva, pea, A);
     }
     finalize(all, *C);
     C->n_cand_ee = nee;

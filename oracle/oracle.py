@@ -55,7 +55,7 @@ def lib():
         L.orc_faces_to_edges.restype = i32
         L.orc_faces_to_edges.argtypes = [P, i64, P, i64, P]
         L.orc_collisions_build.restype = vp
-        L.orc_collisions_build.argtypes = [P, P, i64, P, i64, P, i64, P, d, d, i32, i32]
+        L.orc_collisions_build.argtypes = [P, P, i64, P, i64, P, i64, P, d, d, i32, i32, i32]
         L.orc_mesh_areas.argtypes = [P, i64, P, i64, P, i64, P, P, P]
         L.orc_collisions_from_arrays.restype = vp
         L.orc_collisions_from_arrays.argtypes = [i64, P, P, i64, P, P, i64, P, P, P, P, i64, P, P]
@@ -221,13 +221,15 @@ def mesh_areas(rest, E, F):
     return va, ea
 
 
-def build_collisions(V, E, F, dhat, dmin=0.0, rest=None, nthreads=None, area_weighting=False):
+def build_collisions(V, E, F, dhat, dmin=0.0, rest=None, nthreads=None, area_weighting=False,
+                     improved_max_approx=False):
     V, E, F = _f64(V), _i32(E), _i32(F)
     rest = V if rest is None else _f64(rest)
     F2E = faces_to_edges(F, E)
     nt = nthreads or os.cpu_count() or 1
     h = lib().orc_collisions_build(_p(V), _p(rest), V.shape[0], _p(E), E.shape[0], _p(F), F.shape[0], _p(F2E),
-                                   float(dhat), float(dmin), int(bool(area_weighting)), int(nt))
+                                   float(dhat), float(dmin), int(bool(area_weighting)),
+                                   int(bool(improved_max_approx)), int(nt))
     return Collisions(h)
 
 

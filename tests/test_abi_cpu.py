@@ -104,3 +104,20 @@ def test_adaptive_stiffness_formulas(ipctk):
     assert ipctk.update_barrier_stiffness(0.5 * eps, 0.25 * eps, 10.0, 3.0, diag) == 6.0
     assert ipctk.update_barrier_stiffness(0.5 * eps, 0.25 * eps, 5.0, 3.0, diag) == 5.0
     assert ipctk.update_barrier_stiffness(0.25 * eps, 0.5 * eps, 10.0, 3.0, diag) == 3.0
+
+
+def test_collision_set_type_validation_without_gpu(ipctk):
+    """OGC is not provided and is rejected; the setters touch no device."""
+    L = C.CDLL(ipctk.LIB_PATH)
+    L.ipcg_last_error.restype = C.c_char_p
+    h = C.c_void_p()
+    assert L.ipcg_collisions_create(C.byref(h)) == 0
+    L.ipcg_collisions_set_collision_set_type.argtypes = [C.c_void_p, C.c_int]
+    L.ipcg_collisions_collision_set_type.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
+    assert L.ipcg_collisions_set_collision_set_type(h, 2) == 1
+    assert b"collision set type" in L.ipcg_last_error()
+    assert L.ipcg_collisions_set_collision_set_type(h, 1) == 0
+    t = C.c_int()
+    assert L.ipcg_collisions_collision_set_type(h, C.byref(t)) == 0 and t.value == 1
+    L.ipcg_collisions_destroy.argtypes = [C.c_void_p]
+    assert L.ipcg_collisions_destroy(h) == 0

@@ -560,3 +560,78 @@ def test_area_weighted_collision_set(oracle_mod):
     big = 0.25 * max(va.max(), 2 * ea.max())
     assert np.all(aw.vv_w <= plain.vv_w * big * (1 + 1e-15))
     assert np.all(aw.ev_w <= plain.ev_w * big * (1 + 1e-15))
+
+
+# --- improved max approximation --------------------------------------------------
+
+def _fan_with_point(p):
+    """Six triangles around a centre vertex 0 on z = 0, plus a free vertex 7 at p."""
+    ang = np.arange(6) * np.pi / 3
+    V = np.vstack([[0.0, 0, 0], np.c_[np.cos(ang), np.sin(ang), np.zeros(6)], [p]])
+    F = np.array([[0, 1 + k, 1 + (k + 1) % 6] for k in range(6)])
+    E = np.array(sorted({tuple(sorted(e)) for f in F for e in ((f[0], f[1]), (f[1], f[2]), (f[2], f[0]))}))
+    return V, E, F
+
+
+def test_improved_max_approx_counts_a_vertex_contact_once(oracle_mod):
+    """A vertex over the centre of a 6-triangle fan: the IPC set counts the
+    vertex-vertex contact once per incident face (weight 6); the improved max
+    approximation (normal_collisions_builder.cpp:340-455) brings it to 1."""
+    h, dhat, kappa = 1e-3, 1e-2, 1.0
+    V, E, F = _fan_with_point([0.0, 0.0, h])
+    one = kappa * oracle_mod.barrier(h * h, dhat * dhat)
+    ipc = oracle_mod.build_collisions(V, E, F, dhat)
+    assert ipc.vv.tolist() == [[0, 7]] and ipc.vv_w.tolist() == [6.0]
+    assert oracle_mod.barrier_energy(ipc, V, E, F, dhat, kappa) == pytest.approx(6 * one, rel=1e-14)
+    imp = oracle_mod.build_collisions(V, E, F, dhat, improved_max_approx=True)
+    # +1 on the vertex pair (face-vertex -> vertex-vertex), -1 on each of the
+    # six spokes (face-vertex -> edge-vertex; the projection ratio is exactly 0,
+    # so the point-edge type is P_E and the records stay edge-vertex)
+    assert imp.vv.tolist() == [[0, 7]] and imp.vv_w.tolist() == [7.0]
+    assert imp.ev.tolist() == [[e, 7] for e in range(6)] and imp.ev_w.tolist() == [-1.0] * 6
+    assert oracle_mod.barrier_energy(imp, V, E, F, dhat, kappa) == pytest.approx(one, rel=1e-12)
+
+
+def test_improved_max_approx_counts_an_edge_contact_once(oracle_mod):
+    """A vertex over the middle of an edge shared by two triangles: IPC gives
+    the edge-vertex contact weight 2, the improved set weight 1."""
+    V = np.array([[0.0, 0, 0], [1, 0, 0], [0.5, 1, 0], [0.5, -1, 0], [0.5, 0, 1e-3]])
+    F = np.array([[0, 1, 2], [1, 0, 3]])
+    E = np.array([[0, 1], [1, 2], [2, 0], [0, 3], [3, 1]])
+    ipc = oracle_mod.build_collisions(V, E, F, 1e-2)
+    assert ipc.ev.tolist() == [[0, 4]] and ipc.ev_w.tolist() == [2.0]
+    imp = oracle_mod.build_collisions(V, E, F, 1e-2, improved_max_approx=True)
+    assert imp.ev.tolist() == [[0, 4]] and imp.ev_w.tolist() == [1.0]
+    assert len(imp.vv) == len(imp.ee) == len(imp.fv) == 0
+    one = oracle_mod.barrier(1e-6, 1e-4)
+    assert oracle_mod.barrier_energy(imp, V, E, F, 1e-2, 1.0) == pytest.approx(one, rel=1e-12)
+    # area weighting scales the weight to a quarter of the vertex's area
+    aw = oracle_mod.build_collisions(V, E, F, 1e-2, improved_max_approx=True, area_weighting=True)
+    va, _ = oracle_mod.mesh_areas(V, E, F)
+    assert aw.ev.tolist() == [[0, 4]]
+    assert aw.ev_w[0] == pytest.approx(0.25 * va[4], rel=1e-15)
+
+
+def test_improved_max_approx_face_interior_unchanged(oracle_mod):
+    V = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0], [0.25, 0.25, 1e-3]])
+    F = np.array([[0, 1, 2]])
+    E = np.array([[0, 1], [1, 2], [2, 0]])
+    imp = oracle_mod.build_collisions(V, E, F, 1e-2, improved_max_approx=True)
+    assert imp.fv.tolist() == [[0, 3]] and imp.fv_w.tolist() == [1.0]
+    assert len(imp.vv) == len(imp.ev) == len(imp.ee) == 0
+
+
+def test_improved_max_approx_on_sheets(oracle_mod):
+    """On two close sheets every contact of the improved set has a nonzero
+    weight, none of the IPC set's face-vertex contacts is lost, and the
+    total weight does not grow (the improved set removes double counting)."""
+    from ipctk_gb300 import scenes
+    sc = scenes.two_sheet(side=12, seed=4)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    ipc = oracle_mod.build_collisions(V, E, F, sc["dhat"])
+    imp = oracle_mod.build_collisions(V, E, F, sc["dhat"], improved_max_approx=True)
+    for w in (imp.vv_w, imp.ev_w, imp.ee_w, imp.fv_w):
+        assert np.all(w != 0)
+    np.testing.assert_array_equal(imp.fv, ipc.fv)
+    total = lambda c: sum(float(np.sum(w)) for w in (c.vv_w, c.ev_w, c.ee_w, c.fv_w))
+    assert total(imp) <= total(ipc)
