@@ -346,6 +346,39 @@ int ipcg_has_intersections(const ipcg_mesh* mesh, const double* vertices, int* o
 /* Candidates (src/ipc/candidates/candidates.hpp): a kept broad-phase
  * candidate set on the device (EE pairs, then FV (face, vertex) pairs) and
  * the step-size rules that read it.  Single-scene 3D meshes. */
+/* ---------------------------------------------------------------------- */
+/* Friction: TangentialCollisions and FrictionPotential (isotropic)        */
+/* ---------------------------------------------------------------------- */
+
+typedef struct ipcg_tangential ipcg_tangential;
+int ipcg_tangential_create(ipcg_tangential** out);
+int ipcg_tangential_destroy(ipcg_tangential* tangential);
+
+/* TangentialCollisions::build(mesh, V, collisions, BarrierPotential(dhat,
+ * stiffness, use_physical_barrier), mu_s, mu_k) (tangential_collisions.cpp:
+ * 60-170) with the default blend (mu0 + mu1) / 2: for each normal collision
+ * but the near-parallel edge-edge ones (cross^2 < eps_x), the normal force
+ * magnitude -kappa b'(d^2 - dmin^2) 2 d (times the physical scaling), the
+ * closest point, the tangent basis and the blended coefficients.  mu_s,
+ * mu_k: num_vertices doubles (host or device).  Single-scene meshes. */
+int ipcg_tangential_build(ipcg_tangential* tangential, const ipcg_mesh* mesh, const double* vertices,
+                          const ipcg_collisions* collisions, double dhat, double stiffness,
+                          int use_physical_barrier, const double* mu_s, const double* mu_k);
+/* counts[4]: VV, EV, EE, FV tangential collisions */
+int ipcg_tangential_counts(const ipcg_tangential* tangential, int64_t counts[4]);
+/* Any output may be NULL.  Stencils as in ipcg_collisions_get; per collision
+ * (VV | EV | EE | FV order): weight, normal_force, closest_point (2),
+ * tangent_basis (6: the two 3-vector columns), mu_s, mu_k. */
+int ipcg_tangential_get(const ipcg_tangential* tangential, int32_t* vv, int32_t* ev, int32_t* ee, int32_t* fv,
+                        double* weight, double* normal_force, double* closest_point, double* tangent_basis,
+                        double* mu_s, double* mu_k);
+
+/* FrictionPotential(eps_v) energy, gradient and Hessian at velocities
+ * (tangential_potential.cpp:156-331; potential.cpp:36-222): any output may
+ * be NULL; the Hessian's inner 2x2 blocks are projected with psd_method. */
+int ipcg_friction_potential(const ipcg_tangential* tangential, const ipcg_mesh* mesh, const double* velocities,
+                            double eps_v, int psd_method, double* energy, double* gradient, ipcg_csr** hessian);
+
 typedef struct ipcg_candidates ipcg_candidates;
 int ipcg_candidates_create(ipcg_candidates** out);
 int ipcg_candidates_destroy(ipcg_candidates* candidates);

@@ -730,6 +730,114 @@ int ipcg_barrier_gauss_newton_hessian_quadratic_form(const ipcg_collisions* c, c
     return gauss_newton_call(c, mesh, V, dhat, stiffness, physical, nullptr, p, out);
 }
 
+int ipcg_tangential_create(ipcg_tangential** out)
+{
+    return guarded([&] {
+        require(out != nullptr, "out is NULL");
+        *out = new ipcg_tangential();
+    });
+}
+
+int ipcg_tangential_destroy(ipcg_tangential* t)
+{
+    return guarded([&] { delete t; });
+}
+
+int ipcg_tangential_build(ipcg_tangential* t, const ipcg_mesh* mesh, const double* V, const ipcg_collisions* c,
+    double dhat, double stiffness, int physical, const double* mu_s, const double* mu_k)
+{
+    return guarded([&] {
+        require(t && mesh && c && mu_s && mu_k && (V || mesh->nV == 0), "NULL argument");
+        require(mesh->n_scenes == 1, "friction on a batch mesh is not provided");
+        require(dhat > 0, "dhat must be positive");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        BarrierArgs a { dhat, stiffness, c->dmin, 0, IPCG_PSD_NONE };
+        barrier_options(physical, a);
+        DBuf<double> ms, mk;
+        upload(ms, mu_s, m->nV, m->stream);
+        upload(mk, mu_k, m->nV, m->stream);
+        tangential_build(c, m, dV, a, ms.p, mk.p, &t->st, t->N, t->cp, t->P, t->mu_s, t->mu_k);
+        t->mesh = mesh;
+    });
+}
+
+int ipcg_tangential_counts(const ipcg_tangential* t, int64_t counts[4])
+{
+    return guarded([&] {
+        require(t && counts, "NULL argument");
+        counts[0] = t->st.nvv;
+        counts[1] = t->st.nev;
+        counts[2] = t->st.nee;
+        counts[3] = t->st.nfv;
+    });
+}
+
+int ipcg_tangential_get(const ipcg_tangential* t, int32_t* vv, int32_t* ev, int32_t* ee, int32_t* fv,
+    double* weight, double* normal_force, double* closest_point, double* tangent_basis, double* mu_s, double* mu_k)
+{
+    return guarded([&] {
+        require(t != nullptr, "NULL argument");
+        const ipcg_collisions& st = t->st;
+        const int64_t n = st.size();
+        cudaStream_t s = 0;
+        copy_out(vv, st.vv.p, sizeof(int2) * st.nvv, s);
+        copy_out(ev, st.ev.p, sizeof(int2) * st.nev, s);
+        copy_out(ee, st.ee.p, sizeof(int2) * st.nee, s);
+        copy_out(fv, st.fv.p, sizeof(int2) * st.nfv, s);
+        if (weight) {
+            copy_out(weight, st.vv_w.p, sizeof(double) * st.nvv, s);
+            copy_out(weight + st.nvv, st.ev_w.p, sizeof(double) * st.nev, s);
+            copy_out(weight + st.nvv + st.nev, st.ee_w.p, sizeof(double) * st.nee, s);
+            copy_out(weight + st.nvv + st.nev + st.nee, st.fv_w.p, sizeof(double) * st.nfv, s);
+        }
+        copy_out(normal_force, t->N.p, sizeof(double) * n, s);
+        copy_out(closest_point, t->cp.p, sizeof(double) * 2 * n, s);
+        copy_out(tangent_basis, t->P.p, sizeof(double) * 6 * n, s);
+        copy_out(mu_s, t->mu_s.p, sizeof(double) * n, s);
+        copy_out(mu_k, t->mu_k.p, sizeof(double) * n, s);
+        IPCG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* U, double eps_v, int psd,
+    double* energy, double* gradient, ipcg_csr** hessian)
+{
+    return guarded([&] {
+        require(t && mesh && (U || mesh->nV == 0), "NULL argument");
+        require(t->mesh == mesh, "tangential collisions were built on another mesh");
+        require(eps_v > 0, "eps_v must be positive");
+        require(psd >= IPCG_PSD_NONE && psd <= IPCG_PSD_ABS, "Invalid type of PSD projection!");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dU = stage_positions(m, U, m->V0);
+        const FrictionView f { t->N.p, t->cp.p, t->P.p, t->mu_s.p, t->mu_k.p, eps_v };
+        double* gdev = nullptr;
+        DBuf<double> gtmp;
+        if (gradient) {
+            if (is_device_ptr(gradient)) gdev = gradient;
+            else {
+                gtmp.reserve(3 * m->nV + 1);
+                gdev = gtmp.p;
+            }
+        }
+        ipcg_csr* H = hessian ? new ipcg_csr() : nullptr;
+        try {
+            barrier_evaluate_friction(&t->st, m, dU, f, psd, energy, gdev, H);
+            if (gradient && gdev != gradient) {
+                IPCG_CUDA(cudaMemcpyAsync(gradient, gdev, sizeof(double) * 3 * m->nV, cudaMemcpyDeviceToHost,
+                    m->stream));
+                IPCG_CUDA(cudaStreamSynchronize(m->stream));
+            }
+        } catch (...) {
+            delete H;
+            throw;
+        }
+        if (hessian) *hessian = H;
+    });
+}
+
 int ipcg_csr_shape(const ipcg_csr* h, int64_t* rows, int64_t* nnz)
 {
     return guarded([&] {

@@ -1290,6 +1290,336 @@ __device__ __forceinline__ void decode_contribution(const ContactsView& cv, int6
 // Sort-by-key reduction into CSR: one thread per stored value (block q,
 // entry k,l) sums the contributions of block q in sorted (deterministic)
 // order and writes the value once.
+// ---- Friction (tangential_potential.cpp:156-331, friction/smooth_mu.cpp,
+// friction/smooth_friction_mollifier.cpp; isotropic) ----
+__device__ __forceinline__ double fr_smooth_mu(double y, double ms, double mk, double ev)
+{
+    if (ms == mk || fabs(y) >= ev) return mk;
+    const double z = fabs(y) / ev;
+    if (fabs(y) < 0.5 * ev) return 2 * (mk - ms) * z * z + ms;
+    return -2 * (mk - ms) * (z * (z - 2) + 1) + mk;
+}
+__device__ __forceinline__ double fr_mu_f0(double y, double ms, double mk, double ev)
+{
+    if (ms == mk || fabs(y) >= ev) {
+        const double f0 = fabs(y) >= ev ? y : y * y * (1 - y / (3 * ev)) / ev + ev / 3;
+        return mk * f0;
+    }
+    const double dm = mk - ms, z = fabs(y) / ev;
+    if (fabs(y) < 0.5 * ev)
+        return y * z * (z * (z * (1 - 0.4 * z) * dm - ms / 3.0) + ms) + (9.0 / 16.0) * ev * mk - (11.0 / 48.0) * ev * ms;
+    return y * z * (z * (z * (0.4 * z - 2) * dm + (3 * mk - (10.0 / 3.0) * ms)) + (2 * ms - mk)) + 0.6 * ev * mk
+        - (4.0 / 15.0) * ev * ms;
+}
+__device__ __forceinline__ double fr_mu_f1_over_x(double y, double ms, double mk, double ev)
+{
+    const double f1x = fabs(y) >= ev ? 1 / y : (2 - y / ev) / ev;
+    return fr_smooth_mu(y, ms, mk, ev) * f1x;
+}
+__device__ __forceinline__ double fr_mu_f2_x_minus_f1_over_x3(double y, double ms, double mk, double ev)
+{
+    if (ms == mk || fabs(y) >= ev) return mk * (fabs(y) >= ev ? -1 / (y * y * y) : -1 / (y * ev * ev));
+    const double dm = mk - ms, z = 1 / ev;
+    if (fabs(y) < 0.5 * ev) return z * z * (z * (8 - 6 * y * z) * dm - ms / y);
+    return z * z * (z * (6 * y * z - 16) * dm + (9 * mk - 10 * ms) / y);
+}
+
+// One tangential collision at velocities v: u = P^T (relative velocity),
+// T = Gamma^T P (rows 3k+d = g_k (P(d,0), P(d,1))), mu and w N.
+struct FrictionLocal {
+    double T[12][2];
+    double u0, u1, nu, ms, mk, scl;
+};
+__device__ __forceinline__ void friction_setup(const FrictionView& f, int64_t i, const Local& c, const V3* v,
+    FrictionLocal& L)
+{
+    const double c0 = f.cp[2 * i], c1 = f.cp[2 * i + 1];
+    const double* P = f.P + 6 * i;
+    const V3 b0 { P[0], P[1], P[2] }, b1 { P[3], P[4], P[5] };
+    V3 rv;
+    double g[4] = { 0, 0, 0, 0 };
+    if (c.type == CT_VV) {
+        rv = v[0] - v[1];
+        g[0] = 1, g[1] = -1;
+    } else if (c.type == CT_EV) {
+        rv = v[0] - ((v[2] - v[1]) * c0 + v[1]);
+        g[0] = 1, g[1] = c0 - 1, g[2] = -c0;
+    } else if (c.type == CT_EE) {
+        rv = ((v[1] - v[0]) * c0 + v[0]) - ((v[3] - v[2]) * c1 + v[2]);
+        g[0] = 1 - c0, g[1] = c0, g[2] = c1 - 1, g[3] = -c1;
+    } else {
+        rv = v[0] - ((v[1] + (v[2] - v[1]) * c0) + (v[3] - v[1]) * c1);
+        g[0] = 1, g[1] = c0 + c1 - 1, g[2] = -c0, g[3] = -c1;
+    }
+    L.u0 = dot(b0, rv);
+    L.u1 = dot(b1, rv);
+    L.nu = sqrt(L.u0 * L.u0 + L.u1 * L.u1);
+    L.ms = f.mu_s[i];
+    L.mk = f.mu_k[i];
+    L.scl = c.w * f.N[i];
+    for (int k = 0; k < c.n; ++k)
+        for (int d = 0; d < 3; ++d) {
+            L.T[3 * k + d][0] = g[k] * P[d];
+            L.T[3 * k + d][1] = g[k] * P[3 + d];
+        }
+}
+
+// Symmetric 2x2 PSD projection (eigen_ext.tpp:64-108 for n = 2): unchanged
+// when the smaller eigenvalue is >= 0, else negative eigenvalues clamped to 0
+// (CLAMP) or flipped (ABS).  Row-major A; the lower entry is the off-diagonal.
+__device__ void project_psd2(double* A, int method)
+{
+    if (method == IPCG_PSD_NONE) return;
+    const double a = A[0], b = A[2], c = A[3];
+    double l1, l2, vx, vy;
+    if (b == 0) {
+        l1 = a <= c ? a : c;
+        l2 = a <= c ? c : a;
+        vx = a <= c ? 1.0 : 0.0;
+        vy = a <= c ? 0.0 : 1.0;
+    } else {
+        const double m = 0.5 * (a + c), h = 0.5 * (a - c);
+        const double r = sqrt(h * h + b * b);
+        l1 = m - r;
+        l2 = m + r;
+        // eigenvector of l1 from the better-conditioned row
+        const double px = l1 - c, py = b, qx = b, qy = l1 - a;
+        if (px * px + py * py >= qx * qx + qy * qy) vx = px, vy = py;
+        else vx = qx, vy = qy;
+        const double nv = sqrt(vx * vx + vy * vy);
+        vx /= nv;
+        vy /= nv;
+    }
+    if (l1 >= 0.0) return;
+    l1 = method == IPCG_PSD_CLAMP ? 0.0 : -l1;
+    if (l2 < 0) l2 = method == IPCG_PSD_CLAMP ? 0.0 : -l2;
+    const double wx = -vy, wy = vx;
+    A[0] = l1 * vx * vx + l2 * wx * wx;
+    A[1] = A[2] = l1 * vx * vy + l2 * wx * wy;
+    A[3] = l1 * vy * vy + l2 * wy * wy;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_friction_energy(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ U, FrictionView f, double* __restrict__ partial)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (i < n) {
+        Local c;
+        load_contact(cv, E, F, i, c);
+        V3 v[4];
+        gather(U, c, v);
+        FrictionLocal L;
+        friction_setup(f, i, c, v, L);
+        e = L.scl * fr_mu_f0(L.nu, L.ms, L.mk, f.eps_v);
+    }
+    typedef cub::BlockReduce<double, BLOCK> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const double sum = BR(tmp).Sum(e);
+    if (threadIdx.x == 0) partial[blockIdx.x] = sum;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_friction_gradient(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ U, FrictionView f, double* __restrict__ grad)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    V3 v[4];
+    gather(U, c, v);
+    FrictionLocal L;
+    friction_setup(f, i, c, v, L);
+    const double f1x = fr_mu_f1_over_x(L.nu, L.ms, L.mk, f.eps_v);
+    const double s0 = (f1x * L.u0) * L.scl, s1 = (f1x * L.u1) * L.scl;
+    for (int a = 0; a < c.n; ++a)
+        for (int k = 0; k < 3; ++k) {
+            const int r = 3 * a + k;
+            const double val = L.T[r][0] * s0 + L.T[r][1] * s1;
+            if (val != 0) atomicAdd(grad + 3 * (int64_t)c.vid[a] + k, val);
+        }
+}
+
+// Local friction Hessian (tangential_potential.cpp:233-331) into the slab:
+// dynamic (|u| > eps_v) rank one along u's perpendicular, |u| = 0 the
+// isotropic limit, otherwise the 2x2 inner matrix projected in place.
+template <int TYPE>
+__global__ void __launch_bounds__(LH_BLOCK) k_friction_local_hessian(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ U, FrictionView f, Slab hs, int64_t first, int64_t count,
+    int psd)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t i = first + t;
+    constexpr int NS = TYPE == CT_VV ? 2 : (TYPE == CT_EV ? 3 : 4);
+    constexpr int N = 3 * NS;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    V3 v[4];
+    gather(U, c, v);
+    FrictionLocal L;
+    friction_setup(f, i, c, v, L);
+    const double f1x = fr_mu_f1_over_x(L.nu, L.ms, L.mk, f.eps_v);
+    if (L.nu > f.eps_v) {
+        if (psd != IPCG_PSD_NONE && L.scl <= 0) {
+            for (int k = 0; k < N * N; ++k) hs.at(i, k) = 0.0;
+            return;
+        }
+        const double cc = L.scl * f1x / (L.nu * L.nu);
+        const double q0 = cc * -L.u1, q1 = cc * L.u0;
+        for (int r = 0; r < N; ++r) {
+            const double ar = L.T[r][0] * q0 + L.T[r][1] * q1;
+            for (int q = 0; q < N; ++q) hs.at(i, r * N + q) = ar * (-L.u1 * L.T[q][0] + L.u0 * L.T[q][1]);
+        }
+    } else if (L.nu == 0) {
+        if (psd != IPCG_PSD_NONE && L.scl <= 0) {
+            for (int k = 0; k < N * N; ++k) hs.at(i, k) = 0.0;
+            return;
+        }
+        const double cc = L.scl * f1x;
+        for (int r = 0; r < N; ++r)
+            for (int q = 0; q < N; ++q)
+                hs.at(i, r * N + q) = (cc * L.T[r][0]) * L.T[q][0] + (cc * L.T[r][1]) * L.T[q][1];
+    } else {
+        const double f2 = fr_mu_f2_x_minus_f1_over_x3(L.nu, L.ms, L.mk, f.eps_v);
+        double in[4] = { f2 * L.u0 * L.u0, f2 * L.u0 * L.u1, f2 * L.u1 * L.u0, f2 * L.u1 * L.u1 };
+        in[0] += f1x;
+        in[3] += f1x;
+        for (int k = 0; k < 4; ++k) in[k] *= L.scl;
+        project_psd2(in, psd);
+        for (int r = 0; r < N; ++r) {
+            const double t0 = L.T[r][0] * in[0] + L.T[r][1] * in[2], t1 = L.T[r][0] * in[1] + L.T[r][1] * in[3];
+            for (int q = 0; q < N; ++q) hs.at(i, r * N + q) = t0 * L.T[q][0] + t1 * L.T[q][1];
+        }
+    }
+}
+
+// ---- TangentialCollisions::build (tangential_collisions.cpp:60-170) ----
+__device__ __forceinline__ V3 normalized(V3 a)
+{
+    const double n = sqnorm(a);
+    if (!(n > 0)) return a;
+    const double r = sqrt(n);
+    return V3 { a.x / r, a.y / r, a.z / r };
+}
+
+// EE collisions with cross^2 < eps_x are left out of the tangential set.
+__global__ void k_tangential_keep_ee(ContactsView cv, const int* __restrict__ E, const double* __restrict__ V,
+    int* __restrict__ keep)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= cv.nee) return;
+    const int2 p = cv.ee[j];
+    const V3 a0 = load_v3(V, E[2 * p.x]), a1 = load_v3(V, E[2 * p.x + 1]);
+    const V3 b0 = load_v3(V, E[2 * p.y]), b1 = load_v3(V, E[2 * p.y + 1]);
+    keep[j] = ee_cross_sqnorm(a0, a1, b0, b1) < cv.ee_eps[j] ? 0 : 1;
+}
+
+struct TangentialOut {
+    int2 *vv, *ev, *ee, *fv;
+    double *vv_w, *ev_w, *ee_w, *fv_w, *ee_eps;
+    int8_t* ee_dtype;
+    double *N, *cp, *P, *mu_s, *mu_k;
+};
+
+__global__ void k_tangential_build(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    const double* __restrict__ V, const Params* __restrict__ sp, SceneView sv, const double* __restrict__ mu_s,
+    const double* __restrict__ mu_k, const int* __restrict__ keep, const int* __restrict__ offs, int64_t nee_kept,
+    TangentialOut o)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    int64_t slot, j;
+    if (c.type == CT_VV) slot = j = i;
+    else if (c.type == CT_EV) {
+        j = i - cv.nvv;
+        slot = i;
+    } else if (c.type == CT_EE) {
+        j = i - cv.nvv - cv.nev;
+        if (!keep[j]) return;
+        slot = cv.nvv + cv.nev + offs[j];
+    } else {
+        j = i - cv.nvv - cv.nev - cv.nee;
+        slot = cv.nvv + cv.nev + nee_kept + j;
+    }
+    const Params P = sp[sv.of(c.vid[0])];
+    V3 x[4];
+    gather(V, c, x);
+    double d2;
+    if (c.type == CT_VV) d2 = point_point_distance(x[0], x[1]);
+    else if (c.type == CT_EV) d2 = point_edge_distance(x[0], x[1], x[2], point_edge_distance_type(x[0], x[1], x[2]));
+    else if (c.type == CT_EE)
+        d2 = edge_edge_distance(x[0], x[1], x[2], x[3], edge_edge_distance_type(x[0], x[1], x[2], x[3]));
+    else d2 = point_triangle_distance(x[0], x[1], x[2], x[3], point_triangle_distance_type(x[0], x[1], x[2], x[3]));
+    // barrier_force_magnitude.cpp:5-15, then the physical scaling
+    const double Nf = -P.kappa * barrier_fn<1, double>(P.kind, d2 - P.dmin2, P.xhat) * 2 * sqrt(d2) * P.scale;
+    double cp0 = 0, cp1 = 0, ms, mk;
+    V3 b0, b1;
+    const int* v = c.vid;
+    auto blend = [](double a, double b) { return (a + b) / 2; };
+    if (c.type == CT_VV) {
+        // point_point_tangent_basis (tangent/tangent_basis.cpp)
+        const V3 d = x[1] - x[0];
+        const V3 cx = cross(V3 { 1, 0, 0 }, d), cy = cross(V3 { 0, 1, 0 }, d);
+        const V3 cc = sqnorm(cx) > sqnorm(cy) ? cx : cy;
+        b0 = normalized(cc);
+        b1 = normalized(cross(d, cc));
+        ms = blend(mu_s[v[0]], mu_s[v[1]]);
+        mk = blend(mu_k[v[0]], mu_k[v[1]]);
+    } else if (c.type == CT_EV) {
+        const V3 e = x[2] - x[1];
+        cp0 = dot(x[0] - x[1], e) / sqnorm(e);
+        b0 = normalized(e);
+        b1 = normalized(cross(e, x[0] - x[1]));
+        ms = blend((mu_s[v[2]] - mu_s[v[1]]) * cp0 + mu_s[v[1]], mu_s[v[0]]);
+        mk = blend((mu_k[v[2]] - mu_k[v[1]]) * cp0 + mu_k[v[1]], mu_k[v[0]]);
+    } else if (c.type == CT_EE) {
+        const V3 ea = x[1] - x[0], eb = x[3] - x[2];
+        ldlt2_solve(ea, eb * -1.0, x[2] - x[0], cp0, cp1);
+        b0 = normalized(ea);
+        b1 = normalized(cross(cross(ea, eb), ea));
+        ms = blend((mu_s[v[1]] - mu_s[v[0]]) * cp0 + mu_s[v[0]], (mu_s[v[3]] - mu_s[v[2]]) * cp1 + mu_s[v[2]]);
+        mk = blend((mu_k[v[1]] - mu_k[v[0]]) * cp0 + mu_k[v[0]], (mu_k[v[3]] - mu_k[v[2]]) * cp1 + mu_k[v[2]]);
+    } else {
+        const V3 e0 = x[2] - x[1];
+        ldlt2_solve(e0, x[3] - x[1], x[0] - x[1], cp0, cp1);
+        b0 = normalized(e0);
+        b1 = normalized(cross(cross(e0, x[3] - x[1]), e0));
+        ms = blend(mu_s[v[1]] + cp0 * (mu_s[v[2]] - mu_s[v[1]]) + cp1 * (mu_s[v[3]] - mu_s[v[1]]), mu_s[v[0]]);
+        mk = blend(mu_k[v[1]] + cp0 * (mu_k[v[2]] - mu_k[v[1]]) + cp1 * (mu_k[v[3]] - mu_k[v[1]]), mu_k[v[0]]);
+    }
+    if (c.type == CT_VV) {
+        o.vv[slot] = cv.vv[j];
+        o.vv_w[slot] = c.w;
+    } else if (c.type == CT_EV) {
+        o.ev[slot - cv.nvv] = cv.ev[j];
+        o.ev_w[slot - cv.nvv] = c.w;
+    } else if (c.type == CT_EE) {
+        const int64_t k = slot - cv.nvv - cv.nev;
+        o.ee[k] = cv.ee[j];
+        o.ee_w[k] = c.w;
+        o.ee_eps[k] = cv.ee_eps[j];
+        o.ee_dtype[k] = cv.ee_dt[j];
+    } else {
+        const int64_t k = slot - cv.nvv - cv.nev - nee_kept;
+        o.fv[k] = cv.fv[j];
+        o.fv_w[k] = c.w;
+    }
+    o.N[slot] = Nf;
+    o.cp[2 * slot] = cp0;
+    o.cp[2 * slot + 1] = cp1;
+    double* Po = o.P + 6 * slot;
+    Po[0] = b0.x, Po[1] = b0.y, Po[2] = b0.z;
+    Po[3] = b1.x, Po[4] = b1.y, Po[5] = b1.z;
+    o.mu_s[slot] = ms;
+    o.mu_k[slot] = mk;
+}
+
 __global__ void k_assemble(ContactsView cv, const unsigned long long* __restrict__ ukeys,
     const int* __restrict__ run_start, const int* __restrict__ run_len, const int* __restrict__ contrib,
     Slab hs, const int* __restrict__ bptr, int r0, int64_t B0, int nb, double* __restrict__ val)
@@ -1523,16 +1853,18 @@ static const Params* upload_params(const ipcg_collisions* cs, ipcg_mesh* m, cons
     return reinterpret_cast<const Params*>(m->params_buf.p);
 }
 
+// With fr set, the same pipeline evaluates the friction potential of the
+// tangential set whose stencils are cs at velocities V (single scene).
 void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
-    double* energy_host, double* grad_dev, ipcg_csr* hess)
+    double* energy_host, double* grad_dev, ipcg_csr* hess, const FrictionView* fr)
 {
     cudaStream_t s = m->stream;
     ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
         cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
     const int64_t n = cs->size();
     const int ns = (int)m->n_scenes;
-    Params P;
-    const Params* sp = upload_params(cs, m, a, P);
+    Params P {};
+    const Params* sp = fr ? nullptr : upload_params(cs, m, a, P);
     const SceneView sv = scene_view(m);
     const int nblk = grid_for(n, BLOCK);
     const int64_t nV = m->nV;
@@ -1547,7 +1879,11 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     } else if (energy_host) {
         m->partial.reserve(nblk + 2);
         if (n > 0) {
-            IPCG_LAUNCH("k_energy", s, k_energy<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, m->partial.p));
+            if (fr)
+                IPCG_LAUNCH("k_friction_energy", s, k_friction_energy<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V,
+                    *fr, m->partial.p));
+            else
+                IPCG_LAUNCH("k_energy", s, k_energy<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, P, m->partial.p));
             IPCG_LAUNCH("k_sum_partials", s, k_sum_partials<<<1, 1024, 0, s>>>(m->partial.p, nblk, m->partial.p + nblk));
             IPCG_CHECK_LAUNCH();
             IPCG_CUDA(cudaMemcpyAsync(energy_host, m->partial.p + nblk, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1558,7 +1894,12 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     if (grad_dev) {
         IPCG_CUDA(cudaMemsetAsync(grad_dev, 0, sizeof(double) * 3 * nV, s));
         if (n > 0) {
-            IPCG_LAUNCH("k_gradient", s, k_gradient<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, sp, sv, grad_dev));
+            if (fr)
+                IPCG_LAUNCH("k_friction_gradient", s, k_friction_gradient<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p,
+                    V, *fr, grad_dev));
+            else
+                IPCG_LAUNCH("k_gradient", s, k_gradient<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, sp, sv,
+                    grad_dev));
             IPCG_CHECK_LAUNCH();
         }
     }
@@ -1615,6 +1956,24 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
             if (nc > 0) {
                 const int64_t first[4] = { 0, cc.nvv, cc.nvv + cc.nev, cc.nvv + cc.nev + cc.nee };
                 const int64_t count[4] = { cc.nvv, cc.nev, cc.nee, cc.nfv };
+                if (fr) {
+                    // friction: local Hessians are projected in place (2x2 inner matrix)
+                    const FrictionView f = *fr;
+                    if (count[0])
+                        IPCG_LAUNCH("k_friction_local_hessian_vv", t, k_friction_local_hessian<CT_VV><<<grid_for(count[0],
+                            LH_BLOCK), LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, f, slab, first[0], count[0], a.psd));
+                    if (count[1])
+                        IPCG_LAUNCH("k_friction_local_hessian_ev", t, k_friction_local_hessian<CT_EV><<<grid_for(count[1],
+                            LH_BLOCK), LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, f, slab, first[1], count[1], a.psd));
+                    IPCG_CUDA(cudaEventRecord(m->ev_side, t));
+                    if (count[2])
+                        IPCG_LAUNCH("k_friction_local_hessian_ee", s, k_friction_local_hessian<CT_EE><<<grid_for(count[2],
+                            LH_BLOCK), LH_BLOCK, 0, s>>>(cc, m->E.p, m->F.p, V, f, slab, first[2], count[2], a.psd));
+                    if (count[3])
+                        IPCG_LAUNCH("k_friction_local_hessian_fv", s, k_friction_local_hessian<CT_FV><<<grid_for(count[3],
+                            LH_BLOCK), LH_BLOCK, 0, s>>>(cc, m->E.p, m->F.p, V, f, slab, first[3], count[3], a.psd));
+                    IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
+                } else {
                 if (count[0])
                     IPCG_LAUNCH("k_local_hessian_vv", t, k_local_hessian<CT_VV><<<grid_for(count[0], LH_BLOCK), LH_BLOCK, 0,
                         t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[0], count[0]));
@@ -1632,6 +1991,7 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
                 if (a.psd != IPCG_PSD_NONE)
                     IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(nc, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, slab,
                         m->proj.p, a.psd, d_fail));
+                }
                 // sparsity pattern: sort (block key, contribution) and run-length encode
                 IPCG_LAUNCH("k_block_keys", t, k_block_keys<<<nblk_c, BLOCK, 0, t>>>(cc, m->E.p, m->F.p,
                     m->keys_a.p, ids_in, nk, gd));
@@ -1730,6 +2090,69 @@ void barrier_gauss_newton(const ipcg_collisions* cs, ipcg_mesh* m, const double*
         IPCG_CUDA(cudaMemcpyAsync(qf_host, m->partial.p + nblk, sizeof(double), cudaMemcpyDeviceToHost, s));
         IPCG_CUDA(cudaStreamSynchronize(s));
     }
+}
+
+void barrier_evaluate_friction(const ipcg_collisions* stencils, ipcg_mesh* m, const double* U, const FrictionView& f,
+    int psd, double* energy_host, double* grad_dev, ipcg_csr* hess)
+{
+    BarrierArgs a { 1.0, 1.0, 0.0, 0, psd };
+    barrier_evaluate(stencils, m, U, a, energy_host, grad_dev, hess, &f);
+}
+
+void tangential_build(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    const double* mu_s, const double* mu_k, ipcg_collisions* st, DBuf<double>& N, DBuf<double>& cp, DBuf<double>& P,
+    DBuf<double>& ms, DBuf<double>& mk)
+{
+    cudaStream_t s = m->stream;
+    ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
+        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
+    Params P0;
+    const Params* sp = upload_params(cs, m, a, P0);
+    // EE collisions kept: flags, then their compacted slots
+    m->widx.reserve(2 * (cs->nee + 1));
+    int* keep = m->widx.p;
+    int* offs = m->widx.p + cs->nee + 1;
+    int64_t nee_kept = 0;
+    if (cs->nee) {
+        IPCG_LAUNCH("k_tangential_keep_ee", s, k_tangential_keep_ee<<<grid_for(cs->nee, BLOCK), BLOCK, 0, s>>>(cv,
+            m->E.p, V, keep));
+        exclusive_sum_i32(m, s, keep, offs, (int)cs->nee);
+        int tail[2];
+        IPCG_CUDA(cudaMemcpyAsync(&tail[0], keep + cs->nee - 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaMemcpyAsync(&tail[1], offs + cs->nee - 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        nee_kept = tail[0] + tail[1];
+    }
+    st->nvv = cs->nvv;
+    st->nev = cs->nev;
+    st->nee = nee_kept;
+    st->nfv = cs->nfv;
+    st->dmin = cs->dmin;
+    st->scene_dmin = cs->scene_dmin;
+    st->sorted = cs->sorted;
+    st->vv.reserve(st->nvv + 1);
+    st->ev.reserve(st->nev + 1);
+    st->ee.reserve(st->nee + 1);
+    st->fv.reserve(st->nfv + 1);
+    st->vv_w.reserve(st->nvv + 1);
+    st->ev_w.reserve(st->nev + 1);
+    st->ee_w.reserve(st->nee + 1);
+    st->fv_w.reserve(st->nfv + 1);
+    st->ee_eps.reserve(st->nee + 1);
+    st->ee_dtype.reserve(st->nee + 1);
+    const int64_t nt = st->size();
+    N.reserve(nt + 1);
+    cp.reserve(2 * nt + 2);
+    P.reserve(6 * nt + 6);
+    ms.reserve(nt + 1);
+    mk.reserve(nt + 1);
+    const TangentialOut o { st->vv.p, st->ev.p, st->ee.p, st->fv.p, st->vv_w.p, st->ev_w.p, st->ee_w.p, st->fv_w.p,
+        st->ee_eps.p, st->ee_dtype.p, N.p, cp.p, P.p, ms.p, mk.p };
+    const int64_t n = cs->size();
+    if (n)
+        IPCG_LAUNCH("k_tangential_build", s, k_tangential_build<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(cv, m->E.p,
+            m->F.p, V, sp, scene_view(m), mu_s, mu_k, keep, offs, nee_kept, o));
+    IPCG_CUDA(cudaStreamSynchronize(s));
 }
 
 } // namespace ipcg

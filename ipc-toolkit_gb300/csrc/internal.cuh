@@ -229,6 +229,15 @@ struct ipcg_collisions {
     int64_t size() const { return nvv + nev + nee + nfv; }
 };
 
+// TangentialCollisions: stencils (and weights) in an ipcg_collisions, plus
+// per collision the normal force, closest point (2), tangent basis (6) and
+// blended mu_s / mu_k.
+struct ipcg_tangential {
+    ipcg_collisions st;
+    ipcg::DBuf<double> N, cp, P, mu_s, mu_k;
+    const ipcg_mesh* mesh = nullptr;
+};
+
 struct ipcg_csr {
     int64_t rows = 0, nnz = 0;
     ipcg::PBuf<int64_t> row_ptr;
@@ -280,8 +289,23 @@ struct BarrierArgs {
     int mixed = 0;                       // FP32 point-triangle contacts
     int kind = 0;                        // barrier function (IPCG_BARRIER_* kinds)
 };
+struct FrictionView;
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
-    double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null);
+    double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null, const FrictionView* friction = nullptr);
+// Friction (tangential_potential.cpp): per tangential collision, in the
+// order of its stencil lists, the normal force N, closest point cp (2), tangent
+// basis P (b0 xyz, b1 xyz) and blended mu_s / mu_k.
+struct FrictionView {
+    const double *N, *cp, *P, *mu_s, *mu_k;
+    double eps_v;
+};
+void barrier_evaluate_friction(const ipcg_collisions* stencils, ipcg_mesh* m, const double* U, const FrictionView& f,
+    int psd, double* energy_host, double* grad_dev, ipcg_csr* hess);
+// TangentialCollisions::build: from the normal set at positions V with the
+// barrier potential a, per-vertex mu (device); fills the stencils and arrays.
+void tangential_build(const ipcg_collisions* normal, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    const double* mu_s_dev, const double* mu_k_dev, ipcg_collisions* stencils, ipcg::DBuf<double>& N,
+    ipcg::DBuf<double>& cp, ipcg::DBuf<double>& P, ipcg::DBuf<double>& mu_s, ipcg::DBuf<double>& mu_k);
 // Gauss-Newton Hessian diagonal (device, 3 nV) and/or quadratic form p^T H p
 // (p on the device, result on the host).
 void barrier_gauss_newton(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,

@@ -93,6 +93,12 @@ def _load():
         "ipcg_collisions_use_area_weighting": (i32, [P, P]),
         "ipcg_collisions_set_collision_set_type": (i32, [P, i32]),
         "ipcg_collisions_collision_set_type": (i32, [P, P]),
+        "ipcg_tangential_create": (i32, [PP]),
+        "ipcg_tangential_destroy": (i32, [P]),
+        "ipcg_tangential_build": (i32, [P, P, P, P, d, d, i32, P, P]),
+        "ipcg_tangential_counts": (i32, [P, P]),
+        "ipcg_tangential_get": (i32, [P] + [P] * 10),
+        "ipcg_friction_potential": (i32, [P, P, P, d, i32, P, P, PP]),
         "ipcg_candidates_create": (i32, [PP]),
         "ipcg_candidates_destroy": (i32, [P]),
         "ipcg_candidates_build": (i32, [P, P, P, d]),
@@ -937,6 +943,95 @@ class Server:
         _check(_load().ipcg_server_stats(self._h, _ptr(st)))
         return {"completed": int(st[0]), "queued": int(st[1]), "running": int(st[2]), "releases": int(st[3]),
                 "resident_bytes": int(st[4])}
+
+
+class TangentialCollisions:
+    """TangentialCollisions (src/ipc/collisions/tangential/tangential_collisions.hpp),
+    isotropic, built from a NormalCollisions set on the device."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        _check(_load().ipcg_tangential_create(C.byref(h)))
+        self._h = h
+        self._mesh = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.ipcg_tangential_destroy(h)
+            self._h = None
+
+    def build(self, mesh: CollisionMesh, vertices, collisions: NormalCollisions, normal_potential, mu_s, mu_k=None):
+        """tangential_collisions.cpp:60-170; mu_s / mu_k scalars or per-vertex
+        arrays (mu_k defaults to mu_s)."""
+        V = _as_f64(vertices)
+        nV = mesh.num_vertices
+        ms = np.ascontiguousarray(np.broadcast_to(np.asarray(mu_s, np.float64), (nV,)))
+        mk = np.ascontiguousarray(np.broadcast_to(np.asarray(mu_s if mu_k is None else mu_k, np.float64), (nV,)))
+        _check(_load().ipcg_tangential_build(self._h, mesh._h, _ptr(V), collisions._h, normal_potential.dhat,
+                                             normal_potential.stiffness, normal_potential._options, _ptr(ms),
+                                             _ptr(mk)))
+        self._mesh = mesh
+
+    def counts(self):
+        c = np.zeros(4, np.int64)
+        _check(_load().ipcg_tangential_counts(self._h, _ptr(c)))
+        return c
+
+    def __len__(self):
+        return int(self.counts().sum())
+
+    def to_arrays(self):
+        """dict: vv, ev, ee, fv stencils; per collision weight, normal_force,
+        closest_point (n, 2), tangent_basis (n, 3, 2), mu_s, mu_k."""
+        nvv, nev, nee, nfv = (int(x) for x in self.counts())
+        n = nvv + nev + nee + nfv
+        out = {k: np.zeros((m, 2), np.int32) for k, m in (("vv", nvv), ("ev", nev), ("ee", nee), ("fv", nfv))}
+        w, N, mus, muk = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(n)
+        cp, P = np.zeros((n, 2)), np.zeros((n, 6))
+        _check(_load().ipcg_tangential_get(self._h, _ptr(out["vv"]), _ptr(out["ev"]), _ptr(out["ee"]),
+                                           _ptr(out["fv"]), _ptr(w), _ptr(N), _ptr(cp), _ptr(P), _ptr(mus),
+                                           _ptr(muk)))
+        out.update(weight=w, normal_force=N, closest_point=cp, tangent_basis=P.reshape(n, 2, 3).transpose(0, 2, 1),
+                   mu_s=mus, mu_k=muk)
+        return out
+
+
+class FrictionPotential:
+    """FrictionPotential(eps_v) (src/ipc/potentials/friction_potential.hpp):
+    energy, gradient and Hessian of the lagged smooth friction at velocities."""
+
+    def __init__(self, eps_v: float):
+        if not eps_v > 0:
+            raise ValueError("eps_v must be positive")
+        self.eps_v = float(eps_v)
+
+    def _call(self, collisions, mesh, velocities, psd, e=None, g=None, h=None):
+        U = _as_f64(velocities)
+        _check(_load().ipcg_friction_potential(collisions._h, mesh._h, _ptr(U), self.eps_v, int(psd),
+                                               _ptr(e) if e is not None else None,
+                                               _ptr(g) if g is not None else None,
+                                               C.byref(h) if h is not None else None))
+
+    def __call__(self, collisions: TangentialCollisions, mesh: CollisionMesh, velocities) -> float:
+        e = np.zeros(1)
+        self._call(collisions, mesh, velocities, 0, e=e)
+        return float(e[0])
+
+    def gradient(self, collisions, mesh, velocities):
+        U = _as_f64(velocities)
+        if _is_torch_cuda(U):
+            import torch
+            g = torch.empty(U.numel(), dtype=torch.float64, device=U.device)
+        else:
+            g = np.zeros(3 * mesh.num_vertices)
+        self._call(collisions, mesh, U, 0, g=g)
+        return g
+
+    def hessian(self, collisions, mesh, velocities, project_hessian_to_psd=PSDProjectionMethod.NONE):
+        h = C.c_void_p()
+        self._call(collisions, mesh, velocities, int(project_hessian_to_psd), h=h)
+        return _csr_to_scipy(h, 3 * mesh.num_vertices)
 
 
 class Candidates:

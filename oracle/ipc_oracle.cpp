@@ -2388,12 +2388,425 @@ double orc_barrier_gn_quadratic_form(void* h, const double* V, const int32_t* E,
     return s;
 }
 
+// ---------------------------------------------------------------------------
+// Friction: TangentialCollisions::build (tangential_collisions.cpp:60-170)
+// and FrictionPotential (tangential_potential.cpp:156-331, friction_potential.cpp,
+// friction/smooth_mu.cpp, friction/smooth_friction_mollifier.cpp), isotropic.
+// ---------------------------------------------------------------------------
+static V3 normalized(V3 a)
+{
+    const double n = sqnorm(a);
+    if (!(n > 0)) return a;
+    const double r = std::sqrt(n);
+    return { a.x / r, a.y / r, a.z / r };
+}
+// tangent bases (tangent/tangent_basis.cpp): columns b0, b1
+static void pp_basis(V3 p0, V3 p1, V3& b0, V3& b1)
+{
+    const V3 d = sub(p1, p0);
+    const V3 cx = cross(V3 { 1, 0, 0 }, d), cy = cross(V3 { 0, 1, 0 }, d);
+    const V3 c = sqnorm(cx) > sqnorm(cy) ? cx : cy;
+    b0 = normalized(c);
+    b1 = normalized(cross(d, c));
+}
+static void pe_basis(V3 p, V3 e0, V3 e1, V3& b0, V3& b1)
+{
+    const V3 e = sub(e1, e0);
+    b0 = normalized(e);
+    b1 = normalized(cross(e, sub(p, e0)));
+}
+static void ee_basis(V3 ea0, V3 ea1, V3 eb0, V3 eb1, V3& b0, V3& b1)
+{
+    const V3 ea = sub(ea1, ea0);
+    const V3 n = cross(ea, sub(eb1, eb0));
+    b0 = normalized(ea);
+    b1 = normalized(cross(n, ea));
+}
+static void pt_basis(V3 p, V3 t0, V3 t1, V3 t2, V3& b0, V3& b1)
+{
+    (void)p;
+    const V3 e0 = sub(t1, t0);
+    const V3 n = cross(e0, sub(t2, t0));
+    b0 = normalized(e0);
+    b1 = normalized(cross(n, e0));
+}
+// smooth friction mollifier f0, f1/x, (f2 x - f1)/x^3 and the smooth mu
+// blend of static and kinetic coefficients (isotropic)
+static double mu_f0(double y, double ms, double mk, double ev)
+{
+    if (ms == mk || std::abs(y) >= ev) {
+        const double f0 = std::abs(y) >= ev ? y : y * y * (1 - y / (3 * ev)) / ev + ev / 3;
+        return mk * f0;
+    }
+    const double dm = mk - ms, z = std::abs(y) / ev;
+    if (std::abs(y) < 0.5 * ev)
+        return y * z * (z * (z * (1 - 0.4 * z) * dm - ms / 3.0) + ms) + (9.0 / 16.0) * ev * mk - (11.0 / 48.0) * ev * ms;
+    return y * z * (z * (z * (0.4 * z - 2) * dm + (3 * mk - (10.0 / 3.0) * ms)) + (2 * ms - mk)) + 0.6 * ev * mk
+        - (4.0 / 15.0) * ev * ms;
+}
+static double smooth_mu_value(double y, double ms, double mk, double ev)
+{
+    if (ms == mk || std::abs(y) >= ev) return mk;
+    const double z = std::abs(y) / ev;
+    if (std::abs(y) < 0.5 * ev) return 2 * (mk - ms) * z * z + ms;
+    return -2 * (mk - ms) * (z * (z - 2) + 1) + mk;
+}
+static double mu_f1_over_x(double y, double ms, double mk, double ev)
+{
+    const double f1x = std::abs(y) >= ev ? 1 / y : (2 - y / ev) / ev;
+    return smooth_mu_value(y, ms, mk, ev) * f1x;
+}
+static double mu_f2_x_minus_f1_over_x3(double y, double ms, double mk, double ev)
+{
+    if (ms == mk || std::abs(y) >= ev) {
+        const double f = std::abs(y) >= ev ? -1 / (y * y * y) : -1 / (y * ev * ev);
+        return mk * f;
+    }
+    const double dm = mk - ms, z = 1 / ev;
+    if (std::abs(y) < 0.5 * ev) return z * z * (z * (8 - 6 * y * z) * dm - ms / y);
+    return z * z * (z * (6 * y * z - 16) * dm + (9 * mk - 10 * ms) / y);
+}
+
+struct Tangential {
+    Collisions base;                        // stencils and weights (vv | ev | ee | fv)
+    std::vector<double> N, cp, P, mu_s, mu_k; // per collision: cp 2, P 6 (b0 xyz, b1 xyz)
+};
+
+// Relative-velocity coefficients g (relative velocity = sum_k g_k v_k) of a
+// tangential collision (tangent/relative_velocity.cpp jacobians).
+static void friction_gamma(const Contact& c, const double* cp, double* g)
+{
+    if (c.type == CT_VV) g[0] = 1, g[1] = -1;
+    else if (c.type == CT_EV) g[0] = 1, g[1] = cp[0] - 1, g[2] = -cp[0];
+    else if (c.type == CT_EE) g[0] = 1 - cp[0], g[1] = cp[0], g[2] = cp[1] - 1, g[3] = -cp[1];
+    else g[0] = 1, g[1] = cp[0] + cp[1] - 1, g[2] = -cp[0], g[3] = -cp[1];
+}
+// relative velocity in the reference's functional forms
+static V3 friction_rel_velocity(const Contact& c, const double* cp, const V3* v)
+{
+    if (c.type == CT_VV) return sub(v[0], v[1]);
+    if (c.type == CT_EV) return sub(v[0], add(scale(sub(v[2], v[1]), cp[0]), v[1]));
+    if (c.type == CT_EE)
+        return sub(add(scale(sub(v[1], v[0]), cp[0]), v[0]), add(scale(sub(v[3], v[2]), cp[1]), v[2]));
+    return sub(v[0], add(add(v[1], scale(sub(v[2], v[1]), cp[0])), scale(sub(v[3], v[1]), cp[1])));
+}
+
+// One tangential collision's energy, gradient (3n) and Hessian (3n x 3n).
+static void friction_local(const Tangential& T, int64_t i, const Contact& c, const V3* v, double ev, int psd,
+    double* e, double* g, double* H)
+{
+    const double* cp = &T.cp[2 * i];
+    const double* P = &T.P[6 * i];
+    const V3 rv = friction_rel_velocity(c, cp, v);
+    const V3 b0 { P[0], P[1], P[2] }, b1 { P[3], P[4], P[5] };
+    const double u0 = dot(b0, rv), u1 = dot(b1, rv);
+    const double nu = std::sqrt(u0 * u0 + u1 * u1);
+    const double ms = T.mu_s[i], mk = T.mu_k[i];
+    const double scl = c.w * T.N[i];
+    if (e) *e = scl * mu_f0(nu, ms, mk, ev);
+    double gm[4];
+    friction_gamma(c, cp, gm);
+    const int N = 3 * c.n;
+    // T = Gamma^T P: row 3k+d = g_k (P(d,0), P(d,1))
+    double Tm[12][2];
+    for (int k = 0; k < c.n; ++k)
+        for (int d = 0; d < 3; ++d) {
+            Tm[3 * k + d][0] = gm[k] * P[d];
+            Tm[3 * k + d][1] = gm[k] * P[3 + d];
+        }
+    const double f1x = mu_f1_over_x(nu, ms, mk, ev);
+    if (g) {
+        const double s0 = (f1x * u0) * scl, s1 = (f1x * u1) * scl;
+        for (int r = 0; r < N; ++r) g[r] = Tm[r][0] * s0 + Tm[r][1] * s1;
+    }
+    if (!H) return;
+    for (int r = 0; r < N * N; ++r) H[r] = 0;
+    if (nu > ev) {
+        if (psd != 0 && scl <= 0) return;
+        const double cc = scl * f1x / (nu * nu);
+        const double q0 = cc * -u1, q1 = cc * u0;
+        double a[12], b[12];
+        for (int r = 0; r < N; ++r) {
+            a[r] = Tm[r][0] * q0 + Tm[r][1] * q1;
+            b[r] = -u1 * Tm[r][0] + u0 * Tm[r][1];
+        }
+        for (int r = 0; r < N; ++r)
+            for (int s = 0; s < N; ++s) H[r * N + s] = a[r] * b[s];
+    } else if (nu == 0) {
+        if (psd != 0 && scl <= 0) return;
+        const double cc = scl * f1x;
+        for (int r = 0; r < N; ++r)
+            for (int s = 0; s < N; ++s) H[r * N + s] = (cc * Tm[r][0]) * Tm[s][0] + (cc * Tm[r][1]) * Tm[s][1];
+    } else {
+        const double f2 = mu_f2_x_minus_f1_over_x3(nu, ms, mk, ev);
+        double in[4] = { f2 * u0 * u0, f2 * u0 * u1, f2 * u1 * u0, f2 * u1 * u1 };
+        in[0] += f1x;
+        in[3] += f1x;
+        for (double& x : in) x *= scl;
+        project_psd(2, in, psd);
+        for (int r = 0; r < N; ++r) {
+            const double t0 = Tm[r][0] * in[0] + Tm[r][1] * in[2], t1 = Tm[r][0] * in[1] + Tm[r][1] * in[3];
+            for (int s = 0; s < N; ++s) H[r * N + s] = t0 * Tm[s][0] + t1 * Tm[s][1];
+        }
+    }
+}
+
 struct CSR {
     int64_t n = 0;
     std::vector<int64_t> rowptr;
     std::vector<int32_t> col;
     std::vector<double> val;
 };
+
+} // extern "C"
+template <typename LocalFn>
+static CSR* assemble_csr(int64_t n, int64_t nV, int nthreads, LocalFn&& local)
+{
+    struct Trip {
+        int64_t key;
+        double v;
+    };
+    const int nt = std::max(1, nthreads);
+    std::vector<std::vector<Trip>> loc(nt);
+    const int64_t ndof = 3 * nV;
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t i = b; i < e; ++i) {
+            int nv = 0;
+            int vid[4];
+            double Hl[144];
+            local(i, nv, vid, Hl);
+            const int N = 3 * nv;
+            for (int a = 0; a < nv; ++a)
+                for (int bb = 0; bb < nv; ++bb)
+                    for (int k = 0; k < 3; ++k)
+                        for (int l = 0; l < 3; ++l) {
+                            const double val = Hl[(3 * a + k) * N + 3 * bb + l];
+                            if (val != 0)
+                                loc[t].push_back({ (3 * (int64_t)vid[a] + k) * ndof + 3 * (int64_t)vid[bb] + l, val });
+                        }
+        }
+    });
+    std::vector<Trip> all;
+    for (auto& l : loc) all.insert(all.end(), l.begin(), l.end());
+    std::stable_sort(all.begin(), all.end(), [](const Trip& a, const Trip& b) { return a.key < b.key; });
+    CSR* M = new CSR();
+    M->n = ndof;
+    M->rowptr.assign(ndof + 1, 0);
+    for (size_t i = 0; i < all.size();) {
+        size_t j = i;
+        double sum = 0;
+        while (j < all.size() && all[j].key == all[i].key) sum += all[j++].v;
+        M->col.push_back((int32_t)(all[i].key % ndof));
+        M->val.push_back(sum);
+        M->rowptr[all[i].key / ndof + 1]++;
+        i = j;
+    }
+    for (int64_t r = 0; r < ndof; ++r) M->rowptr[r + 1] += M->rowptr[r];
+    return M;
+}
+extern "C" {
+
+// TangentialCollisions::build (tangential_collisions.cpp:60-170): normal
+// force, closest point, tangent basis and blended mu per collision; EE
+// collisions with cross^2 < eps_x are skipped.  dists use the classified
+// (AUTO) type at V, as the tangential collision's compute_distance does.
+void* orc_tangential_build(void* h, const double* V, const int32_t* E, const int32_t* F, double dhat, double kappa,
+    double dmin, int physical, const double* mu_s, const double* mu_k)
+{
+    const Collisions& C = *(const Collisions*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    Tangential* T = new Tangential();
+    Collisions& B = T->base;
+    const int64_t n = C.vv_w.size() + C.ev_w.size() + C.ee_w.size() + C.fv_w.size();
+    const double xh = (2 * dmin + dhat) * dhat;
+    for (int64_t i = 0; i < n; ++i) {
+        Contact c;
+        contact_stencil(C, E, F, i, c);
+        V3 x[4];
+        gather(V, c, x);
+        if (c.type == CT_EE && ee_cross_sqnorm(x[0], x[1], x[2], x[3]) < c.eps) continue;
+        double d2;
+        if (c.type == CT_VV) d2 = point_point_distance(x[0], x[1]);
+        else if (c.type == CT_EV) d2 = point_edge_distance(x[0], x[1], x[2], point_edge_distance_type(x[0], x[1], x[2]));
+        else if (c.type == CT_EE)
+            d2 = edge_edge_distance(x[0], x[1], x[2], x[3], edge_edge_distance_type(x[0], x[1], x[2], x[3]));
+        else d2 = point_triangle_distance(x[0], x[1], x[2], x[3], point_triangle_distance_type(x[0], x[1], x[2], x[3]));
+        // barrier_force_magnitude.cpp:5-15 with the physical scaling
+        double Nf = -kappa * barrier_any(barrier_kind(P), 1, d2 - dmin * dmin, xh) * 2 * std::sqrt(d2);
+        if (P.physical & 1) Nf *= dhat / (barrier_kind(P) == 1 ? 1.0 : xh * xh);
+        double cp[2] = { 0, 0 };
+        V3 b0, b1;
+        double ms, mk;
+        auto blend = [](double a, double b) { return (a + b) / 2; };
+        const int* v = c.vid;
+        if (c.type == CT_VV) {
+            pp_basis(x[0], x[1], b0, b1);
+            ms = blend(mu_s[v[0]], mu_s[v[1]]);
+            mk = blend(mu_k[v[0]], mu_k[v[1]]);
+        } else if (c.type == CT_EV) {
+            const V3 e = sub(x[2], x[1]);
+            cp[0] = dot(sub(x[0], x[1]), e) / sqnorm(e);
+            pe_basis(x[0], x[1], x[2], b0, b1);
+            ms = blend((mu_s[v[2]] - mu_s[v[1]]) * cp[0] + mu_s[v[1]], mu_s[v[0]]);
+            mk = blend((mu_k[v[2]] - mu_k[v[1]]) * cp[0] + mu_k[v[1]], mu_k[v[0]]);
+        } else if (c.type == CT_EE) {
+            ldlt2_solve(sub(x[1], x[0]), scale(sub(x[3], x[2]), -1.0), sub(x[2], x[0]), cp[0], cp[1]);
+            ee_basis(x[0], x[1], x[2], x[3], b0, b1);
+            ms = blend((mu_s[v[1]] - mu_s[v[0]]) * cp[0] + mu_s[v[0]], (mu_s[v[3]] - mu_s[v[2]]) * cp[1] + mu_s[v[2]]);
+            mk = blend((mu_k[v[1]] - mu_k[v[0]]) * cp[0] + mu_k[v[0]], (mu_k[v[3]] - mu_k[v[2]]) * cp[1] + mu_k[v[2]]);
+        } else {
+            ldlt2_solve(sub(x[2], x[1]), sub(x[3], x[1]), sub(x[0], x[1]), cp[0], cp[1]);
+            pt_basis(x[0], x[1], x[2], x[3], b0, b1);
+            ms = blend(mu_s[v[1]] + cp[0] * (mu_s[v[2]] - mu_s[v[1]]) + cp[1] * (mu_s[v[3]] - mu_s[v[1]]), mu_s[v[0]]);
+            mk = blend(mu_k[v[1]] + cp[0] * (mu_k[v[2]] - mu_k[v[1]]) + cp[1] * (mu_k[v[3]] - mu_k[v[1]]), mu_k[v[0]]);
+        }
+        // stencil record, in the normal set's order
+        const int64_t nvv = C.vv_w.size(), nev = C.ev_w.size(), nee = C.ee_w.size();
+        if (c.type == CT_VV) {
+            B.vv.push_back(C.vv[2 * i]);
+            B.vv.push_back(C.vv[2 * i + 1]);
+            B.vv_w.push_back(c.w);
+        } else if (c.type == CT_EV) {
+            const int64_t j = i - nvv;
+            B.ev.push_back(C.ev[2 * j]);
+            B.ev.push_back(C.ev[2 * j + 1]);
+            B.ev_w.push_back(c.w);
+        } else if (c.type == CT_EE) {
+            const int64_t j = i - nvv - nev;
+            B.ee.push_back(C.ee[2 * j]);
+            B.ee.push_back(C.ee[2 * j + 1]);
+            B.ee_w.push_back(c.w);
+            B.ee_eps.push_back(C.ee_eps[j]);
+            B.ee_dtype.push_back(C.ee_dtype[j]);
+        } else {
+            const int64_t j = i - nvv - nev - nee;
+            B.fv.push_back(C.fv[2 * j]);
+            B.fv.push_back(C.fv[2 * j + 1]);
+            B.fv_w.push_back(c.w);
+        }
+        T->N.push_back(Nf);
+        T->cp.push_back(cp[0]);
+        T->cp.push_back(cp[1]);
+        for (V3 b : { b0, b1 }) {
+            T->P.push_back(b.x);
+            T->P.push_back(b.y);
+            T->P.push_back(b.z);
+        }
+        T->mu_s.push_back(ms);
+        T->mu_k.push_back(mk);
+    }
+    return T;
+}
+
+// The records are stored per type; reorder the per-collision arrays (built
+// in normal-set order, which is also vv | ev | ee | fv) - nothing to do.
+void orc_tangential_counts(void* h, int64_t* out)
+{
+    const Tangential* T = (const Tangential*)h;
+    out[0] = T->base.vv_w.size();
+    out[1] = T->base.ev_w.size();
+    out[2] = T->base.ee_w.size();
+    out[3] = T->base.fv_w.size();
+}
+void orc_tangential_get(void* h, int32_t* vv, int32_t* ev, int32_t* ee, int32_t* fv, double* w, double* N, double* cp,
+    double* P, double* mu_s, double* mu_k)
+{
+    const Tangential* T = (const Tangential*)h;
+    const Collisions& B = T->base;
+    std::copy(B.vv.begin(), B.vv.end(), vv);
+    std::copy(B.ev.begin(), B.ev.end(), ev);
+    std::copy(B.ee.begin(), B.ee.end(), ee);
+    std::copy(B.fv.begin(), B.fv.end(), fv);
+    double* o = w;
+    for (auto* a : { &B.vv_w, &B.ev_w, &B.ee_w, &B.fv_w }) o = std::copy(a->begin(), a->end(), o);
+    std::copy(T->N.begin(), T->N.end(), N);
+    std::copy(T->cp.begin(), T->cp.end(), cp);
+    std::copy(T->P.begin(), T->P.end(), P);
+    std::copy(T->mu_s.begin(), T->mu_s.end(), mu_s);
+    std::copy(T->mu_k.begin(), T->mu_k.end(), mu_k);
+}
+void orc_tangential_free(void* h) { delete (Tangential*)h; }
+
+static int64_t tangential_size(const Tangential& T)
+{
+    return T.base.vv_w.size() + T.base.ev_w.size() + T.base.ee_w.size() + T.base.fv_w.size();
+}
+
+double orc_friction_energy(void* h, const double* U, const int32_t* E, const int32_t* F, double eps_v, int nthreads)
+{
+    const Tangential& T = *(const Tangential*)h;
+    const int64_t n = tangential_size(T);
+    const int nt = std::max(1, nthreads);
+    std::vector<double> part(nt, 0.0);
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        double sum = 0;
+        for (int64_t i = b; i < e; ++i) {
+            Contact c;
+            contact_stencil(T.base, E, F, i, c);
+            V3 v[4];
+            gather(U, c, v);
+            double en;
+            friction_local(T, i, c, v, eps_v, 0, &en, nullptr, nullptr);
+            sum += en;
+        }
+        part[t] += sum;
+    });
+    double sum = 0;
+    for (double x : part) sum += x;
+    return sum;
+}
+
+void orc_friction_gradient(void* h, const double* U, int64_t nV, const int32_t* E, const int32_t* F, double eps_v,
+    int nthreads, double* grad)
+{
+    const Tangential& T = *(const Tangential*)h;
+    const int64_t n = tangential_size(T);
+    const int nt = std::max(1, nthreads);
+    std::vector<std::vector<double>> loc(nt, std::vector<double>(3 * nV, 0.0));
+    parallel_for(n, nt, [&](int64_t b, int64_t e, int t) {
+        for (int64_t i = b; i < e; ++i) {
+            Contact c;
+            contact_stencil(T.base, E, F, i, c);
+            V3 v[4];
+            gather(U, c, v);
+            double g[12];
+            friction_local(T, i, c, v, eps_v, 0, nullptr, g, nullptr);
+            for (int k = 0; k < c.n; ++k)
+                for (int d = 0; d < 3; ++d) loc[t][3 * c.vid[k] + d] += g[3 * k + d];
+        }
+    });
+    for (int64_t i = 0; i < 3 * nV; ++i) {
+        double sum = 0;
+        for (int t = 0; t < nt; ++t) sum += loc[t][i];
+        grad[i] = sum;
+    }
+}
+
+void* orc_friction_hessian(void* h, const double* U, int64_t nV, const int32_t* E, const int32_t* F, double eps_v,
+    int psd, int nthreads)
+{
+    const Tangential& T = *(const Tangential*)h;
+    return assemble_csr(tangential_size(T), nV, nthreads, [&](int64_t i, int& nv, int* vid, double* Hl) {
+        Contact c;
+        contact_stencil(T.base, E, F, i, c);
+        V3 v[4];
+        gather(U, c, v);
+        friction_local(T, i, c, v, eps_v, psd, nullptr, nullptr, Hl);
+        nv = c.n;
+        for (int k = 0; k < c.n; ++k) vid[k] = c.vid[k];
+    });
+}
+
+// scalar smooth-friction functions for derivative checks
+double orc_friction_mu(int which, double y, double mu_s, double mu_k, double eps_v)
+{
+    switch (which) {
+    case 0: return mu_f0(y, mu_s, mu_k, eps_v);
+    case 1: return mu_f1_over_x(y, mu_s, mu_k, eps_v);
+    case 2: return mu_f2_x_minus_f1_over_x3(y, mu_s, mu_k, eps_v);
+    default: return smooth_mu_value(y, mu_s, mu_k, eps_v);
+    }
+}
 
 // Local Hessians → triplets (skip exact zeros, local_to_global.hpp:291) →
 // duplicates summed → compressed rows.

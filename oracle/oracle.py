@@ -82,6 +82,18 @@ def lib():
         L.orc_ccd_candidates_get.argtypes = [vp, P, P]
         L.orc_collision_free_stepsize.restype = d
         L.orc_collision_free_stepsize.argtypes = [P, P, i64, P, i64, P, i64, d, d, C.c_long, d, i32, P]
+        L.orc_tangential_build.restype = vp
+        L.orc_tangential_build.argtypes = [vp, P, P, P, d, d, d, i32, P, P]
+        L.orc_tangential_counts.argtypes = [vp, P]
+        L.orc_tangential_get.argtypes = [vp] + [P] * 10
+        L.orc_tangential_free.argtypes = [vp]
+        L.orc_friction_energy.restype = d
+        L.orc_friction_energy.argtypes = [vp, P, P, P, d, i32]
+        L.orc_friction_gradient.argtypes = [vp, P, i64, P, P, d, i32, P]
+        L.orc_friction_hessian.restype = vp
+        L.orc_friction_hessian.argtypes = [vp, P, i64, P, P, d, i32, i32]
+        L.orc_friction_mu.restype = d
+        L.orc_friction_mu.argtypes = [i32, d, d, d, d]
         _lib = L
     return _lib
 
@@ -370,3 +382,80 @@ def has_intersections_bruteforce(V, E, F):
                 return True
     return False
 
+
+
+# --- friction -----------------------------------------------------------------
+
+class Tangential:
+    """TangentialCollisions built by the oracle: stencils (vv, ev, ee, fv),
+    and per collision (vv | ev | ee | fv order) w, N, cp (2), P (3x2 as b0, b1),
+    mu_s, mu_k."""
+
+    def __init__(self, handle):
+        self.h = handle
+        L = lib()
+        cnt = np.zeros(4, np.int64)
+        L.orc_tangential_counts(self.h, _p(cnt))
+        nvv, nev, nee, nfv = (int(c) for c in cnt)
+        n = nvv + nev + nee + nfv
+        self.vv = np.zeros((nvv, 2), np.int32)
+        self.ev = np.zeros((nev, 2), np.int32)
+        self.ee = np.zeros((nee, 2), np.int32)
+        self.fv = np.zeros((nfv, 2), np.int32)
+        self.w, self.N = np.zeros(n), np.zeros(n)
+        self.cp, self.P = np.zeros((n, 2)), np.zeros((n, 6))
+        self.mu_s, self.mu_k = np.zeros(n), np.zeros(n)
+        L.orc_tangential_get(self.h, _p(self.vv), _p(self.ev), _p(self.ee), _p(self.fv), _p(self.w), _p(self.N),
+                             _p(self.cp), _p(self.P), _p(self.mu_s), _p(self.mu_k))
+
+    def __len__(self):
+        return len(self.w)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_tangential_free(self.h)
+            self.h = None
+
+
+def tangential_build(col, V, E, F, dhat, kappa, mu_s, mu_k=None, dmin=0.0, physical=0):
+    V, E, F = _f64(V), _i32(E), _i32(F)
+    nV = V.shape[0]
+    ms = _f64(np.broadcast_to(np.asarray(mu_s, np.float64), (nV,)))
+    mk = _f64(np.broadcast_to(np.asarray(mu_s if mu_k is None else mu_k, np.float64), (nV,)))
+    t = Tangential(lib().orc_tangential_build(col.h, _p(V), _p(E), _p(F), float(dhat), float(kappa), float(dmin),
+                                              int(physical), _p(ms), _p(mk)))
+    t._keep = (ms, mk)
+    return t
+
+
+def friction_energy(t, U, E, F, eps_v, nthreads=None):
+    U, E, F = _f64(U), _i32(E), _i32(F)
+    return lib().orc_friction_energy(t.h, _p(U), _p(E), _p(F), float(eps_v), int(nthreads or os.cpu_count() or 1))
+
+
+def friction_gradient(t, U, E, F, eps_v, nthreads=None):
+    U, E, F = _f64(U), _i32(E), _i32(F)
+    g = np.zeros(U.size)
+    lib().orc_friction_gradient(t.h, _p(U), U.shape[0], _p(E), _p(F), float(eps_v),
+                                int(nthreads or os.cpu_count() or 1), _p(g))
+    return g
+
+
+def friction_hessian(t, U, E, F, eps_v, psd="none", nthreads=None):
+    """(rowptr, col, val) of the friction Hessian."""
+    U, E, F = _f64(U), _i32(E), _i32(F)
+    h = lib().orc_friction_hessian(t.h, _p(U), U.shape[0], _p(E), _p(F), float(eps_v), PSD[psd],
+                                   int(nthreads or os.cpu_count() or 1))
+    L = lib()
+    nnz = L.orc_csr_nnz(h)
+    rp = np.zeros(U.size + 1, np.int64)
+    ci = np.zeros(nnz, np.int32)
+    va = np.zeros(nnz)
+    L.orc_csr_get(h, _p(rp), _p(ci), _p(va))
+    L.orc_csr_free(h)
+    return rp, ci, va
+
+
+def friction_mu(which, y, mu_s, mu_k, eps_v):
+    """0: mu f0, 1: mu f1 / y, 2: (mu f1)' y - mu f1) / y^3, 3: mu(y)."""
+    return lib().orc_friction_mu(int(which), float(y), float(mu_s), float(mu_k), float(eps_v))

@@ -635,3 +635,109 @@ def test_improved_max_approx_on_sheets(oracle_mod):
     np.testing.assert_array_equal(imp.fv, ipc.fv)
     total = lambda c: sum(float(np.sum(w)) for w in (c.vv_w, c.ev_w, c.ee_w, c.fv_w))
     assert total(imp) <= total(ipc)
+
+
+# --- friction ---------------------------------------------------------------------
+
+@pytest.mark.parametrize("ms,mk", [(0.5, 0.5), (0.8, 0.4), (0.3, 0.6)])
+def test_smooth_mu_derivatives(oracle_mod, ms, mk):
+    """friction/smooth_mu.cpp: d/dy (mu f0) = (mu f1/y) y and
+    d/dy (mu f1) = ((mu f1)' y - mu f1)/y^3 * y^3 + mu f1 / y, over the static,
+    transition and kinetic ranges (friction/test_smooth_mu.cpp style)."""
+    ev = 1e-3
+    for y in np.linspace(0.05 * ev, 2 * ev, 23):
+        if abs(y - ev) < 0.02 * ev or abs(y - 0.5 * ev) < 0.02 * ev:
+            continue
+        h = 1e-7 * ev
+        f0 = lambda t: oracle_mod.friction_mu(0, t, ms, mk, ev)
+        f1 = lambda t: oracle_mod.friction_mu(1, t, ms, mk, ev) * t
+        d0 = (f0(y + h) - f0(y - h)) / (2 * h)
+        assert d0 == pytest.approx(f1(y), rel=1e-6)
+        d1 = (f1(y + h) - f1(y - h)) / (2 * h)
+        f2 = oracle_mod.friction_mu(2, y, ms, mk, ev) * y ** 3 + f1(y)
+        assert d1 == pytest.approx(f2 / y, rel=1e-5, abs=1e-9 / ev)
+    # mu(y): mu_s at rest, mu_k beyond eps_v
+    assert oracle_mod.friction_mu(3, 0.0, ms, mk, ev) == ms
+    assert oracle_mod.friction_mu(3, 2 * ev, ms, mk, ev) == mk
+
+
+def _friction_case(oracle_mod, seed=3):
+    from ipctk_gb300 import scenes
+    sc = scenes.two_sheet(side=10, seed=seed)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    col = oracle_mod.build_collisions(V, E, F, sc["dhat"])
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mu_s = rng.uniform(0.3, 0.6, len(V))
+    mu_k = mu_s * rng.uniform(0.6, 1.0, len(V))
+    t = oracle_mod.tangential_build(col, V, E, F, sc["dhat"], sc["kappa"], mu_s, mu_k)
+    return sc, V, E, F, col, t, rng
+
+
+def test_tangential_build_properties(oracle_mod):
+    """Orthonormal tangent bases orthogonal to the contact normal direction,
+    positive normal forces, mu between the per-vertex extremes; one record per
+    normal collision but the near-parallel edge-edge ones."""
+    sc, V, E, F, col, t, _ = _friction_case(oracle_mod)
+    assert len(t) > 0 and len(t.vv) == len(col.vv) and len(t.fv) == len(col.fv) and len(t.ev) == len(col.ev)
+    assert len(t.ee) <= len(col.ee)
+    B = t.P.reshape(-1, 2, 3)
+    np.testing.assert_allclose(np.einsum("nij,nkj->nik", B, B), np.broadcast_to(np.eye(2), (len(t), 2, 2)),
+                               atol=1e-12)
+    assert np.all(t.N > 0)
+    assert np.all((t.mu_s >= 0.3 - 1e-12) & (t.mu_s <= 0.6 + 1e-12))
+    # face-vertex: the basis spans the triangle plane
+    nvv, nev, nee = len(t.vv), len(t.ev), len(t.ee)
+    for j, (f, v) in enumerate(t.fv[:50]):
+        a, b, c = V[F[f]]
+        n = np.cross(b - a, c - a)
+        i = nvv + nev + nee + j
+        assert abs(B[i] @ n).max() <= 1e-12 * np.linalg.norm(n)
+
+
+@pytest.mark.parametrize("regime", ["static", "mixed", "kinetic"])
+def test_friction_potential_derivatives_fd(oracle_mod, regime):
+    """FrictionPotential gradient and Hessian against central differences of
+    the energy and gradient (tangential_potential.cpp:156-331)."""
+    sc, V, E, F, col, t, rng = _friction_case(oracle_mod)
+    ev = 1e-3
+    scale = {"static": 0.2 * ev, "mixed": 1.0 * ev, "kinetic": 20 * ev}[regime]
+    U = rng.uniform(-1, 1, V.shape) * scale
+    e = oracle_mod.friction_energy(t, U, E, F, ev)
+    g = oracle_mod.friction_gradient(t, U, E, F, ev)
+    assert e > 0 and np.linalg.norm(g) > 0
+    idx = np.argsort(-np.abs(g))[:8]
+    h = 1e-6 * scale
+    for k in idx:
+        d = np.zeros(U.size)
+        d[k] = h
+        fd = (oracle_mod.friction_energy(t, U + d.reshape(U.shape), E, F, ev)
+              - oracle_mod.friction_energy(t, U - d.reshape(U.shape), E, F, ev)) / (2 * h)
+        assert fd == pytest.approx(g[k], rel=1e-5, abs=1e-9 * np.abs(g).max())
+    import scipy.sparse as sps
+    rp, ci, va = oracle_mod.friction_hessian(t, U, E, F, ev)
+    H = sps.csr_matrix((va, ci, rp), shape=(U.size, U.size))
+    for k in idx[:4]:
+        d = np.zeros(U.size)
+        d[k] = h
+        fd = (oracle_mod.friction_gradient(t, U + d.reshape(U.shape), E, F, ev)
+              - oracle_mod.friction_gradient(t, U - d.reshape(U.shape), E, F, ev)) / (2 * h)
+        col_k = H[:, k].toarray().ravel()
+        assert np.linalg.norm(fd - col_k) <= 1e-4 * np.linalg.norm(col_k) + 1e-9 * abs(va).max()
+    # the projected Hessian is positive semi-definite
+    rp, ci, va = oracle_mod.friction_hessian(t, U, E, F, ev, psd="clamp")
+    Hp = sps.csr_matrix((va, ci, rp), shape=(U.size, U.size)).toarray()
+    used = np.unique(np.concatenate([t.vv.ravel(), t.ev[:, 1], t.fv[:, 1]]))
+    assert np.linalg.eigvalsh(Hp).min() >= -1e-9 * abs(Hp).max()
+
+
+def test_friction_energy_identities(oracle_mod):
+    """Zero velocity: energy = sum w N mu_s eps_v / 3 (f0(0) = eps_v / 3,
+    mu(0) = mu_s) for mu_s = mu_k; rigid translation in the normal direction
+    gives no tangential slip."""
+    sc, V, E, F, col, t, _ = _friction_case(oracle_mod)
+    ev = 1e-3
+    same = oracle_mod.tangential_build(col, V, E, F, sc["dhat"], sc["kappa"], 0.4)
+    e0 = oracle_mod.friction_energy(same, np.zeros_like(V), E, F, ev)
+    assert e0 == pytest.approx(float(np.sum(same.w * same.N)) * 0.4 * ev / 3, rel=1e-12)
+    g0 = oracle_mod.friction_gradient(same, np.zeros_like(V), E, F, ev)
+    assert np.abs(g0).max() == 0
