@@ -9,7 +9,7 @@ PSD-projected (CLAMP) Hessian with CSR assembly over the prebuilt collision
 set, exactly the three reference calls of one Newton iteration.
 
     value   contacts/s with positions resident in HBM (device pointers)
-    e2e     the same calls through the public API with host (pinned) buffers:
+    e2e     the same work through the public API with host buffers (one fused call):
             positions copied in, energy / gradient / CSR Hessian copied out
             inside the timed region
     roofline  the dominant kernel's algorithmic bytes per launch over its
@@ -390,6 +390,47 @@ def mixed_leg(dev, warmup=2, steps=5):
     return out
 
 
+def friction_leg(dev, warmup=2, steps=5, eps_v=1e-3):
+    """Friction on the sphere pack (512 icospheres, seed 0): TangentialCollisions
+    build from the collision set at the same positions (mu_s 0.5, mu_k 0.4) and
+    FrictionPotential(eps_v = 1e-3) energy + gradient + CLAMP Hessian at
+    device-resident velocities drawn in [-eps_v, eps_v] (a mix of static and
+    sliding contacts), timed on the device."""
+    import torch
+    import ipctk_gb300 as ipctk
+    from ipctk_gb300 import scenes
+    sc = scenes.sphere_pack()
+    mesh = ipctk.CollisionMesh(sc["V"], sc["E"], sc["F"])
+    Vd = torch.from_numpy(sc["V"]).to(dev)
+    col = ipctk.NormalCollisions()
+    col.build(mesh, Vd, sc["dhat"])
+    B = ipctk.BarrierPotential(sc["dhat"], sc["kappa"])
+    tc = ipctk.TangentialCollisions()
+    rng = np.random.Generator(np.random.PCG64(5))
+    Ud = torch.from_numpy(rng.uniform(-eps_v, eps_v, sc["V"].shape)).to(dev)
+    D = ipctk.FrictionPotential(eps_v)
+    CL = ipctk.PSDProjectionMethod.CLAMP
+    tb, te = [], []
+    for i in range(warmup + steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tc.build(mesh, Vd, col, B, 0.5, 0.4)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e = D(tc, mesh, Ud)
+        g = D.gradient(tc, mesh, Ud)
+        H = D.hessian(tc, mesh, Ud, CL)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if i >= warmup:
+            tb.append(t1 - t0)
+            te.append(t2 - t1)
+    n = len(tc)
+    return {"workload": "sphere pack 512 x 642 verts, eps_v 1e-3, mu_s 0.5, mu_k 0.4", "tangential_collisions": n,
+            "egh": {"value": n / statistics.median(te), "unit": UNIT, "ms": 1000 * statistics.median(te)},
+            "build_ms": 1000 * statistics.median(tb), "hessian_nnz": int(H.nnz), "energy": float(e)}
+
+
 def served_leg(dev, seed=4):
     """Served request stream: 64 resident scenes drawn from the batch size
     distribution plus 4 sphere packs; requests alternate barrier (collision
@@ -552,18 +593,28 @@ def run_gb300(args, rank, world):
             fused.append(time.perf_counter() - t0)
     fused_ms = 1000 * statistics.median(fused)
 
-    # end to end through the public API with pinned host buffers
+    # end to end through the public API with pinned host positions and host
+    # (numpy / scipy) results: one fused energy + gradient + Hessian call per
+    # step (positions staged once); the three separate calls of the
+    # reference's API are timed beside it
     Vh = torch.from_numpy(V).pin_memory().numpy()
-    e2e_times = []
-    for i in range(max(2, args.warmup // 2) + args.steps):
+    nw = max(2, args.warmup // 2)
+    e2e_times, sep_times = [], []
+    for i in range(nw + args.steps):
+        t0 = time.perf_counter()
+        e, g, H = B.energy_gradient_hessian(col, mesh, Vh, CLAMP)
+        if i >= nw:
+            e2e_times.append(time.perf_counter() - t0)
+    for i in range(nw + args.steps):
         t0 = time.perf_counter()
         e = B(col, mesh, Vh)
         g = B.gradient(col, mesh, Vh)
         H = B.hessian(col, mesh, Vh, CLAMP)
-        if i >= max(2, args.warmup // 2):
-            e2e_times.append(time.perf_counter() - t0)
+        if i >= nw:
+            sep_times.append(time.perf_counter() - t0)
     e2e_ms = 1000 * statistics.median(e2e_times)
-    h2d = 3 * V.nbytes
+    sep_ms = 1000 * statistics.median(sep_times)
+    h2d = V.nbytes
     d2h = 8 + g.nbytes + H.indptr.nbytes + H.indices.nbytes + H.data.nbytes
 
     # CCD and collision-set build (device-resident inputs)
@@ -585,6 +636,7 @@ def run_gb300(args, rank, world):
     batch = None
     served = None
     mixed = None
+    friction = None
     if not args.no_batch:
         del mesh, col, Vd, V1d, flush
         batch = batch_leg(dev)
@@ -593,6 +645,8 @@ def run_gb300(args, rank, world):
         served = served_leg(dev)
         gc.collect()
         mixed = mixed_leg(dev)
+        gc.collect()
+        friction = friction_leg(dev)
     cpu = None
     ccd_cpu = None
     if not args.no_cpu_baseline:
@@ -612,7 +666,11 @@ def run_gb300(args, rank, world):
         "roofline": roof, "kernel_share": step_share,
         "cpu_baseline": cpu,
         "e2e": {"value": C / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+                "call": "BarrierPotential.energy_gradient_hessian (one fused C-ABI call)"},
+        "e2e_separate_calls": {"value": C / (sep_ms / 1000.0), "unit": UNIT, "ms_per_step": sep_ms,
+                               "h2d_bytes_per_step": int(3 * V.nbytes), "d2h_bytes_per_step": int(d2h),
+                               "call": "energy, gradient and hessian calls (positions staged three times)"},
         "gpu_launches": int(launches), "gpu_launches_per_step": launches / args.steps,
         "clocks": clk,
         "fused_egh": {"value": C / (fused_ms / 1000.0), "unit": UNIT, "ms_per_step": fused_ms},
@@ -622,6 +680,7 @@ def run_gb300(args, rank, world):
         "batch": batch,
         "served": served,
         "mixed_precision": mixed,
+        "friction": friction,
     }
     print(json.dumps(line), flush=True)
 

@@ -290,6 +290,10 @@ int ipcg_barrier_energy_noalloc(const double* vertices, int64_t num_vertices,
 int ipcg_csr_shape(const ipcg_csr* csr, int64_t* rows, int64_t* nnz);
 /* row_ptr: rows+1 int64, col: nnz int32, val: nnz float64 (host or device) */
 int ipcg_csr_get(const ipcg_csr* csr, int64_t* row_ptr, int32_t* col, double* val);
+/* Same with 32-bit row pointers (converted on the device), for callers whose
+ * sparse format keeps both index arrays 32-bit (scipy, Eigen with int
+ * StorageIndex); fails when nnz >= 2^31. */
+int ipcg_csr_get_int32(const ipcg_csr* hessian, int32_t* row_ptr, int32_t* col, double* val);
 int ipcg_csr_destroy(ipcg_csr* csr);
 
 /* ---------------------------------------------------------------------- */

@@ -605,12 +605,12 @@ static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const d
             a.scene_kappa = stiffness;
         }
         double* gdev = nullptr;
-        DBuf<double> gtmp;
         if (gradient) {
             if (is_device_ptr(gradient)) gdev = gradient;
             else {
-                gtmp.reserve(3 * m->nV + 1);
-                gdev = gtmp.p;
+                // a host gradient is computed in the mesh's staging buffer
+                m->grad_stage.reserve(3 * m->nV + 1);
+                gdev = m->grad_stage.p;
             }
         }
         ipcg_csr* H = nullptr;
@@ -689,22 +689,16 @@ static int gauss_newton_call(const ipcg_collisions* c, const ipcg_mesh* mesh, co
         const size_t bytes = sizeof(double) * 3 * m->nV;
         if (diag) {
             double* ddev = diag;
-            DBuf<double> dtmp;
             if (!is_device_ptr(diag)) {
-                dtmp.reserve(3 * m->nV + 1);
-                ddev = dtmp.p;
+                m->grad_stage.reserve(3 * m->nV + 1);
+                ddev = m->grad_stage.p;
             }
             barrier_gauss_newton(c, m, dV, a, ddev, nullptr, nullptr);
             if (ddev != diag) IPCG_CUDA(cudaMemcpyAsync(diag, ddev, bytes, cudaMemcpyDeviceToHost, m->stream));
             IPCG_CUDA(cudaStreamSynchronize(m->stream));
         } else {
-            const double* pdev = p;
-            DBuf<double> ptmp;
-            if (!is_device_ptr(p)) {
-                ptmp.reserve(3 * m->nV + 1);
-                IPCG_CUDA(cudaMemcpyAsync(ptmp.p, p, bytes, cudaMemcpyHostToDevice, m->stream));
-                pdev = ptmp.p;
-            }
+            // a host p is staged in the mesh's second position buffer
+            const double* pdev = stage_positions(m, p, m->V1);
             barrier_gauss_newton(c, m, dV, a, nullptr, pdev, qf);
         }
     });
@@ -814,12 +808,12 @@ int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, con
         const double* dU = stage_positions(m, U, m->V0);
         const FrictionView f { t->N.p, t->cp.p, t->P.p, t->mu_s.p, t->mu_k.p, eps_v };
         double* gdev = nullptr;
-        DBuf<double> gtmp;
         if (gradient) {
             if (is_device_ptr(gradient)) gdev = gradient;
             else {
-                gtmp.reserve(3 * m->nV + 1);
-                gdev = gtmp.p;
+                // a host gradient is computed in the mesh's staging buffer
+                m->grad_stage.reserve(3 * m->nV + 1);
+                gdev = m->grad_stage.p;
             }
         }
         ipcg_csr* H = hessian ? new ipcg_csr() : nullptr;
@@ -844,6 +838,34 @@ int ipcg_csr_shape(const ipcg_csr* h, int64_t* rows, int64_t* nnz)
         require(h != nullptr, "NULL argument");
         if (rows) *rows = h->rows;
         if (nnz) *nnz = h->nnz;
+    });
+}
+
+namespace {
+__global__ void k_row_ptr_i32(const int64_t* __restrict__ in, int64_t n, int32_t* __restrict__ out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (int32_t)in[i];
+}
+} // namespace
+
+int ipcg_csr_get_int32(const ipcg_csr* h, int32_t* row_ptr, int32_t* col, double* val)
+{
+    return guarded([&] {
+        require(h != nullptr, "NULL argument");
+        require(h->nnz < INT32_MAX, "matrix too large for 32-bit row pointers: use ipcg_csr_get");
+        cudaStream_t s = 0;
+        if (row_ptr) {
+            PBuf<int32_t> tmp; // stream-ordered pool memory, freed after the copy
+            tmp.reserve(h->rows + 1, s);
+            k_row_ptr_i32<<<(int)((h->rows + 1 + 255) / 256), 256, 0, s>>>(h->row_ptr.p, h->rows + 1, tmp.p);
+            IPCG_CUDA(cudaGetLastError());
+            copy_out(row_ptr, tmp.p, sizeof(int32_t) * (h->rows + 1), s);
+            IPCG_CUDA(cudaStreamSynchronize(s));
+        }
+        copy_out(col, h->col.p, sizeof(int32_t) * h->nnz, s);
+        copy_out(val, h->val.p, sizeof(double) * h->nnz, s);
+        IPCG_CUDA(cudaStreamSynchronize(s));
     });
 }
 

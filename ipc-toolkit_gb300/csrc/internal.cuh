@@ -196,6 +196,7 @@ struct ipcg_mesh {
     ipcg::DBuf<double> edge_area;
     // work space shared by the calls on this mesh
     ipcg::DBuf<double> V0, V1;       // device copies of host position inputs
+    ipcg::DBuf<double> grad_stage;   // device gradient for a host gradient output
     ipcg::DBuf<double> bounds;       // mesh AABB scratch
     ipcg::LBVH ebvh, fbvh;
     ipcg::DBuf<int2> cand;           // broad-phase candidates (EE then FV)

@@ -99,6 +99,7 @@ def _load():
         "ipcg_tangential_counts": (i32, [P, P]),
         "ipcg_tangential_get": (i32, [P] + [P] * 10),
         "ipcg_friction_potential": (i32, [P, P, P, d, i32, P, P, PP]),
+        "ipcg_csr_get_int32": (i32, [P, P, P, P]),
         "ipcg_candidates_create": (i32, [PP]),
         "ipcg_candidates_destroy": (i32, [P]),
         "ipcg_candidates_build": (i32, [P, P, P, d]),
@@ -528,13 +529,21 @@ def _csr_to_scipy(h, ndof):
     L = _load()
     rows, nnz = C.c_int64(), C.c_int64()
     _check(L.ipcg_csr_shape(h, C.byref(rows), C.byref(nnz)))
-    rp = np.zeros(rows.value + 1, np.int64)
-    ci = np.zeros(nnz.value, np.int32)
-    va = np.zeros(nnz.value)
-    _check(L.ipcg_csr_get(h, _ptr(rp), _ptr(ci), _ptr(va)))
-    _check(L.ipcg_csr_destroy(h))
+    # both index arrays 32-bit when they fit, so scipy keeps them as given
+    # (mixed widths make it copy and convert); outputs are fully written
+    small = nnz.value < 2 ** 31 - 1
+    rp = np.empty(rows.value + 1, np.int32 if small else np.int64)
+    ci = np.empty(nnz.value, np.int32)
+    va = np.empty(nnz.value)
+    try:
+        if small:
+            _check(L.ipcg_csr_get_int32(h, _ptr(rp), _ptr(ci), _ptr(va)))
+        else:
+            _check(L.ipcg_csr_get(h, _ptr(rp), _ptr(ci), _ptr(va)))
+    finally:
+        _check(L.ipcg_csr_destroy(h))
     # symmetric: CSR arrays are also the CSC arrays (Eigen ColMajor)
-    return sp.csc_matrix((va, ci, rp), shape=(ndof, ndof))
+    return sp.csc_matrix((va, ci, rp), shape=(ndof, ndof), copy=False)
 
 
 class Barrier:
@@ -675,7 +684,7 @@ class BarrierPotential:
             import torch
             g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
         else:
-            g = np.zeros(V.size)
+            g = np.empty(V.size)
         _check(_load().ipcg_barrier_gauss_newton_hessian_diagonal(collisions._h, mesh._h, _ptr(V), self.dhat,
                                                                   self.stiffness, self._options, _ptr(g)))
         return g
@@ -703,7 +712,7 @@ class BarrierPotential:
             import torch
             g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
         else:
-            g = np.zeros(V.size)
+            g = np.empty(V.size)
         _check(_load().ipcg_barrier_gradient(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
                                              self._options, _ptr(g)))
         return g
@@ -736,7 +745,7 @@ class BarrierPotential:
             import torch
             g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
         else:
-            g = np.zeros(3 * mesh.num_vertices)
+            g = np.empty(3 * mesh.num_vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_energy_gradient_hessian(
             collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, self._options,
@@ -747,7 +756,7 @@ class BarrierPotential:
         """Energy, gradient and Hessian from one call."""
         V = _as_f64(vertices)
         e = np.zeros(1)
-        g = np.zeros(3 * mesh.num_vertices)
+        g = np.empty(3 * mesh.num_vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_energy_gradient_hessian(
             collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness, self._options,
@@ -1024,7 +1033,7 @@ class FrictionPotential:
             import torch
             g = torch.empty(U.numel(), dtype=torch.float64, device=U.device)
         else:
-            g = np.zeros(3 * mesh.num_vertices)
+            g = np.empty(3 * mesh.num_vertices)
         self._call(collisions, mesh, U, 0, g=g)
         return g
 
