@@ -393,7 +393,7 @@ def mixed_leg(dev, warmup=2, steps=5):
 def friction_leg(dev, warmup=2, steps=5, eps_v=1e-3):
     """Friction on the sphere pack (512 icospheres, seed 0): TangentialCollisions
     build from the collision set at the same positions (mu_s 0.5, mu_k 0.4) and
-    FrictionPotential(eps_v = 1e-3) energy + gradient + CLAMP Hessian at
+    FrictionPotential(eps_v = 1e-3) energy + gradient + CLAMP Hessian (one call) at
     device-resident velocities drawn in [-eps_v, eps_v] (a mix of static and
     sliding contacts), timed on the device."""
     import torch
@@ -417,9 +417,7 @@ def friction_leg(dev, warmup=2, steps=5, eps_v=1e-3):
         tc.build(mesh, Vd, col, B, 0.5, 0.4)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        e = D(tc, mesh, Ud)
-        g = D.gradient(tc, mesh, Ud)
-        H = D.hessian(tc, mesh, Ud, CL)
+        e, g, H = D.energy_gradient_hessian(tc, mesh, Ud, CL)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         if i >= warmup:

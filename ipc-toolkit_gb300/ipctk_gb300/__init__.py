@@ -1042,6 +1042,19 @@ class FrictionPotential:
         self._call(collisions, mesh, velocities, int(project_hessian_to_psd), h=h)
         return _csr_to_scipy(h, 3 * mesh.num_vertices)
 
+    def energy_gradient_hessian(self, collisions, mesh, velocities, project_hessian_to_psd=PSDProjectionMethod.NONE):
+        """Energy, gradient and Hessian from one call (velocities staged once)."""
+        U = _as_f64(velocities)
+        e = np.zeros(1)
+        if _is_torch_cuda(U):
+            import torch
+            g = torch.empty(U.numel(), dtype=torch.float64, device=U.device)
+        else:
+            g = np.empty(3 * mesh.num_vertices)
+        h = C.c_void_p()
+        self._call(collisions, mesh, U, int(project_hessian_to_psd), e=e, g=g, h=h)
+        return float(e[0]), g, _csr_to_scipy(h, 3 * mesh.num_vertices)
+
 
 class Candidates:
     """Candidates (src/ipc/candidates/candidates.hpp): a broad-phase candidate

@@ -103,3 +103,15 @@ def test_friction_device_inputs(ipctk, oracle_mod):
     g_host = D.gradient(tc, mesh, U)
     g_dev = D.gradient(tc, mesh, torch.from_numpy(U).cuda())
     assert np.linalg.norm(g_dev.cpu().numpy() - g_host) <= 1e-14 * np.linalg.norm(g_host)
+
+
+def test_friction_fused_matches_separate(ipctk, oracle_mod):
+    sc, mesh, tc, tref, rng = _setup(ipctk, oracle_mod, "two_sheet_16")
+    U = rng.uniform(-1, 1, sc["V"].shape) * EPS_V
+    D = ipctk.FrictionPotential(EPS_V)
+    e, g, H = D.energy_gradient_hessian(tc, mesh, U, ipctk.PSDProjectionMethod.CLAMP)
+    assert e == D(tc, mesh, U)
+    g2 = D.gradient(tc, mesh, U)  # atomics: summation order may differ
+    assert np.linalg.norm(g - g2) <= 1e-14 * np.linalg.norm(g2)
+    H2 = D.hessian(tc, mesh, U, ipctk.PSDProjectionMethod.CLAMP)
+    assert sp.linalg.norm(H - H2) == 0
