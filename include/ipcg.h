@@ -158,6 +158,12 @@ int ipcg_collisions_use_area_weighting(const ipcg_collisions* collisions, int* u
  * shared edge or vertex is counted once; merged weights that cancel to zero
  * are dropped.  Equal edge-edge records (unordered pair and type) merge into
  * the orientation with ea < eb when one exists.  OGC is not provided. */
+/* NormalCollisions::set_enable_shape_derivatives / enable_shape_derivatives
+ * (normal_collisions.hpp); must be on at build time for
+ * ipcg_barrier_shape_derivative. */
+int ipcg_collisions_set_enable_shape_derivatives(ipcg_collisions* collisions, int enable);
+int ipcg_collisions_enable_shape_derivatives(const ipcg_collisions* collisions, int* enable);
+
 #define IPCG_COLLISION_SET_IPC 0
 #define IPCG_COLLISION_SET_IMPROVED_MAX_APPROX 1
 int ipcg_collisions_set_collision_set_type(ipcg_collisions* collisions, int type);
@@ -243,6 +249,17 @@ int ipcg_barrier_batch(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
                        const double* vertices, const double* dhat, const double* stiffness,
                        int use_physical_barrier, int psd_method,
                        double* energies, double* gradient, ipcg_csr** hessian);
+
+/* NormalPotential::shape_derivative(collisions, mesh, V)
+ * (normal_potential.cpp:85-123, 310-416): the derivative of the gradient with
+ * respect to the rest positions, ndof x ndof (rows: displacement dofs,
+ * columns: rest dofs; not symmetric).  Per collision w times the unprojected
+ * local Hessian, edge-edge collisions in the reference's mollified form with
+ * eps_x from the rest positions.  Sets built with area weighting (nonzero
+ * weight gradients) are not provided. */
+int ipcg_barrier_shape_derivative(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
+                                  const double* vertices, double dhat, double stiffness,
+                                  int use_physical_barrier, ipcg_csr** out);
 
 /* Gauss-Newton forms of the barrier Hessian
  * (NormalPotential::gauss_newton_hessian_diagonal / _quadratic_form,

@@ -469,6 +469,22 @@ int ipcg_collisions_collision_set_type(const ipcg_collisions* c, int* type)
     });
 }
 
+int ipcg_collisions_set_enable_shape_derivatives(ipcg_collisions* c, int on)
+{
+    return guarded([&] {
+        require(c != nullptr, "NULL argument");
+        c->enable_shape_derivatives = on ? 1 : 0;
+    });
+}
+
+int ipcg_collisions_enable_shape_derivatives(const ipcg_collisions* c, int* on)
+{
+    return guarded([&] {
+        require(c && on, "NULL argument");
+        *on = c->enable_shape_derivatives;
+    });
+}
+
 int ipcg_mesh_areas(const ipcg_mesh* m, double* vertex_areas, double* edge_areas)
 {
     return guarded([&] {
@@ -829,6 +845,33 @@ int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, con
             throw;
         }
         if (hessian) *hessian = H;
+    });
+}
+
+int ipcg_barrier_shape_derivative(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,
+    double stiffness, int physical, ipcg_csr** out)
+{
+    return guarded([&] {
+        require(c && mesh && out && (V || mesh->nV == 0), "NULL argument");
+        require(mesh->n_scenes == 1, "mesh is a batch: shape derivatives are per scene");
+        require(c->built_with_shape, "Shape derivative is not computed for collisions!");
+        require(!c->use_area_weighting, "shape derivatives of area-weighted collision sets are not provided");
+        require(dhat > 0, "dhat must be positive");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        BarrierArgs a { dhat, stiffness, c->dmin, 0, IPCG_PSD_NONE };
+        barrier_options(physical, a);
+        a.mixed = 0;
+        a.shape = 1;
+        ipcg_csr* H = new ipcg_csr();
+        try {
+            barrier_evaluate(c, m, dV, a, nullptr, nullptr, H);
+        } catch (...) {
+            delete H;
+            throw;
+        }
+        *out = H;
     });
 }
 

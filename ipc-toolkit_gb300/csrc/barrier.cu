@@ -1290,6 +1290,69 @@ __device__ __forceinline__ void decode_contribution(const ContactsView& cv, int6
 // Sort-by-key reduction into CSR: one thread per stored value (block q,
 // entry k,l) sums the contributions of block q in sorted (deterministic)
 // order and writes the value once.
+// ---- Shape derivative (normal_potential.cpp:310-416), edge-edge part ----
+// Without area weighting the shape derivative of a collision is w times its
+// unprojected local Hessian; edge-edge collisions use the reference's
+// mollified form
+//   f jac_m + gradx_m gradu_f^T + gradu_f gradu_m^T + gradu_m gradu_f^T + m hessu_f
+// with eps_x and its gradient from the rest positions (rows and columns as
+// the reference writes them).
+__global__ void __launch_bounds__(LH_BLOCK) k_shape_local_ee(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ V, const double* __restrict__ rest,
+    const Params* __restrict__ sp, SceneView sv, Slab hs, int64_t first, int64_t count)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t i = first + t;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    const Params P = sp[sv.of(c.vid[0])];
+    V3 x[4], xr[4];
+    gather(V, c, x);
+    gather(rest, c, xr);
+    double g[12], H[144];
+    const double d = ee_local(x, c.dtype, g, H);
+    const double f = c.w * fval(P, d), a1 = c.w * fd1(P, d), a2 = c.w * fd2(P, d);
+    const double eps = ee_mollifier_threshold(xr[0], xr[1], xr[2], xr[3]);
+    const double sq = ee_cross_sqnorm(x[0], x[1], x[2], x[3]);
+    double gs[12], ge[12], Hs[144];
+    double m = 1.0, m1 = 0, dme = 0, dmse = 0;
+    const bool act = sq < eps;
+    if (act) {
+        const double xe = sq / eps;
+        m = (-xe + 2) * xe;
+        const double inv = 1 / eps;
+        m1 = 2 * inv * fma(-inv, sq, 1.0);
+        dme = 2 * sq * (-eps + sq) / (eps * eps * eps);
+        dmse = 2 * (-eps + 2 * sq) / (eps * eps * eps);
+        double gr[6], Hr[36];
+        cross_sq(x[1] - x[0], x[3] - x[2], gr, Hr);
+        const int pos[2] = { 1, 3 }, neg[2] = { 0, 2 };
+        expand_g<2>(12, pos, neg, gr, gs);
+        expand_h<2>(12, pos, neg, Hr, Hs);
+        // gradient of eps_x = 1e-3 |ea|^2 |eb|^2 with respect to the rest positions
+        const V3 ea = xr[0] - xr[1], eb = xr[2] - xr[3];
+        const double la = sqnorm(ea), lb = sqnorm(eb);
+        for (int k = 0; k < 3; ++k) {
+            ge[k] = 1e-3 * 2 * comp(ea, k) * lb;
+            ge[3 + k] = -ge[k];
+            ge[6 + k] = 1e-3 * la * 2 * comp(eb, k);
+            ge[9 + k] = -ge[6 + k];
+        }
+    }
+    for (int r = 0; r < 12; ++r)
+        for (int q = 0; q < 12; ++q) {
+            const double gfr = a1 * g[r], gfq = a1 * g[q];
+            const double hf = a2 * g[r] * g[q] + a1 * H[r * 12 + q];
+            double v = m * hf;
+            if (act) {
+                const double jm = dmse * ge[r] * gs[q] + m1 * Hs[r * 12 + q];
+                v = f * jm + (dme * ge[r]) * gfq + gfr * (m1 * gs[q]) + (m1 * gs[r]) * gfq + m * hf;
+            }
+            hs.at(i, r * 12 + q) = v;
+        }
+}
+
 // ---- Friction (tangential_potential.cpp:156-331, friction/smooth_mu.cpp,
 // friction/smooth_friction_mollifier.cpp; isotropic) ----
 __device__ __forceinline__ double fr_smooth_mu(double y, double ms, double mk, double ev)
@@ -1981,7 +2044,10 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
                     IPCG_LAUNCH("k_local_hessian_ev", t, k_local_hessian<CT_EV><<<grid_for(count[1], LH_BLOCK), LH_BLOCK, 0,
                         t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[1], count[1]));
                 IPCG_CUDA(cudaEventRecord(m->ev_side, t));
-                if (count[2])
+                if (count[2] && a.shape)
+                    IPCG_LAUNCH("k_shape_local_ee", s, k_shape_local_ee<<<grid_for(count[2], LH_BLOCK), LH_BLOCK, 0,
+                        s>>>(cc, m->E.p, m->F.p, V, m->rest.p, sp, sv, slab, first[2], count[2]));
+                else if (count[2])
                     IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], LH_BLOCK), LH_BLOCK, 0,
                         s>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[2], count[2]));
                 if (count[3])

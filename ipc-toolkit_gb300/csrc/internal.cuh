@@ -224,6 +224,8 @@ struct ipcg_collisions {
     bool sorted = false;             // lists sorted by key (built here, not loaded)
     int use_area_weighting = 0;      // NormalCollisions::use_area_weighting()
     int set_type = 0;                // CollisionSetType: 0 IPC, 1 IMPROVED_MAX_APPROX
+    int enable_shape_derivatives = 0; // NormalCollisions::enable_shape_derivatives()
+    int built_with_shape = 0;        // the flag as it was at the last build
     ipcg::DBuf<int2> vv, ev, ee, fv;
     ipcg::DBuf<double> vv_w, ev_w, ee_w, fv_w, ee_eps;
     ipcg::DBuf<int8_t> ee_dtype;
@@ -289,6 +291,7 @@ struct BarrierArgs {
     const double* scene_kappa = nullptr; // per scene (batches), host
     int mixed = 0;                       // FP32 point-triangle contacts
     int kind = 0;                        // barrier function (IPCG_BARRIER_* kinds)
+    int shape = 0;                       // Hessian slot holds the shape derivative
 };
 struct FrictionView;
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,

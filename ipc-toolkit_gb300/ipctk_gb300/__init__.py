@@ -92,6 +92,9 @@ def _load():
         "ipcg_collisions_set_use_area_weighting": (i32, [P, i32]),
         "ipcg_collisions_use_area_weighting": (i32, [P, P]),
         "ipcg_collisions_set_collision_set_type": (i32, [P, i32]),
+        "ipcg_collisions_set_enable_shape_derivatives": (i32, [P, i32]),
+        "ipcg_collisions_enable_shape_derivatives": (i32, [P, P]),
+        "ipcg_barrier_shape_derivative": (i32, [P, P, P, d, d, i32, PP]),
         "ipcg_collisions_collision_set_type": (i32, [P, P]),
         "ipcg_tangential_create": (i32, [PP]),
         "ipcg_tangential_destroy": (i32, [P]),
@@ -423,6 +426,17 @@ class NormalCollisions:
     def use_area_weighting(self, on: bool):
         _check(_load().ipcg_collisions_set_use_area_weighting(self._h, int(bool(on))))
 
+    @property
+    def enable_shape_derivatives(self) -> bool:
+        """NormalCollisions::enable_shape_derivatives (applies to the next build)."""
+        v = C.c_int()
+        _check(_load().ipcg_collisions_enable_shape_derivatives(self._h, C.byref(v)))
+        return bool(v.value)
+
+    @enable_shape_derivatives.setter
+    def enable_shape_derivatives(self, on: bool):
+        _check(_load().ipcg_collisions_set_enable_shape_derivatives(self._h, int(bool(on))))
+
     class CollisionSetType(enum.IntEnum):
         """NormalCollisions::CollisionSetType (normal_collisions.hpp); OGC is
         not provided."""
@@ -676,6 +690,17 @@ class BarrierPotential:
     def _options(self):
         return (int(self.use_physical_barrier) | (2 if self.mixed_precision else 0)
                 | (int(self.barrier.kind) << 4))
+
+    def shape_derivative(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices):
+        """NormalPotential::shape_derivative (normal_potential.cpp:85-123):
+        scipy CSR, rows displacement dofs, columns rest dofs."""
+        import scipy.sparse as sp
+        V = _as_f64(vertices)
+        h = C.c_void_p()
+        _check(_load().ipcg_barrier_shape_derivative(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
+                                                     self._options & ~2, C.byref(h)))
+        A = _csr_to_scipy(h, 3 * mesh.num_vertices)  # CSC view of the CSR arrays = transpose
+        return sp.csr_matrix((A.data, A.indices, A.indptr), shape=A.shape)
 
     def gauss_newton_hessian_diagonal(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices):
         """NormalPotential::gauss_newton_hessian_diagonal (normal_potential.cpp:15-48)."""

@@ -2797,6 +2797,76 @@ void* orc_friction_hessian(void* h, const double* U, int64_t nV, const int32_t* 
     });
 }
 
+// NormalPotential::shape_derivative (normal_potential.cpp:85-123, 310-416)
+// for sets without area weighting (zero weight gradients): per collision
+// w times the unprojected local Hessian, and for edge-edge collisions the
+// reference's mollified form
+//   f jac_m + gradx_m gradu_f^T + gradu_f gradu_m^T + gradu_m gradu_f^T + m hessu_f
+// with eps_x and its gradient taken from the rest positions.
+static void shape_local_ee(const BarrierParams& P, const Contact& c, const V3* x, const V3* xr, double* out)
+{
+    double g[12], H[144];
+    const double d = contact_distance(c, x, g, H);
+    const double f = c.w * f0(P, d), a1 = c.w * f1(P, d), a2 = c.w * f2(P, d);
+    double gf[12];
+    for (int i = 0; i < 12; ++i) gf[i] = a1 * g[i];
+    const double eps = ee_mollifier_threshold(xr[0], xr[1], xr[2], xr[3]);
+    double gr[6], Hr[6][6];
+    const double sq = cross_sq(sub(x[1], x[0]), sub(x[3], x[2]), gr, Hr);
+    double gm[12] = {}, gx[12] = {}, jm[144] = {};
+    double m = 1.0;
+    if (sq < eps) {
+        const double xe = sq / eps;
+        m = (-xe + 2) * xe;
+        const double inv = 1 / eps;
+        const double m1 = 2 * inv * std::fma(-inv, sq, 1);
+        const double dme = 2 * sq * (-eps + sq) / (eps * eps * eps);
+        const double dmse = 2 * (-eps + 2 * sq) / (eps * eps * eps);
+        double gs[12], Hs[144];
+        Reduced R { 2, { 1, 3, 0 }, { 0, 2, 0 } };
+        expand(R, 4, gr, &Hr[0][0], 6, gs, Hs);
+        // gradient of eps_x = 1e-3 |ea|^2 |eb|^2 with respect to the rest positions
+        const V3 ea = sub(xr[0], xr[1]), eb = sub(xr[2], xr[3]);
+        const double la = sqnorm(ea), lb = sqnorm(eb);
+        double ge[12];
+        for (int k = 0; k < 3; ++k) {
+            ge[k] = 1e-3 * 2 * comp(ea, k) * lb;
+            ge[3 + k] = -ge[k];
+            ge[6 + k] = 1e-3 * la * 2 * comp(eb, k);
+            ge[9 + k] = -ge[6 + k];
+        }
+        for (int i = 0; i < 12; ++i) {
+            gm[i] = m1 * gs[i];
+            gx[i] = dme * ge[i];
+            for (int j = 0; j < 12; ++j) jm[i * 12 + j] = dmse * ge[i] * gs[j] + m1 * Hs[i * 12 + j];
+        }
+    }
+    for (int i = 0; i < 12; ++i)
+        for (int j = 0; j < 12; ++j) {
+            const double hf = a2 * g[i] * g[j] + a1 * H[i * 12 + j];
+            out[i * 12 + j] = f * jm[i * 12 + j] + gx[i] * gf[j] + gf[i] * gm[j] + gm[i] * gf[j] + m * hf;
+        }
+}
+
+void* orc_barrier_shape_derivative(void* h, const double* V, const double* Vrest, int64_t nV, const int32_t* E,
+    const int32_t* F, double dhat, double kappa, double dmin, int physical, int nthreads)
+{
+    const Collisions& C = *(const Collisions*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    const int64_t n = C.vv_w.size() + C.ev_w.size() + C.ee_w.size() + C.fv_w.size();
+    return assemble_csr(n, nV, nthreads, [&](int64_t i, int& nv, int* vid, double* Hl) {
+        Contact c;
+        contact_stencil(C, E, F, i, c);
+        V3 x[4], xr[4];
+        gather(V, c, x);
+        gather(Vrest, c, xr);
+        if (c.type == CT_EE) shape_local_ee(P, c, x, xr, Hl);
+        else contact_hessian(P, c, x, 0, Hl);
+        nv = c.n;
+        for (int k = 0; k < c.n; ++k) vid[k] = c.vid[k];
+    });
+}
+
 // scalar smooth-friction functions for derivative checks
 double orc_friction_mu(int which, double y, double mu_s, double mu_k, double eps_v)
 {

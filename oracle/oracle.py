@@ -92,6 +92,8 @@ def lib():
         L.orc_friction_gradient.argtypes = [vp, P, i64, P, P, d, i32, P]
         L.orc_friction_hessian.restype = vp
         L.orc_friction_hessian.argtypes = [vp, P, i64, P, P, d, i32, i32]
+        L.orc_barrier_shape_derivative.restype = vp
+        L.orc_barrier_shape_derivative.argtypes = [vp, P, P, i64, P, P, d, d, d, i32, i32]
         L.orc_friction_mu.restype = d
         L.orc_friction_mu.argtypes = [i32, d, d, d, d]
         _lib = L
@@ -459,3 +461,20 @@ def friction_hessian(t, U, E, F, eps_v, psd="none", nthreads=None):
 def friction_mu(which, y, mu_s, mu_k, eps_v):
     """0: mu f0, 1: mu f1 / y, 2: (mu f1)' y - mu f1) / y^3, 3: mu(y)."""
     return lib().orc_friction_mu(int(which), float(y), float(mu_s), float(mu_k), float(eps_v))
+
+
+def barrier_shape_derivative(col, V, E, F, dhat, kappa, rest=None, dmin=0.0, physical=0, nthreads=None):
+    """(rowptr, col, val) of NormalPotential::shape_derivative for a set built
+    without area weighting (rows: displacement dofs, columns: rest dofs)."""
+    V, E, F = _f64(V), _i32(E), _i32(F)
+    rest = V if rest is None else _f64(rest)
+    L = lib()
+    h = L.orc_barrier_shape_derivative(col.h, _p(V), _p(rest), V.shape[0], _p(E), _p(F), float(dhat), float(kappa),
+                                       float(dmin), int(physical), int(nthreads or os.cpu_count() or 1))
+    nnz = L.orc_csr_nnz(h)
+    rp = np.zeros(V.size + 1, np.int64)
+    ci = np.zeros(nnz, np.int32)
+    va = np.zeros(nnz)
+    L.orc_csr_get(h, _p(rp), _p(ci), _p(va))
+    L.orc_csr_free(h)
+    return rp, ci, va

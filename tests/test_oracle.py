@@ -741,3 +741,38 @@ def test_friction_energy_identities(oracle_mod):
     assert e0 == pytest.approx(float(np.sum(same.w * same.N)) * 0.4 * ev / 3, rel=1e-12)
     g0 = oracle_mod.friction_gradient(same, np.zeros_like(V), E, F, ev)
     assert np.abs(g0).max() == 0
+
+
+# --- shape derivative -------------------------------------------------------------
+
+def test_shape_derivative_structure(oracle_mod):
+    """normal_potential.cpp:310-416 without area weighting: w times the
+    unprojected local Hessian for every collision whose mollifier is inactive;
+    only edge-edge stencils with cross^2 < eps_x differ from the Hessian."""
+    import scipy.sparse as sps
+    from ipctk_gb300 import scenes
+    sc = scenes.two_sheet(side=12, seed=4)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    col = oracle_mod.build_collisions(V, E, F, sc["dhat"])
+    n = V.size
+    mat = lambda t: sps.csr_matrix((t[2], t[1], t[0]), shape=(n, n))
+    S = mat(oracle_mod.barrier_shape_derivative(col, V, E, F, sc["dhat"], sc["kappa"]))
+    H = mat(oracle_mod.barrier_hessian(col, V, E, F, sc["dhat"], sc["kappa"]))
+    # without edge-edge records the two are the same matrix
+    z2, z1 = np.zeros((0, 2), np.int32), np.zeros(0)
+    noee = oracle_mod.Collisions.from_arrays(col.vv, col.vv_w, col.ev, col.ev_w, z2, z1, np.zeros(0, np.int8), z1,
+                                             col.fv, col.fv_w)
+    S0 = mat(oracle_mod.barrier_shape_derivative(noee, V, E, F, sc["dhat"], sc["kappa"]))
+    H0 = mat(oracle_mod.barrier_hessian(noee, V, E, F, sc["dhat"], sc["kappa"]))
+    assert sps.linalg.norm(S0 - H0) == 0
+    # with them, differences stay inside the stencils of active (mollified) pairs
+    active = set()
+    for (ea, eb), eps in zip(col.ee, col.ee_eps):
+        x = V[[E[ea, 0], E[ea, 1], E[eb, 0], E[eb, 1]]]
+        if np.sum(np.cross(x[1] - x[0], x[3] - x[2]) ** 2) < eps:
+            active.update(int(v) for v in (E[ea, 0], E[ea, 1], E[eb, 0], E[eb, 1]))
+    assert active, "the two-sheet scene has mollified edge pairs"
+    D = (S - H).tocoo()
+    big = np.abs(D.data) > 1e-12 * abs(H).max()
+    assert big.any()
+    assert all(r // 3 in active and c // 3 in active for r, c in zip(D.row[big], D.col[big]))
