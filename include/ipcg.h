@@ -394,6 +394,24 @@ int ipcg_tangential_get(const ipcg_tangential* tangential, int32_t* vv, int32_t*
                         double* weight, double* normal_force, double* closest_point, double* tangent_basis,
                         double* mu_s, double* mu_k);
 
+/* Anisotropic friction (tangential_collision.hpp:104-139): per collision
+ * (VV | EV | EE | FV order) the slip scaling mu_aniso, the directional static
+ * and kinetic coefficients mu_s_aniso, mu_k_aniso (2 doubles each, along the
+ * collision's tangent basis; host or device; NULL restores the defaults
+ * (1, 1), (0, 0), (0, 0)).  A build restores every default and sets the
+ * lagged effective coefficients to the scalar ones. */
+int ipcg_tangential_set_anisotropy(ipcg_tangential* tangential, const double* mu_aniso, const double* mu_s_aniso,
+                                   const double* mu_k_aniso);
+/* TangentialCollisions::update_lagged_anisotropic_friction_coefficients
+ * (tangential_collisions.cpp:387-420): the elliptical effective
+ * coefficients along the scaled slip at rest + lagged displacements. */
+int ipcg_tangential_update_lagged_mu(ipcg_tangential* tangential, const ipcg_mesh* mesh, const double* rest_positions,
+                                     const double* lagged_displacements, const double* velocities);
+/* TangentialCollisions::reset_lagged_anisotropic_friction_coefficients */
+int ipcg_tangential_reset_lagged_mu(ipcg_tangential* tangential);
+/* The lagged effective coefficients (n doubles each; either may be NULL). */
+int ipcg_tangential_lagged_mu(const ipcg_tangential* tangential, double* mu_s_effective, double* mu_k_effective);
+
 /* FrictionPotential(eps_v) energy, gradient and Hessian at velocities
  * (tangential_potential.cpp:156-331; potential.cpp:36-222): any output may
  * be NULL; the Hessian's inner 2x2 blocks are projected with psd_method. */

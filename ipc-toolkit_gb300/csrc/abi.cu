@@ -768,7 +768,7 @@ int ipcg_tangential_build(ipcg_tangential* t, const ipcg_mesh* mesh, const doubl
         DBuf<double> ms, mk;
         upload(ms, mu_s, m->nV, m->stream);
         upload(mk, mu_k, m->nV, m->stream);
-        tangential_build(c, m, dV, a, ms.p, mk.p, &t->st, t->N, t->cp, t->P, t->mu_s, t->mu_k);
+        tangential_build(c, m, dV, a, ms.p, mk.p, t);
         t->mesh = mesh;
     });
 }
@@ -811,6 +811,74 @@ int ipcg_tangential_get(const ipcg_tangential* t, int32_t* vv, int32_t* ev, int3
     });
 }
 
+int ipcg_tangential_set_anisotropy(ipcg_tangential* t, const double* mu_aniso, const double* mu_s_aniso,
+    const double* mu_k_aniso)
+{
+    return guarded([&] {
+        require(t && t->mesh, "tangential collisions are not built");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(t->mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const int64_t n = t->st.size();
+        cudaStream_t s = m->stream;
+        auto set = [&](DBuf<double>& dst, const double* src, double fill) {
+            if (!n) return;
+            if (src) IPCG_CUDA(cudaMemcpyAsync(dst.p, src, sizeof(double) * 2 * n, cudaMemcpyDefault, s));
+            else if (fill == 0) IPCG_CUDA(cudaMemsetAsync(dst.p, 0, sizeof(double) * 2 * n, s));
+            else {
+                std::vector<double> ones(2 * n, fill);
+                IPCG_CUDA(cudaMemcpyAsync(dst.p, ones.data(), sizeof(double) * 2 * n, cudaMemcpyHostToDevice, s));
+                IPCG_CUDA(cudaStreamSynchronize(s));
+            }
+        };
+        set(t->mu_aniso, mu_aniso, 1.0);
+        set(t->mu_s_aniso, mu_s_aniso, 0.0);
+        set(t->mu_k_aniso, mu_k_aniso, 0.0);
+        IPCG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
+int ipcg_tangential_update_lagged_mu(ipcg_tangential* t, const ipcg_mesh* mesh, const double* rest,
+    const double* lagged_displacements, const double* velocities)
+{
+    return guarded([&] {
+        require(t && mesh && (mesh->nV == 0 || (rest && lagged_displacements && velocities)), "NULL argument");
+        require(t->mesh == mesh, "tangential collisions were built on another mesh");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        DBuf<double> lag;
+        const double* dR = stage_positions(m, rest, m->V0);
+        const double* dL = stage_positions(m, lagged_displacements, m->V1);
+        const double* dU = stage_positions(m, velocities, lag);
+        tangential_update_lagged(t, m, dR, dL, dU);
+    });
+}
+
+int ipcg_tangential_reset_lagged_mu(ipcg_tangential* t)
+{
+    return guarded([&] {
+        require(t && t->mesh, "tangential collisions are not built");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(t->mesh);
+        const int64_t n = t->st.size();
+        if (n) {
+            IPCG_CUDA(cudaMemcpyAsync(t->mu_s_eff.p, t->mu_s.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, m->stream));
+            IPCG_CUDA(cudaMemcpyAsync(t->mu_k_eff.p, t->mu_k.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, m->stream));
+        }
+        IPCG_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
+int ipcg_tangential_lagged_mu(const ipcg_tangential* t, double* mu_s_eff, double* mu_k_eff)
+{
+    return guarded([&] {
+        require(t != nullptr, "NULL argument");
+        const int64_t n = t->st.size();
+        cudaStream_t s = 0;
+        copy_out(mu_s_eff, t->mu_s_eff.p, sizeof(double) * n, s);
+        copy_out(mu_k_eff, t->mu_k_eff.p, sizeof(double) * n, s);
+        IPCG_CUDA(cudaStreamSynchronize(s));
+    });
+}
+
 int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* U, double eps_v, int psd,
     double* energy, double* gradient, ipcg_csr** hessian)
 {
@@ -822,7 +890,7 @@ int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, con
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dU = stage_positions(m, U, m->V0);
-        const FrictionView f { t->N.p, t->cp.p, t->P.p, t->mu_s.p, t->mu_k.p, eps_v };
+        const FrictionView f { t->N.p, t->cp.p, t->P.p, t->mu_s_eff.p, t->mu_k_eff.p, t->mu_aniso.p, eps_v };
         double* gdev = nullptr;
         if (gradient) {
             if (is_device_ptr(gradient)) gdev = gradient;

@@ -1414,16 +1414,18 @@ __device__ __forceinline__ void friction_setup(const FrictionView& f, int64_t i,
         rv = v[0] - ((v[1] + (v[2] - v[1]) * c0) + (v[3] - v[1]) * c1);
         g[0] = 1, g[1] = c0 + c1 - 1, g[2] = -c0, g[3] = -c1;
     }
-    L.u0 = dot(b0, rv);
-    L.u1 = dot(b1, rv);
+    // anisotropic slip scaling (tangential_potential.cpp:166-175, 200-212)
+    const double a0 = f.aniso[2 * i], a1 = f.aniso[2 * i + 1];
+    L.u0 = a0 * dot(b0, rv);
+    L.u1 = a1 * dot(b1, rv);
     L.nu = sqrt(L.u0 * L.u0 + L.u1 * L.u1);
     L.ms = f.mu_s[i];
     L.mk = f.mu_k[i];
     L.scl = c.w * f.N[i];
     for (int k = 0; k < c.n; ++k)
         for (int d = 0; d < 3; ++d) {
-            L.T[3 * k + d][0] = g[k] * P[d];
-            L.T[3 * k + d][1] = g[k] * P[3 + d];
+            L.T[3 * k + d][0] = (g[k] * P[d]) * a0;
+            L.T[3 * k + d][1] = (g[k] * P[3 + d]) * a1;
         }
 }
 
@@ -1568,6 +1570,94 @@ __device__ __forceinline__ V3 normalized(V3 a)
     return V3 { a.x / r, a.y / r, a.z / r };
 }
 
+// Closest point and tangent basis of a tangential collision of the given
+// type at stencil positions x (tangent/closest_point.cpp,
+// tangent/tangent_basis.cpp).
+__device__ void tangential_frame(int type, const V3* x, double& cp0, double& cp1, V3& b0, V3& b1)
+{
+    cp0 = cp1 = 0;
+    if (type == CT_VV) {
+        const V3 d = x[1] - x[0];
+        const V3 cx = cross(V3 { 1, 0, 0 }, d), cy = cross(V3 { 0, 1, 0 }, d);
+        const V3 cc = sqnorm(cx) > sqnorm(cy) ? cx : cy;
+        b0 = normalized(cc);
+        b1 = normalized(cross(d, cc));
+    } else if (type == CT_EV) {
+        const V3 e = x[2] - x[1];
+        cp0 = dot(x[0] - x[1], e) / sqnorm(e);
+        b0 = normalized(e);
+        b1 = normalized(cross(e, x[0] - x[1]));
+    } else if (type == CT_EE) {
+        const V3 ea = x[1] - x[0], eb = x[3] - x[2];
+        ldlt2_solve(ea, eb * -1.0, x[2] - x[0], cp0, cp1);
+        b0 = normalized(ea);
+        b1 = normalized(cross(cross(ea, eb), ea));
+    } else {
+        const V3 e0 = x[2] - x[1];
+        ldlt2_solve(e0, x[3] - x[1], x[0] - x[1], cp0, cp1);
+        b0 = normalized(e0);
+        b1 = normalized(cross(cross(e0, x[3] - x[1]), e0));
+    }
+}
+
+// update_lagged_anisotropic_friction_coefficients (tangential_collisions.cpp:
+// 19-58, 387-420): at rest + lagged displacement, tau = T^T v with T =
+// Gamma^T P, scaled by mu_aniso; the elliptical effective coefficients along
+// tau (smooth_mu.cpp:117-171), or the scalar ones without directional
+// static coefficients.
+__global__ void k_tangential_update_lagged(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    const double* __restrict__ rest, const double* __restrict__ lagged, const double* __restrict__ vel,
+    const double* __restrict__ aniso, const double* __restrict__ ms_a, const double* __restrict__ mk_a,
+    const double* __restrict__ mu_s, const double* __restrict__ mu_k, double* __restrict__ ms_eff,
+    double* __restrict__ mk_eff)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double s0 = ms_a[2 * i], s1 = ms_a[2 * i + 1];
+    if (s0 * s0 + s1 * s1 == 0) {
+        ms_eff[i] = mu_s[i];
+        mk_eff[i] = mu_k[i];
+        return;
+    }
+    Local c;
+    load_contact(cv, E, F, i, c);
+    V3 x[4], v[4];
+    for (int k = 0; k < c.n; ++k) {
+        x[k] = load_v3(rest, c.vid[k]) + load_v3(lagged, c.vid[k]);
+        v[k] = load_v3(vel, c.vid[k]);
+    }
+    double cp0, cp1;
+    V3 b0, b1;
+    tangential_frame(c.type, x, cp0, cp1, b0, b1);
+    double g[4] = { 0, 0, 0, 0 };
+    if (c.type == CT_VV) g[0] = 1, g[1] = -1;
+    else if (c.type == CT_EV) g[0] = 1, g[1] = cp0 - 1, g[2] = -cp0;
+    else if (c.type == CT_EE) g[0] = 1 - cp0, g[1] = cp0, g[2] = cp1 - 1, g[3] = -cp1;
+    else g[0] = 1, g[1] = cp0 + cp1 - 1, g[2] = -cp0, g[3] = -cp1;
+    double t0 = 0, t1 = 0;
+    for (int k = 0; k < c.n; ++k) {
+        t0 += g[k] * dot(b0, v[k]);
+        t1 += g[k] * dot(b1, v[k]);
+    }
+    t0 *= aniso[2 * i];
+    t1 *= aniso[2 * i + 1];
+    const double k0 = mk_a[2 * i], k1 = mk_a[2 * i + 1];
+    const bool use_k = k0 * k0 + k1 * k1 > 0;
+    const double nt = sqrt(t0 * t0 + t1 * t1);
+    double d0 = 1.0, d1 = 0.0;
+    if (!(nt < 1e-10)) d0 = t0 / nt, d1 = t1 / nt;
+    const double a = s0 * d0, b = s1 * d1, cc = k0 * d0, dd = k1 * d1;
+    ms_eff[i] = sqrt(a * a + b * b);
+    mk_eff[i] = use_k ? sqrt(cc * cc + dd * dd) : mu_k[i];
+}
+
+__global__ void k_fill(double* __restrict__ p, int64_t n, double v)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
 // EE collisions with cross^2 < eps_x are left out of the tangential set.
 __global__ void k_tangential_keep_ee(ContactsView cv, const int* __restrict__ E, const double* __restrict__ V,
     int* __restrict__ keep)
@@ -1621,38 +1711,21 @@ __global__ void k_tangential_build(ContactsView cv, const int* __restrict__ E, c
     else d2 = point_triangle_distance(x[0], x[1], x[2], x[3], point_triangle_distance_type(x[0], x[1], x[2], x[3]));
     // barrier_force_magnitude.cpp:5-15, then the physical scaling
     const double Nf = -P.kappa * barrier_fn<1, double>(P.kind, d2 - P.dmin2, P.xhat) * 2 * sqrt(d2) * P.scale;
-    double cp0 = 0, cp1 = 0, ms, mk;
+    double cp0, cp1, ms, mk;
     V3 b0, b1;
     const int* v = c.vid;
     auto blend = [](double a, double b) { return (a + b) / 2; };
+    tangential_frame(c.type, x, cp0, cp1, b0, b1);
     if (c.type == CT_VV) {
-        // point_point_tangent_basis (tangent/tangent_basis.cpp)
-        const V3 d = x[1] - x[0];
-        const V3 cx = cross(V3 { 1, 0, 0 }, d), cy = cross(V3 { 0, 1, 0 }, d);
-        const V3 cc = sqnorm(cx) > sqnorm(cy) ? cx : cy;
-        b0 = normalized(cc);
-        b1 = normalized(cross(d, cc));
         ms = blend(mu_s[v[0]], mu_s[v[1]]);
         mk = blend(mu_k[v[0]], mu_k[v[1]]);
     } else if (c.type == CT_EV) {
-        const V3 e = x[2] - x[1];
-        cp0 = dot(x[0] - x[1], e) / sqnorm(e);
-        b0 = normalized(e);
-        b1 = normalized(cross(e, x[0] - x[1]));
         ms = blend((mu_s[v[2]] - mu_s[v[1]]) * cp0 + mu_s[v[1]], mu_s[v[0]]);
         mk = blend((mu_k[v[2]] - mu_k[v[1]]) * cp0 + mu_k[v[1]], mu_k[v[0]]);
     } else if (c.type == CT_EE) {
-        const V3 ea = x[1] - x[0], eb = x[3] - x[2];
-        ldlt2_solve(ea, eb * -1.0, x[2] - x[0], cp0, cp1);
-        b0 = normalized(ea);
-        b1 = normalized(cross(cross(ea, eb), ea));
         ms = blend((mu_s[v[1]] - mu_s[v[0]]) * cp0 + mu_s[v[0]], (mu_s[v[3]] - mu_s[v[2]]) * cp1 + mu_s[v[2]]);
         mk = blend((mu_k[v[1]] - mu_k[v[0]]) * cp0 + mu_k[v[0]], (mu_k[v[3]] - mu_k[v[2]]) * cp1 + mu_k[v[2]]);
     } else {
-        const V3 e0 = x[2] - x[1];
-        ldlt2_solve(e0, x[3] - x[1], x[0] - x[1], cp0, cp1);
-        b0 = normalized(e0);
-        b1 = normalized(cross(cross(e0, x[3] - x[1]), e0));
         ms = blend(mu_s[v[1]] + cp0 * (mu_s[v[2]] - mu_s[v[1]]) + cp1 * (mu_s[v[3]] - mu_s[v[1]]), mu_s[v[0]]);
         mk = blend(mu_k[v[1]] + cp0 * (mu_k[v[2]] - mu_k[v[1]]) + cp1 * (mu_k[v[3]] - mu_k[v[1]]), mu_k[v[0]]);
     }
@@ -2166,9 +2239,10 @@ void barrier_evaluate_friction(const ipcg_collisions* stencils, ipcg_mesh* m, co
 }
 
 void tangential_build(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
-    const double* mu_s, const double* mu_k, ipcg_collisions* st, DBuf<double>& N, DBuf<double>& cp, DBuf<double>& P,
-    DBuf<double>& ms, DBuf<double>& mk)
+    const double* mu_s, const double* mu_k, ipcg_tangential* t)
 {
+    ipcg_collisions* st = &t->st;
+    DBuf<double>&N = t->N, &cp = t->cp, &P = t->P, &ms = t->mu_s, &mk = t->mu_k;
     cudaStream_t s = m->stream;
     ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
         cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
@@ -2218,6 +2292,34 @@ void tangential_build(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
     if (n)
         IPCG_LAUNCH("k_tangential_build", s, k_tangential_build<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(cv, m->E.p,
             m->F.p, V, sp, scene_view(m), mu_s, mu_k, keep, offs, nee_kept, o));
+    // isotropic defaults and reset_lagged_anisotropic_friction_coefficients
+    t->mu_aniso.reserve(2 * nt + 2);
+    t->mu_s_aniso.reserve(2 * nt + 2);
+    t->mu_k_aniso.reserve(2 * nt + 2);
+    t->mu_s_eff.reserve(nt + 1);
+    t->mu_k_eff.reserve(nt + 1);
+    if (nt) {
+        IPCG_LAUNCH("k_fill", s, k_fill<<<grid_for(2 * nt, BLOCK), BLOCK, 0, s>>>(t->mu_aniso.p, 2 * nt, 1.0));
+        IPCG_CUDA(cudaMemsetAsync(t->mu_s_aniso.p, 0, sizeof(double) * 2 * nt, s));
+        IPCG_CUDA(cudaMemsetAsync(t->mu_k_aniso.p, 0, sizeof(double) * 2 * nt, s));
+        IPCG_CUDA(cudaMemcpyAsync(t->mu_s_eff.p, ms.p, sizeof(double) * nt, cudaMemcpyDeviceToDevice, s));
+        IPCG_CUDA(cudaMemcpyAsync(t->mu_k_eff.p, mk.p, sizeof(double) * nt, cudaMemcpyDeviceToDevice, s));
+    }
+    IPCG_CUDA(cudaStreamSynchronize(s));
+}
+
+void tangential_update_lagged(ipcg_tangential* t, ipcg_mesh* m, const double* rest, const double* lagged,
+    const double* vel)
+{
+    cudaStream_t s = m->stream;
+    const ipcg_collisions* st = &t->st;
+    ContactsView cv { st->nvv, st->nev, st->nee, st->nfv, st->vv.p, st->ev.p, st->ee.p, st->fv.p, st->vv_w.p,
+        st->ev_w.p, st->ee_w.p, st->fv_w.p, st->ee_eps.p, st->ee_dtype.p };
+    const int64_t n = st->size();
+    if (n)
+        IPCG_LAUNCH("k_tangential_update_lagged", s, k_tangential_update_lagged<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(
+            cv, m->E.p, m->F.p, rest, lagged, vel, t->mu_aniso.p, t->mu_s_aniso.p, t->mu_k_aniso.p, t->mu_s.p,
+            t->mu_k.p, t->mu_s_eff.p, t->mu_k_eff.p));
     IPCG_CUDA(cudaStreamSynchronize(s));
 }
 

@@ -238,6 +238,9 @@ struct ipcg_collisions {
 struct ipcg_tangential {
     ipcg_collisions st;
     ipcg::DBuf<double> N, cp, P, mu_s, mu_k;
+    // anisotropy: slip scaling (2 per collision), directional static and
+    // kinetic coefficients (2 each), lagged effective coefficients
+    ipcg::DBuf<double> mu_aniso, mu_s_aniso, mu_k_aniso, mu_s_eff, mu_k_eff;
     const ipcg_mesh* mesh = nullptr;
 };
 
@@ -300,16 +303,19 @@ void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, c
 // order of its stencil lists, the normal force N, closest point cp (2), tangent
 // basis P (b0 xyz, b1 xyz) and blended mu_s / mu_k.
 struct FrictionView {
-    const double *N, *cp, *P, *mu_s, *mu_k;
+    const double *N, *cp, *P, *mu_s, *mu_k; // mu: the lagged effective coefficients
+    const double* aniso;                     // slip scaling per collision (2)
     double eps_v;
 };
 void barrier_evaluate_friction(const ipcg_collisions* stencils, ipcg_mesh* m, const double* U, const FrictionView& f,
     int psd, double* energy_host, double* grad_dev, ipcg_csr* hess);
 // TangentialCollisions::build: from the normal set at positions V with the
-// barrier potential a, per-vertex mu (device); fills the stencils and arrays.
+// barrier potential a, per-vertex mu (device); fills t (isotropic defaults).
 void tangential_build(const ipcg_collisions* normal, ipcg_mesh* m, const double* V, const BarrierArgs& a,
-    const double* mu_s_dev, const double* mu_k_dev, ipcg_collisions* stencils, ipcg::DBuf<double>& N,
-    ipcg::DBuf<double>& cp, ipcg::DBuf<double>& P, ipcg::DBuf<double>& mu_s, ipcg::DBuf<double>& mu_k);
+    const double* mu_s_dev, const double* mu_k_dev, ipcg_tangential* t);
+// update_lagged_anisotropic_friction_coefficients (device inputs)
+void tangential_update_lagged(ipcg_tangential* t, ipcg_mesh* m, const double* rest, const double* lagged,
+    const double* vel);
 // Gauss-Newton Hessian diagonal (device, 3 nV) and/or quadratic form p^T H p
 // (p on the device, result on the host).
 void barrier_gauss_newton(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,

@@ -102,6 +102,10 @@ def _load():
         "ipcg_tangential_counts": (i32, [P, P]),
         "ipcg_tangential_get": (i32, [P] + [P] * 10),
         "ipcg_friction_potential": (i32, [P, P, P, d, i32, P, P, PP]),
+        "ipcg_tangential_set_anisotropy": (i32, [P, P, P, P]),
+        "ipcg_tangential_update_lagged_mu": (i32, [P, P, P, P, P]),
+        "ipcg_tangential_reset_lagged_mu": (i32, [P]),
+        "ipcg_tangential_lagged_mu": (i32, [P, P, P]),
         "ipcg_csr_get_int32": (i32, [P, P, P, P]),
         "ipcg_candidates_create": (i32, [PP]),
         "ipcg_candidates_destroy": (i32, [P]),
@@ -1011,6 +1015,30 @@ class TangentialCollisions:
         c = np.zeros(4, np.int64)
         _check(_load().ipcg_tangential_counts(self._h, _ptr(c)))
         return c
+
+    def set_anisotropy(self, mu_aniso=None, mu_s_aniso=None, mu_k_aniso=None):
+        """Per-collision (n, 2) arrays: the slip scaling and the directional
+        static / kinetic coefficients (None restores the isotropic default)."""
+        n = len(self)
+        arrs = [None if a is None else np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float64), (n, 2)))
+                for a in (mu_aniso, mu_s_aniso, mu_k_aniso)]
+        _check(_load().ipcg_tangential_set_anisotropy(self._h, *[None if a is None else _ptr(a) for a in arrs]))
+
+    def update_lagged_anisotropic_friction_coefficients(self, mesh, rest_positions, lagged_displacements,
+                                                        velocities):
+        """tangential_collisions.cpp:387-420."""
+        R, L, U = _as_f64(rest_positions), _as_f64(lagged_displacements), _as_f64(velocities)
+        _check(_load().ipcg_tangential_update_lagged_mu(self._h, mesh._h, _ptr(R), _ptr(L), _ptr(U)))
+
+    def reset_lagged_anisotropic_friction_coefficients(self):
+        _check(_load().ipcg_tangential_reset_lagged_mu(self._h))
+
+    def lagged_mu(self):
+        """(mu_s_effective, mu_k_effective) per collision."""
+        n = len(self)
+        ms, mk = np.zeros(n), np.zeros(n)
+        _check(_load().ipcg_tangential_lagged_mu(self._h, _ptr(ms), _ptr(mk)))
+        return ms, mk
 
     def __len__(self):
         return int(self.counts().sum())

@@ -2470,7 +2470,29 @@ static double mu_f2_x_minus_f1_over_x3(double y, double ms, double mk, double ev
 struct Tangential {
     Collisions base;                        // stencils and weights (vv | ev | ee | fv)
     std::vector<double> N, cp, P, mu_s, mu_k; // per collision: cp 2, P 6 (b0 xyz, b1 xyz)
+    // anisotropy (tangential_collision.hpp:104-139): slip scaling (default 1),
+    // directional coefficients (default 0 = isotropic), lagged effective mu
+    std::vector<double> mu_aniso, mu_s_aniso, mu_k_aniso, mu_s_eff, mu_k_eff;
 };
+
+// smooth_mu.cpp:117-171: elliptical effective coefficients along the slip
+// direction (default (1, 0) when the slip is below 1e-10).
+static void aniso_mu_eff(const double* tau, const double* ms_a, const double* mk_a, double ms, double mk, double* out)
+{
+    const bool use_s = ms_a[0] * ms_a[0] + ms_a[1] * ms_a[1] > 0;
+    const bool use_k = mk_a[0] * mk_a[0] + mk_a[1] * mk_a[1] > 0;
+    if (!use_s && !use_k) {
+        out[0] = ms;
+        out[1] = mk;
+        return;
+    }
+    const double nt = std::sqrt(tau[0] * tau[0] + tau[1] * tau[1]);
+    double t0 = 1.0, t1 = 0.0;
+    if (!(nt < 1e-10)) t0 = tau[0] / nt, t1 = tau[1] / nt;
+    const double a = ms_a[0] * t0, b = ms_a[1] * t1, c = mk_a[0] * t0, d = mk_a[1] * t1;
+    out[0] = use_s ? std::sqrt(a * a + b * b) : ms;
+    out[1] = use_k ? std::sqrt(c * c + d * d) : mk;
+}
 
 // Relative-velocity coefficients g (relative velocity = sum_k g_k v_k) of a
 // tangential collision (tangent/relative_velocity.cpp jacobians).
@@ -2499,9 +2521,10 @@ static void friction_local(const Tangential& T, int64_t i, const Contact& c, con
     const double* P = &T.P[6 * i];
     const V3 rv = friction_rel_velocity(c, cp, v);
     const V3 b0 { P[0], P[1], P[2] }, b1 { P[3], P[4], P[5] };
-    const double u0 = dot(b0, rv), u1 = dot(b1, rv);
+    const double a0 = T.mu_aniso[2 * i], a1 = T.mu_aniso[2 * i + 1];
+    const double u0 = a0 * dot(b0, rv), u1 = a1 * dot(b1, rv);
     const double nu = std::sqrt(u0 * u0 + u1 * u1);
-    const double ms = T.mu_s[i], mk = T.mu_k[i];
+    const double ms = T.mu_s_eff[i], mk = T.mu_k_eff[i];
     const double scl = c.w * T.N[i];
     if (e) *e = scl * mu_f0(nu, ms, mk, ev);
     double gm[4];
@@ -2511,8 +2534,8 @@ static void friction_local(const Tangential& T, int64_t i, const Contact& c, con
     double Tm[12][2];
     for (int k = 0; k < c.n; ++k)
         for (int d = 0; d < 3; ++d) {
-            Tm[3 * k + d][0] = gm[k] * P[d];
-            Tm[3 * k + d][1] = gm[k] * P[3 + d];
+            Tm[3 * k + d][0] = (gm[k] * P[d]) * a0;
+            Tm[3 * k + d][1] = (gm[k] * P[3 + d]) * a1;
         }
     const double f1x = mu_f1_over_x(nu, ms, mk, ev);
     if (g) {
@@ -2695,7 +2718,90 @@ void* orc_tangential_build(void* h, const double* V, const int32_t* E, const int
         T->mu_s.push_back(ms);
         T->mu_k.push_back(mk);
     }
+    const size_t nt = T->N.size();
+    T->mu_aniso.assign(2 * nt, 1.0);
+    T->mu_s_aniso.assign(2 * nt, 0.0);
+    T->mu_k_aniso.assign(2 * nt, 0.0);
+    T->mu_s_eff = T->mu_s; // reset_lagged_anisotropic_friction_coefficients
+    T->mu_k_eff = T->mu_k;
     return T;
+}
+
+void orc_tangential_set_anisotropy(void* h, const double* mu_aniso, const double* mu_s_aniso, const double* mu_k_aniso)
+{
+    Tangential* T = (Tangential*)h;
+    const size_t n = T->N.size();
+    T->mu_aniso.assign(2 * n, 1.0);
+    T->mu_s_aniso.assign(2 * n, 0.0);
+    T->mu_k_aniso.assign(2 * n, 0.0);
+    if (mu_aniso) std::copy(mu_aniso, mu_aniso + 2 * n, T->mu_aniso.begin());
+    if (mu_s_aniso) std::copy(mu_s_aniso, mu_s_aniso + 2 * n, T->mu_s_aniso.begin());
+    if (mu_k_aniso) std::copy(mu_k_aniso, mu_k_aniso + 2 * n, T->mu_k_aniso.begin());
+}
+
+// update_lagged_anisotropic_friction_coefficients (tangential_collisions.cpp:
+// 19-58, 387-420): tangent basis and closest point at rest + lagged
+// displacement, tau = T^T v with T = Gamma^T P, tau_aniso = mu_aniso . tau.
+void orc_tangential_update_lagged_mu(void* h, const double* rest, const double* lagged, const double* vel,
+    const int32_t* E, const int32_t* F)
+{
+    Tangential* T = (Tangential*)h;
+    const int64_t n = T->N.size();
+    for (int64_t i = 0; i < n; ++i) {
+        Contact c;
+        contact_stencil(T->base, E, F, i, c);
+        V3 x[4], v[4];
+        for (int k = 0; k < c.n; ++k) {
+            x[k] = add(row(rest, c.vid[k]), row(lagged, c.vid[k]));
+            v[k] = row(vel, c.vid[k]);
+        }
+        double cp[2] = { 0, 0 };
+        V3 b0, b1;
+        if (c.type == CT_VV) pp_basis(x[0], x[1], b0, b1);
+        else if (c.type == CT_EV) {
+            const V3 e = sub(x[2], x[1]);
+            cp[0] = dot(sub(x[0], x[1]), e) / sqnorm(e);
+            pe_basis(x[0], x[1], x[2], b0, b1);
+        } else if (c.type == CT_EE) {
+            ldlt2_solve(sub(x[1], x[0]), scale(sub(x[3], x[2]), -1.0), sub(x[2], x[0]), cp[0], cp[1]);
+            ee_basis(x[0], x[1], x[2], x[3], b0, b1);
+        } else {
+            ldlt2_solve(sub(x[2], x[1]), sub(x[3], x[1]), sub(x[0], x[1]), cp[0], cp[1]);
+            pt_basis(x[0], x[1], x[2], x[3], b0, b1);
+        }
+        const double* ms_a = &T->mu_s_aniso[2 * i];
+        if (ms_a[0] * ms_a[0] + ms_a[1] * ms_a[1] == 0) {
+            T->mu_s_eff[i] = T->mu_s[i];
+            T->mu_k_eff[i] = T->mu_k[i];
+            continue;
+        }
+        double g[4];
+        friction_gamma(c, cp, g);
+        double tau[2] = { 0, 0 };
+        for (int k = 0; k < c.n; ++k) {
+            tau[0] += g[k] * dot(b0, v[k]);
+            tau[1] += g[k] * dot(b1, v[k]);
+        }
+        tau[0] *= T->mu_aniso[2 * i];
+        tau[1] *= T->mu_aniso[2 * i + 1];
+        double out[2];
+        aniso_mu_eff(tau, ms_a, &T->mu_k_aniso[2 * i], T->mu_s[i], T->mu_k[i], out);
+        T->mu_s_eff[i] = out[0];
+        T->mu_k_eff[i] = out[1];
+    }
+}
+
+void orc_tangential_lagged_mu(void* h, double* mu_s_eff, double* mu_k_eff)
+{
+    const Tangential* T = (const Tangential*)h;
+    std::copy(T->mu_s_eff.begin(), T->mu_s_eff.end(), mu_s_eff);
+    std::copy(T->mu_k_eff.begin(), T->mu_k_eff.end(), mu_k_eff);
+}
+
+void orc_aniso_mu_eff(const double* tau_aniso, const double* mu_s_aniso, const double* mu_k_aniso, double mu_s,
+    double mu_k, double* out)
+{
+    aniso_mu_eff(tau_aniso, mu_s_aniso, mu_k_aniso, mu_s, mu_k, out);
 }
 
 // The records are stored per type; reorder the per-collision arrays (built

@@ -94,6 +94,10 @@ def lib():
         L.orc_friction_hessian.argtypes = [vp, P, i64, P, P, d, i32, i32]
         L.orc_barrier_shape_derivative.restype = vp
         L.orc_barrier_shape_derivative.argtypes = [vp, P, P, i64, P, P, d, d, d, i32, i32]
+        L.orc_tangential_set_anisotropy.argtypes = [vp, P, P, P]
+        L.orc_tangential_update_lagged_mu.argtypes = [vp, P, P, P, P, P]
+        L.orc_tangential_lagged_mu.argtypes = [vp, P, P]
+        L.orc_aniso_mu_eff.argtypes = [P, P, P, d, d, P]
         L.orc_friction_mu.restype = d
         L.orc_friction_mu.argtypes = [i32, d, d, d, d]
         _lib = L
@@ -478,3 +482,27 @@ def barrier_shape_derivative(col, V, E, F, dhat, kappa, rest=None, dmin=0.0, phy
     L.orc_csr_get(h, _p(rp), _p(ci), _p(va))
     L.orc_csr_free(h)
     return rp, ci, va
+
+
+def tangential_set_anisotropy(t, mu_aniso=None, mu_s_aniso=None, mu_k_aniso=None):
+    arrs = [None if a is None else _f64(np.asarray(a).reshape(-1, 2)) for a in (mu_aniso, mu_s_aniso, mu_k_aniso)]
+    t._aniso = arrs
+    lib().orc_tangential_set_anisotropy(t.h, *[None if a is None else _p(a) for a in arrs])
+
+
+def tangential_update_lagged_mu(t, rest, lagged, velocities, E, F):
+    rest, lagged, velocities, E, F = _f64(rest), _f64(lagged), _f64(velocities), _i32(E), _i32(F)
+    lib().orc_tangential_update_lagged_mu(t.h, _p(rest), _p(lagged), _p(velocities), _p(E), _p(F))
+
+
+def tangential_lagged_mu(t):
+    ms, mk = np.zeros(len(t)), np.zeros(len(t))
+    lib().orc_tangential_lagged_mu(t.h, _p(ms), _p(mk))
+    return ms, mk
+
+
+def aniso_mu_eff(tau_aniso, mu_s_aniso, mu_k_aniso, mu_s, mu_k):
+    a, b, c = (_f64(np.asarray(x, np.float64).reshape(2)) for x in (tau_aniso, mu_s_aniso, mu_k_aniso))
+    out = np.zeros(2)
+    lib().orc_aniso_mu_eff(_p(a), _p(b), _p(c), float(mu_s), float(mu_k), _p(out))
+    return out[0], out[1]

@@ -115,3 +115,43 @@ def test_friction_fused_matches_separate(ipctk, oracle_mod):
     assert np.linalg.norm(g - g2) <= 1e-14 * np.linalg.norm(g2)
     H2 = D.hessian(tc, mesh, U, ipctk.PSDProjectionMethod.CLAMP)
     assert sp.linalg.norm(H - H2) == 0
+
+
+@pytest.mark.parametrize("name", ["two_sheet_16", "spheres_27", "cloth_4x48"])
+def test_anisotropic_friction(ipctk, oracle_mod, name):
+    """Slip scaling and lagged directional coefficients
+    (tangential_collisions.cpp:387-420, smooth_mu.cpp:117-171): lagged mu within
+    1e-12, energy, gradient and Hessian within 1e-10 of the oracle."""
+    sc, mesh, tc, tref, rng = _setup(ipctk, oracle_mod, name)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    n = len(tc)
+    aniso = rng.uniform(0.5, 2.0, (n, 2))
+    ms_a = rng.uniform(0.2, 0.8, (n, 2))
+    ms_a[::5] = 0  # some collisions stay isotropic
+    mk_a = rng.uniform(0.1, 0.5, (n, 2))
+    mk_a[::7] = 0
+    tc.set_anisotropy(aniso, ms_a, mk_a)
+    oracle_mod.tangential_set_anisotropy(tref, aniso, ms_a, mk_a)
+    lag = rng.uniform(-1, 1, V.shape) * 0.05 * sc["dhat"]
+    U = rng.uniform(-1, 1, V.shape) * EPS_V
+    tc.update_lagged_anisotropic_friction_coefficients(mesh, V, lag, U)
+    oracle_mod.tangential_update_lagged_mu(tref, V, lag, U, E, F)
+    ms, mk = tc.lagged_mu()
+    rms, rmk = oracle_mod.tangential_lagged_mu(tref)
+    _close(ms, rms)
+    _close(mk, rmk)
+    D = ipctk.FrictionPotential(EPS_V)
+    e, g, H = D.energy_gradient_hessian(tc, mesh, U, ipctk.PSDProjectionMethod.CLAMP)
+    e_ref = oracle_mod.friction_energy(tref, U, E, F, EPS_V)
+    assert abs(e - e_ref) <= REL * abs(e_ref)
+    g_ref = oracle_mod.friction_gradient(tref, U, E, F, EPS_V)
+    assert np.linalg.norm(g - g_ref) <= REL * np.linalg.norm(g_ref)
+    rp, ci, va = oracle_mod.friction_hessian(tref, U, E, F, EPS_V, psd="clamp")
+    H_ref = sp.csr_matrix((va, ci, rp), shape=H.shape)
+    assert sp.linalg.norm(H - H_ref) <= REL * sp.linalg.norm(H_ref)
+    # reset: back to the scalar coefficients
+    tc.reset_lagged_anisotropic_friction_coefficients()
+    a = tc.to_arrays()
+    ms, mk = tc.lagged_mu()
+    np.testing.assert_array_equal(ms, a["mu_s"])
+    np.testing.assert_array_equal(mk, a["mu_k"])

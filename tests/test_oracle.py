@@ -776,3 +776,57 @@ def test_shape_derivative_structure(oracle_mod):
     big = np.abs(D.data) > 1e-12 * abs(H).max()
     assert big.any()
     assert all(r // 3 in active and c // 3 in active for r, c in zip(D.row[big], D.col[big]))
+
+
+def test_anisotropic_mu_eff(oracle_mod):
+    """friction/test_anisotropic_friction.cpp:23-180: the elliptical effective
+    coefficients along a direction, the principal axes, the (1, 0) default for
+    a vanishing slip, and the isotropic fallback."""
+    for ms0, ms1, mk0, mk1 in ((0.1, 0.7, 0.3, 0.5), (0.9, 0.3, 0.5, 0.1)):
+        for ang in np.arange(0.0, 2 * np.pi, np.pi / 4):
+            t = np.array([np.cos(ang), np.sin(ang)]) * 3.0
+            s, k = oracle_mod.aniso_mu_eff(t, [ms0, ms1], [mk0, mk1], 0.5, 0.4)
+            d = t / np.linalg.norm(t)
+            assert s == pytest.approx(np.hypot(ms0 * d[0], ms1 * d[1]), rel=1e-14)
+            assert k == pytest.approx(np.hypot(mk0 * d[0], mk1 * d[1]), rel=1e-14)
+        assert oracle_mod.aniso_mu_eff([0, 2.0], [ms0, ms1], [mk0, mk1], 0.5, 0.4) == pytest.approx((ms1, mk1))
+        assert oracle_mod.aniso_mu_eff([1e-12, 1e-12], [ms0, ms1], [mk0, mk1], 0.5, 0.4) == pytest.approx((ms0, mk0))
+    assert oracle_mod.aniso_mu_eff([0.6, 0.8], [0, 0], [0, 0], 0.5, 0.4) == (0.5, 0.4)
+    # only the static coefficients directional: kinetic stays isotropic
+    assert oracle_mod.aniso_mu_eff([1.0, 0.0], [0.3, 0.6], [0, 0], 0.5, 0.4) == pytest.approx((0.3, 0.4))
+
+
+def test_anisotropic_friction_fd(oracle_mod):
+    """Anisotropic slip scaling and lagged directional coefficients: the
+    gradient and Hessian stay the derivatives of the energy at fixed lagged mu."""
+    import scipy.sparse as sps
+    sc, V, E, F, col, t, rng = _friction_case(oracle_mod, seed=8)
+    n = len(t)
+    ev = 1e-3
+    same = oracle_mod.friction_energy(t, np.zeros_like(V), E, F, ev)
+    oracle_mod.tangential_set_anisotropy(t, np.ones((n, 2)), None, None)
+    assert oracle_mod.friction_energy(t, np.zeros_like(V), E, F, ev) == same
+    oracle_mod.tangential_set_anisotropy(t, rng.uniform(0.5, 2.0, (n, 2)), rng.uniform(0.2, 0.8, (n, 2)),
+                                         rng.uniform(0.1, 0.5, (n, 2)))
+    U = rng.uniform(-1, 1, V.shape) * ev
+    oracle_mod.tangential_update_lagged_mu(t, V, np.zeros_like(V), U, E, F)
+    ms, mk = oracle_mod.tangential_lagged_mu(t)
+    assert np.any(ms != t.mu_s)
+    e = oracle_mod.friction_energy(t, U, E, F, ev)
+    g = oracle_mod.friction_gradient(t, U, E, F, ev)
+    h = 1e-6 * ev
+    for k in np.argsort(-np.abs(g))[:6]:
+        d = np.zeros(U.size)
+        d[k] = h
+        fd = (oracle_mod.friction_energy(t, U + d.reshape(U.shape), E, F, ev)
+              - oracle_mod.friction_energy(t, U - d.reshape(U.shape), E, F, ev)) / (2 * h)
+        assert fd == pytest.approx(g[k], rel=1e-5, abs=1e-9 * np.abs(g).max())
+        rp, ci, va = oracle_mod.friction_hessian(t, U, E, F, ev)
+    H = sps.csr_matrix((va, ci, rp), shape=(U.size, U.size))
+    for k in np.argsort(-np.abs(g))[:3]:
+        d = np.zeros(U.size)
+        d[k] = h
+        fd = (oracle_mod.friction_gradient(t, U + d.reshape(U.shape), E, F, ev)
+              - oracle_mod.friction_gradient(t, U - d.reshape(U.shape), E, F, ev)) / (2 * h)
+        col_k = H[:, k].toarray().ravel()
+        assert np.linalg.norm(fd - col_k) <= 1e-4 * np.linalg.norm(col_k) + 1e-9 * abs(va).max()
