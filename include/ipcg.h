@@ -412,6 +412,14 @@ int ipcg_tangential_reset_lagged_mu(ipcg_tangential* tangential);
 /* The lagged effective coefficients (n doubles each; either may be NULL). */
 int ipcg_tangential_lagged_mu(const ipcg_tangential* tangential, double* mu_s_effective, double* mu_k_effective);
 
+/* TangentialPotential::force(collisions, mesh, rest, lagged_displacements,
+ * velocities, BarrierPotential(dhat, stiffness, physical), dmin, no_mu)
+ * (tangential_potential.cpp:40-77, 333-410) with FrictionPotential(eps_v):
+ * 3 nV doubles (host or device). */
+int ipcg_friction_force(const ipcg_tangential* tangential, const ipcg_mesh* mesh, const double* rest_positions,
+                        const double* lagged_displacements, const double* velocities, double dhat, double stiffness,
+                        int use_physical_barrier, double dmin, double eps_v, int no_mu, double* force);
+
 /* FrictionPotential(eps_v) energy, gradient and Hessian at velocities
  * (tangential_potential.cpp:156-331; potential.cpp:36-222): any output may
  * be NULL; the Hessian's inner 2x2 blocks are projected with psd_method. */

@@ -879,6 +879,35 @@ int ipcg_tangential_lagged_mu(const ipcg_tangential* t, double* mu_s_eff, double
     });
 }
 
+int ipcg_friction_force(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* rest,
+    const double* lagged_displacements, const double* velocities, double dhat, double stiffness, int physical,
+    double dmin, double eps_v, int no_mu, double* force)
+{
+    return guarded([&] {
+        require(t && mesh && force && (mesh->nV == 0 || (rest && lagged_displacements && velocities)),
+            "NULL argument");
+        require(t->mesh == mesh, "tangential collisions were built on another mesh");
+        require(dhat > 0 && eps_v > 0, "dhat and eps_v must be positive");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        DBuf<double> vbuf;
+        const double* dR = stage_positions(m, rest, m->V0);
+        const double* dL = stage_positions(m, lagged_displacements, m->V1);
+        const double* dU = stage_positions(m, velocities, vbuf);
+        BarrierArgs a { dhat, stiffness, dmin, 0, IPCG_PSD_NONE };
+        barrier_options(physical, a);
+        double* fdev = force;
+        if (!is_device_ptr(force)) {
+            m->grad_stage.reserve(3 * m->nV + 1);
+            fdev = m->grad_stage.p;
+        }
+        friction_force(t, m, dR, dL, dU, a, eps_v, no_mu ? 1 : 0, fdev);
+        if (fdev != force)
+            IPCG_CUDA(cudaMemcpyAsync(force, fdev, sizeof(double) * 3 * m->nV, cudaMemcpyDeviceToHost, m->stream));
+        IPCG_CUDA(cudaStreamSynchronize(m->stream));
+    });
+}
+
 int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* U, double eps_v, int psd,
     double* energy, double* gradient, ipcg_csr** hessian)
 {

@@ -1652,6 +1652,56 @@ __global__ void k_tangential_update_lagged(ContactsView cv, const int* __restric
     mk_eff[i] = use_k ? sqrt(cc * cc + dd * dd) : mu_k[i];
 }
 
+// TangentialPotential::force (tangential_potential.cpp:40-77, 333-410):
+// F = -w N(x+u) mu f1(|tau_a|)/|tau_a| T(x+u) tau_a with tau = T^T v and
+// tau_a = mu_aniso . tau; N, the basis and the closest point at the lagged
+// positions (distance type classified there); scattered like a gradient.
+__global__ void k_friction_force(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    const double* __restrict__ rest, const double* __restrict__ lagged, const double* __restrict__ vel, Params P,
+    const double* __restrict__ aniso, const double* __restrict__ ms_eff, const double* __restrict__ mk_eff,
+    double eps_v, int no_mu, double* __restrict__ force)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    V3 x[4], v[4];
+    for (int k = 0; k < c.n; ++k) {
+        x[k] = load_v3(rest, c.vid[k]) + load_v3(lagged, c.vid[k]);
+        v[k] = load_v3(vel, c.vid[k]);
+    }
+    double d2;
+    if (c.type == CT_VV) d2 = point_point_distance(x[0], x[1]);
+    else if (c.type == CT_EV) d2 = point_edge_distance(x[0], x[1], x[2], point_edge_distance_type(x[0], x[1], x[2]));
+    else if (c.type == CT_EE)
+        d2 = edge_edge_distance(x[0], x[1], x[2], x[3], edge_edge_distance_type(x[0], x[1], x[2], x[3]));
+    else d2 = point_triangle_distance(x[0], x[1], x[2], x[3], point_triangle_distance_type(x[0], x[1], x[2], x[3]));
+    const double Nf = -P.kappa * barrier_fn<1, double>(P.kind, d2 - P.dmin2, P.xhat) * 2 * sqrt(d2) * P.scale;
+    double cp0, cp1;
+    V3 b0, b1;
+    tangential_frame(c.type, x, cp0, cp1, b0, b1);
+    double g[4] = { 0, 0, 0, 0 };
+    if (c.type == CT_VV) g[0] = 1, g[1] = -1;
+    else if (c.type == CT_EV) g[0] = 1, g[1] = cp0 - 1, g[2] = -cp0;
+    else if (c.type == CT_EE) g[0] = 1 - cp0, g[1] = cp0, g[2] = cp1 - 1, g[3] = -cp1;
+    else g[0] = 1, g[1] = cp0 + cp1 - 1, g[2] = -cp0, g[3] = -cp1;
+    double t0 = 0, t1 = 0;
+    for (int k = 0; k < c.n; ++k) {
+        t0 += g[k] * dot(b0, v[k]);
+        t1 += g[k] * dot(b1, v[k]);
+    }
+    const double ta0 = aniso[2 * i] * t0, ta1 = aniso[2 * i + 1] * t1;
+    const double ms = no_mu ? 1.0 : ms_eff[i], mk = no_mu ? 1.0 : mk_eff[i];
+    const double f1x = fr_mu_f1_over_x(sqrt(ta0 * ta0 + ta1 * ta1), ms, mk, eps_v);
+    const double s = -c.w * Nf * f1x;
+    for (int k = 0; k < c.n; ++k)
+        for (int d = 0; d < 3; ++d) {
+            const double val = s * ((g[k] * comp(b0, d)) * ta0 + (g[k] * comp(b1, d)) * ta1);
+            if (val != 0) atomicAdd(force + 3 * (int64_t)c.vid[k] + d, val);
+        }
+}
+
 __global__ void k_fill(double* __restrict__ p, int64_t n, double v)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -2306,6 +2356,23 @@ void tangential_build(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         IPCG_CUDA(cudaMemcpyAsync(t->mu_k_eff.p, mk.p, sizeof(double) * nt, cudaMemcpyDeviceToDevice, s));
     }
     IPCG_CUDA(cudaStreamSynchronize(s));
+}
+
+void friction_force(const ipcg_tangential* t, ipcg_mesh* m, const double* rest, const double* lagged,
+    const double* vel, const BarrierArgs& a, double eps_v, int no_mu, double* force_dev)
+{
+    cudaStream_t s = m->stream;
+    const ipcg_collisions* st = &t->st;
+    ContactsView cv { st->nvv, st->nev, st->nee, st->nfv, st->vv.p, st->ev.p, st->ee.p, st->fv.p, st->vv_w.p,
+        st->ev_w.p, st->ee_w.p, st->fv_w.p, st->ee_eps.p, st->ee_dtype.p };
+    const double xh = (2 * a.dmin + a.dhat) * a.dhat;
+    const Params P { a.kappa, a.dmin * a.dmin, xh, a.physical ? a.dhat / barrier_units(a.kind, xh) : 1.0,
+        IPCG_PSD_NONE, 0, a.kind };
+    IPCG_CUDA(cudaMemsetAsync(force_dev, 0, sizeof(double) * 3 * m->nV, s));
+    const int64_t n = st->size();
+    if (n)
+        IPCG_LAUNCH("k_friction_force", s, k_friction_force<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(cv, m->E.p, m->F.p,
+            rest, lagged, vel, P, t->mu_aniso.p, t->mu_s_eff.p, t->mu_k_eff.p, eps_v, no_mu, force_dev));
 }
 
 void tangential_update_lagged(ipcg_tangential* t, ipcg_mesh* m, const double* rest, const double* lagged,

@@ -313,6 +313,9 @@ void barrier_evaluate_friction(const ipcg_collisions* stencils, ipcg_mesh* m, co
 // barrier potential a, per-vertex mu (device); fills t (isotropic defaults).
 void tangential_build(const ipcg_collisions* normal, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     const double* mu_s_dev, const double* mu_k_dev, ipcg_tangential* t);
+// TangentialPotential::force into force_dev (3 nV, zeroed first; device inputs)
+void friction_force(const ipcg_tangential* t, ipcg_mesh* m, const double* rest, const double* lagged,
+    const double* vel, const BarrierArgs& a, double eps_v, int no_mu, double* force_dev);
 // update_lagged_anisotropic_friction_coefficients (device inputs)
 void tangential_update_lagged(ipcg_tangential* t, ipcg_mesh* m, const double* rest, const double* lagged,
     const double* vel);

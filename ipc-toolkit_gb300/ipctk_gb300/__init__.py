@@ -103,6 +103,7 @@ def _load():
         "ipcg_tangential_get": (i32, [P] + [P] * 10),
         "ipcg_friction_potential": (i32, [P, P, P, d, i32, P, P, PP]),
         "ipcg_tangential_set_anisotropy": (i32, [P, P, P, P]),
+        "ipcg_friction_force": (i32, [P, P, P, P, P, d, d, i32, d, d, i32, P]),
         "ipcg_tangential_update_lagged_mu": (i32, [P, P, P, P, P]),
         "ipcg_tangential_reset_lagged_mu": (i32, [P]),
         "ipcg_tangential_lagged_mu": (i32, [P, P, P]),
@@ -1094,6 +1095,16 @@ class FrictionPotential:
         h = C.c_void_p()
         self._call(collisions, mesh, velocities, int(project_hessian_to_psd), h=h)
         return _csr_to_scipy(h, 3 * mesh.num_vertices)
+
+    def force(self, collisions, mesh, rest_positions, lagged_displacements, velocities, normal_potential,
+              dmin: float = 0.0, no_mu: bool = False):
+        """TangentialPotential::force (tangential_potential.cpp:40-77)."""
+        R, L, U = _as_f64(rest_positions), _as_f64(lagged_displacements), _as_f64(velocities)
+        out = np.empty(3 * mesh.num_vertices)
+        _check(_load().ipcg_friction_force(collisions._h, mesh._h, _ptr(R), _ptr(L), _ptr(U), normal_potential.dhat,
+                                           normal_potential.stiffness, normal_potential._options & ~2, float(dmin),
+                                           self.eps_v, int(bool(no_mu)), _ptr(out)))
+        return out
 
     def energy_gradient_hessian(self, collisions, mesh, velocities, project_hessian_to_psd=PSDProjectionMethod.NONE):
         """Energy, gradient and Hessian from one call (velocities staged once)."""

@@ -2791,6 +2791,69 @@ void orc_tangential_update_lagged_mu(void* h, const double* rest, const double* 
     }
 }
 
+// TangentialPotential::force (tangential_potential.cpp:40-77, 333-410):
+// F = -w N(x+u) mu f1(|tau_a|)/|tau_a| T(x+u) tau_a, tau = T^T v,
+// tau_a = mu_aniso . tau, with N, P and the closest point at the lagged
+// positions x + u (distance type classified there) and the lagged effective
+// mu (1 with no_mu).
+void orc_friction_force(void* h, const double* rest, const double* lagged, const double* vel, int64_t nV,
+    const int32_t* E, const int32_t* F, double dhat, double kappa, double dmin, int physical, double eps_v, int no_mu,
+    double* force)
+{
+    const Tangential* T = (const Tangential*)h;
+    const BarrierParams P { dhat, kappa, dmin, physical };
+    const double xh = (2 * dmin + dhat) * dhat;
+    const int64_t n = T->N.size();
+    std::fill(force, force + 3 * nV, 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        Contact c;
+        contact_stencil(T->base, E, F, i, c);
+        V3 x[4], v[4];
+        for (int k = 0; k < c.n; ++k) {
+            x[k] = add(row(rest, c.vid[k]), row(lagged, c.vid[k]));
+            v[k] = row(vel, c.vid[k]);
+        }
+        double d2;
+        if (c.type == CT_VV) d2 = point_point_distance(x[0], x[1]);
+        else if (c.type == CT_EV) d2 = point_edge_distance(x[0], x[1], x[2], point_edge_distance_type(x[0], x[1], x[2]));
+        else if (c.type == CT_EE)
+            d2 = edge_edge_distance(x[0], x[1], x[2], x[3], edge_edge_distance_type(x[0], x[1], x[2], x[3]));
+        else d2 = point_triangle_distance(x[0], x[1], x[2], x[3], point_triangle_distance_type(x[0], x[1], x[2], x[3]));
+        double Nf = -kappa * barrier_any(barrier_kind(P), 1, d2 - dmin * dmin, xh) * 2 * std::sqrt(d2);
+        if (P.physical & 1) Nf *= dhat / (barrier_kind(P) == 1 ? 1.0 : xh * xh);
+        double cp[2] = { 0, 0 };
+        V3 b0, b1;
+        if (c.type == CT_VV) pp_basis(x[0], x[1], b0, b1);
+        else if (c.type == CT_EV) {
+            const V3 e = sub(x[2], x[1]);
+            cp[0] = dot(sub(x[0], x[1]), e) / sqnorm(e);
+            pe_basis(x[0], x[1], x[2], b0, b1);
+        } else if (c.type == CT_EE) {
+            ldlt2_solve(sub(x[1], x[0]), scale(sub(x[3], x[2]), -1.0), sub(x[2], x[0]), cp[0], cp[1]);
+            ee_basis(x[0], x[1], x[2], x[3], b0, b1);
+        } else {
+            ldlt2_solve(sub(x[2], x[1]), sub(x[3], x[1]), sub(x[0], x[1]), cp[0], cp[1]);
+            pt_basis(x[0], x[1], x[2], x[3], b0, b1);
+        }
+        double g[4];
+        friction_gamma(c, cp, g);
+        double tau[2] = { 0, 0 };
+        for (int k = 0; k < c.n; ++k) {
+            tau[0] += g[k] * dot(b0, v[k]);
+            tau[1] += g[k] * dot(b1, v[k]);
+        }
+        const double ta0 = T->mu_aniso[2 * i] * tau[0], ta1 = T->mu_aniso[2 * i + 1] * tau[1];
+        const double ms = no_mu ? 1.0 : T->mu_s_eff[i], mk = no_mu ? 1.0 : T->mu_k_eff[i];
+        const double f1x = mu_f1_over_x(std::sqrt(ta0 * ta0 + ta1 * ta1), ms, mk, eps_v);
+        const double s = -c.w * Nf * f1x;
+        for (int k = 0; k < c.n; ++k)
+            for (int d = 0; d < 3; ++d) {
+                const double Tr0 = g[k] * comp(b0, d), Tr1 = g[k] * comp(b1, d);
+                force[3 * c.vid[k] + d] += s * (Tr0 * ta0 + Tr1 * ta1);
+            }
+    }
+}
+
 void orc_tangential_lagged_mu(void* h, double* mu_s_eff, double* mu_k_eff)
 {
     const Tangential* T = (const Tangential*)h;

@@ -98,6 +98,7 @@ def lib():
         L.orc_tangential_update_lagged_mu.argtypes = [vp, P, P, P, P, P]
         L.orc_tangential_lagged_mu.argtypes = [vp, P, P]
         L.orc_aniso_mu_eff.argtypes = [P, P, P, d, d, P]
+        L.orc_friction_force.argtypes = [vp, P, P, P, i64, P, P, d, d, d, i32, d, i32, P]
         L.orc_friction_mu.restype = d
         L.orc_friction_mu.argtypes = [i32, d, d, d, d]
         _lib = L
@@ -506,3 +507,11 @@ def aniso_mu_eff(tau_aniso, mu_s_aniso, mu_k_aniso, mu_s, mu_k):
     out = np.zeros(2)
     lib().orc_aniso_mu_eff(_p(a), _p(b), _p(c), float(mu_s), float(mu_k), _p(out))
     return out[0], out[1]
+
+
+def friction_force(t, rest, lagged, velocities, E, F, dhat, kappa, eps_v, dmin=0.0, physical=0, no_mu=False):
+    rest, lagged, velocities, E, F = _f64(rest), _f64(lagged), _f64(velocities), _i32(E), _i32(F)
+    out = np.zeros(velocities.size)
+    lib().orc_friction_force(t.h, _p(rest), _p(lagged), _p(velocities), rest.shape[0], _p(E), _p(F), float(dhat),
+                             float(kappa), float(dmin), int(physical), float(eps_v), int(bool(no_mu)), _p(out))
+    return out

@@ -155,3 +155,24 @@ def test_anisotropic_friction(ipctk, oracle_mod, name):
     ms, mk = tc.lagged_mu()
     np.testing.assert_array_equal(ms, a["mu_s"])
     np.testing.assert_array_equal(mk, a["mu_k"])
+
+
+@pytest.mark.parametrize("name", ["two_sheet_16", "spheres_27"])
+@pytest.mark.parametrize("no_mu", [False, True])
+def test_friction_force(ipctk, oracle_mod, name, no_mu):
+    """TangentialPotential::force at lagged positions, with anisotropy, against
+    the oracle within 1e-10 relative."""
+    sc, mesh, tc, tref, rng = _setup(ipctk, oracle_mod, name, physical=True)
+    V, E, F = sc["V"], sc["E"], sc["F"]
+    n = len(tc)
+    aniso = rng.uniform(0.5, 2.0, (n, 2))
+    tc.set_anisotropy(aniso)
+    oracle_mod.tangential_set_anisotropy(tref, aniso)
+    lag = rng.uniform(-1, 1, V.shape) * 0.05 * sc["dhat"]
+    U = rng.uniform(-1, 1, V.shape) * EPS_V
+    B = ipctk.BarrierPotential(sc["dhat"], sc["kappa"], True)
+    D = ipctk.FrictionPotential(EPS_V)
+    f = D.force(tc, mesh, V, lag, U, B, no_mu=no_mu)
+    f_ref = oracle_mod.friction_force(tref, V, lag, U, E, F, sc["dhat"], sc["kappa"], EPS_V, physical=1, no_mu=no_mu)
+    assert np.linalg.norm(f_ref) > 0
+    assert np.linalg.norm(f - f_ref) <= REL * np.linalg.norm(f_ref)

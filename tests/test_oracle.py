@@ -830,3 +830,18 @@ def test_anisotropic_friction_fd(oracle_mod):
               - oracle_mod.friction_gradient(t, U - d.reshape(U.shape), E, F, ev)) / (2 * h)
         col_k = H[:, k].toarray().ravel()
         assert np.linalg.norm(fd - col_k) <= 1e-4 * np.linalg.norm(col_k) + 1e-9 * abs(va).max()
+
+
+def test_friction_force_is_minus_gradient_at_build_state(oracle_mod):
+    """With zero lagged displacement, isotropic coefficients and mu from the
+    build, the force at velocity v is minus the potential's gradient at v
+    (tangential_potential.cpp:333-410 against :184-231)."""
+    sc, V, E, F, col, t, rng = _friction_case(oracle_mod, seed=9)
+    ev = 1e-3
+    U = rng.uniform(-1, 1, V.shape) * ev
+    f = oracle_mod.friction_force(t, V, np.zeros_like(V), U, E, F, sc["dhat"], sc["kappa"], ev)
+    g = oracle_mod.friction_gradient(t, U, E, F, ev)
+    assert np.linalg.norm(f + g) <= 1e-12 * np.linalg.norm(g)
+    # no_mu: the force of unit coefficients
+    f1 = oracle_mod.friction_force(t, V, np.zeros_like(V), U, E, F, sc["dhat"], sc["kappa"], ev, no_mu=True)
+    assert np.linalg.norm(f1) > np.linalg.norm(f)
