@@ -385,6 +385,12 @@ int ipcg_tangential_destroy(ipcg_tangential* tangential);
 int ipcg_tangential_build(ipcg_tangential* tangential, const ipcg_mesh* mesh, const double* vertices,
                           const ipcg_collisions* collisions, double dhat, double stiffness,
                           int use_physical_barrier, const double* mu_s, const double* mu_k);
+/* The same on a batch mesh (ipcg_mesh_create_batch): dhat[n_scenes],
+ * stiffness[n_scenes] (host); the normal set must come from
+ * ipcg_collisions_build_batch on the same mesh. */
+int ipcg_tangential_build_batch(ipcg_tangential* tangential, const ipcg_mesh* mesh, const double* vertices,
+                                const ipcg_collisions* collisions, const double* dhat, const double* stiffness,
+                                int use_physical_barrier, const double* mu_s, const double* mu_k);
 /* counts[4]: VV, EV, EE, FV tangential collisions */
 int ipcg_tangential_counts(const ipcg_tangential* tangential, int64_t counts[4]);
 /* Any output may be NULL.  Stencils as in ipcg_collisions_get; per collision
@@ -425,6 +431,11 @@ int ipcg_friction_force(const ipcg_tangential* tangential, const ipcg_mesh* mesh
  * be NULL; the Hessian's inner 2x2 blocks are projected with psd_method. */
 int ipcg_friction_potential(const ipcg_tangential* tangential, const ipcg_mesh* mesh, const double* velocities,
                             double eps_v, int psd_method, double* energy, double* gradient, ipcg_csr** hessian);
+/* The same on a batch mesh: energies[n_scenes] (one eps_v for every scene);
+ * the gradient and the Hessian are the packed (block-diagonal) ones. */
+int ipcg_friction_potential_batch(const ipcg_tangential* tangential, const ipcg_mesh* mesh,
+                                  const double* velocities, double eps_v, int psd_method, double* energies,
+                                  double* gradient, ipcg_csr** hessian);
 
 typedef struct ipcg_candidates ipcg_candidates;
 int ipcg_candidates_create(ipcg_candidates** out);

@@ -753,24 +753,42 @@ int ipcg_tangential_destroy(ipcg_tangential* t)
     return guarded([&] { delete t; });
 }
 
-int ipcg_tangential_build(ipcg_tangential* t, const ipcg_mesh* mesh, const double* V, const ipcg_collisions* c,
-    double dhat, double stiffness, int physical, const double* mu_s, const double* mu_k)
+// dhat / stiffness: one value, or one per scene (scene_params) for batches
+static int tangential_build_call(ipcg_tangential* t, const ipcg_mesh* mesh, const double* V, const ipcg_collisions* c,
+    const double* dhat, const double* stiffness, int scene_params, int physical, const double* mu_s,
+    const double* mu_k)
 {
     return guarded([&] {
-        require(t && mesh && c && mu_s && mu_k && (V || mesh->nV == 0), "NULL argument");
-        require(mesh->n_scenes == 1, "friction on a batch mesh is not provided");
-        require(dhat > 0, "dhat must be positive");
+        require(t && mesh && c && dhat && stiffness && mu_s && mu_k && (V || mesh->nV == 0), "NULL argument");
+        require(scene_params || mesh->n_scenes == 1, "mesh is a batch: use ipcg_tangential_build_batch");
+        for (int64_t k = 0; k < (scene_params ? mesh->n_scenes : 1); ++k) require(dhat[k] > 0, "dhat must be positive");
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dV = stage_positions(m, V, m->V0);
-        BarrierArgs a { dhat, stiffness, c->dmin, 0, IPCG_PSD_NONE };
+        BarrierArgs a { dhat[0], stiffness[0], c->dmin, 0, IPCG_PSD_NONE };
         barrier_options(physical, a);
+        if (scene_params) {
+            a.scene_dhat = dhat;
+            a.scene_kappa = stiffness;
+        }
         DBuf<double> ms, mk;
         upload(ms, mu_s, m->nV, m->stream);
         upload(mk, mu_k, m->nV, m->stream);
         tangential_build(c, m, dV, a, ms.p, mk.p, t);
         t->mesh = mesh;
     });
+}
+
+int ipcg_tangential_build(ipcg_tangential* t, const ipcg_mesh* mesh, const double* V, const ipcg_collisions* c,
+    double dhat, double stiffness, int physical, const double* mu_s, const double* mu_k)
+{
+    return tangential_build_call(t, mesh, V, c, &dhat, &stiffness, 0, physical, mu_s, mu_k);
+}
+
+int ipcg_tangential_build_batch(ipcg_tangential* t, const ipcg_mesh* mesh, const double* V, const ipcg_collisions* c,
+    const double* dhat, const double* stiffness, int physical, const double* mu_s, const double* mu_k)
+{
+    return tangential_build_call(t, mesh, V, c, dhat, stiffness, 1, physical, mu_s, mu_k);
 }
 
 int ipcg_tangential_counts(const ipcg_tangential* t, int64_t counts[4])
@@ -887,6 +905,7 @@ int ipcg_friction_force(const ipcg_tangential* t, const ipcg_mesh* mesh, const d
         require(t && mesh && force && (mesh->nV == 0 || (rest && lagged_displacements && velocities)),
             "NULL argument");
         require(t->mesh == mesh, "tangential collisions were built on another mesh");
+        require(mesh->n_scenes == 1, "the friction force takes one normal potential: single-scene meshes");
         require(dhat > 0 && eps_v > 0, "dhat and eps_v must be positive");
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
@@ -908,11 +927,13 @@ int ipcg_friction_force(const ipcg_tangential* t, const ipcg_mesh* mesh, const d
     });
 }
 
-int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* U, double eps_v, int psd,
-    double* energy, double* gradient, ipcg_csr** hessian)
+// batch: the energy output holds one value per scene
+static int friction_call(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* U, double eps_v, int psd,
+    double* energy, double* gradient, ipcg_csr** hessian, int batch)
 {
     return guarded([&] {
         require(t && mesh && (U || mesh->nV == 0), "NULL argument");
+        require(batch || mesh->n_scenes == 1, "mesh is a batch: use ipcg_friction_potential_batch");
         require(t->mesh == mesh, "tangential collisions were built on another mesh");
         require(eps_v > 0, "eps_v must be positive");
         require(psd >= IPCG_PSD_NONE && psd <= IPCG_PSD_ABS, "Invalid type of PSD projection!");
@@ -943,6 +964,18 @@ int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, con
         }
         if (hessian) *hessian = H;
     });
+}
+
+int ipcg_friction_potential(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* U, double eps_v, int psd,
+    double* energy, double* gradient, ipcg_csr** hessian)
+{
+    return friction_call(t, mesh, U, eps_v, psd, energy, gradient, hessian, 0);
+}
+
+int ipcg_friction_potential_batch(const ipcg_tangential* t, const ipcg_mesh* mesh, const double* U, double eps_v,
+    int psd, double* energies, double* gradient, ipcg_csr** hessian)
+{
+    return friction_call(t, mesh, U, eps_v, psd, energies, gradient, hessian, 1);
 }
 
 int ipcg_barrier_shape_derivative(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,

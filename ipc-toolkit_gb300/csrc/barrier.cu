@@ -1485,6 +1485,46 @@ __global__ void __launch_bounds__(BLOCK) k_friction_energy(ContactsView cv, cons
     if (threadIdx.x == 0) partial[blockIdx.x] = sum;
 }
 
+// Batches: per-scene friction energies (a block almost always holds one
+// scene, as in k_energy_scenes).
+__global__ void __launch_bounds__(BLOCK) k_friction_energy_scenes(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const double* __restrict__ U, FrictionView f, SceneView sv, double* __restrict__ energy)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    int scene = -1;
+    if (i < n) {
+        Local c;
+        load_contact(cv, E, F, i, c);
+        scene = sv.of(c.vid[0]);
+        V3 v[4];
+        gather(U, c, v);
+        FrictionLocal L;
+        friction_setup(f, i, c, v, L);
+        e = L.scl * fr_mu_f0(L.nu, L.ms, L.mk, f.eps_v);
+    }
+    __shared__ int s_lo, s_hi;
+    if (threadIdx.x == 0) {
+        s_lo = 0x7fffffff;
+        s_hi = -1;
+    }
+    __syncthreads();
+    if (scene >= 0) {
+        atomicMin(&s_lo, scene);
+        atomicMax(&s_hi, scene);
+    }
+    __syncthreads();
+    if (s_lo == s_hi) {
+        typedef cub::BlockReduce<double, BLOCK> BR;
+        __shared__ typename BR::TempStorage tmp;
+        const double sum = BR(tmp).Sum(e);
+        if (threadIdx.x == 0 && s_hi >= 0) atomicAdd(energy + s_hi, sum);
+    } else if (scene >= 0 && e != 0) {
+        atomicAdd(energy + scene, e);
+    }
+}
+
 __global__ void __launch_bounds__(BLOCK) k_friction_gradient(ContactsView cv, const int* __restrict__ E,
     const int* __restrict__ F, const double* __restrict__ U, FrictionView f, double* __restrict__ grad)
 {
@@ -2058,7 +2098,10 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         // per-scene energies (batches)
         m->partial.reserve(ns + 2);
         IPCG_CUDA(cudaMemsetAsync(m->partial.p, 0, sizeof(double) * ns, s));
-        if (n > 0)
+        if (n > 0 && fr)
+            IPCG_LAUNCH("k_friction_energy_scenes", s, k_friction_energy_scenes<<<nblk, BLOCK, 0, s>>>(cv, m->E.p,
+                m->F.p, V, *fr, sv, m->partial.p));
+        else if (n > 0)
             IPCG_LAUNCH("k_energy_scenes", s, k_energy_scenes<<<nblk, BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V, sp, sv,
                 m->partial.p));
         IPCG_CUDA(cudaMemcpyAsync(energy_host, m->partial.p, sizeof(double) * ns, cudaMemcpyDefault, s));

@@ -104,6 +104,8 @@ def _load():
         "ipcg_friction_potential": (i32, [P, P, P, d, i32, P, P, PP]),
         "ipcg_tangential_set_anisotropy": (i32, [P, P, P, P]),
         "ipcg_friction_force": (i32, [P, P, P, P, P, d, d, i32, d, d, i32, P]),
+        "ipcg_tangential_build_batch": (i32, [P, P, P, P, P, P, i32, P, P]),
+        "ipcg_friction_potential_batch": (i32, [P, P, P, d, i32, P, P, PP]),
         "ipcg_tangential_update_lagged_mu": (i32, [P, P, P, P, P]),
         "ipcg_tangential_reset_lagged_mu": (i32, [P]),
         "ipcg_tangential_lagged_mu": (i32, [P, P, P]),
@@ -1007,9 +1009,17 @@ class TangentialCollisions:
         nV = mesh.num_vertices
         ms = np.ascontiguousarray(np.broadcast_to(np.asarray(mu_s, np.float64), (nV,)))
         mk = np.ascontiguousarray(np.broadcast_to(np.asarray(mu_s if mu_k is None else mu_k, np.float64), (nV,)))
-        _check(_load().ipcg_tangential_build(self._h, mesh._h, _ptr(V), collisions._h, normal_potential.dhat,
-                                             normal_potential.stiffness, normal_potential._options, _ptr(ms),
-                                             _ptr(mk)))
+        if isinstance(mesh, SceneBatch):
+            # a BatchBarrierPotential (or any potential): one dhat / stiffness per scene
+            dh = mesh.per_scene(normal_potential.dhat)
+            kap = mesh.per_scene(normal_potential.stiffness)
+            opts = int(getattr(normal_potential, "use_physical_barrier", False))
+            _check(_load().ipcg_tangential_build_batch(self._h, mesh._h, _ptr(V), collisions._h, _ptr(dh),
+                                                       _ptr(kap), opts, _ptr(ms), _ptr(mk)))
+        else:
+            _check(_load().ipcg_tangential_build(self._h, mesh._h, _ptr(V), collisions._h, normal_potential.dhat,
+                                                 normal_potential.stiffness, normal_potential._options, _ptr(ms),
+                                                 _ptr(mk)))
         self._mesh = mesh
 
     def counts(self):
@@ -1071,15 +1081,16 @@ class FrictionPotential:
 
     def _call(self, collisions, mesh, velocities, psd, e=None, g=None, h=None):
         U = _as_f64(velocities)
-        _check(_load().ipcg_friction_potential(collisions._h, mesh._h, _ptr(U), self.eps_v, int(psd),
-                                               _ptr(e) if e is not None else None,
-                                               _ptr(g) if g is not None else None,
-                                               C.byref(h) if h is not None else None))
+        fn = _load().ipcg_friction_potential_batch if isinstance(mesh, SceneBatch) else _load().ipcg_friction_potential
+        _check(fn(collisions._h, mesh._h, _ptr(U), self.eps_v, int(psd), _ptr(e) if e is not None else None,
+                  _ptr(g) if g is not None else None, C.byref(h) if h is not None else None))
 
-    def __call__(self, collisions: TangentialCollisions, mesh: CollisionMesh, velocities) -> float:
-        e = np.zeros(1)
+    def __call__(self, collisions: TangentialCollisions, mesh: CollisionMesh, velocities):
+        """The friction energy (on a SceneBatch: one energy per scene)."""
+        batch = isinstance(mesh, SceneBatch)
+        e = np.zeros(mesh.num_scenes if batch else 1)
         self._call(collisions, mesh, velocities, 0, e=e)
-        return float(e[0])
+        return e if batch else float(e[0])
 
     def gradient(self, collisions, mesh, velocities):
         U = _as_f64(velocities)
@@ -1109,7 +1120,8 @@ class FrictionPotential:
     def energy_gradient_hessian(self, collisions, mesh, velocities, project_hessian_to_psd=PSDProjectionMethod.NONE):
         """Energy, gradient and Hessian from one call (velocities staged once)."""
         U = _as_f64(velocities)
-        e = np.zeros(1)
+        batch = isinstance(mesh, SceneBatch)
+        e = np.zeros(mesh.num_scenes if batch else 1)
         if _is_torch_cuda(U):
             import torch
             g = torch.empty(U.numel(), dtype=torch.float64, device=U.device)
@@ -1117,7 +1129,7 @@ class FrictionPotential:
             g = np.empty(3 * mesh.num_vertices)
         h = C.c_void_p()
         self._call(collisions, mesh, U, int(project_hessian_to_psd), e=e, g=g, h=h)
-        return float(e[0]), g, _csr_to_scipy(h, 3 * mesh.num_vertices)
+        return (e if batch else float(e[0])), g, _csr_to_scipy(h, 3 * mesh.num_vertices)
 
 
 class Candidates:

@@ -176,3 +176,38 @@ def test_friction_force(ipctk, oracle_mod, name, no_mu):
     f_ref = oracle_mod.friction_force(tref, V, lag, U, E, F, sc["dhat"], sc["kappa"], EPS_V, physical=1, no_mu=no_mu)
     assert np.linalg.norm(f_ref) > 0
     assert np.linalg.norm(f - f_ref) <= REL * np.linalg.norm(f_ref)
+
+
+def test_friction_batch_equals_scenes(ipctk):
+    """Friction on a SceneBatch: per-scene energies, the packed gradient and
+    the block-diagonal Hessian equal each scene's own evaluation."""
+    from ipctk_gb300 import scenes
+    parts = [scenes.two_sheet(side=s, seed=s) for s in (8, 12, 16)]
+    batch = ipctk.SceneBatch([(p["V"], p["E"], p["F"]) for p in parts])
+    V = np.concatenate([p["V"] for p in parts])
+    dh = [p["dhat"] for p in parts]
+    kap = [p["kappa"] for p in parts]
+    col = ipctk.NormalCollisions()
+    col.build(batch, V, dh)
+    tc = ipctk.TangentialCollisions()
+    tc.build(batch, V, col, ipctk.BatchBarrierPotential(dh, kap), 0.5, 0.4)
+    rng = np.random.Generator(np.random.PCG64(2))
+    U = rng.uniform(-1, 1, V.shape) * EPS_V
+    D = ipctk.FrictionPotential(EPS_V)
+    e, g, H = D.energy_gradient_hessian(tc, batch, U, ipctk.PSDProjectionMethod.CLAMP)
+    off = 0
+    blocks = []
+    for k, p in enumerate(parts):
+        n = len(p["V"])
+        m = ipctk.CollisionMesh(p["V"], p["E"], p["F"])
+        c = ipctk.NormalCollisions()
+        c.build(m, p["V"], p["dhat"])
+        t = ipctk.TangentialCollisions()
+        t.build(m, p["V"], c, ipctk.BarrierPotential(p["dhat"], p["kappa"]), 0.5, 0.4)
+        ek, gk, Hk = D.energy_gradient_hessian(t, m, U[off:off + n], ipctk.PSDProjectionMethod.CLAMP)
+        assert e[k] == pytest.approx(ek, rel=1e-12)
+        np.testing.assert_allclose(g[3 * off:3 * (off + n)], gk, rtol=0, atol=1e-14 * np.abs(gk).max())
+        blocks.append(Hk)
+        off += n
+    Hb = sp.block_diag(blocks)
+    assert sp.linalg.norm(H - Hb) <= 1e-14 * sp.linalg.norm(Hb)
