@@ -255,8 +255,10 @@ int ipcg_barrier_batch(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
  * respect to the rest positions, ndof x ndof (rows: displacement dofs,
  * columns: rest dofs; not symmetric).  Per collision w times the unprojected
  * local Hessian, edge-edge collisions in the reference's mollified form with
- * eps_x from the rest positions.  Sets built with area weighting (nonzero
- * weight gradients) are not provided. */
+ * eps_x from the rest positions; with area weighting also
+ * (grad_u f / w)(grad_x w)^T, grad_x w from the rest mesh's area Jacobians
+ * (collision_mesh.cpp:376-432) summed over each record's merged candidates.
+ * Area-weighted IMPROVED_MAX_APPROX sets are not provided. */
 int ipcg_barrier_shape_derivative(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
                                   const double* vertices, double dhat, double stiffness,
                                   int use_physical_barrier, ipcg_csr** out);

@@ -985,7 +985,8 @@ int ipcg_barrier_shape_derivative(const ipcg_collisions* c, const ipcg_mesh* mes
         require(c && mesh && out && (V || mesh->nV == 0), "NULL argument");
         require(mesh->n_scenes == 1, "mesh is a batch: shape derivatives are per scene");
         require(c->built_with_shape, "Shape derivative is not computed for collisions!");
-        require(!c->use_area_weighting, "shape derivatives of area-weighted collision sets are not provided");
+        require(!(c->built_with_area && c->set_type != IPCG_COLLISION_SET_IPC),
+            "shape derivatives of area-weighted IMPROVED_MAX_APPROX sets are not provided");
         require(dhat > 0, "dhat must be positive");
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
@@ -996,7 +997,8 @@ int ipcg_barrier_shape_derivative(const ipcg_collisions* c, const ipcg_mesh* mes
         a.shape = 1;
         ipcg_csr* H = new ipcg_csr();
         try {
-            barrier_evaluate(c, m, dV, a, nullptr, nullptr, H);
+            if (c->built_with_area) shape_derivative_area(c, m, dV, a, H);
+            else barrier_evaluate(c, m, dV, a, nullptr, nullptr, H);
         } catch (...) {
             delete H;
             throw;

@@ -1353,6 +1353,224 @@ __global__ void __launch_bounds__(LH_BLOCK) k_shape_local_ee(ContactsView cv, co
         }
 }
 
+// ---- Area-weighted shape derivative (normal_potential.cpp:310-416 with the
+// weight gradients of normal_collisions_builder.cpp:146,181-191 and the area
+// Jacobians of collision_mesh.cpp:376-432) ----
+// Both terms are emitted as (row * ndof + col, value) triplets and summed
+// by key: the second term from the local slabs, the first term
+// (grad_u f / w)(grad_x w)^T with grad_x w summed over the record's weight
+// sources, 0.25 times a vertex's or the two edges' area Jacobians.
+struct ShapeSources {
+    const int *vv_off, *ev_off;
+    const int2 *vv_src, *ev_src;
+    const int *vf_off, *vf_adj, *ef_off, *ef_adj, *ve_off, *ve_adj;
+};
+__device__ __forceinline__ int vertex_jac_entries(const ShapeSources& S, int v)
+{
+    const int nf = S.vf_off[v + 1] - S.vf_off[v];
+    return nf > 0 ? 9 * nf : 6 * (S.ve_off[v + 1] - S.ve_off[v]);
+}
+__device__ __forceinline__ int edge_jac_entries(const ShapeSources& S, int e)
+{
+    const int nf = S.ef_off[e + 1] - S.ef_off[e];
+    return nf > 0 ? 9 * nf : 6;
+}
+// d|A_f|/dx / 3 over the face's 9 rest dofs: n x (t_{i+2} - t_{i+1}) / 6
+__device__ __forceinline__ void face_area_grad3(const double* __restrict__ R, const int* __restrict__ F, int f,
+    double* g)
+{
+    const V3 t0 = load_v3(R, F[3 * f]), t1 = load_v3(R, F[3 * f + 1]), t2 = load_v3(R, F[3 * f + 2]);
+    V3 n = cross(t1 - t0, t2 - t0);
+    const double nn = sqnorm(n);
+    if (nn > 0) {
+        const double r = sqrt(nn);
+        n = V3 { n.x / r, n.y / r, n.z / r };
+    }
+    const V3 a = cross(n, t2 - t1) * 0.5, b = cross(n, t0 - t2) * 0.5, c = cross(n, t1 - t0) * 0.5;
+    const V3 gg[3] = { a, b, c };
+    for (int k = 0; k < 3; ++k)
+        for (int d = 0; d < 3; ++d) g[3 * k + d] = (1.0 / 3.0) * comp(gg[k], d);
+}
+// d|e|/dx over the edge's 6 rest dofs
+__device__ __forceinline__ void edge_len_grad(const double* __restrict__ R, const int* __restrict__ E, int e, double* g)
+{
+    const V3 d = load_v3(R, E[2 * e]) - load_v3(R, E[2 * e + 1]);
+    const double l = sqrt(sqnorm(d));
+    g[0] = d.x / l, g[1] = d.y / l, g[2] = d.z / l;
+    g[3] = -g[0], g[4] = -g[1], g[5] = -g[2];
+}
+// visit (dof, value) of 0.25 x an entity's area Jacobian
+template <class Fn> __device__ void visit_vertex_jac(const ShapeSources& S, const double* R, const int* E,
+    const int* F, int v, Fn&& fn)
+{
+    const int f0 = S.vf_off[v], f1 = S.vf_off[v + 1];
+    if (f1 > f0) {
+        for (int q = f0; q < f1; ++q) {
+            const int f = S.vf_adj[q];
+            double g[9];
+            face_area_grad3(R, F, f, g);
+            for (int k = 0; k < 3; ++k)
+                for (int d = 0; d < 3; ++d) fn(3 * (int64_t)F[3 * f + k] + d, 0.25 * g[3 * k + d]);
+        }
+    } else {
+        for (int q = S.ve_off[v]; q < S.ve_off[v + 1]; ++q) {
+            const int e = S.ve_adj[q];
+            double g[6];
+            edge_len_grad(R, E, e, g);
+            for (int k = 0; k < 2; ++k)
+                for (int d = 0; d < 3; ++d) fn(3 * (int64_t)E[2 * e + k] + d, 0.25 * (0.5 * g[3 * k + d]));
+        }
+    }
+}
+template <class Fn> __device__ void visit_edge_jac(const ShapeSources& S, const double* R, const int* E,
+    const int* F, int e, Fn&& fn)
+{
+    const int f0 = S.ef_off[e], f1 = S.ef_off[e + 1];
+    if (f1 > f0) {
+        for (int q = f0; q < f1; ++q) {
+            const int f = S.ef_adj[q];
+            double g[9];
+            face_area_grad3(R, F, f, g);
+            for (int k = 0; k < 3; ++k)
+                for (int d = 0; d < 3; ++d) fn(3 * (int64_t)F[3 * f + k] + d, 0.25 * g[3 * k + d]);
+        }
+    } else {
+        double g[6];
+        edge_len_grad(R, E, e, g);
+        for (int k = 0; k < 2; ++k)
+            for (int d = 0; d < 3; ++d) fn(3 * (int64_t)E[2 * e + k] + d, 0.25 * g[3 * k + d]);
+    }
+}
+// the weight sources of contact i: calls fn(s0, s1) for each
+template <class Fn> __device__ void visit_sources(const ContactsView& cv, const ShapeSources& S, int64_t i, Fn&& fn)
+{
+    if (i < cv.nvv) {
+        for (int q = S.vv_off[i]; q < S.vv_off[i + 1]; ++q) fn(S.vv_src[q].x, S.vv_src[q].y);
+    } else if (i < cv.nvv + cv.nev) {
+        const int64_t j = i - cv.nvv;
+        for (int q = S.ev_off[j]; q < S.ev_off[j + 1]; ++q) fn(S.ev_src[q].x, S.ev_src[q].y);
+    } else if (i < cv.nvv + cv.nev + cv.nee) {
+        const int2 p = cv.ee[i - cv.nvv - cv.nev];
+        fn(p.x, p.y);
+    } else {
+        const int2 p = cv.fv[i - cv.nvv - cv.nev - cv.nee];
+        fn(p.y, -1);
+    }
+}
+
+__global__ void k_shape_count(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    ShapeSources S, int64_t* __restrict__ counts)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    const int N = 3 * c.n;
+    int64_t cnt = (int64_t)N * N;
+    visit_sources(cv, S, i, [&](int s0, int s1) {
+        cnt += (int64_t)N * (s1 < 0 ? vertex_jac_entries(S, s0) : edge_jac_entries(S, s0) + edge_jac_entries(S, s1));
+    });
+    counts[i] = cnt;
+}
+
+__global__ void k_shape_emit(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    const double* __restrict__ V, const double* __restrict__ R, const Params* __restrict__ sp, SceneView sv, Slab hs,
+    ShapeSources S, const int64_t* __restrict__ offs, int64_t ndof, unsigned long long* __restrict__ keys,
+    double* __restrict__ vals)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    const int N = 3 * c.n;
+    int64_t o = offs[i];
+    // second term: the local matrix of the slab
+    for (int a = 0; a < c.n; ++a)
+        for (int b = 0; b < c.n; ++b)
+            for (int k = 0; k < 3; ++k)
+                for (int l = 0; l < 3; ++l) {
+                    keys[o] = (unsigned long long)((3 * (int64_t)c.vid[a] + k) * ndof + 3 * (int64_t)c.vid[b] + l);
+                    vals[o] = hs.at(i, (3 * a + k) * N + 3 * b + l);
+                    ++o;
+                }
+    // first term: q = (per-collision gradient) / w, times the weight gradient
+    const Params P = sp[sv.of(c.vid[0])];
+    V3 x[4];
+    gather(V, c, x);
+    double q[12];
+    double gm[12];
+    bool act;
+    const double mm = mollifier(c, x, gm, nullptr, act);
+    if (mm <= 0) {
+        for (int r = 0; r < N; ++r) q[r] = 0;
+    } else {
+        double g[12];
+        const double d = contact_distance(c, x, g, nullptr);
+        const double fd = fd1(P, d);
+        if (c.type != CT_EE) {
+            for (int r = 0; r < N; ++r) q[r] = ((c.w * fd) * g[r]) / c.w;
+        } else {
+            const double fv = fval(P, d);
+            for (int r = 0; r < N; ++r) q[r] = ((c.w * fv) * (act ? gm[r] : 0.0) + (c.w * mm * fd) * g[r]) / c.w;
+        }
+    }
+    auto emit = [&](int64_t col, double wv) {
+        for (int a = 0; a < c.n; ++a)
+            for (int k = 0; k < 3; ++k) {
+                keys[o] = (unsigned long long)((3 * (int64_t)c.vid[a] + k) * ndof + col);
+                vals[o] = q[3 * a + k] * wv;
+                ++o;
+            }
+    };
+    visit_sources(cv, S, i, [&](int s0, int s1) {
+        if (s1 < 0) visit_vertex_jac(S, R, E, F, s0, emit);
+        else {
+            visit_edge_jac(S, R, E, F, s0, emit);
+            visit_edge_jac(S, R, E, F, s1, emit);
+        }
+    });
+}
+
+__global__ void k_iota(int* __restrict__ p, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = i;
+}
+__global__ void k_gather_vals(const double* __restrict__ v, const int* __restrict__ idx, int n, double* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = v[idx[i]];
+}
+// duplicates summed in key order; column of each unique key
+__global__ void k_sum_key_runs(const unsigned long long* __restrict__ uniq, const int* __restrict__ counts,
+    const int* __restrict__ offs, const int* __restrict__ d_num, const double* __restrict__ v, int64_t ndof,
+    int* __restrict__ col, double* __restrict__ val)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *d_num) return;
+    double s = 0.0;
+    for (int j = offs[i], e = offs[i] + counts[i]; j < e; ++j) s += v[j];
+    col[i] = (int)((int64_t)uniq[i] % ndof);
+    val[i] = s;
+}
+// row pointers of sorted unique keys: the first key of each row
+__global__ void k_rows_from_keys(const unsigned long long* __restrict__ uniq, const int* __restrict__ d_num,
+    int64_t ndof, int64_t* __restrict__ row_ptr)
+{
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > ndof) return;
+    const unsigned long long key = (unsigned long long)(r * ndof);
+    int lo = 0, hi = *d_num;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (uniq[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    row_ptr[r] = lo;
+}
+
 // ---- Friction (tangential_potential.cpp:156-331, friction/smooth_mu.cpp,
 // friction/smooth_friction_mollifier.cpp; isotropic) ----
 __device__ __forceinline__ double fr_smooth_mu(double y, double ms, double mk, double ev)
@@ -2322,6 +2540,97 @@ void barrier_gauss_newton(const ipcg_collisions* cs, ipcg_mesh* m, const double*
         IPCG_CUDA(cudaMemcpyAsync(qf_host, m->partial.p + nblk, sizeof(double), cudaMemcpyDeviceToHost, s));
         IPCG_CUDA(cudaStreamSynchronize(s));
     }
+}
+
+void shape_derivative_area(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    ipcg_csr* out)
+{
+    cudaStream_t s = m->stream;
+    ensure_adjacency(m);
+    ContactsView cv { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
+        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
+    const int64_t n = cs->size();
+    const int64_t ndof = 3 * m->nV;
+    Params P0;
+    const Params* sp = upload_params(cs, m, a, P0);
+    const SceneView sv = scene_view(m);
+    out->rows = ndof;
+    out->stream = s;
+    out->row_ptr.reserve(ndof + 1, s);
+    if (n == 0) {
+        IPCG_CUDA(cudaMemsetAsync(out->row_ptr.p, 0, sizeof(int64_t) * (ndof + 1), s));
+        out->nnz = 0;
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        return;
+    }
+    // second-term local matrices
+    m->hs.reserve(144 * (n + 1));
+    const Slab slab { m->hs.p, n + 1 };
+    m->proj.reserve(n + 1);
+    const int64_t first[4] = { 0, cs->nvv, cs->nvv + cs->nev, cs->nvv + cs->nev + cs->nee };
+    const int64_t count[4] = { cs->nvv, cs->nev, cs->nee, cs->nfv };
+    if (count[0])
+        IPCG_LAUNCH("k_local_hessian_vv", s, k_local_hessian<CT_VV><<<grid_for(count[0], LH_BLOCK), LH_BLOCK, 0, s>>>(
+            cv, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[0], count[0]));
+    if (count[1])
+        IPCG_LAUNCH("k_local_hessian_ev", s, k_local_hessian<CT_EV><<<grid_for(count[1], LH_BLOCK), LH_BLOCK, 0, s>>>(
+            cv, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[1], count[1]));
+    if (count[2])
+        IPCG_LAUNCH("k_shape_local_ee", s, k_shape_local_ee<<<grid_for(count[2], LH_BLOCK), LH_BLOCK, 0, s>>>(cv,
+            m->E.p, m->F.p, V, m->rest.p, sp, sv, slab, first[2], count[2]));
+    if (count[3])
+        IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], LH_BLOCK), LH_BLOCK, 0, s>>>(
+            cv, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[3], count[3]));
+    const ShapeSources S { cs->vv_src_off.p, cs->ev_src_off.p, cs->vv_src.p, cs->ev_src.p, m->vf_off.p, m->vf_adj.p,
+        m->ef_off.p, m->ef_adj.p, m->ve_off.p, m->ve_adj.p };
+    // triplet counts and offsets
+    PBuf<int64_t> cnt, offs;
+    cnt.reserve(n + 1, s);
+    offs.reserve(n + 1, s);
+    IPCG_CUDA(cudaMemsetAsync(cnt.p + n, 0, sizeof(int64_t), s));
+    IPCG_LAUNCH("k_shape_count", s, k_shape_count<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(cv, m->E.p, m->F.p, S,
+        cnt.p));
+    exclusive_sum_i64(m, s, cnt.p, offs.p, (int)(n + 1));
+    int64_t T = 0;
+    IPCG_CUDA(cudaMemcpyAsync(&T, offs.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    if (T >= INT32_MAX) throw Error(IPCG_ERR_INVALID, "shape derivative too large (2^31 triplets)");
+    const int Ti = (int)T;
+    PBuf<unsigned long long> keys, skeys, uniq;
+    PBuf<double> vals, svals;
+    PBuf<int> idx, sidx, rcnt, roff;
+    keys.reserve(T + 1, s);
+    skeys.reserve(T + 1, s);
+    uniq.reserve(T + 1, s);
+    vals.reserve(T + 1, s);
+    svals.reserve(T + 1, s);
+    idx.reserve(T + 1, s);
+    sidx.reserve(T + 1, s);
+    rcnt.reserve(T + 2, s);
+    roff.reserve(T + 2, s);
+    IPCG_LAUNCH("k_shape_emit", s, k_shape_emit<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(cv, m->E.p, m->F.p, V,
+        m->rest.p, sp, sv, slab, S, offs.p, ndof, keys.p, vals.p));
+    IPCG_LAUNCH("k_iota", s, k_iota<<<grid_for(T, BLOCK), BLOCK, 0, s>>>(idx.p, Ti));
+    const int kbits = std::min(64, bits_for(ndof) * 2 + 1);
+    sort_pairs_u64(m, s, keys.p, skeys.p, idx.p, sidx.p, Ti, kbits);
+    IPCG_LAUNCH("k_gather_vals", s, k_gather_vals<<<grid_for(T, BLOCK), BLOCK, 0, s>>>(vals.p, sidx.p, Ti, svals.p));
+    m->counters.reserve(32);
+    int* d_num = m->counters.p + 28;
+    IPCG_CUDA(cudaMemsetAsync(rcnt.p, 0, sizeof(int) * (T + 1), s));
+    rle_u64(m, s, skeys.p, uniq.p, rcnt.p, d_num, Ti);
+    exclusive_sum_i32(m, s, rcnt.p, roff.p, Ti + 1);
+    int nnz = 0;
+    IPCG_CUDA(cudaMemcpyAsync(&nnz, d_num, sizeof(int), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    out->col.reserve(nnz + 1, s);
+    out->val.reserve(nnz + 1, s);
+    out->nnz = nnz;
+    if (nnz)
+        IPCG_LAUNCH("k_sum_key_runs", s, k_sum_key_runs<<<grid_for(nnz, BLOCK), BLOCK, 0, s>>>(uniq.p, rcnt.p, roff.p,
+            d_num, svals.p, ndof, out->col.p, out->val.p));
+    IPCG_LAUNCH("k_rows_from_keys", s, k_rows_from_keys<<<grid_for(ndof + 1, BLOCK), BLOCK, 0, s>>>(uniq.p, d_num,
+        ndof, out->row_ptr.p));
+    IPCG_CUDA(cudaStreamSynchronize(s));
 }
 
 void barrier_evaluate_friction(const ipcg_collisions* stencils, ipcg_mesh* m, const double* U, const FrictionView& f,

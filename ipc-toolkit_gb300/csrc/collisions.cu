@@ -46,6 +46,9 @@ struct Out {
     unsigned long long* ev; // EV keys (e,v)
     double* vv_w;           // VV / EV record weights (area weighting; else null)
     double* ev_w;
+    int2* vv_src;           // VV / EV record weight sources (area-weighted shape derivatives; else null)
+    int2* ev_src;
+    int2 src;               // the weight source of the candidate being filtered
     const double* varea;    // rest-mesh areas (area weighting; else null)
     const double* earea;
     unsigned long long* ee; // EE keys (ea,eb)
@@ -62,12 +65,14 @@ __device__ __forceinline__ void put_vv(const Out& o, int a, int b, double w)
     const int s = append(o.count + 0);
     o.vv[s] = key2(min(a, b), max(a, b));
     if (o.vv_w) o.vv_w[s] = w;
+    if (o.vv_src) o.vv_src[s] = o.src;
 }
 __device__ __forceinline__ void put_ev(const Out& o, int e, int v, double w)
 {
     const int s = append(o.count + 1);
     o.ev[s] = key2(e, v);
     if (o.ev_w) o.ev_w[s] = w;
+    if (o.ev_src) o.ev_src[s] = o.src;
 }
 // Area weights (normal_collisions_builder.cpp:146, 181-183): FV and its
 // reductions vertex_area(v) / 4, EE and its reductions
@@ -101,6 +106,7 @@ __global__ void k_filter_ee(const int2* __restrict__ cand, int n, const double* 
     const double cr = ee_cross_sqnorm(xa0, xa1, xb0, xb1);
     const int dtype = cr < eps_x ? (int)EA_EB : actual;
     const double w = ee_weight(o.earea, ea, eb);
+    o.src = make_int2(ea, eb);
     switch (dtype) {
     case EA0_EB0: put_vv(o, a0, b0, w); break;
     case EA0_EB1: put_vv(o, a0, b1, w); break;
@@ -137,6 +143,7 @@ __global__ void k_filter_fv(const int2* __restrict__ cand, int n, const double* 
     const double d = point_triangle_distance(p, t0, t1, t2, dtype);
     if (!(d < offset_sqr)) return;
     const double w = fv_weight(o.varea, vi);
+    o.src = make_int2(vi, -1);
     switch (dtype) {
     case P_T0: put_vv(o, vi, f0, w); break;
     case P_T1: put_vv(o, vi, f1, w); break;
@@ -417,6 +424,12 @@ __global__ void k_ee_group_runs(const int* __restrict__ counts, const int* __res
     keep[i] = sum != 0 ? 1 : 0;
 }
 
+__global__ void k_gather_src(const int2* __restrict__ src, const int* __restrict__ idx, int n, int2* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = src[idx[i]];
+}
+
 // Zero-weight removal (builder.cpp:666-688): keep[i] -> compacted slot offs[i].
 __global__ void k_flag_nonzero(const double* __restrict__ w, const int* __restrict__ d_num, int* __restrict__ keep)
 {
@@ -451,7 +464,7 @@ static void require_ee_bits(const ipcg_mesh* m)
 
 // CollisionMesh::init_adjacencies (collision_mesh.cpp:247-291) on the host,
 // uploaded as CSR lists; built the first time a build needs them.
-static void ensure_adjacency(ipcg_mesh* m)
+void ensure_adjacency(ipcg_mesh* m)
 {
     if (m->adj_ready) return;
     const int64_t nV = m->nV, nE = m->nE, nF = m->nF;
@@ -482,10 +495,20 @@ static void ensure_adjacency(ipcg_mesh* m)
     }
     for (int64_t f = 0; f < nF; ++f)
         for (int j = 0; j < 3; ++j) ev.emplace_back(m->h_F2E[3 * f + j], F[3 * f + (j + 2) % 3]);
-    std::vector<int32_t> vv_off, vv_adj, ve_off, ve_adj, ev_off, ev_adj;
+    std::vector<std::pair<int32_t, int32_t>> vf, ef;
+    vf.reserve(3 * nF);
+    ef.reserve(3 * nF);
+    for (int64_t f = 0; f < nF; ++f)
+        for (int j = 0; j < 3; ++j) {
+            vf.emplace_back(F[3 * f + j], (int32_t)f);
+            ef.emplace_back(m->h_F2E[3 * f + j], (int32_t)f);
+        }
+    std::vector<int32_t> vv_off, vv_adj, ve_off, ve_adj, ev_off, ev_adj, vf_off, vf_adj, ef_off, ef_adj;
     csr(vv, nV, vv_off, vv_adj);
     csr(ve, nV, ve_off, ve_adj);
     csr(ev, nE, ev_off, ev_adj);
+    csr(vf, nV, vf_off, vf_adj);
+    csr(ef, nE, ef_off, ef_adj);
     std::vector<uint8_t> boundary(nV, 1);
     for (int64_t e = 0; e < nE; ++e)
         if (ev_off[e + 1] - ev_off[e] >= 2) boundary[E[2 * e]] = boundary[E[2 * e + 1]] = 0;
@@ -502,6 +525,10 @@ static void ensure_adjacency(ipcg_mesh* m)
     up(m->ve_adj, ve_adj);
     up(m->ev_off, ev_off);
     up(m->ev_adj, ev_adj);
+    up(m->vf_off, vf_off);
+    up(m->vf_adj, vf_adj);
+    up(m->ef_off, ef_off);
+    up(m->ef_adj, ef_adj);
     up(m->boundary, boundary);
     m->max_vertex_edges = maxdeg;
     m->adj_ready = true;
@@ -604,6 +631,14 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
         m->rec_ee_w.reserve(cap);
         o.ee_w = m->rec_ee_w.p;
     }
+    o.vv_src = o.ev_src = nullptr;
+    o.src = make_int2(-1, -1);
+    c->built_with_area = area ? 1 : 0;
+    if (area && c->enable_shape_derivatives && !improved) {
+        m->rec_src.reserve(2 * cap);
+        o.vv_src = m->rec_src.p;
+        o.ev_src = m->rec_src.p + cap;
+    }
     m->counters.reserve(32);
     m->h_counters.reserve(32);
     o.count = m->counters.p + 4;
@@ -651,6 +686,9 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     } else {
         m->wkeys.reserve(2 * cap);
         m->widx.reserve(3 * cap);
+        const int2* src_raw = nullptr;
+        DBuf<int2>* src_out = nullptr;
+        DBuf<int>* src_off = nullptr;
         auto merge = [&](unsigned long long* raw, const double* w, int n, unsigned long long* sorted, int* cnt,
                          int* num, int2* ids, double* wout) {
             if (n == 0) {
@@ -663,15 +701,35 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
             sort_pairs_u64(m, m->stream, wk, wk2, i0, i1, n, 64);
             IPCG_LAUNCH("k_gather_keys", s, k_gather_keys<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(raw, i1, n, wk));
             sort_pairs_u64(m, m->stream, wk, sorted, i1, i2, n, idbits);
-            IPCG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * n, s));
+            IPCG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(int) * (n + 1), s));
             rle_u64(m, m->stream, sorted, raw, cnt, num, n);
-            exclusive_sum_i32(m, m->stream, cnt, i0, n);
+            // n + 1 offsets: past the last run they all equal n
+            exclusive_sum_i32(m, m->stream, cnt, i0, n + 1);
             IPCG_LAUNCH("k_sum_runs", s, k_sum_runs<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(raw, cnt, i0, num, i2, w,
                 ids, wout));
+            if (src_raw) {
+                // keep each merged record's weight sources (in merge order)
+                src_out->reserve(n + 1);
+                src_off->reserve(n + 2);
+                IPCG_LAUNCH("k_gather_src", s, k_gather_src<<<grid_for(n, BLOCK), BLOCK, 0, s>>>(src_raw, i2, n,
+                    src_out->p));
+                IPCG_CUDA(cudaMemcpyAsync(src_off->p, i0, sizeof(int) * (n + 1), cudaMemcpyDeviceToDevice, s));
+            }
         };
         if (!improved) {
+            if (o.vv_src) {
+                src_raw = o.vv_src;
+                src_out = &c->vv_src;
+                src_off = &c->vv_src_off;
+            }
             merge(o.vv, o.vv_w, rvv, ks, counts, d_num + 0, c->vv.p, c->vv_w.p);
+            if (o.ev_src) {
+                src_raw = o.ev_src;
+                src_out = &c->ev_src;
+                src_off = &c->ev_src_off;
+            }
             merge(o.ev, o.ev_w, rev, ks + cap, counts + cap, d_num + 1, c->ev.p, c->ev_w.p);
+            src_raw = nullptr;
         } else {
             // sums that cancel to zero are dropped (builder.cpp:666-688)
             m->imp_ids.reserve(cap);

@@ -178,6 +178,7 @@ struct ipcg_mesh {
     ipcg::DBuf<int> E, F, F2E;
     std::vector<int32_t> h_F2E;
     ipcg::DBuf<double> rec_w;        // area weighting: VV / EV record weights
+    ipcg::DBuf<int2> rec_src;        // area-weighted shape derivatives: VV / EV record sources
     ipcg::DBuf<unsigned long long> wkeys; // weighted merge scratch
     ipcg::DBuf<int> widx;
     // adjacencies of CollisionMesh::init_adjacencies (built on first use):
@@ -185,6 +186,7 @@ struct ipcg_mesh {
     bool adj_ready = false;
     int max_vertex_edges = 0;
     ipcg::DBuf<int> vv_off, vv_adj, ve_off, ve_adj, ev_off, ev_adj;
+    ipcg::DBuf<int> vf_off, vf_adj, ef_off, ef_adj; // vertex -> faces, edge -> faces
     ipcg::DBuf<uint8_t> boundary;
     // improved-max-approximation scratch
     ipcg::DBuf<unsigned long long> imp_keys;
@@ -226,6 +228,12 @@ struct ipcg_collisions {
     int set_type = 0;                // CollisionSetType: 0 IPC, 1 IMPROVED_MAX_APPROX
     int enable_shape_derivatives = 0; // NormalCollisions::enable_shape_derivatives()
     int built_with_shape = 0;        // the flag as it was at the last build
+    int built_with_area = 0;         // area weighting at the last build
+    // area-weighted shape derivatives: the weight sources of each merged VV /
+    // EV record ((v, -1) for a face-vertex candidate's vertex, (ea, eb) for an
+    // edge-edge candidate's edges), with per-record offsets
+    ipcg::DBuf<int> vv_src_off, ev_src_off;
+    ipcg::DBuf<int2> vv_src, ev_src;
     ipcg::DBuf<int2> vv, ev, ee, fv;
     ipcg::DBuf<double> vv_w, ev_w, ee_w, fv_w, ee_eps;
     ipcg::DBuf<int8_t> ee_dtype;
@@ -282,6 +290,8 @@ void detect_candidates(ipcg_mesh* m, const double* V0, const double* V1, const d
 // (collision_mesh.cpp:309-374), summed in face order on the host.
 void mesh_areas_host(const double* rest, int64_t nV, const int32_t* E, int64_t nE, const int32_t* F, int64_t nF,
     const int32_t* F2E, double* vertex_area, double* edge_area);
+// collisions.cu: the mesh adjacencies (built once, on first use)
+void ensure_adjacency(ipcg_mesh* m);
 // collisions.cu: per-scene dhat / dmin (host arrays of n_scenes)
 void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, const double* dhat, const double* dmin);
 
@@ -361,6 +371,10 @@ void sort_pairs_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_i
 void rle_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_in, unsigned long long* uniq, int* counts, int* d_num, int n);
 void unique_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_in, unsigned long long* uniq, int* d_num, int n);
 void exclusive_sum_i32(ipcg_mesh* m, cudaStream_t st, const int* in, int* out, int n);
+void exclusive_sum_i64(ipcg_mesh* m, cudaStream_t st, const int64_t* in, int64_t* out, int n);
+// barrier.cu: NormalPotential::shape_derivative of an area-weighted set
+void shape_derivative_area(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
+    ipcg_csr* out);
 
 inline int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
 inline int bits_for(int64_t n)

@@ -73,6 +73,14 @@ void unique_u64(ipcg_mesh* m, cudaStream_t st, const unsigned long long* k_in, u
     });
 }
 
+void exclusive_sum_i64(ipcg_mesh* m, cudaStream_t st, const int64_t* in, int64_t* out, int n)
+{
+    if (n <= 0) return;
+    with_temp(m, st, "cub_exclusive_sum", [&](void* t, size_t& b) {
+        return cub::DeviceScan::ExclusiveSum(t, b, in, out, n, st);
+    });
+}
+
 void exclusive_sum_i32(ipcg_mesh* m, cudaStream_t st, const int* in, int* out, int n)
 {
     if (n <= 0) return;

@@ -37,6 +37,7 @@
 #include <functional>
 #include <limits>
 #include <mutex>
+#include <map>
 #include <numeric>
 #include <thread>
 #include <unordered_map>
@@ -613,11 +614,17 @@ struct Collisions {
     std::vector<double> fv_w;
     std::vector<int32_t> cand; // last candidate set: ee pairs then fv pairs
     int64_t n_cand_ee = 0, n_cand_fv = 0;
+    // weight sources of each merged VV / EV record (area weighting): a face-
+    // vertex candidate's vertex (v, -1) or an edge-edge candidate's edges
+    // (ea, eb), in the record's merge order; offsets per record
+    std::vector<int64_t> vv_src_off, ev_src_off;
+    std::vector<int32_t> vv_src, ev_src;
 };
 
 struct Raw {
     std::vector<uint64_t> vv, ev;
     std::vector<double> vv_w, ev_w;
+    std::vector<int32_t> vv_src, ev_src; // pairs: the weight source of each record
     std::vector<int32_t> ee;
     std::vector<double> ee_eps, ee_w;
     std::vector<int8_t> ee_dt;
@@ -662,15 +669,21 @@ static void mesh_areas(const double* R, int64_t nV, const int32_t* E, int64_t nE
 
 static inline uint64_t key2(uint32_t a, uint32_t b) { return ((uint64_t)a << 32) | b; }
 
+// the weight source of the records being added (set by the candidate's adder)
+static thread_local int32_t g_src[2] = { -1, -1 };
 static void add_vv(Raw& r, int a, int b, double w)
 {
     r.vv.push_back(key2(std::min(a, b), std::max(a, b)));
     r.vv_w.push_back(w);
+    r.vv_src.push_back(g_src[0]);
+    r.vv_src.push_back(g_src[1]);
 }
 static void add_ev(Raw& r, int e, int v, double w)
 {
     r.ev.push_back(key2(e, v));
     r.ev_w.push_back(w);
+    r.ev_src.push_back(g_src[0]);
+    r.ev_src.push_back(g_src[1]);
 }
 
 // builder.cpp:239-336
@@ -681,6 +694,8 @@ static void add_face_vertex(Raw& r, const double* V, const int32_t* F, const int
     double offset_sqr, const double* va)
 {
     const double w = va ? 0.25 * va[vi] : 1.0;
+    g_src[0] = vi;
+    g_src[1] = -1;
     const int f0 = F[3 * fi], f1 = F[3 * fi + 1], f2 = F[3 * fi + 2];
     const V3 p = row(V, vi), t0 = row(V, f0), t1 = row(V, f1), t2 = row(V, f2);
     const int dtype = point_triangle_distance_type(p, t0, t1, t2);
@@ -705,6 +720,8 @@ static void add_edge_edge(Raw& r, const double* V, const double* Vrest, const in
     double offset_sqr, const double* earea)
 {
     const double w = earea ? 0.25 * (earea[ea] + earea[eb]) : 1.0;
+    g_src[0] = ea;
+    g_src[1] = eb;
     const int a0 = E[2 * ea], a1 = E[2 * ea + 1], b0 = E[2 * eb], b1 = E[2 * eb + 1];
     const V3 xa0 = row(V, a0), xa1 = row(V, a1), xb0 = row(V, b0), xb1 = row(V, b1);
     const int actual = edge_edge_distance_type(xa0, xa1, xb0, xb1);
@@ -787,6 +804,7 @@ static void improved_max_approx(Raw& r, const double* V, const double* Vrest, co
     const int32_t* F2E, const std::vector<int32_t>& cee, const std::vector<int32_t>& cfv, double offset_sqr,
     const double* va, const double* ea, const Adjacency& A)
 {
+    g_src[0] = g_src[1] = -2; // improved terms: no area-weighted shape derivative
     auto active = [&](double d2) { return d2 < offset_sqr; };
     auto pe_dist = [&](int v, int e) {
         const V3 p = row(V, v), e0 = row(V, E[2 * e]), e1 = row(V, E[2 * e + 1]);
@@ -880,8 +898,11 @@ static void finalize(Raw& all, Collisions& C)
     // Lists are sorted by key and each key's weights are summed in ascending
     // order (without area weighting they are all 1, so the sum is a count);
     // the reference's order is thread-dependent, this one is not.
-    auto merge = [](const std::vector<uint64_t>& keys, const std::vector<double>& win, std::vector<int32_t>& ids,
-                     std::vector<double>& w) {
+    auto merge = [](const std::vector<uint64_t>& keys, const std::vector<double>& win, const std::vector<int32_t>& src,
+                     std::vector<int32_t>& ids, std::vector<double>& w, std::vector<int64_t>& soff,
+                     std::vector<int32_t>& sout) {
+        soff.assign(1, 0);
+        sout.clear();
         std::vector<size_t> perm(keys.size());
         std::iota(perm.begin(), perm.end(), 0);
         std::sort(perm.begin(), perm.end(), [&](size_t a, size_t b) {
@@ -898,12 +919,19 @@ static void finalize(Raw& all, Collisions& C)
                 ids.push_back((int32_t)(keys[perm[i]] >> 32));
                 ids.push_back((int32_t)(keys[perm[i]] & 0xffffffffu));
                 w.push_back(sum);
+                if (!src.empty()) {
+                    for (size_t q = i; q < j; ++q) {
+                        sout.push_back(src[2 * perm[q]]);
+                        sout.push_back(src[2 * perm[q] + 1]);
+                    }
+                    soff.push_back((int64_t)sout.size() / 2);
+                }
             }
             i = j;
         }
     };
-    merge(all.vv, all.vv_w, C.vv, C.vv_w);
-    merge(all.ev, all.ev_w, C.ev, C.ev_w);
+    merge(all.vv, all.vv_w, all.vv_src, C.vv, C.vv_w, C.vv_src_off, C.vv_src);
+    merge(all.ev, all.ev_w, all.ev_src, C.ev, C.ev_w, C.ev_src_off, C.ev_src);
     // EE: records are equal when their edges match as an unordered pair and
     // their distance types match (normal/edge_edge.cpp:123-142); equal
     // records sum their weights (ascending order) and zero sums are dropped.
@@ -2211,6 +2239,8 @@ void* orc_collisions_build(const double* V, const double* Vrest, int64_t nV, con
     for (auto& r : raw) {
         all.vv.insert(all.vv.end(), r.vv.begin(), r.vv.end());
         all.vv_w.insert(all.vv_w.end(), r.vv_w.begin(), r.vv_w.end());
+        all.vv_src.insert(all.vv_src.end(), r.vv_src.begin(), r.vv_src.end());
+        all.ev_src.insert(all.ev_src.end(), r.ev_src.begin(), r.ev_src.end());
         all.ev.insert(all.ev.end(), r.ev.begin(), r.ev.end());
         all.ev_w.insert(all.ev_w.end(), r.ev_w.begin(), r.ev_w.end());
         all.ee_w.insert(all.ee_w.end(), r.ee_w.begin(), r.ee_w.end());
@@ -3017,23 +3047,132 @@ static void shape_local_ee(const BarrierParams& P, const Contact& c, const V3* x
         }
 }
 
-void* orc_barrier_shape_derivative(void* h, const double* V, const double* Vrest, int64_t nV, const int32_t* E,
-    const int32_t* F, double dhat, double kappa, double dmin, int physical, int nthreads)
+// Area Jacobians of the rest mesh (collision_mesh.cpp:376-432): per vertex
+// the sum of its faces' area gradients / 3 (else half its edges' length
+// gradients), per edge its faces' area gradients / 3 (else its length
+// gradient); sparse over the 3 nV dofs.
+typedef std::map<int64_t, double> SpVec;
+static void add_to(SpVec& v, const int32_t* ids, int n, const double* g, double s)
 {
+    for (int a = 0; a < n; ++a)
+        for (int d = 0; d < 3; ++d) v[3 * (int64_t)ids[a] + d] += s * g[3 * a + d];
+}
+static void area_jacobians(const double* R, int64_t nV, const int32_t* E, int64_t nE, const int32_t* F, int64_t nF,
+    const int32_t* F2E, std::vector<SpVec>& vj, std::vector<SpVec>& ej)
+{
+    vj.assign(nV, {});
+    ej.assign(nE, {});
+    std::vector<char> vis_v(nV, 0), vis_e(nE, 0);
+    for (int64_t f = 0; f < nF; ++f) {
+        const V3 t0 = row(R, F[3 * f]), t1 = row(R, F[3 * f + 1]), t2 = row(R, F[3 * f + 2]);
+        const V3 n = normalized(cross(sub(t1, t0), sub(t2, t0)));
+        // d|A|/dt_i = n x (t_{i+2} - t_{i+1}) / 2
+        const V3 g0 = scale(cross(n, sub(t2, t1)), 0.5), g1 = scale(cross(n, sub(t0, t2)), 0.5),
+                 g2 = scale(cross(n, sub(t1, t0)), 0.5);
+        const double g[9] = { g0.x, g0.y, g0.z, g1.x, g1.y, g1.z, g2.x, g2.y, g2.z };
+        for (int j = 0; j < 3; ++j) {
+            vis_v[F[3 * f + j]] = 1;
+            add_to(vj[F[3 * f + j]], F + 3 * f, 3, g, 1.0 / 3.0);
+            vis_e[F2E[3 * f + j]] = 1;
+            add_to(ej[F2E[3 * f + j]], F + 3 * f, 3, g, 1.0 / 3.0);
+        }
+    }
+    for (int64_t e = 0; e < nE; ++e) {
+        const int32_t a = E[2 * e];
+        if (vis_v[a] && vis_e[e]) continue;
+        const V3 d = sub(row(R, E[2 * e]), row(R, E[2 * e + 1]));
+        const double l = std::sqrt(sqnorm(d));
+        const double g[6] = { d.x / l, d.y / l, d.z / l, -d.x / l, -d.y / l, -d.z / l };
+        if (!vis_v[a])
+            for (int j = 0; j < 2; ++j) add_to(vj[E[2 * e + j]], E + 2 * e, 2, g, 0.5);
+        if (!vis_e[e]) add_to(ej[e], E + 2 * e, 2, g, 1.0);
+    }
+}
+
+// General triplets -> CSR with duplicates summed.
+static CSR* csr_from_triplets(int64_t ndof, std::vector<std::pair<int64_t, double>>& t)
+{
+    std::stable_sort(t.begin(), t.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    CSR* M = new CSR();
+    M->n = ndof;
+    M->rowptr.assign(ndof + 1, 0);
+    for (size_t i = 0; i < t.size();) {
+        size_t j = i;
+        double sum = 0;
+        while (j < t.size() && t[j].first == t[i].first) sum += t[j++].second;
+        M->col.push_back((int32_t)(t[i].first % ndof));
+        M->val.push_back(sum);
+        M->rowptr[t[i].first / ndof + 1]++;
+        i = j;
+    }
+    for (int64_t r = 0; r < ndof; ++r) M->rowptr[r + 1] += M->rowptr[r];
+    return M;
+}
+
+void* orc_barrier_shape_derivative(void* h, const double* V, const double* Vrest, int64_t nV, const int32_t* E,
+    int64_t nE, const int32_t* F, int64_t nF, const int32_t* F2E, double dhat, double kappa, double dmin, int physical,
+    int area_weighting, int nthreads)
+{
+    (void)nthreads;
     const Collisions& C = *(const Collisions*)h;
     const BarrierParams P { dhat, kappa, dmin, physical };
-    const int64_t n = C.vv_w.size() + C.ev_w.size() + C.ee_w.size() + C.fv_w.size();
-    return assemble_csr(n, nV, nthreads, [&](int64_t i, int& nv, int* vid, double* Hl) {
+    const int64_t nvv = C.vv_w.size(), nev = C.ev_w.size(), nee = C.ee_w.size();
+    const int64_t n = nvv + nev + nee + C.fv_w.size();
+    const int64_t ndof = 3 * nV;
+    std::vector<SpVec> vj, ej;
+    if (area_weighting) area_jacobians(Vrest, nV, E, nE, F, nF, F2E, vj, ej);
+    std::vector<std::pair<int64_t, double>> trip;
+    for (int64_t i = 0; i < n; ++i) {
         Contact c;
         contact_stencil(C, E, F, i, c);
         V3 x[4], xr[4];
         gather(V, c, x);
         gather(Vrest, c, xr);
+        // second term: w times the unprojected local Hessian (mollified form for EE)
+        double Hl[144];
         if (c.type == CT_EE) shape_local_ee(P, c, x, xr, Hl);
         else contact_hessian(P, c, x, 0, Hl);
-        nv = c.n;
-        for (int k = 0; k < c.n; ++k) vid[k] = c.vid[k];
-    });
+        const int N = 3 * c.n;
+        for (int a = 0; a < c.n; ++a)
+            for (int b = 0; b < c.n; ++b)
+                for (int k = 0; k < 3; ++k)
+                    for (int l = 0; l < 3; ++l) {
+                        const double val = Hl[(3 * a + k) * N + 3 * b + l];
+                        if (val != 0)
+                            trip.push_back({ (3 * (int64_t)c.vid[a] + k) * ndof + 3 * (int64_t)c.vid[b] + l, val });
+                    }
+        if (!area_weighting) continue;
+        // first term: (grad_u f / w) (grad_x w)^T, grad_x w from the sources'
+        // area Jacobians (normal_potential.cpp:330-355)
+        SpVec wg;
+        auto add_src = [&](int32_t s0, int32_t s1) {
+            if (s1 < 0) {
+                for (const auto& kv : vj[s0]) wg[kv.first] += 0.25 * kv.second;
+            } else {
+                SpVec sum = ej[s0];
+                for (const auto& kv : ej[s1]) sum[kv.first] += kv.second;
+                for (const auto& kv : sum) wg[kv.first] += 0.25 * kv.second;
+            }
+        };
+        if (c.type == CT_VV)
+            for (int64_t q = C.vv_src_off[i]; q < C.vv_src_off[i + 1]; ++q) add_src(C.vv_src[2 * q], C.vv_src[2 * q + 1]);
+        else if (c.type == CT_EV) {
+            const int64_t r = i - nvv;
+            for (int64_t q = C.ev_src_off[r]; q < C.ev_src_off[r + 1]; ++q) add_src(C.ev_src[2 * q], C.ev_src[2 * q + 1]);
+        } else if (c.type == CT_EE) {
+            const int64_t r = i - nvv - nev;
+            add_src(C.ee[2 * r], C.ee[2 * r + 1]);
+        } else {
+            add_src(c.vid[0], -1);
+        }
+        double g[12];
+        contact_gradient(P, c, x, g);
+        for (int r = 0; r < N; ++r) g[r] /= c.w;
+        for (int a = 0; a < c.n; ++a)
+            for (int d = 0; d < 3; ++d)
+                for (const auto& kv : wg) trip.push_back({ (3 * (int64_t)c.vid[a] + d) * ndof + kv.first, g[3 * a + d] * kv.second });
+    }
+    return csr_from_triplets(ndof, trip);
 }
 
 // scalar smooth-friction functions for derivative checks

@@ -93,7 +93,7 @@ def lib():
         L.orc_friction_hessian.restype = vp
         L.orc_friction_hessian.argtypes = [vp, P, i64, P, P, d, i32, i32]
         L.orc_barrier_shape_derivative.restype = vp
-        L.orc_barrier_shape_derivative.argtypes = [vp, P, P, i64, P, P, d, d, d, i32, i32]
+        L.orc_barrier_shape_derivative.argtypes = [vp, P, P, i64, P, i64, P, i64, P, d, d, d, i32, i32, i32]
         L.orc_tangential_set_anisotropy.argtypes = [vp, P, P, P]
         L.orc_tangential_update_lagged_mu.argtypes = [vp, P, P, P, P, P]
         L.orc_tangential_lagged_mu.argtypes = [vp, P, P]
@@ -468,14 +468,18 @@ def friction_mu(which, y, mu_s, mu_k, eps_v):
     return lib().orc_friction_mu(int(which), float(y), float(mu_s), float(mu_k), float(eps_v))
 
 
-def barrier_shape_derivative(col, V, E, F, dhat, kappa, rest=None, dmin=0.0, physical=0, nthreads=None):
-    """(rowptr, col, val) of NormalPotential::shape_derivative for a set built
-    without area weighting (rows: displacement dofs, columns: rest dofs)."""
+def barrier_shape_derivative(col, V, E, F, dhat, kappa, rest=None, dmin=0.0, physical=0, area_weighting=False,
+                             nthreads=None):
+    """(rowptr, col, val) of NormalPotential::shape_derivative (rows:
+    displacement dofs, columns: rest dofs); area_weighting adds the weight
+    gradient term of a set built with area weighting."""
     V, E, F = _f64(V), _i32(E), _i32(F)
     rest = V if rest is None else _f64(rest)
+    F2E = faces_to_edges(F, E)
     L = lib()
-    h = L.orc_barrier_shape_derivative(col.h, _p(V), _p(rest), V.shape[0], _p(E), _p(F), float(dhat), float(kappa),
-                                       float(dmin), int(physical), int(nthreads or os.cpu_count() or 1))
+    h = L.orc_barrier_shape_derivative(col.h, _p(V), _p(rest), V.shape[0], _p(E), E.shape[0], _p(F), F.shape[0],
+                                       _p(F2E), float(dhat), float(kappa), float(dmin), int(physical),
+                                       int(bool(area_weighting)), int(nthreads or os.cpu_count() or 1))
     nnz = L.orc_csr_nnz(h)
     rp = np.zeros(V.size + 1, np.int64)
     ci = np.zeros(nnz, np.int32)

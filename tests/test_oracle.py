@@ -845,3 +845,35 @@ def test_friction_force_is_minus_gradient_at_build_state(oracle_mod):
     # no_mu: the force of unit coefficients
     f1 = oracle_mod.friction_force(t, V, np.zeros_like(V), U, E, F, sc["dhat"], sc["kappa"], ev, no_mu=True)
     assert np.linalg.norm(f1) > np.linalg.norm(f)
+
+
+def test_area_weighted_shape_derivative_weight_term_fd(oracle_mod):
+    """The area-weighted shape derivative's extra term (grad_u f / w)(grad_x w)^T
+    (normal_potential.cpp:330-355) against central differences of the
+    gradient with respect to the rest positions (positions fixed), on a scene
+    with no active mollifier, where that derivative is the whole term."""
+    import scipy.sparse as sps
+    from ipctk_gb300 import scenes
+    sc = scenes.sphere_pack(n_side=2, subdiv=2, seed=3)
+    V, E, F, dh, kp = sc["V"], sc["E"], sc["F"], sc["dhat"], sc["kappa"]
+    col = oracle_mod.build_collisions(V, E, F, dh, area_weighting=True)
+    assert len(col) > 0
+    for (ea, eb), eps in zip(col.ee, col.ee_eps):
+        x = V[[E[ea, 0], E[ea, 1], E[eb, 0], E[eb, 1]]]
+        assert np.sum(np.cross(x[1] - x[0], x[3] - x[2]) ** 2) >= eps
+    n = V.size
+    mat = lambda t: sps.csr_matrix((t[2], t[1], t[0]), shape=(n, n))
+    S = mat(oracle_mod.barrier_shape_derivative(col, V, E, F, dh, kp, area_weighting=True))
+    S2 = mat(oracle_mod.barrier_shape_derivative(col, V, E, F, dh, kp, area_weighting=False))
+    W = (S - S2).tocsc()
+    assert abs(W).max() > 0
+    g = lambda R: oracle_mod.barrier_gradient(oracle_mod.build_collisions(V, E, F, dh, rest=R, area_weighting=True),
+                                              V, E, F, dh, kp)
+    cols = np.unique(W.indices)[:: max(1, len(np.unique(W.indices)) // 8)]
+    h = 1e-7
+    for j in cols:
+        d = np.zeros(n)
+        d[j] = h
+        fd = (g(V + d.reshape(V.shape)) - g(V - d.reshape(V.shape))) / (2 * h)
+        wj = W[:, j].toarray().ravel()
+        assert np.linalg.norm(fd - wj) <= 1e-5 * np.linalg.norm(wj) + 1e-9 * abs(W).max()
