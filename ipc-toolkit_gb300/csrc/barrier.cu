@@ -1243,21 +1243,85 @@ __device__ __forceinline__ int stencil_size(const ContactsView& cv, int64_t i)
 
 // PSD projection (eigen_ext.tpp:64-108) of every local Hessian, in place.
 constexpr int PSD_BLOCK = LH_BLOCK;
+// M = C H C^T read straight from contact i's slab (the element-major layout
+// makes each element a coalesced load across the warp's contacts).
+template <int NS> __device__ void to_contrasts_slab(const Slab& hs, int64_t i, double* M)
+{
+    constexpr int N = 3 * NS;
+#pragma unroll 1
+    for (int r = 0; r < 3 * (NS - 1); ++r) {
+        const int k = r / 3, c = r % 3;
+        double row[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+            double s = 0;
+#pragma unroll
+            for (int a = 0; a < NS; ++a) s += contrast<NS>(k, a) * hs.at(i, (3 * a + c) * N + j);
+            row[j] = s;
+        }
+#pragma unroll
+        for (int l = 0; l < NS - 1; ++l)
+#pragma unroll
+            for (int e = 0; e < 3; ++e) {
+                double s = 0;
+#pragma unroll
+                for (int b = 0; b < NS; ++b) s += contrast<NS>(l, b) * row[3 * b + e];
+                M[r * MAXR + 3 * l + e] = s;
+            }
+    }
+}
+
+// project_psd on contact i's slab in place: M from the slab, the negative
+// eigenvectors kept, then one read-modify-write pass over the slab applying
+// H -= f lam w w^T for each of them in eigenvalue order (the same operations
+// as project_psd on a local copy, without the 144-double local array).
+__device__ bool project_psd_slab(int n, const Slab& hs, int64_t i, int method)
+{
+    const int N = 3 * n, m = 3 * (n - 1);
+    double M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
+    if (n == 4) to_contrasts_slab<4>(hs, i, M);
+    else if (n == 3) to_contrasts_slab<3>(hs, i, M);
+    else to_contrasts_slab<2>(hs, i, M);
+    for (int r = 0; r < m; ++r)
+        for (int s = r + 1; s < m; ++s) {
+            const double avg = 0.5 * (M[r * MAXR + s] + M[s * MAXR + r]);
+            M[r * MAXR + s] = M[s * MAXR + r] = avg;
+        }
+    double rc[MAXROT], rs[MAXROT], hv[MAXR * MAXR], htau[MAXR];
+    int8_t rk[MAXROT];
+    int nrot;
+    if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, hv, htau)) return false;
+    const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
+    double wv[MAXR * 12], sl[MAXR];
+    int nneg = 0;
+    for (int k = 0; k < m; ++k) {
+        if (!(lam[k] < 0)) continue;
+        double q[MAXR];
+        eigvec(m, k, Q, rc, rs, rk, nrot, hv, htau, q);
+        double* w = wv + 12 * nneg;
+        if (n == 4) from_contrasts<4>(q, w);
+        else if (n == 3) from_contrasts<3>(q, w);
+        else from_contrasts<2>(q, w);
+        sl[nneg++] = f * lam[k];
+    }
+    if (nneg == 0) return true; // already PSD: returned as is
+#pragma unroll 1
+    for (int r = 0; r < N; ++r)
+        for (int c = 0; c < N; ++c) {
+            double v = hs.at(i, r * N + c);
+            for (int t = 0; t < nneg; ++t) v -= (sl[t] * wv[12 * t + r]) * wv[12 * t + c];
+            hs.at(i, r * N + c) = v;
+        }
+    return true;
+}
+
 __global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, Slab hs,
     const uint8_t* __restrict__ proj, int method, int* __restrict__ fail)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || !proj[i]) return;
-    const int ns = stencil_size(cv, i);
-    const int N = 3 * ns;
-    double Hl[144];
-    for (int k = 0; k < N * N; ++k) Hl[k] = hs.at(i, k);
-    if (!project_psd(ns, Hl, method)) {
-        atomicOr(fail, 1);
-        return;
-    }
-    for (int k = 0; k < N * N; ++k) hs.at(i, k) = Hl[k];
+    if (!project_psd_slab(stencil_size(cv, i), hs, i, method)) atomicOr(fail, 1);
 }
 
 // Contribution id j (position in the block-key list) -> contact, local
