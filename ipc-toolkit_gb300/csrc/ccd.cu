@@ -47,6 +47,10 @@ constexpr int BLOCK = 128;
 // which starts it again with the then earliest time as its horizon and runs
 // it to completion.
 constexpr long long CCD_PASS1_BUDGET = 512;
+// A first pass with a few boxes settles the many candidates whose first
+// inclusion tests exclude a root, and compacts the rest, so the 512-box pass
+// runs with full warps of candidates that need subdividing.
+constexpr long long CCD_PASS0_BUDGET = 8;
 
 struct Query {
     V3 s[4], e[4];
@@ -640,12 +644,17 @@ void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, in
     const SceneView sv = scene_view(m);
     const int nc = (int)(n_ee + n_fv);
     if (nc == 0) return;
-    m->ivals_a.reserve(nc + 1);
-    int* hard = m->ivals_a.p; // deferred by pass 1
-    int* hard_n = m->counters.p + 3;
-    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
+    m->ivals_a.reserve(2 * (nc + 1));
+    int* open = m->ivals_a.p;           // left by pass 0
+    int* hard = m->ivals_a.p + nc + 1;  // left by pass 1
+    m->counters.reserve(32);
+    int* open_n = m->counters.p + 30;
+    int* hard_n = m->counters.p + 31;
+    IPCG_CUDA(cudaMemsetAsync(open_n, 0, 2 * sizeof(int), s));
+    IPCG_LAUNCH("k_ccd_pass0", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS0_BUDGET, nullptr, nullptr, open, open_n, any_hit));
     IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, nullptr, nullptr, hard, hard_n, any_hit));
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, open, open_n, hard, hard_n, any_hit));
     IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
         m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, any_hit));
 }
