@@ -1301,9 +1301,83 @@ def edges(F):
     return scenes.edges_from_faces(np.asarray(F))
 
 
+# -- the reference's free distance functions (src/ipc/distance/*.hpp), with
+#    the classified (AUTO) type, on the device; arguments may be single points
+#    or stacked (n, 3) arrays, results scalars or (n,) arrays --
+
+def _stencil(kind, pts, _unused=None):
+    X = np.stack([np.asarray(q, np.float64).reshape(-1, 3) for q in pts], axis=1)
+    dt, d = distance_stencils(kind, X)
+    single = all(np.asarray(q).ndim == 1 for q in pts)
+    return (dt[0], d[0]) if single else (dt, d)
+
+
+def _auto_only(dtype):
+    if dtype is not None and int(dtype) != -1:
+        raise ValueError("only the classified (AUTO) distance type is provided by these free functions")
+
+
+def point_point_distance(p0, p1):
+    """point_point.hpp: squared distance (a degenerate edge on the device)."""
+    return _stencil(0, (p0, p1, p1), None)[1]
+
+
+def point_edge_distance(p, e0, e1, dtype=None):
+    """point_edge.hpp: squared distance with the classified type."""
+    _auto_only(dtype)
+    return _stencil(0, (p, e0, e1), None)[1]
+
+
+def point_triangle_distance(p, t0, t1, t2, dtype=None):
+    """point_triangle.hpp: squared distance with the classified type."""
+    _auto_only(dtype)
+    return _stencil(1, (p, t0, t1, t2), None)[1]
+
+
+def edge_edge_distance(ea0, ea1, eb0, eb1, dtype=None):
+    """edge_edge.hpp: squared distance with the classified type."""
+    _auto_only(dtype)
+    return _stencil(2, (ea0, ea1, eb0, eb1), None)[1]
+
+
+def point_edge_distance_type(p, e0, e1):
+    t = _stencil(0, (p, e0, e1), None)[0]
+    return PointEdgeDistanceType(int(t)) if np.ndim(t) == 0 else t
+
+
+def point_triangle_distance_type(p, t0, t1, t2):
+    t = _stencil(1, (p, t0, t1, t2), None)[0]
+    return PointTriangleDistanceType(int(t)) if np.ndim(t) == 0 else t
+
+
+def edge_edge_distance_type(ea0, ea1, eb0, eb1):
+    t = _stencil(2, (ea0, ea1, eb0, eb1), None)[0]
+    return EdgeEdgeDistanceType(int(t)) if np.ndim(t) == 0 else t
+
+
+# -- barrier.hpp's free functions (the clamped log barrier) --
+
+def barrier(d: float, dhat: float) -> float:
+    return ClampedLogBarrier()(d, dhat)
+
+
+def barrier_first_derivative(d: float, dhat: float) -> float:
+    return ClampedLogBarrier().first_derivative(d, dhat)
+
+
+def barrier_second_derivative(d: float, dhat: float) -> float:
+    return ClampedLogBarrier().second_derivative(d, dhat)
+
+
 __all__ = [
-    "CollisionMesh", "NormalCollisions", "BarrierPotential", "PSDProjectionMethod", "TightInclusionCCD",
-    "compute_collision_free_stepsize", "EdgeEdgeDistanceType", "PointTriangleDistanceType",
-    "PointEdgeDistanceType", "distance_stencils", "edges", "lib", "LIB_PATH", "profile_enable",
-    "profile_report", "launch_count", "DeviceCSR",
+    "CollisionMesh", "SceneBatch", "NormalCollisions", "TangentialCollisions", "Candidates", "BarrierPotential",
+    "BatchBarrierPotential", "FrictionPotential", "Barrier", "ClampedLogBarrier", "NormalizedClampedLogBarrier",
+    "ClampedLogSqBarrier", "CubicBarrier", "TwoStageBarrier", "PSDProjectionMethod", "TightInclusionCCD",
+    "DEFAULT_NARROW_PHASE_CCD", "compute_collision_free_stepsize", "compute_collision_free_stepsize_batch",
+    "is_step_collision_free", "has_intersections", "initial_barrier_stiffness", "update_barrier_stiffness",
+    "EdgeEdgeDistanceType", "PointTriangleDistanceType", "PointEdgeDistanceType", "point_point_distance",
+    "point_edge_distance", "point_triangle_distance", "edge_edge_distance", "point_edge_distance_type",
+    "point_triangle_distance_type", "edge_edge_distance_type", "barrier", "barrier_first_derivative",
+    "barrier_second_derivative", "distance_stencils", "edges", "Server", "RequestResult", "DeviceCSR", "lib",
+    "LIB_PATH", "profile_enable", "profile_report", "launch_count", "set_hessian_chunk_contacts",
 ]

@@ -121,3 +121,14 @@ def test_collision_set_type_validation_without_gpu(ipctk):
     assert L.ipcg_collisions_collision_set_type(h, C.byref(t)) == 0 and t.value == 1
     L.ipcg_collisions_destroy.argtypes = [C.c_void_p]
     assert L.ipcg_collisions_destroy(h) == 0
+
+
+def test_public_names(ipctk):
+    """Every name the package exports exists (the reference's ipctk names the
+    path uses: classes, free functions, enums)."""
+    missing = [n for n in ipctk.__all__ if not hasattr(ipctk, n)]
+    assert not missing, missing
+    for n in ("CollisionMesh", "NormalCollisions", "BarrierPotential", "FrictionPotential", "TangentialCollisions",
+              "Candidates", "compute_collision_free_stepsize", "is_step_collision_free", "has_intersections",
+              "point_triangle_distance", "edge_edge_distance", "barrier"):
+        assert n in ipctk.__all__

@@ -84,3 +84,23 @@ def test_has_intersections_sheets(ipctk, oracle_mod):
     # at the end of the step it lies wholly below it
     assert ipctk.has_intersections(mesh, sc["V1"]) == oracle_mod.has_intersections_bruteforce(sc["V1"], sc["E"],
                                                                                              sc["F"])
+
+
+def test_free_distance_functions(ipctk, oracle_mod):
+    """The reference's free distance functions (AUTO type) on the device
+    against the oracle, single and stacked."""
+    rng = np.random.Generator(np.random.PCG64(12))
+    for _ in range(20):
+        x = rng.uniform(-1, 1, (4, 3))
+        assert ipctk.point_triangle_distance(*x) == oracle_mod.point_triangle_distance(*x)
+        assert ipctk.edge_edge_distance(*x) == oracle_mod.edge_edge_distance(*x)
+        assert ipctk.point_edge_distance(*x[:3]) == oracle_mod.point_edge_distance(*x[:3])
+        assert int(ipctk.point_triangle_distance_type(*x)) == oracle_mod.point_triangle_distance_type(*x)
+        assert int(ipctk.edge_edge_distance_type(*x)) == oracle_mod.edge_edge_distance_type(*x)
+        assert ipctk.point_point_distance(x[0], x[1]) == float(np.sum((x[1] - x[0]) ** 2))
+    X = rng.uniform(-1, 1, (50, 4, 3))
+    d = ipctk.point_triangle_distance(X[:, 0], X[:, 1], X[:, 2], X[:, 3])
+    assert d.shape == (50,)
+    assert np.all(d == [oracle_mod.point_triangle_distance(*x) for x in X])
+    with pytest.raises(ValueError):
+        ipctk.point_triangle_distance(*X[0], dtype=ipctk.PointTriangleDistanceType.P_T0)
