@@ -740,35 +740,6 @@ template <int NS> __device__ __forceinline__ constexpr double contrast(int k, in
                   : (a == 0 ? 0.70710678118654752440 : -0.70710678118654752440);
 }
 
-// M = C H C^T (rows of M with stride MAXR), H row-major N x N, one row of
-// M at a time (row 3k+c of C H, then its product with C^T), so no N-wide
-// intermediate matrix is kept.
-template <int NS> __device__ void to_contrasts(const double* H, double* M)
-{
-    constexpr int N = 3 * NS;
-#pragma unroll 1
-    for (int r = 0; r < 3 * (NS - 1); ++r) {
-        const int k = r / 3, c = r % 3;
-        double row[N];
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-            double s = 0;
-#pragma unroll
-            for (int a = 0; a < NS; ++a) s += contrast<NS>(k, a) * H[(3 * a + c) * N + j];
-            row[j] = s;
-        }
-#pragma unroll
-        for (int l = 0; l < NS - 1; ++l)
-#pragma unroll
-            for (int e = 0; e < 3; ++e) {
-                double s = 0;
-#pragma unroll
-                for (int b = 0; b < NS; ++b) s += contrast<NS>(l, b) * row[3 * b + e];
-                M[r * MAXR + 3 * l + e] = s;
-            }
-    }
-}
-
 // w = C^T q (length 3 NS) for a length-3(NS-1) vector q.
 template <int NS> __device__ __forceinline__ void from_contrasts(const double* q, double* w)
 {
@@ -781,43 +752,6 @@ template <int NS> __device__ __forceinline__ void from_contrasts(const double* q
             for (int k = 0; k < NS - 1; ++k) s += contrast<NS>(k, a) * q[3 * k + c];
             w[3 * a + c] = s;
         }
-}
-
-// In-place PSD projection of the 3n×3n local Hessian (row-major, N = 3n).
-// Returns false if the eigensolver did not converge.
-__device__ bool project_psd(int n, double* H, int method)
-{
-    if (method == IPCG_PSD_NONE) return true;
-    const int N = 3 * n, m = 3 * (n - 1);
-    double M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
-    if (n == 4) to_contrasts<4>(H, M);
-    else if (n == 3) to_contrasts<3>(H, M);
-    else to_contrasts<2>(H, M);
-    // symmetrise (rounding)
-    for (int r = 0; r < m; ++r)
-        for (int s = r + 1; s < m; ++s) {
-            const double avg = 0.5 * (M[r * MAXR + s] + M[s * MAXR + r]);
-            M[r * MAXR + s] = M[s * MAXR + r] = avg;
-        }
-    double rc[MAXROT], rs[MAXROT], hv[MAXR * MAXR], htau[MAXR];
-    int8_t rk[MAXROT];
-    int nrot;
-    if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, hv, htau)) return false;
-    const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
-    for (int i = 0; i < m; ++i) {
-        if (!(lam[i] < 0)) continue;
-        double q[MAXR], v[12];
-        eigvec(m, i, Q, rc, rs, rk, nrot, hv, htau, q);
-        if (n == 4) from_contrasts<4>(q, v);
-        else if (n == 3) from_contrasts<3>(q, v);
-        else from_contrasts<2>(q, v);
-        const double sl = f * lam[i];
-        for (int r = 0; r < N; ++r) {
-            const double svr = sl * v[r];
-            for (int s = 0; s < N; ++s) H[r * N + s] -= svr * v[s];
-        }
-    }
-    return true;
 }
 
 __device__ __forceinline__ double fval(const Params& P, double d2)
@@ -1271,10 +1205,10 @@ template <int NS> __device__ void to_contrasts_slab(const Slab& hs, int64_t i, d
     }
 }
 
-// project_psd on contact i's slab in place: M from the slab, the negative
+// PSD projection of contact i's slab in place: M from the slab, the negative
 // eigenvectors kept, then one read-modify-write pass over the slab applying
-// H -= f lam w w^T for each of them in eigenvalue order (the same operations
-// as project_psd on a local copy, without the 144-double local array).
+// H -= f lam w w^T for each of them in eigenvalue order.  Returns false if
+// the eigensolver did not converge.
 __device__ bool project_psd_slab(int n, const Slab& hs, int64_t i, int method)
 {
     const int N = 3 * n, m = 3 * (n - 1);
@@ -1315,12 +1249,15 @@ __device__ bool project_psd_slab(int n, const Slab& hs, int64_t i, int method)
     return true;
 }
 
+// Contacts [first, first + count) of the chunk; the launches over the VV+EV
+// and the EE+FV ranges run on different streams.
 __global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, Slab hs,
-    const uint8_t* __restrict__ proj, int method, int* __restrict__ fail)
+    const uint8_t* __restrict__ proj, int method, int* __restrict__ fail, int64_t first, int64_t count)
 {
-    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || !proj[i]) return;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t i = first + t;
+    if (!proj[i]) return;
     if (!project_psd_slab(stencil_size(cv, i), hs, i, method)) atomicOr(fail, 1);
 }
 
@@ -2363,6 +2300,21 @@ static const Params* upload_params(const ipcg_collisions* cs, ipcg_mesh* m, cons
 
 // With fr set, the same pipeline evaluates the friction potential of the
 // tangential set whose stencils are cs at velocities V (single scene).
+// Contacts k_psd keeps resident on the current device at once (its blocks
+// per SM at full occupancy x SMs x block size), measured once per process
+// (a function-local static, so concurrent first calls are safe).
+static int64_t psd_resident_contacts()
+{
+    static const int64_t cached = [] {
+        int dev = 0, sms = 0, per_sm = 0;
+        IPCG_CUDA(cudaGetDevice(&dev));
+        IPCG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        IPCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_psd, PSD_BLOCK, 0));
+        return (int64_t)std::max(per_sm, 1) * std::max(sms, 1) * PSD_BLOCK;
+    }();
+    return cached;
+}
+
 void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev, ipcg_csr* hess, const FrictionView* fr)
 {
@@ -2455,15 +2407,19 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
             int* bptr = m->ivals_a.p;                    // block row pointers of this chunk's rows
             int* run_start = m->ivals_a.p + (nr + 2);    // first contribution of each block
             int nb = 0;
-            // The sparsity pattern (block keys, sort, run-length encoding,
-            // row and column arrays) does not depend on the values, so it is
-            // built on the side stream while the main stream computes and
-            // projects the local Hessians; the small VV and EV local Hessian
-            // launches also run there, beside EE and FV.  The side stream
-            // starts after everything queued so far on the main one.
-            cudaStream_t t = m->side;
+            // Three streams, forked after everything queued so far on the main
+            // one.  The side stream computes the VV, EV and FV local Hessians
+            // and projects VV and EV; the main stream computes the EE local
+            // Hessians and, once FV's are in, projects the contiguous EE+FV
+            // range (all 12 x 12).  The pattern stream builds the sparsity
+            // pattern (block keys, sort, run-length encoding, row and column
+            // arrays), which does not depend on the values.  Each of these
+            // launches fills only a few warps per SM, so running them side by
+            // side keeps the FP64 pipes busier than running them in turn.
+            cudaStream_t t = m->side, u = m->side2;
             IPCG_CUDA(cudaEventRecord(m->ev_fork, s));
             IPCG_CUDA(cudaStreamWaitEvent(t, m->ev_fork, 0));
+            IPCG_CUDA(cudaStreamWaitEvent(u, m->ev_fork, 0));
             if (nc > 0) {
                 const int64_t first[4] = { 0, cc.nvv, cc.nvv + cc.nev, cc.nvv + cc.nev + cc.nee };
                 const int64_t count[4] = { cc.nvv, cc.nev, cc.nee, cc.nfv };
@@ -2476,64 +2432,75 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
                     if (count[1])
                         IPCG_LAUNCH("k_friction_local_hessian_ev", t, k_friction_local_hessian<CT_EV><<<grid_for(count[1],
                             LH_BLOCK), LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, f, slab, first[1], count[1], a.psd));
+                    if (count[3])
+                        IPCG_LAUNCH("k_friction_local_hessian_fv", t, k_friction_local_hessian<CT_FV><<<grid_for(count[3],
+                            LH_BLOCK), LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, f, slab, first[3], count[3], a.psd));
                     IPCG_CUDA(cudaEventRecord(m->ev_side, t));
                     if (count[2])
                         IPCG_LAUNCH("k_friction_local_hessian_ee", s, k_friction_local_hessian<CT_EE><<<grid_for(count[2],
                             LH_BLOCK), LH_BLOCK, 0, s>>>(cc, m->E.p, m->F.p, V, f, slab, first[2], count[2], a.psd));
-                    if (count[3])
-                        IPCG_LAUNCH("k_friction_local_hessian_fv", s, k_friction_local_hessian<CT_FV><<<grid_for(count[3],
-                            LH_BLOCK), LH_BLOCK, 0, s>>>(cc, m->E.p, m->F.p, V, f, slab, first[3], count[3], a.psd));
-                    IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
                 } else {
-                if (count[0])
-                    IPCG_LAUNCH("k_local_hessian_vv", t, k_local_hessian<CT_VV><<<grid_for(count[0], LH_BLOCK), LH_BLOCK, 0,
-                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[0], count[0]));
-                if (count[1])
-                    IPCG_LAUNCH("k_local_hessian_ev", t, k_local_hessian<CT_EV><<<grid_for(count[1], LH_BLOCK), LH_BLOCK, 0,
-                        t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[1], count[1]));
-                IPCG_CUDA(cudaEventRecord(m->ev_side, t));
-                if (count[2] && a.shape)
-                    IPCG_LAUNCH("k_shape_local_ee", s, k_shape_local_ee<<<grid_for(count[2], LH_BLOCK), LH_BLOCK, 0,
-                        s>>>(cc, m->E.p, m->F.p, V, m->rest.p, sp, sv, slab, first[2], count[2]));
-                else if (count[2])
-                    IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], LH_BLOCK), LH_BLOCK, 0,
-                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[2], count[2]));
-                if (count[3])
-                    IPCG_LAUNCH("k_local_hessian_fv", s, k_local_hessian<CT_FV><<<grid_for(count[3], LH_BLOCK), LH_BLOCK, 0,
-                        s>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[3], count[3]));
-                IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
-                if (a.psd != IPCG_PSD_NONE)
-                    IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(nc, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, slab,
-                        m->proj.p, a.psd, d_fail));
+                    if (count[0])
+                        IPCG_LAUNCH("k_local_hessian_vv", t, k_local_hessian<CT_VV><<<grid_for(count[0], LH_BLOCK),
+                            LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[0], count[0]));
+                    if (count[1])
+                        IPCG_LAUNCH("k_local_hessian_ev", t, k_local_hessian<CT_EV><<<grid_for(count[1], LH_BLOCK),
+                            LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[1], count[1]));
+                    if (count[3])
+                        IPCG_LAUNCH("k_local_hessian_fv", t, k_local_hessian<CT_FV><<<grid_for(count[3], LH_BLOCK),
+                            LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[3], count[3]));
+                    IPCG_CUDA(cudaEventRecord(m->ev_lh, t));
+                    // The VV+EV projection runs beside the EE+FV one only while
+                    // the chunk fills less than half of the contacts k_psd keeps
+                    // resident; past that, concurrent launches only contend for
+                    // the same L1 and one launch over the chunk does better.
+                    const bool split = 2 * nc < psd_resident_contacts();
+                    const int64_t n_small = split ? count[0] + count[1] : 0;
+                    if (a.psd != IPCG_PSD_NONE && n_small)
+                        IPCG_LAUNCH("k_psd_vv_ev", t, k_psd<<<grid_for(n_small, PSD_BLOCK), PSD_BLOCK, 0, t>>>(cc,
+                            slab, m->proj.p, a.psd, d_fail, first[0], n_small));
+                    IPCG_CUDA(cudaEventRecord(m->ev_side, t));
+                    if (count[2] && a.shape)
+                        IPCG_LAUNCH("k_shape_local_ee", s, k_shape_local_ee<<<grid_for(count[2], LH_BLOCK), LH_BLOCK,
+                            0, s>>>(cc, m->E.p, m->F.p, V, m->rest.p, sp, sv, slab, first[2], count[2]));
+                    else if (count[2])
+                        IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], LH_BLOCK),
+                            LH_BLOCK, 0, s>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[2], count[2]));
+                    IPCG_CUDA(cudaStreamWaitEvent(s, split ? m->ev_lh : m->ev_side, 0));
+                    const int64_t p0 = split ? first[2] : 0, n_big = split ? count[2] + count[3] : nc;
+                    if (a.psd != IPCG_PSD_NONE && n_big)
+                        IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(n_big, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, slab,
+                            m->proj.p, a.psd, d_fail, p0, n_big));
                 }
+                IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
                 // sparsity pattern: sort (block key, contribution) and run-length encode
-                IPCG_LAUNCH("k_block_keys", t, k_block_keys<<<nblk_c, BLOCK, 0, t>>>(cc, m->E.p, m->F.p,
+                IPCG_LAUNCH("k_block_keys", u, k_block_keys<<<nblk_c, BLOCK, 0, u>>>(cc, m->E.p, m->F.p,
                     m->keys_a.p, ids_in, nk, gd));
-                sort_pairs_u64(m, t, m->keys_a.p, m->keys_b.p, ids_in, contrib, (int)nk, 32 + bits_for(nV + 1));
-                rle_u64(m, t, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
-                IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, t));
-                IPCG_CUDA(cudaStreamSynchronize(t)); // the main stream keeps running
+                sort_pairs_u64(m, u, m->keys_a.p, m->keys_b.p, ids_in, contrib, (int)nk, 32 + bits_for(nV + 1));
+                rle_u64(m, u, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
+                IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, u));
+                IPCG_CUDA(cudaStreamSynchronize(u)); // the other streams keep running
                 nb = m->h_counters.p[0];
-                exclusive_sum_i32(m, t, run_len, run_start, nb);
+                exclusive_sum_i32(m, u, run_len, run_start, nb);
             } else {
-                IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), t));
+                IPCG_CUDA(cudaMemsetAsync(d_nb, 0, sizeof(int), u));
             }
             // output arrays grow as chunks finish (the last chunk's estimate is exact)
             done += nc;
             const int64_t need = 9 * (B0 + nb);
             const int64_t guess = done < n ? (int64_t)((double)need * (double)n / (double)std::max<int64_t>(done, 1))
                                            : need;
-            hess->col.grow_keep(std::max(need, guess) + 1, 9 * B0, t);
-            hess->val.grow_keep(std::max(need, guess) + 1, 9 * B0, t);
-            IPCG_LAUNCH("k_block_rowptr", t, k_block_rowptr<<<grid_for(nr + 1, 256), 256, 0, t>>>(m->keys_a.p, d_nb,
+            hess->col.grow_keep(std::max(need, guess) + 1, 9 * B0, u);
+            hess->val.grow_keep(std::max(need, guess) + 1, 9 * B0, u);
+            IPCG_LAUNCH("k_block_rowptr", u, k_block_rowptr<<<grid_for(nr + 1, 256), 256, 0, u>>>(m->keys_a.p, d_nb,
                 r0, nr, bptr, nk, gd));
-            IPCG_LAUNCH("k_csr_rows", t, k_csr_rows<<<grid_for(nr + 1, 256), 256, 0, t>>>(bptr, r0, nr, B0,
+            IPCG_LAUNCH("k_csr_rows", u, k_csr_rows<<<grid_for(nr + 1, 256), 256, 0, u>>>(bptr, r0, nr, B0,
                 hess->row_ptr.p));
             if (nb > 0)
-                IPCG_LAUNCH("k_csr_cols", t, k_csr_cols<<<grid_for(nb, 256), 256, 0, t>>>(m->keys_a.p, nb, bptr, r0,
+                IPCG_LAUNCH("k_csr_cols", u, k_csr_cols<<<grid_for(nb, 256), 256, 0, u>>>(m->keys_a.p, nb, bptr, r0,
                     nr, B0, hess->col.p, gd));
             // join: values need the projected local Hessians and the pattern
-            IPCG_CUDA(cudaEventRecord(m->ev_pattern, t));
+            IPCG_CUDA(cudaEventRecord(m->ev_pattern, u));
             IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_pattern, 0));
             if (nb > 0)
                 IPCG_LAUNCH("k_assemble", s, k_assemble<<<grid_for(9 * (int64_t)nb, 256), 256, 0, s>>>(cc,
