@@ -72,14 +72,9 @@ BYTES_PER_CONTACT = {2: 504, 3: 1104, 4: 1944}
 PSD_BYTES = {2: 2 * 8 * 36, 3: 2 * 8 * 81, 4: 2 * 8 * 144}
 
 
-def psd_bytes(counts, split):
-    """Slab bytes of one k_psd launch.  With `split` (the library ran
-    k_psd_vv_ev beside it, which it does while the contacts fill less than
-    half of the GPU's resident k_psd threads) k_psd covers the edge-edge and
-    face-vertex range (12 x 12 local Hessians), otherwise every contact."""
+def psd_bytes(counts):
     nvv, nev, nee, nfv = (int(x) for x in counts[:4])
-    small = 0 if split else nvv * PSD_BYTES[2] + nev * PSD_BYTES[3]
-    return small + (nee + nfv) * PSD_BYTES[4]
+    return nvv * PSD_BYTES[2] + nev * PSD_BYTES[3] + (nee + nfv) * PSD_BYTES[4]
 
 
 def fp64_peak_tflops(dev):
@@ -566,7 +561,7 @@ def run_gb300(args, rank, world):
     top_ms = own[top]["ms"] / max(1, own[top]["launches"])
     peak, peak_kind = measured_peaks()
     if top == "k_psd":
-        abytes = psd_bytes(counts, "k_psd_vv_ev" in own)
+        abytes = psd_bytes(counts)
     else:
         abytes = algorithmic_bytes(counts, ndof)
     achieved = abytes / (top_ms / 1000.0) / 1e9

@@ -145,7 +145,6 @@ ipcg_mesh::~ipcg_mesh()
 {
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_side) cudaEventDestroy(ev_side);
-    if (ev_lh) cudaEventDestroy(ev_lh);
     if (ev_pattern) cudaEventDestroy(ev_pattern);
     if (side) cudaStreamDestroy(side);
     if (side2) cudaStreamDestroy(side2);
@@ -333,7 +332,6 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
             IPCG_CUDA(cudaStreamCreateWithFlags(&m->side2, cudaStreamNonBlocking));
             IPCG_CUDA(cudaEventCreateWithFlags(&m->ev_fork, cudaEventDisableTiming));
             IPCG_CUDA(cudaEventCreateWithFlags(&m->ev_side, cudaEventDisableTiming));
-            IPCG_CUDA(cudaEventCreateWithFlags(&m->ev_lh, cudaEventDisableTiming));
             IPCG_CUDA(cudaEventCreateWithFlags(&m->ev_pattern, cudaEventDisableTiming));
             m->nV = nV;
             m->nE = nE;

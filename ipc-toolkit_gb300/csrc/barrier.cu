@@ -1249,8 +1249,7 @@ __device__ bool project_psd_slab(int n, const Slab& hs, int64_t i, int method)
     return true;
 }
 
-// Contacts [first, first + count) of the chunk; the launches over the VV+EV
-// and the EE+FV ranges run on different streams.
+// Contacts [first, first + count) of the chunk.
 __global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, Slab hs,
     const uint8_t* __restrict__ proj, int method, int* __restrict__ fail, int64_t first, int64_t count)
 {
@@ -2300,21 +2299,6 @@ static const Params* upload_params(const ipcg_collisions* cs, ipcg_mesh* m, cons
 
 // With fr set, the same pipeline evaluates the friction potential of the
 // tangential set whose stencils are cs at velocities V (single scene).
-// Contacts k_psd keeps resident on the current device at once (its blocks
-// per SM at full occupancy x SMs x block size), measured once per process
-// (a function-local static, so concurrent first calls are safe).
-static int64_t psd_resident_contacts()
-{
-    static const int64_t cached = [] {
-        int dev = 0, sms = 0, per_sm = 0;
-        IPCG_CUDA(cudaGetDevice(&dev));
-        IPCG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        IPCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_psd, PSD_BLOCK, 0));
-        return (int64_t)std::max(per_sm, 1) * std::max(sms, 1) * PSD_BLOCK;
-    }();
-    return cached;
-}
-
 void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev, ipcg_csr* hess, const FrictionView* fr)
 {
@@ -2409,13 +2393,12 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
             int nb = 0;
             // Three streams, forked after everything queued so far on the main
             // one.  The side stream computes the VV, EV and FV local Hessians
-            // and projects VV and EV; the main stream computes the EE local
-            // Hessians and, once FV's are in, projects the contiguous EE+FV
-            // range (all 12 x 12).  The pattern stream builds the sparsity
-            // pattern (block keys, sort, run-length encoding, row and column
-            // arrays), which does not depend on the values.  Each of these
-            // launches fills only a few warps per SM, so running them side by
-            // side keeps the FP64 pipes busier than running them in turn.
+            // while the main one computes the EE ones (each launch fills only
+            // a few warps per SM, so side by side they keep the FP64 pipes
+            // busier than in turn); the main stream then projects them all.
+            // The pattern stream builds the sparsity pattern (block keys, sort,
+            // run-length encoding, row and column arrays), which does not
+            // depend on the values, beside both.
             cudaStream_t t = m->side, u = m->side2;
             IPCG_CUDA(cudaEventRecord(m->ev_fork, s));
             IPCG_CUDA(cudaStreamWaitEvent(t, m->ev_fork, 0));
@@ -2449,16 +2432,6 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
                     if (count[3])
                         IPCG_LAUNCH("k_local_hessian_fv", t, k_local_hessian<CT_FV><<<grid_for(count[3], LH_BLOCK),
                             LH_BLOCK, 0, t>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[3], count[3]));
-                    IPCG_CUDA(cudaEventRecord(m->ev_lh, t));
-                    // The VV+EV projection runs beside the EE+FV one only while
-                    // the chunk fills less than half of the contacts k_psd keeps
-                    // resident; past that, concurrent launches only contend for
-                    // the same L1 and one launch over the chunk does better.
-                    const bool split = 2 * nc < psd_resident_contacts();
-                    const int64_t n_small = split ? count[0] + count[1] : 0;
-                    if (a.psd != IPCG_PSD_NONE && n_small)
-                        IPCG_LAUNCH("k_psd_vv_ev", t, k_psd<<<grid_for(n_small, PSD_BLOCK), PSD_BLOCK, 0, t>>>(cc,
-                            slab, m->proj.p, a.psd, d_fail, first[0], n_small));
                     IPCG_CUDA(cudaEventRecord(m->ev_side, t));
                     if (count[2] && a.shape)
                         IPCG_LAUNCH("k_shape_local_ee", s, k_shape_local_ee<<<grid_for(count[2], LH_BLOCK), LH_BLOCK,
@@ -2466,11 +2439,10 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
                     else if (count[2])
                         IPCG_LAUNCH("k_local_hessian_ee", s, k_local_hessian<CT_EE><<<grid_for(count[2], LH_BLOCK),
                             LH_BLOCK, 0, s>>>(cc, m->E.p, m->F.p, V, sp, sv, slab, m->proj.p, first[2], count[2]));
-                    IPCG_CUDA(cudaStreamWaitEvent(s, split ? m->ev_lh : m->ev_side, 0));
-                    const int64_t p0 = split ? first[2] : 0, n_big = split ? count[2] + count[3] : nc;
-                    if (a.psd != IPCG_PSD_NONE && n_big)
-                        IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(n_big, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, slab,
-                            m->proj.p, a.psd, d_fail, p0, n_big));
+                    IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
+                    if (a.psd != IPCG_PSD_NONE)
+                        IPCG_LAUNCH("k_psd", s, k_psd<<<grid_for(nc, PSD_BLOCK), PSD_BLOCK, 0, s>>>(cc, slab,
+                            m->proj.p, a.psd, d_fail, 0, nc));
                 }
                 IPCG_CUDA(cudaStreamWaitEvent(s, m->ev_side, 0));
                 // sparsity pattern: sort (block key, contribution) and run-length encode

@@ -170,11 +170,11 @@ struct ipcg_mesh {
     std::vector<unsigned char> params_host; // what params_buf holds
     ipcg::DBuf<double> scene_md;     // CCD: per-scene 0.5*min_distance, then min_distance
     cudaStream_t stream = nullptr;
-    // streams for work that overlaps the main one (the Hessian's small-stencil
-    // local Hessians and projections on `side`, its sparsity pattern on
-    // `side2`), with the events that fork and join them
+    // streams for work that overlaps the main one (the Hessian's VV, EV and
+    // FV local Hessians on `side`, its sparsity pattern on `side2`), with the
+    // events that fork and join them
     cudaStream_t side = nullptr, side2 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_side = nullptr, ev_lh = nullptr, ev_pattern = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_side = nullptr, ev_pattern = nullptr;
     ipcg::DBuf<double> rest;
     ipcg::DBuf<int> E, F, F2E;
     std::vector<int32_t> h_F2E;
