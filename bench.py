@@ -45,7 +45,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--workload", choices=["sphere_pack", "two_sheet", "layered_cloth"], default="sphere_pack")
@@ -106,35 +106,51 @@ def algorithmic_bytes(counts, ndof):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling around the timed region.
+
+    Rows are timestamped on arrival; start() returns once the first row is in
+    (nvidia-smi takes a moment to start), and stop() keeps the rows that
+    arrived inside the window given by mark() (the timed region), or the first
+    row after its start when the region is shorter than the sampling interval."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    INTERVAL_MS = 50
 
     def __init__(self, index=0):
         self.index = index
         self.rows = []
         self.proc = None
         self.thread = None
+        self.window = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", str(self.INTERVAL_MS)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
             return
         self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        t0 = time.perf_counter()
+        while not self.rows and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 9:
-                self.rows.append(parts)
+                self.rows.append((time.perf_counter(), parts))
+
+    def mark(self, t_begin, t_end):
+        self.window = (t_begin, t_end)
 
     def stop(self):
+        if self.window is not None:
+            # let the row that covers the end of the window arrive
+            time.sleep(2 * self.INTERVAL_MS / 1000.0)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -143,14 +159,20 @@ class ClockSampler:
                 self.proc.kill()
         if self.thread is not None:
             self.thread.join(timeout=2)
-        if not self.rows:
+        rows = [r for _, r in self.rows]
+        if self.window is not None and self.rows:
+            lo, hi = self.window
+            inside = [r for t, r in self.rows if lo <= t <= hi + self.INTERVAL_MS / 1000.0]
+            after = [r for t, r in self.rows if t >= lo]
+            rows = inside or after[:1] or rows[-1:]
+        if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows), "interval_ms": self.INTERVAL_MS}
 
 
 def measured_peaks():
@@ -522,6 +544,8 @@ def run_gb300(args, rank, world):
         H.free()
         return nnz
 
+    clocks = ClockSampler(local)
+    clocks.start()  # before the warm-up, so the GPU is busy when the timed steps start
     for _ in range(max(3, args.warmup)):
         nnz = step()
     torch.cuda.synchronize()
@@ -529,9 +553,8 @@ def run_gb300(args, rank, world):
         import torch.distributed as dist
         dist.barrier()
     ipctk.profile_enable(True)
-    clocks = ClockSampler(local)
-    clocks.start()
     launches0 = ipctk.launch_count()
+    t_region = time.perf_counter()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
         flush.zero_()  # L2 flush between timed steps (outside the events)
@@ -540,6 +563,7 @@ def run_gb300(args, rank, world):
         step()
         ev[i][1].record(stream)
     torch.cuda.synchronize()
+    clocks.mark(t_region, time.perf_counter())
     launches = ipctk.launch_count() - launches0
     clk = clocks.stop()
     prof = ipctk.profile_report()
