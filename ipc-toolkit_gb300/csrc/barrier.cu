@@ -619,8 +619,13 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
         }
         K *= 0.5 * tau;
         for (int i = k + 1; i < n; ++i) p[i] -= K * v[i];
+        // the update is symmetric: form the upper triangle, mirror it
         for (int i = k + 1; i < n; ++i)
-            for (int j = k + 1; j < n; ++j) A[i * MAXR + j] -= v[i] * p[j] + p[i] * v[j];
+            for (int j = i; j < n; ++j) {
+                const double a = A[i * MAXR + j] - (v[i] * p[j] + p[i] * v[j]);
+                A[i * MAXR + j] = a;
+                A[j * MAXR + i] = a;
+            }
         e[k] = alpha;
         htau[k] = tau;
     }
@@ -1177,30 +1182,57 @@ __device__ __forceinline__ int stencil_size(const ContactsView& cv, int64_t i)
 
 // PSD projection (eigen_ext.tpp:64-108) of every local Hessian, in place.
 constexpr int PSD_BLOCK = LH_BLOCK;
-// M = C H C^T read straight from contact i's slab (the element-major layout
-// makes each element a coalesced load across the warp's contacts).
+
+// The NS - 1 contrasts sum_a C[k][a] v[a] of one value per stencil vertex.
+// NS = 4: C is the Hadamard matrix's rows without the all-ones one, times
+// 1/2; the butterflies here leave out that 1/2 (applied once by the caller).
+// NS = 3, 2: scaled in place.
+template <int NS> __device__ __forceinline__ void contrast_apply(const double* v, double* o)
+{
+    constexpr double R2 = 0.70710678118654752440, R6 = 0.40824829046386301637;
+    if (NS == 4) {
+        const double s01 = v[0] + v[1], d01 = v[0] - v[1], s23 = v[2] + v[3], d23 = v[2] - v[3];
+        o[0] = d01 + d23;
+        o[1] = s01 - s23;
+        o[2] = d01 - d23;
+    } else if (NS == 3) {
+        o[0] = (v[0] - v[1]) * R2;
+        o[1] = fma(-2.0, v[2], v[0] + v[1]) * R6;
+    } else {
+        o[0] = (v[0] - v[1]) * R2;
+    }
+}
+
+// M = C H C^T (rows of M with stride MAXR) straight from contact i's slab:
+// for each coordinate c, T = C H restricted to the rows of coordinate c (each
+// slab element loaded once, coalesced across the warp's contacts), then row
+// 3k+c of M from T's row k.
 template <int NS> __device__ void to_contrasts_slab(const Slab& hs, int64_t i, double* M)
 {
-    constexpr int N = 3 * NS;
+    constexpr int N = 3 * NS, K = NS - 1;
+    constexpr double S = NS == 4 ? 0.25 : 1.0; // the two butterfly stages' missing (1/2)^2
 #pragma unroll 1
-    for (int r = 0; r < 3 * (NS - 1); ++r) {
-        const int k = r / 3, c = r % 3;
-        double row[N];
+    for (int c = 0; c < 3; ++c) {
+        double T[K][N];
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            double s = 0;
+            double v[NS], o[K];
 #pragma unroll
-            for (int a = 0; a < NS; ++a) s += contrast<NS>(k, a) * hs.at(i, (3 * a + c) * N + j);
-            row[j] = s;
+            for (int a = 0; a < NS; ++a) v[a] = hs.at(i, (3 * a + c) * N + j);
+            contrast_apply<NS>(v, o);
+#pragma unroll
+            for (int k = 0; k < K; ++k) T[k][j] = o[k];
         }
 #pragma unroll
-        for (int l = 0; l < NS - 1; ++l)
+        for (int k = 0; k < K; ++k)
 #pragma unroll
             for (int e = 0; e < 3; ++e) {
-                double s = 0;
+                double v[NS], o[K];
 #pragma unroll
-                for (int b = 0; b < NS; ++b) s += contrast<NS>(l, b) * row[3 * b + e];
-                M[r * MAXR + 3 * l + e] = s;
+                for (int b = 0; b < NS; ++b) v[b] = T[k][3 * b + e];
+                contrast_apply<NS>(v, o);
+#pragma unroll
+                for (int l = 0; l < K; ++l) M[(3 * k + c) * MAXR + 3 * l + e] = NS == 4 ? S * o[l] : o[l];
             }
     }
 }
