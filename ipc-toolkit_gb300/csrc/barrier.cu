@@ -1271,13 +1271,18 @@ __device__ bool project_psd_slab(int n, const Slab& hs, int64_t i, int method)
         sl[nneg++] = f * lam[k];
     }
     if (nneg == 0) return true; // already PSD: returned as is
+    // H+ is symmetric: the upper triangle is formed and mirrored
 #pragma unroll 1
-    for (int r = 0; r < N; ++r)
-        for (int c = 0; c < N; ++c) {
+    for (int r = 0; r < N; ++r) {
+        double swr[MAXR];
+        for (int t = 0; t < nneg; ++t) swr[t] = sl[t] * wv[12 * t + r];
+        for (int c = r; c < N; ++c) {
             double v = hs.at(i, r * N + c);
-            for (int t = 0; t < nneg; ++t) v -= (sl[t] * wv[12 * t + r]) * wv[12 * t + c];
+            for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
             hs.at(i, r * N + c) = v;
+            if (c != r) hs.at(i, c * N + r) = v;
         }
+    }
     return true;
 }
 
