@@ -1128,7 +1128,11 @@ __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, con
         const float d = fv_local_f(x, gf, Hf);
         const float w = (float)c.w, a = w * fd2f(P, d), b = w * fd1f(P, d);
         for (int r = 0; r < 12; ++r)
-            for (int q = 0; q < 12; ++q) hs.at(i, r * 12 + q) = (double)(a * gf[r] * gf[q] + b * Hf[r * 12 + q]);
+            for (int q = r; q < 12; ++q) {
+                const double v = (double)(a * gf[r] * gf[q] + b * Hf[r * 12 + q]);
+                hs.at(i, r * 12 + q) = v;
+                hs.at(i, q * 12 + r) = v;
+            }
         proj[i] = 1;
         return;
     }
@@ -1149,28 +1153,46 @@ __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, con
         if (act && m <= 0) {
             double gm[12];
             mollifier(c, x, gm, H, act);
-            for (int k = 0; k < 144; ++k) hs.at(i, k) = (c.w * fv) * H[k];
+            for (int r = 0; r < 12; ++r)
+                for (int q = r; q < 12; ++q) {
+                    const double v = (c.w * fv) * H[r * 12 + q];
+                    hs.at(i, r * 12 + q) = v;
+                    hs.at(i, q * 12 + r) = v;
+                }
             pr = 0;
         } else {
             const double fd = fd1(P, d), fdd = fd2(P, d);
             const double wm = c.w * m;
+            // the matrices are symmetric: upper triangles formed, mirrored
             for (int r = 0; r < 12; ++r)
-                for (int q = 0; q < 12; ++q) hs.at(i, r * 12 + q) = (wm * fdd) * g[r] * g[q] + (wm * fd) * H[r * 12 + q];
+                for (int q = r; q < 12; ++q) {
+                    const double v = (wm * fdd) * g[r] * g[q] + (wm * fd) * H[r * 12 + q];
+                    hs.at(i, r * 12 + q) = v;
+                    hs.at(i, q * 12 + r) = v;
+                }
             if (act) {
                 double gm[12];
                 mollifier(c, x, gm, H, act);
                 for (int r = 0; r < 12; ++r)
-                    for (int q = 0; q < 12; ++q) {
+                    for (int q = r; q < 12; ++q) {
                         const double gfm_rq = (c.w * fd) * g[r] * gm[q];
                         const double gfm_qr = (c.w * fd) * g[q] * gm[r];
-                        hs.at(i, r * 12 + q) += (c.w * fv) * H[r * 12 + q] + gfm_rq + gfm_qr;
+                        const double v = hs.at(i, r * 12 + q) + ((c.w * fv) * H[r * 12 + q] + gfm_rq + gfm_qr);
+                        hs.at(i, r * 12 + q) = v;
+                        hs.at(i, q * 12 + r) = v;
                     }
             }
         }
     } else {
         const double fd = fd1(P, d), fdd = fd2(P, d);
+#pragma unroll
         for (int r = 0; r < N; ++r)
-            for (int q = 0; q < N; ++q) hs.at(i, r * N + q) = (c.w * fdd) * g[r] * g[q] + (c.w * fd) * H[r * N + q];
+#pragma unroll
+            for (int q = r; q < N; ++q) {
+                const double v = (c.w * fdd) * g[r] * g[q] + (c.w * fd) * H[r * N + q];
+                hs.at(i, r * N + q) = v;
+                hs.at(i, q * N + r) = v;
+            }
     }
     proj[i] = pr;
 }
