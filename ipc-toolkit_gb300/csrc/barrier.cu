@@ -590,9 +590,11 @@ constexpr int MAXR = 9;
 constexpr int MAXROT = 128; // recorded rotations; beyond, Q is accumulated
 
 __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* d, double* Q, double* rc, double* rs,
-    int8_t* rk, int& nrot, double* hv, double* htau)
+    int8_t* rk, int& nrot, double* htau)
 {
-    // Householder tridiagonalisation; reflector k kept in hv[k*MAXR + .], htau[k]
+    // Householder tridiagonalisation; reflector k is I - htau[k] v v^T with
+    // v[k+1..n) kept in A[k+1..n)[k], the column it annihilates (the updates
+    // below touch only rows and columns past k)
     double e[MAXR];
     for (int k = 0; k + 2 < n; ++k) {
         double sig = 0;
@@ -605,24 +607,23 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
         }
         const double nx = sqrt(x0 * x0 + sig);
         const double alpha = (x0 >= 0) ? -nx : nx;
-        double* v = hv + k * MAXR;
+        const double v0 = x0 - alpha;
+        A[(k + 1) * MAXR + k] = v0;
         double p[MAXR];
-        v[k + 1] = x0 - alpha;
-        for (int i = k + 2; i < n; ++i) v[i] = A[i * MAXR + k];
-        const double tau = 2.0 / (v[k + 1] * v[k + 1] + sig);
+        const double tau = 2.0 / (v0 * v0 + sig);
         double K = 0;
         for (int i = k + 1; i < n; ++i) {
             double s = 0;
-            for (int j = k + 1; j < n; ++j) s += A[i * MAXR + j] * v[j];
+            for (int j = k + 1; j < n; ++j) s += A[i * MAXR + j] * A[j * MAXR + k];
             p[i] = tau * s;
-            K += p[i] * v[i];
+            K += p[i] * A[i * MAXR + k];
         }
         K *= 0.5 * tau;
-        for (int i = k + 1; i < n; ++i) p[i] -= K * v[i];
+        for (int i = k + 1; i < n; ++i) p[i] -= K * A[i * MAXR + k];
         // the update is symmetric: form the upper triangle, mirror it
         for (int i = k + 1; i < n; ++i)
             for (int j = i; j < n; ++j) {
-                const double a = A[i * MAXR + j] - (v[i] * p[j] + p[i] * v[j]);
+                const double a = A[i * MAXR + j] - (A[i * MAXR + k] * p[j] + p[i] * A[j * MAXR + k]);
                 A[i * MAXR + j] = a;
                 A[j * MAXR + i] = a;
             }
@@ -707,31 +708,36 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
     return true;
 }
 
-// Eigenvector i of M: Q_h G e_i.  G e_i comes from the recorded rotations
-// (applied last first) or, if they were not recorded (nrot < 0), from
-// column i of Q; then the Householder reflectors, H_{n-3} first.
-__device__ void eigvec(int n, int i, const double* Q, const double* rc, const double* rs, const int8_t* rk, int nrot,
-    const double* hv, const double* htau, double* y)
+// Eigenvectors idx[0..cnt) of M, rows of Y (stride MAXR): Q_h G e_i.  G e_i
+// comes from the recorded rotations, applied last first to all cnt vectors in
+// one pass (each rotation loaded once), or, if they were not recorded
+// (nrot < 0), from column i of Q; then the Householder reflectors kept in A's
+// lower columns, H_{n-3} first.
+__device__ void eigvecs(int n, const int* idx, int cnt, const double* Q, const double* rc, const double* rs,
+    const int8_t* rk, int nrot, const double* A, const double* htau, double* Y)
 {
-    if (nrot >= 0) {
-        for (int q = 0; q < n; ++q) y[q] = (q == i) ? 1.0 : 0.0;
-        for (int r = nrot - 1; r >= 0; --r) {
-            const int k = rk[r];
-            const double c = rc[r], s = rs[r];
+    for (int t = 0; t < cnt; ++t)
+        for (int q = 0; q < n; ++q)
+            Y[t * MAXR + q] = nrot >= 0 ? (q == idx[t] ? 1.0 : 0.0) : Q[q * MAXR + idx[t]];
+    for (int r = nrot - 1; r >= 0; --r) {
+        const int k = rk[r];
+        const double c = rc[r], s = rs[r];
+        for (int t = 0; t < cnt; ++t) {
+            double* y = Y + t * MAXR;
             const double ya = y[k], yb = y[k + 1];
             y[k] = c * ya + s * yb;
             y[k + 1] = c * yb - s * ya;
         }
-    } else {
-        for (int q = 0; q < n; ++q) y[q] = Q[q * MAXR + i];
     }
     for (int k = n - 3; k >= 0; --k) {
         if (htau[k] == 0) continue;
-        const double* v = hv + k * MAXR;
-        double s = 0;
-        for (int q = k + 1; q < n; ++q) s += v[q] * y[q];
-        s *= htau[k];
-        for (int q = k + 1; q < n; ++q) y[q] -= s * v[q];
+        for (int t = 0; t < cnt; ++t) {
+            double* y = Y + t * MAXR;
+            double s = 0;
+            for (int q = k + 1; q < n; ++q) s += A[q * MAXR + k] * y[q];
+            s *= htau[k];
+            for (int q = k + 1; q < n; ++q) y[q] -= s * A[q * MAXR + k];
+        }
     }
 }
 
@@ -1275,24 +1281,30 @@ __device__ bool project_psd_slab(int n, const Slab& hs, int64_t i, int method)
             const double avg = 0.5 * (M[r * MAXR + s] + M[s * MAXR + r]);
             M[r * MAXR + s] = M[s * MAXR + r] = avg;
         }
-    double rc[MAXROT], rs[MAXROT], hv[MAXR * MAXR], htau[MAXR];
+    double rc[MAXROT], rs[MAXROT], htau[MAXR];
     int8_t rk[MAXROT];
     int nrot;
-    if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, hv, htau)) return false;
+    if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, htau)) return false;
     const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
-    double wv[MAXR * 12], sl[MAXR];
+    int idx[MAXR];
     int nneg = 0;
-    for (int k = 0; k < m; ++k) {
-        if (!(lam[k] < 0)) continue;
+    for (int k = 0; k < m; ++k)
+        if (lam[k] < 0) idx[nneg++] = k;
+    if (nneg == 0) return true; // already PSD: returned as is
+    // the eigenvectors (rows of 9) and then the w = C^T q (rows of 12) share
+    // wv: row t of w is written after rows t.. of q are read (t descending),
+    // and rows below t lie below 12 t
+    double wv[MAXR * 12], sl[MAXR];
+    eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, wv);
+    for (int t = nneg - 1; t >= 0; --t) {
         double q[MAXR];
-        eigvec(m, k, Q, rc, rs, rk, nrot, hv, htau, q);
-        double* w = wv + 12 * nneg;
+        for (int j = 0; j < m; ++j) q[j] = wv[t * MAXR + j];
+        double* w = wv + 12 * t;
         if (n == 4) from_contrasts<4>(q, w);
         else if (n == 3) from_contrasts<3>(q, w);
         else from_contrasts<2>(q, w);
-        sl[nneg++] = f * lam[k];
+        sl[t] = f * lam[idx[t]];
     }
-    if (nneg == 0) return true; // already PSD: returned as is
     // H+ is symmetric: the upper triangle is formed and mirrored
 #pragma unroll 1
     for (int r = 0; r < N; ++r) {
