@@ -105,6 +105,23 @@ def algorithmic_bytes(counts, ndof):
     return b
 
 
+def ccd_candidate_count(ipctk, mesh, V0, V1, strict=False):
+    """Broad-phase candidate count of one compute_collision_free_stepsize call
+    (the C ABI's n_candidates output), or None if it cannot be read."""
+    try:
+        import ctypes
+        d = ipctk.DEFAULT_NARROW_PHASE_CCD
+        step, count = np.zeros(1), np.zeros(1, np.int64)
+        ipctk._check(ipctk._load().ipcg_collision_free_stepsize(
+            mesh._h, ipctk._ptr(V0), ipctk._ptr(V1), 0.0, d.tolerance, int(d.max_iterations),
+            d.conservative_rescaling, step.ctypes.data_as(ctypes.c_void_p), count.ctypes.data_as(ctypes.c_void_p)))
+        return int(count[0])
+    except Exception:
+        if strict:
+            raise
+        return None
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling around the timed region.
 
@@ -657,6 +674,7 @@ def run_gb300(args, rank, world):
             ccd_ms.append(1000 * (t1 - t0))
             build_ms.append(1000 * (t2 - t1))
     step_size = ipctk.compute_collision_free_stepsize(mesh, Vd, V1d)
+    ccd_candidates = ccd_candidate_count(ipctk, mesh, Vd, V1d)
 
     if rank != 0:
         return
@@ -702,7 +720,10 @@ def run_gb300(args, rank, world):
         "clocks": clk,
         "fused_egh": {"value": C / (fused_ms / 1000.0), "unit": UNIT, "ms_per_step": fused_ms},
         "ccd": {"steps_per_s": 1000.0 / statistics.median(ccd_ms), "p50_ms": pct(ccd_ms, 50),
-                "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "cpu_baseline": ccd_cpu},
+                "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "candidates": ccd_candidates,
+                "candidates_per_s": (ccd_candidates / (statistics.median(ccd_ms) / 1000.0)
+                                     if ccd_candidates else None),
+                "cpu_baseline": ccd_cpu},
         "collision_build": {"p50_ms": pct(build_ms, 50), "p99_ms": pct(build_ms, 99)},
         "batch": batch,
         "served": served,

@@ -76,3 +76,20 @@ def test_reference_arm_json_line():
     assert line["e2e"] == {"value": line["value"], "unit": "contacts/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
     assert line["config"]["contacts"] == 31066
+
+
+def test_ccd_candidate_count_marshalling():
+    # No device here: the library answers with an error status (raised by the
+    # mirror as ValueError / RuntimeError), not a ctypes argument error.
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "ipc-toolkit_gb300"))
+    import ipctk_gb300 as ipctk
+    b = load_bench()
+
+    class NoMesh:
+        _h = None
+
+    V = np.zeros((4, 3))
+    with pytest.raises((ValueError, RuntimeError)):
+        b.ccd_candidate_count(ipctk, NoMesh(), V, V, strict=True)
+    assert b.ccd_candidate_count(ipctk, NoMesh(), V, V) is None
