@@ -4,8 +4,10 @@ Each test restates an analytic test of the reference (cited by file:line of
 tests/src/tests/ in ipc-toolkit) or checks a derivative by central finite
 differences, the way the reference's FD tests do.  The reference itself
 cannot be built in this container (its CMake dependencies are absent), so
-these tests and the committed fixtures in tests/golden/ are what pins the
-oracle.
+these restated known-answer tests are what pins the oracle to the reference.
+The fixtures in tests/golden/ (inputs stored with the oracle's outputs) then
+hold the oracle (test_golden.py) and the CUDA path (test_gpu_golden.py) to
+those results.
 """
 import numpy as np
 import pytest
