@@ -97,6 +97,18 @@ int ipcg_mesh_destroy(ipcg_mesh* mesh);
 /* CollisionMesh::num_vertices/num_edges/num_faces (collision_mesh.hpp) */
 int ipcg_mesh_sizes(const ipcg_mesh* mesh, int64_t sizes[3]);
 
+/* CollisionMesh::num_codim_vertices() / num_codim_edges() (collision_mesh.cpp:
+ * 145-183): counts[0] vertices that belong to no edge, counts[1] edges that
+ * belong to no face.  The reference finds extra vertex-vertex candidates among
+ * codimensional vertices and edge-vertex candidates between codimensional
+ * edges and codimensional vertices (candidates.cpp:66-116, 152-210).  Those
+ * passes are not provided: collision-set builds, candidate builds and step-size
+ * calls on a mesh with codimensional vertices fail with IPCG_ERR_INVALID
+ * instead of returning an incomplete result.  Codimensional edges alone need
+ * no extra pass (their contacts with surface vertices are edge-edge or
+ * face-vertex candidates) and are supported. */
+int ipcg_mesh_codim_counts(const ipcg_mesh* mesh, int64_t counts[2]);
+
 /* CollisionMesh::faces_to_edges() (collision_mesh.hpp:327-329): num_faces*3 */
 int ipcg_mesh_faces_to_edges(const ipcg_mesh* mesh, int32_t* out);
 
@@ -283,18 +295,22 @@ int ipcg_barrier_gauss_newton_hessian_quadratic_form(const ipcg_collisions* coll
  * hard budget, or that cannot afford cudaMalloc/cudaFree synchronising the
  * device under their other streams.  It computes the same value as
  * ipcg_barrier_energy from a collision set held entirely in caller-owned
- * DEVICE arrays (layout of ipcg_collisions_get, topology as for
- * ipcg_mesh_create) and writes it to the device double *energy.  It
- * allocates nothing: the reduction's partial sums live in a static device
- * array of 16385 doubles (128 KiB) that every GPU loading this library keeps
- * until exit.  At most 2,097,152 contacts per call (larger sets are
- * rejected with IPCG_ERR_INVALID).  The work is enqueued on `stream`
- * (a cudaStream_t, NULL for the default stream) and the call returns without
- * waiting; *energy is valid once the stream reaches it.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress), so make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU (on different streams or host threads) race
- * and must be serialised by the caller. */
+ * DEVICE arrays of the current device (layout of ipcg_collisions_get,
+ * topology as for ipcg_mesh_create) and writes it to the device double
+ * *energy.  It allocates nothing: the reduction's partial sums live in a
+ * static device array of 16385 doubles (128 KiB) that every GPU loading this
+ * library keeps until exit.  At most 2,097,152 contacts per call (larger sets
+ * are rejected with IPCG_ERR_INVALID before anything is launched).  The
+ * indices are checked on the device against num_vertices / num_edges /
+ * num_faces (and edge-edge distance types against 0..8): a contact with an
+ * index out of range is not evaluated and the energy comes back NaN.  The
+ * work is enqueued on `stream` (a cudaStream_t, NULL for the default stream)
+ * and the call returns without waiting; *energy is valid once the stream
+ * reaches it.  The first call on a device (and the first after its context
+ * is replaced, e.g. by cudaDeviceReset) looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU (on different
+ * streams or host threads) race and must be serialised by the caller. */
 int ipcg_barrier_energy_noalloc(const double* vertices, int64_t num_vertices,
                                 const int32_t* edges, int64_t num_edges,
                                 const int32_t* faces, int64_t num_faces,

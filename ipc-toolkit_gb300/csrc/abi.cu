@@ -129,6 +129,21 @@ bool is_device_ptr(const void* p)
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+bool is_device_ptr_on_current(const void* p)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (a.type == cudaMemoryTypeManaged) return true;
+    if (a.type != cudaMemoryTypeDevice) return false;
+    // memory of another device is rejected: a kernel on this device would
+    // fault on it unless peer access happened to be enabled
+    int dev = -1;
+    return cudaGetDevice(&dev) == cudaSuccess && a.device == dev;
+}
+
 const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf)
 {
     if (is_device_ptr(V)) return V;
@@ -138,6 +153,15 @@ const double* stage_positions(ipcg_mesh* m, const double* V, DBuf<double>& buf)
 }
 
 void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+void require_no_codim_vertices(const ipcg_mesh* m)
+{
+    if (m && m->n_codim_vertices > 0)
+        throw Error(IPCG_ERR_INVALID,
+            "the mesh has " + std::to_string(m->n_codim_vertices)
+                + " codimensional vertices (vertices in no edge): their vertex-vertex and edge-vertex candidate "
+                  "passes are not provided");
+}
 
 } // namespace ipcg
 
@@ -324,8 +348,19 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
                 if (it == emap.end()) throw Error(IPCG_ERR_TOPOLOGY, "Unable to find edge!");
                 f2e[3 * f + j] = it->second;
             }
+        // codimensional vertices (in no edge) and edges (in no face)
+        int64_t n_codim_v = 0, n_codim_e = 0;
+        {
+            std::vector<uint8_t> used(nV, 0), in_face(nE, 0);
+            for (int32_t v : hE) used[v] = 1;
+            for (int32_t e : f2e) in_face[e] = 1;
+            for (uint8_t u : used) n_codim_v += !u;
+            for (uint8_t u : in_face) n_codim_e += !u;
+        }
         auto* m = new ipcg_mesh();
         try {
+            m->n_codim_vertices = n_codim_v;
+            m->n_codim_edges = n_codim_e;
             IPCG_CUDA(cudaGetDevice(&m->device));
             IPCG_CUDA(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
             IPCG_CUDA(cudaStreamCreateWithFlags(&m->side, cudaStreamNonBlocking));
@@ -413,6 +448,15 @@ int ipcg_mesh_sizes(const ipcg_mesh* m, int64_t sizes[3])
         sizes[0] = m->nV;
         sizes[1] = m->nE;
         sizes[2] = m->nF;
+    });
+}
+
+int ipcg_mesh_codim_counts(const ipcg_mesh* m, int64_t counts[2])
+{
+    return guarded([&] {
+        require(m && counts, "NULL argument");
+        counts[0] = m->n_codim_vertices;
+        counts[1] = m->n_codim_edges;
     });
 }
 
@@ -516,6 +560,7 @@ int ipcg_collisions_build_batch(ipcg_collisions* c, const ipcg_mesh* mesh, const
             require(dhat[k] > 0, "dhat must be positive");
             require(dmin[k] >= 0, "dmin must be non-negative");
         }
+        require_no_codim_vertices(mesh);
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dV = stage_positions(m, V, m->V0);
@@ -1084,6 +1129,7 @@ int ipcg_collision_free_stepsize_batch(const ipcg_mesh* mesh, const double* V0, 
             require(min_distance[k] >= 0, "min_distance must be non-negative");
         require(tolerance > 0, "tolerance must be positive");
         require(rescale > 0 && rescale <= 1, "conservative_rescaling must be in (0, 1]");
+        require_no_codim_vertices(mesh);
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* d0 = stage_positions(m, V0, m->V0);
@@ -1111,6 +1157,7 @@ int ipcg_is_step_collision_free(const ipcg_mesh* mesh, const double* V0, const d
         require(min_distance >= 0, "min_distance must be non-negative");
         require(tolerance > 0, "tolerance must be positive");
         require(rescale > 0 && rescale <= 1, "conservative_rescaling must be in (0, 1]");
+        require_no_codim_vertices(mesh);
         ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* d0 = stage_positions(m, V0, m->V0);
@@ -1192,15 +1239,17 @@ int ipcg_barrier_energy_noalloc(const double* vertices, int64_t num_vertices, co
             nee ? ee_eps_x : nullptr, nee ? ee_dtype : nullptr, nee ? ee_w : nullptr, nee ? edges : nullptr,
             nfv ? fv : nullptr, nfv ? fv_w : nullptr, nfv ? faces : nullptr };
         for (const void* p : must_be_device)
-            if (p != nullptr) require(is_device_ptr(p), "allocation-free energy: every array must be device memory");
+            if (p != nullptr)
+                require(is_device_ptr_on_current(p),
+                    "allocation-free energy: every array must be device memory of the current device");
         require(nvv + nev + nee + nfv == 0 || vertices, "vertices is NULL");
         require(nvv == 0 || (vv && vv_w), "vv arrays are NULL");
         require(nev == 0 || (ev && ev_w && edges), "ev arrays are NULL");
         require(nee == 0 || (ee && ee_eps_x && ee_dtype && ee_w && edges), "ee arrays are NULL");
         require(nfv == 0 || (fv && fv_w && faces), "fv arrays are NULL");
         const ContactsNoAlloc in { nvv, nev, nee, nfv, vv, ev, ee, fv, vv_w, ev_w, ee_w, fv_w, ee_eps_x, ee_dtype };
-        barrier_energy_noalloc(vertices, edges, faces, in, dhat, stiffness, dmin, use_physical_barrier ? 1 : 0,
-            energy, (cudaStream_t)stream);
+        barrier_energy_noalloc(vertices, edges, faces, num_vertices, num_edges, num_faces, in, dhat, stiffness, dmin,
+            use_physical_barrier ? 1 : 0, energy, (cudaStream_t)stream);
     });
 }
 

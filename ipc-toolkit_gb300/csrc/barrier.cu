@@ -2837,6 +2837,66 @@ constexpr int NOALLOC_MAX_BLOCKS = 16384; // at most 16384 * BLOCK = 2,097,152 c
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mu;
 double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+void* g_noalloc_ctx[NOALLOC_MAX_DEVICES] = {}; // the context each cached address belongs to
+
+// The caller's topology arrays hold indices this library did not check, so
+// this path validates every index before it reads through it: a contact with
+// an edge, face or vertex index outside [0, num_*) (or an edge-edge distance
+// type outside 0..8) reads nothing further and contributes NaN, which makes
+// its block's partial sum, and so the returned energy, NaN.
+__device__ __forceinline__ bool load_contact_checked(const ContactsView& cv, const int* __restrict__ E,
+    const int* __restrict__ F, int64_t nV, int64_t nE, int64_t nF, int64_t i, Local& c)
+{
+    auto vok = [nV](int v) { return v >= 0 && (int64_t)v < nV; };
+    if (i < cv.nvv) {
+        const int2 p = cv.vv[i];
+        if (!vok(p.x) || !vok(p.y)) return false;
+    } else if (i < cv.nvv + cv.nev) {
+        const int2 p = cv.ev[i - cv.nvv];
+        if (!vok(p.y) || p.x < 0 || (int64_t)p.x >= nE) return false;
+        if (!vok(E[2 * p.x]) || !vok(E[2 * p.x + 1])) return false;
+    } else if (i < cv.nvv + cv.nev + cv.nee) {
+        const int64_t k = i - cv.nvv - cv.nev;
+        const int2 p = cv.ee[k];
+        if (p.x < 0 || (int64_t)p.x >= nE || p.y < 0 || (int64_t)p.y >= nE) return false;
+        if (!vok(E[2 * p.x]) || !vok(E[2 * p.x + 1]) || !vok(E[2 * p.y]) || !vok(E[2 * p.y + 1])) return false;
+        const int dt = cv.ee_dt[k];
+        if (dt < 0 || dt > 8) return false;
+    } else {
+        const int2 p = cv.fv[i - cv.nvv - cv.nev - cv.nee];
+        if (!vok(p.y) || p.x < 0 || (int64_t)p.x >= nF) return false;
+        if (!vok(F[3 * p.x]) || !vok(F[3 * p.x + 1]) || !vok(F[3 * p.x + 2])) return false;
+    }
+    load_contact(cv, E, F, i, c);
+    return true;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_energy_checked(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, int64_t nV, int64_t nE, int64_t nF, const double* __restrict__ V, Params P,
+    double* __restrict__ partial)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0;
+    if (i < n) {
+        Local c;
+        if (!load_contact_checked(cv, E, F, nV, nE, nF, i, c)) {
+            e = __longlong_as_double(0x7ff8000000000000ULL); // NaN
+        } else {
+            V3 x[4];
+            gather(V, c, x);
+            double g[12];
+            const double d = contact_distance(c, x, g, nullptr);
+            bool act;
+            const double m = mollifier(c, x, nullptr, nullptr, act);
+            e = c.w * m * fval(P, d);
+        }
+    }
+    typedef cub::BlockReduce<double, BLOCK> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const double s = BR(tmp).Sum(e);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
 } // namespace
 } // namespace ipcg
 
@@ -2844,36 +2904,59 @@ static __device__ __align__(256) double g_noalloc_partials[ipcg::NOALLOC_MAX_BLO
 
 namespace ipcg {
 namespace {
+// The current CUDA context (driver handle), read through the runtime's driver
+// entry point so that this library does not link the driver library itself.
+void* current_context()
+{
+    typedef int (*CtxGetCurrent)(void**);
+    static CtxGetCurrent fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess
+            || q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<CtxGetCurrent>(f);
+    }();
+    void* ctx = nullptr;
+    if (fn) fn(&ctx);
+    return ctx;
+}
+
 // Device address of the partial-sum array on `device` (which must be
-// current).  Looked up once per device with cudaGetSymbolAddress: in host
-// code the array's name is only a host-side stand-in, not a device address.
+// current).  In host code the array's name is only a host-side stand-in, not
+// a device address, so the address is looked up with cudaGetSymbolAddress
+// once per device and context: the first call on a device (and the first one
+// after its context was replaced, e.g. by cudaDeviceReset) does the look-up.
 double* noalloc_scratch(int device)
 {
     if (device < 0 || device >= NOALLOC_MAX_DEVICES) throw Error(IPCG_ERR_INVALID, "device index out of range");
+    void* ctx = current_context();
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
+    if (!g_noalloc_ptr[device] || g_noalloc_ctx[device] != ctx) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
         if (e != cudaSuccess || p == nullptr)
             throw Error(IPCG_ERR_CUDA, std::string("cudaGetSymbolAddress of the energy scratch failed: ")
                     + cudaGetErrorString(e));
         g_noalloc_ptr[device] = static_cast<double*>(p);
+        g_noalloc_ctx[device] = ctx;
     }
     return g_noalloc_ptr[device];
 }
 } // namespace
 
-void barrier_energy_noalloc(const double* V, const int* E, const int* F, const ContactsNoAlloc& in, double dhat,
-    double kappa, double dmin, int physical, double* energy, cudaStream_t s)
+void barrier_energy_noalloc(const double* V, const int* E, const int* F, int64_t nV, int64_t nE, int64_t nF,
+    const ContactsNoAlloc& in, double dhat, double kappa, double dmin, int physical, double* energy, cudaStream_t s)
 {
     const int64_t n = in.nvv + in.nev + in.nee + in.nfv;
-    const int nblk = grid_for(n, BLOCK);
-    if (nblk > NOALLOC_MAX_BLOCKS) {
+    // the limit is checked on the 64-bit count, before any block count is formed
+    if (n > (int64_t)NOALLOC_MAX_BLOCKS * BLOCK) {
         char msg[160];
         snprintf(msg, sizeof(msg), "too many contacts for the allocation-free energy: %lld > %lld",
             (long long)n, (long long)NOALLOC_MAX_BLOCKS * BLOCK);
         throw Error(IPCG_ERR_INVALID, msg);
     }
+    const int nblk = grid_for(n, BLOCK);
     int dev = 0;
     IPCG_CUDA(cudaGetDevice(&dev));
     double* partial = noalloc_scratch(dev);
@@ -2887,7 +2970,8 @@ void barrier_energy_noalloc(const double* V, const int* E, const int* F, const C
     Params P { kappa, dmin * dmin, xhat, physical ? dhat / barrier_units(0, xhat) : 1.0, IPCG_PSD_NONE, 0, 0 };
     // every block overwrites its partial and the final kernel overwrites the
     // result, so nothing in the shared array needs clearing between calls
-    IPCG_LAUNCH("k_energy", s, k_energy<<<nblk, BLOCK, 0, s>>>(cv, E, F, V, P, partial));
+    IPCG_LAUNCH("k_energy_checked", s, k_energy_checked<<<nblk, BLOCK, 0, s>>>(cv, E, F, nV, nE, nF, V, P,
+        partial));
     IPCG_LAUNCH("k_sum_partials", s, k_sum_partials<<<1, 1024, 0, s>>>(partial, nblk, energy));
 }
 

@@ -155,6 +155,7 @@ ipcg_mesh* checked_mesh(const ipcg_candidates* c, const ipcg_mesh* mesh)
     check(c && mesh, "NULL argument");
     check(mesh->n_scenes == 1, "candidate sets are built on single-scene meshes");
     check(c->mesh == nullptr || c->mesh == mesh, "the candidates were built on another mesh");
+    require_no_codim_vertices(mesh);
     ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
     IPCG_CUDA(cudaSetDevice(m->device));
     return m;

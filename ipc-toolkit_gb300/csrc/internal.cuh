@@ -161,6 +161,9 @@ struct ipcg_mesh {
     int device = 0;
     int64_t nV = 0, nE = 0, nF = 0;
     int64_t n_scenes = 1;
+    // CollisionMesh::num_codim_vertices / num_codim_edges (collision_mesh.cpp:
+    // 145-183): vertices in no edge, edges in no face
+    int64_t n_codim_vertices = 0, n_codim_edges = 0;
     std::vector<int64_t> h_voff;     // vertex offsets of the scenes (n_scenes + 1)
     ipcg::DBuf<int64_t> scene_offs;  // batches: vertex, edge, edge, face offsets (4 x (n_scenes + 1))
     ipcg::DBuf<int> vscene;          // per-vertex scene id (batches only)
@@ -276,6 +279,14 @@ inline SceneView scene_view(const ipcg_mesh* m) { return SceneView { (int)m->n_s
 // abi.cu: the calling thread's message for ipcg_last_error()
 void set_last_error(const std::string& msg);
 
+// Collision-set builds, candidate builds and step sizes find contacts through
+// the edge-edge and face-vertex passes only.  The reference adds
+// vertex-vertex candidates among codimensional vertices (vertices in no edge)
+// and edge-vertex candidates between codimensional edges and those vertices
+// (candidates.cpp:66-116, 152-210); those passes are not built here, so a mesh
+// with codimensional vertices is refused instead of giving an incomplete set.
+void require_no_codim_vertices(const ipcg_mesh* m);
+
 // barrier.cu: contacts per Hessian chunk of a batch (scratch memory bound)
 extern std::atomic<int64_t> g_hess_chunk_contacts;
 
@@ -350,9 +361,13 @@ struct ContactsNoAlloc {
     const double *vv_w, *ev_w, *ee_w, *fv_w, *ee_eps;
     const int8_t* ee_dtype;
 };
-// barrier.cu: the energy with its reduction scratch in a static device array
-void barrier_energy_noalloc(const double* V, const int* E, const int* F, const ContactsNoAlloc& in, double dhat,
-    double kappa, double dmin, int physical, double* energy, cudaStream_t s);
+// barrier.cu: the energy with its reduction scratch in a static device array;
+// every index is checked against nV / nE / nF on the device (a bad one makes
+// the energy NaN instead of reading out of bounds)
+void barrier_energy_noalloc(const double* V, const int* E, const int* F, int64_t nV, int64_t nE, int64_t nF,
+    const ContactsNoAlloc& in, double dhat, double kappa, double dmin, int physical, double* energy, cudaStream_t s);
+// whether p is device (or managed) memory that the current device can address
+bool is_device_ptr_on_current(const void* p);
 
 // ccd.cu
 // Per scene: min_distance[n_scenes] (host) in, steps[n_scenes] (host) out.

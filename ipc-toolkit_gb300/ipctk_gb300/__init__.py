@@ -56,6 +56,7 @@ def _load():
         "ipcg_mesh_create": (i32, [P, i64, P, i64, P, i64, PP]),
         "ipcg_mesh_destroy": (i32, [P]),
         "ipcg_mesh_sizes": (i32, [P, P]),
+        "ipcg_mesh_codim_counts": (i32, [P, P]),
         "ipcg_mesh_faces_to_edges": (i32, [P, P]),
         "ipcg_collisions_create": (i32, [PP]),
         "ipcg_collisions_destroy": (i32, [P]),
@@ -333,6 +334,23 @@ class CollisionMesh:
         p = C.c_void_p()
         _check(_load().ipcg_mesh_stream(self._h, C.byref(p)))
         return int(p.value or 0)
+
+    def _codim_counts(self):
+        c = np.zeros(2, np.int64)
+        _check(_load().ipcg_mesh_codim_counts(self._h, _ptr(c)))
+        return c
+
+    @property
+    def num_codim_vertices(self):
+        """CollisionMesh::num_codim_vertices(): vertices that belong to no edge.
+        Collision builds, candidate builds and step sizes refuse meshes that
+        have any (their extra candidate passes are not provided)."""
+        return int(self._codim_counts()[0])
+
+    @property
+    def num_codim_edges(self):
+        """CollisionMesh::num_codim_edges(): edges that belong to no face."""
+        return int(self._codim_counts()[1])
 
     @property
     def faces_to_edges(self):
