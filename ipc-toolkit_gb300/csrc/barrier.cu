@@ -17,9 +17,14 @@
 // where a Householder tridiagonalisation plus implicit QR with Wilkinson
 // shifts gives the eigenpairs, and only the negative ones are removed from
 // the 3n×3n Hessian.  The Hessian is assembled into a CSR matrix whose
-// pattern is the union of the contacts' 3×3 vertex blocks: block keys are
-// radix-sorted and de-duplicated, and each contact adds its values with
-// FP64 atomics at positions found by binary search in its block row.
+// pattern is the union of the contacts' 3×3 vertex blocks: the (block key,
+// contribution) pairs are radix-sorted and run-length encoded, which gives
+// the CSR pattern and, per block, its contributions in a fixed order;
+// k_assemble then sums each stored value's contributions in that order and
+// writes it once (no atomics, deterministic).  This file holds the per-type
+// kernels used by friction and shape derivatives and the energy / gradient
+// kernels; the barrier's own energy + gradient + Hessian pass with a cached
+// pattern lives in egh.cu, and the per-contact math in contact.cuh.
 #include <cub/block/block_reduce.cuh>
 
 #include <cstdio>
@@ -29,777 +34,12 @@
 #include <mutex>
 #include <vector>
 
-#include "geom.cuh"
-#include "internal.cuh"
+#include "contact.cuh"
 #include "profile.cuh"
 
 namespace ipcg {
 
 namespace {
-
-constexpr int BLOCK = 128;
-
-struct ContactsView {
-    int64_t nvv, nev, nee, nfv;
-    const int2 *vv, *ev, *ee, *fv;
-    const double *vv_w, *ev_w, *ee_w, *fv_w, *ee_eps;
-    const int8_t* ee_dt;
-};
-
-enum : int { CT_VV = 0, CT_EV = 1, CT_EE = 2, CT_FV = 3 };
-
-struct Local {
-    int type, n, dtype;
-    int vid[4];
-    double w, eps;
-};
-
-__device__ __forceinline__ void load_contact(const ContactsView& cv, const int* __restrict__ E,
-    const int* __restrict__ F, int64_t i, Local& c)
-{
-    if (i < cv.nvv) {
-        const int2 p = cv.vv[i];
-        c.type = CT_VV;
-        c.n = 2;
-        c.vid[0] = p.x;
-        c.vid[1] = p.y;
-        c.w = cv.vv_w[i];
-        return;
-    }
-    i -= cv.nvv;
-    if (i < cv.nev) {
-        const int2 p = cv.ev[i];
-        c.type = CT_EV;
-        c.n = 3;
-        c.vid[0] = p.y;
-        c.vid[1] = E[2 * p.x];
-        c.vid[2] = E[2 * p.x + 1];
-        c.w = cv.ev_w[i];
-        return;
-    }
-    i -= cv.nev;
-    if (i < cv.nee) {
-        const int2 p = cv.ee[i];
-        c.type = CT_EE;
-        c.n = 4;
-        c.vid[0] = E[2 * p.x];
-        c.vid[1] = E[2 * p.x + 1];
-        c.vid[2] = E[2 * p.y];
-        c.vid[3] = E[2 * p.y + 1];
-        c.w = cv.ee_w[i];
-        c.eps = cv.ee_eps[i];
-        c.dtype = cv.ee_dt[i];
-        return;
-    }
-    i -= cv.nee;
-    const int2 p = cv.fv[i];
-    c.type = CT_FV;
-    c.n = 4;
-    c.vid[0] = p.y;
-    c.vid[1] = F[3 * p.x];
-    c.vid[2] = F[3 * p.x + 1];
-    c.vid[3] = F[3 * p.x + 2];
-    c.w = cv.fv_w[i];
-}
-
-// ---- barrier functions (barrier.cpp:11-154, barrier.hpp:82-340) ----
-// kind: 0 ClampedLogBarrier, 1 NormalizedBarrier<ClampedLogBarrier>,
-// 2 ClampedLogSqBarrier, 3 CubicBarrier, 4 TwoStageBarrier; D = derivative
-// order.  One template serves the FP64 path and the FP32 (mixed) path.
-__device__ __forceinline__ double blog(double x) { return log(x); }
-__device__ __forceinline__ float blog(float x) { return logf(x); }
-__device__ __forceinline__ double binf(double) { return __longlong_as_double(0x7ff0000000000000ULL); }
-__device__ __forceinline__ float binf(float) { return __int_as_float(0x7f800000); }
-
-template <int D, class T> __device__ __forceinline__ T clamped_log(T d, T dh)
-{
-    if (D == 0) {
-        if (d <= T(0)) return binf(d);
-        if (d >= dh) return T(0);
-        const T dm = d - dh;
-        return -dm * dm * blog(d / dh);
-    }
-    if (d <= T(0) || d >= dh) return T(0);
-    if (D == 1) return (dh - d) * (T(2) * blog(d / dh) - dh / d + T(1));
-    const T r = dh / d;
-    return (r + T(2)) * r - T(2) * blog(d / dh) - T(3);
-}
-template <int D, class T> __device__ __forceinline__ T clamped_log_sq(T d, T dh)
-{
-    if (D == 0) {
-        if (d <= T(0)) return binf(d);
-        if (d >= dh) return T(0);
-        const T dm = d - dh, l = blog(d / dh);
-        return dm * dm * l * l;
-    }
-    if (d <= T(0) || d >= dh) return T(0);
-    if (D == 1) {
-        const T dm = d - dh, l = blog(d / dh);
-        return T(2) * dm * l * (l + dm / d);
-    }
-    const T t0 = dh - d, t1 = blog(d / dh), t2 = (t0 * t0) / (d * d);
-    return T(2) * ((t1 * t1) - (t1 - T(1)) * t2 - T(4) * t1 * t0 / d);
-}
-template <int D, class T> __device__ __forceinline__ T cubic(T d, T dh)
-{
-    if (!(d < dh)) return T(0);
-    const T dm = d - dh;
-    if (D == 0) return T(-2) / T(3) / dh * dm * dm * dm;
-    if (D == 1) return T(-2) / dh * dm * dm;
-    return T(4) * (T(1) - d / dh);
-}
-template <int D, class T> __device__ __forceinline__ T two_stage(T d, T dh)
-{
-    if (d >= dh) return T(0);
-    if (d >= T(0.5) * dh) return D == 0 ? T(0.5) * (dh - d) * (dh - d) : (D == 1 ? d - dh : T(1));
-    if (D == 0) return T(-0.25) * dh * dh * (blog(T(2) * d / dh) - T(0.5));
-    if (D == 1) return T(-0.25) * dh * dh / d;
-    return (T(0.25) * dh * dh) / (d * d);
-}
-// The other barriers are called out of line so that the default one adds
-// no registers to the local-Hessian kernels.
-template <int D, class T> __device__ __noinline__ T barrier_other(int kind, T d, T dh)
-{
-    switch (kind) {
-    case 1: {
-        // NormalizedBarrier: b(d / dh, 1) / dh^D
-        const T v = clamped_log<D, T>(d / dh, T(1));
-        return D == 0 ? v : (D == 1 ? v / dh : v / (dh * dh));
-    }
-    case 2: return clamped_log_sq<D, T>(d, dh);
-    case 3: return cubic<D, T>(d, dh);
-    case 4: return two_stage<D, T>(d, dh);
-    default: return clamped_log<D, T>(d, dh);
-    }
-}
-template <int D, class T> __device__ __forceinline__ T barrier_fn(int kind, T d, T dh)
-{
-    return kind == 0 ? clamped_log<D, T>(d, dh) : barrier_other<D, T>(kind, d, dh);
-}
-
-struct Params {
-    double kappa, dmin2, xhat, scale; // scale = physical factor (or 1)
-    int psd;
-    int mixed; // point-triangle contacts in FP32 (IPCG_BARRIER_FP32_PT)
-    int kind;  // barrier function (barrier_fn)
-};
-// Barrier::units(x̂) (barrier.hpp): x̂² for every barrier but the normalized
-// one, which is dimensionless (1).  The physical barrier scales by dhat / units.
-__host__ __device__ inline double barrier_units(int kind, double xhat) { return kind == 1 ? 1.0 : xhat * xhat; }
-
-// ---- FP32 point-triangle contacts (mixed precision) ----
-// The point-plane squared distance d = N^2/D (N = a.(u x v), D = |u x v|^2,
-// a = p - t0, u = t1 - t0, v = t2 - t0) and its derivatives, and the barrier
-// derivatives, in FP32.  The relative vectors are formed in FP64 first, so
-// FP32 only sees edge-sized numbers.  Used for triangles that are not
-// degenerate (sin^2 of the corner angle above 1e-6); FV contacts whose
-// triangles are, and every other contact type, stay FP64.
-struct F3 {
-    float x, y, z;
-};
-__device__ __forceinline__ F3 to_f3(V3 a) { return F3 { (float)a.x, (float)a.y, (float)a.z }; }
-__device__ __forceinline__ F3 f3_cross(F3 a, F3 b)
-{
-    return F3 { a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x };
-}
-__device__ __forceinline__ float f3_dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ float f3c(F3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
-__device__ __forceinline__ void f3_skew(F3 a, float M[3][3])
-{
-    M[0][0] = 0;
-    M[0][1] = -a.z;
-    M[0][2] = a.y;
-    M[1][0] = a.z;
-    M[1][1] = 0;
-    M[1][2] = -a.x;
-    M[2][0] = -a.y;
-    M[2][1] = a.x;
-    M[2][2] = 0;
-}
-
-// FP64 test of the triangle's corner angle at t0 (u = t1 - t0, v = t2 - t0).
-__device__ __forceinline__ bool fv_fp32_ok(const V3* x)
-{
-    const V3 u = x[2] - x[1], v = x[3] - x[1];
-    return sqnorm(cross(u, v)) > 1e-6 * sqnorm(u) * sqnorm(v);
-}
-
-// d, reduced gradient g (9, in r = (a, u, v)) and Hessian H (81 or null).
-__device__ float triple_quot_f(F3 a, F3 u, F3 v, float* g, float* H)
-{
-    const F3 w = f3_cross(u, v);
-    const float Nn = f3_dot(a, w);
-    const float D = f3_dot(w, w);
-    const float iD = 1.0f / D;
-    const F3 gNa = w, gNu = f3_cross(v, a), gNv = f3_cross(a, u);
-    const F3 cvw = f3_cross(v, w), cwu = f3_cross(w, u);
-    float gN[9], gD[9];
-    for (int i = 0; i < 3; ++i) {
-        gN[i] = f3c(gNa, i);
-        gN[3 + i] = f3c(gNu, i);
-        gN[6 + i] = f3c(gNv, i);
-        gD[i] = 0;
-        gD[3 + i] = 2.0f * f3c(cvw, i);
-        gD[6 + i] = 2.0f * f3c(cwu, i);
-    }
-    const float c1 = 2 * Nn * iD, c2 = Nn * Nn * iD * iD;
-    for (int i = 0; i < 9; ++i) g[i] = c1 * gN[i] - c2 * gD[i];
-    if (H) {
-        float Sv[3][3], Su[3][3], Sa[3][3], Sw[3][3];
-        f3_skew(v, Sv);
-        f3_skew(u, Su);
-        f3_skew(a, Sa);
-        f3_skew(w, Sw);
-        float HN[81], HD[81];
-        for (int i = 0; i < 81; ++i) {
-            HN[i] = 0;
-            HD[i] = 0;
-        }
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) {
-                HN[i * 9 + 3 + j] = HN[(3 + j) * 9 + i] = -Sv[i][j];
-                HN[i * 9 + 6 + j] = HN[(6 + j) * 9 + i] = Su[i][j];
-                HN[(3 + i) * 9 + 6 + j] = HN[(6 + j) * 9 + 3 + i] = -Sa[i][j];
-                float uu = 0, vv = 0, uv = 0;
-                for (int k = 0; k < 3; ++k) {
-                    uu += Sv[k][i] * Sv[k][j];
-                    vv += Su[k][i] * Su[k][j];
-                    uv -= Sv[k][i] * Su[k][j];
-                }
-                HD[(3 + i) * 9 + 3 + j] = 2 * uu;
-                HD[(6 + i) * 9 + 6 + j] = 2 * vv;
-                HD[(3 + i) * 9 + 6 + j] = HD[(6 + j) * 9 + 3 + i] = 2 * (uv - Sw[i][j]);
-            }
-        const float iD2 = iD * iD;
-        const float k1 = 2 * iD, k2 = 2 * Nn * iD, k3 = 2 * Nn * iD2, k4 = Nn * Nn * iD2, k5 = 2 * Nn * Nn * iD2 * iD;
-        for (int i = 0; i < 9; ++i)
-            for (int j = 0; j < 9; ++j)
-                H[i * 9 + j] = k1 * gN[i] * gN[j] + k2 * HN[i * 9 + j] - k3 * (gN[i] * gD[j] + gD[i] * gN[j])
-                    - k4 * HD[i * 9 + j] + k5 * gD[i] * gD[j];
-    }
-    return Nn * Nn * iD;
-}
-
-// FV contact in FP32: squared distance, stencil gradient (12) and Hessian
-// (144 or null) of d, as floats.
-__device__ float fv_local_f(const V3* x, float* g, float* H)
-{
-    // a = p - t0, u = t1 - t0, v = t2 - t0 (FP64 differences, then FP32)
-    const F3 a = to_f3(x[0] - x[1]), u = to_f3(x[2] - x[1]), v = to_f3(x[3] - x[1]);
-    float gr[9], Hr[81];
-    const float d = triple_quot_f(a, u, v, gr, H ? Hr : nullptr);
-    // expand to the stencil (p, t0, t1, t2): reduced vectors (0-1, 2-1, 3-1)
-    const int pos[3] = { 0, 2, 3 };
-    for (int i = 0; i < 12; ++i) g[i] = 0;
-    for (int k = 0; k < 3; ++k)
-        for (int c = 0; c < 3; ++c) {
-            g[3 * pos[k] + c] += gr[3 * k + c];
-            g[3 + c] -= gr[3 * k + c];
-        }
-    if (H) {
-        for (int i = 0; i < 144; ++i) H[i] = 0;
-        for (int k = 0; k < 3; ++k)
-            for (int l = 0; l < 3; ++l)
-                for (int c = 0; c < 3; ++c)
-                    for (int e = 0; e < 3; ++e) {
-                        const float h = Hr[(3 * k + c) * 9 + 3 * l + e];
-                        H[(3 * pos[k] + c) * 12 + 3 * pos[l] + e] += h;
-                        H[(3 * pos[k] + c) * 12 + 3 + e] -= h;
-                        H[(3 + c) * 12 + 3 * pos[l] + e] -= h;
-                        H[(3 + c) * 12 + 3 + e] += h;
-                    }
-    }
-    return d;
-}
-
-// ---- closed-form squared-distance derivatives ----
-__device__ __forceinline__ void skew(V3 a, double M[3][3])
-{
-    M[0][0] = 0;
-    M[0][1] = -a.z;
-    M[0][2] = a.y;
-    M[1][0] = a.z;
-    M[1][1] = 0;
-    M[1][2] = -a.x;
-    M[2][0] = -a.y;
-    M[2][1] = a.x;
-    M[2][2] = 0;
-}
-
-// Accumulate reduced derivatives into stencil coordinates: reduced vector k
-// is x[pos[k]] - x[neg[k]].
-template <int M>
-__device__ __forceinline__ void expand_g(int N, const int* pos, const int* neg, const double* gr, double* g)
-{
-    for (int i = 0; i < N; ++i) g[i] = 0;
-    for (int k = 0; k < M; ++k)
-        for (int c = 0; c < 3; ++c) {
-            g[3 * pos[k] + c] += gr[3 * k + c];
-            g[3 * neg[k] + c] -= gr[3 * k + c];
-        }
-}
-template <int M>
-__device__ __forceinline__ void expand_h(int N, const int* pos, const int* neg, const double* Hr, double* H)
-{
-    for (int i = 0; i < N * N; ++i) H[i] = 0;
-    for (int k = 0; k < M; ++k)
-        for (int l = 0; l < M; ++l)
-            for (int c = 0; c < 3; ++c)
-                for (int e = 0; e < 3; ++e) {
-                    const double h = Hr[(3 * k + c) * (3 * M) + 3 * l + e];
-                    H[(3 * pos[k] + c) * N + 3 * pos[l] + e] += h;
-                    H[(3 * pos[k] + c) * N + 3 * neg[l] + e] -= h;
-                    H[(3 * neg[k] + c) * N + 3 * pos[l] + e] -= h;
-                    H[(3 * neg[k] + c) * N + 3 * neg[l] + e] += h;
-                }
-}
-
-// d = N²/D, N = a·(u×v), D = |u×v|²; r = (a,u,v)
-__device__ void triple_quot(V3 a, V3 u, V3 v, double* g, double* H /*81 or null*/)
-{
-    const V3 w = cross(u, v);
-    const double Nn = dot(a, w);
-    const double D = sqnorm(w);
-    const double iD = 1.0 / D;
-    const V3 gNa = w, gNu = cross(v, a), gNv = cross(a, u);
-    const V3 gDu = cross(v, w) * 2.0, gDv = cross(w, u) * 2.0;
-    double gN[9], gD[9];
-    for (int i = 0; i < 3; ++i) {
-        gN[i] = comp(gNa, i);
-        gN[3 + i] = comp(gNu, i);
-        gN[6 + i] = comp(gNv, i);
-        gD[i] = 0;
-        gD[3 + i] = comp(gDu, i);
-        gD[6 + i] = comp(gDv, i);
-    }
-    const double c1 = 2 * Nn * iD, c2 = Nn * Nn * iD * iD;
-    for (int i = 0; i < 9; ++i) g[i] = c1 * gN[i] - c2 * gD[i];
-    if (!H) return;
-    double Sv[3][3], Su[3][3], Sa[3][3], Sw[3][3];
-    skew(v, Sv);
-    skew(u, Su);
-    skew(a, Sa);
-    skew(w, Sw);
-    double HN[81], HD[81];
-    for (int i = 0; i < 81; ++i) {
-        HN[i] = 0;
-        HD[i] = 0;
-    }
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            HN[i * 9 + 3 + j] = HN[(3 + j) * 9 + i] = -Sv[i][j];
-            HN[i * 9 + 6 + j] = HN[(6 + j) * 9 + i] = Su[i][j];
-            HN[(3 + i) * 9 + 6 + j] = HN[(6 + j) * 9 + 3 + i] = -Sa[i][j];
-            double uu = 0, vv = 0, uv = 0;
-            for (int k = 0; k < 3; ++k) {
-                uu += Sv[k][i] * Sv[k][j];
-                vv += Su[k][i] * Su[k][j];
-                uv -= Sv[k][i] * Su[k][j];
-            }
-            HD[(3 + i) * 9 + 3 + j] = 2 * uu;
-            HD[(6 + i) * 9 + 6 + j] = 2 * vv;
-            HD[(3 + i) * 9 + 6 + j] = HD[(6 + j) * 9 + 3 + i] = 2 * (uv - Sw[i][j]);
-        }
-    const double iD2 = iD * iD;
-    const double k1 = 2 * iD, k2 = 2 * Nn * iD, k3 = 2 * Nn * iD2, k4 = Nn * Nn * iD2, k5 = 2 * Nn * Nn * iD2 * iD;
-    for (int i = 0; i < 9; ++i)
-        for (int j = 0; j < 9; ++j)
-            H[i * 9 + j] = k1 * gN[i] * gN[j] + k2 * HN[i * 9 + j] - k3 * (gN[i] * gD[j] + gD[i] * gN[j])
-                - k4 * HD[i * 9 + j] + k5 * gD[i] * gD[j];
-}
-
-// D = |u×v|² in r = (u,v)
-__device__ void cross_sq(V3 u, V3 v, double* g, double* H /*36 or null*/)
-{
-    const V3 w = cross(u, v);
-    const V3 gu = cross(v, w) * 2.0, gv = cross(w, u) * 2.0;
-    for (int i = 0; i < 3; ++i) {
-        g[i] = comp(gu, i);
-        g[3 + i] = comp(gv, i);
-    }
-    if (!H) return;
-    double Sv[3][3], Su[3][3], Sw[3][3];
-    skew(v, Sv);
-    skew(u, Su);
-    skew(w, Sw);
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            double uu = 0, vv = 0, uv = 0;
-            for (int k = 0; k < 3; ++k) {
-                uu += Sv[k][i] * Sv[k][j];
-                vv += Su[k][i] * Su[k][j];
-                uv -= Sv[k][i] * Su[k][j];
-            }
-            H[i * 6 + j] = 2 * uu;
-            H[(3 + i) * 6 + 3 + j] = 2 * vv;
-            H[i * 6 + 3 + j] = H[(3 + j) * 6 + i] = 2 * (uv - Sw[i][j]);
-        }
-}
-
-// d = |a×b|²/|b−a|² in r = (a,b)
-__device__ void point_line_r(V3 a, V3 b, double* g, double* H /*36 or null*/)
-{
-    const V3 c = cross(a, b);
-    const double P = sqnorm(c);
-    const V3 e = b - a;
-    const double L = sqnorm(e);
-    const double iL = 1.0 / L;
-    double gP[6], gL[6];
-    const V3 gPa = cross(b, c) * 2.0, gPb = cross(c, a) * 2.0;
-    for (int i = 0; i < 3; ++i) {
-        gP[i] = comp(gPa, i);
-        gP[3 + i] = comp(gPb, i);
-        gL[i] = -2 * comp(e, i);
-        gL[3 + i] = 2 * comp(e, i);
-    }
-    const double iL2 = iL * iL;
-    for (int i = 0; i < 6; ++i) g[i] = gP[i] * iL - P * gL[i] * iL2;
-    if (!H) return;
-    double Sa[3][3], Sb[3][3], Sc[3][3];
-    skew(a, Sa);
-    skew(b, Sb);
-    skew(c, Sc);
-    // ∇²P = 2(JᵀJ + Σ c_k ∇²c_k) with J = [-[b]×, [a]×], ∂²c_k/∂a_i∂b_j = ε_kij
-    double HP[36];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            double aa = 0, bb = 0, ab = 0;
-            for (int k = 0; k < 3; ++k) {
-                aa += Sb[k][i] * Sb[k][j];
-                bb += Sa[k][i] * Sa[k][j];
-                ab -= Sb[k][i] * Sa[k][j];
-            }
-            HP[i * 6 + j] = 2 * aa;
-            HP[(3 + i) * 6 + 3 + j] = 2 * bb;
-            HP[i * 6 + 3 + j] = HP[(3 + j) * 6 + i] = 2 * (ab - Sc[i][j]);
-        }
-    // ∇²L = 2 [[I, -I], [-I, I]]
-    const double k5 = 2 * P * iL2 * iL;
-    for (int r = 0; r < 6; ++r)
-        for (int q = 0; q < 6; ++q) {
-            const double hl = (r % 3 == q % 3) ? ((r < 3) == (q < 3) ? 2.0 : -2.0) : 0.0;
-            H[r * 6 + q] = HP[r * 6 + q] * iL - (gP[r] * gL[q] + gL[r] * gP[q]) * iL2 - P * hl * iL2
-                + k5 * gL[r] * gL[q];
-        }
-}
-
-// stencil-local squared distance + derivatives (H may be null)
-__device__ double pp_local(const V3* x, int N, int i, int j, double* g, double* H)
-{
-    const V3 r = x[i] - x[j];
-    const double gr[3] = { 2 * r.x, 2 * r.y, 2 * r.z };
-    const int pos[1] = { i }, neg[1] = { j };
-    expand_g<1>(N, pos, neg, gr, g);
-    if (H) {
-        const double Hr[9] = { 2, 0, 0, 0, 2, 0, 0, 0, 2 };
-        expand_h<1>(N, pos, neg, Hr, H);
-    }
-    return point_point_distance(x[i], x[j]);
-}
-__device__ double pl_local(const V3* x, int N, int p, int e0, int e1, double* g, double* H)
-{
-    double gr[6], Hr[36];
-    point_line_r(x[e0] - x[p], x[e1] - x[p], gr, H ? Hr : nullptr);
-    const int pos[2] = { e0, e1 }, neg[2] = { p, p };
-    expand_g<2>(N, pos, neg, gr, g);
-    if (H) expand_h<2>(N, pos, neg, Hr, H);
-    return point_line_distance(x[p], x[e0], x[e1]);
-}
-__device__ double pplane_local(const V3* x, double* g, double* H)
-{
-    double gr[9], Hr[81];
-    triple_quot(x[0] - x[1], x[2] - x[1], x[3] - x[1], gr, H ? Hr : nullptr);
-    const int pos[3] = { 0, 2, 3 }, neg[3] = { 1, 1, 1 };
-    expand_g<3>(12, pos, neg, gr, g);
-    if (H) expand_h<3>(12, pos, neg, Hr, H);
-    return point_plane_distance(x[0], x[1], x[2], x[3]);
-}
-__device__ double ll_local(const V3* x, double* g, double* H)
-{
-    double gr[9], Hr[81];
-    triple_quot(x[2] - x[0], x[1] - x[0], x[3] - x[2], gr, H ? Hr : nullptr);
-    const int pos[3] = { 2, 1, 3 }, neg[3] = { 0, 0, 2 };
-    expand_g<3>(12, pos, neg, gr, g);
-    if (H) expand_h<3>(12, pos, neg, Hr, H);
-    return line_line_distance(x[0], x[1], x[2], x[3]);
-}
-__device__ double ee_local(const V3* x, int dtype, double* g, double* H)
-{
-    switch (dtype) {
-    case EA0_EB0: return pp_local(x, 12, 0, 2, g, H);
-    case EA0_EB1: return pp_local(x, 12, 0, 3, g, H);
-    case EA1_EB0: return pp_local(x, 12, 1, 2, g, H);
-    case EA1_EB1: return pp_local(x, 12, 1, 3, g, H);
-    case EA_EB0: return pl_local(x, 12, 2, 0, 1, g, H);
-    case EA_EB1: return pl_local(x, 12, 3, 0, 1, g, H);
-    case EA0_EB: return pl_local(x, 12, 0, 2, 3, g, H);
-    case EA1_EB: return pl_local(x, 12, 1, 2, 3, g, H);
-    default: return ll_local(x, g, H);
-    }
-}
-__device__ double contact_distance(const Local& c, const V3* x, double* g, double* H)
-{
-    switch (c.type) {
-    case CT_VV: return pp_local(x, 6, 0, 1, g, H);
-    case CT_EV: return pl_local(x, 9, 0, 1, 2, g, H);
-    case CT_EE: return ee_local(x, c.dtype, g, H);
-    default: return pplane_local(x, g, H);
-    }
-}
-
-// EE mollifier m(x) (edge_edge_mollifier.cpp:42-136); gm/Hm filled iff active
-__device__ double mollifier(const Local& c, const V3* x, double* gm, double* Hm, bool& active)
-{
-    active = false;
-    if (c.type != CT_EE) return 1.0;
-    const double s = ee_cross_sqnorm(x[0], x[1], x[2], x[3]);
-    if (!(s < c.eps)) return 1.0;
-    active = true;
-    const double xe = s / c.eps;
-    const double m = (-xe + 2) * xe;
-    if (!gm) return m;
-    const double inv = 1 / c.eps;
-    const double m1 = 2 * inv * fma(-inv, s, 1.0);
-    double gr[6], Hr[36];
-    cross_sq(x[1] - x[0], x[3] - x[2], gr, Hm ? Hr : nullptr);
-    const int pos[2] = { 1, 3 }, neg[2] = { 0, 2 };
-    double gs[12];
-    expand_g<2>(12, pos, neg, gr, gs);
-    for (int i = 0; i < 12; ++i) gm[i] = m1 * gs[i];
-    if (Hm) {
-        const double m2 = -2 / (c.eps * c.eps);
-        expand_h<2>(12, pos, neg, Hr, Hm);
-        for (int i = 0; i < 12; ++i)
-            for (int j = 0; j < 12; ++j) Hm[i * 12 + j] = m1 * Hm[i * 12 + j] + m2 * gs[i] * gs[j];
-    }
-    return m;
-}
-
-// ---- PSD projection (eigen_ext.tpp:64-108) -------------------------------
-// The local Hessian annihilates rigid translations (per coordinate its rows
-// sum to zero over the stencil's vertices), so it is projected in the
-// 3(n-1)-dimensional translation-free subspace spanned by orthonormal vertex
-// contrasts: M = C H C^T (at most 9 x 9), and H+ = H - f sum_{lam<0} lam w w^T
-// with w = C^T q over the negative eigenpairs (lam, q) of M (f = 1 to clamp,
-// 2 for the absolute value).  M = Q_h T Q_h^T (Householder), T = G D G^T
-// (implicit QL with Wilkinson shifts, G = G_1 ... G_R plane rotations).
-// Only the negative eigenvectors are formed: q_i = Q_h G_1 ... G_R e_i,
-// replaying the recorded rotations on e_i, which costs a few hundred flops
-// per vector instead of updating all of Q at every rotation.
-constexpr int MAXR = 9;
-constexpr int MAXROT = 128; // recorded rotations; beyond, Q is accumulated
-
-__device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* d, double* Q, double* rc, double* rs,
-    int8_t* rk, int& nrot, double* htau)
-{
-    // Householder tridiagonalisation; reflector k is I - htau[k] v v^T with
-    // v[k+1..n) kept in A[k+1..n)[k], the column it annihilates (the updates
-    // below touch only rows and columns past k)
-    double e[MAXR];
-    for (int k = 0; k + 2 < n; ++k) {
-        double sig = 0;
-        for (int i = k + 2; i < n; ++i) sig += A[i * MAXR + k] * A[i * MAXR + k];
-        const double x0 = A[(k + 1) * MAXR + k];
-        htau[k] = 0;
-        if (sig == 0) {
-            e[k] = x0;
-            continue;
-        }
-        const double nx = sqrt(x0 * x0 + sig);
-        const double alpha = (x0 >= 0) ? -nx : nx;
-        const double v0 = x0 - alpha;
-        A[(k + 1) * MAXR + k] = v0;
-        double p[MAXR];
-        const double tau = 2.0 / (v0 * v0 + sig);
-        double K = 0;
-        for (int i = k + 1; i < n; ++i) {
-            double s = 0;
-            for (int j = k + 1; j < n; ++j) s += A[i * MAXR + j] * A[j * MAXR + k];
-            p[i] = tau * s;
-            K += p[i] * A[i * MAXR + k];
-        }
-        K *= 0.5 * tau;
-        for (int i = k + 1; i < n; ++i) p[i] -= K * A[i * MAXR + k];
-        // the update is symmetric: form the upper triangle, mirror it
-        for (int i = k + 1; i < n; ++i)
-            for (int j = i; j < n; ++j) {
-                const double a = A[i * MAXR + j] - (A[i * MAXR + k] * p[j] + p[i] * A[j * MAXR + k]);
-                A[i * MAXR + j] = a;
-                A[j * MAXR + i] = a;
-            }
-        e[k] = alpha;
-        htau[k] = tau;
-    }
-    if (n >= 2) e[n - 2] = A[(n - 1) * MAXR + n - 2];
-    e[n - 1] = 0;
-    for (int i = 0; i < n; ++i) d[i] = A[i * MAXR + i];
-    nrot = 0;
-    bool record = true; // false once MAXROT is exceeded: then Q holds G
-    const double eps = 2.220446049250313e-16;
-    int end = n - 1, iter = 0;
-    while (end > 0) {
-        for (int i = 0; i < end; ++i)
-            if (fabs(e[i]) <= eps * (fabs(d[i]) + fabs(d[i + 1])) || fabs(e[i]) <= 1e-300) e[i] = 0;
-        while (end > 0 && e[end - 1] == 0) --end;
-        if (end <= 0) break;
-        if (++iter > 40 * n) return false;
-        int start = end - 1;
-        while (start > 0 && e[start - 1] != 0) --start;
-        if (record && nrot + (end - start) > MAXROT) {
-            // too many rotations to record: form G from those so far and
-            // accumulate the rest into it
-            for (int i = 0; i < n; ++i)
-                for (int j = 0; j < n; ++j) Q[i * MAXR + j] = (i == j) ? 1.0 : 0.0;
-            for (int r = 0; r < nrot; ++r) {
-                const int k = rk[r];
-                const double c = rc[r], s = rs[r];
-                for (int q = 0; q < n; ++q) {
-                    const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
-                    Q[q * MAXR + k] = c * qa - s * qb;
-                    Q[q * MAXR + k + 1] = s * qa + c * qb;
-                }
-            }
-            record = false;
-            nrot = -1;
-        }
-        const double td = 0.5 * (d[end - 1] - d[end]);
-        const double b = e[end - 1];
-        double mu = d[end];
-        if (td == 0) mu -= fabs(b);
-        else {
-            const double h = hypot(td, b);
-            mu -= b * b / (td + (td > 0 ? h : -h));
-        }
-        double x = d[start] - mu, z = e[start];
-        for (int k = start; k < end; ++k) {
-            // (c, s) from one reciprocal square root: x and z are entries of
-            // a local Hessian, far from the range where x^2 + z^2 overflows
-            const double r2 = x * x + z * z;
-            double c = 1, s = 0;
-            if (r2 != 0) {
-                const double ir = rsqrt(r2);
-                c = x * ir;
-                s = -z * ir;
-            }
-            if (k > start) e[k - 1] = c * e[k - 1] - s * z;
-            const double dk = d[k], dk1 = d[k + 1], ek = e[k];
-            d[k] = c * c * dk - 2 * c * s * ek + s * s * dk1;
-            d[k + 1] = s * s * dk + 2 * c * s * ek + c * c * dk1;
-            e[k] = c * s * (dk - dk1) + (c * c - s * s) * ek;
-            if (k < end - 1) {
-                z = -s * e[k + 1];
-                e[k + 1] = c * e[k + 1];
-            }
-            x = e[k];
-            if (record) {
-                rc[nrot] = c;
-                rs[nrot] = s;
-                rk[nrot] = (int8_t)k;
-                ++nrot;
-            } else {
-                for (int q = 0; q < n; ++q) {
-                    const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
-                    Q[q * MAXR + k] = c * qa - s * qb;
-                    Q[q * MAXR + k + 1] = s * qa + c * qb;
-                }
-            }
-        }
-    }
-    return true;
-}
-
-// Eigenvectors idx[0..cnt) of M, rows of Y (stride MAXR): Q_h G e_i.  G e_i
-// comes from the recorded rotations, applied last first to all cnt vectors in
-// one pass (each rotation loaded once), or, if they were not recorded
-// (nrot < 0), from column i of Q; then the Householder reflectors kept in A's
-// lower columns, H_{n-3} first.
-__device__ void eigvecs(int n, const int* idx, int cnt, const double* Q, const double* rc, const double* rs,
-    const int8_t* rk, int nrot, const double* A, const double* htau, double* Y)
-{
-    for (int t = 0; t < cnt; ++t)
-        for (int q = 0; q < n; ++q)
-            Y[t * MAXR + q] = nrot >= 0 ? (q == idx[t] ? 1.0 : 0.0) : Q[q * MAXR + idx[t]];
-    for (int r = nrot - 1; r >= 0; --r) {
-        const int k = rk[r];
-        const double c = rc[r], s = rs[r];
-        for (int t = 0; t < cnt; ++t) {
-            double* y = Y + t * MAXR;
-            const double ya = y[k], yb = y[k + 1];
-            y[k] = c * ya + s * yb;
-            y[k + 1] = c * yb - s * ya;
-        }
-    }
-    for (int k = n - 3; k >= 0; --k) {
-        if (htau[k] == 0) continue;
-        for (int t = 0; t < cnt; ++t) {
-            double* y = Y + t * MAXR;
-            double s = 0;
-            for (int q = k + 1; q < n; ++q) s += A[q * MAXR + k] * y[q];
-            s *= htau[k];
-            for (int q = k + 1; q < n; ++q) y[q] -= s * A[q * MAXR + k];
-        }
-    }
-}
-
-// Orthonormal contrasts (rows orthogonal to (1,..,1)) for NS = 2, 3, 4
-// stencil vertices: C[k][a], k < NS - 1 (compile-time constants).
-template <int NS> __device__ __forceinline__ constexpr double contrast(int k, int a)
-{
-    return NS == 4 ? 0.5 * ((k == 0 ? (a & 1) : k == 1 ? (a >> 1) : ((a ^ (a >> 1)) & 1)) ? -1.0 : 1.0)
-        : NS == 3 ? (k == 0 ? (a == 0 ? 0.70710678118654752440 : a == 1 ? -0.70710678118654752440 : 0.0)
-                            : (a == 2 ? -0.81649658092772603273 : 0.40824829046386301637))
-                  : (a == 0 ? 0.70710678118654752440 : -0.70710678118654752440);
-}
-
-// w = C^T q (length 3 NS) for a length-3(NS-1) vector q.
-template <int NS> __device__ __forceinline__ void from_contrasts(const double* q, double* w)
-{
-#pragma unroll
-    for (int a = 0; a < NS; ++a)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            double s = 0;
-#pragma unroll
-            for (int k = 0; k < NS - 1; ++k) s += contrast<NS>(k, a) * q[3 * k + c];
-            w[3 * a + c] = s;
-        }
-}
-
-__device__ __forceinline__ double fval(const Params& P, double d2)
-{
-    return P.kappa * (barrier_fn<0, double>(P.kind, d2 - P.dmin2, P.xhat) * P.scale);
-}
-__device__ __forceinline__ double fd1(const Params& P, double d2)
-{
-    return P.kappa * (barrier_fn<1, double>(P.kind, d2 - P.dmin2, P.xhat) * P.scale);
-}
-__device__ __forceinline__ double fd2(const Params& P, double d2)
-{
-    return P.kappa * (barrier_fn<2, double>(P.kind, d2 - P.dmin2, P.xhat) * P.scale);
-}
-__device__ __forceinline__ float fvalf(const Params& P, float d2)
-{
-    return (float)P.kappa * (barrier_fn<0, float>(P.kind, d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
-}
-__device__ __forceinline__ float fd1f(const Params& P, float d2)
-{
-    return (float)P.kappa * (barrier_fn<1, float>(P.kind, d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
-}
-__device__ __forceinline__ float fd2f(const Params& P, float d2)
-{
-    return (float)P.kappa * (barrier_fn<2, float>(P.kind, d2 - (float)P.dmin2, (float)P.xhat) * (float)P.scale);
-}
-// Whether contact c is evaluated in FP32 (mixed precision, FV, triangle not
-// degenerate).
-__device__ __forceinline__ bool fp32_contact(const Params& P, const Local& c, const V3* x)
-{
-    return P.mixed && c.type == CT_FV && fv_fp32_ok(x);
-}
-
-__device__ __forceinline__ void gather(const double* __restrict__ V, const Local& c, V3* x)
-{
-    for (int i = 0; i < c.n; ++i) x[i] = load_v3(V, c.vid[i]);
-}
 
 // ---- kernels ----
 __global__ void __launch_bounds__(BLOCK) k_energy(ContactsView cv, const int* __restrict__ E,
@@ -1065,48 +305,6 @@ __global__ void __launch_bounds__(BLOCK) k_gn_quadratic_form(ContactsView cv, co
     if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-// Self-check of the Hessian path: an index outside its buffer is recorded
-// (first one wins) and the access is skipped.
-struct Guard {
-    long long* rec; // [code, index, limit, contact]
-};
-__device__ __forceinline__ bool in_range(const Guard& gd, int code, long long idx, long long limit, long long who)
-{
-    if (idx >= 0 && idx < limit) return true;
-    if (atomicCAS((unsigned long long*)gd.rec, 0ull, (unsigned long long)code) == 0ull) {
-        gd.rec[1] = idx;
-        gd.rec[2] = limit;
-        gd.rec[3] = who;
-    }
-    return false;
-}
-
-__device__ __forceinline__ int lower_bound_u64(const unsigned long long* __restrict__ a, int lo, int hi,
-    unsigned long long key)
-{
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (a[mid] < key) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-// Local-Hessian scratch, element-major: element k (row-major within the
-// 3n x 3n matrix) of contact i is at p[k * stride + i].  A warp's 32
-// consecutive contacts then read and write 256 contiguous bytes per element
-// instead of 32 addresses 1,152 bytes apart.
-struct Slab {
-    double* p;
-    int64_t stride;
-    __device__ __forceinline__ double& at(int64_t i, int k) const { return p[(int64_t)k * stride + i]; }
-};
-
-// Launch width of the local Hessian and PSD kernels: one warp per block.
-// Their per-contact work is long and even, and a type's contacts can be few
-// (5,465 FV contacts fill only 43 blocks of 128 threads on 152 SMs), so small
-// blocks spread them over all SMs without a ragged last wave.
-constexpr int LH_BLOCK = 32;
 
 // Local Hessian of one contact (normal_potential.cpp:174-232 before the PSD
 // projection) written to its 144-double slab of Hs (row-major, N = 3n).
@@ -1131,7 +329,7 @@ __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, con
     constexpr int N = 3 * NS;
     if (TYPE == CT_FV && fp32_contact(P, c, x)) {
         float gf[12], Hf[144];
-        const float d = fv_local_f(x, gf, Hf);
+        const double d = fv_local_f(x, gf, Hf);
         const float w = (float)c.w, a = w * fd2f(P, d), b = w * fd1f(P, d);
         for (int r = 0; r < 12; ++r)
             for (int q = r; q < 12; ++q) {
@@ -1203,122 +401,6 @@ __global__ void __launch_bounds__(LH_BLOCK) k_local_hessian(ContactsView cv, con
     proj[i] = pr;
 }
 
-__device__ __forceinline__ int stencil_size(const ContactsView& cv, int64_t i)
-{
-    return i < cv.nvv ? 2 : (i < cv.nvv + cv.nev ? 3 : 4);
-}
-
-// PSD projection (eigen_ext.tpp:64-108) of every local Hessian, in place.
-constexpr int PSD_BLOCK = LH_BLOCK;
-
-// The NS - 1 contrasts sum_a C[k][a] v[a] of one value per stencil vertex.
-// NS = 4: C is the Hadamard matrix's rows without the all-ones one, times
-// 1/2; the butterflies here leave out that 1/2 (applied once by the caller).
-// NS = 3, 2: scaled in place.
-template <int NS> __device__ __forceinline__ void contrast_apply(const double* v, double* o)
-{
-    constexpr double R2 = 0.70710678118654752440, R6 = 0.40824829046386301637;
-    if (NS == 4) {
-        const double s01 = v[0] + v[1], d01 = v[0] - v[1], s23 = v[2] + v[3], d23 = v[2] - v[3];
-        o[0] = d01 + d23;
-        o[1] = s01 - s23;
-        o[2] = d01 - d23;
-    } else if (NS == 3) {
-        o[0] = (v[0] - v[1]) * R2;
-        o[1] = fma(-2.0, v[2], v[0] + v[1]) * R6;
-    } else {
-        o[0] = (v[0] - v[1]) * R2;
-    }
-}
-
-// M = C H C^T (rows of M with stride MAXR) straight from contact i's slab:
-// for each coordinate c, T = C H restricted to the rows of coordinate c (each
-// slab element loaded once, coalesced across the warp's contacts), then row
-// 3k+c of M from T's row k.
-template <int NS> __device__ void to_contrasts_slab(const Slab& hs, int64_t i, double* M)
-{
-    constexpr int N = 3 * NS, K = NS - 1;
-    constexpr double S = NS == 4 ? 0.25 : 1.0; // the two butterfly stages' missing (1/2)^2
-#pragma unroll 1
-    for (int c = 0; c < 3; ++c) {
-        double T[K][N];
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-            double v[NS], o[K];
-#pragma unroll
-            for (int a = 0; a < NS; ++a) v[a] = hs.at(i, (3 * a + c) * N + j);
-            contrast_apply<NS>(v, o);
-#pragma unroll
-            for (int k = 0; k < K; ++k) T[k][j] = o[k];
-        }
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-#pragma unroll
-            for (int e = 0; e < 3; ++e) {
-                double v[NS], o[K];
-#pragma unroll
-                for (int b = 0; b < NS; ++b) v[b] = T[k][3 * b + e];
-                contrast_apply<NS>(v, o);
-#pragma unroll
-                for (int l = 0; l < K; ++l) M[(3 * k + c) * MAXR + 3 * l + e] = NS == 4 ? S * o[l] : o[l];
-            }
-    }
-}
-
-// PSD projection of contact i's slab in place: M from the slab, the negative
-// eigenvectors kept, then one read-modify-write pass over the slab applying
-// H -= f lam w w^T for each of them in eigenvalue order.  Returns false if
-// the eigensolver did not converge.
-__device__ bool project_psd_slab(int n, const Slab& hs, int64_t i, int method)
-{
-    const int N = 3 * n, m = 3 * (n - 1);
-    double M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
-    if (n == 4) to_contrasts_slab<4>(hs, i, M);
-    else if (n == 3) to_contrasts_slab<3>(hs, i, M);
-    else to_contrasts_slab<2>(hs, i, M);
-    for (int r = 0; r < m; ++r)
-        for (int s = r + 1; s < m; ++s) {
-            const double avg = 0.5 * (M[r * MAXR + s] + M[s * MAXR + r]);
-            M[r * MAXR + s] = M[s * MAXR + r] = avg;
-        }
-    double rc[MAXROT], rs[MAXROT], htau[MAXR];
-    int8_t rk[MAXROT];
-    int nrot;
-    if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, htau)) return false;
-    const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
-    int idx[MAXR];
-    int nneg = 0;
-    for (int k = 0; k < m; ++k)
-        if (lam[k] < 0) idx[nneg++] = k;
-    if (nneg == 0) return true; // already PSD: returned as is
-    // the eigenvectors (rows of 9) and then the w = C^T q (rows of 12) share
-    // wv: row t of w is written after rows t.. of q are read (t descending),
-    // and rows below t lie below 12 t
-    double wv[MAXR * 12], sl[MAXR];
-    eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, wv);
-    for (int t = nneg - 1; t >= 0; --t) {
-        double q[MAXR];
-        for (int j = 0; j < m; ++j) q[j] = wv[t * MAXR + j];
-        double* w = wv + 12 * t;
-        if (n == 4) from_contrasts<4>(q, w);
-        else if (n == 3) from_contrasts<3>(q, w);
-        else from_contrasts<2>(q, w);
-        sl[t] = f * lam[idx[t]];
-    }
-    // H+ is symmetric: the upper triangle is formed and mirrored
-#pragma unroll 1
-    for (int r = 0; r < N; ++r) {
-        double swr[MAXR];
-        for (int t = 0; t < nneg; ++t) swr[t] = sl[t] * wv[12 * t + r];
-        for (int c = r; c < N; ++c) {
-            double v = hs.at(i, r * N + c);
-            for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
-            hs.at(i, r * N + c) = v;
-            if (c != r) hs.at(i, c * N + r) = v;
-        }
-    }
-    return true;
-}
 
 // Contacts [first, first + count) of the chunk.
 __global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, Slab hs,
@@ -1328,7 +410,7 @@ __global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, Slab hs,
     if (t >= count) return;
     const int64_t i = first + t;
     if (!proj[i]) return;
-    if (!project_psd_slab(stencil_size(cv, i), hs, i, method)) atomicOr(fail, 1);
+    if (!project_psd(stencil_size(cv, i), SlabAcc { hs, i }, method)) atomicOr(fail, 1);
 }
 
 // Contribution id j (position in the block-key list) -> contact, local
