@@ -46,6 +46,16 @@ extern "C" {
  * about 1e-6 relative. */
 #define IPCG_BARRIER_PHYSICAL 1
 #define IPCG_BARRIER_FP32_PT 2
+/* Bit 2 (no counterpart in the reference) widens the mixed precision to
+ * every contact but near-parallel (mollified) edge-edge ones and face-vertex
+ * ones on degenerate triangles: the point-point, point-line, point-plane and
+ * line-line distance gradients and Hessians and the barrier derivatives of
+ * the energy + gradient + Hessian pass run in FP32, with the squared distance
+ * and the cancellation-prone scalars (the point-plane / line-line numerator
+ * a.(u x v), the point-line cross product) from FP64.  The PSD
+ * eigen-projection, the mollifier, assembly and CCD stay FP64.  Results agree
+ * with FP64 to about 1e-6 relative. */
+#define IPCG_BARRIER_FP32_LOCAL 4
 
 /* Bits 4-7 of the same argument select the barrier function
  * (src/ipc/barrier/barrier.hpp; BarrierPotential(barrier, dhat, stiffness,
@@ -262,6 +272,25 @@ int ipcg_barrier_batch(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
                        int use_physical_barrier, int psd_method,
                        double* energies, double* gradient, ipcg_csr** hessian);
 
+/* Every call above that asks for a Hessian evaluates energy, gradient and
+ * Hessian in one pass over a sparsity pattern cached with the collision set
+ * (the reference's SparseMatrixCache, matrix_cache.cpp:80-214, does the same
+ * between Newton iterations): the pattern is built at the first such call
+ * after each build or load of the set, and each later call replays one
+ * captured CUDA graph (no host synchronisation inside it).  The fused
+ * kernel's launch shape is per device: ipcg_barrier_autotune times candidate
+ * shapes (threads per block 32/64/128, resident blocks per SM, 32-contact
+ * tiles taken per work-queue grab) on this set's largest chunk and keeps the
+ * fastest; the report is JSON ({"candidates": [...], "chosen": {...}}) in
+ * report (truncated to report_len; *needed gets the full length with the
+ * terminator; both may be NULL).  No counterpart in the reference. */
+int ipcg_barrier_autotune(const ipcg_collisions* collisions, const ipcg_mesh* mesh, const double* vertices,
+                          const double* dhat, const double* stiffness, int use_physical_barrier, int psd_method,
+                          char* report, int64_t report_len, int64_t* needed);
+/* The fused kernel's launch shape on the current device (get / set). */
+int ipcg_barrier_tuning(int* threads, int* blocks_per_sm, int* tiles_per_grab);
+int ipcg_barrier_set_tuning(int threads, int blocks_per_sm, int tiles_per_grab);
+
 /* NormalPotential::shape_derivative(collisions, mesh, V)
  * (normal_potential.cpp:85-123, 310-416): the derivative of the gradient with
  * respect to the rest positions, ndof x ndof (rows: displacement dofs,
@@ -366,6 +395,26 @@ int ipcg_collision_free_stepsize_batch(const ipcg_mesh* mesh,
  * set is empty. */
 int ipcg_collisions_minimum_distance(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
                                      const double* vertices, double* out);
+
+/* Replaces initial_barrier_stiffness(bbox_diagonal, barrier, dhat,
+ * average_mass, grad_energy, grad_barrier, max_barrier_stiffness,
+ * min_barrier_stiffness_scale, dmin) (barrier/adaptive_stiffness.cpp:12-48):
+ * barrier_kind is an IPCG_BARRIER_* kind (0 ClampedLogBarrier); grad_energy
+ * and grad_barrier are n doubles (host or device; both in the same memory).
+ * *kappa receives the clamped stiffness, *max_barrier_stiffness 100 times the
+ * minimum. */
+int ipcg_initial_barrier_stiffness(double bbox_diagonal, int barrier_kind, double dhat, double average_mass,
+                                   const double* grad_energy, const double* grad_barrier, int64_t n,
+                                   double min_barrier_stiffness_scale, double dmin, double* kappa,
+                                   double* max_barrier_stiffness);
+/* Replaces update_barrier_stiffness(prev_min_distance, min_distance,
+ * max_barrier_stiffness, barrier_stiffness, bbox_diagonal,
+ * dhat_epsilon_scale, dmin) (barrier/adaptive_stiffness.cpp:51-68): the
+ * stiffness doubles (up to the maximum) while the minimum (squared) distance
+ * keeps shrinking below (dhat_epsilon_scale (bbox_diagonal + dmin))^2. */
+int ipcg_update_barrier_stiffness(double prev_min_distance, double min_distance, double max_barrier_stiffness,
+                                  double barrier_stiffness, double bbox_diagonal, double dhat_epsilon_scale,
+                                  double dmin, double* out);
 
 /* Replaces is_step_collision_free(mesh, V0, V1, min_distance, nullptr,
  * TightInclusionCCD(tolerance, max_iterations, conservative_rescaling))

@@ -6,6 +6,7 @@
 // computation: without a CUDA device every compute call fails with
 // IPCG_ERR_NO_DEVICE.
 #include <atomic>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -99,6 +100,7 @@ void drain()
 
 bool enabled() { return g_enabled.load(std::memory_order_relaxed); }
 void count() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void count_graph(int kernels) { g_launches.fetch_add(kernels, std::memory_order_relaxed); }
 void make_events(cudaEvent_t* a, cudaEvent_t* b)
 {
     std::lock_guard<std::mutex> lk(g_mu);
@@ -357,8 +359,10 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
             for (uint8_t u : used) n_codim_v += !u;
             for (uint8_t u : in_face) n_codim_e += !u;
         }
+        static std::atomic<uint64_t> serials { 0 };
         auto* m = new ipcg_mesh();
         try {
+            m->serial = ++serials;
             m->n_codim_vertices = n_codim_v;
             m->n_codim_edges = n_codim_e;
             IPCG_CUDA(cudaGetDevice(&m->device));
@@ -624,6 +628,7 @@ int ipcg_collisions_set(ipcg_collisions* c, double dmin, int64_t nvv, const int3
         upload(c->fv, (const int2*)fv, nfv, s);
         upload(c->fv_w, fv_w, nfv, s);
         IPCG_CUDA(cudaStreamSynchronize(s));
+        ++c->version;
         c->nvv = nvv;
         c->nev = nev;
         c->nee = nee;
@@ -640,11 +645,15 @@ int ipcg_collisions_set(ipcg_collisions* c, double dmin, int64_t nvv, const int3
 static void barrier_options(int bits, BarrierArgs& a)
 {
     const int kind = (bits >> 4) & 15;
-    require(bits >= 0 && (bits & ~(IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT | IPCG_BARRIER_FUNCTION(15))) == 0
+    require(bits >= 0
+            && (bits & ~(IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT | IPCG_BARRIER_FP32_LOCAL
+                           | IPCG_BARRIER_FUNCTION(15)))
+                == 0
             && kind <= IPCG_BARRIER_TWO_STAGE,
         "unknown barrier option bits");
     a.physical = (bits & IPCG_BARRIER_PHYSICAL) ? 1 : 0;
     a.mixed = (bits & IPCG_BARRIER_FP32_PT) ? 1 : 0;
+    a.fp32_local = (bits & IPCG_BARRIER_FP32_LOCAL) ? 1 : 0;
     a.kind = kind;
 }
 
@@ -679,7 +688,7 @@ static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const d
         ipcg_csr* H = nullptr;
         if (hessian) H = new ipcg_csr();
         try {
-            barrier_evaluate(c, m, dV, a, energy, gdev, H);
+            if (!(H && barrier_egh(c, m, dV, a, energy, gdev, H))) barrier_evaluate(c, m, dV, a, energy, gdev, H);
             if (gradient && gdev != gradient) {
                 IPCG_CUDA(cudaMemcpyAsync(gradient, gdev, sizeof(double) * 3 * m->nV, cudaMemcpyDeviceToHost,
                     m->stream));
@@ -733,6 +742,49 @@ int ipcg_barrier_batch(const ipcg_collisions* c, const ipcg_mesh* mesh, const do
     const double* stiffness, int physical, int psd, double* energies, double* gradient, ipcg_csr** hessian)
 {
     return barrier_call(c, mesh, V, dhat, stiffness, 1, physical, psd, energies, gradient, hessian);
+}
+
+int ipcg_barrier_autotune(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, const double* dhat,
+    const double* stiffness, int physical, int psd, char* report, int64_t report_len, int64_t* needed)
+{
+    return guarded([&] {
+        require(c && mesh && dhat && stiffness && (V || mesh->nV == 0), "NULL argument");
+        for (int64_t k = 0; k < mesh->n_scenes; ++k) require(dhat[k] > 0, "dhat must be positive");
+        require(psd >= IPCG_PSD_NONE && psd <= IPCG_PSD_ABS, "Invalid type of PSD projection!");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        const double* dV = stage_positions(m, V, m->V0);
+        BarrierArgs a { dhat[0], stiffness[0], c->dmin, 0, psd };
+        barrier_options(physical, a);
+        a.scene_dhat = dhat;
+        a.scene_kappa = stiffness;
+        const std::string rep = egh_autotune(c, m, dV, a);
+        if (needed) *needed = (int64_t)rep.size() + 1;
+        if (report && report_len > 0) {
+            const size_t k = std::min<size_t>(rep.size(), (size_t)report_len - 1);
+            memcpy(report, rep.data(), k);
+            report[k] = 0;
+        }
+    });
+}
+
+int ipcg_barrier_tuning(int* threads, int* blocks_per_sm, int* tiles_per_grab)
+{
+    return guarded([&] {
+        require_device();
+        const EghTuning t = egh_tuning();
+        if (threads) *threads = t.threads;
+        if (blocks_per_sm) *blocks_per_sm = t.blocks_per_sm;
+        if (tiles_per_grab) *tiles_per_grab = t.tiles_per_grab;
+    });
+}
+
+int ipcg_barrier_set_tuning(int threads, int blocks_per_sm, int tiles_per_grab)
+{
+    return guarded([&] {
+        require_device();
+        egh_set_tuning(EghTuning { threads, blocks_per_sm, tiles_per_grab });
+    });
 }
 
 // Gauss-Newton forms (normal_potential.cpp:15-83): the FP64 path serves
@@ -1080,12 +1132,12 @@ int ipcg_csr_get_int32(const ipcg_csr* h, int32_t* row_ptr, int32_t* col, double
         if (row_ptr) {
             PBuf<int32_t> tmp; // stream-ordered pool memory, freed after the copy
             tmp.reserve(h->rows + 1, s);
-            k_row_ptr_i32<<<(int)((h->rows + 1 + 255) / 256), 256, 0, s>>>(h->row_ptr.p, h->rows + 1, tmp.p);
+            k_row_ptr_i32<<<(int)((h->rows + 1 + 255) / 256), 256, 0, s>>>(h->rowp(), h->rows + 1, tmp.p);
             IPCG_CUDA(cudaGetLastError());
             copy_out(row_ptr, tmp.p, sizeof(int32_t) * (h->rows + 1), s);
             IPCG_CUDA(cudaStreamSynchronize(s));
         }
-        copy_out(col, h->col.p, sizeof(int32_t) * h->nnz, s);
+        copy_out(col, h->colp(), sizeof(int32_t) * h->nnz, s);
         copy_out(val, h->val.p, sizeof(double) * h->nnz, s);
         IPCG_CUDA(cudaStreamSynchronize(s));
     });
@@ -1096,8 +1148,8 @@ int ipcg_csr_get(const ipcg_csr* h, int64_t* row_ptr, int32_t* col, double* val)
     return guarded([&] {
         require(h != nullptr, "NULL argument");
         cudaStream_t s = 0;
-        copy_out(row_ptr, h->row_ptr.p, sizeof(int64_t) * (h->rows + 1), s);
-        copy_out(col, h->col.p, sizeof(int32_t) * h->nnz, s);
+        copy_out(row_ptr, h->rowp(), sizeof(int64_t) * (h->rows + 1), s);
+        copy_out(col, h->colp(), sizeof(int32_t) * h->nnz, s);
         copy_out(val, h->val.p, sizeof(double) * h->nnz, s);
         IPCG_CUDA(cudaStreamSynchronize(s));
     });
@@ -1146,6 +1198,58 @@ int ipcg_collisions_minimum_distance(const ipcg_collisions* c, const ipcg_mesh* 
         IPCG_CUDA(cudaSetDevice(m->device));
         const double* dV = stage_positions(m, V, m->V0);
         *out = collisions_min_distance(c, m, dV);
+    });
+}
+
+int ipcg_initial_barrier_stiffness(double bbox_diagonal, int kind, double dhat, double average_mass,
+    const double* grad_energy, const double* grad_barrier, int64_t n, double min_scale, double dmin, double* kappa,
+    double* max_kappa)
+{
+    return guarded([&] {
+        require(kappa && max_kappa && (n == 0 || (grad_energy && grad_barrier)), "NULL argument");
+        require(n >= 0, "negative size");
+        require(average_mass > 0 && min_scale > 0, "average_mass and min_barrier_stiffness_scale must be positive");
+        require(bbox_diagonal > 0, "bbox_diagonal must be positive");
+        require(dhat > 0 && dmin >= 0, "dhat must be positive and dmin non-negative");
+        require(kind >= IPCG_BARRIER_CLAMPED_LOG && kind <= IPCG_BARRIER_TWO_STAGE, "unknown barrier kind");
+        const double dhat2 = dhat * dhat, dmin2 = dmin * dmin;
+        double d0 = 1e-8 * bbox_diagonal + dmin;
+        d0 *= d0;
+        if (d0 - dmin2 >= 2 * dmin * dhat + dhat2) d0 = dmin * dhat + 0.5 * dhat2;
+        double kmin = 4 * d0 * barrier_derivative_host(kind, 2, d0 - dmin2, 2 * dmin * dhat + dhat2);
+        kmin = min_scale * average_mass / kmin;
+        require(std::isfinite(kmin), "minimum barrier stiffness is not finite");
+        const double kmax = 100 * kmin;
+        double ab = 0, bb = 0;
+        if (n > 0) {
+            const bool de = is_device_ptr(grad_energy), db = is_device_ptr(grad_barrier);
+            require(de == db, "grad_energy and grad_barrier must both be host or both be device memory");
+            if (de) {
+                dot_pair_device(grad_energy, grad_barrier, n, &ab, &bb);
+            } else {
+                for (int64_t i = 0; i < n; ++i) {
+                    ab += grad_barrier[i] * grad_energy[i];
+                    bb += grad_barrier[i] * grad_barrier[i];
+                }
+            }
+        }
+        double k = 1.0;
+        if (bb > 0) k = -ab / bb;
+        *kappa = std::min(std::max(k, kmin), kmax);
+        *max_kappa = kmax;
+    });
+}
+
+int ipcg_update_barrier_stiffness(double prev_min_distance, double min_distance, double max_kappa, double kappa,
+    double bbox_diagonal, double dhat_epsilon_scale, double dmin, double* out)
+{
+    return guarded([&] {
+        require(out != nullptr, "NULL argument");
+        double eps = dhat_epsilon_scale * (bbox_diagonal + dmin);
+        eps *= eps;
+        *out = (prev_min_distance < eps && min_distance < eps && min_distance < prev_min_distance)
+            ? std::min(max_kappa, 2 * kappa)
+            : kappa;
     });
 }
 

@@ -1647,6 +1647,62 @@ void barrier_evaluate(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, 
         throw Error(IPCG_ERR_CUDA, "unable to project matrix onto positive semi-definite cone");
 }
 
+double barrier_derivative_host(int kind, int order, double x, double xhat)
+{
+    return order == 0 ? barrier_fn<0, double>(kind, x, xhat)
+                      : (order == 1 ? barrier_fn<1, double>(kind, x, xhat) : barrier_fn<2, double>(kind, x, xhat));
+}
+
+namespace {
+// a . b and b . b over n entries: per-block partial sums, then one thread
+// adds them in a fixed order (deterministic)
+__global__ void __launch_bounds__(BLOCK) k_dots(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+    double* __restrict__ partial)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double ab = 0, bb = 0;
+    for (int64_t j = i; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+        ab += a[j] * b[j];
+        bb += b[j] * b[j];
+    }
+    typedef cub::BlockReduce<double, BLOCK> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const double s1 = BR(tmp).Sum(ab);
+    __syncthreads();
+    const double s2 = BR(tmp).Sum(bb);
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = s1;
+        partial[2 * blockIdx.x + 1] = s2;
+    }
+}
+__global__ void k_dots_final(const double* __restrict__ partial, int nb, double* __restrict__ out)
+{
+    if (threadIdx.x != 0) return;
+    double s1 = 0, s2 = 0;
+    for (int i = 0; i < nb; ++i) {
+        s1 += partial[2 * i];
+        s2 += partial[2 * i + 1];
+    }
+    out[0] = s1;
+    out[1] = s2;
+}
+} // namespace
+
+void dot_pair_device(const double* a, const double* b, int64_t n, double* ab, double* bb)
+{
+    const int nb = (int)std::min<int64_t>(1024, std::max<int64_t>(1, grid_for(n, BLOCK)));
+    DBuf<double> part;
+    part.reserve(2 * nb + 2);
+    cudaStream_t s = 0;
+    IPCG_LAUNCH("k_dots", s, k_dots<<<nb, BLOCK, 0, s>>>(a, b, n, part.p));
+    IPCG_LAUNCH("k_dots_final", s, k_dots_final<<<1, 32, 0, s>>>(part.p, nb, part.p + 2 * nb));
+    double h[2];
+    IPCG_CUDA(cudaMemcpyAsync(h, part.p + 2 * nb, sizeof(h), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    *ab = h[0];
+    *bb = h[1];
+}
+
 double collisions_min_distance(const ipcg_collisions* cs, ipcg_mesh* m, const double* V)
 {
     const int64_t n = cs->size();

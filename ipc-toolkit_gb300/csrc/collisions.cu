@@ -556,6 +556,7 @@ void build_collision_set(ipcg_collisions* c, ipcg_mesh* m, const double* V, cons
     c->dmin = dmin[0];
     c->scene_dmin.assign(dmin, dmin + ns);
     c->sorted = true;
+    ++c->version;
     c->built_with_shape = c->enable_shape_derivatives;
     const int64_t nc = n_ee + n_fv;
     const bool improved = c->set_type == 1;

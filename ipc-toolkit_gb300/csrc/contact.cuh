@@ -963,6 +963,263 @@ template <class Acc> __device__ bool project_psd(int n, const Acc& hs, int metho
     }
     return true;
 }
+
+// ---- fused energy, gradient and local Hessian of one contact ----
+// (normal_potential.cpp:127-232 in one pass; the PSD projection follows.)
+
+// FP32 stencil expansions of reduced derivatives (reduced vector k is
+// x[pos[k]] - x[neg[k]]).
+template <int M> __device__ __forceinline__ void expand_g_f(int N, const int* pos, const int* neg, const float* gr,
+    float* g)
+{
+    for (int i = 0; i < N; ++i) g[i] = 0;
+    for (int k = 0; k < M; ++k)
+        for (int c = 0; c < 3; ++c) {
+            g[3 * pos[k] + c] += gr[3 * k + c];
+            g[3 * neg[k] + c] -= gr[3 * k + c];
+        }
+}
+template <int M> __device__ __forceinline__ void expand_h_f(int N, const int* pos, const int* neg, const float* Hr,
+    float* H)
+{
+    for (int i = 0; i < N * N; ++i) H[i] = 0;
+    for (int k = 0; k < M; ++k)
+        for (int l = 0; l < M; ++l)
+            for (int c = 0; c < 3; ++c)
+                for (int e = 0; e < 3; ++e) {
+                    const float h = Hr[(3 * k + c) * (3 * M) + 3 * l + e];
+                    H[(3 * pos[k] + c) * N + 3 * pos[l] + e] += h;
+                    H[(3 * pos[k] + c) * N + 3 * neg[l] + e] -= h;
+                    H[(3 * neg[k] + c) * N + 3 * pos[l] + e] -= h;
+                    H[(3 * neg[k] + c) * N + 3 * neg[l] + e] += h;
+                }
+}
+
+// FP32 point-line form d = |c|^2 / L in r = (a, b) (a = e0 - p, b = e1 - p),
+// with c = a x b and L = |b - a|^2 from FP64 (c is the small, cancellation-
+// prone quantity: |c| = d |b - a|).
+__device__ void point_line_f(F3 a, F3 b, F3 c, float P, float L, float* g /*6*/, float* H /*36*/)
+{
+    const F3 e { b.x - a.x, b.y - a.y, b.z - a.z };
+    const float iL = 1.0f / L, iL2 = iL * iL;
+    const F3 gPa = f3_cross(b, c), gPb = f3_cross(c, a);
+    float gP[6], gL[6];
+    for (int i = 0; i < 3; ++i) {
+        gP[i] = 2.0f * f3c(gPa, i);
+        gP[3 + i] = 2.0f * f3c(gPb, i);
+        gL[i] = -2.0f * f3c(e, i);
+        gL[3 + i] = 2.0f * f3c(e, i);
+    }
+    for (int i = 0; i < 6; ++i) g[i] = gP[i] * iL - P * gL[i] * iL2;
+    float Sa[3][3], Sb[3][3], Sc[3][3];
+    f3_skew(a, Sa);
+    f3_skew(b, Sb);
+    f3_skew(c, Sc);
+    float HP[36];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            float aa = 0, bb = 0, ab = 0;
+            for (int k = 0; k < 3; ++k) {
+                aa += Sb[k][i] * Sb[k][j];
+                bb += Sa[k][i] * Sa[k][j];
+                ab -= Sb[k][i] * Sa[k][j];
+            }
+            HP[i * 6 + j] = 2 * aa;
+            HP[(3 + i) * 6 + 3 + j] = 2 * bb;
+            HP[i * 6 + 3 + j] = HP[(3 + j) * 6 + i] = 2 * (ab - Sc[i][j]);
+        }
+    const float k5 = 2 * P * iL2 * iL;
+    for (int r = 0; r < 6; ++r)
+        for (int q = 0; q < 6; ++q) {
+            const float hl = (r % 3 == q % 3) ? ((r < 3) == (q < 3) ? 2.0f : -2.0f) : 0.0f;
+            H[r * 6 + q] = HP[r * 6 + q] * iL - (gP[r] * gL[q] + gL[r] * gP[q]) * iL2 - P * hl * iL2
+                + k5 * gL[r] * gL[q];
+        }
+}
+
+// FP32 stencil gradient and Hessian of the squared distance of each form;
+// each returns the squared distance itself in FP64 (the barrier's argument).
+__device__ double pp_f(const V3* x, int N, int i, int j, float* g, float* K)
+{
+    const F3 r = to_f3(x[i] - x[j]);
+    const float gr[3] = { 2 * r.x, 2 * r.y, 2 * r.z };
+    const int pos[1] = { i }, neg[1] = { j };
+    expand_g_f<1>(N, pos, neg, gr, g);
+    const float Hr[9] = { 2, 0, 0, 0, 2, 0, 0, 0, 2 };
+    expand_h_f<1>(N, pos, neg, Hr, K);
+    return point_point_distance(x[i], x[j]);
+}
+__device__ double pl_f(const V3* x, int N, int p, int e0, int e1, float* g, float* K)
+{
+    const V3 a = x[e0] - x[p], b = x[e1] - x[p];
+    const V3 c = cross(a, b);
+    float gr[6], Hr[36];
+    point_line_f(to_f3(a), to_f3(b), to_f3(c), (float)sqnorm(c), (float)sqnorm(b - a), gr, Hr);
+    const int pos[2] = { e0, e1 }, neg[2] = { p, p };
+    expand_g_f<2>(N, pos, neg, gr, g);
+    expand_h_f<2>(N, pos, neg, Hr, K);
+    return point_line_distance(x[p], x[e0], x[e1]);
+}
+// d = N^2 / D in r = (a, u, v) with a = x[pos[0]] - x[neg[0]], u = x[pos[1]] -
+// x[neg[1]], v = x[pos[2]] - x[neg[2]]: point-plane (p, t0, t1, t2) and
+// line-line forms.
+__device__ void triple_f(const V3* x, const int* pos, const int* neg, float* g, float* K)
+{
+    const V3 a = x[pos[0]] - x[neg[0]], u = x[pos[1]] - x[neg[1]], v = x[pos[2]] - x[neg[2]];
+    const V3 w = cross(u, v);
+    float gr[9], Hr[81];
+    triple_quot_f(to_f3(a), to_f3(u), to_f3(v), to_f3(w), (float)dot(a, w), (float)sqnorm(w), gr, Hr);
+    expand_g_f<3>(12, pos, neg, gr, g);
+    expand_h_f<3>(12, pos, neg, Hr, K);
+}
+__device__ double ee_f(const V3* x, int dtype, float* g, float* K)
+{
+    switch (dtype) {
+    case EA0_EB0: return pp_f(x, 12, 0, 2, g, K);
+    case EA0_EB1: return pp_f(x, 12, 0, 3, g, K);
+    case EA1_EB0: return pp_f(x, 12, 1, 2, g, K);
+    case EA1_EB1: return pp_f(x, 12, 1, 3, g, K);
+    case EA_EB0: return pl_f(x, 12, 2, 0, 1, g, K);
+    case EA_EB1: return pl_f(x, 12, 3, 0, 1, g, K);
+    case EA0_EB: return pl_f(x, 12, 0, 2, 3, g, K);
+    case EA1_EB: return pl_f(x, 12, 1, 2, 3, g, K);
+    default: {
+        const int pos[3] = { 2, 1, 3 }, neg[3] = { 0, 0, 2 };
+        triple_f(x, pos, neg, g, K);
+        return line_line_distance(x[0], x[1], x[2], x[3]);
+    }
+    }
+}
+__device__ double contact_distance_f(const Local& c, const V3* x, float* g, float* K)
+{
+    switch (c.type) {
+    case CT_VV: return pp_f(x, 6, 0, 1, g, K);
+    case CT_EV: return pl_f(x, 9, 0, 1, 2, g, K);
+    case CT_EE: return ee_f(x, c.dtype, g, K);
+    default: {
+        const int pos[3] = { 0, 2, 3 }, neg[3] = { 1, 1, 1 };
+        triple_f(x, pos, neg, g, K);
+        return point_plane_distance(x[0], x[1], x[2], x[3]);
+    }
+    }
+}
+
+// EE mollifier in reduced form: m, the stencil gradient gs of s = |ea x eb|^2
+// (gm = m1 gs), the reduced Hessian Hr (6 x 6, in (ea, eb)) of s, m1 and m2,
+// so that the mollifier Hessian's stencil entry (3a+c, 3b+e) is
+// m1 sg(a) sg(b) Hr[3 k(a) + c][3 k(b) + e] + m2 gs_r gs_q with k(a) = a / 2
+// and sg(a) = +1 for a = 1, 3, -1 for a = 0, 2 (the values of mollifier()'s
+// expanded matrix: each stencil entry is one reduced entry).
+struct MollifierR {
+    bool active;
+    double m, m1, m2;
+    double gs[12], Hr[36];
+};
+__device__ void mollifier_reduced(const Local& c, const V3* x, bool want_h, MollifierR& o)
+{
+    o.active = false;
+    o.m = 1.0;
+    if (c.type != CT_EE) return;
+    const double s = ee_cross_sqnorm(x[0], x[1], x[2], x[3]);
+    if (!(s < c.eps)) return;
+    o.active = true;
+    const double xe = s / c.eps;
+    o.m = (-xe + 2) * xe;
+    const double inv = 1 / c.eps;
+    o.m1 = 2 * inv * fma(-inv, s, 1.0);
+    o.m2 = -2 / (c.eps * c.eps);
+    double gr[6];
+    cross_sq(x[1] - x[0], x[3] - x[2], gr, want_h ? o.Hr : nullptr);
+    const int pos[2] = { 1, 3 }, neg[2] = { 0, 2 };
+    expand_g<2>(12, pos, neg, gr, o.gs);
+}
+__device__ __forceinline__ double mollifier_h(const MollifierR& o, int r, int q)
+{
+    const int a = r / 3, cc = r % 3, b = q / 3, e = q % 3;
+    const double sg = ((a & 1) ? 1.0 : -1.0) * ((b & 1) ? 1.0 : -1.0);
+    return o.m1 * (sg * o.Hr[(3 * (a >> 1) + cc) * 6 + 3 * (b >> 1) + e]) + o.m2 * o.gs[r] * o.gs[q];
+}
+
+// Whether contact c is evaluated in FP32: with IPCG_BARRIER_FP32_LOCAL every
+// contact but near-parallel (mollified) edge-edge ones and face-vertex ones
+// on degenerate triangles; with IPCG_BARRIER_FP32_PT only face-vertex ones on
+// non-degenerate triangles.
+__device__ __forceinline__ bool fp32_local_contact(const Params& P, const Local& c, const V3* x)
+{
+    if (c.type == CT_FV) return (P.mixed || P.fp32_local) && fv_fp32_ok(x);
+    if (!P.fp32_local) return false;
+    if (c.type == CT_EE) return !(ee_cross_sqnorm(x[0], x[1], x[2], x[3]) < c.eps);
+    return true;
+}
+
+// Energy e, stencil gradient g (3n) and local Hessian H (3n x 3n row-major,
+// both triangles written) of one contact.  Returns whether H is to be
+// projected: the mollified edge-edge case with m <= 0 is returned as is, as
+// the reference does (normal_potential.cpp:185-189).
+__device__ bool contact_egh(const Local& c, const V3* x, const Params& P, double& e, double* g, double* H)
+{
+    const int N = 3 * c.n;
+    if (fp32_local_contact(P, c, x)) {
+        float gf[12], Kf[144];
+        const double d = contact_distance_f(c, x, gf, Kf);
+        e = c.w * (double)fvalf(P, d);
+        const float wf = (float)c.w, a = wf * fd2f(P, d), b = wf * fd1f(P, d);
+        for (int k = 0; k < N; ++k) g[k] = (double)(b * gf[k]);
+        for (int r = 0; r < N; ++r)
+            for (int q = r; q < N; ++q) {
+                const double v = (double)(a * gf[r] * gf[q] + b * Kf[r * N + q]);
+                H[r * N + q] = v;
+                H[q * N + r] = v;
+            }
+        return true;
+    }
+    double gd[12];
+    const double d = contact_distance(c, x, gd, H); // H: the distance Hessian, overwritten below
+    const double fv = fval(P, d), fd = fd1(P, d), fdd = fd2(P, d);
+    if (c.type != CT_EE) {
+        e = c.w * 1.0 * fv;
+        for (int k = 0; k < N; ++k) g[k] = (c.w * fd) * gd[k];
+        for (int r = 0; r < N; ++r)
+            for (int q = r; q < N; ++q) {
+                const double v = (c.w * fdd) * gd[r] * gd[q] + (c.w * fd) * H[r * N + q];
+                H[r * N + q] = v;
+                H[q * N + r] = v;
+            }
+        return true;
+    }
+    MollifierR mo;
+    mollifier_reduced(c, x, true, mo);
+    const double m = mo.m;
+    e = c.w * m * fv;
+    if (m <= 0) {
+        for (int k = 0; k < 12; ++k) g[k] = 0;
+    } else {
+        for (int k = 0; k < 12; ++k)
+            g[k] = (c.w * fv) * (mo.active ? mo.m1 * mo.gs[k] : 0.0) + (c.w * m * fd) * gd[k];
+    }
+    if (mo.active && m <= 0) {
+        for (int r = 0; r < 12; ++r)
+            for (int q = r; q < 12; ++q) {
+                const double v = (c.w * fv) * mollifier_h(mo, r, q);
+                H[r * 12 + q] = v;
+                H[q * 12 + r] = v;
+            }
+        return false;
+    }
+    const double wm = c.w * m;
+    for (int r = 0; r < 12; ++r)
+        for (int q = r; q < 12; ++q) {
+            double v = (wm * fdd) * gd[r] * gd[q] + (wm * fd) * H[r * 12 + q];
+            if (mo.active) {
+                const double gfm_rq = (c.w * fd) * gd[r] * (mo.m1 * mo.gs[q]);
+                const double gfm_qr = (c.w * fd) * gd[q] * (mo.m1 * mo.gs[r]);
+                v = v + ((c.w * fv) * mollifier_h(mo, r, q) + gfm_rq + gfm_qr);
+            }
+            H[r * 12 + q] = v;
+            H[q * 12 + r] = v;
+        }
+    return true;
+}
 } // namespace
 
 } // namespace ipcg

@@ -1,0 +1,838 @@
+// egh.cu — barrier energy, gradient and PSD-projected Hessian in one pass,
+// with a cached sparsity pattern and the whole step replayed as a CUDA graph.
+//
+// Restates src/ipc/potentials/potential.cpp:36-222 (sum over contacts, dense
+// gradient, sparse Hessian from local 3n x 3n blocks with duplicates summed),
+// normal_potential.cpp:127-232 (per-contact energy, gradient and Hessian) and
+// eigen_ext.tpp:64-108 (PSD projection), the way SparseMatrixCache
+// (matrix_cache.cpp:80-214) reuses a pattern between Newton iterations.
+//
+// Per collision set (rebuilt only when the set, the mesh or the chunk bound
+// changes) the pattern is built once: every contact's n^2 vertex blocks are
+// keyed (row << 32 | col), radix-sorted and run-length encoded, which gives
+// the CSR pattern, and for every contribution its slot in block-sorted order
+// (perm).  The gradient's contributions (a contact's diagonal blocks) get
+// slots grouped by vertex the same way.  A step is then
+//   k_egh (persistent): warps take 32-contact tiles from a work queue; each
+//     lane computes one contact's energy, gradient and local Hessian,
+//     projects the Hessian to PSD and writes each 3x3 block to its sorted
+//     slot, the gradient to its vertex-grouped slot, the energy to its own;
+//   k_hess_reduce / k_grad_reduce / k_energy_reduce: streaming sums of
+//     contiguous runs of slots into the CSR values, the gradient and the
+//     per-scene energies, each value written once.
+// Everything is in fixed order (deterministic) and every size is known from
+// the pattern, so no step needs the host: the launches of a step are
+// captured once into a CUDA graph and replayed, reading the call's pointers
+// (positions, outputs, scratch) from a small device-side argument block that
+// is updated before each replay.
+//
+// The fused kernel's per-thread scratch (the local Hessian and the PSD
+// solver's work arrays) lives in local memory; how many warps stay resident
+// decides whether that scratch stays in L1/L2, so the grid shape (threads per
+// block, blocks per SM) and the work-queue grab size are chosen by a small
+// autotuner per device.
+#include <cstdio>
+#include <cstring>
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "contact.cuh"
+#include "profile.cuh"
+
+namespace ipcg {
+
+// CSR row pointers and columns of a cached pattern; matrices built on it
+// share them (and keep them alive after the set is rebuilt).
+struct EghPattern {
+    DBuf<int64_t> row_ptr;
+    DBuf<int> col;
+};
+
+namespace {
+
+// Pointers of one call, read by the graph's kernels from device memory: the
+// positions, the outputs, and the step's scratch (taken from the library's
+// stream-ordered pool for the call, so sets on many meshes share it).
+struct EghDev {
+    const double* V;
+    double* grad;
+    double* val;
+    double *slab, *gslab, *eslab;
+};
+
+// A run of consecutive scenes whose contacts are processed together (one
+// chunk for a single scene or a small batch).  Contacts of type t in the
+// chunk are [lo[t], hi[t]) of that type's list; the chunk-local contact
+// index runs VV | EV | EE | FV.
+struct EChunk {
+    int64_t lo[4], hi[4];
+    int64_t r0, r1;        // vertex rows
+    int64_t k0, k1;        // scenes
+    int64_t n, ncontrib;   // contacts, Hessian contributions (sum of n^2)
+    int64_t B0, nb;        // first CSR block, blocks
+    int64_t perm_off;      // offset of the chunk in perm (contributions)
+    int64_t rs_off;        // offset in run_start (nb + 1 entries per chunk)
+    int64_t gs_off;        // offset in gstart (r1 - r0 + 1 entries per chunk)
+    int64_t gslot_off;     // offset in gslot (4 per contact)
+};
+
+} // namespace
+
+struct EghCache {
+    // key
+    uint64_t version = 0, mesh_serial = 0;
+    int64_t budget = 0;
+    bool valid = false;
+    std::vector<EChunk> chunks;
+    int64_t n = 0, nb = 0, max_contrib = 0, max_n = 0, max_gs = 0;
+    std::shared_ptr<EghPattern> pattern;
+    DBuf<unsigned> perm, run_start, gstart, gslot;
+    DBuf<int64_t> vbase;   // per block: CSR position of its entry (0, 0)
+    DBuf<int> vnbr;        // per block: blocks in its block row
+    DBuf<int64_t> srange;  // per scene: chunk-local [begin, end) of each type (8 values)
+    DBuf<double> energy;   // per-scene energies of the last step
+    DBuf<unsigned long long> queue;
+    DBuf<int> fail;
+    DBuf<EghDev> dev;
+    HBuf<EghDev> hdev;
+    // captured step
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::string graph_key;
+    int graph_kernels = 0;
+    ~EghCache()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+namespace {
+
+constexpr int WANT_E = 1, WANT_G = 2, WANT_H = 4;
+
+std::mutex g_tune_mu;
+EghTuning g_tune[64];
+bool g_tune_set[64] = {};
+
+ContactsView full_view(const ipcg_collisions* cs)
+{
+    return ContactsView { cs->nvv, cs->nev, cs->nee, cs->nfv, cs->vv.p, cs->ev.p, cs->ee.p, cs->fv.p, cs->vv_w.p,
+        cs->ev_w.p, cs->ee_w.p, cs->fv_w.p, cs->ee_eps.p, cs->ee_dtype.p };
+}
+
+ContactsView chunk_view(const ContactsView& cv, const EChunk& c)
+{
+    ContactsView v = cv;
+    v.nvv = c.hi[0] - c.lo[0];
+    v.nev = c.hi[1] - c.lo[1];
+    v.nee = c.hi[2] - c.lo[2];
+    v.nfv = c.hi[3] - c.lo[3];
+    v.vv = cv.vv + c.lo[0];
+    v.vv_w = cv.vv_w + c.lo[0];
+    v.ev = cv.ev + c.lo[1];
+    v.ev_w = cv.ev_w + c.lo[1];
+    v.ee = cv.ee + c.lo[2];
+    v.ee_w = cv.ee_w + c.lo[2];
+    v.ee_eps = cv.ee_eps + c.lo[2];
+    v.ee_dt = cv.ee_dt + c.lo[2];
+    v.fv = cv.fv + c.lo[3];
+    v.fv_w = cv.fv_w + c.lo[3];
+    return v;
+}
+
+// First contribution of chunk-local contact i (VV: 4, EV: 9, EE / FV: 16 each).
+__device__ __forceinline__ int64_t contrib_offset(const ContactsView& cv, int64_t i)
+{
+    if (i < cv.nvv) return 4 * i;
+    if (i < cv.nvv + cv.nev) return 4 * cv.nvv + 9 * (i - cv.nvv);
+    return 4 * cv.nvv + 9 * cv.nev + 16 * (i - cv.nvv - cv.nev);
+}
+
+// ---- pattern build (once per collision set) ----
+
+__global__ void k_p_scene_ranges(ContactsView cv, const int64_t* __restrict__ offs, int S, int64_t* __restrict__ out)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 4 * S) return;
+    const int type = t / S;
+    const int2* list = type == 0 ? cv.vv : (type == 1 ? cv.ev : (type == 2 ? cv.ee : cv.fv));
+    const int64_t n = type == 0 ? cv.nvv : (type == 1 ? cv.nev : (type == 2 ? cv.nee : cv.nfv));
+    const int64_t key = offs[t];
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (list[mid].x < key) lo = mid + 1;
+        else hi = mid;
+    }
+    out[t] = lo;
+}
+
+__global__ void k_p_keys(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    unsigned long long* __restrict__ keys, int* __restrict__ ids)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    const int64_t off = contrib_offset(cv, i);
+    for (int a = 0; a < c.n; ++a)
+        for (int b = 0; b < c.n; ++b) {
+            keys[off + a * c.n + b] = ((unsigned long long)c.vid[a] << 32) | (unsigned)c.vid[b];
+            ids[off + a * c.n + b] = (int)(off + a * c.n + b);
+        }
+}
+
+__global__ void k_p_perm(const int* __restrict__ sorted_ids, int64_t n, unsigned* __restrict__ perm)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) perm[sorted_ids[s]] = (unsigned)s;
+}
+
+__global__ void k_p_runs(const int* __restrict__ start, int nb, unsigned total, unsigned* __restrict__ run_start)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nb) run_start[q] = (unsigned)start[q];
+    if (q == nb) run_start[q] = total;
+}
+
+// Block row pointers (chunk-local) of rows r0 .. r0 + nr from the sorted keys.
+__global__ void k_p_bptr(const unsigned long long* __restrict__ ukeys, int nb, int64_t r0, int nr, int* __restrict__ bptr)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > nr) return;
+    const unsigned long long key = (unsigned long long)(r0 + j) << 32;
+    int lo = 0, hi = nb;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ukeys[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    bptr[j] = lo;
+}
+
+// CSR rows 3 r0 .. 3 r1 of the chunk (B0 blocks of earlier chunks first).
+__global__ void k_p_rows(const int* __restrict__ bptr, int64_t r0, int nr, int64_t B0, int64_t* __restrict__ row_ptr)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j > nr) return;
+    const int64_t b0 = B0 + bptr[j];
+    const int64_t r = r0 + j;
+    if (j == nr) {
+        row_ptr[3 * r] = 9 * b0;
+        return;
+    }
+    const int64_t nbr = bptr[j + 1] - bptr[j];
+    for (int k = 0; k < 3; ++k) row_ptr[3 * r + k] = 9 * b0 + 3 * k * nbr;
+}
+
+// Per block: CSR columns, the position of entry (0, 0) and the row's block
+// count; diagonal blocks record their run for the gradient slots.
+__global__ void k_p_blocks(const unsigned long long* __restrict__ ukeys, int nb, const int* __restrict__ bptr,
+    int64_t r0, int64_t B0, const int* __restrict__ run_len, int* __restrict__ col, int64_t* __restrict__ vbase,
+    int* __restrict__ vnbr, int* __restrict__ diag_len, int* __restrict__ diag_q)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nb) return;
+    const unsigned long long key = ukeys[q];
+    const int64_t row = (int64_t)(key >> 32);
+    const int cc = (int)(key & 0xffffffffu);
+    const int j = (int)(row - r0);
+    const int b0 = bptr[j];
+    const int nbr = bptr[j + 1] - b0;
+    const int64_t base = 9 * (B0 + b0) + 3 * (int64_t)(q - b0);
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) col[base + 3 * (int64_t)k * nbr + l] = 3 * cc + l;
+    vbase[q] = base;
+    vnbr[q] = nbr;
+    if (row == cc) {
+        diag_len[j] = run_len[q];
+        diag_q[j] = q;
+    }
+}
+
+// Gradient slot of (contact i, local vertex a): the rank of its diagonal
+// contribution within the vertex's diagonal block, after the vertex's start.
+__global__ void k_p_gslot(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F, int64_t r0,
+    const unsigned* __restrict__ perm, const unsigned* __restrict__ run_start, const int* __restrict__ diag_q,
+    const int* __restrict__ gstart, unsigned* __restrict__ gslot)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    const int64_t off = contrib_offset(cv, i);
+    for (int a = 0; a < c.n; ++a) {
+        const int v = (int)(c.vid[a] - r0);
+        const unsigned s = perm[off + a * c.n + a];
+        gslot[4 * i + a] = (unsigned)gstart[v] + (s - run_start[diag_q[v]]);
+    }
+}
+
+// ---- the step ----
+
+// One lane per contact of a 32-contact tile; warps take tiles from the queue,
+// the last tiles (face-vertex and edge-edge, the costly ones) first.
+__global__ void __launch_bounds__(128) k_egh(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv, const unsigned* __restrict__ perm,
+    const unsigned* __restrict__ gslot, unsigned long long* __restrict__ queue, int psd, int want, int grab,
+    int* __restrict__ fail)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t ntiles = (n + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    const double* __restrict__ V = dev->V;
+    double* __restrict__ slab = dev->slab;
+    double* __restrict__ gslab = dev->gslab;
+    double* __restrict__ eslab = dev->eslab;
+    for (;;) {
+        unsigned long long t0 = 0;
+        if (lane == 0) t0 = atomicAdd(queue, (unsigned long long)grab);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if ((int64_t)t0 >= ntiles) break;
+        const int64_t t1 = min((int64_t)t0 + grab, ntiles);
+        for (int64_t tt = (int64_t)t0; tt < t1; ++tt) {
+            const int64_t i = (ntiles - 1 - tt) * 32 + lane;
+            if (i >= n) continue;
+            Local c;
+            load_contact(cv, E, F, i, c);
+            const Params P = sp[sv.of(c.vid[0])];
+            V3 x[4];
+            gather(V, c, x);
+            double e, g[12], H[144];
+            const bool pr = contact_egh(c, x, P, e, g, H);
+            if (want & WANT_E) eslab[i] = e;
+            if (want & WANT_G)
+                for (int a = 0; a < c.n; ++a) {
+                    const int64_t s = gslot[4 * i + a];
+                    gslab[3 * s] = g[3 * a];
+                    gslab[3 * s + 1] = g[3 * a + 1];
+                    gslab[3 * s + 2] = g[3 * a + 2];
+                }
+            if (want & WANT_H) {
+                if (psd != IPCG_PSD_NONE && pr && !project_psd(c.n, LocalAcc { H }, psd)) atomicOr(fail, 1);
+                const int N = 3 * c.n;
+                const int64_t off = contrib_offset(cv, i);
+                for (int a = 0; a < c.n; ++a)
+                    for (int b = 0; b < c.n; ++b) {
+                        double* o = slab + 9 * (int64_t)perm[off + a * c.n + b];
+#pragma unroll
+                        for (int k = 0; k < 3; ++k)
+#pragma unroll
+                            for (int l = 0; l < 3; ++l) o[3 * k + l] = H[(3 * a + k) * N + 3 * b + l];
+                    }
+            }
+        }
+    }
+}
+
+// CSR values: each stored value sums its block's contiguous run of slots.
+__global__ void k_hess_reduce(int64_t nb, const unsigned* __restrict__ run_start, const int64_t* __restrict__ vbase,
+    const int* __restrict__ vnbr, const EghDev* __restrict__ dev)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 9 * nb) return;
+    const double* __restrict__ slab = dev->slab;
+    const int64_t q = t / 9;
+    const int kl = (int)(t % 9), k = kl / 3, l = kl % 3;
+    double sum = 0;
+    for (unsigned s = run_start[q]; s < run_start[q + 1]; ++s) sum += slab[9 * (int64_t)s + kl];
+    dev->val[vbase[q] + 3 * (int64_t)k * vnbr[q] + l] = sum;
+}
+
+// Gradient entries of vertex rows [r0, r0 + nr): contiguous runs of slots.
+__global__ void k_grad_reduce(int64_t r0, int64_t nr, const unsigned* __restrict__ gstart,
+    const EghDev* __restrict__ dev)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * nr) return;
+    const double* __restrict__ gslab = dev->gslab;
+    const int64_t v = t / 3;
+    const int k = (int)(t % 3);
+    double sum = 0;
+    for (unsigned s = gstart[v]; s < gstart[v + 1]; ++s) sum += gslab[3 * (int64_t)s + k];
+    dev->grad[3 * (r0 + v) + k] = sum;
+}
+
+// Per-scene energies: one block per scene sums its four contact ranges
+// (fixed per-thread order and a fixed reduction tree: deterministic).
+constexpr int ER_BLOCK = 256;
+__global__ void __launch_bounds__(ER_BLOCK) k_energy_reduce(const int64_t* __restrict__ srange,
+    const EghDev* __restrict__ dev, double* __restrict__ energy)
+{
+    const int64_t* r = srange + 8 * (int64_t)blockIdx.x;
+    const double* __restrict__ eslab = dev->eslab;
+    double s = 0;
+    for (int t = 0; t < 4; ++t)
+        for (int64_t i = r[2 * t] + threadIdx.x; i < r[2 * t + 1]; i += ER_BLOCK) s += eslab[i];
+    typedef cub::BlockReduce<double, ER_BLOCK> BR;
+    __shared__ typename BR::TempStorage tmp;
+    const double tot = BR(tmp).Sum(s);
+    if (threadIdx.x == 0) energy[blockIdx.x] = tot;
+}
+
+int device_index()
+{
+    int d = 0;
+    IPCG_CUDA(cudaGetDevice(&d));
+    return d < 0 || d >= 64 ? 0 : d;
+}
+
+// Work per chunk: runs of whole scenes with at most `budget` contacts.
+std::vector<EChunk> plan(const ipcg_collisions* cs, ipcg_mesh* m, const ContactsView& cv, int64_t budget,
+    std::vector<int64_t>& ranges /* 4 x (ns + 1) */)
+{
+    const int64_t ns = m->n_scenes;
+    const int S = (int)(ns + 1);
+    ranges.assign(4 * S, 0);
+    const int64_t counts[4] = { cs->nvv, cs->nev, cs->nee, cs->nfv };
+    if (ns == 1) {
+        for (int t = 0; t < 4; ++t) ranges[t * S + 1] = counts[t];
+    } else {
+        DBuf<int64_t> d_out;
+        d_out.reserve(4 * S);
+        IPCG_LAUNCH("k_p_scene_ranges", m->stream, k_p_scene_ranges<<<grid_for(4 * S, 256), 256, 0, m->stream>>>(cv,
+            m->scene_offs.p, S, d_out.p));
+        IPCG_CUDA(cudaMemcpyAsync(ranges.data(), d_out.p, sizeof(int64_t) * 4 * S, cudaMemcpyDeviceToHost, m->stream));
+        IPCG_CUDA(cudaStreamSynchronize(m->stream));
+    }
+    auto count = [&](int64_t a, int64_t b) {
+        int64_t c = 0;
+        for (int t = 0; t < 4; ++t) c += ranges[t * S + b] - ranges[t * S + a];
+        return c;
+    };
+    std::vector<EChunk> out;
+    int64_t k0 = 0;
+    while (k0 < ns) {
+        int64_t k1 = k0 + 1;
+        while (k1 < ns && count(k0, k1 + 1) <= budget) ++k1;
+        EChunk c {};
+        for (int t = 0; t < 4; ++t) {
+            c.lo[t] = ranges[t * S + k0];
+            c.hi[t] = ranges[t * S + k1];
+        }
+        c.r0 = m->h_voff[k0];
+        c.r1 = m->h_voff[k1];
+        c.k0 = k0;
+        c.k1 = k1;
+        c.n = count(k0, k1);
+        c.ncontrib = 4 * (c.hi[0] - c.lo[0]) + 9 * (c.hi[1] - c.lo[1]) + 16 * ((c.hi[2] - c.lo[2]) + (c.hi[3] - c.lo[3]));
+        out.push_back(c);
+        k0 = k1;
+    }
+    return out;
+}
+
+void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
+{
+    cudaStream_t s = m->stream;
+    const ContactsView cv = full_view(cs);
+    const int64_t budget = g_hess_chunk_contacts.load();
+    std::vector<int64_t> ranges;
+    C.chunks = plan(cs, m, cv, budget, ranges);
+    const int64_t ns = m->n_scenes, S = ns + 1, nV = m->nV;
+    int64_t tot_contrib = 0, tot_n = 0;
+    C.max_contrib = C.max_n = 0;
+    for (EChunk& c : C.chunks) {
+        if (c.ncontrib >= (int64_t)INT32_MAX) throw Error(IPCG_ERR_INVALID, "too many Hessian contributions in one chunk");
+        c.perm_off = tot_contrib;
+        c.gslot_off = 4 * tot_n;
+        tot_contrib += c.ncontrib;
+        tot_n += c.n;
+        C.max_contrib = std::max(C.max_contrib, c.ncontrib);
+        C.max_n = std::max(C.max_n, c.n);
+    }
+    C.n = tot_n;
+    // per-scene chunk-local ranges of each type (energy sums)
+    std::vector<int64_t> sr(8 * ns);
+    for (const EChunk& c : C.chunks) {
+        const int64_t base[4] = { 0, c.hi[0] - c.lo[0], (c.hi[0] - c.lo[0]) + (c.hi[1] - c.lo[1]),
+            (c.hi[0] - c.lo[0]) + (c.hi[1] - c.lo[1]) + (c.hi[2] - c.lo[2]) };
+        for (int64_t k = c.k0; k < c.k1; ++k)
+            for (int t = 0; t < 4; ++t) {
+                sr[8 * k + 2 * t] = base[t] + ranges[t * S + k] - c.lo[t];
+                sr[8 * k + 2 * t + 1] = base[t] + ranges[t * S + k + 1] - c.lo[t];
+            }
+    }
+    C.srange.reserve(8 * ns + 1);
+    IPCG_CUDA(cudaMemcpyAsync(C.srange.p, sr.data(), sizeof(int64_t) * 8 * ns, cudaMemcpyHostToDevice, s));
+    C.perm.reserve(tot_contrib + 1);
+    C.gslot.reserve(4 * tot_n + 1);
+    // work space of the sort
+    const int64_t mk = C.max_contrib + 1;
+    m->keys_a.reserve(mk);
+    m->keys_b.reserve(mk);
+    m->ivals_a.reserve(nV + 2);
+    m->ivals_b.reserve(3 * mk + 3);
+    m->counters.reserve(16);
+    int* d_nb = m->counters.p + 13;
+    auto pat = std::make_shared<EghPattern>();
+    pat->row_ptr.reserve(3 * nV + 1);
+    // the chunks' block counts are only known after their sorts: columns and
+    // block arrays grow as chunks finish (the row pointers are sized already)
+    int64_t B0 = 0, rs_tot = 0, gs_tot = 0;
+    DBuf<int> tmp_start, diag_len, diag_q, gstart_i;
+    C.max_gs = 0;
+    for (size_t ci = 0; ci < C.chunks.size(); ++ci) {
+        EChunk& ch = C.chunks[ci];
+        const ContactsView cc = chunk_view(cv, ch);
+        const int64_t nk = ch.ncontrib;
+        const int64_t nr = ch.r1 - ch.r0;
+        ch.B0 = B0;
+        ch.rs_off = rs_tot;
+        ch.gs_off = gs_tot;
+        int nb = 0;
+        int* ids_in = m->ivals_b.p;
+        int* sorted_ids = m->ivals_b.p + (nk + 1);
+        int* run_len = m->ivals_b.p + 2 * (nk + 1);
+        if (ch.n > 0) {
+            IPCG_LAUNCH("k_p_keys", s, k_p_keys<<<grid_for(ch.n, 128), 128, 0, s>>>(cc, m->E.p, m->F.p, m->keys_a.p,
+                ids_in));
+            sort_pairs_u64(m, s, m->keys_a.p, m->keys_b.p, ids_in, sorted_ids, (int)nk, 32 + bits_for(nV + 1));
+            rle_u64(m, s, m->keys_b.p, m->keys_a.p, run_len, d_nb, (int)nk);
+            IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p, d_nb, sizeof(int), cudaMemcpyDeviceToHost, s));
+            IPCG_CUDA(cudaStreamSynchronize(s));
+            nb = m->h_counters.p[0];
+        }
+        ch.nb = nb;
+        // blocks of this chunk: run starts, CSR columns, positions
+        C.run_start.grow_keep(rs_tot + nb + 2, rs_tot, s);
+        C.vbase.grow_keep(B0 + nb + 1, B0, s);
+        C.vnbr.grow_keep(B0 + nb + 1, B0, s);
+        pat->col.grow_keep(9 * (B0 + nb) + 1, 9 * B0, s);
+        tmp_start.reserve(nb + 1);
+        diag_len.reserve(nr + 2);
+        diag_q.reserve(nr + 2);
+        gstart_i.reserve(nr + 2);
+        int* bptr = m->ivals_a.p;
+        IPCG_CUDA(cudaMemsetAsync(diag_len.p, 0, sizeof(int) * (nr + 1), s));
+        if (nb > 0) {
+            exclusive_sum_i32(m, s, run_len, tmp_start.p, nb);
+            IPCG_LAUNCH("k_p_runs", s, k_p_runs<<<grid_for(nb + 1, 256), 256, 0, s>>>(tmp_start.p, nb, (unsigned)nk,
+                C.run_start.p + rs_tot));
+            IPCG_LAUNCH("k_p_perm", s, k_p_perm<<<grid_for(nk, 256), 256, 0, s>>>(sorted_ids, nk,
+                C.perm.p + ch.perm_off));
+        }
+        IPCG_LAUNCH("k_p_bptr", s, k_p_bptr<<<grid_for(nr + 1, 256), 256, 0, s>>>(m->keys_a.p, nb, ch.r0, (int)nr,
+            bptr));
+        IPCG_LAUNCH("k_p_rows", s, k_p_rows<<<grid_for(nr + 1, 256), 256, 0, s>>>(bptr, ch.r0, (int)nr, B0,
+            pat->row_ptr.p));
+        if (nb > 0)
+            IPCG_LAUNCH("k_p_blocks", s, k_p_blocks<<<grid_for(nb, 256), 256, 0, s>>>(m->keys_a.p, nb, bptr, ch.r0, B0,
+                run_len, pat->col.p, C.vbase.p + B0, C.vnbr.p + B0, diag_len.p, diag_q.p));
+        // gradient slots: vertex starts from the diagonal runs
+        exclusive_sum_i32(m, s, diag_len.p, gstart_i.p, (int)(nr + 1));
+        C.gstart.grow_keep(gs_tot + nr + 2, gs_tot, s);
+        IPCG_CUDA(cudaMemcpyAsync(C.gstart.p + gs_tot, gstart_i.p, sizeof(int) * (nr + 1), cudaMemcpyDeviceToDevice, s));
+        if (ch.n > 0)
+            IPCG_LAUNCH("k_p_gslot", s, k_p_gslot<<<grid_for(ch.n, 128), 128, 0, s>>>(cc, m->E.p, m->F.p, ch.r0,
+                C.perm.p + ch.perm_off, C.run_start.p + rs_tot, diag_q.p, gstart_i.p, C.gslot.p + ch.gslot_off));
+        int gtot = 0;
+        IPCG_CUDA(cudaMemcpyAsync(&gtot, gstart_i.p + nr, sizeof(int), cudaMemcpyDeviceToHost, s));
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        C.max_gs = std::max<int64_t>(C.max_gs, gtot);
+        rs_tot += nb + 1;
+        gs_tot += nr + 1;
+        B0 += nb;
+    }
+    C.nb = B0;
+    C.pattern = pat;
+    C.energy.reserve(ns + 1);
+    C.queue.reserve(C.chunks.size() + 1);
+    C.fail.reserve(1);
+    C.dev.reserve(1);
+    C.hdev.reserve(1);
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    C.version = cs->version;
+    C.mesh_serial = m->serial;
+    C.budget = budget;
+    C.valid = true;
+    if (C.exec) {
+        cudaGraphExecDestroy(C.exec);
+        C.exec = nullptr;
+    }
+    if (C.graph) {
+        cudaGraphDestroy(C.graph);
+        C.graph = nullptr;
+    }
+    C.graph_key.clear();
+}
+
+// Launch geometry of the fused kernel for a tuning: a persistent grid of
+// blocks_per_sm blocks per SM, never more warps than tiles.
+void egh_grid(const EghTuning& t, int64_t n, int& blocks, int& threads)
+{
+    int dev = 0, sms = 1;
+    IPCG_CUDA(cudaGetDevice(&dev));
+    IPCG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    threads = t.threads;
+    const int64_t need = (n + 31) / 32 * 32 / threads + 1;
+    blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * t.blocks_per_sm, need));
+}
+
+// Enqueue the launches of one step on the mesh stream (also while capturing).
+int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Params* sp, int psd, int want,
+    const EghTuning& tune)
+{
+    cudaStream_t s = m->stream;
+    const ContactsView cv = full_view(cs);
+    const SceneView sv = scene_view(m);
+    int kernels = 0;
+    for (size_t ci = 0; ci < C.chunks.size(); ++ci) {
+        const EChunk& ch = C.chunks[ci];
+        const ContactsView cc = chunk_view(cv, ch);
+        if (ch.n > 0) {
+            IPCG_CUDA(cudaMemsetAsync(C.queue.p + ci, 0, sizeof(unsigned long long), s));
+            int blocks, threads;
+            egh_grid(tune, ch.n, blocks, threads);
+            IPCG_LAUNCH("k_egh", s, k_egh<<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv,
+                C.perm.p + ch.perm_off, C.gslot.p + ch.gslot_off, C.queue.p + ci, psd, want, tune.tiles_per_grab,
+                C.fail.p));
+            ++kernels;
+        }
+        if ((want & WANT_H) && ch.nb > 0) {
+            IPCG_LAUNCH("k_hess_reduce", s, k_hess_reduce<<<grid_for(9 * ch.nb, 256), 256, 0, s>>>(ch.nb,
+                C.run_start.p + ch.rs_off, C.vbase.p + ch.B0, C.vnbr.p + ch.B0, C.dev.p));
+            ++kernels;
+        }
+        const int64_t nr = ch.r1 - ch.r0;
+        if ((want & WANT_G) && nr > 0) {
+            IPCG_LAUNCH("k_grad_reduce", s, k_grad_reduce<<<grid_for(3 * nr, 256), 256, 0, s>>>(ch.r0, nr,
+                C.gstart.p + ch.gs_off, C.dev.p));
+            ++kernels;
+        }
+        if ((want & WANT_E) && ch.k1 > ch.k0) {
+            IPCG_LAUNCH("k_energy_reduce", s, k_energy_reduce<<<(int)(ch.k1 - ch.k0), ER_BLOCK, 0, s>>>(
+                C.srange.p + 8 * ch.k0, C.dev.p, C.energy.p + ch.k0));
+            ++kernels;
+        }
+    }
+    return kernels;
+}
+
+Params* upload_params_egh(const ipcg_collisions* cs, ipcg_mesh* m, const BarrierArgs& a)
+{
+    const int ns = (int)m->n_scenes;
+    std::vector<Params> hp(ns);
+    for (int k = 0; k < ns; ++k) {
+        const double dh = a.scene_dhat ? a.scene_dhat[k] : a.dhat;
+        const double kap = a.scene_kappa ? a.scene_kappa[k] : a.kappa;
+        const double dm = (k < (int)cs->scene_dmin.size()) ? cs->scene_dmin[k] : cs->dmin;
+        const double xh = (2 * dm + dh) * dh;
+        hp[k] = Params { kap, dm * dm, xh, a.physical ? dh / barrier_units(a.kind, xh) : 1.0, a.psd, a.mixed, a.kind,
+            a.fp32_local };
+    }
+    const size_t pbytes = sizeof(Params) * ns;
+    const unsigned char* hb = reinterpret_cast<const unsigned char*>(hp.data());
+    if (m->params_host.size() != pbytes || memcmp(m->params_host.data(), hb, pbytes) != 0) {
+        m->params_buf.reserve(pbytes);
+        IPCG_CUDA(cudaMemcpyAsync(m->params_buf.p, hb, pbytes, cudaMemcpyHostToDevice, m->stream));
+        m->params_host.assign(hb, hb + pbytes);
+    }
+    return reinterpret_cast<Params*>(m->params_buf.p);
+}
+
+// The step's scratch for the largest chunk from the library's pool (freed in
+// stream order after the step): Hessian slots, gradient slots, energies.
+struct Scratch {
+    double *slab = nullptr, *gslab = nullptr, *eslab = nullptr;
+    cudaStream_t s = nullptr;
+    void alloc(const EghCache& C, cudaStream_t st)
+    {
+        s = st;
+        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&slab, sizeof(double) * (9 * C.max_contrib + 9), device_pool(), s));
+        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&gslab, sizeof(double) * (3 * C.max_gs + 3), device_pool(), s));
+        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&eslab, sizeof(double) * (C.max_n + 1), device_pool(), s));
+    }
+    ~Scratch()
+    {
+        if (slab) cudaFreeAsync(slab, s);
+        if (gslab) cudaFreeAsync(gslab, s);
+        if (eslab) cudaFreeAsync(eslab, s);
+    }
+};
+
+EghCache& cache_for(const ipcg_collisions* cs, ipcg_mesh* m)
+{
+    auto* c = const_cast<ipcg_collisions*>(cs);
+    if (!c->egh) c->egh = std::make_shared<EghCache>();
+    EghCache& C = *c->egh;
+    if (!C.valid || C.version != cs->version || C.mesh_serial != m->serial
+        || C.budget != g_hess_chunk_contacts.load())
+        build_pattern(cs, m, C);
+    return C;
+}
+
+} // namespace
+
+EghTuning egh_tuning()
+{
+    const int d = device_index();
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return g_tune_set[d] ? g_tune[d] : EghTuning {};
+}
+
+void egh_set_tuning(const EghTuning& t)
+{
+    if (!(t.threads == 32 || t.threads == 64 || t.threads == 128) || t.blocks_per_sm < 1 || t.blocks_per_sm > 64
+        || t.tiles_per_grab < 1 || t.tiles_per_grab > 64)
+        throw Error(IPCG_ERR_INVALID, "tuning out of range: threads 32/64/128, blocks_per_sm 1-64, tiles_per_grab 1-64");
+    const int d = device_index();
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[d] = t;
+    g_tune_set[d] = true;
+}
+
+bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a, double* energy_host,
+    double* grad_dev, ipcg_csr* hess)
+{
+    if (!hess || a.shape) return false;
+    if (m->n_scenes > 1 && !cs->sorted) return false;
+    cudaStream_t s = m->stream;
+    const int64_t n = cs->size();
+    const int ns = (int)m->n_scenes;
+    hess->rows = 3 * m->nV;
+    hess->stream = s;
+    if (n == 0) {
+        // nothing to evaluate: zero energies and gradient, an empty matrix
+        if (energy_host) std::fill(energy_host, energy_host + ns, 0.0);
+        if (grad_dev) IPCG_CUDA(cudaMemsetAsync(grad_dev, 0, sizeof(double) * 3 * m->nV, s));
+        hess->row_ptr.reserve(3 * m->nV + 1, s);
+        IPCG_CUDA(cudaMemsetAsync(hess->row_ptr.p, 0, sizeof(int64_t) * (3 * m->nV + 1), s));
+        hess->nnz = 0;
+        IPCG_CUDA(cudaStreamSynchronize(s));
+        return true;
+    }
+    EghCache& C = cache_for(cs, m);
+    const Params* sp = upload_params_egh(cs, m, a);
+    const int want = WANT_H | (energy_host ? WANT_E : 0) | (grad_dev ? WANT_G : 0);
+    // outputs: the values are the call's own; the pattern is shared
+    const int64_t nnz = 9 * C.nb;
+    hess->val.reserve(nnz + 1, s);
+    hess->nnz = nnz;
+    hess->pattern = C.pattern;
+    hess->row_ptr_shared = C.pattern->row_ptr.p;
+    hess->col_shared = C.pattern->col.p;
+    Scratch scr;
+    scr.alloc(C, s);
+    C.hdev.p[0] = EghDev { V, grad_dev, hess->val.p, scr.slab, scr.gslab, scr.eslab };
+    IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
+    IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(int), s));
+    const EghTuning tune = egh_tuning();
+    if (prof::enabled()) {
+        // per-kernel timing needs the launches themselves, not a replay
+        enqueue_step(cs, m, C, sp, a.psd, want, tune);
+    } else {
+        char key[160];
+        snprintf(key, sizeof(key), "%p|%d|%d|%d|%d|%d", (const void*)sp, a.psd, want, tune.threads, tune.blocks_per_sm,
+            tune.tiles_per_grab);
+        if (!C.exec || C.graph_key != key) {
+            if (C.exec) cudaGraphExecDestroy(C.exec);
+            if (C.graph) cudaGraphDestroy(C.graph);
+            C.exec = nullptr;
+            C.graph = nullptr;
+            IPCG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            int kernels = 0;
+            try {
+                kernels = enqueue_step(cs, m, C, sp, a.psd, want, tune);
+            } catch (...) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(s, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            IPCG_CUDA(cudaStreamEndCapture(s, &C.graph));
+            IPCG_CUDA(cudaGraphInstantiate(&C.exec, C.graph, 0));
+            C.graph_key = key;
+            C.graph_kernels = kernels;
+        }
+        IPCG_CUDA(cudaGraphLaunch(C.exec, s));
+        prof::count_graph(C.graph_kernels);
+    }
+    if (energy_host)
+        IPCG_CUDA(cudaMemcpyAsync(energy_host, C.energy.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p + 1, C.fail.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaStreamSynchronize(s));
+    if (m->h_counters.p[1]) throw Error(IPCG_ERR_CUDA, "unable to project matrix onto positive semi-definite cone");
+    return true;
+}
+
+std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a)
+{
+    cudaStream_t s = m->stream;
+    if (cs->size() == 0) throw Error(IPCG_ERR_INVALID, "autotuning needs a non-empty collision set");
+    if (m->n_scenes > 1 && !cs->sorted) throw Error(IPCG_ERR_INVALID, "autotuning needs a built collision set");
+    EghCache& C = cache_for(cs, m);
+    const Params* sp = upload_params_egh(cs, m, a);
+    // the largest chunk is the workload
+    size_t big = 0;
+    for (size_t i = 0; i < C.chunks.size(); ++i)
+        if (C.chunks[i].n > C.chunks[big].n) big = i;
+    const EChunk& ch = C.chunks[big];
+    const ContactsView cc = chunk_view(full_view(cs), ch);
+    const SceneView sv = scene_view(m);
+    Scratch scr;
+    scr.alloc(C, s);
+    C.hdev.p[0] = EghDev { V, nullptr, nullptr, scr.slab, scr.gslab, scr.eslab };
+    IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
+    IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(int), s));
+    int dev = 0;
+    IPCG_CUDA(cudaGetDevice(&dev));
+    cudaEvent_t e0, e1;
+    IPCG_CUDA(cudaEventCreate(&e0));
+    IPCG_CUDA(cudaEventCreate(&e1));
+    EghTuning best {};
+    float best_ms = 1e30f;
+    std::string rep = "{\"workload_contacts\": " + std::to_string(ch.n) + ", \"candidates\": [";
+    bool first = true;
+    for (int threads : { 32, 64, 128 }) {
+        int occ = 0;
+        IPCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_egh, threads, 0));
+        for (int bps : { 1, 2, 3, 4, 6, 8, 12, 16 }) {
+            if (bps * threads > 1024 || bps > occ) continue;
+            for (int grab : { 1, 4 }) {
+                const EghTuning t { threads, bps, grab };
+                float ms = 0;
+                for (int rep_i = 0; rep_i < 3; ++rep_i) {
+                    IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long), s));
+                    int blocks, thr;
+                    egh_grid(t, ch.n, blocks, thr);
+                    IPCG_CUDA(cudaEventRecord(e0, s));
+                    k_egh<<<blocks, thr, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv, C.perm.p + ch.perm_off,
+                        C.gslot.p + ch.gslot_off, C.queue.p, a.psd, WANT_H | WANT_G | WANT_E, grab, C.fail.p);
+                    IPCG_CHECK_LAUNCH();
+                    prof::count();
+                    IPCG_CUDA(cudaEventRecord(e1, s));
+                    IPCG_CUDA(cudaEventSynchronize(e1));
+                    float t_ms = 0;
+                    IPCG_CUDA(cudaEventElapsedTime(&t_ms, e0, e1));
+                    if (rep_i > 0) ms += t_ms; // the first run warms the caches
+                }
+                ms /= 2;
+                char buf[160];
+                snprintf(buf, sizeof(buf), "%s{\"threads\": %d, \"blocks_per_sm\": %d, \"tiles_per_grab\": %d, \"ms\": %.4f}",
+                    first ? "" : ", ", threads, bps, grab, ms);
+                rep += buf;
+                first = false;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best = t;
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    egh_set_tuning(best);
+    char buf[200];
+    snprintf(buf, sizeof(buf), "], \"device\": %d, \"chosen\": {\"threads\": %d, \"blocks_per_sm\": %d, "
+        "\"tiles_per_grab\": %d, \"ms\": %.4f}}", dev, best.threads, best.blocks_per_sm, best.tiles_per_grab, best_ms);
+    rep += buf;
+    return rep;
+}
+
+} // namespace ipcg

@@ -6,6 +6,7 @@
 #include <stdexcept>
 #include <string>
 #include <atomic>
+#include <memory>
 #include <vector>
 
 #include "../../include/ipcg.h"
@@ -157,8 +158,14 @@ enum : int { GUARD_STACK = 1, GUARD_CAPACITY = 2 };
 
 } // namespace ipcg
 
+namespace ipcg {
+struct EghCache;   // egh.cu: cached Hessian pattern and captured graph of a collision set
+struct EghPattern; // egh.cu: CSR row pointers and columns shared with the matrices built on them
+}
+
 struct ipcg_mesh {
     int device = 0;
+    uint64_t serial = 0;             // unique per mesh created in this process (cache keys)
     int64_t nV = 0, nE = 0, nF = 0;
     int64_t n_scenes = 1;
     // CollisionMesh::num_codim_vertices / num_codim_edges (collision_mesh.cpp:
@@ -224,6 +231,8 @@ struct ipcg_mesh {
 
 struct ipcg_collisions {
     int64_t nvv = 0, nev = 0, nee = 0, nfv = 0;
+    uint64_t version = 0;            // bumped by every build or load (cache keys)
+    std::shared_ptr<ipcg::EghCache> egh; // cached Hessian pattern + graph (egh.cu)
     int64_t n_cand_ee = 0, n_cand_fv = 0;
     double dmin = 0;
     std::vector<double> scene_dmin;  // per scene (batches)
@@ -262,6 +271,13 @@ struct ipcg_csr {
     ipcg::PBuf<int> col;
     ipcg::PBuf<double> val;
     cudaStream_t stream = nullptr;
+    // A matrix built on a cached pattern shares its row pointers and columns
+    // (kept alive by `pattern`) instead of owning copies.
+    std::shared_ptr<const ipcg::EghPattern> pattern;
+    const int64_t* row_ptr_shared = nullptr;
+    const int* col_shared = nullptr;
+    const int64_t* rowp() const { return row_ptr_shared ? row_ptr_shared : row_ptr.p; }
+    const int* colp() const { return col_shared ? col_shared : col.p; }
     // Freed on the default stream: the matrix may outlive its mesh's stream,
     // and every call that produced or read it has finished by then.
     ~ipcg_csr() { row_ptr.s = col.s = val.s = nullptr; }
@@ -317,6 +333,7 @@ struct BarrierArgs {
     int mixed = 0;                       // FP32 point-triangle contacts
     int kind = 0;                        // barrier function (IPCG_BARRIER_* kinds)
     int shape = 0;                       // Hessian slot holds the shape derivative
+    int fp32_local = 0;                  // FP32 local Hessians but near-parallel EE
 };
 struct FrictionView;
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
@@ -353,6 +370,29 @@ double collisions_min_distance(const ipcg_collisions* c, ipcg_mesh* m, const dou
 // is_step_collision_free (ipc.cpp:20-40): no candidate has a hit in [0, 1].
 bool step_collision_free(ipcg_mesh* m, const double* V0, const double* V1, double min_distance, double tolerance,
     int64_t max_iterations, double rescale);
+
+// egh.cu: energy (host, one per scene), gradient (device, 3 nV) and Hessian of
+// the barrier in one pass with the collision set's cached pattern, replayed as
+// one CUDA graph.  Returns false (nothing done) when the request is not one
+// this pipeline serves (shape derivatives, no Hessian, or a batch set loaded
+// unsorted); the caller then uses barrier_evaluate.
+bool barrier_egh(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a, double* energy_host,
+    double* grad_dev, ipcg_csr* hess);
+// Tuning of the fused kernel on the current device: threads per block, blocks
+// per SM and warp tiles taken per work-queue grab.
+struct EghTuning {
+    int threads = 64, blocks_per_sm = 4, tiles_per_grab = 1;
+};
+EghTuning egh_tuning();
+void egh_set_tuning(const EghTuning& t);
+// Time the fused kernel over candidate tunings on this set's largest chunk and
+// keep the fastest for the device; returns a JSON report.
+std::string egh_autotune(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a);
+// barrier.cu: derivative `order` (0-2) of barrier function `kind`
+// (IPCG_BARRIER_* kinds) at x with activation xhat, on the host.
+double barrier_derivative_host(int kind, int order, double x, double xhat);
+// barrier.cu: a . b and b . b of two device vectors of n doubles (deterministic).
+void dot_pair_device(const double* a, const double* b, int64_t n, double* ab, double* bb);
 
 // Caller-owned device arrays of a collision set (layout of ipcg_collisions_get).
 struct ContactsNoAlloc {

@@ -13,6 +13,8 @@ namespace ipcg {
 namespace prof {
 bool enabled();
 void count();
+// a replayed CUDA graph launches `kernels` kernel nodes
+void count_graph(int kernels);
 void record(const char* name, cudaEvent_t a, cudaEvent_t b);
 void make_events(cudaEvent_t* a, cudaEvent_t* b);
 } // namespace prof

@@ -128,6 +128,11 @@ def _load():
         "ipcg_server_submit_stepsize": (i32, [P, i64, P, P, d, P]),
         "ipcg_server_wait": (i32, [P, i64, P, P, PP]),
         "ipcg_server_stats": (i32, [P, P]),
+        "ipcg_barrier_autotune": (i32, [P, P, P, P, P, i32, i32, C.c_char_p, i64, P]),
+        "ipcg_barrier_tuning": (i32, [P, P, P]),
+        "ipcg_barrier_set_tuning": (i32, [i32, i32, i32]),
+        "ipcg_initial_barrier_stiffness": (i32, [d, i32, d, d, P, P, i64, d, d, P, P]),
+        "ipcg_update_barrier_stiffness": (i32, [d, d, d, d, d, d, d, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -171,6 +176,14 @@ def _as_f64(x, ncols=3):
     return a
 
 
+def _as_f64_vec(x):
+    """A flat float64 vector (numpy array or contiguous CUDA tensor)."""
+    if _is_torch_cuda(x):
+        import torch
+        return x.to(torch.float64).contiguous().reshape(-1)
+    return np.ascontiguousarray(x, dtype=np.float64).reshape(-1)
+
+
 def _as_i32(x, ncols):
     a = np.ascontiguousarray(np.asarray(x), dtype=np.int32)
     if a.size == 0:
@@ -202,6 +215,43 @@ def set_hessian_chunk_contacts(contacts: int = 0):
     _check(_load().ipcg_set_hessian_chunk_contacts(int(contacts)))
 
 
+def _precision_bits(mode) -> int:
+    """Option bits of a mixed-precision mode: False / "fp64", True / "pt",
+    "local" (IPCG_BARRIER_FP32_PT = 2, IPCG_BARRIER_FP32_LOCAL = 4)."""
+    if mode in (False, None, "fp64"):
+        return 0
+    if mode in (True, "pt"):
+        return 2
+    if mode == "local":
+        return 2 | 4
+    raise ValueError(f"unknown mixed-precision mode {mode!r}")
+
+
+def autotune_barrier(collisions, mesh, vertices, dhat, stiffness, options: int = 0, project_hessian_to_psd=1) -> dict:
+    """ipcg_barrier_autotune: dhat / stiffness one per scene; returns the
+    JSON report as a dict (candidates and the chosen launch shape)."""
+    import json
+    V = _as_f64(vertices)
+    dh = np.ascontiguousarray(np.atleast_1d(np.asarray(dhat, np.float64)))
+    kap = np.ascontiguousarray(np.atleast_1d(np.asarray(stiffness, np.float64)))
+    need = C.c_int64()
+    buf = C.create_string_buffer(1 << 16)
+    _check(_load().ipcg_barrier_autotune(collisions._h, mesh._h, _ptr(V), _ptr(dh), _ptr(kap), int(options),
+                                         int(project_hessian_to_psd), buf, len(buf), C.byref(need)))
+    return json.loads(buf.value.decode())
+
+
+def barrier_tuning() -> dict:
+    """The fused kernel's launch shape on the current device."""
+    t, b, g = C.c_int(), C.c_int(), C.c_int()
+    _check(_load().ipcg_barrier_tuning(C.byref(t), C.byref(b), C.byref(g)))
+    return {"threads": t.value, "blocks_per_sm": b.value, "tiles_per_grab": g.value}
+
+
+def set_barrier_tuning(threads: int, blocks_per_sm: int, tiles_per_grab: int = 1):
+    _check(_load().ipcg_barrier_set_tuning(int(threads), int(blocks_per_sm), int(tiles_per_grab)))
+
+
 def launch_count() -> int:
     """Kernel launches issued by the library since it was loaded."""
     n = C.c_int64()
@@ -222,6 +272,14 @@ class DeviceCSR:
     def to_scipy(self):
         h, self._h = self._h, None
         return _csr_to_scipy(h, self.ndof)
+
+    def values_into(self, out):
+        """Copy the nnz values into ``out`` (a float64 torch CUDA tensor or
+        numpy array of nnz entries) without the index arrays."""
+        if self._h is None:
+            raise ValueError("matrix already released")
+        _check(_load().ipcg_csr_get(self._h, None, None, _ptr(out)))
+        return out
 
     def free(self):
         if self._h:
@@ -690,9 +748,12 @@ class BarrierPotential:
     (src/ipc/potentials/barrier_potential.hpp:24-37); ClampedLogBarrier by
     default."""
 
-    def __init__(self, *args, use_physical_barrier: bool = False, mixed_precision: bool = False, **kw):
-        """``mixed_precision`` (no counterpart in the reference): face-vertex
-        contacts in FP32, everything else FP64 (IPCG_BARRIER_FP32_PT)."""
+    def __init__(self, *args, use_physical_barrier: bool = False, mixed_precision=False, **kw):
+        """``mixed_precision`` (no counterpart in the reference): False for
+        FP64 throughout; True or "pt" for face-vertex contacts in FP32
+        (IPCG_BARRIER_FP32_PT); "local" for every contact but near-parallel
+        edge-edge ones in FP32 (IPCG_BARRIER_FP32_LOCAL).  The PSD projection,
+        the mollifier and assembly stay FP64 in every mode."""
         args = list(args)
         barrier = kw.pop("barrier", None)
         if args and isinstance(args[0], Barrier):
@@ -709,11 +770,11 @@ class BarrierPotential:
         self.dhat = float(dhat)
         self.stiffness = float(stiffness)
         self.use_physical_barrier = bool(vals["use_physical_barrier"])
-        self.mixed_precision = bool(mixed_precision)
+        self.mixed_precision = mixed_precision
 
     @property
     def _options(self):
-        return (int(self.use_physical_barrier) | (2 if self.mixed_precision else 0)
+        return (int(self.use_physical_barrier) | _precision_bits(self.mixed_precision)
                 | (int(self.barrier.kind) << 4))
 
     def shape_derivative(self, collisions: NormalCollisions, mesh: CollisionMesh, vertices):
@@ -723,7 +784,7 @@ class BarrierPotential:
         V = _as_f64(vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_shape_derivative(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
-                                                     self._options & ~2, C.byref(h)))
+                                                     self._options & ~6, C.byref(h)))
         A = _csr_to_scipy(h, 3 * mesh.num_vertices)  # CSC view of the CSR arrays = transpose
         return sp.csr_matrix((A.data, A.indices, A.indptr), shape=A.shape)
 
@@ -817,14 +878,27 @@ class BarrierPotential:
 class BatchBarrierPotential:
     """BarrierPotential with one dhat and one stiffness per scene of a
     SceneBatch.  Energies come back per scene; the gradient and Hessian are
-    the packed ones (block diagonal over scenes)."""
+    the packed ones (block diagonal over scenes).  ``mixed_precision`` as for
+    BarrierPotential."""
 
-    def __init__(self, dhat, stiffness, use_physical_barrier: bool = False):
+    def __init__(self, dhat, stiffness, use_physical_barrier: bool = False, mixed_precision=False):
         self.dhat = np.asarray(dhat, np.float64)
         self.stiffness = np.asarray(stiffness, np.float64)
         if not np.all(self.dhat > 0):
             raise ValueError("dhat must be positive")
         self.use_physical_barrier = bool(use_physical_barrier)
+        self.mixed_precision = mixed_precision
+
+    @property
+    def _options(self):
+        return int(self.use_physical_barrier) | _precision_bits(self.mixed_precision)
+
+    def autotune(self, collisions, batch, vertices, project_hessian_to_psd=None) -> dict:
+        """Time the fused energy / gradient / Hessian kernel's launch shapes on
+        this set and keep the fastest for the device (ipcg_barrier_autotune)."""
+        psd = PSDProjectionMethod.CLAMP if project_hessian_to_psd is None else project_hessian_to_psd
+        return autotune_barrier(collisions, batch, vertices, batch.per_scene(self.dhat),
+                                batch.per_scene(self.stiffness), self._options, psd)
 
     def evaluate(self, collisions: NormalCollisions, batch: SceneBatch, vertices, energy=True, gradient=False,
                  hessian=False, project_hessian_to_psd=PSDProjectionMethod.NONE, device=False):
@@ -842,7 +916,7 @@ class BatchBarrierPotential:
                 g = np.zeros(3 * batch.num_vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_batch(collisions._h, batch._h, _ptr(V), _ptr(dh), _ptr(kap),
-                                          int(self.use_physical_barrier), int(project_hessian_to_psd), _ptr(e),
+                                          self._options, int(project_hessian_to_psd), _ptr(e),
                                           _ptr(g), C.byref(h) if hessian else None))
         H = None
         if hessian:
@@ -1228,46 +1302,36 @@ class Candidates:
         return float(out[0])
 
 
-def _clamped_log_barrier_second_derivative(d, dhat):
-    """barrier.cpp:31-43 (on squared distances)."""
-    if d <= 0.0 or d >= dhat:
-        return 0.0
-    r = dhat / d
-    return (r + 2) * r - 2 * np.log(d / dhat) - 3
-
-
 def initial_barrier_stiffness(bbox_diagonal: float, dhat: float, average_mass: float, grad_energy, grad_barrier,
-                              min_barrier_stiffness_scale: float = 1e11, dmin: float = 0.0):
-    """barrier/adaptive_stiffness.cpp:12-48 with the default ClampedLogBarrier:
+                              min_barrier_stiffness_scale: float = 1e11, dmin: float = 0.0, barrier=None):
+    """barrier/adaptive_stiffness.cpp:12-48 (ipcg_initial_barrier_stiffness):
     returns (kappa, max_barrier_stiffness).  The gradients may be numpy
-    arrays or CUDA tensors (their two dot products run where they live)."""
-    if not (average_mass > 0 and min_barrier_stiffness_scale > 0 and bbox_diagonal > 0):
-        raise ValueError("average_mass, min_barrier_stiffness_scale and bbox_diagonal must be positive")
-    dhat2, dmin2 = dhat * dhat, dmin * dmin
-    d0 = 1e-8 * bbox_diagonal + dmin
-    d0 *= d0
-    if d0 - dmin2 >= 2 * dmin * dhat + dhat2:
-        d0 = dmin * dhat + 0.5 * dhat2
-    kmin = 4 * d0 * _clamped_log_barrier_second_derivative(d0 - dmin2, 2 * dmin * dhat + dhat2)
-    kmin = min_barrier_stiffness_scale * average_mass / kmin
-    kmax = 100 * kmin
-    gb2 = float((grad_barrier * grad_barrier).sum())
-    kappa = 1.0
-    if gb2 > 0:
-        kappa = -float((grad_barrier * grad_energy).sum()) / gb2
-    return min(max(kappa, kmin), kmax), kmax
+    arrays or CUDA tensors (the two dot products run where they live);
+    ``barrier`` defaults to ClampedLogBarrier."""
+    ge, gb = _as_f64_vec(grad_energy), _as_f64_vec(grad_barrier)
+    n = int(ge.shape[0])
+    if int(gb.shape[0]) != n:
+        raise ValueError("grad_energy and grad_barrier must have the same size")
+    kind = 0 if barrier is None else int(barrier.kind)
+    k, kmax = C.c_double(), C.c_double()
+    _check(_load().ipcg_initial_barrier_stiffness(float(bbox_diagonal), kind, float(dhat), float(average_mass),
+                                                  _ptr(ge), _ptr(gb), n, float(min_barrier_stiffness_scale),
+                                                  float(dmin), C.byref(k), C.byref(kmax)))
+    return k.value, kmax.value
 
 
 def update_barrier_stiffness(prev_min_distance: float, min_distance: float, max_barrier_stiffness: float,
                              barrier_stiffness: float, bbox_diagonal: float, dhat_epsilon_scale: float = 1e-9,
                              dmin: float = 0.0) -> float:
-    """barrier/adaptive_stiffness.cpp:51-68: double the stiffness (up to the
-    maximum) while the minimum distance keeps shrinking below
-    (dhat_epsilon_scale (bbox_diagonal + dmin))^2."""
-    eps = (dhat_epsilon_scale * (bbox_diagonal + dmin)) ** 2
-    if prev_min_distance < eps and min_distance < eps and min_distance < prev_min_distance:
-        return min(max_barrier_stiffness, 2 * barrier_stiffness)
-    return barrier_stiffness
+    """barrier/adaptive_stiffness.cpp:51-68 (ipcg_update_barrier_stiffness):
+    double the stiffness (up to the maximum) while the minimum distance keeps
+    shrinking below (dhat_epsilon_scale (bbox_diagonal + dmin))^2."""
+    out = C.c_double()
+    _check(_load().ipcg_update_barrier_stiffness(float(prev_min_distance), float(min_distance),
+                                                 float(max_barrier_stiffness), float(barrier_stiffness),
+                                                 float(bbox_diagonal), float(dhat_epsilon_scale), float(dmin),
+                                                 C.byref(out)))
+    return out.value
 
 
 def is_step_collision_free(mesh: CollisionMesh, vertices_t0, vertices_t1, min_distance: float = 0.0,

@@ -43,7 +43,7 @@ def test_codim_vertices_are_refused(ipctk):
     with pytest.raises(ValueError, match="codimensional vertices"):
         ipctk.is_step_collision_free(mesh, V, V1)
     with pytest.raises(ValueError, match="codimensional vertices"):
-        ipctk.Candidates().build(mesh, V, 1e-3)
+        ipctk.Candidates().build(mesh, V, inflation_radius=1e-3)
 
 
 def test_free_edge_only_is_supported(ipctk, oracle_mod):
