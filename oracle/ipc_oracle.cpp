@@ -3254,6 +3254,42 @@ void orc_csr_free(void* h) { delete (CSR*)h; }
 
 // Local (stencil) Hessian of one contact for kernel-level tests.
 // type: 0 VV,1 EV,2 EE,3 FV; x: stencil positions (3n)
+// Edge-edge cross product norm and mollifier (edge_edge_mollifier.cpp:7-14,
+// 42-136, 194-202): x = (ea0, ea1, eb0, eb1) rows.  s = |ea x eb|^2 with its
+// gradient (12) and Hessian (144); the threshold 1e-3 |ea|^2 |eb|^2; the
+// mollifier m (1 when s >= eps) with its gradient and Hessian (zero when
+// inactive).
+double orc_ee_cross_sqnorm(const double* x, double* g, double* H)
+{
+    double gr[6], Hr[6][6];
+    const double s = cross_sq(sub(row(x, 1), row(x, 0)), sub(row(x, 3), row(x, 2)), gr, Hr);
+    Reduced R { 2, { 1, 3, 0 }, { 0, 2, 0 } };
+    double Hs[144];
+    expand(R, 4, gr, &Hr[0][0], 6, g, Hs);
+    if (H)
+        for (int i = 0; i < 144; ++i) H[i] = Hs[i];
+    return s;
+}
+double orc_ee_mollifier_threshold(const double* x)
+{
+    return ee_mollifier_threshold(row(x, 0), row(x, 1), row(x, 2), row(x, 3));
+}
+double orc_ee_mollifier(const double* x, double eps, double* g, double* H)
+{
+    Contact c {};
+    c.type = CT_EE;
+    c.n = 4;
+    c.eps = eps;
+    V3 v[4];
+    for (int i = 0; i < 4; ++i) v[i] = row(x, i);
+    bool act = false;
+    double gm[12], Hm[144];
+    const double m = mollifier(c, v, gm, Hm, act);
+    for (int i = 0; i < 12; ++i) g[i] = act ? gm[i] : 0.0;
+    for (int i = 0; i < 144; ++i) H[i] = act ? Hm[i] : 0.0;
+    return m;
+}
+
 void orc_contact_local(int type, int dtype, double eps, double w, const double* x, double dhat, double kappa,
     double dmin, int physical, int psd, double* energy, double* grad, double* hess)
 {

@@ -72,6 +72,12 @@ def lib():
         L.orc_csr_get.argtypes = [vp, P, P, P]
         L.orc_csr_free.argtypes = [vp]
         L.orc_contact_local.argtypes = [i32, i32, d, d, P, d, d, d, i32, i32, P, P, P]
+        L.orc_ee_cross_sqnorm.restype = d
+        L.orc_ee_cross_sqnorm.argtypes = [P, P, P]
+        L.orc_ee_mollifier_threshold.restype = d
+        L.orc_ee_mollifier_threshold.argtypes = [P]
+        L.orc_ee_mollifier.restype = d
+        L.orc_ee_mollifier.argtypes = [P, d, P, P]
         L.orc_point_triangle_ccd.restype = i32
         L.orc_point_triangle_ccd.argtypes = [P, P, d, d, d, C.c_long, d, P]
         L.orc_edge_edge_ccd.restype = i32
@@ -176,6 +182,26 @@ def contact_local(ctype, x, dhat, kappa, dmin=0.0, physical=False, psd="none", w
     H = np.zeros((n, n))
     lib().orc_contact_local(ctype, dtype, eps, w, _p(x), dhat, kappa, dmin, int(physical), PSD[psd], _p(e), _p(g), _p(H))
     return e[0], g, H
+
+
+def ee_cross_sqnorm(x):
+    """|ea x eb|^2 of x = (ea0, ea1, eb0, eb1) with its gradient and Hessian."""
+    x = _f64(x).reshape(4, 3)
+    g, H = np.zeros(12), np.zeros((12, 12))
+    s = lib().orc_ee_cross_sqnorm(_p(x), _p(g), _p(H))
+    return s, g, H
+
+
+def ee_mollifier_threshold(x_rest):
+    return lib().orc_ee_mollifier_threshold(_p(_f64(x_rest).reshape(4, 3)))
+
+
+def ee_mollifier(x, eps_x):
+    """Edge-edge mollifier m(x) with its gradient and Hessian."""
+    x = _f64(x).reshape(4, 3)
+    g, H = np.zeros(12), np.zeros((12, 12))
+    m = lib().orc_ee_mollifier(_p(x), float(eps_x), _p(g), _p(H))
+    return m, g, H
 
 
 def faces_to_edges(F, E):

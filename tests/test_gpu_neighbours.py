@@ -104,3 +104,17 @@ def test_free_distance_functions(ipctk, oracle_mod):
     assert np.all(d == [oracle_mod.point_triangle_distance(*x) for x in X])
     with pytest.raises(ValueError):
         ipctk.point_triangle_distance(*X[0], dtype=ipctk.PointTriangleDistanceType.P_T0)
+
+
+def test_initial_barrier_stiffness_device_vectors(ipctk):
+    """The dot products of initial_barrier_stiffness run on the device when
+    the gradients live there, and agree with the host path."""
+    import torch
+    rng = np.random.default_rng(51)
+    gE = rng.normal(size=300_000)
+    gB = rng.normal(size=300_000)
+    host = ipctk.initial_barrier_stiffness(2.0, 1e-3, 0.5, gE, gB, min_barrier_stiffness_scale=1e3)
+    dev = ipctk.initial_barrier_stiffness(2.0, 1e-3, 0.5, torch.from_numpy(gE).cuda(), torch.from_numpy(gB).cuda(),
+                                          min_barrier_stiffness_scale=1e3)
+    assert dev[1] == host[1]
+    assert abs(dev[0] - host[0]) <= 1e-12 * abs(host[0])

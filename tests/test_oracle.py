@@ -879,3 +879,84 @@ def test_area_weighted_shape_derivative_weight_term_fd(oracle_mod):
         fd = (g(V + d.reshape(V.shape)) - g(V - d.reshape(V.shape))) / (2 * h)
         wj = W[:, j].toarray().ravel()
         assert np.linalg.norm(fd - wj) <= 1e-5 * np.linalg.norm(wj) + 1e-9 * abs(W).max()
+
+
+# --- edge-edge mollifier (distance/test_edge_edge_mollifier.cpp:14-292) --------
+
+def _mollifier_edges(which):
+    # get_edges(): "Perp" and "Almost parallel" (test_edge_edge_mollifier.cpp:14-38)
+    if which == "perp":
+        return np.array([[-1, 0, 0], [1, 0, 0], [0, -1, 0], [0, 1, 0]], float)
+    return np.array([[-1, 0, 0], [1, 0, 0], [-1, 1e-9, 0], [1, -1e-9, 0]], float)
+
+
+@pytest.mark.parametrize("which", ["perp", "almost_parallel"])
+def test_ee_cross_squarednorm_kat_and_fd(oracle_mod, which):
+    """Edge-Edge Cross Squarednorm (test_edge_edge_mollifier.cpp:40-80):
+    16 for the perpendicular pair, 0 (margin 1e-9) for the almost parallel
+    one; gradient and Hessian against finite differences."""
+    x = _mollifier_edges(which)
+    s, g, H = oracle_mod.ee_cross_sqnorm(x)
+    if which == "perp":
+        assert s == pytest.approx(16)
+    else:
+        assert abs(s) <= 1e-9
+    f = lambda y: oracle_mod.ee_cross_sqnorm(y)[0]
+    fg = _fd(f, x.ravel(), 1e-6)
+    assert np.linalg.norm(g - fg) <= 1e-6 * max(1.0, np.linalg.norm(fg))
+    fH = np.stack([_fd(lambda y: oracle_mod.ee_cross_sqnorm(y)[1][i], x.ravel(), 1e-6) for i in range(12)])
+    assert np.linalg.norm(H - fH) <= 1e-5 * max(1.0, np.linalg.norm(fH))
+
+
+@pytest.mark.parametrize("rel_x", [0.0, 0.5, 1.0, 2.0])
+@pytest.mark.parametrize("eps_x", [1e-3, 1e-1, 1.0, 2.0])
+def test_ee_mollifier_scalar(oracle_mod, rel_x, eps_x):
+    """Edge-Edge Mollifier Scalar (test_edge_edge_mollifier.cpp:82-157):
+    m in [0, 1], m = 1 beyond eps_x, and dm/dx against finite differences.
+    The scalar is read through edges whose cross norm squared is x: ea along
+    x with length 2, eb = (2 cos t, 2 sin t, 0) with 16 sin^2 t = x."""
+    x = rel_x * eps_x
+
+    def edges(xv):
+        st = np.sqrt(min(xv / 16.0, 1.0))
+        ct = np.sqrt(1.0 - st * st)
+        return np.array([[-1, 0, 0], [1, 0, 0], [0, 0, 0.5], [2 * ct, 2 * st, 0.5]], float)
+
+    m = oracle_mod.ee_mollifier(edges(x), eps_x)[0]
+    assert 0 <= m <= 1
+    if x > eps_x:
+        assert m == 1
+    # the closed form (edge_edge_mollifier.cpp:42-60) on the cross norm the edges really have
+    s = oracle_mod.ee_cross_sqnorm(edges(x))[0]
+    expect = 1.0 if s >= eps_x else (-s / eps_x + 2) * (s / eps_x)
+    assert m == pytest.approx(expect, rel=1e-12, abs=1e-15)
+    if abs(x - eps_x) > 1e-6 and 1e-4 < x < eps_x:
+        h = 1e-8 * eps_x
+        fd = (oracle_mod.ee_mollifier(edges(x + h), eps_x)[0] - oracle_mod.ee_mollifier(edges(x - h), eps_x)[0]) / (2 * h)
+        assert fd == pytest.approx(2 / eps_x * (1 - x / eps_x), rel=1e-4)
+
+
+@pytest.mark.parametrize("which", ["perp", "almost_parallel"])
+def test_ee_mollifier_kat_and_fd(oracle_mod, which):
+    """Edge-Edge Mollifier (test_edge_edge_mollifier.cpp:159-266) with rest
+    edges along x and y (eps_x = 1e-3): m in [0, 1] (1 for the perpendicular
+    pair, 0 for the parallel one), gradient and Hessian against finite
+    differences."""
+    rest = np.array([[0, 0, 0], [1, 0, 0], [0, 0, 0], [0, 1, 0]], float)
+    eps = oracle_mod.ee_mollifier_threshold(rest)
+    assert eps == pytest.approx(1e-3)
+    x = _mollifier_edges(which)
+    m, g, H = oracle_mod.ee_mollifier(x, eps)
+    assert 0 <= m <= 1
+    assert m == (1.0 if which == "perp" else pytest.approx(0.0, abs=1e-12))
+    f = lambda y: oracle_mod.ee_mollifier(y, eps)[0]
+    fg = _fd(f, x.ravel(), 1e-7)
+    assert np.linalg.norm(g - fg) <= 1e-5 * max(1.0, np.linalg.norm(fg))
+    fH = np.stack([_fd(lambda y: oracle_mod.ee_mollifier(y, eps)[1][i], x.ravel(), 1e-7) for i in range(12)])
+    assert np.linalg.norm(H - fH) <= 1e-4 * max(1.0, np.linalg.norm(fH))
+
+
+def test_ee_mollifier_threshold_kat(oracle_mod):
+    """Edge-Edge Mollifier Threshold (test_edge_edge_mollifier.cpp:268-292):
+    the perpendicular pair's eps_x is 1e-3 * 4 * 4 = 0.016."""
+    assert oracle_mod.ee_mollifier_threshold(_mollifier_edges("perp")) == pytest.approx(0.016)
