@@ -1,24 +1,32 @@
 #!/usr/bin/env python
 """Benchmark of the contact hot path on GB300.
 
-Workload (N=1): the sphere pack of 512 icospheres (642 vertices and 1280
-triangles each; 328,704 vertices) on a jittered 8x8x8 lattice with gaps
-U(0.1e-3, 1.5e-3), dhat = 1e-3, stiffness 1e4 -- seeded synthetic data
-(numpy PCG64, seed 1).  One step = BarrierPotential energy + gradient +
-PSD-projected (CLAMP) Hessian with CSR assembly over the prebuilt collision
-set, exactly the three reference calls of one Newton iteration.
+Workload (N=1): the 256-scene batch -- 256 uneven two-sheet scenes (grid side
+log-uniform in [16, 256], 5,911,266 vertices in all; per-scene dhat
+log-uniform in [1e-4, 1e-2], gap U(0.2, 0.9) dhat, stiffness 1e4) --
+seeded synthetic data (numpy PCG64, seed 3).  One step = BarrierPotential
+energy + gradient + PSD-projected (CLAMP) Hessian with CSR assembly of every
+scene over the prebuilt collision sets (76.6 M contacts), in one batched call
+(SceneBatch, mixed FP32/FP64: every contact but near-parallel edge-edge ones
+computes its distance derivatives in FP32; the PSD eigen-projection, the
+mollifier and assembly are FP64), replayed as one CUDA graph.
 
-    value   contacts/s with positions resident in HBM (device pointers)
-    e2e     the same work through the public API with host buffers (one fused call):
-            positions copied in, energy / gradient / CSR Hessian copied out
-            inside the timed region
-    roofline  the dominant kernel's algorithmic bytes per launch over its
-            average launch time (CUDA events on the launching stream)
-    cpu_baseline  the CPU restatement timed on this host's cores
+    value   contacts/s of the batched call, positions resident in HBM
+    e2e     the same call through the public API with host positions (pinned)
+            copied in and the per-scene energies and the gradient copied out
+            every step; the Hessian stays on the device (DeviceCSR)
+    plain   the same work as the reference is used: one CollisionMesh and
+            one FP64 energy + gradient + Hessian call per scene
+    roofline  the dominant kernel's FP64 rate (ncu flop count per launch over
+            its CUDA-event launch time) against the measured cuBLAS DGEMM
+            rate, and its algorithmic HBM bytes per launch against the
+            measured copy bandwidth
+    cpu_baseline  the CPU restatement (oracle/) on this host's cores, on a
+            bounded sample of the same scenes
 
 --impl reference times the reference algorithm on the host cores (the CPU
 restatement under oracle/, since the reference itself cannot be built here)
-and prints the same line with "impl": "reference".
+on that sample and prints the same line with "impl": "reference".
 """
 from __future__ import annotations
 
@@ -45,13 +53,37 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["sphere_pack", "two_sheet", "layered_cloth"], default="sphere_pack")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-batch", action="store_true", help="skip the 256-scene batched-vs-plain leg")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="skip the legs beside the headline (served, layered cloth, friction, sphere pack)")
     return ap.parse_args()
+
+
+BATCH_DESC = ("256 uneven two-sheet scenes (5,911,266 verts; side log-uniform [16, 256], dhat log-uniform "
+              "[1e-4, 1e-2], gap U(0.2, 0.9) dhat, stiffness 1e4; seed 3)")
+BATCH_CONTACTS = 76_649_164  # merged collisions of the batch (oracle and GPU agree)
+
+
+def batch_config(contacts=BATCH_CONTACTS):
+    """The config dict both arms print (same keys, same workload)."""
+    return {"workload": BATCH_DESC, "contacts": contacts, "psd": "clamp", "scenes": 256,
+            "l2": "inputs larger than L2 (5.9 M vertices; ~80 GB of Hessian slots per step)",
+            "parallelism": "single"}
+
+
+def cpu_sample(scs, vertex_budget=40_000):
+    """A bounded, deterministic sample of the batch for the CPU arms: every
+    8th scene (by index) whose vertex count fits the running budget."""
+    out, tot = [], 0
+    for k in range(0, len(scs), 8):
+        nv = scs[k]["V"].shape[0]
+        if tot + nv <= vertex_budget:
+            out.append(k)
+            tot += nv
+    return out
 
 
 def make_scene(name):
@@ -212,22 +244,23 @@ def ncu_counts(kernel, workload):
         return {}
 
 
-def cpu_baseline_run(sc, steps, budget_s=20.0, warmup=0):
+def cpu_baseline_run(scenes_list, steps, budget_s=20.0, warmup=0, desc=None):
     """Time the CPU restatement (oracle/) on this host: E + grad + PSD Hessian
-    with CSR assembly over the collision set, all host threads, after
-    `warmup` untimed passes."""
+    with CSR assembly over each scene's prebuilt collision set, all host
+    threads, after `warmup` untimed passes.  One pass = every scene once."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    V, E, F = sc["V"], sc["E"], sc["F"]
     nt = os.cpu_count() or 1
-    col = oracle.build_collisions(V, E, F, sc["dhat"], nthreads=nt)
-    C = len(col)
+    built = [(sc, oracle.build_collisions(sc["V"], sc["E"], sc["F"], sc["dhat"], nthreads=nt)) for sc in scenes_list]
+    C = sum(len(col) for _, col in built)
 
     def one_pass():
-        oracle.barrier_energy(col, V, E, F, sc["dhat"], sc["kappa"], nthreads=nt)
-        oracle.barrier_gradient(col, V, E, F, sc["dhat"], sc["kappa"], nthreads=nt)
-        oracle.barrier_hessian(col, V, E, F, sc["dhat"], sc["kappa"], psd="clamp", nthreads=nt)
+        for sc, col in built:
+            V, E, F = sc["V"], sc["E"], sc["F"]
+            oracle.barrier_energy(col, V, E, F, sc["dhat"], sc["kappa"], nthreads=nt)
+            oracle.barrier_gradient(col, V, E, F, sc["dhat"], sc["kappa"], nthreads=nt)
+            oracle.barrier_hessian(col, V, E, F, sc["dhat"], sc["kappa"], psd="clamp", nthreads=nt)
 
     for _ in range(warmup):
         one_pass()
@@ -240,8 +273,9 @@ def cpu_baseline_run(sc, steps, budget_s=20.0, warmup=0):
         if time.perf_counter() - t_start > budget_s:
             break
     med = statistics.median(times)
+    sample = desc or f"{len(scenes_list)} scenes"
     return {"value": C / med, "unit": UNIT, "cores": nt, "kind": "port",
-            "sample": f"full collision set ({C} contacts), {len(times)} passes, median"}, C, times
+            "sample": f"{sample}: {C} contacts per pass, {len(times)} passes, median"}, C, times
 
 
 def ccd_baseline_run(sc, budget_s=20.0):
@@ -267,130 +301,95 @@ def ccd_baseline_run(sc, budget_s=20.0):
 def run_reference(args, rank):
     if rank != 0:
         return
-    sc, desc = make_scene(args.workload)
-    # each pass is the whole collision set; the timed passes stop after 120 s
+    from ipctk_gb300 import scenes
+    scs = scenes.batch()
+    idx = cpu_sample(scs)
+    desc = f"scenes {idx} of the 256-scene batch"
     warm = max(0, args.warmup)
-    base, C, times = cpu_baseline_run(sc, args.steps, budget_s=120.0, warmup=warm)
+    # each step is one pass over the sample; the timed passes stop after 120 s
+    base, C, times = cpu_baseline_run([scs[k] for k in idx], args.steps, budget_s=120.0, warmup=min(warm, 1),
+                                      desc=desc)
     ms = 1000 * statistics.median(times)
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": len(times), "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded numpy PCG64 scene)",
-            "config": {"workload": desc, "contacts": C, "psd": "clamp"},
+            "data": "synthetic (seeded numpy PCG64 scenes; the reference publishes no dataset for this path)",
+            "config": batch_config(),
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def batch_leg(dev, warmup=1, steps=3):
-    """The 256-scene batch (uneven two-sheet scenes, side log-uniform in
-    [16, 256], per-scene dhat log-uniform in [1e-4, 1e-2]; seed 3): one step
-    is E + grad + CLAMP Hessian of every scene, and one CCD step is the
-    collision-free step of every scene.  "plain" runs the single-scene API
-    once per scene (one CollisionMesh each, as the reference is used);
-    "batched" runs each of the three calls once over a SceneBatch.  The plain
-    objects are released before the batched ones are made (the two sets of
-    device scratch do not fit together)."""
+def timed_host(fn, n_warm, n_steps):
+    """Wall-clock ms of n_steps calls of fn (each ends synchronised)."""
+    import torch
+    for _ in range(n_warm):
+        fn()
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(n_steps):
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        out.append(1000 * (time.perf_counter() - t0))
+    return out
+
+
+def plain_leg(dev, scs, warmup=1, steps=2):
+    """The plain FP64 form on the batch, as the reference is used: one
+    CollisionMesh, one collision set and one fused FP64 energy + gradient +
+    CLAMP Hessian call per scene (device-resident positions), then one
+    compute_collision_free_stepsize per scene."""
     import gc
     import torch
     import ipctk_gb300 as ipctk
-    from ipctk_gb300 import scenes
-    scs = scenes.batch()
     CLAMP = ipctk.PSDProjectionMethod.CLAMP
-    nverts = sum(s["V"].shape[0] for s in scs)
-    pct = lambda a, q: float(np.percentile(np.array(a), q))
-
-    def timed(fn, n_warm, n_steps):
-        for _ in range(n_warm):
-            fn()
-        torch.cuda.synchronize()
-        out = []
-        for _ in range(n_steps):
-            t0 = time.perf_counter()
-            fn()
-            torch.cuda.synchronize()
-            out.append(1000 * (time.perf_counter() - t0))
-        return out
-
-    # plain: one mesh per scene
     plain = []
     for s in scs:
         m = ipctk.CollisionMesh(s["V"], s["E"], s["F"])
         Vd = torch.from_numpy(s["V"]).to(dev)
         V1d = torch.from_numpy(s["V1"]).to(dev)
         c = ipctk.NormalCollisions()
+        c.build(m, Vd, s["dhat"])
         plain.append((s, m, Vd, V1d, c, ipctk.BarrierPotential(s["dhat"], s["kappa"])))
-
-    def plain_build():
-        for s, m, Vd, V1d, c, B in plain:
-            c.build(m, Vd, s["dhat"])
-
-    def plain_egh():
-        for s, m, Vd, V1d, c, B in plain:
-            B(c, m, Vd)
-            B.gradient(c, m, Vd)
-            B.hessian_device(c, m, Vd, CLAMP).free()
-
-    def plain_ccd():
-        return [ipctk.compute_collision_free_stepsize(m, Vd, V1d) for s, m, Vd, V1d, c, B in plain]
-
-    p_build = timed(plain_build, 1, 2)
     C = sum(len(p[4]) for p in plain)
+
+    def egh():
+        for s, m, Vd, V1d, c, B in plain:
+            B.energy_gradient_hessian_device(c, m, Vd, CLAMP)[2].free()
+
     l0 = ipctk.launch_count()
-    p_egh = timed(plain_egh, warmup, steps)
-    p_launch = (ipctk.launch_count() - l0) / (warmup + steps)
-    # one CCD pass per arm (the small-dhat scenes make a pass tens of seconds)
-    plain_steps = []
-    p_ccd = timed(lambda: plain_steps.append(plain_ccd()), 0, 1)
-    plain_steps = plain_steps[-1]
-    free_after_plain = torch.cuda.mem_get_info(dev)[0]
+    t = timed_host(egh, warmup, steps)
+    launches = (ipctk.launch_count() - l0) / (warmup + steps)
+    steps_out = []
+    t_ccd = timed_host(lambda: steps_out.append(
+        [ipctk.compute_collision_free_stepsize(m, Vd, V1d) for s, m, Vd, V1d, c, B in plain]), 0, 1)
     del plain
     gc.collect()
     torch.cuda.synchronize()
-
-    # batched: one packed mesh
-    batch = ipctk.SceneBatch([(s["V"], s["E"], s["F"]) for s in scs])
-    Vd = torch.from_numpy(batch.pack([s["V"] for s in scs])).to(dev)
-    V1d = torch.from_numpy(batch.pack([s["V1"] for s in scs])).to(dev)
-    dh = np.array([s["dhat"] for s in scs])
-    kap = np.array([s["kappa"] for s in scs])
-    col = ipctk.NormalCollisions()
-    BB = ipctk.BatchBarrierPotential(dh, kap)
-
-    def batch_egh():
-        BB(col, batch, Vd)
-        BB.gradient(col, batch, Vd)
-        BB.evaluate(col, batch, Vd, energy=False, hessian=True, project_hessian_to_psd=CLAMP, device=True)[2].free()
-
-    b_build = timed(lambda: col.build(batch, Vd, dh), 1, 2)
-    Cb = len(col)
-    l0 = ipctk.launch_count()
-    b_egh = timed(batch_egh, warmup, steps)
-    b_launch = (ipctk.launch_count() - l0) / (warmup + steps)
-    batch_steps = []
-    b_ccd = timed(lambda: batch_steps.append(ipctk.compute_collision_free_stepsize_batch(batch, Vd, V1d)), 0, 1)
-    batch_steps = batch_steps[-1]
-    free_after_batch = torch.cuda.mem_get_info(dev)[0]
-    del col, batch, Vd, V1d
-    gc.collect()
-    ns = len(scs)
     med = statistics.median
-    return {
-        "workload": f"{ns} uneven two-sheet scenes ({nverts:,} verts; side log-uniform [16, 256], dhat "
-                    "log-uniform [1e-4, 1e-2], gap U(0.2, 0.9) dhat; seed 3)",
-        "contacts": C, "contacts_equal": Cb == C,
-        "steps_equal": bool(np.array_equal(np.array(plain_steps), batch_steps)),
-        "egh": {"unit": UNIT, "warmup": warmup, "steps": steps,
-                "batched": {"value": C / (med(b_egh) / 1000.0), "p50_ms": pct(b_egh, 50), "p99_ms": pct(b_egh, 99),
-                            "launches_per_step": b_launch},
-                "plain": {"value": C / (med(p_egh) / 1000.0), "p50_ms": pct(p_egh, 50), "p99_ms": pct(p_egh, 99),
-                          "launches_per_step": p_launch}},
-        "ccd": {"unit": "scene-steps/s",
-                "batched": {"value": ns / (med(b_ccd) / 1000.0), "p50_ms": pct(b_ccd, 50)},
-                "plain": {"value": ns / (med(p_ccd) / 1000.0), "p50_ms": pct(p_ccd, 50)}},
-        "build_ms": {"batched": med(b_build), "plain": med(p_build)},
-        "free_gb_after": {"plain": free_after_plain / 1e9, "batched": free_after_batch / 1e9},
-    }
+    pct = lambda a, q: float(np.percentile(np.array(a), q))
+    return {"egh": {"value": C / (med(t) / 1000.0), "unit": UNIT, "p50_ms": pct(t, 50), "p99_ms": pct(t, 99),
+                    "steps": steps, "warmup": warmup, "launches_per_step": launches, "contacts": C,
+                    "precision": "fp64", "call": "BarrierPotential.energy_gradient_hessian_device per scene"},
+            "ccd": {"value": len(scs) / (med(t_ccd) / 1000.0), "unit": "scene-steps/s", "p50_ms": pct(t_ccd, 50)},
+            "steps": steps_out[-1]}
+
+
+def ccd_leg(dev, steps=5):
+    """Config 0's step size (two 64x64 sheets, 8,192 verts): the GPU call with
+    device positions, and the CPU restatement on all host threads."""
+    import torch
+    import ipctk_gb300 as ipctk
+    sc, desc = make_scene("two_sheet")
+    mesh = ipctk.CollisionMesh(sc["V"], sc["E"], sc["F"])
+    Vd = torch.from_numpy(sc["V"]).to(dev)
+    V1d = torch.from_numpy(sc["V1"]).to(dev)
+    t = timed_host(lambda: ipctk.compute_collision_free_stepsize(mesh, Vd, V1d), 2, steps)
+    step = ipctk.compute_collision_free_stepsize(mesh, Vd, V1d)
+    cpu = ccd_baseline_run(sc)
+    return {"workload": desc, "gpu_ms": statistics.median(t), "steps_per_s": 1000.0 / statistics.median(t),
+            "step_size": step, "cpu_baseline": cpu, "step_equal_cpu": cpu["step_size"] == step}
 
 
 def mixed_leg(dev, warmup=2, steps=5):
@@ -533,53 +532,94 @@ def served_leg(dev, seed=4):
             "resident_gb": st["resident_bytes"] / 1e9, "workspace_releases": st["releases"]}
 
 
-def run_gb300(args, rank, world):
+def sphere_pack_leg(dev, steps=20):
+    """Config 1: the plain FP64 form on the 512-icosphere pack (31,066
+    contacts), one fused E + grad + CLAMP Hessian call per step, device
+    positions, L2 flushed between steps."""
     import torch
     import ipctk_gb300 as ipctk
+    sc, desc = make_scene("sphere_pack")
+    mesh = ipctk.CollisionMesh(sc["V"], sc["E"], sc["F"])
+    Vd = torch.from_numpy(sc["V"]).to(dev)
+    V1d = torch.from_numpy(sc["V1"]).to(dev)
+    col = ipctk.NormalCollisions()
+    col.build(mesh, Vd, sc["dhat"])
+    C = len(col)
+    B = ipctk.BarrierPotential(sc["dhat"], sc["kappa"])
+    CL = ipctk.PSDProjectionMethod.CLAMP
+    stream = torch.cuda.ExternalStream(mesh.stream, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(3):
+        B.energy_gradient_hessian_device(col, mesh, Vd, CL)[2].free()
+    per = []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        B.energy_gradient_hessian_device(col, mesh, Vd, CL)[2].free()
+        b.record(stream)
+        torch.cuda.synchronize()
+        per.append(a.elapsed_time(b))
+    ccd = timed_host(lambda: ipctk.compute_collision_free_stepsize(mesh, Vd, V1d), 1, 5)
+    build = timed_host(lambda: col.build(mesh, Vd, sc["dhat"]), 1, 5)
+    med = statistics.median(per)
+    return {"workload": desc, "contacts": C, "egh": {"value": C / (med / 1000.0), "unit": UNIT, "ms": med},
+            "ccd_ms": statistics.median(ccd), "collision_build_ms": statistics.median(build)}
+
+
+def run_gb300(args, rank, world):
+    import gc
+    import torch
+    import ipctk_gb300 as ipctk
+    from ipctk_gb300 import scenes
 
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    sc, desc = make_scene(args.workload)
-    V, E, F = sc["V"], sc["E"], sc["F"]
-    dhat, kappa = sc["dhat"], sc["kappa"]
-    mesh = ipctk.CollisionMesh(V, E, F)
-    Vd = torch.from_numpy(V).to(dev)
-    V1d = torch.from_numpy(sc["V1"]).to(dev)
+    # replicas: each rank takes its own batch (seed 3 + rank); rank 0's is the config's
+    scs = scenes.batch(seed=3 + rank)
+    CLAMP = ipctk.PSDProjectionMethod.CLAMP
+    batch = ipctk.SceneBatch([(s["V"], s["E"], s["F"]) for s in scs])
+    Vh_np = batch.pack([s["V"] for s in scs])
+    Vd = torch.from_numpy(Vh_np).to(dev)
+    Vh = torch.from_numpy(Vh_np).pin_memory()
+    dh = np.array([s["dhat"] for s in scs])
+    kap = np.array([s["kappa"] for s in scs])
     col = ipctk.NormalCollisions()
-    col.build(mesh, Vd, dhat)
+    t0 = time.perf_counter()
+    col.build(batch, Vd, dh)
+    torch.cuda.synchronize()
+    build_ms = 1000 * (time.perf_counter() - t0)
     counts = col.counts()
     C = int(counts[:4].sum())
-    B = ipctk.BarrierPotential(dhat, kappa)
-    CLAMP = ipctk.PSDProjectionMethod.CLAMP
-    ndof = 3 * V.shape[0]
-    stream = torch.cuda.ExternalStream(mesh.stream, device=dev)
-    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
-    grad_d = None
+    ndof = 3 * batch.num_vertices
+    BB = ipctk.BatchBarrierPotential(dh, kap, mixed_precision="local")
+    stream = torch.cuda.ExternalStream(batch.stream, device=dev)
 
     def step():
-        nonlocal grad_d
-        B(col, mesh, Vd)
-        grad_d = B.gradient(col, mesh, Vd)
-        H = B.hessian_device(col, mesh, Vd, CLAMP)
+        e, g, H = BB.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True,
+                              project_hessian_to_psd=CLAMP, device=True)
         nnz = H.nnz
         H.free()
         return nnz
 
+    t0 = time.perf_counter()
+    nnz = step()  # builds the cached pattern
+    first_ms = 1000 * (time.perf_counter() - t0)
+    tune = BB.autotune(col, batch, Vd, CLAMP)
     clocks = ClockSampler(local)
     clocks.start()  # before the warm-up, so the GPU is busy when the timed steps start
     for _ in range(max(3, args.warmup)):
-        nnz = step()
+        step()
     torch.cuda.synchronize()
     if world > 1:
         import torch.distributed as dist
         dist.barrier()
-    ipctk.profile_enable(True)
     launches0 = ipctk.launch_count()
     t_region = time.perf_counter()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for i in range(args.steps):
-        flush.zero_()  # L2 flush between timed steps (outside the events)
         torch.cuda.synchronize()
         ev[i][0].record(stream)
         step()
@@ -588,8 +628,6 @@ def run_gb300(args, rank, world):
     clocks.mark(t_region, time.perf_counter())
     launches = ipctk.launch_count() - launches0
     clk = clocks.stop()
-    prof = ipctk.profile_report()
-    ipctk.profile_enable(False)
     per = [a.elapsed_time(b) for a, b in ev]
     total_ms = sum(per)
     if world > 1:
@@ -601,134 +639,127 @@ def run_gb300(args, rank, world):
     ms_per_step = total_ms / args.steps
     value = world * C / (ms_per_step / 1000.0)
 
-    # roofline of the dominant kernel (largest accumulated time)
+    # per-kernel times from one profiled step (direct launches instead of the
+    # graph replay, so each kernel is bracketed by events on its stream)
+    ipctk.profile_enable(True)
+    step()
+    torch.cuda.synchronize()
+    prof = ipctk.profile_report()
+    ipctk.profile_enable(False)
     own = {k: v for k, v in prof.items() if k.startswith("k_")}
     top = max(own, key=lambda k: own[k]["ms"])
     top_ms = own[top]["ms"] / max(1, own[top]["launches"])
+    prof_total = sum(v["ms"] for v in own.values())
+    step_share = {k: round(v["ms"] / prof_total, 4) for k, v in sorted(own.items(), key=lambda kv: -kv[1]["ms"])}
     peak, peak_kind = measured_peaks()
-    if top == "k_psd":
-        abytes = psd_bytes(counts)
-    else:
-        abytes = algorithmic_bytes(counts, ndof)
-    achieved = abytes / (top_ms / 1000.0) / 1e9
-    nc = ncu_counts(top, args.workload)
-    roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": nc.get("dram_bytes"), "algorithmic_bytes": abytes,
-            "avg_launch_ms": top_ms, "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)"}
     fp64_peak = fp64_peak_tflops(dev)
+    nc = ncu_counts(top, "batch")
+    launches_top = own[top]["launches"]
+    # algorithmic bytes of the fused kernel per launch: the E+G+H bytes per
+    # contact over the contacts one launch processes (the batch over its
+    # chunks' launches)
+    abytes = algorithmic_bytes(counts, ndof) / max(1, launches_top)
+    achieved_gbs = abytes / (top_ms / 1000.0) / 1e9
+    roof = {"kernel": top, "avg_launch_ms": top_ms, "launches_per_step": launches_top,
+            "hbm": {"achieved": achieved_gbs, "peak": peak, "unit": "GB/s", "frac": achieved_gbs / peak,
+                    "algorithmic_bytes": abytes, "peak_source": f"{peak_kind} hbm_gbs (MEASURED_PEAKS.json)"},
+            "traffic": nc.get("dram_bytes"), "traffic_source": nc.get("source")}
     if nc.get("fp64_flops"):
         ach = nc["fp64_flops"] / (top_ms / 1000.0) / 1e12
-        roof["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
-                        "flops_per_launch": nc["fp64_flops"], "pipe_util_ncu": nc.get("fp64_pipe_pct"),
-                        "peak_source": "measured: cuBLAS DGEMM 4096^3 on this GPU"}
+        roof.update({"bound": "fp64", "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                     "flops_per_launch": nc["fp64_flops"], "fp64_pipe_util_ncu": nc.get("fp64_pipe_pct"),
+                     "peak_source": "measured: cuBLAS DGEMM 4096^3 on this GPU (MEASURED_PEAKS.json has no FP64 entry)"})
     else:
-        roof["fp64"] = {"peak_tflops": fp64_peak, "peak_source": "measured: cuBLAS DGEMM 4096^3 on this GPU"}
-    step_share = {k: round(v["ms"] / total_ms, 4) for k, v in sorted(own.items(), key=lambda kv: -kv[1]["ms"])}
+        roof.update({"bound": "hbm", "achieved": achieved_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": achieved_gbs / peak, "fp64_peak_tflops": fp64_peak})
 
-    # the same three quantities from the fused entry point (one pass, one copy-in)
-    fused = []
-    for i in range(3 + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e_, g_, Hd = B.energy_gradient_hessian_device(col, mesh, Vd, CLAMP)
-        Hd.free()
-        torch.cuda.synchronize()
-        if i >= 3:
-            fused.append(time.perf_counter() - t0)
-    fused_ms = 1000 * statistics.median(fused)
-
-    # end to end through the public API with pinned host positions and host
-    # (numpy / scipy) results: one fused energy + gradient + Hessian call per
-    # step (positions staged once); the three separate calls of the
-    # reference's API are timed beside it
-    Vh = torch.from_numpy(V).pin_memory().numpy()
+    # end to end through the public API: pinned host positions in, per-scene
+    # energies and the gradient out (host arrays) every step
+    e2e = []
     nw = max(2, args.warmup // 2)
-    e2e_times, sep_times = [], []
     for i in range(nw + args.steps):
         t0 = time.perf_counter()
-        e, g, H = B.energy_gradient_hessian(col, mesh, Vh, CLAMP)
+        e_h, g_h, H = BB.evaluate(col, batch, Vh.numpy(), energy=True, gradient=True, hessian=True,
+                                  project_hessian_to_psd=CLAMP, device=True)
+        H.free()
         if i >= nw:
-            e2e_times.append(time.perf_counter() - t0)
-    for i in range(nw + args.steps):
-        t0 = time.perf_counter()
-        e = B(col, mesh, Vh)
-        g = B.gradient(col, mesh, Vh)
-        H = B.hessian(col, mesh, Vh, CLAMP)
-        if i >= nw:
-            sep_times.append(time.perf_counter() - t0)
-    e2e_ms = 1000 * statistics.median(e2e_times)
-    sep_ms = 1000 * statistics.median(sep_times)
-    h2d = V.nbytes
-    d2h = 8 + g.nbytes + H.indptr.nbytes + H.indices.nbytes + H.data.nbytes
+            e2e.append(1000 * (time.perf_counter() - t0))
+    e2e_ms = statistics.median(e2e)
+    h2d = Vh_np.nbytes
+    d2h = 8 * len(scs) + 8 * ndof
 
-    # CCD and collision-set build (device-resident inputs)
-    ccd_ms, build_ms = [], []
-    for i in range(2 + max(3, args.steps // 4)):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        ipctk.compute_collision_free_stepsize(mesh, Vd, V1d)
-        t1 = time.perf_counter()
-        col.build(mesh, Vd, dhat)
-        t2 = time.perf_counter()
-        if i >= 2:
-            ccd_ms.append(1000 * (t1 - t0))
-            build_ms.append(1000 * (t2 - t1))
-    step_size = ipctk.compute_collision_free_stepsize(mesh, Vd, V1d)
-    ccd_candidates = ccd_candidate_count(ipctk, mesh, Vd, V1d)
-
+    # the batched form in FP64 (batching without mixed precision) and the
+    # mixed results' error against it
+    BB64 = ipctk.BatchBarrierPotential(dh, kap)
+    b64 = timed_host(lambda: BB64.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True,
+                                           project_hessian_to_psd=CLAMP, device=True)[2].free(), 1, 3)
+    e0, g0, H0 = BB64.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True, project_hessian_to_psd=CLAMP,
+                               device=True)
+    v0 = torch.empty(H0.nnz, dtype=torch.float64, device=dev)
+    H0.values_into(v0)
+    H0.free()
+    e1, g1, H1 = BB.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True, project_hessian_to_psd=CLAMP,
+                             device=True)
+    v1 = torch.empty(H1.nnz, dtype=torch.float64, device=dev)
+    H1.values_into(v1)
+    H1.free()
+    err = {"energy_max_scene": float(np.max(np.abs(e1 - e0) / np.abs(e0))),
+           "gradient": float(torch.linalg.norm(g1 - g0).item() / torch.linalg.norm(g0).item()),
+           "hessian": float(torch.linalg.norm(v1 - v0).item() / torch.linalg.norm(v0).item())}
+    del v0, v1, g0, g1
+    # batched CCD: one compute_collision_free_stepsize over every scene
+    V1d = torch.from_numpy(batch.pack([s["V1"] for s in scs])).to(dev)
+    b_steps = []
+    b_ccd = timed_host(lambda: b_steps.append(ipctk.compute_collision_free_stepsize_batch(batch, Vd, V1d)), 0, 1)
+    del col, batch, Vd, V1d, BB, BB64
+    gc.collect()
+    torch.cuda.synchronize()
     if rank != 0:
         return
-    batch = None
-    served = None
-    mixed = None
-    friction = None
-    if not args.no_batch:
-        del mesh, col, Vd, V1d, flush
-        batch = batch_leg(dev)
-        import gc
-        gc.collect()
-        served = served_leg(dev)
-        gc.collect()
-        mixed = mixed_leg(dev)
-        gc.collect()
-        friction = friction_leg(dev)
+    legs = {}
+    plain = plain_leg(dev, scs)
+    legs["plain"] = plain["egh"]
+    legs["ccd"] = {"unit": "scene-steps/s", "batched": {"value": len(scs) / (b_ccd[0] / 1000.0), "ms": b_ccd[0]},
+                   "plain": plain["ccd"], "steps_equal": bool(np.array_equal(np.array(plain["steps"]), b_steps[-1]))}
+    legs["collision_build_ms"] = build_ms
+    legs["first_call_ms"] = first_ms
+    if not args.no_legs:
+        for name, fn in (("two_sheet_ccd", ccd_leg), ("served", served_leg), ("layered_cloth_mixed", mixed_leg),
+                         ("friction", friction_leg), ("sphere_pack", sphere_pack_leg)):
+            gc.collect()
+            legs[name] = fn(dev)
     cpu = None
-    ccd_cpu = None
     if not args.no_cpu_baseline:
-        cpu, _, _ = cpu_baseline_run(sc, 3, budget_s=20.0, warmup=1)
-        ccd_cpu = ccd_baseline_run(sc)
+        idx = cpu_sample(scs)
+        cpu, _, _ = cpu_baseline_run([scs[k] for k in idx], 3, budget_s=20.0, warmup=1,
+                                     desc=f"scenes {idx} of the 256-scene batch")
     pct = lambda a, q: float(np.percentile(np.array(a), q))
+    cfg = batch_config(C)
+    cfg.update({"contacts_by_type": {"vv": int(counts[0]), "ev": int(counts[1]), "ee": int(counts[2]),
+                                     "fv": int(counts[3])}, "hessian_nnz": int(nnz),
+                "precision": "mixed: FP32 distance derivatives except near-parallel edge-edge; FP64 PSD, "
+                             "mollifier, assembly", "tuning": tune["chosen"]})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded numpy PCG64 scene; the reference publishes no dataset for this path)",
-        "config": {"workload": desc, "contacts": C, "contacts_by_type": {"vv": int(counts[0]), "ev": int(counts[1]),
-                   "ee": int(counts[2]), "fv": int(counts[3])}, "dhat": dhat, "stiffness": kappa,
-                   "psd": "clamp", "hessian_nnz": int(nnz), "l2": "flushed between steps (258 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single"},
+        "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic (seeded numpy PCG64 scenes; the reference publishes no dataset for this path)",
+        "config": cfg,
         "p50_ms": pct(per, 50), "p99_ms": pct(per, 99),
+        "batched_vs_plain": value / plain["egh"]["value"],
+        "batched_fp64": {"value": C / (statistics.median(b64) / 1000.0), "unit": UNIT,
+                         "ms": statistics.median(b64)},
+        "mixed_rel_error_vs_fp64": err,
         "roofline": roof, "kernel_share": step_share,
         "cpu_baseline": cpu,
         "e2e": {"value": C / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-                "call": "BarrierPotential.energy_gradient_hessian (one fused C-ABI call)"},
-        "e2e_separate_calls": {"value": C / (sep_ms / 1000.0), "unit": UNIT, "ms_per_step": sep_ms,
-                               "h2d_bytes_per_step": int(3 * V.nbytes), "d2h_bytes_per_step": int(d2h),
-                               "call": "energy, gradient and hessian calls (positions staged three times)"},
+                "call": "BatchBarrierPotential.evaluate with host positions; energies and gradient to host, "
+                        "Hessian kept on the device"},
         "gpu_launches": int(launches), "gpu_launches_per_step": launches / args.steps,
+        "graph_launches_per_step": 1,
         "clocks": clk,
-        "fused_egh": {"value": C / (fused_ms / 1000.0), "unit": UNIT, "ms_per_step": fused_ms},
-        "ccd": {"steps_per_s": 1000.0 / statistics.median(ccd_ms), "p50_ms": pct(ccd_ms, 50),
-                "p99_ms": pct(ccd_ms, 99), "step_size": step_size, "candidates": ccd_candidates,
-                "candidates_per_s": (ccd_candidates / (statistics.median(ccd_ms) / 1000.0)
-                                     if ccd_candidates else None),
-                "cpu_baseline": ccd_cpu},
-        "collision_build": {"p50_ms": pct(build_ms, 50), "p99_ms": pct(build_ms, 99)},
-        "batch": batch,
-        "served": served,
-        "mixed_precision": mixed,
-        "friction": friction,
+        "legs": legs,
     }
     print(json.dumps(line), flush=True)
 

@@ -75,7 +75,10 @@ def test_reference_arm_json_line():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"] == {"value": line["value"], "unit": "contacts/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
-    assert line["config"]["contacts"] == 31066
+    # the same config dict as the GPU arm: the 256-scene batch
+    assert line["config"] == load_bench().batch_config()
+    assert line["config"]["contacts"] == 76_649_164
+    assert "of the 256-scene batch" in line["cpu_baseline"]["sample"]
 
 
 def test_ccd_candidate_count_marshalling():
