@@ -113,10 +113,12 @@ int ipcg_mesh_sizes(const ipcg_mesh* mesh, int64_t sizes[3]);
  * codimensional vertices and edge-vertex candidates between codimensional
  * edges and codimensional vertices (candidates.cpp:66-116, 152-210).  Those
  * passes are not provided: collision-set builds, candidate builds and step-size
- * calls on a mesh with codimensional vertices fail with IPCG_ERR_INVALID
- * instead of returning an incomplete result.  Codimensional edges alone need
- * no extra pass (their contacts with surface vertices are edge-edge or
- * face-vertex candidates) and are supported. */
+ * calls on a mesh where they would find pairs -- two or more codimensional
+ * vertices, or one together with a codimensional edge -- fail with
+ * IPCG_ERR_INVALID instead of returning an incomplete result.  Codimensional
+ * edges alone, or a single codimensional vertex without them, need no extra
+ * pass (their contacts are edge-edge or face-vertex candidates) and are
+ * supported. */
 int ipcg_mesh_codim_counts(const ipcg_mesh* mesh, int64_t counts[2]);
 
 /* CollisionMesh::faces_to_edges() (collision_mesh.hpp:327-329): num_faces*3 */

@@ -158,11 +158,13 @@ void set_last_error(const std::string& msg) { g_last_error = msg; }
 
 void require_no_codim_vertices(const ipcg_mesh* m)
 {
-    if (m && m->n_codim_vertices > 0)
+    // the vertex-vertex pass pairs codimensional vertices (needs two), the
+    // edge-vertex pass pairs them with codimensional edges (needs one of each)
+    if (m && (m->n_codim_vertices >= 2 || (m->n_codim_vertices >= 1 && m->n_codim_edges >= 1)))
         throw Error(IPCG_ERR_INVALID,
-            "the mesh has " + std::to_string(m->n_codim_vertices)
-                + " codimensional vertices (vertices in no edge): their vertex-vertex and edge-vertex candidate "
-                  "passes are not provided");
+            "the mesh has " + std::to_string(m->n_codim_vertices) + " codimensional vertices (vertices in no edge) and "
+                + std::to_string(m->n_codim_edges)
+                + " codimensional edges: their vertex-vertex and edge-vertex candidate passes are not provided");
 }
 
 } // namespace ipcg

@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(PSD_BLOCK) k_psd(ContactsView cv, Slab hs,
     if (t >= count) return;
     const int64_t i = first + t;
     if (!proj[i]) return;
-    if (!project_psd(stencil_size(cv, i), SlabAcc { hs, i }, method)) atomicOr(fail, 1);
+    if (!project_psd<double>(stencil_size(cv, i), SlabAcc { hs, i }, method)) atomicOr(fail, 1);
 }
 
 // Contribution id j (position in the block-key list) -> contact, local

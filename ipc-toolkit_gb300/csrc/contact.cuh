@@ -12,6 +12,7 @@
 
 #include <cmath>
 
+#include "df64.cuh"
 #include "geom.cuh"
 #include "internal.cuh"
 
@@ -574,34 +575,80 @@ __device__ double mollifier(const Local& c, const V3* x, double* gm, double* Hm,
 // Only the negative eigenvectors are formed: q_i = Q_h G_1 ... G_R e_i,
 // replaying the recorded rotations on e_i, which costs a few hundred flops
 // per vector instead of updating all of Q at every rotation.
+// Arithmetic of the PSD solver: FP64 (the plain path), or df64 (pairs of
+// FP32, about 48 bits) with exact power-of-two rescaling so that FP32's
+// exponent range never clips a square.  in() reads an FP64 entry scaled by
+// 2^-sc, out() returns a df64 value scaled back to FP64.
+template <class T> struct PsdReal;
+template <> struct PsdReal<double> {
+    static constexpr bool rescale = false;
+    __device__ static double eps() { return 2.220446049250313e-16; }
+    __device__ static double tiny() { return 1e-300; }
+    __device__ static double in(double x, int) { return x; }
+    __device__ static double out(double x, int) { return x; }
+    template <class Acc> __device__ static int scale_of(const Acc&, int) { return 0; }
+};
+template <> struct PsdReal<dd> {
+    static constexpr bool rescale = true;
+    __device__ static dd eps() { return dd { 7.1e-15f, 0.f }; }
+    __device__ static dd tiny() { return dd { 1e-36f, 0.f }; }
+    __device__ static dd in(double x, int sc) { return dd_from_double(scalbn(x, -sc)); }
+    __device__ static double out(dd x, int sc) { return scalbn(dd_to_double(x), sc); }
+    // exponent of the largest |entry| (from the FP64 bit patterns, integer ops)
+    template <class Acc> __device__ static int scale_of(const Acc& hs, int N)
+    {
+        unsigned long long mx = 0;
+        for (int k = 0; k < N * N; ++k) {
+            const unsigned long long b = (unsigned long long)__double_as_longlong(hs(k)) & 0x7fffffffffffffffULL;
+            mx = b > mx ? b : mx;
+        }
+        return mx == 0 ? 0 : (int)(mx >> 52) - 1022;
+    }
+};
+
 constexpr int MAXR = 9;
 constexpr int MAXROT = 128; // recorded rotations; beyond, Q is accumulated
 
-__device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* d, double* Q, double* rc, double* rs,
-    int8_t* rk, int& nrot, double* htau)
+template <class T> __device__ bool sym_eig(int n, T* A /*MAXR*MAXR, full symmetric*/, T* d, T* Q, T* rc, T* rs,
+    int8_t* rk, int& nrot, T* htau)
 {
     // Householder tridiagonalisation; reflector k is I - htau[k] v v^T with
     // v[k+1..n) kept in A[k+1..n)[k], the column it annihilates (the updates
     // below touch only rows and columns past k)
-    double e[MAXR];
+    T e[MAXR];
     for (int k = 0; k + 2 < n; ++k) {
-        double sig = 0;
+        T sig = 0;
         for (int i = k + 2; i < n; ++i) sig += A[i * MAXR + k] * A[i * MAXR + k];
-        const double x0 = A[(k + 1) * MAXR + k];
+        T x0 = A[(k + 1) * MAXR + k];
         htau[k] = 0;
         if (sig == 0) {
             e[k] = x0;
             continue;
         }
-        const double nx = sqrt(x0 * x0 + sig);
-        const double alpha = (x0 >= 0) ? -nx : nx;
-        const double v0 = x0 - alpha;
+        // df64: the column is scaled by a power of two (exact) so that its
+        // squares stay inside FP32's exponent range; the reflector
+        // I - tau v v^T is unchanged and alpha is scaled back
+        int cex = 0;
+        if constexpr (PsdReal<T>::rescale) {
+            T amax = fabs(x0);
+            for (int i = k + 2; i < n; ++i) amax = dmax(amax, fabs(A[i * MAXR + k]));
+            cex = pow2_exp(amax);
+            x0 = scale2(x0, -cex);
+            sig = T(0);
+            for (int i = k + 2; i < n; ++i) {
+                A[i * MAXR + k] = scale2(A[i * MAXR + k], -cex);
+                sig += A[i * MAXR + k] * A[i * MAXR + k];
+            }
+        }
+        const T nx = sqrt(x0 * x0 + sig);
+        const T alpha = (x0 >= 0) ? -nx : nx;
+        const T v0 = x0 - alpha;
         A[(k + 1) * MAXR + k] = v0;
-        double p[MAXR];
-        const double tau = 2.0 / (v0 * v0 + sig);
-        double K = 0;
+        T p[MAXR];
+        const T tau = 2.0 / (v0 * v0 + sig);
+        T K = 0;
         for (int i = k + 1; i < n; ++i) {
-            double s = 0;
+            T s = 0;
             for (int j = k + 1; j < n; ++j) s += A[i * MAXR + j] * A[j * MAXR + k];
             p[i] = tau * s;
             K += p[i] * A[i * MAXR + k];
@@ -611,11 +658,12 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
         // the update is symmetric: form the upper triangle, mirror it
         for (int i = k + 1; i < n; ++i)
             for (int j = i; j < n; ++j) {
-                const double a = A[i * MAXR + j] - (A[i * MAXR + k] * p[j] + p[i] * A[j * MAXR + k]);
+                const T a = A[i * MAXR + j] - (A[i * MAXR + k] * p[j] + p[i] * A[j * MAXR + k]);
                 A[i * MAXR + j] = a;
                 A[j * MAXR + i] = a;
             }
-        e[k] = alpha;
+        if constexpr (PsdReal<T>::rescale) e[k] = scale2(alpha, cex);
+        else e[k] = alpha;
         htau[k] = tau;
     }
     if (n >= 2) e[n - 2] = A[(n - 1) * MAXR + n - 2];
@@ -623,11 +671,11 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
     for (int i = 0; i < n; ++i) d[i] = A[i * MAXR + i];
     nrot = 0;
     bool record = true; // false once MAXROT is exceeded: then Q holds G
-    const double eps = 2.220446049250313e-16;
+    const T eps = PsdReal<T>::eps();
     int end = n - 1, iter = 0;
     while (end > 0) {
         for (int i = 0; i < end; ++i)
-            if (fabs(e[i]) <= eps * (fabs(d[i]) + fabs(d[i + 1])) || fabs(e[i]) <= 1e-300) e[i] = 0;
+            if (fabs(e[i]) <= eps * (fabs(d[i]) + fabs(d[i + 1])) || fabs(e[i]) <= PsdReal<T>::tiny()) e[i] = 0;
         while (end > 0 && e[end - 1] == 0) --end;
         if (end <= 0) break;
         if (++iter > 40 * n) return false;
@@ -640,9 +688,9 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
                 for (int j = 0; j < n; ++j) Q[i * MAXR + j] = (i == j) ? 1.0 : 0.0;
             for (int r = 0; r < nrot; ++r) {
                 const int k = rk[r];
-                const double c = rc[r], s = rs[r];
+                const T c = rc[r], s = rs[r];
                 for (int q = 0; q < n; ++q) {
-                    const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
+                    const T qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
                     Q[q * MAXR + k] = c * qa - s * qb;
                     Q[q * MAXR + k + 1] = s * qa + c * qb;
                 }
@@ -650,27 +698,39 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
             record = false;
             nrot = -1;
         }
-        const double td = 0.5 * (d[end - 1] - d[end]);
-        const double b = e[end - 1];
-        double mu = d[end];
+        const T td = 0.5 * (d[end - 1] - d[end]);
+        const T b = e[end - 1];
+        T mu = d[end];
         if (td == 0) mu -= fabs(b);
         else {
-            const double h = hypot(td, b);
+            const T h = hypot(td, b);
             mu -= b * b / (td + (td > 0 ? h : -h));
         }
-        double x = d[start] - mu, z = e[start];
+        T x = d[start] - mu, z = e[start];
         for (int k = start; k < end; ++k) {
             // (c, s) from one reciprocal square root: x and z are entries of
             // a local Hessian, far from the range where x^2 + z^2 overflows
-            const double r2 = x * x + z * z;
-            double c = 1, s = 0;
-            if (r2 != 0) {
-                const double ir = rsqrt(r2);
-                c = x * ir;
-                s = -z * ir;
+            T c = 1, s = 0;
+            if constexpr (PsdReal<T>::rescale) {
+                // df64: (x, z) scaled by a power of two before squaring
+                const T xz = dmax(fabs(x), fabs(z));
+                if (xz != T(0)) {
+                    const int rex = pow2_exp(xz);
+                    const T xs = scale2(x, -rex), zs = scale2(z, -rex);
+                    const T ir = rsqrt(xs * xs + zs * zs);
+                    c = xs * ir;
+                    s = -zs * ir;
+                }
+            } else {
+                const T r2 = x * x + z * z;
+                if (r2 != 0) {
+                    const T ir = rsqrt(r2);
+                    c = x * ir;
+                    s = -z * ir;
+                }
             }
             if (k > start) e[k - 1] = c * e[k - 1] - s * z;
-            const double dk = d[k], dk1 = d[k + 1], ek = e[k];
+            const T dk = d[k], dk1 = d[k + 1], ek = e[k];
             d[k] = c * c * dk - 2 * c * s * ek + s * s * dk1;
             d[k + 1] = s * s * dk + 2 * c * s * ek + c * c * dk1;
             e[k] = c * s * (dk - dk1) + (c * c - s * s) * ek;
@@ -686,7 +746,7 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
                 ++nrot;
             } else {
                 for (int q = 0; q < n; ++q) {
-                    const double qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
+                    const T qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
                     Q[q * MAXR + k] = c * qa - s * qb;
                     Q[q * MAXR + k + 1] = s * qa + c * qb;
                 }
@@ -701,18 +761,18 @@ __device__ bool sym_eig(int n, double* A /*MAXR*MAXR, full symmetric*/, double* 
 // one pass (each rotation loaded once), or, if they were not recorded
 // (nrot < 0), from column i of Q; then the Householder reflectors kept in A's
 // lower columns, H_{n-3} first.
-__device__ void eigvecs(int n, const int* idx, int cnt, const double* Q, const double* rc, const double* rs,
-    const int8_t* rk, int nrot, const double* A, const double* htau, double* Y)
+template <class T> __device__ void eigvecs(int n, const int* idx, int cnt, const T* Q, const T* rc, const T* rs,
+    const int8_t* rk, int nrot, const T* A, const T* htau, T* Y)
 {
     for (int t = 0; t < cnt; ++t)
         for (int q = 0; q < n; ++q)
             Y[t * MAXR + q] = nrot >= 0 ? (q == idx[t] ? 1.0 : 0.0) : Q[q * MAXR + idx[t]];
     for (int r = nrot - 1; r >= 0; --r) {
         const int k = rk[r];
-        const double c = rc[r], s = rs[r];
+        const T c = rc[r], s = rs[r];
         for (int t = 0; t < cnt; ++t) {
-            double* y = Y + t * MAXR;
-            const double ya = y[k], yb = y[k + 1];
+            T* y = Y + t * MAXR;
+            const T ya = y[k], yb = y[k + 1];
             y[k] = c * ya + s * yb;
             y[k + 1] = c * yb - s * ya;
         }
@@ -720,8 +780,8 @@ __device__ void eigvecs(int n, const int* idx, int cnt, const double* Q, const d
     for (int k = n - 3; k >= 0; --k) {
         if (htau[k] == 0) continue;
         for (int t = 0; t < cnt; ++t) {
-            double* y = Y + t * MAXR;
-            double s = 0;
+            T* y = Y + t * MAXR;
+            T s = 0;
             for (int q = k + 1; q < n; ++q) s += A[q * MAXR + k] * y[q];
             s *= htau[k];
             for (int q = k + 1; q < n; ++q) y[q] -= s * A[q * MAXR + k];
@@ -740,13 +800,13 @@ template <int NS> __device__ __forceinline__ constexpr double contrast(int k, in
 }
 
 // w = C^T q (length 3 NS) for a length-3(NS-1) vector q.
-template <int NS> __device__ __forceinline__ void from_contrasts(const double* q, double* w)
+template <int NS, class T> __device__ __forceinline__ void from_contrasts(const T* q, T* w)
 {
 #pragma unroll
     for (int a = 0; a < NS; ++a)
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            double s = 0;
+            T s = 0;
 #pragma unroll
             for (int k = 0; k < NS - 1; ++k) s += contrast<NS>(k, a) * q[3 * k + c];
             w[3 * a + c] = s;
@@ -859,17 +919,17 @@ constexpr int PSD_BLOCK = LH_BLOCK;
 // NS = 4: C is the Hadamard matrix's rows without the all-ones one, times
 // 1/2; the butterflies here leave out that 1/2 (applied once by the caller).
 // NS = 3, 2: scaled in place.
-template <int NS> __device__ __forceinline__ void contrast_apply(const double* v, double* o)
+template <int NS, class T> __device__ __forceinline__ void contrast_apply(const T* v, T* o)
 {
-    constexpr double R2 = 0.70710678118654752440, R6 = 0.40824829046386301637;
+    const T R2 = T(0.70710678118654752440), R6 = T(0.40824829046386301637);
     if (NS == 4) {
-        const double s01 = v[0] + v[1], d01 = v[0] - v[1], s23 = v[2] + v[3], d23 = v[2] - v[3];
+        const T s01 = v[0] + v[1], d01 = v[0] - v[1], s23 = v[2] + v[3], d23 = v[2] - v[3];
         o[0] = d01 + d23;
         o[1] = s01 - s23;
         o[2] = d01 - d23;
     } else if (NS == 3) {
         o[0] = (v[0] - v[1]) * R2;
-        o[1] = fma(-2.0, v[2], v[0] + v[1]) * R6;
+        o[1] = fma(T(-2.0), v[2], v[0] + v[1]) * R6;
     } else {
         o[0] = (v[0] - v[1]) * R2;
     }
@@ -879,30 +939,30 @@ template <int NS> __device__ __forceinline__ void contrast_apply(const double* v
 // for each coordinate c, T = C H restricted to the rows of coordinate c (each
 // slab element loaded once, coalesced across the warp's contacts), then row
 // 3k+c of M from T's row k.
-template <int NS, class Acc> __device__ void to_contrasts(const Acc& hs, double* M)
+template <int NS, class T, class Acc> __device__ void to_contrasts(const Acc& hs, T* M, int sc)
 {
     constexpr int N = 3 * NS, K = NS - 1;
-    constexpr double S = NS == 4 ? 0.25 : 1.0; // the two butterfly stages' missing (1/2)^2
+    const T S = T(NS == 4 ? 0.25 : 1.0); // the two butterfly stages' missing (1/2)^2
 #pragma unroll 1
     for (int c = 0; c < 3; ++c) {
-        double T[K][N];
+        T Tm[K][N];
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            double v[NS], o[K];
+            T v[NS], o[K];
 #pragma unroll
-            for (int a = 0; a < NS; ++a) v[a] = hs((3 * a + c) * N + j);
-            contrast_apply<NS>(v, o);
+            for (int a = 0; a < NS; ++a) v[a] = PsdReal<T>::in(hs((3 * a + c) * N + j), sc);
+            contrast_apply<NS, T>(v, o);
 #pragma unroll
-            for (int k = 0; k < K; ++k) T[k][j] = o[k];
+            for (int k = 0; k < K; ++k) Tm[k][j] = o[k];
         }
 #pragma unroll
         for (int k = 0; k < K; ++k)
 #pragma unroll
             for (int e = 0; e < 3; ++e) {
-                double v[NS], o[K];
+                T v[NS], o[K];
 #pragma unroll
-                for (int b = 0; b < NS; ++b) v[b] = T[k][3 * b + e];
-                contrast_apply<NS>(v, o);
+                for (int b = 0; b < NS; ++b) v[b] = Tm[k][3 * b + e];
+                contrast_apply<NS, T>(v, o);
 #pragma unroll
                 for (int l = 0; l < K; ++l) M[(3 * k + c) * MAXR + 3 * l + e] = NS == 4 ? S * o[l] : o[l];
             }
@@ -913,50 +973,61 @@ template <int NS, class Acc> __device__ void to_contrasts(const Acc& hs, double*
 // eigenvectors kept, then one read-modify-write pass over the slab applying
 // H -= f lam w w^T for each of them in eigenvalue order.  Returns false if
 // the eigensolver did not converge.
-template <class Acc> __device__ bool project_psd(int n, const Acc& hs, int method)
+template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, int method)
 {
     const int N = 3 * n, m = 3 * (n - 1);
-    double M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
-    if (n == 4) to_contrasts<4>(hs, M);
-    else if (n == 3) to_contrasts<3>(hs, M);
-    else to_contrasts<2>(hs, M);
+    T M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
+    // df64: the matrix is read scaled by 2^-sc so that its entries are O(1)
+    const int sc = PsdReal<T>::scale_of(hs, N);
+    if (n == 4) to_contrasts<4, T>(hs, M, sc);
+    else if (n == 3) to_contrasts<3, T>(hs, M, sc);
+    else to_contrasts<2, T>(hs, M, sc);
     for (int r = 0; r < m; ++r)
         for (int s = r + 1; s < m; ++s) {
-            const double avg = 0.5 * (M[r * MAXR + s] + M[s * MAXR + r]);
+            const T avg = T(0.5) * (M[r * MAXR + s] + M[s * MAXR + r]);
             M[r * MAXR + s] = M[s * MAXR + r] = avg;
         }
-    double rc[MAXROT], rs[MAXROT], htau[MAXR];
+    T rc[MAXROT], rs[MAXROT], htau[MAXR];
     int8_t rk[MAXROT];
     int nrot;
     if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, htau)) return false;
-    const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
+    const T f = T((method == IPCG_PSD_CLAMP) ? 1.0 : 2.0);
     int idx[MAXR];
     int nneg = 0;
     for (int k = 0; k < m; ++k)
-        if (lam[k] < 0) idx[nneg++] = k;
+        if (lam[k] < T(0)) idx[nneg++] = k;
     if (nneg == 0) return true; // already PSD: returned as is
     // the eigenvectors (rows of 9) and then the w = C^T q (rows of 12) share
     // wv: row t of w is written after rows t.. of q are read (t descending),
     // and rows below t lie below 12 t
-    double wv[MAXR * 12], sl[MAXR];
+    T wv[MAXR * 12], sl[MAXR];
     eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, wv);
     for (int t = nneg - 1; t >= 0; --t) {
-        double q[MAXR];
+        T q[MAXR];
         for (int j = 0; j < m; ++j) q[j] = wv[t * MAXR + j];
-        double* w = wv + 12 * t;
-        if (n == 4) from_contrasts<4>(q, w);
-        else if (n == 3) from_contrasts<3>(q, w);
-        else from_contrasts<2>(q, w);
+        T* w = wv + 12 * t;
+        if (n == 4) from_contrasts<4, T>(q, w);
+        else if (n == 3) from_contrasts<3, T>(q, w);
+        else from_contrasts<2, T>(q, w);
         sl[t] = f * lam[idx[t]];
     }
     // H+ is symmetric: the upper triangle is formed and mirrored
 #pragma unroll 1
     for (int r = 0; r < N; ++r) {
-        double swr[MAXR];
+        T swr[MAXR];
         for (int t = 0; t < nneg; ++t) swr[t] = sl[t] * wv[12 * t + r];
         for (int c = r; c < N; ++c) {
-            double v = hs(r * N + c);
-            for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
+            double v;
+            if constexpr (PsdReal<T>::rescale) {
+                // df64: the correction in df64, subtracted in FP64 (entries
+                // without a correction keep their FP64 bits)
+                T corr = T(0);
+                for (int t = 0; t < nneg; ++t) corr = fma(swr[t], wv[12 * t + c], corr);
+                v = hs(r * N + c) - PsdReal<T>::out(corr, sc);
+            } else {
+                v = hs(r * N + c);
+                for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
+            }
             hs(r * N + c) = v;
             if (c != r) hs(c * N + r) = v;
         }

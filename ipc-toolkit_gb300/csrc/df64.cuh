@@ -1,0 +1,110 @@
+// df64.cuh — double-FP32 ("df64") arithmetic: a value is the unevaluated sum
+// hi + lo of two floats with |lo| <= ulp(hi) / 2, about 48 significant bits.
+//
+// GB300 issues FP32 at 64 times its FP64 rate, so FP64-accurate work that
+// does not need FP64's exponent range can run in pairs of FP32 operations
+// instead.  The error-free transformations are the classical ones: Knuth's
+// two-sum and Dekker's fast two-sum for addition, a fused multiply-add for the
+// exact product error.  Every operation uses explicitly rounded intrinsics
+// (__fadd_rn, __fmul_rn, __fmaf_rn), which the compiler never contracts or
+// reassociates, so the transformations stay exact.  The exponent range is
+// FP32's: callers scale their data by powers of two (exact) first.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+namespace ipcg {
+
+// the FP64 / FP32 math functions stay visible beside the df64 overloads below
+using ::fabs;
+using ::fma;
+using ::rsqrt;
+using ::sqrt;
+
+struct dd {
+    float hi, lo;
+};
+
+__device__ __forceinline__ dd dd_make(float h, float l) { return dd { h, l }; }
+
+// double -> df64: hi = x rounded to FP32; x - hi is exact in FP64 (at most 29
+// significant bits) and rounded once more, so hi + lo carries x to about 48
+// bits (x must lie in FP32's normal range)
+__device__ __forceinline__ dd dd_from_double(double x)
+{
+    const float h = __double2float_rn(x);
+    return dd { h, __double2float_rn(x - (double)h) };
+}
+__device__ __forceinline__ double dd_to_double(dd a) { return (double)a.hi + (double)a.lo; }
+
+__device__ __forceinline__ dd two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return dd { s, e };
+}
+__device__ __forceinline__ dd fast_two_sum(float a, float b) // |a| >= |b|
+{
+    const float s = __fadd_rn(a, b);
+    return dd { s, __fsub_rn(b, __fsub_rn(s, a)) };
+}
+__device__ __forceinline__ dd operator+(dd a, dd b)
+{
+    dd s = two_sum(a.hi, b.hi);
+    const dd t = two_sum(a.lo, b.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ dd operator-(dd a) { return dd { -a.hi, -a.lo }; }
+__device__ __forceinline__ dd operator-(dd a, dd b) { return a + (-b); }
+__device__ __forceinline__ dd operator*(dd a, dd b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p, e);
+}
+__device__ __forceinline__ dd operator/(dd a, dd b)
+{
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    dd r = a - dd { q1, 0.f } * b;
+    const float q2 = __fdiv_rn(r.hi, b.hi);
+    r = r - dd { q2, 0.f } * b;
+    const float q3 = __fdiv_rn(r.hi, b.hi);
+    return fast_two_sum(q1, q2) + dd { q3, 0.f };
+}
+__device__ __forceinline__ dd& operator+=(dd& a, dd b) { return a = a + b; }
+__device__ __forceinline__ dd& operator-=(dd& a, dd b) { return a = a - b; }
+__device__ __forceinline__ dd& operator*=(dd& a, dd b) { return a = a * b; }
+__device__ __forceinline__ bool operator<(dd a, dd b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ bool operator>(dd a, dd b) { return b < a; }
+__device__ __forceinline__ bool operator<=(dd a, dd b) { return !(b < a); }
+__device__ __forceinline__ bool operator>=(dd a, dd b) { return !(a < b); }
+__device__ __forceinline__ bool operator==(dd a, dd b) { return a.hi == b.hi && a.lo == b.lo; }
+__device__ __forceinline__ bool operator!=(dd a, dd b) { return !(a == b); }
+__device__ __forceinline__ dd fabs(dd a) { return a.hi < 0.f ? -a : a; }
+__device__ __forceinline__ dd sqrt(dd a)
+{
+    if (!(a.hi > 0.f)) return dd { 0.f, 0.f };
+    const float y = __fsqrt_rn(a.hi);
+    const dd r = a - dd { y, 0.f } * dd { y, 0.f };
+    return fast_two_sum(y, __fdiv_rn(r.hi, __fmul_rn(2.f, y)));
+}
+__device__ __forceinline__ dd rsqrt(dd a) { return dd { 1.f, 0.f } / sqrt(a); }
+__device__ __forceinline__ dd fma(dd a, dd b, dd c) { return a * b + c; }
+// power-of-two exponent of |a| (frexp convention) and exact scaling by 2^e
+__device__ __forceinline__ int pow2_exp(dd a)
+{
+    int e;
+    frexpf(a.hi, &e);
+    return e;
+}
+__device__ __forceinline__ dd scale2(dd a, int e) { return dd { ldexpf(a.hi, e), ldexpf(a.lo, e) }; }
+__device__ __forceinline__ dd dmax(dd a, dd b) { return a < b ? b : a; }
+
+} // namespace ipcg

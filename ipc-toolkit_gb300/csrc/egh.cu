@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(128) k_egh(ContactsView cv, const int* __restr
                     gslab[3 * s + 2] = g[3 * a + 2];
                 }
             if (want & WANT_H) {
-                if (psd != IPCG_PSD_NONE && pr && !project_psd(c.n, LocalAcc { H }, psd)) atomicOr(fail, 1);
+                if (psd != IPCG_PSD_NONE && pr && !project_psd<double>(c.n, LocalAcc { H }, psd)) atomicOr(fail, 1);
                 const int N = 3 * c.n;
                 const int64_t off = contrib_offset(cv, i);
                 for (int a = 0; a < c.n; ++a)

@@ -300,7 +300,9 @@ void set_last_error(const std::string& msg);
 // vertex-vertex candidates among codimensional vertices (vertices in no edge)
 // and edge-vertex candidates between codimensional edges and those vertices
 // (candidates.cpp:66-116, 152-210); those passes are not built here, so a mesh
-// with codimensional vertices is refused instead of giving an incomplete set.
+// on which they would find anything -- two or more codimensional vertices, or
+// one with a codimensional edge -- is refused instead of giving an incomplete
+// set.  (A single loose vertex is still found by the face-vertex pass.)
 void require_no_codim_vertices(const ipcg_mesh* m);
 
 // barrier.cu: contacts per Hessian chunk of a batch (scratch memory bound)

@@ -201,7 +201,9 @@ struct ipcg_server {
             BarrierArgs a { sc.dhat, sc.kappa, sc.col->dmin, 0, r.psd };
             sc.grad.reserve(3 * m->nV + 1);
             r.hess = new ipcg_csr();
-            barrier_evaluate(sc.col, m, dV, a, &r.energy, sc.grad.p, r.hess);
+            // the same cached-pattern pass as a direct call, so results are identical
+            if (!(r.hess && barrier_egh(sc.col, m, dV, a, &r.energy, sc.grad.p, r.hess)))
+                barrier_evaluate(sc.col, m, dV, a, &r.energy, sc.grad.p, r.hess);
             r.grad.resize(3 * m->nV);
             if (m->nV)
                 IPCG_CUDA(cudaMemcpyAsync(r.grad.data(), sc.grad.p, sizeof(double) * 3 * m->nV,

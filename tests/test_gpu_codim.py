@@ -4,10 +4,11 @@ The reference finds vertex-vertex candidates among codimensional vertices
 (vertices in no edge) and edge-vertex candidates between codimensional edges
 and those vertices (candidates.cpp:66-116, 152-210).  Those passes are not
 provided here, so every call that would need them -- the collision-set build,
-candidate builds and the step-size calls -- must refuse a mesh with
-codimensional vertices instead of returning an incomplete result.  A mesh
-whose only codimensional elements are free edges needs no extra pass and stays
-supported."""
+candidate builds and the step-size calls -- must refuse a mesh on which they
+would find pairs (two codimensional vertices, or one with a codimensional
+edge) instead of returning an incomplete result.  A mesh whose only
+codimensional elements are free edges, or a single loose vertex, needs no
+extra pass and stays supported."""
 import numpy as np
 import pytest
 
@@ -60,3 +61,24 @@ def test_free_edge_only_is_supported(ipctk, oracle_mod):
     assert len(col) == len(ref) > 0
     for k in ("vv", "ev", "ee", "fv"):
         np.testing.assert_array_equal(a[k], np.asarray(getattr(ref, k)).reshape(np.asarray(a[k]).shape), err_msg=k)
+
+
+def test_single_loose_vertex_is_supported(ipctk, oracle_mod):
+    # one point above the triangle and no free edge: nothing for the
+    # codimensional passes to pair, its contact is a face-vertex candidate
+    V, E, F = _cloud_and_free_edge()
+    V = np.concatenate([V[:3], V[5:6]])
+    E = E[:3]
+    mesh = ipctk.CollisionMesh(V, E, F)
+    assert mesh.num_codim_vertices == 1 and mesh.num_codim_edges == 0
+    col = ipctk.NormalCollisions()
+    col.build(mesh, V, 1e-3)
+    ref = oracle_mod.build_collisions(V, E, F, 1e-3)
+    a = col.to_arrays()
+    assert len(col) == len(ref) > 0
+    for k in ("vv", "ev", "ee", "fv"):
+        np.testing.assert_array_equal(a[k], np.asarray(getattr(ref, k)).reshape(np.asarray(a[k]).shape), err_msg=k)
+    V1 = V.copy()
+    V1[3, 2] -= 1e-3
+    t = ipctk.compute_collision_free_stepsize(mesh, V, V1)
+    assert 0.0 < t < 1.0

@@ -122,7 +122,7 @@ def test_noalloc_energy_out_of_range_index_gives_nan(ipctk):
     mesh = ipctk.CollisionMesh(sc["V"], sc["E"], sc["F"])
     col = ipctk.NormalCollisions()
     col.build(mesh, sc["V"], sc["dhat"])
-    arrays = col.to_arrays()
+    arrays = dict(col.to_arrays())  # a copy: to_arrays() returns the set's cached dict
     assert len(arrays["fv_w"]) > 0
     arrays["fv"] = arrays["fv"].copy()
     arrays["fv"][0, 0] = sc["F"].shape[0] + 1000
