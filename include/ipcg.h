@@ -56,6 +56,15 @@ extern "C" {
  * eigen-projection, the mollifier, assembly and CCD stay FP64.  Results agree
  * with FP64 to about 1e-6 relative. */
 #define IPCG_BARRIER_FP32_LOCAL 4
+/* Bit 3 (no counterpart in the reference) computes the negative eigenpairs
+ * of the PSD projection in df64 (pairs of FP32 values, about 48 significant
+ * bits, with exact power-of-two rescaling) instead of FP64, on the FP32
+ * pipes, which GB300 runs at 64 times its FP64 rate.  The correction
+ * sum lam w w^T is subtracted from the FP64 local Hessian in FP64.  The
+ * projected Hessians agree with the FP64 projection to about 1e-13 relative.
+ * It applies to the calls that return a Hessian (the cached-pattern pass);
+ * other calls ignore it. */
+#define IPCG_BARRIER_DF64_PSD 8
 
 /* Bits 4-7 of the same argument select the barrier function
  * (src/ipc/barrier/barrier.hpp; BarrierPotential(barrier, dhat, stiffness,
@@ -279,19 +288,26 @@ int ipcg_barrier_batch(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
  * (the reference's SparseMatrixCache, matrix_cache.cpp:80-214, does the same
  * between Newton iterations): the pattern is built at the first such call
  * after each build or load of the set, and each later call replays one
- * captured CUDA graph (no host synchronisation inside it).  The fused
- * kernel's launch shape is per device: ipcg_barrier_autotune times candidate
- * shapes (threads per block 32/64/128, resident blocks per SM, 32-contact
- * tiles taken per work-queue grab) on this set's largest chunk and keeps the
- * fastest; the report is JSON ({"candidates": [...], "chosen": {...}}) in
- * report (truncated to report_len; *needed gets the full length with the
- * terminator; both may be NULL).  No counterpart in the reference. */
+ * captured CUDA graph (no host synchronisation inside it).  Each chunk of
+ * contacts runs two persistent work-queue kernels: stage 0 computes every
+ * contact's energy, gradient and local Hessian, stage 1 projects the local
+ * Hessians to PSD and writes their blocks to block-sorted slots, which
+ * streaming reductions sum into the CSR values.  Each stage's launch shape is
+ * per device: ipcg_barrier_autotune times candidate shapes (threads per block
+ * 32/64/128, resident blocks per SM, 32-contact tiles taken per work-queue
+ * grab) on this set's largest chunk and keeps the fastest for each stage;
+ * the report is JSON ({"local": {"candidates": [...], "chosen": {...}},
+ * "psd": {...}}) in report (truncated to report_len; *needed gets the full
+ * length with the terminator; both may be NULL).  No counterpart in the
+ * reference. */
 int ipcg_barrier_autotune(const ipcg_collisions* collisions, const ipcg_mesh* mesh, const double* vertices,
                           const double* dhat, const double* stiffness, int use_physical_barrier, int psd_method,
                           char* report, int64_t report_len, int64_t* needed);
-/* The fused kernel's launch shape on the current device (get / set). */
-int ipcg_barrier_tuning(int* threads, int* blocks_per_sm, int* tiles_per_grab);
-int ipcg_barrier_set_tuning(int threads, int blocks_per_sm, int tiles_per_grab);
+/* A stage's launch shape on the current device (get / set). */
+#define IPCG_STAGE_LOCAL 0
+#define IPCG_STAGE_PSD 1
+int ipcg_barrier_tuning(int stage, int* threads, int* blocks_per_sm, int* tiles_per_grab);
+int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles_per_grab);
 
 /* NormalPotential::shape_derivative(collisions, mesh, V)
  * (normal_potential.cpp:85-123, 310-416): the derivative of the gradient with

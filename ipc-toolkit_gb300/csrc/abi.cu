@@ -649,13 +649,14 @@ static void barrier_options(int bits, BarrierArgs& a)
     const int kind = (bits >> 4) & 15;
     require(bits >= 0
             && (bits & ~(IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT | IPCG_BARRIER_FP32_LOCAL
-                           | IPCG_BARRIER_FUNCTION(15)))
+                           | IPCG_BARRIER_DF64_PSD | IPCG_BARRIER_FUNCTION(15)))
                 == 0
             && kind <= IPCG_BARRIER_TWO_STAGE,
         "unknown barrier option bits");
     a.physical = (bits & IPCG_BARRIER_PHYSICAL) ? 1 : 0;
     a.mixed = (bits & IPCG_BARRIER_FP32_PT) ? 1 : 0;
     a.fp32_local = (bits & IPCG_BARRIER_FP32_LOCAL) ? 1 : 0;
+    a.df64_psd = (bits & IPCG_BARRIER_DF64_PSD) ? 1 : 0;
     a.kind = kind;
 }
 
@@ -770,22 +771,24 @@ int ipcg_barrier_autotune(const ipcg_collisions* c, const ipcg_mesh* mesh, const
     });
 }
 
-int ipcg_barrier_tuning(int* threads, int* blocks_per_sm, int* tiles_per_grab)
+int ipcg_barrier_tuning(int stage, int* threads, int* blocks_per_sm, int* tiles_per_grab)
 {
     return guarded([&] {
+        require(stage == IPCG_STAGE_LOCAL || stage == IPCG_STAGE_PSD, "unknown stage");
         require_device();
-        const EghTuning t = egh_tuning();
+        const EghTuning t = egh_tuning(stage);
         if (threads) *threads = t.threads;
         if (blocks_per_sm) *blocks_per_sm = t.blocks_per_sm;
         if (tiles_per_grab) *tiles_per_grab = t.tiles_per_grab;
     });
 }
 
-int ipcg_barrier_set_tuning(int threads, int blocks_per_sm, int tiles_per_grab)
+int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles_per_grab)
 {
     return guarded([&] {
+        require(stage == IPCG_STAGE_LOCAL || stage == IPCG_STAGE_PSD, "unknown stage");
         require_device();
-        egh_set_tuning(EghTuning { threads, blocks_per_sm, tiles_per_grab });
+        egh_set_tuning(stage, EghTuning { threads, blocks_per_sm, tiles_per_grab });
     });
 }
 

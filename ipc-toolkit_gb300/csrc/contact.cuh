@@ -969,16 +969,19 @@ template <int NS, class T, class Acc> __device__ void to_contrasts(const Acc& hs
     }
 }
 
-// PSD projection of contact i's slab in place: M from the slab, the negative
-// eigenvectors kept, then one read-modify-write pass over the slab applying
-// H -= f lam w w^T for each of them in eigenvalue order.  Returns false if
-// the eigensolver did not converge.
-template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, int method)
+// Negative eigenpairs of one local Hessian for its PSD projection
+// (eigen_ext.tpp:64-108): M = C H C^T from the accessor, its eigenpairs, and
+// for each negative eigenvalue lam the stencil vector w = C^T q (rows of 12 in
+// wv) and sl = f lam (f = 1 clamps, 2 takes the absolute value), so that
+// H+ = H - sum_t sl[t] w_t w_t^T.  sc is the power-of-two scale the df64 form
+// read the matrix with.  Returns false if the eigensolver did not converge.
+template <class T, class Acc>
+__device__ bool psd_negative(int n, const Acc& hs, int method, T* wv /*MAXR*12*/, T* sl, int& nneg, int& sc)
 {
     const int N = 3 * n, m = 3 * (n - 1);
     T M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
     // df64: the matrix is read scaled by 2^-sc so that its entries are O(1)
-    const int sc = PsdReal<T>::scale_of(hs, N);
+    sc = PsdReal<T>::scale_of(hs, N);
     if (n == 4) to_contrasts<4, T>(hs, M, sc);
     else if (n == 3) to_contrasts<3, T>(hs, M, sc);
     else to_contrasts<2, T>(hs, M, sc);
@@ -990,17 +993,16 @@ template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, 
     T rc[MAXROT], rs[MAXROT], htau[MAXR];
     int8_t rk[MAXROT];
     int nrot;
+    nneg = 0;
     if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, htau)) return false;
     const T f = T((method == IPCG_PSD_CLAMP) ? 1.0 : 2.0);
     int idx[MAXR];
-    int nneg = 0;
     for (int k = 0; k < m; ++k)
         if (lam[k] < T(0)) idx[nneg++] = k;
     if (nneg == 0) return true; // already PSD: returned as is
     // the eigenvectors (rows of 9) and then the w = C^T q (rows of 12) share
     // wv: row t of w is written after rows t.. of q are read (t descending),
     // and rows below t lie below 12 t
-    T wv[MAXR * 12], sl[MAXR];
     eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, wv);
     for (int t = nneg - 1; t >= 0; --t) {
         T q[MAXR];
@@ -1011,7 +1013,17 @@ template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, 
         else from_contrasts<2, T>(q, w);
         sl[t] = f * lam[idx[t]];
     }
-    // H+ is symmetric: the upper triangle is formed and mirrored
+    return true;
+}
+
+// H+ entry by entry from psd_negative's pairs: out(r, c, v) for every r <= c
+// (H+ is symmetric; the caller mirrors).  With nneg = 0 the entries are H's
+// own bits.
+template <class T, class Acc, class Out>
+__device__ __forceinline__ void psd_apply(int n, const Acc& hs, const T* wv, const T* sl, int nneg, int sc,
+    const Out& out)
+{
+    const int N = 3 * n;
 #pragma unroll 1
     for (int r = 0; r < N; ++r) {
         T swr[MAXR];
@@ -1021,17 +1033,34 @@ template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, 
             if constexpr (PsdReal<T>::rescale) {
                 // df64: the correction in df64, subtracted in FP64 (entries
                 // without a correction keep their FP64 bits)
-                T corr = T(0);
-                for (int t = 0; t < nneg; ++t) corr = fma(swr[t], wv[12 * t + c], corr);
-                v = hs(r * N + c) - PsdReal<T>::out(corr, sc);
+                v = hs(r * N + c);
+                if (nneg > 0) {
+                    T corr = T(0);
+                    for (int t = 0; t < nneg; ++t) corr = fma(swr[t], wv[12 * t + c], corr);
+                    v -= PsdReal<T>::out(corr, sc);
+                }
             } else {
                 v = hs(r * N + c);
                 for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
             }
-            hs(r * N + c) = v;
-            if (c != r) hs(c * N + r) = v;
+            out(r, c, v);
         }
     }
+}
+
+// PSD projection of one local Hessian in place.  Returns false if the
+// eigensolver did not converge.
+template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, int method)
+{
+    T wv[MAXR * 12], sl[MAXR];
+    int nneg, sc;
+    if (!psd_negative<T>(n, hs, method, wv, sl, nneg, sc)) return false;
+    if (nneg == 0) return true;
+    const int N = 3 * n;
+    psd_apply<T>(n, hs, wv, sl, nneg, sc, [&](int r, int c, double v) {
+        hs(r * N + c) = v;
+        if (c != r) hs(c * N + r) = v;
+    });
     return true;
 }
 

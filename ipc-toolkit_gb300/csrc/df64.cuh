@@ -19,23 +19,27 @@ namespace ipcg {
 // the FP64 / FP32 math functions stay visible beside the df64 overloads below
 using ::fabs;
 using ::fma;
+using ::hypot;
 using ::rsqrt;
 using ::sqrt;
 
-struct dd {
-    float hi, lo;
-};
-
-__device__ __forceinline__ dd dd_make(float h, float l) { return dd { h, l }; }
-
 // double -> df64: hi = x rounded to FP32; x - hi is exact in FP64 (at most 29
 // significant bits) and rounded once more, so hi + lo carries x to about 48
-// bits (x must lie in FP32's normal range)
-__device__ __forceinline__ dd dd_from_double(double x)
-{
-    const float h = __double2float_rn(x);
-    return dd { h, __double2float_rn(x - (double)h) };
-}
+// bits (x must lie in FP32's normal range).  Constants and small integers
+// convert implicitly, so generic code reads the same for double and dd.
+struct dd {
+    float hi, lo;
+    dd() = default;
+    __device__ __forceinline__ constexpr dd(float h, float l) : hi(h), lo(l) { }
+    __device__ __forceinline__ dd(double x)
+    {
+        hi = __double2float_rn(x);
+        lo = __double2float_rn(x - (double)hi);
+    }
+    __device__ __forceinline__ constexpr dd(int x) : hi((float)x), lo(0.f) { }
+};
+
+__device__ __forceinline__ dd dd_from_double(double x) { return dd(x); }
 __device__ __forceinline__ double dd_to_double(dd a) { return (double)a.hi + (double)a.lo; }
 
 __device__ __forceinline__ dd two_sum(float a, float b)
@@ -96,6 +100,7 @@ __device__ __forceinline__ dd sqrt(dd a)
     return fast_two_sum(y, __fdiv_rn(r.hi, __fmul_rn(2.f, y)));
 }
 __device__ __forceinline__ dd rsqrt(dd a) { return dd { 1.f, 0.f } / sqrt(a); }
+__device__ __forceinline__ dd hypot(dd a, dd b) { return sqrt(a * a + b * b); }
 __device__ __forceinline__ dd fma(dd a, dd b, dd c) { return a * b + c; }
 // power-of-two exponent of |a| (frexp convention) and exact scaling by 2^e
 __device__ __forceinline__ int pow2_exp(dd a)

@@ -12,29 +12,35 @@
 // keyed (row << 32 | col), radix-sorted and run-length encoded, which gives
 // the CSR pattern, and for every contribution its slot in block-sorted order
 // (perm).  The gradient's contributions (a contact's diagonal blocks) get
-// slots grouped by vertex the same way.  A step is then
-//   k_egh (persistent): warps take 32-contact tiles from a work queue; each
-//     lane computes one contact's energy, gradient and local Hessian,
-//     projects the Hessian to PSD and writes each 3x3 block to its sorted
-//     slot, the gradient to its vertex-grouped slot, the energy to its own;
-//   k_hess_reduce / k_grad_reduce / k_energy_reduce: streaming sums of
-//     contiguous runs of slots into the CSR values, the gradient and the
-//     per-scene energies, each value written once.
-// Everything is in fixed order (deterministic) and every size is known from
-// the pattern, so no step needs the host: the launches of a step are
-// captured once into a CUDA graph and replayed, reading the call's pointers
-// (positions, outputs, scratch) from a small device-side argument block that
-// is updated before each replay.
+// slots grouped by vertex the same way.  A step is then, per chunk,
+//   k_local (persistent): warps take 32-contact tiles from a work queue; each
+//     lane computes one contact's energy, gradient and local Hessian and
+//     writes the energy to its own slot, the gradient to its vertex-grouped
+//     slots and the Hessian to an element-major local slab;
+//   k_psd_scatter (persistent, same queue scheme): each lane projects one
+//     local Hessian to PSD (its negative eigenpairs in FP64, or in df64 on
+//     the FP32 pipes) and writes each 3x3 block to its block-sorted slot;
+//   k_hess_reduce / k_grad_reduce / k_energy_parts: streaming sums of
+//     contiguous runs of slots into the CSR values, the gradient and partial
+//     energies, each value written once;
+// and k_energy_scenes sums each scene's partial energies at the end.
+// Everything is in fixed order (deterministic: no launch shape changes a
+// bit) and every size is known from the pattern, so no step needs the host:
+// the launches of a step are captured once into a CUDA graph and replayed,
+// reading the call's pointers (positions, outputs, scratch) from a small
+// device-side argument block that is updated before each replay.
 //
-// The fused kernel's per-thread scratch (the local Hessian and the PSD
-// solver's work arrays) lives in local memory; how many warps stay resident
-// decides whether that scratch stays in L1/L2, so the grid shape (threads per
-// block, blocks per SM) and the work-queue grab size are chosen by a small
-// autotuner per device.
+// The two per-contact stages are split because they want different
+// residency: the local Hessian code is long and register-heavy, the
+// projection short of registers but heavy on per-thread scratch.  Each
+// stage's grid shape (threads per block, blocks per SM) and work-queue grab
+// size are chosen by a small autotuner per device.
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -60,6 +66,9 @@ struct EghDev {
     double* grad;
     double* val;
     double *slab, *gslab, *eslab;
+    double* lh;             // local Hessians, element-major
+    unsigned char* pflag;   // per contact: its Hessian is to be projected
+    double* epart;          // energy partial sums
 };
 
 // A run of consecutive scenes whose contacts are processed together (one
@@ -76,6 +85,7 @@ struct EChunk {
     int64_t rs_off;        // offset in run_start (nb + 1 entries per chunk)
     int64_t gs_off;        // offset in gstart (r1 - r0 + 1 entries per chunk)
     int64_t gslot_off;     // offset in gslot (4 per contact)
+    int64_t ep0, nep;      // energy parts
 };
 
 } // namespace
@@ -91,7 +101,9 @@ struct EghCache {
     DBuf<unsigned> perm, run_start, gstart, gslot;
     DBuf<int64_t> vbase;   // per block: CSR position of its entry (0, 0)
     DBuf<int> vnbr;        // per block: blocks in its block row
-    DBuf<int64_t> srange;  // per scene: chunk-local [begin, end) of each type (8 values)
+    DBuf<int64_t> eparts;  // energy parts: chunk-local [begin, end) of eslab
+    DBuf<int64_t> epstart; // per scene: its first energy part (ns + 1)
+    int64_t nparts = 0;
     DBuf<double> energy;   // per-scene energies of the last step
     DBuf<unsigned long long> queue;
     DBuf<int> fail;
@@ -114,8 +126,8 @@ namespace {
 constexpr int WANT_E = 1, WANT_G = 2, WANT_H = 4;
 
 std::mutex g_tune_mu;
-EghTuning g_tune[64];
-bool g_tune_set[64] = {};
+EghTuning g_tune[64][2];
+bool g_tune_set[64][2] = {};
 
 ContactsView full_view(const ipcg_collisions* cs)
 {
@@ -275,20 +287,107 @@ __global__ void k_p_gslot(ContactsView cv, const int* __restrict__ E, const int*
 
 // ---- the step ----
 
-// One lane per contact of a 32-contact tile; warps take tiles from the queue,
-// the last tiles (face-vertex and edge-edge, the costly ones) first.
-__global__ void __launch_bounds__(128) k_egh(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
-    const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv, const unsigned* __restrict__ perm,
-    const unsigned* __restrict__ gslot, unsigned long long* __restrict__ queue, int psd, int want, int grab,
-    int* __restrict__ fail)
+// Local Hessians, element-major per stencil size: the VV contacts' 6x6
+// matrices, then the EV contacts' 9x9, then the EE and FV contacts' 12x12
+// (EE first), element k of the r-th matrix of a group at k * stride + r.
+struct LhLayout {
+    int64_t off[3], stride[3], first[3]; // per group: offset, contacts, first chunk-local contact
+    __device__ __forceinline__ LhLayout(const ContactsView& cv)
+    {
+        first[0] = 0;
+        first[1] = cv.nvv;
+        first[2] = cv.nvv + cv.nev;
+        stride[0] = cv.nvv;
+        stride[1] = cv.nev;
+        stride[2] = cv.nee + cv.nfv;
+        off[0] = 0;
+        off[1] = 36 * cv.nvv;
+        off[2] = 36 * cv.nvv + 81 * cv.nev;
+    }
+};
+
+// Contact j of type CT (j counts within the type's list).
+template <int CT>
+__device__ __forceinline__ void load_typed(const ContactsView& cv, const int* __restrict__ E, const int* __restrict__ F,
+    int64_t j, Local& c)
 {
-    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    c.type = CT;
+    if constexpr (CT == CT_VV) {
+        const int2 p = cv.vv[j];
+        c.n = 2;
+        c.vid[0] = p.x;
+        c.vid[1] = p.y;
+        c.w = cv.vv_w[j];
+    } else if constexpr (CT == CT_EV) {
+        const int2 p = cv.ev[j];
+        c.n = 3;
+        c.vid[0] = p.y;
+        c.vid[1] = E[2 * p.x];
+        c.vid[2] = E[2 * p.x + 1];
+        c.w = cv.ev_w[j];
+    } else if constexpr (CT == CT_EE) {
+        const int2 p = cv.ee[j];
+        c.n = 4;
+        c.vid[0] = E[2 * p.x];
+        c.vid[1] = E[2 * p.x + 1];
+        c.vid[2] = E[2 * p.y];
+        c.vid[3] = E[2 * p.y + 1];
+        c.w = cv.ee_w[j];
+        c.eps = cv.ee_eps[j];
+        c.dtype = cv.ee_dt[j];
+    } else {
+        const int2 p = cv.fv[j];
+        c.n = 4;
+        c.vid[0] = p.y;
+        c.vid[1] = F[3 * p.x];
+        c.vid[2] = F[3 * p.x + 1];
+        c.vid[3] = F[3 * p.x + 2];
+        c.w = cv.fv_w[j];
+    }
+}
+
+// Energy, gradient and local Hessian of contact j of type CT (chunk-local
+// index i): the energy to its own slot, the gradient to its vertex-grouped
+// slots, the Hessian to the element-major local slab, whether it is to be
+// projected to pflag.
+template <int CT>
+__device__ __forceinline__ void local_one(const ContactsView& cv, const int* __restrict__ E, const int* __restrict__ F,
+    const EghDev& d, const Params* __restrict__ sp, const SceneView& sv, const unsigned* __restrict__ gslot,
+    const LhLayout& L, int64_t i, int64_t j, int want)
+{
+    constexpr int NS = CT == CT_VV ? 2 : (CT == CT_EV ? 3 : 4), N = 3 * NS, G = CT == CT_VV ? 0 : (CT == CT_EV ? 1 : 2);
+    Local c;
+    load_typed<CT>(cv, E, F, j, c);
+    const Params P = sp[sv.of(c.vid[0])];
+    V3 x[4];
+#pragma unroll
+    for (int a = 0; a < NS; ++a) x[a] = load_v3(d.V, c.vid[a]);
+    double e, g[12], H[144];
+    const bool pr = contact_egh(c, x, P, e, g, H);
+    if (want & WANT_E) d.eslab[i] = e;
+    if (want & WANT_G)
+#pragma unroll
+        for (int a = 0; a < NS; ++a) {
+            const int64_t s = gslot[4 * i + a];
+            d.gslab[3 * s] = g[3 * a];
+            d.gslab[3 * s + 1] = g[3 * a + 1];
+            d.gslab[3 * s + 2] = g[3 * a + 2];
+        }
+    double* __restrict__ lh = d.lh + L.off[G] + (i - L.first[G]);
+    const int64_t st = L.stride[G];
+#pragma unroll 4
+    for (int k = 0; k < N * N; ++k) lh[k * st] = H[k];
+    d.pflag[i] = pr ? 1 : 0;
+}
+
+// Persistent work-queue loop: warps take `grab` 32-contact tiles at a time,
+// the last tiles (the edge-edge and face-vertex contacts, the costly ones)
+// first; body(i) runs for every chunk-local contact i < n.
+template <class Body>
+__device__ __forceinline__ void tile_queue(int64_t n, unsigned long long* __restrict__ queue, int grab, const Body& body)
+{
     const int64_t ntiles = (n + 31) / 32;
     const int lane = threadIdx.x & 31;
-    const double* __restrict__ V = dev->V;
-    double* __restrict__ slab = dev->slab;
-    double* __restrict__ gslab = dev->gslab;
-    double* __restrict__ eslab = dev->eslab;
     for (;;) {
         unsigned long long t0 = 0;
         if (lane == 0) t0 = atomicAdd(queue, (unsigned long long)grab);
@@ -297,37 +396,69 @@ __global__ void __launch_bounds__(128) k_egh(ContactsView cv, const int* __restr
         const int64_t t1 = min((int64_t)t0 + grab, ntiles);
         for (int64_t tt = (int64_t)t0; tt < t1; ++tt) {
             const int64_t i = (ntiles - 1 - tt) * 32 + lane;
-            if (i >= n) continue;
-            Local c;
-            load_contact(cv, E, F, i, c);
-            const Params P = sp[sv.of(c.vid[0])];
-            V3 x[4];
-            gather(V, c, x);
-            double e, g[12], H[144];
-            const bool pr = contact_egh(c, x, P, e, g, H);
-            if (want & WANT_E) eslab[i] = e;
-            if (want & WANT_G)
-                for (int a = 0; a < c.n; ++a) {
-                    const int64_t s = gslot[4 * i + a];
-                    gslab[3 * s] = g[3 * a];
-                    gslab[3 * s + 1] = g[3 * a + 1];
-                    gslab[3 * s + 2] = g[3 * a + 2];
-                }
-            if (want & WANT_H) {
-                if (psd != IPCG_PSD_NONE && pr && !project_psd<double>(c.n, LocalAcc { H }, psd)) atomicOr(fail, 1);
-                const int N = 3 * c.n;
-                const int64_t off = contrib_offset(cv, i);
-                for (int a = 0; a < c.n; ++a)
-                    for (int b = 0; b < c.n; ++b) {
-                        double* o = slab + 9 * (int64_t)perm[off + a * c.n + b];
-#pragma unroll
-                        for (int k = 0; k < 3; ++k)
-#pragma unroll
-                            for (int l = 0; l < 3; ++l) o[3 * k + l] = H[(3 * a + k) * N + 3 * b + l];
-                    }
-            }
+            if (i < n) body(i);
         }
     }
+}
+
+// Stage 1: per contact, energy, gradient and local Hessian (one lane each).
+__global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv, const unsigned* __restrict__ gslot,
+    unsigned long long* __restrict__ queue, int want, int grab)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const EghDev d = *dev;
+    const LhLayout L(cv);
+    tile_queue(n, queue, grab, [&](int64_t i) {
+        if (i < L.first[1]) local_one<CT_VV>(cv, E, F, d, sp, sv, gslot, L, i, i, want);
+        else if (i < L.first[2]) local_one<CT_EV>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[1], want);
+        else if (i < L.first[2] + cv.nee) local_one<CT_EE>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[2], want);
+        else local_one<CT_FV>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[2] - cv.nee, want);
+    });
+}
+
+// Stage 2 for one contact with an NS-vertex stencil: the PSD projection of
+// its local Hessian (its negative eigenpairs in arithmetic T), applied while
+// each 3x3 block is written to its block-sorted slot.
+template <int NS, class T>
+__device__ __forceinline__ void psd_one(const EghDev& d, const unsigned* __restrict__ pm, int64_t i, int64_t r,
+    int64_t off, int64_t stride, int psd, int* __restrict__ fail)
+{
+    const Slab hs { d.lh + off, stride };
+    const SlabAcc acc { hs, r };
+    T wv[MAXR * 12], sl[MAXR];
+    int nneg = 0, sc = 0;
+    if (psd != IPCG_PSD_NONE && d.pflag[i] && !psd_negative<T>(NS, acc, psd, wv, sl, nneg, sc)) {
+        atomicOr(fail, 1);
+        nneg = 0;
+    }
+    unsigned slot[NS * NS];
+#pragma unroll
+    for (int q = 0; q < NS * NS; ++q) slot[q] = pm[q];
+    double* __restrict__ slab = d.slab;
+    psd_apply<T>(NS, acc, wv, sl, nneg, sc, [&](int rr, int cc, double v) {
+        const int a = rr / 3, k = rr % 3, b = cc / 3, l = cc % 3;
+        slab[9 * (int64_t)slot[a * NS + b] + 3 * k + l] = v;
+        if (cc != rr) slab[9 * (int64_t)slot[b * NS + a] + 3 * l + k] = v;
+    });
+}
+
+// Stage 2: PSD projection and scatter of every local Hessian to the
+// block-sorted slots (T = double: FP64; T = dd: df64 eigenpairs).
+template <class T>
+__global__ void __launch_bounds__(128) k_psd_scatter(ContactsView cv, const EghDev* __restrict__ dev,
+    const unsigned* __restrict__ perm, unsigned long long* __restrict__ queue, int psd, int grab,
+    int* __restrict__ fail)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const EghDev d = *dev;
+    const LhLayout L(cv);
+    tile_queue(n, queue, grab, [&](int64_t i) {
+        const int64_t off = contrib_offset(cv, i);
+        if (i < L.first[1]) psd_one<2, T>(d, perm + off, i, i, L.off[0], L.stride[0], psd, fail);
+        else if (i < L.first[2]) psd_one<3, T>(d, perm + off, i, i - L.first[1], L.off[1], L.stride[1], psd, fail);
+        else psd_one<4, T>(d, perm + off, i, i - L.first[2], L.off[2], L.stride[2], psd, fail);
+    });
 }
 
 // CSR values: each stored value sums its block's contiguous run of slots.
@@ -358,21 +489,34 @@ __global__ void k_grad_reduce(int64_t r0, int64_t nr, const unsigned* __restrict
     dev->grad[3 * (r0 + v) + k] = sum;
 }
 
-// Per-scene energies: one block per scene sums its four contact ranges
-// (fixed per-thread order and a fixed reduction tree: deterministic).
+// Per-scene energies in two fixed-order stages (deterministic): parts of at
+// most EPART contacts, each inside one scene's range of one contact type,
+// summed by one block each (a fixed reduction tree); then each scene's parts
+// in order.  Parts are numbered across the chunks, scene by scene.
 constexpr int ER_BLOCK = 256;
-__global__ void __launch_bounds__(ER_BLOCK) k_energy_reduce(const int64_t* __restrict__ srange,
-    const EghDev* __restrict__ dev, double* __restrict__ energy)
+constexpr int64_t EPART = 8192;
+__global__ void __launch_bounds__(ER_BLOCK) k_energy_parts(const int64_t* __restrict__ parts, int64_t p0,
+    const EghDev* __restrict__ dev)
 {
-    const int64_t* r = srange + 8 * (int64_t)blockIdx.x;
+    const int64_t p = p0 + blockIdx.x;
+    const int64_t b = parts[2 * p], e = parts[2 * p + 1];
     const double* __restrict__ eslab = dev->eslab;
     double s = 0;
-    for (int t = 0; t < 4; ++t)
-        for (int64_t i = r[2 * t] + threadIdx.x; i < r[2 * t + 1]; i += ER_BLOCK) s += eslab[i];
+    for (int64_t i = b + threadIdx.x; i < e; i += ER_BLOCK) s += eslab[i];
     typedef cub::BlockReduce<double, ER_BLOCK> BR;
     __shared__ typename BR::TempStorage tmp;
     const double tot = BR(tmp).Sum(s);
-    if (threadIdx.x == 0) energy[blockIdx.x] = tot;
+    if (threadIdx.x == 0) dev->epart[p] = tot;
+}
+__global__ void k_energy_scenes(const int64_t* __restrict__ pstart, int64_t ns, const EghDev* __restrict__ dev,
+    double* __restrict__ energy)
+{
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ns) return;
+    const double* __restrict__ ep = dev->epart;
+    double s = 0;
+    for (int64_t p = pstart[k]; p < pstart[k + 1]; ++p) s += ep[p];
+    energy[k] = s;
 }
 
 int device_index()
@@ -447,19 +591,33 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
         C.max_n = std::max(C.max_n, c.n);
     }
     C.n = tot_n;
-    // per-scene chunk-local ranges of each type (energy sums)
-    std::vector<int64_t> sr(8 * ns);
-    for (const EChunk& c : C.chunks) {
+    // energy parts: each scene's chunk-local range of each type in pieces of
+    // at most EPART contacts
+    std::vector<int64_t> parts, pstart(ns + 1, 0);
+    for (EChunk& c : C.chunks) {
         const int64_t base[4] = { 0, c.hi[0] - c.lo[0], (c.hi[0] - c.lo[0]) + (c.hi[1] - c.lo[1]),
             (c.hi[0] - c.lo[0]) + (c.hi[1] - c.lo[1]) + (c.hi[2] - c.lo[2]) };
-        for (int64_t k = c.k0; k < c.k1; ++k)
+        c.ep0 = (int64_t)parts.size() / 2;
+        for (int64_t k = c.k0; k < c.k1; ++k) {
+            pstart[k] = (int64_t)parts.size() / 2;
             for (int t = 0; t < 4; ++t) {
-                sr[8 * k + 2 * t] = base[t] + ranges[t * S + k] - c.lo[t];
-                sr[8 * k + 2 * t + 1] = base[t] + ranges[t * S + k + 1] - c.lo[t];
+                const int64_t b = base[t] + ranges[t * S + k] - c.lo[t];
+                const int64_t e = base[t] + ranges[t * S + k + 1] - c.lo[t];
+                for (int64_t q = b; q < e; q += EPART) {
+                    parts.push_back(q);
+                    parts.push_back(std::min(e, q + EPART));
+                }
             }
+        }
+        c.nep = (int64_t)parts.size() / 2 - c.ep0;
     }
-    C.srange.reserve(8 * ns + 1);
-    IPCG_CUDA(cudaMemcpyAsync(C.srange.p, sr.data(), sizeof(int64_t) * 8 * ns, cudaMemcpyHostToDevice, s));
+    pstart[ns] = (int64_t)parts.size() / 2;
+    C.nparts = pstart[ns];
+    C.eparts.reserve(parts.size() + 2);
+    C.epstart.reserve(ns + 1);
+    if (!parts.empty())
+        IPCG_CUDA(cudaMemcpyAsync(C.eparts.p, parts.data(), sizeof(int64_t) * parts.size(), cudaMemcpyHostToDevice, s));
+    IPCG_CUDA(cudaMemcpyAsync(C.epstart.p, pstart.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, s));
     C.perm.reserve(tot_contrib + 1);
     C.gslot.reserve(4 * tot_n + 1);
     // work space of the sort
@@ -542,7 +700,7 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
     C.nb = B0;
     C.pattern = pat;
     C.energy.reserve(ns + 1);
-    C.queue.reserve(C.chunks.size() + 1);
+    C.queue.reserve(2 * C.chunks.size() + 1);
     C.fail.reserve(1);
     C.dev.reserve(1);
     C.hdev.reserve(1);
@@ -562,39 +720,82 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
     C.graph_key.clear();
 }
 
-// Launch geometry of the fused kernel for a tuning: a persistent grid of
-// blocks_per_sm blocks per SM, never more warps than tiles.
-void egh_grid(const EghTuning& t, int64_t n, int& blocks, int& threads)
+// Launch geometry of a stage for a tuning: a persistent grid of
+// blocks_per_sm blocks per SM (at most what fits), never more warps than
+// tiles.
+// Resident blocks per SM of a kernel at a block size, per device (cached, so
+// that launches enqueued while capturing a graph query nothing).
+std::mutex g_occ_mu;
+std::map<std::tuple<int, const void*, int>, int> g_occ;
+template <class K> int occupancy(int dev, K kernel, int threads)
+{
+    const auto key = std::make_tuple(dev, (const void*)kernel, threads);
+    {
+        std::lock_guard<std::mutex> lk(g_occ_mu);
+        auto it = g_occ.find(key);
+        if (it != g_occ.end()) return it->second;
+    }
+    int occ = 0;
+    IPCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, 0));
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    g_occ[key] = occ;
+    return occ;
+}
+
+template <class K> void egh_grid(const EghTuning& t, int64_t n, K kernel, int& blocks, int& threads)
 {
     int dev = 0, sms = 1;
     IPCG_CUDA(cudaGetDevice(&dev));
     IPCG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     threads = t.threads;
+    const int occ = occupancy(dev, kernel, threads);
     const int64_t need = (n + 31) / 32 * 32 / threads + 1;
-    blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * t.blocks_per_sm, need));
+    const int64_t per_sm = std::max(1, std::min(t.blocks_per_sm, occ));
+    blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, need));
+}
+
+void launch_local(const ContactsView& cc, const ipcg_mesh* m, EghCache& C, const EChunk& ch, const Params* sp,
+    const SceneView& sv, unsigned long long* q, int want, const EghTuning& t, cudaStream_t s)
+{
+    int blocks, threads;
+    egh_grid(t, ch.n, k_local, blocks, threads);
+    IPCG_LAUNCH("k_local", s, k_local<<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv,
+        C.gslot.p + ch.gslot_off, q, want, t.tiles_per_grab));
+}
+
+void launch_psd(const ContactsView& cc, EghCache& C, const EChunk& ch, unsigned long long* q, int psd, bool df64,
+    const EghTuning& t, cudaStream_t s)
+{
+    int blocks, threads;
+    if (df64) {
+        egh_grid(t, ch.n, k_psd_scatter<dd>, blocks, threads);
+        IPCG_LAUNCH("k_psd_scatter", s, k_psd_scatter<dd><<<blocks, threads, 0, s>>>(cc, C.dev.p,
+            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, C.fail.p));
+    } else {
+        egh_grid(t, ch.n, k_psd_scatter<double>, blocks, threads);
+        IPCG_LAUNCH("k_psd_scatter", s, k_psd_scatter<double><<<blocks, threads, 0, s>>>(cc, C.dev.p,
+            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, C.fail.p));
+    }
 }
 
 // Enqueue the launches of one step on the mesh stream (also while capturing).
-int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Params* sp, int psd, int want,
-    const EghTuning& tune)
+int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Params* sp, int psd, bool df64, int want,
+    const EghTuning* tune)
 {
     cudaStream_t s = m->stream;
     const ContactsView cv = full_view(cs);
     const SceneView sv = scene_view(m);
     int kernels = 0;
+    IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 2 * C.chunks.size(), s));
     for (size_t ci = 0; ci < C.chunks.size(); ++ci) {
         const EChunk& ch = C.chunks[ci];
         const ContactsView cc = chunk_view(cv, ch);
         if (ch.n > 0) {
-            IPCG_CUDA(cudaMemsetAsync(C.queue.p + ci, 0, sizeof(unsigned long long), s));
-            int blocks, threads;
-            egh_grid(tune, ch.n, blocks, threads);
-            IPCG_LAUNCH("k_egh", s, k_egh<<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv,
-                C.perm.p + ch.perm_off, C.gslot.p + ch.gslot_off, C.queue.p + ci, psd, want, tune.tiles_per_grab,
-                C.fail.p));
-            ++kernels;
+            launch_local(cc, m, C, ch, sp, sv, C.queue.p + 2 * ci, want, tune[0], s);
+            launch_psd(cc, C, ch, C.queue.p + 2 * ci + 1, psd, df64, tune[1], s);
+            kernels += 2;
         }
-        if ((want & WANT_H) && ch.nb > 0) {
+        if (ch.nb > 0) {
             IPCG_LAUNCH("k_hess_reduce", s, k_hess_reduce<<<grid_for(9 * ch.nb, 256), 256, 0, s>>>(ch.nb,
                 C.run_start.p + ch.rs_off, C.vbase.p + ch.B0, C.vnbr.p + ch.B0, C.dev.p));
             ++kernels;
@@ -605,11 +806,17 @@ int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Par
                 C.gstart.p + ch.gs_off, C.dev.p));
             ++kernels;
         }
-        if ((want & WANT_E) && ch.k1 > ch.k0) {
-            IPCG_LAUNCH("k_energy_reduce", s, k_energy_reduce<<<(int)(ch.k1 - ch.k0), ER_BLOCK, 0, s>>>(
-                C.srange.p + 8 * ch.k0, C.dev.p, C.energy.p + ch.k0));
+        if ((want & WANT_E) && ch.nep > 0) {
+            IPCG_LAUNCH("k_energy_parts", s, k_energy_parts<<<(int)ch.nep, ER_BLOCK, 0, s>>>(C.eparts.p, ch.ep0,
+                C.dev.p));
             ++kernels;
         }
+    }
+    if (want & WANT_E) {
+        const int64_t ns = m->n_scenes;
+        IPCG_LAUNCH("k_energy_scenes", s, k_energy_scenes<<<grid_for(ns, 256), 256, 0, s>>>(C.epstart.p, ns, C.dev.p,
+            C.energy.p));
+        ++kernels;
     }
     return kernels;
 }
@@ -637,22 +844,34 @@ Params* upload_params_egh(const ipcg_collisions* cs, ipcg_mesh* m, const Barrier
 }
 
 // The step's scratch for the largest chunk from the library's pool (freed in
-// stream order after the step): Hessian slots, gradient slots, energies.
+// stream order after the step): local Hessians and their block-sorted
+// copies, projection flags, gradient slots, energies and energy parts.
 struct Scratch {
-    double *slab = nullptr, *gslab = nullptr, *eslab = nullptr;
+    double *slab = nullptr, *gslab = nullptr, *eslab = nullptr, *lh = nullptr, *epart = nullptr;
+    unsigned char* pflag = nullptr;
     cudaStream_t s = nullptr;
+    template <class P> void take(P*& p, size_t count)
+    {
+        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&p, sizeof(P) * count, device_pool(), s));
+    }
     void alloc(const EghCache& C, cudaStream_t st)
     {
         s = st;
-        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&slab, sizeof(double) * (9 * C.max_contrib + 9), device_pool(), s));
-        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&gslab, sizeof(double) * (3 * C.max_gs + 3), device_pool(), s));
-        IPCG_CUDA(cudaMallocFromPoolAsync((void**)&eslab, sizeof(double) * (C.max_n + 1), device_pool(), s));
+        take(slab, 9 * C.max_contrib + 9);
+        take(lh, 9 * C.max_contrib + 9);
+        take(gslab, 3 * C.max_gs + 3);
+        take(eslab, C.max_n + 1);
+        take(pflag, C.max_n + 1);
+        take(epart, C.nparts + 1);
+    }
+    EghDev dev(const double* V, double* grad, double* val) const
+    {
+        return EghDev { V, grad, val, slab, gslab, eslab, lh, pflag, epart };
     }
     ~Scratch()
     {
-        if (slab) cudaFreeAsync(slab, s);
-        if (gslab) cudaFreeAsync(gslab, s);
-        if (eslab) cudaFreeAsync(eslab, s);
+        for (void* p : { (void*)slab, (void*)gslab, (void*)eslab, (void*)lh, (void*)epart, (void*)pflag })
+            if (p) cudaFreeAsync(p, s);
     }
 };
 
@@ -669,22 +888,23 @@ EghCache& cache_for(const ipcg_collisions* cs, ipcg_mesh* m)
 
 } // namespace
 
-EghTuning egh_tuning()
+EghTuning egh_tuning(int stage)
 {
     const int d = device_index();
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    return g_tune_set[d] ? g_tune[d] : EghTuning {};
+    return g_tune_set[d][stage & 1] ? g_tune[d][stage & 1] : EghTuning {};
 }
 
-void egh_set_tuning(const EghTuning& t)
+void egh_set_tuning(int stage, const EghTuning& t)
 {
+    if (stage != 0 && stage != 1) throw Error(IPCG_ERR_INVALID, "tuning stage is 0 (local Hessians) or 1 (projection)");
     if (!(t.threads == 32 || t.threads == 64 || t.threads == 128) || t.blocks_per_sm < 1 || t.blocks_per_sm > 64
         || t.tiles_per_grab < 1 || t.tiles_per_grab > 64)
         throw Error(IPCG_ERR_INVALID, "tuning out of range: threads 32/64/128, blocks_per_sm 1-64, tiles_per_grab 1-64");
     const int d = device_index();
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[d] = t;
-    g_tune_set[d] = true;
+    g_tune[d][stage] = t;
+    g_tune_set[d][stage] = true;
 }
 
 bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a, double* energy_host,
@@ -719,26 +939,35 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     hess->col_shared = C.pattern->col.p;
     Scratch scr;
     scr.alloc(C, s);
-    C.hdev.p[0] = EghDev { V, grad_dev, hess->val.p, scr.slab, scr.gslab, scr.eslab };
+    C.hdev.p[0] = scr.dev(V, grad_dev, hess->val.p);
     IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
     IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(int), s));
-    const EghTuning tune = egh_tuning();
+    const EghTuning tune[2] = { egh_tuning(0), egh_tuning(1) };
+    const bool df64 = a.df64_psd != 0;
     if (prof::enabled()) {
         // per-kernel timing needs the launches themselves, not a replay
-        enqueue_step(cs, m, C, sp, a.psd, want, tune);
+        enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
     } else {
-        char key[160];
-        snprintf(key, sizeof(key), "%p|%d|%d|%d|%d|%d", (const void*)sp, a.psd, want, tune.threads, tune.blocks_per_sm,
-            tune.tiles_per_grab);
+        char key[200];
+        snprintf(key, sizeof(key), "%p|%d|%d|%d|%d,%d,%d|%d,%d,%d", (const void*)sp, a.psd, (int)df64, want,
+            tune[0].threads, tune[0].blocks_per_sm, tune[0].tiles_per_grab, tune[1].threads, tune[1].blocks_per_sm,
+            tune[1].tiles_per_grab);
         if (!C.exec || C.graph_key != key) {
             if (C.exec) cudaGraphExecDestroy(C.exec);
             if (C.graph) cudaGraphDestroy(C.graph);
             C.exec = nullptr;
             C.graph = nullptr;
+            {
+                // launch shapes (and their occupancy queries) before capturing
+                int b, t;
+                egh_grid(tune[0], C.max_n, k_local, b, t);
+                if (df64) egh_grid(tune[1], C.max_n, k_psd_scatter<dd>, b, t);
+                else egh_grid(tune[1], C.max_n, k_psd_scatter<double>, b, t);
+            }
             IPCG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             int kernels = 0;
             try {
-                kernels = enqueue_step(cs, m, C, sp, a.psd, want, tune);
+                kernels = enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
             } catch (...) {
                 cudaGraph_t g = nullptr;
                 cudaStreamEndCapture(s, &g);
@@ -768,6 +997,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     if (m->n_scenes > 1 && !cs->sorted) throw Error(IPCG_ERR_INVALID, "autotuning needs a built collision set");
     EghCache& C = cache_for(cs, m);
     const Params* sp = upload_params_egh(cs, m, a);
+    const bool df64 = a.df64_psd != 0;
     // the largest chunk is the workload
     size_t big = 0;
     for (size_t i = 0; i < C.chunks.size(); ++i)
@@ -777,7 +1007,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     const SceneView sv = scene_view(m);
     Scratch scr;
     scr.alloc(C, s);
-    C.hdev.p[0] = EghDev { V, nullptr, nullptr, scr.slab, scr.gslab, scr.eslab };
+    C.hdev.p[0] = scr.dev(V, nullptr, nullptr);
     IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
     IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(int), s));
     int dev = 0;
@@ -785,53 +1015,62 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     cudaEvent_t e0, e1;
     IPCG_CUDA(cudaEventCreate(&e0));
     IPCG_CUDA(cudaEventCreate(&e1));
-    EghTuning best {};
-    float best_ms = 1e30f;
-    std::string rep = "{\"workload_contacts\": " + std::to_string(ch.n) + ", \"candidates\": [";
-    bool first = true;
-    for (int threads : { 32, 64, 128 }) {
-        int occ = 0;
-        IPCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_egh, threads, 0));
-        for (int bps : { 1, 2, 3, 4, 6, 8, 12, 16 }) {
-            if (bps * threads > 1024 || bps > occ) continue;
-            for (int grab : { 1, 4 }) {
-                const EghTuning t { threads, bps, grab };
-                float ms = 0;
-                for (int rep_i = 0; rep_i < 3; ++rep_i) {
-                    IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long), s));
-                    int blocks, thr;
-                    egh_grid(t, ch.n, blocks, thr);
-                    IPCG_CUDA(cudaEventRecord(e0, s));
-                    k_egh<<<blocks, thr, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv, C.perm.p + ch.perm_off,
-                        C.gslot.p + ch.gslot_off, C.queue.p, a.psd, WANT_H | WANT_G | WANT_E, grab, C.fail.p);
-                    IPCG_CHECK_LAUNCH();
-                    prof::count();
-                    IPCG_CUDA(cudaEventRecord(e1, s));
-                    IPCG_CUDA(cudaEventSynchronize(e1));
-                    float t_ms = 0;
-                    IPCG_CUDA(cudaEventElapsedTime(&t_ms, e0, e1));
-                    if (rep_i > 0) ms += t_ms; // the first run warms the caches
-                }
-                ms /= 2;
-                char buf[160];
-                snprintf(buf, sizeof(buf), "%s{\"threads\": %d, \"blocks_per_sm\": %d, \"tiles_per_grab\": %d, \"ms\": %.4f}",
-                    first ? "" : ", ", threads, bps, grab, ms);
-                rep += buf;
-                first = false;
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best = t;
-                }
-            }
+    const int want = WANT_H | WANT_G | WANT_E;
+    // one stage, one tuning: a warm-up run and a timed one
+    auto time_stage = [&](int stage, const EghTuning& t) {
+        float ms = 0;
+        for (int r = 0; r < 2; ++r) {
+            IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 2, s));
+            IPCG_CUDA(cudaEventRecord(e0, s));
+            if (stage == 0) launch_local(cc, m, C, ch, sp, sv, C.queue.p, want, t, s);
+            else launch_psd(cc, C, ch, C.queue.p + 1, a.psd, df64, t, s);
+            prof::count();
+            IPCG_CUDA(cudaEventRecord(e1, s));
+            IPCG_CUDA(cudaEventSynchronize(e1));
+            IPCG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
         }
+        return ms;
+    };
+    std::string rep = "{\"workload_contacts\": " + std::to_string(ch.n) + ", \"device\": " + std::to_string(dev);
+    const char* names[2] = { "local", "psd" };
+    for (int stage = 0; stage < 2; ++stage) {
+        // stage 1 projects the local Hessians stage 0 left in the scratch
+        EghTuning best {};
+        float best_ms = 1e30f;
+        rep += std::string(", \"") + names[stage] + "\": {\"candidates\": [";
+        bool first = true;
+        auto consider = [&](const EghTuning& t) {
+            const float ms = time_stage(stage, t);
+            char buf[160];
+            snprintf(buf, sizeof(buf), "%s{\"threads\": %d, \"blocks_per_sm\": %d, \"tiles_per_grab\": %d, \"ms\": %.4f}",
+                first ? "" : ", ", t.threads, t.blocks_per_sm, t.tiles_per_grab, ms);
+            rep += buf;
+            first = false;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        };
+        for (int threads : { 32, 64, 128 }) {
+            const int occ = stage == 0 ? occupancy(dev, k_local, threads)
+                : (df64 ? occupancy(dev, k_psd_scatter<dd>, threads) : occupancy(dev, k_psd_scatter<double>, threads));
+            for (int bps : { 1, 2, 4, 8, 16, 32 }) {
+                if (bps > occ) break;
+                consider(EghTuning { threads, bps, 1 });
+            }
+            if (occ > 0 && occ < 32 && (occ & (occ - 1)) != 0) consider(EghTuning { threads, occ, 1 });
+        }
+        consider(EghTuning { best.threads, best.blocks_per_sm, 4 });
+        egh_set_tuning(stage, best);
+        char buf[200];
+        snprintf(buf, sizeof(buf), "], \"chosen\": {\"threads\": %d, \"blocks_per_sm\": %d, \"tiles_per_grab\": %d, "
+            "\"ms\": %.4f}}", best.threads, best.blocks_per_sm, best.tiles_per_grab, best_ms);
+        rep += buf;
+        if (stage == 0) time_stage(0, best); // leave stage 0's output for stage 1
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    egh_set_tuning(best);
-    char buf[200];
-    snprintf(buf, sizeof(buf), "], \"device\": %d, \"chosen\": {\"threads\": %d, \"blocks_per_sm\": %d, "
-        "\"tiles_per_grab\": %d, \"ms\": %.4f}}", dev, best.threads, best.blocks_per_sm, best.tiles_per_grab, best_ms);
-    rep += buf;
+    rep += "}";
     return rep;
 }
 

@@ -336,6 +336,7 @@ struct BarrierArgs {
     int kind = 0;                        // barrier function (IPCG_BARRIER_* kinds)
     int shape = 0;                       // Hessian slot holds the shape derivative
     int fp32_local = 0;                  // FP32 local Hessians but near-parallel EE
+    int df64_psd = 0;                    // PSD eigenpairs in df64 (cached-pattern pass)
 };
 struct FrictionView;
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
@@ -385,9 +386,12 @@ bool barrier_egh(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const 
 struct EghTuning {
     int threads = 64, blocks_per_sm = 4, tiles_per_grab = 1;
 };
-EghTuning egh_tuning();
-void egh_set_tuning(const EghTuning& t);
-// Time the fused kernel over candidate tunings on this set's largest chunk and
+// Launch shapes of the two per-contact stages of the cached-pattern pass on
+// the current device: stage 0 the local Hessians, stage 1 the projection and
+// scatter.
+EghTuning egh_tuning(int stage);
+void egh_set_tuning(int stage, const EghTuning& t);
+// Time both stages over candidate tunings on this set's largest chunk and
 // keep the fastest for the device; returns a JSON report.
 std::string egh_autotune(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a);
 // barrier.cu: derivative `order` (0-2) of barrier function `kind`

@@ -129,8 +129,8 @@ def _load():
         "ipcg_server_wait": (i32, [P, i64, P, P, PP]),
         "ipcg_server_stats": (i32, [P, P]),
         "ipcg_barrier_autotune": (i32, [P, P, P, P, P, i32, i32, C.c_char_p, i64, P]),
-        "ipcg_barrier_tuning": (i32, [P, P, P]),
-        "ipcg_barrier_set_tuning": (i32, [i32, i32, i32]),
+        "ipcg_barrier_tuning": (i32, [i32, P, P, P]),
+        "ipcg_barrier_set_tuning": (i32, [i32, i32, i32, i32]),
         "ipcg_initial_barrier_stiffness": (i32, [d, i32, d, d, P, P, i64, d, d, P, P]),
         "ipcg_update_barrier_stiffness": (i32, [d, d, d, d, d, d, d, P]),
     }
@@ -217,13 +217,19 @@ def set_hessian_chunk_contacts(contacts: int = 0):
 
 def _precision_bits(mode) -> int:
     """Option bits of a mixed-precision mode: False / "fp64", True / "pt",
-    "local" (IPCG_BARRIER_FP32_PT = 2, IPCG_BARRIER_FP32_LOCAL = 4)."""
+    "local" (IPCG_BARRIER_FP32_PT = 2, IPCG_BARRIER_FP32_LOCAL = 4), and
+    "psd_df64" / "local_df64": FP64 or "local" with the PSD projection's
+    eigenpairs in df64 (IPCG_BARRIER_DF64_PSD = 8)."""
     if mode in (False, None, "fp64"):
         return 0
     if mode in (True, "pt"):
         return 2
     if mode == "local":
         return 2 | 4
+    if mode == "psd_df64":
+        return 8
+    if mode == "local_df64":
+        return 2 | 4 | 8
     raise ValueError(f"unknown mixed-precision mode {mode!r}")
 
 
@@ -241,15 +247,19 @@ def autotune_barrier(collisions, mesh, vertices, dhat, stiffness, options: int =
     return json.loads(buf.value.decode())
 
 
-def barrier_tuning() -> dict:
-    """The fused kernel's launch shape on the current device."""
+STAGE_LOCAL, STAGE_PSD = 0, 1
+
+
+def barrier_tuning(stage: int = STAGE_PSD) -> dict:
+    """A stage's launch shape on the current device (ipcg_barrier_tuning):
+    STAGE_LOCAL the local Hessians, STAGE_PSD the projection and scatter."""
     t, b, g = C.c_int(), C.c_int(), C.c_int()
-    _check(_load().ipcg_barrier_tuning(C.byref(t), C.byref(b), C.byref(g)))
+    _check(_load().ipcg_barrier_tuning(int(stage), C.byref(t), C.byref(b), C.byref(g)))
     return {"threads": t.value, "blocks_per_sm": b.value, "tiles_per_grab": g.value}
 
 
-def set_barrier_tuning(threads: int, blocks_per_sm: int, tiles_per_grab: int = 1):
-    _check(_load().ipcg_barrier_set_tuning(int(threads), int(blocks_per_sm), int(tiles_per_grab)))
+def set_barrier_tuning(stage: int, threads: int, blocks_per_sm: int, tiles_per_grab: int = 1):
+    _check(_load().ipcg_barrier_set_tuning(int(stage), int(threads), int(blocks_per_sm), int(tiles_per_grab)))
 
 
 def launch_count() -> int:
@@ -752,8 +762,11 @@ class BarrierPotential:
         """``mixed_precision`` (no counterpart in the reference): False for
         FP64 throughout; True or "pt" for face-vertex contacts in FP32
         (IPCG_BARRIER_FP32_PT); "local" for every contact but near-parallel
-        edge-edge ones in FP32 (IPCG_BARRIER_FP32_LOCAL).  The PSD projection,
-        the mollifier and assembly stay FP64 in every mode."""
+        edge-edge ones in FP32 (IPCG_BARRIER_FP32_LOCAL); "psd_df64" and
+        "local_df64" add the PSD projection's eigenpairs in df64
+        (IPCG_BARRIER_DF64_PSD, about 1e-13 from FP64) to FP64 or "local".
+        The mollifier, the projected Hessian's subtraction and assembly stay
+        FP64 in every mode."""
         args = list(args)
         barrier = kw.pop("barrier", None)
         if args and isinstance(args[0], Barrier):
@@ -784,7 +797,7 @@ class BarrierPotential:
         V = _as_f64(vertices)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_shape_derivative(collisions._h, mesh._h, _ptr(V), self.dhat, self.stiffness,
-                                                     self._options & ~6, C.byref(h)))
+                                                     self._options & ~14, C.byref(h)))
         A = _csr_to_scipy(h, 3 * mesh.num_vertices)  # CSC view of the CSR arrays = transpose
         return sp.csr_matrix((A.data, A.indices, A.indptr), shape=A.shape)
 
@@ -894,8 +907,9 @@ class BatchBarrierPotential:
         return int(self.use_physical_barrier) | _precision_bits(self.mixed_precision)
 
     def autotune(self, collisions, batch, vertices, project_hessian_to_psd=None) -> dict:
-        """Time the fused energy / gradient / Hessian kernel's launch shapes on
-        this set and keep the fastest for the device (ipcg_barrier_autotune)."""
+        """Time the launch shapes of the energy / gradient / local Hessian stage
+        and of the projection stage on this set and keep the fastest of each
+        for the device (ipcg_barrier_autotune)."""
         psd = PSDProjectionMethod.CLAMP if project_hessian_to_psd is None else project_hessian_to_psd
         return autotune_barrier(collisions, batch, vertices, batch.per_scene(self.dhat),
                                 batch.per_scene(self.stiffness), self._options, psd)

@@ -7,9 +7,11 @@ The benchmark times two workloads; both are held to the oracle here:
   * sixteen scenes of the 256-scene batch, one from each sixteenth of its
     dhat range (the smallest scene of each bin, so the oracle stays quick),
     evaluated together as a SceneBatch: per scene the collision set
-    bit-exact, energy / gradient / Hessian within 1e-10 in FP64 and within
-    1e-6 in the mixed mode the benchmark runs (IPCG_BARRIER_FP32_LOCAL), and
-    the batched step sizes identical to the oracle's.
+    bit-exact, energy / gradient / Hessian within 1e-10 in FP64 and with the
+    projection's eigenpairs in df64 (IPCG_BARRIER_DF64_PSD), within 1e-6 in
+    the mixed modes the benchmark runs (IPCG_BARRIER_FP32_LOCAL, with and
+    without df64 eigenpairs), and the batched step sizes identical to the
+    oracle's.
 Norms as in the other parity tests: |a-b| <= tol |b| for energies,
 ||a-b||_2 <= tol ||b||_2 for gradients, ||A-B||_F <= tol ||B||_F for
 Hessians (the reference skips exact-zero local entries; whole blocks are
@@ -64,6 +66,12 @@ def test_sphere_pack_full_size(ipctk, oracle_mod):
     step = ipctk.compute_collision_free_stepsize(mesh, V, V1)
     step_ref, _ = oracle_mod.collision_free_stepsize(V, V1, E, F)
     assert step == step_ref
+    # the df64 projection meets the FP64 tolerance on the same set
+    B64 = ipctk.BarrierPotential(sc["dhat"], sc["kappa"], mixed_precision="psd_df64")
+    e2, g2, H2 = B64.energy_gradient_hessian(col, mesh, V, ipctk.PSDProjectionMethod.CLAMP)
+    assert e2 == e and np.array_equal(g2, g)
+    assert sp.linalg.norm(H2 - H_ref) <= REL * sp.linalg.norm(H_ref)
+    assert sp.linalg.norm(H2 - H) <= 1e-12 * sp.linalg.norm(H)
 
 
 def _batch_sample():
@@ -112,7 +120,10 @@ def test_batch_sample_collision_sets(batch16):
         _assert_set(sl, ref, vshift=voff[k], eshift=eoff[k], fshift=foff[k])
 
 
-@pytest.mark.parametrize("mode,tol", [(False, REL), ("local", MIXED_REL)])
+# "psd_df64": FP64 local Hessians, projection eigenpairs in df64 -- held to
+# the FP64 tolerance; "local_df64": the benchmark's mixed mode with them
+@pytest.mark.parametrize("mode,tol", [(False, REL), ("local", MIXED_REL), ("psd_df64", REL),
+                                      ("local_df64", MIXED_REL)])
 def test_batch_sample_potential(ipctk, oracle_mod, batch16, mode, tol):
     scs, batch, V, dh, kap, col, refs = batch16
     BB = ipctk.BatchBarrierPotential(dh, kap, mixed_precision=mode)
