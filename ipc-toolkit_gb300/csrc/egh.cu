@@ -106,7 +106,8 @@ struct EghCache {
     int64_t nparts = 0;
     DBuf<double> energy;   // per-scene energies of the last step
     DBuf<unsigned long long> queue;
-    DBuf<int> fail;
+    DBuf<long long> fail;  // [failed, chunk-local contact, chunk, non-finite entries]
+    HBuf<long long> hfail;
     DBuf<EghDev> dev;
     HBuf<EghDev> hdev;
     // captured step
@@ -422,14 +423,22 @@ __global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __res
 // each 3x3 block is written to its block-sorted slot.
 template <int NS, class T>
 __device__ __forceinline__ void psd_one(const EghDev& d, const unsigned* __restrict__ pm, int64_t i, int64_t r,
-    int64_t off, int64_t stride, int psd, int* __restrict__ fail)
+    int64_t off, int64_t stride, int psd, int chunk, long long* __restrict__ fail)
 {
     const Slab hs { d.lh + off, stride };
     const SlabAcc acc { hs, r };
     T wv[MAXR * 12], sl[MAXR];
     int nneg = 0, sc = 0;
     if (psd != IPCG_PSD_NONE && d.pflag[i] && !psd_negative<T>(NS, acc, psd, wv, sl, nneg, sc)) {
-        atomicOr(fail, 1);
+        // the first failure records which contact and whether its matrix
+        // had non-finite entries; the unprojected matrix is written
+        if (atomicCAS((unsigned long long*)fail, 0ull, 1ull) == 0ull) {
+            int bad = 0;
+            for (int k = 0; k < 9 * NS * NS; ++k) bad += isfinite(acc(k)) ? 0 : 1;
+            fail[1] = i;
+            fail[2] = chunk;
+            fail[3] = bad;
+        }
         nneg = 0;
     }
     unsigned slot[NS * NS];
@@ -447,17 +456,17 @@ __device__ __forceinline__ void psd_one(const EghDev& d, const unsigned* __restr
 // block-sorted slots (T = double: FP64; T = dd: df64 eigenpairs).
 template <class T>
 __global__ void __launch_bounds__(128) k_psd_scatter(ContactsView cv, const EghDev* __restrict__ dev,
-    const unsigned* __restrict__ perm, unsigned long long* __restrict__ queue, int psd, int grab,
-    int* __restrict__ fail)
+    const unsigned* __restrict__ perm, unsigned long long* __restrict__ queue, int psd, int grab, int chunk,
+    long long* __restrict__ fail)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const EghDev d = *dev;
     const LhLayout L(cv);
     tile_queue(n, queue, grab, [&](int64_t i) {
         const int64_t off = contrib_offset(cv, i);
-        if (i < L.first[1]) psd_one<2, T>(d, perm + off, i, i, L.off[0], L.stride[0], psd, fail);
-        else if (i < L.first[2]) psd_one<3, T>(d, perm + off, i, i - L.first[1], L.off[1], L.stride[1], psd, fail);
-        else psd_one<4, T>(d, perm + off, i, i - L.first[2], L.off[2], L.stride[2], psd, fail);
+        if (i < L.first[1]) psd_one<2, T>(d, perm + off, i, i, L.off[0], L.stride[0], psd, chunk, fail);
+        else if (i < L.first[2]) psd_one<3, T>(d, perm + off, i, i - L.first[1], L.off[1], L.stride[1], psd, chunk, fail);
+        else psd_one<4, T>(d, perm + off, i, i - L.first[2], L.off[2], L.stride[2], psd, chunk, fail);
     });
 }
 
@@ -701,7 +710,8 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
     C.pattern = pat;
     C.energy.reserve(ns + 1);
     C.queue.reserve(2 * C.chunks.size() + 1);
-    C.fail.reserve(1);
+    C.fail.reserve(4);
+    C.hfail.reserve(4);
     C.dev.reserve(1);
     C.hdev.reserve(1);
     IPCG_CUDA(cudaStreamSynchronize(s));
@@ -763,18 +773,18 @@ void launch_local(const ContactsView& cc, const ipcg_mesh* m, EghCache& C, const
         C.gslot.p + ch.gslot_off, q, want, t.tiles_per_grab));
 }
 
-void launch_psd(const ContactsView& cc, EghCache& C, const EChunk& ch, unsigned long long* q, int psd, bool df64,
-    const EghTuning& t, cudaStream_t s)
+void launch_psd(const ContactsView& cc, EghCache& C, const EChunk& ch, int ci, unsigned long long* q, int psd,
+    bool df64, const EghTuning& t, cudaStream_t s)
 {
     int blocks, threads;
     if (df64) {
         egh_grid(t, ch.n, k_psd_scatter<dd>, blocks, threads);
         IPCG_LAUNCH("k_psd_scatter", s, k_psd_scatter<dd><<<blocks, threads, 0, s>>>(cc, C.dev.p,
-            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, C.fail.p));
+            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, ci, C.fail.p));
     } else {
         egh_grid(t, ch.n, k_psd_scatter<double>, blocks, threads);
         IPCG_LAUNCH("k_psd_scatter", s, k_psd_scatter<double><<<blocks, threads, 0, s>>>(cc, C.dev.p,
-            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, C.fail.p));
+            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, ci, C.fail.p));
     }
 }
 
@@ -792,7 +802,7 @@ int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Par
         const ContactsView cc = chunk_view(cv, ch);
         if (ch.n > 0) {
             launch_local(cc, m, C, ch, sp, sv, C.queue.p + 2 * ci, want, tune[0], s);
-            launch_psd(cc, C, ch, C.queue.p + 2 * ci + 1, psd, df64, tune[1], s);
+            launch_psd(cc, C, ch, (int)ci, C.queue.p + 2 * ci + 1, psd, df64, tune[1], s);
             kernels += 2;
         }
         if (ch.nb > 0) {
@@ -888,6 +898,28 @@ EghCache& cache_for(const ipcg_collisions* cs, ipcg_mesh* m)
 
 } // namespace
 
+// The message of a projection failure: which contact, from the record.
+static std::string psd_failure(const EghCache& C)
+{
+    const long long* r = C.hfail.p;
+    std::string msg = "unable to project matrix onto positive semi-definite cone";
+    if (r[2] < 0 || r[2] >= (long long)C.chunks.size()) return msg;
+    const EChunk& ch = C.chunks[r[2]];
+    int64_t i = r[1];
+    static const char* names[4] = { "vertex-vertex", "edge-vertex", "edge-edge", "face-vertex" };
+    for (int t = 0; t < 4; ++t) {
+        const int64_t cnt = ch.hi[t] - ch.lo[t];
+        if (i < cnt) {
+            msg += " (the eigensolver did not converge on " + std::string(names[t]) + " collision "
+                + std::to_string(ch.lo[t] + i) + "; its local Hessian has " + std::to_string(r[3])
+                + " non-finite entries)";
+            break;
+        }
+        i -= cnt;
+    }
+    return msg;
+}
+
 EghTuning egh_tuning(int stage)
 {
     const int d = device_index();
@@ -941,7 +973,7 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     scr.alloc(C, s);
     C.hdev.p[0] = scr.dev(V, grad_dev, hess->val.p);
     IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
-    IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(int), s));
+    IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(long long) * 4, s));
     const EghTuning tune[2] = { egh_tuning(0), egh_tuning(1) };
     const bool df64 = a.df64_psd != 0;
     if (prof::enabled()) {
@@ -984,11 +1016,12 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     }
     if (energy_host)
         IPCG_CUDA(cudaMemcpyAsync(energy_host, C.energy.p, sizeof(double) * ns, cudaMemcpyDeviceToHost, s));
-    IPCG_CUDA(cudaMemcpyAsync(m->h_counters.p + 1, C.fail.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    IPCG_CUDA(cudaMemcpyAsync(C.hfail.p, C.fail.p, sizeof(long long) * 4, cudaMemcpyDeviceToHost, s));
     IPCG_CUDA(cudaStreamSynchronize(s));
-    if (m->h_counters.p[1]) throw Error(IPCG_ERR_CUDA, "unable to project matrix onto positive semi-definite cone");
+    if (C.hfail.p[0]) throw Error(IPCG_ERR_CUDA, psd_failure(C));
     return true;
 }
+
 
 std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const BarrierArgs& a)
 {
@@ -1009,7 +1042,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     scr.alloc(C, s);
     C.hdev.p[0] = scr.dev(V, nullptr, nullptr);
     IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
-    IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(int), s));
+    IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(long long) * 4, s));
     int dev = 0;
     IPCG_CUDA(cudaGetDevice(&dev));
     cudaEvent_t e0, e1;
@@ -1023,7 +1056,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
             IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 2, s));
             IPCG_CUDA(cudaEventRecord(e0, s));
             if (stage == 0) launch_local(cc, m, C, ch, sp, sv, C.queue.p, want, t, s);
-            else launch_psd(cc, C, ch, C.queue.p + 1, a.psd, df64, t, s);
+            else launch_psd(cc, C, ch, (int)big, C.queue.p + 1, a.psd, df64, t, s);
             prof::count();
             IPCG_CUDA(cudaEventRecord(e1, s));
             IPCG_CUDA(cudaEventSynchronize(e1));
