@@ -308,6 +308,11 @@ int ipcg_barrier_autotune(const ipcg_collisions* collisions, const ipcg_mesh* me
 #define IPCG_STAGE_PSD 1
 int ipcg_barrier_tuning(int stage, int* threads, int* blocks_per_sm, int* tiles_per_grab);
 int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles_per_grab);
+/* Testing switch: with on != 0, the df64 projection (IPCG_BARRIER_DF64_PSD)
+ * hands every local Hessian to its FP64 fix-up pass, the path taken by the
+ * rare matrix on which the df64 eigensolver does not converge.  No
+ * counterpart in the reference. */
+int ipcg_testing_defer_df64_psd(int on);
 
 /* NormalPotential::shape_derivative(collisions, mesh, V)
  * (normal_potential.cpp:85-123, 310-416): the derivative of the gradient with

@@ -792,6 +792,11 @@ int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles
     });
 }
 
+int ipcg_testing_defer_df64_psd(int on)
+{
+    return guarded([&] { egh_defer_df64(on != 0); });
+}
+
 // Gauss-Newton forms (normal_potential.cpp:15-83): the FP64 path serves
 // every option; the FP32 bit does not apply to them.
 static int gauss_newton_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, double dhat,

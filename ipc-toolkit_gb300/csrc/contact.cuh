@@ -583,6 +583,7 @@ template <class T> struct PsdReal;
 template <> struct PsdReal<double> {
     static constexpr bool rescale = false;
     __device__ static double eps() { return 2.220446049250313e-16; }
+    __device__ static double eps_norm() { return 2.220446049250313e-16; } // 2^-52
     __device__ static double tiny() { return 1e-300; }
     __device__ static double in(double x, int) { return x; }
     __device__ static double out(double x, int) { return x; }
@@ -591,6 +592,7 @@ template <> struct PsdReal<double> {
 template <> struct PsdReal<dd> {
     static constexpr bool rescale = true;
     __device__ static dd eps() { return dd { 7.1e-15f, 0.f }; }
+    __device__ static dd eps_norm() { return dd { 2.842170943040401e-14f, 0.f }; } // 2^-45
     __device__ static dd tiny() { return dd { 1e-36f, 0.f }; }
     __device__ static dd in(double x, int sc) { return dd_from_double(scalbn(x, -sc)); }
     __device__ static double out(dd x, int sc) { return scalbn(dd_to_double(x), sc); }
@@ -671,11 +673,21 @@ template <class T> __device__ bool sym_eig(int n, T* A /*MAXR*MAXR, full symmetr
     for (int i = 0; i < n; ++i) d[i] = A[i * MAXR + i];
     nrot = 0;
     bool record = true; // false once MAXROT is exceeded: then Q holds G
+    // an off-diagonal entry is zero when it is negligible next to its two
+    // diagonal neighbours, or next to the whole tridiagonal matrix (the
+    // latter as EISPACK's tql2 tests it: a QL sweep cannot drive an entry
+    // below its own rounding of the matrix's largest entries, which decides
+    // when the neighbours are small, and more so in df64)
     const T eps = PsdReal<T>::eps();
+    T tnorm = T(0);
+    for (int i = 0; i < n; ++i) tnorm = dmax(tnorm, fabs(d[i]) + fabs(e[i]));
+    const T floor_ = PsdReal<T>::eps_norm() * tnorm;
     int end = n - 1, iter = 0;
     while (end > 0) {
         for (int i = 0; i < end; ++i)
-            if (fabs(e[i]) <= eps * (fabs(d[i]) + fabs(d[i + 1])) || fabs(e[i]) <= PsdReal<T>::tiny()) e[i] = 0;
+            if (fabs(e[i]) <= eps * (fabs(d[i]) + fabs(d[i + 1])) || fabs(e[i]) <= PsdReal<T>::tiny()
+                || fabs(e[i]) <= floor_)
+                e[i] = 0;
         while (end > 0 && e[end - 1] == 0) --end;
         if (end <= 0) break;
         if (++iter > 40 * n) return false;

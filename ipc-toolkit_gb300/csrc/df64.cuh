@@ -111,5 +111,6 @@ __device__ __forceinline__ int pow2_exp(dd a)
 }
 __device__ __forceinline__ dd scale2(dd a, int e) { return dd { ldexpf(a.hi, e), ldexpf(a.lo, e) }; }
 __device__ __forceinline__ dd dmax(dd a, dd b) { return a < b ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return fmax(a, b); }
 
 } // namespace ipcg

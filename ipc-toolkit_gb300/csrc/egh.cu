@@ -38,6 +38,7 @@
 #include <cstdio>
 #include <cstring>
 #include <algorithm>
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -69,6 +70,7 @@ struct EghDev {
     double* lh;             // local Hessians, element-major
     unsigned char* pflag;   // per contact: its Hessian is to be projected
     double* epart;          // energy partial sums
+    int64_t* fixlist;       // contacts the df64 projection left to FP64
 };
 
 // A run of consecutive scenes whose contacts are processed together (one
@@ -126,6 +128,7 @@ namespace {
 
 constexpr int WANT_E = 1, WANT_G = 2, WANT_H = 4;
 
+std::atomic<int> g_defer_df64 { 0 };
 std::mutex g_tune_mu;
 EghTuning g_tune[64][2];
 bool g_tune_set[64][2] = {};
@@ -418,38 +421,69 @@ __global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __res
     });
 }
 
+// Flag on the projection method: the df64 pass leaves every projection to
+// the FP64 fix-up pass (a testing switch, ipcg_testing_defer_df64_psd).
+constexpr int PSD_DEFER = 16;
+
+// A 3x3-block scatter of one projected local Hessian: entry (r, c), r <= c,
+// and its mirror to the block-sorted slots of the contact's contributions.
+template <int NS> struct BlockScatter {
+    double* __restrict__ slab;
+    unsigned slot[NS * NS];
+    __device__ __forceinline__ BlockScatter(double* s, const unsigned* __restrict__ pm) : slab(s)
+    {
+#pragma unroll
+        for (int q = 0; q < NS * NS; ++q) slot[q] = pm[q];
+    }
+    __device__ __forceinline__ void operator()(int rr, int cc, double v) const
+    {
+        const int a = rr / 3, k = rr % 3, b = cc / 3, l = cc % 3;
+        slab[9 * (int64_t)slot[a * NS + b] + 3 * k + l] = v;
+        if (cc != rr) slab[9 * (int64_t)slot[b * NS + a] + 3 * l + k] = v;
+    }
+};
+
+__device__ __forceinline__ void record_failure(long long* __restrict__ fail, const SlabAcc& acc, int N, int64_t i,
+    int chunk)
+{
+    // the first failure records which contact and whether its matrix had
+    // non-finite entries
+    if (atomicCAS((unsigned long long*)fail, 0ull, 1ull) == 0ull) {
+        int bad = 0;
+        for (int k = 0; k < N * N; ++k) bad += isfinite(acc(k)) ? 0 : 1;
+        fail[1] = i;
+        fail[2] = chunk;
+        fail[3] = bad;
+    }
+}
+
 // Stage 2 for one contact with an NS-vertex stencil: the PSD projection of
 // its local Hessian (its negative eigenpairs in arithmetic T), applied while
-// each 3x3 block is written to its block-sorted slot.
+// each 3x3 block is written to its block-sorted slot.  If the eigensolver
+// does not converge, FP64 records the failure (and writes the unprojected
+// matrix); df64 writes nothing and appends the contact to the list that the
+// FP64 fix-up pass (k_psd_fixup) projects after it.
 template <int NS, class T>
 __device__ __forceinline__ void psd_one(const EghDev& d, const unsigned* __restrict__ pm, int64_t i, int64_t r,
-    int64_t off, int64_t stride, int psd, int chunk, long long* __restrict__ fail)
+    int64_t off, int64_t stride, int psd, int chunk, unsigned long long* __restrict__ nfix,
+    long long* __restrict__ fail)
 {
     const Slab hs { d.lh + off, stride };
     const SlabAcc acc { hs, r };
     T wv[MAXR * 12], sl[MAXR];
     int nneg = 0, sc = 0;
-    if (psd != IPCG_PSD_NONE && d.pflag[i] && !psd_negative<T>(NS, acc, psd, wv, sl, nneg, sc)) {
-        // the first failure records which contact and whether its matrix
-        // had non-finite entries; the unprojected matrix is written
-        if (atomicCAS((unsigned long long*)fail, 0ull, 1ull) == 0ull) {
-            int bad = 0;
-            for (int k = 0; k < 9 * NS * NS; ++k) bad += isfinite(acc(k)) ? 0 : 1;
-            fail[1] = i;
-            fail[2] = chunk;
-            fail[3] = bad;
+    const int method = psd & 15;
+    const bool defer = PsdReal<T>::rescale && (psd & PSD_DEFER); // testing: every projection to the fix-up
+    if (method != IPCG_PSD_NONE && d.pflag[i] && (defer || !psd_negative<T>(NS, acc, method, wv, sl, nneg, sc))) {
+        if constexpr (PsdReal<T>::rescale) {
+            d.fixlist[atomicAdd(nfix, 1ull)] = i; // at most one entry per contact
+            return;
+        } else {
+            record_failure(fail, acc, 3 * NS, i, chunk);
+            nneg = 0;
         }
-        nneg = 0;
     }
-    unsigned slot[NS * NS];
-#pragma unroll
-    for (int q = 0; q < NS * NS; ++q) slot[q] = pm[q];
-    double* __restrict__ slab = d.slab;
-    psd_apply<T>(NS, acc, wv, sl, nneg, sc, [&](int rr, int cc, double v) {
-        const int a = rr / 3, k = rr % 3, b = cc / 3, l = cc % 3;
-        slab[9 * (int64_t)slot[a * NS + b] + 3 * k + l] = v;
-        if (cc != rr) slab[9 * (int64_t)slot[b * NS + a] + 3 * l + k] = v;
-    });
+    psd_apply<T>(NS, acc, wv, sl, nneg, sc, BlockScatter<NS>(d.slab, pm));
 }
 
 // Stage 2: PSD projection and scatter of every local Hessian to the
@@ -462,12 +496,35 @@ __global__ void __launch_bounds__(128) k_psd_scatter(ContactsView cv, const EghD
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const EghDev d = *dev;
     const LhLayout L(cv);
+    unsigned long long* nfix = queue + 1;
     tile_queue(n, queue, grab, [&](int64_t i) {
         const int64_t off = contrib_offset(cv, i);
-        if (i < L.first[1]) psd_one<2, T>(d, perm + off, i, i, L.off[0], L.stride[0], psd, chunk, fail);
-        else if (i < L.first[2]) psd_one<3, T>(d, perm + off, i, i - L.first[1], L.off[1], L.stride[1], psd, chunk, fail);
-        else psd_one<4, T>(d, perm + off, i, i - L.first[2], L.off[2], L.stride[2], psd, chunk, fail);
+        if (i < L.first[1]) psd_one<2, T>(d, perm + off, i, i, L.off[0], L.stride[0], psd, chunk, nfix, fail);
+        else if (i < L.first[2])
+            psd_one<3, T>(d, perm + off, i, i - L.first[1], L.off[1], L.stride[1], psd, chunk, nfix, fail);
+        else psd_one<4, T>(d, perm + off, i, i - L.first[2], L.off[2], L.stride[2], psd, chunk, nfix, fail);
     });
+}
+
+// The df64 pass's fix-up: the contacts it listed, projected in FP64 (a fixed
+// grid striding over the list, whose length is read on the device).
+constexpr int FIX_BLOCKS = 152, FIX_THREADS = 32;
+__global__ void __launch_bounds__(FIX_THREADS) k_psd_fixup(ContactsView cv, const EghDev* __restrict__ dev,
+    const unsigned* __restrict__ perm, const unsigned long long* __restrict__ nfix, int psd, int chunk,
+    long long* __restrict__ fail)
+{
+    const EghDev d = *dev;
+    const LhLayout L(cv);
+    const int64_t cnt = (int64_t)*nfix;
+    psd &= 15;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < cnt; j += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = d.fixlist[j];
+        const int64_t off = contrib_offset(cv, i);
+        if (i < L.first[1]) psd_one<2, double>(d, perm + off, i, i, L.off[0], L.stride[0], psd, chunk, nullptr, fail);
+        else if (i < L.first[2])
+            psd_one<3, double>(d, perm + off, i, i - L.first[1], L.off[1], L.stride[1], psd, chunk, nullptr, fail);
+        else psd_one<4, double>(d, perm + off, i, i - L.first[2], L.off[2], L.stride[2], psd, chunk, nullptr, fail);
+    }
 }
 
 // CSR values: each stored value sums its block's contiguous run of slots.
@@ -709,7 +766,7 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
     C.nb = B0;
     C.pattern = pat;
     C.energy.reserve(ns + 1);
-    C.queue.reserve(2 * C.chunks.size() + 1);
+    C.queue.reserve(3 * C.chunks.size() + 1);
     C.fail.reserve(4);
     C.hfail.reserve(4);
     C.dev.reserve(1);
@@ -773,19 +830,26 @@ void launch_local(const ContactsView& cc, const ipcg_mesh* m, EghCache& C, const
         C.gslot.p + ch.gslot_off, q, want, t.tiles_per_grab));
 }
 
-void launch_psd(const ContactsView& cc, EghCache& C, const EChunk& ch, int ci, unsigned long long* q, int psd,
+// Stage 2 of one chunk; q[0] is its work queue, q[1] the fix-up count.
+// Returns the kernels launched.
+int launch_psd(const ContactsView& cc, EghCache& C, const EChunk& ch, int ci, unsigned long long* q, int psd,
     bool df64, const EghTuning& t, cudaStream_t s)
 {
     int blocks, threads;
     if (df64) {
         egh_grid(t, ch.n, k_psd_scatter<dd>, blocks, threads);
+        const int pm = psd | (g_defer_df64.load() ? PSD_DEFER : 0);
         IPCG_LAUNCH("k_psd_scatter", s, k_psd_scatter<dd><<<blocks, threads, 0, s>>>(cc, C.dev.p,
-            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, ci, C.fail.p));
-    } else {
-        egh_grid(t, ch.n, k_psd_scatter<double>, blocks, threads);
-        IPCG_LAUNCH("k_psd_scatter", s, k_psd_scatter<double><<<blocks, threads, 0, s>>>(cc, C.dev.p,
-            C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, ci, C.fail.p));
+            C.perm.p + ch.perm_off, q, pm, t.tiles_per_grab, ci, C.fail.p));
+        if (psd == IPCG_PSD_NONE) return 1;
+        IPCG_LAUNCH("k_psd_fixup", s, k_psd_fixup<<<FIX_BLOCKS, FIX_THREADS, 0, s>>>(cc, C.dev.p,
+            C.perm.p + ch.perm_off, q + 1, psd, ci, C.fail.p));
+        return 2;
     }
+    egh_grid(t, ch.n, k_psd_scatter<double>, blocks, threads);
+    IPCG_LAUNCH("k_psd_scatter", s, k_psd_scatter<double><<<blocks, threads, 0, s>>>(cc, C.dev.p,
+        C.perm.p + ch.perm_off, q, psd, t.tiles_per_grab, ci, C.fail.p));
+    return 1;
 }
 
 // Enqueue the launches of one step on the mesh stream (also while capturing).
@@ -796,14 +860,13 @@ int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Par
     const ContactsView cv = full_view(cs);
     const SceneView sv = scene_view(m);
     int kernels = 0;
-    IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 2 * C.chunks.size(), s));
+    IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 3 * C.chunks.size(), s));
     for (size_t ci = 0; ci < C.chunks.size(); ++ci) {
         const EChunk& ch = C.chunks[ci];
         const ContactsView cc = chunk_view(cv, ch);
         if (ch.n > 0) {
-            launch_local(cc, m, C, ch, sp, sv, C.queue.p + 2 * ci, want, tune[0], s);
-            launch_psd(cc, C, ch, (int)ci, C.queue.p + 2 * ci + 1, psd, df64, tune[1], s);
-            kernels += 2;
+            launch_local(cc, m, C, ch, sp, sv, C.queue.p + 3 * ci, want, tune[0], s);
+            kernels += 1 + launch_psd(cc, C, ch, (int)ci, C.queue.p + 3 * ci + 1, psd, df64, tune[1], s);
         }
         if (ch.nb > 0) {
             IPCG_LAUNCH("k_hess_reduce", s, k_hess_reduce<<<grid_for(9 * ch.nb, 256), 256, 0, s>>>(ch.nb,
@@ -859,6 +922,7 @@ Params* upload_params_egh(const ipcg_collisions* cs, ipcg_mesh* m, const Barrier
 struct Scratch {
     double *slab = nullptr, *gslab = nullptr, *eslab = nullptr, *lh = nullptr, *epart = nullptr;
     unsigned char* pflag = nullptr;
+    int64_t* fixlist = nullptr;
     cudaStream_t s = nullptr;
     template <class P> void take(P*& p, size_t count)
     {
@@ -873,14 +937,16 @@ struct Scratch {
         take(eslab, C.max_n + 1);
         take(pflag, C.max_n + 1);
         take(epart, C.nparts + 1);
+        take(fixlist, C.max_n + 1);
     }
     EghDev dev(const double* V, double* grad, double* val) const
     {
-        return EghDev { V, grad, val, slab, gslab, eslab, lh, pflag, epart };
+        return EghDev { V, grad, val, slab, gslab, eslab, lh, pflag, epart, fixlist };
     }
     ~Scratch()
     {
-        for (void* p : { (void*)slab, (void*)gslab, (void*)eslab, (void*)lh, (void*)epart, (void*)pflag })
+        for (void* p : { (void*)slab, (void*)gslab, (void*)eslab, (void*)lh, (void*)epart, (void*)pflag,
+                 (void*)fixlist })
             if (p) cudaFreeAsync(p, s);
     }
 };
@@ -919,6 +985,8 @@ static std::string psd_failure(const EghCache& C)
     }
     return msg;
 }
+
+void egh_defer_df64(bool on) { g_defer_df64.store(on ? 1 : 0); }
 
 EghTuning egh_tuning(int stage)
 {
@@ -981,7 +1049,8 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
         enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
     } else {
         char key[200];
-        snprintf(key, sizeof(key), "%p|%d|%d|%d|%d,%d,%d|%d,%d,%d", (const void*)sp, a.psd, (int)df64, want,
+        snprintf(key, sizeof(key), "%p|%d|%d%d|%d|%d,%d,%d|%d,%d,%d", (const void*)sp, a.psd, (int)df64,
+            g_defer_df64.load(), want,
             tune[0].threads, tune[0].blocks_per_sm, tune[0].tiles_per_grab, tune[1].threads, tune[1].blocks_per_sm,
             tune[1].tiles_per_grab);
         if (!C.exec || C.graph_key != key) {
@@ -1053,7 +1122,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     auto time_stage = [&](int stage, const EghTuning& t) {
         float ms = 0;
         for (int r = 0; r < 2; ++r) {
-            IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 2, s));
+            IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 3, s));
             IPCG_CUDA(cudaEventRecord(e0, s));
             if (stage == 0) launch_local(cc, m, C, ch, sp, sv, C.queue.p, want, t, s);
             else launch_psd(cc, C, ch, (int)big, C.queue.p + 1, a.psd, df64, t, s);

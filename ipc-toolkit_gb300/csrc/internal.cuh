@@ -390,6 +390,8 @@ struct EghTuning {
 // the current device: stage 0 the local Hessians, stage 1 the projection and
 // scatter.
 EghTuning egh_tuning(int stage);
+// Testing: the df64 projection defers every contact to its FP64 fix-up pass.
+void egh_defer_df64(bool on);
 void egh_set_tuning(int stage, const EghTuning& t);
 // Time both stages over candidate tunings on this set's largest chunk and
 // keep the fastest for the device; returns a JSON report.

@@ -131,6 +131,7 @@ def _load():
         "ipcg_barrier_autotune": (i32, [P, P, P, P, P, i32, i32, C.c_char_p, i64, P]),
         "ipcg_barrier_tuning": (i32, [i32, P, P, P]),
         "ipcg_barrier_set_tuning": (i32, [i32, i32, i32, i32]),
+        "ipcg_testing_defer_df64_psd": (i32, [i32]),
         "ipcg_initial_barrier_stiffness": (i32, [d, i32, d, d, P, P, i64, d, d, P, P]),
         "ipcg_update_barrier_stiffness": (i32, [d, d, d, d, d, d, d, P]),
     }
@@ -260,6 +261,12 @@ def barrier_tuning(stage: int = STAGE_PSD) -> dict:
 
 def set_barrier_tuning(stage: int, threads: int, blocks_per_sm: int, tiles_per_grab: int = 1):
     _check(_load().ipcg_barrier_set_tuning(int(stage), int(threads), int(blocks_per_sm), int(tiles_per_grab)))
+
+
+def testing_defer_df64_psd(on: bool):
+    """Testing switch (ipcg_testing_defer_df64_psd): the df64 projection
+    hands every local Hessian to its FP64 fix-up pass."""
+    _check(_load().ipcg_testing_defer_df64_psd(int(bool(on))))
 
 
 def launch_count() -> int:

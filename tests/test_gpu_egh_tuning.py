@@ -84,3 +84,22 @@ def test_autotune_reports_both_stages(ipctk, small_batch):
     finally:
         for stage, t in zip((ipctk.STAGE_LOCAL, ipctk.STAGE_PSD), saved):
             ipctk.set_barrier_tuning(stage, t["threads"], t["blocks_per_sm"], t["tiles_per_grab"])
+
+
+def test_df64_fixup_pass_matches_fp64(ipctk, small_batch):
+    # the FP64 fix-up pass behind the df64 projection (taken by matrices on
+    # which the df64 eigensolver does not converge), forced for every
+    # contact, gives the FP64 projection
+    import scipy.sparse as sp
+    e64, g64, H64 = _evaluate(ipctk, small_batch, False)
+    ipctk.testing_defer_df64_psd(True)
+    try:
+        e, g, H = _evaluate(ipctk, small_batch, "psd_df64")
+    finally:
+        ipctk.testing_defer_df64_psd(False)
+    np.testing.assert_array_equal(e, e64)
+    np.testing.assert_array_equal(g, g64)
+    assert sp.linalg.norm(sp.csr_matrix(H) - sp.csr_matrix(H64)) <= 1e-14 * sp.linalg.norm(sp.csr_matrix(H64))
+    # and without the switch df64 stays within its own accuracy
+    e2, g2, H2 = _evaluate(ipctk, small_batch, "psd_df64")
+    assert sp.linalg.norm(sp.csr_matrix(H2) - sp.csr_matrix(H64)) <= 1e-12 * sp.linalg.norm(sp.csr_matrix(H64))
