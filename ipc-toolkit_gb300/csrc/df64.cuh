@@ -27,7 +27,7 @@ using ::sqrt;
 // significant bits) and rounded once more, so hi + lo carries x to about 48
 // bits (x must lie in FP32's normal range).  Constants and small integers
 // convert implicitly, so generic code reads the same for double and dd.
-struct dd {
+struct alignas(8) dd {
     float hi, lo;
     dd() = default;
     __device__ __forceinline__ constexpr dd(float h, float l) : hi(h), lo(l) { }
@@ -73,13 +73,18 @@ __device__ __forceinline__ dd operator*(dd a, dd b)
     e = __fmaf_rn(a.lo, b.hi, e);
     return fast_two_sum(p, e);
 }
+// a / b: three quotient digits, each from the remainder times an
+// approximate reciprocal of b.hi (about 22 correct bits); the remainders are
+// exact to df64 precision, so every digit adds ~22 bits and the result is
+// correct to df64 precision although the reciprocal is not.
 __device__ __forceinline__ dd operator/(dd a, dd b)
 {
-    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float inv = __fdividef(1.f, b.hi);
+    const float q1 = __fmul_rn(a.hi, inv);
     dd r = a - dd { q1, 0.f } * b;
-    const float q2 = __fdiv_rn(r.hi, b.hi);
+    const float q2 = __fmul_rn(r.hi, inv);
     r = r - dd { q2, 0.f } * b;
-    const float q3 = __fdiv_rn(r.hi, b.hi);
+    const float q3 = __fmul_rn(r.hi, inv);
     return fast_two_sum(q1, q2) + dd { q3, 0.f };
 }
 __device__ __forceinline__ dd& operator+=(dd& a, dd b) { return a = a + b; }
@@ -92,24 +97,46 @@ __device__ __forceinline__ bool operator>=(dd a, dd b) { return !(a < b); }
 __device__ __forceinline__ bool operator==(dd a, dd b) { return a.hi == b.hi && a.lo == b.lo; }
 __device__ __forceinline__ bool operator!=(dd a, dd b) { return !(a == b); }
 __device__ __forceinline__ dd fabs(dd a) { return a.hi < 0.f ? -a : a; }
+// sqrt and 1/sqrt: an approximate FP32 reciprocal square root (about 22
+// correct bits) refined by one Newton step whose residual is formed in
+// df64, which doubles the correct bits (about 44).
 __device__ __forceinline__ dd sqrt(dd a)
 {
     if (!(a.hi > 0.f)) return dd { 0.f, 0.f };
-    const float y = __fsqrt_rn(a.hi);
+    const float rs = rsqrtf(a.hi);
+    const float y = __fmul_rn(a.hi, rs);
     const dd r = a - dd { y, 0.f } * dd { y, 0.f };
-    return fast_two_sum(y, __fdiv_rn(r.hi, __fmul_rn(2.f, y)));
+    return fast_two_sum(y, __fmul_rn(r.hi, __fmul_rn(0.5f, rs)));
 }
-__device__ __forceinline__ dd rsqrt(dd a) { return dd { 1.f, 0.f } / sqrt(a); }
+__device__ __forceinline__ dd rsqrt(dd a)
+{
+    const float y = rsqrtf(a.hi);
+    const dd yy = dd { y, 0.f } * dd { y, 0.f };
+    const dd d = dd { 1.f, 0.f } - a * yy; // 1 - a y^2, small
+    return fast_two_sum(y, __fmul_rn(__fmul_rn(0.5f, y), d.hi));
+}
 __device__ __forceinline__ dd hypot(dd a, dd b) { return sqrt(a * a + b * b); }
 __device__ __forceinline__ dd fma(dd a, dd b, dd c) { return a * b + c; }
-// power-of-two exponent of |a| (frexp convention) and exact scaling by 2^e
+// power-of-two exponent of |a| (frexp convention: |a.hi| = m 2^e with m in
+// [1/2, 1); from the exponent bits; 0 for zero) and exact scaling by 2^e
+// (a multiplication by a power of two built from its bits, in two steps when
+// 2^e is outside FP32's normal range)
 __device__ __forceinline__ int pow2_exp(dd a)
 {
-    int e;
-    frexpf(a.hi, &e);
-    return e;
+    const int bits = (__float_as_int(a.hi) >> 23) & 0xff;
+    return bits == 0 ? 0 : bits - 126;
 }
-__device__ __forceinline__ dd scale2(dd a, int e) { return dd { ldexpf(a.hi, e), ldexpf(a.lo, e) }; }
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((e + 127) << 23); } // e in [-126, 127]
+__device__ __forceinline__ dd scale2(dd a, int e)
+{
+    if (e >= -126 && e <= 127) {
+        const float p = pow2f(e);
+        return dd { __fmul_rn(a.hi, p), __fmul_rn(a.lo, p) };
+    }
+    const int e1 = e / 2, e2 = e - e1;
+    const float p1 = pow2f(e1), p2 = pow2f(e2);
+    return dd { __fmul_rn(__fmul_rn(a.hi, p1), p2), __fmul_rn(__fmul_rn(a.lo, p1), p2) };
+}
 __device__ __forceinline__ dd dmax(dd a, dd b) { return a < b ? b : a; }
 __device__ __forceinline__ double dmax(double a, double b) { return fmax(a, b); }
 
