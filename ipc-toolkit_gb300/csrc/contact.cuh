@@ -611,7 +611,7 @@ template <> struct PsdReal<dd> {
 constexpr int MAXR = 9;
 constexpr int MAXROT = 128; // recorded rotations; beyond, Q is accumulated
 
-template <class T> __device__ bool sym_eig(int n, T* A /*MAXR*MAXR, full symmetric*/, T* d, T* Q, T* rc, T* rs,
+template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full symmetric*/, T* d, T* Q, T* rc, T* rs,
     int8_t* rk, int& nrot, T* htau)
 {
     // Householder tridiagonalisation; reflector k is I - htau[k] v v^T with
@@ -773,7 +773,7 @@ template <class T> __device__ bool sym_eig(int n, T* A /*MAXR*MAXR, full symmetr
 // one pass (each rotation loaded once), or, if they were not recorded
 // (nrot < 0), from column i of Q; then the Householder reflectors kept in A's
 // lower columns, H_{n-3} first.
-template <class T> __device__ void eigvecs(int n, const int* idx, int cnt, const T* Q, const T* rc, const T* rs,
+template <class T> __device__ void eigvecs_impl(int n, const int* idx, int cnt, const T* Q, const T* rc, const T* rs,
     const int8_t* rk, int nrot, const T* A, const T* htau, T* Y)
 {
     for (int t = 0; t < cnt; ++t)
@@ -799,6 +799,31 @@ template <class T> __device__ void eigvecs(int n, const int* idx, int cnt, const
             for (int q = k + 1; q < n; ++q) y[q] -= s * A[q * MAXR + k];
         }
     }
+}
+
+// The df64 solver is long (each df64 operation is tens of FP32
+// instructions): one out-of-line copy serves every stencil size, which keeps
+// the kernel inside the instruction cache; the FP64 solver is inlined.
+__device__ __noinline__ bool sym_eig_dd(int n, dd* A, dd* d, dd* Q, dd* rc, dd* rs, int8_t* rk, int& nrot, dd* htau)
+{
+    return sym_eig_impl<dd>(n, A, d, Q, rc, rs, rk, nrot, htau);
+}
+__device__ __noinline__ void eigvecs_dd(int n, const int* idx, int cnt, const dd* Q, const dd* rc, const dd* rs,
+    const int8_t* rk, int nrot, const dd* A, const dd* htau, dd* Y)
+{
+    eigvecs_impl<dd>(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y);
+}
+template <class T> __device__ __forceinline__ bool sym_eig(int n, T* A, T* d, T* Q, T* rc, T* rs, int8_t* rk,
+    int& nrot, T* htau)
+{
+    if constexpr (PsdReal<T>::rescale) return sym_eig_dd(n, A, d, Q, rc, rs, rk, nrot, htau);
+    else return sym_eig_impl<T>(n, A, d, Q, rc, rs, rk, nrot, htau);
+}
+template <class T> __device__ __forceinline__ void eigvecs(int n, const int* idx, int cnt, const T* Q, const T* rc,
+    const T* rs, const int8_t* rk, int nrot, const T* A, const T* htau, T* Y)
+{
+    if constexpr (PsdReal<T>::rescale) eigvecs_dd(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y);
+    else eigvecs_impl<T>(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y);
 }
 
 // Orthonormal contrasts (rows orthogonal to (1,..,1)) for NS = 2, 3, 4
