@@ -588,6 +588,25 @@ template <> struct PsdReal<double> {
     __device__ static double in(double x, int) { return x; }
     __device__ static double out(double x, int) { return x; }
     template <class Acc> __device__ static int scale_of(const Acc&, int) { return 0; }
+    // deflation test of a QL off-diagonal entry e between diagonal entries
+    // d0 and d1 (eps relative to them, or below the floor)
+    __device__ static bool negligible(double e, double d0, double d1, double eps, double floor_)
+    {
+        return fabs(e) <= eps * (fabs(d0) + fabs(d1)) || fabs(e) <= tiny() || fabs(e) <= floor_;
+    }
+    // Wilkinson shift of the trailing 2x2 block [[d0, b], [b, d1]]: its
+    // eigenvalue closer to d1
+    __device__ static double shift(double d0, double d1, double b)
+    {
+        const double td = 0.5 * (d0 - d1);
+        double mu = d1;
+        if (td == 0) mu -= fabs(b);
+        else {
+            const double h = hypot(td, b);
+            mu -= b * b / (td + (td > 0 ? h : -h));
+        }
+        return mu;
+    }
 };
 template <> struct PsdReal<dd> {
     static constexpr bool rescale = true;
@@ -605,6 +624,26 @@ template <> struct PsdReal<dd> {
             mx = b > mx ? b : mx;
         }
         return mx == 0 ? 0 : (int)(mx >> 52) - 1022;
+    }
+    // the deflation test and the shift only steer the iteration (neither
+    // enters the result but through where it stops), so they run in FP32
+    // on the leading parts
+    __device__ static bool negligible(dd e, dd d0, dd d1, dd eps, dd floor_)
+    {
+        const float ae = fabsf(e.hi);
+        return ae <= eps.hi * (fabsf(d0.hi) + fabsf(d1.hi)) || ae <= tiny().hi || ae <= floor_.hi;
+    }
+    __device__ static dd shift(dd d0, dd d1, dd b)
+    {
+        // d1 minus an FP32 correction (exact in df64)
+        const float td = 0.5f * (d0.hi - d1.hi), bf = b.hi;
+        float corr;
+        if (td == 0.f) corr = fabsf(bf);
+        else {
+            const float h = hypotf(td, bf);
+            corr = bf * bf / (td + (td > 0.f ? h : -h));
+        }
+        return d1 - dd { corr, 0.f };
     }
 };
 
@@ -685,9 +724,7 @@ template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full sy
     int end = n - 1, iter = 0;
     while (end > 0) {
         for (int i = 0; i < end; ++i)
-            if (fabs(e[i]) <= eps * (fabs(d[i]) + fabs(d[i + 1])) || fabs(e[i]) <= PsdReal<T>::tiny()
-                || fabs(e[i]) <= floor_)
-                e[i] = 0;
+            if (PsdReal<T>::negligible(e[i], d[i], d[i + 1], eps, floor_)) e[i] = 0;
         while (end > 0 && e[end - 1] == 0) --end;
         if (end <= 0) break;
         if (++iter > 40 * n) return false;
@@ -710,14 +747,7 @@ template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full sy
             record = false;
             nrot = -1;
         }
-        const T td = 0.5 * (d[end - 1] - d[end]);
-        const T b = e[end - 1];
-        T mu = d[end];
-        if (td == 0) mu -= fabs(b);
-        else {
-            const T h = hypot(td, b);
-            mu -= b * b / (td + (td > 0 ? h : -h));
-        }
+        const T mu = PsdReal<T>::shift(d[end - 1], d[end], e[end - 1]);
         T x = d[start] - mu, z = e[start];
         for (int k = start; k < end; ++k) {
             // (c, s) from one reciprocal square root: x and z are entries of
@@ -978,17 +1008,19 @@ template <int NS, class T> __device__ __forceinline__ void contrast_apply(const 
 // 3k+c of M from T's row k.
 template <int NS, class T, class Acc> __device__ void to_contrasts(const Acc& hs, T* M, int sc)
 {
+    // the butterflies run in FP64 whatever the solver's arithmetic; the
+    // entries are stored as T (scaled by 2^-sc for df64)
     constexpr int N = 3 * NS, K = NS - 1;
-    const T S = T(NS == 4 ? 0.25 : 1.0); // the two butterfly stages' missing (1/2)^2
+    const double S = NS == 4 ? 0.25 : 1.0; // the two butterfly stages' missing (1/2)^2
 #pragma unroll 1
     for (int c = 0; c < 3; ++c) {
-        T Tm[K][N];
+        double Tm[K][N];
 #pragma unroll
         for (int j = 0; j < N; ++j) {
-            T v[NS], o[K];
+            double v[NS], o[K];
 #pragma unroll
-            for (int a = 0; a < NS; ++a) v[a] = PsdReal<T>::in(hs((3 * a + c) * N + j), sc);
-            contrast_apply<NS, T>(v, o);
+            for (int a = 0; a < NS; ++a) v[a] = hs((3 * a + c) * N + j);
+            contrast_apply<NS, double>(v, o);
 #pragma unroll
             for (int k = 0; k < K; ++k) Tm[k][j] = o[k];
         }
@@ -996,29 +1028,31 @@ template <int NS, class T, class Acc> __device__ void to_contrasts(const Acc& hs
         for (int k = 0; k < K; ++k)
 #pragma unroll
             for (int e = 0; e < 3; ++e) {
-                T v[NS], o[K];
+                double v[NS], o[K];
 #pragma unroll
                 for (int b = 0; b < NS; ++b) v[b] = Tm[k][3 * b + e];
-                contrast_apply<NS, T>(v, o);
+                contrast_apply<NS, double>(v, o);
 #pragma unroll
-                for (int l = 0; l < K; ++l) M[(3 * k + c) * MAXR + 3 * l + e] = NS == 4 ? S * o[l] : o[l];
+                for (int l = 0; l < K; ++l)
+                    M[(3 * k + c) * MAXR + 3 * l + e] = PsdReal<T>::in(NS == 4 ? S * o[l] : o[l], sc);
             }
     }
 }
 
 // Negative eigenpairs of one local Hessian for its PSD projection
-// (eigen_ext.tpp:64-108): M = C H C^T from the accessor, its eigenpairs, and
+// (eigen_ext.tpp:64-108): M = C H C^T from the accessor, its eigenpairs in
+// arithmetic T (FP64, or df64 on the matrix scaled by a power of two), and
 // for each negative eigenvalue lam the stencil vector w = C^T q (rows of 12 in
-// wv) and sl = f lam (f = 1 clamps, 2 takes the absolute value), so that
-// H+ = H - sum_t sl[t] w_t w_t^T.  sc is the power-of-two scale the df64 form
-// read the matrix with.  Returns false if the eigensolver did not converge.
+// wv) and sl = f lam (f = 1 clamps, 2 takes the absolute value), both FP64,
+// so that H+ = H - sum_t sl[t] w_t w_t^T.  Returns false if the eigensolver
+// did not converge.
 template <class T, class Acc>
-__device__ bool psd_negative(int n, const Acc& hs, int method, T* wv /*MAXR*12*/, T* sl, int& nneg, int& sc)
+__device__ bool psd_negative(int n, const Acc& hs, int method, double* wv /*MAXR*12*/, double* sl, int& nneg)
 {
     const int N = 3 * n, m = 3 * (n - 1);
     T M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
     // df64: the matrix is read scaled by 2^-sc so that its entries are O(1)
-    sc = PsdReal<T>::scale_of(hs, N);
+    const int sc = PsdReal<T>::scale_of(hs, N);
     if (n == 4) to_contrasts<4, T>(hs, M, sc);
     else if (n == 3) to_contrasts<3, T>(hs, M, sc);
     else to_contrasts<2, T>(hs, M, sc);
@@ -1032,7 +1066,7 @@ __device__ bool psd_negative(int n, const Acc& hs, int method, T* wv /*MAXR*12*/
     int nrot;
     nneg = 0;
     if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, htau)) return false;
-    const T f = T((method == IPCG_PSD_CLAMP) ? 1.0 : 2.0);
+    const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
     int idx[MAXR];
     for (int k = 0; k < m; ++k)
         if (lam[k] < T(0)) idx[nneg++] = k;
@@ -1040,15 +1074,21 @@ __device__ bool psd_negative(int n, const Acc& hs, int method, T* wv /*MAXR*12*/
     // the eigenvectors (rows of 9) and then the w = C^T q (rows of 12) share
     // wv: row t of w is written after rows t.. of q are read (t descending),
     // and rows below t lie below 12 t
-    eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, wv);
+    if constexpr (PsdReal<T>::rescale) {
+        T Y[MAXR * MAXR];
+        eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, Y);
+        for (int i = 0; i < nneg * MAXR; ++i) wv[i] = dd_to_double(Y[i]);
+    } else {
+        eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, wv);
+    }
     for (int t = nneg - 1; t >= 0; --t) {
-        T q[MAXR];
+        double q[MAXR];
         for (int j = 0; j < m; ++j) q[j] = wv[t * MAXR + j];
-        T* w = wv + 12 * t;
-        if (n == 4) from_contrasts<4, T>(q, w);
-        else if (n == 3) from_contrasts<3, T>(q, w);
-        else from_contrasts<2, T>(q, w);
-        sl[t] = f * lam[idx[t]];
+        double* w = wv + 12 * t;
+        if (n == 4) from_contrasts<4, double>(q, w);
+        else if (n == 3) from_contrasts<3, double>(q, w);
+        else from_contrasts<2, double>(q, w);
+        sl[t] = f * PsdReal<T>::out(lam[idx[t]], sc);
     }
     return true;
 }
@@ -1056,30 +1096,18 @@ __device__ bool psd_negative(int n, const Acc& hs, int method, T* wv /*MAXR*12*/
 // H+ entry by entry from psd_negative's pairs: out(r, c, v) for every r <= c
 // (H+ is symmetric; the caller mirrors).  With nneg = 0 the entries are H's
 // own bits.
-template <class T, class Acc, class Out>
-__device__ __forceinline__ void psd_apply(int n, const Acc& hs, const T* wv, const T* sl, int nneg, int sc,
+template <class Acc, class Out>
+__device__ __forceinline__ void psd_apply(int n, const Acc& hs, const double* wv, const double* sl, int nneg,
     const Out& out)
 {
     const int N = 3 * n;
 #pragma unroll 1
     for (int r = 0; r < N; ++r) {
-        T swr[MAXR];
+        double swr[MAXR];
         for (int t = 0; t < nneg; ++t) swr[t] = sl[t] * wv[12 * t + r];
         for (int c = r; c < N; ++c) {
-            double v;
-            if constexpr (PsdReal<T>::rescale) {
-                // df64: the correction in df64, subtracted in FP64 (entries
-                // without a correction keep their FP64 bits)
-                v = hs(r * N + c);
-                if (nneg > 0) {
-                    T corr = T(0);
-                    for (int t = 0; t < nneg; ++t) corr = fma(swr[t], wv[12 * t + c], corr);
-                    v -= PsdReal<T>::out(corr, sc);
-                }
-            } else {
-                v = hs(r * N + c);
-                for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
-            }
+            double v = hs(r * N + c);
+            for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
             out(r, c, v);
         }
     }
@@ -1089,12 +1117,12 @@ __device__ __forceinline__ void psd_apply(int n, const Acc& hs, const T* wv, con
 // eigensolver did not converge.
 template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, int method)
 {
-    T wv[MAXR * 12], sl[MAXR];
-    int nneg, sc;
-    if (!psd_negative<T>(n, hs, method, wv, sl, nneg, sc)) return false;
+    double wv[MAXR * 12], sl[MAXR];
+    int nneg;
+    if (!psd_negative<T>(n, hs, method, wv, sl, nneg)) return false;
     if (nneg == 0) return true;
     const int N = 3 * n;
-    psd_apply<T>(n, hs, wv, sl, nneg, sc, [&](int r, int c, double v) {
+    psd_apply(n, hs, wv, sl, nneg, [&](int r, int c, double v) {
         hs(r * N + c) = v;
         if (c != r) hs(c * N + r) = v;
     });

@@ -470,11 +470,11 @@ __device__ __forceinline__ void psd_one(const EghDev& d, const unsigned* __restr
 {
     const Slab hs { d.lh + off, stride };
     const SlabAcc acc { hs, r };
-    T wv[MAXR * 12], sl[MAXR];
-    int nneg = 0, sc = 0;
+    double wv[MAXR * 12], sl[MAXR];
+    int nneg = 0;
     const int method = psd & 15;
     const bool defer = PsdReal<T>::rescale && (psd & PSD_DEFER); // testing: every projection to the fix-up
-    if (method != IPCG_PSD_NONE && d.pflag[i] && (defer || !psd_negative<T>(NS, acc, method, wv, sl, nneg, sc))) {
+    if (method != IPCG_PSD_NONE && d.pflag[i] && (defer || !psd_negative<T>(NS, acc, method, wv, sl, nneg))) {
         if constexpr (PsdReal<T>::rescale) {
             d.fixlist[atomicAdd(nfix, 1ull)] = i; // at most one entry per contact
             return;
@@ -483,7 +483,7 @@ __device__ __forceinline__ void psd_one(const EghDev& d, const unsigned* __restr
             nneg = 0;
         }
     }
-    psd_apply<T>(NS, acc, wv, sl, nneg, sc, BlockScatter<NS>(d.slab, pm));
+    psd_apply(NS, acc, wv, sl, nneg, BlockScatter<NS>(d.slab, pm));
 }
 
 // Stage 2: PSD projection and scatter of every local Hessian to the
