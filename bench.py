@@ -65,6 +65,16 @@ def parse():
 BATCH_DESC = ("256 uneven two-sheet scenes (5,911,266 verts; side log-uniform [16, 256], dhat log-uniform "
               "[1e-4, 1e-2], gap U(0.2, 0.9) dhat, stiffness 1e4; seed 3)")
 BATCH_CONTACTS = 76_649_164  # merged collisions of the batch (oracle and GPU agree)
+# the headline's precision: FP32 distance derivatives and barrier terms for
+# every contact but near-parallel edge-edge ones, FP64 PSD eigen-projection
+HEADLINE_MODE = "local"
+PRECISION = {
+    "local": "mixed: FP32 distance derivatives and barrier terms except near-parallel edge-edge and degenerate "
+             "point-triangle; FP64 PSD eigen-projection, mollifier, assembly",
+    "fp64": "FP64 throughout",
+    "psd_df64": "FP64 local Hessians; PSD eigenpairs in df64 (pairs of FP32), contrasts and correction FP64",
+    "local_df64": "the mixed mode with the PSD eigenpairs in df64",
+}
 
 
 def batch_config(contacts=BATCH_CONTACTS):
@@ -594,15 +604,39 @@ def run_gb300(args, rank, world):
     counts = col.counts()
     C = int(counts[:4].sum())
     ndof = 3 * batch.num_vertices
-    BB = ipctk.BatchBarrierPotential(dh, kap, mixed_precision="local")
+    BB = ipctk.BatchBarrierPotential(dh, kap, mixed_precision=HEADLINE_MODE)
     stream = torch.cuda.ExternalStream(batch.stream, device=dev)
 
-    def step():
-        e, g, H = BB.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True,
-                              project_hessian_to_psd=CLAMP, device=True)
+    def step(pot=None):
+        e, g, H = (pot or BB).evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True,
+                                       project_hessian_to_psd=CLAMP, device=True)
         nnz = H.nnz
         H.free()
         return nnz
+
+    def timed_steps(pot, k):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for a, b in evs:
+            torch.cuda.synchronize()
+            a.record(stream)
+            step(pot)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    def values(pot):
+        e, g, H = pot.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True,
+                               project_hessian_to_psd=CLAMP, device=True)
+        v = torch.empty(H.nnz, dtype=torch.float64, device=dev)
+        H.values_into(v)
+        H.free()
+        return e, g, v
+
+    def rel_err(a, b):
+        (e1, g1, v1), (e0, g0, v0) = a, b
+        return {"energy_max_scene": float(np.max(np.abs(e1 - e0) / np.abs(e0))),
+                "gradient": float(torch.linalg.norm(g1 - g0).item() / torch.linalg.norm(g0).item()),
+                "hessian": float(torch.linalg.norm(v1 - v0).item() / torch.linalg.norm(v0).item())}
 
     t0 = time.perf_counter()
     nnz = step()  # builds the cached pattern
@@ -655,10 +689,21 @@ def run_gb300(args, rank, world):
     fp64_peak = fp64_peak_tflops(dev)
     nc = ncu_counts(top, "batch")
     launches_top = own[top]["launches"]
+    # the ncu figures were taken on a smaller batch of the same scenes and
+    # are per contact; a launch processes one chunk of the batch
+    per_launch = C / max(1, launches_top)
+    if nc.get("fp64_flops_per_contact"):
+        nc = dict(nc, fp64_flops=nc["fp64_flops_per_contact"] * per_launch,
+                  dram_bytes=nc["dram_bytes_per_contact"] * per_launch)
     # algorithmic bytes of the fused kernel per launch: the E+G+H bytes per
     # contact over the contacts one launch processes (the batch over its
     # chunks' launches)
     abytes = algorithmic_bytes(counts, ndof) / max(1, launches_top)
+    if top == "k_psd_scatter":
+        # the projection reads each local Hessian and writes its blocks, reading
+        # their slots: 2 x 8 N^2 + 4 n^2 bytes per contact
+        contribs = 4 * int(counts[0]) + 9 * int(counts[1]) + 16 * int(counts[2] + counts[3])
+        abytes = (psd_bytes(counts) + 4 * contribs) / max(1, launches_top)
     achieved_gbs = abytes / (top_ms / 1000.0) / 1e9
     roof = {"kernel": top, "avg_launch_ms": top_ms, "launches_per_step": launches_top,
             "hbm": {"achieved": achieved_gbs, "peak": peak, "unit": "GB/s", "frac": achieved_gbs / peak,
@@ -688,30 +733,30 @@ def run_gb300(args, rank, world):
     h2d = Vh_np.nbytes
     d2h = 8 * len(scs) + 8 * ndof
 
-    # the batched form in FP64 (batching without mixed precision) and the
-    # mixed results' error against it
-    BB64 = ipctk.BatchBarrierPotential(dh, kap)
-    b64 = timed_host(lambda: BB64.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True,
-                                           project_hessian_to_psd=CLAMP, device=True)[2].free(), 1, 3)
-    e0, g0, H0 = BB64.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True, project_hessian_to_psd=CLAMP,
-                               device=True)
-    v0 = torch.empty(H0.nnz, dtype=torch.float64, device=dev)
-    H0.values_into(v0)
-    H0.free()
-    e1, g1, H1 = BB.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True, project_hessian_to_psd=CLAMP,
-                             device=True)
-    v1 = torch.empty(H1.nnz, dtype=torch.float64, device=dev)
-    H1.values_into(v1)
-    H1.free()
-    err = {"energy_max_scene": float(np.max(np.abs(e1 - e0) / np.abs(e0))),
-           "gradient": float(torch.linalg.norm(g1 - g0).item() / torch.linalg.norm(g0).item()),
-           "hessian": float(torch.linalg.norm(v1 - v0).item() / torch.linalg.norm(v0).item())}
-    del v0, v1, g0, g1
+    # the batched form in the other precision modes (each autotuned, a few
+    # timed steps), and every mode's error against the batched FP64 results
+    ref64 = None
+    modes = {}
+    for mode in ("fp64", "psd_df64", "local_df64"):
+        pot = ipctk.BatchBarrierPotential(dh, kap, mixed_precision=mode)
+        step(pot)
+        tm = pot.autotune(col, batch, Vd, CLAMP)
+        step(pot)
+        ms = statistics.median(timed_steps(pot, min(5, args.steps)))
+        modes[mode] = {"value": C / (ms / 1000.0), "unit": UNIT, "ms": ms,
+                       "tuning": {k: tm[k]["chosen"] for k in ("local", "psd")}}
+        if mode == "fp64":
+            ref64 = values(pot)
+        else:
+            modes[mode]["rel_error_vs_fp64"] = rel_err(values(pot), ref64)
+        del pot
+    err = rel_err(values(BB), ref64)
+    del ref64
     # batched CCD: one compute_collision_free_stepsize over every scene
     V1d = torch.from_numpy(batch.pack([s["V1"] for s in scs])).to(dev)
     b_steps = []
     b_ccd = timed_host(lambda: b_steps.append(ipctk.compute_collision_free_stepsize_batch(batch, Vd, V1d)), 0, 1)
-    del col, batch, Vd, V1d, BB, BB64
+    del col, batch, Vd, V1d, BB
     gc.collect()
     torch.cuda.synchronize()
     if rank != 0:
@@ -737,8 +782,8 @@ def run_gb300(args, rank, world):
     cfg = batch_config(C)
     cfg.update({"contacts_by_type": {"vv": int(counts[0]), "ev": int(counts[1]), "ee": int(counts[2]),
                                      "fv": int(counts[3])}, "hessian_nnz": int(nnz),
-                "precision": "mixed: FP32 distance derivatives except near-parallel edge-edge; FP64 PSD, "
-                             "mollifier, assembly", "tuning": {k: tune[k]["chosen"] for k in ("local", "psd")}})
+                "precision": PRECISION[HEADLINE_MODE], "mode": HEADLINE_MODE,
+                "tuning": {k: tune[k]["chosen"] for k in ("local", "psd")}})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -747,9 +792,9 @@ def run_gb300(args, rank, world):
         "config": cfg,
         "p50_ms": pct(per, 50), "p99_ms": pct(per, 99),
         "batched_vs_plain": value / plain["egh"]["value"],
-        "batched_fp64": {"value": C / (statistics.median(b64) / 1000.0), "unit": UNIT,
-                         "ms": statistics.median(b64)},
+        "batched_fp64": {"value": modes["fp64"]["value"], "unit": UNIT, "ms": modes["fp64"]["ms"]},
         "mixed_rel_error_vs_fp64": err,
+        "batched_modes": modes,
         "roofline": roof, "kernel_share": step_share,
         "cpu_baseline": cpu,
         "e2e": {"value": C / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),

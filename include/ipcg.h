@@ -303,9 +303,13 @@ int ipcg_barrier_batch(const ipcg_collisions* collisions, const ipcg_mesh* mesh,
 int ipcg_barrier_autotune(const ipcg_collisions* collisions, const ipcg_mesh* mesh, const double* vertices,
                           const double* dhat, const double* stiffness, int use_physical_barrier, int psd_method,
                           char* report, int64_t report_len, int64_t* needed);
-/* A stage's launch shape on the current device (get / set). */
+/* A stage's launch shape on the current device (get / set): the local
+ * Hessians, the FP64 projection, the df64 projection (IPCG_BARRIER_DF64_PSD).
+ * ipcg_barrier_autotune sets the local stage and the projection stage its
+ * options select. */
 #define IPCG_STAGE_LOCAL 0
 #define IPCG_STAGE_PSD 1
+#define IPCG_STAGE_PSD_DF64 2
 int ipcg_barrier_tuning(int stage, int* threads, int* blocks_per_sm, int* tiles_per_grab);
 int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles_per_grab);
 /* Testing switch: with on != 0, the df64 projection (IPCG_BARRIER_DF64_PSD)

@@ -774,7 +774,7 @@ int ipcg_barrier_autotune(const ipcg_collisions* c, const ipcg_mesh* mesh, const
 int ipcg_barrier_tuning(int stage, int* threads, int* blocks_per_sm, int* tiles_per_grab)
 {
     return guarded([&] {
-        require(stage == IPCG_STAGE_LOCAL || stage == IPCG_STAGE_PSD, "unknown stage");
+        require(stage == IPCG_STAGE_LOCAL || stage == IPCG_STAGE_PSD || stage == IPCG_STAGE_PSD_DF64, "unknown stage");
         require_device();
         const EghTuning t = egh_tuning(stage);
         if (threads) *threads = t.threads;
@@ -786,7 +786,7 @@ int ipcg_barrier_tuning(int stage, int* threads, int* blocks_per_sm, int* tiles_
 int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles_per_grab)
 {
     return guarded([&] {
-        require(stage == IPCG_STAGE_LOCAL || stage == IPCG_STAGE_PSD, "unknown stage");
+        require(stage == IPCG_STAGE_LOCAL || stage == IPCG_STAGE_PSD || stage == IPCG_STAGE_PSD_DF64, "unknown stage");
         require_device();
         egh_set_tuning(stage, EghTuning { threads, blocks_per_sm, tiles_per_grab });
     });

@@ -130,8 +130,8 @@ constexpr int WANT_E = 1, WANT_G = 2, WANT_H = 4;
 
 std::atomic<int> g_defer_df64 { 0 };
 std::mutex g_tune_mu;
-EghTuning g_tune[64][2];
-bool g_tune_set[64][2] = {};
+EghTuning g_tune[64][3];
+bool g_tune_set[64][3] = {};
 
 ContactsView full_view(const ipcg_collisions* cs)
 {
@@ -991,13 +991,15 @@ void egh_defer_df64(bool on) { g_defer_df64.store(on ? 1 : 0); }
 EghTuning egh_tuning(int stage)
 {
     const int d = device_index();
+    if (stage < 0 || stage > 2) stage = 1;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    return g_tune_set[d][stage & 1] ? g_tune[d][stage & 1] : EghTuning {};
+    return g_tune_set[d][stage] ? g_tune[d][stage] : EghTuning {};
 }
 
 void egh_set_tuning(int stage, const EghTuning& t)
 {
-    if (stage != 0 && stage != 1) throw Error(IPCG_ERR_INVALID, "tuning stage is 0 (local Hessians) or 1 (projection)");
+    if (stage < 0 || stage > 2)
+        throw Error(IPCG_ERR_INVALID, "tuning stage is 0 (local Hessians), 1 (FP64 projection) or 2 (df64 projection)");
     if (!(t.threads == 32 || t.threads == 64 || t.threads == 128) || t.blocks_per_sm < 1 || t.blocks_per_sm > 64
         || t.tiles_per_grab < 1 || t.tiles_per_grab > 64)
         throw Error(IPCG_ERR_INVALID, "tuning out of range: threads 32/64/128, blocks_per_sm 1-64, tiles_per_grab 1-64");
@@ -1042,8 +1044,8 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     C.hdev.p[0] = scr.dev(V, grad_dev, hess->val.p);
     IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
     IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(long long) * 4, s));
-    const EghTuning tune[2] = { egh_tuning(0), egh_tuning(1) };
     const bool df64 = a.df64_psd != 0;
+    const EghTuning tune[2] = { egh_tuning(0), egh_tuning(df64 ? 2 : 1) };
     if (prof::enabled()) {
         // per-kernel timing needs the launches themselves, not a replay
         enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
@@ -1136,6 +1138,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     std::string rep = "{\"workload_contacts\": " + std::to_string(ch.n) + ", \"device\": " + std::to_string(dev);
     const char* names[2] = { "local", "psd" };
     for (int stage = 0; stage < 2; ++stage) {
+        const int slot = stage == 0 ? 0 : (df64 ? 2 : 1);
         // stage 1 projects the local Hessians stage 0 left in the scratch
         EghTuning best {};
         float best_ms = 1e30f;
@@ -1163,10 +1166,11 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
             if (occ > 0 && occ < 32 && (occ & (occ - 1)) != 0) consider(EghTuning { threads, occ, 1 });
         }
         consider(EghTuning { best.threads, best.blocks_per_sm, 4 });
-        egh_set_tuning(stage, best);
-        char buf[200];
-        snprintf(buf, sizeof(buf), "], \"chosen\": {\"threads\": %d, \"blocks_per_sm\": %d, \"tiles_per_grab\": %d, "
-            "\"ms\": %.4f}}", best.threads, best.blocks_per_sm, best.tiles_per_grab, best_ms);
+        egh_set_tuning(slot, best);
+        char buf[220];
+        snprintf(buf, sizeof(buf), "], \"stage\": %d, \"chosen\": {\"threads\": %d, \"blocks_per_sm\": %d, "
+            "\"tiles_per_grab\": %d, \"ms\": %.4f}}", slot, best.threads, best.blocks_per_sm, best.tiles_per_grab,
+            best_ms);
         rep += buf;
         if (stage == 0) time_stage(0, best); // leave stage 0's output for stage 1
     }

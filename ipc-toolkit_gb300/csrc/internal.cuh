@@ -386,9 +386,9 @@ bool barrier_egh(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const 
 struct EghTuning {
     int threads = 64, blocks_per_sm = 4, tiles_per_grab = 1;
 };
-// Launch shapes of the two per-contact stages of the cached-pattern pass on
-// the current device: stage 0 the local Hessians, stage 1 the projection and
-// scatter.
+// Launch shapes of the per-contact stages of the cached-pattern pass on the
+// current device: 0 the local Hessians, 1 the FP64 projection and scatter,
+// 2 the df64 one.
 EghTuning egh_tuning(int stage);
 // Testing: the df64 projection defers every contact to its FP64 fix-up pass.
 void egh_defer_df64(bool on);

@@ -248,12 +248,13 @@ def autotune_barrier(collisions, mesh, vertices, dhat, stiffness, options: int =
     return json.loads(buf.value.decode())
 
 
-STAGE_LOCAL, STAGE_PSD = 0, 1
+STAGE_LOCAL, STAGE_PSD, STAGE_PSD_DF64 = 0, 1, 2
 
 
 def barrier_tuning(stage: int = STAGE_PSD) -> dict:
     """A stage's launch shape on the current device (ipcg_barrier_tuning):
-    STAGE_LOCAL the local Hessians, STAGE_PSD the projection and scatter."""
+    STAGE_LOCAL the local Hessians, STAGE_PSD the FP64 projection and
+    scatter, STAGE_PSD_DF64 the df64 one."""
     t, b, g = C.c_int(), C.c_int(), C.c_int()
     _check(_load().ipcg_barrier_tuning(int(stage), C.byref(t), C.byref(b), C.byref(g)))
     return {"threads": t.value, "blocks_per_sm": b.value, "tiles_per_grab": g.value}

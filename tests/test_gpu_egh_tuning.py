@@ -36,11 +36,12 @@ def _evaluate(ipctk, small_batch, mode):
 
 @pytest.mark.parametrize("mode", [False, "local_df64"])
 def test_results_do_not_depend_on_launch_shape(ipctk, small_batch, mode):
-    saved = [ipctk.barrier_tuning(s) for s in (ipctk.STAGE_LOCAL, ipctk.STAGE_PSD)]
+    stages = (ipctk.STAGE_LOCAL, ipctk.STAGE_PSD, ipctk.STAGE_PSD_DF64)
+    saved = [ipctk.barrier_tuning(s) for s in stages]
     try:
         ref = None
         for threads, bps, grab in ((32, 1, 1), (64, 4, 4), (128, 2, 1), (32, 16, 2)):
-            for stage in (ipctk.STAGE_LOCAL, ipctk.STAGE_PSD):
+            for stage in stages:
                 ipctk.set_barrier_tuning(stage, threads, bps, grab)
             assert ipctk.barrier_tuning(ipctk.STAGE_PSD) == {"threads": threads, "blocks_per_sm": bps,
                                                               "tiles_per_grab": grab}
@@ -54,7 +55,7 @@ def test_results_do_not_depend_on_launch_shape(ipctk, small_batch, mode):
             np.testing.assert_array_equal(H.indices, ref[2].indices)
             np.testing.assert_array_equal(H.data, ref[2].data)
     finally:
-        for stage, t in zip((ipctk.STAGE_LOCAL, ipctk.STAGE_PSD), saved):
+        for stage, t in zip(stages, saved):
             ipctk.set_barrier_tuning(stage, t["threads"], t["blocks_per_sm"], t["tiles_per_grab"])
 
 
@@ -64,17 +65,18 @@ def test_tuning_rejects_bad_shapes(ipctk):
     with pytest.raises(ValueError):
         ipctk.set_barrier_tuning(ipctk.STAGE_PSD, 64, 0, 1)
     with pytest.raises(ValueError):
-        ipctk.set_barrier_tuning(2, 64, 1, 1)
+        ipctk.set_barrier_tuning(3, 64, 1, 1)
 
 
 def test_autotune_reports_both_stages(ipctk, small_batch):
     batch, V, dh, kap, col = small_batch
-    saved = [ipctk.barrier_tuning(s) for s in (ipctk.STAGE_LOCAL, ipctk.STAGE_PSD)]
+    saved = [ipctk.barrier_tuning(s) for s in (ipctk.STAGE_LOCAL, ipctk.STAGE_PSD_DF64)]
     try:
         BB = ipctk.BatchBarrierPotential(dh, kap, mixed_precision="local_df64")
         rep = BB.autotune(col, batch, V)
         assert rep["workload_contacts"] == len(col)
-        for stage, name in ((ipctk.STAGE_LOCAL, "local"), (ipctk.STAGE_PSD, "psd")):
+        assert rep["psd"]["stage"] == ipctk.STAGE_PSD_DF64
+        for stage, name in ((ipctk.STAGE_LOCAL, "local"), (ipctk.STAGE_PSD_DF64, "psd")):
             cands = rep[name]["candidates"]
             assert len(cands) >= 3 and all(c["ms"] > 0 for c in cands)
             chosen = rep[name]["chosen"]
@@ -82,7 +84,7 @@ def test_autotune_reports_both_stages(ipctk, small_batch):
             assert ipctk.barrier_tuning(stage) == {k: chosen[k] for k in ("threads", "blocks_per_sm",
                                                                           "tiles_per_grab")}
     finally:
-        for stage, t in zip((ipctk.STAGE_LOCAL, ipctk.STAGE_PSD), saved):
+        for stage, t in zip((ipctk.STAGE_LOCAL, ipctk.STAGE_PSD_DF64), saved):
             ipctk.set_barrier_tuning(stage, t["threads"], t["blocks_per_sm"], t["tiles_per_grab"])
 
 
