@@ -41,16 +41,12 @@ namespace {
 constexpr int CCD_HEAP = 64;
 constexpr int CCD_STACK = 184;
 constexpr int BLOCK = 128;
-// Two passes over the candidates.  Pass 1 runs every query with a small box
-// budget, pruned by the earliest time found so far (re-read as it runs); a
-// query that does not finish within the budget is deferred to the hard pass,
-// which starts it again with the then earliest time as its horizon and runs
-// it to completion.
+// The budgeted pass runs the queries (sorted by a lower bound on their time
+// of impact) with a box budget, pruned by the earliest time found so far
+// (re-read as it runs); a query that does not finish within the budget is
+// deferred to the hard pass, which starts it again with the then earliest
+// time as its horizon and runs it to completion.
 constexpr long long CCD_PASS1_BUDGET = 512;
-// A first pass with a few boxes settles the many candidates whose first
-// inclusion tests exclude a root, and compacts the rest, so the 512-box pass
-// runs with full warps of candidates that need subdividing.
-constexpr long long CCD_PASS0_BUDGET = 8;
 
 struct Query {
     V3 s[4], e[4];
@@ -526,6 +522,93 @@ __device__ int stencil_ccd(Query& q, double min_distance, const CCDParams& P, do
     return strategy(q, min_distance, d0, P, adj, tmax, toi, shared_best, bud);
 }
 
+// A lower bound on the time of impact stencil_ccd can return for a query
+// (+inf when it can only miss).  For one coordinate c, the co-planarity
+// function F_c(t, u, v) is linear in t at each corner (u, v) of [0, 1]^2, so
+// g(t) = min and h(t) = max of F_c(t, ., .) over [0, 1]^2 are the min and max
+// of four lines.  A box [t0, t1] x U x V that the inclusion test keeps has,
+// in every coordinate, a corner box meeting [-r, r] (r = err + ms), hence a
+// time t in [t0, t1] with g(t) <= r and h(t) >= -r (g and h bound F_c over
+// any (u, v), and are continuous).  So every kept box ends at or after
+// T = max_c T_c, T_c the first such time, and an accepted box starts at or
+// after T minus its own width in t -- which is below the time tolerance
+// unless the box was accepted for its narrow codomain (then every coordinate
+// lies within r + delta over the whole box, so T computed with r + delta is
+// at most its start) or for lying inside (then T is at most its start).  T is
+// computed with r + delta + 2 err (the corner values' rounding), the
+// candidate times are tested with a relative slack, and the result is
+// lowered by the time tolerance and a relative 1e-9.  Only used to skip
+// queries that cannot lower the earliest time found so far (and only when
+// it is at least 1e-6, above which the strategy's small-ToI rerun cannot
+// apply).
+__device__ double toi_lower_bound(const Query& q, double min_distance, const CCDParams& P)
+{
+    const double INF = __longlong_as_double(0x7ff0000000000000LL);
+    double d2;
+    if (q.vf) d2 = point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
+        point_triangle_distance_type(q.s[0], q.s[1], q.s[2], q.s[3]));
+    else d2 = edge_edge_distance(q.s[0], q.s[1], q.s[2], q.s[3],
+        edge_edge_distance_type(q.s[0], q.s[1], q.s[2], q.s[3]));
+    const double d0 = sqrt(d2);
+    if (d0 <= min_distance) return 0.0;
+    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) return INF;
+    const double ms = fmin((1.0 - P.rescale) * (d0 - min_distance), 1e-4) + min_distance;
+    const double delta = fmin(0.5 * d0, P.tolerance);
+    double err[3];
+    numerical_error(q, ms > 0, err);
+    double T = 0.0;
+    for (int c = 0; c < 3; ++c) {
+        // corner lines a + b t at (u, v) in {0, 1}^2
+        double A[4], B[4];
+        for (int k = 0; k < 4; ++k) {
+            const double u = (k & 1) ? 1.0 : 0.0, v = (k & 2) ? 1.0 : 0.0;
+            const double s0 = comp(q.s[0], c), s1 = comp(q.s[1], c), s2 = comp(q.s[2], c), s3 = comp(q.s[3], c);
+            const double e0 = comp(q.d[0], c), e1 = comp(q.d[1], c), e2 = comp(q.d[2], c), e3 = comp(q.d[3], c);
+            if (q.vf) {
+                A[k] = s0 - s1 - u * (s2 - s1) - v * (s3 - s1);
+                B[k] = e0 - e1 - u * (e2 - e1) - v * (e3 - e1);
+            } else {
+                A[k] = s0 + u * (s1 - s0) - s2 - v * (s3 - s2);
+                B[k] = e0 + u * (e1 - e0) - e2 - v * (e3 - e2);
+            }
+        }
+        const double R = 3.0 * err[c] + ms + delta;
+        double slack = R;
+        for (int k = 0; k < 4; ++k) slack = fmax(slack, fabs(A[k]) + fabs(B[k]));
+        slack *= 1e-12;
+        // the first time in {g <= R} and {h >= -R}: 0 or a time where a
+        // line enters one of them
+        double Tc = INF;
+        for (int j = 0; j < 9; ++j) {
+            double tj;
+            if (j == 0) tj = 0.0;
+            else {
+                const int k = (j - 1) >> 1;
+                if (j & 1) {
+                    if (!(B[k] < 0)) continue;
+                    tj = (R - A[k]) / B[k];
+                } else {
+                    if (!(B[k] > 0)) continue;
+                    tj = (-R - A[k]) / B[k];
+                }
+                if (!(tj >= 0.0 && tj <= 1.0) || !(tj < Tc)) continue;
+            }
+            double g = A[0] + B[0] * tj, h = g;
+            for (int k = 1; k < 4; ++k) {
+                const double f = A[k] + B[k] * tj;
+                g = fmin(g, f);
+                h = fmax(h, f);
+            }
+            if (g <= R + slack && h >= -R - slack) Tc = fmin(Tc, tj);
+        }
+        if (!(Tc < INF)) return INF;
+        T = fmax(T, Tc);
+    }
+    double tol[3];
+    domain_tol(q, delta, tol);
+    return fmax(0.0, (T - tol[0] - 0x1p-60) * (1.0 - 1e-9) - 1e-12);
+}
+
 // Loads candidate i; returns its first vertex (which names its scene).
 __device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_ee, int n_ee,
     const int2* __restrict__ cand_fv, const double* __restrict__ V0, const double* __restrict__ V1,
@@ -555,6 +638,24 @@ __device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_e
     return ids[0];
 }
 
+// Per candidate: its lower bound (by candidate index) and, for sorting the
+// queries by it, its bit pattern (non-negative doubles order like their
+// bits) with the candidate index.
+__global__ void k_ccd_bound(const int2* __restrict__ cand_ee, int n_ee, const int2* __restrict__ cand_fv, int n_fv,
+    const double* __restrict__ V0, const double* __restrict__ V1, const int* __restrict__ E, const int* __restrict__ F,
+    const double* __restrict__ min_distance, SceneView sv, CCDParams P, double* __restrict__ lb,
+    unsigned long long* __restrict__ keys, int* __restrict__ ids)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_ee + n_fv) return;
+    Query q;
+    const int scene = sv.of(load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q));
+    const double b = toi_lower_bound(q, __ldg(min_distance + scene), P);
+    lb[i] = b;
+    keys[i] = (unsigned long long)__double_as_longlong(b);
+    ids[i] = i;
+}
+
 // One thread per candidate (candidates.cpp:252-292).  With a box budget
 // (pass 1) a query that does not finish within it is appended to `hard`
 // instead; those are run to completion in pass 2 (hard != null selects the
@@ -566,16 +667,23 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
     const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,
     CCDParams P, unsigned long long* toi_bits, long long budget, const int* __restrict__ list,
-    const int* __restrict__ list_n, int* __restrict__ hard, int* __restrict__ hard_n, int any_hit)
+    const int* __restrict__ list_n, int list_len, int* __restrict__ hard, int* __restrict__ hard_n, int any_hit,
+    const double* __restrict__ lb)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int n = list ? *list_n : n_ee + n_fv;
+    const int n = list ? (list_n ? *list_n : list_len) : n_ee + n_fv;
     if (t >= n) return;
     const int i = list ? list[t] : t;
     Query q;
     const int scene = sv.of(load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q));
     unsigned long long* best = toi_bits + scene;
     const double tmax = __longlong_as_double((long long)*(volatile unsigned long long*)best);
+    // a query whose time of impact cannot come before the scene's earliest
+    // so far cannot change the result
+    if (lb) {
+        const double b = lb[i];
+        if (b >= 1e-6 && b >= tmax) return;
+    }
     double toi = __longlong_as_double(0x7ff0000000000000ULL);
     Budget bud { budget, 0 };
     const int st = stencil_ccd(q, __ldg(min_distance + scene), P, tmax, toi, best, bud);
@@ -633,30 +741,41 @@ __global__ void k_distance_stencils(int kind, int n, const double* __restrict__ 
 
 } // namespace
 
-// The two CCD passes over candidate lists (EE pairs, then FV (face, vertex)
-// pairs): pass 1 with a box budget, then the unfinished queries to
-// completion.  toi_bits (one per scene, set by the caller) is the scene's
-// earliest time so far; with any_hit a hit sets it to 0 instead.
+// The CCD passes over candidate lists (EE pairs, then FV (face, vertex)
+// pairs).  Every query first gets a lower bound on its time of impact; the
+// queries are sorted by it, so that each scene's likely earliest impacts run
+// first and set its earliest time, which then skips every query whose bound
+// is not below it.  The sorted list runs with a box budget, then the
+// unfinished queries to completion.  toi_bits (one per scene, set by the
+// caller) is the scene's earliest time so far; with any_hit a hit sets it to
+// 0 instead.
 void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, int64_t n_fv, const double* V0,
     const double* V1, const double* md, const CCDParams& P, int any_hit)
 {
     cudaStream_t s = m->stream;
     const SceneView sv = scene_view(m);
+    if (n_ee + n_fv >= (int64_t)INT32_MAX) throw Error(IPCG_ERR_INVALID, "too many CCD candidates");
     const int nc = (int)(n_ee + n_fv);
     if (nc == 0) return;
-    m->ivals_a.reserve(2 * (nc + 1));
-    int* open = m->ivals_a.p;           // left by pass 0
-    int* hard = m->ivals_a.p + nc + 1;  // left by pass 1
+    m->ivals_a.reserve(nc + 1);
+    m->ivals_b.reserve(2 * (nc + 1));
+    m->keys_a.reserve(nc + 1);
+    m->keys_b.reserve(nc + 1);
+    m->ccd_lb.reserve(nc + 1);
+    int* hard = m->ivals_a.p;           // left by the budgeted pass
+    int* ids = m->ivals_b.p;
+    int* sorted = m->ivals_b.p + nc + 1;
     m->counters.reserve(32);
-    int* open_n = m->counters.p + 30;
     int* hard_n = m->counters.p + 31;
-    IPCG_CUDA(cudaMemsetAsync(open_n, 0, 2 * sizeof(int), s));
-    IPCG_LAUNCH("k_ccd_pass0", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS0_BUDGET, nullptr, nullptr, open, open_n, any_hit));
+    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
+    IPCG_LAUNCH("k_ccd_bound", s, k_ccd_bound<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv,
+        V0, V1, m->E.p, m->F.p, md, sv, P, m->ccd_lb.p, m->keys_a.p, ids));
+    sort_pairs_u64(m, s, m->keys_a.p, m->keys_b.p, ids, sorted, nc, 64);
     IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, open, open_n, hard, hard_n, any_hit));
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, sorted, nullptr, nc, hard, hard_n, any_hit,
+        m->ccd_lb.p));
     IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, any_hit));
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, 0, nullptr, nullptr, any_hit, m->ccd_lb.p));
 }
 
 void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, const double* min_distance,

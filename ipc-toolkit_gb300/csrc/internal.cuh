@@ -217,6 +217,7 @@ struct ipcg_mesh {
     ipcg::HBuf<int> h_counters;
     ipcg::DBuf<char> tmp;            // CUB temporary storage
     ipcg::DBuf<unsigned long long> keys_a, keys_b;
+    ipcg::DBuf<double> ccd_lb; // per CCD candidate: lower bound on its time of impact
     ipcg::DBuf<int> ivals_a, ivals_b;
     ipcg::DBuf<int8_t> i8tmp;
     ipcg::DBuf<double> partial;      // reduction partials

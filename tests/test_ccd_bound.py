@@ -1,0 +1,111 @@
+"""The lower bound on a query's time of impact that lets the step-size pass
+skip queries (ccd.cu, toi_lower_bound), restated in numpy and checked against
+the oracle's Tight-Inclusion times of impact (oracle ccd_stencils, which
+follows tight_inclusion_ccd.cpp:33-336) on the candidates of the two-sheet
+scene and of batch scenes: the bound must never exceed a query's time of
+impact, so a query whose bound is at or after the earliest time found so far
+cannot change the step.  Also checks that the bound prunes: most queries of
+a colliding scene have bounds after the scene's earliest impact.
+"""
+import numpy as np
+import pytest
+
+INF = np.inf
+
+
+def _num_err(s, e, vf):
+    filt = 7.549516567451064e-15 if vf else 7.105427357601002e-15  # with a minimum separation
+    m = np.maximum(np.abs(s).max(axis=1), np.abs(e).max(axis=1))
+    return filt * np.minimum(m, 1.0) ** 3
+
+
+def _F(s, e, vf, t, u, v):
+    x = s + (e - s) * t
+    if vf:
+        return x[:, 0] - (x[:, 1] + u * (x[:, 2] - x[:, 1]) + v * (x[:, 3] - x[:, 1]))
+    return (x[:, 0] + u * (x[:, 1] - x[:, 0])) - (x[:, 2] + v * (x[:, 3] - x[:, 2]))
+
+
+def _tol_t(s, e, vf, delta):
+    L = np.zeros(s.shape[0])
+    for u in (0.0, 1.0):
+        for v in (0.0, 1.0):
+            L = np.maximum(L, np.abs(_F(s, e, vf, 1.0, u, v) - _F(s, e, vf, 0.0, u, v)).max(axis=1))
+    L = 3 * L
+    return np.where(L == 0, delta, delta / np.where(L == 0, 1.0, L))
+
+
+def _first_time(A, B, R):
+    """First t in [0, 1] with min_k(A_k + B_k t) <= R and max_k(...) >= -R."""
+    n = A.shape[1]
+    slack = 1e-12 * np.maximum(R, (np.abs(A) + np.abs(B)).max(axis=0))
+    starts = [np.zeros(n)]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        for k in range(4):
+            starts.append(np.where(B[k] < 0, (R - A[k]) / B[k], np.nan))
+            starts.append(np.where(B[k] > 0, (-R - A[k]) / B[k], np.nan))
+    T = np.full(n, INF)
+    for t in starts:
+        ok = (t >= 0) & (t <= 1)
+        tc = np.clip(np.nan_to_num(t, nan=0.0), 0.0, 1.0)
+        f = A + B * tc
+        T = np.where(ok & (f.min(axis=0) <= R + slack) & (f.max(axis=0) >= -R - slack), np.minimum(T, tc), T)
+    return T
+
+
+def toi_lower_bound(x0, x1, d0, vf, min_distance=0.0, tolerance=1e-6, rescale=0.8):
+    ms = np.minimum((1 - rescale) * (d0 - min_distance), 1e-4) + min_distance
+    delta = np.minimum(0.5 * d0, tolerance)
+    err = _num_err(x0, x1, vf)
+    d = x1 - x0
+    T = np.zeros(x0.shape[0])
+    for c in range(3):
+        A, B = [], []
+        for k in range(4):
+            u, v = float(k & 1), float((k >> 1) & 1)
+            s_, e_ = x0[:, :, c], d[:, :, c]
+            if vf:
+                A.append(s_[:, 0] - s_[:, 1] - u * (s_[:, 2] - s_[:, 1]) - v * (s_[:, 3] - s_[:, 1]))
+                B.append(e_[:, 0] - e_[:, 1] - u * (e_[:, 2] - e_[:, 1]) - v * (e_[:, 3] - e_[:, 1]))
+            else:
+                A.append(s_[:, 0] + u * (s_[:, 1] - s_[:, 0]) - s_[:, 2] - v * (s_[:, 3] - s_[:, 2]))
+                B.append(e_[:, 0] + u * (e_[:, 1] - e_[:, 0]) - e_[:, 2] - v * (e_[:, 3] - e_[:, 2]))
+        T = np.maximum(T, _first_time(np.array(A), np.array(B), 3 * err[:, c] + ms + delta))
+    with np.errstate(invalid="ignore"):
+        out = np.maximum(0.0, (T - _tol_t(x0, x1, vf, delta) - 2.0 ** -60) * (1 - 1e-9) - 1e-12)
+    out = np.where(np.isinf(T), INF, out)
+    out = np.where(np.all(x0 == x1, axis=(1, 2)), INF, out)
+    return np.where(d0 <= min_distance, 0.0, out)
+
+
+def _d0(oracle_mod, x0, vf):
+    f = oracle_mod.point_triangle_distance if vf else oracle_mod.edge_edge_distance
+    return np.sqrt(np.array([f(a[0], a[1], a[2], a[3]) for a in x0]))
+
+
+@pytest.mark.parametrize("scene", ["two_sheet", "batch0", "batch8"])
+def test_bound_never_exceeds_time_of_impact(oracle_mod, scene):
+    from ipctk_gb300 import scenes
+    if scene == "two_sheet":
+        sc = scenes.two_sheet()
+    else:
+        sc = scenes.batch()[int(scene[5:])]
+    V0, V1, E, F = sc["V"], sc["V1"], sc["E"], sc["F"]
+    ee, fv = oracle_mod.ccd_candidates(V0, V1, E, F)
+    (xe0, xe1), (xf0, xf1) = oracle_mod.ccd_stencil_positions(V0, V1, E, F, ee, fv)
+    rng = np.random.default_rng(0)
+    earliest, pruned, total = INF, 0, 0
+    bounds = []
+    for vf, x0, x1 in ((False, xe0, xe1), (True, xf0, xf1)):
+        # a seeded sample keeps the oracle's root finding to seconds
+        pick = rng.choice(x0.shape[0], size=min(x0.shape[0], 6000), replace=False)
+        x0, x1 = x0[pick], x1[pick]
+        hit, toi, _ = oracle_mod.ccd_stencils(0 if vf else 1, x0, x1)
+        lb = toi_lower_bound(x0, x1, _d0(oracle_mod, x0, vf), vf)
+        assert np.all(lb[hit] <= toi[hit]), (vf, np.max(lb[hit] - toi[hit]))
+        earliest = min(earliest, toi[hit].min() if hit.any() else INF)
+        bounds.append(lb)
+    lb = np.concatenate(bounds)
+    # the scenes collide: most queries are skipped once the earliest impact is known
+    assert earliest < 1.0
+    assert np.mean(lb >= earliest) > 0.5
