@@ -47,6 +47,10 @@ constexpr int BLOCK = 128;
 // deferred to the hard pass, which starts it again with the then earliest
 // time as its horizon and runs it to completion.
 constexpr long long CCD_PASS1_BUDGET = 512;
+// The seed queries (each scene's first queries by their lower bound) run
+// first with a larger budget, so that a scene's earliest time is known
+// before the bulk of its queries runs.
+constexpr long long CCD_SEED_BUDGET = 8192;
 
 struct Query {
     V3 s[4], e[4];
@@ -535,12 +539,12 @@ __device__ int stencil_ccd(Query& q, double min_distance, const CCDParams& P, do
 // unless the box was accepted for its narrow codomain (then every coordinate
 // lies within r + delta over the whole box, so T computed with r + delta is
 // at most its start) or for lying inside (then T is at most its start).  T is
-// computed with r + delta + 2 err (the corner values' rounding), the
-// candidate times are tested with a relative slack, and the result is
-// lowered by the time tolerance and a relative 1e-9.  Only used to skip
-// queries that cannot lower the earliest time found so far (and only when
-// it is at least 1e-6, above which the strategy's small-ToI rerun cannot
-// apply).
+// computed with r + delta + 2 err (the corner values' rounding); the search
+// for the first time runs in FP32 on the FP64 corner lines, with slacks that
+// cover its rounding, and the result is lowered by 2^-20, the time tolerance
+// and a relative 1e-6.  Only used to skip queries that cannot lower the
+// earliest time found so far (and only when it is at least 1e-6, above which
+// the strategy's small-ToI rerun cannot apply).
 __device__ double toi_lower_bound(const Query& q, double min_distance, const CCDParams& P)
 {
     const double INF = __longlong_as_double(0x7ff0000000000000LL);
@@ -556,57 +560,64 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
     const double delta = fmin(0.5 * d0, P.tolerance);
     double err[3];
     numerical_error(q, ms > 0, err);
-    double T = 0.0;
+    double T = 0.0, bmax = 0.0;
     for (int c = 0; c < 3; ++c) {
-        // corner lines a + b t at (u, v) in {0, 1}^2
-        double A[4], B[4];
+        // corner lines a + b t at (u, v) in {0, 1}^2 (FP64), then the search
+        // in FP32 with a slack that covers its rounding (2^-20 of the lines'
+        // size) and a final 2^-20 margin on the time
+        float A[4], B[4];
+        float slack = 0.f;
         for (int k = 0; k < 4; ++k) {
             const double u = (k & 1) ? 1.0 : 0.0, v = (k & 2) ? 1.0 : 0.0;
             const double s0 = comp(q.s[0], c), s1 = comp(q.s[1], c), s2 = comp(q.s[2], c), s3 = comp(q.s[3], c);
             const double e0 = comp(q.d[0], c), e1 = comp(q.d[1], c), e2 = comp(q.d[2], c), e3 = comp(q.d[3], c);
+            double a, b;
             if (q.vf) {
-                A[k] = s0 - s1 - u * (s2 - s1) - v * (s3 - s1);
-                B[k] = e0 - e1 - u * (e2 - e1) - v * (e3 - e1);
+                a = s0 - s1 - u * (s2 - s1) - v * (s3 - s1);
+                b = e0 - e1 - u * (e2 - e1) - v * (e3 - e1);
             } else {
-                A[k] = s0 + u * (s1 - s0) - s2 - v * (s3 - s2);
-                B[k] = e0 + u * (e1 - e0) - e2 - v * (e3 - e2);
+                a = s0 + u * (s1 - s0) - s2 - v * (s3 - s2);
+                b = e0 + u * (e1 - e0) - e2 - v * (e3 - e2);
             }
+            bmax = fmax(bmax, fabs(b));
+            A[k] = (float)a;
+            B[k] = (float)b;
+            slack = fmaxf(slack, fabsf(A[k]) + fabsf(B[k]));
         }
-        const double R = 3.0 * err[c] + ms + delta;
-        double slack = R;
-        for (int k = 0; k < 4; ++k) slack = fmax(slack, fabs(A[k]) + fabs(B[k]));
-        slack *= 1e-12;
+        const float R = (float)(3.0 * err[c] + ms + delta);
+        slack = (slack + R) * 0x1p-20f;
         // the first time in {g <= R} and {h >= -R}: 0 or a time where a
         // line enters one of them
-        double Tc = INF;
+        float Tc = __int_as_float(0x7f800000);
         for (int j = 0; j < 9; ++j) {
-            double tj;
-            if (j == 0) tj = 0.0;
+            float tj;
+            if (j == 0) tj = 0.f;
             else {
                 const int k = (j - 1) >> 1;
                 if (j & 1) {
-                    if (!(B[k] < 0)) continue;
+                    if (!(B[k] < 0.f)) continue;
                     tj = (R - A[k]) / B[k];
                 } else {
-                    if (!(B[k] > 0)) continue;
+                    if (!(B[k] > 0.f)) continue;
                     tj = (-R - A[k]) / B[k];
                 }
-                if (!(tj >= 0.0 && tj <= 1.0) || !(tj < Tc)) continue;
+                if (!(tj >= 0.f && tj <= 1.f) || !(tj < Tc)) continue;
             }
-            double g = A[0] + B[0] * tj, h = g;
+            float g = A[0] + B[0] * tj, h = g;
             for (int k = 1; k < 4; ++k) {
-                const double f = A[k] + B[k] * tj;
-                g = fmin(g, f);
-                h = fmax(h, f);
+                const float f = A[k] + B[k] * tj;
+                g = fminf(g, f);
+                h = fmaxf(h, f);
             }
-            if (g <= R + slack && h >= -R - slack) Tc = fmin(Tc, tj);
+            if (g <= R + slack && h >= -R - slack) Tc = fminf(Tc, tj);
         }
-        if (!(Tc < INF)) return INF;
-        T = fmax(T, Tc);
+        if (!(Tc <= 1.f)) return INF;
+        T = fmax(T, (double)Tc);
     }
-    double tol[3];
-    domain_tol(q, delta, tol);
-    return fmax(0.0, (T - tol[0] - 0x1p-60) * (1.0 - 1e-9) - 1e-12);
+    // the time tolerance of the inclusion search: delta / (3 max |F(1) - F(0)|)
+    // over the corners, F(1) - F(0) being the corner lines' slopes
+    const double tol0 = bmax == 0.0 ? delta : delta / (3.0 * bmax);
+    return fmax(0.0, (T - 0x1p-20 - tol0 * (1.0 + 1e-6) - 0x1p-60) * (1.0 - 1e-6));
 }
 
 // Loads candidate i; returns its first vertex (which names its scene).
@@ -641,6 +652,9 @@ __device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_e
 // Per candidate: its lower bound (by candidate index) and, for sorting the
 // queries by it, its bit pattern (non-negative doubles order like their
 // bits) with the candidate index.
+// keys: scene in the top 20 bits, then the bound's leading 44 bits (its
+// sign is clear), so that a scene's queries sort together by bound.
+constexpr int CCD_SCENE_SHIFT = 44;
 __global__ void k_ccd_bound(const int2* __restrict__ cand_ee, int n_ee, const int2* __restrict__ cand_fv, int n_fv,
     const double* __restrict__ V0, const double* __restrict__ V1, const int* __restrict__ E, const int* __restrict__ F,
     const double* __restrict__ min_distance, SceneView sv, CCDParams P, double* __restrict__ lb,
@@ -652,8 +666,31 @@ __global__ void k_ccd_bound(const int2* __restrict__ cand_ee, int n_ee, const in
     const int scene = sv.of(load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q));
     const double b = toi_lower_bound(q, __ldg(min_distance + scene), P);
     lb[i] = b;
-    keys[i] = (unsigned long long)__double_as_longlong(b);
+    keys[i] = ((unsigned long long)scene << CCD_SCENE_SHIFT) | ((unsigned long long)__double_as_longlong(b) >> 20);
     ids[i] = i;
+}
+
+// First sorted position of every scene that has queries.
+__global__ void k_ccd_segments(const unsigned long long* __restrict__ keys, int n, int* __restrict__ seg)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int scene = (int)(keys[p] >> CCD_SCENE_SHIFT);
+    if (p == 0 || (int)(keys[p - 1] >> CCD_SCENE_SHIFT) != scene) seg[scene] = p;
+}
+
+// The seed list: each scene's first CCD_SEEDS queries by bound (thread
+// k * CCD_SEEDS + j takes the j-th of scene k, if it has one).
+constexpr int CCD_SEEDS = 32;
+__global__ void k_ccd_seed_list(const unsigned long long* __restrict__ keys, const int* __restrict__ sorted, int n,
+    const int* __restrict__ seg, int n_scenes, int* __restrict__ seeds, int* __restrict__ n_seeds)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_scenes * CCD_SEEDS) return;
+    const int k = t / CCD_SEEDS, j = t % CCD_SEEDS;
+    const int p = seg[k] + j;
+    if (seg[k] < 0 || p >= n || (int)(keys[p] >> CCD_SCENE_SHIFT) != k) return;
+    seeds[atomicAdd(n_seeds, 1)] = sorted[p];
 }
 
 // One thread per candidate (candidates.cpp:252-292).  With a box budget
@@ -668,7 +705,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,
     CCDParams P, unsigned long long* toi_bits, long long budget, const int* __restrict__ list,
     const int* __restrict__ list_n, int list_len, int* __restrict__ hard, int* __restrict__ hard_n, int any_hit,
-    const double* __restrict__ lb)
+    const double* __restrict__ lb, const int* __restrict__ seg)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = list ? (list_n ? *list_n : list_len) : n_ee + n_fv;
@@ -676,6 +713,8 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     const int i = list ? list[t] : t;
     Query q;
     const int scene = sv.of(load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q));
+    // the sorted list's first CCD_SEEDS queries of each scene ran as seeds
+    if (seg && t - seg[scene] < CCD_SEEDS) return;
     unsigned long long* best = toi_bits + scene;
     const double tmax = __longlong_as_double((long long)*(volatile unsigned long long*)best);
     // a query whose time of impact cannot come before the scene's earliest
@@ -755,27 +794,42 @@ void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, in
     cudaStream_t s = m->stream;
     const SceneView sv = scene_view(m);
     if (n_ee + n_fv >= (int64_t)INT32_MAX) throw Error(IPCG_ERR_INVALID, "too many CCD candidates");
+    if (m->n_scenes >= (1 << (64 - CCD_SCENE_SHIFT))) throw Error(IPCG_ERR_INVALID, "too many scenes for the CCD");
     const int nc = (int)(n_ee + n_fv);
     if (nc == 0) return;
-    m->ivals_a.reserve(nc + 1);
+    const int ns = (int)m->n_scenes;
+    m->ivals_a.reserve((int64_t)nc + 1 + ns + (int64_t)ns * CCD_SEEDS + 1);
     m->ivals_b.reserve(2 * (nc + 1));
     m->keys_a.reserve(nc + 1);
     m->keys_b.reserve(nc + 1);
     m->ccd_lb.reserve(nc + 1);
-    int* hard = m->ivals_a.p;           // left by the budgeted pass
+    int* hard = m->ivals_a.p;                       // left by the budgeted passes
+    int* seg = m->ivals_a.p + nc + 1;               // per scene: its first sorted position
+    int* seeds = m->ivals_a.p + nc + 1 + ns;        // each scene's first queries by bound
     int* ids = m->ivals_b.p;
     int* sorted = m->ivals_b.p + nc + 1;
     m->counters.reserve(32);
+    int* seeds_n = m->counters.p + 30;
     int* hard_n = m->counters.p + 31;
-    IPCG_CUDA(cudaMemsetAsync(hard_n, 0, sizeof(int), s));
+    IPCG_CUDA(cudaMemsetAsync(seeds_n, 0, 2 * sizeof(int), s));
+    IPCG_CUDA(cudaMemsetAsync(seg, 0xff, sizeof(int) * ns, s));
     IPCG_LAUNCH("k_ccd_bound", s, k_ccd_bound<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv,
         V0, V1, m->E.p, m->F.p, md, sv, P, m->ccd_lb.p, m->keys_a.p, ids));
     sort_pairs_u64(m, s, m->keys_a.p, m->keys_b.p, ids, sorted, nc, 64);
+    IPCG_LAUNCH("k_ccd_segments", s, k_ccd_segments<<<grid_for(nc, 256), 256, 0, s>>>(m->keys_b.p, nc, seg));
+    IPCG_LAUNCH("k_ccd_seed_list", s, k_ccd_seed_list<<<grid_for((int64_t)ns * CCD_SEEDS, 256), 256, 0, s>>>(
+        m->keys_b.p, sorted, nc, seg, ns, seeds, seeds_n));
+    // seeds first: each scene's likeliest earliest impacts set its earliest
+    // time before the bulk of its queries runs
+    IPCG_LAUNCH("k_ccd_seeds", s, k_ccd<<<grid_for((int64_t)ns * CCD_SEEDS, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee,
+        cfv, (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_SEED_BUDGET, seeds, seeds_n, 0, hard,
+        hard_n, any_hit, m->ccd_lb.p, nullptr));
     IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
         m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, sorted, nullptr, nc, hard, hard_n, any_hit,
-        m->ccd_lb.p));
+        m->ccd_lb.p, seg));
     IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, 0, nullptr, nullptr, any_hit, m->ccd_lb.p));
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, 0, nullptr, nullptr, any_hit, m->ccd_lb.p,
+        nullptr));
 }
 
 void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, const double* min_distance,

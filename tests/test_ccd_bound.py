@@ -19,35 +19,23 @@ def _num_err(s, e, vf):
     return filt * np.minimum(m, 1.0) ** 3
 
 
-def _F(s, e, vf, t, u, v):
-    x = s + (e - s) * t
-    if vf:
-        return x[:, 0] - (x[:, 1] + u * (x[:, 2] - x[:, 1]) + v * (x[:, 3] - x[:, 1]))
-    return (x[:, 0] + u * (x[:, 1] - x[:, 0])) - (x[:, 2] + v * (x[:, 3] - x[:, 2]))
-
-
-def _tol_t(s, e, vf, delta):
-    L = np.zeros(s.shape[0])
-    for u in (0.0, 1.0):
-        for v in (0.0, 1.0):
-            L = np.maximum(L, np.abs(_F(s, e, vf, 1.0, u, v) - _F(s, e, vf, 0.0, u, v)).max(axis=1))
-    L = 3 * L
-    return np.where(L == 0, delta, delta / np.where(L == 0, 1.0, L))
-
-
 def _first_time(A, B, R):
-    """First t in [0, 1] with min_k(A_k + B_k t) <= R and max_k(...) >= -R."""
+    """First t in [0, 1] with min_k(A_k + B_k t) <= R and max_k(...) >= -R,
+    searched in FP32 on the FP64 corner lines with a 2^-20 slack."""
+    A = A.astype(np.float32)
+    B = B.astype(np.float32)
+    R = R.astype(np.float32)
     n = A.shape[1]
-    slack = 1e-12 * np.maximum(R, (np.abs(A) + np.abs(B)).max(axis=0))
-    starts = [np.zeros(n)]
+    slack = ((np.abs(A) + np.abs(B)).max(axis=0) + R) * np.float32(2.0 ** -20)
+    starts = [np.zeros(n, np.float32)]
     with np.errstate(divide="ignore", invalid="ignore"):
         for k in range(4):
-            starts.append(np.where(B[k] < 0, (R - A[k]) / B[k], np.nan))
-            starts.append(np.where(B[k] > 0, (-R - A[k]) / B[k], np.nan))
+            starts.append(np.where(B[k] < 0, (R - A[k]) / B[k], np.nan).astype(np.float32))
+            starts.append(np.where(B[k] > 0, (-R - A[k]) / B[k], np.nan).astype(np.float32))
     T = np.full(n, INF)
     for t in starts:
         ok = (t >= 0) & (t <= 1)
-        tc = np.clip(np.nan_to_num(t, nan=0.0), 0.0, 1.0)
+        tc = np.clip(np.nan_to_num(t, nan=0.0), 0.0, 1.0).astype(np.float32)
         f = A + B * tc
         T = np.where(ok & (f.min(axis=0) <= R + slack) & (f.max(axis=0) >= -R - slack), np.minimum(T, tc), T)
     return T
@@ -59,6 +47,7 @@ def toi_lower_bound(x0, x1, d0, vf, min_distance=0.0, tolerance=1e-6, rescale=0.
     err = _num_err(x0, x1, vf)
     d = x1 - x0
     T = np.zeros(x0.shape[0])
+    bmax = np.zeros(x0.shape[0])
     for c in range(3):
         A, B = [], []
         for k in range(4):
@@ -70,9 +59,12 @@ def toi_lower_bound(x0, x1, d0, vf, min_distance=0.0, tolerance=1e-6, rescale=0.
             else:
                 A.append(s_[:, 0] + u * (s_[:, 1] - s_[:, 0]) - s_[:, 2] - v * (s_[:, 3] - s_[:, 2]))
                 B.append(e_[:, 0] + u * (e_[:, 1] - e_[:, 0]) - e_[:, 2] - v * (e_[:, 3] - e_[:, 2]))
-        T = np.maximum(T, _first_time(np.array(A), np.array(B), 3 * err[:, c] + ms + delta))
-    with np.errstate(invalid="ignore"):
-        out = np.maximum(0.0, (T - _tol_t(x0, x1, vf, delta) - 2.0 ** -60) * (1 - 1e-9) - 1e-12)
+        B = np.array(B)
+        bmax = np.maximum(bmax, np.abs(B).max(axis=0))
+        T = np.maximum(T, _first_time(np.array(A), B, 3 * err[:, c] + ms + delta))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        tol0 = np.where(bmax == 0, delta, delta / (3 * np.where(bmax == 0, 1.0, bmax)))
+        out = np.maximum(0.0, (T - 2.0 ** -20 - tol0 * (1 + 1e-6) - 2.0 ** -60) * (1 - 1e-6))
     out = np.where(np.isinf(T), INF, out)
     out = np.where(np.all(x0 == x1, axis=(1, 2)), INF, out)
     return np.where(d0 <= min_distance, 0.0, out)
