@@ -317,6 +317,13 @@ int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles
  * rare matrix on which the df64 eigensolver does not converge.  No
  * counterpart in the reference. */
 int ipcg_testing_defer_df64_psd(int on);
+/* Testing: statistics of the step-size passes (compute_collision_free_stepsize
+ * and the other CCD calls on this mesh).  out (12 values, may be NULL) gets,
+ * for the seed, budgeted and hard passes in turn, the queries run, the boxes
+ * they examined, the most boxes of one query and the hits, accumulated since
+ * the previous call; enable != 0 keeps collecting (for every mesh).  No
+ * counterpart in the reference. */
+int ipcg_testing_ccd_stats(const ipcg_mesh* mesh, int enable, int64_t* out);
 
 /* NormalPotential::shape_derivative(collisions, mesh, V)
  * (normal_potential.cpp:85-123, 310-416): the derivative of the gradient with

@@ -792,6 +792,25 @@ int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles
     });
 }
 
+int ipcg_testing_ccd_stats(const ipcg_mesh* mesh, int enable, int64_t* out)
+{
+    return guarded([&] {
+        require(mesh, "NULL argument");
+        ipcg_mesh* m = const_cast<ipcg_mesh*>(mesh);
+        IPCG_CUDA(cudaSetDevice(m->device));
+        if (out) {
+            for (int k = 0; k < 12; ++k) out[k] = 0;
+            if (m->ccd_stats_live) {
+                IPCG_CUDA(cudaMemcpyAsync(out, m->ccd_stats.p, sizeof(int64_t) * 12, cudaMemcpyDeviceToHost,
+                    m->stream));
+                IPCG_CUDA(cudaStreamSynchronize(m->stream));
+            }
+        }
+        m->ccd_stats_live = false;
+        g_ccd_stats.store(enable ? 1 : 0);
+    });
+}
+
 int ipcg_testing_defer_df64_psd(int on)
 {
     return guarded([&] { egh_defer_df64(on != 0); });

@@ -27,11 +27,15 @@
 // walks best first with an unbounded heap and returns the same box.  One
 // thread per candidate; this file is compiled with -fmad=false so every
 // value matches the CPU oracle bit for bit.
+#include <atomic>
+
 #include "geom.cuh"
 #include "internal.cuh"
 #include "profile.cuh"
 
 namespace ipcg {
+
+std::atomic<int> g_ccd_stats { 0 };
 
 namespace {
 
@@ -352,7 +356,7 @@ struct Search {
     {
         nch = 0;
         ++itr;
-        if (bud.limit > 0 && ++bud.spent > bud.limit) {
+        if (++bud.spent > bud.limit && bud.limit > 0) {
             unresolved = true;
             return 0;
         }
@@ -705,7 +709,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,
     CCDParams P, unsigned long long* toi_bits, long long budget, const int* __restrict__ list,
     const int* __restrict__ list_n, int list_len, int* __restrict__ hard, int* __restrict__ hard_n, int any_hit,
-    const double* __restrict__ lb, const int* __restrict__ seg)
+    const double* __restrict__ lb, const int* __restrict__ seg, long long* __restrict__ stats)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = list ? (list_n ? *list_n : list_len) : n_ee + n_fv;
@@ -731,6 +735,13 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     if (st == CCD_HIT && any_hit) atomicMin(best, 0ULL);
     else if (st == CCD_HIT && toi < tmax) atomicMin(best, (unsigned long long)__double_as_longlong(toi));
     else if (st == CCD_UNRESOLVED) hard[atomicAdd(hard_n, 1)] = i;
+    if (stats) {
+        // testing: queries run, boxes, the largest query, hits
+        atomicAdd((unsigned long long*)stats, 1ull);
+        atomicAdd((unsigned long long*)stats + 1, (unsigned long long)bud.spent);
+        atomicMax(stats + 2, bud.spent);
+        if (st == CCD_HIT) atomicAdd((unsigned long long*)stats + 3, 1ull);
+    }
 }
 
 __global__ void k_ccd_stencils(int is_ee, int n, const double* __restrict__ x0, const double* __restrict__ x1,
@@ -812,6 +823,17 @@ void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, in
     int* seeds_n = m->counters.p + 30;
     int* hard_n = m->counters.p + 31;
     IPCG_CUDA(cudaMemsetAsync(seeds_n, 0, 2 * sizeof(int), s));
+    // testing: per pass (seeds, budgeted, hard) queries run, boxes, the
+    // largest query, hits, accumulated until read
+    long long* st = nullptr;
+    if (g_ccd_stats.load()) {
+        m->ccd_stats.reserve(12);
+        if (!m->ccd_stats_live) {
+            IPCG_CUDA(cudaMemsetAsync(m->ccd_stats.p, 0, sizeof(long long) * 12, s));
+            m->ccd_stats_live = true;
+        }
+        st = m->ccd_stats.p;
+    }
     IPCG_CUDA(cudaMemsetAsync(seg, 0xff, sizeof(int) * ns, s));
     IPCG_LAUNCH("k_ccd_bound", s, k_ccd_bound<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv,
         V0, V1, m->E.p, m->F.p, md, sv, P, m->ccd_lb.p, m->keys_a.p, ids));
@@ -823,13 +845,13 @@ void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, in
     // time before the bulk of its queries runs
     IPCG_LAUNCH("k_ccd_seeds", s, k_ccd<<<grid_for((int64_t)ns * CCD_SEEDS, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee,
         cfv, (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_SEED_BUDGET, seeds, seeds_n, 0, hard,
-        hard_n, any_hit, m->ccd_lb.p, nullptr));
+        hard_n, any_hit, m->ccd_lb.p, nullptr, st ? st : nullptr));
     IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
         m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, sorted, nullptr, nc, hard, hard_n, any_hit,
-        m->ccd_lb.p, seg));
+        m->ccd_lb.p, seg, st ? st + 4 : nullptr));
     IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
         m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, 0, nullptr, nullptr, any_hit, m->ccd_lb.p,
-        nullptr));
+        nullptr, st ? st + 8 : nullptr));
 }
 
 void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, const double* min_distance,

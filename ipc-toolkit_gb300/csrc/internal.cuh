@@ -218,6 +218,8 @@ struct ipcg_mesh {
     ipcg::DBuf<char> tmp;            // CUB temporary storage
     ipcg::DBuf<unsigned long long> keys_a, keys_b;
     ipcg::DBuf<double> ccd_lb; // per CCD candidate: lower bound on its time of impact
+    ipcg::DBuf<long long> ccd_stats; // testing: CCD pass statistics (ipcg_testing_ccd_stats)
+    bool ccd_stats_live = false;
     ipcg::DBuf<int> ivals_a, ivals_b;
     ipcg::DBuf<int8_t> i8tmp;
     ipcg::DBuf<double> partial;      // reduction partials
@@ -393,6 +395,8 @@ struct EghTuning {
 EghTuning egh_tuning(int stage);
 // Testing: the df64 projection defers every contact to its FP64 fix-up pass.
 void egh_defer_df64(bool on);
+// ccd.cu: testing switch for the step-size passes' statistics
+extern std::atomic<int> g_ccd_stats;
 void egh_set_tuning(int stage, const EghTuning& t);
 // Time both stages over candidate tunings on this set's largest chunk and
 // keep the fastest for the device; returns a JSON report.

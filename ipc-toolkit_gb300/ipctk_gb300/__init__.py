@@ -132,6 +132,7 @@ def _load():
         "ipcg_barrier_tuning": (i32, [i32, P, P, P]),
         "ipcg_barrier_set_tuning": (i32, [i32, i32, i32, i32]),
         "ipcg_testing_defer_df64_psd": (i32, [i32]),
+        "ipcg_testing_ccd_stats": (i32, [P, i32, P]),
         "ipcg_initial_barrier_stiffness": (i32, [d, i32, d, d, P, P, i64, d, d, P, P]),
         "ipcg_update_barrier_stiffness": (i32, [d, d, d, d, d, d, d, P]),
     }
@@ -268,6 +269,16 @@ def testing_defer_df64_psd(on: bool):
     """Testing switch (ipcg_testing_defer_df64_psd): the df64 projection
     hands every local Hessian to its FP64 fix-up pass."""
     _check(_load().ipcg_testing_defer_df64_psd(int(bool(on))))
+
+
+def testing_ccd_stats(mesh, enable: bool = True) -> dict:
+    """Testing (ipcg_testing_ccd_stats): per step-size pass (seeds, budgeted,
+    hard) the queries run, boxes examined, the largest query's boxes and the
+    hits since the previous call; enable keeps collecting."""
+    out = np.zeros(12, np.int64)
+    _check(_load().ipcg_testing_ccd_stats(mesh._h, int(bool(enable)), _ptr(out)))
+    keys = ("queries", "boxes", "max_boxes", "hits")
+    return {p: dict(zip(keys, (int(x) for x in out[4 * k:4 * k + 4]))) for k, p in enumerate(("seeds", "budgeted", "hard"))}
 
 
 def launch_count() -> int:
