@@ -51,9 +51,9 @@ constexpr int BLOCK = 128;
 // deferred to the hard pass, which starts it again with the then earliest
 // time as its horizon and runs it to completion.
 constexpr long long CCD_PASS1_BUDGET = 512;
-// The seed queries (each scene's first queries by their lower bound) run
-// first with a larger budget, so that a scene's earliest time is known
-// before the bulk of its queries runs.
+// The seed queries (each scene's likeliest earliest impacts) run first with a
+// larger budget, so that a scene's earliest time is known before the bulk of
+// its queries runs.
 constexpr long long CCD_SEED_BUDGET = 8192;
 
 struct Query {
@@ -656,8 +656,48 @@ __device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_e
 // Per candidate: its lower bound (by candidate index) and, for sorting the
 // queries by it, its bit pattern (non-negative doubles order like their
 // bits) with the candidate index.
-// keys: scene in the top 20 bits, then the bound's leading 44 bits (its
-// sign is clear), so that a scene's queries sort together by bound.
+// An estimate of a query's time of impact, for ordering only: the time at
+// which the signed volume of its four points (linear between its values at
+// t = 0 and t = 1) changes sign, if the two primitives' closest points lie
+// on them (with a 10 % margin) at that time; otherwise 1 + its lower bound
+// (after every likely hit).
+__device__ double toi_estimate(const Query& q, double lower)
+{
+    auto at = [&](int k, double t) { return q.s[k] + q.d[k] * t; };
+    auto vol = [&](double t) {
+        const V3 a = at(0, t), b = at(1, t), c = at(2, t), d = at(3, t);
+        return q.vf ? dot(cross(c - b, d - b), a - b) : dot(cross(b - a, d - c), c - a);
+    };
+    const double v0 = vol(0.0), v1 = vol(1.0);
+    if (!(lower < 1.0) || !((v0 > 0) != (v1 > 0) || v1 == 0)) return 1.0 + lower;
+    const double t = fmax(lower, fmin(1.0, v0 / (v0 - v1)));
+    const V3 a = at(0, t), b = at(1, t), c = at(2, t), d = at(3, t);
+    double x, y, z = 0;
+    if (q.vf) {
+        // barycentric coordinates of a's projection onto triangle (b, c, d)
+        const V3 e0 = c - b, e1 = d - b, w = a - b;
+        const double d00 = dot(e0, e0), d01 = dot(e0, e1), d11 = dot(e1, e1), d20 = dot(w, e0), d21 = dot(w, e1);
+        const double den = d00 * d11 - d01 * d01;
+        if (!(den > 0)) return 1.0 + lower;
+        x = (d11 * d20 - d01 * d21) / den;
+        y = (d00 * d21 - d01 * d20) / den;
+        z = 1.0 - x - y;
+    } else {
+        // closest-point parameters of the lines (a, b) and (c, d)
+        const V3 u = b - a, v = d - c, w = a - c;
+        const double aa = dot(u, u), bb = dot(u, v), cc = dot(v, v), dd = dot(u, w), ee = dot(v, w);
+        const double den = aa * cc - bb * bb;
+        if (!(den > 0)) return 1.0 + lower;
+        x = (bb * ee - cc * dd) / den;
+        y = (aa * ee - bb * dd) / den;
+    }
+    const bool on = x >= -0.1 && x <= 1.1 && y >= -0.1 && y <= 1.1 && z >= -0.1 && z <= 1.1;
+    return on ? t : 1.0 + lower;
+}
+
+// keys: scene in the top 20 bits, then the leading 44 bits of the query's
+// time-of-impact estimate (its sign is clear), so that a scene's likely
+// earliest impacts sort first.
 constexpr int CCD_SCENE_SHIFT = 44;
 __global__ void k_ccd_bound(const int2* __restrict__ cand_ee, int n_ee, const int2* __restrict__ cand_fv, int n_fv,
     const double* __restrict__ V0, const double* __restrict__ V1, const int* __restrict__ E, const int* __restrict__ F,
@@ -670,7 +710,8 @@ __global__ void k_ccd_bound(const int2* __restrict__ cand_ee, int n_ee, const in
     const int scene = sv.of(load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q));
     const double b = toi_lower_bound(q, __ldg(min_distance + scene), P);
     lb[i] = b;
-    keys[i] = ((unsigned long long)scene << CCD_SCENE_SHIFT) | ((unsigned long long)__double_as_longlong(b) >> 20);
+    const double est = toi_estimate(q, b);
+    keys[i] = ((unsigned long long)scene << CCD_SCENE_SHIFT) | ((unsigned long long)__double_as_longlong(est) >> 20);
     ids[i] = i;
 }
 
@@ -683,7 +724,7 @@ __global__ void k_ccd_segments(const unsigned long long* __restrict__ keys, int 
     if (p == 0 || (int)(keys[p - 1] >> CCD_SCENE_SHIFT) != scene) seg[scene] = p;
 }
 
-// The seed list: each scene's first CCD_SEEDS queries by bound (thread
+// The seed list: each scene's first CCD_SEEDS queries by estimate (thread
 // k * CCD_SEEDS + j takes the j-th of scene k, if it has one).
 constexpr int CCD_SEEDS = 32;
 __global__ void k_ccd_seed_list(const unsigned long long* __restrict__ keys, const int* __restrict__ sorted, int n,
@@ -792,10 +833,10 @@ __global__ void k_distance_stencils(int kind, int n, const double* __restrict__ 
 } // namespace
 
 // The CCD passes over candidate lists (EE pairs, then FV (face, vertex)
-// pairs).  Every query first gets a lower bound on its time of impact; the
-// queries are sorted by it, so that each scene's likely earliest impacts run
-// first and set its earliest time, which then skips every query whose bound
-// is not below it.  The sorted list runs with a box budget, then the
+// pairs).  Every query first gets a lower bound on its time of impact and an
+// estimate of it; the queries are sorted by scene and estimate, each scene's
+// likeliest earliest impacts run first (the seeds) and set its earliest
+// time, which then skips every query whose bound is not below it.  The sorted list runs with a box budget, then the
 // unfinished queries to completion.  toi_bits (one per scene, set by the
 // caller) is the scene's earliest time so far; with any_hit a hit sets it to
 // 0 instead.
@@ -842,7 +883,7 @@ void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, in
     IPCG_LAUNCH("k_ccd_seed_list", s, k_ccd_seed_list<<<grid_for((int64_t)ns * CCD_SEEDS, 256), 256, 0, s>>>(
         m->keys_b.p, sorted, nc, seg, ns, seeds, seeds_n));
     // seeds first: each scene's likeliest earliest impacts set its earliest
-    // time before the bulk of its queries runs
+    // time before the bulk of its queries runs (in the same order)
     IPCG_LAUNCH("k_ccd_seeds", s, k_ccd<<<grid_for((int64_t)ns * CCD_SEEDS, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee,
         cfv, (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_SEED_BUDGET, seeds, seeds_n, 0, hard,
         hard_n, any_hit, m->ccd_lb.p, nullptr, st ? st : nullptr));
