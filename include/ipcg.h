@@ -324,6 +324,9 @@ int ipcg_testing_defer_df64_psd(int on);
  * the previous call; enable != 0 keeps collecting (for every mesh).  No
  * counterpart in the reference. */
 int ipcg_testing_ccd_stats(const ipcg_mesh* mesh, int enable, int64_t* out);
+/* Testing: the box budget of the step-size passes' one-thread pass, after
+ * which a query moves to the warp-per-query pass (0 restores the default). */
+int ipcg_testing_ccd_budget(int64_t boxes);
 
 /* NormalPotential::shape_derivative(collisions, mesh, V)
  * (normal_potential.cpp:85-123, 310-416): the derivative of the gradient with

@@ -811,6 +811,14 @@ int ipcg_testing_ccd_stats(const ipcg_mesh* mesh, int enable, int64_t* out)
     });
 }
 
+int ipcg_testing_ccd_budget(int64_t boxes)
+{
+    return guarded([&] {
+        require(boxes >= 0, "the budget is a box count (0: the default)");
+        g_ccd_thread_budget.store(boxes);
+    });
+}
+
 int ipcg_testing_defer_df64_psd(int on)
 {
     return guarded([&] { egh_defer_df64(on != 0); });

@@ -27,6 +27,7 @@
 // walks best first with an unbounded heap and returns the same box.  One
 // thread per candidate; this file is compiled with -fmad=false so every
 // value matches the CPU oracle bit for bit.
+#include <algorithm>
 #include <atomic>
 
 #include "geom.cuh"
@@ -36,6 +37,8 @@
 namespace ipcg {
 
 std::atomic<int> g_ccd_stats { 0 };
+// testing: the box budget of the one-thread pass (0: the default)
+std::atomic<long long> g_ccd_thread_budget { 0 };
 
 namespace {
 
@@ -50,7 +53,7 @@ constexpr int BLOCK = 128;
 // (re-read as it runs); a query that does not finish within the budget is
 // deferred to the hard pass, which starts it again with the then earliest
 // time as its horizon and runs it to completion.
-constexpr long long CCD_PASS1_BUDGET = 512;
+constexpr long long CCD_PASS1_BUDGET = 128;
 // The seed queries (each scene's likeliest earliest impacts) run first with a
 // larger budget, so that a scene's earliest time is known before the bulk of
 // its queries runs.
@@ -458,8 +461,276 @@ __device__ int root_finder(const Query& q, const double err[3], double ms, const
     return S.found ? CCD_HIT : CCD_MISS;
 }
 
+// ---- the same search with a warp per query ----
+// FP64 instructions cost the same pipe time however many lanes are active,
+// so a long query's boxes are better examined 32 at a time: every round the
+// warp takes the 32 first boxes (in box order) of a pool kept sorted in
+// shared memory, examines them in parallel, keeps the first accepted box of
+// the round if it comes before the best so far, and merges the kept children
+// (sorted by a bitonic network) back into the pool.  The search ends when the
+// pool's first box is skipped.  The result -- the first accepted box in box
+// order -- is the same as the one-thread search's: every box before it is
+// examined either way.  A pool that would overflow hands its last boxes to
+// the lanes, which walk their subtrees depth first (as the one-thread search
+// does with a full heap).  The box count for the iteration cap and the budget
+// is the warp's total (checked per round).
+constexpr int WPOOL = 256; // sorted pool per warp
+constexpr int WCH = 64;    // children per round (2 per lane)
+struct WarpPool {
+    CBox* cur;  // WPOOL + WCH
+    CBox* nxt;  // WPOOL + WCH
+    CBox* ch;   // WCH
+};
+constexpr int CCD_WARP_SMEM = (2 * (WPOOL + WCH) + WCH) * (int)sizeof(CBox); // per warp
+
+__device__ __forceinline__ CBox shfl_box(const CBox& b, int src_or_mask, bool xor_mode)
+{
+    CBox r;
+    const unsigned FULL = 0xffffffffu;
+    const int packed = (b.lvl[0] & 0xff) | ((b.lvl[1] & 0xff) << 8) | ((b.lvl[2] & 0xff) << 16);
+    int pk;
+    if (xor_mode) {
+        for (int d = 0; d < 3; ++d) r.lo[d] = __shfl_xor_sync(FULL, b.lo[d], src_or_mask);
+        pk = __shfl_xor_sync(FULL, packed, src_or_mask);
+    } else {
+        for (int d = 0; d < 3; ++d) r.lo[d] = __shfl_sync(FULL, b.lo[d], src_or_mask);
+        pk = __shfl_sync(FULL, packed, src_or_mask);
+    }
+    for (int d = 0; d < 3; ++d) r.lvl[d] = (int8_t)((pk >> (8 * d)) & 0xff);
+    return r;
+}
+
+__device__ __forceinline__ CBox end_box()
+{
+    CBox b;
+    b.lo[0] = b.lo[1] = b.lo[2] = __longlong_as_double(0x7ff0000000000000LL);
+    b.lvl[0] = b.lvl[1] = b.lvl[2] = 0;
+    return b;
+}
+
+// Number of boxes in a[0, n) (sorted) that come before x (strict) or, with
+// or_equal, not after it.
+__device__ __forceinline__ int rank_in(const CBox* a, int n, const CBox& x, bool or_equal)
+{
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const bool left = or_equal ? !box_before(x, a[mid]) : box_before(a[mid], x);
+        if (left) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ int root_finder_warp(const Query& q, const double err[3], double ms, const double tol[3], double delta,
+    double tmax, long long max_itr, double& toi, double& out_tol, const unsigned long long* shared_best, Budget& bud,
+    const WarpPool& w)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    Search S { q, err, ms, delta, tol, tmax, CBox {}, false, 0.0, 0, max_itr > 0 ? max_itr : 100000000LL, bud, false,
+        false };
+    CBox* cur = w.cur;
+    CBox* nxt = w.nxt;
+    if (lane == 0) {
+        CBox root;
+        root.lo[0] = root.lo[1] = root.lo[2] = 0;
+        root.lvl[0] = root.lvl[1] = root.lvl[2] = 0;
+        cur[0] = root;
+    }
+    __syncwarp();
+    int n = 1;
+    double capped_t = tmax;
+    long long itr0 = 0, spent0 = bud.spent;
+    CBox st[CCD_STACK];
+    while (n > 0) {
+        if (shared_best)
+            S.tmax = fmin(S.tmax, __longlong_as_double((long long)*(volatile const unsigned long long*)shared_best));
+        S.tmax = __shfl_sync(FULL, S.tmax, 0);
+        if (S.skip(cur[0])) break; // the pool's first box: every other one comes later
+        const int m = min(32, n);
+        // examine the round's boxes
+        S.itr = itr0;
+        bud.spent = spent0;
+        CBox ch[2];
+        int nch = 0;
+        bool acc = false;
+        CBox accb = end_box();
+        double acc_tol = 0;
+        if (lane < m) {
+            const CBox b = cur[lane];
+            if (!S.skip(b)) {
+                const bool had = S.found;
+                const CBox prev = S.best;
+                if (!S.step(b, ch, nch)) {
+                    if (S.found && (!had || box_before(S.best, prev))) {
+                        acc = true;
+                        accb = S.best;
+                        acc_tol = S.out_tol;
+                    }
+                    if (S.capped) capped_t = fmin(capped_t, b.lo[0]);
+                }
+            }
+        }
+        // the warp's totals and verdicts
+        const int done = __popc(__ballot_sync(FULL, lane < m));
+        itr0 += done;
+        spent0 += done;
+        const bool any_unres = __any_sync(FULL, S.unresolved);
+        const bool any_cap = __any_sync(FULL, S.capped);
+        if (any_unres) {
+            bud.spent = spent0;
+            return CCD_UNRESOLVED;
+        }
+        if (__any_sync(FULL, acc)) {
+            // the first accepted box of the round
+            CBox c = accb;
+            double ct = acc_tol;
+            for (int off = 16; off > 0; off >>= 1) {
+                const CBox o = shfl_box(c, off, true);
+                const double ot = __shfl_xor_sync(FULL, ct, off);
+                if (box_before(o, c)) {
+                    c = o;
+                    ct = ot;
+                }
+            }
+            S.best = c;
+            S.out_tol = ct;
+            S.found = true;
+        } else {
+            // every lane keeps the warp's best (lanes that examined nothing
+            // may not have it)
+            const int src = __ffs(__ballot_sync(FULL, S.found)) - 1;
+            if (src >= 0) {
+                S.best = shfl_box(S.best, src, false);
+                S.out_tol = __shfl_sync(FULL, S.out_tol, src);
+                S.found = true;
+            }
+        }
+        if (any_cap) {
+            S.capped = true;
+            for (int off = 16; off > 0; off >>= 1) capped_t = fmin(capped_t, __shfl_xor_sync(FULL, capped_t, off));
+            // the unexamined boxes bound the root from below
+            for (int i = lane; i < n; i += 32) capped_t = fmin(capped_t, cur[i].lo[0]);
+            for (int off = 16; off > 0; off >>= 1) capped_t = fmin(capped_t, __shfl_xor_sync(FULL, capped_t, off));
+            break;
+        }
+        // the kept children, compacted into the round's buffer and sorted
+        int keep = 0;
+        CBox kc[2];
+        for (int c = 0; c < nch; ++c)
+            if (!S.skip(ch[c])) kc[keep++] = ch[c];
+        int off = keep;
+        for (int d = 1; d < 32; d <<= 1) {
+            const int v = __shfl_up_sync(FULL, off, d);
+            if (lane >= d) off += v;
+        }
+        const int C = __shfl_sync(FULL, off, 31);
+        off -= keep;
+        for (int c = 0; c < keep; ++c) w.ch[off + c] = kc[c];
+        for (int i = C + lane; i < WCH; i += 32) w.ch[i] = end_box();
+        __syncwarp();
+        for (int k = 2; k <= WCH; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                // lane handles the pair (i, i ^ j) with i = its index with bit j clear
+                const int i = ((lane & ~(j - 1)) << 1) | (lane & (j - 1));
+                const int l = i ^ j;
+                const bool up = (i & k) == 0;
+                const CBox a = w.ch[i], b = w.ch[l];
+                if (box_before(b, a) == up) {
+                    w.ch[i] = b;
+                    w.ch[l] = a;
+                }
+                __syncwarp();
+            }
+        // merge the pool's rest cur[m, n) with the children
+        const int r = n - m;
+        for (int i = lane; i < r; i += 32) {
+            const CBox x = cur[m + i];
+            nxt[i + rank_in(w.ch, C, x, false)] = x;
+        }
+        for (int k = lane; k < C; k += 32) {
+            const CBox y = w.ch[k];
+            nxt[k + rank_in(cur + m, r, y, true)] = y;
+        }
+        __syncwarp();
+        n = r + C;
+        CBox* t = cur;
+        cur = nxt;
+        nxt = t;
+        if (n > WPOOL) {
+            // overflow: the last boxes' subtrees are walked depth first, one
+            // box per lane (at most 2 per lane)
+            bool lane_acc = false;
+            S.itr = itr0;
+            bud.spent = spent0;
+            for (int i = WPOOL + lane; i < n; i += 32) {
+                int sp = 0;
+                st[sp++] = cur[i];
+                while (sp > 0 && !S.capped && !S.unresolved) {
+                    const CBox d = st[--sp];
+                    if (S.skip(d)) continue;
+                    CBox dc[2];
+                    int ndc;
+                    const bool had = S.found;
+                    const CBox prev = S.best;
+                    if (!S.step(d, dc, ndc)) {
+                        if (S.found && (!had || box_before(S.best, prev))) lane_acc = true;
+                        if (S.capped) capped_t = fmin(capped_t, d.lo[0]);
+                        continue;
+                    }
+                    for (int k = 0; k < ndc; ++k) st[sp++] = dc[k];
+                }
+                if (S.capped)
+                    for (int k = 0; k < sp; ++k) capped_t = fmin(capped_t, st[k].lo[0]);
+            }
+            // totals again
+            long long extra = S.itr - itr0;
+            for (int o = 16; o > 0; o >>= 1) extra += __shfl_xor_sync(FULL, extra, o);
+            itr0 += extra;
+            spent0 += extra;
+            if (__any_sync(FULL, S.unresolved)) {
+                bud.spent = spent0;
+                return CCD_UNRESOLVED;
+            }
+            CBox c = lane_acc || S.found ? S.best : end_box();
+            double ct = S.out_tol;
+            for (int o = 16; o > 0; o >>= 1) {
+                const CBox ob = shfl_box(c, o, true);
+                const double ot = __shfl_xor_sync(FULL, ct, o);
+                if (box_before(ob, c)) {
+                    c = ob;
+                    ct = ot;
+                }
+            }
+            if (__any_sync(FULL, S.found)) {
+                S.best = c;
+                S.out_tol = ct;
+                S.found = true;
+            }
+            if (__any_sync(FULL, S.capped)) {
+                S.capped = true;
+                for (int o = 16; o > 0; o >>= 1) capped_t = fmin(capped_t, __shfl_xor_sync(FULL, capped_t, o));
+                for (int i = lane; i < WPOOL; i += 32) capped_t = fmin(capped_t, cur[i].lo[0]);
+                for (int o = 16; o > 0; o >>= 1) capped_t = fmin(capped_t, __shfl_xor_sync(FULL, capped_t, o));
+                break;
+            }
+            n = WPOOL;
+        }
+    }
+    bud.spent = spent0;
+    if (S.capped) {
+        toi = S.found ? fmin(S.best.lo[0], capped_t) : capped_t;
+        out_tol = S.out_tol;
+        return CCD_HIT;
+    }
+    out_tol = S.found ? S.out_tol : 0;
+    if (S.found) toi = S.best.lo[0];
+    return S.found ? CCD_HIT : CCD_MISS;
+}
+
 __device__ int ti_ccd(const Query& q, double ms_in, double& toi, double tol_in, double tmax_in, long long max_itr,
-    double& out_tol, bool no_zero_toi, const unsigned long long* shared_best, Budget& bud)
+    double& out_tol, bool no_zero_toi, const unsigned long long* shared_best, Budget& bud, const WarpPool* wp)
 {
     double err[3];
     numerical_error(q, ms_in > 0, err);
@@ -469,7 +740,8 @@ __device__ int ti_ccd(const Query& q, double ms_in, double& toi, double tol_in, 
     int hit = CCD_MISS;
     for (int it = 0; it < 256; ++it) {
         double t = 0;
-        hit = root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol, shared_best, bud);
+        hit = wp ? root_finder_warp(q, err, ms, tol, delta, tmax, max_itr, t, out_tol, shared_best, bud, *wp)
+                 : root_finder(q, err, ms, tol, delta, tmax, max_itr, t, out_tol, shared_best, bud);
         if (hit == CCD_UNRESOLVED) return hit;
         if (hit == CCD_HIT) toi = t;
         if (!(no_zero_toi && hit == CCD_HIT && toi == 0)) return hit;
@@ -490,7 +762,7 @@ struct CCDParams {
 };
 
 __device__ int strategy(const Query& q, double min_distance, double d0, const CCDParams& P, double adj, double tmax,
-    double& toi, const unsigned long long* shared_best, Budget& bud)
+    double& toi, const unsigned long long* shared_best, Budget& bud, const WarpPool* wp)
 {
     if (d0 <= min_distance) {
         toi = 0;
@@ -500,9 +772,9 @@ __device__ int strategy(const Query& q, double min_distance, double d0, const CC
     mind = fmin(mind, 1e-4);
     mind += min_distance;
     double out_tol;
-    int hit = ti_ccd(q, mind, toi, adj, tmax, P.max_iterations, out_tol, false, shared_best, bud);
+    int hit = ti_ccd(q, mind, toi, adj, tmax, P.max_iterations, out_tol, false, shared_best, bud, wp);
     if (hit == CCD_HIT && toi < 1e-6) {
-        hit = ti_ccd(q, min_distance, toi, adj, tmax, -1, out_tol, true, shared_best, bud);
+        hit = ti_ccd(q, min_distance, toi, adj, tmax, -1, out_tol, true, shared_best, bud, wp);
         if (hit == CCD_HIT) toi *= P.rescale;
     }
     return hit;
@@ -511,7 +783,7 @@ __device__ int strategy(const Query& q, double min_distance, double d0, const CC
 __device__ __forceinline__ bool v3eq(V3 a, V3 b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
 
 __device__ int stencil_ccd(Query& q, double min_distance, const CCDParams& P, double tmax, double& toi,
-    const unsigned long long* shared_best, Budget& bud)
+    const unsigned long long* shared_best, Budget& bud, const WarpPool* wp = nullptr)
 {
     double d2;
     if (q.vf) d2 = point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
@@ -527,7 +799,7 @@ __device__ int stencil_ccd(Query& q, double min_distance, const CCDParams& P, do
         return CCD_MISS;
     }
     const double adj = fmin(0.5 * d0, P.tolerance);
-    return strategy(q, min_distance, d0, P, adj, tmax, toi, shared_best, bud);
+    return strategy(q, min_distance, d0, P, adj, tmax, toi, shared_best, bud, wp);
 }
 
 // A lower bound on the time of impact stencil_ccd can return for a query
@@ -785,6 +1057,51 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
     }
 }
 
+// The warp-per-query pass (the seeds, and the queries the budgeted pass left
+// unfinished): like k_ccd, with every lane of a warp on the same query.
+constexpr int WARPS_PER_BLOCK = 4;
+__global__ void __launch_bounds__(32 * WARPS_PER_BLOCK) k_ccd_warp(const int2* __restrict__ cand_ee, int n_ee,
+    const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
+    const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,
+    CCDParams P, unsigned long long* toi_bits, long long budget, const int* __restrict__ list,
+    const int* __restrict__ list_n, int* __restrict__ hard, int* __restrict__ hard_n, int any_hit,
+    const double* __restrict__ lb, long long* __restrict__ stats)
+{
+    extern __shared__ unsigned char smem[];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    CBox* base = reinterpret_cast<CBox*>(smem + (size_t)wib * CCD_WARP_SMEM);
+    const WarpPool wp { base, base + (WPOOL + WCH), base + 2 * (WPOOL + WCH) };
+    const int n = *list_n;
+    for (int t = blockIdx.x * WARPS_PER_BLOCK + wib; t < n; t += gridDim.x * WARPS_PER_BLOCK) {
+        const int i = list[t];
+        Query q;
+        const int scene = sv.of(load_query(i, cand_ee, n_ee, cand_fv, V0, V1, E, F, q));
+        unsigned long long* best = toi_bits + scene;
+        double tmax = 0;
+        if (lane == 0) tmax = __longlong_as_double((long long)*(volatile unsigned long long*)best);
+        tmax = __shfl_sync(0xffffffffu, tmax, 0);
+        if (lb) {
+            const double b = lb[i];
+            if (b >= 1e-6 && b >= tmax) continue;
+        }
+        double toi = __longlong_as_double(0x7ff0000000000000ULL);
+        Budget bud { budget, 0 };
+        const int st = stencil_ccd(q, __ldg(min_distance + scene), P, tmax, toi, best, bud, &wp);
+        if (lane == 0) {
+            if (st == CCD_HIT && any_hit) atomicMin(best, 0ULL);
+            else if (st == CCD_HIT && toi < tmax) atomicMin(best, (unsigned long long)__double_as_longlong(toi));
+            else if (st == CCD_UNRESOLVED) hard[atomicAdd(hard_n, 1)] = i;
+            if (stats) {
+                atomicAdd((unsigned long long*)stats, 1ull);
+                atomicAdd((unsigned long long*)stats + 1, (unsigned long long)bud.spent);
+                atomicMax(stats + 2, bud.spent);
+                if (st == CCD_HIT) atomicAdd((unsigned long long*)stats + 3, 1ull);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void k_ccd_stencils(int is_ee, int n, const double* __restrict__ x0, const double* __restrict__ x1,
     double min_distance, double tmax, CCDParams P, int8_t* __restrict__ hit, double* __restrict__ toi)
 {
@@ -882,17 +1199,25 @@ void ccd_passes(ipcg_mesh* m, const int2* cee, int64_t n_ee, const int2* cfv, in
     IPCG_LAUNCH("k_ccd_segments", s, k_ccd_segments<<<grid_for(nc, 256), 256, 0, s>>>(m->keys_b.p, nc, seg));
     IPCG_LAUNCH("k_ccd_seed_list", s, k_ccd_seed_list<<<grid_for((int64_t)ns * CCD_SEEDS, 256), 256, 0, s>>>(
         m->keys_b.p, sorted, nc, seg, ns, seeds, seeds_n));
+    const long long tb = g_ccd_thread_budget.load() > 0 ? g_ccd_thread_budget.load() : CCD_PASS1_BUDGET;
     // seeds first: each scene's likeliest earliest impacts set its earliest
     // time before the bulk of its queries runs (in the same order)
-    IPCG_LAUNCH("k_ccd_seeds", s, k_ccd<<<grid_for((int64_t)ns * CCD_SEEDS, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee,
-        cfv, (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_SEED_BUDGET, seeds, seeds_n, 0, hard,
-        hard_n, any_hit, m->ccd_lb.p, nullptr, st ? st : nullptr));
+    const int wsmem = WARPS_PER_BLOCK * CCD_WARP_SMEM;
+    static bool smem_set[64] = {};
+    if (m->device >= 0 && m->device < 64 && !smem_set[m->device]) {
+        IPCG_CUDA(cudaFuncSetAttribute(k_ccd_warp, cudaFuncAttributeMaxDynamicSharedMemorySize, wsmem));
+        smem_set[m->device] = true;
+    }
+    const int wblocks = std::max(1, std::min(ns * CCD_SEEDS / WARPS_PER_BLOCK + 1, 152 * 8));
+    IPCG_LAUNCH("k_ccd_seeds", s, k_ccd_warp<<<wblocks, 32 * WARPS_PER_BLOCK, wsmem, s>>>(cee, (int)n_ee, cfv,
+        (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_SEED_BUDGET, seeds, seeds_n, hard, hard_n,
+        any_hit, m->ccd_lb.p, st ? st : nullptr));
     IPCG_LAUNCH("k_ccd", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, CCD_PASS1_BUDGET, sorted, nullptr, nc, hard, hard_n, any_hit,
+        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, tb, sorted, nullptr, nc, hard, hard_n, any_hit,
         m->ccd_lb.p, seg, st ? st + 4 : nullptr));
-    IPCG_LAUNCH("k_ccd_hard", s, k_ccd<<<grid_for(nc, BLOCK), BLOCK, 0, s>>>(cee, (int)n_ee, cfv, (int)n_fv, V0, V1,
-        m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, 0, nullptr, nullptr, any_hit, m->ccd_lb.p,
-        nullptr, st ? st + 8 : nullptr));
+    IPCG_LAUNCH("k_ccd_hard", s, k_ccd_warp<<<152 * 8, 32 * WARPS_PER_BLOCK, wsmem, s>>>(cee, (int)n_ee, cfv,
+        (int)n_fv, V0, V1, m->E.p, m->F.p, md, sv, P, m->toi_bits.p, 0, hard, hard_n, nullptr, nullptr, any_hit,
+        m->ccd_lb.p, st ? st + 8 : nullptr));
 }
 
 void collision_free_stepsize(ipcg_mesh* m, const double* V0, const double* V1, const double* min_distance,

@@ -397,6 +397,7 @@ EghTuning egh_tuning(int stage);
 void egh_defer_df64(bool on);
 // ccd.cu: testing switch for the step-size passes' statistics
 extern std::atomic<int> g_ccd_stats;
+extern std::atomic<long long> g_ccd_thread_budget;
 void egh_set_tuning(int stage, const EghTuning& t);
 // Time both stages over candidate tunings on this set's largest chunk and
 // keep the fastest for the device; returns a JSON report.

@@ -133,6 +133,7 @@ def _load():
         "ipcg_barrier_set_tuning": (i32, [i32, i32, i32, i32]),
         "ipcg_testing_defer_df64_psd": (i32, [i32]),
         "ipcg_testing_ccd_stats": (i32, [P, i32, P]),
+        "ipcg_testing_ccd_budget": (i32, [i64]),
         "ipcg_initial_barrier_stiffness": (i32, [d, i32, d, d, P, P, i64, d, d, P, P]),
         "ipcg_update_barrier_stiffness": (i32, [d, d, d, d, d, d, d, P]),
     }
@@ -279,6 +280,13 @@ def testing_ccd_stats(mesh, enable: bool = True) -> dict:
     _check(_load().ipcg_testing_ccd_stats(mesh._h, int(bool(enable)), _ptr(out)))
     keys = ("queries", "boxes", "max_boxes", "hits")
     return {p: dict(zip(keys, (int(x) for x in out[4 * k:4 * k + 4]))) for k, p in enumerate(("seeds", "budgeted", "hard"))}
+
+
+def testing_ccd_budget(boxes: int = 0):
+    """Testing (ipcg_testing_ccd_budget): the one-thread step-size pass's box
+    budget, after which a query moves to the warp-per-query pass; 0 restores
+    the default."""
+    _check(_load().ipcg_testing_ccd_budget(int(boxes)))
 
 
 def launch_count() -> int:
