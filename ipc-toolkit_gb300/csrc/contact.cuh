@@ -589,11 +589,19 @@ template <> struct PsdReal<double> {
     __device__ static double out(double x, int) { return x; }
     template <class Acc> __device__ static int scale_of(const Acc&, int) { return 0; }
     // deflation test of a QL off-diagonal entry e between diagonal entries
-    // d0 and d1 (eps relative to them, or below the floor)
-    __device__ static bool negligible(double e, double d0, double d1, double eps, double floor_)
+    // d0 and d1, on the exponent bits (the integer pipe; GB300's FP64 pipe
+    // is the projection's limit): e is negligible when its exponent is at
+    // least 52 below the larger neighbour's (|e| < 2^-51 max(|d0|, |d1|), the
+    // reference's eps (|d0| + |d1|) within a factor 2), not above the
+    // floor's (2^-52 of the tridiagonal matrix's norm, within a factor 2),
+    // or when it is zero or subnormal
+    __device__ static int expo(double x) { return (__double2hiint(x) >> 20) & 0x7ff; }
+    __device__ static bool negligible(double e, double d0, double d1, double, double floor_)
     {
-        return fabs(e) <= eps * (fabs(d0) + fabs(d1)) || fabs(e) <= tiny() || fabs(e) <= floor_;
+        const int ee = expo(e);
+        return ee == 0 || ee + 52 <= max(expo(d0), expo(d1)) || ee <= expo(floor_);
     }
+    __device__ static bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
     // Wilkinson shift of the trailing 2x2 block [[d0, b], [b, d1]]: its
     // eigenvalue closer to d1
     __device__ static double shift(double d0, double d1, double b)
@@ -628,6 +636,7 @@ template <> struct PsdReal<dd> {
     // the deflation test and the shift only steer the iteration (neither
     // enters the result but through where it stops), so they run in FP32
     // on the leading parts
+    __device__ static bool is_zero(dd x) { return x.hi == 0.f; }
     __device__ static bool negligible(dd e, dd d0, dd d1, dd eps, dd floor_)
     {
         const float ae = fabsf(e.hi);
@@ -725,11 +734,11 @@ template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full sy
     while (end > 0) {
         for (int i = 0; i < end; ++i)
             if (PsdReal<T>::negligible(e[i], d[i], d[i + 1], eps, floor_)) e[i] = 0;
-        while (end > 0 && e[end - 1] == 0) --end;
+        while (end > 0 && PsdReal<T>::is_zero(e[end - 1])) --end;
         if (end <= 0) break;
         if (++iter > 40 * n) return false;
         int start = end - 1;
-        while (start > 0 && e[start - 1] != 0) --start;
+        while (start > 0 && !PsdReal<T>::is_zero(e[start - 1])) --start;
         if (record && nrot + (end - start) > MAXROT) {
             // too many rotations to record: form G from those so far and
             // accumulate the rest into it
@@ -1321,23 +1330,30 @@ __device__ __forceinline__ bool fp32_local_contact(const Params& P, const Local&
 // both triangles written) of one contact.  Returns whether H is to be
 // projected: the mollified edge-edge case with m <= 0 is returned as is, as
 // the reference does (normal_potential.cpp:185-189).
-__device__ bool contact_egh(const Local& c, const V3* x, const Params& P, double& e, double* g, double* H)
+// The FP32 path (fp32_local_contact true).
+__device__ __forceinline__ bool contact_egh_f32(const Local& c, const V3* x, const Params& P, double& e, double* g,
+    double* H)
 {
     const int N = 3 * c.n;
-    if (fp32_local_contact(P, c, x)) {
-        float gf[12], Kf[144];
-        const double d = contact_distance_f(c, x, gf, Kf);
-        e = c.w * (double)fvalf(P, d);
-        const float wf = (float)c.w, a = wf * fd2f(P, d), b = wf * fd1f(P, d);
-        for (int k = 0; k < N; ++k) g[k] = (double)(b * gf[k]);
-        for (int r = 0; r < N; ++r)
-            for (int q = r; q < N; ++q) {
-                const double v = (double)(a * gf[r] * gf[q] + b * Kf[r * N + q]);
-                H[r * N + q] = v;
-                H[q * N + r] = v;
-            }
-        return true;
-    }
+    float gf[12], Kf[144];
+    const double d = contact_distance_f(c, x, gf, Kf);
+    e = c.w * (double)fvalf(P, d);
+    const float wf = (float)c.w, a = wf * fd2f(P, d), b = wf * fd1f(P, d);
+    for (int k = 0; k < N; ++k) g[k] = (double)(b * gf[k]);
+    for (int r = 0; r < N; ++r)
+        for (int q = r; q < N; ++q) {
+            const double v = (double)(a * gf[r] * gf[q] + b * Kf[r * N + q]);
+            H[r * N + q] = v;
+            H[q * N + r] = v;
+        }
+    return true;
+}
+
+// The FP64 path.
+__device__ __forceinline__ bool contact_egh_f64(const Local& c, const V3* x, const Params& P, double& e, double* g,
+    double* H)
+{
+    const int N = 3 * c.n;
     double gd[12];
     const double d = contact_distance(c, x, gd, H); // H: the distance Hessian, overwritten below
     const double fv = fval(P, d), fd = fd1(P, d), fdd = fd2(P, d);
@@ -1384,6 +1400,11 @@ __device__ bool contact_egh(const Local& c, const V3* x, const Params& P, double
             H[q * 12 + r] = v;
         }
     return true;
+}
+
+__device__ bool contact_egh(const Local& c, const V3* x, const Params& P, double& e, double* g, double* H)
+{
+    return fp32_local_contact(P, c, x) ? contact_egh_f32(c, x, P, e, g, H) : contact_egh_f64(c, x, P, e, g, H);
 }
 } // namespace
 

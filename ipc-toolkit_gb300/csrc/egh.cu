@@ -45,6 +45,8 @@
 #include <string>
 #include <vector>
 
+#include <cub/device/device_partition.cuh>
+
 #include "contact.cuh"
 #include "profile.cuh"
 
@@ -107,7 +109,11 @@ struct EghCache {
     DBuf<int64_t> epstart; // per scene: its first energy part (ns + 1)
     int64_t nparts = 0;
     DBuf<double> energy;   // per-scene energies of the last step
-    DBuf<unsigned long long> queue;
+    DBuf<unsigned long long> queue;    // per chunk: local F64, local F32 / any, projection, fix-up count
+    // partition of a chunk's contacts by arithmetic path (mixed precision)
+    DBuf<int> iota, list, nsel;
+    DBuf<unsigned char> path, part_tmp;
+    size_t part_bytes = 0;
     DBuf<long long> fail;  // [failed, chunk-local contact, chunk, non-finite entries]
     HBuf<long long> hfail;
     DBuf<EghDev> dev;
@@ -354,7 +360,11 @@ __device__ __forceinline__ void load_typed(const ContactsView& cv, const int* __
 // index i): the energy to its own slot, the gradient to its vertex-grouped
 // slots, the Hessian to the element-major local slab, whether it is to be
 // projected to pflag.
-template <int CT>
+// Which arithmetic a local-stage launch runs: every contact decides (ANY),
+// or the launch takes only contacts of the FP32 or of the FP64 path.
+enum : int { PATH_ANY = 0, PATH_F32 = 1, PATH_F64 = 2 };
+
+template <int CT, int PATH>
 __device__ __forceinline__ void local_one(const ContactsView& cv, const int* __restrict__ E, const int* __restrict__ F,
     const EghDev& d, const Params* __restrict__ sp, const SceneView& sv, const unsigned* __restrict__ gslot,
     const LhLayout& L, int64_t i, int64_t j, int want)
@@ -367,7 +377,10 @@ __device__ __forceinline__ void local_one(const ContactsView& cv, const int* __r
 #pragma unroll
     for (int a = 0; a < NS; ++a) x[a] = load_v3(d.V, c.vid[a]);
     double e, g[12], H[144];
-    const bool pr = contact_egh(c, x, P, e, g, H);
+    bool pr;
+    if constexpr (PATH == PATH_F32) pr = contact_egh_f32(c, x, P, e, g, H);
+    else if constexpr (PATH == PATH_F64) pr = contact_egh_f64(c, x, P, e, g, H);
+    else pr = contact_egh(c, x, P, e, g, H);
     if (want & WANT_E) d.eslab[i] = e;
     if (want & WANT_G)
 #pragma unroll
@@ -406,19 +419,53 @@ __device__ __forceinline__ void tile_queue(int64_t n, unsigned long long* __rest
 }
 
 // Stage 1: per contact, energy, gradient and local Hessian (one lane each).
+// With a list, the launch takes the contacts list[0, *nsel) (FP64 path) or
+// list[*nsel, n) (FP32 path) of the chunk's partition by path.
+template <int PATH>
 __global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
     const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv, const unsigned* __restrict__ gslot,
-    unsigned long long* __restrict__ queue, int want, int grab)
+    unsigned long long* __restrict__ queue, int want, int grab, const int* __restrict__ list,
+    const int* __restrict__ nsel)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const EghDev d = *dev;
     const LhLayout L(cv);
-    tile_queue(n, queue, grab, [&](int64_t i) {
-        if (i < L.first[1]) local_one<CT_VV>(cv, E, F, d, sp, sv, gslot, L, i, i, want);
-        else if (i < L.first[2]) local_one<CT_EV>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[1], want);
-        else if (i < L.first[2] + cv.nee) local_one<CT_EE>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[2], want);
-        else local_one<CT_FV>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[2] - cv.nee, want);
+    int64_t first = 0, count = n;
+    if (list) {
+        const int64_t k = *nsel;
+        first = PATH == PATH_F64 ? 0 : k;
+        count = PATH == PATH_F64 ? k : n - k;
+    }
+    tile_queue(count, queue, grab, [&](int64_t t) {
+        const int64_t i = list ? (int64_t)list[first + t] : t;
+        if (i < L.first[1]) local_one<CT_VV, PATH>(cv, E, F, d, sp, sv, gslot, L, i, i, want);
+        else if (i < L.first[2]) local_one<CT_EV, PATH>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[1], want);
+        else if (i < L.first[2] + cv.nee)
+            local_one<CT_EE, PATH>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[2], want);
+        else local_one<CT_FV, PATH>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[2] - cv.nee, want);
     });
+}
+
+// Per contact of the chunk: 1 if its local Hessian takes the FP64 path.
+__global__ void k_path_flags(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
+    const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv, unsigned char* __restrict__ f64)
+{
+    const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* __restrict__ V = dev->V;
+    Local c;
+    load_contact(cv, E, F, i, c);
+    const Params P = sp[sv.of(c.vid[0])];
+    V3 x[4];
+    gather(V, c, x);
+    f64[i] = fp32_local_contact(P, c, x) ? 0 : 1;
+}
+
+__global__ void k_iota(int* __restrict__ a, int64_t n)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (int)i;
 }
 
 // Flag on the projection method: the df64 pass leaves every projection to
@@ -766,7 +813,18 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
     C.nb = B0;
     C.pattern = pat;
     C.energy.reserve(ns + 1);
-    C.queue.reserve(3 * C.chunks.size() + 1);
+    C.queue.reserve(4 * C.chunks.size() + 1);
+    C.iota.reserve(C.max_n + 1);
+    C.list.reserve(C.max_n + 1);
+    C.path.reserve(C.max_n + 1);
+    C.nsel.reserve(1);
+    if (C.max_n > 0) {
+        IPCG_LAUNCH("k_iota", s, k_iota<<<grid_for(C.max_n, 256), 256, 0, s>>>(C.iota.p, C.max_n));
+        C.part_bytes = 0;
+        IPCG_CUDA(cub::DevicePartition::Flagged(nullptr, C.part_bytes, C.iota.p, C.path.p, C.list.p, C.nsel.p,
+            (int)C.max_n, s));
+        C.part_tmp.reserve(C.part_bytes + 16);
+    }
     C.fail.reserve(4);
     C.hfail.reserve(4);
     C.dev.reserve(1);
@@ -821,13 +879,33 @@ template <class K> void egh_grid(const EghTuning& t, int64_t n, K kernel, int& b
     blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, need));
 }
 
-void launch_local(const ContactsView& cc, const ipcg_mesh* m, EghCache& C, const EChunk& ch, const Params* sp,
-    const SceneView& sv, unsigned long long* q, int want, const EghTuning& t, cudaStream_t s)
+// Stage 1 of one chunk; q[0], q[1] are its work queues.  In a mixed mode the
+// chunk's contacts are first partitioned by arithmetic path (FP64 first), so
+// that no warp runs both paths and each path has its own register budget.
+// Returns the kernels launched.
+int launch_local(const ContactsView& cc, const ipcg_mesh* m, EghCache& C, const EChunk& ch, const Params* sp,
+    const SceneView& sv, unsigned long long* q, int want, bool split, const EghTuning& t, cudaStream_t s)
 {
     int blocks, threads;
-    egh_grid(t, ch.n, k_local, blocks, threads);
-    IPCG_LAUNCH("k_local", s, k_local<<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv,
-        C.gslot.p + ch.gslot_off, q, want, t.tiles_per_grab));
+    const unsigned* gs = C.gslot.p + ch.gslot_off;
+    if (!split) {
+        egh_grid(t, ch.n, k_local<PATH_ANY>, blocks, threads);
+        IPCG_LAUNCH("k_local", s, k_local<PATH_ANY><<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv,
+            gs, q, want, t.tiles_per_grab, nullptr, nullptr));
+        return 1;
+    }
+    IPCG_LAUNCH("k_path_flags", s, k_path_flags<<<grid_for(ch.n, 256), 256, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp,
+        sv, C.path.p));
+    size_t bytes = C.part_bytes;
+    IPCG_LAUNCH("cub_partition", s, IPCG_CUDA(cub::DevicePartition::Flagged(C.part_tmp.p, bytes, C.iota.p, C.path.p,
+        C.list.p, C.nsel.p, (int)ch.n, s)));
+    egh_grid(t, ch.n, k_local<PATH_F64>, blocks, threads);
+    IPCG_LAUNCH("k_local", s, k_local<PATH_F64><<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv, gs,
+        q, want, t.tiles_per_grab, C.list.p, C.nsel.p));
+    egh_grid(t, ch.n, k_local<PATH_F32>, blocks, threads);
+    IPCG_LAUNCH("k_local_f32", s, k_local<PATH_F32><<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv,
+        gs, q + 1, want, t.tiles_per_grab, C.list.p, C.nsel.p));
+    return 4;
 }
 
 // Stage 2 of one chunk; q[0] is its work queue, q[1] the fix-up count.
@@ -854,19 +932,19 @@ int launch_psd(const ContactsView& cc, EghCache& C, const EChunk& ch, int ci, un
 
 // Enqueue the launches of one step on the mesh stream (also while capturing).
 int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Params* sp, int psd, bool df64, int want,
-    const EghTuning* tune)
+    bool split, const EghTuning* tune)
 {
     cudaStream_t s = m->stream;
     const ContactsView cv = full_view(cs);
     const SceneView sv = scene_view(m);
     int kernels = 0;
-    IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 3 * C.chunks.size(), s));
+    IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 4 * C.chunks.size(), s));
     for (size_t ci = 0; ci < C.chunks.size(); ++ci) {
         const EChunk& ch = C.chunks[ci];
         const ContactsView cc = chunk_view(cv, ch);
         if (ch.n > 0) {
-            launch_local(cc, m, C, ch, sp, sv, C.queue.p + 3 * ci, want, tune[0], s);
-            kernels += 1 + launch_psd(cc, C, ch, (int)ci, C.queue.p + 3 * ci + 1, psd, df64, tune[1], s);
+            kernels += launch_local(cc, m, C, ch, sp, sv, C.queue.p + 4 * ci, want, split, tune[0], s);
+            kernels += launch_psd(cc, C, ch, (int)ci, C.queue.p + 4 * ci + 2, psd, df64, tune[1], s);
         }
         if (ch.nb > 0) {
             IPCG_LAUNCH("k_hess_reduce", s, k_hess_reduce<<<grid_for(9 * ch.nb, 256), 256, 0, s>>>(ch.nb,
@@ -1045,14 +1123,15 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
     IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(long long) * 4, s));
     const bool df64 = a.df64_psd != 0;
+    const bool split = a.mixed || a.fp32_local;
     const EghTuning tune[2] = { egh_tuning(0), egh_tuning(df64 ? 2 : 1) };
     if (prof::enabled()) {
         // per-kernel timing needs the launches themselves, not a replay
-        enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
+        enqueue_step(cs, m, C, sp, a.psd, df64, want, split, tune);
     } else {
         char key[200];
-        snprintf(key, sizeof(key), "%p|%d|%d%d|%d|%d,%d,%d|%d,%d,%d", (const void*)sp, a.psd, (int)df64,
-            g_defer_df64.load(), want,
+        snprintf(key, sizeof(key), "%p|%d|%d%d%d|%d|%d,%d,%d|%d,%d,%d", (const void*)sp, a.psd, (int)df64,
+            g_defer_df64.load(), (int)split, want,
             tune[0].threads, tune[0].blocks_per_sm, tune[0].tiles_per_grab, tune[1].threads, tune[1].blocks_per_sm,
             tune[1].tiles_per_grab);
         if (!C.exec || C.graph_key != key) {
@@ -1063,14 +1142,16 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
             {
                 // launch shapes (and their occupancy queries) before capturing
                 int b, t;
-                egh_grid(tune[0], C.max_n, k_local, b, t);
+                egh_grid(tune[0], C.max_n, k_local<PATH_ANY>, b, t);
+                egh_grid(tune[0], C.max_n, k_local<PATH_F64>, b, t);
+                egh_grid(tune[0], C.max_n, k_local<PATH_F32>, b, t);
                 if (df64) egh_grid(tune[1], C.max_n, k_psd_scatter<dd>, b, t);
                 else egh_grid(tune[1], C.max_n, k_psd_scatter<double>, b, t);
             }
             IPCG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             int kernels = 0;
             try {
-                kernels = enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
+                kernels = enqueue_step(cs, m, C, sp, a.psd, df64, want, split, tune);
             } catch (...) {
                 cudaGraph_t g = nullptr;
                 cudaStreamEndCapture(s, &g);
@@ -1102,6 +1183,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     EghCache& C = cache_for(cs, m);
     const Params* sp = upload_params_egh(cs, m, a);
     const bool df64 = a.df64_psd != 0;
+    const bool split = a.mixed || a.fp32_local;
     // the largest chunk is the workload
     size_t big = 0;
     for (size_t i = 0; i < C.chunks.size(); ++i)
@@ -1124,10 +1206,10 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     auto time_stage = [&](int stage, const EghTuning& t) {
         float ms = 0;
         for (int r = 0; r < 2; ++r) {
-            IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 3, s));
+            IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 4, s));
             IPCG_CUDA(cudaEventRecord(e0, s));
-            if (stage == 0) launch_local(cc, m, C, ch, sp, sv, C.queue.p, want, t, s);
-            else launch_psd(cc, C, ch, (int)big, C.queue.p + 1, a.psd, df64, t, s);
+            if (stage == 0) launch_local(cc, m, C, ch, sp, sv, C.queue.p, want, split, t, s);
+            else launch_psd(cc, C, ch, (int)big, C.queue.p + 2, a.psd, df64, t, s);
             prof::count();
             IPCG_CUDA(cudaEventRecord(e1, s));
             IPCG_CUDA(cudaEventSynchronize(e1));
@@ -1157,7 +1239,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
             }
         };
         for (int threads : { 32, 64, 128 }) {
-            const int occ = stage == 0 ? occupancy(dev, k_local, threads)
+            const int occ = stage == 0 ? occupancy(dev, split ? k_local<PATH_F64> : k_local<PATH_ANY>, threads)
                 : (df64 ? occupancy(dev, k_psd_scatter<dd>, threads) : occupancy(dev, k_psd_scatter<double>, threads));
             for (int bps : { 1, 2, 4, 8, 16, 32 }) {
                 if (bps > occ) break;
