@@ -26,9 +26,10 @@
 // and k_energy_scenes sums each scene's partial energies at the end.
 // Everything is in fixed order (deterministic: no launch shape changes a
 // bit) and every size is known from the pattern, so no step needs the host:
-// the launches of a step are captured once into a CUDA graph and replayed,
-// reading the call's pointers (positions, outputs, scratch) from a small
-// device-side argument block that is updated before each replay.
+// from a pattern's second step on, the launches of a step are captured once
+// into a CUDA graph and replayed, reading the call's pointers (positions,
+// outputs, scratch) from a small device-side argument block that is updated
+// before each replay (a pattern's first step runs as plain launches).
 //
 // The two per-contact stages are split because they want different
 // residency: the local Hessian code is long and register-heavy, the
@@ -123,6 +124,7 @@ struct EghCache {
     cudaGraphExec_t exec = nullptr;
     std::string graph_key;
     int graph_kernels = 0;
+    int64_t steps = 0; // steps run on this pattern
     ~EghCache()
     {
         if (exec) cudaGraphExecDestroy(exec);
@@ -843,6 +845,7 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
         C.graph = nullptr;
     }
     C.graph_key.clear();
+    C.steps = 0;
 }
 
 // Launch geometry of a stage for a tuning: a persistent grid of
@@ -1125,8 +1128,14 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     const bool df64 = a.df64_psd != 0;
     const bool split = a.mixed || a.fp32_local;
     const EghTuning tune[2] = { egh_tuning(0), egh_tuning(df64 ? 2 : 1) };
-    if (prof::enabled()) {
-        // per-kernel timing needs the launches themselves, not a replay
+    // A pattern's first step runs as plain launches: a set that is rebuilt
+    // before its next Hessian (a Newton loop whose collision set changes,
+    // a served request) would pay the capture and instantiation for nothing.
+    // From its second step on, the step is captured once and replayed.
+    const bool direct = prof::enabled() || C.steps == 0;
+    ++C.steps;
+    if (direct) {
+        // (per-kernel timing also needs the launches themselves)
         enqueue_step(cs, m, C, sp, a.psd, df64, want, split, tune);
     } else {
         char key[200];
