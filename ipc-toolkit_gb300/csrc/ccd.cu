@@ -821,9 +821,54 @@ __device__ int stencil_ccd(Query& q, double min_distance, const CCDParams& P, do
 // and a relative 1e-6.  Only used to skip queries that cannot lower the
 // earliest time found so far (and only when it is at least 1e-6, above which
 // the strategy's small-ToI rerun cannot apply).
+// First time in [0, 1] at which min_k (A_k + B_k t) <= R and max_k (...)
+// >= -R (+inf if none): 0 or a time where a line enters one of the two sets.
+__device__ __forceinline__ float first_time(const float A[4], const float B[4], float R, float slack)
+{
+    float Tc = __int_as_float(0x7f800000);
+    for (int j = 0; j < 9; ++j) {
+        float tj;
+        if (j == 0) tj = 0.f;
+        else {
+            const int k = (j - 1) >> 1;
+            if (j & 1) {
+                if (!(B[k] < 0.f)) continue;
+                tj = (R - A[k]) / B[k];
+            } else {
+                if (!(B[k] > 0.f)) continue;
+                tj = (-R - A[k]) / B[k];
+            }
+            if (!(tj >= 0.f && tj <= 1.f) || !(tj < Tc)) continue;
+        }
+        float g = A[0] + B[0] * tj, h = g;
+        for (int k = 1; k < 4; ++k) {
+            const float f = A[k] + B[k] * tj;
+            g = fminf(g, f);
+            h = fmaxf(h, f);
+        }
+        if (g <= R + slack && h >= -R - slack) Tc = fminf(Tc, tj);
+    }
+    return Tc;
+}
+
+// min over t in [0, 1] of |a + t b| (3-vectors)
+__device__ __forceinline__ double min_norm_on_segment(const double a[3], const double b[3])
+{
+    const double bb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+    const double ab = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    const double t = bb > 0 ? fmin(1.0, fmax(0.0, -ab / bb)) : 0.0;
+    double n = 0;
+    for (int c = 0; c < 3; ++c) {
+        const double x = a[c] + t * b[c];
+        n += x * x;
+    }
+    return sqrt(n);
+}
+
 __device__ double toi_lower_bound(const Query& q, double min_distance, const CCDParams& P)
 {
     const double INF = __longlong_as_double(0x7ff0000000000000LL);
+    const float FINF = __int_as_float(0x7f800000);
     double d2;
     if (q.vf) d2 = point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
         point_triangle_distance_type(q.s[0], q.s[1], q.s[2], q.s[3]));
@@ -836,59 +881,76 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
     const double delta = fmin(0.5 * d0, P.tolerance);
     double err[3];
     numerical_error(q, ms > 0, err);
-    double T = 0.0, bmax = 0.0;
+    // per coordinate, F = A00 + u Au + v Av + t (B00 + u Bu + v Bv) (FP64)
+    double a00[3], au[3], av[3], b00[3], bu[3], bv[3];
     for (int c = 0; c < 3; ++c) {
-        // corner lines a + b t at (u, v) in {0, 1}^2 (FP64), then the search
-        // in FP32 with a slack that covers its rounding (2^-20 of the lines'
-        // size) and a final 2^-20 margin on the time
+        const double s0 = comp(q.s[0], c), s1 = comp(q.s[1], c), s2 = comp(q.s[2], c), s3 = comp(q.s[3], c);
+        const double e0 = comp(q.d[0], c), e1 = comp(q.d[1], c), e2 = comp(q.d[2], c), e3 = comp(q.d[3], c);
+        if (q.vf) {
+            a00[c] = s0 - s1;
+            au[c] = -(s2 - s1);
+            av[c] = -(s3 - s1);
+            b00[c] = e0 - e1;
+            bu[c] = -(e2 - e1);
+            bv[c] = -(e3 - e1);
+        } else {
+            a00[c] = s0 - s2;
+            au[c] = s1 - s0;
+            av[c] = -(s3 - s2);
+            b00[c] = e0 - e2;
+            bu[c] = e1 - e0;
+            bv[c] = -(e3 - e2);
+        }
+    }
+    double T = 0.0, bmax = 0.0, rmax = 0.0;
+    float R[3], scale[3];
+    for (int c = 0; c < 3; ++c) {
+        // corner lines at (u, v) in {0, 1}^2, the search in FP32 with a
+        // slack that covers its rounding (2^-20 of the lines' size) and a
+        // final 2^-20 margin on the time
         float A[4], B[4];
-        float slack = 0.f;
         for (int k = 0; k < 4; ++k) {
             const double u = (k & 1) ? 1.0 : 0.0, v = (k & 2) ? 1.0 : 0.0;
-            const double s0 = comp(q.s[0], c), s1 = comp(q.s[1], c), s2 = comp(q.s[2], c), s3 = comp(q.s[3], c);
-            const double e0 = comp(q.d[0], c), e1 = comp(q.d[1], c), e2 = comp(q.d[2], c), e3 = comp(q.d[3], c);
-            double a, b;
-            if (q.vf) {
-                a = s0 - s1 - u * (s2 - s1) - v * (s3 - s1);
-                b = e0 - e1 - u * (e2 - e1) - v * (e3 - e1);
-            } else {
-                a = s0 + u * (s1 - s0) - s2 - v * (s3 - s2);
-                b = e0 + u * (e1 - e0) - e2 - v * (e3 - e2);
-            }
+            const double a = a00[c] + u * au[c] + v * av[c], b = b00[c] + u * bu[c] + v * bv[c];
             bmax = fmax(bmax, fabs(b));
             A[k] = (float)a;
             B[k] = (float)b;
-            slack = fmaxf(slack, fabsf(A[k]) + fabsf(B[k]));
         }
-        const float R = (float)(3.0 * err[c] + ms + delta);
-        slack = (slack + R) * 0x1p-20f;
-        // the first time in {g <= R} and {h >= -R}: 0 or a time where a
-        // line enters one of them
-        float Tc = __int_as_float(0x7f800000);
-        for (int j = 0; j < 9; ++j) {
-            float tj;
-            if (j == 0) tj = 0.f;
-            else {
-                const int k = (j - 1) >> 1;
-                if (j & 1) {
-                    if (!(B[k] < 0.f)) continue;
-                    tj = (R - A[k]) / B[k];
-                } else {
-                    if (!(B[k] > 0.f)) continue;
-                    tj = (-R - A[k]) / B[k];
-                }
-                if (!(tj >= 0.f && tj <= 1.f) || !(tj < Tc)) continue;
-            }
-            float g = A[0] + B[0] * tj, h = g;
-            for (int k = 1; k < 4; ++k) {
-                const float f = A[k] + B[k] * tj;
-                g = fminf(g, f);
-                h = fmaxf(h, f);
-            }
-            if (g <= R + slack && h >= -R - slack) Tc = fminf(Tc, tj);
-        }
+        R[c] = (float)(3.0 * err[c] + ms + delta);
+        rmax = fmax(rmax, 3.0 * err[c] + ms + delta);
+        scale[c] = (float)(fabs(a00[c]) + fabs(au[c]) + fabs(av[c]) + fabs(b00[c]) + fabs(bu[c]) + fabs(bv[c]));
+        const float Tc = first_time(A, B, R[c], (scale[c] + R[c]) * 0x1p-20f);
         if (!(Tc <= 1.f)) return INF;
         T = fmax(T, (double)Tc);
+    }
+    // Quarters of the (u, v) square: when both primitives' edges along u and
+    // v stay longer than sqrt(3) (2 r + delta) over the step, no box wider
+    // than 1/2 in u or v can be accepted (one coordinate of F would change
+    // by more than 2 r + delta across it, while acceptance needs every
+    // coordinate inside the separation box or narrower than delta), so the
+    // accepted box lies in one quarter and the bound is the least of the
+    // quarters' bounds.
+    const double lu = min_norm_on_segment(au, bu), lv = min_norm_on_segment(av, bv);
+    const double need = 1.7320508075688772 * (2.0 * rmax + delta) * (1.0 + 1e-6);
+    if (lu > need && lv > need) {
+        float Tq_min = FINF;
+        for (int qd = 0; qd < 4; ++qd) {
+            const float uq = (qd & 1) ? 0.5f : 0.f, vq = (qd & 2) ? 0.5f : 0.f;
+            float Tq = 0.f;
+            for (int c = 0; c < 3 && Tq <= 1.f; ++c) {
+                float A[4], B[4];
+                for (int k = 0; k < 4; ++k) {
+                    const float u = uq + ((k & 1) ? 0.5f : 0.f), v = vq + ((k & 2) ? 0.5f : 0.f);
+                    A[k] = (float)a00[c] + u * (float)au[c] + v * (float)av[c];
+                    B[k] = (float)b00[c] + u * (float)bu[c] + v * (float)bv[c];
+                }
+                const float Tc = first_time(A, B, R[c], (scale[c] + R[c]) * 0x1p-20f);
+                Tq = fmaxf(Tq, Tc);
+            }
+            Tq_min = fminf(Tq_min, Tq);
+        }
+        if (!(Tq_min <= 1.f)) return INF;
+        T = fmax(T, (double)Tq_min);
     }
     // the time tolerance of the inclusion search: delta / (3 max |F(1) - F(0)|)
     // over the corners, F(1) - F(0) being the corner lines' slopes
@@ -925,9 +987,6 @@ __device__ __forceinline__ int load_query(int i, const int2* __restrict__ cand_e
     return ids[0];
 }
 
-// Per candidate: its lower bound (by candidate index) and, for sorting the
-// queries by it, its bit pattern (non-negative doubles order like their
-// bits) with the candidate index.
 // An estimate of a query's time of impact, for ordering only: the time at
 // which the signed volume of its four points (linear between its values at
 // t = 0 and t = 1) changes sign, if the two primitives' closest points lie

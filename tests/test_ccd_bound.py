@@ -5,7 +5,8 @@ follows tight_inclusion_ccd.cpp:33-336) on the candidates of the two-sheet
 scene and of batch scenes: the bound must never exceed a query's time of
 impact, so a query whose bound is at or after the earliest time found so far
 cannot change the step.  Also checks that the bound prunes: most queries of
-a colliding scene have bounds after the scene's earliest impact.
+a colliding scene (over 80 % here) have bounds after the scene's earliest
+impact.
 """
 import numpy as np
 import pytest
@@ -19,14 +20,14 @@ def _num_err(s, e, vf):
     return filt * np.minimum(m, 1.0) ** 3
 
 
-def _first_time(A, B, R):
+def _first_time(A, B, R, scale):
     """First t in [0, 1] with min_k(A_k + B_k t) <= R and max_k(...) >= -R,
-    searched in FP32 on the FP64 corner lines with a 2^-20 slack."""
+    searched in FP32 with a slack of 2^-20 (scale + R)."""
     A = A.astype(np.float32)
     B = B.astype(np.float32)
     R = R.astype(np.float32)
     n = A.shape[1]
-    slack = ((np.abs(A) + np.abs(B)).max(axis=0) + R) * np.float32(2.0 ** -20)
+    slack = (scale.astype(np.float32) + R) * np.float32(2.0 ** -20)
     starts = [np.zeros(n, np.float32)]
     with np.errstate(divide="ignore", invalid="ignore"):
         for k in range(4):
@@ -41,27 +42,68 @@ def _first_time(A, B, R):
     return T
 
 
+def _lines(x0, d, vf, c):
+    """F_c = A00 + u Au + v Av + t (B00 + u Bu + v Bv)."""
+    s_, e_ = x0[:, :, c], d[:, :, c]
+    if vf:
+        return (s_[:, 0] - s_[:, 1], -(s_[:, 2] - s_[:, 1]), -(s_[:, 3] - s_[:, 1]),
+                e_[:, 0] - e_[:, 1], -(e_[:, 2] - e_[:, 1]), -(e_[:, 3] - e_[:, 1]))
+    return (s_[:, 0] - s_[:, 2], s_[:, 1] - s_[:, 0], -(s_[:, 3] - s_[:, 2]),
+            e_[:, 0] - e_[:, 2], e_[:, 1] - e_[:, 0], -(e_[:, 3] - e_[:, 2]))
+
+
+def _min_norm(a, b):
+    bb = (b * b).sum(0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        t = np.where(bb > 0, np.clip(-(a * b).sum(0) / np.where(bb > 0, bb, 1.0), 0, 1), 0.0)
+    return np.sqrt(((a + t * b) ** 2).sum(0))
+
+
+def _first_time_grid(A00, Au, Av, B00, Bu, Bv, R, uq, vq, w):
+    """_first_time over the corners of the cell [uq, uq + w] x [vq, vq + w],
+    the corner lines formed in FP32 from the FP64 coefficients."""
+    f32 = np.float32
+    A = np.array([f32(A00) + f32(uq + w * (k & 1)) * Au.astype(f32) + f32(vq + w * ((k >> 1) & 1)) * Av.astype(f32)
+                  for k in range(4)], dtype=f32)
+    B = np.array([f32(B00) + f32(uq + w * (k & 1)) * Bu.astype(f32) + f32(vq + w * ((k >> 1) & 1)) * Bv.astype(f32)
+                  for k in range(4)], dtype=f32)
+    return A, B
+
+
 def toi_lower_bound(x0, x1, d0, vf, min_distance=0.0, tolerance=1e-6, rescale=0.8):
     ms = np.minimum((1 - rescale) * (d0 - min_distance), 1e-4) + min_distance
     delta = np.minimum(0.5 * d0, tolerance)
     err = _num_err(x0, x1, vf)
     d = x1 - x0
-    T = np.zeros(x0.shape[0])
-    bmax = np.zeros(x0.shape[0])
+    n = x0.shape[0]
+    coef = [_lines(x0, d, vf, c) for c in range(3)]
+    T = np.zeros(n)
+    bmax = np.zeros(n)
+    Rs, scales = [], []
     for c in range(3):
-        A, B = [], []
-        for k in range(4):
-            u, v = float(k & 1), float((k >> 1) & 1)
-            s_, e_ = x0[:, :, c], d[:, :, c]
-            if vf:
-                A.append(s_[:, 0] - s_[:, 1] - u * (s_[:, 2] - s_[:, 1]) - v * (s_[:, 3] - s_[:, 1]))
-                B.append(e_[:, 0] - e_[:, 1] - u * (e_[:, 2] - e_[:, 1]) - v * (e_[:, 3] - e_[:, 1]))
-            else:
-                A.append(s_[:, 0] + u * (s_[:, 1] - s_[:, 0]) - s_[:, 2] - v * (s_[:, 3] - s_[:, 2]))
-                B.append(e_[:, 0] + u * (e_[:, 1] - e_[:, 0]) - e_[:, 2] - v * (e_[:, 3] - e_[:, 2]))
-        B = np.array(B)
+        A00, Au, Av, B00, Bu, Bv = coef[c]
+        A = np.array([A00 + (k & 1) * Au + ((k >> 1) & 1) * Av for k in range(4)])
+        B = np.array([B00 + (k & 1) * Bu + ((k >> 1) & 1) * Bv for k in range(4)])
         bmax = np.maximum(bmax, np.abs(B).max(axis=0))
-        T = np.maximum(T, _first_time(np.array(A), B, 3 * err[:, c] + ms + delta))
+        R = 3 * err[:, c] + ms + delta
+        Rs.append(R)
+        scales.append(np.abs(A00) + np.abs(Au) + np.abs(Av) + np.abs(B00) + np.abs(Bu) + np.abs(Bv))
+        T = np.maximum(T, _first_time(A, B, R, scales[c]))
+    # quarters, for primitives whose edges stay long next to the separation
+    rmax = np.max(Rs, axis=0)
+    au = np.array([coef[c][1] for c in range(3)]); bu = np.array([coef[c][4] for c in range(3)])
+    av = np.array([coef[c][2] for c in range(3)]); bv = np.array([coef[c][5] for c in range(3)])
+    need = np.sqrt(3.0) * (2 * rmax + delta) * (1 + 1e-6)
+    longp = (_min_norm(au, bu) > need) & (_min_norm(av, bv) > need)
+    Tq = np.full(n, INF)
+    for uq in (0.0, 0.5):
+        for vq in (0.0, 0.5):
+            t = np.zeros(n)
+            for c in range(3):
+                A, B = _first_time_grid(*coef[c], Rs[c], uq, vq, 0.5)
+                t = np.maximum(t, _first_time(A, B, Rs[c], scales[c]))
+            Tq = np.minimum(Tq, t)
+    T = np.where(longp, np.maximum(T, Tq), T)
     with np.errstate(invalid="ignore", divide="ignore"):
         tol0 = np.where(bmax == 0, delta, delta / (3 * np.where(bmax == 0, 1.0, bmax)))
         out = np.maximum(0.0, (T - 2.0 ** -20 - tol0 * (1 + 1e-6) - 2.0 ** -60) * (1 - 1e-6))
@@ -100,4 +142,4 @@ def test_bound_never_exceeds_time_of_impact(oracle_mod, scene):
     lb = np.concatenate(bounds)
     # the scenes collide: most queries are skipped once the earliest impact is known
     assert earliest < 1.0
-    assert np.mean(lb >= earliest) > 0.5
+    assert np.mean(lb >= earliest) > 0.8
