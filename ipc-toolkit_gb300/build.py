@@ -23,7 +23,7 @@ COMMON = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcom
                  "-Xcompiler", "-ffp-contract=off",
                  "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 EXACT = {"broad_phase.cu", "collisions.cu", "ccd.cu", "candidates.cu"}
-SOURCES = ["abi.cu", "broad_phase.cu", "collisions.cu", "barrier.cu", "egh.cu", "ccd.cu", "sort.cu", "server.cu",
+SOURCES = ["abi.cu", "broad_phase.cu", "collisions.cu", "barrier.cu", "egh.cu", "ccd.cu", "ccd_bound.cu", "sort.cu", "server.cu",
            "candidates.cu"]
 
 

@@ -397,6 +397,12 @@ EghTuning egh_tuning(int stage);
 void egh_defer_df64(bool on);
 // ccd.cu: testing switch for the step-size passes' statistics
 extern std::atomic<int> g_ccd_stats;
+// ccd_bound.cu: per step-size query (EE candidates, then FV), a lower bound
+// on its time of impact (lb), and sort keys (scene | estimate) with the
+// query indices
+void ccd_bound_launch(cudaStream_t s, const int2* cee, int n_ee, const int2* cfv, int n_fv, const double* V0,
+    const double* V1, const int* E, const int* F, const double* min_distance, SceneView sv, double tolerance,
+    double rescale, double* lb, unsigned long long* keys, int* ids);
 extern std::atomic<long long> g_ccd_thread_budget;
 void egh_set_tuning(int stage, const EghTuning& t);
 // Time both stages over candidate tunings on this set's largest chunk and
