@@ -447,7 +447,7 @@ __device__ int root_finder(const Query& q, const double err[3], double ms, const
 // the lanes, which walk their subtrees depth first (as the one-thread search
 // does with a full heap).  The box count for the iteration cap and the budget
 // is the warp's total (checked per round).
-constexpr int WPOOL = 1024; // sorted pool per warp
+constexpr int WPOOL = 256; // sorted pool per warp
 constexpr int WCH = 64;    // children per round (2 per lane)
 struct WarpPool {
     CBox* cur;  // WPOOL + WCH
@@ -839,7 +839,7 @@ __global__ void __launch_bounds__(BLOCK, 3) k_ccd(const int2* __restrict__ cand_
 
 // The warp-per-query pass (the seeds, and the queries the budgeted pass left
 // unfinished): like k_ccd, with every lane of a warp on the same query.
-constexpr int WARPS_PER_BLOCK = 2;
+constexpr int WARPS_PER_BLOCK = 4;
 __global__ void __launch_bounds__(32 * WARPS_PER_BLOCK) k_ccd_warp(const int2* __restrict__ cand_ee, int n_ee,
     const int2* __restrict__ cand_fv, int n_fv, const double* __restrict__ V0, const double* __restrict__ V1,
     const int* __restrict__ E, const int* __restrict__ F, const double* __restrict__ min_distance, SceneView sv,

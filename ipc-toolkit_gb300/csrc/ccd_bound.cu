@@ -131,24 +131,26 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
         if (!(Tc <= 1.f)) return INF;
         T = fmax(T, (double)Tc);
     }
-    // Quarters of the (u, v) square: when both primitives' edges along u and
-    // v stay longer than sqrt(3) (2 r + delta) over the step, no box wider
-    // than 1/2 in u or v can be accepted (one coordinate of F would change
-    // by more than 2 r + delta across it, while acceptance needs every
-    // coordinate inside the separation box or narrower than delta), so the
-    // accepted box lies in one quarter and the bound is the least of the
-    // quarters' bounds.
+    // Cells of the (u, v) square (4 x 4): when both primitives' edges along u
+    // and v stay longer than 2 sqrt(3) (2 r + delta) over the step, no box
+    // wider than 1/4 in u or v can be accepted (one coordinate of F would
+    // change by more than 2 r + delta across it, while acceptance needs every
+    // coordinate inside the separation box or narrower than delta, and the
+    // domain tolerance would be below 1/4), so the accepted box lies in one
+    // cell and the bound is the least of the cells' bounds.
+    constexpr int NCELL = 4;
     const double lu = min_norm_on_segment(au, bu), lv = min_norm_on_segment(av, bv);
-    const double need = 1.7320508075688772 * (2.0 * rmax + delta) * (1.0 + 1e-6);
+    const double need = 1.7320508075688772 * (2.0 * rmax + delta) * (0.5 * NCELL) * (1.0 + 1e-6);
     if (lu > need && lv > need) {
+        const float w = 1.f / NCELL;
         float Tq_min = FINF;
-        for (int qd = 0; qd < 4; ++qd) {
-            const float uq = (qd & 1) ? 0.5f : 0.f, vq = (qd & 2) ? 0.5f : 0.f;
+        for (int cell = 0; cell < NCELL * NCELL; ++cell) {
+            const float uq = w * (float)(cell % NCELL), vq = w * (float)(cell / NCELL);
             float Tq = 0.f;
-            for (int c = 0; c < 3 && Tq <= 1.f; ++c) {
+            for (int c = 0; c < 3 && Tq <= 1.f && Tq < Tq_min; ++c) {
                 float A[4], B[4];
                 for (int k = 0; k < 4; ++k) {
-                    const float u = uq + ((k & 1) ? 0.5f : 0.f), v = vq + ((k & 2) ? 0.5f : 0.f);
+                    const float u = uq + ((k & 1) ? w : 0.f), v = vq + ((k & 2) ? w : 0.f);
                     A[k] = (float)a00[c] + u * (float)au[c] + v * (float)av[c];
                     B[k] = (float)b00[c] + u * (float)bu[c] + v * (float)bv[c];
                 }
