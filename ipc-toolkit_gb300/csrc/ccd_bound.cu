@@ -73,18 +73,82 @@ __device__ __forceinline__ double min_norm_on_segment(const double a[3], const d
     return sqrt(n);
 }
 
+struct F3b {
+    float x, y, z;
+};
+__device__ __forceinline__ F3b f3(V3 a) { return F3b { (float)a.x, (float)a.y, (float)a.z }; }
+__device__ __forceinline__ F3b operator-(F3b a, F3b b) { return F3b { a.x - b.x, a.y - b.y, a.z - b.z }; }
+__device__ __forceinline__ float fdot(F3b a, F3b b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float clamp01(float x) { return fminf(1.f, fmaxf(0.f, x)); }
+
+// An upper bound on the distance between the primitives at t = 0: the FP64
+// distance between two points on them, at closest-point parameters found in
+// FP32 (the region tests of the standard point-triangle and segment-segment
+// closest-point algorithms; the parameters are clamped onto the primitives,
+// so the points lie on them whatever the FP32 rounding).  Only used to size
+// the separation of the bound, where a larger distance is the conservative
+// side.
+__device__ double distance_upper_bound(const Query& q)
+{
+    double s, t;
+    if (q.vf) {
+        // point s0, triangle (s1, s2, s3): parameters along s2 - s1 and s3 - s1
+        const F3b p = f3(q.s[0]), a = f3(q.s[1]), b = f3(q.s[2]), c = f3(q.s[3]);
+        const F3b ab = b - a, ac = c - a, ap = p - a, bp = p - b, cp = p - c;
+        const float d1 = fdot(ab, ap), d2 = fdot(ac, ap), d3 = fdot(ab, bp), d4 = fdot(ac, bp);
+        const float d5 = fdot(ab, cp), d6 = fdot(ac, cp);
+        const float vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+        if (d1 <= 0.f && d2 <= 0.f) s = t = 0;
+        else if (d3 >= 0.f && d4 <= d3) s = 1, t = 0;
+        else if (d6 >= 0.f && d5 <= d6) s = 0, t = 1;
+        else if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) s = clamp01(d1 / (d1 - d3)), t = 0;
+        else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) s = 0, t = clamp01(d2 / (d2 - d6));
+        else if (va <= 0.f && d4 - d3 >= 0.f && d5 - d6 >= 0.f) {
+            const float w = clamp01((d4 - d3) / ((d4 - d3) + (d5 - d6)));
+            s = 1.f - w, t = w;
+        } else {
+            const float den = va + vb + vc;
+            const float v = den != 0.f ? clamp01(vb / den) : 0.f, w = den != 0.f ? clamp01(vc / den) : 0.f;
+            s = v, t = fminf(w, 1.f - v);
+        }
+        const V3 x = q.s[1] + (q.s[2] - q.s[1]) * s + (q.s[3] - q.s[1]) * t;
+        return sqrt(sqnorm(q.s[0] - x));
+    }
+    // segments (s0, s1) and (s2, s3)
+    const F3b p1 = f3(q.s[0]), p2 = f3(q.s[2]);
+    const F3b d1 = f3(q.s[1]) - p1, d2 = f3(q.s[3]) - p2, r = p1 - p2;
+    const float a = fdot(d1, d1), e = fdot(d2, d2), f = fdot(d2, r);
+    float sf = 0.f, tf = 0.f;
+    if (a > 0.f || e > 0.f) {
+        if (!(a > 0.f)) tf = clamp01(f / e);
+        else {
+            const float c = fdot(d1, r);
+            if (!(e > 0.f)) sf = clamp01(-c / a);
+            else {
+                const float b = fdot(d1, d2), den = a * e - b * b;
+                sf = den > 0.f ? clamp01((b * f - c * e) / den) : 0.f;
+                tf = (b * sf + f) / e;
+                if (tf < 0.f) tf = 0.f, sf = clamp01(-c / a);
+                else if (tf > 1.f) tf = 1.f, sf = clamp01((b - c) / a);
+            }
+        }
+    }
+    s = sf, t = clamp01(tf);
+    const V3 x = q.s[0] + (q.s[1] - q.s[0]) * s, y = q.s[2] + (q.s[3] - q.s[2]) * t;
+    return sqrt(sqnorm(x - y));
+}
+
 __device__ double toi_lower_bound(const Query& q, double min_distance, const CCDParams& P)
 {
     const double INF = __longlong_as_double(0x7ff0000000000000LL);
     const float FINF = __int_as_float(0x7f800000);
-    double d2;
-    if (q.vf) d2 = point_triangle_distance(q.s[0], q.s[1], q.s[2], q.s[3],
-        point_triangle_distance_type(q.s[0], q.s[1], q.s[2], q.s[3]));
-    else d2 = edge_edge_distance(q.s[0], q.s[1], q.s[2], q.s[3],
-        edge_edge_distance_type(q.s[0], q.s[1], q.s[2], q.s[3]));
-    const double d0 = sqrt(d2);
+    // a query that does not move is decided at once by the search (0 or a
+    // miss, from its exact distance): never skipped
+    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) return 0.0;
+    // an upper bound of the distance at t = 0 gives a larger separation, the
+    // conservative side (0 if it is within the minimum distance)
+    const double d0 = distance_upper_bound(q);
     if (d0 <= min_distance) return 0.0;
-    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) return INF;
     const double ms = fmin((1.0 - P.rescale) * (d0 - min_distance), 1e-4) + min_distance;
     const double delta = fmin(0.5 * d0, P.tolerance);
     double err[3];
