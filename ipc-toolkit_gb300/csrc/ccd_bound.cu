@@ -142,13 +142,17 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
 {
     const double INF = __longlong_as_double(0x7ff0000000000000LL);
     const float FINF = __int_as_float(0x7f800000);
-    // a query that does not move is decided at once by the search (0 or a
-    // miss, from its exact distance): never skipped
-    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) return 0.0;
     // an upper bound of the distance at t = 0 gives a larger separation, the
     // conservative side (0 if it is within the minimum distance)
     const double d0 = distance_upper_bound(q);
     if (d0 <= min_distance) return 0.0;
+    if (v3eq(q.s[0], q.e[0]) && v3eq(q.s[1], q.e[1]) && v3eq(q.s[2], q.e[2]) && v3eq(q.s[3], q.e[3])) {
+        // a query that does not move is a miss unless its exact distance is
+        // within the minimum distance; the upper bound exceeds the exact
+        // distance by at most the FP32 parameters' error along the edges
+        const double ext = sqrt(sqnorm(q.s[1] - q.s[0])) + sqrt(sqnorm(q.s[2] - q.s[0])) + sqrt(sqnorm(q.s[3] - q.s[0]));
+        return d0 > min_distance + 1e-5 * ext ? INF : 0.0;
+    }
     const double ms = fmin((1.0 - P.rescale) * (d0 - min_distance), 1e-4) + min_distance;
     const double delta = fmin(0.5 * d0, P.tolerance);
     double err[3];

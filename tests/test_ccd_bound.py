@@ -113,8 +113,8 @@ def toi_lower_bound(x0, x1, d0, vf, min_distance=0.0, tolerance=1e-6, rescale=0.
         tol0 = np.where(bmax == 0, delta, delta / (3 * np.where(bmax == 0, 1.0, bmax)))
         out = np.maximum(0.0, (T - 2.0 ** -20 - tol0 * (1 + 1e-6) - 2.0 ** -60) * (1 - 1e-6))
     out = np.where(np.isinf(T), INF, out)
-    # queries that do not move are never skipped
-    out = np.where(np.all(x0 == x1, axis=(1, 2)), 0.0, out)
+    # queries that do not move miss unless within the minimum distance
+    out = np.where(np.all(x0 == x1, axis=(1, 2)), INF, out)
     return np.where(d0 <= min_distance, 0.0, out)
 
 
