@@ -312,6 +312,11 @@ int ipcg_barrier_autotune(const ipcg_collisions* collisions, const ipcg_mesh* me
 #define IPCG_STAGE_PSD_DF64 2
 int ipcg_barrier_tuning(int stage, int* threads, int* blocks_per_sm, int* tiles_per_grab);
 int ipcg_barrier_set_tuning(int stage, int threads, int blocks_per_sm, int tiles_per_grab);
+/* The current device's FP64 fused multiply-add rate in TFLOP/s, measured by
+ * a kernel of independent DFMA chains (the pipe's peak for non-tensor FP64
+ * code such as this path's per-contact work).  No counterpart in the
+ * reference. */
+int ipcg_fp64_fma_rate(double* tflops);
 /* Testing switch: with on != 0, the df64 projection (IPCG_BARRIER_DF64_PSD)
  * hands every local Hessian to its FP64 fix-up pass, the path taken by the
  * rare matrix on which the df64 eigensolver does not converge.  No

@@ -811,6 +811,15 @@ int ipcg_testing_ccd_stats(const ipcg_mesh* mesh, int enable, int64_t* out)
     });
 }
 
+int ipcg_fp64_fma_rate(double* tflops)
+{
+    return guarded([&] {
+        require(tflops, "NULL argument");
+        require_device();
+        *tflops = fp64_fma_rate();
+    });
+}
+
 int ipcg_testing_ccd_budget(int64_t boxes)
 {
     return guarded([&] {

@@ -1069,6 +1069,54 @@ static std::string psd_failure(const EghCache& C)
 
 void egh_defer_df64(bool on) { g_defer_df64.store(on ? 1 : 0); }
 
+// ---- the device's FP64 FMA rate ----
+// Each thread runs FP64_CHAINS independent chains of fused multiply-adds
+// (independent so that the pipe, not the latency, is the limit), on a grid
+// of 64 warps per SM; the sum of the chains is written so that nothing is
+// removed as dead code.
+constexpr int FP64_CHAINS = 8, FP64_ITERS = 4096;
+__global__ void __launch_bounds__(256) k_fp64_rate(double a, double b, double* __restrict__ out)
+{
+    double x[FP64_CHAINS];
+#pragma unroll
+    for (int k = 0; k < FP64_CHAINS; ++k) x[k] = threadIdx.x + k;
+    for (int it = 0; it < FP64_ITERS; ++it)
+#pragma unroll
+        for (int k = 0; k < FP64_CHAINS; ++k) x[k] = fma(x[k], a, b);
+    double sum = 0;
+#pragma unroll
+    for (int k = 0; k < FP64_CHAINS; ++k) sum += x[k];
+    if (sum == 12345.678) out[0] = sum;
+}
+
+double fp64_fma_rate()
+{
+    int dev = 0, sms = 1;
+    IPCG_CUDA(cudaGetDevice(&dev));
+    IPCG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DBuf<double> out;
+    out.reserve(1);
+    cudaEvent_t e0, e1;
+    IPCG_CUDA(cudaEventCreate(&e0));
+    IPCG_CUDA(cudaEventCreate(&e1));
+    const int blocks = sms * 8, threads = 256;
+    float best = 1e30f;
+    for (int r = 0; r < 4; ++r) {
+        IPCG_CUDA(cudaEventRecord(e0, 0));
+        k_fp64_rate<<<blocks, threads>>>(0.999999, 1e-7, out.p);
+        IPCG_CHECK_LAUNCH();
+        IPCG_CUDA(cudaEventRecord(e1, 0));
+        IPCG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0;
+        IPCG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (r > 0) best = std::min(best, ms); // the first run warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const double flops = 2.0 * FP64_CHAINS * FP64_ITERS * (double)blocks * threads;
+    return flops / (best * 1e-3) / 1e12;
+}
+
 EghTuning egh_tuning(int stage)
 {
     const int d = device_index();

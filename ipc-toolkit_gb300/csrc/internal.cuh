@@ -393,6 +393,9 @@ struct EghTuning {
 // current device: 0 the local Hessians, 1 the FP64 projection and scatter,
 // 2 the df64 one.
 EghTuning egh_tuning(int stage);
+// The device's FP64 fused multiply-add rate (TFLOP/s), measured by a kernel
+// of independent DFMA chains: the roofline of FP64-bound, non-tensor code.
+double fp64_fma_rate();
 // Testing: the df64 projection defers every contact to its FP64 fix-up pass.
 void egh_defer_df64(bool on);
 // ccd.cu: testing switch for the step-size passes' statistics

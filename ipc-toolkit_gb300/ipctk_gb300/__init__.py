@@ -134,6 +134,7 @@ def _load():
         "ipcg_testing_defer_df64_psd": (i32, [i32]),
         "ipcg_testing_ccd_stats": (i32, [P, i32, P]),
         "ipcg_testing_ccd_budget": (i32, [i64]),
+        "ipcg_fp64_fma_rate": (i32, [P]),
         "ipcg_initial_barrier_stiffness": (i32, [d, i32, d, d, P, P, i64, d, d, P, P]),
         "ipcg_update_barrier_stiffness": (i32, [d, d, d, d, d, d, d, P]),
     }
@@ -280,6 +281,13 @@ def testing_ccd_stats(mesh, enable: bool = True) -> dict:
     _check(_load().ipcg_testing_ccd_stats(mesh._h, int(bool(enable)), _ptr(out)))
     keys = ("queries", "boxes", "max_boxes", "hits")
     return {p: dict(zip(keys, (int(x) for x in out[4 * k:4 * k + 4]))) for k, p in enumerate(("seeds", "budgeted", "hard"))}
+
+
+def fp64_fma_rate() -> float:
+    """ipcg_fp64_fma_rate: the device's FP64 fused multiply-add rate, TFLOP/s."""
+    r = C.c_double()
+    _check(_load().ipcg_fp64_fma_rate(C.byref(r)))
+    return float(r.value)
 
 
 def testing_ccd_budget(boxes: int = 0):
