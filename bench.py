@@ -502,6 +502,7 @@ def served_leg(dev, seed=4):
     for s in scs:
         m = ipctk.CollisionMesh(s["V"], s["E"], s["F"])
         ids.append(srv.add_scene(m, ipctk.NormalCollisions(), s["dhat"], 0.0, s["kappa"]))
+        srv.set_scene_options(ids[-1], mixed_precision=HEADLINE_MODE)
     for t in [srv.submit_barrier(i, s["V"]) for i, s in zip(ids, scs)]:
         srv.wait(t)  # every scene's collision set and work space resident
     pct = lambda a, q: float(np.percentile(np.array(a), q))
@@ -538,7 +539,8 @@ def served_leg(dev, seed=4):
     return {"workload": f"64 two-sheet scenes (batch size distribution, seed {seed}) + 4 sphere packs; "
                         f"{sum(s['V'].shape[0] for s in scs):,} verts resident; requests alternate barrier "
                         "(build + E + grad + CLAMP Hessian) and step size, positions +-0.1 dhat noise",
-            "workers": 8, "hbm_budget_gb": 120, "offered": offered, "below_capacity": below,
+            "workers": 8, "hbm_budget_gb": 120, "precision": PRECISION[HEADLINE_MODE],
+            "offered": offered, "below_capacity": below,
             "resident_gb": st["resident_bytes"] / 1e9, "workspace_releases": st["releases"]}
 
 

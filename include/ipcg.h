@@ -616,6 +616,10 @@ int ipcg_server_destroy(ipcg_server* server);
  * parameters. */
 int ipcg_server_add_scene(ipcg_server* server, ipcg_mesh* mesh, ipcg_collisions* collisions,
                           double dhat, double dmin, double stiffness, int64_t* scene);
+/* The barrier option bits (use_physical_barrier of ipcg_barrier_*: physical
+ * scaling, precision modes, barrier function) of a scene's barrier requests;
+ * 0 (the default) is the reference's plain FP64 form. */
+int ipcg_server_set_scene_options(ipcg_server* server, int64_t scene, int barrier_options);
 /* Host positions are copied at submission. */
 int ipcg_server_submit_barrier(ipcg_server* server, int64_t scene, const double* vertices,
                                int psd_method, int64_t* ticket);

@@ -408,6 +408,26 @@ int mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE
 }
 } // namespace
 
+namespace ipcg {
+// The barrier calls' option bits: physical scaling, the precision modes and
+// the barrier function.
+void barrier_options(int bits, BarrierArgs& a)
+{
+    const int kind = (bits >> 4) & 15;
+    require(bits >= 0
+            && (bits & ~(IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT | IPCG_BARRIER_FP32_LOCAL
+                           | IPCG_BARRIER_DF64_PSD | IPCG_BARRIER_FUNCTION(15)))
+                == 0
+            && kind <= IPCG_BARRIER_TWO_STAGE,
+        "unknown barrier option bits");
+    a.physical = (bits & IPCG_BARRIER_PHYSICAL) ? 1 : 0;
+    a.mixed = (bits & IPCG_BARRIER_FP32_PT) ? 1 : 0;
+    a.fp32_local = (bits & IPCG_BARRIER_FP32_LOCAL) ? 1 : 0;
+    a.df64_psd = (bits & IPCG_BARRIER_DF64_PSD) ? 1 : 0;
+    a.kind = kind;
+}
+} // namespace ipcg
+
 extern "C" {
 
 int ipcg_mesh_create(const double* rest, int64_t nV, const int32_t* edges, int64_t nE, const int32_t* faces,
@@ -642,23 +662,6 @@ int ipcg_collisions_set(ipcg_collisions* c, double dmin, int64_t nvv, const int3
     });
 }
 
-// The barrier calls' option bits: physical scaling, FP32 point-triangle
-// contacts and the barrier function.
-static void barrier_options(int bits, BarrierArgs& a)
-{
-    const int kind = (bits >> 4) & 15;
-    require(bits >= 0
-            && (bits & ~(IPCG_BARRIER_PHYSICAL | IPCG_BARRIER_FP32_PT | IPCG_BARRIER_FP32_LOCAL
-                           | IPCG_BARRIER_DF64_PSD | IPCG_BARRIER_FUNCTION(15)))
-                == 0
-            && kind <= IPCG_BARRIER_TWO_STAGE,
-        "unknown barrier option bits");
-    a.physical = (bits & IPCG_BARRIER_PHYSICAL) ? 1 : 0;
-    a.mixed = (bits & IPCG_BARRIER_FP32_PT) ? 1 : 0;
-    a.fp32_local = (bits & IPCG_BARRIER_FP32_LOCAL) ? 1 : 0;
-    a.df64_psd = (bits & IPCG_BARRIER_DF64_PSD) ? 1 : 0;
-    a.kind = kind;
-}
 
 // dhat / stiffness: one value (scene_params == 0) or one per scene (host arrays).
 static int barrier_call(const ipcg_collisions* c, const ipcg_mesh* mesh, const double* V, const double* dhat,

@@ -341,6 +341,9 @@ struct BarrierArgs {
     int fp32_local = 0;                  // FP32 local Hessians but near-parallel EE
     int df64_psd = 0;                    // PSD eigenpairs in df64 (cached-pattern pass)
 };
+// The barrier option bits of the C ABI (physical scaling, precision modes,
+// barrier function) into a; throws IPCG_ERR_INVALID on unknown bits.
+void barrier_options(int bits, BarrierArgs& a);
 struct FrictionView;
 void barrier_evaluate(const ipcg_collisions* c, ipcg_mesh* m, const double* V, const BarrierArgs& a,
     double* energy_host, double* grad_dev_or_null, ipcg_csr* hess_or_null, const FrictionView* friction = nullptr);

@@ -113,6 +113,7 @@ struct Scene {
     ipcg_mesh* mesh;
     ipcg_collisions* col;
     double dhat, dmin, kappa;
+    int options = 0;       // barrier option bits of its barrier requests
     bool busy = false;
     int64_t need = 0;      // expected peak working memory of one request
     int64_t last_used = 0; // admission order of its last request (LRU)
@@ -199,6 +200,7 @@ struct ipcg_server {
             const double* dV = stage_positions(m, r.V.data(), m->V0);
             build_collision_set(sc.col, m, dV, &sc.dhat, &sc.dmin);
             BarrierArgs a { sc.dhat, sc.kappa, sc.col->dmin, 0, r.psd };
+            barrier_options(sc.options, a);
             sc.grad.reserve(3 * m->nV + 1);
             r.hess = new ipcg_csr();
             // the same cached-pattern pass as a direct call, so results are identical
@@ -355,6 +357,18 @@ int ipcg_server_add_scene(ipcg_server* sv, ipcg_mesh* mesh, ipcg_collisions* col
             check(x->mesh != mesh && x->col != col, "mesh or collision set already registered");
         *scene = (int64_t)sv->scenes.size();
         sv->scenes.push_back(s);
+    });
+}
+
+int ipcg_server_set_scene_options(ipcg_server* sv, int64_t scene, int barrier_options_bits)
+{
+    return server_call([&] {
+        check(sv != nullptr, "NULL argument");
+        BarrierArgs probe { 1.0, 1.0, 0.0, 0, IPCG_PSD_NONE };
+        barrier_options(barrier_options_bits, probe); // validates the bits
+        std::lock_guard<std::mutex> lk(sv->mu);
+        check(scene >= 0 && scene < (int64_t)sv->scenes.size(), "unknown scene");
+        sv->scenes[scene]->options = barrier_options_bits;
     });
 }
 

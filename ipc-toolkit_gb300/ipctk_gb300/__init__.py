@@ -125,6 +125,7 @@ def _load():
         "ipcg_server_destroy": (i32, [P]),
         "ipcg_server_add_scene": (i32, [P, P, P, d, d, d, P]),
         "ipcg_server_submit_barrier": (i32, [P, i64, P, i32, P]),
+        "ipcg_server_set_scene_options": (i32, [P, i64, i32]),
         "ipcg_server_submit_stepsize": (i32, [P, i64, P, P, d, P]),
         "ipcg_server_wait": (i32, [P, i64, P, P, PP]),
         "ipcg_server_stats": (i32, [P, P]),
@@ -1079,6 +1080,13 @@ class Server:
                                              float(stiffness), C.byref(sid)))
         self._scenes.append((mesh, collisions))  # keep them alive
         return sid.value
+
+    def set_scene_options(self, scene: int, use_physical_barrier: bool = False, mixed_precision=False):
+        """ipcg_server_set_scene_options: the physical scaling and mixed
+        precision mode (as for BarrierPotential) of a scene's barrier
+        requests."""
+        bits = int(bool(use_physical_barrier)) | _precision_bits(mixed_precision)
+        _check(_load().ipcg_server_set_scene_options(self._h, int(scene), bits))
 
     def submit_barrier(self, scene: int, vertices, project_hessian_to_psd=PSDProjectionMethod.CLAMP) -> int:
         V = np.ascontiguousarray(vertices, np.float64)

@@ -22,18 +22,19 @@ def _scenes():
             scenes.layered_cloth(layers=3, side=16, seed=44)]
 
 
-def _direct(ipctk, sc, V, V1):
+def _direct(ipctk, sc, V, V1, mode=False):
     mesh = ipctk.CollisionMesh(sc["V"], sc["E"], sc["F"])
     col = ipctk.NormalCollisions()
     col.build(mesh, V, sc["dhat"])
-    B = ipctk.BarrierPotential(sc["dhat"], sc["kappa"])
+    B = ipctk.BarrierPotential(sc["dhat"], sc["kappa"], mixed_precision=mode)
     e, g, H = B.energy_gradient_hessian(col, mesh, V, ipctk.PSDProjectionMethod.CLAMP)
     step = ipctk.compute_collision_free_stepsize(mesh, V, V1)
     return e, g, H, step
 
 
-@pytest.mark.parametrize("budget", [120e9, 2e6])
-def test_served_results_equal_direct_calls(ipctk, budget):
+# the mixed mode too: a scene's barrier options (ipcg_server_set_scene_options)
+@pytest.mark.parametrize("budget,mode", [(120e9, False), (2e6, False), (120e9, "local")])
+def test_served_results_equal_direct_calls(ipctk, budget, mode):
     scs = _scenes()
     rng = np.random.default_rng(5)
     # two Newton-like iterations per scene: perturbed positions, then a step
@@ -50,6 +51,8 @@ def test_served_results_equal_direct_calls(ipctk, budget):
         mesh = ipctk.CollisionMesh(sc["V"], sc["E"], sc["F"])
         col = ipctk.NormalCollisions()
         ids.append(server.add_scene(mesh, col, sc["dhat"], 0.0, sc["kappa"]))
+        if mode:
+            server.set_scene_options(ids[-1], mixed_precision=mode)
     tickets = []
     for it in range(2):  # interleave the scenes' requests
         for k, sc in enumerate(scs):
@@ -67,7 +70,7 @@ def test_served_results_equal_direct_calls(ipctk, budget):
     for k, sc in enumerate(scs):
         for it in range(2):
             V, V1 = plans[k][it]
-            e, g, H, step = _direct(ipctk, sc, V, V1)
+            e, g, H, step = _direct(ipctk, sc, V, V1, mode)
             rb, rs = results[(k, it, "barrier")], results[(k, it, "step")]
             assert rb["energy"] == e, (k, it)
             assert np.linalg.norm(rb["gradient"] - g) <= 1e-12 * max(np.linalg.norm(g), 1e-300)
@@ -85,4 +88,6 @@ def test_server_rejects_bad_requests(ipctk):
     server = ipctk.Server(workers=1, hbm_budget_bytes=1e9)
     with pytest.raises(ValueError):
         server.submit_barrier(0, np.zeros((3, 3)))
+    with pytest.raises(ValueError):
+        server.set_scene_options(0, mixed_precision="local")
     server.close()
