@@ -59,7 +59,42 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-legs", action="store_true",
                     help="skip the legs beside the headline (served, layered cloth, friction, sphere pack)")
+    ap.add_argument("--profile-case", choices=["egh", "ccd"],
+                    help="for ncu captures: a 24-scene batch of the headline's distribution (sides 48-96, seed 5), "
+                         "one energy/gradient/Hessian call per mode of --modes (egh) or two batched step sizes (ccd); "
+                         "prints one line, times nothing")
+    ap.add_argument("--modes", default="local,local_df64", help="precision modes of --profile-case egh")
     return ap.parse_args()
+
+
+def run_profile_case(args):
+    import torch
+    import ipctk_gb300 as ipctk
+    from ipctk_gb300 import scenes
+    scs = scenes.batch(n_scenes=24, side_lo=48, side_hi=96, seed=5)
+    batch = ipctk.SceneBatch([(s["V"], s["E"], s["F"]) for s in scs])
+    Vd = torch.from_numpy(batch.pack([s["V"] for s in scs])).cuda()
+    dh = np.array([s["dhat"] for s in scs])
+    kap = np.array([s["kappa"] for s in scs])
+    out = {"case": args.profile_case, "scenes": len(scs)}
+    if args.profile_case == "egh":
+        col = ipctk.NormalCollisions()
+        col.build(batch, Vd, dh)
+        out["contacts"] = len(col)
+        for mode in args.modes.split(","):
+            BB = ipctk.BatchBarrierPotential(dh, kap, mixed_precision=mode)
+            e, g, H = BB.evaluate(col, batch, Vd, energy=True, gradient=True, hessian=True,
+                                  project_hessian_to_psd=ipctk.PSDProjectionMethod.CLAMP, device=True)
+            torch.cuda.synchronize()
+            H.free()
+            out[mode] = float(np.sum(e))
+    else:
+        V1d = torch.from_numpy(batch.pack([s["V1"] for s in scs])).cuda()
+        for _ in range(2):
+            steps = ipctk.compute_collision_free_stepsize_batch(batch, Vd, V1d)
+            torch.cuda.synchronize()
+        out["steps"] = [float(x) for x in steps[:4]]
+    print(json.dumps(out), flush=True)
 
 
 BATCH_DESC = ("256 uneven two-sheet scenes (5,911,266 verts; side log-uniform [16, 256], dhat log-uniform "
@@ -818,6 +853,9 @@ def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank)
         return
