@@ -658,9 +658,12 @@ template <> struct PsdReal<dd> {
 
 constexpr int MAXR = 9;
 constexpr int MAXROT = 128; // recorded rotations; beyond, Q is accumulated
+// The projection keeps the smaller of the negative and the non-negative
+// eigenpair sets: at most MAXR / 2 pairs.
+constexpr int MAXPAIRS = MAXR / 2;
 
 template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full symmetric*/, T* d, T* Q, T* rc, T* rs,
-    int8_t* rk, int& nrot, T* htau)
+    int8_t* rk, int& nrot, T* htau, unsigned wm)
 {
     // Householder tridiagonalisation; reflector k is I - htau[k] v v^T with
     // v[k+1..n) kept in A[k+1..n)[k], the column it annihilates (the updates
@@ -730,32 +733,61 @@ template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full sy
     T tnorm = T(0);
     for (int i = 0; i < n; ++i) tnorm = dmax(tnorm, fabs(d[i]) + fabs(e[i]));
     const T floor_ = PsdReal<T>::eps_norm() * tnorm;
+    // The lanes of warp mask wm (0: this lane alone) iterate in step: the
+    // loop runs while any of them still has an unreduced block and a lane
+    // that has finished idles through the rest.  Left to themselves the
+    // lanes leave the loop at different iterations and stay apart for the
+    // rest of the projection, each group issuing it on its own.
     int end = n - 1, iter = 0;
-    while (end > 0) {
-        for (int i = 0; i < end; ++i)
-            if (PsdReal<T>::negligible(e[i], d[i], d[i + 1], eps, floor_)) e[i] = 0;
-        while (end > 0 && PsdReal<T>::is_zero(e[end - 1])) --end;
-        if (end <= 0) break;
-        if (++iter > 40 * n) return false;
-        int start = end - 1;
-        while (start > 0 && !PsdReal<T>::is_zero(e[start - 1])) --start;
-        if (record && nrot + (end - start) > MAXROT) {
-            // too many rotations to record: form G from those so far and
-            // accumulate the rest into it
-            for (int i = 0; i < n; ++i)
-                for (int j = 0; j < n; ++j) Q[i * MAXR + j] = (i == j) ? 1.0 : 0.0;
-            for (int r = 0; r < nrot; ++r) {
-                const int k = rk[r];
-                const T c = rc[r], s = rs[r];
-                for (int q = 0; q < n; ++q) {
-                    const T qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
-                    Q[q * MAXR + k] = c * qa - s * qb;
-                    Q[q * MAXR + k + 1] = s * qa + c * qb;
-                }
+    bool ok = true;
+    for (;;) {
+        if (wm ? !__any_sync(wm, end > 0) : end <= 0) break;
+        // deflate at the bottom, then walk up to the top of the unreduced
+        // block; an entry is set to zero where the walks stop at it (the
+        // entries above the block are tested when their block's turn comes,
+        // with the same neighbours: the sweeps below do not touch them)
+        int start = 0;
+        bool sweep = false;
+        if (end > 0) {
+            while (end > 0
+                && (PsdReal<T>::is_zero(e[end - 1])
+                    || PsdReal<T>::negligible(e[end - 1], d[end - 1], d[end], eps, floor_))) {
+                e[end - 1] = 0;
+                --end;
             }
-            record = false;
-            nrot = -1;
+            if (end > 0 && ++iter > 40 * n) {
+                ok = false;
+                end = 0;
+            }
+            if (end > 0) {
+                start = end - 1;
+                while (start > 0 && !PsdReal<T>::is_zero(e[start - 1])
+                    && !PsdReal<T>::negligible(e[start - 1], d[start - 1], d[start], eps, floor_))
+                    --start;
+                if (start > 0) e[start - 1] = 0;
+                if (record && nrot + (end - start) > MAXROT) {
+                    // too many rotations to record: form G from those so far
+                    // and accumulate the rest into it
+                    for (int i = 0; i < n; ++i)
+                        for (int j = 0; j < n; ++j) Q[i * MAXR + j] = (i == j) ? 1.0 : 0.0;
+                    for (int r = 0; r < nrot; ++r) {
+                        const int k = rk[r];
+                        const T c = rc[r], s = rs[r];
+                        for (int q = 0; q < n; ++q) {
+                            const T qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
+                            Q[q * MAXR + k] = c * qa - s * qb;
+                            Q[q * MAXR + k + 1] = s * qa + c * qb;
+                        }
+                    }
+                    record = false;
+                    nrot = -1;
+                }
+                sweep = true;
+            }
         }
+        // the lanes meet again before the sweeps (each of its own length)
+        if (wm) __syncwarp(wm);
+        if (!sweep) continue;
         const T mu = PsdReal<T>::shift(d[end - 1], d[end], e[end - 1]);
         T x = d[start] - mu, z = e[start];
         for (int k = start; k < end; ++k) {
@@ -804,65 +836,88 @@ template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full sy
             }
         }
     }
-    return true;
+    return ok;
 }
 
 // Eigenvectors idx[0..cnt) of M, rows of Y (stride MAXR): Q_h G e_i.  G e_i
 // comes from the recorded rotations, applied last first to all cnt vectors in
 // one pass (each rotation loaded once), or, if they were not recorded
 // (nrot < 0), from column i of Q; then the Householder reflectors kept in A's
-// lower columns, H_{n-3} first.
+// lower columns, H_{n-3} first.  wm: the lanes of this warp that call it
+// together (cnt may be 0), which meet again after the rotations and after
+// every reflector, or 0.
 template <class T> __device__ void eigvecs_impl(int n, const int* idx, int cnt, const T* Q, const T* rc, const T* rs,
-    const int8_t* rk, int nrot, const T* A, const T* htau, T* Y)
+    const int8_t* rk, int nrot, const T* A, const T* htau, T* Y, unsigned wm)
 {
     for (int t = 0; t < cnt; ++t)
         for (int q = 0; q < n; ++q)
             Y[t * MAXR + q] = nrot >= 0 ? (q == idx[t] ? 1.0 : 0.0) : Q[q * MAXR + idx[t]];
-    for (int r = nrot - 1; r >= 0; --r) {
+    // FP64: the pair loops run MAXPAIRS times with a predicate (unrolled);
+    // df64: as counted loops (its operations are long: unrolled copies
+    // would not fit the instruction cache)
+    for (int r = (cnt > 0 ? nrot : 0) - 1; r >= 0; --r) {
         const int k = rk[r];
         const T c = rc[r], s = rs[r];
-        for (int t = 0; t < cnt; ++t) {
+        const auto rotate = [&](int t) {
             T* y = Y + t * MAXR;
             const T ya = y[k], yb = y[k + 1];
             y[k] = c * ya + s * yb;
             y[k + 1] = c * yb - s * ya;
+        };
+        if constexpr (PsdReal<T>::rescale) {
+            for (int t = 0; t < cnt; ++t) rotate(t);
+        } else {
+#pragma unroll
+            for (int t = 0; t < MAXPAIRS; ++t)
+                if (t < cnt) rotate(t);
         }
     }
+    if (wm) __syncwarp(wm);
     for (int k = n - 3; k >= 0; --k) {
-        if (htau[k] == 0) continue;
-        for (int t = 0; t < cnt; ++t) {
+        const auto reflect = [&](int t) {
             T* y = Y + t * MAXR;
             T s = 0;
             for (int q = k + 1; q < n; ++q) s += A[q * MAXR + k] * y[q];
             s *= htau[k];
             for (int q = k + 1; q < n; ++q) y[q] -= s * A[q * MAXR + k];
+        };
+        if (htau[k] != 0) {
+            if constexpr (PsdReal<T>::rescale) {
+                for (int t = 0; t < cnt; ++t) reflect(t);
+            } else {
+#pragma unroll
+                for (int t = 0; t < MAXPAIRS; ++t)
+                    if (t < cnt) reflect(t);
+            }
         }
+        if (wm) __syncwarp(wm);
     }
 }
 
 // The df64 solver is long (each df64 operation is tens of FP32
 // instructions): one out-of-line copy serves every stencil size, which keeps
 // the kernel inside the instruction cache; the FP64 solver is inlined.
-__device__ __noinline__ bool sym_eig_dd(int n, dd* A, dd* d, dd* Q, dd* rc, dd* rs, int8_t* rk, int& nrot, dd* htau)
+__device__ __noinline__ bool sym_eig_dd(int n, dd* A, dd* d, dd* Q, dd* rc, dd* rs, int8_t* rk, int& nrot, dd* htau,
+    unsigned wm)
 {
-    return sym_eig_impl<dd>(n, A, d, Q, rc, rs, rk, nrot, htau);
+    return sym_eig_impl<dd>(n, A, d, Q, rc, rs, rk, nrot, htau, wm);
 }
 __device__ __noinline__ void eigvecs_dd(int n, const int* idx, int cnt, const dd* Q, const dd* rc, const dd* rs,
-    const int8_t* rk, int nrot, const dd* A, const dd* htau, dd* Y)
+    const int8_t* rk, int nrot, const dd* A, const dd* htau, dd* Y, unsigned wm)
 {
-    eigvecs_impl<dd>(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y);
+    eigvecs_impl<dd>(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y, wm);
 }
 template <class T> __device__ __forceinline__ bool sym_eig(int n, T* A, T* d, T* Q, T* rc, T* rs, int8_t* rk,
-    int& nrot, T* htau)
+    int& nrot, T* htau, unsigned wm)
 {
-    if constexpr (PsdReal<T>::rescale) return sym_eig_dd(n, A, d, Q, rc, rs, rk, nrot, htau);
-    else return sym_eig_impl<T>(n, A, d, Q, rc, rs, rk, nrot, htau);
+    if constexpr (PsdReal<T>::rescale) return sym_eig_dd(n, A, d, Q, rc, rs, rk, nrot, htau, wm);
+    else return sym_eig_impl<T>(n, A, d, Q, rc, rs, rk, nrot, htau, wm);
 }
 template <class T> __device__ __forceinline__ void eigvecs(int n, const int* idx, int cnt, const T* Q, const T* rc,
-    const T* rs, const int8_t* rk, int nrot, const T* A, const T* htau, T* Y)
+    const T* rs, const int8_t* rk, int nrot, const T* A, const T* htau, T* Y, unsigned wm)
 {
-    if constexpr (PsdReal<T>::rescale) eigvecs_dd(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y);
-    else eigvecs_impl<T>(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y);
+    if constexpr (PsdReal<T>::rescale) eigvecs_dd(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y, wm);
+    else eigvecs_impl<T>(n, idx, cnt, Q, rc, rs, rk, nrot, A, htau, Y, wm);
 }
 
 // Orthonormal contrasts (rows orthogonal to (1,..,1)) for NS = 2, 3, 4
@@ -1048,15 +1103,25 @@ template <int NS, class T, class Acc> __device__ void to_contrasts(const Acc& hs
     }
 }
 
-// Negative eigenpairs of one local Hessian for its PSD projection
-// (eigen_ext.tpp:64-108): M = C H C^T from the accessor, its eigenpairs in
-// arithmetic T (FP64, or df64 on the matrix scaled by a power of two), and
-// for each negative eigenvalue lam the stencil vector w = C^T q (rows of 12 in
-// wv) and sl = f lam (f = 1 clamps, 2 takes the absolute value), both FP64,
-// so that H+ = H - sum_t sl[t] w_t w_t^T.  Returns false if the eigensolver
-// did not converge.
+// The eigenpairs of one local Hessian that its PSD projection
+// (eigen_ext.tpp:64-108) needs.  M = C H C^T from the accessor; H is
+// translation invariant, so H = C^T M C and with w = C^T q for each unit
+// eigenvector q of M, H = sum lam w w^T over all eigenpairs.  The eigenpairs
+// are computed in arithmetic T (FP64, or df64 on the matrix scaled by a power
+// of two) and the smaller of two sets is kept: the negative eigenvalues, with
+//   H+ = H - sum f lam w w^T,
+// or the non-negative ones, with
+//   H+ = (1 - f) H + sum f lam w w^T
+// (f = 1 clamps, 2 takes the absolute value).  Out, in FP64: np pairs, the
+// stencil vectors w (rows of 12 in wv), sl and sigma, such that
+//   H+ = sigma H - sum_t sl[t] w_t w_t^T.
+// An already PSD matrix gives np = 0 and sigma = 1: H as it is.  Returns
+// false (np = 0, sigma = 1) if the eigensolver did not converge.  wm: the
+// lanes of this warp that call it together (each of them makes the same
+// __syncwarp calls), or 0 for a lane on its own.
 template <class T, class Acc>
-__device__ bool psd_negative(int n, const Acc& hs, int method, double* wv /*MAXR*12*/, double* sl, int& nneg)
+__device__ bool psd_pairs(int n, const Acc& hs, int method, double* wv /*MAXPAIRS*12*/, double* sl, int& np,
+    double& sigma, unsigned wm = 0)
 {
     const int N = 3 * n, m = 3 * (n - 1);
     T M[MAXR * MAXR], Q[MAXR * MAXR], lam[MAXR];
@@ -1073,52 +1138,65 @@ __device__ bool psd_negative(int n, const Acc& hs, int method, double* wv /*MAXR
     T rc[MAXROT], rs[MAXROT], htau[MAXR];
     int8_t rk[MAXROT];
     int nrot;
-    nneg = 0;
-    if (!sym_eig(m, M, lam, Q, rc, rs, rk, nrot, htau)) return false;
+    const bool ok = sym_eig(m, M, lam, Q, rc, rs, rk, nrot, htau, wm);
+    if (wm) __syncwarp(wm);
     const double f = (method == IPCG_PSD_CLAMP) ? 1.0 : 2.0;
+    int nneg = 0;
+    if (ok)
+        for (int k = 0; k < m; ++k) nneg += lam[k] < T(0) ? 1 : 0;
+    const bool flip = 2 * nneg > m;
     int idx[MAXR];
-    for (int k = 0; k < m; ++k)
-        if (lam[k] < T(0)) idx[nneg++] = k;
-    if (nneg == 0) return true; // already PSD: returned as is
-    // the eigenvectors (rows of 9) and then the w = C^T q (rows of 12) share
+    np = 0;
+    if (ok && nneg > 0)
+        for (int k = 0; k < m; ++k)
+            if ((lam[k] < T(0)) != flip) idx[np++] = k;
+    sigma = flip ? 1.0 - f : 1.0;
+    const double fs = flip ? -f : f;
+    // The eigenvectors (rows of 9) and then the w = C^T q (rows of 12) share
     // wv: row t of w is written after rows t.. of q are read (t descending),
-    // and rows below t lie below 12 t
+    // and rows below t lie below 12 t.
     if constexpr (PsdReal<T>::rescale) {
-        T Y[MAXR * MAXR];
-        eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, Y);
-        for (int i = 0; i < nneg * MAXR; ++i) wv[i] = dd_to_double(Y[i]);
+        T Y[MAXPAIRS * MAXR];
+        eigvecs(m, idx, np, Q, rc, rs, rk, nrot, M, htau, Y, wm);
+        for (int i = 0; i < np * MAXR; ++i) wv[i] = dd_to_double(Y[i]);
     } else {
-        eigvecs(m, idx, nneg, Q, rc, rs, rk, nrot, M, htau, wv);
+        eigvecs(m, idx, np, Q, rc, rs, rk, nrot, M, htau, wv, wm);
     }
-    for (int t = nneg - 1; t >= 0; --t) {
+    if (wm) __syncwarp(wm);
+    for (int t = np - 1; t >= 0; --t) {
         double q[MAXR];
         for (int j = 0; j < m; ++j) q[j] = wv[t * MAXR + j];
         double* w = wv + 12 * t;
         if (n == 4) from_contrasts<4, double>(q, w);
         else if (n == 3) from_contrasts<3, double>(q, w);
         else from_contrasts<2, double>(q, w);
-        sl[t] = f * PsdReal<T>::out(lam[idx[t]], sc);
+        sl[t] = fs * PsdReal<T>::out(lam[idx[t]], sc);
     }
-    return true;
+    return ok;
 }
 
-// H+ entry by entry from psd_negative's pairs: out(r, c, v) for every r <= c
-// (H+ is symmetric; the caller mirrors).  With nneg = 0 the entries are H's
-// own bits.
+// H+ entry by entry from psd_pairs' output: out(r, c, v) for every r <= c
+// (H+ is symmetric; the caller mirrors).  With np = 0 and sigma = 1 the
+// entries are H's own bits.  wm: the lanes of this warp that call it together
+// with the same n (they meet after every row), or 0.
 template <class Acc, class Out>
-__device__ __forceinline__ void psd_apply(int n, const Acc& hs, const double* wv, const double* sl, int nneg,
-    const Out& out)
+__device__ __forceinline__ void psd_apply(int n, const Acc& hs, const double* wv, const double* sl, int np,
+    double sigma, const Out& out, unsigned wm = 0)
 {
     const int N = 3 * n;
 #pragma unroll 1
     for (int r = 0; r < N; ++r) {
-        double swr[MAXR];
-        for (int t = 0; t < nneg; ++t) swr[t] = sl[t] * wv[12 * t + r];
+        double swr[MAXPAIRS];
+#pragma unroll
+        for (int t = 0; t < MAXPAIRS; ++t) swr[t] = t < np ? sl[t] * wv[12 * t + r] : 0.0;
         for (int c = r; c < N; ++c) {
-            double v = hs(r * N + c);
-            for (int t = 0; t < nneg; ++t) v = fma(-swr[t], wv[12 * t + c], v);
+            double v = sigma * hs(r * N + c);
+#pragma unroll
+            for (int t = 0; t < MAXPAIRS; ++t)
+                if (t < np) v = fma(-swr[t], wv[12 * t + c], v);
             out(r, c, v);
         }
+        if (wm) __syncwarp(wm);
     }
 }
 
@@ -1126,12 +1204,12 @@ __device__ __forceinline__ void psd_apply(int n, const Acc& hs, const double* wv
 // eigensolver did not converge.
 template <class T, class Acc> __device__ bool project_psd(int n, const Acc& hs, int method)
 {
-    double wv[MAXR * 12], sl[MAXR];
-    int nneg;
-    if (!psd_negative<T>(n, hs, method, wv, sl, nneg)) return false;
-    if (nneg == 0) return true;
+    double wv[MAXPAIRS * 12], sl[MAXPAIRS], sigma;
+    int np;
+    if (!psd_pairs<T>(n, hs, method, wv, sl, np, sigma)) return false;
+    if (np == 0 && sigma == 1.0) return true;
     const int N = 3 * n;
-    psd_apply(n, hs, wv, sl, nneg, [&](int r, int c, double v) {
+    psd_apply(n, hs, wv, sl, np, sigma, [&](int r, int c, double v) {
         hs(r * N + c) = v;
         if (c != r) hs(c * N + r) = v;
     });

@@ -519,20 +519,32 @@ __device__ __forceinline__ void psd_one(const EghDev& d, const unsigned* __restr
 {
     const Slab hs { d.lh + off, stride };
     const SlabAcc acc { hs, r };
-    double wv[MAXR * 12], sl[MAXR];
-    int nneg = 0;
+    double wv[MAXPAIRS * 12], sl[MAXPAIRS], sigma = 1.0;
+    int np = 0;
     const int method = psd & 15;
     const bool defer = PsdReal<T>::rescale && (psd & PSD_DEFER); // testing: every projection to the fix-up
-    if (method != IPCG_PSD_NONE && d.pflag[i] && (defer || !psd_negative<T>(NS, acc, method, wv, sl, nneg))) {
+    const bool project = method != IPCG_PSD_NONE && d.pflag[i];
+    // The lanes that arrive here together solve in step (wm) and all of them
+    // meet again before the scatter (all): each makes the same __syncwarp
+    // calls, and none returns before the last of them.
+    const unsigned all = __activemask();
+    const unsigned wm = __ballot_sync(all, project && !defer);
+    bool unsolved = project && defer;
+    if (project && !defer && !psd_pairs<T>(NS, acc, method, wv, sl, np, sigma, wm)) unsolved = true;
+    // the lanes that go on to the scatter (df64 hands unsolved contacts to the
+    // fix-up pass instead)
+    const unsigned keep = all & ~__ballot_sync(all, unsolved && PsdReal<T>::rescale);
+    if (unsolved) {
         if constexpr (PsdReal<T>::rescale) {
             d.fixlist[atomicAdd(nfix, 1ull)] = i; // at most one entry per contact
             return;
         } else {
             record_failure(fail, acc, 3 * NS, i, chunk);
-            nneg = 0;
+            np = 0;
+            sigma = 1.0;
         }
     }
-    psd_apply(NS, acc, wv, sl, nneg, BlockScatter<NS>(d.slab, pm));
+    psd_apply(NS, acc, wv, sl, np, sigma, BlockScatter<NS>(d.slab, pm), keep);
 }
 
 // Stage 2: PSD projection and scatter of every local Hessian to the
