@@ -59,16 +59,18 @@ __device__ __forceinline__ float first_time(const float A[4], const float B[4], 
     return Tc;
 }
 
-// min over t in [0, 1] of |a + t b| (3-vectors), in FP32 (its callers
-// compare it with a margin)
-__device__ __forceinline__ float min_norm_on_segment(const double a[3], const double b[3])
+// min over t in [0, 1] of |a + t b| (3-vectors)
+__device__ __forceinline__ double min_norm_on_segment(const double a[3], const double b[3])
 {
-    const float a0 = (float)a[0], a1 = (float)a[1], a2 = (float)a[2];
-    const float b0 = (float)b[0], b1 = (float)b[1], b2 = (float)b[2];
-    const float bb = b0 * b0 + b1 * b1 + b2 * b2, ab = a0 * b0 + a1 * b1 + a2 * b2;
-    const float t = bb > 0.f ? fminf(1.f, fmaxf(0.f, -ab / bb)) : 0.f;
-    const float x = a0 + t * b0, y = a1 + t * b1, z = a2 + t * b2;
-    return sqrtf(x * x + y * y + z * z);
+    const double bb = b[0] * b[0] + b[1] * b[1] + b[2] * b[2];
+    const double ab = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    const double t = bb > 0 ? fmin(1.0, fmax(0.0, -ab / bb)) : 0.0;
+    double n = 0;
+    for (int c = 0; c < 3; ++c) {
+        const double x = a[c] + t * b[c];
+        n += x * x;
+    }
+    return sqrt(n);
 }
 
 struct F3b {
@@ -154,22 +156,7 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
     const double ms = fmin((1.0 - P.rescale) * (d0 - min_distance), 1e-4) + min_distance;
     const double delta = fmin(0.5 * d0, P.tolerance);
     double err[3];
-    // the inclusion search's numerical error filter (numerical_error), with
-    // the maxima of |coordinates| taken on the bit patterns (the same values)
-    {
-        const double filt = q.vf ? (ms > 0 ? 7.549516567451064e-15 : 6.661338147750939e-15)
-                                 : (ms > 0 ? 7.105427357601002e-15 : 6.217248937900877e-15);
-        for (int c = 0; c < 3; ++c) {
-            unsigned long long mb = 0;
-            for (int k = 0; k < 4; ++k) {
-                const unsigned long long a = (unsigned long long)__double_as_longlong(comp(q.s[k], c)) << 1 >> 1;
-                const unsigned long long b = (unsigned long long)__double_as_longlong(comp(q.e[k], c)) << 1 >> 1;
-                mb = max(mb, max(a, b));
-            }
-            const double dl = fmin(__longlong_as_double((long long)mb), 1.0);
-            err[c] = filt * (dl * dl * dl);
-        }
-    }
+    numerical_error(q, ms > 0, err);
     // per coordinate, F = A00 + u Au + v Av + t (B00 + u Bu + v Bv) (FP64)
     double a00[3], au[3], av[3], b00[3], bu[3], bv[3];
     for (int c = 0; c < 3; ++c) {
@@ -191,8 +178,7 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
             bv[c] = -(e3 - e2);
         }
     }
-    double T = 0.0, rmax = 0.0;
-    unsigned long long bmax_bits = 0;
+    double T = 0.0, bmax = 0.0, rmax = 0.0;
     float R[3], scale[3];
     for (int c = 0; c < 3; ++c) {
         // corner lines at (u, v) in {0, 1}^2, the search in FP32 with a
@@ -202,7 +188,7 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
         for (int k = 0; k < 4; ++k) {
             const double u = (k & 1) ? 1.0 : 0.0, v = (k & 2) ? 1.0 : 0.0;
             const double a = a00[c] + u * au[c] + v * av[c], b = b00[c] + u * bu[c] + v * bv[c];
-            bmax_bits = max(bmax_bits, (unsigned long long)__double_as_longlong(b) << 1 >> 1);
+            bmax = fmax(bmax, fabs(b));
             A[k] = (float)a;
             B[k] = (float)b;
         }
@@ -222,14 +208,8 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
     // cell and the bound is the least of the cells' bounds.
     constexpr int NCELL = 4;
     const double lu = min_norm_on_segment(au, bu), lv = min_norm_on_segment(av, bv);
-    const double need = 1.7320508075688772 * (2.0 * rmax + delta) * (0.5 * NCELL) * (1.0 + 1e-4);
-    // the FP32 lengths' rounding: 2^-20 of the vectors' size
-    double su = 0, sv = 0;
-    for (int c = 0; c < 3; ++c) {
-        su += fabs(au[c]) + fabs(bu[c]);
-        sv += fabs(av[c]) + fabs(bv[c]);
-    }
-    if (lu > need + su * 0x1p-20 && lv > need + sv * 0x1p-20) {
+    const double need = 1.7320508075688772 * (2.0 * rmax + delta) * (0.5 * NCELL) * (1.0 + 1e-6);
+    if (lu > need && lv > need) {
         const float w = 1.f / NCELL;
         float Tq_min = FINF;
         for (int cell = 0; cell < NCELL * NCELL; ++cell) {
@@ -252,7 +232,6 @@ __device__ double toi_lower_bound(const Query& q, double min_distance, const CCD
     }
     // the time tolerance of the inclusion search: delta / (3 max |F(1) - F(0)|)
     // over the corners, F(1) - F(0) being the corner lines' slopes
-    const double bmax = __longlong_as_double((long long)bmax_bits);
     const double tol0 = bmax == 0.0 ? delta : delta / (3.0 * bmax);
     return fmax(0.0, (T - 0x1p-20 - tol0 * (1.0 + 1e-6) - 0x1p-60) * (1.0 - 1e-6));
 }
