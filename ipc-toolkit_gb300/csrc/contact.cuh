@@ -1480,10 +1480,6 @@ __device__ __forceinline__ bool contact_egh_f64(const Local& c, const V3* x, con
     return true;
 }
 
-__device__ bool contact_egh(const Local& c, const V3* x, const Params& P, double& e, double* g, double* H)
-{
-    return fp32_local_contact(P, c, x) ? contact_egh_f32(c, x, P, e, g, H) : contact_egh_f64(c, x, P, e, g, H);
-}
 } // namespace
 
 } // namespace ipcg

@@ -46,7 +46,7 @@
 #include <string>
 #include <vector>
 
-#include <cub/device/device_partition.cuh>
+#include <cub/device/device_radix_sort.cuh>
 
 #include "contact.cuh"
 #include "profile.cuh"
@@ -110,10 +110,11 @@ struct EghCache {
     DBuf<int64_t> epstart; // per scene: its first energy part (ns + 1)
     int64_t nparts = 0;
     DBuf<double> energy;   // per-scene energies of the last step
-    DBuf<unsigned long long> queue;    // per chunk: local F64, local F32 / any, projection, fix-up count
-    // partition of a chunk's contacts by arithmetic path (mixed precision)
+    DBuf<unsigned long long> queue;    // per chunk: local F64, local F32, projection, fix-up count
+    // a chunk's contacts ordered by arithmetic path and kind: keys (path),
+    // sorted keys (pkey), contact indices (iota -> list), FP64 count (nsel)
     DBuf<int> iota, list, nsel;
-    DBuf<unsigned char> path, part_tmp;
+    DBuf<unsigned char> path, pkey, part_tmp;
     size_t part_bytes = 0;
     DBuf<long long> fail;  // [failed, chunk-local contact, chunk, non-finite entries]
     HBuf<long long> hfail;
@@ -362,9 +363,9 @@ __device__ __forceinline__ void load_typed(const ContactsView& cv, const int* __
 // index i): the energy to its own slot, the gradient to its vertex-grouped
 // slots, the Hessian to the element-major local slab, whether it is to be
 // projected to pflag.
-// Which arithmetic a local-stage launch runs: every contact decides (ANY),
-// or the launch takes only contacts of the FP32 or of the FP64 path.
-enum : int { PATH_ANY = 0, PATH_F32 = 1, PATH_F64 = 2 };
+// Which arithmetic a local-stage launch runs: it takes only contacts of the
+// FP32 or only contacts of the FP64 path.
+enum : int { PATH_F32 = 1, PATH_F64 = 2 };
 
 template <int CT, int PATH>
 __device__ __forceinline__ void local_one(const ContactsView& cv, const int* __restrict__ E, const int* __restrict__ F,
@@ -381,8 +382,7 @@ __device__ __forceinline__ void local_one(const ContactsView& cv, const int* __r
     double e, g[12], H[144];
     bool pr;
     if constexpr (PATH == PATH_F32) pr = contact_egh_f32(c, x, P, e, g, H);
-    else if constexpr (PATH == PATH_F64) pr = contact_egh_f64(c, x, P, e, g, H);
-    else pr = contact_egh(c, x, P, e, g, H);
+    else pr = contact_egh_f64(c, x, P, e, g, H);
     if (want & WANT_E) d.eslab[i] = e;
     if (want & WANT_G)
 #pragma unroll
@@ -421,8 +421,8 @@ __device__ __forceinline__ void tile_queue(int64_t n, unsigned long long* __rest
 }
 
 // Stage 1: per contact, energy, gradient and local Hessian (one lane each).
-// With a list, the launch takes the contacts list[0, *nsel) (FP64 path) or
-// list[*nsel, n) (FP32 path) of the chunk's partition by path.
+// The launch takes the contacts list[0, *nsel) (FP64 path) or list[*nsel, n)
+// (FP32 path) of the chunk's order by path and kind (k_path_keys).
 template <int PATH>
 __global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
     const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv, const unsigned* __restrict__ gslot,
@@ -432,14 +432,10 @@ __global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __res
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const EghDev d = *dev;
     const LhLayout L(cv);
-    int64_t first = 0, count = n;
-    if (list) {
-        const int64_t k = *nsel;
-        first = PATH == PATH_F64 ? 0 : k;
-        count = PATH == PATH_F64 ? k : n - k;
-    }
+    const int64_t k = *nsel;
+    const int64_t first = PATH == PATH_F64 ? 0 : k, count = PATH == PATH_F64 ? k : n - k;
     tile_queue(count, queue, grab, [&](int64_t t) {
-        const int64_t i = list ? (int64_t)list[first + t] : t;
+        const int64_t i = list[first + t];
         if (i < L.first[1]) local_one<CT_VV, PATH>(cv, E, F, d, sp, sv, gslot, L, i, i, want);
         else if (i < L.first[2]) local_one<CT_EV, PATH>(cv, E, F, d, sp, sv, gslot, L, i, i - L.first[1], want);
         else if (i < L.first[2] + cv.nee)
@@ -448,20 +444,31 @@ __global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __res
     });
 }
 
-// Per contact of the chunk: 1 if its local Hessian takes the FP64 path.
-__global__ void k_path_flags(ContactsView cv, const int* __restrict__ E, const int* __restrict__ F,
-    const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv, unsigned char* __restrict__ f64)
+// Stage 1's order in a mixed mode.  Per contact of the chunk a 4-bit key:
+// its kind on the FP64 path (VV, EV, each edge-edge distance type, FV) or
+// KEY_F32; nsel counts the FP64 contacts.  A radix sort on the keys puts the
+// FP64 contacts first, grouped by kind, so that the FP64 distance code's
+// branches (one inlined copy per distance type) agree across a warp's lanes.
+constexpr unsigned char KEY_F32 = 15;
+__global__ void __launch_bounds__(256) k_path_keys(ContactsView cv, const int* __restrict__ E,
+    const int* __restrict__ F, const EghDev* __restrict__ dev, const Params* __restrict__ sp, SceneView sv,
+    unsigned char* __restrict__ key, int* __restrict__ nsel)
 {
     const int64_t n = cv.nvv + cv.nev + cv.nee + cv.nfv;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double* __restrict__ V = dev->V;
-    Local c;
-    load_contact(cv, E, F, i, c);
-    const Params P = sp[sv.of(c.vid[0])];
-    V3 x[4];
-    gather(V, c, x);
-    f64[i] = fp32_local_contact(P, c, x) ? 0 : 1;
+    bool f64 = false;
+    if (i < n) {
+        Local c;
+        load_contact(cv, E, F, i, c);
+        const Params P = sp[sv.of(c.vid[0])];
+        V3 x[4];
+        gather(dev->V, c, x);
+        f64 = !fp32_local_contact(P, c, x);
+        key[i] = !f64 ? KEY_F32
+                      : (unsigned char)(c.type == CT_VV ? 0 : c.type == CT_EV ? 1 : c.type == CT_EE ? 2 + c.dtype : 11);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, f64);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(nsel, __popc(b));
 }
 
 __global__ void k_iota(int* __restrict__ a, int64_t n)
@@ -831,12 +838,13 @@ void build_pattern(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C)
     C.iota.reserve(C.max_n + 1);
     C.list.reserve(C.max_n + 1);
     C.path.reserve(C.max_n + 1);
+    C.pkey.reserve(C.max_n + 1);
     C.nsel.reserve(1);
     if (C.max_n > 0) {
         IPCG_LAUNCH("k_iota", s, k_iota<<<grid_for(C.max_n, 256), 256, 0, s>>>(C.iota.p, C.max_n));
         C.part_bytes = 0;
-        IPCG_CUDA(cub::DevicePartition::Flagged(nullptr, C.part_bytes, C.iota.p, C.path.p, C.list.p, C.nsel.p,
-            (int)C.max_n, s));
+        IPCG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, C.part_bytes, C.path.p, C.pkey.p, C.iota.p, C.list.p,
+            (int)C.max_n, 0, 4, s));
         C.part_tmp.reserve(C.part_bytes + 16);
     }
     C.fail.reserve(4);
@@ -894,26 +902,23 @@ template <class K> void egh_grid(const EghTuning& t, int64_t n, K kernel, int& b
     blocks = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * per_sm, need));
 }
 
-// Stage 1 of one chunk; q[0], q[1] are its work queues.  In a mixed mode the
-// chunk's contacts are first partitioned by arithmetic path (FP64 first), so
-// that no warp runs both paths and each path has its own register budget.
+// Stage 1 of one chunk; q[0], q[1] are its work queues.  The chunk's
+// contacts are first ordered by arithmetic path (FP64 first, grouped by kind:
+// k_path_keys), so that no warp runs both paths, each path has its own
+// register budget and the FP64 path's warps take one distance branch (in the
+// all-FP64 mode every contact is on the FP64 path and the order is by kind).
 // Returns the kernels launched.
 int launch_local(const ContactsView& cc, const ipcg_mesh* m, EghCache& C, const EChunk& ch, const Params* sp,
-    const SceneView& sv, unsigned long long* q, int want, bool split, const EghTuning& t, cudaStream_t s)
+    const SceneView& sv, unsigned long long* q, int want, const EghTuning& t, cudaStream_t s)
 {
     int blocks, threads;
     const unsigned* gs = C.gslot.p + ch.gslot_off;
-    if (!split) {
-        egh_grid(t, ch.n, k_local<PATH_ANY>, blocks, threads);
-        IPCG_LAUNCH("k_local", s, k_local<PATH_ANY><<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv,
-            gs, q, want, t.tiles_per_grab, nullptr, nullptr));
-        return 1;
-    }
-    IPCG_LAUNCH("k_path_flags", s, k_path_flags<<<grid_for(ch.n, 256), 256, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp,
-        sv, C.path.p));
+    IPCG_CUDA(cudaMemsetAsync(C.nsel.p, 0, sizeof(int), s));
+    IPCG_LAUNCH("k_path_keys", s, k_path_keys<<<grid_for(ch.n, 256), 256, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp,
+        sv, C.path.p, C.nsel.p));
     size_t bytes = C.part_bytes;
-    IPCG_LAUNCH("cub_partition", s, IPCG_CUDA(cub::DevicePartition::Flagged(C.part_tmp.p, bytes, C.iota.p, C.path.p,
-        C.list.p, C.nsel.p, (int)ch.n, s)));
+    IPCG_LAUNCH("cub_path_sort", s, IPCG_CUDA(cub::DeviceRadixSort::SortPairs(C.part_tmp.p, bytes, C.path.p, C.pkey.p,
+        C.iota.p, C.list.p, (int)ch.n, 0, 4, s)));
     egh_grid(t, ch.n, k_local<PATH_F64>, blocks, threads);
     IPCG_LAUNCH("k_local", s, k_local<PATH_F64><<<blocks, threads, 0, s>>>(cc, m->E.p, m->F.p, C.dev.p, sp, sv, gs,
         q, want, t.tiles_per_grab, C.list.p, C.nsel.p));
@@ -947,7 +952,7 @@ int launch_psd(const ContactsView& cc, EghCache& C, const EChunk& ch, int ci, un
 
 // Enqueue the launches of one step on the mesh stream (also while capturing).
 int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Params* sp, int psd, bool df64, int want,
-    bool split, const EghTuning* tune)
+    const EghTuning* tune)
 {
     cudaStream_t s = m->stream;
     const ContactsView cv = full_view(cs);
@@ -958,7 +963,7 @@ int enqueue_step(const ipcg_collisions* cs, ipcg_mesh* m, EghCache& C, const Par
         const EChunk& ch = C.chunks[ci];
         const ContactsView cc = chunk_view(cv, ch);
         if (ch.n > 0) {
-            kernels += launch_local(cc, m, C, ch, sp, sv, C.queue.p + 4 * ci, want, split, tune[0], s);
+            kernels += launch_local(cc, m, C, ch, sp, sv, C.queue.p + 4 * ci, want, tune[0], s);
             kernels += launch_psd(cc, C, ch, (int)ci, C.queue.p + 4 * ci + 2, psd, df64, tune[1], s);
         }
         if (ch.nb > 0) {
@@ -1186,7 +1191,6 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     IPCG_CUDA(cudaMemcpyAsync(C.dev.p, C.hdev.p, sizeof(EghDev), cudaMemcpyHostToDevice, s));
     IPCG_CUDA(cudaMemsetAsync(C.fail.p, 0, sizeof(long long) * 4, s));
     const bool df64 = a.df64_psd != 0;
-    const bool split = a.mixed || a.fp32_local;
     const EghTuning tune[2] = { egh_tuning(0), egh_tuning(df64 ? 2 : 1) };
     // A pattern's first step runs as plain launches: a set that is rebuilt
     // before its next Hessian (a Newton loop whose collision set changes,
@@ -1196,11 +1200,11 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
     ++C.steps;
     if (direct) {
         // (per-kernel timing also needs the launches themselves)
-        enqueue_step(cs, m, C, sp, a.psd, df64, want, split, tune);
+        enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
     } else {
         char key[200];
-        snprintf(key, sizeof(key), "%p|%d|%d%d%d|%d|%d,%d,%d|%d,%d,%d", (const void*)sp, a.psd, (int)df64,
-            g_defer_df64.load(), (int)split, want,
+        snprintf(key, sizeof(key), "%p|%d|%d%d|%d|%d,%d,%d|%d,%d,%d", (const void*)sp, a.psd, (int)df64,
+            g_defer_df64.load(), want,
             tune[0].threads, tune[0].blocks_per_sm, tune[0].tiles_per_grab, tune[1].threads, tune[1].blocks_per_sm,
             tune[1].tiles_per_grab);
         if (!C.exec || C.graph_key != key) {
@@ -1211,7 +1215,6 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
             {
                 // launch shapes (and their occupancy queries) before capturing
                 int b, t;
-                egh_grid(tune[0], C.max_n, k_local<PATH_ANY>, b, t);
                 egh_grid(tune[0], C.max_n, k_local<PATH_F64>, b, t);
                 egh_grid(tune[0], C.max_n, k_local<PATH_F32>, b, t);
                 if (df64) egh_grid(tune[1], C.max_n, k_psd_scatter<dd>, b, t);
@@ -1220,7 +1223,7 @@ bool barrier_egh(const ipcg_collisions* cs, ipcg_mesh* m, const double* V, const
             IPCG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
             int kernels = 0;
             try {
-                kernels = enqueue_step(cs, m, C, sp, a.psd, df64, want, split, tune);
+                kernels = enqueue_step(cs, m, C, sp, a.psd, df64, want, tune);
             } catch (...) {
                 cudaGraph_t g = nullptr;
                 cudaStreamEndCapture(s, &g);
@@ -1252,7 +1255,6 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
     EghCache& C = cache_for(cs, m);
     const Params* sp = upload_params_egh(cs, m, a);
     const bool df64 = a.df64_psd != 0;
-    const bool split = a.mixed || a.fp32_local;
     // the largest chunk is the workload
     size_t big = 0;
     for (size_t i = 0; i < C.chunks.size(); ++i)
@@ -1277,7 +1279,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
         for (int r = 0; r < 2; ++r) {
             IPCG_CUDA(cudaMemsetAsync(C.queue.p, 0, sizeof(unsigned long long) * 4, s));
             IPCG_CUDA(cudaEventRecord(e0, s));
-            if (stage == 0) launch_local(cc, m, C, ch, sp, sv, C.queue.p, want, split, t, s);
+            if (stage == 0) launch_local(cc, m, C, ch, sp, sv, C.queue.p, want, t, s);
             else launch_psd(cc, C, ch, (int)big, C.queue.p + 2, a.psd, df64, t, s);
             prof::count();
             IPCG_CUDA(cudaEventRecord(e1, s));
@@ -1308,7 +1310,7 @@ std::string egh_autotune(const ipcg_collisions* cs, ipcg_mesh* m, const double* 
             }
         };
         for (int threads : { 32, 64, 128 }) {
-            const int occ = stage == 0 ? occupancy(dev, split ? k_local<PATH_F64> : k_local<PATH_ANY>, threads)
+            const int occ = stage == 0 ? occupancy(dev, k_local<PATH_F64>, threads)
                 : (df64 ? occupancy(dev, k_psd_scatter<dd>, threads) : occupancy(dev, k_psd_scatter<double>, threads));
             for (int bps : { 1, 2, 4, 8, 16, 32 }) {
                 if (bps > occ) break;
