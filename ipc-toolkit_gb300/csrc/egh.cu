@@ -605,7 +605,18 @@ __global__ void k_hess_reduce(int64_t nb, const unsigned* __restrict__ run_start
     const int64_t q = t / 9;
     const int kl = (int)(t % 9), k = kl / 3, l = kl % 3;
     double sum = 0;
-    for (unsigned s = run_start[q]; s < run_start[q + 1]; ++s) sum += slab[9 * (int64_t)s + kl];
+    const unsigned s1 = run_start[q + 1];
+    unsigned s = run_start[q];
+    // four loads in flight, summed in slot order
+    for (; s + 4 <= s1; s += 4) {
+        const double a = slab[9 * (int64_t)s + kl], b = slab[9 * (int64_t)(s + 1) + kl];
+        const double c = slab[9 * (int64_t)(s + 2) + kl], e = slab[9 * (int64_t)(s + 3) + kl];
+        sum += a;
+        sum += b;
+        sum += c;
+        sum += e;
+    }
+    for (; s < s1; ++s) sum += slab[9 * (int64_t)s + kl];
     dev->val[vbase[q] + 3 * (int64_t)k * vnbr[q] + l] = sum;
 }
 
