@@ -788,52 +788,70 @@ template <class T> __device__ bool sym_eig_impl(int n, T* A /*MAXR*MAXR, full sy
         // the lanes meet again before the sweeps (each of its own length)
         if (wm) __syncwarp(wm);
         if (!sweep) continue;
+        // One implicitly shifted QL sweep down the block [start, end], in the
+        // carried form of the EISPACK tql / Numerical Recipes tqli recurrence
+        // (mirrored: the bulge is chased from the top, the shift is taken at
+        // the bottom).  Per step, (c, s) from one reciprocal square root of
+        // f^2 + g^2 (entries of a local Hessian, far from overflow) and the
+        // carried correction p of the diagonal.
         const T mu = PsdReal<T>::shift(d[end - 1], d[end], e[end - 1]);
-        T x = d[start] - mu, z = e[start];
+        T g = d[start] - mu, s = 1, c = 1, p = 0;
+        bool whole = true;
         for (int k = start; k < end; ++k) {
-            // (c, s) from one reciprocal square root: x and z are entries of
-            // a local Hessian, far from the range where x^2 + z^2 overflows
-            T c = 1, s = 0;
+            const T f = s * e[k], b = c * e[k];
+            T r = 0;
+            bool zero;
             if constexpr (PsdReal<T>::rescale) {
-                // df64: (x, z) scaled by a power of two before squaring
-                const T xz = dmax(fabs(x), fabs(z));
-                if (xz != T(0)) {
-                    const int rex = pow2_exp(xz);
-                    const T xs = scale2(x, -rex), zs = scale2(z, -rex);
-                    const T ir = rsqrt(xs * xs + zs * zs);
-                    c = xs * ir;
-                    s = -zs * ir;
+                // df64: (f, g) scaled by a power of two before squaring
+                const T fg = dmax(fabs(f), fabs(g));
+                zero = fg == T(0);
+                if (!zero) {
+                    const int rex = pow2_exp(fg);
+                    const T fs = scale2(f, -rex), gs = scale2(g, -rex);
+                    const T r2 = fs * fs + gs * gs, ir = rsqrt(r2);
+                    r = scale2(r2 * ir, rex);
+                    s = fs * ir;
+                    c = gs * ir;
                 }
             } else {
-                const T r2 = x * x + z * z;
-                if (r2 != 0) {
+                const T r2 = f * f + g * g;
+                zero = r2 == 0;
+                if (!zero) {
                     const T ir = rsqrt(r2);
-                    c = x * ir;
-                    s = -z * ir;
+                    r = r2 * ir;
+                    s = f * ir;
+                    c = g * ir;
                 }
             }
-            if (k > start) e[k - 1] = c * e[k - 1] - s * z;
-            const T dk = d[k], dk1 = d[k + 1], ek = e[k];
-            d[k] = c * c * dk - 2 * c * s * ek + s * s * dk1;
-            d[k + 1] = s * s * dk + 2 * c * s * ek + c * c * dk1;
-            e[k] = c * s * (dk - dk1) + (c * c - s * s) * ek;
-            if (k < end - 1) {
-                z = -s * e[k + 1];
-                e[k + 1] = c * e[k + 1];
+            if (k > start) e[k - 1] = r;
+            if (zero) {
+                // the block split exactly above k
+                d[k] = d[k] - p;
+                whole = false;
+                break;
             }
-            x = e[k];
+            g = d[k] - p;
+            const T q = (d[k + 1] - g) * s + 2 * c * b;
+            p = s * q;
+            d[k] = g + p;
+            g = c * q - b;
+            // the step's rotation of coordinates (k, k + 1): cos c, sin -s
             if (record) {
                 rc[nrot] = c;
-                rs[nrot] = s;
+                rs[nrot] = -s;
                 rk[nrot] = (int8_t)k;
                 ++nrot;
             } else {
-                for (int q = 0; q < n; ++q) {
-                    const T qa = Q[q * MAXR + k], qb = Q[q * MAXR + k + 1];
-                    Q[q * MAXR + k] = c * qa - s * qb;
-                    Q[q * MAXR + k + 1] = s * qa + c * qb;
+                for (int j = 0; j < n; ++j) {
+                    const T qa = Q[j * MAXR + k], qb = Q[j * MAXR + k + 1];
+                    Q[j * MAXR + k] = c * qa + s * qb;
+                    Q[j * MAXR + k + 1] = c * qb - s * qa;
                 }
             }
+        }
+        if (whole) {
+            d[end] = d[end] - p;
+            e[end - 1] = g;
         }
     }
     return ok;
