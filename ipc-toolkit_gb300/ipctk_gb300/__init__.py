@@ -951,19 +951,35 @@ class BatchBarrierPotential:
                                 batch.per_scene(self.stiffness), self._options, psd)
 
     def evaluate(self, collisions: NormalCollisions, batch: SceneBatch, vertices, energy=True, gradient=False,
-                 hessian=False, project_hessian_to_psd=PSDProjectionMethod.NONE, device=False):
+                 hessian=False, project_hessian_to_psd=PSDProjectionMethod.NONE, device=False, out_gradient=None):
         """(energies, gradient or None, Hessian or None) from one call.  With
-        ``device`` the Hessian is a DeviceCSR, else a scipy matrix."""
+        ``device`` the Hessian is a DeviceCSR, else a scipy matrix.
+        ``out_gradient`` (with ``gradient``): the array the gradient is written
+        to and returned as -- 3 x vertices float64 values, contiguous: a host
+        array (page-locked memory, e.g. a pinned torch tensor's ``.numpy()``,
+        makes the copy out fastest) or a CUDA tensor; by default a new array
+        of the same kind as ``vertices``."""
         V = _as_f64(vertices)
         dh, kap = batch.per_scene(self.dhat), batch.per_scene(self.stiffness)
         e = np.zeros(batch.num_scenes) if energy else None
         g = None
         if gradient:
-            if _is_torch_cuda(V):
+            n = 3 * batch.num_vertices
+            if out_gradient is not None:
+                g = out_gradient
+                if _is_torch_cuda(g):
+                    import torch
+                    ok = g.dtype == torch.float64 and g.is_contiguous() and g.numel() == n
+                else:
+                    ok = (isinstance(g, np.ndarray) and g.dtype == np.float64 and g.flags.c_contiguous
+                          and g.flags.writeable and g.size == n)
+                if not ok:
+                    raise ValueError(f"out_gradient must be a contiguous, writable float64 array of {n} values")
+            elif _is_torch_cuda(V):
                 import torch
                 g = torch.empty(V.numel(), dtype=torch.float64, device=V.device)
             else:
-                g = np.zeros(3 * batch.num_vertices)
+                g = np.zeros(n)
         h = C.c_void_p()
         _check(_load().ipcg_barrier_batch(collisions._h, batch._h, _ptr(V), _ptr(dh), _ptr(kap),
                                           self._options, int(project_hessian_to_psd), _ptr(e),

@@ -119,6 +119,36 @@ def test_batch_energies_gradient(batch_setup, ipctk, physical):
         assert np.linalg.norm(g_parts[k] - g1) <= REL * np.linalg.norm(g1), k
 
 
+def test_batch_gradient_into_caller_array(batch_setup, ipctk):
+    # out_gradient: a pinned host array and a CUDA tensor receive the same
+    # gradient as the default new array, and are what the call returns (the
+    # fused energy / gradient / Hessian pass sums in a fixed order, so the
+    # gradients are bit-identical)
+    import torch
+    scs, batch, V, V1, dhat, kappa, dmin, col, singles = batch_setup
+    B = ipctk.BatchBarrierPotential(dhat, kappa)
+    kw = dict(energy=True, gradient=True, hessian=True, project_hessian_to_psd=ipctk.PSDProjectionMethod.CLAMP,
+              device=True)
+
+    def run(x, **extra):
+        e, g, H = B.evaluate(col, batch, x, **kw, **extra)
+        H.free()
+        return g
+
+    g = run(V)
+    pinned = torch.full((g.size,), np.nan, dtype=torch.float64).pin_memory()
+    out = pinned.numpy()
+    assert run(V, out_gradient=out) is out
+    np.testing.assert_array_equal(out, g)
+    gd = torch.full((g.size,), np.nan, dtype=torch.float64, device="cuda")
+    assert run(torch.from_numpy(V).cuda(), out_gradient=gd) is gd
+    np.testing.assert_array_equal(gd.cpu().numpy(), g)
+    with pytest.raises(ValueError):
+        B.evaluate(col, batch, V, energy=False, gradient=True, out_gradient=np.zeros(g.size - 3))
+    with pytest.raises(ValueError):
+        B.evaluate(col, batch, V, energy=False, gradient=True, out_gradient=np.zeros(g.size, np.float32))
+
+
 @pytest.mark.parametrize("psd", ["none", "clamp"])
 def test_batch_hessian_block_diagonal(batch_setup, ipctk, psd):
     scs, batch, V, V1, dhat, kappa, dmin, col, singles = batch_setup
