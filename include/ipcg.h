@@ -10,7 +10,9 @@
  * Pointer arguments may be host memory or device memory of the current CUDA
  * device (unified addressing decides which); host inputs are copied to the
  * device inside the call and host outputs are written before the call
- * returns.  Objects are not thread-safe: do not use one ipcg_mesh or
+ * returns.  Host buffers in page-locked memory (cudaHostAlloc, or
+ * cudaHostRegister on an existing array) are copied at the link's rate;
+ * pageable ones go through a staging copy.  Objects are not thread-safe: do not use one ipcg_mesh or
  * ipcg_collisions from two threads at once.
  */
 #ifndef IPCG_H
