@@ -444,8 +444,8 @@ __global__ void __launch_bounds__(128) k_local(ContactsView cv, const int* __res
     });
 }
 
-// Stage 1's order in a mixed mode.  Per contact of the chunk a 4-bit key:
-// its kind on the FP64 path (VV, EV, each edge-edge distance type, FV) or
+// Stage 1's order (every mode).  Per contact of the chunk a 4-bit key: its
+// kind on the FP64 path (VV, EV, each edge-edge distance type, FV) or
 // KEY_F32; nsel counts the FP64 contacts.  A radix sort on the keys puts the
 // FP64 contacts first, grouped by kind, so that the FP64 distance code's
 // branches (one inlined copy per distance type) agree across a warp's lanes.
