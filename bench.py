@@ -112,6 +112,30 @@ PRECISION = {
 }
 
 
+def ranks_max(x, device):
+    """The largest of every rank's x (the job's time is its slowest rank's),
+    once all ranks have arrived; x itself with one process."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.barrier()
+    return float(t.item())
+
+
+def ranks_sum(n, device):
+    """The units all ranks processed (each replica its own batch)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return int(n)
+    t = torch.tensor([int(n)], dtype=torch.int64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return int(t.item())
+
+
 def batch_config(contacts=BATCH_CONTACTS):
     """The config dict both arms print (same keys, same workload)."""
     return {"workload": BATCH_DESC, "contacts": contacts, "psd": "clamp", "scenes": 256,
@@ -700,15 +724,11 @@ def run_gb300(args, rank, world):
     launches = ipctk.launch_count() - launches0
     clk = clocks.stop()
     per = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(per)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-        dist.barrier()
+    total_ms = ranks_max(sum(per), dev)
     ms_per_step = total_ms / args.steps
-    value = world * C / (ms_per_step / 1000.0)
+    # whole job: the contacts of every rank's batch over the slowest rank's time
+    C_job = ranks_sum(C, dev)
+    value = C_job / (ms_per_step / 1000.0)
 
     # per-kernel times from one profiled step (direct launches instead of the
     # graph replay, so each kernel is bracketed by events on its stream)
@@ -770,7 +790,7 @@ def run_gb300(args, rank, world):
         H.free()
         if i >= nw:
             e2e.append(1000 * (time.perf_counter() - t0))
-    e2e_ms = statistics.median(e2e)
+    e2e_ms = ranks_max(statistics.median(e2e), dev)
     h2d = Vh_np.nbytes
     d2h = 8 * len(scs) + 8 * ndof
 
@@ -838,7 +858,7 @@ def run_gb300(args, rank, world):
         "batched_modes": modes,
         "roofline": roof, "kernel_share": step_share,
         "cpu_baseline": cpu,
-        "e2e": {"value": C / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+        "e2e": {"value": C_job / (e2e_ms / 1000.0), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
                 "call": "BatchBarrierPotential.evaluate with pinned host positions; energies to host, the "
                         "gradient into a pinned host array (out_gradient), Hessian kept on the device"},
